@@ -1,0 +1,224 @@
+/*
+ * xg.h -- C ABI of libxg, the GB300 (sm_103a) cut-element assembly library.
+ *
+ * The library replaces ngsxfem's cut-element hot path:
+ *   CutInfo element marking        -> xg_cutinfo_update
+ *   GetFacetsWithNeighborTypes     -> xg_facets_with_neighbor_types
+ *   StraightCutIntegrationRule     -> xg_cut_rules
+ *   SymbolicCutBFI / SymbolicFacetPatchBFI element matrices + the sparse
+ *   scatter of BilinearForm::Assemble -> xg_form_assemble
+ *   Integrate(cf * dCut(...))      -> xg_integrate
+ *
+ * Conventions
+ *  - Plain pointers and sizes only.  Arguments named d_* are device pointers,
+ *    h_* host pointers.  `stream` is a cudaStream_t passed as void* (NULL = the
+ *    legacy default stream).
+ *  - Every entry point returns an xg_status; none throws across the ABI.
+ *    xg_status_string() names a status; xg_last_error() gives the last message
+ *    of the calling thread.
+ *  - The caller owns every buffer it passes in (level-set values, bitsets,
+ *    CSR output).  Objects (xg_mesh, xg_space, xg_form) own their device
+ *    workspace; calls on different objects may run concurrently from
+ *    different threads, calls on one object must be serialised.
+ *  - Launch entry points enqueue work on `stream` and return without a host
+ *    synchronisation, so a whole assembly step can be captured in a CUDA graph.
+ *    Device-side failures (bad decomposition, capacity overflow, non-finite
+ *    weights) are recorded in the object's device error word and read by
+ *    xg_*_check() after the stream has been synchronised.
+ *  - Bitsets: bit i of element/facet i lives in 64-bit word i/64, bit i%64.
+ *
+ * Domain types and combined domain types use ngsxfem's values
+ * (utils/ngsxstd.hpp:16-35).
+ */
+#ifndef XG_H
+#define XG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  XG_OK = 0,
+  XG_ERR_ARG = 1,          /* invalid argument */
+  XG_ERR_CUDA = 2,         /* CUDA runtime error (message in xg_last_error) */
+  XG_ERR_CAPACITY = 3,     /* an output or workspace capacity was too small */
+  XG_ERR_PLAIN_CUT = 4,    /* cut of an uncut sub-simplex: straightcutrule.cpp:43-48 */
+  XG_ERR_BAD_DECOMP = 5,   /* unsupported cut topology: straightcutrule.cpp:148,193 */
+  XG_ERR_UNSUPPORTED = 6,  /* element type / order / term not supported */
+  XG_ERR_NONFINITE = 7,    /* a non-finite weight or matrix entry was produced */
+  XG_ERR_NO_DEVICE = 8     /* no CUDA device, or the library was not built for it */
+} xg_status;
+
+enum { XG_NEG = 0, XG_POS = 1, XG_IF = 2 };
+enum {
+  XG_CDOM_NO = 0, XG_CDOM_NEG = 1, XG_CDOM_POS = 2, XG_CDOM_UNCUT = 3,
+  XG_CDOM_IF = 4, XG_CDOM_HASNEG = 5, XG_CDOM_HASPOS = 6, XG_CDOM_ANY = 7
+};
+
+/* Integrand menu of the bilinear-form terms (the CoefficientFunction trees the
+ * reference interprets, symboliccutbfi.cpp:168-194, reduced to the products
+ * the cut forms use).  u = trial, v = test, n = grad(lset)/|grad(lset)| of the
+ * P1 level set, b = constant vector, u' / v' = the neighbour's polynomial
+ * extended over the facet patch (u.Other()). */
+typedef enum {
+  XG_TERM_MASS = 0,       /* c * u * v                      */
+  XG_TERM_LAPLACE = 1,    /* c * grad u . grad v            */
+  XG_TERM_NGRADU_V = 2,   /* c * (n . grad u) * v           */
+  XG_TERM_U_NGRADV = 3,   /* c * u * (n . grad v)           */
+  XG_TERM_CONV = 4,       /* c * (b . grad u) * v           */
+  XG_TERM_GHOST_MASS = 5  /* c * (u - u') * (v - v') on a facet patch (dFacetPatch) */
+} xg_term_kind;
+
+typedef enum { XG_PREC_FP64 = 0, XG_PREC_MIXED = 1 } xg_precision;
+
+/* One integrator: SymbolicBFI(cf * dCut(lset, domain, order, definedonelements))
+ * or cf * dFacetPatch(definedonelements).  c = coef * h^hpow with
+ * h = |det F|^(1/dim) of the element (of the first element of a patch). */
+typedef struct {
+  int32_t kind;              /* xg_term_kind */
+  int32_t domain;            /* XG_NEG / XG_POS / XG_IF (ignored for patches) */
+  int32_t order;             /* -1: ngsxfem's default, symboliccutbfi.cpp:100-111 */
+  int32_t hpow;
+  double coef;
+  double b[3];               /* XG_TERM_CONV only */
+  const uint64_t* d_defined_on; /* element bits (volume) / facet bits (patch); NULL = all */
+} xg_term;
+
+typedef struct xg_mesh xg_mesh;
+typedef struct xg_space xg_space;
+typedef struct xg_form xg_form;
+
+/* ---- status ------------------------------------------------------------- */
+const char* xg_status_string(int status);
+const char* xg_last_error(void);
+/* Device count visible to the library and whether it carries sm_103a code. */
+int xg_device_ok(int* ok);
+
+/* ---- mesh (ngcomp::MeshAccess stand-in) ---------------------------------- */
+/* Builds edges, faces and the facet->element table on the host and uploads
+ * coordinates (SoA) and topology to the current device.
+ * h_coords: nv*dim (AoS), h_elv: ne*(dim+1).  dim 2 (trig) or 3 (tet). */
+int xg_mesh_create(int dim, int32_t nv, const double* h_coords, int32_t ne, const int32_t* h_elv,
+                   xg_mesh** out);
+int xg_mesh_destroy(xg_mesh* mesh);
+/* out: [dim, nv, ne, nedges, nfaces, nfacets] */
+int xg_mesh_info(const xg_mesh* mesh, int64_t* h_out6);
+/* Host copies of the facet->element table (nfacets*2, -1 = boundary). */
+int xg_mesh_facet_elements(const xg_mesh* mesh, int32_t* h_out);
+
+/* ---- H1 space (ngcomp::H1HighOrderFESpace stand-in) ---------------------- */
+/* Dof numbering: vertices, then (order-1) dofs per edge (edges sorted by
+ * vertex pair), then for order 3 one bubble per face (3D) / cell (2D). */
+int xg_space_create(xg_mesh* mesh, int order, xg_space** out);
+int xg_space_destroy(xg_space* space);
+/* out: [ndof, ndof_per_element, order] */
+int xg_space_info(const xg_space* space, int64_t* h_out3);
+int xg_space_element_dofs(const xg_space* space, int32_t* h_out /* ne*ndof_el */);
+
+/* ---- level set preparation ----------------------------------------------- */
+/* InterpolateToP1's vertex perturbation, utils/p1interpol.cpp:104-107:
+ * |v| < eps -> v = eps. */
+int xg_interpolate_p1_perturb(double* d_vals, int64_t n, double eps, void* stream);
+
+/* ---- marking -------------------------------------------------------------- */
+/* CutInformation::Update (xfem/cutinfo.cpp:61-132): per element the NEG/POS
+ * volume fractions of the order-0 cut rules give cut_ratio = NEG/(NEG+POS)
+ * and the domain type; d_bits receives the 8 COMBINED_DOMAIN_TYPE bitsets
+ * ([8][ceil(ne/64)] words, row c = XG_CDOM value c).
+ * Replaces CutInformation::Update(cf, subdivlvl=0, time_order=-1, lh). */
+int xg_cutinfo_update(xg_mesh* mesh, const double* d_lset, uint8_t* d_dom, double* d_cut_ratio,
+                      uint64_t* d_bits, void* stream);
+/* Device error word of the mesh (decomposition failures during marking or
+ * rule export); synchronise the stream first. Resets the word. */
+int xg_mesh_check(xg_mesh* mesh);
+/* GetFacetsWithNeighborTypes (xfem/cutinfo.cpp:476-538). */
+int xg_facets_with_neighbor_types(xg_mesh* mesh, const uint64_t* d_a, const uint64_t* d_b, int bnd_val_a,
+                                  int bnd_val_b, int use_and, uint64_t* d_out, void* stream);
+/* GetElementsWithNeighborFacets (xfem/cutinfo.cpp:540-566). */
+int xg_elements_with_neighbor_facets(xg_mesh* mesh, const uint64_t* d_facets, uint64_t* d_out, void* stream);
+
+/* ---- quadrature ------------------------------------------------------------ */
+/* StraightCutIntegrationRule (cutint/straightcutrule.cpp:582-677) for the n
+ * elements in d_elems: element i writes d_counts[i] points (-1 = no rule, the
+ * reference's nullptr) into d_pts[(i*max_pts + q)*3 + c] (reference
+ * coordinates) and d_wts[i*max_pts + q] (interface weights already carry
+ * |F^-T n_ref|, to be multiplied by |det F|). */
+int xg_cut_rules(xg_mesh* mesh, const double* d_lset, const int32_t* d_elems, int32_t n, int dt, int order,
+                 int32_t max_pts, int32_t* d_counts, double* d_pts, double* d_wts, void* stream);
+/* Number of points of the rule family for (element dim d, order p). */
+int xg_base_rule_size(int d, int p);
+
+/* Integrate(x^ex y^ey z^ez * dCut(lset, dt, order)) over the elements in
+ * d_defined_on (NULL = all): cutint/cutintegral.cpp:126-212.  The sum is
+ * formed in a fixed order (deterministic) and written to d_result[0]. */
+int xg_integrate(xg_mesh* mesh, const double* d_lset, int dt, int order, int ex, int ey, int ez,
+                 const uint64_t* d_defined_on, double* d_result, void* stream);
+
+/* ---- bilinear forms ---------------------------------------------------------- */
+/* A form is a list of integrators over one H1 space (trial = test space).
+ * Volume terms run on their element sets with the cut rule of their domain;
+ * patch terms run on their facet sets.  Creation uploads the term table and
+ * sizes the workspace for the whole mesh (no allocation during assembly). */
+int xg_form_create(xg_space* space, const xg_term* terms, int32_t nterms, int precision, xg_form** out);
+int xg_form_destroy(xg_form* form);
+/* Replace the element/facet set of term t (device bitset, NULL = all). */
+int xg_form_set_defined_on(xg_form* form, int32_t t, const uint64_t* d_defined_on);
+
+/* Output matrix in compressed-row form over the form's active dofs (the dofs
+ * of elements and facet patches that carry a term, numbered ascending as
+ * ngcomp::CompressedFESpace / Restrict() does):
+ *   d_row_dof[r]  global dof of row r (= of column index r)
+ *   d_rowptr[r]   start of row r, r = 0..nrows
+ *   d_cols[k]     compressed column index, ascending within a row
+ *   d_vals[k]     value (FP64)
+ *   d_counts[0]   nrows, d_counts[1] nnz (device, written by the step)
+ * Capacities are the caller's allocation sizes; xg_form_capacity() gives
+ * sufficient ones. */
+typedef struct {
+  int32_t* d_row_dof;
+  int64_t* d_rowptr;
+  int32_t* d_cols;
+  double* d_vals;
+  int64_t* d_counts;
+  int64_t cap_rows;
+  int64_t cap_nnz;
+} xg_csr;
+
+/* out: [cap_rows, cap_nnz] sufficient for any level set on this mesh. */
+int xg_form_capacity(const xg_form* form, int64_t* h_out2);
+
+/* BilinearForm::Assemble for the form: element matrices of all volume terms
+ * (SymbolicCutBilinearFormIntegrator::T_CalcElementMatrixAdd,
+ * xfem/symboliccutbfi.cpp:76-486, summed per element), facet-patch matrices of
+ * the patch terms (SymbolicFacetPatchBilinearFormIntegrator::T_CalcFacetMatrix,
+ * :1982-2377) and their deterministic row-wise scatter into `out`.  d_dom is
+ * the per-element domain type from xg_cutinfo_update for d_lset. */
+int xg_form_assemble(xg_form* form, const double* d_lset, const uint8_t* d_dom, xg_csr* out, void* stream);
+/* Device error word of the form; synchronise the stream first. Resets it. */
+int xg_form_check(xg_form* form);
+/* Profiling hook: with n = 8 cudaEvent_t handles (passed as void*), every
+ * xg_cutfem_step records them on its stream at the stage boundaries
+ *   [0] start, [1] marking done, [2] work lists done, [3] uncut element
+ *   matrices, [4] cut element matrices, [5] facet-patch matrices,
+ *   [6] row pattern counted, [7] values scattered.
+ * n = 0 switches it off.  The events are the caller's. */
+int xg_form_stage_events(xg_form* form, void* const* events, int n);
+
+/* ---- the CutFEM step (demos/fictdom.py:95-133) ----------------------------- */
+/* One call runs the whole cut-assembly step on `stream`: CutInfo marking,
+ * HASNEG / IF / HASPOS element sets, ghost facets (HASNEG, IF) when the form
+ * has patch terms, and xg_form_assemble with NEG terms on HASNEG, IF terms on
+ * IF, POS terms on HASPOS and patch terms on the ghost facets.  The level set
+ * is the P1 vertex vector (already perturbed).  Graph-capturable. */
+int xg_cutfem_step(xg_form* form, const double* d_lset, xg_csr* out, void* stream);
+/* Device views of the marking of the last step (owned by the form). */
+int xg_cutfem_marking(xg_form* form, const uint8_t** d_dom, const double** d_cut_ratio, const uint64_t** d_bits,
+                      const uint64_t** d_facets);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

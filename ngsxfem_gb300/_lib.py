@@ -1,0 +1,122 @@
+"""ctypes binding of libxg.so (the C ABI declared in include/xg.h).
+
+The library is the product path: there is no CPU fallback.  If libxg.so is
+missing or cannot be loaded, every entry point raises.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libxg.so")
+
+XG_OK = 0
+STATUS = {
+    0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "capacity exceeded",
+    4: "cut requested on an uncut (sub-)simplex", 5: "unsupported cut topology",
+    6: "unsupported element, order or term", 7: "non-finite weight or matrix entry",
+    8: "no usable CUDA device",
+}
+
+# every symbol include/xg.h declares, checked by the CPU test suite
+EXPORTS = [
+    "xg_status_string", "xg_last_error", "xg_device_ok",
+    "xg_mesh_create", "xg_mesh_destroy", "xg_mesh_info", "xg_mesh_facet_elements",
+    "xg_space_create", "xg_space_destroy", "xg_space_info", "xg_space_element_dofs",
+    "xg_interpolate_p1_perturb", "xg_cutinfo_update", "xg_mesh_check",
+    "xg_facets_with_neighbor_types", "xg_elements_with_neighbor_facets",
+    "xg_cut_rules", "xg_base_rule_size", "xg_integrate",
+    "xg_form_create", "xg_form_destroy", "xg_form_set_defined_on", "xg_form_capacity",
+    "xg_form_assemble", "xg_form_check", "xg_form_stage_events", "xg_cutfem_step", "xg_cutfem_marking",
+]
+
+
+class XgError(RuntimeError):
+    def __init__(self, status, where, msg=""):
+        super().__init__("%s: %s%s" % (where, STATUS.get(status, "status %d" % status), (" (" + msg + ")") if msg else ""))
+        self.status = status
+
+
+class Term(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int32),
+        ("domain", ctypes.c_int32),
+        ("order", ctypes.c_int32),
+        ("hpow", ctypes.c_int32),
+        ("coef", ctypes.c_double),
+        ("b", ctypes.c_double * 3),
+        ("d_defined_on", ctypes.c_void_p),
+    ]
+
+
+class Csr(ctypes.Structure):
+    _fields_ = [
+        ("d_row_dof", ctypes.c_void_p),
+        ("d_rowptr", ctypes.c_void_p),
+        ("d_cols", ctypes.c_void_p),
+        ("d_vals", ctypes.c_void_p),
+        ("d_counts", ctypes.c_void_p),
+        ("cap_rows", ctypes.c_int64),
+        ("cap_nnz", ctypes.c_int64),
+    ]
+
+
+_lib = None
+
+
+def load():
+    """Loads libxg.so; raises if it is missing (no fallback path exists)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(
+            "libxg.so is not built (%s). Build it with `python -m ngsxfem_gb300.build` "
+            "or __graft_entry__.build(); there is no CPU fallback." % LIB_PATH)
+    L = ctypes.CDLL(LIB_PATH)
+    P, I, I64, D = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_double
+    sig = {
+        "xg_status_string": (ctypes.c_char_p, [I]),
+        "xg_last_error": (ctypes.c_char_p, []),
+        "xg_device_ok": (I, [P]),
+        "xg_mesh_create": (I, [I, ctypes.c_int32, P, ctypes.c_int32, P, P]),
+        "xg_mesh_destroy": (I, [P]),
+        "xg_mesh_info": (I, [P, P]),
+        "xg_mesh_facet_elements": (I, [P, P]),
+        "xg_space_create": (I, [P, I, P]),
+        "xg_space_destroy": (I, [P]),
+        "xg_space_info": (I, [P, P]),
+        "xg_space_element_dofs": (I, [P, P]),
+        "xg_interpolate_p1_perturb": (I, [P, I64, D, P]),
+        "xg_cutinfo_update": (I, [P, P, P, P, P, P]),
+        "xg_mesh_check": (I, [P]),
+        "xg_facets_with_neighbor_types": (I, [P, P, P, I, I, I, P, P]),
+        "xg_elements_with_neighbor_facets": (I, [P, P, P, P]),
+        "xg_cut_rules": (I, [P, P, P, ctypes.c_int32, I, I, ctypes.c_int32, P, P, P, P]),
+        "xg_base_rule_size": (I, [I, I]),
+        "xg_integrate": (I, [P, P, I, I, I, I, I, P, P, P]),
+        "xg_form_create": (I, [P, P, ctypes.c_int32, I, P]),
+        "xg_form_destroy": (I, [P]),
+        "xg_form_set_defined_on": (I, [P, ctypes.c_int32, P]),
+        "xg_form_capacity": (I, [P, P]),
+        "xg_form_assemble": (I, [P, P, P, P, P]),
+        "xg_form_check": (I, [P]),
+        "xg_form_stage_events": (I, [P, P, I]),
+        "xg_cutfem_step": (I, [P, P, P, P]),
+        "xg_cutfem_marking": (I, [P, P, P, P, P]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def check(status, where):
+    if status != XG_OK:
+        msg = load().xg_last_error()
+        raise XgError(status, where, msg.decode() if msg else "")
+
+
+def call(name, *args):
+    check(getattr(load(), name)(*args), name)

@@ -1,0 +1,1495 @@
+// Assembly kernels of libxg: work-list compaction, cut element matrices,
+// facet-patch (ghost-penalty) matrices and the deterministic row-wise scatter
+// into a compressed-row matrix, plus the xg_form object and the CutFEM step.
+//
+// Reference behaviour:
+//   SymbolicCutBilinearFormIntegrator::T_CalcElementMatrixAdd  xfem/symboliccutbfi.cpp:76-486
+//   SymbolicFacetPatchBilinearFormIntegrator::T_CalcFacetMatrix xfem/symboliccutbfi.cpp:1982-2377
+//   MapPatchIntegrationPoint                                   xfem/symboliccutbfi.cpp:1747-1846
+//   RestrictedBilinearForm graph / Restrict()                  utils/restrictedblf.cpp:7-168
+#include <algorithm>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <thread>
+
+#include "xg_basis.cuh"
+#include "xg_cut.cuh"
+#include "xg_internal.h"
+
+namespace xg {
+
+static __constant__ RuleTable c_rules;
+
+int upload_rules_asm() {
+  XG_CUDA(cudaMemcpyToSymbol(c_rules, &host_rules(), sizeof(RuleTable)));
+  return XG_OK;
+}
+
+__device__ __forceinline__ bool tbit(const uint64_t* b, int64_t i) { return (b[i >> 6] >> (i & 63)) & 1ull; }
+__device__ __forceinline__ bool tbit32(const uint32_t* b, int64_t i) { return (b[i >> 5] >> (i & 31)) & 1u; }
+
+// ============================================================================
+// Compaction of a bitset into an ascending index list (deterministic):
+// block popcounts -> single-block scan -> per-block write.
+// ============================================================================
+constexpr int kCThreads = 256;
+constexpr int kCWordsPerThread = 8;
+constexpr int kCChunk = kCThreads * kCWordsPerThread;  // 32-bit words per block
+
+__device__ __forceinline__ int block_excl_scan_int(int v, int* total, int* sm /* >= 32 */) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sm[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int t = lane < nw ? sm[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    sm[lane] = t;  // inclusive warp totals
+  }
+  __syncthreads();
+  int base = wid > 0 ? sm[wid - 1] : 0;
+  if (total) *total = sm[nw - 1];
+  __syncthreads();
+  return base + x - v;
+}
+
+__global__ void k_popc_blocks(const uint32_t* __restrict__ bits, int64_t nwords, int* __restrict__ bsum) {
+  __shared__ int sm[32];
+  int64_t w0 = (int64_t)blockIdx.x * kCChunk + (int64_t)threadIdx.x * kCWordsPerThread;
+  int c = 0;
+#pragma unroll
+  for (int k = 0; k < kCWordsPerThread; k++)
+    if (w0 + k < nwords) c += __popc(bits[w0 + k]);
+  int total;
+  block_excl_scan_int(c, &total, sm);
+  if (threadIdx.x == 0) bsum[blockIdx.x] = total;
+}
+
+// single block: in-place exclusive scan of n ints, total -> *total_out (+ *extra if given)
+__global__ void k_scan_small(int* __restrict__ v, int n, int* __restrict__ total_out) {
+  __shared__ int sm[32];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < n; base += blockDim.x) {
+    int i = base + threadIdx.x;
+    int x = i < n ? v[i] : 0;
+    int tot;
+    int ex = block_excl_scan_int(x, &tot, sm);
+    if (i < n) v[i] = ex + carry;
+    __syncthreads();
+    if (threadIdx.x == 0) carry += tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total_out = carry;
+}
+
+__global__ void k_write_list(const uint32_t* __restrict__ bits, int64_t nwords, const int* __restrict__ boff,
+                             int32_t* __restrict__ list, int32_t* __restrict__ slot, const int* __restrict__ slot_base) {
+  __shared__ int sm[32];
+  const int sb = slot_base ? *slot_base : 0;
+  int64_t w0 = (int64_t)blockIdx.x * kCChunk + (int64_t)threadIdx.x * kCWordsPerThread;
+  uint32_t w[kCWordsPerThread];
+  int c = 0;
+#pragma unroll
+  for (int k = 0; k < kCWordsPerThread; k++) {
+    w[k] = (w0 + k < nwords) ? bits[w0 + k] : 0u;
+    c += __popc(w[k]);
+  }
+  int pos = boff[blockIdx.x] + block_excl_scan_int(c, nullptr, sm);
+#pragma unroll
+  for (int k = 0; k < kCWordsPerThread; k++) {
+    uint32_t x = w[k];
+    while (x) {
+      int b = __ffs(x) - 1;
+      x &= x - 1;
+      int idx = (int)((w0 + k) * 32 + b);
+      list[pos] = idx;
+      if (slot) slot[idx] = pos + sb;
+      pos++;
+    }
+  }
+}
+
+// ============================================================================
+// Row-pointer scan over int64 counts (n read from the device).
+// ============================================================================
+constexpr int kSThreads = 256;
+constexpr int kSPerThread = 8;
+constexpr int kSChunk = kSThreads * kSPerThread;
+
+__device__ __forceinline__ long long block_excl_scan_ll(long long v, long long* total, long long* sm) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  long long x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    long long y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sm[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    long long t = lane < nw ? sm[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      long long y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    sm[lane] = t;
+  }
+  __syncthreads();
+  long long base = wid > 0 ? sm[wid - 1] : 0;
+  if (total) *total = sm[nw - 1];
+  __syncthreads();
+  return base + x - v;
+}
+
+__global__ void k_sum64_blocks(const int64_t* __restrict__ v, const int* __restrict__ n_ptr, long long* bsum) {
+  __shared__ long long sm[32];
+  const int n = *n_ptr;
+  int64_t i0 = (int64_t)blockIdx.x * kSChunk + (int64_t)threadIdx.x * kSPerThread;
+  long long c = 0;
+  for (int k = 0; k < kSPerThread; k++)
+    if (i0 + k < n) c += v[i0 + k];
+  long long tot;
+  block_excl_scan_ll(c, &tot, sm);
+  if (threadIdx.x == 0) bsum[blockIdx.x] = tot;
+}
+
+__global__ void k_scan64_small(long long* v, int nblocks) {
+  __shared__ long long sm[32];
+  __shared__ long long carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < nblocks; base += blockDim.x) {
+    int i = base + threadIdx.x;
+    long long x = i < nblocks ? v[i] : 0;
+    long long tot;
+    long long ex = block_excl_scan_ll(x, &tot, sm);
+    if (i < nblocks) v[i] = ex + carry;
+    __syncthreads();
+    if (threadIdx.x == 0) carry += tot;
+    __syncthreads();
+  }
+}
+
+// rowptr[i] = exclusive prefix of cnt, rowptr[n] = total, counts_out[1] = total
+__global__ void k_scan64_apply(const int64_t* __restrict__ cnt, const int* __restrict__ n_ptr,
+                               const long long* __restrict__ boff, int64_t* __restrict__ rowptr,
+                               int64_t* __restrict__ counts_out, int64_t cap_nnz, int* err) {
+  __shared__ long long sm[32];
+  const int n = *n_ptr;
+  int64_t i0 = (int64_t)blockIdx.x * kSChunk + (int64_t)threadIdx.x * kSPerThread;
+  long long c[kSPerThread];
+  long long s = 0;
+  for (int k = 0; k < kSPerThread; k++) {
+    c[k] = (i0 + k < n) ? cnt[i0 + k] : 0;
+    s += c[k];
+  }
+  long long tot;
+  long long pos = boff[blockIdx.x] + block_excl_scan_ll(s, &tot, sm);
+  for (int k = 0; k < kSPerThread; k++) {
+    if (i0 + k < n) rowptr[i0 + k] = pos;
+    if (i0 + k == n - 1) {
+      rowptr[n] = pos + c[k];
+      counts_out[0] = n;
+      counts_out[1] = pos + c[k];
+      if (pos + c[k] > cap_nnz) set_err(err, XG_ERR_CAPACITY);
+    }
+    pos += c[k];
+  }
+  if (n == 0 && blockIdx.x == 0 && threadIdx.x == 0) {
+    rowptr[0] = 0;
+    counts_out[0] = 0;
+    counts_out[1] = 0;
+  }
+}
+
+// ============================================================================
+// Active sets
+// ============================================================================
+// uncut-active: domain of the element equals the domain of a volume group that
+// contains it; cut-active: a cut element contained in any volume group.
+__global__ void k_active_elements(int ne, const uint8_t* __restrict__ dom, FormDesc form, uint32_t* uncut_bits,
+                                  uint32_t* cut_bits, int64_t nw32) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  bool un = false, cu = false;
+  if (e < ne) {
+    const int d = dom[e];
+    for (int g = 0; g < form.ngroups; g++) {
+      const GroupDesc& G = form.g[g];
+      bool in = !G.defined_on || tbit(G.defined_on, e);
+      if (!in) continue;
+      if (d == XG_IF) cu = true;
+      else if (G.domain == d) un = true;
+    }
+  }
+  unsigned mu = __ballot_sync(0xffffffffu, un), mc = __ballot_sync(0xffffffffu, cu);
+  if ((threadIdx.x & 31) == 0 && (e >> 5) < nw32) {
+    uncut_bits[e >> 5] = mu;
+    cut_bits[e >> 5] = mc;
+  }
+}
+
+__global__ void k_active_facets(int64_t nf, const int32_t* __restrict__ fel, FormDesc form, uint32_t* bits,
+                                int64_t nw32) {
+  const int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  bool act = false;
+  if (f < nf && fel[nf + f] >= 0)
+    for (int p = 0; p < form.npatch; p++)
+      if (!form.p[p].defined_on || tbit(form.p[p].defined_on, f)) act = true;
+  unsigned m = __ballot_sync(0xffffffffu, act);
+  if ((threadIdx.x & 31) == 0 && (f >> 5) < nw32) bits[f >> 5] = m;
+}
+
+// dofs of active elements and of both elements of active facets
+__global__ void k_mark_dofs(int ne, int nd, const int32_t* __restrict__ el_dofs, const int32_t* __restrict__ l_un,
+                            const int32_t* __restrict__ l_cut, const int32_t* __restrict__ l_fa,
+                            const int* __restrict__ counts, int64_t nf, const int32_t* __restrict__ fel,
+                            unsigned* dof_bits) {
+  const int nun = counts[0], ncut = counts[1], nfa = counts[2];
+  const int64_t total = (int64_t)(nun + ncut + 2 * nfa) * nd;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    int64_t item = t / nd;
+    int j = (int)(t % nd);
+    int e;
+    if (item < nun) e = l_un[item];
+    else if (item < nun + ncut) e = l_cut[item - nun];
+    else {
+      int64_t q = item - nun - ncut;
+      e = fel[(q & 1) * nf + l_fa[q >> 1]];
+    }
+    int dof = el_dofs[(int64_t)j * ne + e];
+    atomicOr(&dof_bits[dof >> 5], 1u << (dof & 31));
+  }
+}
+
+// ============================================================================
+// Element matrices.  Thread (element, row i); EPB elements per block.
+// Phase 1 (thread per element): geometry, orientation, coefficients and the
+// sub-simplex decompositions.  Then per term group and chunk of quadrature
+// points: point generation, basis evaluation (thread per function) and the
+// contraction elmat[i][j] += w * (terms) (thread per row).
+// ============================================================================
+// FP64 accumulation for the plain path; FP32 with Kahan compensation per
+// entry for the mixed path.
+template <typename T>
+struct Acc;
+template <>
+struct Acc<double> {
+  double s;
+  __device__ __forceinline__ void init() { s = 0.0; }
+  __device__ __forceinline__ void add(double v) { s += v; }
+  __device__ __forceinline__ double get() const { return s; }
+};
+template <>
+struct Acc<float> {
+  float s, c;
+  __device__ __forceinline__ void init() { s = 0.f; c = 0.f; }
+  __device__ __forceinline__ void add(float v) {
+    float y = v - c;
+    float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ __forceinline__ float get() const { return s; }
+};
+
+template <int D, int K, bool CUT, typename T>
+struct ElCfg {
+  static constexpr int N = ndof_el(D, K);
+  static constexpr int EPB0 = N <= 4 ? 32 : (N <= 10 ? 16 : 8);
+  static constexpr int EPB = CUT ? (EPB0 > 8 ? EPB0 / 2 : EPB0) : EPB0;
+  static constexpr int CH = (N <= 4 ? 4 : (N <= 10 ? (sizeof(T) == 8 ? 4 : 8) : 4));
+  static constexpr int NT = N * EPB;
+  static constexpr int ND = D + 2;
+};
+
+struct ElGeoS {
+  double g[4][3];  // physical gradients of the barycentric coordinates
+  double nrm[3];   // unit normal of the P1 level set (physical)
+  double meas;     // |det F|
+  double iffac;    // |F^-T n_ref|
+  double l[4];
+  int gv[4];
+  int elem;
+  int slot;
+  int dom;
+  int ns[3];       // #sub-simplices for NEG, POS, IF (cut elements)
+  double coef[kMaxGroups][5];
+};
+struct ElSubS {
+  Sub sub[3][3];
+  double vol[3][3];
+};
+
+template <int D, int K, bool CUT, typename T>
+__global__ void __launch_bounds__(ElCfg<D, K, CUT, T>::NT) k_elmat(
+    int ne, int nv, const int32_t* __restrict__ elv, const double* __restrict__ xyz, const double* __restrict__ lset,
+    const uint8_t* __restrict__ dom, FormDesc form, const int32_t* __restrict__ list, const int* __restrict__ counts,
+    int which, T* __restrict__ elmat, int* err, int needs_mask) {
+  using C = ElCfg<D, K, CUT, T>;
+  constexpr int N = C::N, EPB = C::EPB, CH = C::CH, ND = C::ND;
+  __shared__ ElGeoS geo[EPB];
+  __shared__ ElSubS subs[CUT ? EPB : 1];
+  __shared__ double pts[EPB][CH][4];
+  __shared__ T B[EPB][CH][N][ND];  // phi, grad (D), e
+  __shared__ int npts_s[EPB];
+  __shared__ int maxpts_s;
+  static_assert(sizeof(geo) + sizeof(subs) + sizeof(pts) + sizeof(B) < 48 * 1024, "k_elmat shared memory");
+
+  const int count = counts[which];
+  const int slot_base = which == 0 ? 0 : counts[0];
+  const int le = threadIdx.x / N, i = threadIdx.x % N;
+
+  for (int batch = blockIdx.x; batch * EPB < count; batch += gridDim.x) {
+    // ---------------- phase 1: per-element data ----------------
+    if (threadIdx.x < EPB) {
+      ElGeoS& G = geo[threadIdx.x];
+      const int idx = batch * EPB + threadIdx.x;
+      G.elem = idx < count ? list[idx] : -1;
+      G.slot = slot_base + idx;
+      if (G.elem >= 0) {
+        const int e = G.elem;
+        double xv[D + 1][3];
+#pragma unroll
+        for (int v = 0; v <= D; v++) {
+          int vid = elv[(int64_t)v * ne + e];
+          G.gv[v] = vid;
+          G.l[v] = lset[vid];
+#pragma unroll
+          for (int c = 0; c < 3; c++) xv[v][c] = c < D ? xyz[(int64_t)c * nv + vid] : 0.0;
+        }
+        Geo<D> g;
+        make_geo<D>(xv, g);
+        G.meas = fabs(g.det);
+        double gs[3] = {0, 0, 0};
+#pragma unroll
+        for (int a = 0; a < D; a++)
+#pragma unroll
+          for (int k = 0; k < 3; k++) {
+            G.g[a][k] = k < D ? g.Finv[a][k] : 0.0;
+            gs[k] += G.g[a][k];
+          }
+#pragma unroll
+        for (int k = 0; k < 3; k++) G.g[D][k] = -gs[k];
+        // Normalize(grad(lsetp1)) in physical coordinates
+        double gl[3] = {0, 0, 0};
+#pragma unroll
+        for (int k = 0; k < D; k++) {
+          double s = 0;
+#pragma unroll
+          for (int a = 0; a < D; a++) s += g.Finv[a][k] * (G.l[a] - G.l[D]);
+          gl[k] = s;
+        }
+        double nn = l2norm3(gl[0], gl[1], gl[2]);
+#pragma unroll
+        for (int k = 0; k < 3; k++) G.nrm[k] = gl[k] / nn;
+        const double h = pow(G.meas, 1.0 / D);
+        for (int q = 0; q < form.ngroups; q++)
+          for (int k = 0; k < 5; k++) {
+            double c = form.g[q].c[k];
+            int hp = form.g[q].hpow[k];
+            G.coef[q][k] = hp == 0 ? c : c * pow(h, (double)hp);
+          }
+        G.dom = dom[e];
+        G.iffac = 0.0;
+        G.ns[0] = G.ns[1] = G.ns[2] = 0;
+        if (CUT) {
+          ElSubS& SS = subs[CUT ? threadIdx.x : 0];
+          for (int dt = 0; dt < 3; dt++) {
+            if (!((needs_mask >> dt) & 1)) continue;
+            int ns = decompose<D>(G.l, dt, SS.sub[dt]);
+            if (ns < 0) {
+              set_err(err, -ns);
+              ns = 0;
+            }
+            G.ns[dt] = ns;
+            const int sd = dt == XG_IF ? D - 1 : D;
+            for (int s = 0; s < ns; s++) SS.vol[dt][s] = simplex_volume(SS.sub[dt][s].p, sd + 1);
+          }
+          if ((needs_mask >> XG_IF) & 1) G.iffac = if_factor<D>(g, G.l);
+        }
+      }
+    }
+    __syncthreads();
+
+    const ElGeoS& G = geo[le];
+    const int desc = G.elem >= 0 ? fn_desc<D, K>(i, G.gv) : 0;
+    T gT[D + 1][D];
+#pragma unroll
+    for (int a = 0; a <= D; a++)
+#pragma unroll
+      for (int k = 0; k < D; k++) gT[a][k] = (T)G.g[a][k];
+    Acc<T> acc[N];
+#pragma unroll
+    for (int j = 0; j < N; j++) acc[j].init();
+
+    for (int q = 0; q < form.ngroups; q++) {
+      const GroupDesc& Gq = form.g[q];
+      const int p = clamp_order(Gq.order);
+      const int dt = Gq.domain;
+      const int sd = dt == XG_IF ? D - 1 : D;
+      const int nqb = CUT ? c_rules.cnt[sd][p] : c_rules.cnt[D][p];
+      const int offb = CUT ? c_rules.off[sd][p] : c_rules.off[D][p];
+      if (i == 0) {
+        int np = 0;
+        if (G.elem >= 0 && (!Gq.defined_on || tbit(Gq.defined_on, G.elem))) {
+          if (CUT) np = G.ns[dt] * nqb;
+          else if (G.dom == dt) np = nqb;
+        }
+        npts_s[le] = np;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        int mx = 0;
+        for (int k = 0; k < EPB; k++) mx = max(mx, npts_s[k]);
+        maxpts_s = mx;
+      }
+      __syncthreads();
+      const int maxpts = maxpts_s;
+      const int np = npts_s[le];
+      const T cM = (T)G.coef[q][0], cL = (T)G.coef[q][1], cN1 = (T)G.coef[q][2], cN2 = (T)G.coef[q][3],
+              cC = (T)G.coef[q][4];
+      const int used = Gq.used;
+      const bool has_e = (used & ((1 << 2) | (1 << 4))) != 0;
+      for (int q0 = 0; q0 < maxpts; q0 += CH) {
+        // --- point generation (FP64: cut points, sub-simplex volumes)
+        for (int qq = i; qq < CH; qq += N) {
+          const int qi = q0 + qq;
+          if (qi < np) {
+            double pt[3], w;
+            if (CUT) {
+              const ElSubS& SS = subs[CUT ? le : 0];
+              const int s = qi / nqb, b = qi % nqb;
+              plain_point(SS.sub[dt][s], sd + 1, c_rules.x[offb + b], pt);
+              w = c_rules.w[offb + b] * SS.vol[dt][s];
+              if (dt == XG_IF) w = w * G.iffac;
+            } else {
+              pt[0] = c_rules.x[offb + qi][0];
+              pt[1] = c_rules.x[offb + qi][1];
+              pt[2] = c_rules.x[offb + qi][2];
+              w = c_rules.w[offb + qi];
+            }
+            pts[le][qq][0] = pt[0];
+            pts[le][qq][1] = pt[1];
+            pts[le][qq][2] = pt[2];
+            pts[le][qq][3] = w * G.meas;
+          }
+        }
+        __syncthreads();
+        const int nch = min(CH, np - q0);
+        // --- basis: thread i evaluates function i at the chunk's points
+        for (int qq = 0; qq < nch; qq++) {
+          T lam[D + 1];
+          T s = 0;
+#pragma unroll
+          for (int a = 0; a < D; a++) {
+            lam[a] = (T)pts[le][qq][a];
+            s += lam[a];
+          }
+          lam[D] = (T)1 - s;
+          T phi, grad[D];
+          eval_fn<D, T>(desc, lam, gT, phi, grad);
+          T ev = 0;
+          if (used & (1 << 2)) {
+            T dn = 0;
+#pragma unroll
+            for (int k = 0; k < D; k++) dn += (T)G.nrm[k] * grad[k];
+            ev += cN1 * dn;
+          }
+          if (used & (1 << 4)) {
+            T db = 0;
+#pragma unroll
+            for (int k = 0; k < D; k++) db += (T)Gq.b[k] * grad[k];
+            ev += cC * db;
+          }
+          B[le][qq][i][0] = phi;
+#pragma unroll
+          for (int k = 0; k < D; k++) B[le][qq][i][1 + k] = grad[k];
+          B[le][qq][i][1 + D] = ev;
+        }
+        __syncthreads();
+        // --- contraction: row i
+        for (int qq = 0; qq < nch; qq++) {
+          const T w = (T)pts[le][qq][3];
+          const T phi_i = B[le][qq][i][0];
+          T a_i = 0;
+          if (used & 1) a_i += cM * phi_i;
+          if (used & (1 << 3)) {
+            T dn = 0;
+#pragma unroll
+            for (int k = 0; k < D; k++) dn += (T)G.nrm[k] * B[le][qq][i][1 + k];
+            a_i += cN2 * dn;
+          }
+          a_i *= w;
+          const T b_i = w * phi_i;
+          T gl[D];
+#pragma unroll
+          for (int k = 0; k < D; k++) gl[k] = (used & 2) ? w * cL * B[le][qq][i][1 + k] : (T)0;
+#pragma unroll
+          for (int j = 0; j < N; j++) {
+            T v = a_i * B[le][qq][j][0];
+            if (used & 2) {
+#pragma unroll
+              for (int k = 0; k < D; k++) v += gl[k] * B[le][qq][j][1 + k];
+            }
+            if (has_e) v += b_i * B[le][qq][j][1 + D];
+            acc[j].add(v);
+          }
+        }
+        __syncthreads();
+      }
+    }
+    // ---------------- write ----------------
+    if (G.elem >= 0) {
+      T* out = elmat + ((int64_t)G.slot * N + i) * N;
+      bool finite = true;
+#pragma unroll
+      for (int j = 0; j < N; j++) {
+        T v = acc[j].get();
+        finite &= isfinite(v);
+        out[j] = v;
+      }
+      if (!finite) set_err(err, XG_ERR_NONFINITE);
+    }
+    __syncthreads();
+  }
+}
+
+// ============================================================================
+// Facet-patch matrices (ghost penalty).  Thread (facet, patch row a), 2N rows.
+// ============================================================================
+template <int D, int K>
+struct PaCfg {
+  static constexpr int N = ndof_el(D, K);
+  static constexpr int N2 = 2 * N;
+  static constexpr int FPB = N2 <= 8 ? 16 : (N2 <= 20 ? 8 : 4);
+  static constexpr int CH = 8;
+  static constexpr int NT = N2 * FPB;
+};
+
+template <int D>
+struct PaGeoS {
+  Geo<D> g1, g2;
+  int gv1[4], gv2[4];
+  int facet;
+};
+
+// MapPatchIntegrationPoint (symboliccutbfi.cpp:1747-1846) for affine elements:
+// low-order guess A^-1 (x - x(0)) plus the Newton correction loop.
+template <int D>
+__device__ __forceinline__ void map_patch_point(const Geo<D>& from, const Geo<D>& to, const double* xi_from,
+                                                double* xi_to) {
+  double vec[D];
+#pragma unroll
+  for (int i = 0; i < D; i++) {
+    double s = from.x0[i];
+#pragma unroll
+    for (int k = 0; k < D; k++) s += from.F[i][k] * xi_from[k];
+    vec[i] = s;
+  }
+  const double h = sqrt(from.det);
+  double x00[D], x0[D];
+#pragma unroll
+  for (int i = 0; i < D; i++) {
+    double s = 0;
+#pragma unroll
+    for (int k = 0; k < D; k++) s += to.Finv[i][k] * (vec[k] - to.x0[k]);
+    x00[i] = s;
+    x0[i] = s;
+  }
+  int its = 0;
+  double diffn = 0;
+  while (its == 0 || (diffn > 1e-12 * h && its < 15)) {
+    double diff[D];
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+      double s = to.x0[i];
+#pragma unroll
+      for (int k = 0; k < D; k++) s += to.F[i][k] * x0[k];
+      diff[i] = vec[i] - s;
+    }
+    diffn = 0;
+#pragma unroll
+    for (int i = 0; i < D; i++) diffn += diff[i] * diff[i];
+    diffn = sqrt(diffn);
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+      double s = 0;
+#pragma unroll
+      for (int k = 0; k < D; k++) s += to.Finv[i][k] * diff[k];
+      x0[i] += s;
+    }
+    its++;
+  }
+  double dist = 0;
+#pragma unroll
+  for (int i = 0; i < D; i++) dist += (x0[i] - x00[i]) * (x0[i] - x00[i]);
+  const bool fallback = its >= 15 || diffn > 1e-12 * h || sqrt(dist) > 10.0;
+#pragma unroll
+  for (int i = 0; i < D; i++) xi_to[i] = fallback ? x00[i] : x0[i];
+}
+
+template <int D, int K, typename T>
+__global__ void __launch_bounds__(PaCfg<D, K>::NT) k_patch(
+    int ne, int nv, const int32_t* __restrict__ elv, const double* __restrict__ xyz, int64_t nf,
+    const int32_t* __restrict__ fel, FormDesc form, const int32_t* __restrict__ list, const int* __restrict__ counts,
+    T* __restrict__ famat, int64_t cap_fa, int* err) {
+  using C = PaCfg<D, K>;
+  constexpr int N = C::N, N2 = C::N2, FPB = C::FPB, CH = C::CH;
+  __shared__ PaGeoS<D> geo[FPB];
+  __shared__ double pts[FPB][CH][2 * D + 1];
+  __shared__ T S[FPB][CH][N2];
+  const int count = counts[2];
+  const int lf = threadIdx.x / N2, a = threadIdx.x % N2;
+
+  for (int batch = blockIdx.x; batch * FPB < count; batch += gridDim.x) {
+    if (threadIdx.x < FPB) {
+      PaGeoS<D>& G = geo[threadIdx.x];
+      const int idx = batch * FPB + threadIdx.x;
+      G.facet = idx < count ? list[idx] : -1;
+      if (G.facet >= 0) {
+        const int e1 = fel[G.facet], e2 = fel[nf + G.facet];
+        double xv[D + 1][3];
+#pragma unroll
+        for (int v = 0; v <= D; v++) {
+          int vid = elv[(int64_t)v * ne + e1];
+          G.gv1[v] = vid;
+#pragma unroll
+          for (int c = 0; c < 3; c++) xv[v][c] = c < D ? xyz[(int64_t)c * nv + vid] : 0.0;
+        }
+        make_geo<D>(xv, G.g1);
+#pragma unroll
+        for (int v = 0; v <= D; v++) {
+          int vid = elv[(int64_t)v * ne + e2];
+          G.gv2[v] = vid;
+#pragma unroll
+          for (int c = 0; c < 3; c++) xv[v][c] = c < D ? xyz[(int64_t)c * nv + vid] : 0.0;
+        }
+        make_geo<D>(xv, G.g2);
+      }
+    }
+    __syncthreads();
+    const PaGeoS<D>& G = geo[lf];
+    const bool mine1 = a < N;
+    const int desc = G.facet >= 0 ? fn_desc<D, K>(mine1 ? a : a - N, mine1 ? G.gv1 : G.gv2) : 0;
+    Acc<T> acc[N2];
+#pragma unroll
+    for (int j = 0; j < N2; j++) acc[j].init();
+
+    for (int pp = 0; pp < form.npatch; pp++) {
+      const PatchDesc& P = form.p[pp];
+      const int p = clamp_order(P.order);
+      const int nq = c_rules.cnt[D][p], off = c_rules.off[D][p];
+      const bool on = G.facet >= 0 && (!P.defined_on || tbit(P.defined_on, G.facet));
+      const int np = on ? 2 * nq : 0;
+      const double h = G.facet >= 0 ? pow(fabs(G.g1.det), 1.0 / D) : 1.0;
+      const double coef = P.hpow == 0 ? P.c : P.c * pow(h, (double)P.hpow);
+      for (int q0 = 0; q0 < 2 * nq; q0 += CH) {
+        for (int qq = a; qq < CH; qq += N2) {
+          const int qi = q0 + qq;
+          if (qi < np) {
+            double x1[3] = {0, 0, 0}, x2[3] = {0, 0, 0}, W;
+            if (qi < nq) {
+#pragma unroll
+              for (int k = 0; k < D; k++) x1[k] = c_rules.x[off + qi][k];
+              map_patch_point<D>(G.g1, G.g2, x1, x2);
+              W = c_rules.w[off + qi] * fabs(G.g1.det);
+            } else {
+              const int m = qi - nq;
+#pragma unroll
+              for (int k = 0; k < D; k++) x2[k] = c_rules.x[off + m][k];
+              map_patch_point<D>(G.g2, G.g1, x2, x1);
+              W = (c_rules.w[off + m] * fabs(G.g2.det) / fabs(G.g1.det)) * fabs(G.g1.det);
+            }
+#pragma unroll
+            for (int k = 0; k < D; k++) {
+              pts[lf][qq][k] = x1[k];
+              pts[lf][qq][D + k] = x2[k];
+            }
+            pts[lf][qq][2 * D] = W * coef;
+          }
+        }
+        __syncthreads();
+        const int nch = min(CH, np - q0);
+        for (int qq = 0; qq < nch; qq++) {
+          T lam[D + 1];
+          T s = 0;
+#pragma unroll
+          for (int k = 0; k < D; k++) {
+            lam[k] = (T)pts[lf][qq][(mine1 ? 0 : D) + k];
+            s += lam[k];
+          }
+          lam[D] = (T)1 - s;
+          T v = eval_fn_value<D, T>(desc, lam);
+          S[lf][qq][a] = mine1 ? v : -v;
+        }
+        __syncthreads();
+        for (int qq = 0; qq < nch; qq++) {
+          const T wa = (T)pts[lf][qq][2 * D] * S[lf][qq][a];
+#pragma unroll
+          for (int b = 0; b < N2; b++) acc[b].add(wa * S[lf][qq][b]);
+        }
+        __syncthreads();
+      }
+    }
+    const int idx = batch * FPB + lf;
+    if (G.facet >= 0 && idx >= cap_fa) {
+      if (a == 0) set_err(err, XG_ERR_CAPACITY);
+    } else if (G.facet >= 0) {
+      T* out = famat + ((int64_t)idx * N2 + a) * N2;
+      bool finite = true;
+#pragma unroll
+      for (int b = 0; b < N2; b++) {
+        T v = acc[b].get();
+        finite &= isfinite(v);
+        out[b] = v;
+      }
+      if (!finite) set_err(err, XG_ERR_NONFINITE);
+    }
+    __syncthreads();
+  }
+}
+
+// ============================================================================
+// Scatter: one warp per active row.  Candidate columns are the dofs of the
+// active elements containing the row's dof and of the active facet patches
+// of those elements; a warp bitonic sort + unique gives the row pattern, and
+// the row's values are summed in the fixed order (adjacent elements
+// ascending, then their facets in local order) -- no atomics.
+// ============================================================================
+struct ScatterArgs {
+  int ne, nd, nfl;
+  int64_t nf;
+  const int32_t* el_dofs;   // [nd][ne]
+  const int32_t* el_facets; // [nfl][ne]
+  const int32_t* fel;       // [2][nf]
+  const int32_t* adj_ptr;
+  const int32_t* adj;
+  const uint32_t* act_un;
+  const uint32_t* act_cut;
+  const uint32_t* act_fa;
+  const int32_t* el_slot;   // valid for active elements
+  const int32_t* fa_slot;   // valid for active facets
+  const int32_t* rows;      // active dofs (row -> dof)
+  const int32_t* dof_row;   // dof -> row (valid for active dofs)
+  const int* counts;        // [3] = nrows
+  int64_t cap_fa;           // facet-patch workspace slots
+  int cap;                  // candidate buffer per warp (pow2)
+  int capu;                 // unique capacity per warp
+};
+
+constexpr int kScWarps = 4;
+
+__device__ __forceinline__ bool el_active(const ScatterArgs& A, int e) {
+  return tbit32(A.act_un, e) || tbit32(A.act_cut, e);
+}
+
+// gathers the candidate dofs of row dof r into buf; returns count (or -1 on overflow)
+__device__ int gather_candidates(const ScatterArgs& A, int r, int* buf) {
+  const int lane = threadIdx.x & 31;
+  const int a0 = A.adj_ptr[r], a1 = A.adj_ptr[r + 1];
+  int total = 0;
+  for (int base = a0; base < a1; base += 32) {
+    const int a = base + lane;
+    int e = -1, ncand = 0;
+    int fmask = 0;
+    if (a < a1) {
+      e = A.adj[a] >> 5;
+      if (el_active(A, e)) ncand += A.nd;
+      for (int lf = 0; lf < A.nfl; lf++) {
+        int f = A.el_facets[(int64_t)lf * A.ne + e];
+        if (tbit32(A.act_fa, f)) {
+          fmask |= 1 << lf;
+          ncand += 2 * A.nd;
+        }
+      }
+    }
+    // warp prefix
+    int x = ncand;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    const int my = total + x - ncand;
+    total += __shfl_sync(0xffffffffu, x, 31);
+    if (total > A.cap) return -1;
+    if (a < a1) {
+      int k = my;
+      if (el_active(A, e))
+        for (int j = 0; j < A.nd; j++) buf[k++] = A.el_dofs[(int64_t)j * A.ne + e];
+      for (int lf = 0; lf < A.nfl; lf++)
+        if (fmask & (1 << lf)) {
+          int f = A.el_facets[(int64_t)lf * A.ne + e];
+          int e1 = A.fel[f], e2 = A.fel[A.nf + f];
+          for (int j = 0; j < A.nd; j++) buf[k++] = A.el_dofs[(int64_t)j * A.ne + e1];
+          for (int j = 0; j < A.nd; j++) buf[k++] = A.el_dofs[(int64_t)j * A.ne + e2];
+        }
+    }
+  }
+  return total;
+}
+
+__device__ void warp_bitonic_sort(int* buf, int n) {
+  const int lane = threadIdx.x & 31;
+  for (int k = 2; k <= n; k <<= 1)
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = lane; i < n; i += 32) {
+        int l = i ^ j;
+        if (l > i) {
+          int x = buf[i], y = buf[l];
+          bool up = (i & k) == 0;
+          if ((x > y) == up) {
+            buf[i] = y;
+            buf[l] = x;
+          }
+        }
+      }
+      __syncwarp();
+    }
+}
+
+// sort + unique in place; returns #unique
+__device__ int warp_sort_unique(int* buf, int n) {
+  const int lane = threadIdx.x & 31;
+  int m = 32;
+  while (m < n) m <<= 1;
+  for (int i = n + lane; i < m; i += 32) buf[i] = 0x7fffffff;
+  __syncwarp();
+  warp_bitonic_sort(buf, m);
+  // compact unique values to the front (stable, ascending)
+  int out = 0;
+  int last = 0;
+  for (int base = 0; base < n; base += 32) {
+    const int i = base + lane;
+    int v = i < n ? buf[i] : 0x7fffffff;
+    int pv = lane == 0 ? last : buf[i - 1];
+    bool keep = i < n && (i == 0 || pv != v);
+    last = __shfl_sync(0xffffffffu, v, 31);
+    unsigned mk = __ballot_sync(0xffffffffu, keep);
+    __syncwarp();
+    if (keep) buf[out + __popc(mk & ((1u << lane) - 1))] = v;
+    out += __popc(mk);
+    __syncwarp();
+  }
+  return out;
+}
+
+__global__ void __launch_bounds__(kScWarps * 32) k_rowcount(ScatterArgs A, int64_t* rowcnt, int* err) {
+  extern __shared__ int sm_sc[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int* buf = sm_sc + warp * A.cap;
+  const int nrows = A.counts[3];
+  for (int row = blockIdx.x * kScWarps + warp; row < nrows; row += gridDim.x * kScWarps) {
+    const int r = A.rows[row];
+    int n = gather_candidates(A, r, buf);
+    __syncwarp();
+    if (n < 0) {
+      if (lane == 0) set_err(err, XG_ERR_CAPACITY);
+      n = 0;
+    }
+    int u = warp_sort_unique(buf, n);
+    if (u > A.capu && lane == 0) set_err(err, XG_ERR_CAPACITY);
+    if (lane == 0) rowcnt[row] = u;
+    __syncwarp();
+  }
+}
+
+__device__ __forceinline__ int lower_bound_sm(const int* a, int n, int v) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (a[mid] < v) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kScWarps * 32) k_rowfill(ScatterArgs A, const T* __restrict__ elmat,
+                                                           const T* __restrict__ famat,
+                                                           const int64_t* __restrict__ rowptr,
+                                                           int32_t* __restrict__ cols, double* __restrict__ vals,
+                                                           int64_t cap_nnz, int* err) {
+  extern __shared__ int sm_sc[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int* buf = sm_sc + warp * A.cap;
+  double* acc = (double*)(sm_sc + kScWarps * A.cap) + warp * A.capu;
+  const int nrows = A.counts[3];
+  const int nd = A.nd, n2 = 2 * nd;
+  for (int row = blockIdx.x * kScWarps + warp; row < nrows; row += gridDim.x * kScWarps) {
+    const int r = A.rows[row];
+    int n = gather_candidates(A, r, buf);
+    __syncwarp();
+    if (n < 0) n = 0;
+    int u = warp_sort_unique(buf, n);
+    if (u > A.capu) u = A.capu;
+    const int64_t rp = rowptr[row];
+    if (rp + u > cap_nnz) {
+      if (lane == 0) set_err(err, XG_ERR_CAPACITY);
+      continue;
+    }
+    for (int k = lane; k < u; k += 32) acc[k] = 0.0;
+    __syncwarp();
+    const int a0 = A.adj_ptr[r], a1 = A.adj_ptr[r + 1];
+    for (int a = a0; a < a1; a++) {
+      const int e = A.adj[a] >> 5, i = A.adj[a] & 31;
+      if (el_active(A, e)) {
+        const T* m = elmat + ((int64_t)A.el_slot[e] * nd + i) * nd;
+        if (lane < nd) {
+          int c = A.el_dofs[(int64_t)lane * A.ne + e];
+          int pos = lower_bound_sm(buf, u, c);
+          if (pos < u) acc[pos] += (double)m[lane];
+        }
+        __syncwarp();
+      }
+      for (int lf = 0; lf < A.nfl; lf++) {
+        const int f = A.el_facets[(int64_t)lf * A.ne + e];
+        if (!tbit32(A.act_fa, f)) continue;
+        const int e1 = A.fel[f], e2 = A.fel[A.nf + f];
+        const int prow = (e == e1) ? i : nd + i;
+        if (A.fa_slot[f] >= A.cap_fa) continue;
+        const T* m = famat + ((int64_t)A.fa_slot[f] * n2 + prow) * n2;
+        for (int half = 0; half < 2; half++) {
+          const int eh = half == 0 ? e1 : e2;
+          for (int j = lane; j < nd; j += 32) {
+            int c = A.el_dofs[(int64_t)j * A.ne + eh];
+            int pos = lower_bound_sm(buf, u, c);
+            if (pos < u) acc[pos] += (double)m[half * nd + j];
+          }
+          __syncwarp();
+        }
+      }
+    }
+    for (int k = lane; k < u; k += 32) {
+      cols[rp + k] = A.dof_row[buf[k]];
+      vals[rp + k] = acc[k];
+    }
+    __syncwarp();
+  }
+}
+
+}  // namespace xg
+
+using namespace xg;
+
+// ============================================================================
+// The form object
+// ============================================================================
+struct xg_form {
+  xg_space* space = nullptr;
+  xg_mesh* mesh = nullptr;
+  int precision = XG_PREC_FP64;
+  std::vector<xg_term> terms;
+  std::vector<int> term_slot;  // group index (volume) or patch index
+  FormDesc desc;
+  int needs_mask = 0;  // domains needing decompositions on cut elements
+  int64_t nw32_el = 0, nw32_fa = 0, nw32_dof = 0;
+  int64_t cap_el = 0, cap_fa = 0;
+  // workspace
+  uint32_t* d_act_un = nullptr;
+  uint32_t* d_act_cut = nullptr;
+  uint32_t* d_act_fa = nullptr;
+  uint32_t* d_dof_bits = nullptr;
+  int32_t* d_l_un = nullptr;
+  int32_t* d_l_cut = nullptr;
+  int32_t* d_l_fa = nullptr;
+  int32_t* d_el_slot = nullptr;
+  int32_t* d_fa_slot = nullptr;
+  int32_t* d_dof_row = nullptr;
+  int64_t* d_rowcnt = nullptr;
+  int* d_counts = nullptr;  // [n_uncut, n_cut, n_facets, n_rows]
+  int* d_bsum = nullptr;    // compaction block sums
+  int nbsum = 0;
+  long long* d_bsum64 = nullptr;
+  int nbsum64 = 0;
+  void* d_elmat = nullptr;
+  void* d_famat = nullptr;
+  int* d_err = nullptr;
+  int sc_cap = 0, sc_capu = 0;
+  size_t sc_smem = 0;
+  int grid_el_un = 0, grid_el_cut = 0, grid_fa = 0, grid_sc = 0;
+  // CutFEM step state
+  uint8_t* d_dom = nullptr;
+  double* d_ratio = nullptr;
+  uint64_t* d_bits = nullptr;
+  uint64_t* d_fbits = nullptr;
+  bool has_patch = false;
+  cudaEvent_t ev[8] = {};
+  bool use_ev = false;
+};
+
+namespace {
+
+int form_free(xg_form* f) {
+  void* ptrs[] = {f->d_act_un, f->d_act_cut, f->d_act_fa, f->d_dof_bits, f->d_l_un, f->d_l_cut, f->d_l_fa,
+                  f->d_el_slot, f->d_fa_slot, f->d_dof_row, f->d_rowcnt, f->d_counts, f->d_bsum, f->d_bsum64,
+                  f->d_elmat, f->d_famat, f->d_err, f->d_dom, f->d_ratio, f->d_bits, f->d_fbits};
+  for (void* p : ptrs) cudaFree(p);
+  delete f;
+  return XG_OK;
+}
+
+int default_order(int kind, int k) {
+  switch (kind) {
+    case XG_TERM_MASS: return 2 * k;
+    case XG_TERM_LAPLACE: return 2 * k - 2;
+    case XG_TERM_NGRADU_V:
+    case XG_TERM_U_NGRADV:
+    case XG_TERM_CONV: return 2 * k - 1;
+    case XG_TERM_GHOST_MASS: return 2 * k;
+  }
+  return 2 * k;
+}
+
+// rebuild the group table from the term list
+int build_desc(xg_form* f) {
+  FormDesc& d = f->desc;
+  std::memset(&d, 0, sizeof(d));
+  f->term_slot.assign(f->terms.size(), -1);
+  f->needs_mask = 0;
+  f->has_patch = false;
+  for (size_t t = 0; t < f->terms.size(); t++) {
+    const xg_term& T = f->terms[t];
+    const int order = T.order >= 0 ? T.order : default_order(T.kind, f->space->order);
+    if (order > kMaxOrder) {
+      set_last_error("xg_form: integration order above 8");
+      return XG_ERR_UNSUPPORTED;
+    }
+    if (T.kind == XG_TERM_GHOST_MASS) {
+      if (d.npatch >= kMaxPatch) return XG_ERR_UNSUPPORTED;
+      PatchDesc& P = d.p[d.npatch];
+      P.order = order;
+      P.defined_on = T.d_defined_on;
+      P.c = T.coef;
+      P.hpow = T.hpow;
+      f->term_slot[t] = d.npatch++;
+      f->has_patch = true;
+      continue;
+    }
+    if (T.kind < 0 || T.kind > XG_TERM_CONV || T.domain < 0 || T.domain > 2) {
+      set_last_error("xg_form: bad term kind or domain");
+      return XG_ERR_ARG;
+    }
+    int g = -1;
+    for (int q = 0; q < d.ngroups; q++) {
+      const GroupDesc& G = d.g[q];
+      bool same_b = T.kind != XG_TERM_CONV || !(G.used & (1 << XG_TERM_CONV)) ||
+                    (G.b[0] == T.b[0] && G.b[1] == T.b[1] && G.b[2] == T.b[2]);
+      if (G.domain == T.domain && G.order == order && G.defined_on == T.d_defined_on && same_b &&
+          !(G.used & (1 << T.kind)))
+        g = q;
+    }
+    if (g < 0) {
+      if (d.ngroups >= kMaxGroups) {
+        set_last_error("xg_form: too many term groups");
+        return XG_ERR_UNSUPPORTED;
+      }
+      g = d.ngroups++;
+      d.g[g].domain = T.domain;
+      d.g[g].order = order;
+      d.g[g].defined_on = T.d_defined_on;
+    }
+    GroupDesc& G = d.g[g];
+    G.c[T.kind] = T.coef;
+    G.hpow[T.kind] = T.hpow;
+    G.used |= 1 << T.kind;
+    if (T.kind == XG_TERM_CONV)
+      for (int k = 0; k < 3; k++) G.b[k] = T.b[k];
+    f->term_slot[t] = g;
+    f->needs_mask |= 1 << T.domain;
+  }
+  return XG_OK;
+}
+
+template <class K>
+int grid_for(K kernel, int threads, size_t smem) {
+  int dev = 0, nsm = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, smem);
+  if (per < 1) per = 1;
+  return nsm * per;
+}
+
+int compact(xg_form* f, const uint32_t* bits, int64_t nw32, int32_t* list, int32_t* slot, int* count_out,
+            cudaStream_t s, const int* slot_base = nullptr) {
+  const int nb = (int)((nw32 + kCChunk - 1) / kCChunk);
+  if (nb > f->nbsum) return XG_ERR_CAPACITY;
+  k_popc_blocks<<<nb, kCThreads, 0, s>>>(bits, nw32, f->d_bsum);
+  k_scan_small<<<1, 1024, 0, s>>>(f->d_bsum, nb, count_out);
+  k_write_list<<<nb, kCThreads, 0, s>>>(bits, nw32, f->d_bsum, list, slot, slot_base);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? XG_OK : cuda_fail(e, "compact");
+}
+
+template <int D, int K, typename T>
+int launch_volume(xg_form* f, const double* d_lset, const uint8_t* d_dom, cudaStream_t s) {
+  using CU = ElCfg<D, K, false, T>;
+  using CC = ElCfg<D, K, true, T>;
+  xg_mesh* m = f->mesh;
+  auto ku = k_elmat<D, K, false, T>;
+  auto kc = k_elmat<D, K, true, T>;
+  if (!f->grid_el_un) {
+    f->grid_el_un = grid_for(ku, CU::NT, 0);
+    f->grid_el_cut = grid_for(kc, CC::NT, 0);
+  }
+  ku<<<f->grid_el_un, CU::NT, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, d_lset, d_dom, f->desc, f->d_l_un,
+                                     f->d_counts, 0, (T*)f->d_elmat, f->d_err, f->needs_mask);
+  if (f->use_ev) cudaEventRecord(f->ev[3], s);
+  kc<<<f->grid_el_cut, CC::NT, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, d_lset, d_dom, f->desc, f->d_l_cut,
+                                      f->d_counts, 1, (T*)f->d_elmat, f->d_err, f->needs_mask);
+  if (f->use_ev) cudaEventRecord(f->ev[4], s);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? XG_OK : cuda_fail(e, "k_elmat");
+}
+
+template <int D, int K, typename T>
+int launch_patch(xg_form* f, cudaStream_t s) {
+  using C = PaCfg<D, K>;
+  xg_mesh* m = f->mesh;
+  auto kp = k_patch<D, K, T>;
+  if (!f->grid_fa) f->grid_fa = grid_for(kp, C::NT, 0);
+  kp<<<f->grid_fa, C::NT, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, m->nfacets, m->d_facet_els, f->desc, f->d_l_fa,
+                                  f->d_counts, (T*)f->d_famat, f->cap_fa, f->d_err);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? XG_OK : cuda_fail(e, "k_patch");
+}
+
+template <typename T>
+int dispatch_volume(xg_form* f, const double* d_lset, const uint8_t* d_dom, cudaStream_t s) {
+  const int D = f->mesh->dim, K = f->space->order;
+  if (D == 2) {
+    if (K == 1) return launch_volume<2, 1, T>(f, d_lset, d_dom, s);
+    if (K == 2) return launch_volume<2, 2, T>(f, d_lset, d_dom, s);
+    return launch_volume<2, 3, T>(f, d_lset, d_dom, s);
+  }
+  if (K == 1) return launch_volume<3, 1, T>(f, d_lset, d_dom, s);
+  if (K == 2) return launch_volume<3, 2, T>(f, d_lset, d_dom, s);
+  return launch_volume<3, 3, T>(f, d_lset, d_dom, s);
+}
+
+template <typename T>
+int dispatch_patch(xg_form* f, cudaStream_t s) {
+  const int D = f->mesh->dim, K = f->space->order;
+  if (D == 2) {
+    if (K == 1) return launch_patch<2, 1, T>(f, s);
+    if (K == 2) return launch_patch<2, 2, T>(f, s);
+    return launch_patch<2, 3, T>(f, s);
+  }
+  if (K == 1) return launch_patch<3, 1, T>(f, s);
+  if (K == 2) return launch_patch<3, 2, T>(f, s);
+  return launch_patch<3, 3, T>(f, s);
+}
+
+ScatterArgs scatter_args(xg_form* f) {
+  ScatterArgs A;
+  xg_mesh* m = f->mesh;
+  xg_space* sp = f->space;
+  A.ne = m->ne;
+  A.nd = sp->nd;
+  A.nfl = m->dim + 1;
+  A.nf = m->nfacets;
+  A.el_dofs = sp->d_el_dofs;
+  A.el_facets = m->d_el_facets;
+  A.fel = m->d_facet_els;
+  A.adj_ptr = sp->d_dof_adj_ptr;
+  A.adj = sp->d_dof_adj;
+  A.act_un = f->d_act_un;
+  A.act_cut = f->d_act_cut;
+  A.act_fa = f->d_act_fa;
+  A.el_slot = f->d_el_slot;
+  A.fa_slot = f->d_fa_slot;
+  A.rows = nullptr;
+  A.dof_row = f->d_dof_row;
+  A.counts = f->d_counts;
+  A.cap_fa = f->cap_fa;
+  A.cap = f->sc_cap;
+  A.capu = f->sc_capu;
+  return A;
+}
+
+}  // namespace
+
+extern "C" {
+
+int xg_form_create(xg_space* space, const xg_term* terms, int32_t nterms, int precision, xg_form** out) {
+  if (!space || !out || (nterms > 0 && !terms) || nterms < 0 ||
+      (precision != XG_PREC_FP64 && precision != XG_PREC_MIXED)) {
+    set_last_error("xg_form_create: bad arguments");
+    return XG_ERR_ARG;
+  }
+  *out = nullptr;
+  auto* f = new xg_form();
+  f->space = space;
+  f->mesh = space->mesh;
+  f->precision = precision;
+  f->terms.assign(terms, terms + nterms);
+  int st = build_desc(f);
+  if (st) {
+    delete f;
+    return st;
+  }
+  xg_mesh* m = f->mesh;
+  const int nd = space->nd;
+  const size_t esz = precision == XG_PREC_FP64 ? sizeof(double) : sizeof(float);
+  f->nw32_el = 2 * ((m->ne + 63) / 64);
+  f->nw32_fa = 2 * ((m->nfacets + 63) / 64);
+  f->nw32_dof = 2 * ((space->ndof + 63) / 64);
+  f->cap_el = m->ne;
+  // facet-patch workspace: all facets when small, else a quarter of them
+  const size_t fa_bytes = (size_t)m->nfacets * (2 * nd) * (2 * nd) * esz;
+  f->cap_fa = fa_bytes <= ((size_t)4 << 30) ? m->nfacets : std::max<int64_t>(m->nfacets / 4, 1);
+  int64_t maxw = std::max(f->nw32_el, std::max(f->nw32_fa, f->nw32_dof));
+  f->nbsum = (int)((maxw + kCChunk - 1) / kCChunk) + 1;
+  f->nbsum64 = (int)((space->ndof + kSChunk - 1) / kSChunk) + 1;
+  // scatter buffers
+  const int nfl = m->dim + 1;
+  int maxc = space->max_adj * (nd + (f->has_patch ? nfl * 2 * nd : 0));
+  int cap = 32;
+  while (cap < maxc) cap <<= 1;
+  f->sc_cap = cap;
+  f->sc_capu = std::min(cap, 2048);
+  f->sc_smem = (size_t)kScWarps * (cap * sizeof(int) + f->sc_capu * sizeof(double));
+  auto A = [&](void** p, size_t bytes) { return cudaMalloc(p, bytes ? bytes : 16); };
+  cudaError_t e = cudaSuccess;
+  e = e ? e : A((void**)&f->d_act_un, f->nw32_el * 4);
+  e = e ? e : A((void**)&f->d_act_cut, f->nw32_el * 4);
+  e = e ? e : A((void**)&f->d_act_fa, f->nw32_fa * 4);
+  e = e ? e : A((void**)&f->d_dof_bits, f->nw32_dof * 4);
+  e = e ? e : A((void**)&f->d_l_un, (size_t)m->ne * 4);
+  e = e ? e : A((void**)&f->d_l_cut, (size_t)m->ne * 4);
+  e = e ? e : A((void**)&f->d_l_fa, (size_t)m->nfacets * 4);
+  e = e ? e : A((void**)&f->d_el_slot, (size_t)m->ne * 4);
+  e = e ? e : A((void**)&f->d_fa_slot, (size_t)m->nfacets * 4);
+  e = e ? e : A((void**)&f->d_dof_row, (size_t)space->ndof * 4);
+  e = e ? e : A((void**)&f->d_rowcnt, (size_t)space->ndof * 8);
+  e = e ? e : A((void**)&f->d_counts, 8 * sizeof(int));
+  e = e ? e : A((void**)&f->d_bsum, (size_t)f->nbsum * 4);
+  e = e ? e : A((void**)&f->d_bsum64, (size_t)f->nbsum64 * 8);
+  e = e ? e : A(&f->d_elmat, (size_t)f->cap_el * nd * nd * esz);
+  e = e ? e : A(&f->d_famat, f->has_patch ? (size_t)f->cap_fa * 4 * nd * nd * esz : 16);
+  e = e ? e : A((void**)&f->d_err, sizeof(int));
+  e = e ? e : A((void**)&f->d_dom, (size_t)m->ne);
+  e = e ? e : A((void**)&f->d_ratio, (size_t)m->ne * 8);
+  e = e ? e : A((void**)&f->d_bits, (size_t)8 * (f->nw32_el / 2) * 8);
+  e = e ? e : A((void**)&f->d_fbits, (size_t)(f->nw32_fa / 2) * 8);
+  if (e == cudaSuccess) e = cudaMemset(f->d_err, 0, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(f->d_counts, 0, 8 * sizeof(int));
+  if (e != cudaSuccess) {
+    form_free(f);
+    return cuda_fail(e, "xg_form_create");
+  }
+  {
+    // the attribute is an upper bound shared by all forms: only ever raise it
+    static std::mutex mu;
+    static size_t raised = 48 * 1024;
+    std::lock_guard<std::mutex> lock(mu);
+    if (f->sc_smem > raised) {
+      if (cudaFuncSetAttribute(k_rowcount, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->sc_smem) ||
+          cudaFuncSetAttribute(k_rowfill<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->sc_smem) ||
+          cudaFuncSetAttribute(k_rowfill<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->sc_smem)) {
+        form_free(f);
+        set_last_error("xg_form_create: scatter shared memory too large for this mesh");
+        return XG_ERR_CAPACITY;
+      }
+      raised = f->sc_smem;
+    }
+  }
+  f->grid_sc = grid_for(k_rowcount, kScWarps * 32, f->sc_smem);
+  *out = f;
+  return XG_OK;
+}
+
+int xg_form_destroy(xg_form* f) {
+  if (!f) return XG_OK;
+  return form_free(f);
+}
+
+int xg_form_set_defined_on(xg_form* f, int32_t t, const uint64_t* d_defined_on) {
+  if (!f || t < 0 || t >= (int)f->terms.size()) return XG_ERR_ARG;
+  f->terms[t].d_defined_on = d_defined_on;
+  return build_desc(f);
+}
+
+int xg_form_capacity(const xg_form* f, int64_t* o) {
+  if (!f || !o) return XG_ERR_ARG;
+  // exact pattern size when every element and every interior facet is active
+  // (the largest pattern any level set can produce on this mesh)
+  const xg_space* sp = f->space;
+  const xg_mesh* m = f->mesh;
+  const int nd = sp->nd, nfl = m->dim + 1, ne = m->ne;
+  const int64_t ndof = sp->ndof;
+  const std::vector<int32_t>& ed = sp->h_el_dofs;
+  const std::vector<int32_t>& efa = m->dim == 2 ? m->h_el_edges : m->h_el_faces;
+  const int efs = m->dim == 2 ? 3 : 4;
+  std::vector<int32_t> ptr(ndof + 1, 0), adj(ed.size());
+  for (size_t k = 0; k < ed.size(); k++) ptr[ed[k] + 1]++;
+  for (int64_t r = 0; r < ndof; r++) ptr[r + 1] += ptr[r];
+  {
+    std::vector<int32_t> fill(ptr.begin(), ptr.end() - 1);
+    for (int e = 0; e < ne; e++)
+      for (int k = 0; k < nd; k++) adj[fill[ed[(size_t)e * nd + k]]++] = e;
+  }
+  const int nth = std::max(1, std::min(16, (int)std::thread::hardware_concurrency()));
+  std::vector<int64_t> part(nth, 0);
+  std::vector<std::thread> th;
+  for (int t = 0; t < nth; t++)
+    th.emplace_back([&, t]() {
+      std::vector<int32_t> c;
+      int64_t sum = 0;
+      for (int64_t r = t; r < ndof; r += nth) {
+        c.clear();
+        for (int a = ptr[r]; a < ptr[r + 1]; a++) {
+          int e = adj[a];
+          c.insert(c.end(), ed.begin() + (size_t)e * nd, ed.begin() + (size_t)(e + 1) * nd);
+          if (f->has_patch)
+            for (int lf = 0; lf < nfl; lf++) {
+              int fc = efa[(size_t)e * efs + lf];
+              int e2 = m->h_facet_els[2 * (size_t)fc] == e ? m->h_facet_els[2 * (size_t)fc + 1] : m->h_facet_els[2 * (size_t)fc];
+              if (e2 >= 0) c.insert(c.end(), ed.begin() + (size_t)e2 * nd, ed.begin() + (size_t)(e2 + 1) * nd);
+            }
+        }
+        std::sort(c.begin(), c.end());
+        sum += std::unique(c.begin(), c.end()) - c.begin();
+      }
+      part[t] = sum;
+    });
+  for (auto& x : th) x.join();
+  int64_t nnz = 0;
+  for (auto v : part) nnz += v;
+  o[0] = ndof;
+  o[1] = nnz;
+  return XG_OK;
+}
+
+int xg_form_check(xg_form* f) {
+  if (!f) return XG_ERR_ARG;
+  int h = 0;
+  XG_CUDA(cudaMemcpy(&h, f->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  XG_CUDA(cudaMemset(f->d_err, 0, sizeof(int)));
+  if (h) set_last_error(std::string("device error: ") + xg_status_string(h));
+  return h;
+}
+
+int xg_form_assemble(xg_form* f, const double* d_lset, const uint8_t* d_dom, xg_csr* out, void* stream) {
+  if (!f || !d_lset || !d_dom || !out || !out->d_row_dof || !out->d_rowptr || !out->d_cols || !out->d_vals ||
+      !out->d_counts)
+    return XG_ERR_ARG;
+  if (out->cap_rows < f->space->ndof) {
+    set_last_error("xg_form_assemble: cap_rows below ndof");
+    return XG_ERR_CAPACITY;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  xg_mesh* m = f->mesh;
+  xg_space* sp = f->space;
+  int st;
+  // 1. active elements / facets and their lists
+  k_active_elements<<<(unsigned)((f->nw32_el * 32 + 255) / 256), 256, 0, s>>>(m->ne, d_dom, f->desc, f->d_act_un,
+                                                                              f->d_act_cut, f->nw32_el);
+  if ((st = compact(f, f->d_act_un, f->nw32_el, f->d_l_un, f->d_el_slot, f->d_counts + 0, s))) return st;
+  if ((st = compact(f, f->d_act_cut, f->nw32_el, f->d_l_cut, f->d_el_slot, f->d_counts + 1, s, f->d_counts + 0)))
+    return st;
+  if (f->has_patch) {
+    k_active_facets<<<(unsigned)((f->nw32_fa * 32 + 255) / 256), 256, 0, s>>>(m->nfacets, m->d_facet_els, f->desc,
+                                                                              f->d_act_fa, f->nw32_fa);
+    if ((st = compact(f, f->d_act_fa, f->nw32_fa, f->d_l_fa, f->d_fa_slot, f->d_counts + 2, s))) return st;
+  } else {
+    XG_CUDA(cudaMemsetAsync(f->d_act_fa, 0, f->nw32_fa * 4, s));
+    XG_CUDA(cudaMemsetAsync(f->d_counts + 2, 0, sizeof(int), s));
+  }
+  if (f->use_ev) cudaEventRecord(f->ev[2], s);
+  // 2. element and patch matrices (the cut list's slots follow the uncut list's)
+  if (f->precision == XG_PREC_FP64) {
+    if ((st = dispatch_volume<double>(f, d_lset, d_dom, s))) return st;
+    if (f->has_patch && (st = dispatch_patch<double>(f, s))) return st;
+  } else {
+    if ((st = dispatch_volume<float>(f, d_lset, d_dom, s))) return st;
+    if (f->has_patch && (st = dispatch_patch<float>(f, s))) return st;
+  }
+  if (f->use_ev) cudaEventRecord(f->ev[5], s);
+  // 3. active dofs -> rows
+  XG_CUDA(cudaMemsetAsync(f->d_dof_bits, 0, f->nw32_dof * 4, s));
+  k_mark_dofs<<<152 * 8, 256, 0, s>>>(m->ne, sp->nd, sp->d_el_dofs, f->d_l_un, f->d_l_cut, f->d_l_fa, f->d_counts,
+                                      m->nfacets, m->d_facet_els, f->d_dof_bits);
+  if ((st = compact(f, f->d_dof_bits, f->nw32_dof, out->d_row_dof, f->d_dof_row, f->d_counts + 3, s))) return st;
+  // 4. pattern and values
+  ScatterArgs A = scatter_args(f);
+  A.rows = out->d_row_dof;
+  k_rowcount<<<f->grid_sc, kScWarps * 32, f->sc_smem, s>>>(A, f->d_rowcnt, f->d_err);
+  const int nb64 = (int)((sp->ndof + kSChunk - 1) / kSChunk);
+  k_sum64_blocks<<<nb64, kSThreads, 0, s>>>(f->d_rowcnt, f->d_counts + 3, f->d_bsum64);
+  k_scan64_small<<<1, 1024, 0, s>>>(f->d_bsum64, nb64);
+  k_scan64_apply<<<nb64, kSThreads, 0, s>>>(f->d_rowcnt, f->d_counts + 3, f->d_bsum64, out->d_rowptr, out->d_counts,
+                                            out->cap_nnz, f->d_err);
+  if (f->use_ev) cudaEventRecord(f->ev[6], s);
+  if (f->precision == XG_PREC_FP64)
+    k_rowfill<double><<<f->grid_sc, kScWarps * 32, f->sc_smem, s>>>(A, (const double*)f->d_elmat,
+                                                                    (const double*)f->d_famat, out->d_rowptr,
+                                                                    out->d_cols, out->d_vals, out->cap_nnz, f->d_err);
+  else
+    k_rowfill<float><<<f->grid_sc, kScWarps * 32, f->sc_smem, s>>>(A, (const float*)f->d_elmat,
+                                                                   (const float*)f->d_famat, out->d_rowptr,
+                                                                   out->d_cols, out->d_vals, out->cap_nnz, f->d_err);
+  if (f->use_ev) cudaEventRecord(f->ev[7], s);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? XG_OK : cuda_fail(e, "xg_form_assemble");
+}
+
+int xg_cutfem_step(xg_form* f, const double* d_lset, xg_csr* out, void* stream) {
+  if (!f || !d_lset || !out) return XG_ERR_ARG;
+  xg_mesh* m = f->mesh;
+  if (f->use_ev) cudaEventRecord(f->ev[0], (cudaStream_t)stream);
+  int st = xg_cutinfo_update(m, d_lset, f->d_dom, f->d_ratio, f->d_bits, stream);
+  if (st) return st;
+  const int64_t nw = f->nw32_el / 2;
+  const uint64_t* hasneg = f->d_bits + XG_CDOM_HASNEG * nw;
+  const uint64_t* ifb = f->d_bits + XG_CDOM_IF * nw;
+  const uint64_t* haspos = f->d_bits + XG_CDOM_HASPOS * nw;
+  if (f->has_patch) {
+    st = xg_facets_with_neighbor_types(m, hasneg, ifb, 1, 1, 1, f->d_fbits, stream);
+    if (st) return st;
+  }
+  // effective element / facet sets of the CutFEM form
+  FormDesc saved = f->desc;
+  for (int q = 0; q < f->desc.ngroups; q++) {
+    GroupDesc& G = f->desc.g[q];
+    G.defined_on = G.domain == XG_NEG ? hasneg : (G.domain == XG_IF ? ifb : haspos);
+  }
+  for (int p = 0; p < f->desc.npatch; p++) f->desc.p[p].defined_on = f->d_fbits;
+  if (f->use_ev) cudaEventRecord(f->ev[1], (cudaStream_t)stream);
+  st = xg_form_assemble(f, d_lset, f->d_dom, out, stream);
+  f->desc = saved;
+  return st;
+}
+
+int xg_form_stage_events(xg_form* f, void* const* events, int n) {
+  if (!f || (n != 0 && n != 8) || (n == 8 && !events)) return XG_ERR_ARG;
+  f->use_ev = n == 8;
+  for (int i = 0; i < 8; i++) f->ev[i] = n == 8 ? (cudaEvent_t)events[i] : nullptr;
+  return XG_OK;
+}
+
+int xg_cutfem_marking(xg_form* f, const uint8_t** d_dom, const double** d_ratio, const uint64_t** d_bits,
+                      const uint64_t** d_facets) {
+  if (!f) return XG_ERR_ARG;
+  if (d_dom) *d_dom = f->d_dom;
+  if (d_ratio) *d_ratio = f->d_ratio;
+  if (d_bits) *d_bits = f->d_bits;
+  if (d_facets) *d_facets = f->d_fbits;
+  return XG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,373 @@
+// Marking, rule export and integration kernels of libxg.
+// This translation unit is compiled with -fmad=false: cut points, sub-simplex
+// volumes, cut ratios and rule points/weights follow the CPU statement of
+// ngsxfem's straightcutrule.cpp operation by operation.
+#include <algorithm>
+#include <mutex>
+
+#include "xg_cut.cuh"
+#include "xg_internal.h"
+
+namespace xg {
+
+static __constant__ RuleTable c_rules;
+
+int upload_rules_asm();  // xg_asm.cu
+
+int ensure_device_rules() {
+  static std::mutex mu;
+  static std::vector<int> done;
+  int dev = 0;
+  XG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  if (std::find(done.begin(), done.end(), dev) != done.end()) return XG_OK;
+  XG_CUDA(cudaMemcpyToSymbol(c_rules, &host_rules(), sizeof(RuleTable)));
+  int st = upload_rules_asm();
+  if (st) return st;
+  done.push_back(dev);
+  return XG_OK;
+}
+
+// ---- InterpolateToP1 perturbation (utils/p1interpol.cpp:104-107) -------------------
+__global__ void k_perturb(double* v, int64_t n, double eps) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if (fabs(v[i]) < eps) v[i] = eps;
+}
+
+// ---- CutInformation::Update, element part (xfem/cutinfo.cpp:83-132) ------------------
+// One thread per element, 32 elements per warp; the warp's ballots are the
+// 32-bit words of the 8 combined-domain bitsets.
+template <int D>
+__global__ void k_cutinfo(int ne, const int32_t* __restrict__ elv, const double* __restrict__ lset,
+                          uint8_t* __restrict__ dom, double* __restrict__ ratio, uint32_t* __restrict__ bits,
+                          int64_t nw32, int* err) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool valid = e < ne;
+  int t = XG_POS;
+  if (valid) {
+    double l[D + 1];
+#pragma unroll
+    for (int i = 0; i <= D; i++) l[i] = __ldg(&lset[__ldg(&elv[(int64_t)i * ne + e])]);
+    const double w0 = c_rules.w[c_rules.off[D][0]];
+    double part_vol[2] = {0.0, 0.0};
+    int cdom = check_if_straight_cut(l, D + 1);
+    if (cdom == XG_IF) {
+      // order-0 cut rules for POS then NEG, weights summed in rule order
+#pragma unroll
+      for (int pass = 0; pass < 2; pass++) {
+        const int np = pass == 0 ? XG_POS : XG_NEG;
+        Sub subs[3];
+        int ns = decompose<D>(l, np, subs);
+        if (ns < 0) {
+          set_err(err, -ns);
+          ns = 0;
+        }
+        const double wb = c_rules.w[c_rules.off[D][0]];
+        for (int s = 0; s < ns; s++) part_vol[np] += wb * simplex_volume(subs[s].p, D + 1);
+      }
+    } else {
+      part_vol[cdom] += w0;
+    }
+    ratio[e] = part_vol[XG_NEG] / (part_vol[XG_NEG] + part_vol[XG_POS]);
+    if (part_vol[XG_NEG] > 0.0) t = (part_vol[XG_POS] > 0.0) ? XG_IF : XG_NEG;
+    else t = XG_POS;
+    dom[e] = (uint8_t)t;
+  }
+  const unsigned mneg = __ballot_sync(0xffffffffu, valid && t == XG_NEG);
+  const unsigned mpos = __ballot_sync(0xffffffffu, valid && t == XG_POS);
+  const unsigned mif = __ballot_sync(0xffffffffu, valid && t == XG_IF);
+  const unsigned many = __ballot_sync(0xffffffffu, valid);
+  const int64_t w = e >> 5;
+  if ((threadIdx.x & 31) == 0 && w < nw32) {
+    bits[0 * nw32 + w] = 0u;
+    bits[1 * nw32 + w] = mneg;
+    bits[2 * nw32 + w] = mpos;
+    bits[3 * nw32 + w] = mneg | mpos;
+    bits[4 * nw32 + w] = mif;
+    bits[5 * nw32 + w] = mneg | mif;
+    bits[6 * nw32 + w] = mpos | mif;
+    bits[7 * nw32 + w] = many;
+  }
+}
+
+__device__ __forceinline__ bool tbit(const uint64_t* b, int64_t i) { return (b[i >> 6] >> (i & 63)) & 1ull; }
+
+// ---- GetFacetsWithNeighborTypes (xfem/cutinfo.cpp:476-538) ----------------------------
+__global__ void k_facet_mark(int64_t nf, const int32_t* __restrict__ fel, const uint64_t* __restrict__ a,
+                             const uint64_t* __restrict__ b, int bnd_a, int bnd_b, int use_and, uint32_t* out,
+                             int64_t nw32) {
+  const int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  bool set = false;
+  if (f < nf) {
+    int l = fel[f], r = fel[nf + f];
+    bool al = tbit(a, l), bl = tbit(b, l);
+    bool ar = r >= 0 ? tbit(a, r) : (bool)bnd_a;
+    bool br = r >= 0 ? tbit(b, r) : (bool)bnd_b;
+    set = use_and ? ((al && br) || (ar && bl)) : ((al || br) || (ar || bl));
+  }
+  const unsigned m = __ballot_sync(0xffffffffu, set);
+  if ((threadIdx.x & 31) == 0 && (f >> 5) < nw32) out[f >> 5] = m;
+}
+
+// ---- GetElementsWithNeighborFacets (xfem/cutinfo.cpp:540-566) --------------------------
+__global__ void k_el_nbr_facets(int64_t nf, const int32_t* __restrict__ fel, const uint64_t* __restrict__ fb,
+                                unsigned long long* out) {
+  const int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (f >= nf || !tbit(fb, f)) return;
+  for (int s = 0; s < 2; s++) {
+    int e = fel[s * nf + f];
+    if (e >= 0) atomicOr(&out[e >> 6], 1ull << (e & 63));
+  }
+}
+
+// ---- StraightCutIntegrationRule export (cutint/straightcutrule.cpp:582-677) ------------
+template <int D>
+__global__ void k_cut_rules(int ne, const int32_t* __restrict__ elv, const double* __restrict__ xyz, int nv,
+                            const double* __restrict__ lset, const int32_t* __restrict__ elems, int n, int dt,
+                            int order, int max_pts, int32_t* counts, double* pts, double* wts, int* err) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int e = elems[i];
+  double l[D + 1];
+  double xv[D + 1][3];
+#pragma unroll
+  for (int v = 0; v <= D; v++) {
+    int vid = elv[(int64_t)v * ne + e];
+    l[v] = lset[vid];
+#pragma unroll
+    for (int c = 0; c < 3; c++) xv[v][c] = c < D ? xyz[(int64_t)c * nv + vid] : 0.0;
+  }
+  const int cdom = check_if_straight_cut(l, D + 1);
+  const int p = clamp_order(order);
+  double* P = pts + (int64_t)i * max_pts * 3;
+  double* W = wts + (int64_t)i * max_pts;
+  if (cdom != XG_IF) {
+    if (cdom != dt) { counts[i] = -1; return; }
+    const int off = c_rules.off[D][p], cnt = c_rules.cnt[D][p];
+    if (cnt > max_pts) { set_err(err, XG_ERR_CAPACITY); counts[i] = 0; return; }
+    for (int q = 0; q < cnt; q++) {
+      for (int c = 0; c < 3; c++) P[3 * q + c] = c_rules.x[off + q][c];
+      W[q] = c_rules.w[off + q];
+    }
+    counts[i] = cnt;
+    return;
+  }
+  Sub subs[3];
+  const int ns = decompose<D>(l, dt, subs);
+  if (ns < 0) { set_err(err, -ns); counts[i] = 0; return; }
+  const int sd = dt == XG_IF ? D - 1 : D;  // sub-simplex dimension
+  const int off = c_rules.off[sd][p], cnt = c_rules.cnt[sd][p];
+  if (ns * cnt > max_pts) { set_err(err, XG_ERR_CAPACITY); counts[i] = 0; return; }
+  double fac = 1.0;
+  if (dt == XG_IF) {
+    Geo<D> g;
+    make_geo<D>(xv, g);
+    fac = if_factor<D>(g, l);
+  }
+  int k = 0;
+  for (int s = 0; s < ns; s++) {
+    const double trafofac = simplex_volume(subs[s].p, sd + 1);
+    for (int q = 0; q < cnt; q++, k++) {
+      double pt[3];
+      plain_point(subs[s], sd + 1, c_rules.x[off + q], pt);
+      for (int c = 0; c < 3; c++) P[3 * k + c] = pt[c];
+      double w = c_rules.w[off + q] * trafofac;
+      if (dt == XG_IF) w = w * fac;
+      W[k] = w;
+    }
+  }
+  counts[i] = k;
+}
+
+// ---- Integrate (cutint/cutintegral.cpp:126-212) ---------------------------------------
+// Fixed assignment of elements to threads and a fixed reduction tree make the
+// sum deterministic.
+constexpr int kIntThreads = 256;
+
+__device__ __forceinline__ double ipow(double x, int e) {
+  double r = 1.0;
+  for (int i = 0; i < e; i++) r *= x;
+  return r;
+}
+
+template <int D>
+__global__ void k_integrate(int ne, const int32_t* __restrict__ elv, const double* __restrict__ xyz, int nv,
+                            const double* __restrict__ lset, int dt, int order, int ex, int ey, int ez,
+                            const uint64_t* __restrict__ defined_on, double* block_sums, int* err) {
+  __shared__ double red[kIntThreads];
+  double acc = 0.0;
+  const int p = clamp_order(order);
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
+    if (defined_on && !tbit(defined_on, e)) continue;
+    double l[D + 1];
+    double xv[D + 1][3];
+#pragma unroll
+    for (int v = 0; v <= D; v++) {
+      int vid = elv[(int64_t)v * ne + e];
+      l[v] = lset[vid];
+#pragma unroll
+      for (int c = 0; c < 3; c++) xv[v][c] = c < D ? xyz[(int64_t)c * nv + vid] : 0.0;
+    }
+    Geo<D> g;
+    make_geo<D>(xv, g);
+    const double meas = fabs(g.det);
+    const int cdom = check_if_straight_cut(l, D + 1);
+    auto point_value = [&](const double* xi, double w) {
+      double x[3] = {0, 0, 0};
+#pragma unroll
+      for (int i = 0; i < D; i++) {
+        double s = g.x0[i];
+#pragma unroll
+        for (int k = 0; k < D; k++) s += g.F[i][k] * xi[k];
+        x[i] = s;
+      }
+      double fv = ipow(x[0], ex) * ipow(x[1], ey) * (D == 3 ? ipow(x[2], ez) : 1.0);
+      acc += w * meas * fv;
+    };
+    if (cdom != XG_IF) {
+      if (cdom != dt) continue;
+      const int off = c_rules.off[D][p], cnt = c_rules.cnt[D][p];
+      for (int q = 0; q < cnt; q++) point_value(c_rules.x[off + q], c_rules.w[off + q]);
+      continue;
+    }
+    Sub subs[3];
+    const int ns = decompose<D>(l, dt, subs);
+    if (ns < 0) { set_err(err, -ns); continue; }
+    const int sd = dt == XG_IF ? D - 1 : D;
+    const int off = c_rules.off[sd][p], cnt = c_rules.cnt[sd][p];
+    const double fac = dt == XG_IF ? if_factor<D>(g, l) : 1.0;
+    for (int s = 0; s < ns; s++) {
+      const double trafofac = simplex_volume(subs[s].p, sd + 1);
+      for (int q = 0; q < cnt; q++) {
+        double pt[3];
+        plain_point(subs[s], sd + 1, c_rules.x[off + q], pt);
+        double w = c_rules.w[off + q] * trafofac;
+        if (dt == XG_IF) w = w * fac;
+        point_value(pt, w);
+      }
+    }
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = kIntThreads / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) block_sums[blockIdx.x] = red[0];
+}
+
+__global__ void k_sum_fixed(const double* v, int n, double* out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < n; i++) s += v[i];
+    out[0] = s;
+  }
+}
+
+}  // namespace xg
+
+using namespace xg;
+
+static int launch_check(const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, what);
+  return XG_OK;
+}
+
+static inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+extern "C" {
+
+int xg_interpolate_p1_perturb(double* d_vals, int64_t n, double eps, void* stream) {
+  if (!d_vals || n < 0) return XG_ERR_ARG;
+  if (n == 0) return XG_OK;
+  unsigned g = nblk(n, 256);
+  if (g > 152 * 32) g = 152 * 32;
+  k_perturb<<<g, 256, 0, (cudaStream_t)stream>>>(d_vals, n, eps);
+  return launch_check("k_perturb");
+}
+
+int xg_cutinfo_update(xg_mesh* m, const double* d_lset, uint8_t* d_dom, double* d_ratio, uint64_t* d_bits,
+                      void* stream) {
+  if (!m || !d_lset || !d_dom || !d_ratio || !d_bits) return XG_ERR_ARG;
+  const int64_t nw64 = (m->ne + 63) / 64;
+  // grid covers whole 64-bit words so every 32-bit half is written
+  const int64_t nthreads = nw64 * 64;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (m->dim == 2)
+    k_cutinfo<2><<<nblk(nthreads, 256), 256, 0, s>>>(m->ne, m->d_elv, d_lset, d_dom, d_ratio, (uint32_t*)d_bits,
+                                                     2 * nw64, m->d_err);
+  else
+    k_cutinfo<3><<<nblk(nthreads, 256), 256, 0, s>>>(m->ne, m->d_elv, d_lset, d_dom, d_ratio, (uint32_t*)d_bits,
+                                                     2 * nw64, m->d_err);
+  return launch_check("k_cutinfo");
+}
+
+int xg_mesh_check(xg_mesh* m) {
+  if (!m) return XG_ERR_ARG;
+  int h = 0;
+  XG_CUDA(cudaMemcpy(&h, m->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  XG_CUDA(cudaMemset(m->d_err, 0, sizeof(int)));
+  if (h) set_last_error(std::string("device error: ") + xg_status_string(h));
+  return h;
+}
+
+int xg_facets_with_neighbor_types(xg_mesh* m, const uint64_t* d_a, const uint64_t* d_b, int bnd_a, int bnd_b,
+                                  int use_and, uint64_t* d_out, void* stream) {
+  if (!m || !d_a || !d_b || !d_out) return XG_ERR_ARG;
+  const int64_t nw64 = (m->nfacets + 63) / 64;
+  k_facet_mark<<<nblk(nw64 * 64, 256), 256, 0, (cudaStream_t)stream>>>(m->nfacets, m->d_facet_els, d_a, d_b, bnd_a,
+                                                                       bnd_b, use_and, (uint32_t*)d_out, 2 * nw64);
+  return launch_check("k_facet_mark");
+}
+
+int xg_elements_with_neighbor_facets(xg_mesh* m, const uint64_t* d_facets, uint64_t* d_out, void* stream) {
+  if (!m || !d_facets || !d_out) return XG_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  XG_CUDA(cudaMemsetAsync(d_out, 0, sizeof(uint64_t) * ((m->ne + 63) / 64), s));
+  k_el_nbr_facets<<<nblk(m->nfacets, 256), 256, 0, s>>>(m->nfacets, m->d_facet_els, d_facets,
+                                                         (unsigned long long*)d_out);
+  return launch_check("k_el_nbr_facets");
+}
+
+int xg_cut_rules(xg_mesh* m, const double* d_lset, const int32_t* d_elems, int32_t n, int dt, int order,
+                 int32_t max_pts, int32_t* d_counts, double* d_pts, double* d_wts, void* stream) {
+  if (!m || !d_lset || !d_elems || n < 0 || dt < 0 || dt > 2 || order < 0 || order > kMaxOrder || max_pts <= 0 ||
+      !d_counts || !d_pts || !d_wts)
+    return XG_ERR_ARG;
+  if (n == 0) return XG_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (m->dim == 2)
+    k_cut_rules<2><<<nblk(n, 128), 128, 0, s>>>(m->ne, m->d_elv, m->d_xyz, m->nv, d_lset, d_elems, n, dt, order,
+                                                max_pts, d_counts, d_pts, d_wts, m->d_err);
+  else
+    k_cut_rules<3><<<nblk(n, 128), 128, 0, s>>>(m->ne, m->d_elv, m->d_xyz, m->nv, d_lset, d_elems, n, dt, order,
+                                                max_pts, d_counts, d_pts, d_wts, m->d_err);
+  return launch_check("k_cut_rules");
+}
+
+int xg_integrate(xg_mesh* m, const double* d_lset, int dt, int order, int ex, int ey, int ez,
+                 const uint64_t* d_defined_on, double* d_result, void* stream) {
+  if (!m || !d_lset || !d_result || dt < 0 || dt > 2 || order < 0 || order > kMaxOrder || ex < 0 || ey < 0 || ez < 0)
+    return XG_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int nb = 152 * 4;
+  if (m->scratch_bytes < nb * sizeof(double)) {
+    cudaFree(m->d_scratch);
+    m->d_scratch = nullptr;
+    m->scratch_bytes = 0;
+    XG_CUDA(cudaMalloc(&m->d_scratch, nb * sizeof(double)));
+    m->scratch_bytes = nb * sizeof(double);
+  }
+  double* bs = (double*)m->d_scratch;
+  if (m->dim == 2)
+    k_integrate<2><<<nb, kIntThreads, 0, s>>>(m->ne, m->d_elv, m->d_xyz, m->nv, d_lset, dt, order, ex, ey, ez,
+                                              d_defined_on, bs, m->d_err);
+  else
+    k_integrate<3><<<nb, kIntThreads, 0, s>>>(m->ne, m->d_elv, m->d_xyz, m->nv, d_lset, dt, order, ex, ey, ez,
+                                              d_defined_on, bs, m->d_err);
+  k_sum_fixed<<<1, 32, 0, s>>>(bs, nb, d_result);
+  return launch_check("k_integrate");
+}
+
+}  // extern "C"

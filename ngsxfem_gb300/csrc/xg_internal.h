@@ -1,0 +1,114 @@
+// Internal declarations shared by the host objects and the kernels of libxg.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/xg.h"
+
+namespace xg {
+
+// ---- quadrature rule family (host-built, device __constant__) ------------------
+// segment order p: Gauss-Legendre with p/2+1 points on [0,1]
+// trig: p<=1 centroid; p==2 3-point (1/6,1/6,2/3); p>=3 collapsed Gauss-Jacobi
+//       conical product, p/2+1 points per direction
+// tet : p<=1 centroid; p==2 4-point (a,b,b,b), a=(5+3sqrt5)/20;
+//       p>=3 conical product, p/2+1 points per direction
+constexpr int kMaxOrder = 8;
+constexpr int kRuleCap = 512;  // total points of all tables
+
+struct RuleTable {
+  int off[4][kMaxOrder + 1];
+  int cnt[4][kMaxOrder + 1];
+  double x[kRuleCap][3];
+  double w[kRuleCap];
+};
+const RuleTable& host_rules();
+int ensure_device_rules();  // uploads the table to the current device (once per device)
+
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+inline int clamp_order(int p) { return p < 0 ? 0 : (p > kMaxOrder ? kMaxOrder : p); }
+
+// ---- device error word -----------------------------------------------------------
+// first error wins (atomicCAS from 0)
+#ifdef __CUDACC__
+__device__ __forceinline__ void set_err(int* err, int code) {
+  if (err) atomicCAS(err, 0, code);
+}
+#endif
+
+// ---- errors ----------------------------------------------------------------------
+void set_last_error(const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+#define XG_CUDA(call)                                 \
+  do {                                                \
+    cudaError_t _e = (call);                          \
+    if (_e != cudaSuccess) return cuda_fail(_e, #call); \
+  } while (0)
+
+// ---- term groups passed by value to the kernels -------------------------------
+constexpr int kMaxGroups = 6;
+constexpr int kMaxPatch = 4;
+
+// volume terms with equal (domain, order, defined_on) share one quadrature rule
+struct GroupDesc {
+  int domain;
+  int order;
+  const uint64_t* defined_on;
+  double c[5];    // coefficients of MASS, LAPLACE, NGRADU_V, U_NGRADV, CONV
+  int hpow[5];
+  int used;       // bitmask of kinds present
+  double b[3];
+};
+struct PatchDesc {
+  int order;
+  const uint64_t* defined_on;
+  double c;
+  int hpow;
+};
+struct FormDesc {
+  int ngroups;
+  GroupDesc g[kMaxGroups];
+  int npatch;
+  PatchDesc p[kMaxPatch];
+};
+
+}  // namespace xg
+
+// ---- objects behind the opaque handles ------------------------------------------
+struct xg_mesh {
+  int dim = 0, nv = 0, ne = 0, device = 0;
+  int64_t nedges = 0, nfaces = 0, nfacets = 0;
+  int max_vertex_elems = 0;  // max elements sharing a vertex
+  // device (SoA)
+  double* d_xyz = nullptr;       // [dim][nv]
+  int32_t* d_elv = nullptr;      // [dim+1][ne]
+  int32_t* d_el_edges = nullptr; // [3|6][ne]
+  int32_t* d_el_faces = nullptr; // [4][ne] (3D)
+  int32_t* d_el_facets = nullptr;// [dim+1][ne] (alias of edges / faces)
+  int32_t* d_facet_els = nullptr;// [2][nfacets]
+  int* d_err = nullptr;
+  // host
+  std::vector<int32_t> h_elv;       // ne*(dim+1)
+  std::vector<int32_t> h_el_edges;  // ne*nel_edges
+  std::vector<int32_t> h_el_faces;  // ne*4
+  std::vector<int32_t> h_facet_els; // nfacets*2
+  // compaction scratch (sized for max(ne, nfacets))
+  void* d_scratch = nullptr;
+  size_t scratch_bytes = 0;
+};
+
+struct xg_space {
+  xg_mesh* mesh = nullptr;
+  int order = 1, nd = 0;
+  int64_t ndof = 0;
+  int32_t* d_el_dofs = nullptr;     // [nd][ne]
+  int32_t* d_dof_adj_ptr = nullptr; // [ndof+1]
+  int32_t* d_dof_adj = nullptr;     // element*32 + local index, elements ascending
+  int max_adj = 0;
+  std::vector<int32_t> h_el_dofs;   // ne*nd
+};

@@ -1,0 +1,666 @@
+"""Python surface of the cut-element path, shaped like ngsxfem's `xfem` module
+(python/__init__.py, xfem/python_xfem.cpp, cutint/python_cutint.cpp) so that a
+script written like demos/fictdom.py:95-133 keeps its structure:
+
+    ci = CutInfo(mesh, lsetp1)
+    hasneg = ci.GetElementsOfType(HASNEG)
+    ba_facets = GetFacetsWithNeighborTypes(mesh, a=hasneg, b=ci.GetElementsOfType(IF))
+    u, v = V.TnT()
+    a = BilinearForm(V)
+    a += grad(u) * grad(v) * dCut(lsetp1, NEG, definedonelements=hasneg)
+    a += gamma / h**2 * (u - u.Other()) * (v - v.Other()) * dFacetPatch(definedonelements=ba_facets)
+    a.Assemble()
+
+Every operation runs on the GPU through libxg (include/xg.h); device memory is
+held in torch tensors.  Integrands are parsed into the term menu of the C ABI
+(mass, Laplace, Nitsche normal-derivative terms, convection, ghost-penalty
+patch mass); anything outside the menu raises.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .meshes import Mesh, MakeStructured2DMesh, MakeStructured3DMesh  # noqa: F401
+
+NEG, POS, IF = 0, 1, 2
+CDOM_NO, CDOM_NEG, CDOM_POS, CDOM_UNCUT, CDOM_IF, CDOM_HASNEG, CDOM_HASPOS, CDOM_ANY = range(8)
+UNCUT, HASNEG, HASPOS, ANY = CDOM_UNCUT, CDOM_HASNEG, CDOM_HASPOS, CDOM_ANY
+VOL, BND = "VOL", "BND"
+
+TERM_MASS, TERM_LAPLACE, TERM_NGRADU_V, TERM_U_NGRADV, TERM_CONV, TERM_GHOST_MASS = range(6)
+PREC_FP64, PREC_MIXED = 0, 1
+
+
+def _vp(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _dev():
+    if not torch.cuda.is_available():
+        raise RuntimeError("ngsxfem_gb300 needs a CUDA device (GB300, sm_103a); there is no CPU path")
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+# ----------------------------------------------------------------------------
+# mesh / space / grid functions
+# ----------------------------------------------------------------------------
+class DeviceMesh:
+    """libxg mesh handle (topology built once, resident on the device)."""
+
+    def __init__(self, mesh):
+        _dev()
+        self.mesh = mesh
+        h = ctypes.c_void_p()
+        _lib.call("xg_mesh_create", mesh.dim, mesh.nv, mesh.coords.ctypes.data_as(ctypes.c_void_p), mesh.ne,
+                  mesh.elements.ctypes.data_as(ctypes.c_void_p), ctypes.byref(h))
+        self.h = h
+        info = np.zeros(6, dtype=np.int64)
+        _lib.call("xg_mesh_info", self.h, info.ctypes.data_as(ctypes.c_void_p))
+        self.dim, self.nv, self.ne, self.nedges, self.nfaces, self.nfacets = (int(x) for x in info)
+
+    def facet_elements(self):
+        out = np.zeros((self.nfacets, 2), dtype=np.int32)
+        _lib.call("xg_mesh_facet_elements", self.h, out.ctypes.data_as(ctypes.c_void_p))
+        return out
+
+    def check(self):
+        torch.cuda.synchronize()
+        _lib.check(_lib.load().xg_mesh_check(self.h), "device (mesh)")
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib._lib is not None:
+            _lib.load().xg_mesh_destroy(self.h)
+            self.h = None
+
+
+def device_mesh(mesh):
+    if getattr(mesh, "_device", None) is None:
+        mesh._device = DeviceMesh(mesh)
+    return mesh._device
+
+
+class BitArray:
+    """Bit set on the device: bit i of 64-bit word i//64 (int64 storage)."""
+
+    def __init__(self, n, words=None):
+        self.n = int(n)
+        nw = (self.n + 63) // 64
+        self.words = words if words is not None else torch.zeros(nw, dtype=torch.int64, device=_dev())
+
+    def __len__(self):
+        return self.n
+
+    def numpy(self):
+        w = self.words.cpu().numpy().view(np.uint64)
+        bits = np.unpackbits(w.view(np.uint8), bitorder="little")
+        return bits[: self.n].astype(bool)
+
+    def NumSet(self):
+        return int(self.numpy().sum())
+
+    def __getitem__(self, i):
+        return bool((int(self.words[i // 64].item()) >> (i % 64)) & 1)
+
+    def _mask(self):
+        extra = self.words.numel() * 64 - self.n
+        m = torch.full_like(self.words, -1)
+        if extra:
+            m[-1] = (1 << (64 - extra)) - 1
+        return m
+
+    def __or__(self, o):
+        return BitArray(self.n, self.words | o.words)
+
+    def __and__(self, o):
+        return BitArray(self.n, self.words & o.words)
+
+    def __invert__(self):
+        return BitArray(self.n, (~self.words) & self._mask())
+
+    @staticmethod
+    def from_numpy(bits):
+        bits = np.asarray(bits, dtype=bool)
+        n = bits.size
+        packed = np.packbits(bits, bitorder="little")
+        pad = (-packed.size) % 8
+        packed = np.concatenate([packed, np.zeros(pad, np.uint8)]).view(np.int64)
+        return BitArray(n, torch.from_numpy(packed.copy()).to(_dev()))
+
+
+class H1:
+    """H1 space of order 1..3 on a simplex mesh (libxg dof numbering)."""
+
+    def __init__(self, mesh, order=1, dgjumps=False, **kwargs):
+        self.mesh = mesh
+        self.order = int(order)
+        self.dm = device_mesh(mesh)
+        h = ctypes.c_void_p()
+        _lib.call("xg_space_create", self.dm.h, self.order, ctypes.byref(h))
+        self.h = h
+        info = np.zeros(3, dtype=np.int64)
+        _lib.call("xg_space_info", self.h, info.ctypes.data_as(ctypes.c_void_p))
+        self.ndof, self.ndof_el = int(info[0]), int(info[1])
+
+    def element_dofs(self):
+        out = np.zeros((self.mesh.ne, self.ndof_el), dtype=np.int32)
+        _lib.call("xg_space_element_dofs", self.h, out.ctypes.data_as(ctypes.c_void_p))
+        return out
+
+    def TrialFunction(self):
+        return _Expr.atom(("u", False))
+
+    def TestFunction(self):
+        return _Expr.atom(("v", False))
+
+    def TnT(self):
+        return self.TrialFunction(), self.TestFunction()
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib._lib is not None:
+            _lib.load().xg_space_destroy(self.h)
+            self.h = None
+
+
+class GridFunction:
+    def __init__(self, space):
+        self.space = space
+        self.vec = torch.zeros(space.ndof, dtype=torch.float64, device=_dev())
+
+
+def InterpolateToP1(f, gf, eps_perturbation=1e-14):
+    """Vertex values of f (callable on coordinate arrays, or an array of vertex
+    values) into the P1 GridFunction gf, with ngsxfem's |v| < eps -> eps
+    perturbation (utils/p1interpol.cpp:104-107) applied on the device."""
+    mesh = gf.space.mesh
+    if callable(f):
+        vals = np.asarray(f(*[mesh.coords[:, k] for k in range(mesh.dim)]), dtype=np.float64)
+    else:
+        vals = np.asarray(f, dtype=np.float64)
+    gf.vec[: mesh.nv].copy_(torch.from_numpy(np.ascontiguousarray(vals)))
+    _lib.call("xg_interpolate_p1_perturb", _vp(gf.vec), mesh.nv, eps_perturbation, _stream())
+    return gf
+
+
+def _lset_vec(levelset):
+    if isinstance(levelset, GridFunction):
+        if levelset.space.order != 1:
+            raise ValueError("the straight-cut path needs a P1 level set (CF2GFForStraightCutRule)")
+        return levelset.vec
+    if isinstance(levelset, torch.Tensor):
+        return levelset
+    raise TypeError("level set must be a P1 GridFunction or a device tensor of vertex values")
+
+
+# ----------------------------------------------------------------------------
+# marking
+# ----------------------------------------------------------------------------
+class CutInfo:
+    """CutInformation (xfem/cutinfo.cpp): element domain types, cut ratios and
+    the combined-domain bitsets of a P1 level set."""
+
+    def __init__(self, mesh, levelset=None, subdivlvl=0, time_order=-1, heapsize=None):
+        self.mesh = mesh
+        self.dm = device_mesh(mesh)
+        ne = mesh.ne
+        dev = _dev()
+        self.dom = torch.zeros(ne, dtype=torch.uint8, device=dev)
+        self.cut_ratio = torch.zeros(ne, dtype=torch.float64, device=dev)
+        self.bits = torch.zeros((8, (ne + 63) // 64), dtype=torch.int64, device=dev)
+        self.levelset = None
+        if levelset is not None:
+            self.Update(levelset, subdivlvl, time_order)
+
+    def Update(self, levelset, subdivlvl=0, time_order=-1, heapsize=None):
+        if subdivlvl != 0 or time_order > 0:
+            raise NotImplementedError("CutInfo on the GPU supports P1 level sets (subdivlvl=0, time_order<=0)")
+        self.levelset = levelset
+        lv = _lset_vec(levelset)
+        _lib.call("xg_cutinfo_update", self.dm.h, _vp(lv), _vp(self.dom), _vp(self.cut_ratio), _vp(self.bits),
+                  _stream())
+
+    def GetElementsOfType(self, domain_type, VorB=VOL):
+        if VorB != VOL:
+            raise NotImplementedError("boundary elements are not part of the GPU path")
+        cdt = {NEG: CDOM_NEG, POS: CDOM_POS, IF: CDOM_IF}.get(domain_type, domain_type) \
+            if isinstance(domain_type, int) and domain_type < 3 else domain_type
+        return BitArray(self.mesh.ne, self.bits[cdt].clone())
+
+    def GetCutRatios(self, VorB=VOL):
+        return self.cut_ratio
+
+    def Mesh(self):
+        return self.mesh
+
+
+def GetFacetsWithNeighborTypes(mesh, a, bnd_val_a=True, bnd_val_b=True, use_and=True, b=None, heapsize=None):
+    dm = device_mesh(mesh)
+    b = a if b is None else b
+    out = BitArray(dm.nfacets)
+    _lib.call("xg_facets_with_neighbor_types", dm.h, _vp(a.words), _vp(b.words), int(bnd_val_a), int(bnd_val_b),
+              int(use_and), _vp(out.words), _stream())
+    return out
+
+
+def GetElementsWithNeighborFacets(mesh, a, heapsize=None):
+    dm = device_mesh(mesh)
+    out = BitArray(mesh.ne)
+    _lib.call("xg_elements_with_neighbor_facets", dm.h, _vp(a.words), _vp(out.words), _stream())
+    return out
+
+
+# ----------------------------------------------------------------------------
+# integrands
+# ----------------------------------------------------------------------------
+class _Mono:
+    """c * h^hpow * (scalar atoms) * (dot products) * (at most one free vector)."""
+    __slots__ = ("c", "hpow", "scal", "dots", "vec")
+
+    def __init__(self, c=1.0, hpow=0, scal=(), dots=(), vec=None):
+        self.c, self.hpow, self.scal, self.dots, self.vec = c, hpow, tuple(scal), tuple(dots), vec
+
+    def mul(self, o):
+        vec, dots = None, self.dots + o.dots
+        if self.vec is not None and o.vec is not None:
+            dots = dots + (tuple(sorted((self.vec, o.vec), key=repr)),)
+        else:
+            vec = self.vec if self.vec is not None else o.vec
+        return _Mono(self.c * o.c, self.hpow + o.hpow, tuple(sorted(self.scal + o.scal, key=repr)), dots, vec)
+
+
+class _Expr:
+    def __init__(self, monos):
+        self.monos = monos
+
+    @staticmethod
+    def atom(a, vector=False):
+        return _Expr([_Mono(vec=a)] if vector else [_Mono(scal=(a,))])
+
+    @staticmethod
+    def wrap(x):
+        if isinstance(x, _Expr):
+            return x
+        if isinstance(x, (int, float)):
+            return _Expr([_Mono(c=float(x))])
+        if isinstance(x, (tuple, list)):
+            return _Expr([_Mono(vec=("b", tuple(float(v) for v in x)))])
+        raise TypeError("unsupported coefficient %r" % (x,))
+
+    def __add__(self, o):
+        return _Expr(self.monos + _Expr.wrap(o).monos)
+
+    __radd__ = __add__
+
+    def __neg__(self):
+        return _Expr([_Mono(-m.c, m.hpow, m.scal, m.dots, m.vec) for m in self.monos])
+
+    def __sub__(self, o):
+        return self + (-_Expr.wrap(o))
+
+    def __rsub__(self, o):
+        return _Expr.wrap(o) - self
+
+    def __mul__(self, o):
+        if isinstance(o, _Measure):
+            return _Integral(self, o)
+        o = _Expr.wrap(o)
+        return _Expr([a.mul(b) for a in self.monos for b in o.monos])
+
+    __rmul__ = __mul__
+
+    def __truediv__(self, o):
+        o = _Expr.wrap(o)
+        if len(o.monos) != 1 or o.monos[0].scal or o.monos[0].dots or o.monos[0].vec is not None:
+            raise TypeError("can only divide by constants and powers of the mesh size")
+        m = o.monos[0]
+        return self * _Expr([_Mono(1.0 / m.c, -m.hpow)])
+
+    def __rtruediv__(self, o):
+        if len(self.monos) != 1 or self.monos[0].scal or self.monos[0].dots or self.monos[0].vec is not None:
+            raise TypeError("can only divide by constants and powers of the mesh size")
+        m = self.monos[0]
+        return _Expr.wrap(o) * _Expr([_Mono(1.0 / m.c, -m.hpow)])
+
+    def __pow__(self, p):
+        if len(self.monos) != 1 or self.monos[0].scal or self.monos[0].vec is not None or int(p) != p:
+            raise TypeError("only powers of the mesh size / constants are supported")
+        m = self.monos[0]
+        return _Expr([_Mono(m.c ** p, m.hpow * int(p))])
+
+    def Other(self):
+        out = []
+        for m in self.monos:
+            scal = tuple((a[0], True) if a[0] in ("u", "v") else a for a in m.scal)
+            out.append(_Mono(m.c, m.hpow, scal, m.dots, m.vec))
+        return _Expr(out)
+
+
+def grad(x):
+    if isinstance(x, GridFunction):
+        return _LsetGrad(x)
+    if isinstance(x, _Expr) and len(x.monos) == 1 and len(x.monos[0].scal) == 1 and x.monos[0].scal[0][0] in ("u", "v"):
+        return _Expr([_Mono(vec=("g" + x.monos[0].scal[0][0], x.monos[0].scal[0][1]))])
+    raise TypeError("grad() of a trial/test function or a P1 level set GridFunction only")
+
+
+class _LsetGrad:
+    def __init__(self, gf):
+        self.gf = gf
+
+
+def Normalize(g):
+    if isinstance(g, _LsetGrad):
+        return _Expr([_Mono(vec=("n", id(g.gf)))])
+    raise TypeError("Normalize(grad(lset)) only")
+
+
+class _SpecialCF:
+    @property
+    def mesh_size(self):
+        return _Expr([_Mono(hpow=1)])
+
+
+specialcf = _SpecialCF()
+
+
+def CoefficientFunction(x):
+    return _Expr.wrap(x)
+
+
+class _Measure:
+    def __init__(self, kind, levelset=None, domain_type=None, order=None, definedonelements=None, **kw):
+        self.kind, self.levelset, self.domain_type, self.order = kind, levelset, domain_type, order
+        self.definedonelements = definedonelements
+        for k in ("deformation", "skeleton", "element_boundary", "element_vb", "definedon"):
+            if kw.get(k) is not None and kw.get(k) is not False:
+                raise NotImplementedError("dCut/dFacetPatch option %r is not part of the GPU path" % k)
+        if kw.get("time_order", -1) not in (-1, None) or kw.get("subdivlvl") not in (None, 0):
+            raise NotImplementedError("space-time / subdivision rules are not part of dCut on the GPU path")
+        if kw.get("downscale", 1.0) != 1.0:
+            raise NotImplementedError("downscale != 1 is not supported")
+
+
+def dCut(levelset, domain_type, order=None, subdivlvl=None, time_order=-1, levelset_domain=None, **kwargs):
+    """Differential symbol for cut integration (python/__init__.py:781-864)."""
+    if levelset_domain is not None:
+        levelset = levelset_domain["levelset"]
+        domain_type = levelset_domain["domain_type"]
+        order = levelset_domain.get("order", order)
+    return _Measure("cut", levelset, domain_type, order, kwargs.pop("definedonelements", None),
+                    subdivlvl=subdivlvl, time_order=time_order, **kwargs)
+
+
+def dFacetPatch(**kwargs):
+    """Differential symbol for facet patch integrators (python/__init__.py:749-778)."""
+    return _Measure("patch", None, None, kwargs.pop("order", None), kwargs.pop("definedonelements", None), **kwargs)
+
+
+class _Integral:
+    def __init__(self, expr, measure):
+        self.expr, self.measure = expr, measure
+
+    def __add__(self, o):
+        return _SumOfIntegrals([self]) + o
+
+    def terms(self, nrm_gf):
+        """Maps the integrand onto the C ABI term menu (list of dicts)."""
+        m = self.measure
+        out = []
+        if m.kind == "patch":
+            # expect c * (u - u')(v - v') = c*(uv - u'v - uv' + u'v')
+            for mono in self.expr.monos:
+                if mono.dots or mono.vec is not None or len(mono.scal) != 2:
+                    raise NotImplementedError("facet patch integrands: c * (u - u.Other()) * (v - v.Other()) only")
+            sign = {(("u", False), ("v", False)): 1, (("u", True), ("v", False)): -1,
+                    (("u", False), ("v", True)): -1, (("u", True), ("v", True)): 1}
+            acc = {}
+            for mono in self.expr.monos:
+                key = tuple(sorted(mono.scal, key=repr))
+                if key not in sign:
+                    raise NotImplementedError("facet patch integrand outside the ghost-penalty form")
+                acc.setdefault((key, mono.hpow), 0.0)
+                acc[(key, mono.hpow)] += mono.c
+            hps = {k[1] for k in acc}
+            if len(hps) != 1:
+                raise NotImplementedError("mixed mesh-size powers in a facet patch integrand")
+            hp = hps.pop()
+            vals = {k[0]: v for k, v in acc.items()}
+            c_uv = vals.get((("u", False), ("v", False)), 0.0)
+            for key, sgn in sign.items():
+                if abs(vals.get(key, 0.0) - sgn * c_uv) > 1e-14 * max(1.0, abs(c_uv)):
+                    raise NotImplementedError("facet patch integrand is not c*(u-u.Other())*(v-v.Other())")
+            out.append(dict(kind=TERM_GHOST_MASS, domain=NEG, order=-1 if m.order is None else m.order, hpow=hp,
+                            coef=c_uv, b=(0.0, 0.0, 0.0), defined_on=m.definedonelements))
+            return out
+        dom = m.domain_type
+        for mono in self.expr.monos:
+            if mono.vec is not None:
+                raise TypeError("integrand is a vector, not a scalar")
+            scal = [a for a in mono.scal]
+            if any(a[1] for a in scal if a[0] in ("u", "v")):
+                raise NotImplementedError(".Other() is only meaningful on facet patches")
+            names = sorted(a[0] for a in scal)
+            dots = [tuple(sorted((d[0][0], d[1][0]))) for d in mono.dots]
+            kind, b = None, (0.0, 0.0, 0.0)
+            for d in mono.dots:
+                for v in d:
+                    if v[0] == "n" and nrm_gf is not None and v[1] != id(nrm_gf):
+                        raise NotImplementedError("the normal must be Normalize(grad(levelset)) of the cut's level set")
+            if names == ["u", "v"] and not dots:
+                kind = TERM_MASS
+            elif not names and dots == [("gu", "gv")]:
+                kind = TERM_LAPLACE
+            elif names == ["v"] and dots == [("gu", "n")]:
+                kind = TERM_NGRADU_V
+            elif names == ["u"] and dots == [("gv", "n")]:
+                kind = TERM_U_NGRADV
+            elif names == ["v"] and len(dots) == 1 and set(dots[0]) == {"gu", "b"}:
+                kind = TERM_CONV
+                bv = [x for x in mono.dots[0] if x[0] == "b"][0][1]
+                b = tuple(list(bv) + [0.0] * (3 - len(bv)))
+            else:
+                raise NotImplementedError("integrand term outside the supported menu: %s" % (names + dots,))
+            out.append(dict(kind=kind, domain=dom, order=-1 if m.order is None else m.order, hpow=mono.hpow,
+                            coef=mono.c, b=b, defined_on=m.definedonelements))
+        return out
+
+
+class _SumOfIntegrals:
+    def __init__(self, items):
+        self.items = list(items)
+
+    def __add__(self, o):
+        if isinstance(o, _Integral):
+            return _SumOfIntegrals(self.items + [o])
+        if isinstance(o, _SumOfIntegrals):
+            return _SumOfIntegrals(self.items + o.items)
+        raise TypeError("can only add integrals")
+
+
+# ----------------------------------------------------------------------------
+# bilinear forms
+# ----------------------------------------------------------------------------
+class SparseMatrix:
+    """Compressed-row matrix over the form's active dofs (device tensors)."""
+
+    def __init__(self, ndof, row_dof, rowptr, cols, vals, nrows, nnz):
+        self.ndof, self.row_dof, self.rowptr, self.cols, self.vals = ndof, row_dof, rowptr, cols, vals
+        self.nrows, self.nnz = nrows, nnz
+
+    def global_coo(self):
+        """(rows, cols, vals) numpy arrays in global dof numbering."""
+        n, z = self.nrows, self.nnz
+        rd = self.row_dof[:n].cpu().numpy()
+        rp = self.rowptr[: n + 1].cpu().numpy()
+        c = self.cols[:z].cpu().numpy()
+        v = self.vals[:z].cpu().numpy()
+        rows = np.repeat(rd, np.diff(rp))
+        return rows, rd[c], v
+
+    def to_scipy(self):
+        import scipy.sparse as sp
+        r, c, v = self.global_coo()
+        return sp.csr_matrix((v, (r, c)), shape=(self.ndof, self.ndof))
+
+
+class BilinearForm:
+    """BilinearForm over one H1 space: `a += integrand * dCut(...)` /
+    `* dFacetPatch(...)`, `a.Assemble()` -> `a.mat` (SparseMatrix)."""
+
+    def __init__(self, space, symmetric=False, precision=PREC_FP64, **kwargs):
+        self.space = space
+        self.integrals = []
+        self.precision = precision
+        self.mat = None
+        self._form = None
+        self._key = None
+        self._out = None
+
+    def __iadd__(self, integral):
+        if isinstance(integral, _Integral):
+            self.integrals.append(integral)
+        elif isinstance(integral, _SumOfIntegrals):
+            self.integrals.extend(integral.items)
+        else:
+            raise TypeError("add integrand * dCut(...) or integrand * dFacetPatch(...)")
+        self._form = None
+        return self
+
+    def _levelset(self):
+        ls = [i.measure.levelset for i in self.integrals if i.measure.kind == "cut"]
+        if not ls:
+            return None
+        for l in ls[1:]:
+            if l is not ls[0]:
+                raise NotImplementedError("all dCut integrals of one form must share the level set")
+        return ls[0]
+
+    def _build(self):
+        lset = self._levelset()
+        terms = []
+        for it in self.integrals:
+            terms += it.terms(lset)
+        arr = (_lib.Term * len(terms))()
+        self._keep = []
+        for k, t in enumerate(terms):
+            arr[k].kind, arr[k].domain, arr[k].order, arr[k].hpow = t["kind"], t["domain"], t["order"], t["hpow"]
+            arr[k].coef = t["coef"]
+            for j in range(3):
+                arr[k].b[j] = t["b"][j]
+            d = t["defined_on"]
+            if d is not None:
+                self._keep.append(d)
+                arr[k].d_defined_on = d.words.data_ptr()
+            else:
+                arr[k].d_defined_on = None
+        h = ctypes.c_void_p()
+        _lib.call("xg_form_create", self.space.h, arr, len(terms), self.precision, ctypes.byref(h))
+        self._form = h
+        self._terms = terms
+        cap = np.zeros(2, dtype=np.int64)
+        _lib.call("xg_form_capacity", h, cap.ctypes.data_as(ctypes.c_void_p))
+        self._alloc(int(cap[0]), int(cap[1]))
+
+    def _alloc(self, cap_rows, cap_nnz):
+        dev = _dev()
+        self._row_dof = torch.zeros(cap_rows, dtype=torch.int32, device=dev)
+        self._rowptr = torch.zeros(cap_rows + 1, dtype=torch.int64, device=dev)
+        self._cols = torch.zeros(max(cap_nnz, 1), dtype=torch.int32, device=dev)
+        self._vals = torch.zeros(max(cap_nnz, 1), dtype=torch.float64, device=dev)
+        self._counts = torch.zeros(2, dtype=torch.int64, device=dev)
+        c = _lib.Csr()
+        c.d_row_dof, c.d_rowptr = self._row_dof.data_ptr(), self._rowptr.data_ptr()
+        c.d_cols, c.d_vals, c.d_counts = self._cols.data_ptr(), self._vals.data_ptr(), self._counts.data_ptr()
+        c.cap_rows, c.cap_nnz = cap_rows, cap_nnz
+        self._csr = c
+
+    def Assemble(self, cutinfo=None):
+        if self._form is None:
+            self._build()
+        lset = self._levelset()
+        if cutinfo is None:
+            if lset is None:
+                # no cut integrals: every element counts as NEG for domain-free terms
+                raise NotImplementedError("forms without dCut integrals are not part of the GPU path")
+            cutinfo = CutInfo(self.space.mesh, lset)
+        _lib.call("xg_form_assemble", self._form, _vp(_lset_vec(lset)), _vp(cutinfo.dom), ctypes.byref(self._csr),
+                  _stream())
+        torch.cuda.synchronize()
+        _lib.check(_lib.load().xg_form_check(self._form), "device (form)")
+        nrows, nnz = (int(x) for x in self._counts.cpu().tolist())
+        self.mat = SparseMatrix(self.space.ndof, self._row_dof, self._rowptr, self._cols, self._vals, nrows, nnz)
+        return self
+
+    def __del__(self):
+        if getattr(self, "_form", None) and _lib._lib is not None:
+            _lib.load().xg_form_destroy(self._form)
+            self._form = None
+
+
+# ----------------------------------------------------------------------------
+# Integrate
+# ----------------------------------------------------------------------------
+class _Monomial:
+    def __init__(self, e=(0, 0, 0)):
+        self.e = tuple(e)
+
+    def __mul__(self, o):
+        if isinstance(o, _Monomial):
+            return _Monomial(tuple(a + b for a, b in zip(self.e, o.e)))
+        if isinstance(o, _Measure):
+            return ("integral", self, o)
+        raise TypeError("monomial coefficient functions only")
+
+    def __pow__(self, p):
+        return _Monomial(tuple(a * int(p) for a in self.e))
+
+
+x, y, z = _Monomial((1, 0, 0)), _Monomial((0, 1, 0)), _Monomial((0, 0, 1))
+
+
+def Integrate(levelset_domain=None, cf=None, mesh=None, order=5, integrand=None):
+    """Integrate(x^a y^b z^c * dCut(lset, dt, order)) on the GPU
+    (cutint/cutintegral.cpp:126-212): a deterministic fixed-order sum."""
+    if integrand is not None:
+        _, mono, meas = integrand
+        lset, dt, order = meas.levelset, meas.domain_type, meas.order if meas.order is not None else order
+        defined = meas.definedonelements
+    else:
+        lset, dt = levelset_domain["levelset"], levelset_domain["domain_type"]
+        order = levelset_domain.get("order", order)
+        mono = cf if isinstance(cf, _Monomial) else _Monomial()
+        defined = None
+    mesh = mesh if mesh is not None else lset.space.mesh
+    dm = device_mesh(mesh)
+    res = torch.zeros(1, dtype=torch.float64, device=_dev())
+    _lib.call("xg_integrate", dm.h, _vp(_lset_vec(lset)), dt, order, mono.e[0], mono.e[1], mono.e[2],
+              _vp(defined.words) if defined is not None else None, _vp(res), _stream())
+    dm.check()
+    return float(res.item())
+
+
+# ----------------------------------------------------------------------------
+# rule export
+# ----------------------------------------------------------------------------
+def CutIntegrationRules(mesh, levelset, elements, domain_type, order, max_pts=None):
+    """StraightCutIntegrationRule for a list of elements; returns (counts,
+    points (n, max_pts, 3), weights (n, max_pts)) as device tensors."""
+    dm = device_mesh(mesh)
+    el = torch.as_tensor(np.asarray(elements, dtype=np.int32)).to(_dev())
+    n = el.numel()
+    if max_pts is None:
+        sd = mesh.dim - 1 if domain_type == IF else mesh.dim
+        max_pts = max(3 * _lib.load().xg_base_rule_size(sd, order), _lib.load().xg_base_rule_size(mesh.dim, order))
+    dev = _dev()
+    counts = torch.zeros(n, dtype=torch.int32, device=dev)
+    pts = torch.zeros((n, max_pts, 3), dtype=torch.float64, device=dev)
+    wts = torch.zeros((n, max_pts), dtype=torch.float64, device=dev)
+    _lib.call("xg_cut_rules", dm.h, _vp(_lset_vec(levelset)), _vp(el), n, domain_type, order, max_pts, _vp(counts),
+              _vp(pts), _vp(wts), _stream())
+    dm.check()
+    return counts, pts, wts

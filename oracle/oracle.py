@@ -1,0 +1,222 @@
+"""ctypes front end of the oracle library (test infrastructure only).
+
+Loaded by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline and
+reference legs.  Never imported by the product package.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+
+NEG, POS, IF = 0, 1, 2
+TERM_MASS, TERM_LAPLACE, TERM_NGRADU_V, TERM_U_NGRADV, TERM_CONV, TERM_GHOST_MASS = range(6)
+
+
+class Term(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int),
+        ("domain", ctypes.c_int),
+        ("order", ctypes.c_int),
+        ("hpow", ctypes.c_int),
+        ("coef", ctypes.c_double),
+        ("b", ctypes.c_double * 3),
+        ("defined_on", ctypes.c_void_p),
+    ]
+
+
+def build():
+    subprocess.check_call(["make", "-s", "-C", HERE])
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        L = ctypes.CDLL(LIB)
+        P = ctypes.c_void_p
+        L.orc_check_if_straight_cut.argtypes = [P, ctypes.c_int, ctypes.c_double]
+        L.orc_interpolate_p1_perturb.argtypes = [P, ctypes.c_int, ctypes.c_double]
+        L.orc_base_rule.argtypes = [ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int]
+        L.orc_straight_cut_rule.argtypes = [ctypes.c_int, P, P, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int]
+        L.orc_space_create.restype = P
+        L.orc_space_create.argtypes = [ctypes.c_int, ctypes.c_int, P, ctypes.c_int, P, ctypes.c_int]
+        L.orc_space_destroy.argtypes = [P]
+        L.orc_space_info.argtypes = [P, P]
+        L.orc_space_el_dofs.argtypes = [P, P]
+        L.orc_space_facet_els.argtypes = [P, P]
+        L.orc_cutinfo.argtypes = [P, P, P, P, P, ctypes.c_int]
+        L.orc_facets_with_neighbor_types.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P]
+        L.orc_integrate.restype = ctypes.c_double
+        L.orc_integrate.argtypes = [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, P]
+        L.orc_element_matrix.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int, P]
+        L.orc_patch_matrix.argtypes = [P, P, ctypes.c_int, ctypes.c_int, P]
+        L.orc_assemble.restype = P
+        L.orc_assemble.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int]
+        L.orc_csr_nnz.restype = ctypes.c_int64
+        L.orc_csr_nnz.argtypes = [P]
+        L.orc_csr_get.argtypes = [P, P, P, P]
+        L.orc_csr_destroy.argtypes = [P]
+        L.orc_pipeline.restype = ctypes.c_int64
+        L.orc_pipeline.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def check_if_straight_cut(vals, eps=0.0):
+    v = np.ascontiguousarray(vals, dtype=np.float64)
+    return lib().orc_check_if_straight_cut(_p(v), len(v), eps)
+
+
+def interpolate_p1_perturb(vals, eps=1e-14):
+    v = np.array(vals, dtype=np.float64, copy=True)
+    lib().orc_interpolate_p1_perturb(_p(v), len(v), eps)
+    return v
+
+
+def base_rule(d, p):
+    pts = np.zeros((4096, 3))
+    w = np.zeros(4096)
+    n = lib().orc_base_rule(d, p, _p(pts), _p(w), 4096)
+    return pts[:n].copy(), w[:n].copy()
+
+
+def straight_cut_rule(elcoords, lset, dt, order):
+    """Returns (points (n,3) in reference coordinates, weights) or None (no rule)."""
+    elc = np.ascontiguousarray(elcoords, dtype=np.float64)
+    D = elc.shape[1]
+    l = np.ascontiguousarray(lset, dtype=np.float64)
+    pts = np.zeros((2048, 3))
+    w = np.zeros(2048)
+    n = lib().orc_straight_cut_rule(D, _p(elc), _p(l), dt, order, _p(pts), _p(w), 2048)
+    if n == -1:
+        return None
+    if n < -1:
+        raise RuntimeError("oracle cut rule error %d" % n)
+    return pts[:n].copy(), w[:n].copy()
+
+
+class Space:
+    """H1 space of order k over a simplex mesh, with the oracle's topology."""
+
+    def __init__(self, mesh, order):
+        self.mesh = mesh
+        self.order = order
+        self.h = lib().orc_space_create(mesh.dim, mesh.nv, _p(mesh.coords), mesh.ne, _p(mesh.elements), order)
+        if not self.h:
+            raise ValueError("bad space")
+        info = np.zeros(5, dtype=np.int64)
+        lib().orc_space_info(self.h, _p(info))
+        self.ndof, self.nedges, self.nfaces, self.nfacets, self.ndof_el = (int(x) for x in info)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_space_destroy(self.h)
+            self.h = None
+
+    def el_dofs(self):
+        out = np.zeros((self.mesh.ne, self.ndof_el), dtype=np.int32)
+        lib().orc_space_el_dofs(self.h, _p(out))
+        return out
+
+    def facet_els(self):
+        out = np.zeros((self.nfacets, 2), dtype=np.int32)
+        lib().orc_space_facet_els(self.h, _p(out))
+        return out
+
+    def cutinfo(self, lset, nthreads=1):
+        ne = self.mesh.ne
+        nw = (ne + 63) // 64
+        dom = np.zeros(ne, dtype=np.uint8)
+        ratio = np.zeros(ne)
+        bits = np.zeros((8, nw), dtype=np.uint64)
+        l = np.ascontiguousarray(lset, dtype=np.float64)
+        r = lib().orc_cutinfo(self.h, _p(l), _p(dom), _p(ratio), _p(bits), nthreads)
+        if r:
+            raise RuntimeError("oracle cutinfo error %d" % r)
+        return dom, ratio, bits
+
+    def facets_with_neighbor_types(self, a, b, bnd_a=False, bnd_b=False, use_and=True):
+        out = np.zeros((self.nfacets + 63) // 64, dtype=np.uint64)
+        a = np.ascontiguousarray(a, dtype=np.uint64)
+        b = np.ascontiguousarray(b, dtype=np.uint64)
+        lib().orc_facets_with_neighbor_types(self.h, _p(a), _p(b), int(bnd_a), int(bnd_b), int(use_and), _p(out))
+        return out
+
+    def integrate(self, lset, dt, order, ex=0, ey=0, ez=0, defined_on=None):
+        l = np.ascontiguousarray(lset, dtype=np.float64)
+        d = None if defined_on is None else np.ascontiguousarray(defined_on, dtype=np.uint64)
+        return lib().orc_integrate(self.h, _p(l), dt, order, ex, ey, ez, _p(d))
+
+    @staticmethod
+    def _terms(terms):
+        arr = (Term * len(terms))()
+        keep = []
+        for i, t in enumerate(terms):
+            arr[i].kind = t["kind"]
+            arr[i].domain = t.get("domain", NEG)
+            arr[i].order = t.get("order", -1)
+            arr[i].hpow = t.get("hpow", 0)
+            arr[i].coef = t.get("coef", 1.0)
+            b = t.get("b", (0.0, 0.0, 0.0))
+            for k in range(3):
+                arr[i].b[k] = b[k]
+            d = t.get("defined_on")
+            if d is not None:
+                d = np.ascontiguousarray(d, dtype=np.uint64)
+                keep.append(d)
+                arr[i].defined_on = d.ctypes.data
+            else:
+                arr[i].defined_on = None
+        return arr, keep
+
+    def element_matrix(self, lset, terms, e):
+        arr, keep = self._terms(terms)
+        n = self.ndof_el
+        out = np.zeros((n, n))
+        l = np.ascontiguousarray(lset, dtype=np.float64)
+        r = lib().orc_element_matrix(self.h, _p(l), ctypes.cast(arr, ctypes.c_void_p), len(terms), e, _p(out))
+        if r:
+            raise RuntimeError("oracle element matrix error %d" % r)
+        return out
+
+    def patch_matrix(self, terms, f):
+        arr, keep = self._terms(terms)
+        n = 2 * self.ndof_el
+        out = np.zeros((n, n))
+        r = lib().orc_patch_matrix(self.h, ctypes.cast(arr, ctypes.c_void_p), len(terms), f, _p(out))
+        if r:
+            raise RuntimeError("oracle patch matrix error %d" % r)
+        return out
+
+    def assemble(self, lset, terms, nthreads=1):
+        """Returns scipy-free CSR triple (rowptr int64, cols int32, vals float64) over all dofs."""
+        arr, keep = self._terms(terms)
+        l = np.ascontiguousarray(lset, dtype=np.float64)
+        c = lib().orc_assemble(self.h, _p(l), ctypes.cast(arr, ctypes.c_void_p), len(terms), nthreads)
+        if not c:
+            raise RuntimeError("oracle assembly error")
+        nnz = lib().orc_csr_nnz(c)
+        rowptr = np.zeros(self.ndof + 1, dtype=np.int64)
+        cols = np.zeros(nnz, dtype=np.int32)
+        vals = np.zeros(nnz)
+        lib().orc_csr_get(c, _p(rowptr), _p(cols), _p(vals))
+        lib().orc_csr_destroy(c)
+        return rowptr, cols, vals
+
+    def pipeline(self, lset, terms, ghost_facets=True, nthreads=1):
+        arr, keep = self._terms(terms)
+        l = np.ascontiguousarray(lset, dtype=np.float64)
+        return lib().orc_pipeline(self.h, _p(l), ctypes.cast(arr, ctypes.c_void_p), len(terms), int(ghost_facets),
+                                  nthreads)

@@ -1,0 +1,1078 @@
+// Oracle: CPU restatement of ngsxfem's straight-cut assembly path.
+// TEST INFRASTRUCTURE ONLY (see xg_oracle.h).  Built with -ffp-contract=off so
+// that x86 and Arm hosts produce identical bits.
+//
+// Reference files restated here (paths inside the ngsxfem project):
+//   cutint/straightcutrule.cpp:11-24   CheckIfStraightCut
+//   cutint/straightcutrule.cpp:41-64   SimpleX::CalcIFPolytopEUsingLset
+//   cutint/straightcutrule.cpp:66-72   SimpleX::GetVolume
+//   cutint/straightcutrule.cpp:80-100  SimpleX::GetPlainIntegrationRule
+//   cutint/straightcutrule.cpp:131-196 LevelsetCutSimplex::Decompose
+//   cutint/straightcutrule.cpp:503-538 LevelsetWrapper (coefficients, gradient, normal)
+//   cutint/straightcutrule.cpp:558-578 TransformQuadUntrafoToIRInterface
+//   cutint/straightcutrule.cpp:582-677 StraightCutIntegrationRule
+//   xfem/cutinfo.cpp:61-132            CutInformation::Update (element part)
+//   xfem/cutinfo.cpp:476-538           GetFacetsWithNeighborTypes
+//   xfem/symboliccutbfi.cpp:76-313     SymbolicCutBilinearFormIntegrator::T_CalcElementMatrixAdd
+//   xfem/symboliccutbfi.cpp:1747-1846  MapPatchIntegrationPoint
+//   xfem/symboliccutbfi.cpp:1982-2377  SymbolicFacetPatchBilinearFormIntegrator::T_CalcFacetMatrix
+//   utils/p1interpol.cpp:104-107       vertex perturbation of InterpolateToP1
+//   cutint/cutintegral.cpp:126-212     CutIntegral::T_CutIntegrate (Integrate)
+// NGSolve pieces the reference calls but which are not in the reference tree
+// (quadrature tables, H1 shape functions, the sparse scatter) are replaced by
+// this project's own definitions, stated next to the code below.
+#include "xg_oracle.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <functional>
+#include <thread>
+#include <vector>
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Quadrature: Golub-Welsch for Gauss-Jacobi nodes (weight (1-x)^a on [-1,1]),
+// eigenvalues by the cyclic Jacobi rotation method.
+// Rule family (shared definition with the product):
+//   segment order p : Gauss-Legendre, n = p/2+1 points on [0,1]
+//   trig   order p : p<=1 centroid; p==2 3-point (1/6,1/6,2/3); p>=3 collapsed
+//                    Gauss-Jacobi conical product, n = p/2+1 per direction
+//   tet    order p : p<=1 centroid; p==2 4-point (a,b,b,b), a=(5+3sqrt5)/20;
+//                    p>=3 conical product n = p/2+1 per direction
+// ---------------------------------------------------------------------------
+void sym_eig(int n, std::vector<double>& A, std::vector<double>& V) {
+  V.assign(n * n, 0.0);
+  for (int i = 0; i < n; i++) V[i * n + i] = 1.0;
+  for (int sweep = 0; sweep < 100; sweep++) {
+    double off = 0;
+    for (int p = 0; p < n; p++)
+      for (int q = p + 1; q < n; q++) off += A[p * n + q] * A[p * n + q];
+    if (off < 1e-34) break;
+    for (int p = 0; p < n; p++)
+      for (int q = p + 1; q < n; q++) {
+        double apq = A[p * n + q];
+        if (std::fabs(apq) < 1e-300) continue;
+        double app = A[p * n + p], aqq = A[q * n + q];
+        double theta = (aqq - app) / (2 * apq);
+        double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1));
+        double c = 1 / std::sqrt(t * t + 1), s = t * c;
+        for (int k = 0; k < n; k++) {
+          double akp = A[k * n + p], akq = A[k * n + q];
+          A[k * n + p] = c * akp - s * akq;
+          A[k * n + q] = s * akp + c * akq;
+        }
+        for (int k = 0; k < n; k++) {
+          double apk = A[p * n + k], aqk = A[q * n + k];
+          A[p * n + k] = c * apk - s * aqk;
+          A[q * n + k] = s * apk + c * aqk;
+        }
+        for (int k = 0; k < n; k++) {
+          double vkp = V[k * n + p], vkq = V[k * n + q];
+          V[k * n + p] = c * vkp - s * vkq;
+          V[k * n + q] = s * vkp + c * vkq;
+        }
+      }
+  }
+}
+
+// nodes/weights on [0,1] for weight (1-u)^alpha
+void gauss_jacobi01(int n, int alpha, std::vector<double>& x, std::vector<double>& w) {
+  const double a = alpha, b = 0.0;
+  std::vector<double> J(n * n, 0.0), V;
+  for (int k = 0; k < n; k++) {
+    double diag;
+    if (k == 0) diag = (b - a) / (a + b + 2);
+    else diag = (b * b - a * a) / ((2 * k + a + b) * (2 * k + a + b + 2));
+    J[k * n + k] = diag;
+    if (k >= 1) {
+      double kk = k;
+      double num = 4 * kk * (kk + a) * (kk + b) * (kk + a + b);
+      double s = 2 * kk + a + b;
+      double den = s * s * (s + 1) * (s - 1);
+      double off = std::sqrt(num / den);
+      J[(k - 1) * n + k] = off;
+      J[k * n + (k - 1)] = off;
+    }
+  }
+  sym_eig(n, J, V);
+  double mu0 = (alpha == 0) ? 2.0 : (alpha == 1 ? 2.0 : 8.0 / 3.0);
+  std::vector<std::pair<double, double>> nw(n);
+  for (int i = 0; i < n; i++) nw[i] = {J[i * n + i], mu0 * V[0 * n + i] * V[0 * n + i]};
+  std::sort(nw.begin(), nw.end());
+  x.resize(n);
+  w.resize(n);
+  double scale = std::ldexp(1.0, -alpha - 1);
+  for (int i = 0; i < n; i++) {
+    x[i] = (1.0 + nw[i].first) * 0.5;
+    w[i] = nw[i].second * scale;
+  }
+}
+
+struct Rule {
+  std::vector<double> p;  // 3 per point
+  std::vector<double> w;
+  int size() const { return (int)w.size(); }
+};
+
+Rule make_rule(int d, int p) {
+  Rule r;
+  if (p < 0) p = 0;
+  auto add = [&](double a, double b, double c, double w) {
+    r.p.push_back(a); r.p.push_back(b); r.p.push_back(c); r.w.push_back(w);
+  };
+  int n = p / 2 + 1;
+  if (d == 0) { add(0, 0, 0, 1.0); return r; }
+  if (d == 1) {
+    std::vector<double> x, w;
+    gauss_jacobi01(n, 0, x, w);
+    for (int i = 0; i < n; i++) add(x[i], 0, 0, w[i]);
+    return r;
+  }
+  if (d == 2) {
+    if (p <= 1) { add(1.0 / 3, 1.0 / 3, 0, 0.5); return r; }
+    if (p == 2) {
+      add(1.0 / 6, 1.0 / 6, 0, 1.0 / 6);
+      add(2.0 / 3, 1.0 / 6, 0, 1.0 / 6);
+      add(1.0 / 6, 2.0 / 3, 0, 1.0 / 6);
+      return r;
+    }
+    std::vector<double> xu, wu, xv, wv;
+    gauss_jacobi01(n, 1, xu, wu);
+    gauss_jacobi01(n, 0, xv, wv);
+    for (int i = 0; i < n; i++)
+      for (int j = 0; j < n; j++) add(xu[i], xv[j] * (1 - xu[i]), 0, wu[i] * wv[j]);
+    return r;
+  }
+  // d == 3
+  if (p <= 1) { add(0.25, 0.25, 0.25, 1.0 / 6); return r; }
+  if (p == 2) {
+    double a = (5.0 + 3.0 * std::sqrt(5.0)) / 20.0, b = (5.0 - std::sqrt(5.0)) / 20.0;
+    add(a, b, b, 1.0 / 24);
+    add(b, a, b, 1.0 / 24);
+    add(b, b, a, 1.0 / 24);
+    add(b, b, b, 1.0 / 24);
+    return r;
+  }
+  std::vector<double> xu, wu, xv, wv, xw, ww;
+  gauss_jacobi01(n, 2, xu, wu);
+  gauss_jacobi01(n, 1, xv, wv);
+  gauss_jacobi01(n, 0, xw, ww);
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++)
+      for (int k = 0; k < n; k++) {
+        double u = xu[i], v = xv[j], t = xw[k];
+        add(u, (1 - u) * v, (1 - u) * (1 - v) * t, wu[i] * wv[j] * ww[k]);
+      }
+  return r;
+}
+
+const Rule& get_rule(int d, int p) {
+  static std::vector<Rule> cache[4];
+  static bool init = false;
+  if (!init) {
+    for (int dd = 0; dd < 4; dd++)
+      for (int pp = 0; pp <= 16; pp++) cache[dd].push_back(make_rule(dd, pp));
+    init = true;
+  }
+  if (p < 0) p = 0;
+  if (p > 16) p = 16;
+  return cache[d][p];
+}
+struct RuleInit { RuleInit() { get_rule(0, 0); } } rule_init_instance;
+
+// ---------------------------------------------------------------------------
+// Straight-cut geometry (restatement of cutint/straightcutrule.cpp).
+// ---------------------------------------------------------------------------
+struct P3 { double c[3]; };
+enum { NEG = 0, POS = 1, IF = 2 };
+enum { ERR_PLAIN_CUT = -2, ERR_BAD_DECOMP = -3, ERR_CAPACITY = -4 };
+
+// straightcutrule.cpp:11-24
+int check_if_straight_cut(const double* v, int n, double eps = 0.0) {
+  bool haspos = false, hasneg = false;
+  for (int i = 0; i < n; i++) {
+    if (!haspos && (v[i] > eps)) haspos = true;
+    if (!hasneg && (v[i] < -eps)) hasneg = true;
+    if (haspos && hasneg) break;
+  }
+  if ((hasneg && haspos) || (!hasneg && !haspos)) return IF;
+  return hasneg ? NEG : POS;
+}
+
+P3 seg_point(const P3& a, const P3& b, double la, double lb) {
+  // straightcutrule.cpp:50  p0 + (l0/(l0-l1))*(p1-p0)
+  double t = la / (la - lb);
+  P3 r;
+  for (int k = 0; k < 3; k++) r.c[k] = a.c[k] + t * (b.c[k] - a.c[k]);
+  return r;
+}
+
+// straightcutrule.cpp:41-64; returns #points or error
+int calc_if_points(const P3* pts, int np, const double* l, P3* out) {
+  if (check_if_straight_cut(l, np) != IF) return ERR_PLAIN_CUT;
+  if (np == 2) { out[0] = seg_point(pts[0], pts[1], l[0], l[1]); return 1; }
+  int n = 0;
+  for (int i = 0; i < np; i++)
+    for (int j = i + 1; j < np; j++)
+      if ((l[i] >= 0) != (l[j] >= 0)) {
+        double lij[2] = {l[i], l[j]};
+        if (check_if_straight_cut(lij, 2) != IF) return ERR_PLAIN_CUT;
+        out[n++] = seg_point(pts[i], pts[j], l[i], l[j]);
+      }
+  return n;
+}
+
+double l2norm3(const double* v) { return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); }
+
+// straightcutrule.cpp:66-72
+double simplex_volume(const P3* p, int np) {
+  int D = np - 1;
+  if (D == 0) return 1;
+  if (D == 1) {
+    double d[3] = {p[1].c[0] - p[0].c[0], p[1].c[1] - p[0].c[1], p[1].c[2] - p[0].c[2]};
+    return l2norm3(d);
+  }
+  if (D == 2) {
+    double a[3], b[3], c[3];
+    for (int k = 0; k < 3; k++) { a[k] = p[2].c[k] - p[0].c[k]; b[k] = p[1].c[k] - p[0].c[k]; }
+    c[0] = a[1] * b[2] - a[2] * b[1];
+    c[1] = a[2] * b[0] - a[0] * b[2];
+    c[2] = a[0] * b[1] - a[1] * b[0];
+    return l2norm3(c);
+  }
+  double a[3], b[3], c[3];
+  for (int k = 0; k < 3; k++) {
+    a[k] = p[3].c[k] - p[0].c[k]; b[k] = p[2].c[k] - p[0].c[k]; c[k] = p[1].c[k] - p[0].c[k];
+  }
+  double det = a[0] * (b[1] * c[2] - b[2] * c[1]) + a[1] * (b[2] * c[0] - b[0] * c[2]) +
+               a[2] * (b[0] * c[1] - b[1] * c[0]);
+  return std::fabs(det);
+}
+
+struct Sub { int np; P3 p[4]; };
+
+// straightcutrule.cpp:80-100
+void plain_rule(const Sub& s, int order, std::vector<double>& pts, std::vector<double>& wts) {
+  double trafofac = simplex_volume(s.p, s.np);
+  const Rule& r = get_rule(s.np - 1, order);
+  for (int q = 0; q < r.size(); q++) {
+    const double* ip = &r.p[3 * q];
+    double originweight = 1.0;
+    for (int m = 0; m < s.np - 1; ++m) originweight -= ip[m];
+    double pt[3];
+    for (int k = 0; k < 3; k++) pt[k] = originweight * s.p[0].c[k];
+    for (int m = 0; m < s.np - 1; ++m)
+      for (int k = 0; k < 3; k++) pt[k] += ip[m] * s.p[m + 1].c[k];
+    pts.push_back(pt[0]); pts.push_back(pt[1]); pts.push_back(pt[2]);
+    wts.push_back(r.w[q] * trafofac);
+  }
+}
+
+void ref_simplex(int D, P3* p) {
+  // straightcutrule.hpp:55-60 reference vertices
+  for (int i = 0; i <= D; i++)
+    for (int k = 0; k < 3; k++) p[i].c[k] = 0.0;
+  for (int i = 0; i < D; i++) p[i].c[i] = 1.0;
+}
+
+// straightcutrule.cpp:131-196
+int decompose(int D, const double* lset, int dt, Sub* subs) {
+  P3 s[4];
+  ref_simplex(D, s);
+  P3 cut[4];
+  int nc = calc_if_points(s, D + 1, lset, cut);
+  if (nc < 0) return nc;
+  int ns = 0;
+  if (dt == IF) {
+    if (nc == D) {
+      subs[0].np = nc;
+      for (int i = 0; i < nc; i++) subs[0].p[i] = cut[i];
+      return 1;
+    } else if (nc == 4 && D == 3) {
+      subs[0].np = 3; subs[0].p[0] = cut[0]; subs[0].p[1] = cut[1]; subs[0].p[2] = cut[3];
+      subs[1].np = 3; subs[1].p[0] = cut[0]; subs[1].p[1] = cut[2]; subs[1].p[2] = cut[3];
+      return 2;
+    }
+    return ERR_BAD_DECOMP;
+  }
+  int rel[4], nr = 0;
+  for (int i = 0; i < D + 1; i++)
+    if (((dt == POS) && (lset[i] >= 0)) || ((dt == NEG) && (lset[i] < 0))) rel[nr++] = i;
+  if (nr == 1) {
+    Sub& a = subs[ns++];
+    a.np = nc + 1;
+    for (int i = 0; i < nc; i++) a.p[i] = cut[i];
+    a.p[nc] = s[rel[0]];
+    if (a.np != D + 1) return ERR_BAD_DECOMP;
+  } else if (nr == 2 && D == 2) {
+    Sub& a = subs[ns++];
+    a.np = 3; a.p[0] = s[rel[0]]; a.p[1] = s[rel[1]]; a.p[2] = cut[1];
+    Sub& b = subs[ns++];
+    b.np = 3; b.p[0] = cut[0]; b.p[1] = cut[1]; b.p[2] = s[rel[0]];
+  } else if (nr == 2 && D == 3) {
+    if (nc != 4) return ERR_BAD_DECOMP;
+    Sub& a = subs[ns++];
+    a.np = 4; a.p[0] = s[rel[1]]; a.p[1] = cut[1]; a.p[2] = cut[2]; a.p[3] = cut[3];
+    Sub& b = subs[ns++];
+    b.np = 4; b.p[0] = s[rel[0]]; b.p[1] = s[rel[1]]; b.p[2] = cut[1]; b.p[3] = cut[2];
+    Sub& c = subs[ns++];
+    c.np = 4; c.p[0] = cut[0]; c.p[1] = cut[1]; c.p[2] = cut[2]; c.p[3] = s[rel[0]];
+  } else if (nr == 3 && D == 3) {
+    if (nc != 3) return ERR_BAD_DECOMP;
+    Sub& a = subs[ns++];
+    a.np = 4; a.p[0] = cut[0]; a.p[1] = cut[1]; a.p[2] = cut[2]; a.p[3] = s[rel[2]];
+    Sub& b = subs[ns++];
+    b.np = 4; b.p[0] = s[rel[0]]; b.p[1] = s[rel[1]]; b.p[2] = s[rel[2]]; b.p[3] = cut[1];
+    Sub& c = subs[ns++];
+    c.np = 4; c.p[0] = cut[0]; c.p[1] = cut[1]; c.p[2] = s[rel[0]]; c.p[3] = s[rel[2]];
+  } else {
+    return ERR_BAD_DECOMP;
+  }
+  return ns;
+}
+
+// Element geometry: x(xi) = x_D + F xi, F(:,k) = x_k - x_D (reference vertices
+// (1,0,0),(0,1,0),(0,0,1),(0,0,0) as in straightcutrule.hpp:55-60).
+struct Geo {
+  int D;
+  double x0[3];      // x_D
+  double F[3][3];    // F[i][k] = d x_i / d xi_k
+  double Finv[3][3];
+  double det;
+};
+
+void make_geo(int D, const double* elc, Geo& g) {
+  g.D = D;
+  for (int i = 0; i < 3; i++) {
+    g.x0[i] = 0;
+    for (int k = 0; k < 3; k++) { g.F[i][k] = (i == k && i >= D) ? 1.0 : 0.0; g.Finv[i][k] = g.F[i][k]; }
+  }
+  for (int i = 0; i < D; i++) g.x0[i] = elc[D * D + i];
+  for (int k = 0; k < D; k++)
+    for (int i = 0; i < D; i++) g.F[i][k] = elc[k * D + i] - elc[D * D + i];
+  if (D == 2) {
+    double a = g.F[0][0], b = g.F[0][1], c = g.F[1][0], d = g.F[1][1];
+    g.det = a * d - b * c;
+    double id = 1.0 / g.det;
+    g.Finv[0][0] = d * id; g.Finv[0][1] = -b * id;
+    g.Finv[1][0] = -c * id; g.Finv[1][1] = a * id;
+  } else {
+    const double(*F)[3] = g.F;
+    double c00 = F[1][1] * F[2][2] - F[1][2] * F[2][1];
+    double c01 = F[1][2] * F[2][0] - F[1][0] * F[2][2];
+    double c02 = F[1][0] * F[2][1] - F[1][1] * F[2][0];
+    g.det = F[0][0] * c00 + F[0][1] * c01 + F[0][2] * c02;
+    double id = 1.0 / g.det;
+    g.Finv[0][0] = c00 * id;
+    g.Finv[1][0] = c01 * id;
+    g.Finv[2][0] = c02 * id;
+    g.Finv[0][1] = (F[0][2] * F[2][1] - F[0][1] * F[2][2]) * id;
+    g.Finv[1][1] = (F[0][0] * F[2][2] - F[0][2] * F[2][0]) * id;
+    g.Finv[2][1] = (F[0][1] * F[2][0] - F[0][0] * F[2][1]) * id;
+    g.Finv[0][2] = (F[0][1] * F[1][2] - F[0][2] * F[1][1]) * id;
+    g.Finv[1][2] = (F[0][2] * F[1][0] - F[0][0] * F[1][2]) * id;
+    g.Finv[2][2] = (F[0][0] * F[1][1] - F[0][1] * F[1][0]) * id;
+  }
+}
+
+// LevelsetWrapper gradient for simplices (straightcutrule.cpp:509-513, 525-538):
+// constant reference gradient (v0-vD, v1-vD, v2-vD), normalised.
+void lset_ref_normal(int D, const double* l, double* n) {
+  double g[3] = {0, 0, 0};
+  for (int k = 0; k < D; k++) g[k] = l[k] - l[D];
+  double nn = l2norm3(g);
+  double inv = 1.0 / nn;
+  for (int k = 0; k < 3; k++) n[k] = g[k] * inv;
+}
+
+// straightcutrule.cpp:582-677 for simplices; returns #points, -1 for nullptr, <-1 error
+int straight_cut_rule(const Geo& g, const double* lset, int dt, int order,
+                      std::vector<double>& pts, std::vector<double>& wts) {
+  int D = g.D;
+  pts.clear(); wts.clear();
+  int element_domain = check_if_straight_cut(lset, D + 1);
+  if (element_domain == IF) {
+    Sub subs[3];
+    int ns = decompose(D, lset, dt, subs);
+    if (ns < 0) return ns;
+    for (int i = 0; i < ns; i++) plain_rule(subs[i], order, pts, wts);
+    if (dt == IF) {
+      // TransformQuadUntrafoToIRInterface (straightcutrule.cpp:558-578)
+      double nref[3];
+      lset_ref_normal(D, lset, nref);
+      double nphys[3] = {0, 0, 0};
+      for (int k = 0; k < D; k++) {
+        double s = 0;
+        for (int j = 0; j < D; j++) s += g.Finv[j][k] * nref[j];
+        nphys[k] = s;
+      }
+      double fac = l2norm3(nphys);
+      for (auto& w : wts) w = w * fac;
+    }
+    return (int)wts.size();
+  }
+  if (element_domain != dt) return -1;
+  const Rule& r = get_rule(D, order);
+  pts = r.p;
+  wts = r.w;
+  return r.size();
+}
+
+// ---------------------------------------------------------------------------
+// H1 basis of this project (NGSolve's own shape functions are not available):
+// vertex i: lambda_i; edge (a,b) with s/e the endpoints of smaller/larger global
+// vertex number: lambda_s*lambda_e (k>=2), lambda_s*lambda_e*(lambda_s-lambda_e) (k=3);
+// face (a,b,c) (3D, k=3) or cell (2D, k=3): lambda_a*lambda_b*lambda_c.
+// Local order: vertices, then edges (dofs of one edge adjacent), then faces.
+// ---------------------------------------------------------------------------
+const int TRI_EDGES[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+const int TET_EDGES[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+const int TET_FACES[4][3] = {{0, 1, 2}, {0, 1, 3}, {0, 2, 3}, {1, 2, 3}};
+
+int ndof_el(int D, int k) { return D == 2 ? (k + 1) * (k + 2) / 2 : (k + 1) * (k + 2) * (k + 3) / 6; }
+
+// phi[n], dphi[n][3] (reference gradient)
+void basis(int D, int k, const int* gv, const double* xi, double* phi, double (*dphi)[3]) {
+  double lam[4], dl[4][3];
+  double s = 0;
+  for (int i = 0; i < D; i++) { lam[i] = xi[i]; s += xi[i]; }
+  lam[D] = 1.0 - s;
+  for (int i = 0; i <= D; i++)
+    for (int c = 0; c < 3; c++) dl[i][c] = (i < D) ? (c == i ? 1.0 : 0.0) : (c < D ? -1.0 : 0.0);
+  int n = 0;
+  for (int i = 0; i <= D; i++, n++) {
+    phi[n] = lam[i];
+    for (int c = 0; c < 3; c++) dphi[n][c] = dl[i][c];
+  }
+  if (k >= 2) {
+    int ne = D == 2 ? 3 : 6;
+    for (int e = 0; e < ne; e++) {
+      int a = D == 2 ? TRI_EDGES[e][0] : TET_EDGES[e][0];
+      int b = D == 2 ? TRI_EDGES[e][1] : TET_EDGES[e][1];
+      int si = gv[a] < gv[b] ? a : b, ei = gv[a] < gv[b] ? b : a;
+      double ls = lam[si], le = lam[ei];
+      double q = ls * le;
+      double dq[3];
+      for (int c = 0; c < 3; c++) dq[c] = le * dl[si][c] + ls * dl[ei][c];
+      phi[n] = q;
+      for (int c = 0; c < 3; c++) dphi[n][c] = dq[c];
+      n++;
+      if (k >= 3) {
+        double t = ls - le;
+        phi[n] = q * t;
+        for (int c = 0; c < 3; c++) dphi[n][c] = dq[c] * t + q * (dl[si][c] - dl[ei][c]);
+        n++;
+      }
+    }
+  }
+  if (k >= 3) {
+    int nf = D == 2 ? 1 : 4;
+    for (int f = 0; f < nf; f++) {
+      int a = D == 2 ? 0 : TET_FACES[f][0], b = D == 2 ? 1 : TET_FACES[f][1], c2 = D == 2 ? 2 : TET_FACES[f][2];
+      phi[n] = lam[a] * lam[b] * lam[c2];
+      for (int c = 0; c < 3; c++)
+        dphi[n][c] = lam[b] * lam[c2] * dl[a][c] + lam[a] * lam[c2] * dl[b][c] + lam[a] * lam[b] * dl[c2][c];
+      n++;
+    }
+  }
+}
+
+void parallel_for(int64_t n, int nthreads, const std::function<void(int64_t, int64_t)>& f) {
+  if (nthreads <= 1 || n < 2 * nthreads) { f(0, n); return; }
+  std::vector<std::thread> th;
+  std::atomic<int64_t> next(0);
+  const int64_t chunk = std::max<int64_t>(64, n / (nthreads * 16));
+  for (int t = 0; t < nthreads; t++)
+    th.emplace_back([&]() {
+      for (;;) {
+        int64_t b = next.fetch_add(chunk);
+        if (b >= n) break;
+        f(b, std::min(n, b + chunk));
+      }
+    });
+  for (auto& t : th) t.join();
+}
+
+inline bool test_bit(const uint64_t* bits, int64_t i) { return (bits[i >> 6] >> (i & 63)) & 1u; }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Mesh / space
+// ---------------------------------------------------------------------------
+struct orc_space {
+  int D, k, nv, ne, nd;  // nd = ndof per element
+  std::vector<double> coords;
+  std::vector<int32_t> elv;
+  int64_t nedges = 0, nfaces = 0, nfacets = 0, ndof = 0;
+  std::vector<int32_t> el_edges, el_faces, el_facets;  // per element
+  std::vector<int32_t> facet_els;                      // 2 per facet, -1 boundary
+  std::vector<int32_t> el_dofs;
+  std::vector<int64_t> dof_adj_ptr;
+  std::vector<int32_t> dof_adj;  // element*32 + local
+};
+
+extern "C" {
+
+int orc_check_if_straight_cut(const double* vals, int n, double eps) {
+  return check_if_straight_cut(vals, n, eps);
+}
+
+// utils/p1interpol.cpp:104-107
+void orc_interpolate_p1_perturb(double* vals, int n, double eps) {
+  for (int i = 0; i < n; i++)
+    if (std::fabs(vals[i]) < eps) vals[i] = eps;
+}
+
+int orc_base_rule(int d, int p, double* pts, double* wts, int maxpts) {
+  const Rule& r = get_rule(d, p);
+  if (r.size() > maxpts) return ERR_CAPACITY;
+  std::memcpy(pts, r.p.data(), sizeof(double) * 3 * r.size());
+  std::memcpy(wts, r.w.data(), sizeof(double) * r.size());
+  return r.size();
+}
+
+int orc_straight_cut_rule(int D, const double* elc, const double* lset, int dt, int order,
+                          double* pts, double* wts, int maxpts) {
+  Geo g;
+  make_geo(D, elc, g);
+  std::vector<double> p, w;
+  int n = straight_cut_rule(g, lset, dt, order, p, w);
+  if (n < 0) return n;
+  if (n > maxpts) return ERR_CAPACITY;
+  std::memcpy(pts, p.data(), sizeof(double) * 3 * n);
+  std::memcpy(wts, w.data(), sizeof(double) * n);
+  return n;
+}
+
+orc_space* orc_space_create(int D, int nv, const double* coords, int ne, const int32_t* elv, int order) {
+  if ((D != 2 && D != 3) || order < 1 || order > 3) return nullptr;
+  auto* s = new orc_space();
+  s->D = D; s->k = order; s->nv = nv; s->ne = ne; s->nd = ndof_el(D, order);
+  s->coords.assign(coords, coords + (size_t)nv * D);
+  s->elv.assign(elv, elv + (size_t)ne * (D + 1));
+  // edges: sorted unique (min,max) pairs
+  const int ne_loc = D == 2 ? 3 : 6;
+  std::vector<uint64_t> keys;
+  keys.reserve((size_t)ne * ne_loc);
+  for (int e = 0; e < ne; e++)
+    for (int j = 0; j < ne_loc; j++) {
+      int a = elv[e * (D + 1) + (D == 2 ? TRI_EDGES[j][0] : TET_EDGES[j][0])];
+      int b = elv[e * (D + 1) + (D == 2 ? TRI_EDGES[j][1] : TET_EDGES[j][1])];
+      if (a > b) std::swap(a, b);
+      keys.push_back(((uint64_t)a << 32) | (uint32_t)b);
+    }
+  std::vector<uint64_t> ek(keys);
+  std::sort(ek.begin(), ek.end());
+  ek.erase(std::unique(ek.begin(), ek.end()), ek.end());
+  s->nedges = (int64_t)ek.size();
+  s->el_edges.resize((size_t)ne * ne_loc);
+  for (size_t i = 0; i < keys.size(); i++)
+    s->el_edges[i] = (int32_t)(std::lower_bound(ek.begin(), ek.end(), keys[i]) - ek.begin());
+  // faces (3D): sorted unique triples, packed 21 bits each
+  std::vector<uint64_t> fk;
+  std::vector<uint64_t> fkeys;
+  if (D == 3) {
+    fkeys.reserve((size_t)ne * 4);
+    for (int e = 0; e < ne; e++)
+      for (int j = 0; j < 4; j++) {
+        int v[3];
+        for (int m = 0; m < 3; m++) v[m] = elv[e * 4 + TET_FACES[j][m]];
+        std::sort(v, v + 3);
+        fkeys.push_back(((uint64_t)v[0] << 42) | ((uint64_t)v[1] << 21) | (uint64_t)v[2]);
+      }
+    fk = fkeys;
+    std::sort(fk.begin(), fk.end());
+    fk.erase(std::unique(fk.begin(), fk.end()), fk.end());
+    s->nfaces = (int64_t)fk.size();
+    s->el_faces.resize((size_t)ne * 4);
+    for (size_t i = 0; i < fkeys.size(); i++)
+      s->el_faces[i] = (int32_t)(std::lower_bound(fk.begin(), fk.end(), fkeys[i]) - fk.begin());
+  }
+  // facets
+  const int nfl = D + 1;
+  s->nfacets = D == 2 ? s->nedges : s->nfaces;
+  s->el_facets.resize((size_t)ne * nfl);
+  for (int e = 0; e < ne; e++)
+    for (int j = 0; j < nfl; j++)
+      s->el_facets[(size_t)e * nfl + j] = D == 2 ? s->el_edges[(size_t)e * 3 + j] : s->el_faces[(size_t)e * 4 + j];
+  s->facet_els.assign((size_t)s->nfacets * 2, -1);
+  for (int e = 0; e < ne; e++)
+    for (int j = 0; j < nfl; j++) {
+      int f = s->el_facets[(size_t)e * nfl + j];
+      if (s->facet_els[2 * f] < 0) s->facet_els[2 * f] = e;
+      else s->facet_els[2 * f + 1] = e;
+    }
+  // dofs
+  const int k = order;
+  int64_t nbub = (k == 3) ? (D == 3 ? s->nfaces : ne) : 0;
+  s->ndof = nv + s->nedges * (k - 1) + nbub;
+  s->el_dofs.resize((size_t)ne * s->nd);
+  for (int e = 0; e < ne; e++) {
+    int32_t* d = &s->el_dofs[(size_t)e * s->nd];
+    int n = 0;
+    for (int i = 0; i <= D; i++) d[n++] = elv[e * (D + 1) + i];
+    for (int j = 0; j < ne_loc && k >= 2; j++)
+      for (int m = 0; m < k - 1; m++) d[n++] = (int32_t)(nv + (int64_t)s->el_edges[(size_t)e * ne_loc + j] * (k - 1) + m);
+    if (k == 3) {
+      if (D == 3)
+        for (int j = 0; j < 4; j++) d[n++] = (int32_t)(nv + s->nedges * 2 + s->el_faces[(size_t)e * 4 + j]);
+      else
+        d[n++] = (int32_t)(nv + s->nedges * 2 + e);
+    }
+  }
+  // dof -> (element, local) adjacency, ascending elements
+  s->dof_adj_ptr.assign(s->ndof + 1, 0);
+  for (size_t i = 0; i < s->el_dofs.size(); i++) s->dof_adj_ptr[s->el_dofs[i] + 1]++;
+  for (int64_t i = 0; i < s->ndof; i++) s->dof_adj_ptr[i + 1] += s->dof_adj_ptr[i];
+  s->dof_adj.resize(s->el_dofs.size());
+  std::vector<int64_t> fill(s->dof_adj_ptr.begin(), s->dof_adj_ptr.end() - 1);
+  for (int e = 0; e < ne; e++)
+    for (int i = 0; i < s->nd; i++) s->dof_adj[fill[s->el_dofs[(size_t)e * s->nd + i]]++] = e * 32 + i;
+  return s;
+}
+
+void orc_space_destroy(orc_space* s) { delete s; }
+
+int orc_space_info(const orc_space* s, int64_t* out) {
+  out[0] = s->ndof; out[1] = s->nedges; out[2] = s->nfaces; out[3] = s->nfacets; out[4] = s->nd;
+  return 0;
+}
+int orc_space_el_dofs(const orc_space* s, int32_t* out) {
+  std::memcpy(out, s->el_dofs.data(), sizeof(int32_t) * s->el_dofs.size());
+  return 0;
+}
+int orc_space_facet_els(const orc_space* s, int32_t* out) {
+  std::memcpy(out, s->facet_els.data(), sizeof(int32_t) * s->facet_els.size());
+  return 0;
+}
+
+}  // extern "C"
+
+namespace {
+
+void element_geo(const orc_space* s, int e, Geo& g, double* lset_el, const double* lset_vertex) {
+  double elc[12];
+  const int D = s->D;
+  for (int i = 0; i <= D; i++) {
+    int v = s->elv[(size_t)e * (D + 1) + i];
+    for (int c = 0; c < D; c++) elc[i * D + c] = s->coords[(size_t)v * D + c];
+    if (lset_el) lset_el[i] = lset_vertex[v];
+  }
+  make_geo(D, elc, g);
+}
+
+void phys_grad(const Geo& g, const double* dref, double* dphys) {
+  // grad_x = F^{-T} grad_xi
+  for (int i = 0; i < 3; i++) {
+    double s = 0;
+    for (int k = 0; k < g.D; k++) s += g.Finv[k][i] * dref[k];
+    dphys[i] = (i < g.D) ? s : 0.0;
+  }
+}
+
+int default_order(int kind, int k) {
+  switch (kind) {
+    case ORC_TERM_MASS: return 2 * k;
+    case ORC_TERM_LAPLACE: return 2 * k - 2;
+    case ORC_TERM_NGRADU_V: case ORC_TERM_U_NGRADV: case ORC_TERM_CONV: return 2 * k - 1;
+    case ORC_TERM_GHOST_MASS: return 2 * k;
+  }
+  return 2 * k;
+}
+
+double hcoef(const orc_term& t, const Geo& g) {
+  double c = t.coef;
+  if (t.hpow != 0) {
+    double h = std::pow(std::fabs(g.det), 1.0 / g.D);
+    c *= std::pow(h, (double)t.hpow);
+  }
+  return c;
+}
+
+// T_CalcElementMatrixAdd (symboliccutbfi.cpp:76-313) restated for the term menu.
+int element_matrix(const orc_space* s, const double* lset_vertex, const orc_term* terms, int nterms, int e,
+                   double* elmat) {
+  const int D = s->D, n = s->nd;
+  Geo g;
+  double l[4];
+  element_geo(s, e, g, l, lset_vertex);
+  const int* gv = &s->elv[(size_t)e * (D + 1)];
+  std::vector<double> pts, wts;
+  double phi[20], dphi[20][3], gphys[20][3];
+  std::fill(elmat, elmat + n * n, 0.0);
+  // unit normal of the P1 level set (Normalize(grad(lsetp1)))
+  double gl[3] = {0, 0, 0}, nrm[3];
+  {
+    double gr[3] = {0, 0, 0};
+    for (int k = 0; k < D; k++) gr[k] = l[k] - l[D];
+    phys_grad(g, gr, gl);
+    double nn = l2norm3(gl);
+    for (int c = 0; c < 3; c++) nrm[c] = gl[c] / nn;
+  }
+  for (int t = 0; t < nterms; t++) {
+    const orc_term& T = terms[t];
+    if (T.kind == ORC_TERM_GHOST_MASS) continue;
+    if (T.defined_on && !test_bit(T.defined_on, e)) continue;
+    int order = T.order >= 0 ? T.order : default_order(T.kind, s->k);
+    int np = straight_cut_rule(g, l, T.domain, order, pts, wts);
+    if (np < -1) return np;
+    if (np <= 0) continue;
+    double c = hcoef(T, g);
+    double meas = std::fabs(g.det);
+    for (int q = 0; q < np; q++) {
+      basis(D, s->k, gv, &pts[3 * q], phi, dphi);
+      for (int i = 0; i < n; i++) phys_grad(g, dphi[i], gphys[i]);
+      double w = wts[q] * meas * c;
+      for (int i = 0; i < n; i++)      // test
+        for (int j = 0; j < n; j++) {  // trial
+          double v;
+          switch (T.kind) {
+            case ORC_TERM_MASS: v = phi[i] * phi[j]; break;
+            case ORC_TERM_LAPLACE: v = gphys[i][0] * gphys[j][0] + gphys[i][1] * gphys[j][1] + gphys[i][2] * gphys[j][2]; break;
+            case ORC_TERM_NGRADU_V: v = (nrm[0] * gphys[j][0] + nrm[1] * gphys[j][1] + nrm[2] * gphys[j][2]) * phi[i]; break;
+            case ORC_TERM_U_NGRADV: v = phi[j] * (nrm[0] * gphys[i][0] + nrm[1] * gphys[i][1] + nrm[2] * gphys[i][2]); break;
+            case ORC_TERM_CONV: v = (T.b[0] * gphys[j][0] + T.b[1] * gphys[j][1] + T.b[2] * gphys[j][2]) * phi[i]; break;
+            default: v = 0;
+          }
+          elmat[i * n + j] += w * v;
+        }
+    }
+  }
+  return 0;
+}
+
+// MapPatchIntegrationPoint (symboliccutbfi.cpp:1747-1846) for affine elements.
+void map_patch_point(const Geo& from, const Geo& to, const double* xi_from, double w_from, double* xi_to,
+                     double* w_to) {
+  const int D = from.D;
+  double vec[3] = {0, 0, 0};
+  for (int i = 0; i < D; i++) {
+    double sacc = from.x0[i];
+    for (int k = 0; k < D; k++) sacc += from.F[i][k] * xi_from[k];
+    vec[i] = sacc;
+  }
+  const double h = std::sqrt(from.det);  // GetJacobiDet (may be negative -> NaN as in the reference)
+  // low order guess: A = [x(e_d) - x(0)] = F_to, x00 = A^{-1} (vec - x(0))
+  double x00[3] = {0, 0, 0}, f[3];
+  for (int i = 0; i < D; i++) f[i] = vec[i] - to.x0[i];
+  for (int i = 0; i < D; i++) {
+    double sacc = 0;
+    for (int k = 0; k < D; k++) sacc += to.Finv[i][k] * f[k];
+    x00[i] = sacc;
+  }
+  double x0[3] = {x00[0], x00[1], x00[2]};
+  const double eps = 1e-12;  // EPS_FACET_PATCH_INTEGRATOR (utils/ngsxstd.cpp:72)
+  const int maxit = 15;      // NEWTON_ITER_TRESHOLD (utils/ngsxstd.cpp:73)
+  int its = 0;
+  double diffn = 0, w = 0;
+  while (its == 0 || (diffn > eps * h && its < maxit)) {
+    double diff[3];
+    for (int i = 0; i < D; i++) {
+      double sacc = to.x0[i];
+      for (int k = 0; k < D; k++) sacc += to.F[i][k] * x0[k];
+      diff[i] = vec[i] - sacc;
+    }
+    diffn = 0;
+    for (int i = 0; i < D; i++) diffn += diff[i] * diff[i];
+    diffn = std::sqrt(diffn);
+    for (int i = 0; i < D; i++) {
+      double sacc = 0;
+      for (int k = 0; k < D; k++) sacc += to.Finv[i][k] * diff[k];
+      x0[i] += sacc;
+    }
+    its++;
+    w = std::fabs(to.det);
+  }
+  double mipw = w_from * std::fabs(from.det);
+  double dist = 0;
+  for (int i = 0; i < D; i++) dist += (x0[i] - x00[i]) * (x0[i] - x00[i]);
+  dist = std::sqrt(dist);
+  if (its >= maxit || diffn > eps * h || dist > 10.0) {
+    for (int i = 0; i < 3; i++) xi_to[i] = x00[i];
+    *w_to = mipw / std::fabs(to.det);
+  } else {
+    for (int i = 0; i < 3; i++) xi_to[i] = x0[i];
+    *w_to = mipw / w;
+  }
+}
+
+// T_CalcFacetMatrix (symboliccutbfi.cpp:1982-2377), non-space-time, downscale = 1.
+int patch_matrix(const orc_space* s, const orc_term* terms, int nterms, int f, double* elmat) {
+  const int D = s->D, n = s->nd, n2 = 2 * n;
+  std::fill(elmat, elmat + n2 * n2, 0.0);
+  int e1 = s->facet_els[2 * f], e2 = s->facet_els[2 * f + 1];
+  if (e1 < 0 || e2 < 0) return -5;  // LocalFacetNr2==-1 (symboliccutbfi.cpp:1992)
+  Geo g1, g2;
+  element_geo(s, e1, g1, nullptr, nullptr);
+  element_geo(s, e2, g2, nullptr, nullptr);
+  const int* gv1 = &s->elv[(size_t)e1 * (D + 1)];
+  const int* gv2 = &s->elv[(size_t)e2 * (D + 1)];
+  for (int t = 0; t < nterms; t++) {
+    const orc_term& T = terms[t];
+    if (T.kind != ORC_TERM_GHOST_MASS) continue;
+    if (T.defined_on && !test_bit(T.defined_on, f)) continue;
+    int order = T.order >= 0 ? T.order : 2 * s->k;
+    const Rule& r = get_rule(D, order);
+    const int nq = r.size();
+    std::vector<double> p1(3 * 2 * nq, 0.0), p2(3 * 2 * nq, 0.0), w1(2 * nq);
+    for (int l = 0; l < 2 * nq; l++) {
+      if (l < nq) {
+        for (int c = 0; c < 3; c++) p1[3 * l + c] = r.p[3 * l + c];
+        w1[l] = r.w[l];
+        double wdummy;
+        map_patch_point(g1, g2, &p1[3 * l], w1[l], &p2[3 * l], &wdummy);
+      } else {
+        int m = l - nq;
+        for (int c = 0; c < 3; c++) p2[3 * l + c] = r.p[3 * m + c];
+        map_patch_point(g2, g1, &p2[3 * l], r.w[m], &p1[3 * l], &w1[l]);
+      }
+    }
+    double c = hcoef(T, g1);
+    double phi1[20], phi2[20], dphi[20][3];
+    double sh[40];
+    for (int l = 0; l < 2 * nq; l++) {
+      basis(D, s->k, gv1, &p1[3 * l], phi1, dphi);
+      basis(D, s->k, gv2, &p2[3 * l], phi2, dphi);
+      for (int i = 0; i < n; i++) { sh[i] = phi1[i]; sh[n + i] = -phi2[i]; }
+      double W = w1[l] * std::fabs(g1.det) * c;
+      for (int i = 0; i < n2; i++)
+        for (int j = 0; j < n2; j++) elmat[i * n2 + j] += W * sh[i] * sh[j];
+    }
+  }
+  return 0;
+}
+
+}  // namespace
+
+struct orc_csr {
+  std::vector<int64_t> rowptr;
+  std::vector<int32_t> cols;
+  std::vector<double> vals;
+};
+
+extern "C" {
+
+int orc_cutinfo(const orc_space* s, const double* lset_vertex, uint8_t* dom, double* cut_ratio, uint64_t* bits,
+                int nthreads) {
+  const int ne = s->ne, D = s->D;
+  const int64_t nw = (ne + 63) / 64;
+  std::vector<uint8_t> d8(ne);
+  std::atomic<int> err(0);
+  parallel_for(ne, nthreads, [&](int64_t b, int64_t en) {
+    std::vector<double> pts, wts;
+    for (int64_t e = b; e < en; e++) {
+      Geo g;
+      double l[4];
+      element_geo(s, (int)e, g, l, lset_vertex);
+      double part_vol[2] = {0.0, 0.0};
+      for (int np : {POS, NEG}) {
+        int n = straight_cut_rule(g, l, np, 0, pts, wts);
+        if (n < -1) err = n;
+        if (n > 0)
+          for (int q = 0; q < n; q++) part_vol[np] += wts[q];
+      }
+      cut_ratio[e] = part_vol[NEG] / (part_vol[NEG] + part_vol[POS]);
+      uint8_t t;
+      if (part_vol[NEG] > 0.0) t = (part_vol[POS] > 0.0) ? IF : NEG;
+      else t = POS;
+      d8[e] = t;
+      dom[e] = t;
+    }
+  });
+  std::memset(bits, 0, sizeof(uint64_t) * nw * 8);
+  for (int e = 0; e < ne; e++) {
+    int cdt = d8[e] == NEG ? 1 : (d8[e] == POS ? 2 : 4);
+    for (int c = 0; c < 8; c++)
+      if ((c & cdt) || c == 7) bits[c * nw + (e >> 6)] |= (uint64_t)1 << (e & 63);
+  }
+  (void)D;
+  return err.load();
+}
+
+int orc_facets_with_neighbor_types(const orc_space* s, const uint64_t* a, const uint64_t* b, int bnd_a,
+                                   int bnd_b, int use_and, uint64_t* out) {
+  const int64_t nf = s->nfacets;
+  std::memset(out, 0, sizeof(uint64_t) * ((nf + 63) / 64));
+  for (int64_t f = 0; f < nf; f++) {
+    int l = s->facet_els[2 * f], r = s->facet_els[2 * f + 1];
+    bool a_left = test_bit(a, l), b_left = test_bit(b, l);
+    bool a_right = r >= 0 ? test_bit(a, r) : (bool)bnd_a;
+    bool b_right = r >= 0 ? test_bit(b, r) : (bool)bnd_b;
+    bool set = use_and ? ((a_left && b_right) || (a_right && b_left)) : ((a_left || b_right) || (a_right || b_left));
+    if (set) out[f >> 6] |= (uint64_t)1 << (f & 63);
+  }
+  return 0;
+}
+
+// CutIntegral::T_CutIntegrate (cutint/cutintegral.cpp:126-212) for f = x^ex y^ey z^ez.
+double orc_integrate(const orc_space* s, const double* lset_vertex, int dt, int order, int ex, int ey, int ez,
+                     const uint64_t* defined_on) {
+  const int D = s->D;
+  double sum = 0;
+  std::vector<double> pts, wts;
+  for (int e = 0; e < s->ne; e++) {
+    if (defined_on && !test_bit(defined_on, e)) continue;
+    Geo g;
+    double l[4];
+    element_geo(s, e, g, l, lset_vertex);
+    int n = straight_cut_rule(g, l, dt, order, pts, wts);
+    if (n <= 0) continue;
+    double meas = std::fabs(g.det);
+    for (int q = 0; q < n; q++) {
+      double x[3] = {0, 0, 0};
+      for (int i = 0; i < D; i++) {
+        double sacc = g.x0[i];
+        for (int k = 0; k < D; k++) sacc += g.F[i][k] * pts[3 * q + k];
+        x[i] = sacc;
+      }
+      double fv = std::pow(x[0], ex) * std::pow(x[1], ey) * (D == 3 ? std::pow(x[2], ez) : 1.0);
+      sum += wts[q] * meas * fv;
+    }
+  }
+  return sum;
+}
+
+int orc_element_matrix(const orc_space* s, const double* lset_vertex, const orc_term* terms, int nterms, int e,
+                       double* elmat) {
+  return element_matrix(s, lset_vertex, terms, nterms, e, elmat);
+}
+
+int orc_patch_matrix(const orc_space* s, const orc_term* terms, int nterms, int f, double* elmat) {
+  return patch_matrix(s, terms, nterms, f, elmat);
+}
+
+orc_csr* orc_assemble(const orc_space* s, const double* lset_vertex, const orc_term* terms, int nterms,
+                      int nthreads) {
+  const int ne = s->ne, n = s->nd, n2 = 2 * n;
+  const int64_t nf = s->nfacets;
+  // active elements: in the definedon set of some volume term
+  std::vector<int32_t> el_slot(ne, -1), fa_slot(nf, -1);
+  bool any_vol = false, any_patch = false;
+  for (int t = 0; t < nterms; t++) (terms[t].kind == ORC_TERM_GHOST_MASS ? any_patch : any_vol) = true;
+  int nact = 0;
+  for (int e = 0; e < ne && any_vol; e++) {
+    bool act = false;
+    for (int t = 0; t < nterms; t++)
+      if (terms[t].kind != ORC_TERM_GHOST_MASS && (!terms[t].defined_on || test_bit(terms[t].defined_on, e))) act = true;
+    if (act) el_slot[e] = nact++;
+  }
+  int nfa = 0;
+  for (int64_t f = 0; f < nf && any_patch; f++) {
+    if (s->facet_els[2 * f + 1] < 0) continue;
+    bool act = false;
+    for (int t = 0; t < nterms; t++)
+      if (terms[t].kind == ORC_TERM_GHOST_MASS && (!terms[t].defined_on || test_bit(terms[t].defined_on, f))) act = true;
+    if (act) fa_slot[f] = nfa++;
+  }
+  std::vector<int32_t> el_list(nact), fa_list(nfa);
+  for (int e = 0; e < ne; e++) if (el_slot[e] >= 0) el_list[el_slot[e]] = e;
+  for (int64_t f = 0; f < nf; f++) if (fa_slot[f] >= 0) fa_list[fa_slot[f]] = (int32_t)f;
+  std::vector<double> elm((size_t)nact * n * n), fam((size_t)nfa * n2 * n2);
+  std::atomic<int> err(0);
+  parallel_for(nact, nthreads, [&](int64_t b, int64_t en) {
+    for (int64_t i = b; i < en; i++) {
+      int r = element_matrix(s, lset_vertex, terms, nterms, el_list[i], &elm[(size_t)i * n * n]);
+      if (r) err = r;
+    }
+  });
+  parallel_for(nfa, nthreads, [&](int64_t b, int64_t en) {
+    for (int64_t i = b; i < en; i++) {
+      int r = patch_matrix(s, terms, nterms, fa_list[i], &fam[(size_t)i * n2 * n2]);
+      if (r) err = r;
+    }
+  });
+  if (err.load()) return nullptr;
+  // row-wise gather (dof -> element adjacency, elements ascending)
+  const int64_t ndof = s->ndof;
+  const int nfl = s->D + 1;
+  auto* csr = new orc_csr();
+  csr->rowptr.assign(ndof + 1, 0);
+  std::vector<std::vector<int32_t>> rc(ndof);
+  std::vector<std::vector<double>> rv(ndof);
+  parallel_for(ndof, nthreads, [&](int64_t b, int64_t en) {
+    std::vector<std::pair<int32_t, double>> cand;
+    for (int64_t r = b; r < en; r++) {
+      cand.clear();
+      for (int64_t a = s->dof_adj_ptr[r]; a < s->dof_adj_ptr[r + 1]; a++) {
+        int e = s->dof_adj[a] >> 5, i = s->dof_adj[a] & 31;
+        const int32_t* de = &s->el_dofs[(size_t)e * n];
+        if (el_slot[e] >= 0) {
+          const double* m = &elm[(size_t)el_slot[e] * n * n];
+          for (int j = 0; j < n; j++) cand.push_back({de[j], m[i * n + j]});
+        }
+        for (int lf = 0; lf < nfl; lf++) {
+          int f = s->el_facets[(size_t)e * nfl + lf];
+          if (fa_slot[f] < 0) continue;
+          int e1 = s->facet_els[2 * f], e2 = s->facet_els[2 * f + 1];
+          int row = (e == e1) ? i : n + i;
+          const double* m = &fam[(size_t)fa_slot[f] * n2 * n2];
+          const int32_t* d1 = &s->el_dofs[(size_t)e1 * n];
+          const int32_t* d2 = &s->el_dofs[(size_t)e2 * n];
+          for (int j = 0; j < n; j++) cand.push_back({d1[j], m[row * n2 + j]});
+          for (int j = 0; j < n; j++) cand.push_back({d2[j], m[row * n2 + n + j]});
+        }
+      }
+      std::stable_sort(cand.begin(), cand.end(),
+                       [](const std::pair<int32_t, double>& x, const std::pair<int32_t, double>& y) { return x.first < y.first; });
+      for (size_t c = 0; c < cand.size();) {
+        size_t d = c;
+        double sacc = 0;
+        while (d < cand.size() && cand[d].first == cand[c].first) sacc += cand[d++].second;
+        rc[r].push_back(cand[c].first);
+        rv[r].push_back(sacc);
+        c = d;
+      }
+    }
+  });
+  for (int64_t r = 0; r < ndof; r++) csr->rowptr[r + 1] = csr->rowptr[r] + (int64_t)rc[r].size();
+  csr->cols.resize(csr->rowptr[ndof]);
+  csr->vals.resize(csr->rowptr[ndof]);
+  for (int64_t r = 0; r < ndof; r++) {
+    std::copy(rc[r].begin(), rc[r].end(), csr->cols.begin() + csr->rowptr[r]);
+    std::copy(rv[r].begin(), rv[r].end(), csr->vals.begin() + csr->rowptr[r]);
+  }
+  return csr;
+}
+
+int64_t orc_csr_nnz(const orc_csr* c) { return c->rowptr.back(); }
+void orc_csr_get(const orc_csr* c, int64_t* rowptr, int32_t* cols, double* vals) {
+  std::memcpy(rowptr, c->rowptr.data(), sizeof(int64_t) * c->rowptr.size());
+  std::memcpy(cols, c->cols.data(), sizeof(int32_t) * c->cols.size());
+  std::memcpy(vals, c->vals.data(), sizeof(double) * c->vals.size());
+}
+void orc_csr_destroy(orc_csr* c) { delete c; }
+
+// CutFEM pipeline as in demos/fictdom.py:95-133: CutInfo -> HASNEG / IF element
+// sets -> ghost facets (HASNEG, IF) -> assembly.  Volume terms on NEG get the
+// HASNEG set, IF terms the IF set, POS terms the HASPOS set; patch terms get the
+// ghost facets.
+int64_t orc_pipeline(const orc_space* s, const double* lset_vertex, const orc_term* terms, int nterms,
+                     int ghost_facets, int nthreads) {
+  const int ne = s->ne;
+  const int64_t nw = (ne + 63) / 64, nfw = (s->nfacets + 63) / 64;
+  std::vector<uint8_t> dom(ne);
+  std::vector<double> ratio(ne);
+  std::vector<uint64_t> bits(8 * nw), fb(nfw);
+  if (orc_cutinfo(s, lset_vertex, dom.data(), ratio.data(), bits.data(), nthreads)) return -1;
+  const uint64_t* hasneg = &bits[5 * nw];
+  const uint64_t* ifb = &bits[4 * nw];
+  const uint64_t* haspos = &bits[6 * nw];
+  if (ghost_facets) orc_facets_with_neighbor_types(s, hasneg, ifb, 1, 1, 1, fb.data());
+  std::vector<orc_term> t2(terms, terms + nterms);
+  for (auto& t : t2) {
+    if (t.kind == ORC_TERM_GHOST_MASS) t.defined_on = fb.data();
+    else t.defined_on = t.domain == ORC_NEG ? hasneg : (t.domain == ORC_IF ? ifb : haspos);
+  }
+  orc_csr* c = orc_assemble(s, lset_vertex, t2.data(), nterms, nthreads);
+  if (!c) return -2;
+  int64_t nnz = orc_csr_nnz(c);
+  orc_csr_destroy(c);
+  return nnz;
+}
+
+}  // extern "C"

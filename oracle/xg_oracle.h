@@ -1,0 +1,98 @@
+/*
+ * Oracle for the cut-element hot path: a CPU restatement of ngsxfem's
+ * straight-cut quadrature, CutInfo marking, facet marking, cut bilinear-form
+ * and facet-patch (ghost-penalty) element matrices and their sparse assembly.
+ *
+ * THIS IS TEST INFRASTRUCTURE. Only tests/, __graft_entry__.smoke() and the
+ * cpu_baseline / reference legs of bench.py may load it, and only as the
+ * checker or the timed CPU baseline.  The product (ngsxfem_gb300/) never links
+ * or calls it.
+ *
+ * Parity status: the reference (ngsxfem) needs NGSolve, which cannot be built
+ * or imported here, so point- and entry-level parity with the real reference
+ * is unpinned.  The oracle is pinned against the closed-form known answers the
+ * reference's own tests assert (areas, perimeters, monomial moments of planar
+ * cuts, space-time planar cuts); see tests/test_oracle_known_answers.py.
+ */
+#ifndef XG_ORACLE_H
+#define XG_ORACLE_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Domain types, same values as ngsxfem utils/ngsxstd.hpp:16-35. */
+enum { ORC_NEG = 0, ORC_POS = 1, ORC_IF = 2 };
+
+/* Term kinds; identical numbering to the product's XG_TERM_*. */
+enum {
+  ORC_TERM_MASS = 0,       /* c * u * v                          */
+  ORC_TERM_LAPLACE = 1,    /* c * grad u . grad v                */
+  ORC_TERM_NGRADU_V = 2,   /* c * (n . grad u) * v, n = grad(lset)/|grad(lset)| */
+  ORC_TERM_U_NGRADV = 3,   /* c * u * (n . grad v)               */
+  ORC_TERM_CONV = 4,       /* c * (b . grad u) * v               */
+  ORC_TERM_GHOST_MASS = 5  /* c * (u - u.Other()) * (v - v.Other()) on a facet patch */
+};
+
+typedef struct {
+  int kind;
+  int domain;      /* ORC_NEG / ORC_POS / ORC_IF (ignored for GHOST_MASS) */
+  int order;       /* -1: default order (trial+test-difforders; 2*maxorder for patches) */
+  int hpow;        /* coefficient multiplied by h^hpow, h = |det F|^(1/D) of the (first) element */
+  double coef;
+  double b[3];     /* convection field for ORC_TERM_CONV */
+  const uint64_t* defined_on; /* element bits (volume terms) or facet bits (patch terms); NULL = all */
+} orc_term;
+
+/* --- single-element functions -------------------------------------------- */
+int orc_check_if_straight_cut(const double* vals, int n, double eps);
+void orc_interpolate_p1_perturb(double* vals, int n, double eps);
+/* Base rule of the rule family for element dimension d (1 segment, 2 trig, 3 tet) and order p.
+ * Returns number of points; pts has 3 doubles per point. */
+int orc_base_rule(int d, int p, double* pts, double* wts, int maxpts);
+/* Straight-cut rule on one simplex with physical vertex coords elc[(D+1)*D].
+ * Returns number of points, -1 for "no rule" (nullptr), or < -1 on error. */
+int orc_straight_cut_rule(int D, const double* elc, const double* lset, int dt, int order,
+                          double* pts, double* wts, int maxpts);
+
+/* --- mesh-level functions ------------------------------------------------- */
+typedef struct orc_space orc_space;
+/* coords: nv*D (AoS), elv: ne*(D+1). order: H1 order 1..3. */
+orc_space* orc_space_create(int D, int nv, const double* coords, int ne, const int32_t* elv, int order);
+void orc_space_destroy(orc_space*);
+int orc_space_info(const orc_space*, int64_t* out /* [ndof, nedges, nfaces, nfacets, ndof_el] */);
+int orc_space_el_dofs(const orc_space*, int32_t* out /* ne*ndof_el */);
+int orc_space_facet_els(const orc_space*, int32_t* out /* nfacets*2 */);
+
+/* CutInfo.Update: dom[ne] (NEG/POS/IF by volume fractions), cut_ratio[ne],
+ * bits[8][nwords] element bitsets per COMBINED_DOMAIN_TYPE (64 elements per word). */
+int orc_cutinfo(const orc_space*, const double* lset_vertex, uint8_t* dom, double* cut_ratio,
+                uint64_t* bits, int nthreads);
+int orc_facets_with_neighbor_types(const orc_space*, const uint64_t* a, const uint64_t* b,
+                                   int bnd_a, int bnd_b, int use_and, uint64_t* out);
+double orc_integrate(const orc_space*, const double* lset_vertex, int dt, int order,
+                     int ex, int ey, int ez, const uint64_t* defined_on);
+
+/* Element matrix of the sum of volume terms on element e (row = test, col = trial). */
+int orc_element_matrix(const orc_space*, const double* lset_vertex, const orc_term* terms, int nterms,
+                       int e, double* elmat);
+/* Facet-patch matrix of patch terms on facet f: (2n)^2, dofs [el1, el2]. */
+int orc_patch_matrix(const orc_space*, const orc_term* terms, int nterms, int f, double* elmat);
+
+typedef struct orc_csr orc_csr;
+/* Full assembly: volume terms over their elements, patch terms over their facets,
+ * summed into a CSR over all dofs (rows of untouched dofs are empty). */
+orc_csr* orc_assemble(const orc_space*, const double* lset_vertex, const orc_term* terms, int nterms,
+                      int nthreads);
+int64_t orc_csr_nnz(const orc_csr*);
+void orc_csr_get(const orc_csr*, int64_t* rowptr, int32_t* cols, double* vals);
+void orc_csr_destroy(orc_csr*);
+
+/* Whole CPU pipeline (CutInfo + facet marking + assembly) for timing: returns nnz. */
+int64_t orc_pipeline(const orc_space*, const double* lset_vertex, const orc_term* terms, int nterms,
+                     int ghost_facets, int nthreads);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
