@@ -20,7 +20,6 @@ import json
 import os
 import subprocess
 import sys
-import threading
 import time
 
 import numpy as np
@@ -197,6 +196,9 @@ def main():
 
     # stage events (profiling hook, recorded on the launching stream)
     evs = [torch.cuda.Event(enable_timing=True) for _ in range(8)]
+    for e in evs:  # torch creates the CUDA event on first record
+        e.record(stream)
+    torch.cuda.synchronize()
     ev_arr = (ctypes.c_void_p * 8)(*[ctypes.c_void_p(e.cuda_event) for e in evs])
 
     def step():

@@ -150,6 +150,9 @@ int xg_cut_rules(xg_mesh* mesh, const double* d_lset, const int32_t* d_elems, in
                  int32_t max_pts, int32_t* d_counts, double* d_pts, double* d_wts, void* stream);
 /* Number of points of the rule family for (element dim d, order p). */
 int xg_base_rule_size(int d, int p);
+/* Host copy of that rule (NGSolve's SelectIntegrationRule(ET, p) stand-in):
+ * h_pts[3*q + c], h_wts[q]; returns the point count or -1 if max_pts is too small. */
+int xg_base_rule(int d, int p, double* h_pts, double* h_wts, int max_pts);
 
 /* Integrate(x^ex y^ey z^ez * dCut(lset, dt, order)) over the elements in
  * d_defined_on (NULL = all): cutint/cutintegral.cpp:126-212.  The sum is

@@ -22,11 +22,12 @@ int cuda_fail(cudaError_t e, const char* what) {
 // P_n^{(a,0)} by the three-term recurrence; weights 2^{a+1} / ((1-x^2) P_n'(x)^2).
 static void jacobi_eval(int n, double a, double x, double* p, double* dp) {
   const double b = 0.0;
-  double p0 = 1.0, p1 = (a + 1.0) + (a + b + 2.0) * (x - 1.0) * 0.5;
+  // P_1 = ((a - b) + (a + b + 2) x) / 2, written so that x = 0 stays exact
+  double p0 = 1.0, p1 = 0.5 * (a - b) + 0.5 * (a + b + 2.0) * x;
   if (n == 0) { *p = 1.0; *dp = 0.0; return; }
   // derivative: d/dx P_n^{(a,b)} = (n+a+b+1)/2 * P_{n-1}^{(a+1,b+1)}
   auto pval = [](int m, double aa, double bb, double xx) {
-    double q0 = 1.0, q1 = (aa + 1.0) + (aa + bb + 2.0) * (xx - 1.0) * 0.5;
+    double q0 = 1.0, q1 = 0.5 * (aa - bb) + 0.5 * (aa + bb + 2.0) * xx;
     if (m == 0) return q0;
     for (int k = 2; k <= m; k++) {
       double c = 2.0 * k + aa + bb;
@@ -59,6 +60,7 @@ static void gauss_jacobi01(int n, int alpha, std::vector<double>& x01, std::vect
   const double a = alpha;
   for (int k = 0; k < n; k++) {
     double z = -std::cos(M_PI * (k + 0.75) / (n + 0.5));  // ascending initial guesses
+    if (alpha == 0 && n % 2 == 1 && k == n / 2) z = 0.0;   // middle Gauss-Legendre node
     for (int it = 0; it < 100; it++) {
       double p, dp;
       jacobi_eval(n, a, z, &p, &dp);
@@ -213,6 +215,18 @@ int xg_device_ok(int* ok) {
 int xg_base_rule_size(int d, int p) {
   if (d < 0 || d > 3) return -1;
   return host_rules().cnt[d][clamp_order(p)];
+}
+
+int xg_base_rule(int d, int p, double* h_pts, double* h_wts, int max_pts) {
+  if (d < 0 || d > 3 || !h_pts || !h_wts) return -1;
+  const RuleTable& t = host_rules();
+  const int q = clamp_order(p), off = t.off[d][q], cnt = t.cnt[d][q];
+  if (cnt > max_pts) return -1;
+  for (int i = 0; i < cnt; i++) {
+    for (int c = 0; c < 3; c++) h_pts[3 * i + c] = t.x[off + i][c];
+    h_wts[i] = t.w[off + i];
+  }
+  return cnt;
 }
 
 int xg_mesh_create(int dim, int32_t nv, const double* h_coords, int32_t ne, const int32_t* h_elv, xg_mesh** out) {

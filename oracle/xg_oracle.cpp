@@ -103,6 +103,37 @@ void gauss_jacobi01(int n, int alpha, std::vector<double>& x, std::vector<double
   std::vector<std::pair<double, double>> nw(n);
   for (int i = 0; i < n; i++) nw[i] = {J[i * n + i], mu0 * V[0 * n + i] * V[0 * n + i]};
   std::sort(nw.begin(), nw.end());
+  // Newton polish of the eigenvalues on P_n^{(a,0)} (values and derivatives by
+  // the recurrences of P_n and of P'_n), weights from the Christoffel formula
+  // 2^{a+1} / ((1 - x^2) P_n'(x)^2)
+  auto jac = [&](double xx, double& pv, double& dv) {
+    double p0 = 1.0, p1 = 0.5 * (a - b) + 0.5 * (a + b + 2.0) * xx;
+    double d0 = 0.0, d1 = 0.5 * (a + b + 2.0);
+    if (n == 0) { pv = 1.0; dv = 0.0; return; }
+    for (int k = 2; k <= n; k++) {
+      double c = 2.0 * k + a + b;
+      double A1 = 2.0 * k * (k + a + b) * (c - 2.0);
+      double A2 = (c - 1.0) * (a * a - b * b);
+      double A3 = (c - 2.0) * (c - 1.0) * c;
+      double A4 = 2.0 * (k + a - 1.0) * (k + b - 1.0) * c;
+      double p2 = ((A2 + A3 * xx) * p1 - A4 * p0) / A1;
+      double d2 = ((A2 + A3 * xx) * d1 + A3 * p1 - A4 * d0) / A1;
+      p0 = p1; p1 = p2; d0 = d1; d1 = d2;
+    }
+    pv = p1; dv = d1;
+  };
+  for (int i = 0; i < n; i++) {
+    double xx = nw[i].first;
+    if (alpha == 0 && (n % 2) == 1 && i == n / 2) xx = 0.0;
+    for (int it = 0; it < 3; it++) {
+      double pv, dv;
+      jac(xx, pv, dv);
+      xx -= pv / dv;
+    }
+    double pv, dv;
+    jac(xx, pv, dv);
+    nw[i] = {xx, std::ldexp(1.0, alpha + 1) / ((1.0 - xx * xx) * dv * dv)};
+  }
   x.resize(n);
   w.resize(n);
   double scale = std::ldexp(1.0, -alpha - 1);

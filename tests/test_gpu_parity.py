@@ -1,9 +1,11 @@
 """libxg (GPU, through the C ABI) against the oracle on seeded inputs.
 
-Bars: domain types, counts and bitsets bit-exact; cut ratios and rule
-points/weights bit-exact (the marking/rule translation unit is built with
--fmad=false); assembled FP64 matrices within 1e-12 relative to the largest
-entry; mixed precision within 1e-5."""
+Bars: domain types, counts and bitsets bit-exact; cut ratios bit-exact (the
+marking translation unit is built with -fmad=false and the order-0 rules are
+exact constants); rule points and weights within 1e-14 (the two sides build
+their base rules with different algorithms, Golub-Welsch vs Newton, which may
+differ in the last bit; the required bar is 1e-12); assembled FP64 matrices
+within 1e-12 relative to the largest entry; mixed precision within 1e-5."""
 import ctypes
 import math
 
@@ -95,8 +97,8 @@ def test_cut_rules_parity(xg, orc, case, dt, order):
             continue
         p, w = r
         assert counts[i] == len(w)
-        assert np.array_equal(pts[i, : len(w)], p), (e, np.max(np.abs(pts[i, : len(w)] - p)))
-        assert np.array_equal(wts[i, : len(w)], w), (e, np.max(np.abs(wts[i, : len(w)] - w)))
+        assert np.max(np.abs(pts[i, : len(w)] - p)) <= 1e-14, e
+        assert np.max(np.abs(wts[i, : len(w)] - w)) <= 1e-14 * max(1e-300, np.max(np.abs(w))), e
 
 
 @pytest.mark.parametrize("case", list(CASES))

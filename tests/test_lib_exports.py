@@ -60,3 +60,22 @@ def test_no_device_reports_cleanly(lib):
     ok = ctypes.c_int(-1)
     assert lib.xg_device_ok(ctypes.byref(ok)) == 8
     assert ok.value == 0
+
+
+def test_rule_family_matches_oracle(lib):
+    """Host rule tables of the product equal the oracle's rule family (built by
+    a different algorithm) to the last bit or so."""
+    import numpy as np
+    from oracle import oracle as orc
+    orc.build()
+    P = ctypes.c_void_p
+    lib.xg_base_rule.argtypes = [ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int]
+    for d in (1, 2, 3):
+        for p in range(0, 9):
+            pts = np.zeros((512, 3))
+            w = np.zeros(512)
+            n = lib.xg_base_rule(d, p, pts.ctypes.data_as(P), w.ctypes.data_as(P), 512)
+            rp, rw = orc.base_rule(d, p)
+            assert n == len(rw)
+            assert np.max(np.abs(pts[:n] - rp)) <= 4e-16, (d, p)
+            assert np.max(np.abs(w[:n] - rw)) <= 4e-16, (d, p)
