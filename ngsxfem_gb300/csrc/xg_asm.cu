@@ -763,83 +763,171 @@ __global__ void __launch_bounds__(PaCfg<D, K>::NT) k_patch(
 }
 
 // ============================================================================
-// Scatter: one warp per active row.  Candidate columns are the dofs of the
-// active elements containing the row's dof and of the active facet patches
-// of those elements; a warp bitonic sort + unique gives the row pattern, and
-// the row's values are summed in the fixed order (adjacent elements
-// ascending, then their facets in local order) -- no atomics.
+// Scatter: one warp per active row (the row of dof r).  The row's columns are
+// the dofs of the active elements containing r and, for every active facet of
+// an element containing r, the dofs of both elements of that facet patch.
+// Pass 1 counts the distinct columns (shared-memory hash); pass 2 rebuilds the
+// set, sorts it, stages (position, value) pairs with independent global loads
+// and adds them in the fixed order (adjacent elements ascending; per element
+// its own matrix row, then its facets in local order, first then second
+// element's columns) -- the sum order never depends on scheduling, no atomics.
 // ============================================================================
 struct ScatterArgs {
   int ne, nd, nfl;
-  int64_t nf;
-  const int32_t* el_dofs;   // [nd][ne]
-  const int32_t* el_facets; // [nfl][ne]
-  const int32_t* fel;       // [2][nf]
+  const int32_t* el_dofs;    // [ne][nd]
+  const int32_t* el_facets;  // [ne][nfl]
+  const int2* fel;           // [nf] first / second element
   const int32_t* adj_ptr;
   const int32_t* adj;
   const uint32_t* act_un;
   const uint32_t* act_cut;
   const uint32_t* act_fa;
-  const int32_t* el_slot;   // valid for active elements
-  const int32_t* fa_slot;   // valid for active facets
-  const int32_t* rows;      // active dofs (row -> dof)
-  const int32_t* dof_row;   // dof -> row (valid for active dofs)
-  const int* counts;        // [3] = nrows
-  int64_t cap_fa;           // facet-patch workspace slots
-  int cap;                  // candidate buffer per warp (pow2)
-  int capu;                 // unique capacity per warp
+  const int32_t* el_slot;    // valid for active elements
+  const int32_t* fa_slot;    // valid for active facets
+  const int32_t* rows;       // active dofs (row -> dof)
+  const int32_t* dof_row;    // dof -> row (valid for active dofs)
+  const int* counts;         // [3] = nrows
+  int64_t cap_fa;
+  int hs;                    // hash slots per warp (pow2)
+  int maxu;                  // distinct-column capacity per warp (pow2)
+  int stage;                 // staged (pos, value) pairs per warp
+  int wbytes;                // shared bytes per warp
 };
 
-constexpr int kScWarps = 4;
+constexpr int kRowWarps = 8;
+constexpr int kEnt = 32;  // adjacency entries per chunk
+
+struct RowSm {
+  int* hash;
+  int* ucols;
+  double* acc;
+  double* sval;
+  int* spos;
+  int* ent_e;
+  int* ent_i;
+  int* ent_nb;     // [kEnt][4] other element of an active facet, -1 if inactive
+  int* ent_fs;     // [kEnt][4] facet slot
+  int* ent_first;  // [kEnt][4] 1 if the row's element is the facet's first element
+  int* celem;      // [kEnt * 5]
+  int* grp;        // [kEnt * 9] (entry << 4) | kind
+};
+
+__host__ __device__ inline int row_smem_bytes(int hs, int maxu, int stage) {
+  return hs * 4 + maxu * 4 + maxu * 8 + stage * 8 + stage * 4 + kEnt * 4 * 2 + kEnt * 4 * 4 * 3 + kEnt * 5 * 4 +
+         kEnt * 9 * 4 + 16;
+}
+
+__device__ __forceinline__ RowSm row_sm(const ScatterArgs& A, unsigned char* base) {
+  RowSm S;
+  S.hash = (int*)base;
+  S.ucols = S.hash + A.hs;
+  S.acc = (double*)(S.ucols + A.maxu);  // hs, maxu are powers of two >= 32: 8-byte aligned
+  S.sval = S.acc + A.maxu;
+  S.spos = (int*)(S.sval + A.stage);
+  S.ent_e = S.spos + A.stage;
+  S.ent_i = S.ent_e + kEnt;
+  S.ent_nb = S.ent_i + kEnt;
+  S.ent_fs = S.ent_nb + kEnt * 4;
+  S.ent_first = S.ent_fs + kEnt * 4;
+  S.celem = S.ent_first + kEnt * 4;
+  S.grp = S.celem + kEnt * 5;
+  return S;
+}
 
 __device__ __forceinline__ bool el_active(const ScatterArgs& A, int e) {
   return tbit32(A.act_un, e) || tbit32(A.act_cut, e);
 }
 
-// gathers the candidate dofs of row dof r into buf; returns count (or -1 on overflow)
-__device__ int gather_candidates(const ScatterArgs& A, int r, int* buf) {
+// Loads adjacency entries [c0, c0+na) of the row into shared memory; returns the
+// number of candidate elements written to S.celem.
+__device__ int load_entries(const ScatterArgs& A, const RowSm& S, int c0, int na) {
   const int lane = threadIdx.x & 31;
-  const int a0 = A.adj_ptr[r], a1 = A.adj_ptr[r + 1];
-  int total = 0;
-  for (int base = a0; base < a1; base += 32) {
-    const int a = base + lane;
-    int e = -1, ncand = 0;
-    int fmask = 0;
-    if (a < a1) {
-      e = A.adj[a] >> 5;
-      if (el_active(A, e)) ncand += A.nd;
-      for (int lf = 0; lf < A.nfl; lf++) {
-        int f = A.el_facets[(int64_t)lf * A.ne + e];
-        if (tbit32(A.act_fa, f)) {
-          fmask |= 1 << lf;
-          ncand += 2 * A.nd;
-        }
+  int ncand = 0;
+  if (lane < na) {
+    const int v = A.adj[c0 + lane];
+    const int e = v >> 5, i = v & 31;
+    const bool act = el_active(A, e);
+    S.ent_e[lane] = act ? e : ~e;  // sign marks an inactive element
+    S.ent_i[lane] = i;
+    int nf = 0;
+    for (int lf = 0; lf < A.nfl; lf++) {
+      int nb = -1, fs = 0, first = 0;
+      const int f = A.el_facets[(int64_t)e * A.nfl + lf];
+      if (tbit32(A.act_fa, f)) {
+        const int2 p = A.fel[f];
+        first = p.x == e;
+        nb = first ? p.y : p.x;
+        fs = A.fa_slot[f];
+        nf++;
       }
+      S.ent_nb[lane * 4 + lf] = nb;
+      S.ent_fs[lane * 4 + lf] = fs;
+      S.ent_first[lane * 4 + lf] = first;
     }
-    // warp prefix
-    int x = ncand;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      int y = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += y;
-    }
-    const int my = total + x - ncand;
-    total += __shfl_sync(0xffffffffu, x, 31);
-    if (total > A.cap) return -1;
-    if (a < a1) {
-      int k = my;
-      if (el_active(A, e))
-        for (int j = 0; j < A.nd; j++) buf[k++] = A.el_dofs[(int64_t)j * A.ne + e];
-      for (int lf = 0; lf < A.nfl; lf++)
-        if (fmask & (1 << lf)) {
-          int f = A.el_facets[(int64_t)lf * A.ne + e];
-          int e1 = A.fel[f], e2 = A.fel[A.nf + f];
-          for (int j = 0; j < A.nd; j++) buf[k++] = A.el_dofs[(int64_t)j * A.ne + e1];
-          for (int j = 0; j < A.nd; j++) buf[k++] = A.el_dofs[(int64_t)j * A.ne + e2];
-        }
-    }
+    ncand = ((act || nf) ? 1 : 0) + nf;
   }
+  int x = ncand;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  const int total = __shfl_sync(0xffffffffu, x, 31);
+  if (lane < na && ncand) {
+    int k = x - ncand;
+    const int e = S.ent_e[lane] >= 0 ? S.ent_e[lane] : ~S.ent_e[lane];
+    S.celem[k++] = e;
+    for (int lf = 0; lf < A.nfl; lf++)
+      if (S.ent_nb[lane * 4 + lf] >= 0) S.celem[k++] = S.ent_nb[lane * 4 + lf];
+  }
+  __syncwarp();
   return total;
+}
+
+__device__ __forceinline__ bool hash_insert(int* hash, int hs, int key) {
+  unsigned h = ((unsigned)key * 2654435761u) & (unsigned)(hs - 1);
+  for (int probe = 0; probe < hs; probe++) {
+    int old = atomicCAS(&hash[h], 0, key + 1);
+    if (old == 0 || old == key + 1) return true;
+    h = (h + 1) & (unsigned)(hs - 1);
+  }
+  return false;  // table full: reported as a capacity error
+}
+
+// Builds the row's column set in the hash table; returns false on overflow.
+__device__ bool row_columns(const ScatterArgs& A, const RowSm& S, int r) {
+  const int lane = threadIdx.x & 31;
+  for (int k = lane; k < A.hs; k += 32) S.hash[k] = 0;
+  __syncwarp();
+  const int a0 = A.adj_ptr[r], a1 = A.adj_ptr[r + 1];
+  bool ok = true;
+  for (int c0 = a0; c0 < a1; c0 += kEnt) {
+    const int na = min(kEnt, a1 - c0);
+    const int nc = load_entries(A, S, c0, na);
+    for (int t = lane; t < nc * A.nd; t += 32) {
+      const int e = S.celem[t / A.nd], j = t % A.nd;
+      ok &= hash_insert(S.hash, A.hs, A.el_dofs[(int64_t)e * A.nd + j]);
+    }
+    __syncwarp();
+  }
+  return __all_sync(0xffffffffu, ok);
+}
+
+// Occupied hash slots -> S.ucols (unordered); returns the count.
+__device__ int hash_extract(const ScatterArgs& A, const RowSm& S, bool write) {
+  const int lane = threadIdx.x & 31;
+  int out = 0;
+  for (int base = 0; base < A.hs; base += 32) {
+    const int v = S.hash[base + lane];
+    const unsigned m = __ballot_sync(0xffffffffu, v != 0);
+    if (write && v != 0) {
+      const int k = out + __popc(m & ((1u << lane) - 1));
+      if (k < A.maxu) S.ucols[k] = v - 1;
+    }
+    out += __popc(m);
+  }
+  __syncwarp();
+  return out;
 }
 
 __device__ void warp_bitonic_sort(int* buf, int n) {
@@ -861,52 +949,6 @@ __device__ void warp_bitonic_sort(int* buf, int n) {
     }
 }
 
-// sort + unique in place; returns #unique
-__device__ int warp_sort_unique(int* buf, int n) {
-  const int lane = threadIdx.x & 31;
-  int m = 32;
-  while (m < n) m <<= 1;
-  for (int i = n + lane; i < m; i += 32) buf[i] = 0x7fffffff;
-  __syncwarp();
-  warp_bitonic_sort(buf, m);
-  // compact unique values to the front (stable, ascending)
-  int out = 0;
-  int last = 0;
-  for (int base = 0; base < n; base += 32) {
-    const int i = base + lane;
-    int v = i < n ? buf[i] : 0x7fffffff;
-    int pv = lane == 0 ? last : buf[i - 1];
-    bool keep = i < n && (i == 0 || pv != v);
-    last = __shfl_sync(0xffffffffu, v, 31);
-    unsigned mk = __ballot_sync(0xffffffffu, keep);
-    __syncwarp();
-    if (keep) buf[out + __popc(mk & ((1u << lane) - 1))] = v;
-    out += __popc(mk);
-    __syncwarp();
-  }
-  return out;
-}
-
-__global__ void __launch_bounds__(kScWarps * 32) k_rowcount(ScatterArgs A, int64_t* rowcnt, int* err) {
-  extern __shared__ int sm_sc[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  int* buf = sm_sc + warp * A.cap;
-  const int nrows = A.counts[3];
-  for (int row = blockIdx.x * kScWarps + warp; row < nrows; row += gridDim.x * kScWarps) {
-    const int r = A.rows[row];
-    int n = gather_candidates(A, r, buf);
-    __syncwarp();
-    if (n < 0) {
-      if (lane == 0) set_err(err, XG_ERR_CAPACITY);
-      n = 0;
-    }
-    int u = warp_sort_unique(buf, n);
-    if (u > A.capu && lane == 0) set_err(err, XG_ERR_CAPACITY);
-    if (lane == 0) rowcnt[row] = u;
-    __syncwarp();
-  }
-}
-
 __device__ __forceinline__ int lower_bound_sm(const int* a, int n, int v) {
   int lo = 0, hi = n;
   while (lo < hi) {
@@ -917,65 +959,114 @@ __device__ __forceinline__ int lower_bound_sm(const int* a, int n, int v) {
   return lo;
 }
 
-template <typename T>
-__global__ void __launch_bounds__(kScWarps * 32) k_rowfill(ScatterArgs A, const T* __restrict__ elmat,
-                                                           const T* __restrict__ famat,
-                                                           const int64_t* __restrict__ rowptr,
-                                                           int32_t* __restrict__ cols, double* __restrict__ vals,
-                                                           int64_t cap_nnz, int* err) {
-  extern __shared__ int sm_sc[];
+__global__ void __launch_bounds__(kRowWarps * 32) k_row_count(ScatterArgs A, int64_t* rowcnt, int* err) {
+  extern __shared__ __align__(16) unsigned char sm_rows[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  int* buf = sm_sc + warp * A.cap;
-  double* acc = (double*)(sm_sc + kScWarps * A.cap) + warp * A.capu;
+  const RowSm S = row_sm(A, sm_rows + (size_t)warp * A.wbytes);
+  const int nrows = A.counts[3];
+  for (int row = blockIdx.x * kRowWarps + warp; row < nrows; row += gridDim.x * kRowWarps) {
+    const bool ok = row_columns(A, S, A.rows[row]);
+    const int u = hash_extract(A, S, false);
+    if (lane == 0) {
+      if (!ok || u > A.maxu) set_err(err, XG_ERR_CAPACITY);
+      rowcnt[row] = u;
+    }
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kRowWarps * 32) k_row_fill(ScatterArgs A, const T* __restrict__ elmat,
+                                                             const T* __restrict__ famat,
+                                                             const int64_t* __restrict__ rowptr,
+                                                             int32_t* __restrict__ cols, double* __restrict__ vals,
+                                                             int64_t cap_nnz, int* err) {
+  extern __shared__ __align__(16) unsigned char sm_rows[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const RowSm S = row_sm(A, sm_rows + (size_t)warp * A.wbytes);
   const int nrows = A.counts[3];
   const int nd = A.nd, n2 = 2 * nd;
-  for (int row = blockIdx.x * kScWarps + warp; row < nrows; row += gridDim.x * kScWarps) {
+  const int gpb = A.stage / nd;  // groups per staged batch
+  for (int row = blockIdx.x * kRowWarps + warp; row < nrows; row += gridDim.x * kRowWarps) {
     const int r = A.rows[row];
-    int n = gather_candidates(A, r, buf);
-    __syncwarp();
-    if (n < 0) n = 0;
-    int u = warp_sort_unique(buf, n);
-    if (u > A.capu) u = A.capu;
+    const bool ok = row_columns(A, S, r);
+    const int u = hash_extract(A, S, true);
     const int64_t rp = rowptr[row];
-    if (rp + u > cap_nnz) {
+    if (!ok || u > A.maxu || rp + u > cap_nnz) {
       if (lane == 0) set_err(err, XG_ERR_CAPACITY);
       continue;
     }
-    for (int k = lane; k < u; k += 32) acc[k] = 0.0;
+    int m = 32;
+    while (m < u) m <<= 1;
+    for (int k = u + lane; k < m; k += 32) S.ucols[k] = 0x7fffffff;
+    for (int k = lane; k < u; k += 32) S.acc[k] = 0.0;
     __syncwarp();
+    warp_bitonic_sort(S.ucols, m);
     const int a0 = A.adj_ptr[r], a1 = A.adj_ptr[r + 1];
-    for (int a = a0; a < a1; a++) {
-      const int e = A.adj[a] >> 5, i = A.adj[a] & 31;
-      if (el_active(A, e)) {
-        const T* m = elmat + ((int64_t)A.el_slot[e] * nd + i) * nd;
-        if (lane < nd) {
-          int c = A.el_dofs[(int64_t)lane * A.ne + e];
-          int pos = lower_bound_sm(buf, u, c);
-          if (pos < u) acc[pos] += (double)m[lane];
+    for (int c0 = a0; c0 < a1; c0 += kEnt) {
+      const int na = min(kEnt, a1 - c0);
+      load_entries(A, S, c0, na);
+      // groups in the fixed order: per entry its element row, then its active facets (first, second half)
+      int ng = 0;
+      {
+        int cnt = 0;
+        if (lane < na) {
+          cnt = S.ent_e[lane] >= 0 ? 1 : 0;
+          for (int lf = 0; lf < A.nfl; lf++) cnt += S.ent_nb[lane * 4 + lf] >= 0 ? 2 : 0;
+        }
+        int x = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          int y = __shfl_up_sync(0xffffffffu, x, o);
+          if (lane >= o) x += y;
+        }
+        ng = __shfl_sync(0xffffffffu, x, 31);
+        if (lane < na) {
+          int k = x - cnt;
+          if (S.ent_e[lane] >= 0) S.grp[k++] = (lane << 4) | 0;
+          for (int lf = 0; lf < A.nfl; lf++)
+            if (S.ent_nb[lane * 4 + lf] >= 0) {
+              S.grp[k++] = (lane << 4) | (1 + 2 * lf);
+              S.grp[k++] = (lane << 4) | (2 + 2 * lf);
+            }
         }
         __syncwarp();
       }
-      for (int lf = 0; lf < A.nfl; lf++) {
-        const int f = A.el_facets[(int64_t)lf * A.ne + e];
-        if (!tbit32(A.act_fa, f)) continue;
-        const int e1 = A.fel[f], e2 = A.fel[A.nf + f];
-        const int prow = (e == e1) ? i : nd + i;
-        if (A.fa_slot[f] >= A.cap_fa) continue;
-        const T* m = famat + ((int64_t)A.fa_slot[f] * n2 + prow) * n2;
-        for (int half = 0; half < 2; half++) {
-          const int eh = half == 0 ? e1 : e2;
-          for (int j = lane; j < nd; j += 32) {
-            int c = A.el_dofs[(int64_t)j * A.ne + eh];
-            int pos = lower_bound_sm(buf, u, c);
-            if (pos < u) acc[pos] += (double)m[half * nd + j];
+      for (int g0 = 0; g0 < ng; g0 += gpb) {
+        const int gb = min(gpb, ng - g0);
+        for (int t = lane; t < gb * nd; t += 32) {
+          const int g = g0 + t / nd, j = t % nd;
+          const int a = S.grp[g] >> 4, kind = S.grp[g] & 15;
+          const int ee = S.ent_e[a];
+          const int e = ee >= 0 ? ee : ~ee, i = S.ent_i[a];
+          int colel;
+          double v;
+          if (kind == 0) {
+            colel = e;
+            v = (double)elmat[((int64_t)A.el_slot[e] * nd + i) * nd + j];
+          } else {
+            const int lf = (kind - 1) >> 1, h = (kind - 1) & 1;
+            const int first = S.ent_first[a * 4 + lf], nb = S.ent_nb[a * 4 + lf], fs = S.ent_fs[a * 4 + lf];
+            const int prow = first ? i : nd + i;
+            colel = (h == 0) == (first != 0) ? e : nb;
+            v = fs < A.cap_fa ? (double)famat[((int64_t)fs * n2 + prow) * n2 + h * nd + j] : 0.0;
+          }
+          const int c = A.el_dofs[(int64_t)colel * nd + j];
+          S.spos[t] = lower_bound_sm(S.ucols, u, c);
+          S.sval[t] = v;
+        }
+        __syncwarp();
+        for (int g = 0; g < gb; g++) {
+          if (lane < nd) {
+            const int pos = S.spos[g * nd + lane];
+            if (pos < u) S.acc[pos] += S.sval[g * nd + lane];
           }
           __syncwarp();
         }
       }
     }
     for (int k = lane; k < u; k += 32) {
-      cols[rp + k] = A.dof_row[buf[k]];
-      vals[rp + k] = acc[k];
+      cols[rp + k] = A.dof_row[S.ucols[k]];
+      vals[rp + k] = S.acc[k];
     }
     __syncwarp();
   }
@@ -1018,8 +1109,10 @@ struct xg_form {
   void* d_elmat = nullptr;
   void* d_famat = nullptr;
   int* d_err = nullptr;
-  int sc_cap = 0, sc_capu = 0;
+  int sc_hs = 0, sc_maxu = 0, sc_stage = 0, sc_wbytes = 0;
   size_t sc_smem = 0;
+  int64_t full_nnz = 0;
+  int max_unique = 0;
   int grid_el_un = 0, grid_el_cut = 0, grid_fa = 0, grid_sc = 0;
   // CutFEM step state
   uint8_t* d_dom = nullptr;
@@ -1201,10 +1294,9 @@ ScatterArgs scatter_args(xg_form* f) {
   A.ne = m->ne;
   A.nd = sp->nd;
   A.nfl = m->dim + 1;
-  A.nf = m->nfacets;
-  A.el_dofs = sp->d_el_dofs;
-  A.el_facets = m->d_el_facets;
-  A.fel = m->d_facet_els;
+  A.el_dofs = sp->d_el_dofs_aos;
+  A.el_facets = m->d_el_facets_aos;
+  A.fel = m->d_facet_els_aos;
   A.adj_ptr = sp->d_dof_adj_ptr;
   A.adj = sp->d_dof_adj;
   A.act_un = f->d_act_un;
@@ -1216,9 +1308,68 @@ ScatterArgs scatter_args(xg_form* f) {
   A.dof_row = f->d_dof_row;
   A.counts = f->d_counts;
   A.cap_fa = f->cap_fa;
-  A.cap = f->sc_cap;
-  A.capu = f->sc_capu;
+  A.hs = f->sc_hs;
+  A.maxu = f->sc_maxu;
+  A.stage = f->sc_stage;
+  A.wbytes = f->sc_wbytes;
   return A;
+}
+
+// Exact size of the largest pattern any level set can produce on this mesh
+// (every element and interior facet active) and its widest row.
+void full_pattern_stats(const xg_form* f, int64_t* nnz, int* max_unique) {
+  const xg_space* sp = f->space;
+  const xg_mesh* m = f->mesh;
+  const int nd = sp->nd, nfl = m->dim + 1, ne = m->ne;
+  const int64_t ndof = sp->ndof;
+  const std::vector<int32_t>& ed = sp->h_el_dofs;
+  const std::vector<int32_t>& efa = m->dim == 2 ? m->h_el_edges : m->h_el_faces;
+  const int efs = m->dim == 2 ? 3 : 4;
+  std::vector<int32_t> ptr(ndof + 1, 0), adj(ed.size());
+  for (size_t k = 0; k < ed.size(); k++) ptr[ed[k] + 1]++;
+  for (int64_t r = 0; r < ndof; r++) ptr[r + 1] += ptr[r];
+  {
+    std::vector<int32_t> fill(ptr.begin(), ptr.end() - 1);
+    for (int e = 0; e < ne; e++)
+      for (int k = 0; k < nd; k++) adj[fill[ed[(size_t)e * nd + k]]++] = e;
+  }
+  const int nth = std::max(1, std::min(16, (int)std::thread::hardware_concurrency()));
+  std::vector<int64_t> part(nth, 0);
+  std::vector<int> pmax(nth, 0);
+  std::vector<std::thread> th;
+  for (int t = 0; t < nth; t++)
+    th.emplace_back([&, t]() {
+      std::vector<int32_t> c;
+      int64_t sum = 0;
+      int mx = 0;
+      for (int64_t r = t; r < ndof; r += nth) {
+        c.clear();
+        for (int a = ptr[r]; a < ptr[r + 1]; a++) {
+          int e = adj[a];
+          c.insert(c.end(), ed.begin() + (size_t)e * nd, ed.begin() + (size_t)(e + 1) * nd);
+          if (f->has_patch)
+            for (int lf = 0; lf < nfl; lf++) {
+              int fc = efa[(size_t)e * efs + lf];
+              int e2 = m->h_facet_els[2 * (size_t)fc] == e ? m->h_facet_els[2 * (size_t)fc + 1]
+                                                            : m->h_facet_els[2 * (size_t)fc];
+              if (e2 >= 0) c.insert(c.end(), ed.begin() + (size_t)e2 * nd, ed.begin() + (size_t)(e2 + 1) * nd);
+            }
+        }
+        std::sort(c.begin(), c.end());
+        int u = (int)(std::unique(c.begin(), c.end()) - c.begin());
+        sum += u;
+        mx = std::max(mx, u);
+      }
+      part[t] = sum;
+      pmax[t] = mx;
+    });
+  for (auto& x : th) x.join();
+  *nnz = 0;
+  *max_unique = 0;
+  for (int t = 0; t < nth; t++) {
+    *nnz += part[t];
+    *max_unique = std::max(*max_unique, pmax[t]);
+  }
 }
 
 }  // namespace
@@ -1255,14 +1406,17 @@ int xg_form_create(xg_space* space, const xg_term* terms, int32_t nterms, int pr
   int64_t maxw = std::max(f->nw32_el, std::max(f->nw32_fa, f->nw32_dof));
   f->nbsum = (int)((maxw + kCChunk - 1) / kCChunk) + 1;
   f->nbsum64 = (int)((space->ndof + kSChunk - 1) / kSChunk) + 1;
-  // scatter buffers
-  const int nfl = m->dim + 1;
-  int maxc = space->max_adj * (nd + (f->has_patch ? nfl * 2 * nd : 0));
-  int cap = 32;
-  while (cap < maxc) cap <<= 1;
-  f->sc_cap = cap;
-  f->sc_capu = std::min(cap, 2048);
-  f->sc_smem = (size_t)kScWarps * (cap * sizeof(int) + f->sc_capu * sizeof(double));
+  // scatter buffers sized by the widest row of the full pattern
+  full_pattern_stats(f, &f->full_nnz, &f->max_unique);
+  {
+    int maxu = 32;
+    while (maxu < f->max_unique) maxu <<= 1;
+    f->sc_maxu = maxu;
+    f->sc_hs = 2 * maxu;
+    f->sc_stage = nd * std::max(1, 192 / nd);
+    f->sc_wbytes = (row_smem_bytes(f->sc_hs, f->sc_maxu, f->sc_stage) + 15) & ~15;
+    f->sc_smem = (size_t)kRowWarps * f->sc_wbytes;
+  }
   auto A = [&](void** p, size_t bytes) { return cudaMalloc(p, bytes ? bytes : 16); };
   cudaError_t e = cudaSuccess;
   e = e ? e : A((void**)&f->d_act_un, f->nw32_el * 4);
@@ -1298,9 +1452,9 @@ int xg_form_create(xg_space* space, const xg_term* terms, int32_t nterms, int pr
     static size_t raised = 48 * 1024;
     std::lock_guard<std::mutex> lock(mu);
     if (f->sc_smem > raised) {
-      if (cudaFuncSetAttribute(k_rowcount, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->sc_smem) ||
-          cudaFuncSetAttribute(k_rowfill<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->sc_smem) ||
-          cudaFuncSetAttribute(k_rowfill<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->sc_smem)) {
+      if (cudaFuncSetAttribute(k_row_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->sc_smem) ||
+          cudaFuncSetAttribute(k_row_fill<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->sc_smem) ||
+          cudaFuncSetAttribute(k_row_fill<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->sc_smem)) {
         form_free(f);
         set_last_error("xg_form_create: scatter shared memory too large for this mesh");
         return XG_ERR_CAPACITY;
@@ -1308,7 +1462,7 @@ int xg_form_create(xg_space* space, const xg_term* terms, int32_t nterms, int pr
       raised = f->sc_smem;
     }
   }
-  f->grid_sc = grid_for(k_rowcount, kScWarps * 32, f->sc_smem);
+  f->grid_sc = grid_for(k_row_count, kRowWarps * 32, f->sc_smem);
   *out = f;
   return XG_OK;
 }
@@ -1326,52 +1480,10 @@ int xg_form_set_defined_on(xg_form* f, int32_t t, const uint64_t* d_defined_on) 
 
 int xg_form_capacity(const xg_form* f, int64_t* o) {
   if (!f || !o) return XG_ERR_ARG;
-  // exact pattern size when every element and every interior facet is active
-  // (the largest pattern any level set can produce on this mesh)
-  const xg_space* sp = f->space;
-  const xg_mesh* m = f->mesh;
-  const int nd = sp->nd, nfl = m->dim + 1, ne = m->ne;
-  const int64_t ndof = sp->ndof;
-  const std::vector<int32_t>& ed = sp->h_el_dofs;
-  const std::vector<int32_t>& efa = m->dim == 2 ? m->h_el_edges : m->h_el_faces;
-  const int efs = m->dim == 2 ? 3 : 4;
-  std::vector<int32_t> ptr(ndof + 1, 0), adj(ed.size());
-  for (size_t k = 0; k < ed.size(); k++) ptr[ed[k] + 1]++;
-  for (int64_t r = 0; r < ndof; r++) ptr[r + 1] += ptr[r];
-  {
-    std::vector<int32_t> fill(ptr.begin(), ptr.end() - 1);
-    for (int e = 0; e < ne; e++)
-      for (int k = 0; k < nd; k++) adj[fill[ed[(size_t)e * nd + k]]++] = e;
-  }
-  const int nth = std::max(1, std::min(16, (int)std::thread::hardware_concurrency()));
-  std::vector<int64_t> part(nth, 0);
-  std::vector<std::thread> th;
-  for (int t = 0; t < nth; t++)
-    th.emplace_back([&, t]() {
-      std::vector<int32_t> c;
-      int64_t sum = 0;
-      for (int64_t r = t; r < ndof; r += nth) {
-        c.clear();
-        for (int a = ptr[r]; a < ptr[r + 1]; a++) {
-          int e = adj[a];
-          c.insert(c.end(), ed.begin() + (size_t)e * nd, ed.begin() + (size_t)(e + 1) * nd);
-          if (f->has_patch)
-            for (int lf = 0; lf < nfl; lf++) {
-              int fc = efa[(size_t)e * efs + lf];
-              int e2 = m->h_facet_els[2 * (size_t)fc] == e ? m->h_facet_els[2 * (size_t)fc + 1] : m->h_facet_els[2 * (size_t)fc];
-              if (e2 >= 0) c.insert(c.end(), ed.begin() + (size_t)e2 * nd, ed.begin() + (size_t)(e2 + 1) * nd);
-            }
-        }
-        std::sort(c.begin(), c.end());
-        sum += std::unique(c.begin(), c.end()) - c.begin();
-      }
-      part[t] = sum;
-    });
-  for (auto& x : th) x.join();
-  int64_t nnz = 0;
-  for (auto v : part) nnz += v;
-  o[0] = ndof;
-  o[1] = nnz;
+  // the largest pattern any level set can produce on this mesh (every element
+  // and every interior facet active), computed at creation
+  o[0] = f->space->ndof;
+  o[1] = f->full_nnz;
   return XG_OK;
 }
 
@@ -1428,7 +1540,7 @@ int xg_form_assemble(xg_form* f, const double* d_lset, const uint8_t* d_dom, xg_
   // 4. pattern and values
   ScatterArgs A = scatter_args(f);
   A.rows = out->d_row_dof;
-  k_rowcount<<<f->grid_sc, kScWarps * 32, f->sc_smem, s>>>(A, f->d_rowcnt, f->d_err);
+  k_row_count<<<f->grid_sc, kRowWarps * 32, f->sc_smem, s>>>(A, f->d_rowcnt, f->d_err);
   const int nb64 = (int)((sp->ndof + kSChunk - 1) / kSChunk);
   k_sum64_blocks<<<nb64, kSThreads, 0, s>>>(f->d_rowcnt, f->d_counts + 3, f->d_bsum64);
   k_scan64_small<<<1, 1024, 0, s>>>(f->d_bsum64, nb64);
@@ -1436,11 +1548,11 @@ int xg_form_assemble(xg_form* f, const double* d_lset, const uint8_t* d_dom, xg_
                                             out->cap_nnz, f->d_err);
   if (f->use_ev) cudaEventRecord(f->ev[6], s);
   if (f->precision == XG_PREC_FP64)
-    k_rowfill<double><<<f->grid_sc, kScWarps * 32, f->sc_smem, s>>>(A, (const double*)f->d_elmat,
+    k_row_fill<double><<<f->grid_sc, kRowWarps * 32, f->sc_smem, s>>>(A, (const double*)f->d_elmat,
                                                                     (const double*)f->d_famat, out->d_rowptr,
                                                                     out->d_cols, out->d_vals, out->cap_nnz, f->d_err);
   else
-    k_rowfill<float><<<f->grid_sc, kScWarps * 32, f->sc_smem, s>>>(A, (const float*)f->d_elmat,
+    k_row_fill<float><<<f->grid_sc, kRowWarps * 32, f->sc_smem, s>>>(A, (const float*)f->d_elmat,
                                                                    (const float*)f->d_famat, out->d_rowptr,
                                                                    out->d_cols, out->d_vals, out->cap_nnz, f->d_err);
   if (f->use_ev) cudaEventRecord(f->ev[7], s);

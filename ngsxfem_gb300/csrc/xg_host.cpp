@@ -318,6 +318,23 @@ int xg_mesh_create(int dim, int32_t nv, const double* h_coords, int32_t ne, cons
     xg_mesh_destroy(m);
     return st;
   }
+  {
+    std::vector<int32_t> efa((size_t)ne * nvl);
+    const std::vector<int32_t>& src = dim == 2 ? m->h_el_edges : m->h_el_faces;
+    const int stride = dim == 2 ? 3 : 4;
+    for (int e = 0; e < ne; e++)
+      for (int j = 0; j < nvl; j++) efa[(size_t)e * nvl + j] = src[(size_t)e * stride + j];
+    st = upload(&m->d_el_facets_aos, efa);
+    if (!st) {
+      XG_CUDA(cudaMalloc((void**)&m->d_facet_els_aos, sizeof(int2) * (size_t)m->nfacets));
+      XG_CUDA(cudaMemcpy(m->d_facet_els_aos, m->h_facet_els.data(), sizeof(int2) * (size_t)m->nfacets,
+                         cudaMemcpyHostToDevice));
+    }
+  }
+  if (st) {
+    xg_mesh_destroy(m);
+    return st;
+  }
   m->d_el_facets = dim == 2 ? m->d_el_edges : m->d_el_faces;
   if (cudaMalloc((void**)&m->d_err, sizeof(int)) != cudaSuccess || cudaMemset(m->d_err, 0, sizeof(int)) != cudaSuccess) {
     xg_mesh_destroy(m);
@@ -339,6 +356,8 @@ int xg_mesh_destroy(xg_mesh* m) {
   cudaFree(m->d_el_edges);
   cudaFree(m->d_el_faces);
   cudaFree(m->d_facet_els);
+  cudaFree(m->d_el_facets_aos);
+  cudaFree(m->d_facet_els_aos);
   cudaFree(m->d_err);
   cudaFree(m->d_scratch);
   delete m;
@@ -404,7 +423,8 @@ int xg_space_create(xg_mesh* m, int order, xg_space** out) {
   for (int e = 0; e < ne; e++)
     for (int i = 0; i < nd; i++) adj[fill[s->h_el_dofs[(size_t)e * nd + i]]++] = e * 32 + i;
   int st;
-  if ((st = upload(&s->d_el_dofs, to_soa(s->h_el_dofs, ne, nd))) || (st = upload(&s->d_dof_adj_ptr, ptr)) ||
+  if ((st = upload(&s->d_el_dofs, to_soa(s->h_el_dofs, ne, nd))) || (st = upload(&s->d_el_dofs_aos, s->h_el_dofs)) ||
+      (st = upload(&s->d_dof_adj_ptr, ptr)) ||
       (st = upload(&s->d_dof_adj, adj))) {
     xg_space_destroy(s);
     return st;
@@ -416,6 +436,7 @@ int xg_space_create(xg_mesh* m, int order, xg_space** out) {
 int xg_space_destroy(xg_space* s) {
   if (!s) return XG_OK;
   cudaFree(s->d_el_dofs);
+  cudaFree(s->d_el_dofs_aos);
   cudaFree(s->d_dof_adj_ptr);
   cudaFree(s->d_dof_adj);
   delete s;

@@ -91,6 +91,8 @@ struct xg_mesh {
   int32_t* d_el_faces = nullptr; // [4][ne] (3D)
   int32_t* d_el_facets = nullptr;// [dim+1][ne] (alias of edges / faces)
   int32_t* d_facet_els = nullptr;// [2][nfacets]
+  int32_t* d_el_facets_aos = nullptr;  // [ne][dim+1] element-major
+  int2* d_facet_els_aos = nullptr;     // [nfacets] (first, second element; -1 boundary)
   int* d_err = nullptr;
   // host
   std::vector<int32_t> h_elv;       // ne*(dim+1)
@@ -107,6 +109,7 @@ struct xg_space {
   int order = 1, nd = 0;
   int64_t ndof = 0;
   int32_t* d_el_dofs = nullptr;     // [nd][ne]
+  int32_t* d_el_dofs_aos = nullptr; // [ne][nd] element-major (scatter gathers)
   int32_t* d_dof_adj_ptr = nullptr; // [ndof+1]
   int32_t* d_dof_adj = nullptr;     // element*32 + local index, elements ascending
   int max_adj = 0;

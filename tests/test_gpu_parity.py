@@ -110,7 +110,8 @@ def test_integrate_parity(xg, orc, case, dt):
         ref = sp.integrate(l, dt, 4, *e)
         got = xg.Integrate(levelset_domain={"levelset": gf, "domain_type": dt, "order": 4},
                            cf=xg._Monomial(e), mesh=m)
-        assert abs(got - ref) <= 1e-13 * max(1.0, abs(ref))
+        # summation orders differ (fixed tree on the GPU, sequential on the CPU)
+        assert abs(got - ref) <= 1e-12 * max(1.0, abs(ref))
 
 
 def test_planar_known_answers_gpu(xg):
@@ -282,9 +283,10 @@ def test_no_active_elements(xg, orc):
 def test_exact_zero_vertex_is_an_error(xg):
     """A vertex value exactly 0 next to a negative vertex: the reference throws
     (straightcutrule.cpp:43-48); libxg reports XG_ERR_PLAIN_CUT."""
-    m = MakeStructured2DMesh(2, 2)
+    m = MakeStructured2DMesh(1, 1)
     gf = xg.GridFunction(xg.H1(m, 1))
-    vals = m.coords[:, 0] - 0.5  # vertices at x=0.5 are exactly zero
+    # vertices p00, p10, p01, p11; triangle (p00, p10, p11) gets (0, -1, 1)
+    vals = np.array([0.0, -1.0, 1.0, 1.0])
     gf.vec[: m.nv] = torch.from_numpy(vals)
     ci = xg.CutInfo(m, gf)
     with pytest.raises(xg._lib.XgError) as ei:
