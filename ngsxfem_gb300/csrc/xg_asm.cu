@@ -275,11 +275,17 @@ __global__ void k_mark_dofs(int ne, int nd, const int32_t* __restrict__ el_dofs,
 }
 
 // ============================================================================
-// Element matrices.  Thread (element, row i); EPB elements per block.
-// Phase 1 (thread per element): geometry, orientation, coefficients and the
-// sub-simplex decompositions.  Then per term group and chunk of quadrature
-// points: point generation, basis evaluation (thread per function) and the
-// contraction elmat[i][j] += w * (terms) (thread per row).
+// Element matrices.
+//
+// FP64 is the narrow pipe of GB300, so the kernels minimise FP64 work:
+//  * uncut elements (standard rule on an affine simplex): the rule's sums are
+//    pre-contracted on the host into reference tables per term group
+//    (mass, gradient pairs, convection), the kernel combines them with
+//    G = F^-1 F^-T, |det F| and the coefficients -- the same rule, reassociated;
+//  * cut elements: sub-simplex quadrature (StraightCutIntegrationRule) with the
+//    contraction over matrix entries, only the upper triangle for symmetric
+//    forms;
+//  * matrices of symmetric forms are stored as packed upper triangles.
 // ============================================================================
 // FP64 accumulation for the plain path; FP32 with Kahan compensation per
 // entry for the mixed path.
@@ -305,66 +311,232 @@ struct Acc<float> {
   __device__ __forceinline__ float get() const { return s; }
 };
 
-template <int D, int K, bool CUT, typename T>
-struct ElCfg {
-  static constexpr int N = ndof_el(D, K);
-  static constexpr int EPB0 = N <= 4 ? 32 : (N <= 10 ? 16 : 8);
-  static constexpr int EPB = CUT ? (EPB0 > 8 ? EPB0 / 2 : EPB0) : EPB0;
-  static constexpr int CH = (N <= 4 ? 4 : (N <= 10 ? (sizeof(T) == 8 ? 4 : 8) : 4));
-  static constexpr int NT = N * EPB;
-  static constexpr int ND = D + 2;
+__host__ __device__ constexpr int tri_size(int n) { return n * (n + 1) / 2; }
+__host__ __device__ inline int tri_index(int p, int q, int n) { return p * n - p * (p - 1) / 2 + (q - p); }
+
+// entry k -> (p, q) tables in shared memory
+__device__ __forceinline__ void entry_tables(int n, bool sym, unsigned char* ep, unsigned char* eq) {
+  const int E = sym ? tri_size(n) : n * n;
+  for (int k = threadIdx.x; k < E; k += blockDim.x) {
+    int p, q;
+    if (sym) {
+      p = 0;
+      int rem = k;
+      while (rem >= n - p) {
+        rem -= n - p;
+        p++;
+      }
+      q = p + rem;
+    } else {
+      p = k / n;
+      q = k % n;
+    }
+    ep[k] = (unsigned char)p;
+    eq[k] = (unsigned char)q;
+  }
+}
+
+// Per-group reference tables of the uncut kernel (device pointers, NULL = kind unused).
+struct UncutTabs {
+  const double* m[kMaxGroups];  // [E]
+  const double* t[kMaxGroups];  // [D(D+1)/2][E] gradient-pair tables, (a<=b) row-major
+  const double* c[kMaxGroups];  // [D][E] convection tables (full storage only)
 };
 
-struct ElGeoS {
-  double g[4][3];  // physical gradients of the barycentric coordinates
-  double nrm[3];   // unit normal of the P1 level set (physical)
-  double meas;     // |det F|
-  double iffac;    // |F^-T n_ref|
-  double l[4];
-  int gv[4];
-  int elem;
-  int slot;
-  int dom;
-  int ns[3];       // #sub-simplices for NEG, POS, IF (cut elements)
+// physical-gradient Gram matrix of the barycentric coordinates, G = F^-1 F^-T (a<=b)
+// and per group beta = F^-1 b; per element in shared memory
+template <int D>
+struct UnGeoS {
+  double G[D * (D + 1) / 2];
+  double beta[kMaxGroups][D];
   double coef[kMaxGroups][5];
+  double meas;
+  int gv[D + 1];
+  int elem, slot, dom;
 };
-struct ElSubS {
-  Sub sub[3][3];
-  double vol[3][3];
+
+template <int D, int K, bool SYM, typename T>
+struct UnCfg {
+  static constexpr int N = ndof_el(D, K);
+  static constexpr int E = SYM ? tri_size(N) : N * N;
+  static constexpr int EPB = 32;
+  static constexpr int NT = 256;
 };
 
-template <int D, int K, bool CUT, typename T>
-__global__ void __launch_bounds__(ElCfg<D, K, CUT, T>::NT) k_elmat(
-    int ne, int nv, const int32_t* __restrict__ elv, const double* __restrict__ xyz, const double* __restrict__ lset,
-    const uint8_t* __restrict__ dom, FormDesc form, const int32_t* __restrict__ list, const int* __restrict__ counts,
-    int which, T* __restrict__ elmat, int* err, int needs_mask) {
-  using C = ElCfg<D, K, CUT, T>;
-  constexpr int N = C::N, EPB = C::EPB, CH = C::CH, ND = C::ND;
-  __shared__ ElGeoS geo[EPB];
-  __shared__ ElSubS subs[CUT ? EPB : 1];
-  __shared__ double pts[EPB][CH][4];
-  __shared__ T B[EPB][CH][N][ND];  // phi, grad (D), e
-  __shared__ int npts_s[EPB];
-  __shared__ int maxpts_s;
-  static_assert(sizeof(geo) + sizeof(subs) + sizeof(pts) + sizeof(B) < 48 * 1024, "k_elmat shared memory");
+// Sign of local function i relative to the canonical orientation of the tables
+// (cubic edge functions flip when the edge's global orientation differs).
+template <int D, int K>
+__device__ __forceinline__ int fn_sign(int i, const int* gv) {
+  if (K < 3 || i <= D) return 1;
+  int r = i - (D + 1);
+  const int nedge = D == 2 ? 3 : 6;
+  if (r >= nedge * 2) return 1;
+  if ((r & 1) == 0) return 1;
+  int a, b;
+  local_edge(D, r >> 1, a, b);
+  return gv[a] < gv[b] ? 1 : -1;
+}
 
-  const int count = counts[which];
-  const int slot_base = which == 0 ? 0 : counts[0];
-  const int le = threadIdx.x / N, i = threadIdx.x % N;
-
+template <int D, int K, bool SYM, typename T>
+__global__ void __launch_bounds__(256) k_elmat_uncut(int ne, int nv, const int32_t* __restrict__ elv,
+                                                     const double* __restrict__ xyz,
+                                                     const uint8_t* __restrict__ dom, FormDesc form, UncutTabs tabs,
+                                                     const int32_t* __restrict__ list,
+                                                     const int* __restrict__ counts, T* __restrict__ elmat, int* err) {
+  using C = UnCfg<D, K, SYM, T>;
+  constexpr int N = C::N, E = C::E, EPB = C::EPB, NG = D * (D + 1) / 2;
+  __shared__ UnGeoS<D> geo[EPB];
+  __shared__ unsigned char ep[E], eq[E];
+  entry_tables(N, SYM, ep, eq);
+  const int count = counts[0];
   for (int batch = blockIdx.x; batch * EPB < count; batch += gridDim.x) {
-    // ---------------- phase 1: per-element data ----------------
+    __syncthreads();
     if (threadIdx.x < EPB) {
-      ElGeoS& G = geo[threadIdx.x];
+      UnGeoS<D>& G = geo[threadIdx.x];
       const int idx = batch * EPB + threadIdx.x;
       G.elem = idx < count ? list[idx] : -1;
-      G.slot = slot_base + idx;
+      G.slot = idx;
       if (G.elem >= 0) {
         const int e = G.elem;
         double xv[D + 1][3];
 #pragma unroll
         for (int v = 0; v <= D; v++) {
-          int vid = elv[(int64_t)v * ne + e];
+          const int vid = elv[(int64_t)v * ne + e];
+          G.gv[v] = vid;
+#pragma unroll
+          for (int c = 0; c < 3; c++) xv[v][c] = c < D ? xyz[(int64_t)c * nv + vid] : 0.0;
+        }
+        Geo<D> g;
+        make_geo<D>(xv, g);
+        G.meas = fabs(g.det);
+        int k = 0;
+#pragma unroll
+        for (int a = 0; a < D; a++)
+#pragma unroll
+          for (int b = a; b < D; b++) {
+            double s = 0;
+#pragma unroll
+            for (int c = 0; c < D; c++) s += g.Finv[a][c] * g.Finv[b][c];
+            G.G[k++] = s;
+          }
+        G.dom = dom[e];
+        double h = -1.0;
+        for (int q = 0; q < form.ngroups; q++) {
+          for (int kk = 0; kk < 5; kk++) {
+            const int hp = form.g[q].hpow[kk];
+            if (hp != 0 && h < 0) h = pow(G.meas, 1.0 / D);
+            G.coef[q][kk] = hp == 0 ? form.g[q].c[kk] : form.g[q].c[kk] * pow(h, (double)hp);
+          }
+          if (form.g[q].used & (1 << XG_TERM_CONV))
+#pragma unroll
+            for (int a = 0; a < D; a++) {
+              double s = 0;
+#pragma unroll
+              for (int c = 0; c < D; c++) s += g.Finv[a][c] * form.g[q].b[c];
+              G.beta[q][a] = s;
+            }
+        }
+      }
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < EPB * E; t += blockDim.x) {
+      const int le = t / E, k = t % E;
+      const UnGeoS<D>& G = geo[le];
+      if (G.elem < 0) continue;
+      double v = 0.0;
+      for (int q = 0; q < form.ngroups; q++) {
+        const GroupDesc& Gq = form.g[q];
+        if (Gq.domain != G.dom || (Gq.defined_on && !tbit(Gq.defined_on, G.elem))) continue;
+        if (Gq.used & (1 << XG_TERM_MASS)) v += G.coef[q][0] * __ldg(&tabs.m[q][k]);
+        if (Gq.used & (1 << XG_TERM_LAPLACE)) {
+          double s = 0;
+#pragma unroll
+          for (int a = 0; a < NG; a++) s += G.G[a] * __ldg(&tabs.t[q][a * E + k]);
+          v += G.coef[q][1] * s;
+        }
+        if (Gq.used & (1 << XG_TERM_CONV)) {
+          double s = 0;
+#pragma unroll
+          for (int a = 0; a < D; a++) s += G.beta[q][a] * __ldg(&tabs.c[q][a * E + k]);
+          v += G.coef[q][4] * s;
+        }
+      }
+      v *= G.meas;
+      if (K == 3) v *= (double)(fn_sign<D, K>(ep[k], G.gv) * fn_sign<D, K>(eq[k], G.gv));
+      if (!isfinite(v)) set_err(err, XG_ERR_NONFINITE);
+      elmat[(int64_t)G.slot * E + k] = (T)v;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Cut elements: sub-simplex quadrature.  Per chunk of points: point
+// generation (FP64), features per function (thread per function), then the
+// contraction over matrix entries flattened over the block.
+// ---------------------------------------------------------------------------
+template <int D, int K, bool SYM, typename T>
+struct CutCfg {
+  static constexpr int N = ndof_el(D, K);
+  static constexpr int E = SYM ? tri_size(N) : N * N;
+  static constexpr int EPB = N <= 4 ? 16 : (N <= 10 ? 8 : 4);
+  static constexpr int CH = 4;
+  static constexpr int NT = N * EPB;
+  static constexpr int NACC = (EPB * E + NT - 1) / NT;
+  static constexpr int NF = D + 3;  // phi, grad (D), n.grad, b.grad
+};
+
+struct CutGeoS {
+  double g[4][3];
+  double nrm[3];
+  double meas;
+  double iffac;
+  double l[4];
+  int gv[4];
+  int elem, slot;
+  int ns[3];
+  double coef[kMaxGroups][5];
+};
+struct CutSubS {
+  Sub sub[3][3];
+  double vol[3][3];
+};
+
+template <int D, int K, bool SYM, typename T>
+__global__ void __launch_bounds__(CutCfg<D, K, SYM, T>::NT) k_elmat_cut(
+    int ne, int nv, const int32_t* __restrict__ elv, const double* __restrict__ xyz, const double* __restrict__ lset,
+    FormDesc form, const int32_t* __restrict__ list, const int* __restrict__ counts, T* __restrict__ elmat, int* err,
+    int needs_mask) {
+  using C = CutCfg<D, K, SYM, T>;
+  constexpr int N = C::N, E = C::E, EPB = C::EPB, CH = C::CH, NT = C::NT, NACC = C::NACC, NF = C::NF;
+  __shared__ CutGeoS geo[EPB];
+  __shared__ CutSubS subs[EPB];
+  __shared__ double pts[EPB][CH][4];
+  __shared__ T tr[EPB][CH][N][NF];  // trial features: phi, grad, n.grad, b.grad
+  __shared__ T te[EPB][CH][N][NF];  // test features scaled by w and the coefficients
+  __shared__ unsigned char ep[E], eq[E];
+  __shared__ int npts_s[EPB];
+  __shared__ int maxpts_s;
+  static_assert(sizeof(geo) + sizeof(subs) + sizeof(pts) + sizeof(tr) + sizeof(te) < 48 * 1024,
+                "k_elmat_cut shared memory");
+  entry_tables(N, SYM, ep, eq);
+  const int count = counts[1];
+  const int slot_base = counts[0];
+  const int le = threadIdx.x / N, i = threadIdx.x % N;
+
+  for (int batch = blockIdx.x; batch * EPB < count; batch += gridDim.x) {
+    __syncthreads();
+    if (threadIdx.x < EPB) {
+      CutGeoS& G = geo[threadIdx.x];
+      const int idx = batch * EPB + threadIdx.x;
+      G.elem = idx < count ? list[idx] : -1;
+      G.slot = slot_base + idx;
+      G.ns[0] = G.ns[1] = G.ns[2] = 0;
+      if (G.elem >= 0) {
+        const int e = G.elem;
+        double xv[D + 1][3];
+#pragma unroll
+        for (int v = 0; v <= D; v++) {
+          const int vid = elv[(int64_t)v * ne + e];
           G.gv[v] = vid;
           G.l[v] = lset[vid];
 #pragma unroll
@@ -383,7 +555,6 @@ __global__ void __launch_bounds__(ElCfg<D, K, CUT, T>::NT) k_elmat(
           }
 #pragma unroll
         for (int k = 0; k < 3; k++) G.g[D][k] = -gs[k];
-        // Normalize(grad(lsetp1)) in physical coordinates
         double gl[3] = {0, 0, 0};
 #pragma unroll
         for (int k = 0; k < D; k++) {
@@ -392,62 +563,53 @@ __global__ void __launch_bounds__(ElCfg<D, K, CUT, T>::NT) k_elmat(
           for (int a = 0; a < D; a++) s += g.Finv[a][k] * (G.l[a] - G.l[D]);
           gl[k] = s;
         }
-        double nn = l2norm3(gl[0], gl[1], gl[2]);
+        const double nn = l2norm3(gl[0], gl[1], gl[2]);
 #pragma unroll
         for (int k = 0; k < 3; k++) G.nrm[k] = gl[k] / nn;
-        const double h = pow(G.meas, 1.0 / D);
+        double h = -1.0;
         for (int q = 0; q < form.ngroups; q++)
           for (int k = 0; k < 5; k++) {
-            double c = form.g[q].c[k];
-            int hp = form.g[q].hpow[k];
-            G.coef[q][k] = hp == 0 ? c : c * pow(h, (double)hp);
+            const int hp = form.g[q].hpow[k];
+            if (hp != 0 && h < 0) h = pow(G.meas, 1.0 / D);
+            G.coef[q][k] = hp == 0 ? form.g[q].c[k] : form.g[q].c[k] * pow(h, (double)hp);
           }
-        G.dom = dom[e];
-        G.iffac = 0.0;
-        G.ns[0] = G.ns[1] = G.ns[2] = 0;
-        if (CUT) {
-          ElSubS& SS = subs[CUT ? threadIdx.x : 0];
-          for (int dt = 0; dt < 3; dt++) {
-            if (!((needs_mask >> dt) & 1)) continue;
-            int ns = decompose<D>(G.l, dt, SS.sub[dt]);
-            if (ns < 0) {
-              set_err(err, -ns);
-              ns = 0;
-            }
-            G.ns[dt] = ns;
-            const int sd = dt == XG_IF ? D - 1 : D;
-            for (int s = 0; s < ns; s++) SS.vol[dt][s] = simplex_volume(SS.sub[dt][s].p, sd + 1);
+        CutSubS& SS = subs[threadIdx.x];
+        for (int dt = 0; dt < 3; dt++) {
+          if (!((needs_mask >> dt) & 1)) continue;
+          int ns = decompose<D>(G.l, dt, SS.sub[dt]);
+          if (ns < 0) {
+            set_err(err, -ns);
+            ns = 0;
           }
-          if ((needs_mask >> XG_IF) & 1) G.iffac = if_factor<D>(g, G.l);
+          G.ns[dt] = ns;
+          const int sd = dt == XG_IF ? D - 1 : D;
+          for (int s = 0; s < ns; s++) SS.vol[dt][s] = simplex_volume(SS.sub[dt][s].p, sd + 1);
         }
+        G.iffac = ((needs_mask >> XG_IF) & 1) ? if_factor<D>(g, G.l) : 0.0;
       }
     }
     __syncthreads();
 
-    const ElGeoS& G = geo[le];
+    const CutGeoS& G = geo[le];
     const int desc = G.elem >= 0 ? fn_desc<D, K>(i, G.gv) : 0;
     T gT[D + 1][D];
 #pragma unroll
     for (int a = 0; a <= D; a++)
 #pragma unroll
       for (int k = 0; k < D; k++) gT[a][k] = (T)G.g[a][k];
-    Acc<T> acc[N];
+    Acc<T> acc[NACC];
 #pragma unroll
-    for (int j = 0; j < N; j++) acc[j].init();
+    for (int m = 0; m < NACC; m++) acc[m].init();
 
     for (int q = 0; q < form.ngroups; q++) {
       const GroupDesc& Gq = form.g[q];
       const int p = clamp_order(Gq.order);
       const int dt = Gq.domain;
       const int sd = dt == XG_IF ? D - 1 : D;
-      const int nqb = CUT ? c_rules.cnt[sd][p] : c_rules.cnt[D][p];
-      const int offb = CUT ? c_rules.off[sd][p] : c_rules.off[D][p];
+      const int nqb = c_rules.cnt[sd][p], offb = c_rules.off[sd][p];
       if (i == 0) {
         int np = 0;
-        if (G.elem >= 0 && (!Gq.defined_on || tbit(Gq.defined_on, G.elem))) {
-          if (CUT) np = G.ns[dt] * nqb;
-          else if (G.dom == dt) np = nqb;
-        }
+        if (G.elem >= 0 && (!Gq.defined_on || tbit(Gq.defined_on, G.elem))) np = G.ns[dt] * nqb;
         npts_s[le] = np;
       }
       __syncthreads();
@@ -462,35 +624,26 @@ __global__ void __launch_bounds__(ElCfg<D, K, CUT, T>::NT) k_elmat(
       const T cM = (T)G.coef[q][0], cL = (T)G.coef[q][1], cN1 = (T)G.coef[q][2], cN2 = (T)G.coef[q][3],
               cC = (T)G.coef[q][4];
       const int used = Gq.used;
-      const bool has_e = (used & ((1 << 2) | (1 << 4))) != 0;
       for (int q0 = 0; q0 < maxpts; q0 += CH) {
-        // --- point generation (FP64: cut points, sub-simplex volumes)
         for (int qq = i; qq < CH; qq += N) {
           const int qi = q0 + qq;
+          double w = 0.0, pt[3] = {0.25, 0.25, 0.25};
           if (qi < np) {
-            double pt[3], w;
-            if (CUT) {
-              const ElSubS& SS = subs[CUT ? le : 0];
-              const int s = qi / nqb, b = qi % nqb;
-              plain_point(SS.sub[dt][s], sd + 1, c_rules.x[offb + b], pt);
-              w = c_rules.w[offb + b] * SS.vol[dt][s];
-              if (dt == XG_IF) w = w * G.iffac;
-            } else {
-              pt[0] = c_rules.x[offb + qi][0];
-              pt[1] = c_rules.x[offb + qi][1];
-              pt[2] = c_rules.x[offb + qi][2];
-              w = c_rules.w[offb + qi];
-            }
-            pts[le][qq][0] = pt[0];
-            pts[le][qq][1] = pt[1];
-            pts[le][qq][2] = pt[2];
-            pts[le][qq][3] = w * G.meas;
+            const CutSubS& SS = subs[le];
+            const int s = qi / nqb, b = qi % nqb;
+            plain_point(SS.sub[dt][s], sd + 1, c_rules.x[offb + b], pt);
+            w = c_rules.w[offb + b] * SS.vol[dt][s];
+            if (dt == XG_IF) w = w * G.iffac;
           }
+          pts[le][qq][0] = pt[0];
+          pts[le][qq][1] = pt[1];
+          pts[le][qq][2] = pt[2];
+          pts[le][qq][3] = w * G.meas;
         }
         __syncthreads();
-        const int nch = min(CH, np - q0);
-        // --- basis: thread i evaluates function i at the chunk's points
-        for (int qq = 0; qq < nch; qq++) {
+        // features of function i at the chunk's points (zero weight beyond np)
+#pragma unroll
+        for (int qq = 0; qq < CH; qq++) {
           T lam[D + 1];
           T s = 0;
 #pragma unroll
@@ -501,82 +654,86 @@ __global__ void __launch_bounds__(ElCfg<D, K, CUT, T>::NT) k_elmat(
           lam[D] = (T)1 - s;
           T phi, grad[D];
           eval_fn<D, T>(desc, lam, gT, phi, grad);
-          T ev = 0;
-          if (used & (1 << 2)) {
-            T dn = 0;
+          T dn = 0, db = 0;
 #pragma unroll
-            for (int k = 0; k < D; k++) dn += (T)G.nrm[k] * grad[k];
-            ev += cN1 * dn;
+          for (int k = 0; k < D; k++) {
+            dn += (T)G.nrm[k] * grad[k];
+            db += (T)Gq.b[k] * grad[k];
           }
-          if (used & (1 << 4)) {
-            T db = 0;
-#pragma unroll
-            for (int k = 0; k < D; k++) db += (T)Gq.b[k] * grad[k];
-            ev += cC * db;
-          }
-          B[le][qq][i][0] = phi;
-#pragma unroll
-          for (int k = 0; k < D; k++) B[le][qq][i][1 + k] = grad[k];
-          B[le][qq][i][1 + D] = ev;
-        }
-        __syncthreads();
-        // --- contraction: row i
-        for (int qq = 0; qq < nch; qq++) {
           const T w = (T)pts[le][qq][3];
-          const T phi_i = B[le][qq][i][0];
-          T a_i = 0;
-          if (used & 1) a_i += cM * phi_i;
-          if (used & (1 << 3)) {
-            T dn = 0;
+          tr[le][qq][i][0] = phi;
 #pragma unroll
-            for (int k = 0; k < D; k++) dn += (T)G.nrm[k] * B[le][qq][i][1 + k];
-            a_i += cN2 * dn;
-          }
-          a_i *= w;
-          const T b_i = w * phi_i;
-          T gl[D];
+          for (int k = 0; k < D; k++) tr[le][qq][i][1 + k] = grad[k];
+          tr[le][qq][i][1 + D] = dn;
+          tr[le][qq][i][2 + D] = db;
+          // test side: v = A phi_q + G.grad_q + E dn_q + F db_q
+          T A = 0;
+          if (used & (1 << XG_TERM_MASS)) A += cM * phi;
+          if (used & (1 << XG_TERM_U_NGRADV)) A += cN2 * dn;
+          te[le][qq][i][0] = w * A;
 #pragma unroll
-          for (int k = 0; k < D; k++) gl[k] = (used & 2) ? w * cL * B[le][qq][i][1 + k] : (T)0;
+          for (int k = 0; k < D; k++) te[le][qq][i][1 + k] = (used & (1 << XG_TERM_LAPLACE)) ? w * cL * grad[k] : (T)0;
+          te[le][qq][i][1 + D] = (used & (1 << XG_TERM_NGRADU_V)) ? w * cN1 * phi : (T)0;
+          te[le][qq][i][2 + D] = (used & (1 << XG_TERM_CONV)) ? w * cC * phi : (T)0;
+        }
+        __syncthreads();
+        const int nch = min(CH, maxpts - q0);
+        const bool uA = used & ((1 << XG_TERM_MASS) | (1 << XG_TERM_U_NGRADV));
+        const bool uL = used & (1 << XG_TERM_LAPLACE);
+        const bool uE = used & (1 << XG_TERM_NGRADU_V);
+        const bool uF = used & (1 << XG_TERM_CONV);
 #pragma unroll
-          for (int j = 0; j < N; j++) {
-            T v = a_i * B[le][qq][j][0];
-            if (used & 2) {
+        for (int m = 0; m < NACC; m++) {
+          const int t = threadIdx.x + m * NT;
+          if (t < EPB * E) {
+            const int el = t / E, k = t % E, pp = ep[k], qv = eq[k];
+            T v = 0;
+            for (int qq = 0; qq < nch; qq++) {
+              const T* a = te[el][qq][pp];
+              const T* b = tr[el][qq][qv];
+              if (uA) v += a[0] * b[0];
+              if (uL) {
 #pragma unroll
-              for (int k = 0; k < D; k++) v += gl[k] * B[le][qq][j][1 + k];
+                for (int kk = 1; kk <= D; kk++) v += a[kk] * b[kk];
+              }
+              if (uE) v += a[1 + D] * b[1 + D];
+              if (uF) v += a[2 + D] * b[2 + D];
             }
-            if (has_e) v += b_i * B[le][qq][j][1 + D];
-            acc[j].add(v);
+            acc[m].add(v);
           }
         }
         __syncthreads();
       }
     }
-    // ---------------- write ----------------
-    if (G.elem >= 0) {
-      T* out = elmat + ((int64_t)G.slot * N + i) * N;
-      bool finite = true;
 #pragma unroll
-      for (int j = 0; j < N; j++) {
-        T v = acc[j].get();
-        finite &= isfinite(v);
-        out[j] = v;
+    for (int m = 0; m < NACC; m++) {
+      const int t = threadIdx.x + m * NT;
+      if (t < EPB * E) {
+        const int el = t / E, k = t % E;
+        if (geo[el].elem >= 0) {
+          const T v = acc[m].get();
+          if (!isfinite(v)) set_err(err, XG_ERR_NONFINITE);
+          elmat[(int64_t)geo[el].slot * E + k] = v;
+        }
       }
-      if (!finite) set_err(err, XG_ERR_NONFINITE);
     }
-    __syncthreads();
   }
 }
 
 // ============================================================================
-// Facet-patch matrices (ghost penalty).  Thread (facet, patch row a), 2N rows.
+// Facet-patch matrices (ghost penalty): patch rule = the volume rule of order
+// 2*maxorder on each element mapped into the neighbour; contraction over the
+// packed upper triangle of the (2N)^2 symmetric patch matrix.
 // ============================================================================
 template <int D, int K>
 struct PaCfg {
   static constexpr int N = ndof_el(D, K);
   static constexpr int N2 = 2 * N;
+  static constexpr int E = tri_size(N2);
   static constexpr int FPB = N2 <= 8 ? 16 : (N2 <= 20 ? 8 : 4);
   static constexpr int CH = 8;
   static constexpr int NT = N2 * FPB;
+  static constexpr int NACC = (FPB * E + NT - 1) / NT;
 };
 
 template <int D>
@@ -584,6 +741,7 @@ struct PaGeoS {
   Geo<D> g1, g2;
   int gv1[4], gv2[4];
   int facet;
+  double coef[kMaxPatch];
 };
 
 // MapPatchIntegrationPoint (symboliccutbfi.cpp:1747-1846) for affine elements:
@@ -647,14 +805,18 @@ __global__ void __launch_bounds__(PaCfg<D, K>::NT) k_patch(
     const int32_t* __restrict__ fel, FormDesc form, const int32_t* __restrict__ list, const int* __restrict__ counts,
     T* __restrict__ famat, int64_t cap_fa, int* err) {
   using C = PaCfg<D, K>;
-  constexpr int N = C::N, N2 = C::N2, FPB = C::FPB, CH = C::CH;
+  constexpr int N = C::N, N2 = C::N2, E = C::E, FPB = C::FPB, CH = C::CH, NT = C::NT, NACC = C::NACC;
   __shared__ PaGeoS<D> geo[FPB];
   __shared__ double pts[FPB][CH][2 * D + 1];
-  __shared__ T S[FPB][CH][N2];
+  __shared__ T S[FPB][CH][N2];   // s_a = phi1_a / -phi2_(a-N)
+  __shared__ T SW[FPB][CH][N2];  // weighted
+  __shared__ unsigned char ep[E], eq[E];
+  entry_tables(N2, true, ep, eq);
   const int count = counts[2];
   const int lf = threadIdx.x / N2, a = threadIdx.x % N2;
 
   for (int batch = blockIdx.x; batch * FPB < count; batch += gridDim.x) {
+    __syncthreads();
     if (threadIdx.x < FPB) {
       PaGeoS<D>& G = geo[threadIdx.x];
       const int idx = batch * FPB + threadIdx.x;
@@ -664,7 +826,7 @@ __global__ void __launch_bounds__(PaCfg<D, K>::NT) k_patch(
         double xv[D + 1][3];
 #pragma unroll
         for (int v = 0; v <= D; v++) {
-          int vid = elv[(int64_t)v * ne + e1];
+          const int vid = elv[(int64_t)v * ne + e1];
           G.gv1[v] = vid;
 #pragma unroll
           for (int c = 0; c < 3; c++) xv[v][c] = c < D ? xyz[(int64_t)c * nv + vid] : 0.0;
@@ -672,35 +834,38 @@ __global__ void __launch_bounds__(PaCfg<D, K>::NT) k_patch(
         make_geo<D>(xv, G.g1);
 #pragma unroll
         for (int v = 0; v <= D; v++) {
-          int vid = elv[(int64_t)v * ne + e2];
+          const int vid = elv[(int64_t)v * ne + e2];
           G.gv2[v] = vid;
 #pragma unroll
           for (int c = 0; c < 3; c++) xv[v][c] = c < D ? xyz[(int64_t)c * nv + vid] : 0.0;
         }
         make_geo<D>(xv, G.g2);
+        double h = -1.0;
+        for (int pp = 0; pp < form.npatch; pp++) {
+          const PatchDesc& P = form.p[pp];
+          const bool on = !P.defined_on || tbit(P.defined_on, G.facet);
+          if (P.hpow != 0 && h < 0) h = pow(fabs(G.g1.det), 1.0 / D);
+          G.coef[pp] = !on ? 0.0 : (P.hpow == 0 ? P.c : P.c * pow(h, (double)P.hpow));
+        }
       }
     }
     __syncthreads();
     const PaGeoS<D>& G = geo[lf];
     const bool mine1 = a < N;
     const int desc = G.facet >= 0 ? fn_desc<D, K>(mine1 ? a : a - N, mine1 ? G.gv1 : G.gv2) : 0;
-    Acc<T> acc[N2];
+    Acc<T> acc[NACC];
 #pragma unroll
-    for (int j = 0; j < N2; j++) acc[j].init();
+    for (int m = 0; m < NACC; m++) acc[m].init();
 
     for (int pp = 0; pp < form.npatch; pp++) {
       const PatchDesc& P = form.p[pp];
       const int p = clamp_order(P.order);
       const int nq = c_rules.cnt[D][p], off = c_rules.off[D][p];
-      const bool on = G.facet >= 0 && (!P.defined_on || tbit(P.defined_on, G.facet));
-      const int np = on ? 2 * nq : 0;
-      const double h = G.facet >= 0 ? pow(fabs(G.g1.det), 1.0 / D) : 1.0;
-      const double coef = P.hpow == 0 ? P.c : P.c * pow(h, (double)P.hpow);
       for (int q0 = 0; q0 < 2 * nq; q0 += CH) {
         for (int qq = a; qq < CH; qq += N2) {
           const int qi = q0 + qq;
-          if (qi < np) {
-            double x1[3] = {0, 0, 0}, x2[3] = {0, 0, 0}, W;
+          double x1[3] = {0.25, 0.25, 0.25}, x2[3] = {0.25, 0.25, 0.25}, W = 0.0;
+          if (qi < 2 * nq && G.facet >= 0) {
             if (qi < nq) {
 #pragma unroll
               for (int k = 0; k < D; k++) x1[k] = c_rules.x[off + qi][k];
@@ -713,17 +878,17 @@ __global__ void __launch_bounds__(PaCfg<D, K>::NT) k_patch(
               map_patch_point<D>(G.g2, G.g1, x2, x1);
               W = (c_rules.w[off + m] * fabs(G.g2.det) / fabs(G.g1.det)) * fabs(G.g1.det);
             }
-#pragma unroll
-            for (int k = 0; k < D; k++) {
-              pts[lf][qq][k] = x1[k];
-              pts[lf][qq][D + k] = x2[k];
-            }
-            pts[lf][qq][2 * D] = W * coef;
           }
+#pragma unroll
+          for (int k = 0; k < D; k++) {
+            pts[lf][qq][k] = x1[k];
+            pts[lf][qq][D + k] = x2[k];
+          }
+          pts[lf][qq][2 * D] = W * G.coef[pp];
         }
         __syncthreads();
-        const int nch = min(CH, np - q0);
-        for (int qq = 0; qq < nch; qq++) {
+#pragma unroll
+        for (int qq = 0; qq < CH; qq++) {
           T lam[D + 1];
           T s = 0;
 #pragma unroll
@@ -732,33 +897,43 @@ __global__ void __launch_bounds__(PaCfg<D, K>::NT) k_patch(
             s += lam[k];
           }
           lam[D] = (T)1 - s;
-          T v = eval_fn_value<D, T>(desc, lam);
-          S[lf][qq][a] = mine1 ? v : -v;
+          const T v = eval_fn_value<D, T>(desc, lam);
+          const T sv = mine1 ? v : -v;
+          S[lf][qq][a] = sv;
+          SW[lf][qq][a] = (T)pts[lf][qq][2 * D] * sv;
         }
         __syncthreads();
-        for (int qq = 0; qq < nch; qq++) {
-          const T wa = (T)pts[lf][qq][2 * D] * S[lf][qq][a];
+        const int nch = min(CH, 2 * nq - q0);
 #pragma unroll
-          for (int b = 0; b < N2; b++) acc[b].add(wa * S[lf][qq][b]);
+        for (int m = 0; m < NACC; m++) {
+          const int t = threadIdx.x + m * NT;
+          if (t < FPB * E) {
+            const int fl = t / E, k = t % E, pa = ep[k], pb = eq[k];
+            T v = 0;
+            for (int qq = 0; qq < nch; qq++) v += SW[fl][qq][pa] * S[fl][qq][pb];
+            acc[m].add(v);
+          }
         }
         __syncthreads();
       }
     }
-    const int idx = batch * FPB + lf;
-    if (G.facet >= 0 && idx >= cap_fa) {
-      if (a == 0) set_err(err, XG_ERR_CAPACITY);
-    } else if (G.facet >= 0) {
-      T* out = famat + ((int64_t)idx * N2 + a) * N2;
-      bool finite = true;
 #pragma unroll
-      for (int b = 0; b < N2; b++) {
-        T v = acc[b].get();
-        finite &= isfinite(v);
-        out[b] = v;
+    for (int m = 0; m < NACC; m++) {
+      const int t = threadIdx.x + m * NT;
+      if (t < FPB * E) {
+        const int fl = t / E, k = t % E;
+        const int idx = batch * FPB + fl;
+        if (geo[fl].facet >= 0) {
+          if (idx >= cap_fa) {
+            if (k == 0) set_err(err, XG_ERR_CAPACITY);
+          } else {
+            const T v = acc[m].get();
+            if (!isfinite(v)) set_err(err, XG_ERR_NONFINITE);
+            famat[(int64_t)idx * E + k] = v;
+          }
+        }
       }
-      if (!finite) set_err(err, XG_ERR_NONFINITE);
     }
-    __syncthreads();
   }
 }
 
@@ -788,6 +963,7 @@ struct ScatterArgs {
   const int32_t* dof_row;    // dof -> row (valid for active dofs)
   const int* counts;         // [3] = nrows
   int64_t cap_fa;
+  int el_sym;                // element matrices stored as packed upper triangles
   int hs;                    // hash slots per warp (pow2)
   int maxu;                  // distinct-column capacity per warp (pow2)
   int stage;                 // staged (pos, value) pairs per warp
@@ -1042,13 +1218,17 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_row_fill(ScatterArgs A, cons
           double v;
           if (kind == 0) {
             colel = e;
-            v = (double)elmat[((int64_t)A.el_slot[e] * nd + i) * nd + j];
+            const int64_t eo = (int64_t)A.el_slot[e];
+            v = A.el_sym ? (double)elmat[eo * tri_size(nd) + (i <= j ? tri_index(i, j, nd) : tri_index(j, i, nd))]
+                         : (double)elmat[(eo * nd + i) * nd + j];
           } else {
             const int lf = (kind - 1) >> 1, h = (kind - 1) & 1;
             const int first = S.ent_first[a * 4 + lf], nb = S.ent_nb[a * 4 + lf], fs = S.ent_fs[a * 4 + lf];
-            const int prow = first ? i : nd + i;
+            const int prow = first ? i : nd + i, pcol = h * nd + j;
             colel = (h == 0) == (first != 0) ? e : nb;
-            v = fs < A.cap_fa ? (double)famat[((int64_t)fs * n2 + prow) * n2 + h * nd + j] : 0.0;
+            v = fs < A.cap_fa ? (double)famat[(int64_t)fs * tri_size(n2) +
+                                              (prow <= pcol ? tri_index(prow, pcol, n2) : tri_index(pcol, prow, n2))]
+                              : 0.0;
           }
           const int c = A.el_dofs[(int64_t)colel * nd + j];
           S.spos[t] = lower_bound_sm(S.ucols, u, c);
@@ -1087,6 +1267,9 @@ struct xg_form {
   std::vector<int> term_slot;  // group index (volume) or patch index
   FormDesc desc;
   int needs_mask = 0;  // domains needing decompositions on cut elements
+  int el_sym = 0;      // every volume group symmetric: packed element matrices
+  double* d_tabs = nullptr;  // reference tables of the uncut kernel
+  UncutTabs tabs = {};
   int64_t nw32_el = 0, nw32_fa = 0, nw32_dof = 0;
   int64_t cap_el = 0, cap_fa = 0;
   // workspace
@@ -1127,7 +1310,7 @@ struct xg_form {
 namespace {
 
 int form_free(xg_form* f) {
-  void* ptrs[] = {f->d_act_un, f->d_act_cut, f->d_act_fa, f->d_dof_bits, f->d_l_un, f->d_l_cut, f->d_l_fa,
+  void* ptrs[] = {f->d_tabs, f->d_act_un, f->d_act_cut, f->d_act_fa, f->d_dof_bits, f->d_l_un, f->d_l_cut, f->d_l_fa,
                   f->d_el_slot, f->d_fa_slot, f->d_dof_row, f->d_rowcnt, f->d_counts, f->d_bsum, f->d_bsum64,
                   f->d_elmat, f->d_famat, f->d_err, f->d_dom, f->d_ratio, f->d_bits, f->d_fbits};
   for (void* p : ptrs) cudaFree(p);
@@ -1199,10 +1382,142 @@ int build_desc(xg_form* f) {
     G.c[T.kind] = T.coef;
     G.hpow[T.kind] = T.hpow;
     G.used |= 1 << T.kind;
+
     if (T.kind == XG_TERM_CONV)
       for (int k = 0; k < 3; k++) G.b[k] = T.b[k];
     f->term_slot[t] = g;
     f->needs_mask |= 1 << T.domain;
+  }
+  f->el_sym = 1;
+  for (int q = 0; q < d.ngroups; q++) {
+    const GroupDesc& G = d.g[q];
+    const int n1 = 1 << XG_TERM_NGRADU_V, n2 = 1 << XG_TERM_U_NGRADV;
+    bool sym = !(G.used & (1 << XG_TERM_CONV));
+    if ((G.used & n1) || (G.used & n2))
+      sym = sym && (G.used & n1) && (G.used & n2) && G.c[XG_TERM_NGRADU_V] == G.c[XG_TERM_U_NGRADV] &&
+            G.hpow[XG_TERM_NGRADU_V] == G.hpow[XG_TERM_U_NGRADV];
+    if (!sym) f->el_sym = 0;
+  }
+  return XG_OK;
+}
+
+// Reference tables of the uncut kernel for every NEG/POS group: the group's
+// rule on the reference simplex applied to products of the canonical basis
+// (edge orientation by local vertex number).
+template <int D, int K>
+std::vector<double> uncut_tables(const FormDesc& d, bool sym, size_t offs[][3]) {
+  constexpr int N = ndof_el(D, K);
+  const int E = sym ? tri_size(N) : N * N;
+  const int NG = D * (D + 1) / 2;
+  const RuleTable& R = host_rules();
+  std::vector<double> buf;
+  int gv[4] = {0, 1, 2, 3};
+  int desc[N];
+  for (int i = 0; i < N; i++) desc[i] = fn_desc<D, K>(i, gv);
+  double g[D + 1][D];
+  for (int a = 0; a <= D; a++)
+    for (int k = 0; k < D; k++) g[a][k] = a < D ? (a == k ? 1.0 : 0.0) : -1.0;
+  for (int q = 0; q < d.ngroups; q++) {
+    offs[q][0] = offs[q][1] = offs[q][2] = (size_t)-1;
+    const GroupDesc& G = d.g[q];
+    if (G.domain == XG_IF) continue;
+    const int p = clamp_order(G.order), off = R.off[D][p], cnt = R.cnt[D][p];
+    std::vector<double> phi((size_t)cnt * N), dphi((size_t)cnt * N * D);
+    for (int x = 0; x < cnt; x++) {
+      double lam[D + 1], s = 0;
+      for (int a = 0; a < D; a++) {
+        lam[a] = R.x[off + x][a];
+        s += lam[a];
+      }
+      lam[D] = 1.0 - s;
+      for (int i = 0; i < N; i++) {
+        double gr[D];
+        eval_fn<D, double>(desc[i], lam, g, phi[(size_t)x * N + i], gr);
+        for (int k = 0; k < D; k++) dphi[((size_t)x * N + i) * D + k] = gr[k];
+      }
+    }
+    auto entry = [&](int k, int& pp, int& qq) {
+      if (sym) {
+        pp = 0;
+        int rem = k;
+        while (rem >= N - pp) {
+          rem -= N - pp;
+          pp++;
+        }
+        qq = pp + rem;
+      } else {
+        pp = k / N;
+        qq = k % N;
+      }
+    };
+    if (G.used & (1 << XG_TERM_MASS)) {
+      offs[q][0] = buf.size();
+      for (int k = 0; k < E; k++) {
+        int pp, qq;
+        entry(k, pp, qq);
+        double s = 0;
+        for (int x = 0; x < cnt; x++) s += R.w[off + x] * phi[(size_t)x * N + pp] * phi[(size_t)x * N + qq];
+        buf.push_back(s);
+      }
+    }
+    if (G.used & (1 << XG_TERM_LAPLACE)) {
+      offs[q][1] = buf.size();
+      for (int a = 0; a < D; a++)
+        for (int b = a; b < D; b++)
+          for (int k = 0; k < E; k++) {
+            int pp, qq;
+            entry(k, pp, qq);
+            double s = 0;
+            for (int x = 0; x < cnt; x++) {
+              const double* dp = &dphi[((size_t)x * N + pp) * D];
+              const double* dq = &dphi[((size_t)x * N + qq) * D];
+              double v = dp[a] * dq[b];
+              if (a != b) v += dp[b] * dq[a];
+              s += R.w[off + x] * v;
+            }
+            buf.push_back(s);
+          }
+    }
+    if (G.used & (1 << XG_TERM_CONV)) {
+      offs[q][2] = buf.size();
+      for (int a = 0; a < D; a++)
+        for (int k = 0; k < E; k++) {
+          int pp, qq;
+          entry(k, pp, qq);
+          double s = 0;
+          for (int x = 0; x < cnt; x++) s += R.w[off + x] * phi[(size_t)x * N + pp] * dphi[((size_t)x * N + qq) * D + a];
+          buf.push_back(s);
+        }
+    }
+    (void)NG;
+  }
+  return buf;
+}
+
+int upload_tables(xg_form* f) {
+  size_t offs[kMaxGroups][3];
+  std::vector<double> buf;
+  const int D = f->mesh->dim, K = f->space->order;
+  const bool sym = f->el_sym;
+  if (D == 2) {
+    if (K == 1) buf = uncut_tables<2, 1>(f->desc, sym, offs);
+    else if (K == 2) buf = uncut_tables<2, 2>(f->desc, sym, offs);
+    else buf = uncut_tables<2, 3>(f->desc, sym, offs);
+  } else {
+    if (K == 1) buf = uncut_tables<3, 1>(f->desc, sym, offs);
+    else if (K == 2) buf = uncut_tables<3, 2>(f->desc, sym, offs);
+    else buf = uncut_tables<3, 3>(f->desc, sym, offs);
+  }
+  cudaFree(f->d_tabs);
+  f->d_tabs = nullptr;
+  std::memset(&f->tabs, 0, sizeof(f->tabs));
+  if (buf.empty()) return XG_OK;
+  XG_CUDA(cudaMalloc((void**)&f->d_tabs, buf.size() * sizeof(double)));
+  XG_CUDA(cudaMemcpy(f->d_tabs, buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice));
+  for (int q = 0; q < f->desc.ngroups; q++) {
+    f->tabs.m[q] = offs[q][0] == (size_t)-1 ? nullptr : f->d_tabs + offs[q][0];
+    f->tabs.t[q] = offs[q][1] == (size_t)-1 ? nullptr : f->d_tabs + offs[q][1];
+    f->tabs.c[q] = offs[q][2] == (size_t)-1 ? nullptr : f->d_tabs + offs[q][2];
   }
   return XG_OK;
 }
@@ -1228,25 +1543,30 @@ int compact(xg_form* f, const uint32_t* bits, int64_t nw32, int32_t* list, int32
   return e == cudaSuccess ? XG_OK : cuda_fail(e, "compact");
 }
 
-template <int D, int K, typename T>
-int launch_volume(xg_form* f, const double* d_lset, const uint8_t* d_dom, cudaStream_t s) {
-  using CU = ElCfg<D, K, false, T>;
-  using CC = ElCfg<D, K, true, T>;
+template <int D, int K, bool SYM, typename T>
+int launch_volume_sym(xg_form* f, const double* d_lset, const uint8_t* d_dom, cudaStream_t s) {
+  using CC = CutCfg<D, K, SYM, T>;
   xg_mesh* m = f->mesh;
-  auto ku = k_elmat<D, K, false, T>;
-  auto kc = k_elmat<D, K, true, T>;
+  auto ku = k_elmat_uncut<D, K, SYM, T>;
+  auto kc = k_elmat_cut<D, K, SYM, T>;
   if (!f->grid_el_un) {
-    f->grid_el_un = grid_for(ku, CU::NT, 0);
+    f->grid_el_un = grid_for(ku, 256, 0);
     f->grid_el_cut = grid_for(kc, CC::NT, 0);
   }
-  ku<<<f->grid_el_un, CU::NT, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, d_lset, d_dom, f->desc, f->d_l_un,
-                                     f->d_counts, 0, (T*)f->d_elmat, f->d_err, f->needs_mask);
+  ku<<<f->grid_el_un, 256, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, d_dom, f->desc, f->tabs, f->d_l_un, f->d_counts,
+                                   (T*)f->d_elmat, f->d_err);
   if (f->use_ev) cudaEventRecord(f->ev[3], s);
-  kc<<<f->grid_el_cut, CC::NT, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, d_lset, d_dom, f->desc, f->d_l_cut,
-                                      f->d_counts, 1, (T*)f->d_elmat, f->d_err, f->needs_mask);
+  kc<<<f->grid_el_cut, CC::NT, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, d_lset, f->desc, f->d_l_cut, f->d_counts,
+                                      (T*)f->d_elmat, f->d_err, f->needs_mask);
   if (f->use_ev) cudaEventRecord(f->ev[4], s);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? XG_OK : cuda_fail(e, "k_elmat");
+}
+
+template <int D, int K, typename T>
+int launch_volume(xg_form* f, const double* d_lset, const uint8_t* d_dom, cudaStream_t s) {
+  return f->el_sym ? launch_volume_sym<D, K, true, T>(f, d_lset, d_dom, s)
+                   : launch_volume_sym<D, K, false, T>(f, d_lset, d_dom, s);
 }
 
 template <int D, int K, typename T>
@@ -1308,6 +1628,7 @@ ScatterArgs scatter_args(xg_form* f) {
   A.dof_row = f->d_dof_row;
   A.counts = f->d_counts;
   A.cap_fa = f->cap_fa;
+  A.el_sym = f->el_sym;
   A.hs = f->sc_hs;
   A.maxu = f->sc_maxu;
   A.stage = f->sc_stage;
@@ -1389,8 +1710,9 @@ int xg_form_create(xg_space* space, const xg_term* terms, int32_t nterms, int pr
   f->precision = precision;
   f->terms.assign(terms, terms + nterms);
   int st = build_desc(f);
+  if (!st) st = upload_tables(f);
   if (st) {
-    delete f;
+    form_free(f);
     return st;
   }
   xg_mesh* m = f->mesh;
@@ -1401,7 +1723,7 @@ int xg_form_create(xg_space* space, const xg_term* terms, int32_t nterms, int pr
   f->nw32_dof = 2 * ((space->ndof + 63) / 64);
   f->cap_el = m->ne;
   // facet-patch workspace: all facets when small, else a quarter of them
-  const size_t fa_bytes = (size_t)m->nfacets * (2 * nd) * (2 * nd) * esz;
+  const size_t fa_bytes = (size_t)m->nfacets * tri_size(2 * nd) * esz;
   f->cap_fa = fa_bytes <= ((size_t)4 << 30) ? m->nfacets : std::max<int64_t>(m->nfacets / 4, 1);
   int64_t maxw = std::max(f->nw32_el, std::max(f->nw32_fa, f->nw32_dof));
   f->nbsum = (int)((maxw + kCChunk - 1) / kCChunk) + 1;
@@ -1434,7 +1756,7 @@ int xg_form_create(xg_space* space, const xg_term* terms, int32_t nterms, int pr
   e = e ? e : A((void**)&f->d_bsum, (size_t)f->nbsum * 4);
   e = e ? e : A((void**)&f->d_bsum64, (size_t)f->nbsum64 * 8);
   e = e ? e : A(&f->d_elmat, (size_t)f->cap_el * nd * nd * esz);
-  e = e ? e : A(&f->d_famat, f->has_patch ? (size_t)f->cap_fa * 4 * nd * nd * esz : 16);
+  e = e ? e : A(&f->d_famat, f->has_patch ? (size_t)f->cap_fa * tri_size(2 * nd) * esz : 16);
   e = e ? e : A((void**)&f->d_err, sizeof(int));
   e = e ? e : A((void**)&f->d_dom, (size_t)m->ne);
   e = e ? e : A((void**)&f->d_ratio, (size_t)m->ne * 8);
@@ -1475,7 +1797,8 @@ int xg_form_destroy(xg_form* f) {
 int xg_form_set_defined_on(xg_form* f, int32_t t, const uint64_t* d_defined_on) {
   if (!f || t < 0 || t >= (int)f->terms.size()) return XG_ERR_ARG;
   f->terms[t].d_defined_on = d_defined_on;
-  return build_desc(f);
+  int st = build_desc(f);
+  return st ? st : upload_tables(f);
 }
 
 int xg_form_capacity(const xg_form* f, int64_t* o) {

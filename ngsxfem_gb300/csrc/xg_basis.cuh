@@ -15,7 +15,7 @@ __host__ __device__ constexpr int ndof_el(int D, int K) {
   return D == 2 ? (K + 1) * (K + 2) / 2 : (K + 1) * (K + 2) * (K + 3) / 6;
 }
 
-__device__ __forceinline__ void local_edge(int D, int j, int& a, int& b) {
+__host__ __device__ __forceinline__ void local_edge(int D, int j, int& a, int& b) {
   // trig edges (0,1),(0,2),(1,2); tet edges (0,1),(0,2),(0,3),(1,2),(1,3),(2,3)
   if (D == 2) {
     a = j == 2 ? 1 : 0;
@@ -28,7 +28,7 @@ __device__ __forceinline__ void local_edge(int D, int j, int& a, int& b) {
   }
 }
 
-__device__ __forceinline__ void local_face(int j, int& a, int& b, int& c) {
+__host__ __device__ __forceinline__ void local_face(int j, int& a, int& b, int& c) {
   // tet faces (0,1,2),(0,1,3),(0,2,3),(1,2,3)
   a = j == 3 ? 1 : 0;
   b = j <= 1 ? 1 : 2;
@@ -38,7 +38,7 @@ __device__ __forceinline__ void local_face(int j, int& a, int& b, int& c) {
 // Descriptor of local function i: type | a<<4 | b<<8 | c<<12
 // type 0 vertex, 1 edge quadratic, 2 edge cubic, 3 face/cell bubble.
 template <int D, int K>
-__device__ __forceinline__ int fn_desc(int i, const int* gv) {
+__host__ __device__ __forceinline__ int fn_desc(int i, const int* gv) {
   if (i <= D) return 0 | (i << 4);
   int r = i - (D + 1);
   const int nedge = D == 2 ? 3 : 6;
@@ -59,7 +59,7 @@ __device__ __forceinline__ int fn_desc(int i, const int* gv) {
 // value and physical gradient of function `desc` at barycentric lam, with
 // physical barycentric gradients g[D+1][D]
 template <int D, typename T>
-__device__ __forceinline__ void eval_fn(int desc, const T* lam, const T (*g)[D], T& phi, T* grad) {
+__host__ __device__ __forceinline__ void eval_fn(int desc, const T* lam, const T (*g)[D], T& phi, T* grad) {
   const int type = desc & 15, a = (desc >> 4) & 15, b = (desc >> 8) & 15, c = (desc >> 12) & 15;
   if (type == 0) {
     phi = lam[a];
@@ -86,7 +86,7 @@ __device__ __forceinline__ void eval_fn(int desc, const T* lam, const T (*g)[D],
 }
 
 template <int D, typename T>
-__device__ __forceinline__ T eval_fn_value(int desc, const T* lam) {
+__host__ __device__ __forceinline__ T eval_fn_value(int desc, const T* lam) {
   const int type = desc & 15, a = (desc >> 4) & 15, b = (desc >> 8) & 15, c = (desc >> 12) & 15;
   if (type == 0) return lam[a];
   if (type == 1) return lam[a] * lam[b];

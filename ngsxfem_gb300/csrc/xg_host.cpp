@@ -91,6 +91,20 @@ static RuleTable build_rules() {
   auto add = [&](double a, double b, double c, double w) {
     t.x[n][0] = a; t.x[n][1] = b; t.x[n][2] = c; t.w[n] = w; n++;
   };
+  // fully symmetric orbits; parameters solved from the moment equations
+  // (oracle/derive_symmetric_rules.py)
+  auto sym21 = [&](double a, double w) {
+    const double b = 1.0 - 2.0 * a;
+    add(a, a, 0, w); add(a, b, 0, w); add(b, a, 0, w);
+  };
+  auto sym31 = [&](double a, double w) {
+    const double b = 1.0 - 3.0 * a;
+    add(a, a, a, w); add(a, a, b, w); add(a, b, a, w); add(b, a, a, w);
+  };
+  auto sym22 = [&](double c, double w) {
+    const double d2 = 0.5 - c;
+    add(c, c, d2, w); add(c, d2, c, w); add(c, d2, d2, w); add(d2, c, c, w); add(d2, c, d2, w); add(d2, d2, c, w);
+  };
   for (int d = 0; d <= 3; d++)
     for (int p = 0; p <= kMaxOrder; p++) {
       t.off[d][p] = n;
@@ -107,6 +121,13 @@ static RuleTable build_rules() {
           add(1.0 / 6, 1.0 / 6, 0, 1.0 / 6);
           add(2.0 / 3, 1.0 / 6, 0, 1.0 / 6);
           add(1.0 / 6, 2.0 / 3, 0, 1.0 / 6);
+        } else if (p == 4) {
+          sym21(0.4459484909159648863183293, 0.1116907948390057328475035);
+          sym21(0.09157621350977074345957146, 0.05497587182766093381916316);
+        } else if (p == 5) {
+          add(1.0 / 3, 1.0 / 3, 0, 0.1125);
+          sym21(0.4701420641051150897704412, 0.06619707639425309036882469);
+          sym21(0.1012865073234563388009874, 0.06296959027241357629784197);
         } else {
           std::vector<double> xu, wu, xv, wv;
           gauss_jacobi01(m, 1, xu, wu);
@@ -122,6 +143,10 @@ static RuleTable build_rules() {
           add(b, a, b, 1.0 / 24);
           add(b, b, a, 1.0 / 24);
           add(b, b, b, 1.0 / 24);
+        } else if (p == 4 || p == 5) {
+          sym31(0.09273525031089122640232391, 0.01224884051939365825728503);
+          sym31(0.3108859192633006097973457, 0.01878132095300264179986428);
+          sym22(0.4544962958743503505081195, 0.007091003462846911073011571);
         } else {
           std::vector<double> xu, wu, xv, wv, xw, ww;
           gauss_jacobi01(m, 2, xu, wu);

@@ -12,10 +12,12 @@ namespace xg {
 
 // ---- quadrature rule family (host-built, device __constant__) ------------------
 // segment order p: Gauss-Legendre with p/2+1 points on [0,1]
-// trig: p<=1 centroid; p==2 3-point (1/6,1/6,2/3); p>=3 collapsed Gauss-Jacobi
+// trig: p<=1 centroid; p==2 3-point (1/6,1/6,2/3); p==4 6-point and p==5
+//       7-point fully symmetric rules; otherwise collapsed Gauss-Jacobi
 //       conical product, p/2+1 points per direction
-// tet : p<=1 centroid; p==2 4-point (a,b,b,b), a=(5+3sqrt5)/20;
-//       p>=3 conical product, p/2+1 points per direction
+// tet : p<=1 centroid; p==2 4-point (a,b,b,b), a=(5+3sqrt5)/20; p==4,5
+//       14-point fully symmetric rule; otherwise conical product, p/2+1
+//       points per direction
 constexpr int kMaxOrder = 8;
 constexpr int kRuleCap = 512;  // total points of all tables
 

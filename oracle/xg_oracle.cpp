@@ -39,10 +39,13 @@ namespace {
 // eigenvalues by the cyclic Jacobi rotation method.
 // Rule family (shared definition with the product):
 //   segment order p : Gauss-Legendre, n = p/2+1 points on [0,1]
-//   trig   order p : p<=1 centroid; p==2 3-point (1/6,1/6,2/3); p>=3 collapsed
+//   trig   order p : p<=1 centroid; p==2 3-point (1/6,1/6,2/3); p==4 6-point and
+//                    p==5 7-point fully symmetric rules; otherwise collapsed
 //                    Gauss-Jacobi conical product, n = p/2+1 per direction
 //   tet    order p : p<=1 centroid; p==2 4-point (a,b,b,b), a=(5+3sqrt5)/20;
-//                    p>=3 conical product n = p/2+1 per direction
+//                    p==4,5 14-point fully symmetric rule; otherwise conical
+//                    product n = p/2+1 per direction
+// The symmetric rules' parameters come from oracle/derive_symmetric_rules.py.
 // ---------------------------------------------------------------------------
 void sym_eig(int n, std::vector<double>& A, std::vector<double>& V) {
   V.assign(n * n, 0.0);
@@ -163,12 +166,36 @@ Rule make_rule(int d, int p) {
     for (int i = 0; i < n; i++) add(x[i], 0, 0, w[i]);
     return r;
   }
+  // orbits in barycentric coordinates (lambda_0, lambda_1, lambda_2[, lambda_3]); point = (lambda_0, lambda_1[, lambda_2])
+  auto s21 = [&](double a, double w) {
+    double b = 1.0 - 2.0 * a;
+    add(a, a, 0, w); add(a, b, 0, w); add(b, a, 0, w);
+  };
+  auto s31 = [&](double a, double w) {
+    double b = 1.0 - 3.0 * a;
+    add(a, a, a, w); add(a, a, b, w); add(a, b, a, w); add(b, a, a, w);
+  };
+  auto s22 = [&](double c, double w) {
+    double dd = 0.5 - c;
+    add(c, c, dd, w); add(c, dd, c, w); add(c, dd, dd, w); add(dd, c, c, w); add(dd, c, dd, w); add(dd, dd, c, w);
+  };
   if (d == 2) {
     if (p <= 1) { add(1.0 / 3, 1.0 / 3, 0, 0.5); return r; }
     if (p == 2) {
       add(1.0 / 6, 1.0 / 6, 0, 1.0 / 6);
       add(2.0 / 3, 1.0 / 6, 0, 1.0 / 6);
       add(1.0 / 6, 2.0 / 3, 0, 1.0 / 6);
+      return r;
+    }
+    if (p == 4) {
+      s21(0.4459484909159648863183293, 0.1116907948390057328475035);
+      s21(0.09157621350977074345957146, 0.05497587182766093381916316);
+      return r;
+    }
+    if (p == 5) {
+      add(1.0 / 3, 1.0 / 3, 0, 0.1125);
+      s21(0.4701420641051150897704412, 0.06619707639425309036882469);
+      s21(0.1012865073234563388009874, 0.06296959027241357629784197);
       return r;
     }
     std::vector<double> xu, wu, xv, wv;
@@ -186,6 +213,12 @@ Rule make_rule(int d, int p) {
     add(b, a, b, 1.0 / 24);
     add(b, b, a, 1.0 / 24);
     add(b, b, b, 1.0 / 24);
+    return r;
+  }
+  if (p == 4 || p == 5) {
+    s31(0.09273525031089122640232391, 0.01224884051939365825728503);
+    s31(0.3108859192633006097973457, 0.01878132095300264179986428);
+    s22(0.4544962958743503505081195, 0.007091003462846911073011571);
     return r;
   }
   std::vector<double> xu, wu, xv, wv, xw, ww;

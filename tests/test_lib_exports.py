@@ -46,10 +46,13 @@ def test_status_strings(lib):
 
 
 def test_rule_sizes(lib):
-    # rule family: tet order 2 -> 4 points, order 4 -> 27, trig order 4 -> 9, segment order 4 -> 3
+    # rule family: tet order 2 -> 4 points, order 4 -> 14, order 6 -> 64 (conical),
+    # trig order 4 -> 6, order 5 -> 7, segment order 4 -> 3
     assert lib.xg_base_rule_size(3, 2) == 4
-    assert lib.xg_base_rule_size(3, 4) == 27
-    assert lib.xg_base_rule_size(2, 4) == 9
+    assert lib.xg_base_rule_size(3, 4) == 14
+    assert lib.xg_base_rule_size(3, 6) == 64
+    assert lib.xg_base_rule_size(2, 4) == 6
+    assert lib.xg_base_rule_size(2, 5) == 7
     assert lib.xg_base_rule_size(1, 4) == 3
 
 
