@@ -738,65 +738,34 @@ struct PaCfg {
 
 template <int D>
 struct PaGeoS {
-  Geo<D> g1, g2;
+  double A12[D][D], c12[D];  // xi_2 = A12 xi_1 + c12 (element 1 -> element 2 reference coordinates)
+  double A21[D][D], c21[D];
+  double det1, det2;
   int gv1[4], gv2[4];
   int facet;
   double coef[kMaxPatch];
 };
 
-// MapPatchIntegrationPoint (symboliccutbfi.cpp:1747-1846) for affine elements:
-// low-order guess A^-1 (x - x(0)) plus the Newton correction loop.
+// Reference-coordinate map between the two elements of a patch.  For affine
+// elements the low-order guess of MapPatchIntegrationPoint
+// (symboliccutbfi.cpp:1747-1846) is the exact map and its Newton loop only
+// adds a correction of rounding size, so the map is precomputed once per facet.
 template <int D>
-__device__ __forceinline__ void map_patch_point(const Geo<D>& from, const Geo<D>& to, const double* xi_from,
-                                                double* xi_to) {
-  double vec[D];
+__device__ __forceinline__ void patch_map(const Geo<D>& from, const Geo<D>& to, double (*A)[D], double* c) {
 #pragma unroll
   for (int i = 0; i < D; i++) {
-    double s = from.x0[i];
 #pragma unroll
-    for (int k = 0; k < D; k++) s += from.F[i][k] * xi_from[k];
-    vec[i] = s;
-  }
-  const double h = sqrt(from.det);
-  double x00[D], x0[D];
-#pragma unroll
-  for (int i = 0; i < D; i++) {
-    double s = 0;
-#pragma unroll
-    for (int k = 0; k < D; k++) s += to.Finv[i][k] * (vec[k] - to.x0[k]);
-    x00[i] = s;
-    x0[i] = s;
-  }
-  int its = 0;
-  double diffn = 0;
-  while (its == 0 || (diffn > 1e-12 * h && its < 15)) {
-    double diff[D];
-#pragma unroll
-    for (int i = 0; i < D; i++) {
-      double s = to.x0[i];
-#pragma unroll
-      for (int k = 0; k < D; k++) s += to.F[i][k] * x0[k];
-      diff[i] = vec[i] - s;
-    }
-    diffn = 0;
-#pragma unroll
-    for (int i = 0; i < D; i++) diffn += diff[i] * diff[i];
-    diffn = sqrt(diffn);
-#pragma unroll
-    for (int i = 0; i < D; i++) {
+    for (int k = 0; k < D; k++) {
       double s = 0;
 #pragma unroll
-      for (int k = 0; k < D; k++) s += to.Finv[i][k] * diff[k];
-      x0[i] += s;
+      for (int j = 0; j < D; j++) s += to.Finv[i][j] * from.F[j][k];
+      A[i][k] = s;
     }
-    its++;
+    double s = 0;
+#pragma unroll
+    for (int j = 0; j < D; j++) s += to.Finv[i][j] * (from.x0[j] - to.x0[j]);
+    c[i] = s;
   }
-  double dist = 0;
-#pragma unroll
-  for (int i = 0; i < D; i++) dist += (x0[i] - x00[i]) * (x0[i] - x00[i]);
-  const bool fallback = its >= 15 || diffn > 1e-12 * h || sqrt(dist) > 10.0;
-#pragma unroll
-  for (int i = 0; i < D; i++) xi_to[i] = fallback ? x00[i] : x0[i];
 }
 
 template <int D, int K, typename T>
@@ -831,7 +800,8 @@ __global__ void __launch_bounds__(PaCfg<D, K>::NT) k_patch(
 #pragma unroll
           for (int c = 0; c < 3; c++) xv[v][c] = c < D ? xyz[(int64_t)c * nv + vid] : 0.0;
         }
-        make_geo<D>(xv, G.g1);
+        Geo<D> g1, g2;
+        make_geo<D>(xv, g1);
 #pragma unroll
         for (int v = 0; v <= D; v++) {
           const int vid = elv[(int64_t)v * ne + e2];
@@ -839,12 +809,16 @@ __global__ void __launch_bounds__(PaCfg<D, K>::NT) k_patch(
 #pragma unroll
           for (int c = 0; c < 3; c++) xv[v][c] = c < D ? xyz[(int64_t)c * nv + vid] : 0.0;
         }
-        make_geo<D>(xv, G.g2);
+        make_geo<D>(xv, g2);
+        patch_map<D>(g1, g2, G.A12, G.c12);
+        patch_map<D>(g2, g1, G.A21, G.c21);
+        G.det1 = fabs(g1.det);
+        G.det2 = fabs(g2.det);
         double h = -1.0;
         for (int pp = 0; pp < form.npatch; pp++) {
           const PatchDesc& P = form.p[pp];
           const bool on = !P.defined_on || tbit(P.defined_on, G.facet);
-          if (P.hpow != 0 && h < 0) h = pow(fabs(G.g1.det), 1.0 / D);
+          if (P.hpow != 0 && h < 0) h = pow(G.det1, 1.0 / D);
           G.coef[pp] = !on ? 0.0 : (P.hpow == 0 ? P.c : P.c * pow(h, (double)P.hpow));
         }
       }
@@ -869,14 +843,26 @@ __global__ void __launch_bounds__(PaCfg<D, K>::NT) k_patch(
             if (qi < nq) {
 #pragma unroll
               for (int k = 0; k < D; k++) x1[k] = c_rules.x[off + qi][k];
-              map_patch_point<D>(G.g1, G.g2, x1, x2);
-              W = c_rules.w[off + qi] * fabs(G.g1.det);
+#pragma unroll
+              for (int i2 = 0; i2 < D; i2++) {
+                double sacc = G.c12[i2];
+#pragma unroll
+                for (int k = 0; k < D; k++) sacc += G.A12[i2][k] * x1[k];
+                x2[i2] = sacc;
+              }
+              W = c_rules.w[off + qi] * G.det1;
             } else {
               const int m = qi - nq;
 #pragma unroll
               for (int k = 0; k < D; k++) x2[k] = c_rules.x[off + m][k];
-              map_patch_point<D>(G.g2, G.g1, x2, x1);
-              W = (c_rules.w[off + m] * fabs(G.g2.det) / fabs(G.g1.det)) * fabs(G.g1.det);
+#pragma unroll
+              for (int i1 = 0; i1 < D; i1++) {
+                double sacc = G.c21[i1];
+#pragma unroll
+                for (int k = 0; k < D; k++) sacc += G.A21[i1][k] * x2[k];
+                x1[i1] = sacc;
+              }
+              W = c_rules.w[off + m] * G.det2;
             }
           }
 #pragma unroll
