@@ -479,7 +479,7 @@ struct CutCfg {
   static constexpr int N = ndof_el(D, K);
   static constexpr int E = SYM ? tri_size(N) : N * N;
   static constexpr int EPB = N <= 4 ? 16 : (N <= 10 ? 8 : 4);
-  static constexpr int CH = 4;
+  static constexpr int CH = N <= 4 ? 3 : 4;
   static constexpr int NT = N * EPB;
   static constexpr int NACC = (EPB * E + NT - 1) / NT;
   static constexpr int NF = D + 3;  // phi, grad (D), n.grad, b.grad
@@ -510,7 +510,7 @@ __global__ void __launch_bounds__(CutCfg<D, K, SYM, T>::NT) k_elmat_cut(
   constexpr int N = C::N, E = C::E, EPB = C::EPB, CH = C::CH, NT = C::NT, NACC = C::NACC, NF = C::NF;
   __shared__ CutGeoS geo[EPB];
   __shared__ CutSubS subs[EPB];
-  __shared__ double pts[EPB][CH][4];
+  __shared__ T pts[EPB][CH][D + 2];  // barycentric coordinates and w |det F|
   __shared__ T tr[EPB][CH][N][NF];  // trial features: phi, grad, n.grad, b.grad
   __shared__ T te[EPB][CH][N][NF];  // test features scaled by w and the coefficients
   __shared__ unsigned char ep[E], eq[E];
@@ -635,32 +635,35 @@ __global__ void __launch_bounds__(CutCfg<D, K, SYM, T>::NT) k_elmat_cut(
             w = c_rules.w[offb + b] * SS.vol[dt][s];
             if (dt == XG_IF) w = w * G.iffac;
           }
-          pts[le][qq][0] = pt[0];
-          pts[le][qq][1] = pt[1];
-          pts[le][qq][2] = pt[2];
-          pts[le][qq][3] = w * G.meas;
-        }
-        __syncthreads();
-        // features of function i at the chunk's points (zero weight beyond np)
-#pragma unroll
-        for (int qq = 0; qq < CH; qq++) {
-          T lam[D + 1];
-          T s = 0;
+          double s3 = 0;
 #pragma unroll
           for (int a = 0; a < D; a++) {
-            lam[a] = (T)pts[le][qq][a];
-            s += lam[a];
+            pts[le][qq][a] = (T)pt[a];
+            s3 += pt[a];
           }
-          lam[D] = (T)1 - s;
+          pts[le][qq][D] = (T)(1.0 - s3);
+          pts[le][qq][D + 1] = (T)(w * G.meas);
+        }
+        __syncthreads();
+        // features of function i at the chunk's points (zero weight beyond np);
+        // only the parts the group's integrand kinds use
+        const bool need_dn = used & ((1 << XG_TERM_NGRADU_V) | (1 << XG_TERM_U_NGRADV));
+        const bool need_db = used & (1 << XG_TERM_CONV);
+#pragma unroll
+        for (int qq = 0; qq < CH; qq++) {
+          const T* lam = pts[le][qq];
           T phi, grad[D];
           eval_fn<D, T>(desc, lam, gT, phi, grad);
           T dn = 0, db = 0;
+          if (need_dn) {
 #pragma unroll
-          for (int k = 0; k < D; k++) {
-            dn += (T)G.nrm[k] * grad[k];
-            db += (T)Gq.b[k] * grad[k];
+            for (int k = 0; k < D; k++) dn += (T)G.nrm[k] * grad[k];
           }
-          const T w = (T)pts[le][qq][3];
+          if (need_db) {
+#pragma unroll
+            for (int k = 0; k < D; k++) db += (T)Gq.b[k] * grad[k];
+          }
+          const T w = pts[le][qq][D + 1];
           tr[le][qq][i][0] = phi;
 #pragma unroll
           for (int k = 0; k < D; k++) tr[le][qq][i][1 + k] = grad[k];
@@ -671,8 +674,11 @@ __global__ void __launch_bounds__(CutCfg<D, K, SYM, T>::NT) k_elmat_cut(
           if (used & (1 << XG_TERM_MASS)) A += cM * phi;
           if (used & (1 << XG_TERM_U_NGRADV)) A += cN2 * dn;
           te[le][qq][i][0] = w * A;
+          if (used & (1 << XG_TERM_LAPLACE)) {
+            const T wl = w * cL;
 #pragma unroll
-          for (int k = 0; k < D; k++) te[le][qq][i][1 + k] = (used & (1 << XG_TERM_LAPLACE)) ? w * cL * grad[k] : (T)0;
+            for (int k = 0; k < D; k++) te[le][qq][i][1 + k] = wl * grad[k];
+          }
           te[le][qq][i][1 + D] = (used & (1 << XG_TERM_NGRADU_V)) ? w * cN1 * phi : (T)0;
           te[le][qq][i][2 + D] = (used & (1 << XG_TERM_CONV)) ? w * cC * phi : (T)0;
         }
@@ -776,7 +782,7 @@ __global__ void __launch_bounds__(PaCfg<D, K>::NT) k_patch(
   using C = PaCfg<D, K>;
   constexpr int N = C::N, N2 = C::N2, E = C::E, FPB = C::FPB, CH = C::CH, NT = C::NT, NACC = C::NACC;
   __shared__ PaGeoS<D> geo[FPB];
-  __shared__ double pts[FPB][CH][2 * D + 1];
+  __shared__ T pts[FPB][CH][2 * D + 3];  // barycentrics in element 1 and 2, weight
   __shared__ T S[FPB][CH][N2];   // s_a = phi1_a / -phi2_(a-N)
   __shared__ T SW[FPB][CH][N2];  // weighted
   __shared__ unsigned char ep[E], eq[E];
@@ -865,28 +871,25 @@ __global__ void __launch_bounds__(PaCfg<D, K>::NT) k_patch(
               W = c_rules.w[off + m] * G.det2;
             }
           }
+          double s1 = 0, s2 = 0;
 #pragma unroll
           for (int k = 0; k < D; k++) {
-            pts[lf][qq][k] = x1[k];
-            pts[lf][qq][D + k] = x2[k];
+            pts[lf][qq][k] = (T)x1[k];
+            pts[lf][qq][D + 1 + k] = (T)x2[k];
+            s1 += x1[k];
+            s2 += x2[k];
           }
-          pts[lf][qq][2 * D] = W * G.coef[pp];
+          pts[lf][qq][D] = (T)(1.0 - s1);
+          pts[lf][qq][2 * D + 1] = (T)(1.0 - s2);
+          pts[lf][qq][2 * D + 2] = (T)(W * G.coef[pp]);
         }
         __syncthreads();
 #pragma unroll
         for (int qq = 0; qq < CH; qq++) {
-          T lam[D + 1];
-          T s = 0;
-#pragma unroll
-          for (int k = 0; k < D; k++) {
-            lam[k] = (T)pts[lf][qq][(mine1 ? 0 : D) + k];
-            s += lam[k];
-          }
-          lam[D] = (T)1 - s;
-          const T v = eval_fn_value<D, T>(desc, lam);
+          const T v = eval_fn_value<D, T>(desc, &pts[lf][qq][mine1 ? 0 : D + 1]);
           const T sv = mine1 ? v : -v;
           S[lf][qq][a] = sv;
-          SW[lf][qq][a] = (T)pts[lf][qq][2 * D] * sv;
+          SW[lf][qq][a] = pts[lf][qq][2 * D + 2] * sv;
         }
         __syncthreads();
         const int nch = min(CH, 2 * nq - q0);
@@ -949,6 +952,8 @@ struct ScatterArgs {
   const int32_t* dof_row;    // dof -> row (valid for active dofs)
   const int* counts;         // [3] = nrows
   int64_t cap_fa;
+  const int64_t* full_ptr;   // per dof: offset of its row in tmp_cols (full-pattern row sizes)
+  int32_t* tmp_cols;         // sorted column dofs of each active row, written by the count pass
   int el_sym;                // element matrices stored as packed upper triangles
   int hs;                    // hash slots per warp (pow2)
   int maxu;                  // distinct-column capacity per warp (pow2)
@@ -1121,18 +1126,33 @@ __device__ __forceinline__ int lower_bound_sm(const int* a, int n, int v) {
   return lo;
 }
 
+// Pass 1: the row's distinct columns, sorted, into tmp_cols at the row's
+// full-pattern offset, and the count.
 __global__ void __launch_bounds__(kRowWarps * 32) k_row_count(ScatterArgs A, int64_t* rowcnt, int* err) {
   extern __shared__ __align__(16) unsigned char sm_rows[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const RowSm S = row_sm(A, sm_rows + (size_t)warp * A.wbytes);
   const int nrows = A.counts[3];
   for (int row = blockIdx.x * kRowWarps + warp; row < nrows; row += gridDim.x * kRowWarps) {
-    const bool ok = row_columns(A, S, A.rows[row]);
-    const int u = hash_extract(A, S, false);
-    if (lane == 0) {
-      if (!ok || u > A.maxu) set_err(err, XG_ERR_CAPACITY);
-      rowcnt[row] = u;
+    const int r = A.rows[row];
+    const bool ok = row_columns(A, S, r);
+    int u = hash_extract(A, S, true);
+    const int64_t fo = A.full_ptr[r], fcap = A.full_ptr[r + 1] - fo;
+    if (!ok || u > A.maxu || u > fcap) {
+      if (lane == 0) {
+        set_err(err, XG_ERR_CAPACITY);
+        rowcnt[row] = 0;
+      }
+      continue;
     }
+    int m = 32;
+    while (m < u) m <<= 1;
+    for (int k = u + lane; k < m; k += 32) S.ucols[k] = 0x7fffffff;
+    __syncwarp();
+    warp_bitonic_sort(S.ucols, m);
+    for (int k = lane; k < u; k += 32) A.tmp_cols[fo + k] = S.ucols[k];
+    if (lane == 0) rowcnt[row] = u;
+    __syncwarp();
   }
 }
 
@@ -1150,19 +1170,18 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_row_fill(ScatterArgs A, cons
   const int gpb = A.stage / nd;  // groups per staged batch
   for (int row = blockIdx.x * kRowWarps + warp; row < nrows; row += gridDim.x * kRowWarps) {
     const int r = A.rows[row];
-    const bool ok = row_columns(A, S, r);
-    const int u = hash_extract(A, S, true);
     const int64_t rp = rowptr[row];
-    if (!ok || u > A.maxu || rp + u > cap_nnz) {
+    const int u = (int)(rowptr[row + 1] - rp);
+    if (u > A.maxu || rp + u > cap_nnz) {
       if (lane == 0) set_err(err, XG_ERR_CAPACITY);
       continue;
     }
-    int m = 32;
-    while (m < u) m <<= 1;
-    for (int k = u + lane; k < m; k += 32) S.ucols[k] = 0x7fffffff;
-    for (int k = lane; k < u; k += 32) S.acc[k] = 0.0;
+    const int64_t fo = A.full_ptr[r];
+    for (int k = lane; k < u; k += 32) {
+      S.ucols[k] = A.tmp_cols[fo + k];
+      S.acc[k] = 0.0;
+    }
     __syncwarp();
-    warp_bitonic_sort(S.ucols, m);
     const int a0 = A.adj_ptr[r], a1 = A.adj_ptr[r + 1];
     for (int c0 = a0; c0 < a1; c0 += kEnt) {
       const int na = min(kEnt, a1 - c0);
@@ -1281,6 +1300,8 @@ struct xg_form {
   int sc_hs = 0, sc_maxu = 0, sc_stage = 0, sc_wbytes = 0;
   size_t sc_smem = 0;
   int64_t full_nnz = 0;
+  int64_t* d_full_ptr = nullptr;
+  int32_t* d_tmp_cols = nullptr;
   int max_unique = 0;
   int grid_el_un = 0, grid_el_cut = 0, grid_fa = 0, grid_sc = 0;
   // CutFEM step state
@@ -1296,7 +1317,7 @@ struct xg_form {
 namespace {
 
 int form_free(xg_form* f) {
-  void* ptrs[] = {f->d_tabs, f->d_act_un, f->d_act_cut, f->d_act_fa, f->d_dof_bits, f->d_l_un, f->d_l_cut, f->d_l_fa,
+  void* ptrs[] = {f->d_full_ptr, f->d_tmp_cols, f->d_tabs, f->d_act_un, f->d_act_cut, f->d_act_fa, f->d_dof_bits, f->d_l_un, f->d_l_cut, f->d_l_fa,
                   f->d_el_slot, f->d_fa_slot, f->d_dof_row, f->d_rowcnt, f->d_counts, f->d_bsum, f->d_bsum64,
                   f->d_elmat, f->d_famat, f->d_err, f->d_dom, f->d_ratio, f->d_bits, f->d_fbits};
   for (void* p : ptrs) cudaFree(p);
@@ -1615,6 +1636,8 @@ ScatterArgs scatter_args(xg_form* f) {
   A.counts = f->d_counts;
   A.cap_fa = f->cap_fa;
   A.el_sym = f->el_sym;
+  A.full_ptr = f->d_full_ptr;
+  A.tmp_cols = f->d_tmp_cols;
   A.hs = f->sc_hs;
   A.maxu = f->sc_maxu;
   A.stage = f->sc_stage;
@@ -1624,7 +1647,7 @@ ScatterArgs scatter_args(xg_form* f) {
 
 // Exact size of the largest pattern any level set can produce on this mesh
 // (every element and interior facet active) and its widest row.
-void full_pattern_stats(const xg_form* f, int64_t* nnz, int* max_unique) {
+void full_pattern_stats(const xg_form* f, int64_t* nnz, int* max_unique, std::vector<int64_t>& row_ptr) {
   const xg_space* sp = f->space;
   const xg_mesh* m = f->mesh;
   const int nd = sp->nd, nfl = m->dim + 1, ne = m->ne;
@@ -1643,6 +1666,7 @@ void full_pattern_stats(const xg_form* f, int64_t* nnz, int* max_unique) {
   const int nth = std::max(1, std::min(16, (int)std::thread::hardware_concurrency()));
   std::vector<int64_t> part(nth, 0);
   std::vector<int> pmax(nth, 0);
+  row_ptr.assign(ndof + 1, 0);
   std::vector<std::thread> th;
   for (int t = 0; t < nth; t++)
     th.emplace_back([&, t]() {
@@ -1664,6 +1688,7 @@ void full_pattern_stats(const xg_form* f, int64_t* nnz, int* max_unique) {
         }
         std::sort(c.begin(), c.end());
         int u = (int)(std::unique(c.begin(), c.end()) - c.begin());
+        row_ptr[r + 1] = u;
         sum += u;
         mx = std::max(mx, u);
       }
@@ -1677,6 +1702,7 @@ void full_pattern_stats(const xg_form* f, int64_t* nnz, int* max_unique) {
     *nnz += part[t];
     *max_unique = std::max(*max_unique, pmax[t]);
   }
+  for (int64_t r = 0; r < ndof; r++) row_ptr[r + 1] += row_ptr[r];
 }
 
 }  // namespace
@@ -1715,7 +1741,8 @@ int xg_form_create(xg_space* space, const xg_term* terms, int32_t nterms, int pr
   f->nbsum = (int)((maxw + kCChunk - 1) / kCChunk) + 1;
   f->nbsum64 = (int)((space->ndof + kSChunk - 1) / kSChunk) + 1;
   // scatter buffers sized by the widest row of the full pattern
-  full_pattern_stats(f, &f->full_nnz, &f->max_unique);
+  std::vector<int64_t> full_ptr;
+  full_pattern_stats(f, &f->full_nnz, &f->max_unique, full_ptr);
   {
     int maxu = 32;
     while (maxu < f->max_unique) maxu <<= 1;
@@ -1738,6 +1765,10 @@ int xg_form_create(xg_space* space, const xg_term* terms, int32_t nterms, int pr
   e = e ? e : A((void**)&f->d_fa_slot, (size_t)m->nfacets * 4);
   e = e ? e : A((void**)&f->d_dof_row, (size_t)space->ndof * 4);
   e = e ? e : A((void**)&f->d_rowcnt, (size_t)space->ndof * 8);
+  e = e ? e : A((void**)&f->d_full_ptr, (size_t)(space->ndof + 1) * 8);
+  e = e ? e : A((void**)&f->d_tmp_cols, (size_t)f->full_nnz * 4);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(f->d_full_ptr, full_ptr.data(), (size_t)(space->ndof + 1) * 8, cudaMemcpyHostToDevice);
   e = e ? e : A((void**)&f->d_counts, 8 * sizeof(int));
   e = e ? e : A((void**)&f->d_bsum, (size_t)f->nbsum * 4);
   e = e ? e : A((void**)&f->d_bsum64, (size_t)f->nbsum64 * 8);
