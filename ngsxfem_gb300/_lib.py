@@ -24,7 +24,7 @@ EXPORTS = [
     "xg_space_create", "xg_space_destroy", "xg_space_info", "xg_space_element_dofs",
     "xg_interpolate_p1_perturb", "xg_cutinfo_update", "xg_mesh_check",
     "xg_facets_with_neighbor_types", "xg_elements_with_neighbor_facets",
-    "xg_cut_rules", "xg_base_rule_size", "xg_base_rule", "xg_integrate",
+    "xg_cut_rules", "xg_base_rule_size", "xg_base_rule", "xg_integrate", "xg_integrate_noalloc",
     "xg_form_create", "xg_form_destroy", "xg_form_set_defined_on", "xg_form_capacity",
     "xg_form_assemble", "xg_form_check", "xg_form_stage_events", "xg_cutfem_step", "xg_cutfem_marking",
 ]
@@ -95,6 +95,7 @@ def load():
         "xg_base_rule_size": (I, [I, I]),
         "xg_base_rule": (I, [I, I, P, P, I]),
         "xg_integrate": (I, [P, P, I, I, I, I, I, P, P, P]),
+        "xg_integrate_noalloc": (I, [P, P, I, I, I, I, I, P, P, P]),
         "xg_form_create": (I, [P, P, ctypes.c_int32, I, P]),
         "xg_form_destroy": (I, [P]),
         "xg_form_set_defined_on": (I, [P, ctypes.c_int32, P]),

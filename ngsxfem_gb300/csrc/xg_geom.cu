@@ -264,6 +264,40 @@ __global__ void k_sum_fixed(const double* v, int n, double* out) {
   }
 }
 
+// ---- allocation-free Integrate -----------------------------------------------------
+// Some callers cannot allocate device memory at the time they integrate: code
+// running while a stream is being captured into a CUDA graph (cudaMalloc is
+// not allowed there), real-time loops that forbid allocator calls, and hosts
+// whose device memory is owned by another allocator.  xg_integrate_noalloc
+// serves them: its per-block partial sums live in this file-scope array
+// instead of workspace allocated on first use.  Every GPU that loads the
+// library holds the array (128 KiB) until the process exits.
+constexpr int kNoAllocMaxBlocks = 16384;                      // partial sums held
+constexpr int kNoAllocElemsPerBlock = kIntThreads * 16;      // elements per block
+static __device__ __align__(256) double g_noalloc_partials[kNoAllocMaxBlocks];
+
+// Device address of g_noalloc_partials on the current device.  In host code the
+// array's name is only a host-side stand-in, so the address is looked up once
+// per device (with that device current) and cached.
+static int noalloc_partials(double** out) {
+  static std::mutex mu;
+  static std::vector<std::pair<int, double*>> cache;
+  int dev = 0;
+  XG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  for (auto& c : cache)
+    if (c.first == dev) {
+      *out = c.second;
+      return XG_OK;
+    }
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+  if (e != cudaSuccess) return cuda_fail(e, "xg_integrate_noalloc: cudaGetSymbolAddress");
+  cache.push_back({dev, (double*)p});
+  *out = (double*)p;
+  return XG_OK;
+}
+
 }  // namespace xg
 
 using namespace xg;
@@ -368,6 +402,32 @@ int xg_integrate(xg_mesh* m, const double* d_lset, int dt, int order, int ex, in
                                               d_defined_on, bs, m->d_err);
   k_sum_fixed<<<1, 32, 0, s>>>(bs, nb, d_result);
   return launch_check("k_integrate");
+}
+
+int xg_integrate_noalloc(xg_mesh* m, const double* d_lset, int dt, int order, int ex, int ey, int ez,
+                         const uint64_t* d_defined_on, double* d_result, void* stream) {
+  if (!m || !d_lset || !d_result || dt < 0 || dt > 2 || order < 0 || order > kMaxOrder || ex < 0 || ey < 0 || ez < 0)
+    return XG_ERR_ARG;
+  const int64_t nb64 = (m->ne + kNoAllocElemsPerBlock - 1) / kNoAllocElemsPerBlock;
+  if (nb64 > kNoAllocMaxBlocks) {
+    set_last_error("xg_integrate_noalloc: the mesh has " + std::to_string(m->ne) + " elements; the static scratch of " +
+                   std::to_string(kNoAllocMaxBlocks) + " partial sums covers at most " +
+                   std::to_string((int64_t)kNoAllocMaxBlocks * kNoAllocElemsPerBlock) + " elements");
+    return XG_ERR_CAPACITY;
+  }
+  const int nb = nb64 < 1 ? 1 : (int)nb64;
+  double* partials = nullptr;
+  int st = noalloc_partials(&partials);
+  if (st) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (m->dim == 2)
+    k_integrate<2><<<nb, kIntThreads, 0, s>>>(m->ne, m->d_elv, m->d_xyz, m->nv, d_lset, dt, order, ex, ey, ez,
+                                              d_defined_on, partials, m->d_err);
+  else
+    k_integrate<3><<<nb, kIntThreads, 0, s>>>(m->ne, m->d_elv, m->d_xyz, m->nv, d_lset, dt, order, ex, ey, ez,
+                                              d_defined_on, partials, m->d_err);
+  k_sum_fixed<<<1, 32, 0, s>>>(partials, nb, d_result);
+  return launch_check("xg_integrate_noalloc");
 }
 
 }  // extern "C"
