@@ -69,7 +69,8 @@ typedef enum {
   XG_TERM_NGRADU_V = 2,   /* c * (n . grad u) * v           */
   XG_TERM_U_NGRADV = 3,   /* c * u * (n . grad v)           */
   XG_TERM_CONV = 4,       /* c * (b . grad u) * v           */
-  XG_TERM_GHOST_MASS = 5  /* c * (u - u') * (v - v') on a facet patch (dFacetPatch) */
+  XG_TERM_GHOST_MASS = 5, /* c * (u - u') * (v - v') on a facet patch (dFacetPatch) */
+  XG_TERM_DT_U_V = 6      /* space-time: c * v * d/dtau u (dtref), space-time forms only */
 } xg_term_kind;
 
 typedef enum { XG_PREC_FP64 = 0, XG_PREC_MIXED = 1 } xg_precision;
@@ -225,6 +226,45 @@ int xg_form_check(xg_form* form);
  *   [6] row pattern counted, [7] values scattered.
  * n = 0 switches it off.  The events are the caller's. */
 int xg_form_stage_events(xg_form* form, void* const* events, int n);
+
+/* ---- space-time (cutint/spacetimecutrule.cpp, spacetime/) ------------------------ */
+/* Space-time level sets are P1 in space and P_kt in time on the reference slab
+ * tau in [0,1] (nodal Gauss-Lobatto time basis: kt=1 nodes {0,1}, kt=2 nodes
+ * {0,1/2,1}), stored time-major: d_lset_st[i*nv + v] = value of vertex v at
+ * time node i.  Space-time dofs: (time dof i, spatial dof j) -> i*ndof_space + j. */
+int xg_space_create_st(xg_mesh* mesh, int order, int order_time, xg_space** out);
+/* out: [ndof, ndof_per_element, order, order_time, ndof_space, ndof_per_element_space] */
+int xg_space_info_st(const xg_space* space, int64_t* h_out6);
+/* CutInformation::Update(lset_st, time_order=0) (xfem/cutinfo.cpp:61-132 with
+ * SpaceTimeCutIntegrationRule of orders 0/0): cut ratios, domain types and the
+ * combined-domain bitsets of the space-time prisms. */
+int xg_cutinfo_update_st(xg_mesh* mesh, const double* d_lset_st, int kt_lset, uint8_t* d_dom, double* d_cut_ratio,
+                         uint64_t* d_bits, void* stream);
+/* SpaceTimeCutIntegrationRule (cutint/spacetimecutrule.cpp:106-244): points get
+ * 4 doubles (xi, eta, zeta, tau); weights carry w * w_t * (t1 - t0).
+ * order_space -1 selects 5 as the reference does. */
+int xg_st_cut_rules(xg_mesh* mesh, const double* d_lset_st, int kt_lset, const int32_t* d_elems, int32_t n, int dt,
+                    int order_space, int order_time, int32_t max_pts, int32_t* d_counts, double* d_pts, double* d_wts,
+                    void* stream);
+/* A space-time integrator: dCut(lset_st, domain, time_order=...) over the slab
+ * (tref < 0) or dCut(lset_trace, domain, tref=...) at a fixed reference time,
+ * and dFacetPatch(time_order=...) patch terms (spatial patch rule x time rule).
+ * The convection field may depend on time:
+ *   b(t) = base.b + bc cos(omega t) + bs sin(omega t),  t = t0 + dt * tau. */
+typedef struct {
+  xg_term base;
+  double tref;
+  double bc[3], bs[3];
+  double omega, t0, dt;
+} xg_st_term;
+/* kt_lset: time order of the level set; order_time: time rule order (<= 7). */
+int xg_st_form_create(xg_space* st_space, int kt_lset, int order_time, const xg_st_term* terms, int32_t nterms,
+                      int precision, xg_form** out);
+/* The space-time CutFEM step of demos/spacetime/spacetimeDG_unfitted.py:143-185:
+ * space-time CutInfo, ghost facets (HASNEG, IF), element matrices of the
+ * slab / fixed-time terms on HASNEG (IF terms on IF, POS terms on HASPOS) and
+ * the patch terms on the ghost facets, scattered into `out`. */
+int xg_st_cutfem_step(xg_form* form, const double* d_lset_st, xg_csr* out, void* stream);
 
 /* ---- the CutFEM step (demos/fictdom.py:95-133) ----------------------------- */
 /* One call runs the whole cut-assembly step on `stream`: CutInfo marking,

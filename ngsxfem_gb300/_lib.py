@@ -27,6 +27,8 @@ EXPORTS = [
     "xg_cut_rules", "xg_base_rule_size", "xg_base_rule", "xg_integrate", "xg_integrate_noalloc",
     "xg_form_create", "xg_form_destroy", "xg_form_set_defined_on", "xg_form_capacity",
     "xg_form_assemble", "xg_form_check", "xg_form_stage_events", "xg_cutfem_step", "xg_cutfem_marking",
+    "xg_space_create_st", "xg_space_info_st", "xg_cutinfo_update_st", "xg_st_cut_rules", "xg_st_form_create",
+    "xg_st_cutfem_step",
 ]
 
 
@@ -45,6 +47,18 @@ class Term(ctypes.Structure):
         ("coef", ctypes.c_double),
         ("b", ctypes.c_double * 3),
         ("d_defined_on", ctypes.c_void_p),
+    ]
+
+
+class StTerm(ctypes.Structure):
+    _fields_ = [
+        ("base", Term),
+        ("tref", ctypes.c_double),
+        ("bc", ctypes.c_double * 3),
+        ("bs", ctypes.c_double * 3),
+        ("omega", ctypes.c_double),
+        ("t0", ctypes.c_double),
+        ("dt", ctypes.c_double),
     ]
 
 
@@ -105,6 +119,12 @@ def load():
         "xg_form_stage_events": (I, [P, P, I]),
         "xg_cutfem_step": (I, [P, P, P, P]),
         "xg_cutfem_marking": (I, [P, P, P, P, P]),
+        "xg_space_create_st": (I, [P, I, I, P]),
+        "xg_space_info_st": (I, [P, P]),
+        "xg_cutinfo_update_st": (I, [P, P, I, P, P, P, P]),
+        "xg_st_cut_rules": (I, [P, P, I, P, ctypes.c_int32, I, I, I, ctypes.c_int32, P, P, P, P]),
+        "xg_st_form_create": (I, [P, I, I, P, ctypes.c_int32, I, P]),
+        "xg_st_cutfem_step": (I, [P, P, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

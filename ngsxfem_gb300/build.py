@@ -24,6 +24,7 @@ UNITS = [
     ("xg_host.cpp", []),
     ("xg_geom.cu", ["-fmad=false"]),
     ("xg_asm.cu", []),
+    ("xg_st.cu", []),
 ]
 
 

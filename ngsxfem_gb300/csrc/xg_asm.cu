@@ -241,6 +241,17 @@ __global__ void k_active_elements(int ne, const uint8_t* __restrict__ dom, FormD
   }
 }
 
+// space-time forms: an element is active if a volume group contains it
+__global__ void k_active_st(int ne, StFormDesc form, uint32_t* bits, int64_t nw32) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  bool act = false;
+  if (e < ne)
+    for (int g = 0; g < form.ngroups; g++)
+      if (!form.g[g].defined_on || tbit(form.g[g].defined_on, e)) act = true;
+  const unsigned m = __ballot_sync(0xffffffffu, act);
+  if ((threadIdx.x & 31) == 0 && (e >> 5) < nw32) bits[e >> 5] = m;
+}
+
 __global__ void k_active_facets(int64_t nf, const int32_t* __restrict__ fel, FormDesc form, uint32_t* bits,
                                 int64_t nw32) {
   const int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -287,30 +298,6 @@ __global__ void k_mark_dofs(int ne, int nd, const int32_t* __restrict__ el_dofs,
 //    forms;
 //  * matrices of symmetric forms are stored as packed upper triangles.
 // ============================================================================
-// FP64 accumulation for the plain path; FP32 with Kahan compensation per
-// entry for the mixed path.
-template <typename T>
-struct Acc;
-template <>
-struct Acc<double> {
-  double s;
-  __device__ __forceinline__ void init() { s = 0.0; }
-  __device__ __forceinline__ void add(double v) { s += v; }
-  __device__ __forceinline__ double get() const { return s; }
-};
-template <>
-struct Acc<float> {
-  float s, c;
-  __device__ __forceinline__ void init() { s = 0.f; c = 0.f; }
-  __device__ __forceinline__ void add(float v) {
-    float y = v - c;
-    float t = s + y;
-    c = (t - s) - y;
-    s = t;
-  }
-  __device__ __forceinline__ float get() const { return s; }
-};
-
 __host__ __device__ constexpr int tri_size(int n) { return n * (n + 1) / 2; }
 __host__ __device__ inline int tri_index(int p, int q, int n) { return p * n - p * (p - 1) / 2 + (q - p); }
 
@@ -955,6 +942,8 @@ struct ScatterArgs {
   const int64_t* full_ptr;   // per dof: offset of its row in tmp_cols (full-pattern row sizes)
   int32_t* tmp_cols;         // sorted column dofs of each active row, written by the count pass
   int el_sym;                // element matrices stored as packed upper triangles
+  int nds, kt1;              // spatial dofs per element, time dofs (1 for spatial forms)
+  double mt[9];              // time mass kt1 x kt1: patch value = mt[it][is] * spatial patch value
   int hs;                    // hash slots per warp (pow2)
   int maxu;                  // distinct-column capacity per warp (pow2)
   int stage;                 // staged (pos, value) pairs per warp
@@ -1166,7 +1155,7 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_row_fill(ScatterArgs A, cons
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const RowSm S = row_sm(A, sm_rows + (size_t)warp * A.wbytes);
   const int nrows = A.counts[3];
-  const int nd = A.nd, n2 = 2 * nd;
+  const int nd = A.nd;
   const int gpb = A.stage / nd;  // groups per staged batch
   for (int row = blockIdx.x * kRowWarps + warp; row < nrows; row += gridDim.x * kRowWarps) {
     const int r = A.rows[row];
@@ -1227,12 +1216,16 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_row_fill(ScatterArgs A, cons
             v = A.el_sym ? (double)elmat[eo * tri_size(nd) + (i <= j ? tri_index(i, j, nd) : tri_index(j, i, nd))]
                          : (double)elmat[(eo * nd + i) * nd + j];
           } else {
+            // patch matrices are spatial: local space-time index = time dof * nds + spatial dof
             const int lf = (kind - 1) >> 1, h = (kind - 1) & 1;
             const int first = S.ent_first[a * 4 + lf], nb = S.ent_nb[a * 4 + lf], fs = S.ent_fs[a * 4 + lf];
-            const int prow = first ? i : nd + i, pcol = h * nd + j;
+            const int nds = A.nds, n2s = 2 * nds;
+            const int ir = i / nds, jr = i % nds, ic = j / nds, jc = j % nds;
+            const int prow = first ? jr : nds + jr, pcol = h * nds + jc;
             colel = (h == 0) == (first != 0) ? e : nb;
-            v = fs < A.cap_fa ? (double)famat[(int64_t)fs * tri_size(n2) +
-                                              (prow <= pcol ? tri_index(prow, pcol, n2) : tri_index(pcol, prow, n2))]
+            v = fs < A.cap_fa ? A.mt[ir * A.kt1 + ic] *
+                                    (double)famat[(int64_t)fs * tri_size(n2s) +
+                                                  (prow <= pcol ? tri_index(prow, pcol, n2s) : tri_index(pcol, prow, n2s))]
                               : 0.0;
           }
           const int c = A.el_dofs[(int64_t)colel * nd + j];
@@ -1312,9 +1305,16 @@ struct xg_form {
   bool has_patch = false;
   cudaEvent_t ev[8] = {};
   bool use_ev = false;
+  // space-time forms
+  bool st = false;
+  StFormDesc stdesc = {};
+  std::vector<xg_st_term> st_terms;
+  double mt[9] = {1, 0, 0, 0, 0, 0, 0, 0, 0};  // time mass of the time rule (patch factor)
 };
 
 namespace {
+
+int form_workspace(xg_form* f);
 
 int form_free(xg_form* f) {
   void* ptrs[] = {f->d_full_ptr, f->d_tmp_cols, f->d_tabs, f->d_act_un, f->d_act_cut, f->d_act_fa, f->d_dof_bits, f->d_l_un, f->d_l_cut, f->d_l_fa,
@@ -1636,6 +1636,9 @@ ScatterArgs scatter_args(xg_form* f) {
   A.counts = f->d_counts;
   A.cap_fa = f->cap_fa;
   A.el_sym = f->el_sym;
+  A.nds = sp->nds;
+  A.kt1 = sp->kt >= 0 ? sp->kt + 1 : 1;
+  for (int k = 0; k < 9; k++) A.mt[k] = f->mt[k];
   A.full_ptr = f->d_full_ptr;
   A.tmp_cols = f->d_tmp_cols;
   A.hs = f->sc_hs;
@@ -1644,6 +1647,40 @@ ScatterArgs scatter_args(xg_form* f) {
   A.wbytes = f->sc_wbytes;
   return A;
 }
+
+// active dofs -> rows, then the two scatter passes
+int scatter_phase(xg_form* f, xg_csr* out, cudaStream_t s) {
+  xg_mesh* m = f->mesh;
+  xg_space* sp = f->space;
+  int st;
+  // 3. active dofs -> rows
+  XG_CUDA(cudaMemsetAsync(f->d_dof_bits, 0, f->nw32_dof * 4, s));
+  k_mark_dofs<<<152 * 8, 256, 0, s>>>(m->ne, sp->nd, sp->d_el_dofs, f->d_l_un, f->d_l_cut, f->d_l_fa, f->d_counts,
+                                      m->nfacets, m->d_facet_els, f->d_dof_bits);
+  if ((st = compact(f, f->d_dof_bits, f->nw32_dof, out->d_row_dof, f->d_dof_row, f->d_counts + 3, s))) return st;
+  // 4. pattern and values
+  ScatterArgs A = scatter_args(f);
+  A.rows = out->d_row_dof;
+  k_row_count<<<f->grid_sc, kRowWarps * 32, f->sc_smem, s>>>(A, f->d_rowcnt, f->d_err);
+  const int nb64 = (int)((sp->ndof + kSChunk - 1) / kSChunk);
+  k_sum64_blocks<<<nb64, kSThreads, 0, s>>>(f->d_rowcnt, f->d_counts + 3, f->d_bsum64);
+  k_scan64_small<<<1, 1024, 0, s>>>(f->d_bsum64, nb64);
+  k_scan64_apply<<<nb64, kSThreads, 0, s>>>(f->d_rowcnt, f->d_counts + 3, f->d_bsum64, out->d_rowptr, out->d_counts,
+                                            out->cap_nnz, f->d_err);
+  if (f->use_ev) cudaEventRecord(f->ev[6], s);
+  if (f->precision == XG_PREC_FP64)
+    k_row_fill<double><<<f->grid_sc, kRowWarps * 32, f->sc_smem, s>>>(A, (const double*)f->d_elmat,
+                                                                    (const double*)f->d_famat, out->d_rowptr,
+                                                                    out->d_cols, out->d_vals, out->cap_nnz, f->d_err);
+  else
+    k_row_fill<float><<<f->grid_sc, kRowWarps * 32, f->sc_smem, s>>>(A, (const float*)f->d_elmat,
+                                                                   (const float*)f->d_famat, out->d_rowptr,
+                                                                   out->d_cols, out->d_vals, out->cap_nnz, f->d_err);
+  if (f->use_ev) cudaEventRecord(f->ev[7], s);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? XG_OK : cuda_fail(e, "xg_form_assemble");
+}
+
 
 // Exact size of the largest pattern any level set can produce on this mesh
 // (every element and interior facet active) and its widest row.
@@ -1715,6 +1752,10 @@ int xg_form_create(xg_space* space, const xg_term* terms, int32_t nterms, int pr
     set_last_error("xg_form_create: bad arguments");
     return XG_ERR_ARG;
   }
+  if (space->kt >= 0) {
+    set_last_error("xg_form_create: space-time spaces take xg_st_form_create");
+    return XG_ERR_ARG;
+  }
   *out = nullptr;
   auto* f = new xg_form();
   f->space = space;
@@ -1723,10 +1764,23 @@ int xg_form_create(xg_space* space, const xg_term* terms, int32_t nterms, int pr
   f->terms.assign(terms, terms + nterms);
   int st = build_desc(f);
   if (!st) st = upload_tables(f);
+  if (!st) st = form_workspace(f);
   if (st) {
     form_free(f);
     return st;
   }
+  *out = f;
+  return XG_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// device workspace of a form, sized for the whole mesh
+int form_workspace(xg_form* f) {
+  xg_space* space = f->space;
+  const int precision = f->precision;
   xg_mesh* m = f->mesh;
   const int nd = space->nd;
   const size_t esz = precision == XG_PREC_FP64 ? sizeof(double) : sizeof(float);
@@ -1735,7 +1789,8 @@ int xg_form_create(xg_space* space, const xg_term* terms, int32_t nterms, int pr
   f->nw32_dof = 2 * ((space->ndof + 63) / 64);
   f->cap_el = m->ne;
   // facet-patch workspace: all facets when small, else a quarter of them
-  const size_t fa_bytes = (size_t)m->nfacets * tri_size(2 * nd) * esz;
+  const int nds = space->nds;  // patch matrices are spatial (space-time forms apply the time factor in the scatter)
+  const size_t fa_bytes = (size_t)m->nfacets * tri_size(2 * nds) * esz;
   f->cap_fa = fa_bytes <= ((size_t)4 << 30) ? m->nfacets : std::max<int64_t>(m->nfacets / 4, 1);
   int64_t maxw = std::max(f->nw32_el, std::max(f->nw32_fa, f->nw32_dof));
   f->nbsum = (int)((maxw + kCChunk - 1) / kCChunk) + 1;
@@ -1773,7 +1828,7 @@ int xg_form_create(xg_space* space, const xg_term* terms, int32_t nterms, int pr
   e = e ? e : A((void**)&f->d_bsum, (size_t)f->nbsum * 4);
   e = e ? e : A((void**)&f->d_bsum64, (size_t)f->nbsum64 * 8);
   e = e ? e : A(&f->d_elmat, (size_t)f->cap_el * nd * nd * esz);
-  e = e ? e : A(&f->d_famat, f->has_patch ? (size_t)f->cap_fa * tri_size(2 * nd) * esz : 16);
+  e = e ? e : A(&f->d_famat, f->has_patch ? (size_t)f->cap_fa * tri_size(2 * nds) * esz : 16);
   e = e ? e : A((void**)&f->d_err, sizeof(int));
   e = e ? e : A((void**)&f->d_dom, (size_t)m->ne);
   e = e ? e : A((void**)&f->d_ratio, (size_t)m->ne * 8);
@@ -1781,10 +1836,7 @@ int xg_form_create(xg_space* space, const xg_term* terms, int32_t nterms, int pr
   e = e ? e : A((void**)&f->d_fbits, (size_t)(f->nw32_fa / 2) * 8);
   if (e == cudaSuccess) e = cudaMemset(f->d_err, 0, sizeof(int));
   if (e == cudaSuccess) e = cudaMemset(f->d_counts, 0, 8 * sizeof(int));
-  if (e != cudaSuccess) {
-    form_free(f);
-    return cuda_fail(e, "xg_form_create");
-  }
+  if (e != cudaSuccess) return cuda_fail(e, "xg_form_create");
   {
     // the attribute is an upper bound shared by all forms: only ever raise it
     static std::mutex mu;
@@ -1794,7 +1846,6 @@ int xg_form_create(xg_space* space, const xg_term* terms, int32_t nterms, int pr
       if (cudaFuncSetAttribute(k_row_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->sc_smem) ||
           cudaFuncSetAttribute(k_row_fill<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->sc_smem) ||
           cudaFuncSetAttribute(k_row_fill<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->sc_smem)) {
-        form_free(f);
         set_last_error("xg_form_create: scatter shared memory too large for this mesh");
         return XG_ERR_CAPACITY;
       }
@@ -1802,9 +1853,12 @@ int xg_form_create(xg_space* space, const xg_term* terms, int32_t nterms, int pr
     }
   }
   f->grid_sc = grid_for(k_row_count, kRowWarps * 32, f->sc_smem);
-  *out = f;
   return XG_OK;
 }
+
+}  // namespace
+
+extern "C" {
 
 int xg_form_destroy(xg_form* f) {
   if (!f) return XG_OK;
@@ -1872,32 +1926,7 @@ int xg_form_assemble(xg_form* f, const double* d_lset, const uint8_t* d_dom, xg_
     if (f->has_patch && (st = dispatch_patch<float>(f, s))) return st;
   }
   if (f->use_ev) cudaEventRecord(f->ev[5], s);
-  // 3. active dofs -> rows
-  XG_CUDA(cudaMemsetAsync(f->d_dof_bits, 0, f->nw32_dof * 4, s));
-  k_mark_dofs<<<152 * 8, 256, 0, s>>>(m->ne, sp->nd, sp->d_el_dofs, f->d_l_un, f->d_l_cut, f->d_l_fa, f->d_counts,
-                                      m->nfacets, m->d_facet_els, f->d_dof_bits);
-  if ((st = compact(f, f->d_dof_bits, f->nw32_dof, out->d_row_dof, f->d_dof_row, f->d_counts + 3, s))) return st;
-  // 4. pattern and values
-  ScatterArgs A = scatter_args(f);
-  A.rows = out->d_row_dof;
-  k_row_count<<<f->grid_sc, kRowWarps * 32, f->sc_smem, s>>>(A, f->d_rowcnt, f->d_err);
-  const int nb64 = (int)((sp->ndof + kSChunk - 1) / kSChunk);
-  k_sum64_blocks<<<nb64, kSThreads, 0, s>>>(f->d_rowcnt, f->d_counts + 3, f->d_bsum64);
-  k_scan64_small<<<1, 1024, 0, s>>>(f->d_bsum64, nb64);
-  k_scan64_apply<<<nb64, kSThreads, 0, s>>>(f->d_rowcnt, f->d_counts + 3, f->d_bsum64, out->d_rowptr, out->d_counts,
-                                            out->cap_nnz, f->d_err);
-  if (f->use_ev) cudaEventRecord(f->ev[6], s);
-  if (f->precision == XG_PREC_FP64)
-    k_row_fill<double><<<f->grid_sc, kRowWarps * 32, f->sc_smem, s>>>(A, (const double*)f->d_elmat,
-                                                                    (const double*)f->d_famat, out->d_rowptr,
-                                                                    out->d_cols, out->d_vals, out->cap_nnz, f->d_err);
-  else
-    k_row_fill<float><<<f->grid_sc, kRowWarps * 32, f->sc_smem, s>>>(A, (const float*)f->d_elmat,
-                                                                   (const float*)f->d_famat, out->d_rowptr,
-                                                                   out->d_cols, out->d_vals, out->cap_nnz, f->d_err);
-  if (f->use_ev) cudaEventRecord(f->ev[7], s);
-  cudaError_t e = cudaGetLastError();
-  return e == cudaSuccess ? XG_OK : cuda_fail(e, "xg_form_assemble");
+  return scatter_phase(f, out, s);
 }
 
 int xg_cutfem_step(xg_form* f, const double* d_lset, xg_csr* out, void* stream) {
@@ -1932,6 +1961,183 @@ int xg_form_stage_events(xg_form* f, void* const* events, int n) {
   f->use_ev = n == 8;
   for (int i = 0; i < 8; i++) f->ev[i] = n == 8 ? (cudaEvent_t)events[i] : nullptr;
   return XG_OK;
+}
+
+int xg_st_form_create(xg_space* space, int kt_lset, int order_time, const xg_st_term* terms, int32_t nterms,
+                      int precision, xg_form** out) {
+  if (!space || !out || space->kt < 1 || space->kt > 2 || space->order > 2 || kt_lset < 0 || kt_lset > 2 ||
+      order_time < 0 || order_time > 7 || (nterms > 0 && !terms) || nterms < 0 ||
+      (precision != XG_PREC_FP64 && precision != XG_PREC_MIXED)) {
+    set_last_error("xg_st_form_create: space-time space of space order 1..2 and time order 1..2, level set time "
+                   "order 0..2, time rule order 0..7");
+    return XG_ERR_ARG;
+  }
+  *out = nullptr;
+  auto* f = new xg_form();
+  f->space = space;
+  f->mesh = space->mesh;
+  f->precision = precision;
+  f->st = true;
+  f->st_terms.assign(terms, terms + nterms);
+  std::memset(&f->desc, 0, sizeof(f->desc));
+  StFormDesc& d = f->stdesc;
+  std::memset(&d, 0, sizeof(d));
+  d.kt_l = kt_lset;
+  d.order_time = order_time;
+  const int k = space->order;
+  for (int t = 0; t < nterms; t++) {
+    const xg_st_term& T = terms[t];
+    const xg_term& B = T.base;
+    if (B.kind == XG_TERM_GHOST_MASS) {
+      if (f->desc.npatch >= kMaxPatch) {
+        form_free(f);
+        return XG_ERR_UNSUPPORTED;
+      }
+      PatchDesc& P = f->desc.p[f->desc.npatch++];
+      P.order = B.order >= 0 ? B.order : 2 * k;
+      P.defined_on = B.d_defined_on;
+      P.c = B.coef;
+      P.hpow = B.hpow;
+      f->has_patch = true;
+      continue;
+    }
+    if (!(B.kind == XG_TERM_MASS || B.kind == XG_TERM_LAPLACE || B.kind == XG_TERM_CONV || B.kind == XG_TERM_DT_U_V) ||
+        B.domain < 0 || B.domain > 2) {
+      form_free(f);
+      set_last_error("xg_st_form_create: space-time terms are MASS, LAPLACE, CONV, DT_U_V and GHOST_MASS");
+      return XG_ERR_UNSUPPORTED;
+    }
+    const int order = B.order >= 0 ? B.order
+                                   : (B.kind == XG_TERM_LAPLACE ? 2 * k - 2 : (B.kind == XG_TERM_CONV ? 2 * k - 1 : 2 * k));
+    if (order > kMaxOrder) {
+      form_free(f);
+      return XG_ERR_UNSUPPORTED;
+    }
+    int g = -1;
+    for (int q = 0; q < d.ngroups; q++) {
+      const StGroupDesc& G = d.g[q];
+      bool same_conv = B.kind != XG_TERM_CONV || !(G.used & (1 << XG_TERM_CONV)) ||
+                       (std::memcmp(G.b, B.b, sizeof(G.b)) == 0 && std::memcmp(G.bc, T.bc, sizeof(G.bc)) == 0 &&
+                        std::memcmp(G.bs, T.bs, sizeof(G.bs)) == 0 && G.omega == T.omega && G.t0 == T.t0 &&
+                        G.dt == T.dt);
+      if (G.domain == B.domain && G.order == order && G.defined_on == B.d_defined_on &&
+          (G.tref < 0) == (T.tref < 0) && (T.tref < 0 || G.tref == T.tref) && same_conv && !(G.used & (1 << B.kind)))
+        g = q;
+    }
+    if (g < 0) {
+      if (d.ngroups >= kMaxGroups) {
+        form_free(f);
+        set_last_error("xg_st_form_create: too many term groups");
+        return XG_ERR_UNSUPPORTED;
+      }
+      g = d.ngroups++;
+      d.g[g].domain = B.domain;
+      d.g[g].order = order;
+      d.g[g].defined_on = B.d_defined_on;
+      d.g[g].tref = T.tref < 0 ? -1.0 : T.tref;
+    }
+    StGroupDesc& G = d.g[g];
+    G.c[B.kind] = B.coef;
+    G.hpow[B.kind] = B.hpow;
+    G.used |= 1 << B.kind;
+    if (B.kind == XG_TERM_CONV) {
+      for (int c = 0; c < 3; c++) {
+        G.b[c] = B.b[c];
+        G.bc[c] = T.bc[c];
+        G.bs[c] = T.bs[c];
+      }
+      G.omega = T.omega;
+      G.t0 = T.t0;
+      G.dt = T.dt;
+    }
+  }
+  // time mass of the time rule: factor of the space-time facet patches
+  {
+    const RuleTable& R = host_rules();
+    const int p = clamp_order(order_time), kt = space->kt;
+    for (int a = 0; a < 9; a++) f->mt[a] = 0.0;
+    for (int q = 0; q < R.cnt[1][p]; q++) {
+      double psi[3], dpsi[3];
+      time_basis<double>(kt, R.x[R.off[1][p] + q][0], psi, dpsi);
+      for (int a = 0; a <= kt; a++)
+        for (int b = 0; b <= kt; b++) f->mt[a * (kt + 1) + b] += R.w[R.off[1][p] + q] * psi[a] * psi[b];
+    }
+  }
+  f->el_sym = 0;
+  int st = form_workspace(f);
+  if (st) {
+    form_free(f);
+    return st;
+  }
+  *out = f;
+  return XG_OK;
+}
+
+int xg_st_cutfem_step(xg_form* f, const double* d_lset_st, xg_csr* out, void* stream) {
+  if (!f || !f->st || !d_lset_st || !out || !out->d_row_dof || !out->d_rowptr || !out->d_cols || !out->d_vals ||
+      !out->d_counts)
+    return XG_ERR_ARG;
+  if (out->cap_rows < f->space->ndof) return XG_ERR_CAPACITY;
+  cudaStream_t s = (cudaStream_t)stream;
+  xg_mesh* m = f->mesh;
+  if (f->use_ev) cudaEventRecord(f->ev[0], s);
+  int st = xg_cutinfo_update_st(m, d_lset_st, f->stdesc.kt_l, f->d_dom, f->d_ratio, f->d_bits, stream);
+  if (st) return st;
+  const int64_t nw = f->nw32_el / 2;
+  const uint64_t* hasneg = f->d_bits + XG_CDOM_HASNEG * nw;
+  const uint64_t* ifb = f->d_bits + XG_CDOM_IF * nw;
+  const uint64_t* haspos = f->d_bits + XG_CDOM_HASPOS * nw;
+  if (f->has_patch && (st = xg_facets_with_neighbor_types(m, hasneg, ifb, 1, 1, 1, f->d_fbits, stream))) return st;
+  StFormDesc d = f->stdesc;
+  for (int q = 0; q < d.ngroups; q++)
+    d.g[q].defined_on = d.g[q].domain == XG_NEG ? hasneg : (d.g[q].domain == XG_IF ? ifb : haspos);
+  FormDesc pd = f->desc;
+  for (int p = 0; p < pd.npatch; p++) pd.p[p].defined_on = f->d_fbits;
+  if (f->use_ev) cudaEventRecord(f->ev[1], s);
+  // work lists
+  k_active_st<<<(unsigned)((f->nw32_el * 32 + 255) / 256), 256, 0, s>>>(m->ne, d, f->d_act_un, f->nw32_el);
+  XG_CUDA(cudaMemsetAsync(f->d_act_cut, 0, f->nw32_el * 4, s));
+  if ((st = compact(f, f->d_act_un, f->nw32_el, f->d_l_un, f->d_el_slot, f->d_counts + 0, s))) return st;
+  XG_CUDA(cudaMemsetAsync(f->d_counts + 1, 0, sizeof(int), s));
+  FormDesc saved = f->desc;
+  f->desc = pd;
+  if (f->has_patch) {
+    k_active_facets<<<(unsigned)((f->nw32_fa * 32 + 255) / 256), 256, 0, s>>>(m->nfacets, m->d_facet_els, f->desc,
+                                                                              f->d_act_fa, f->nw32_fa);
+    st = compact(f, f->d_act_fa, f->nw32_fa, f->d_l_fa, f->d_fa_slot, f->d_counts + 2, s);
+  } else {
+    cudaMemsetAsync(f->d_act_fa, 0, f->nw32_fa * 4, s);
+    cudaMemsetAsync(f->d_counts + 2, 0, sizeof(int), s);
+  }
+  if (f->use_ev) cudaEventRecord(f->ev[2], s);
+  if (!st) {
+    StLaunch L;
+    L.D = m->dim;
+    L.K = f->space->order;
+    L.KT = f->space->kt;
+    L.precision = f->precision;
+    L.ne = m->ne;
+    L.nv = m->nv;
+    L.elv = m->d_elv;
+    L.xyz = m->d_xyz;
+    L.lset_st = d_lset_st;
+    L.desc = d;
+    L.list = f->d_l_un;
+    L.count = f->d_counts + 0;
+    L.elmat = f->d_elmat;
+    L.err = f->d_err;
+    st = launch_st_elmat(L, s);
+  }
+  if (f->use_ev) {
+    cudaEventRecord(f->ev[3], s);
+    cudaEventRecord(f->ev[4], s);
+  }
+  if (!st && f->has_patch)
+    st = f->precision == XG_PREC_FP64 ? dispatch_patch<double>(f, s) : dispatch_patch<float>(f, s);
+  f->desc = saved;
+  if (st) return st;
+  if (f->use_ev) cudaEventRecord(f->ev[5], s);
+  return scatter_phase(f, out, s);
 }
 
 int xg_cutfem_marking(xg_form* f, const uint8_t** d_dom, const double** d_ratio, const uint64_t** d_bits,

@@ -94,4 +94,28 @@ __host__ __device__ __forceinline__ T eval_fn_value(int desc, const T* lam) {
   return lam[a] * lam[b] * lam[c];
 }
 
+// FP64 accumulation for the plain path; FP32 with Kahan compensation per
+// entry for the mixed path.
+template <typename T>
+struct Acc;
+template <>
+struct Acc<double> {
+  double s;
+  __device__ __forceinline__ void init() { s = 0.0; }
+  __device__ __forceinline__ void add(double v) { s += v; }
+  __device__ __forceinline__ double get() const { return s; }
+};
+template <>
+struct Acc<float> {
+  float s, c;
+  __device__ __forceinline__ void init() { s = 0.f; c = 0.f; }
+  __device__ __forceinline__ void add(float v) {
+    float y = v - c;
+    float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ __forceinline__ float get() const { return s; }
+};
+
 }  // namespace xg

@@ -246,3 +246,114 @@ __device__ __forceinline__ void plain_point(const Sub& s, int np, const double* 
 }
 
 }  // namespace xg
+
+namespace xg {
+
+// ---- space-time ------------------------------------------------------------------
+// Nodal time basis on Gauss-Lobatto points (spacetime/SpaceTimeFE.cpp:263-281):
+// kt = 0 constant, kt = 1 nodes {0, 1}, kt = 2 nodes {0, 1/2, 1}.
+template <typename T>
+__host__ __device__ __forceinline__ void time_basis(int kt, T x, T* psi, T* dpsi) {
+  if (kt == 0) {
+    psi[0] = (T)1;
+    dpsi[0] = (T)0;
+  } else if (kt == 1) {
+    psi[0] = (T)1 - x;
+    psi[1] = x;
+    dpsi[0] = (T)-1;
+    dpsi[1] = (T)1;
+  } else {
+    psi[0] = ((T)1 - x) * ((T)1 - (T)2 * x);
+    psi[1] = (T)4 * x * ((T)1 - x);
+    psi[2] = x * ((T)2 * x - (T)1);
+    dpsi[0] = (T)4 * x - (T)3;
+    dpsi[1] = (T)4 - (T)8 * x;
+    dpsi[2] = (T)4 * x - (T)1;
+  }
+}
+
+// root_finding (cutint/spacetimecutrule.cpp:8-48) for time orders 0..2
+__device__ __forceinline__ int time_roots(int kt, const double* li, double* roots) {
+  if (kt == 0) return 0;
+  if (kt == 1) {
+    if (d_geq0(li[0]) != d_geq0(li[1])) {
+      roots[0] = -li[0] / (li[1] - li[0]);
+      return 1;
+    }
+    return 0;
+  }
+  const double c = li[0], a = 2 * li[0] + 2 * li[2] - 4. * li[1], b = li[2] - a - c;
+  int n = 0;
+  if (fabs(a) < 1e-12) {
+    const double x = -c / b;
+    if (x < 1 && x > 0) roots[n++] = x;
+  } else {
+    const double w = b * b - 4 * a * c;
+    if (fabs(w) < 1e-12) {
+      const double x = -b / (2 * a);
+      if (x < 1 && x > 0) roots[n++] = x;
+    } else {
+      const double x1 = (b + sqrt(w)) / (-2.0 * a);
+      const double x2 = (b - sqrt(w)) / (-2.0 * a);
+      if (x1 < 1 && x1 > 0) roots[n++] = x1;
+      if (x2 < 1 && x2 > 0) roots[n++] = x2;
+    }
+  }
+  return n;
+}
+
+// sorted time cut points {0, roots..., 1} of an element (at most 2(D+1)+2)
+template <int D>
+__device__ __forceinline__ int time_cuts(int kt, const double* lst /* (kt+1)*(D+1) */, double* cut) {
+  int n = 0;
+  cut[n++] = 0.0;
+  cut[n++] = 1.0;
+  for (int j = 0; j <= D; j++) {
+    double li[3], r[2];
+    for (int i = 0; i <= kt; i++) li[i] = lst[i * (D + 1) + j];
+    const int nr = time_roots(kt, li, r);
+    for (int k = 0; k < nr; k++) cut[n++] = r[k];
+  }
+  // insertion sort (n <= 8)
+  for (int i = 1; i < n; i++) {
+    const double v = cut[i];
+    int j = i - 1;
+    while (j >= 0 && cut[j] > v) {
+      cut[j + 1] = cut[j];
+      j--;
+    }
+    cut[j + 1] = v;
+  }
+  return n;
+}
+
+// level set at tau with the space-time perturbation (|d| < 1e-14 -> +-1e-14,
+// spacetimecutrule.cpp:167-175)
+template <int D>
+__device__ __forceinline__ void lset_at(int kt, const double* lst, double tau, double* l) {
+  double psi[3], dpsi[3];
+  time_basis<double>(kt, tau, psi, dpsi);
+#pragma unroll
+  for (int j = 0; j <= D; j++) {
+    double s = 0;
+    for (int i = 0; i <= kt; i++) s += lst[i * (D + 1) + j] * psi[i];
+    if (fabs(s) < 1e-14) s = d_geq0(s) ? 1e-14 : -1e-14;
+    l[j] = s;
+  }
+}
+
+// trace at a fixed reference time with the InterpolateToP1 perturbation (+1e-14)
+template <int D>
+__device__ __forceinline__ void lset_trace(int kt, const double* lst, double tau, double* l) {
+  double psi[3], dpsi[3];
+  time_basis<double>(kt, tau, psi, dpsi);
+#pragma unroll
+  for (int j = 0; j <= D; j++) {
+    double s = 0;
+    for (int i = 0; i <= kt; i++) s += lst[i * (D + 1) + j] * psi[i];
+    if (fabs(s) < 1e-14) s = 1e-14;
+    l[j] = s;
+  }
+}
+
+}  // namespace xg

@@ -13,6 +13,7 @@ namespace xg {
 static __constant__ RuleTable c_rules;
 
 int upload_rules_asm();  // xg_asm.cu
+int upload_rules_st();   // xg_st.cu
 
 int ensure_device_rules() {
   static std::mutex mu;
@@ -23,6 +24,7 @@ int ensure_device_rules() {
   if (std::find(done.begin(), done.end(), dev) != done.end()) return XG_OK;
   XG_CUDA(cudaMemcpyToSymbol(c_rules, &host_rules(), sizeof(RuleTable)));
   int st = upload_rules_asm();
+  if (!st) st = upload_rules_st();
   if (st) return st;
   done.push_back(dev);
   return XG_OK;
@@ -298,6 +300,142 @@ static int noalloc_partials(double** out) {
   return XG_OK;
 }
 
+
+// ---- space-time CutInfo (xfem/cutinfo.cpp:83-132 with time_order = 0) ---------------
+// SpaceTimeCutIntegrationRule with space and time orders 0: per time interval
+// one time point, per (sub-)simplex one point.
+template <int D>
+__global__ void k_cutinfo_st(int ne, int nv, const int32_t* __restrict__ elv, const double* __restrict__ lset_st,
+                             int kt, uint8_t* __restrict__ dom, double* __restrict__ ratio, uint32_t* __restrict__ bits,
+                             int64_t nw32, int* err) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool valid = e < ne;
+  int t = XG_POS;
+  if (valid) {
+    double lst[3 * (D + 1)];
+    for (int v = 0; v <= D; v++) {
+      const int vid = elv[(int64_t)v * ne + e];
+      for (int i = 0; i <= kt; i++) lst[i * (D + 1) + v] = lset_st[(int64_t)i * nv + vid];
+    }
+    double cut[2 * (D + 1) + 2];
+    const int nc = time_cuts<D>(kt, lst, cut);
+    const double w0 = c_rules.w[c_rules.off[D][0]];
+    const double wt = c_rules.w[c_rules.off[1][0]];
+    const double xt = c_rules.x[c_rules.off[1][0]][0];
+    double part_vol[2] = {0.0, 0.0};
+#pragma unroll
+    for (int pass = 0; pass < 2; pass++) {
+      const int np = pass == 0 ? XG_POS : XG_NEG;
+      for (int i = 0; i + 1 < nc; i++) {
+        const double t0 = cut[i], t1 = cut[i + 1];
+        const double tt = t0 + xt * (t1 - t0);
+        double l[D + 1];
+        lset_at<D>(kt, lst, tt, l);
+        const int cls = check_if_straight_cut(l, D + 1);
+        if (cls == XG_IF) {
+          Sub subs[3];
+          int ns = decompose<D>(l, np, subs);
+          if (ns < 0) {
+            set_err(err, -ns);
+            ns = 0;
+          }
+          for (int k = 0; k < ns; k++) part_vol[np] += w0 * simplex_volume(subs[k].p, D + 1) * wt * (t1 - t0);
+        } else if (cls == np) {
+          part_vol[np] += w0 * wt * (t1 - t0);
+        }
+      }
+    }
+    ratio[e] = part_vol[XG_NEG] / (part_vol[XG_NEG] + part_vol[XG_POS]);
+    if (part_vol[XG_NEG] > 0.0) t = (part_vol[XG_POS] > 0.0) ? XG_IF : XG_NEG;
+    else t = XG_POS;
+    dom[e] = (uint8_t)t;
+  }
+  const unsigned mneg = __ballot_sync(0xffffffffu, valid && t == XG_NEG);
+  const unsigned mpos = __ballot_sync(0xffffffffu, valid && t == XG_POS);
+  const unsigned mif = __ballot_sync(0xffffffffu, valid && t == XG_IF);
+  const unsigned many = __ballot_sync(0xffffffffu, valid);
+  const int64_t w = e >> 5;
+  if ((threadIdx.x & 31) == 0 && w < nw32) {
+    bits[0 * nw32 + w] = 0u;
+    bits[1 * nw32 + w] = mneg;
+    bits[2 * nw32 + w] = mpos;
+    bits[3 * nw32 + w] = mneg | mpos;
+    bits[4 * nw32 + w] = mif;
+    bits[5 * nw32 + w] = mneg | mif;
+    bits[6 * nw32 + w] = mpos | mif;
+    bits[7 * nw32 + w] = many;
+  }
+}
+
+// ---- SpaceTimeCutIntegrationRule export (cutint/spacetimecutrule.cpp:106-244) -------
+template <int D>
+__global__ void k_st_cut_rules(int ne, const int32_t* __restrict__ elv, const double* __restrict__ xyz, int nv,
+                               const double* __restrict__ lset_st, int kt, const int32_t* __restrict__ elems, int n,
+                               int dt, int order_space, int order_time, int max_pts, int32_t* counts, double* pts,
+                               double* wts, int* err) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int e = elems[i];
+  double lst[3 * (D + 1)];
+  double xv[D + 1][3];
+  for (int v = 0; v <= D; v++) {
+    const int vid = elv[(int64_t)v * ne + e];
+    for (int kk = 0; kk <= kt; kk++) lst[kk * (D + 1) + v] = lset_st[(int64_t)kk * nv + vid];
+#pragma unroll
+    for (int c = 0; c < 3; c++) xv[v][c] = c < D ? xyz[(int64_t)c * nv + vid] : 0.0;
+  }
+  Geo<D> g;
+  make_geo<D>(xv, g);
+  double cut[2 * (D + 1) + 2];
+  const int nc = time_cuts<D>(kt, lst, cut);
+  const int ps = clamp_order(order_space < 0 ? 5 : order_space), pt = clamp_order(order_time);
+  const int offt = c_rules.off[1][pt], cntt = c_rules.cnt[1][pt];
+  const int offs = c_rules.off[D][ps], cnts = c_rules.cnt[D][ps];
+  const int sd = dt == XG_IF ? D - 1 : D;
+  const int offc = c_rules.off[sd][ps], cntc = c_rules.cnt[sd][ps];
+  const int maxsize = 5 * cnts * (nc - 1) * cntt;
+  double* P = pts + (int64_t)i * max_pts * 4;
+  double* W = wts + (int64_t)i * max_pts;
+  int k = 0;
+  for (int it = 0; it + 1 < nc; it++) {
+    const double t0 = cut[it], t1 = cut[it + 1];
+    for (int q = 0; q < cntt; q++) {
+      const double tt = t0 + c_rules.x[offt + q][0] * (t1 - t0);
+      const double wtq = c_rules.w[offt + q];
+      double l[D + 1];
+      lset_at<D>(kt, lst, tt, l);
+      const int cls = check_if_straight_cut(l, D + 1);
+      if (cls == XG_IF) {
+        Sub subs[3];
+        const int ns = decompose<D>(l, dt, subs);
+        if (ns < 0) { set_err(err, -ns); counts[i] = 0; return; }
+        if (k + ns * cntc > max_pts) { set_err(err, XG_ERR_CAPACITY); counts[i] = 0; return; }
+        const double fac = dt == XG_IF ? if_factor<D>(g, l) : 1.0;
+        for (int s = 0; s < ns; s++) {
+          const double trafofac = simplex_volume(subs[s].p, sd + 1);
+          for (int b = 0; b < cntc; b++, k++) {
+            double pt3[3];
+            plain_point(subs[s], sd + 1, c_rules.x[offc + b], pt3);
+            P[4 * k + 0] = pt3[0]; P[4 * k + 1] = pt3[1]; P[4 * k + 2] = pt3[2]; P[4 * k + 3] = tt;
+            double w = c_rules.w[offc + b] * trafofac;
+            if (dt == XG_IF) w = w * fac;
+            W[k] = w * wtq * (t1 - t0);
+          }
+        }
+      } else if (cls == dt) {
+        if (k + cnts > max_pts) { set_err(err, XG_ERR_CAPACITY); counts[i] = 0; return; }
+        for (int b = 0; b < cnts; b++, k++) {
+          P[4 * k + 0] = c_rules.x[offs + b][0]; P[4 * k + 1] = c_rules.x[offs + b][1];
+          P[4 * k + 2] = c_rules.x[offs + b][2]; P[4 * k + 3] = tt;
+          W[k] = c_rules.w[offs + b] * wtq * (t1 - t0);
+        }
+      }
+    }
+  }
+  if (k > maxsize) set_err(err, XG_ERR_CAPACITY);
+  counts[i] = k == 0 ? -1 : k;
+}
+
 }  // namespace xg
 
 using namespace xg;
@@ -402,6 +540,38 @@ int xg_integrate(xg_mesh* m, const double* d_lset, int dt, int order, int ex, in
                                               d_defined_on, bs, m->d_err);
   k_sum_fixed<<<1, 32, 0, s>>>(bs, nb, d_result);
   return launch_check("k_integrate");
+}
+
+int xg_cutinfo_update_st(xg_mesh* m, const double* d_lset_st, int kt_lset, uint8_t* d_dom, double* d_ratio,
+                         uint64_t* d_bits, void* stream) {
+  if (!m || !d_lset_st || !d_dom || !d_ratio || !d_bits || kt_lset < 0 || kt_lset > 2) return XG_ERR_ARG;
+  const int64_t nw64 = (m->ne + 63) / 64;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (m->dim == 2)
+    k_cutinfo_st<2><<<nblk(nw64 * 64, 128), 128, 0, s>>>(m->ne, m->nv, m->d_elv, d_lset_st, kt_lset, d_dom, d_ratio,
+                                                         (uint32_t*)d_bits, 2 * nw64, m->d_err);
+  else
+    k_cutinfo_st<3><<<nblk(nw64 * 64, 128), 128, 0, s>>>(m->ne, m->nv, m->d_elv, d_lset_st, kt_lset, d_dom, d_ratio,
+                                                         (uint32_t*)d_bits, 2 * nw64, m->d_err);
+  return launch_check("k_cutinfo_st");
+}
+
+int xg_st_cut_rules(xg_mesh* m, const double* d_lset_st, int kt_lset, const int32_t* d_elems, int32_t n, int dt,
+                    int order_space, int order_time, int32_t max_pts, int32_t* d_counts, double* d_pts, double* d_wts,
+                    void* stream) {
+  if (!m || !d_lset_st || !d_elems || n < 0 || dt < 0 || dt > 2 || kt_lset < 0 || kt_lset > 2 || order_space < -1 ||
+      order_space > kMaxOrder || order_time < 0 || order_time > kMaxOrder || max_pts <= 0 || !d_counts || !d_pts ||
+      !d_wts)
+    return XG_ERR_ARG;
+  if (n == 0) return XG_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (m->dim == 2)
+    k_st_cut_rules<2><<<nblk(n, 64), 64, 0, s>>>(m->ne, m->d_elv, m->d_xyz, m->nv, d_lset_st, kt_lset, d_elems, n, dt,
+                                                 order_space, order_time, max_pts, d_counts, d_pts, d_wts, m->d_err);
+  else
+    k_st_cut_rules<3><<<nblk(n, 64), 64, 0, s>>>(m->ne, m->d_elv, m->d_xyz, m->nv, d_lset_st, kt_lset, d_elems, n, dt,
+                                                 order_space, order_time, max_pts, d_counts, d_pts, d_wts, m->d_err);
+  return launch_check("k_st_cut_rules");
 }
 
 int xg_integrate_noalloc(xg_mesh* m, const double* d_lset, int dt, int order, int ex, int ey, int ez,

@@ -412,9 +412,11 @@ int xg_space_create(xg_mesh* m, int order, xg_space** out) {
   s->mesh = m;
   s->order = k;
   s->nd = D == 2 ? (k + 1) * (k + 2) / 2 : (k + 1) * (k + 2) * (k + 3) / 6;
+  s->nds = s->nd;
   const int nd = s->nd, nel = D == 2 ? 3 : 6;
   const int64_t nbub = (k == 3) ? (D == 3 ? m->nfaces : ne) : 0;
   s->ndof = m->nv + m->nedges * (k - 1) + nbub;
+  s->ndof_s = s->ndof;
   if (s->ndof >= ((int64_t)1 << 31)) {
     delete s;
     set_last_error("xg_space_create: more than 2^31 dofs");
@@ -458,6 +460,59 @@ int xg_space_create(xg_mesh* m, int order, xg_space** out) {
   return XG_OK;
 }
 
+int xg_space_create_st(xg_mesh* m, int order, int order_time, xg_space** out) {
+  if (!m || !out || order < 1 || order > 3 || order_time < 0 || order_time > 2) {
+    set_last_error("xg_space_create_st: space order 1..3, time order 0..2");
+    return XG_ERR_ARG;
+  }
+  *out = nullptr;
+  xg_space* sp = nullptr;
+  int st = xg_space_create(m, order, &sp);
+  if (st) return st;
+  const int nds = sp->nd, nt = order_time + 1, N = nds * nt, ne = m->ne;
+  const int64_t ndof_s = sp->ndof;
+  if (N > 32 || ndof_s * nt >= ((int64_t)1 << 31)) {
+    xg_space_destroy(sp);
+    set_last_error("xg_space_create_st: too many space-time dofs per element or in total");
+    return XG_ERR_CAPACITY;
+  }
+  std::vector<int32_t> spatial = sp->h_el_dofs;
+  cudaFree(sp->d_el_dofs);
+  cudaFree(sp->d_el_dofs_aos);
+  cudaFree(sp->d_dof_adj_ptr);
+  cudaFree(sp->d_dof_adj);
+  sp->d_el_dofs = sp->d_el_dofs_aos = sp->d_dof_adj_ptr = sp->d_dof_adj = nullptr;
+  sp->kt = order_time;
+  sp->nds = nds;
+  sp->ndof_s = ndof_s;
+  sp->nd = N;
+  sp->ndof = ndof_s * nt;
+  sp->h_el_dofs.resize((size_t)ne * N);
+  for (int e = 0; e < ne; e++)
+    for (int it = 0; it < nt; it++)
+      for (int j = 0; j < nds; j++)
+        sp->h_el_dofs[(size_t)e * N + it * nds + j] = (int32_t)(it * ndof_s + spatial[(size_t)e * nds + j]);
+  std::vector<int32_t> ptr(sp->ndof + 1, 0);
+  for (size_t i = 0; i < sp->h_el_dofs.size(); i++) ptr[sp->h_el_dofs[i] + 1]++;
+  int mx = 0;
+  for (int64_t i = 0; i < sp->ndof; i++) {
+    mx = std::max(mx, ptr[i + 1]);
+    ptr[i + 1] += ptr[i];
+  }
+  sp->max_adj = mx;
+  std::vector<int32_t> adj(sp->h_el_dofs.size());
+  std::vector<int32_t> fill(ptr.begin(), ptr.end() - 1);
+  for (int e = 0; e < ne; e++)
+    for (int i = 0; i < N; i++) adj[fill[sp->h_el_dofs[(size_t)e * N + i]]++] = e * 32 + i;
+  if ((st = upload(&sp->d_el_dofs, to_soa(sp->h_el_dofs, ne, N))) || (st = upload(&sp->d_el_dofs_aos, sp->h_el_dofs)) ||
+      (st = upload(&sp->d_dof_adj_ptr, ptr)) || (st = upload(&sp->d_dof_adj, adj))) {
+    xg_space_destroy(sp);
+    return st;
+  }
+  *out = sp;
+  return XG_OK;
+}
+
 int xg_space_destroy(xg_space* s) {
   if (!s) return XG_OK;
   cudaFree(s->d_el_dofs);
@@ -471,6 +526,12 @@ int xg_space_destroy(xg_space* s) {
 int xg_space_info(const xg_space* s, int64_t* o) {
   if (!s || !o) return XG_ERR_ARG;
   o[0] = s->ndof; o[1] = s->nd; o[2] = s->order;
+  return XG_OK;
+}
+
+int xg_space_info_st(const xg_space* s, int64_t* o) {
+  if (!s || !o) return XG_ERR_ARG;
+  o[0] = s->ndof; o[1] = s->nd; o[2] = s->order; o[3] = s->kt; o[4] = s->ndof_s; o[5] = s->nds;
   return XG_OK;
 }
 

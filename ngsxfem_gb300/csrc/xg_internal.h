@@ -79,6 +79,39 @@ struct FormDesc {
   PatchDesc p[kMaxPatch];
 };
 
+// space-time volume terms with equal (domain, order, defined_on, tref,
+// convection) share one space-time rule
+struct StGroupDesc {
+  int domain;
+  int order;       // spatial rule order
+  const uint64_t* defined_on;
+  double tref;     // < 0: over the slab; >= 0: fixed reference time (spatial rule of the trace)
+  double c[7];     // coefficients per kind (MASS, LAPLACE, -, -, CONV, -, DT_U_V)
+  int hpow[7];
+  int used;
+  double b[3], bc[3], bs[3];  // convection b(t) = b + bc cos(omega t) + bs sin(omega t)
+  double omega, t0, dt;       // t = t0 + dt * tau
+};
+struct StFormDesc {
+  int ngroups;
+  StGroupDesc g[kMaxGroups];
+  int kt_l;        // time order of the level set
+  int order_time;  // time rule order
+};
+struct StLaunch {
+  int D, K, KT, precision;
+  int ne, nv;
+  const int32_t* elv;
+  const double* xyz;
+  const double* lset_st;
+  StFormDesc desc;
+  const int32_t* list;
+  const int* count;
+  void* elmat;
+  int* err;
+};
+int launch_st_elmat(const StLaunch& a, cudaStream_t s);
+
 }  // namespace xg
 
 // ---- objects behind the opaque handles ------------------------------------------
@@ -110,6 +143,9 @@ struct xg_space {
   xg_mesh* mesh = nullptr;
   int order = 1, nd = 0;
   int64_t ndof = 0;
+  int kt = -1;          // time order of a space-time space (-1: spatial space)
+  int nds = 0;          // spatial dofs per element
+  int64_t ndof_s = 0;   // spatial dofs
   int32_t* d_el_dofs = nullptr;     // [nd][ne]
   int32_t* d_el_dofs_aos = nullptr; // [ne][nd] element-major (scatter gathers)
   int32_t* d_dof_adj_ptr = nullptr; // [ndof+1]

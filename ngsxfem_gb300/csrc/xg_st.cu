@@ -1,0 +1,353 @@
+// Space-time element matrices (dCut(lset_st, dt, time_order=...) forms of
+// ngsxfem's space-time discretisations, e.g. demos/spacetime/spacetimeDG_unfitted.py:143-168).
+//
+// Per element the space-time rule of cutint/spacetimecutrule.cpp:106-244 is
+// generated on the fly: time cut points (root_finding per vertex), per time
+// interval and time quadrature point the level set at that time (with the
+// +-1e-14 perturbation), its straight-cut rule or the standard rule.  A
+// fixed-time term (tref >= 0, dCut(..., tref=...)) uses the spatial rule of the
+// level-set trace at tref.  Space-time shape functions are products
+// psi_i(tau) phi_j(x) with the nodal Gauss-Lobatto time basis; local index
+// i * nd_space + j.  Terms: c u v, c grad u . grad v, c (b(t) . grad u) v with
+// b(t) = b + bc cos(omega t) + bs sin(omega t), t = t0 + dt tau, and
+// c v d/dtau u.
+#include <mutex>
+
+#include "xg_basis.cuh"
+#include "xg_cut.cuh"
+#include "xg_internal.h"
+
+namespace xg {
+
+static __constant__ RuleTable c_rules;
+
+int upload_rules_st() {
+  XG_CUDA(cudaMemcpyToSymbol(c_rules, &host_rules(), sizeof(RuleTable)));
+  return XG_OK;
+}
+
+__device__ __forceinline__ bool tbit64(const uint64_t* b, int64_t i) { return (b[i >> 6] >> (i & 63)) & 1ull; }
+
+template <int D, int K, int KT>
+struct StCfg {
+  static constexpr int NS = ndof_el(D, K);
+  static constexpr int N = NS * (KT + 1);
+  static constexpr int EPB = N <= 8 ? 8 : (N <= 20 ? 4 : 2);
+  static constexpr int NT = N * EPB;
+  static constexpr int CH = 4;
+  static constexpr int MAXC = (2 * (D + 1) + 1) * 4;  // time intervals x time points
+  static constexpr int NACC = (EPB * N * N + NT - 1) / NT;
+};
+
+struct StCombo {
+  double t, wt;   // reference time and time weight w_t (t1 - t0)
+  double l[4];    // level set at t
+  int cls;        // CheckIfStraightCut at t
+  int npts;
+};
+
+template <int D>
+struct StGeoS {
+  double g[4][3];
+  double meas;
+  double lst[3 * 4];
+  double cut[2 * 4 + 2];
+  int ncut;
+  int gv[4];
+  int elem, slot;
+  double coef[kMaxGroups][7];
+};
+
+// number of sub-simplices of Decompose for the sign pattern (no FP work)
+template <int D>
+__device__ __forceinline__ int n_subs(const double* l, int dt) {
+  if (dt == XG_IF) {
+    int nc = 0;
+    for (int i = 0; i <= D; i++)
+      for (int j = i + 1; j <= D; j++) nc += d_geq0(l[i]) != d_geq0(l[j]);
+    return (D == 3 && nc == 4) ? 2 : 1;
+  }
+  int nr = 0;
+  for (int i = 0; i <= D; i++) nr += (dt == XG_POS && d_geq0(l[i])) || (dt == XG_NEG && d_neg(l[i]));
+  if (nr == 1) return 1;
+  return D == 2 ? 2 : 3;
+}
+
+template <int D, int K, int KT, typename T>
+__global__ void __launch_bounds__(StCfg<D, K, KT>::NT) k_st_elmat(int ne, int nv, const int32_t* __restrict__ elv,
+                                                                   const double* __restrict__ xyz,
+                                                                   const double* __restrict__ lset_st, StFormDesc form,
+                                                                   const int32_t* __restrict__ list,
+                                                                   const int* __restrict__ count_ptr,
+                                                                   T* __restrict__ elmat, int* err) {
+  using C = StCfg<D, K, KT>;
+  constexpr int NS = C::NS, N = C::N, EPB = C::EPB, NT = C::NT, CH = C::CH, MAXC = C::MAXC, NACC = C::NACC;
+  constexpr int NF = D + 4;  // Phi, grad Phi (D), dtau Phi, b . grad Phi
+  __shared__ StGeoS<D> geo[EPB];
+  __shared__ StCombo combo[EPB][MAXC];
+  __shared__ int coff[EPB][MAXC + 1];
+  __shared__ int ncombo_s[EPB];
+  __shared__ double pts[EPB][CH][D + 6];  // lambda (D+1), tau, w, b(t) (3)
+  __shared__ T tr[EPB][CH][N][NF];
+  __shared__ T te[EPB][CH][N][4];        // w*cM*Phi, w*cL*grad(as factor), w*cC*Phi, w*cT*Phi
+  __shared__ int maxpts_s;
+  const int count = *count_ptr;
+  const int le = threadIdx.x / N, a = threadIdx.x % N;
+  const int kl = form.kt_l;
+
+  for (int batch = blockIdx.x; batch * EPB < count; batch += gridDim.x) {
+    __syncthreads();
+    if (threadIdx.x < EPB) {
+      StGeoS<D>& G = geo[threadIdx.x];
+      const int idx = batch * EPB + threadIdx.x;
+      G.elem = idx < count ? list[idx] : -1;
+      G.slot = idx;
+      if (G.elem >= 0) {
+        const int e = G.elem;
+        double xv[D + 1][3];
+        for (int v = 0; v <= D; v++) {
+          const int vid = elv[(int64_t)v * ne + e];
+          G.gv[v] = vid;
+          for (int i = 0; i <= kl; i++) G.lst[i * (D + 1) + v] = lset_st[(int64_t)i * nv + vid];
+#pragma unroll
+          for (int c = 0; c < 3; c++) xv[v][c] = c < D ? xyz[(int64_t)c * nv + vid] : 0.0;
+        }
+        Geo<D> g;
+        make_geo<D>(xv, g);
+        G.meas = fabs(g.det);
+        double gs[3] = {0, 0, 0};
+        for (int aa = 0; aa < D; aa++)
+          for (int k = 0; k < 3; k++) {
+            G.g[aa][k] = k < D ? g.Finv[aa][k] : 0.0;
+            gs[k] += G.g[aa][k];
+          }
+        for (int k = 0; k < 3; k++) G.g[D][k] = -gs[k];
+        G.ncut = time_cuts<D>(kl, G.lst, G.cut);
+        double h = -1.0;
+        for (int q = 0; q < form.ngroups; q++)
+          for (int k = 0; k < 7; k++) {
+            const int hp = form.g[q].hpow[k];
+            if (hp != 0 && h < 0) h = pow(G.meas, 1.0 / D);
+            G.coef[q][k] = hp == 0 ? form.g[q].c[k] : form.g[q].c[k] * pow(h, (double)hp);
+          }
+      }
+    }
+    __syncthreads();
+    const StGeoS<D>& G = geo[le];
+    const int sidx = a % NS, tidx = a / NS;
+    const int desc = G.elem >= 0 ? fn_desc<D, K>(sidx, G.gv) : 0;
+    T gT[D + 1][D];
+#pragma unroll
+    for (int aa = 0; aa <= D; aa++)
+#pragma unroll
+      for (int k = 0; k < D; k++) gT[aa][k] = (T)G.g[aa][k];
+    Acc<T> acc[NACC];
+#pragma unroll
+    for (int m = 0; m < NACC; m++) acc[m].init();
+
+    for (int q = 0; q < form.ngroups; q++) {
+      const StGroupDesc& Gq = form.g[q];
+      const int ps = clamp_order(Gq.order), dt = Gq.domain;
+      const int sd = dt == XG_IF ? D - 1 : D;
+      const int nqc = c_rules.cnt[sd][ps], offc = c_rules.off[sd][ps];
+      const int nqs = c_rules.cnt[D][ps], offs = c_rules.off[D][ps];
+      const int pt = clamp_order(form.order_time);
+      const int nqt = c_rules.cnt[1][pt], offt = c_rules.off[1][pt];
+      const bool fixed = Gq.tref >= 0.0;
+      const bool on = G.elem >= 0 && (!Gq.defined_on || tbit64(Gq.defined_on, G.elem));
+      const int nco = !on ? 0 : (fixed ? 1 : (G.ncut - 1) * nqt);
+      // combos: (time interval, time point) -> level set, classification, #points
+      for (int c = a; c < nco; c += N) {
+        StCombo& Cb = combo[le][c];
+        if (fixed) {
+          Cb.t = Gq.tref;
+          Cb.wt = 1.0;
+          lset_trace<D>(kl, G.lst, Gq.tref, Cb.l);
+        } else {
+          const int iv = c / nqt, iq = c % nqt;
+          const double t0 = G.cut[iv], t1 = G.cut[iv + 1];
+          Cb.t = t0 + c_rules.x[offt + iq][0] * (t1 - t0);
+          Cb.wt = c_rules.w[offt + iq] * (t1 - t0);
+          lset_at<D>(kl, G.lst, Cb.t, Cb.l);
+        }
+        Cb.cls = check_if_straight_cut(Cb.l, D + 1);
+        Cb.npts = Cb.cls == XG_IF ? n_subs<D>(Cb.l, dt) * nqc : (Cb.cls == dt ? nqs : 0);
+      }
+      __syncthreads();
+      if (a == 0) {
+        int o = 0;
+        for (int c = 0; c < nco; c++) {
+          coff[le][c] = o;
+          o += combo[le][c].npts;
+        }
+        coff[le][nco] = o;
+        ncombo_s[le] = nco;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        int mx = 0;
+        for (int k = 0; k < EPB; k++) mx = max(mx, coff[k][ncombo_s[k]]);
+        maxpts_s = mx;
+      }
+      __syncthreads();
+      const int maxpts = maxpts_s, npl = coff[le][ncombo_s[le]];
+      const T cM = (T)G.coef[q][XG_TERM_MASS], cL = (T)G.coef[q][XG_TERM_LAPLACE];
+      const T cC = (T)G.coef[q][XG_TERM_CONV], cT = (T)G.coef[q][6];
+      const int used = Gq.used;
+      for (int q0 = 0; q0 < maxpts; q0 += CH) {
+        for (int qq = a; qq < CH; qq += N) {
+          const int qi = q0 + qq;
+          double lam[4] = {0.25, 0.25, 0.25, 0.25}, w = 0.0, tau = 0.0;
+          if (qi < npl) {
+            int c = 0;
+            while (coff[le][c + 1] <= qi) c++;
+            const StCombo& Cb = combo[le][c];
+            const int k = qi - coff[le][c];
+            tau = Cb.t;
+            double xi[3];
+            if (Cb.cls == XG_IF) {
+              Sub subs[3];
+              const int ns = decompose<D>(Cb.l, dt, subs);
+              if (ns < 0) {
+                set_err(err, -ns);
+              } else {
+                const int s = k / nqc, b = k % nqc;
+                plain_point(subs[s], sd + 1, c_rules.x[offc + b], xi);
+                w = c_rules.w[offc + b] * simplex_volume(subs[s].p, sd + 1);
+                if (dt == XG_IF) {
+                  Geo<D> gg;  // interface factor from the stored inverse Jacobian
+#pragma unroll
+                  for (int r = 0; r < D; r++)
+#pragma unroll
+                    for (int cc = 0; cc < D; cc++) gg.Finv[r][cc] = G.g[r][cc];
+                  w = w * if_factor<D>(gg, Cb.l);
+                }
+              }
+            } else {
+              xi[0] = c_rules.x[offs + k][0];
+              xi[1] = c_rules.x[offs + k][1];
+              xi[2] = c_rules.x[offs + k][2];
+              w = c_rules.w[offs + k];
+            }
+            w = w * Cb.wt * G.meas;
+            double s3 = 0;
+            for (int r = 0; r < D; r++) {
+              lam[r] = xi[r];
+              s3 += xi[r];
+            }
+            lam[D] = 1.0 - s3;
+          }
+          for (int r = 0; r <= D; r++) pts[le][qq][r] = lam[r];
+          pts[le][qq][D + 1] = tau;
+          pts[le][qq][D + 2] = w;
+          double bt[3] = {Gq.b[0], Gq.b[1], Gq.b[2]};
+          if ((used & (1 << XG_TERM_CONV)) && Gq.omega != 0.0) {
+            const double tp = Gq.t0 + Gq.dt * tau;
+            const double cs = cos(Gq.omega * tp), sn = sin(Gq.omega * tp);
+            for (int r = 0; r < 3; r++) bt[r] += Gq.bc[r] * cs + Gq.bs[r] * sn;
+          }
+          for (int r = 0; r < 3; r++) pts[le][qq][D + 3 + r] = bt[r];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int qq = 0; qq < CH; qq++) {
+          T lam[D + 1];
+#pragma unroll
+          for (int r = 0; r <= D; r++) lam[r] = (T)pts[le][qq][r];
+          T phi, grad[D];
+          eval_fn<D, T>(desc, lam, gT, phi, grad);
+          T psi[3], dpsi[3];
+          time_basis<T>(KT, (T)pts[le][qq][D + 1], psi, dpsi);
+          const T ps_ = psi[tidx], dps = dpsi[tidx];
+          const T w = (T)pts[le][qq][D + 2];
+          const T Phi = ps_ * phi;
+          tr[le][qq][a][0] = Phi;
+          T bg = 0;
+#pragma unroll
+          for (int k = 0; k < D; k++) {
+            const T gk = ps_ * grad[k];
+            tr[le][qq][a][1 + k] = gk;
+            bg += (T)pts[le][qq][D + 3 + k] * gk;
+          }
+          tr[le][qq][a][1 + D] = dps * phi;
+          tr[le][qq][a][2 + D] = bg;
+          te[le][qq][a][0] = (used & (1 << XG_TERM_MASS)) ? w * cM * Phi : (T)0;
+          te[le][qq][a][1] = (used & (1 << XG_TERM_LAPLACE)) ? w * cL : (T)0;
+          te[le][qq][a][2] = (used & (1 << XG_TERM_CONV)) ? w * cC * Phi : (T)0;
+          te[le][qq][a][3] = (used & (1 << 6)) ? w * cT * Phi : (T)0;
+        }
+        __syncthreads();
+        const int nch = min(CH, maxpts - q0);
+#pragma unroll
+        for (int m = 0; m < NACC; m++) {
+          const int t = threadIdx.x + m * NT;
+          if (t < EPB * N * N) {
+            const int el = t / (N * N), k = t % (N * N), pp = k / N, qv = k % N;
+            T v = 0;
+            for (int qq = 0; qq < nch; qq++) {
+              const T* A = te[el][qq][pp];
+              const T* B = tr[el][qq][qv];
+              const T* Bp = tr[el][qq][pp];
+              T lap = 0;
+#pragma unroll
+              for (int kk = 1; kk <= D; kk++) lap += Bp[kk] * B[kk];
+              v += A[0] * B[0] + A[1] * lap + A[2] * B[2 + D] + A[3] * B[1 + D];
+            }
+            acc[m].add(v);
+          }
+        }
+        __syncthreads();
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < NACC; m++) {
+      const int t = threadIdx.x + m * NT;
+      if (t < EPB * N * N) {
+        const int el = t / (N * N), k = t % (N * N);
+        if (geo[el].elem >= 0) {
+          const T v = acc[m].get();
+          if (!isfinite(v)) set_err(err, XG_ERR_NONFINITE);
+          elmat[(int64_t)geo[el].slot * N * N + k] = v;
+        }
+      }
+    }
+  }
+}
+
+template <int D, int K, int KT, typename T>
+static int launch_one(const StLaunch& a, cudaStream_t s) {
+  using C = StCfg<D, K, KT>;
+  auto kern = k_st_elmat<D, K, KT, T>;
+  static int grid[2] = {0, 0};
+  int& g = grid[sizeof(T) == 8];
+  if (!g) {
+    int dev = 0, nsm = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, C::NT, 0);
+    g = nsm * (per < 1 ? 1 : per);
+  }
+  kern<<<g, C::NT, 0, s>>>(a.ne, a.nv, a.elv, a.xyz, a.lset_st, a.desc, a.list, a.count, (T*)a.elmat, a.err);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? XG_OK : cuda_fail(e, "k_st_elmat");
+}
+
+template <typename T>
+static int launch_t(const StLaunch& a, cudaStream_t s) {
+  if (a.D == 2) {
+    if (a.K == 1) return a.KT == 1 ? launch_one<2, 1, 1, T>(a, s) : launch_one<2, 1, 2, T>(a, s);
+    return a.KT == 1 ? launch_one<2, 2, 1, T>(a, s) : launch_one<2, 2, 2, T>(a, s);
+  }
+  if (a.K == 1) return a.KT == 1 ? launch_one<3, 1, 1, T>(a, s) : launch_one<3, 1, 2, T>(a, s);
+  return a.KT == 1 ? launch_one<3, 2, 1, T>(a, s) : launch_one<3, 2, 2, T>(a, s);
+}
+
+int launch_st_elmat(const StLaunch& a, cudaStream_t s) {
+  if (a.K < 1 || a.K > 2 || a.KT < 1 || a.KT > 2) {
+    set_last_error("space-time forms: space order 1..2 and time order 1..2");
+    return XG_ERR_UNSUPPORTED;
+  }
+  return a.precision == XG_PREC_FP64 ? launch_t<double>(a, s) : launch_t<float>(a, s);
+}
+
+}  // namespace xg

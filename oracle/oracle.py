@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liboracle.so")
 
 NEG, POS, IF = 0, 1, 2
-TERM_MASS, TERM_LAPLACE, TERM_NGRADU_V, TERM_U_NGRADV, TERM_CONV, TERM_GHOST_MASS = range(6)
+TERM_MASS, TERM_LAPLACE, TERM_NGRADU_V, TERM_U_NGRADV, TERM_CONV, TERM_GHOST_MASS, TERM_DT_U_V = range(7)
 
 
 class Term(ctypes.Structure):
@@ -25,6 +25,24 @@ class Term(ctypes.Structure):
         ("coef", ctypes.c_double),
         ("b", ctypes.c_double * 3),
         ("defined_on", ctypes.c_void_p),
+    ]
+
+
+class StTerm(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int),
+        ("domain", ctypes.c_int),
+        ("order", ctypes.c_int),
+        ("hpow", ctypes.c_int),
+        ("coef", ctypes.c_double),
+        ("b", ctypes.c_double * 3),
+        ("defined_on", ctypes.c_void_p),
+        ("tref", ctypes.c_double),
+        ("bc", ctypes.c_double * 3),
+        ("bs", ctypes.c_double * 3),
+        ("omega", ctypes.c_double),
+        ("t0", ctypes.c_double),
+        ("dt", ctypes.c_double),
     ]
 
 
@@ -64,6 +82,16 @@ def lib():
         L.orc_csr_nnz.argtypes = [P]
         L.orc_csr_get.argtypes = [P, P, P, P]
         L.orc_csr_destroy.argtypes = [P]
+        L.orc_time_basis.argtypes = [ctypes.c_int, ctypes.c_double, P, P]
+        L.orc_spacetime_cut_rule.argtypes = [ctypes.c_int, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                             P, P, ctypes.c_int]
+        L.orc_cutinfo_st.argtypes = [P, P, ctypes.c_int, P, P, P, ctypes.c_int]
+        L.orc_st_element_matrix.argtypes = [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, ctypes.c_int,
+                                            ctypes.c_int, P]
+        L.orc_assemble_st.restype = P
+        L.orc_assemble_st.argtypes = [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, ctypes.c_int, ctypes.c_int]
+        L.orc_integrate_st.restype = ctypes.c_double
+        L.orc_integrate_st.argtypes = [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.orc_pipeline.restype = ctypes.c_int64
         L.orc_pipeline.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         _lib = L
@@ -105,6 +133,55 @@ def straight_cut_rule(elcoords, lset, dt, order):
     if n < -1:
         raise RuntimeError("oracle cut rule error %d" % n)
     return pts[:n].copy(), w[:n].copy()
+
+
+def time_basis(kt, tau):
+    psi = np.zeros(3)
+    dpsi = np.zeros(3)
+    lib().orc_time_basis(kt, tau, _p(psi), _p(dpsi))
+    return psi[: kt + 1].copy(), dpsi[: kt + 1].copy()
+
+
+def spacetime_cut_rule(elcoords, lset_st, kt, dt, order_space, order_time):
+    """lset_st: (kt+1, D+1) time-major values.  Returns (points (n,4): xi,eta,zeta,tau, weights) or None."""
+    elc = np.ascontiguousarray(elcoords, dtype=np.float64)
+    D = elc.shape[1]
+    l = np.ascontiguousarray(lset_st, dtype=np.float64).ravel()
+    pts = np.zeros((8192, 4))
+    w = np.zeros(8192)
+    n = lib().orc_spacetime_cut_rule(D, _p(elc), _p(l), kt, dt, order_space, order_time, _p(pts), _p(w), 8192)
+    if n == -1:
+        return None
+    if n < -1:
+        raise RuntimeError("oracle space-time rule error %d" % n)
+    return pts[:n].copy(), w[:n].copy()
+
+
+def _st_terms(terms):
+    arr = (StTerm * len(terms))()
+    keep = []
+    for i, t in enumerate(terms):
+        arr[i].kind = t["kind"]
+        arr[i].domain = t.get("domain", NEG)
+        arr[i].order = t.get("order", -1)
+        arr[i].hpow = t.get("hpow", 0)
+        arr[i].coef = t.get("coef", 1.0)
+        for k, name in ((0, "b"), (1, "bc"), (2, "bs")):
+            v = t.get(name, (0.0, 0.0, 0.0))
+            for j in range(3):
+                getattr(arr[i], name)[j] = v[j]
+        arr[i].tref = t.get("tref", -1.0)
+        arr[i].omega = t.get("omega", 0.0)
+        arr[i].t0 = t.get("t0", 0.0)
+        arr[i].dt = t.get("dt", 1.0)
+        d = t.get("defined_on")
+        if d is not None:
+            d = np.ascontiguousarray(d, dtype=np.uint64)
+            keep.append(d)
+            arr[i].defined_on = d.ctypes.data
+        else:
+            arr[i].defined_on = None
+    return arr, keep
 
 
 class Space:
@@ -209,6 +286,49 @@ class Space:
             raise RuntimeError("oracle assembly error")
         nnz = lib().orc_csr_nnz(c)
         rowptr = np.zeros(self.ndof + 1, dtype=np.int64)
+        cols = np.zeros(nnz, dtype=np.int32)
+        vals = np.zeros(nnz)
+        lib().orc_csr_get(c, _p(rowptr), _p(cols), _p(vals))
+        lib().orc_csr_destroy(c)
+        return rowptr, cols, vals
+
+    # ---- space-time: lset_st is (kt+1, nv) time-major
+    def cutinfo_st(self, lset_st, kt, nthreads=1):
+        ne = self.mesh.ne
+        nw = (ne + 63) // 64
+        dom = np.zeros(ne, dtype=np.uint8)
+        ratio = np.zeros(ne)
+        bits = np.zeros((8, nw), dtype=np.uint64)
+        l = np.ascontiguousarray(lset_st, dtype=np.float64)
+        r = lib().orc_cutinfo_st(self.h, _p(l), kt, _p(dom), _p(ratio), _p(bits), nthreads)
+        if r:
+            raise RuntimeError("oracle space-time cutinfo error %d" % r)
+        return dom, ratio, bits
+
+    def integrate_st(self, lset_st, kt, dt, order_space, order_time):
+        l = np.ascontiguousarray(lset_st, dtype=np.float64)
+        return lib().orc_integrate_st(self.h, _p(l), kt, dt, order_space, order_time)
+
+    def st_element_matrix(self, lset_st, kt_l, kt, order_time, terms, e):
+        arr, keep = _st_terms(terms)
+        n = self.ndof_el * (kt + 1)
+        out = np.zeros((n, n))
+        l = np.ascontiguousarray(lset_st, dtype=np.float64)
+        r = lib().orc_st_element_matrix(self.h, _p(l), kt_l, kt, order_time, ctypes.cast(arr, ctypes.c_void_p),
+                                        len(terms), e, _p(out))
+        if r:
+            raise RuntimeError("oracle space-time element matrix error %d" % r)
+        return out
+
+    def assemble_st(self, lset_st, kt_l, kt, order_time, terms, nthreads=1):
+        arr, keep = _st_terms(terms)
+        l = np.ascontiguousarray(lset_st, dtype=np.float64)
+        c = lib().orc_assemble_st(self.h, _p(l), kt_l, kt, order_time, ctypes.cast(arr, ctypes.c_void_p), len(terms),
+                                  nthreads)
+        if not c:
+            raise RuntimeError("oracle space-time assembly error")
+        nnz = lib().orc_csr_nnz(c)
+        rowptr = np.zeros(self.ndof * (kt + 1) + 1, dtype=np.int64)
         cols = np.zeros(nnz, dtype=np.int32)
         vals = np.zeros(nnz)
         lib().orc_csr_get(c, _p(rowptr), _p(cols), _p(vals))

@@ -919,6 +919,64 @@ struct orc_csr {
   std::vector<double> vals;
 };
 
+// Row-wise gather of element and facet-patch matrices into CSR over all dofs:
+// per dof, its adjacent elements ascending, each element's own row then its
+// active facets in local order (first element's columns, then the second's).
+orc_csr* gather_csr(int64_t ndof, int n, const std::vector<int32_t>& el_dofs, const std::vector<int64_t>& adj_ptr,
+                    const std::vector<int32_t>& adj, int nfl, const std::vector<int32_t>& el_facets,
+                    const std::vector<int32_t>& facet_els, const std::vector<int32_t>& el_slot,
+                    const std::vector<double>& elm, const std::vector<int32_t>& fa_slot, const std::vector<double>& fam,
+                    int nthreads) {
+  const int n2 = 2 * n;
+  auto* csr = new orc_csr();
+  csr->rowptr.assign(ndof + 1, 0);
+  std::vector<std::vector<int32_t>> rc(ndof);
+  std::vector<std::vector<double>> rv(ndof);
+  parallel_for(ndof, nthreads, [&](int64_t b, int64_t en) {
+    std::vector<std::pair<int32_t, double>> cand;
+    for (int64_t r = b; r < en; r++) {
+      cand.clear();
+      for (int64_t a = adj_ptr[r]; a < adj_ptr[r + 1]; a++) {
+        int e = adj[a] >> 5, i = adj[a] & 31;
+        const int32_t* de = &el_dofs[(size_t)e * n];
+        if (el_slot[e] >= 0) {
+          const double* m = &elm[(size_t)el_slot[e] * n * n];
+          for (int j = 0; j < n; j++) cand.push_back({de[j], m[i * n + j]});
+        }
+        for (int lf = 0; lf < nfl; lf++) {
+          int f = el_facets[(size_t)e * nfl + lf];
+          if (fa_slot[f] < 0) continue;
+          int e1 = facet_els[2 * f], e2 = facet_els[2 * f + 1];
+          int row = (e == e1) ? i : n + i;
+          const double* m = &fam[(size_t)fa_slot[f] * n2 * n2];
+          const int32_t* d1 = &el_dofs[(size_t)e1 * n];
+          const int32_t* d2 = &el_dofs[(size_t)e2 * n];
+          for (int j = 0; j < n; j++) cand.push_back({d1[j], m[row * n2 + j]});
+          for (int j = 0; j < n; j++) cand.push_back({d2[j], m[row * n2 + n + j]});
+        }
+      }
+      std::stable_sort(cand.begin(), cand.end(),
+                       [](const std::pair<int32_t, double>& x, const std::pair<int32_t, double>& y) { return x.first < y.first; });
+      for (size_t c = 0; c < cand.size();) {
+        size_t d = c;
+        double sacc = 0;
+        while (d < cand.size() && cand[d].first == cand[c].first) sacc += cand[d++].second;
+        rc[r].push_back(cand[c].first);
+        rv[r].push_back(sacc);
+        c = d;
+      }
+    }
+  });
+  for (int64_t r = 0; r < ndof; r++) csr->rowptr[r + 1] = csr->rowptr[r] + (int64_t)rc[r].size();
+  csr->cols.resize(csr->rowptr[ndof]);
+  csr->vals.resize(csr->rowptr[ndof]);
+  for (int64_t r = 0; r < ndof; r++) {
+    std::copy(rc[r].begin(), rc[r].end(), csr->cols.begin() + csr->rowptr[r]);
+    std::copy(rv[r].begin(), rv[r].end(), csr->vals.begin() + csr->rowptr[r]);
+  }
+  return csr;
+}
+
 extern "C" {
 
 int orc_cutinfo(const orc_space* s, const double* lset_vertex, uint8_t* dom, double* cut_ratio, uint64_t* bits,
@@ -1051,56 +1109,8 @@ orc_csr* orc_assemble(const orc_space* s, const double* lset_vertex, const orc_t
     }
   });
   if (err.load()) return nullptr;
-  // row-wise gather (dof -> element adjacency, elements ascending)
-  const int64_t ndof = s->ndof;
-  const int nfl = s->D + 1;
-  auto* csr = new orc_csr();
-  csr->rowptr.assign(ndof + 1, 0);
-  std::vector<std::vector<int32_t>> rc(ndof);
-  std::vector<std::vector<double>> rv(ndof);
-  parallel_for(ndof, nthreads, [&](int64_t b, int64_t en) {
-    std::vector<std::pair<int32_t, double>> cand;
-    for (int64_t r = b; r < en; r++) {
-      cand.clear();
-      for (int64_t a = s->dof_adj_ptr[r]; a < s->dof_adj_ptr[r + 1]; a++) {
-        int e = s->dof_adj[a] >> 5, i = s->dof_adj[a] & 31;
-        const int32_t* de = &s->el_dofs[(size_t)e * n];
-        if (el_slot[e] >= 0) {
-          const double* m = &elm[(size_t)el_slot[e] * n * n];
-          for (int j = 0; j < n; j++) cand.push_back({de[j], m[i * n + j]});
-        }
-        for (int lf = 0; lf < nfl; lf++) {
-          int f = s->el_facets[(size_t)e * nfl + lf];
-          if (fa_slot[f] < 0) continue;
-          int e1 = s->facet_els[2 * f], e2 = s->facet_els[2 * f + 1];
-          int row = (e == e1) ? i : n + i;
-          const double* m = &fam[(size_t)fa_slot[f] * n2 * n2];
-          const int32_t* d1 = &s->el_dofs[(size_t)e1 * n];
-          const int32_t* d2 = &s->el_dofs[(size_t)e2 * n];
-          for (int j = 0; j < n; j++) cand.push_back({d1[j], m[row * n2 + j]});
-          for (int j = 0; j < n; j++) cand.push_back({d2[j], m[row * n2 + n + j]});
-        }
-      }
-      std::stable_sort(cand.begin(), cand.end(),
-                       [](const std::pair<int32_t, double>& x, const std::pair<int32_t, double>& y) { return x.first < y.first; });
-      for (size_t c = 0; c < cand.size();) {
-        size_t d = c;
-        double sacc = 0;
-        while (d < cand.size() && cand[d].first == cand[c].first) sacc += cand[d++].second;
-        rc[r].push_back(cand[c].first);
-        rv[r].push_back(sacc);
-        c = d;
-      }
-    }
-  });
-  for (int64_t r = 0; r < ndof; r++) csr->rowptr[r + 1] = csr->rowptr[r] + (int64_t)rc[r].size();
-  csr->cols.resize(csr->rowptr[ndof]);
-  csr->vals.resize(csr->rowptr[ndof]);
-  for (int64_t r = 0; r < ndof; r++) {
-    std::copy(rc[r].begin(), rc[r].end(), csr->cols.begin() + csr->rowptr[r]);
-    std::copy(rv[r].begin(), rv[r].end(), csr->vals.begin() + csr->rowptr[r]);
-  }
-  return csr;
+  return gather_csr(s->ndof, n, s->el_dofs, s->dof_adj_ptr, s->dof_adj, s->D + 1, s->el_facets, s->facet_els,
+                    el_slot, elm, fa_slot, fam, nthreads);
 }
 
 int64_t orc_csr_nnz(const orc_csr* c) { return c->rowptr.back(); }
@@ -1137,6 +1147,404 @@ int64_t orc_pipeline(const orc_space* s, const double* lset_vertex, const orc_te
   int64_t nnz = orc_csr_nnz(c);
   orc_csr_destroy(c);
   return nnz;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Space-time: cutint/spacetimecutrule.cpp:8-244 (root_finding,
+// SpaceTimeCutIntegrationRule), time basis of spacetime/SpaceTimeFE.cpp:263-281
+// (nodal on Gauss-Lobatto points), space-time element and facet-patch
+// matrices (T_CalcFacetMatrix with time_order >= 0, symboliccutbfi.cpp:2095-2160).
+// ===========================================================================
+namespace {
+
+// kt = 0 constant; kt = 1 nodes {0, 1}; kt = 2 nodes {0, 1/2, 1}
+void time_basis(int kt, double x, double* psi, double* dpsi) {
+  if (kt == 0) { psi[0] = 1.0; dpsi[0] = 0.0; return; }
+  if (kt == 1) { psi[0] = 1.0 - x; psi[1] = x; dpsi[0] = -1.0; dpsi[1] = 1.0; return; }
+  psi[0] = (1 - x) * (1 - 2 * x);
+  psi[1] = 4 * x * (1 - x);
+  psi[2] = x * (2 * x - 1);
+  dpsi[0] = 4 * x - 3;
+  dpsi[1] = 4 - 8 * x;
+  dpsi[2] = 4 * x - 1;
+}
+
+// spacetimecutrule.cpp:8-48 (orders 0..2)
+int time_roots(int kt, const double* li, double* roots) {
+  if (kt == 0) return 0;
+  if (kt == 1) {
+    if ((li[0] >= 0) != (li[1] >= 0)) { roots[0] = -li[0] / (li[1] - li[0]); return 1; }
+    return 0;
+  }
+  const double c = li[0], a = 2 * li[0] + 2 * li[2] - 4. * li[1], b = li[2] - a - c;
+  int n = 0;
+  if (std::fabs(a) < 1e-12) {
+    const double x = -c / b;
+    if (x < 1 && x > 0) roots[n++] = x;
+  } else {
+    const double w = b * b - 4 * a * c;
+    if (std::fabs(w) < 1e-12) {
+      const double x = -b / (2 * a);
+      if (x < 1 && x > 0) roots[n++] = x;
+    } else {
+      const double x1 = (b + std::sqrt(w)) / (-2.0 * a);
+      const double x2 = (b - std::sqrt(w)) / (-2.0 * a);
+      if (x1 < 1 && x1 > 0) roots[n++] = x1;
+      if (x2 < 1 && x2 > 0) roots[n++] = x2;
+    }
+  }
+  return n;
+}
+
+// SpaceTimeCutIntegrationRule (spacetimecutrule.cpp:106-244) for simplices.
+// lset_st: (kt+1)*(D+1) time-major; pts4: 4 per point (xi, eta, zeta, tau).
+int st_cut_rule(const Geo& g, const double* lset_st, int kt, int dt, int order_space, int order_time,
+                std::vector<double>& pts4, std::vector<double>& wts) {
+  const int D = g.D, nsp = D + 1;
+  pts4.clear();
+  wts.clear();
+  if (kt < 0 || kt > 2) return ERR_BAD_DECOMP;
+  std::vector<double> cut = {0.0, 1.0};
+  for (int j = 0; j < nsp; j++) {
+    double li[3], r[2];
+    for (int i = 0; i <= kt; i++) li[i] = lset_st[i * nsp + j];
+    int nr = time_roots(kt, li, r);
+    cut.insert(cut.begin(), r, r + nr);
+  }
+  std::sort(cut.begin(), cut.end());
+  const Rule& irt = get_rule(1, order_time);
+  if (order_space == -1) order_space = 5;
+  const Rule& stdir = get_rule(D, order_space);
+  const size_t maxsize = (size_t)5 * stdir.size() * (cut.size() - 1) * irt.size();
+  std::vector<double> p3, w3;
+  for (size_t i = 0; i + 1 < cut.size(); i++) {
+    const double t0 = cut[i], t1 = cut[i + 1];
+    for (int q = 0; q < irt.size(); q++) {
+      const double t = t0 + irt.p[3 * q] * (t1 - t0);
+      double psi[3], dpsi[3], cf[4];
+      time_basis(kt, t, psi, dpsi);
+      for (int j = 0; j < nsp; j++) {
+        double s = 0;
+        for (int ii = 0; ii <= kt; ii++) s += lset_st[ii * nsp + j] * psi[ii];
+        if (std::fabs(s) < 1e-14) s = s >= 0 ? 1e-14 : -1e-14;  // EPS_STCR_LSET_PERTUBATION
+        cf[j] = s;
+      }
+      const int dom = check_if_straight_cut(cf, nsp);
+      if (dom == IF) {
+        int n = straight_cut_rule(g, cf, dt, order_space, p3, w3);
+        if (n < -1) return n;
+        for (int k = 0; k < n; k++) {
+          pts4.push_back(p3[3 * k]); pts4.push_back(p3[3 * k + 1]); pts4.push_back(p3[3 * k + 2]); pts4.push_back(t);
+          wts.push_back(w3[k] * irt.w[q] * (t1 - t0));
+        }
+      } else if (dom == dt) {
+        for (int k = 0; k < stdir.size(); k++) {
+          pts4.push_back(stdir.p[3 * k]); pts4.push_back(stdir.p[3 * k + 1]); pts4.push_back(stdir.p[3 * k + 2]);
+          pts4.push_back(t);
+          wts.push_back(stdir.w[k] * irt.w[q] * (t1 - t0));
+        }
+      }
+    }
+  }
+  if (wts.size() > maxsize) return ERR_CAPACITY;
+  return wts.empty() ? -1 : (int)wts.size();
+}
+
+void lset_trace(const double* lset_st, int kt, int nsp, double tau, double* out) {
+  double psi[3], dpsi[3];
+  time_basis(kt, tau, psi, dpsi);
+  for (int j = 0; j < nsp; j++) {
+    double s = 0;
+    for (int i = 0; i <= kt; i++) s += lset_st[i * nsp + j] * psi[i];
+    if (std::fabs(s) < 1e-14) s = 1e-14;  // InterpolateToP1 perturbation of the trace
+    out[j] = s;
+  }
+}
+
+void element_lset_st(const orc_space* s, int e, const double* lset_st, int kt, double* out) {
+  const int nsp = s->D + 1;
+  for (int i = 0; i <= kt; i++)
+    for (int j = 0; j < nsp; j++) out[i * nsp + j] = lset_st[(size_t)i * s->nv + s->elv[(size_t)e * nsp + j]];
+}
+
+double st_coef(const orc_st_term& T, const Geo& g) {
+  double c = T.coef;
+  if (T.hpow != 0) c *= std::pow(std::pow(std::fabs(g.det), 1.0 / g.D), (double)T.hpow);
+  return c;
+}
+
+int st_default_order(int kind, int k) {
+  switch (kind) {
+    case ORC_TERM_LAPLACE: return 2 * k - 2;
+    case ORC_TERM_CONV: return 2 * k - 1;
+    default: return 2 * k;
+  }
+}
+
+// element matrix (nd*(kt+1))^2 of the space-time volume terms
+int st_element_matrix(const orc_space* s, const double* lset_st, int kt_l, int kt, int order_time,
+                      const orc_st_term* terms, int nterms, int e, double* elmat) {
+  const int D = s->D, nd = s->nd, nt = kt + 1, N = nd * nt, nsp = D + 1;
+  Geo g;
+  element_geo(s, e, g, nullptr, nullptr);
+  const int* gv = &s->elv[(size_t)e * nsp];
+  double lst[12];
+  element_lset_st(s, e, lset_st, kt_l, lst);
+  std::fill(elmat, elmat + (size_t)N * N, 0.0);
+  std::vector<double> pts, wts;
+  double phi[20], dphi[20][3], gp[20][3], psi[3], dpsi[3];
+  std::vector<double> F(N), GX((size_t)N * 3), FT(N);
+  for (int t = 0; t < nterms; t++) {
+    const orc_st_term& T = terms[t];
+    if (T.kind == ORC_TERM_GHOST_MASS) continue;
+    if (T.defined_on && !test_bit(T.defined_on, e)) continue;
+    const int order = T.order >= 0 ? T.order : st_default_order(T.kind, s->k);
+    int np;
+    if (T.tref >= 0) {
+      double ls[4];
+      lset_trace(lst, kt_l, nsp, T.tref, ls);
+      std::vector<double> p3, w3;
+      np = straight_cut_rule(g, ls, T.domain, order, p3, w3);
+      if (np < -1) return np;
+      pts.clear();
+      wts.clear();
+      for (int k = 0; k < np; k++) {
+        pts.push_back(p3[3 * k]); pts.push_back(p3[3 * k + 1]); pts.push_back(p3[3 * k + 2]); pts.push_back(T.tref);
+        wts.push_back(w3[k]);
+      }
+    } else {
+      np = st_cut_rule(g, lst, kt_l, T.domain, order, order_time, pts, wts);
+      if (np < -1) return np;
+    }
+    if (np <= 0) continue;
+    const double c = st_coef(T, g), meas = std::fabs(g.det);
+    for (int q = 0; q < np; q++) {
+      const double tau = pts[4 * q + 3];
+      basis(D, s->k, gv, &pts[4 * q], phi, dphi);
+      for (int i = 0; i < nd; i++) phys_grad(g, dphi[i], gp[i]);
+      time_basis(kt, tau, psi, dpsi);
+      double b[3] = {T.b[0], T.b[1], T.b[2]};
+      if (T.kind == ORC_TERM_CONV && T.omega != 0.0) {
+        const double tp = T.t0 + T.dt * tau;
+        for (int k = 0; k < 3; k++) b[k] += T.bc[k] * std::cos(T.omega * tp) + T.bs[k] * std::sin(T.omega * tp);
+      }
+      for (int it = 0; it < nt; it++)
+        for (int j = 0; j < nd; j++) {
+          const int a = it * nd + j;
+          F[a] = psi[it] * phi[j];
+          FT[a] = dpsi[it] * phi[j];
+          for (int k = 0; k < 3; k++) GX[3 * a + k] = psi[it] * gp[j][k];
+        }
+      const double w = wts[q] * meas * c;
+      for (int p = 0; p < N; p++)
+        for (int r = 0; r < N; r++) {
+          double v;
+          switch (T.kind) {
+            case ORC_TERM_MASS: v = F[p] * F[r]; break;
+            case ORC_TERM_LAPLACE: v = GX[3 * p] * GX[3 * r] + GX[3 * p + 1] * GX[3 * r + 1] + GX[3 * p + 2] * GX[3 * r + 2]; break;
+            case ORC_TERM_CONV: v = (b[0] * GX[3 * r] + b[1] * GX[3 * r + 1] + b[2] * GX[3 * r + 2]) * F[p]; break;
+            case ORC_TERM_DT_U_V: v = F[p] * FT[r]; break;
+            default: v = 0;
+          }
+          elmat[(size_t)p * N + r] += w * v;
+        }
+    }
+  }
+  return 0;
+}
+
+// space-time facet patch: spatial patch rule x time rule (symboliccutbfi.cpp:2095-2160)
+int st_patch_matrix(const orc_space* s, int kt, int order_time, const orc_st_term* terms, int nterms, int f,
+                    double* elmat) {
+  const int D = s->D, nd = s->nd, nt = kt + 1, N = nd * nt, N2 = 2 * N;
+  std::fill(elmat, elmat + (size_t)N2 * N2, 0.0);
+  const int e1 = s->facet_els[2 * f], e2 = s->facet_els[2 * f + 1];
+  if (e1 < 0 || e2 < 0) return -5;
+  Geo g1, g2;
+  element_geo(s, e1, g1, nullptr, nullptr);
+  element_geo(s, e2, g2, nullptr, nullptr);
+  const int* gv1 = &s->elv[(size_t)e1 * (D + 1)];
+  const int* gv2 = &s->elv[(size_t)e2 * (D + 1)];
+  const Rule& irt = get_rule(1, order_time);
+  for (int t = 0; t < nterms; t++) {
+    const orc_st_term& T = terms[t];
+    if (T.kind != ORC_TERM_GHOST_MASS) continue;
+    if (T.defined_on && !test_bit(T.defined_on, f)) continue;
+    const int order = T.order >= 0 ? T.order : 2 * s->k;
+    const Rule& r = get_rule(D, order);
+    const int nq = r.size();
+    std::vector<double> p1(3 * 2 * nq, 0.0), p2(3 * 2 * nq, 0.0), w1(2 * nq);
+    for (int l = 0; l < 2 * nq; l++) {
+      if (l < nq) {
+        for (int c = 0; c < 3; c++) p1[3 * l + c] = r.p[3 * l + c];
+        w1[l] = r.w[l];
+        double wd;
+        map_patch_point(g1, g2, &p1[3 * l], w1[l], &p2[3 * l], &wd);
+      } else {
+        const int m = l - nq;
+        for (int c = 0; c < 3; c++) p2[3 * l + c] = r.p[3 * m + c];
+        map_patch_point(g2, g1, &p2[3 * l], r.w[m], &p1[3 * l], &w1[l]);
+      }
+    }
+    double cc = T.coef;
+    if (T.hpow != 0) cc *= std::pow(std::pow(std::fabs(g1.det), 1.0 / D), (double)T.hpow);
+    double phi1[20], phi2[20], dphi[20][3], psi[3], dpsi[3];
+    std::vector<double> sh(N2);
+    for (int it = 0; it < irt.size(); it++) {
+      time_basis(kt, irt.p[3 * it], psi, dpsi);
+      for (int l = 0; l < 2 * nq; l++) {
+        basis(D, s->k, gv1, &p1[3 * l], phi1, dphi);
+        basis(D, s->k, gv2, &p2[3 * l], phi2, dphi);
+        for (int tt = 0; tt < nt; tt++)
+          for (int j = 0; j < nd; j++) {
+            sh[tt * nd + j] = psi[tt] * phi1[j];
+            sh[N + tt * nd + j] = -psi[tt] * phi2[j];
+          }
+        const double W = irt.w[it] * w1[l] * std::fabs(g1.det) * cc;
+        for (int a = 0; a < N2; a++)
+          for (int b = 0; b < N2; b++) elmat[(size_t)a * N2 + b] += W * sh[a] * sh[b];
+      }
+    }
+  }
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_time_basis(int kt, double tau, double* psi, double* dpsi) {
+  if (kt < 0 || kt > 2) return -1;
+  time_basis(kt, tau, psi, dpsi);
+  return kt + 1;
+}
+
+int orc_spacetime_cut_rule(int D, const double* elc, const double* lset, int kt, int dt, int order_space,
+                           int order_time, double* pts, double* wts, int maxpts) {
+  Geo g;
+  make_geo(D, elc, g);
+  std::vector<double> p, w;
+  int n = st_cut_rule(g, lset, kt, dt, order_space, order_time, p, w);
+  if (n < 0) return n;
+  if (n > maxpts) return ERR_CAPACITY;
+  std::memcpy(pts, p.data(), sizeof(double) * 4 * n);
+  std::memcpy(wts, w.data(), sizeof(double) * n);
+  return n;
+}
+
+// CutInformation::Update with a space-time level set and time_order = 0
+// (xfem/cutinfo.cpp:83-132 calling SpaceTimeCutIntegrationRule with orders 0, 0)
+int orc_cutinfo_st(const orc_space* s, const double* lset_st, int kt, uint8_t* dom, double* ratio, uint64_t* bits,
+                   int nthreads) {
+  const int ne = s->ne;
+  const int64_t nw = (ne + 63) / 64;
+  std::vector<uint8_t> d8(ne);
+  std::atomic<int> err(0);
+  parallel_for(ne, nthreads, [&](int64_t b, int64_t en) {
+    std::vector<double> pts, wts;
+    double lst[12];
+    for (int64_t e = b; e < en; e++) {
+      Geo g;
+      element_geo(s, (int)e, g, nullptr, nullptr);
+      element_lset_st(s, (int)e, lset_st, kt, lst);
+      double part_vol[2] = {0.0, 0.0};
+      for (int np : {POS, NEG}) {
+        int n = st_cut_rule(g, lst, kt, np, 0, 0, pts, wts);
+        if (n < -1) err = n;
+        for (int q = 0; q < n; q++) part_vol[np] += wts[q];
+      }
+      ratio[e] = part_vol[NEG] / (part_vol[NEG] + part_vol[POS]);
+      uint8_t t = part_vol[NEG] > 0.0 ? (part_vol[POS] > 0.0 ? IF : NEG) : POS;
+      d8[e] = t;
+      dom[e] = t;
+    }
+  });
+  std::memset(bits, 0, sizeof(uint64_t) * nw * 8);
+  for (int e = 0; e < ne; e++) {
+    int cdt = d8[e] == NEG ? 1 : (d8[e] == POS ? 2 : 4);
+    for (int c = 0; c < 8; c++)
+      if ((c & cdt) || c == 7) bits[c * nw + (e >> 6)] |= (uint64_t)1 << (e & 63);
+  }
+  return err.load();
+}
+
+int orc_st_element_matrix(const orc_space* s, const double* lset_st, int kt_l, int kt, int order_time,
+                          const orc_st_term* terms, int nterms, int e, double* elmat) {
+  return st_element_matrix(s, lset_st, kt_l, kt, order_time, terms, nterms, e, elmat);
+}
+
+orc_csr* orc_assemble_st(const orc_space* s, const double* lset_st, int kt_l, int kt, int order_time,
+                         const orc_st_term* terms, int nterms, int nthreads) {
+  const int ne = s->ne, nd = s->nd, nt = kt + 1, N = nd * nt, N2 = 2 * N;
+  const int64_t nf = s->nfacets, ndof = s->ndof * nt;
+  std::vector<int32_t> ed((size_t)ne * N);
+  for (int e = 0; e < ne; e++)
+    for (int it = 0; it < nt; it++)
+      for (int j = 0; j < nd; j++) ed[(size_t)e * N + it * nd + j] = (int32_t)(it * s->ndof + s->el_dofs[(size_t)e * nd + j]);
+  std::vector<int64_t> ptr(ndof + 1, 0);
+  for (size_t i = 0; i < ed.size(); i++) ptr[ed[i] + 1]++;
+  for (int64_t i = 0; i < ndof; i++) ptr[i + 1] += ptr[i];
+  std::vector<int32_t> adj(ed.size());
+  {
+    std::vector<int64_t> fill(ptr.begin(), ptr.end() - 1);
+    for (int e = 0; e < ne; e++)
+      for (int i = 0; i < N; i++) adj[fill[ed[(size_t)e * N + i]]++] = e * 32 + i;
+  }
+  std::vector<int32_t> el_slot(ne, -1), fa_slot(nf, -1);
+  int nact = 0, nfa = 0;
+  for (int e = 0; e < ne; e++) {
+    bool act = false;
+    for (int t = 0; t < nterms; t++)
+      if (terms[t].kind != ORC_TERM_GHOST_MASS && (!terms[t].defined_on || test_bit(terms[t].defined_on, e))) act = true;
+    if (act) el_slot[e] = nact++;
+  }
+  for (int64_t f = 0; f < nf; f++) {
+    if (s->facet_els[2 * f + 1] < 0) continue;
+    bool act = false;
+    for (int t = 0; t < nterms; t++)
+      if (terms[t].kind == ORC_TERM_GHOST_MASS && (!terms[t].defined_on || test_bit(terms[t].defined_on, f))) act = true;
+    if (act) fa_slot[f] = nfa++;
+  }
+  std::vector<int32_t> el_list(nact), fa_list(nfa);
+  for (int e = 0; e < ne; e++) if (el_slot[e] >= 0) el_list[el_slot[e]] = e;
+  for (int64_t f = 0; f < nf; f++) if (fa_slot[f] >= 0) fa_list[fa_slot[f]] = (int32_t)f;
+  std::vector<double> elm((size_t)nact * N * N), fam((size_t)nfa * N2 * N2);
+  std::atomic<int> err(0);
+  parallel_for(nact, nthreads, [&](int64_t b, int64_t en) {
+    for (int64_t i = b; i < en; i++) {
+      int r = st_element_matrix(s, lset_st, kt_l, kt, order_time, terms, nterms, el_list[i], &elm[(size_t)i * N * N]);
+      if (r) err = r;
+    }
+  });
+  parallel_for(nfa, nthreads, [&](int64_t b, int64_t en) {
+    for (int64_t i = b; i < en; i++) {
+      int r = st_patch_matrix(s, kt, order_time, terms, nterms, fa_list[i], &fam[(size_t)i * N2 * N2]);
+      if (r) err = r;
+    }
+  });
+  if (err.load()) return nullptr;
+  return gather_csr(ndof, N, ed, ptr, adj, s->D + 1, s->el_facets, s->facet_els, el_slot, elm, fa_slot, fam, nthreads);
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// Integrate(1 * dCut(lset_st, dt, order, time_order)) over the space-time slab
+double orc_integrate_st(const orc_space* s, const double* lset_st, int kt, int dt, int order_space, int order_time) {
+  double sum = 0;
+  std::vector<double> pts, wts;
+  double lst[12];
+  for (int e = 0; e < s->ne; e++) {
+    Geo g;
+    element_geo(s, e, g, nullptr, nullptr);
+    element_lset_st(s, e, lset_st, kt, lst);
+    int n = st_cut_rule(g, lst, kt, dt, order_space, order_time, pts, wts);
+    for (int q = 0; q < n; q++) sum += wts[q] * std::fabs(g.det);
+  }
+  return sum;
 }
 
 }  // extern "C"

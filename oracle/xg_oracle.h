@@ -31,7 +31,8 @@ enum {
   ORC_TERM_NGRADU_V = 2,   /* c * (n . grad u) * v, n = grad(lset)/|grad(lset)| */
   ORC_TERM_U_NGRADV = 3,   /* c * u * (n . grad v)               */
   ORC_TERM_CONV = 4,       /* c * (b . grad u) * v               */
-  ORC_TERM_GHOST_MASS = 5  /* c * (u - u.Other()) * (v - v.Other()) on a facet patch */
+  ORC_TERM_GHOST_MASS = 5, /* c * (u - u.Other()) * (v - v.Other()) on a facet patch */
+  ORC_TERM_DT_U_V = 6      /* space-time: c * v * d/dtau u (dtref) */
 };
 
 typedef struct {
@@ -87,6 +88,30 @@ orc_csr* orc_assemble(const orc_space*, const double* lset_vertex, const orc_ter
 int64_t orc_csr_nnz(const orc_csr*);
 void orc_csr_get(const orc_csr*, int64_t* rowptr, int32_t* cols, double* vals);
 void orc_csr_destroy(orc_csr*);
+
+/* --- space-time (P1 space level set x P_kt time, Gauss-Lobatto time nodes) --- */
+typedef struct {
+  int kind, domain, order, hpow;
+  double coef;
+  double b[3];
+  const uint64_t* defined_on;
+  double tref;          /* < 0: over the slab; >= 0: fixed time tau = tref (spatial rule of the trace) */
+  double bc[3], bs[3];  /* convection b(t) = b + bc cos(omega t) + bs sin(omega t) */
+  double omega, t0, dt; /* t = t0 + dt * tau */
+} orc_st_term;
+int orc_time_basis(int kt, double tau, double* psi, double* dpsi);
+/* lset: (kt+1)*(D+1) time-major; points: 4 doubles (xi, eta, zeta, tau). */
+int orc_spacetime_cut_rule(int D, const double* elc, const double* lset, int kt, int dt, int order_space,
+                           int order_time, double* pts, double* wts, int maxpts);
+/* lset_st: (kt+1)*nv time-major */
+int orc_cutinfo_st(const orc_space*, const double* lset_st, int kt, uint8_t* dom, double* ratio, uint64_t* bits,
+                   int nthreads);
+int orc_st_element_matrix(const orc_space*, const double* lset_st, int kt_l, int kt, int order_time,
+                          const orc_st_term* terms, int nterms, int e, double* elmat);
+double orc_integrate_st(const orc_space*, const double* lset_st, int kt, int dt, int order_space, int order_time);
+/* space-time assembly; dof (it, j) -> it*ndof_space + j */
+orc_csr* orc_assemble_st(const orc_space*, const double* lset_st, int kt_l, int kt, int order_time,
+                         const orc_st_term* terms, int nterms, int nthreads);
 
 /* Whole CPU pipeline (CutInfo + facet marking + assembly) for timing: returns nnz. */
 int64_t orc_pipeline(const orc_space*, const double* lset_vertex, const orc_term* terms, int nterms,

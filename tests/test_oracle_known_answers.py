@@ -224,3 +224,44 @@ def test_cutinfo_config1(orc):
     # ratio rounds to 1.0
     assert np.all(ratio[dom == orc.NEG] == 1.0) and np.all(ratio[dom == orc.POS] == 0.0)
     assert np.all((ratio[dom == orc.IF] >= 0) & (ratio[dom == orc.IF] <= 1))
+
+
+@pytest.mark.parametrize("dt,ref", [(0, 7 / 8), (1, 1 / 8), (2, 0.5)])
+def test_spacetime_planar_cut(orc, dt, ref):
+    """tests/pytests/test_spacetimecutrule.py:41-69: lset 1-2x-2t, P1 in time,
+    order 0 in space and time: POS 1/8, NEG 7/8, IF 1/2 to 5e-15."""
+    m = MakeStructured2DMesh(1, 1)
+    sp = orc.Space(m, 1)
+    X = m.coords[:, 0]
+    lst = np.stack([orc.interpolate_p1_perturb(1 - 2 * X), orc.interpolate_p1_perturb(-1 - 2 * X)])
+    assert abs(sp.integrate_st(lst, 1, dt, 0, 0) - ref) < 5e-15
+
+
+def test_spacetime_time_basis(orc):
+    for kt in (1, 2):
+        nodes = [0.0, 1.0] if kt == 1 else [0.0, 0.5, 1.0]
+        for i, x in enumerate(nodes):
+            psi, _ = orc.time_basis(kt, x)
+            assert np.allclose(psi, np.eye(kt + 1)[i])
+        # derivative by central differences
+        psi_p, _ = orc.time_basis(kt, 0.3 + 1e-6)
+        psi_m, _ = orc.time_basis(kt, 0.3 - 1e-6)
+        _, dpsi = orc.time_basis(kt, 0.3)
+        assert np.allclose((psi_p - psi_m) / 2e-6, dpsi, atol=1e-8)
+
+
+def test_spacetime_moving_circle(orc):
+    """Circle r=0.25 moving on (0.5+0.2cos 2pi t, 0.5+0.2 sin 2pi t), one slab
+    dt=1/16 with P2-in-time level set: slab-averaged area and perimeter O(h^2)."""
+    m = MakeStructured2DMesh(32, 32)
+    sp = orc.Space(m, 1)
+
+    def lsetf(t):
+        cx, cy = 0.5 + 0.2 * math.cos(2 * math.pi * t), 0.5 + 0.2 * math.sin(2 * math.pi * t)
+        return orc.interpolate_p1_perturb(np.sqrt((m.coords[:, 0] - cx) ** 2 + (m.coords[:, 1] - cy) ** 2) - 0.25)
+
+    dt = 1 / 16
+    lst = np.stack([lsetf(0), lsetf(dt / 2), lsetf(dt)])
+    h = 1 / 32
+    assert abs(sp.integrate_st(lst, 2, orc.NEG, 2, 4) - math.pi * 0.0625) < 2 * h * h
+    assert abs(sp.integrate_st(lst, 2, orc.IF, 2, 4) - 2 * math.pi * 0.25) < 2 * h * h
