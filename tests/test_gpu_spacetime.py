@@ -54,7 +54,8 @@ def test_cutinfo_st_parity(xg, orc, case):
     d_dom = torch.zeros(m.ne, dtype=torch.uint8, device="cuda")
     d_ratio = torch.zeros(m.ne, dtype=torch.float64, device="cuda")
     d_bits = torch.zeros((8, (m.ne + 63) // 64), dtype=torch.int64, device="cuda")
-    xg._lib.call("xg_cutinfo_update_st", dm.h, xg._vp(dev(lst)), kt, xg._vp(d_dom), xg._vp(d_ratio), xg._vp(d_bits),
+    d_lst = dev(lst)  # keep the device buffers alive until the kernels have run
+    xg._lib.call("xg_cutinfo_update_st", dm.h, xg._vp(d_lst), kt, xg._vp(d_dom), xg._vp(d_ratio), xg._vp(d_bits),
                  xg._stream())
     dm.check()
     assert np.array_equal(d_dom.cpu().numpy(), dom)
@@ -76,8 +77,9 @@ def test_st_cut_rules_parity(xg, orc, case, dt, orders):
     counts = torch.zeros(n, dtype=torch.int32, device="cuda")
     pts = torch.zeros((n, maxp, 4), dtype=torch.float64, device="cuda")
     wts = torch.zeros((n, maxp), dtype=torch.float64, device="cuda")
-    xg._lib.call("xg_st_cut_rules", dm.h, xg._vp(dev(lst)), kt, xg._vp(dev(els, torch.int32)), n, dt, orders[0],
-                 orders[1], maxp, xg._vp(counts), xg._vp(pts), xg._vp(wts), xg._stream())
+    d_lst, d_els = dev(lst), dev(els, torch.int32)  # alive until the kernel has run
+    xg._lib.call("xg_st_cut_rules", dm.h, xg._vp(d_lst), kt, xg._vp(d_els), n, dt, orders[0], orders[1], maxp,
+                 xg._vp(counts), xg._vp(pts), xg._vp(wts), xg._stream())
     dm.check()
     counts, pts, wts = counts.cpu().numpy(), pts.cpu().numpy(), wts.cpu().numpy()
     D = m.dim
@@ -88,7 +90,8 @@ def test_st_cut_rules_parity(xg, orc, case, dt, orders):
             assert counts[i] == -1
             continue
         p, w = r
-        assert counts[i] == len(w)
+        assert counts[i] == len(w), (int(e), counts[i], len(w), pts[i, : max(counts[i], 0)].tolist(), p.tolist(),
+                                     wts[i, : max(counts[i], 0)].tolist(), w.tolist(), lst[:, vs].tolist())
         assert np.max(np.abs(pts[i, : len(w)] - p)) <= 1e-14
         assert np.max(np.abs(wts[i, : len(w)] - w)) <= 1e-14 * np.max(np.abs(w))
     assert D in (2, 3)
