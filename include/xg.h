@@ -277,6 +277,25 @@ int xg_cutfem_step(xg_form* form, const double* d_lset, xg_csr* out, void* strea
 int xg_cutfem_marking(xg_form* form, const uint8_t** d_dom, const double** d_cut_ratio, const uint64_t** d_bits,
                       const uint64_t** d_facets);
 
+/* ---- batched steps in one CUDA graph --------------------------------------- */
+/* No counterpart in the reference, which assembles one form per
+ * BilinearForm::Assemble call (NGSolve's TaskManager parallelises inside it).
+ * Captures, once, the steps (forms[i], d_lsets[i], outs[i]) i < n -
+ * xg_cutfem_step for plain forms, xg_st_cutfem_step for space-time ones - into
+ * one CUDA graph: the steps of distinct forms are independent branches that
+ * run concurrently, repeated entries of the same form run in list order.
+ * Pointers are baked into the graph, so level sets and outputs must stay at
+ * the same addresses (the caller updates their contents between launches);
+ * distinct forms must write distinct outputs.  Stage events are off inside the
+ * graph.  Check each form with xg_form_check after a launch. */
+typedef struct xg_step_graph xg_step_graph;
+int xg_step_graph_create(xg_form* const* forms, const double* const* d_lsets, const xg_csr* outs, int32_t n,
+                         xg_step_graph** out);
+int xg_step_graph_launch(xg_step_graph* graph, void* stream);
+/* Number of kernel nodes of the graph (the kernels one launch runs). */
+int xg_step_graph_kernel_count(const xg_step_graph* graph, int64_t* h_out);
+int xg_step_graph_destroy(xg_step_graph* graph);
+
 #ifdef __cplusplus
 }
 #endif

@@ -28,7 +28,8 @@ EXPORTS = [
     "xg_form_create", "xg_form_destroy", "xg_form_set_defined_on", "xg_form_capacity",
     "xg_form_assemble", "xg_form_check", "xg_form_stage_events", "xg_cutfem_step", "xg_cutfem_marking",
     "xg_space_create_st", "xg_space_info_st", "xg_cutinfo_update_st", "xg_st_cut_rules", "xg_st_form_create",
-    "xg_st_cutfem_step",
+    "xg_st_cutfem_step", "xg_step_graph_create", "xg_step_graph_launch", "xg_step_graph_destroy",
+    "xg_step_graph_kernel_count",
 ]
 
 
@@ -119,6 +120,10 @@ def load():
         "xg_form_stage_events": (I, [P, P, I]),
         "xg_cutfem_step": (I, [P, P, P, P]),
         "xg_cutfem_marking": (I, [P, P, P, P, P]),
+        "xg_step_graph_create": (I, [P, P, P, I, P]),
+        "xg_step_graph_launch": (I, [P, P]),
+        "xg_step_graph_destroy": (I, [P]),
+        "xg_step_graph_kernel_count": (I, [P, P]),
         "xg_space_create_st": (I, [P, I, I, P]),
         "xg_space_info_st": (I, [P, P]),
         "xg_cutinfo_update_st": (I, [P, P, I, P, P, P, P]),

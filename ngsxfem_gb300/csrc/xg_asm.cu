@@ -1145,6 +1145,26 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_row_count(ScatterArgs A, int
   }
 }
 
+// Full-pattern probe (form creation): distinct columns per dof with every
+// element and interior facet active; sizes the scatter buffers.
+__global__ void __launch_bounds__(kRowWarps * 32) k_row_probe(ScatterArgs A, int64_t ndof, int64_t* rowcnt, int* err) {
+  extern __shared__ __align__(16) unsigned char sm_rows[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const RowSm S = row_sm(A, sm_rows + (size_t)warp * A.wbytes);
+  for (int64_t r = blockIdx.x * (int64_t)kRowWarps + warp; r < ndof; r += (int64_t)gridDim.x * kRowWarps) {
+    const bool ok = row_columns(A, S, (int)r);
+    const int u = hash_extract(A, S, false);
+    if (lane == 0) {
+      if (!ok) set_err(err, XG_ERR_CAPACITY);
+      rowcnt[r] = u;
+    }
+  }
+}
+
+__global__ void k_fill_u32(uint32_t* p, int64_t n, uint32_t v) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = v;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kRowWarps * 32) k_row_fill(ScatterArgs A, const T* __restrict__ elmat,
                                                              const T* __restrict__ famat,
@@ -1777,6 +1797,62 @@ int xg_form_create(xg_space* space, const xg_term* terms, int32_t nterms, int pr
 
 namespace {
 
+// Full pattern (every element and interior facet active) on the GPU: exact
+// distinct-column count per dof -> row offsets of the column scratch, its
+// size and the widest row.  Returns XG_ERR_CAPACITY if a row does not fit the
+// probe's hash table (the caller then counts on the host).
+int full_pattern_probe(xg_form* f, std::vector<int64_t>& full_ptr) {
+  xg_mesh* m = f->mesh;
+  xg_space* sp = f->space;
+  const int64_t ndof = sp->ndof;
+  int32_t* d_rows = nullptr;
+  std::vector<int32_t> iota(ndof);
+  for (int64_t i = 0; i < ndof; i++) iota[i] = (int32_t)i;
+  XG_CUDA(cudaMalloc((void**)&d_rows, sizeof(int32_t) * (ndof > 0 ? ndof : 1)));
+  cudaError_t e = cudaMemcpy(d_rows, iota.data(), sizeof(int32_t) * ndof, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(f->d_act_cut, 0, f->nw32_el * 4);
+  if (e != cudaSuccess) {
+    cudaFree(d_rows);
+    return cuda_fail(e, "full_pattern_probe");
+  }
+  k_fill_u32<<<152 * 4, 256>>>(f->d_act_un, f->nw32_el, 0xffffffffu);
+  if (f->has_patch) {
+    FormDesc all = {};
+    all.npatch = 1;
+    k_active_facets<<<(unsigned)((f->nw32_fa * 32 + 255) / 256), 256>>>(m->nfacets, m->d_facet_els, all, f->d_act_fa,
+                                                                         f->nw32_fa);
+  } else {
+    cudaMemset(f->d_act_fa, 0, f->nw32_fa * 4);
+  }
+  ScatterArgs A = scatter_args(f);
+  A.rows = d_rows;
+  A.hs = 4096;
+  A.maxu = 0;
+  A.stage = 0;
+  A.wbytes = (row_smem_bytes(A.hs, 0, 0) + 15) & ~15;
+  const size_t smem = (size_t)kRowWarps * A.wbytes;
+  cudaFuncSetAttribute(k_row_probe, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const int grid = grid_for(k_row_probe, kRowWarps * 32, smem);
+  k_row_probe<<<grid, kRowWarps * 32, smem>>>(A, ndof, f->d_rowcnt, f->d_err);
+  std::vector<int64_t> cnt(ndof);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpy(cnt.data(), f->d_rowcnt, sizeof(int64_t) * ndof, cudaMemcpyDeviceToHost);
+  int herr = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&herr, f->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(d_rows);
+  if (e != cudaSuccess) return cuda_fail(e, "full_pattern_probe");
+  if (herr) return XG_ERR_CAPACITY;
+  full_ptr.assign(ndof + 1, 0);
+  int mx = 0;
+  for (int64_t r = 0; r < ndof; r++) {
+    full_ptr[r + 1] = full_ptr[r] + cnt[r];
+    mx = std::max(mx, (int)cnt[r]);
+  }
+  f->full_nnz = full_ptr[ndof];
+  f->max_unique = mx;
+  return XG_OK;
+}
+
 // device workspace of a form, sized for the whole mesh
 int form_workspace(xg_form* f) {
   xg_space* space = f->space;
@@ -1795,18 +1871,9 @@ int form_workspace(xg_form* f) {
   int64_t maxw = std::max(f->nw32_el, std::max(f->nw32_fa, f->nw32_dof));
   f->nbsum = (int)((maxw + kCChunk - 1) / kCChunk) + 1;
   f->nbsum64 = (int)((space->ndof + kSChunk - 1) / kSChunk) + 1;
-  // scatter buffers sized by the widest row of the full pattern
+  // scatter buffers sized by the widest row of the full pattern (probed on the
+  // GPU below, after the workspace exists)
   std::vector<int64_t> full_ptr;
-  full_pattern_stats(f, &f->full_nnz, &f->max_unique, full_ptr);
-  {
-    int maxu = 32;
-    while (maxu < f->max_unique) maxu <<= 1;
-    f->sc_maxu = maxu;
-    f->sc_hs = 2 * maxu;
-    f->sc_stage = nd * std::max(1, 192 / nd);
-    f->sc_wbytes = (row_smem_bytes(f->sc_hs, f->sc_maxu, f->sc_stage) + 15) & ~15;
-    f->sc_smem = (size_t)kRowWarps * f->sc_wbytes;
-  }
   auto A = [&](void** p, size_t bytes) { return cudaMalloc(p, bytes ? bytes : 16); };
   cudaError_t e = cudaSuccess;
   e = e ? e : A((void**)&f->d_act_un, f->nw32_el * 4);
@@ -1820,10 +1887,6 @@ int form_workspace(xg_form* f) {
   e = e ? e : A((void**)&f->d_fa_slot, (size_t)m->nfacets * 4);
   e = e ? e : A((void**)&f->d_dof_row, (size_t)space->ndof * 4);
   e = e ? e : A((void**)&f->d_rowcnt, (size_t)space->ndof * 8);
-  e = e ? e : A((void**)&f->d_full_ptr, (size_t)(space->ndof + 1) * 8);
-  e = e ? e : A((void**)&f->d_tmp_cols, (size_t)f->full_nnz * 4);
-  if (e == cudaSuccess)
-    e = cudaMemcpy(f->d_full_ptr, full_ptr.data(), (size_t)(space->ndof + 1) * 8, cudaMemcpyHostToDevice);
   e = e ? e : A((void**)&f->d_counts, 8 * sizeof(int));
   e = e ? e : A((void**)&f->d_bsum, (size_t)f->nbsum * 4);
   e = e ? e : A((void**)&f->d_bsum64, (size_t)f->nbsum64 * 8);
@@ -1836,6 +1899,27 @@ int form_workspace(xg_form* f) {
   e = e ? e : A((void**)&f->d_fbits, (size_t)(f->nw32_fa / 2) * 8);
   if (e == cudaSuccess) e = cudaMemset(f->d_err, 0, sizeof(int));
   if (e == cudaSuccess) e = cudaMemset(f->d_counts, 0, 8 * sizeof(int));
+  if (e != cudaSuccess) return cuda_fail(e, "xg_form_create");
+  int pst = full_pattern_probe(f, full_ptr);
+  if (pst == XG_ERR_CAPACITY) {
+    cudaMemset(f->d_err, 0, sizeof(int));
+    full_pattern_stats(f, &f->full_nnz, &f->max_unique, full_ptr);  // very wide rows: exact host count
+  } else if (pst) {
+    return pst;
+  }
+  {
+    int maxu = 32;
+    while (maxu < f->max_unique) maxu <<= 1;
+    f->sc_maxu = maxu;
+    f->sc_hs = 2 * maxu;
+    f->sc_stage = nd * std::max(1, 192 / nd);
+    f->sc_wbytes = (row_smem_bytes(f->sc_hs, f->sc_maxu, f->sc_stage) + 15) & ~15;
+    f->sc_smem = (size_t)kRowWarps * f->sc_wbytes;
+  }
+  e = A((void**)&f->d_full_ptr, (size_t)(space->ndof + 1) * 8);
+  e = e ? e : A((void**)&f->d_tmp_cols, (size_t)f->full_nnz * 4);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(f->d_full_ptr, full_ptr.data(), (size_t)(space->ndof + 1) * 8, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda_fail(e, "xg_form_create");
   {
     // the attribute is an upper bound shared by all forms: only ever raise it
@@ -2147,6 +2231,124 @@ int xg_cutfem_marking(xg_form* f, const uint8_t** d_dom, const double** d_ratio,
   if (d_ratio) *d_ratio = f->d_ratio;
   if (d_bits) *d_bits = f->d_bits;
   if (d_facets) *d_facets = f->d_fbits;
+  return XG_OK;
+}
+
+}  // extern "C"
+
+struct xg_step_graph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int64_t kernels = 0;
+};
+
+extern "C" {
+
+int xg_step_graph_destroy(xg_step_graph* g) {
+  if (!g) return XG_OK;
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  delete g;
+  return XG_OK;
+}
+
+int xg_step_graph_create(xg_form* const* forms, const double* const* d_lsets, const xg_csr* outs, int32_t n,
+                         xg_step_graph** out) {
+  if (!forms || !d_lsets || !outs || !out || n <= 0) return XG_ERR_ARG;
+  *out = nullptr;
+  // one branch per distinct form; entries of the same form stay in list order
+  std::vector<xg_form*> distinct;
+  std::vector<int> branch(n);
+  for (int i = 0; i < n; i++) {
+    if (!forms[i] || !d_lsets[i]) return XG_ERR_ARG;
+    auto it = std::find(distinct.begin(), distinct.end(), forms[i]);
+    branch[i] = (int)(it - distinct.begin());
+    if (it == distinct.end()) distinct.push_back(forms[i]);
+  }
+  for (size_t a = 0; a < distinct.size(); a++)
+    for (size_t b = a + 1; b < distinct.size(); b++)
+      for (int i = 0; i < n; i++)
+        for (int j = 0; j < n; j++)
+          if (forms[i] == distinct[a] && forms[j] == distinct[b] && outs[i].d_vals == outs[j].d_vals) {
+            set_last_error("xg_step_graph_create: distinct forms must write distinct outputs");
+            return XG_ERR_ARG;
+          }
+  const int nb = (int)distinct.size();
+  std::vector<cudaStream_t> streams(nb, nullptr);
+  std::vector<cudaEvent_t> done(nb, nullptr);
+  cudaEvent_t fork = nullptr;
+  std::vector<xg_csr> o(outs, outs + n);
+  std::vector<bool> use_ev(nb);
+  auto release = [&]() {
+    for (int b = 0; b < nb; b++) {
+      if (streams[b]) cudaStreamDestroy(streams[b]);
+      if (done[b]) cudaEventDestroy(done[b]);
+      distinct[b]->use_ev = use_ev[b];
+    }
+    if (fork) cudaEventDestroy(fork);
+  };
+  cudaError_t e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+  for (int b = 0; b < nb && e == cudaSuccess; b++) {
+    use_ev[b] = distinct[b]->use_ev;
+    distinct[b]->use_ev = false;
+    e = cudaStreamCreateWithFlags(&streams[b], cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&done[b], cudaEventDisableTiming);
+  }
+  if (e != cudaSuccess) {
+    release();
+    return cuda_fail(e, "xg_step_graph_create");
+  }
+  // capture on branch 0's stream; the others fork from it and join back
+  cudaStream_t s0 = streams[0];
+  e = cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) e = cudaEventRecord(fork, s0);
+  for (int b = 1; b < nb && e == cudaSuccess; b++) e = cudaStreamWaitEvent(streams[b], fork, 0);
+  int st = XG_OK;
+  for (int i = 0; i < n && e == cudaSuccess && !st; i++) {
+    xg_form* f = forms[i];
+    void* s = (void*)streams[branch[i]];
+    st = f->st ? xg_st_cutfem_step(f, d_lsets[i], &o[i], s) : xg_cutfem_step(f, d_lsets[i], &o[i], s);
+  }
+  for (int b = 1; b < nb && e == cudaSuccess; b++) {
+    e = cudaEventRecord(done[b], streams[b]);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s0, done[b], 0);
+  }
+  cudaGraph_t graph = nullptr;
+  cudaError_t e2 = cudaStreamEndCapture(s0, &graph);
+  if (e == cudaSuccess) e = e2;
+  auto* g = new xg_step_graph();
+  g->graph = graph;
+  if (e == cudaSuccess && !st) e = cudaGraphInstantiate(&g->exec, graph, 0);
+  if (e == cudaSuccess && !st) {
+    size_t nn = 0;
+    e = cudaGraphGetNodes(graph, nullptr, &nn);
+    std::vector<cudaGraphNode_t> nodes(nn);
+    if (e == cudaSuccess && nn) e = cudaGraphGetNodes(graph, nodes.data(), &nn);
+    for (size_t k = 0; k < nn && e == cudaSuccess; k++) {
+      cudaGraphNodeType t;
+      e = cudaGraphNodeGetType(nodes[k], &t);
+      if (e == cudaSuccess && t == cudaGraphNodeTypeKernel) g->kernels++;
+    }
+  }
+  release();
+  if (st || e != cudaSuccess) {
+    xg_step_graph_destroy(g);
+    cudaGetLastError();
+    return st ? st : cuda_fail(e, "xg_step_graph_create");
+  }
+  *out = g;
+  return XG_OK;
+}
+
+int xg_step_graph_kernel_count(const xg_step_graph* g, int64_t* out) {
+  if (!g || !out) return XG_ERR_ARG;
+  *out = g->kernels;
+  return XG_OK;
+}
+
+int xg_step_graph_launch(xg_step_graph* g, void* stream) {
+  if (!g || !g->exec) return XG_ERR_ARG;
+  XG_CUDA(cudaGraphLaunch(g->exec, (cudaStream_t)stream));
   return XG_OK;
 }
 

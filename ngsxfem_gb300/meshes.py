@@ -80,3 +80,51 @@ def MakeStructured3DMesh(nx=4, ny=None, nz=None, box=((0.0, 1.0), (0.0, 1.0), (0
         tets.append(np.stack([base, base + step[a], base + step[a] + step[b], v111], axis=1))
     el = np.stack(tets, axis=1).reshape(-1, 4)
     return Mesh(coords, el)
+
+
+def concatenate(meshes):
+    """One mesh holding several independent meshes (vertex numbers offset), so a
+    batch of meshes is assembled by one step; each component keeps its own
+    dofs, rows and columns (the matrix is block diagonal)."""
+    coords = np.concatenate([m.coords for m in meshes])
+    off = np.cumsum([0] + [m.nv for m in meshes[:-1]])
+    el = np.concatenate([m.elements + o for m, o in zip(meshes, off)])
+    out = Mesh(coords, el)
+    out.component_vertex_offsets = off
+    out.component_element_counts = np.array([m.ne for m in meshes])
+    return out
+
+
+def replicated_circle_2d(copies, n=40, r=0.5):
+    """`copies` replicas of [-1,1]^2 with n x n x 2 triangles and the level set
+    sqrt(x^2+y^2) - r at the vertices (the 2D circle configuration)."""
+    base = MakeStructured2DMesh(n, n, -1.0, 1.0, -1.0, 1.0)
+    vals = np.sqrt(base.coords[:, 0] ** 2 + base.coords[:, 1] ** 2) - r
+    m = concatenate([base] * copies)
+    return m, np.tile(vals, copies)
+
+
+def batched_ellipsoids(count=512, min_tets=1e3, max_tets=2e5, seed=20261203):
+    """Independent unit-cube Kuhn meshes with log-uniform target sizes (the mesh
+    with 6 n^3 tets closest to the target, n >= 6), each with a rotated ellipsoid
+    level set (centre U[0.3,0.7]^3, semi-axes U[0.1,0.4], rotation = Q of a QR
+    factorisation of a Gaussian 3x3 with sign-fixed diagonal) and an H1 order
+    drawn from {1,2,3}.  Returns a list of (n, order, centre, semi-axes, rotation);
+    `ellipsoid_values` turns one entry into vertex values."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        size = np.exp(rng.uniform(np.log(min_tets), np.log(max_tets)))
+        n = max(6, int(round((size / 6.0) ** (1.0 / 3.0))))
+        centre = rng.uniform(0.3, 0.7, 3)
+        axes = rng.uniform(0.1, 0.4, 3)
+        q, r = np.linalg.qr(rng.standard_normal((3, 3)))
+        q = q * np.sign(np.diag(r))
+        order = int(rng.integers(1, 4))
+        out.append((n, order, centre, axes, q))
+    return out
+
+
+def ellipsoid_values(coords, centre, axes, rot):
+    y = (coords - centre) @ rot
+    return np.sqrt(((y / axes) ** 2).sum(axis=1)) - 1.0
