@@ -1,22 +1,41 @@
 """Benchmark of the cut-element assembly step on one GB300.
 
-Workload (the 3D CutFEM Poisson configuration): unit cube, 64^3 cubes x 6
-Kuhn tetrahedra (1,572,864 tets), level set
-phi = |x - 0.5| - 0.3 + 0.02 sin(7x) sin(7y) sin(7z) interpolated to P1 (with
-InterpolateToP1's +1e-14 perturbation), P2 H1 space, NEG-domain stiffness,
-Nitsche interface terms (lambda = 10 k^2 = 40, scaled by 1/h) on IF and ghost
-penalty 0.1/h^2 (u - u')(v - v') on the facets between HASNEG and IF
-elements.  Synthetic, seeded data (the reference publishes no dataset).
-
 One step = CutInfo marking + ghost-facet marking + cut rules + element and
 facet-patch matrices + the deterministic scatter into a compressed-row
-matrix (xg_cutfem_step).  metric = cut (IF) elements per second.
+matrix (xg_cutfem_step / xg_st_cutfem_step), for every form of the workload,
+replayed as one CUDA graph (xg_step_graph_launch).  metric = cut (IF)
+elements per second.  All inputs are synthetic and seeded (the reference
+publishes no dataset).
 
-    python bench.py [--steps K] [--warmup W] [--precision fp64|mixed] [--impl xg|reference]
+Workloads (--workload):
+  c2 (default)  3D CutFEM Poisson: unit cube, 64^3 cubes x 6 Kuhn tetrahedra
+                (1,572,864 tets), level set
+                phi = |x - 0.5| - 0.3 + 0.02 sin(7x) sin(7y) sin(7z) as P1 (with
+                InterpolateToP1's +1e-14 perturbation), P2 H1 space, NEG-domain
+                stiffness, Nitsche interface terms (lambda = 10 k^2, scaled by
+                1/h) on IF and ghost penalty 0.1/h^2 (u - u')(v - v') on the
+                facets between HASNEG and IF elements.
+  c1            the 2D circle case ([-1,1]^2, 40 x 40 x 2 triangles,
+                phi = sqrt(x^2 + y^2) - 0.5, P1, u v + grad u . grad v on NEG and
+                u v on IF) as 512 replicas in one mesh (one launch).
+  c3            512 independent unit-cube tet meshes of log-uniform sizes
+                1e3..2e5 tets, rotated-ellipsoid level sets, H1 order drawn from
+                {1, 2, 3}; the meshes of one order form one disconnected mesh,
+                the three order groups run as concurrent branches of one graph.
+                Form: the c2 form (stiffness + Nitsche + ghost penalty).
+  c5            space-time: [0,1]^2 with 256 x 256 x 2 triangles, P1 in space x
+                P1 in time, circle of radius 0.25 moving on
+                (0.5 + 0.2 cos 2 pi t, 0.5 + 0.2 sin 2 pi t), 16 slabs of
+                dt = 1/16, convection-diffusion form of the unfitted space-time
+                DG demo with ghost penalty; the 16 slab steps are one graph.
+
+    python bench.py [--steps K] [--warmup W] [--precision fp64|mixed] [--workload c2|c1|c3|c5]
+                    [--impl xg|reference]
 """
 import argparse
 import ctypes
 import json
+import math
 import os
 import subprocess
 import sys
@@ -29,9 +48,16 @@ sys.path.insert(0, ROOT)
 
 METRIC = "cut elems/s, rule+assembly, 1 GB300: plain FP64 vs learned/mixed at equal error"
 UNIT = "cut_elems/s"
+SEED = 20261203
+C5_DT = 1.0 / 16
+C5_SLABS = 16
+C5_KT = [1]  # time order of the c5 level set (set from --kt)
 
 
-def workload(n):
+# ----------------------------------------------------------------------------
+# workloads (host side, shared by both arms)
+# ----------------------------------------------------------------------------
+def c2_mesh(n):
     from ngsxfem_gb300.meshes import MakeStructured3DMesh
     m = MakeStructured3DMesh(n)
     X, Y, Z = m.coords.T
@@ -51,6 +77,178 @@ def terms_c2(order):
     ]
 
 
+def terms_c1():
+    return [
+        dict(kind=0, domain=0, coef=1.0, hpow=0),       # u v on NEG (order 2)
+        dict(kind=1, domain=0, coef=1.0, hpow=0),       # grad u . grad v on NEG (order 0)
+        dict(kind=0, domain=2, coef=1.0, hpow=0),       # u v on IF (order 2)
+    ]
+
+
+def terms_c5(t0):
+    """demos/spacetime/spacetimeDG_unfitted.py:158-168 without deformation:
+    v dt(u) dQ + dt grad u.grad v dQ + dt v (w.grad u) dQ + u v dOmold
+    + ghost penalty (gamma dt / h^2 and gamma dt^2 / h^3 patch terms)."""
+    w = 0.4 * math.pi
+    gamma = 0.05
+    return [
+        dict(kind=6, domain=0, coef=1.0),
+        dict(kind=1, domain=0, coef=C5_DT),
+        dict(kind=4, domain=0, coef=C5_DT, bc=(0.0, w, 0.0), bs=(-w, 0.0, 0.0), omega=2 * math.pi, t0=t0, dt=C5_DT),
+        dict(kind=0, domain=0, coef=1.0, tref=0.0),
+        dict(kind=5, coef=gamma * C5_DT, hpow=-2),
+        dict(kind=5, coef=gamma * C5_DT * C5_DT, hpow=-3),
+    ]
+
+
+def c1_mesh(copies):
+    from ngsxfem_gb300.meshes import replicated_circle_2d
+    return replicated_circle_2d(copies)
+
+
+def c3_groups(count):
+    """The c3 meshes grouped by order: {order: (union mesh, vertex values)}."""
+    from ngsxfem_gb300.meshes import MakeStructured3DMesh, batched_ellipsoids, concatenate, ellipsoid_values
+    spec = batched_ellipsoids(count, seed=SEED)
+    cache = {}
+    groups = {}
+    for n, order, centre, axes, rot in spec:
+        if n not in cache:
+            cache[n] = MakeStructured3DMesh(n)
+        m = cache[n]
+        groups.setdefault(order, ([], []))
+        groups[order][0].append(m)
+        groups[order][1].append(ellipsoid_values(m.coords, centre, axes, rot))
+    return {k: (concatenate(ms), np.concatenate(vs)) for k, (ms, vs) in sorted(groups.items())}
+
+
+def c5_mesh(n=256):
+    from ngsxfem_gb300.meshes import MakeStructured2DMesh
+    return MakeStructured2DMesh(n, n)
+
+
+def c5_slab_values(m, slab, kt_l):
+    """Vertex values of the moving circle at the slab's Gauss-Lobatto time nodes
+    (time-major, (kt_l+1) x nv), not yet perturbed."""
+    nodes = [0.0, 1.0] if kt_l == 1 else [0.0, 0.5, 1.0]
+    out = []
+    for x in nodes:
+        t = (slab + x) * C5_DT
+        cx, cy = 0.5 + 0.2 * math.cos(2 * math.pi * t), 0.5 + 0.2 * math.sin(2 * math.pi * t)
+        out.append(np.sqrt((m.coords[:, 0] - cx) ** 2 + (m.coords[:, 1] - cy) ** 2) - 0.25)
+    return np.stack(out)
+
+
+def workload_config(args):
+    if args.workload == "c2":
+        return {"workload": "3D CutFEM Poisson, %d^3x6 Kuhn tets, P%d, NEG stiffness + Nitsche IF + ghost "
+                            "penalty 0.1/h^2" % (args.n, args.order)}
+    if args.workload == "c1":
+        return {"workload": "2D circle r=0.5 on [-1,1]^2, 40x40x2 tris, P1, NEG mass+stiffness + IF mass, "
+                            "%d replicas in one mesh" % args.copies}
+    if args.workload == "c3":
+        return {"workload": "%d unit-cube Kuhn tet meshes, log-uniform 1e3..2e5 tets, rotated ellipsoids, orders "
+                            "U{1,2,3}, c2 form, one graph (3 concurrent order groups)" % args.meshes}
+    return {"workload": "space-time 2D, 256^2x2 tris, P1 x P%d(time), moving circle r=0.25, %d slabs dt=1/16, "
+                        "convection-diffusion + ghost penalty, one graph" % (args.kt, C5_SLABS)}
+
+
+# ----------------------------------------------------------------------------
+# reference arm / CPU baseline: the oracle (CPU statement of the path)
+# ----------------------------------------------------------------------------
+def cpu_prepare(args, sample):
+    """The oracle's inputs for the workload (or its bounded sample): a list of
+    jobs and a description of the sample.  Not timed."""
+    from oracle import oracle as orc
+    if args.workload == "c5":
+        m = c5_mesh()
+        sp = orc.Space(m, 1)
+        slabs = list(range(C5_SLABS)) if not sample else [0, 5, 10, 15]
+        jobs = []
+        for s in slabs:
+            lst = np.stack([orc.interpolate_p1_perturb(x) for x in c5_slab_values(m, s, args.kt)])
+            jobs.append(("st", sp, lst, terms_c5(s * C5_DT)))
+        desc = "all %d slabs" % C5_SLABS if len(slabs) == C5_SLABS else "slabs %s of %d" % (slabs, C5_SLABS)
+        return jobs, desc
+    if args.workload == "c2":
+        m, vals = c2_mesh(args.n)
+        groups = [(m, vals, args.order, terms_c2(args.order), True)]
+        desc = "full workload"
+    elif args.workload == "c1":
+        copies = args.copies if not sample else min(args.copies, 64)
+        m, vals = c1_mesh(copies)
+        groups = [(m, vals, 1, terms_c1(), False)]
+        desc = "full workload" if copies == args.copies else "%d of %d replicas" % (copies, args.copies)
+    else:
+        count = args.meshes if not sample else min(args.meshes, 48)
+        groups = [(m, v, k, terms_c2(k), True) for k, (m, v) in c3_groups(count).items()]
+        desc = "full workload" if count == args.meshes else "the first %d of the %d meshes" % (count, args.meshes)
+    jobs = []
+    for m, vals, order, terms, ghost in groups:
+        jobs.append(("plain", orc.Space(m, order), orc.interpolate_p1_perturb(vals), terms, ghost))
+    return jobs, desc
+
+
+def cpu_pass(jobs, nth):
+    """One timed CPU pass over the prepared jobs: (seconds, cut elements)."""
+    from oracle import oracle as orc
+    t_tot, n_cut = 0.0, 0
+    for job in jobs:
+        if job[0] == "plain":
+            _, sp, l, terms, ghost = job
+            t0 = time.perf_counter()
+            sp.pipeline(l, terms, ghost, nth)
+            t_tot += time.perf_counter() - t0
+            dom, _, _ = sp.cutinfo(l, nth)
+        else:
+            _, sp, lst, terms = job
+            t0 = time.perf_counter()
+            dom, _, bits = sp.cutinfo_st(lst, C5_KT[0], nth)
+            fb = sp.facets_with_neighbor_types(bits[5], bits[4], True, True, True)
+            t2 = []
+            for t in terms:
+                t = dict(t)
+                t["defined_on"] = fb if t["kind"] == orc.TERM_GHOST_MASS else bits[5]
+                t2.append(t)
+            sp.assemble_st(lst, C5_KT[0], 1, 2, t2, nth)
+            t_tot += time.perf_counter() - t0
+        n_cut += int((dom == 2).sum())
+    return t_tot, n_cut
+
+
+def run_reference(args):
+    """The reference arm: the CPU statement of the path (the reference itself
+    needs NGSolve and cannot be built), all host threads, same workload."""
+    ws, rank = dist_env()
+    if rank != 0:
+        return
+    nth = os.cpu_count() or 1
+    C5_KT[0] = args.kt
+    jobs, desc = cpu_prepare(args, args.workload in ("c3", "c5"))
+    for _ in range(args.warmup):
+        cpu_pass(jobs, nth)
+    times, n_cut = [], 0
+    for _ in range(args.steps):
+        t, n_cut = cpu_pass(jobs, nth)
+        times.append(t)
+    t = float(np.mean(times))
+    value = n_cut / t
+    cfg = workload_config(args)
+    cfg["n_cut_per_step"] = n_cut
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nth, "kind": "port",
+                         "sample": desc + " per step (oracle C++ restatement of ngsxfem's path; the reference needs "
+                                          "NGSolve, which cannot be built here)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+# ----------------------------------------------------------------------------
+# GPU arm
+# ----------------------------------------------------------------------------
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -110,39 +308,199 @@ def peaks():
         return None
 
 
-def run_reference(args):
-    """The reference arm: the CPU statement of the path (the reference itself
-    needs NGSolve and cannot be built), all host threads, same workload."""
-    ws, rank = dist_env()
-    if rank != 0:
-        return
-    from oracle import oracle as orc
-    m, vals = workload(args.n)
-    l = orc.interpolate_p1_perturb(vals)
-    sp = orc.Space(m, args.order)
-    nth = os.cpu_count() or 1
-    dom, _, _ = sp.cutinfo(l, nth)
-    n_if = int((dom == 2).sum())
-    for _ in range(args.warmup):
-        sp.pipeline(l, terms_c2(args.order), True, nth)
-    times = []
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        sp.pipeline(l, terms_c2(args.order), True, nth)
-        times.append(time.perf_counter() - t0)
-    t = float(np.mean(times))
-    value = n_if / t
-    print(json.dumps({
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "3D CutFEM Poisson, 64^3x6 Kuhn tets, P2, NEG stiffness + Nitsche IF + ghost penalty",
-                   "n_tets": int(m.ne), "n_cut": n_if, "order": args.order},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nth, "kind": "port",
-                         "sample": "full workload per step (oracle C++ restatement of ngsxfem's path; the reference "
-                                   "needs NGSolve, which cannot be built here)"},
-        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }))
+class Gpu:
+    """The GPU side of one workload: forms, device level sets, outputs."""
+
+    def __init__(self, args):
+        import torch
+        from ngsxfem_gb300 import _lib
+        from ngsxfem_gb300 import xfem as xg
+        self.torch, self._lib, self.xg = torch, _lib, xg
+        self.args = args
+        self.prec = 0 if args.precision == "fp64" else 1
+        self.stream = torch.cuda.current_stream()
+        self.sp = ctypes.c_void_p(self.stream.cuda_stream)
+        self.keep = []
+        self.entries = []  # dicts: form, lset, st, out, counts
+
+    # --- objects
+    def lset(self, vals):
+        t = self.torch.from_numpy(np.ascontiguousarray(vals, dtype=np.float64)).cuda()
+        self._lib.call("xg_interpolate_p1_perturb", ctypes.c_void_p(t.data_ptr()), t.numel(), 1e-14, self.sp)
+        return t
+
+    def form(self, space_h, terms):
+        arr = (self._lib.Term * len(terms))()
+        for k, t in enumerate(terms):
+            arr[k].kind, arr[k].domain, arr[k].order = t["kind"], t["domain"], -1
+            arr[k].hpow, arr[k].coef = t["hpow"], t["coef"]
+            arr[k].d_defined_on = None
+        f = ctypes.c_void_p()
+        self._lib.call("xg_form_create", space_h, arr, len(terms), self.prec, ctypes.byref(f))
+        return f
+
+    def st_form(self, space_h, kt_l, order_time, terms):
+        arr = (self._lib.StTerm * len(terms))()
+        for k, t in enumerate(terms):
+            B = arr[k].base
+            B.kind, B.domain, B.order, B.hpow, B.coef = t["kind"], t.get("domain", 0), -1, t.get("hpow", 0), t["coef"]
+            for j in range(3):
+                B.b[j] = 0.0
+                arr[k].bc[j] = t.get("bc", (0, 0, 0))[j]
+                arr[k].bs[j] = t.get("bs", (0, 0, 0))[j]
+            B.d_defined_on = None
+            arr[k].tref = t.get("tref", -1.0)
+            arr[k].omega, arr[k].t0, arr[k].dt = t.get("omega", 0.0), t.get("t0", 0.0), t.get("dt", 1.0)
+        f = ctypes.c_void_p()
+        self._lib.call("xg_st_form_create", space_h, kt_l, order_time, arr, len(terms), self.prec, ctypes.byref(f))
+        return f
+
+    def out(self, cap_rows, cap_nnz):
+        torch = self.torch
+        o = {"row_dof": torch.zeros(cap_rows, dtype=torch.int32, device="cuda"),
+             "rowptr": torch.zeros(cap_rows + 1, dtype=torch.int64, device="cuda"),
+             "cols": torch.zeros(max(cap_nnz, 1), dtype=torch.int32, device="cuda"),
+             "vals": torch.zeros(max(cap_nnz, 1), dtype=torch.float64, device="cuda"),
+             "counts": torch.zeros(2, dtype=torch.int64, device="cuda")}
+        c = self._lib.Csr()
+        c.d_row_dof, c.d_rowptr = o["row_dof"].data_ptr(), o["rowptr"].data_ptr()
+        c.d_cols, c.d_vals, c.d_counts = o["cols"].data_ptr(), o["vals"].data_ptr(), o["counts"].data_ptr()
+        c.cap_rows, c.cap_nnz = cap_rows, cap_nnz
+        o["csr"] = c
+        return o
+
+    def eager_step(self, e):
+        name = "xg_st_cutfem_step" if e["st"] else "xg_cutfem_step"
+        self._lib.call(name, e["form"], ctypes.c_void_p(e["lset"].data_ptr()), ctypes.byref(e["out"]["csr"]),
+                       self.sp)
+
+    def add(self, form, lset, st, marking):
+        """Registers one step, sizes its output by an eager step (the full
+        pattern when small, else the step's own count plus 5 %) and records
+        the marking counts of its level set."""
+        cap = np.zeros(2, dtype=np.int64)
+        self._lib.call("xg_form_capacity", form, cap.ctypes.data_as(ctypes.c_void_p))
+        e = {"form": form, "lset": lset, "st": st}
+        first = int(cap[1]) if cap[1] * 12 <= (1 << 31) else 1024
+        e["out"] = self.out(int(cap[0]), first)
+        self.eager_step(e)
+        self.torch.cuda.synchronize()
+        st_ = self._lib.load().xg_form_check(form)
+        nnz = int(e["out"]["counts"][1].item())
+        if st_ == self._lib.XG_ERR_CAPACITY or nnz > first:
+            e["out"] = self.out(int(cap[0]), int(nnz * 1.05) + 4096)
+            self.eager_step(e)
+            self.torch.cuda.synchronize()
+            st_ = self._lib.load().xg_form_check(form)
+        self._lib.check(st_, "bench step")
+        e["nrows"], e["nnz"] = (int(x) for x in e["out"]["counts"].cpu().tolist())
+        e.update(marking)
+        self.entries.append(e)
+        return e
+
+    def marking_plain(self, dm, lset):
+        torch, xg = self.torch, self.xg
+        ne, nf = dm.ne, dm.nfacets
+        dom = torch.zeros(ne, dtype=torch.uint8, device="cuda")
+        ratio = torch.zeros(ne, dtype=torch.float64, device="cuda")
+        bits = torch.zeros((8, (ne + 63) // 64), dtype=torch.int64, device="cuda")
+        fb = torch.zeros((nf + 63) // 64, dtype=torch.int64, device="cuda")
+        self._lib.call("xg_cutinfo_update", dm.h, xg._vp(lset), xg._vp(dom), xg._vp(ratio), xg._vp(bits), self.sp)
+        self._lib.call("xg_facets_with_neighbor_types", dm.h, xg._vp(bits[5]), xg._vp(bits[4]), 1, 1, 1, xg._vp(fb),
+                       self.sp)
+        dm.check()
+        return self._counts(dom, fb, nf, dm)
+
+    def marking_st(self, dm, lset, kt_l):
+        torch, xg = self.torch, self.xg
+        ne, nf = dm.ne, dm.nfacets
+        dom = torch.zeros(ne, dtype=torch.uint8, device="cuda")
+        ratio = torch.zeros(ne, dtype=torch.float64, device="cuda")
+        bits = torch.zeros((8, (ne + 63) // 64), dtype=torch.int64, device="cuda")
+        fb = torch.zeros((nf + 63) // 64, dtype=torch.int64, device="cuda")
+        self._lib.call("xg_cutinfo_update_st", dm.h, xg._vp(lset), kt_l, xg._vp(dom), xg._vp(ratio), xg._vp(bits),
+                       self.sp)
+        self._lib.call("xg_facets_with_neighbor_types", dm.h, xg._vp(bits[5]), xg._vp(bits[4]), 1, 1, 1, xg._vp(fb),
+                       self.sp)
+        dm.check()
+        return self._counts(dom, fb, nf, dm)
+
+    def _counts(self, dom, fb, nf, dm):
+        d = dom.cpu().numpy()
+        w = fb.cpu().numpy().view(np.uint64)
+        n_fa = int(np.unpackbits(w.view(np.uint8), bitorder="little")[:nf].sum())
+        return {"n_if": int((d == 2).sum()), "n_neg": int((d == 0).sum()), "n_facets": n_fa, "ne": dm.ne,
+                "dim": dm.dim}
+
+    # --- graph
+    def graph(self):
+        n = len(self.entries)
+        forms = (ctypes.c_void_p * n)(*[e["form"].value for e in self.entries])
+        lsets = (ctypes.c_void_p * n)(*[e["lset"].data_ptr() for e in self.entries])
+        outs = (self._lib.Csr * n)(*[e["out"]["csr"] for e in self.entries])
+        g = ctypes.c_void_p()
+        self._lib.call("xg_step_graph_create", forms, lsets, outs, n, ctypes.byref(g))
+        kc = np.zeros(1, dtype=np.int64)
+        self._lib.call("xg_step_graph_kernel_count", g, kc.ctypes.data_as(ctypes.c_void_p))
+        self.g, self.kernels = g, int(kc[0])
+        return g
+
+    def launch(self):
+        self._lib.call("xg_step_graph_launch", self.g, self.sp)
+
+    def check_forms(self):
+        self.torch.cuda.synchronize()
+        for f in {e["form"].value for e in self.entries}:
+            self._lib.check(self._lib.load().xg_form_check(ctypes.c_void_p(f)), "bench form")
+
+
+def setup(args, gpu):
+    """Builds the workload's forms and steps on the device; returns the config."""
+    xg = gpu.xg
+    cfg = workload_config(args)
+    if args.workload in ("c2", "c1", "c3"):
+        if args.workload == "c2":
+            m, vals = c2_mesh(args.n)
+            groups = {args.order: (m, vals)}
+            tf = terms_c2
+        elif args.workload == "c1":
+            m, vals = c1_mesh(args.copies)
+            groups = {1: (m, vals)}
+            tf = lambda k: terms_c1()  # noqa: E731
+        else:
+            t0 = time.perf_counter()
+            groups = c3_groups(args.meshes)
+            cfg["host_mesh_gen_s"] = time.perf_counter() - t0
+        for order, (m, vals) in groups.items():
+            V = xg.H1(m, order=order)
+            lset = gpu.lset(vals)
+            form = gpu.form(V.h, (terms_c2 if args.workload == "c3" else tf)(order))
+            gpu.keep += [V, m]
+            mk = gpu.marking_plain(V.dm, lset)
+            mk["ndof_el"] = V.ndof_el
+            if args.workload == "c1":
+                mk["n_facets"] = 0  # no patch terms
+            gpu.add(form, lset, False, mk)
+        if args.workload == "c3":
+            cfg["groups"] = {str(k): {"n_tets": int(m.ne)} for k, (m, _) in groups.items()}
+    else:
+        m = c5_mesh()
+        dm = xg.device_mesh(m)
+        sh = ctypes.c_void_p()
+        gpu._lib.call("xg_space_create_st", dm.h, 1, 1, ctypes.byref(sh))
+        info = np.zeros(6, dtype=np.int64)
+        gpu._lib.call("xg_space_info_st", sh, info.ctypes.data_as(ctypes.c_void_p))
+        gpu.keep += [m, dm]
+        # one form per slab: the convection field's time origin is a form
+        # parameter (t0 of b(t)), so each slab's form differs in t0 only
+        for s in range(C5_SLABS):
+            lset = gpu.lset(c5_slab_values(m, s, args.kt))
+            form = gpu.st_form(sh, args.kt, 2, terms_c5(s * C5_DT))
+            mk = gpu.marking_st(dm, lset, args.kt)
+            mk["ndof_el"] = int(info[1])
+            gpu.add(form, lset, True, mk)
+        gpu.st_space = sh
+    return cfg
 
 
 def main():
@@ -152,13 +510,17 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="xg", choices=["xg", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c3", "c5"])
     ap.add_argument("--n", type=int, default=64)
     ap.add_argument("--order", type=int, default=2)
+    ap.add_argument("--copies", type=int, default=512)
+    ap.add_argument("--meshes", type=int, default=512)
+    ap.add_argument("--kt", type=int, default=1, choices=[1, 2])
     ap.add_argument("--cpu-baseline", type=int, default=1)
     args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
-    args.warmup = max(args.warmup, 3)
 
     import torch
     ws, rank = dist_env()
@@ -170,61 +532,21 @@ def main():
 
     from ngsxfem_gb300 import build as xbuild
     xbuild.build()
-    from ngsxfem_gb300 import _lib
-    from ngsxfem_gb300 import xfem as xg
+    gpu = Gpu(args)
+    _lib = gpu._lib
+    stream = gpu.stream
+    cfg = setup(args, gpu)
+    E = gpu.entries
+    n_cut = sum(e["n_if"] for e in E)
+    gpu.graph()
 
-    m, vals = workload(args.n)
-    gf = xg.GridFunction(xg.H1(m, 1))
-    xg.InterpolateToP1(vals, gf)
-    V = xg.H1(m, order=args.order)
-    terms = terms_c2(args.order)
-    arr = (_lib.Term * len(terms))()
-    for k, t in enumerate(terms):
-        arr[k].kind, arr[k].domain, arr[k].order = t["kind"], t["domain"], -1
-        arr[k].hpow, arr[k].coef = t["hpow"], t["coef"]
-        arr[k].d_defined_on = None
-    prec = 0 if args.precision == "fp64" else 1
-    form = ctypes.c_void_p()
-    _lib.call("xg_form_create", V.h, arr, len(terms), prec, ctypes.byref(form))
-    cap = np.zeros(2, dtype=np.int64)
-    _lib.call("xg_form_capacity", form, cap.ctypes.data_as(ctypes.c_void_p))
-    bf = xg.BilinearForm(V)
-    bf._alloc(int(cap[0]), int(cap[1]))
-    stream = torch.cuda.current_stream()
-    sp = ctypes.c_void_p(stream.cuda_stream)
-    lset = gf.vec
-
-    # stage events (profiling hook, recorded on the launching stream)
-    evs = [torch.cuda.Event(enable_timing=True) for _ in range(8)]
-    for e in evs:  # torch creates the CUDA event on first record
-        e.record(stream)
-    torch.cuda.synchronize()
-    ev_arr = (ctypes.c_void_p * 8)(*[ctypes.c_void_p(e.cuda_event) for e in evs])
-
-    def step():
-        _lib.call("xg_cutfem_step", form, ctypes.c_void_p(lset.data_ptr()), ctypes.byref(bf._csr), sp)
-
+    # ---------------- device-resident timing (graph replay) ----------------
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > L2 (129 MB)
     for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
-    _lib.check(_lib.load().xg_form_check(form), "bench form")
-    nrows, nnz = (int(x) for x in bf._counts.cpu().tolist())
-    # counts of the workload
-    dom_p = ctypes.c_void_p()
-    _lib.call("xg_cutfem_marking", form, ctypes.byref(dom_p), None, None, None)
-    ci = xg.CutInfo(m, gf)
-    dom = ci.dom.cpu().numpy()
-    n_if = int((dom == 2).sum())
-    n_neg = int((dom == 0).sum())
-    hasneg, hasif = ci.GetElementsOfType(xg.HASNEG), ci.GetElementsOfType(xg.IF)
-    n_facets = xg.GetFacetsWithNeighborTypes(m, a=hasneg, b=hasif).NumSet()
-
-    # ---------------- device-resident timing ----------------
-    _lib.call("xg_form_stage_events", form, ev_arr, 8)
+        gpu.launch()
+    gpu.check_forms()
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    stage_ms = np.zeros(7)
     if ws > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -232,108 +554,138 @@ def main():
         for k in range(args.steps):
             flush.fill_(float(k))  # L2 flush between timed steps (not timed)
             starts[k].record(stream)
-            step()
+            gpu.launch()
             ends[k].record(stream)
-            ends[k].synchronize()
-            stage_ms += np.array([evs[i].elapsed_time(evs[i + 1]) for i in range(7)])
-    torch.cuda.synchronize()
-    _lib.call("xg_form_stage_events", form, None, 0)
+        torch.cuda.synchronize()
     ms = float(np.mean([s.elapsed_time(e) for s, e in zip(starts, ends)]))
     if ws > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
-    stage_ms /= args.steps
-    _lib.check(_lib.load().xg_form_check(form), "bench form")
-    value = ws * n_if / (ms * 1e-3)
+    gpu.check_forms()
+    value = ws * n_cut / (ms * 1e-3)
+
+    # ---------------- stage breakdown (eager steps with stage events) ----------------
+    stage_ms = np.zeros(7)
+    names = ["marking", "lists", "elmat_uncut", "elmat_cut", "patch", "pattern", "scatter"]
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(8)]
+    for e in evs:  # torch creates the CUDA event on first record
+        e.record(stream)
+    torch.cuda.synchronize()
+    ev_arr = (ctypes.c_void_p * 8)(*[ctypes.c_void_p(e.cuda_event) for e in evs])
+    for e in E:
+        _lib.call("xg_form_stage_events", e["form"], ev_arr, 8)
+        reps = max(1, min(args.steps, 5))
+        for _ in range(reps):
+            flush.fill_(1.0)
+            gpu.eager_step(e)
+            evs[7].synchronize()
+            stage_ms += np.array([evs[i].elapsed_time(evs[i + 1]) for i in range(7)]) / reps
+        _lib.call("xg_form_stage_events", e["form"], None, 0)
+    gpu.check_forms()
 
     # ---------------- end to end through the C ABI with host buffers ----------------
-    h_lset = torch.empty_like(lset, device="cpu").pin_memory()
-    h_lset.copy_(lset.cpu())
-    h_rowdof = torch.empty(nrows, dtype=torch.int32).pin_memory()
-    h_rowptr = torch.empty(nrows + 1, dtype=torch.int64).pin_memory()
-    h_cols = torch.empty(nnz, dtype=torch.int32).pin_memory()
-    h_vals = torch.empty(nnz, dtype=torch.float64).pin_memory()
-    h_counts = torch.empty(2, dtype=torch.int64).pin_memory()
-    d_lset = torch.empty_like(lset)
+    for e in E:
+        e["h_lset"] = torch.empty(e["lset"].shape, dtype=torch.float64).pin_memory()
+        e["h_lset"].copy_(e["lset"].cpu())
+        o = e["out"]
+        e["h_out"] = {k: torch.empty(n, dtype=o[k].dtype).pin_memory()
+                      for k, n in (("row_dof", e["nrows"]), ("rowptr", e["nrows"] + 1), ("cols", e["nnz"]),
+                                   ("vals", e["nnz"]), ("counts", 2))}
     e2e_times = []
     for k in range(args.steps + 2):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        d_lset.copy_(h_lset, non_blocking=True)
-        _lib.call("xg_cutfem_step", form, ctypes.c_void_p(d_lset.data_ptr()), ctypes.byref(bf._csr), sp)
-        h_counts.copy_(bf._counts, non_blocking=True)
+        for e in E:
+            e["lset"].copy_(e["h_lset"], non_blocking=True)
+        gpu.launch()
+        for e in E:
+            e["h_out"]["counts"].copy_(e["out"]["counts"], non_blocking=True)
         stream.synchronize()
-        r, z = int(h_counts[0]), int(h_counts[1])
-        h_rowdof[:r].copy_(bf._row_dof[:r], non_blocking=True)
-        h_rowptr[: r + 1].copy_(bf._rowptr[: r + 1], non_blocking=True)
-        h_cols[:z].copy_(bf._cols[:z], non_blocking=True)
-        h_vals[:z].copy_(bf._vals[:z], non_blocking=True)
+        for e in E:
+            r, z = int(e["h_out"]["counts"][0]), int(e["h_out"]["counts"][1])
+            h, o = e["h_out"], e["out"]
+            h["row_dof"][:r].copy_(o["row_dof"][:r], non_blocking=True)
+            h["rowptr"][: r + 1].copy_(o["rowptr"][: r + 1], non_blocking=True)
+            h["cols"][:z].copy_(o["cols"][:z], non_blocking=True)
+            h["vals"][:z].copy_(o["vals"][:z], non_blocking=True)
         stream.synchronize()
         if k >= 2:
             e2e_times.append(time.perf_counter() - t0)
+    gpu.check_forms()
     e2e_s = float(np.mean(e2e_times))
-    h2d = lset.numel() * 8
-    d2h = 16 + nrows * 4 + (nrows + 1) * 8 + nnz * 12
+    h2d = sum(e["lset"].numel() * 8 for e in E)
+    d2h = sum(16 + e["nrows"] * 4 + (e["nrows"] + 1) * 8 + e["nnz"] * 12 for e in E)
 
-    # ---------------- roofline of the dominant stage ----------------
-    names = ["marking", "lists", "elmat_uncut", "elmat_cut", "patch", "pattern", "scatter"]
-    dom_i = int(np.argmax(stage_ms))
-    D, nd = 3, V.ndof_el
-    b_el = 4 * (D + 1) + 8 * (D + 1) * (D + 1) + 4 * nd + 8 * nd * nd
-    b_fa = 4 * 2 * (D + 1) + 8 * 2 * (D + 1) * (D + 1) + 4 * 2 * nd + 8 * (2 * nd) ** 2
-    n_uncut_active = n_neg
-    alg = {
-        "marking": m.ne * (4 * (D + 1) + 8 * (D + 1) + 1 + 8),
-        "lists": m.ne / 8 * 3,
-        "elmat_uncut": n_uncut_active * b_el,
-        "elmat_cut": n_if * b_el,
-        "patch": n_facets * b_fa,
-        "pattern": nnz * 4 + nrows * 8,
-        "scatter": nnz * 12 + (n_uncut_active + n_if) * nd * nd * 8 + n_facets * (2 * nd) ** 2 * 8,
-    }
+    # ---------------- roofline ----------------
+    # algorithmic bytes per stage: vertex ids, coordinates + level set per vertex,
+    # dof ids and the element matrix written once (element kernels), the same
+    # for both elements of a patch, and the CSR write (scatter)
+    alg = dict.fromkeys(names, 0.0)
+    for e in E:
+        D, nd, ne = e["dim"], e["ndof_el"], e["ne"]
+        b_el = 4 * (D + 1) + 8 * (D + 1) * (D + 1) + 4 * nd + 8 * nd * nd
+        b_fa = 4 * 2 * (D + 1) + 8 * 2 * (D + 1) * (D + 1) + 4 * 2 * nd + 8 * (2 * nd) ** 2
+        alg["marking"] += ne * (4 * (D + 1) + 8 * (D + 1) + 1 + 8)
+        alg["lists"] += ne / 8 * 3
+        alg["elmat_uncut"] += e["n_neg"] * b_el
+        alg["elmat_cut"] += e["n_if"] * b_el
+        alg["patch"] += e["n_facets"] * b_fa
+        alg["pattern"] += e["nnz"] * 4 + e["nrows"] * 8
+        alg["scatter"] += e["nnz"] * 12 + (e["n_neg"] + e["n_if"]) * nd * nd * 8 + e["n_facets"] * (2 * nd) ** 2 * 8
     pk = peaks()
     peak_bw = pk["hbm_gbs"] if pk else 6800.0
+    if args.workload == "c5":  # the space-time element kernel covers uncut and cut elements in one launch
+        stage_ms[3] += stage_ms[2]
+        stage_ms[2] = 0.0
+        alg["elmat_cut"] += alg["elmat_uncut"]
+        alg["elmat_uncut"] = 0.0
+    dom_i = int(np.argmax(stage_ms))
     dname = names[dom_i]
     achieved = alg[dname] / (stage_ms[dom_i] * 1e-3) / 1e9
+    step_bytes = sum(alg.values())
+    cfg.update({
+        "n_tets_or_tris": int(sum(e["ne"] for e in E)), "n_cut": n_cut, "n_neg_uncut": sum(e["n_neg"] for e in E),
+        "n_ghost_facets": sum(e["n_facets"] for e in E), "nrows": sum(e["nrows"] for e in E),
+        "nnz": sum(e["nnz"] for e in E), "precision": args.precision, "steps_per_graph": len(E),
+        "l2": "flushed between timed steps (512 MB write)", "parallelism": "replicas only",
+        "timing": "CUDA graph replay of the whole step, CUDA events on the launching stream"})
+    if args.workload == "c2":
+        cfg["order"] = args.order
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if prec == 0 else "f32+f64", "data": "synthetic",
-        "config": {"workload": "3D CutFEM Poisson, %d^3x6 Kuhn tets, P%d, NEG stiffness + Nitsche IF + ghost "
-                               "penalty 0.1/h^2" % (args.n, args.order),
-                   "n_tets": int(m.ne), "n_cut": n_if, "n_neg_uncut": n_neg, "n_ghost_facets": n_facets,
-                   "nrows": nrows, "nnz": nnz, "precision": args.precision,
-                   "l2": "flushed between timed steps (512 MB write)", "parallelism": "replicas only"},
-        "e2e": {"value": ws * n_if / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+        "dtype": "f64" if gpu.prec == 0 else "f32+f64", "data": "synthetic", "config": cfg,
+        "e2e": {"value": ws * n_cut / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_s * 1e3},
         "stages_ms": {n: float(v) for n, v in zip(names, stage_ms)},
         "roofline": {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": peak_bw, "unit": "GB/s",
                      "frac": achieved / peak_bw, "traffic": None,
-                     "peak_source": "measured" if pk else "fallback"},
+                     "peak_source": "measured" if pk else "fallback",
+                     "whole_step": {"achieved": step_bytes / (ms * 1e-3) / 1e9,
+                                    "frac": step_bytes / (ms * 1e-3) / 1e9 / peak_bw}},
         "clocks": clk.summary(),
-        "gpu_launches": None,
+        "gpu_launches": args.steps * gpu.kernels,
     }
-    # kernel launches per step: cutinfo 1, facets 1, active 2, compactions 3x4, elmat 2, patch 1,
-    # dof mark 1 (+memset), rowcount 1, scan 3, rowfill 1
-    out["gpu_launches"] = args.steps * 25
     if rank == 0 and args.cpu_baseline:
         try:
-            from oracle import oracle as orc
-            l = orc.interpolate_p1_perturb(vals)
-            spc = orc.Space(m, args.order)
             nth = os.cpu_count() or 1
-            spc.pipeline(l, terms, True, nth)
-            t0 = time.perf_counter()
+            C5_KT[0] = args.kt
+            jobs, desc = cpu_prepare(args, args.workload in ("c3", "c5"))
+            cpu_pass(jobs, nth)  # warm-up
             reps = 2
+            t_cpu, n_cpu = 0.0, 0
             for _ in range(reps):
-                spc.pipeline(l, terms, True, nth)
-            tc = (time.perf_counter() - t0) / reps
-            out["cpu_baseline"] = {"value": n_if / tc, "unit": UNIT, "cores": nth, "kind": "port",
-                                   "sample": "full workload, mean of 2 pipeline runs after 1 warm-up"}
-        except Exception as e:  # the baseline is reported, never required
-            out["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": repr(e)}
-    _lib.load().xg_form_destroy(form)
+                t, nc = cpu_pass(jobs, nth)
+                t_cpu += t
+                n_cpu += nc
+            out["cpu_baseline"] = {"value": n_cpu / t_cpu, "unit": UNIT, "cores": nth, "kind": "port",
+                                   "sample": "%s, %d timed pass(es)" % (desc, reps)}
+        except Exception as ex:  # the baseline is reported, never required
+            out["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": repr(ex)}
+    for f in {e["form"].value for e in E}:
+        _lib.load().xg_form_destroy(ctypes.c_void_p(f))
+    _lib.load().xg_step_graph_destroy(gpu.g)
     if rank == 0:
         print(json.dumps(out))
     if ws > 1:

@@ -10,6 +10,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libxg.so")
 
 XG_OK = 0
+XG_ERR_CAPACITY = 3
 STATUS = {
     0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "capacity exceeded",
     4: "cut requested on an uncut (sub-)simplex", 5: "unsupported cut topology",
