@@ -301,6 +301,29 @@ class Clocks:
                 "samples": len(sm)}
 
 
+# DRAM bytes (read + write) per launch of the dominant kernel from one ncu
+# capture of the same workload (profiles/cutfem_step_3d_poisson_64cube_p2_fp64.md,
+# profiles/st_elmat_spacetime_256sq_p1p1_fp64.md)
+TRAFFIC = {("c2", "patch"): 4.921344e6 + 43.072256e6, ("c2", "scatter"): 660.390144e6 + 103.535104e6,
+           ("c2", "elmat_cut"): 6.448640e6 + 0.466944e6}
+
+
+def fp64_peak(torch):
+    a = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+    b = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    best = None
+    for _ in range(3):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        torch.matmul(a, b)
+        e.record()
+        e.synchronize()
+        t = s.elapsed_time(e) * 1e-3
+        best = t if best is None else min(best, t)
+    return 2 * 4096 ** 3 / best / 1e12
+
+
 def peaks():
     try:
         return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -478,6 +501,7 @@ def setup(args, gpu):
             gpu.keep += [V, m]
             mk = gpu.marking_plain(V.dm, lset)
             mk["ndof_el"] = V.ndof_el
+            mk["order"] = order
             if args.workload == "c1":
                 mk["n_facets"] = 0  # no patch terms
             gpu.add(form, lset, False, mk)
@@ -498,6 +522,7 @@ def setup(args, gpu):
             form = gpu.st_form(sh, args.kt, 2, terms_c5(s * C5_DT))
             mk = gpu.marking_st(dm, lset, args.kt)
             mk["ndof_el"] = int(info[1])
+            mk["order"] = 1
             gpu.add(form, lset, True, mk)
         gpu.st_space = sh
     return cfg
@@ -644,6 +669,22 @@ def main():
     dname = names[dom_i]
     achieved = alg[dname] / (stage_ms[dom_i] * 1e-3) / 1e9
     step_bytes = sum(alg.values())
+    # the element kernels run on the FP64 pipe: algorithmic FLOPs of the patch
+    # stage = sum over patch points of 2 (2n)^2 (mass integrand, full matrix),
+    # with 2 x NQ(2k) points per facet (the order-2k rule on both elements)
+    fp64 = None
+    if dname == "patch":
+        nq = {(2, 2): 3, (2, 4): 6, (2, 6): 16, (3, 2): 4, (3, 4): 14, (3, 6): 64}
+        flops = 0.0
+        for e in E:
+            k = e["order"]
+            nd = e["ndof_el"] if not e["st"] else e["ndof_el"] // 2  # patches are spatial (P1 x P1 in time)
+            flops += e["n_facets"] * 2 * nq[(e["dim"], 2 * k)] * 2 * (2 * nd) ** 2
+        peak_fp64 = fp64_peak(torch)
+        ach = flops / (stage_ms[dom_i] * 1e-3) / 1e12
+        fp64 = {"bound": "fp64", "kernel": dname, "achieved": ach, "peak": peak_fp64, "unit": "TFLOP/s",
+                "frac": ach / peak_fp64, "flops_per_step": flops,
+                "peak_source": "measured here: cuBLAS DGEMM 4096^3 (torch.matmul float64), best of 3"}
     cfg.update({
         "n_tets_or_tris": int(sum(e["ne"] for e in E)), "n_cut": n_cut, "n_neg_uncut": sum(e["n_neg"] for e in E),
         "n_ghost_facets": sum(e["n_facets"] for e in E), "nrows": sum(e["nrows"] for e in E),
@@ -660,13 +701,18 @@ def main():
                 "ms_per_step": e2e_s * 1e3},
         "stages_ms": {n: float(v) for n, v in zip(names, stage_ms)},
         "roofline": {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": peak_bw, "unit": "GB/s",
-                     "frac": achieved / peak_bw, "traffic": None,
+                     "frac": achieved / peak_bw, "traffic": TRAFFIC.get((args.workload, dname)) if
+                     (args.workload, args.n, args.order) == ("c2", 64, 2) or args.workload != "c2" else None,
                      "peak_source": "measured" if pk else "fallback",
                      "whole_step": {"achieved": step_bytes / (ms * 1e-3) / 1e9,
                                     "frac": step_bytes / (ms * 1e-3) / 1e9 / peak_bw}},
         "clocks": clk.summary(),
         "gpu_launches": args.steps * gpu.kernels,
     }
+    if fp64 is not None:  # the bound that binds for the dominant kernel
+        fp64["traffic"] = out["roofline"]["traffic"]
+        fp64["hbm"] = out["roofline"]
+        out["roofline"] = fp64
     if rank == 0 and args.cpu_baseline:
         try:
             nth = os.cpu_count() or 1

@@ -92,6 +92,14 @@ def lib():
         L.orc_assemble_st.argtypes = [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, ctypes.c_int, ctypes.c_int]
         L.orc_integrate_st.restype = ctypes.c_double
         L.orc_integrate_st.argtypes = [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.orc_iso_deformation.argtypes = [ctypes.c_int, P, P, ctypes.c_double, P, P]
+        L.orc_iso_cut_rule.argtypes = [ctypes.c_int, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                       P, P, ctypes.c_int, P]
+        L.orc_iso_moments_tet.argtypes = [ctypes.c_int64, P, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int]
+        L.orc_subdiv_moments_tet.argtypes = [P, ctypes.c_int, P]
+        L.orc_iso_integrate_mesh.restype = ctypes.c_double
+        L.orc_iso_integrate_mesh.argtypes = [ctypes.c_int, ctypes.c_int, P, ctypes.c_int, P, P, ctypes.c_int,
+                                             ctypes.c_int, ctypes.c_double, ctypes.c_int, P]
         L.orc_pipeline.restype = ctypes.c_int64
         L.orc_pipeline.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         _lib = L
@@ -182,6 +190,76 @@ def _st_terms(terms):
         else:
             arr[i].defined_on = None
     return arr, keep
+
+
+def iso_deformation(elcoords, p2vals, threshold=-1.0):
+    """Per-element LevelSetMeshAdaptation deformation: (theta[nedges, D], deformed, nonconv)."""
+    elc = np.ascontiguousarray(elcoords, dtype=np.float64)
+    D = elc.shape[1]
+    v = np.ascontiguousarray(p2vals, dtype=np.float64)
+    th = np.zeros((3 if D == 2 else 6, D))
+    nc = ctypes.c_int(0)
+    r = lib().orc_iso_deformation(D, _p(elc), _p(v), threshold, _p(th), ctypes.byref(nc))
+    if r < 0:
+        raise RuntimeError("orc_iso_deformation failed: %d" % r)
+    return th, bool(r), nc.value
+
+
+def iso_cut_rule(elcoords, p2vals, dt, order, threshold=-1.0, deform=True):
+    """Cut rule of the (per-element) isoparametrically deformed simplex: (points, weights, nonconv)."""
+    elc = np.ascontiguousarray(elcoords, dtype=np.float64)
+    D = elc.shape[1]
+    v = np.ascontiguousarray(p2vals, dtype=np.float64)
+    pts = np.zeros((8192, 3))
+    wts = np.zeros(8192)
+    nc = ctypes.c_int(0)
+    n = lib().orc_iso_cut_rule(D, _p(elc), _p(v), dt, order, threshold, int(deform), _p(pts), _p(wts), 8192,
+                               ctypes.byref(nc))
+    if n == -1:
+        return None
+    if n < 0:
+        raise RuntimeError("orc_iso_cut_rule failed: %d" % n)
+    return pts[:n, :D].copy(), wts[:n].copy(), nc.value
+
+
+def iso_integrate_mesh(mesh, p2vals, dt, order, threshold=-1.0, deform=True):
+    """Integral of 1 over the dt part of the deformed mesh (mesh-level deformation)."""
+    v = np.ascontiguousarray(p2vals, dtype=np.float64)
+    nc = ctypes.c_int(0)
+    r = lib().orc_iso_integrate_mesh(mesh.dim, mesh.nv, _p(mesh.coords), mesh.ne, _p(mesh.elements), _p(v), dt, order,
+                                     threshold, int(deform), ctypes.byref(nc))
+    return r, nc.value
+
+
+def p2_nodal_values(mesh, f):
+    """Element-local P2 nodal values (vertices, then edge midpoints) of f(points)."""
+    D = mesh.dim
+    E = [(0, 1), (0, 2), (1, 2)] if D == 2 else [(0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3)]
+    P = mesh.coords[mesh.elements]  # ne x (D+1) x D
+    nodes = [P[:, i] for i in range(D + 1)] + [0.5 * (P[:, a] + P[:, b]) for a, b in E]
+    return np.stack([f(x) for x in nodes], axis=1)
+
+
+def iso_moments_tet(vals10, order=11, deform=True, nthreads=1):
+    """NEG-part moments (n, 35) of the reference tet for P2 values (n, 10), and the
+    per-element count of non-converged point searches."""
+    v = np.ascontiguousarray(vals10, dtype=np.float64).reshape(-1, 10)
+    out = np.zeros((v.shape[0], 35))
+    nc = np.zeros(v.shape[0], dtype=np.int32)
+    lib().orc_iso_moments_tet(v.shape[0], _p(v), order, int(deform), _p(out), _p(nc), nthreads)
+    return out, nc
+
+
+def subdiv_moments_tet(vals10, levels):
+    v = np.ascontiguousarray(vals10, dtype=np.float64)
+    out = np.zeros(35)
+    lib().orc_subdiv_moments_tet(_p(v), levels, _p(out))
+    return out
+
+
+def moment_exponents():
+    """(a, b, c) of the 35 moments in their graded order."""
+    return [(a, b, t - a - b) for t in range(5) for a in range(t, -1, -1) for b in range(t - a, -1, -1)]
 
 
 class Space:

@@ -113,6 +113,33 @@ double orc_integrate_st(const orc_space*, const double* lset_st, int kt, int dt,
 orc_csr* orc_assemble_st(const orc_space*, const double* lset_st, int kt_l, int kt, int order_time,
                          const orc_st_term* terms, int nterms, int nthreads);
 
+/* --- isoparametric rules for P2 level sets (xg_oracle_iso.cpp) ------------ */
+/* P2 nodal values: D+1 vertex values, then the edge midpoints of (0,1),(0,2),(1,2)
+ * (trig) / (0,1),(0,2),(0,3),(1,2),(1,3),(2,3) (tet).  The per-element
+ * deformation of LevelSetMeshAdaptation (edge coefficients, reference frame,
+ * nedges*D doubles); returns 1 if the element was deformed (relevant band). */
+int orc_iso_deformation(int D, const double* elc, const double* p2vals, double threshold, double* theta,
+                        int* nonconv);
+/* Cut rule of the deformed element: points = deformed reference points, weights
+ * = physical measure (|det J A|, and |(J A)^-T n| on IF).  deform = 0: the plain
+ * straight cut rule of the P1 interpolant with the same weights convention. */
+int orc_iso_cut_rule(int D, const double* elc, const double* p2vals, int dt, int order, double threshold,
+                     int deform, double* pts, double* wts, int maxpts, int* nonconv);
+/* Integral of 1 over the dt part of a whole mesh with the mesh-level
+ * deformation (shared edge dofs averaged over the band elements, all elements
+ * deformed), as Integrate(levelset_domain, cf=1, order) after
+ * mesh.SetDeformation(CalcDeformation(lset_ho)).  p2vals: ne x nnodes per
+ * element (element-local node order above). */
+double orc_iso_integrate_mesh(int D, int nv, const double* coords, int ne, const int32_t* elv, const double* p2vals,
+                              int dt, int order, double threshold, int deform, int* nonconv);
+/* NEG-part moments (35, degree <= 4, graded order) of the reference tet for n
+ * P2 value sets (10 each); nonconv[i] = non-converged searches (-1: rule error). */
+int orc_iso_moments_tet(int64_t n, const double* vals10, int order, int deform, double* out35, int32_t* nonconv,
+                        int nthreads);
+/* The same moments of the exact NEG part {phi_P2 < 0}, approximated by `levels`
+ * red refinements with the straight cut rule of the P1 interpolant on each leaf. */
+int orc_subdiv_moments_tet(const double* vals10, int levels, double* out35);
+
 /* Whole CPU pipeline (CutInfo + facet marking + assembly) for timing: returns nnz. */
 int64_t orc_pipeline(const orc_space*, const double* lset_vertex, const orc_term* terms, int nterms,
                      int ghost_facets, int nthreads);
