@@ -216,6 +216,227 @@ def cpu_pass(jobs, nth):
     return t_tot, n_cut
 
 
+# ----------------------------------------------------------------------------
+# c4: learned cut quadrature on P2 level sets
+# ----------------------------------------------------------------------------
+TET_EDGES = [(0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3)]
+
+
+def c4_eval_values(n=48, R=0.3, r=0.1):
+    """Element-local P2 nodal values of the torus level set
+    sqrt((sqrt((x-.5)^2 + (y-.5)^2) - R)^2 + (z-.5)^2) - r on the n^3 x 6 Kuhn
+    mesh, restricted to the elements whose P1 interpolant (with the +1e-14
+    perturbation) is cut."""
+    from ngsxfem_gb300.meshes import MakeStructured3DMesh
+    m = MakeStructured3DMesh(n)
+
+    def phi(p):
+        q = np.sqrt((p[..., 0] - .5) ** 2 + (p[..., 1] - .5) ** 2) - R
+        return np.sqrt(q ** 2 + (p[..., 2] - .5) ** 2) - r
+    P = m.coords[m.elements]
+    vals = np.stack([phi(P[:, i]) for i in range(4)] + [phi(0.5 * (P[:, a] + P[:, b])) for a, b in TET_EDGES], 1)
+    p1 = np.where(np.abs(vals[:, :4]) < 1e-14, 1e-14, vals[:, :4])
+    cut = (p1.min(1) < 0) & (p1.max(1) > 0)
+    return m, np.ascontiguousarray(vals[cut])
+
+
+def c4_train_values(n, seed):
+    """Training P2 values: half drawn as the configuration states (N(0,1), shifted to a
+    zero crossing, scaled to max |v| = 1), half mildly curved (a level set that
+    the mesh resolves, the regime of the evaluation mesh)."""
+    from oracle import learned_ref as L
+    rng = np.random.default_rng(seed)
+    return np.concatenate([L.spec_values(n // 2, rng), L.resolved_values(n - n // 2, rng)])
+
+
+def run_c4(args):
+    ws, rank = dist_env()
+    cfg = {"workload": "learned cut quadrature, P2 torus (R=0.3, r=0.1) on 48^3x6 Kuhn tets; MLP 10-256-256-24 "
+                       "trained on %d P2 value sets" % args.train}
+    m, vals = c4_eval_values()
+    n = len(vals)
+    cfg.update({"n_tets": int(m.ne), "n_cut": n})
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        from oracle import oracle as orc
+        nth = os.cpu_count() or 1
+        for _ in range(args.warmup):
+            orc.iso_moments_tet(vals, 8, True, nth)
+        times = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            orc.iso_moments_tet(vals, 8, True, nth)
+            times.append(time.perf_counter() - t0)
+        t = float(np.mean(times))
+        print(json.dumps({
+            "impl": "reference", "metric": METRIC, "value": n / t, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
+            "cpu_baseline": {"value": n / t, "unit": UNIT, "cores": nth, "kind": "port",
+                             "sample": "all cut elements per step: per-element isoparametric rule (oracle)"},
+            "e2e": {"value": n / t, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        return
+    import torch
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    from ngsxfem_gb300 import build as xbuild
+    xbuild.build()
+    from ngsxfem_gb300 import _lib
+    stream = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    vp = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+
+    def moments(d_v, order, deform, out=None):
+        out = out if out is not None else torch.zeros((d_v.shape[0], 35), dtype=torch.float64, device="cuda")
+        _lib.call("xg_iso_moments_tet", vp(d_v), d_v.shape[0], order, deform, vp(out), None, sp)
+        return out
+
+    # ---- training set and its targets (GPU isoparametric rule) ----
+    t0 = time.perf_counter()
+    v_tr = torch.from_numpy(c4_train_values(args.train, SEED)).cuda()
+    iso_tr = moments(v_tr, 8, 1)
+    nc_tr = torch.zeros(args.train, dtype=torch.int32, device="cuda")
+    _lib.call("xg_iso_moments_tet", vp(v_tr), args.train, 8, 1, vp(iso_tr), vp(nc_tr), sp)
+    p1_tr = moments(v_tr, 4, 0)
+    t_tr = (iso_tr - p1_tr).float()
+    # samples the network is not meant to take (the fallback's): defects above
+    # 5 % of the element measure or searches that did not converge
+    keep = (t_tr.abs().amax(1) * 6 <= 0.05) & (nc_tr == 0)
+    v_tr, t_tr = v_tr[keep].contiguous(), t_tr[keep].contiguous()
+    n_tr = int(v_tr.shape[0])
+    x_tr = torch.zeros((n_tr, 10), dtype=torch.float32, device="cuda")
+    _lib.call("xg_learned_features", vp(v_tr), n_tr, vp(x_tr), sp)
+    s_tr = torch.full((n_tr,), 1.0 / 6.0, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    t_targets = time.perf_counter() - t0
+    del iso_tr, p1_tr, nc_tr
+    mlp = ctypes.c_void_p()
+    _lib.call("xg_mlp_create", SEED, ctypes.byref(mlp))
+    loss = torch.zeros(1, dtype=torch.float32, device="cuda")
+    B, step, losses = 8192, 0, []
+    g = torch.Generator(device="cuda")
+    g.manual_seed(SEED)
+    t0 = time.perf_counter()
+    for ep in range(args.epochs):
+        perm = torch.randperm(n_tr, device="cuda", generator=g)
+        lr = 2e-3 * (0.5 ** (ep * 5 // max(args.epochs, 1)))
+        for b0 in range(0, n_tr - B + 1, B):
+            idx = perm[b0:b0 + B]
+            xb, tb, sb = x_tr[idx].contiguous(), t_tr[idx].contiguous(), s_tr[idx].contiguous()
+            _lib.call("xg_mlp_loss_grad", mlp, vp(xb), vp(tb), vp(sb), B, vp(loss), None, sp)
+            step += 1
+            _lib.call("xg_mlp_adam_step", mlp, None, ctypes.c_float(lr), step, sp)
+        losses.append(float(loss.item()))
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    del v_tr, x_tr, t_tr, s_tr
+
+    # ---- evaluation on the torus mesh ----
+    d_v = torch.from_numpy(vals).cuda()
+    out_plain = torch.zeros((n, 35), dtype=torch.float64, device="cuda")
+    out_learn = torch.zeros_like(out_plain)
+    out_p1 = torch.zeros_like(out_plain)
+
+    def plain():
+        moments(d_v, 8, 1, out_plain)
+
+    nfb = torch.zeros(1, dtype=torch.int32, device="cuda")
+
+    def learned(kappa=args.kappa):
+        _lib.call("xg_learned_moments_tet", mlp, vp(d_v), n, ctypes.c_double(kappa), vp(out_learn), vp(nfb), sp)
+
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def timeit(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        st = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        en = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            st[k].record(stream)
+            fn()
+            en[k].record(stream)
+        torch.cuda.synchronize()
+        return float(np.mean([a.elapsed_time(b) for a, b in zip(st, en)]))
+
+    with Clocks(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        ms_learn = timeit(learned)
+        ms_plain = timeit(plain)
+    moments(d_v, 4, 0, out_p1)
+    torch.cuda.synchronize()
+    n_fallback = int(nfb.item())
+    ref = out_plain.cpu().numpy()
+    # moment errors in units of the element measure (1/6 for the reference tet)
+    e_learn = np.abs(out_learn.cpu().numpy() - ref).max(1) * 6
+    e_p1 = np.abs(out_p1.cpu().numpy() - ref).max(1) * 6
+
+    def stats(e):
+        return {"median": float(np.median(e)), "p99": float(np.quantile(e, 0.99)), "max": float(e.max()),
+                "frac_le_1e-6": float((e <= 1e-6).mean()), "frac_le_1e-4": float((e <= 1e-4).mean()),
+                "frac_le_1e-3": float((e <= 1e-3).mean())}
+    errs = {"definition": "max over the 35 moments of |m - m_plain| / (measure of the element)",
+            "learned_vs_plain": stats(e_learn), "straight_cut_vs_plain": stats(e_p1)}
+    sweep = {}
+    for kap in (0.0, 0.01, 0.02, 0.05, -1.0):
+        learned(kap)
+        torch.cuda.synchronize()
+        e = np.abs(out_learn.cpu().numpy() - ref).max(1) * 6
+        sweep[str(kap)] = {"fallback_frac": float(nfb.item()) / n, "median": float(np.median(e)),
+                           "p99": float(np.quantile(e, 0.99)), "max": float(e.max())}
+    errs["fallback_sweep (kappa_max: result)"] = sweep
+    # ---- end to end: host values in, moments out ----
+    h_v = torch.from_numpy(vals).pin_memory()
+    h_out = torch.empty((n, 35), dtype=torch.float64).pin_memory()
+    e2e = []
+    for k in range(args.steps + 2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        d_v.copy_(h_v, non_blocking=True)
+        learned()
+        h_out.copy_(out_learn, non_blocking=True)
+        stream.synchronize()
+        if k >= 2:
+            e2e.append(time.perf_counter() - t0)
+    e2e_s = float(np.mean(e2e))
+    flops_mlp = 2.0 * (10 * 256 + 256 * 256 + 256 * 24) * n
+    pk = peaks()
+    peak_tc = pk["bf16_tflops"] if pk else 1900.0
+    ach = flops_mlp / (ms_learn * 1e-3) / 1e12
+    cfg.update({"train": {"samples": args.train, "epochs": args.epochs, "batch": B, "steps": step,
+                          "targets_s": t_targets, "train_s": t_train, "loss_first_last": [losses[0], losses[-1]]},
+                "plain_ms": ms_plain, "learned_ms": ms_learn, "learned_speedup_vs_plain": ms_plain / ms_learn,
+                "kappa_max": args.kappa, "fallback_frac": n_fallback / n, "train_kept": n_tr,
+                "errors": errs, "l2": "flushed between timed steps (512 MB write)",
+                "plain": "GPU per-element isoparametric rule (FP64), the reference's P2 workflow"})
+    out = {
+        "metric": METRIC, "value": n / (ms_learn * 1e-3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_learn, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16 weights, f32 accumulation, f64 moments", "data": "synthetic",
+        "config": cfg,
+        "e2e": {"value": n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n * 80, "d2h_bytes_per_step": n * 280,
+                "ms_per_step": e2e_s * 1e3},
+        "roofline": {"bound": "tensor", "kernel": "MLP products (FP32 FMA tiles)", "achieved": ach, "peak": peak_tc,
+                     "unit": "TFLOP/s", "frac": ach / peak_tc, "traffic": None,
+                     "peak_source": "measured bf16" if pk else "fallback"},
+        "clocks": clk.summary(),
+        # moments, features, 3 products + 3 bias/activation, correction, fallback (memset, list, moments)
+        "gpu_launches": args.steps * (9 + (3 if args.kappa >= 0 else 0)),
+    }
+    if args.cpu_baseline:
+        from oracle import oracle as orc
+        nth = os.cpu_count() or 1
+        orc.iso_moments_tet(vals, 8, True, nth)
+        t0 = time.perf_counter()
+        orc.iso_moments_tet(vals, 8, True, nth)
+        tc = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": n / tc, "unit": UNIT, "cores": nth, "kind": "port",
+                               "sample": "all cut elements: per-element isoparametric rule (oracle), 1 timed pass"}
+    _lib.call("xg_mlp_destroy", mlp)
+    print(json.dumps(out))
+
+
 def run_reference(args):
     """The reference arm: the CPU statement of the path (the reference itself
     needs NGSolve and cannot be built), all host threads, same workload."""
@@ -535,7 +756,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="xg", choices=["xg", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c3", "c5"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c3", "c4", "c5"])
+    ap.add_argument("--train", type=int, default=2000000)
+    ap.add_argument("--epochs", type=int, default=8)
+    ap.add_argument("--kappa", type=float, default=0.05)
     ap.add_argument("--n", type=int, default=64)
     ap.add_argument("--order", type=int, default=2)
     ap.add_argument("--copies", type=int, default=512)
@@ -544,6 +768,8 @@ def main():
     ap.add_argument("--cpu-baseline", type=int, default=1)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.workload == "c4":
+        return run_c4(args)
     if args.impl == "reference":
         return run_reference(args)
 

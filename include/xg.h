@@ -277,6 +277,55 @@ int xg_cutfem_step(xg_form* form, const double* d_lset, xg_csr* out, void* strea
 int xg_cutfem_marking(xg_form* form, const uint8_t** d_dom, const double** d_cut_ratio, const uint64_t** d_bits,
                       const uint64_t** d_facets);
 
+/* ---- P2 level sets on tetrahedra: isoparametric and learned cut quadrature ---- */
+/* P2 nodal values per element (10 doubles): the 4 vertex values, then the
+ * edge midpoints of (0,1),(0,2),(0,3),(1,2),(1,3),(2,3); reference tet
+ * (1,0,0),(0,1,0),(0,0,1),(0,0,0).  Moments: x^a y^b z^c of the NEG part,
+ * a+b+c <= 4, graded order (t = 0..4, a = t..0, b = t-a..0): 35 doubles.
+ *
+ * xg_iso_moments_tet: the reference's P2 workflow on a one-element mesh -
+ * LevelSetMeshAdaptation's deformation (lsetcurving/shiftintegrators.cpp:38-122,
+ * calcpointshift.cpp:143-201, projshift.cpp:58-135) followed by the straight
+ * cut rule of the P1 interpolant on the deformed element (rule order `order`);
+ * deform = 0 gives the straight cut rule alone.  d_nonconv (optional): number
+ * of point searches that did not converge per element (-1: bad decomposition). */
+int xg_iso_moments_tet(const double* d_vals10, int64_t n, int order, int deform, double* d_out35,
+                       int32_t* d_nonconv, void* stream);
+/* The learned cut quadrature (no counterpart in the reference): straight cut
+ * rule of the P1 interpolant + 24 weights at a fixed point set predicted by an
+ * MLP 10 -> 256 -> 256 -> 24 (SiLU) from the normalised nodal values; FP32
+ * master parameters, BF16 copies in every product, FP32 accumulation. */
+typedef struct xg_mlp xg_mlp;
+int xg_mlp_param_count(int64_t* h_out);
+/* the 24 fixed points (reference coordinates, 72 doubles) */
+int xg_learned_points(double* h_pts72);
+int xg_mlp_create(uint64_t seed, xg_mlp** out);
+int xg_mlp_destroy(xg_mlp* mlp);
+/* FP32 master parameters, flat: W1[10][256], b1[256], W2[256][256], b2[256], W3[256][24], b3[24] */
+int xg_mlp_get_params(const xg_mlp* mlp, float* d_out, void* stream);
+int xg_mlp_set_params(xg_mlp* mlp, const float* d_in, void* stream);
+/* y[B][24] = MLP(x[B][10]) (x from xg_learned_features); B <= 4,194,240 */
+int xg_mlp_forward(xg_mlp* mlp, const float* d_x, int64_t B, float* d_y, void* stream);
+/* mean over the batch of sum_a ((U y / 256 - t)_a / s)^2, V = U R the thin QR of
+ * V[a][i] = p_i^a (weights at the points: R^-1 y); t[B][35]
+ * the moment defects, s[B] the scales; gradient into d_grad (flat, like the
+ * parameters; NULL: internal buffer used by xg_mlp_adam_step). */
+int xg_mlp_loss_grad(xg_mlp* mlp, const float* d_x, const float* d_t35, const float* d_s, int64_t B, float* d_loss,
+                     float* d_grad, void* stream);
+/* Adam (0.9, 0.999, 1e-8) step t >= 1 with d_grad (NULL: the internal gradient). */
+int xg_mlp_adam_step(xg_mlp* mlp, const float* d_grad, float lr, int64_t t, void* stream);
+/* the network's input features of n elements (10 floats each): u = v / max|v|,
+ * the 4 vertex values of u, then the 6 edge-midpoint deviations
+ * u_e - (u_a + u_b) / 2 */
+int xg_learned_features(const double* d_vals10, int64_t n, float* d_x10, void* stream);
+/* learned NEG moments of n <= 4,194,240 elements: straight cut part (FP64) +
+ * the network's correction kOutScale * U y with kOutScale = 1/256 (FP64).
+ * kappa_max >= 0: elements in the relevant band whose curvature indicator
+ * max_e |u_e - (u_a + u_b) / 2| exceeds kappa_max take the isoparametric rule
+ * (order 8) instead; their number goes to d_nfallback (optional). */
+int xg_learned_moments_tet(xg_mlp* mlp, const double* d_vals10, int64_t n, double kappa_max, double* d_out35,
+                           int32_t* d_nfallback, void* stream);
+
 /* ---- batched steps in one CUDA graph --------------------------------------- */
 /* No counterpart in the reference, which assembles one form per
  * BilinearForm::Assemble call (NGSolve's TaskManager parallelises inside it).

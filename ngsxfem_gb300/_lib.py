@@ -30,7 +30,9 @@ EXPORTS = [
     "xg_form_assemble", "xg_form_check", "xg_form_stage_events", "xg_cutfem_step", "xg_cutfem_marking",
     "xg_space_create_st", "xg_space_info_st", "xg_cutinfo_update_st", "xg_st_cut_rules", "xg_st_form_create",
     "xg_st_cutfem_step", "xg_step_graph_create", "xg_step_graph_launch", "xg_step_graph_destroy",
-    "xg_step_graph_kernel_count",
+    "xg_step_graph_kernel_count", "xg_iso_moments_tet", "xg_mlp_param_count", "xg_learned_points",
+    "xg_mlp_create", "xg_mlp_destroy", "xg_mlp_get_params", "xg_mlp_set_params", "xg_mlp_forward",
+    "xg_mlp_loss_grad", "xg_mlp_adam_step", "xg_learned_moments_tet", "xg_learned_features",
 ]
 
 
@@ -125,6 +127,18 @@ def load():
         "xg_step_graph_launch": (I, [P, P]),
         "xg_step_graph_destroy": (I, [P]),
         "xg_step_graph_kernel_count": (I, [P, P]),
+        "xg_iso_moments_tet": (I, [P, I64, I, I, P, P, P]),
+        "xg_mlp_param_count": (I, [P]),
+        "xg_learned_points": (I, [P]),
+        "xg_mlp_create": (I, [ctypes.c_uint64, P]),
+        "xg_mlp_destroy": (I, [P]),
+        "xg_mlp_get_params": (I, [P, P, P]),
+        "xg_mlp_set_params": (I, [P, P, P]),
+        "xg_mlp_forward": (I, [P, P, I64, P, P]),
+        "xg_mlp_loss_grad": (I, [P, P, P, P, I64, P, P, P]),
+        "xg_mlp_adam_step": (I, [P, P, ctypes.c_float, I64, P]),
+        "xg_learned_moments_tet": (I, [P, P, I64, D, P, P, P]),
+        "xg_learned_features": (I, [P, I64, P, P]),
         "xg_space_create_st": (I, [P, I, I, P]),
         "xg_space_info_st": (I, [P, P]),
         "xg_cutinfo_update_st": (I, [P, P, I, P, P, P, P]),

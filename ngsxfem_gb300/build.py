@@ -25,6 +25,8 @@ UNITS = [
     ("xg_geom.cu", ["-fmad=false"]),
     ("xg_asm.cu", []),
     ("xg_st.cu", []),
+    ("xg_iso.cu", ["-fmad=false"]),
+    ("xg_learn.cu", []),
 ]
 
 

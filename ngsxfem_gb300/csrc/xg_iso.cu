@@ -36,7 +36,9 @@ static __constant__ double c_minv[100];
 
 namespace {
 
-constexpr int kTetE[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+// edges (0,1),(0,2),(0,3),(1,2),(1,3),(2,3)
+__host__ __device__ __forceinline__ int edge_a(int e) { return e < 3 ? 0 : (e < 5 ? 1 : 2); }
+__host__ __device__ __forceinline__ int edge_b(int e) { return e < 3 ? e + 1 : (e == 3 ? 2 : 3); }
 
 __host__ __device__ __forceinline__ double dlam(int i, int j) { return i < 3 ? (i == j ? 1.0 : 0.0) : -1.0; }
 
@@ -61,7 +63,7 @@ __host__ __device__ __forceinline__ double p2_value(const double* v, const doubl
     for (int j = 0; j < 3; j++) grad[j] += v[i] * dn * dlam(i, j);
   }
   for (int e = 0; e < 6; e++) {
-    const int a = kTetE[e][0], b = kTetE[e][1];
+    const int a = edge_a(e), b = edge_b(e);
     const double c = v[4 + e];
     val += c * 4.0 * l[a] * l[b];
     for (int j = 0; j < 3; j++) grad[j] += c * 4.0 * (dlam(a, j) * l[b] + l[a] * dlam(b, j));
@@ -73,7 +75,7 @@ __host__ __device__ __forceinline__ void p2h_shape(const double* x, double* phi)
   double l[4];
   lambdas(x, l);
   for (int i = 0; i < 4; i++) phi[i] = l[i];
-  for (int e = 0; e < 6; e++) phi[4 + e] = l[kTetE[e][0]] * l[kTetE[e][1]];
+  for (int e = 0; e < 6; e++) phi[4 + e] = l[edge_a(e)] * l[edge_b(e)];
 }
 
 // y = x + Theta(x), A = I + grad Theta
@@ -85,7 +87,7 @@ __device__ __forceinline__ void deform_at(const double (*theta)[3], const double
     for (int c = 0; c < 3; c++) A[r][c] = r == c ? 1.0 : 0.0;
   }
   for (int e = 0; e < 6; e++) {
-    const int a = kTetE[e][0], b = kTetE[e][1];
+    const int a = edge_a(e), b = edge_b(e);
     const double phi = l[a] * l[b];
     double dphi[3];
     for (int c = 0; c < 3; c++) dphi[c] = dlam(a, c) * l[b] + l[a] * dlam(b, c);
@@ -172,10 +174,15 @@ __device__ int iso_theta(const double* v, const double* p1, double (*theta)[3]) 
 }  // namespace
 
 // NEG-part moments of the reference tet under the P2 values of each element
-// (deform = 0: the straight cut rule of the P1 interpolant alone).
-__global__ void __launch_bounds__(128) k_tet_moments(const double* __restrict__ vals, int64_t n, int order,
-                                                      int deform, double* __restrict__ out, int32_t* nonconv) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+// (deform = 0: the straight cut rule of the P1 interpolant alone).  With a
+// list, element list[i] for i < *count (count on the device).
+__global__ void __launch_bounds__(128) k_tet_moments(const double* __restrict__ vals, int64_t n,
+                                                      const int32_t* __restrict__ list, const int32_t* count,
+                                                      int order, int deform, double* __restrict__ out,
+                                                      int32_t* nonconv) {
+  const int64_t cnt = count ? (int64_t)*count : n;
+  for (int64_t ii = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ii < cnt; ii += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = list ? (int64_t)list[ii] : ii;
     double v[10];
     for (int k = 0; k < 10; k++) v[k] = vals[i * 10 + k];
     double p1[4];
@@ -281,12 +288,12 @@ int upload_iso() {
 }  // namespace
 
 int tet_moments_launch(const double* d_vals, int64_t n, int order, int deform, double* d_out, int32_t* d_nonconv,
-                       cudaStream_t s) {
+                       cudaStream_t s, const int32_t* d_list, const int32_t* d_count) {
   int st = upload_iso();
   if (st) return st;
   if (n == 0) return XG_OK;
   const int64_t blocks = std::min<int64_t>((n + 127) / 128, 152 * 16);
-  k_tet_moments<<<(unsigned)blocks, 128, 0, s>>>(d_vals, n, order, deform, d_out, d_nonconv);
+  k_tet_moments<<<(unsigned)blocks, 128, 0, s>>>(d_vals, n, d_list, d_count, order, deform, d_out, d_nonconv);
   XG_CUDA(cudaGetLastError());
   return XG_OK;
 }
@@ -296,5 +303,6 @@ int tet_moments_launch(const double* d_vals, int64_t n, int order, int deform, d
 extern "C" int xg_iso_moments_tet(const double* d_vals10, int64_t n, int order, int deform, double* d_out35,
                                   int32_t* d_nonconv, void* stream) {
   if (!d_vals10 || !d_out35 || n < 0 || order < 0 || order > xg::kMaxOrder) return XG_ERR_ARG;
-  return xg::tet_moments_launch(d_vals10, n, order, deform, d_out35, d_nonconv, (cudaStream_t)stream);
+  return xg::tet_moments_launch(d_vals10, n, order, deform, d_out35, d_nonconv, (cudaStream_t)stream, nullptr,
+                                nullptr);
 }
