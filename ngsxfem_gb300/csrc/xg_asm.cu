@@ -966,11 +966,12 @@ struct RowSm {
   int* ent_first;  // [kEnt][4] 1 if the row's element is the facet's first element
   int* celem;      // [kEnt * 5]
   int* grp;        // [kEnt * 9] (entry << 4) | kind
+  int* ent_slot;   // [kEnt] element-matrix slot of an active element
 };
 
 __host__ __device__ inline int row_smem_bytes(int hs, int maxu, int stage) {
   return hs * 4 + maxu * 4 + maxu * 8 + stage * 8 + stage * 4 + kEnt * 4 * 2 + kEnt * 4 * 4 * 3 + kEnt * 5 * 4 +
-         kEnt * 9 * 4 + 16;
+         kEnt * 9 * 4 + kEnt * 4 + 16;
 }
 
 __device__ __forceinline__ RowSm row_sm(const ScatterArgs& A, unsigned char* base) {
@@ -987,8 +988,29 @@ __device__ __forceinline__ RowSm row_sm(const ScatterArgs& A, unsigned char* bas
   S.ent_first = S.ent_fs + kEnt * 4;
   S.celem = S.ent_first + kEnt * 4;
   S.grp = S.celem + kEnt * 5;
+  S.ent_slot = S.grp + kEnt * 9;
   return S;
 }
+
+// (t / nd, t % nd) for t = lane, lane + 32, ... without an integer division per step
+struct LaneIdx {
+  int g, j, dg, dj, nd;
+  __device__ __forceinline__ void init(int t, int nd_) {
+    nd = nd_;
+    g = t / nd;
+    j = t - g * nd;
+    dg = 32 / nd;
+    dj = 32 - dg * nd;
+  }
+  __device__ __forceinline__ void next() {
+    g += dg;
+    j += dj;
+    if (j >= nd) {
+      j -= nd;
+      g++;
+    }
+  }
+};
 
 __device__ __forceinline__ bool el_active(const ScatterArgs& A, int e) {
   return tbit32(A.act_un, e) || tbit32(A.act_cut, e);
@@ -1000,24 +1022,39 @@ __device__ int load_entries(const ScatterArgs& A, const RowSm& S, int c0, int na
   const int lane = threadIdx.x & 31;
   int ncand = 0;
   if (lane < na) {
+    // three levels of independent loads (element; its facets; the active
+    // facets' neighbours and slots) instead of one dependent chain per facet
     const int v = A.adj[c0 + lane];
     const int e = v >> 5, i = v & 31;
     const bool act = el_active(A, e);
+    const int slot = A.el_slot[e];
+    int f[4], fa[4];
+#pragma unroll
+    for (int lf = 0; lf < 4; lf++) f[lf] = lf < A.nfl ? A.el_facets[(int64_t)e * A.nfl + lf] : 0;
+#pragma unroll
+    for (int lf = 0; lf < 4; lf++) fa[lf] = lf < A.nfl && tbit32(A.act_fa, f[lf]);
+    int2 pr[4];
+    int fsl[4];
+#pragma unroll
+    for (int lf = 0; lf < 4; lf++) {
+      pr[lf] = fa[lf] ? A.fel[f[lf]] : make_int2(-1, -1);
+      fsl[lf] = fa[lf] ? A.fa_slot[f[lf]] : 0;
+    }
     S.ent_e[lane] = act ? e : ~e;  // sign marks an inactive element
     S.ent_i[lane] = i;
+    S.ent_slot[lane] = act ? slot : -1;
     int nf = 0;
-    for (int lf = 0; lf < A.nfl; lf++) {
-      int nb = -1, fs = 0, first = 0;
-      const int f = A.el_facets[(int64_t)e * A.nfl + lf];
-      if (tbit32(A.act_fa, f)) {
-        const int2 p = A.fel[f];
-        first = p.x == e;
-        nb = first ? p.y : p.x;
-        fs = A.fa_slot[f];
+#pragma unroll
+    for (int lf = 0; lf < 4; lf++) {
+      if (lf >= A.nfl) break;
+      int nb = -1, first = 0;
+      if (fa[lf]) {
+        first = pr[lf].x == e;
+        nb = first ? pr[lf].y : pr[lf].x;
         nf++;
       }
       S.ent_nb[lane * 4 + lf] = nb;
-      S.ent_fs[lane * 4 + lf] = fs;
+      S.ent_fs[lane * 4 + lf] = fa[lf] ? fsl[lf] : 0;
       S.ent_first[lane * 4 + lf] = first;
     }
     ncand = ((act || nf) ? 1 : 0) + nf;
@@ -1060,9 +1097,21 @@ __device__ bool row_columns(const ScatterArgs& A, const RowSm& S, int r) {
   for (int c0 = a0; c0 < a1; c0 += kEnt) {
     const int na = min(kEnt, a1 - c0);
     const int nc = load_entries(A, S, c0, na);
-    for (int t = lane; t < nc * A.nd; t += 32) {
-      const int e = S.celem[t / A.nd], j = t % A.nd;
-      ok &= hash_insert(S.hash, A.hs, A.el_dofs[(int64_t)e * A.nd + j]);
+    // four independent dof loads in flight per lane before the inserts
+    LaneIdx L;
+    L.init(lane, A.nd);
+    for (int t0 = lane; t0 < nc * A.nd; t0 += 128) {
+      int key[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const int t = t0 + 32 * q;
+        key[q] = -1;
+        if (t < nc * A.nd) key[q] = A.el_dofs[(int64_t)S.celem[L.g] * A.nd + L.j];
+        L.next();
+      }
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+        if (key[q] >= 0) ok &= hash_insert(S.hash, A.hs, key[q]);
     }
     __syncwarp();
   }
@@ -1223,34 +1272,62 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_row_fill(ScatterArgs A, cons
       }
       for (int g0 = 0; g0 < ng; g0 += gpb) {
         const int gb = min(gpb, ng - g0);
-        for (int t = lane; t < gb * nd; t += 32) {
-          const int g = g0 + t / nd, j = t % nd;
-          const int a = S.grp[g] >> 4, kind = S.grp[g] & 15;
-          const int ee = S.ent_e[a];
-          const int e = ee >= 0 ? ee : ~ee, i = S.ent_i[a];
-          int colel;
-          double v;
-          if (kind == 0) {
-            colel = e;
-            const int64_t eo = (int64_t)A.el_slot[e];
-            v = A.el_sym ? (double)elmat[eo * tri_size(nd) + (i <= j ? tri_index(i, j, nd) : tri_index(j, i, nd))]
-                         : (double)elmat[(eo * nd + i) * nd + j];
-          } else {
-            // patch matrices are spatial: local space-time index = time dof * nds + spatial dof
-            const int lf = (kind - 1) >> 1, h = (kind - 1) & 1;
-            const int first = S.ent_first[a * 4 + lf], nb = S.ent_nb[a * 4 + lf], fs = S.ent_fs[a * 4 + lf];
-            const int nds = A.nds, n2s = 2 * nds;
-            const int ir = i / nds, jr = i % nds, ic = j / nds, jc = j % nds;
-            const int prow = first ? jr : nds + jr, pcol = h * nds + jc;
-            colel = (h == 0) == (first != 0) ? e : nb;
-            v = fs < A.cap_fa ? A.mt[ir * A.kt1 + ic] *
-                                    (double)famat[(int64_t)fs * tri_size(n2s) +
-                                                  (prow <= pcol ? tri_index(prow, pcol, n2s) : tri_index(pcol, prow, n2s))]
-                              : 0.0;
+        // four independent (value, column) loads in flight per lane, then the
+        // position searches
+        LaneIdx L;
+        L.init(lane, nd);
+        for (int t0 = lane; t0 < gb * nd; t0 += 128) {
+          double vq[4];
+          int cq[4];
+#pragma unroll
+          for (int q = 0; q < 4; q++) {
+            const int t = t0 + 32 * q;
+            vq[q] = 0.0;
+            cq[q] = -1;
+            // the tail repeats the last valid entry's loads
+            const bool in = t < gb * nd;
+            const int g = g0 + (in ? L.g : gb - 1), j = in ? L.j : nd - 1;
+            L.next();
+            const int a = S.grp[g] >> 4, kind = S.grp[g] & 15;
+            const int ee = S.ent_e[a];
+            const int e = ee >= 0 ? ee : ~ee, i = S.ent_i[a];
+            int colel;
+            if (kind == 0) {
+              colel = e;
+              const int64_t eo = (int64_t)S.ent_slot[a];
+              vq[q] = A.el_sym ? (double)elmat[eo * tri_size(nd) + (i <= j ? tri_index(i, j, nd) : tri_index(j, i, nd))]
+                               : (double)elmat[(eo * nd + i) * nd + j];
+            } else {
+              // patch matrices are spatial: local space-time index = time dof * nds + spatial dof
+              const int lf = (kind - 1) >> 1, h = (kind - 1) & 1;
+              const int first = S.ent_first[a * 4 + lf], nb = S.ent_nb[a * 4 + lf], fs = S.ent_fs[a * 4 + lf];
+              const int nds = A.nds, n2s = 2 * nds;
+              int ir = 0, jr = i, ic = 0, jc = j;
+              if (A.kt1 > 1) {
+                ir = i / nds;
+                jr = i - ir * nds;
+                ic = j / nds;
+                jc = j - ic * nds;
+              }
+              const int prow = first ? jr : nds + jr, pcol = h * nds + jc;
+              colel = (h == 0) == (first != 0) ? e : nb;
+              vq[q] = fs < A.cap_fa
+                          ? A.mt[ir * A.kt1 + ic] *
+                                (double)famat[(int64_t)fs * tri_size(n2s) +
+                                              (prow <= pcol ? tri_index(prow, pcol, n2s) : tri_index(pcol, prow, n2s))]
+                          : 0.0;
+            }
+            cq[q] = A.el_dofs[(int64_t)colel * nd + j];
+            if (t >= gb * nd) cq[q] = -1;  // tail: loads repeat the last valid entry
           }
-          const int c = A.el_dofs[(int64_t)colel * nd + j];
-          S.spos[t] = lower_bound_sm(S.ucols, u, c);
-          S.sval[t] = v;
+#pragma unroll
+          for (int q = 0; q < 4; q++) {
+            const int t = t0 + 32 * q;
+            if (t < gb * nd) {
+              S.spos[t] = lower_bound_sm(S.ucols, u, cq[q]);
+              S.sval[t] = vq[q];
+            }
+          }
         }
         __syncwarp();
         for (int g = 0; g < gb; g++) {
