@@ -940,12 +940,16 @@ struct ScatterArgs {
   const int* counts;         // [3] = nrows
   int64_t cap_fa;
   const int64_t* full_ptr;   // per dof: offset of its row in tmp_cols (full-pattern row sizes)
-  int32_t* tmp_cols;         // sorted column dofs of each active row, written by the count pass
+  int32_t* tmp_cols;         // full-pattern columns of every dof row, sorted (written once at creation)
+  const uint16_t* fpos_el;   // [ne][nd][nd] positions of element columns in the full rows
+  uint16_t* pbuf;            // [cap_fa][2][nd][nd] positions of neighbour columns of active facets
+  uint8_t* flags;            // [full_nnz] active columns of the active rows
   int el_sym;                // element matrices stored as packed upper triangles
   int nds, kt1;              // spatial dofs per element, time dofs (1 for spatial forms)
   double mt[9];              // time mass kt1 x kt1: patch value = mt[it][is] * spatial patch value
-  int hs;                    // hash slots per warp (pow2)
+  int hs;                    // hash slots per warp (pow2, or 0)
   int maxu;                  // distinct-column capacity per warp (pow2)
+  int ucn, accn;             // shared column ints / accumulator doubles per warp (0 or maxu)
   int stage;                 // staged (pos, value) pairs per warp
   int wbytes;                // shared bytes per warp
 };
@@ -969,8 +973,8 @@ struct RowSm {
   int* ent_slot;   // [kEnt] element-matrix slot of an active element
 };
 
-__host__ __device__ inline int row_smem_bytes(int hs, int maxu, int stage) {
-  return hs * 4 + maxu * 4 + maxu * 8 + stage * 8 + stage * 4 + kEnt * 4 * 2 + kEnt * 4 * 4 * 3 + kEnt * 5 * 4 +
+__host__ __device__ inline int row_smem_bytes(int hs, int ucn, int accn, int stage) {
+  return hs * 4 + ucn * 4 + accn * 8 + stage * 8 + stage * 4 + kEnt * 4 * 2 + kEnt * 4 * 4 * 3 + kEnt * 5 * 4 +
          kEnt * 9 * 4 + kEnt * 4 + 16;
 }
 
@@ -978,8 +982,8 @@ __device__ __forceinline__ RowSm row_sm(const ScatterArgs& A, unsigned char* bas
   RowSm S;
   S.hash = (int*)base;
   S.ucols = S.hash + A.hs;
-  S.acc = (double*)(S.ucols + A.maxu);  // hs, maxu are powers of two >= 32: 8-byte aligned
-  S.sval = S.acc + A.maxu;
+  S.acc = (double*)(S.ucols + A.ucn);  // hs, ucn are 0 or powers of two >= 32: 8-byte aligned
+  S.sval = S.acc + A.accn;
   S.spos = (int*)(S.sval + A.stage);
   S.ent_e = S.spos + A.stage;
   S.ent_i = S.ent_e + kEnt;
@@ -1214,8 +1218,104 @@ __global__ void k_fill_u32(uint32_t* p, int64_t n, uint32_t v) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = v;
 }
 
+// positions of element columns in the full-pattern rows: thread per (e, i, j)
+__global__ void k_fpos_el(ScatterArgs A, uint16_t* __restrict__ fpos, int* err) {
+  const int64_t nd = A.nd, n = (int64_t)A.ne * nd * nd;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = t / (nd * nd);
+    const int i = (int)((t / nd) % nd), j = (int)(t % nd);
+    const int r = A.el_dofs[e * nd + i], c = A.el_dofs[e * nd + j];
+    const int64_t fo = A.full_ptr[r];
+    const int len = (int)(A.full_ptr[r + 1] - fo);
+    int lo = 0, hi = len;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (A.tmp_cols[fo + mid] < c) lo = mid + 1;
+      else hi = mid;
+    }
+    if (lo >= len || A.tmp_cols[fo + lo] != c || lo > 65535) set_err(err, XG_ERR_CAPACITY);
+    fpos[t] = (uint16_t)min(lo, 65535);
+  }
+}
+
+// Pass 1 (per step): per active row, the active columns as flags over the
+// row's full-pattern positions (element columns from the static positions,
+// neighbour columns of active facets by a search of the full row, recorded in
+// pbuf for pass 2), and the count.
+__global__ void __launch_bounds__(kRowWarps * 32) k_row_mark(ScatterArgs A, int64_t* rowcnt, int* err) {
+  extern __shared__ __align__(16) unsigned char sm_rows[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const RowSm S = row_sm(A, sm_rows + (size_t)warp * A.wbytes);
+  uint8_t* sflags = (uint8_t*)S.hash;  // hs * 4 >= maxu bytes
+  const int nrows = A.counts[3];
+  const int nd = A.nd;
+  for (int row = blockIdx.x * kRowWarps + warp; row < nrows; row += gridDim.x * kRowWarps) {
+    const int r = A.rows[row];
+    const int64_t fo = A.full_ptr[r];
+    const int len = (int)(A.full_ptr[r + 1] - fo);
+    if (len > A.maxu) {
+      if (lane == 0) {
+        set_err(err, XG_ERR_CAPACITY);
+        rowcnt[row] = 0;
+      }
+      continue;
+    }
+    for (int k = lane; k < len; k += 32) {
+      S.ucols[k] = A.tmp_cols[fo + k];
+      sflags[k] = 0;
+    }
+    __syncwarp();
+    const int a0 = A.adj_ptr[r], a1 = A.adj_ptr[r + 1];
+    for (int c0 = a0; c0 < a1; c0 += kEnt) {
+      const int na = min(kEnt, a1 - c0);
+      load_entries(A, S, c0, na);
+      // own element columns of entries with an active element or an active facet
+      LaneIdx L;
+      L.init(lane, nd);
+      for (int t = lane; t < na * nd; t += 32, L.next()) {
+        const int a = L.g, j = L.j;
+        const int ee = S.ent_e[a];
+        bool any = ee >= 0;
+        for (int lf = 0; lf < A.nfl; lf++) any |= S.ent_nb[a * 4 + lf] >= 0;
+        if (any) {
+          const int e = ee >= 0 ? ee : ~ee;
+          sflags[A.fpos_el[((int64_t)e * nd + S.ent_i[a]) * nd + j]] = 1;
+        }
+      }
+      // neighbour columns of the active facets
+      L.init(lane, nd);
+      for (int t = lane; t < na * 4 * nd; t += 32, L.next()) {
+        const int a = L.g >> 2, lf = L.g & 3, j = L.j;
+        if (lf >= A.nfl) continue;
+        const int nb = S.ent_nb[a * 4 + lf];
+        if (nb < 0) continue;
+        const int pos = lower_bound_sm(S.ucols, len, A.el_dofs[(int64_t)nb * nd + j]);
+        sflags[min(pos, len - 1)] = 1;
+        const int fs = S.ent_fs[a * 4 + lf];
+        if (fs < A.cap_fa)
+          A.pbuf[(((int64_t)fs * 2 + (S.ent_first[a * 4 + lf] ? 0 : 1)) * nd + S.ent_i[a]) * nd + j] = (uint16_t)pos;
+      }
+      __syncwarp();
+    }
+    int cnt = 0;
+    for (int k = lane; k < len; k += 32) {
+      const uint8_t fl = sflags[k];
+      A.flags[fo + k] = fl;
+      cnt += fl;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    if (lane == 0) rowcnt[row] = cnt;
+    __syncwarp();
+  }
+}
+
+// Pass 2 (per step): values of each active row summed in a fixed order
+// (adjacency order; per entry its element row, then its active facets) over
+// the row's full-pattern positions, then written compressed to the active
+// columns in ascending order.
 template <typename T>
-__global__ void __launch_bounds__(kRowWarps * 32) k_row_fill(ScatterArgs A, const T* __restrict__ elmat,
+__global__ void __launch_bounds__(kRowWarps * 32) k_row_sum(ScatterArgs A, const T* __restrict__ elmat,
                                                              const T* __restrict__ famat,
                                                              const int64_t* __restrict__ rowptr,
                                                              int32_t* __restrict__ cols, double* __restrict__ vals,
@@ -1230,21 +1330,18 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_row_fill(ScatterArgs A, cons
     const int r = A.rows[row];
     const int64_t rp = rowptr[row];
     const int u = (int)(rowptr[row + 1] - rp);
-    if (u > A.maxu || rp + u > cap_nnz) {
+    const int64_t fo = A.full_ptr[r];
+    const int len = (int)(A.full_ptr[r + 1] - fo);
+    if (len > A.maxu || rp + u > cap_nnz) {
       if (lane == 0) set_err(err, XG_ERR_CAPACITY);
       continue;
     }
-    const int64_t fo = A.full_ptr[r];
-    for (int k = lane; k < u; k += 32) {
-      S.ucols[k] = A.tmp_cols[fo + k];
-      S.acc[k] = 0.0;
-    }
+    for (int k = lane; k < len; k += 32) S.acc[k] = 0.0;
     __syncwarp();
     const int a0 = A.adj_ptr[r], a1 = A.adj_ptr[r + 1];
     for (int c0 = a0; c0 < a1; c0 += kEnt) {
       const int na = min(kEnt, a1 - c0);
       load_entries(A, S, c0, na);
-      // groups in the fixed order: per entry its element row, then its active facets (first, second half)
       int ng = 0;
       {
         int cnt = 0;
@@ -1272,35 +1369,32 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_row_fill(ScatterArgs A, cons
       }
       for (int g0 = 0; g0 < ng; g0 += gpb) {
         const int gb = min(gpb, ng - g0);
-        // four independent (value, column) loads in flight per lane, then the
-        // position searches
         LaneIdx L;
         L.init(lane, nd);
         for (int t0 = lane; t0 < gb * nd; t0 += 128) {
           double vq[4];
-          int cq[4];
+          int pq[4];
 #pragma unroll
           for (int q = 0; q < 4; q++) {
             const int t = t0 + 32 * q;
-            vq[q] = 0.0;
-            cq[q] = -1;
-            // the tail repeats the last valid entry's loads
             const bool in = t < gb * nd;
             const int g = g0 + (in ? L.g : gb - 1), j = in ? L.j : nd - 1;
             L.next();
             const int a = S.grp[g] >> 4, kind = S.grp[g] & 15;
             const int ee = S.ent_e[a];
             const int e = ee >= 0 ? ee : ~ee, i = S.ent_i[a];
-            int colel;
+            const int64_t own = ((int64_t)e * nd + i) * nd + j;
+            int pos;
+            double v;
             if (kind == 0) {
-              colel = e;
               const int64_t eo = (int64_t)S.ent_slot[a];
-              vq[q] = A.el_sym ? (double)elmat[eo * tri_size(nd) + (i <= j ? tri_index(i, j, nd) : tri_index(j, i, nd))]
-                               : (double)elmat[(eo * nd + i) * nd + j];
+              v = A.el_sym ? (double)elmat[eo * tri_size(nd) + (i <= j ? tri_index(i, j, nd) : tri_index(j, i, nd))]
+                           : (double)elmat[(eo * nd + i) * nd + j];
+              pos = A.fpos_el[own];
             } else {
               // patch matrices are spatial: local space-time index = time dof * nds + spatial dof
               const int lf = (kind - 1) >> 1, h = (kind - 1) & 1;
-              const int first = S.ent_first[a * 4 + lf], nb = S.ent_nb[a * 4 + lf], fs = S.ent_fs[a * 4 + lf];
+              const int first = S.ent_first[a * 4 + lf], fs = S.ent_fs[a * 4 + lf];
               const int nds = A.nds, n2s = 2 * nds;
               int ir = 0, jr = i, ic = 0, jc = j;
               if (A.kt1 > 1) {
@@ -1310,21 +1404,26 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_row_fill(ScatterArgs A, cons
                 jc = j - ic * nds;
               }
               const int prow = first ? jr : nds + jr, pcol = h * nds + jc;
-              colel = (h == 0) == (first != 0) ? e : nb;
-              vq[q] = fs < A.cap_fa
-                          ? A.mt[ir * A.kt1 + ic] *
-                                (double)famat[(int64_t)fs * tri_size(n2s) +
-                                              (prow <= pcol ? tri_index(prow, pcol, n2s) : tri_index(pcol, prow, n2s))]
-                          : 0.0;
+              const bool self = (h == 0) == (first != 0);
+              if (fs < A.cap_fa) {
+                v = A.mt[ir * A.kt1 + ic] *
+                    (double)famat[(int64_t)fs * tri_size(n2s) +
+                                  (prow <= pcol ? tri_index(prow, pcol, n2s) : tri_index(pcol, prow, n2s))];
+                pos = self ? (int)A.fpos_el[own]
+                           : (int)A.pbuf[(((int64_t)fs * 2 + (first ? 0 : 1)) * nd + i) * nd + j];
+              } else {
+                v = 0.0;
+                pos = -1;
+              }
             }
-            cq[q] = A.el_dofs[(int64_t)colel * nd + j];
-            if (t >= gb * nd) cq[q] = -1;  // tail: loads repeat the last valid entry
+            vq[q] = v;
+            pq[q] = in ? pos : -1;
           }
 #pragma unroll
           for (int q = 0; q < 4; q++) {
             const int t = t0 + 32 * q;
             if (t < gb * nd) {
-              S.spos[t] = lower_bound_sm(S.ucols, u, cq[q]);
+              S.spos[t] = pq[q];
               S.sval[t] = vq[q];
             }
           }
@@ -1333,19 +1432,32 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_row_fill(ScatterArgs A, cons
         for (int g = 0; g < gb; g++) {
           if (lane < nd) {
             const int pos = S.spos[g * nd + lane];
-            if (pos < u) S.acc[pos] += S.sval[g * nd + lane];
+            if (pos >= 0 && pos < len) S.acc[pos] += S.sval[g * nd + lane];
           }
           __syncwarp();
         }
       }
     }
-    for (int k = lane; k < u; k += 32) {
-      cols[rp + k] = A.dof_row[S.ucols[k]];
-      vals[rp + k] = S.acc[k];
+    // compressed write: ascending active columns
+    int base = 0;
+    for (int k0 = 0; k0 < len; k0 += 32) {
+      const int k = k0 + lane;
+      const bool fl = k < len && A.flags[fo + k];
+      const unsigned m = __ballot_sync(0xffffffffu, fl);
+      if (fl) {
+        const int c = base + __popc(m & ((1u << lane) - 1));
+        if (c < u) {
+          cols[rp + c] = A.dof_row[A.tmp_cols[fo + k]];
+          vals[rp + c] = S.acc[k];
+        }
+      }
+      base += __popc(m);
     }
+    if (lane == 0 && base != u) set_err(err, XG_ERR_CAPACITY);
     __syncwarp();
   }
 }
+
 
 }  // namespace xg
 
@@ -1389,9 +1501,14 @@ struct xg_form {
   int* d_err = nullptr;
   int sc_hs = 0, sc_maxu = 0, sc_stage = 0, sc_wbytes = 0;
   size_t sc_smem = 0;
+  int mk_wbytes = 0, sm_wbytes = 0, grid_mk = 0, grid_sm = 0;  // per-step scatter kernels
+  size_t mk_smem = 0, sm_smem = 0;
   int64_t full_nnz = 0;
   int64_t* d_full_ptr = nullptr;
-  int32_t* d_tmp_cols = nullptr;
+  int32_t* d_tmp_cols = nullptr;  // full-pattern columns of every dof row (sorted), built at creation
+  uint16_t* d_fpos_el = nullptr;  // [ne][nd][nd]: position of element column j in the full row of local row i
+  uint16_t* d_pbuf = nullptr;     // [cap_fa][2][nd][nd]: neighbour-column positions of active facets (per step)
+  uint8_t* d_flags = nullptr;     // [full_nnz]: active columns of each active row (per step)
   int max_unique = 0;
   int grid_el_un = 0, grid_el_cut = 0, grid_fa = 0, grid_sc = 0;
   // CutFEM step state
@@ -1414,7 +1531,7 @@ namespace {
 int form_workspace(xg_form* f);
 
 int form_free(xg_form* f) {
-  void* ptrs[] = {f->d_full_ptr, f->d_tmp_cols, f->d_tabs, f->d_act_un, f->d_act_cut, f->d_act_fa, f->d_dof_bits, f->d_l_un, f->d_l_cut, f->d_l_fa,
+  void* ptrs[] = {f->d_full_ptr, f->d_tmp_cols, f->d_fpos_el, f->d_pbuf, f->d_flags, f->d_tabs, f->d_act_un, f->d_act_cut, f->d_act_fa, f->d_dof_bits, f->d_l_un, f->d_l_cut, f->d_l_fa,
                   f->d_el_slot, f->d_fa_slot, f->d_dof_row, f->d_rowcnt, f->d_counts, f->d_bsum, f->d_bsum64,
                   f->d_elmat, f->d_famat, f->d_err, f->d_dom, f->d_ratio, f->d_bits, f->d_fbits};
   for (void* p : ptrs) cudaFree(p);
@@ -1738,9 +1855,14 @@ ScatterArgs scatter_args(xg_form* f) {
   for (int k = 0; k < 9; k++) A.mt[k] = f->mt[k];
   A.full_ptr = f->d_full_ptr;
   A.tmp_cols = f->d_tmp_cols;
+  A.fpos_el = f->d_fpos_el;
+  A.pbuf = f->d_pbuf;
+  A.flags = f->d_flags;
   A.hs = f->sc_hs;
   A.maxu = f->sc_maxu;
-  A.stage = f->sc_stage;
+  A.ucn = f->sc_maxu;
+  A.accn = 0;
+  A.stage = 0;
   A.wbytes = f->sc_wbytes;
   return A;
 }
@@ -1758,21 +1880,31 @@ int scatter_phase(xg_form* f, xg_csr* out, cudaStream_t s) {
   // 4. pattern and values
   ScatterArgs A = scatter_args(f);
   A.rows = out->d_row_dof;
-  k_row_count<<<f->grid_sc, kRowWarps * 32, f->sc_smem, s>>>(A, f->d_rowcnt, f->d_err);
+  A.hs = std::max(32, f->sc_maxu / 4);
+  A.ucn = f->sc_maxu;
+  A.accn = 0;
+  A.stage = 0;
+  A.wbytes = f->mk_wbytes;
+  k_row_mark<<<f->grid_mk, kRowWarps * 32, f->mk_smem, s>>>(A, f->d_rowcnt, f->d_err);
   const int nb64 = (int)((sp->ndof + kSChunk - 1) / kSChunk);
   k_sum64_blocks<<<nb64, kSThreads, 0, s>>>(f->d_rowcnt, f->d_counts + 3, f->d_bsum64);
   k_scan64_small<<<1, 1024, 0, s>>>(f->d_bsum64, nb64);
   k_scan64_apply<<<nb64, kSThreads, 0, s>>>(f->d_rowcnt, f->d_counts + 3, f->d_bsum64, out->d_rowptr, out->d_counts,
                                             out->cap_nnz, f->d_err);
   if (f->use_ev) cudaEventRecord(f->ev[6], s);
+  A.hs = 0;
+  A.ucn = 0;
+  A.accn = f->sc_maxu;
+  A.stage = f->sc_stage;
+  A.wbytes = f->sm_wbytes;
   if (f->precision == XG_PREC_FP64)
-    k_row_fill<double><<<f->grid_sc, kRowWarps * 32, f->sc_smem, s>>>(A, (const double*)f->d_elmat,
-                                                                    (const double*)f->d_famat, out->d_rowptr,
-                                                                    out->d_cols, out->d_vals, out->cap_nnz, f->d_err);
-  else
-    k_row_fill<float><<<f->grid_sc, kRowWarps * 32, f->sc_smem, s>>>(A, (const float*)f->d_elmat,
-                                                                   (const float*)f->d_famat, out->d_rowptr,
+    k_row_sum<double><<<f->grid_sm, kRowWarps * 32, f->sm_smem, s>>>(A, (const double*)f->d_elmat,
+                                                                   (const double*)f->d_famat, out->d_rowptr,
                                                                    out->d_cols, out->d_vals, out->cap_nnz, f->d_err);
+  else
+    k_row_sum<float><<<f->grid_sm, kRowWarps * 32, f->sm_smem, s>>>(A, (const float*)f->d_elmat,
+                                                                  (const float*)f->d_famat, out->d_rowptr,
+                                                                  out->d_cols, out->d_vals, out->cap_nnz, f->d_err);
   if (f->use_ev) cudaEventRecord(f->ev[7], s);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? XG_OK : cuda_fail(e, "xg_form_assemble");
@@ -1905,8 +2037,10 @@ int full_pattern_probe(xg_form* f, std::vector<int64_t>& full_ptr) {
   A.rows = d_rows;
   A.hs = 4096;
   A.maxu = 0;
+  A.ucn = 0;
+  A.accn = 0;
   A.stage = 0;
-  A.wbytes = (row_smem_bytes(A.hs, 0, 0) + 15) & ~15;
+  A.wbytes = (row_smem_bytes(A.hs, 0, 0, 0) + 15) & ~15;
   const size_t smem = (size_t)kRowWarps * A.wbytes;
   cudaFuncSetAttribute(k_row_probe, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   const int grid = grid_for(k_row_probe, kRowWarps * 32, smem);
@@ -1927,6 +2061,55 @@ int full_pattern_probe(xg_form* f, std::vector<int64_t>& full_ptr) {
   }
   f->full_nnz = full_ptr[ndof];
   f->max_unique = mx;
+  return XG_OK;
+}
+
+// Static scatter structure (form creation): the sorted full-pattern columns of
+// every dof row (the row pass with every element and interior facet active),
+// the full-row positions of every element's columns, and the per-step buffers.
+// The activity bits still hold the all-active state of the probe.
+int full_pattern_build(xg_form* f) {
+  xg_mesh* m = f->mesh;
+  xg_space* sp = f->space;
+  const int64_t ndof = sp->ndof;
+  const int64_t nd = sp->nd;
+  auto A_ = [&](void** p, size_t bytes) { return cudaMalloc(p, bytes ? bytes : 16); };
+  cudaError_t e = A_((void**)&f->d_fpos_el, (size_t)m->ne * nd * nd * 2);
+  if (!e) e = A_((void**)&f->d_pbuf, f->has_patch ? (size_t)f->cap_fa * 2 * nd * nd * 2 : 16);
+  if (!e) e = A_((void**)&f->d_flags, (size_t)f->full_nnz);
+  int32_t* d_rows = nullptr;
+  if (!e) e = A_((void**)&d_rows, sizeof(int32_t) * (size_t)std::max<int64_t>(ndof, 1));
+  if (e) {
+    cudaFree(d_rows);
+    return cuda_fail(e, "xg_form_create");
+  }
+  std::vector<int32_t> iota(ndof);
+  for (int64_t i = 0; i < ndof; i++) iota[i] = (int32_t)i;
+  int cnt[8] = {0, 0, 0, (int)ndof, 0, 0, 0, 0};
+  e = cudaMemcpy(d_rows, iota.data(), sizeof(int32_t) * ndof, cudaMemcpyHostToDevice);
+  if (!e) e = cudaMemcpy(f->d_counts, cnt, sizeof(cnt), cudaMemcpyHostToDevice);
+  if (!e) e = cudaMemset(f->d_err, 0, sizeof(int));
+  if (e) {
+    cudaFree(d_rows);
+    return cuda_fail(e, "xg_form_create");
+  }
+  ScatterArgs A = scatter_args(f);
+  A.rows = d_rows;
+  k_row_count<<<f->grid_sc, kRowWarps * 32, f->sc_smem>>>(A, f->d_rowcnt, f->d_err);
+  const int64_t nt = (int64_t)m->ne * nd * nd;
+  k_fpos_el<<<(unsigned)std::min<int64_t>((nt + 255) / 256, 152 * 64), 256>>>(A, f->d_fpos_el, f->d_err);
+  e = cudaGetLastError();
+  int herr = 0;
+  if (!e) e = cudaMemcpy(&herr, f->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+  std::memset(cnt, 0, sizeof(cnt));
+  if (!e) e = cudaMemcpy(f->d_counts, cnt, sizeof(cnt), cudaMemcpyHostToDevice);
+  if (!e) e = cudaMemset(f->d_err, 0, sizeof(int));
+  cudaFree(d_rows);
+  if (e) return cuda_fail(e, "xg_form_create");
+  if (herr) {
+    set_last_error("xg_form_create: full pattern does not fit the scatter buffers");
+    return XG_ERR_CAPACITY;
+  }
   return XG_OK;
 }
 
@@ -1990,7 +2173,7 @@ int form_workspace(xg_form* f) {
     f->sc_maxu = maxu;
     f->sc_hs = 2 * maxu;
     f->sc_stage = nd * std::max(1, 192 / nd);
-    f->sc_wbytes = (row_smem_bytes(f->sc_hs, f->sc_maxu, f->sc_stage) + 15) & ~15;
+    f->sc_wbytes = (row_smem_bytes(f->sc_hs, f->sc_maxu, 0, 0) + 15) & ~15;
     f->sc_smem = (size_t)kRowWarps * f->sc_wbytes;
   }
   e = A((void**)&f->d_full_ptr, (size_t)(space->ndof + 1) * 8);
@@ -2004,9 +2187,7 @@ int form_workspace(xg_form* f) {
     static size_t raised = 48 * 1024;
     std::lock_guard<std::mutex> lock(mu);
     if (f->sc_smem > raised) {
-      if (cudaFuncSetAttribute(k_row_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->sc_smem) ||
-          cudaFuncSetAttribute(k_row_fill<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->sc_smem) ||
-          cudaFuncSetAttribute(k_row_fill<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->sc_smem)) {
+      if (cudaFuncSetAttribute(k_row_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->sc_smem)) {
         set_last_error("xg_form_create: scatter shared memory too large for this mesh");
         return XG_ERR_CAPACITY;
       }
@@ -2014,7 +2195,35 @@ int form_workspace(xg_form* f) {
     }
   }
   f->grid_sc = grid_for(k_row_count, kRowWarps * 32, f->sc_smem);
-  return XG_OK;
+  // per-step scatter kernels, each with its own shared layout: the marking pass
+  // holds the full row's columns and its flags (in the hash region, maxu
+  // bytes), the summing pass the accumulators and the staged values
+  f->mk_wbytes = (row_smem_bytes(std::max(32, f->sc_maxu / 4), f->sc_maxu, 0, 0) + 15) & ~15;
+  f->mk_smem = (size_t)kRowWarps * f->mk_wbytes;
+  f->sm_wbytes = (row_smem_bytes(0, 0, f->sc_maxu, f->sc_stage) + 15) & ~15;
+  f->sm_smem = (size_t)kRowWarps * f->sm_wbytes;
+  {
+    static std::mutex mu;
+    static size_t raised_mk = 48 * 1024, raised_sm = 48 * 1024;
+    std::lock_guard<std::mutex> lock(mu);
+    bool bad = false;
+    if (f->mk_smem > raised_mk) {
+      bad |= cudaFuncSetAttribute(k_row_mark, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->mk_smem) != 0;
+      raised_mk = f->mk_smem;
+    }
+    if (f->sm_smem > raised_sm) {
+      bad |= cudaFuncSetAttribute(k_row_sum<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->sm_smem) != 0;
+      bad |= cudaFuncSetAttribute(k_row_sum<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->sm_smem) != 0;
+      raised_sm = f->sm_smem;
+    }
+    if (bad) {
+      set_last_error("xg_form_create: scatter shared memory too large for this mesh");
+      return XG_ERR_CAPACITY;
+    }
+  }
+  f->grid_mk = grid_for(k_row_mark, kRowWarps * 32, f->mk_smem);
+  f->grid_sm = grid_for(k_row_sum<double>, kRowWarps * 32, f->sm_smem);
+  return full_pattern_build(f);
 }
 
 }  // namespace
