@@ -761,10 +761,59 @@ __device__ __forceinline__ void patch_map(const Geo<D>& from, const Geo<D>& to, 
   }
 }
 
+// Per active facet (thread per facet): the two element maps, the measures and
+// the patch coefficients, read by k_patch.
+template <int D>
+__global__ void k_patch_geo(int ne, int nv, const int32_t* __restrict__ elv, const double* __restrict__ xyz,
+                            int64_t nf, const int32_t* __restrict__ fel, FormDesc form,
+                            const int32_t* __restrict__ list, const int* __restrict__ counts,
+                            PaGeoS<D>* __restrict__ pgeo, int64_t cap_fa, int* err) {
+  const int count = counts[2];
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < count; idx += gridDim.x * blockDim.x) {
+    if (idx >= cap_fa) {
+      set_err(err, XG_ERR_CAPACITY);
+      continue;
+    }
+    PaGeoS<D> G;
+    G.facet = list[idx];
+    const int e1 = fel[G.facet], e2 = fel[nf + G.facet];
+    double xv[D + 1][3];
+#pragma unroll
+    for (int v = 0; v <= D; v++) {
+      const int vid = elv[(int64_t)v * ne + e1];
+      G.gv1[v] = vid;
+#pragma unroll
+      for (int c = 0; c < 3; c++) xv[v][c] = c < D ? xyz[(int64_t)c * nv + vid] : 0.0;
+    }
+    Geo<D> g1, g2;
+    make_geo<D>(xv, g1);
+#pragma unroll
+    for (int v = 0; v <= D; v++) {
+      const int vid = elv[(int64_t)v * ne + e2];
+      G.gv2[v] = vid;
+#pragma unroll
+      for (int c = 0; c < 3; c++) xv[v][c] = c < D ? xyz[(int64_t)c * nv + vid] : 0.0;
+    }
+    make_geo<D>(xv, g2);
+    patch_map<D>(g1, g2, G.A12, G.c12);
+    patch_map<D>(g2, g1, G.A21, G.c21);
+    G.det1 = fabs(g1.det);
+    G.det2 = fabs(g2.det);
+    double h = -1.0;
+    for (int pp = 0; pp < kMaxPatch; pp++) G.coef[pp] = 0.0;
+    for (int pp = 0; pp < form.npatch; pp++) {
+      const PatchDesc& P = form.p[pp];
+      const bool on = !P.defined_on || tbit(P.defined_on, G.facet);
+      if (P.hpow != 0 && h < 0) h = pow(G.det1, 1.0 / D);
+      G.coef[pp] = !on ? 0.0 : (P.hpow == 0 ? P.c : P.c * pow(h, (double)P.hpow));
+    }
+    pgeo[idx] = G;
+  }
+}
+
 template <int D, int K, typename T>
 __global__ void __launch_bounds__(PaCfg<D, K>::NT) k_patch(
-    int ne, int nv, const int32_t* __restrict__ elv, const double* __restrict__ xyz, int64_t nf,
-    const int32_t* __restrict__ fel, FormDesc form, const int32_t* __restrict__ list, const int* __restrict__ counts,
+    FormDesc form, const PaGeoS<D>* __restrict__ pgeo, const int* __restrict__ counts,
     T* __restrict__ famat, int64_t cap_fa, int* err) {
   using C = PaCfg<D, K>;
   constexpr int N = C::N, N2 = C::N2, E = C::E, FPB = C::FPB, CH = C::CH, NT = C::NT, NACC = C::NACC;
@@ -780,41 +829,9 @@ __global__ void __launch_bounds__(PaCfg<D, K>::NT) k_patch(
   for (int batch = blockIdx.x; batch * FPB < count; batch += gridDim.x) {
     __syncthreads();
     if (threadIdx.x < FPB) {
-      PaGeoS<D>& G = geo[threadIdx.x];
       const int idx = batch * FPB + threadIdx.x;
-      G.facet = idx < count ? list[idx] : -1;
-      if (G.facet >= 0) {
-        const int e1 = fel[G.facet], e2 = fel[nf + G.facet];
-        double xv[D + 1][3];
-#pragma unroll
-        for (int v = 0; v <= D; v++) {
-          const int vid = elv[(int64_t)v * ne + e1];
-          G.gv1[v] = vid;
-#pragma unroll
-          for (int c = 0; c < 3; c++) xv[v][c] = c < D ? xyz[(int64_t)c * nv + vid] : 0.0;
-        }
-        Geo<D> g1, g2;
-        make_geo<D>(xv, g1);
-#pragma unroll
-        for (int v = 0; v <= D; v++) {
-          const int vid = elv[(int64_t)v * ne + e2];
-          G.gv2[v] = vid;
-#pragma unroll
-          for (int c = 0; c < 3; c++) xv[v][c] = c < D ? xyz[(int64_t)c * nv + vid] : 0.0;
-        }
-        make_geo<D>(xv, g2);
-        patch_map<D>(g1, g2, G.A12, G.c12);
-        patch_map<D>(g2, g1, G.A21, G.c21);
-        G.det1 = fabs(g1.det);
-        G.det2 = fabs(g2.det);
-        double h = -1.0;
-        for (int pp = 0; pp < form.npatch; pp++) {
-          const PatchDesc& P = form.p[pp];
-          const bool on = !P.defined_on || tbit(P.defined_on, G.facet);
-          if (P.hpow != 0 && h < 0) h = pow(G.det1, 1.0 / D);
-          G.coef[pp] = !on ? 0.0 : (P.hpow == 0 ? P.c : P.c * pow(h, (double)P.hpow));
-        }
-      }
+      if (idx < count && idx < cap_fa) geo[threadIdx.x] = pgeo[idx];
+      else geo[threadIdx.x].facet = -1;
     }
     __syncthreads();
     const PaGeoS<D>& G = geo[lf];
@@ -1509,6 +1526,7 @@ struct xg_form {
   uint16_t* d_fpos_el = nullptr;  // [ne][nd][nd]: position of element column j in the full row of local row i
   uint16_t* d_pbuf = nullptr;     // [cap_fa][2][nd][nd]: neighbour-column positions of active facets (per step)
   uint8_t* d_flags = nullptr;     // [full_nnz]: active columns of each active row (per step)
+  void* d_pgeo = nullptr;         // [cap_fa] per-facet patch geometry (per step)
   int max_unique = 0;
   int grid_el_un = 0, grid_el_cut = 0, grid_fa = 0, grid_sc = 0;
   // CutFEM step state
@@ -1531,7 +1549,7 @@ namespace {
 int form_workspace(xg_form* f);
 
 int form_free(xg_form* f) {
-  void* ptrs[] = {f->d_full_ptr, f->d_tmp_cols, f->d_fpos_el, f->d_pbuf, f->d_flags, f->d_tabs, f->d_act_un, f->d_act_cut, f->d_act_fa, f->d_dof_bits, f->d_l_un, f->d_l_cut, f->d_l_fa,
+  void* ptrs[] = {f->d_full_ptr, f->d_tmp_cols, f->d_fpos_el, f->d_pbuf, f->d_flags, f->d_pgeo, f->d_tabs, f->d_act_un, f->d_act_cut, f->d_act_fa, f->d_dof_bits, f->d_l_un, f->d_l_cut, f->d_l_fa,
                   f->d_el_slot, f->d_fa_slot, f->d_dof_row, f->d_rowcnt, f->d_counts, f->d_bsum, f->d_bsum64,
                   f->d_elmat, f->d_famat, f->d_err, f->d_dom, f->d_ratio, f->d_bits, f->d_fbits};
   for (void* p : ptrs) cudaFree(p);
@@ -1796,8 +1814,10 @@ int launch_patch(xg_form* f, cudaStream_t s) {
   xg_mesh* m = f->mesh;
   auto kp = k_patch<D, K, T>;
   if (!f->grid_fa) f->grid_fa = grid_for(kp, C::NT, 0);
-  kp<<<f->grid_fa, C::NT, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, m->nfacets, m->d_facet_els, f->desc, f->d_l_fa,
-                                  f->d_counts, (T*)f->d_famat, f->cap_fa, f->d_err);
+  PaGeoS<D>* pg = (PaGeoS<D>*)f->d_pgeo;
+  k_patch_geo<D><<<152 * 8, 128, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, m->nfacets, m->d_facet_els, f->desc,
+                                         f->d_l_fa, f->d_counts, pg, f->cap_fa, f->d_err);
+  kp<<<f->grid_fa, C::NT, 0, s>>>(f->desc, pg, f->d_counts, (T*)f->d_famat, f->cap_fa, f->d_err);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? XG_OK : cuda_fail(e, "k_patch");
 }
@@ -2152,6 +2172,7 @@ int form_workspace(xg_form* f) {
   e = e ? e : A((void**)&f->d_bsum64, (size_t)f->nbsum64 * 8);
   e = e ? e : A(&f->d_elmat, (size_t)f->cap_el * nd * nd * esz);
   e = e ? e : A(&f->d_famat, f->has_patch ? (size_t)f->cap_fa * tri_size(2 * nds) * esz : 16);
+  e = e ? e : A(&f->d_pgeo, f->has_patch ? (size_t)f->cap_fa * sizeof(PaGeoS<3>) : 16);
   e = e ? e : A((void**)&f->d_err, sizeof(int));
   e = e ? e : A((void**)&f->d_dom, (size_t)m->ne);
   e = e ? e : A((void**)&f->d_ratio, (size_t)m->ne * 8);
