@@ -488,11 +488,91 @@ struct CutSubS {
   double vol[3][3];
 };
 
+// Per-element setup of a cut element: geometry, unit normal of the P1 level
+// set, coefficients, and the sub-simplices (and their volumes) of the domain
+// types the form integrates over.
+template <int D>
+__device__ void cut_setup(int e, int ne, int nv, const int32_t* __restrict__ elv, const double* __restrict__ xyz,
+                          const double* __restrict__ lset, const FormDesc& form, int needs_mask, CutGeoS& G,
+                          CutSubS& SS, int* err) {
+  G.ns[0] = G.ns[1] = G.ns[2] = 0;
+  double xv[D + 1][3];
+#pragma unroll
+  for (int v = 0; v <= D; v++) {
+    const int vid = elv[(int64_t)v * ne + e];
+    G.gv[v] = vid;
+    G.l[v] = lset[vid];
+#pragma unroll
+    for (int c = 0; c < 3; c++) xv[v][c] = c < D ? xyz[(int64_t)c * nv + vid] : 0.0;
+  }
+  Geo<D> g;
+  make_geo<D>(xv, g);
+  G.meas = fabs(g.det);
+  double gs[3] = {0, 0, 0};
+#pragma unroll
+  for (int a = 0; a < D; a++)
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      G.g[a][k] = k < D ? g.Finv[a][k] : 0.0;
+      gs[k] += G.g[a][k];
+    }
+#pragma unroll
+  for (int k = 0; k < 3; k++) G.g[D][k] = -gs[k];
+  double gl[3] = {0, 0, 0};
+#pragma unroll
+  for (int k = 0; k < D; k++) {
+    double s = 0;
+#pragma unroll
+    for (int a = 0; a < D; a++) s += g.Finv[a][k] * (G.l[a] - G.l[D]);
+    gl[k] = s;
+  }
+  const double nn = l2norm3(gl[0], gl[1], gl[2]);
+#pragma unroll
+  for (int k = 0; k < 3; k++) G.nrm[k] = gl[k] / nn;
+  double h = -1.0;
+  for (int q = 0; q < form.ngroups; q++)
+    for (int k = 0; k < 5; k++) {
+      const int hp = form.g[q].hpow[k];
+      if (hp != 0 && h < 0) h = pow(G.meas, 1.0 / D);
+      G.coef[q][k] = hp == 0 ? form.g[q].c[k] : form.g[q].c[k] * pow(h, (double)hp);
+    }
+  for (int dt = 0; dt < 3; dt++) {
+    if (!((needs_mask >> dt) & 1)) continue;
+    int ns = decompose<D>(G.l, dt, SS.sub[dt]);
+    if (ns < 0) {
+      set_err(err, -ns);
+      ns = 0;
+    }
+    G.ns[dt] = ns;
+    const int sd = dt == XG_IF ? D - 1 : D;
+    for (int s = 0; s < ns; s++) SS.vol[dt][s] = simplex_volume(SS.sub[dt][s].p, sd + 1);
+  }
+  G.iffac = ((needs_mask >> XG_IF) & 1) ? if_factor<D>(g, G.l) : 0.0;
+}
+
+// thread per cut element (the first cap of the list): cut_setup into global memory
+template <int D>
+__global__ void k_cut_geo(int ne, int nv, const int32_t* __restrict__ elv, const double* __restrict__ xyz,
+                          const double* __restrict__ lset, FormDesc form, const int32_t* __restrict__ list,
+                          const int* __restrict__ counts, CutGeoS* __restrict__ cg, CutSubS* __restrict__ cs,
+                          int64_t cap, int* err, int needs_mask) {
+  const int count = counts[1];
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < count && idx < cap; idx += gridDim.x * blockDim.x) {
+    CutGeoS G;
+    CutSubS SS;
+    G.elem = list[idx];
+    G.slot = counts[0] + idx;
+    cut_setup<D>(G.elem, ne, nv, elv, xyz, lset, form, needs_mask, G, SS, err);
+    cg[idx] = G;
+    cs[idx] = SS;
+  }
+}
+
 template <int D, int K, bool SYM, typename T>
 __global__ void __launch_bounds__(CutCfg<D, K, SYM, T>::NT) k_elmat_cut(
     int ne, int nv, const int32_t* __restrict__ elv, const double* __restrict__ xyz, const double* __restrict__ lset,
     FormDesc form, const int32_t* __restrict__ list, const int* __restrict__ counts, T* __restrict__ elmat, int* err,
-    int needs_mask) {
+    int needs_mask, const CutGeoS* __restrict__ cg, const CutSubS* __restrict__ cs, int64_t cap) {
   using C = CutCfg<D, K, SYM, T>;
   constexpr int N = C::N, E = C::E, EPB = C::EPB, CH = C::CH, NT = C::NT, NACC = C::NACC, NF = C::NF;
   __shared__ CutGeoS geo[EPB];
@@ -515,64 +595,14 @@ __global__ void __launch_bounds__(CutCfg<D, K, SYM, T>::NT) k_elmat_cut(
     if (threadIdx.x < EPB) {
       CutGeoS& G = geo[threadIdx.x];
       const int idx = batch * EPB + threadIdx.x;
-      G.elem = idx < count ? list[idx] : -1;
-      G.slot = slot_base + idx;
-      G.ns[0] = G.ns[1] = G.ns[2] = 0;
-      if (G.elem >= 0) {
-        const int e = G.elem;
-        double xv[D + 1][3];
-#pragma unroll
-        for (int v = 0; v <= D; v++) {
-          const int vid = elv[(int64_t)v * ne + e];
-          G.gv[v] = vid;
-          G.l[v] = lset[vid];
-#pragma unroll
-          for (int c = 0; c < 3; c++) xv[v][c] = c < D ? xyz[(int64_t)c * nv + vid] : 0.0;
-        }
-        Geo<D> g;
-        make_geo<D>(xv, g);
-        G.meas = fabs(g.det);
-        double gs[3] = {0, 0, 0};
-#pragma unroll
-        for (int a = 0; a < D; a++)
-#pragma unroll
-          for (int k = 0; k < 3; k++) {
-            G.g[a][k] = k < D ? g.Finv[a][k] : 0.0;
-            gs[k] += G.g[a][k];
-          }
-#pragma unroll
-        for (int k = 0; k < 3; k++) G.g[D][k] = -gs[k];
-        double gl[3] = {0, 0, 0};
-#pragma unroll
-        for (int k = 0; k < D; k++) {
-          double s = 0;
-#pragma unroll
-          for (int a = 0; a < D; a++) s += g.Finv[a][k] * (G.l[a] - G.l[D]);
-          gl[k] = s;
-        }
-        const double nn = l2norm3(gl[0], gl[1], gl[2]);
-#pragma unroll
-        for (int k = 0; k < 3; k++) G.nrm[k] = gl[k] / nn;
-        double h = -1.0;
-        for (int q = 0; q < form.ngroups; q++)
-          for (int k = 0; k < 5; k++) {
-            const int hp = form.g[q].hpow[k];
-            if (hp != 0 && h < 0) h = pow(G.meas, 1.0 / D);
-            G.coef[q][k] = hp == 0 ? form.g[q].c[k] : form.g[q].c[k] * pow(h, (double)hp);
-          }
-        CutSubS& SS = subs[threadIdx.x];
-        for (int dt = 0; dt < 3; dt++) {
-          if (!((needs_mask >> dt) & 1)) continue;
-          int ns = decompose<D>(G.l, dt, SS.sub[dt]);
-          if (ns < 0) {
-            set_err(err, -ns);
-            ns = 0;
-          }
-          G.ns[dt] = ns;
-          const int sd = dt == XG_IF ? D - 1 : D;
-          for (int s = 0; s < ns; s++) SS.vol[dt][s] = simplex_volume(SS.sub[dt][s].p, sd + 1);
-        }
-        G.iffac = ((needs_mask >> XG_IF) & 1) ? if_factor<D>(g, G.l) : 0.0;
+      if (idx < count && idx < cap) {
+        G = cg[idx];
+        subs[threadIdx.x] = cs[idx];
+      } else {
+        G.elem = idx < count ? list[idx] : -1;
+        G.slot = slot_base + idx;
+        G.ns[0] = G.ns[1] = G.ns[2] = 0;
+        if (G.elem >= 0) cut_setup<D>(G.elem, ne, nv, elv, xyz, lset, form, needs_mask, G, subs[threadIdx.x], err);
       }
     }
     __syncthreads();
@@ -1527,6 +1557,9 @@ struct xg_form {
   uint16_t* d_pbuf = nullptr;     // [cap_fa][2][nd][nd]: neighbour-column positions of active facets (per step)
   uint8_t* d_flags = nullptr;     // [full_nnz]: active columns of each active row (per step)
   void* d_pgeo = nullptr;         // [cap_fa] per-facet patch geometry (per step)
+  void* d_cgeo = nullptr;         // [cap_cgeo] per-cut-element geometry and sub-simplices (per step)
+  void* d_csub = nullptr;
+  int64_t cap_cgeo = 0;
   int max_unique = 0;
   int grid_el_un = 0, grid_el_cut = 0, grid_fa = 0, grid_sc = 0;
   // CutFEM step state
@@ -1549,7 +1582,8 @@ namespace {
 int form_workspace(xg_form* f);
 
 int form_free(xg_form* f) {
-  void* ptrs[] = {f->d_full_ptr, f->d_tmp_cols, f->d_fpos_el, f->d_pbuf, f->d_flags, f->d_pgeo, f->d_tabs, f->d_act_un, f->d_act_cut, f->d_act_fa, f->d_dof_bits, f->d_l_un, f->d_l_cut, f->d_l_fa,
+  void* ptrs[] = {f->d_full_ptr, f->d_tmp_cols, f->d_fpos_el, f->d_pbuf, f->d_flags, f->d_pgeo, f->d_cgeo, f->d_csub,
+                  f->d_tabs, f->d_act_un, f->d_act_cut, f->d_act_fa, f->d_dof_bits, f->d_l_un, f->d_l_cut, f->d_l_fa,
                   f->d_el_slot, f->d_fa_slot, f->d_dof_row, f->d_rowcnt, f->d_counts, f->d_bsum, f->d_bsum64,
                   f->d_elmat, f->d_famat, f->d_err, f->d_dom, f->d_ratio, f->d_bits, f->d_fbits};
   for (void* p : ptrs) cudaFree(p);
@@ -1795,8 +1829,12 @@ int launch_volume_sym(xg_form* f, const double* d_lset, const uint8_t* d_dom, cu
   ku<<<f->grid_el_un, 256, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, d_dom, f->desc, f->tabs, f->d_l_un, f->d_counts,
                                    (T*)f->d_elmat, f->d_err);
   if (f->use_ev) cudaEventRecord(f->ev[3], s);
+  k_cut_geo<D><<<152 * 4, 128, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, d_lset, f->desc, f->d_l_cut, f->d_counts,
+                                       (CutGeoS*)f->d_cgeo, (CutSubS*)f->d_csub, f->cap_cgeo, f->d_err,
+                                       f->needs_mask);
   kc<<<f->grid_el_cut, CC::NT, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, d_lset, f->desc, f->d_l_cut, f->d_counts,
-                                      (T*)f->d_elmat, f->d_err, f->needs_mask);
+                                      (T*)f->d_elmat, f->d_err, f->needs_mask, (const CutGeoS*)f->d_cgeo,
+                                      (const CutSubS*)f->d_csub, f->cap_cgeo);
   if (f->use_ev) cudaEventRecord(f->ev[4], s);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? XG_OK : cuda_fail(e, "k_elmat");
@@ -2173,6 +2211,10 @@ int form_workspace(xg_form* f) {
   e = e ? e : A(&f->d_elmat, (size_t)f->cap_el * nd * nd * esz);
   e = e ? e : A(&f->d_famat, f->has_patch ? (size_t)f->cap_fa * tri_size(2 * nds) * esz : 16);
   e = e ? e : A(&f->d_pgeo, f->has_patch ? (size_t)f->cap_fa * sizeof(PaGeoS<3>) : 16);
+  // cut elements beyond this capacity set themselves up inside the element kernel
+  f->cap_cgeo = std::min<int64_t>(m->ne, std::max<int64_t>(65536, m->ne / 8));
+  e = e ? e : A(&f->d_cgeo, (size_t)f->cap_cgeo * sizeof(CutGeoS));
+  e = e ? e : A(&f->d_csub, (size_t)f->cap_cgeo * sizeof(CutSubS));
   e = e ? e : A((void**)&f->d_err, sizeof(int));
   e = e ? e : A((void**)&f->d_dom, (size_t)m->ne);
   e = e ? e : A((void**)&f->d_ratio, (size_t)m->ne * 8);
