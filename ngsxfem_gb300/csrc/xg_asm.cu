@@ -964,11 +964,15 @@ __global__ void __launch_bounds__(PaCfg<D, K>::NT) k_patch(
 // Scatter: one warp per active row (the row of dof r).  The row's columns are
 // the dofs of the active elements containing r and, for every active facet of
 // an element containing r, the dofs of both elements of that facet patch.
-// Pass 1 counts the distinct columns (shared-memory hash); pass 2 rebuilds the
-// set, sorts it, stages (position, value) pairs with independent global loads
-// and adds them in the fixed order (adjacent elements ascending; per element
-// its own matrix row, then its facets in local order, first then second
-// element's columns) -- the sum order never depends on scheduling, no atomics.
+// At form creation the full pattern (every element and interior facet active)
+// is built once: sorted columns of every dof row (hash + sort, k_row_count)
+// and the position of every element column in its rows' full rows
+// (k_fpos_el).  Per step, pass 1 (k_row_mark) flags the active columns of each
+// active row over its full-row positions and counts them; pass 2 (k_row_sum)
+// stages (position, value) pairs and adds them in the fixed order (adjacent
+// elements ascending; per element its own matrix row, then its facets in local
+// order, first then second element's columns) -- the sum order never depends
+// on scheduling, no atomics -- and writes the flagged positions compressed.
 // ============================================================================
 struct ScatterArgs {
   int ne, nd, nfl;
