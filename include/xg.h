@@ -132,6 +132,26 @@ int xg_interpolate_p1_perturb(double* d_vals, int64_t n, double eps, void* strea
  * Replaces CutInformation::Update(cf, subdivlvl=0, time_order=-1, lh). */
 int xg_cutinfo_update(xg_mesh* mesh, const double* d_lset, uint8_t* d_dom, double* d_cut_ratio,
                       uint64_t* d_bits, void* stream);
+/* CutInformation::Update for the BND elements (xfem/cutinfo.cpp:83-131 with
+ * vb == BND): the mesh's boundary facets in facet order (xg_mesh_boundary),
+ * each an (dim-1)-simplex with its vertices in ascending order; outputs as
+ * xg_cutinfo_update over the nbnd BND elements. */
+int xg_cutinfo_update_bnd(xg_mesh* mesh, const double* d_lset, uint8_t* d_dom, double* d_cut_ratio,
+                          uint64_t* d_bits, void* stream);
+/* BND elements: their number and (h_facets, optional) their facet numbers. */
+int xg_mesh_boundary(const xg_mesh* mesh, int64_t* h_nbnd, int32_t* h_facets);
+/* CutInformation::Update, node part (xfem/cutinfo.cpp:134-224), from the VOL
+ * domain types and cut ratios of xg_cutinfo_update: cut-neighbouring bitsets of
+ * vertices, edges, faces (3D; NULL in 2D) and elements, and the domain type of
+ * every vertex, edge, face (3D) and cell (XG_NEG if the node belongs to a NEG
+ * element, else XG_POS; cells: cut ratio > 0.5). */
+int xg_cutinfo_nodes(xg_mesh* mesh, const uint8_t* d_dom, const double* d_cut_ratio, uint64_t* d_nb_vertices,
+                     uint64_t* d_nb_edges, uint64_t* d_nb_faces, uint64_t* d_nb_elements, uint8_t* d_dom_vertices,
+                     uint8_t* d_dom_edges, uint8_t* d_dom_faces, uint8_t* d_dom_cells, void* stream);
+/* GetElementsWithThresholdContribution (xfem/cutinfo.cpp:263-284): bit e set if
+ * ratio[e] >= threshold (dt = XG_NEG) or ratio[e] <= 1 - threshold (XG_POS). */
+int xg_elements_with_threshold(const double* d_cut_ratio, int64_t n, int dt, double threshold, uint64_t* d_out,
+                               void* stream);
 /* Device error word of the mesh (decomposition failures during marking or
  * rule export); synchronise the stream first. Resets the word. */
 int xg_mesh_check(xg_mesh* mesh);

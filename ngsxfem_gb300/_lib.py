@@ -33,6 +33,7 @@ EXPORTS = [
     "xg_step_graph_kernel_count", "xg_iso_moments_tet", "xg_mlp_param_count", "xg_learned_points",
     "xg_mlp_create", "xg_mlp_destroy", "xg_mlp_get_params", "xg_mlp_set_params", "xg_mlp_forward",
     "xg_mlp_loss_grad", "xg_mlp_adam_step", "xg_learned_moments_tet", "xg_learned_features",
+    "xg_cutinfo_update_bnd", "xg_mesh_boundary", "xg_cutinfo_nodes", "xg_elements_with_threshold",
 ]
 
 
@@ -139,6 +140,10 @@ def load():
         "xg_mlp_adam_step": (I, [P, P, ctypes.c_float, I64, P]),
         "xg_learned_moments_tet": (I, [P, P, I64, D, P, P, P]),
         "xg_learned_features": (I, [P, I64, P, P]),
+        "xg_cutinfo_update_bnd": (I, [P, P, P, P, P, P]),
+        "xg_mesh_boundary": (I, [P, P, P]),
+        "xg_cutinfo_nodes": (I, [P, P, P, P, P, P, P, P, P, P, P, P]),
+        "xg_elements_with_threshold": (I, [P, I64, I, D, P, P]),
         "xg_space_create_st": (I, [P, I, I, P]),
         "xg_space_info_st": (I, [P, P]),
         "xg_cutinfo_update_st": (I, [P, P, I, P, P, P, P]),

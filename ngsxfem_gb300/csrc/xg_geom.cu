@@ -92,6 +92,54 @@ __global__ void k_cutinfo(int ne, const int32_t* __restrict__ elv, const double*
   }
 }
 
+// ---- CutInformation::Update, node part (xfem/cutinfo.cpp:134-224) ----------------------
+// Nodes (vertices, edges, faces, the element) of IF elements -> cut-neighbouring
+// bits; nodes of NEG elements -> NEG (all others stay POS); cells: cut ratio > 0.5 -> NEG.
+__global__ void k_cut_nodes(int dim, int ne, const int32_t* __restrict__ elv, const int32_t* __restrict__ el_edges,
+                            const int32_t* __restrict__ el_faces, const uint8_t* __restrict__ dom,
+                            const double* __restrict__ ratio, unsigned long long* nb_v, unsigned long long* nb_e,
+                            unsigned long long* nb_f, unsigned long long* nb_el, uint8_t* dv, uint8_t* de, uint8_t* df,
+                            uint8_t* dc) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  const int t = dom[e], nvl = dim + 1, nle = dim == 2 ? 3 : 6;
+  if (t == XG_IF) {
+    for (int i = 0; i < nvl; i++) {
+      const int v = elv[(int64_t)i * ne + e];
+      atomicOr(&nb_v[v >> 6], 1ull << (v & 63));
+    }
+    for (int j = 0; j < nle; j++) {
+      const int k = el_edges[(int64_t)j * ne + e];
+      atomicOr(&nb_e[k >> 6], 1ull << (k & 63));
+    }
+    if (dim == 3)
+      for (int j = 0; j < 4; j++) {
+        const int k = el_faces[(int64_t)j * ne + e];
+        atomicOr(&nb_f[k >> 6], 1ull << (k & 63));
+      }
+    atomicOr(&nb_el[e >> 6], 1ull << (e & 63));
+  } else if (t == XG_NEG) {
+    for (int i = 0; i < nvl; i++) dv[elv[(int64_t)i * ne + e]] = XG_NEG;
+    for (int j = 0; j < nle; j++) de[el_edges[(int64_t)j * ne + e]] = XG_NEG;
+    if (dim == 3)
+      for (int j = 0; j < 4; j++) df[el_faces[(int64_t)j * ne + e]] = XG_NEG;
+  }
+  dc[e] = ratio[e] > 0.5 ? XG_NEG : XG_POS;
+}
+
+// ---- GetElementsWithThresholdContribution (xfem/cutinfo.cpp:263-284) -------------------
+__global__ void k_threshold(const double* __restrict__ ratio, int64_t n, int dt, double threshold, uint32_t* out,
+                            int64_t nw32) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  bool set = false;
+  if (e < n) {
+    const double thr = dt == XG_POS ? 1.0 - threshold : threshold;
+    set = dt == XG_NEG ? ratio[e] >= thr : ratio[e] <= thr;
+  }
+  const unsigned m = __ballot_sync(0xffffffffu, set);
+  if ((threadIdx.x & 31) == 0 && (e >> 5) < nw32) out[e >> 5] = m;
+}
+
 __device__ __forceinline__ bool tbit(const uint64_t* b, int64_t i) { return (b[i >> 6] >> (i & 63)) & 1ull; }
 
 // ---- GetFacetsWithNeighborTypes (xfem/cutinfo.cpp:476-538) ----------------------------
@@ -473,6 +521,55 @@ int xg_cutinfo_update(xg_mesh* m, const double* d_lset, uint8_t* d_dom, double* 
     k_cutinfo<3><<<nblk(nthreads, 256), 256, 0, s>>>(m->ne, m->d_elv, d_lset, d_dom, d_ratio, (uint32_t*)d_bits,
                                                      2 * nw64, m->d_err);
   return launch_check("k_cutinfo");
+}
+
+int xg_cutinfo_update_bnd(xg_mesh* m, const double* d_lset, uint8_t* d_dom, double* d_ratio, uint64_t* d_bits,
+                          void* stream) {
+  if (!m || !d_lset || !d_dom || !d_ratio || !d_bits) return XG_ERR_ARG;
+  if (m->nbnd == 0) return XG_OK;
+  const int64_t nw64 = (m->nbnd + 63) / 64;
+  cudaStream_t s = (cudaStream_t)stream;
+  // the (D-1)-simplices of the boundary with their vertices in ascending order
+  if (m->dim == 2)
+    k_cutinfo<1><<<nblk(nw64 * 64, 256), 256, 0, s>>>((int)m->nbnd, m->d_bnd_v, d_lset, d_dom, d_ratio,
+                                                      (uint32_t*)d_bits, 2 * nw64, m->d_err);
+  else
+    k_cutinfo<2><<<nblk(nw64 * 64, 256), 256, 0, s>>>((int)m->nbnd, m->d_bnd_v, d_lset, d_dom, d_ratio,
+                                                      (uint32_t*)d_bits, 2 * nw64, m->d_err);
+  return launch_check("k_cutinfo (BND)");
+}
+
+int xg_cutinfo_nodes(xg_mesh* m, const uint8_t* d_dom, const double* d_ratio, uint64_t* d_nb_v, uint64_t* d_nb_e,
+                     uint64_t* d_nb_f, uint64_t* d_nb_el, uint8_t* d_dom_v, uint8_t* d_dom_e, uint8_t* d_dom_f,
+                     uint8_t* d_dom_cell, void* stream) {
+  if (!m || !d_dom || !d_ratio || !d_nb_v || !d_nb_e || !d_nb_el || !d_dom_v || !d_dom_e || !d_dom_cell ||
+      (m->dim == 3 && (!d_nb_f || !d_dom_f)))
+    return XG_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  XG_CUDA(cudaMemsetAsync(d_nb_v, 0, sizeof(uint64_t) * ((m->nv + 63) / 64), s));
+  XG_CUDA(cudaMemsetAsync(d_nb_e, 0, sizeof(uint64_t) * ((m->nedges + 63) / 64), s));
+  XG_CUDA(cudaMemsetAsync(d_nb_el, 0, sizeof(uint64_t) * ((m->ne + 63) / 64), s));
+  XG_CUDA(cudaMemsetAsync(d_dom_v, XG_POS, (size_t)m->nv, s));
+  XG_CUDA(cudaMemsetAsync(d_dom_e, XG_POS, (size_t)m->nedges, s));
+  if (m->dim == 3) {
+    XG_CUDA(cudaMemsetAsync(d_nb_f, 0, sizeof(uint64_t) * ((m->nfaces + 63) / 64), s));
+    XG_CUDA(cudaMemsetAsync(d_dom_f, XG_POS, (size_t)m->nfaces, s));
+  }
+  k_cut_nodes<<<nblk(m->ne, 256), 256, 0, s>>>(m->dim, m->ne, m->d_elv, m->d_el_edges, m->d_el_faces, d_dom, d_ratio,
+                                               (unsigned long long*)d_nb_v, (unsigned long long*)d_nb_e,
+                                               (unsigned long long*)d_nb_f, (unsigned long long*)d_nb_el, d_dom_v,
+                                               d_dom_e, d_dom_f, d_dom_cell);
+  return launch_check("k_cut_nodes");
+}
+
+int xg_elements_with_threshold(const double* d_ratio, int64_t n, int dt, double threshold, uint64_t* d_out,
+                               void* stream) {
+  if (!d_ratio || !d_out || n < 0 || (dt != XG_NEG && dt != XG_POS)) return XG_ERR_ARG;
+  if (n == 0) return XG_OK;
+  const int64_t nw64 = (n + 63) / 64;
+  k_threshold<<<nblk(nw64 * 64, 256), 256, 0, (cudaStream_t)stream>>>(d_ratio, n, dt, threshold, (uint32_t*)d_out,
+                                                                      2 * nw64);
+  return launch_check("k_threshold");
 }
 
 int xg_mesh_check(xg_mesh* m) {

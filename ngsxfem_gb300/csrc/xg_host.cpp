@@ -331,6 +331,24 @@ int xg_mesh_create(int dim, int32_t nv, const double* h_coords, int32_t ne, cons
     for (size_t i = 0; i < m->h_elv.size(); i++) cnt[m->h_elv[i]]++;
     m->max_vertex_elems = *std::max_element(cnt.begin(), cnt.end());
   }
+  // BND elements: boundary facets in facet order, vertices in ascending order
+  std::vector<int32_t> bnd_v;
+  {
+    const int stride = dim == 2 ? 3 : 4;
+    for (int64_t f = 0; f < m->nfacets; f++)
+      if (m->h_facet_els[2 * (size_t)f + 1] < 0) m->h_bnd_facets.push_back((int32_t)f);
+    m->nbnd = (int64_t)m->h_bnd_facets.size();
+    bnd_v.resize((size_t)dim * m->nbnd);
+    for (int64_t b = 0; b < m->nbnd; b++) {
+      const int f = m->h_bnd_facets[b], e = m->h_facet_els[2 * (size_t)f];
+      int lf = 0;
+      while (elf[(size_t)e * stride + lf] != f) lf++;
+      int v[3];
+      for (int q = 0; q < dim; q++) v[q] = h_elv[(size_t)e * nvl + (dim == 2 ? TRI_EDGES[lf][q] : TET_FACES[lf][q])];
+      std::sort(v, v + dim);
+      for (int q = 0; q < dim; q++) bnd_v[(size_t)q * m->nbnd + b] = v[q];
+    }
+  }
   // upload (SoA)
   std::vector<double> xyz((size_t)dim * nv);
   for (int v = 0; v < nv; v++)
@@ -339,7 +357,8 @@ int xg_mesh_create(int dim, int32_t nv, const double* h_coords, int32_t ne, cons
   if ((st = upload(&m->d_xyz, xyz)) || (st = upload(&m->d_elv, to_soa(m->h_elv, ne, nvl))) ||
       (st = upload(&m->d_el_edges, to_soa(m->h_el_edges, ne, nel))) ||
       (dim == 3 && (st = upload(&m->d_el_faces, to_soa(m->h_el_faces, ne, 4)))) ||
-      (st = upload(&m->d_facet_els, to_soa(m->h_facet_els, (size_t)m->nfacets, 2)))) {
+      (st = upload(&m->d_facet_els, to_soa(m->h_facet_els, (size_t)m->nfacets, 2))) ||
+      (st = upload(&m->d_bnd_v, bnd_v))) {
     xg_mesh_destroy(m);
     return st;
   }
@@ -381,6 +400,7 @@ int xg_mesh_destroy(xg_mesh* m) {
   cudaFree(m->d_el_edges);
   cudaFree(m->d_el_faces);
   cudaFree(m->d_facet_els);
+  cudaFree(m->d_bnd_v);
   cudaFree(m->d_el_facets_aos);
   cudaFree(m->d_facet_els_aos);
   cudaFree(m->d_err);
@@ -392,6 +412,13 @@ int xg_mesh_destroy(xg_mesh* m) {
 int xg_mesh_info(const xg_mesh* m, int64_t* o) {
   if (!m || !o) return XG_ERR_ARG;
   o[0] = m->dim; o[1] = m->nv; o[2] = m->ne; o[3] = m->nedges; o[4] = m->nfaces; o[5] = m->nfacets;
+  return XG_OK;
+}
+
+int xg_mesh_boundary(const xg_mesh* m, int64_t* h_nbnd, int32_t* h_facets) {
+  if (!m || !h_nbnd) return XG_ERR_ARG;
+  *h_nbnd = m->nbnd;
+  if (h_facets) std::copy(m->h_bnd_facets.begin(), m->h_bnd_facets.end(), h_facets);
   return XG_OK;
 }
 

@@ -128,12 +128,15 @@ struct xg_mesh {
   int32_t* d_facet_els = nullptr;// [2][nfacets]
   int32_t* d_el_facets_aos = nullptr;  // [ne][dim+1] element-major
   int2* d_facet_els_aos = nullptr;     // [nfacets] (first, second element; -1 boundary)
+  int64_t nbnd = 0;                    // BND elements: the boundary facets in facet order
+  int32_t* d_bnd_v = nullptr;          // [dim][nbnd] their vertices, ascending
   int* d_err = nullptr;
   // host
   std::vector<int32_t> h_elv;       // ne*(dim+1)
   std::vector<int32_t> h_el_edges;  // ne*nel_edges
   std::vector<int32_t> h_el_faces;  // ne*4
   std::vector<int32_t> h_facet_els; // nfacets*2
+  std::vector<int32_t> h_bnd_facets; // nbnd
   // compaction scratch (sized for max(ne, nfacets))
   void* d_scratch = nullptr;
   size_t scratch_bytes = 0;

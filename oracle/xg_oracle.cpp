@@ -1016,6 +1016,102 @@ int orc_cutinfo(const orc_space* s, const double* lset_vertex, uint8_t* dom, dou
   return err.load();
 }
 
+// Boundary elements (NGSolve's BND elements): the boundary facets in facet order,
+// each with its vertices in ascending global order.
+int orc_boundary_elements(const orc_space* s, int32_t* facets, int32_t* verts) {
+  const int D = s->D;
+  int n = 0;
+  for (int64_t f = 0; f < s->nfacets; f++) {
+    if (s->facet_els[2 * f + 1] >= 0) continue;
+    if (facets) facets[n] = (int32_t)f;
+    if (verts) {
+      const int e = s->facet_els[2 * f];
+      int lf = 0;
+      while (s->el_facets[(size_t)e * (D + 1) + lf] != f) lf++;
+      int v[3];
+      for (int q = 0; q < D; q++)
+        v[q] = s->elv[(size_t)e * (D + 1) + (D == 2 ? TRI_EDGES[lf][q] : TET_FACES[lf][q])];
+      std::sort(v, v + D);
+      for (int q = 0; q < D; q++) verts[(size_t)n * D + q] = v[q];
+    }
+    n++;
+  }
+  return n;
+}
+
+// CutInformation::Update for BND elements (xfem/cutinfo.cpp:83-131, vb == BND):
+// order-0 cut rules of the (D-1)-simplex with its vertices in ascending order.
+int orc_cutinfo_bnd(const orc_space* s, const double* lset_vertex, uint8_t* dom, double* cut_ratio,
+                    uint64_t* bits) {
+  const int D = s->D, SD = D - 1;
+  const int nb = orc_boundary_elements(s, nullptr, nullptr);
+  std::vector<int32_t> verts((size_t)nb * D);
+  orc_boundary_elements(s, nullptr, verts.data());
+  const int64_t nw = (nb + 63) / 64;
+  std::memset(bits, 0, sizeof(uint64_t) * nw * 8);
+  double ref[12] = {0};
+  for (int i = 0; i < SD; i++) ref[i * SD + i] = 1.0;  // reference vertices e_i, then the origin
+  Geo g;
+  make_geo(SD, ref, g);
+  std::vector<double> pts, wts;
+  int err = 0;
+  for (int e = 0; e < nb; e++) {
+    double l[4];
+    for (int i = 0; i <= SD; i++) l[i] = lset_vertex[verts[(size_t)e * D + i]];
+    double part_vol[2] = {0.0, 0.0};
+    for (int np : {POS, NEG}) {
+      int n = straight_cut_rule(g, l, np, 0, pts, wts);
+      if (n < -1) err = n;
+      if (n > 0)
+        for (int q = 0; q < n; q++) part_vol[np] += wts[q];
+    }
+    cut_ratio[e] = part_vol[NEG] / (part_vol[NEG] + part_vol[POS]);
+    uint8_t t;
+    if (part_vol[NEG] > 0.0) t = (part_vol[POS] > 0.0) ? IF : NEG;
+    else t = POS;
+    dom[e] = t;
+    int cdt = t == NEG ? 1 : (t == POS ? 2 : 4);
+    for (int c = 0; c < 8; c++)
+      if ((c & cdt) || c == 7) bits[c * nw + (e >> 6)] |= (uint64_t)1 << (e & 63);
+  }
+  return err;
+}
+
+// CutInformation::Update, node part (xfem/cutinfo.cpp:134-224): nodes of IF
+// elements (vertices, edges, faces, elements) and the domain of every node:
+// NEG if it belongs to a NEG element, else POS; elements (cells) by cut ratio > 0.5.
+int orc_cutinfo_nodes(const orc_space* s, const uint8_t* dom, const double* cut_ratio, uint64_t* nb_v,
+                      uint64_t* nb_e, uint64_t* nb_f, uint64_t* nb_el, uint8_t* dv, uint8_t* de, uint8_t* df,
+                      uint8_t* dc) {
+  const int D = s->D, ne = s->ne;
+  const int nle = D == 2 ? 3 : 6;
+  auto setb = [](uint64_t* b, int64_t i) { b[i >> 6] |= (uint64_t)1 << (i & 63); };
+  std::memset(nb_v, 0, sizeof(uint64_t) * ((s->nv + 63) / 64));
+  std::memset(nb_e, 0, sizeof(uint64_t) * ((s->nedges + 63) / 64));
+  if (D == 3) std::memset(nb_f, 0, sizeof(uint64_t) * ((s->nfaces + 63) / 64));
+  std::memset(nb_el, 0, sizeof(uint64_t) * ((ne + 63) / 64));
+  for (int i = 0; i < s->nv; i++) dv[i] = POS;
+  for (int64_t i = 0; i < s->nedges; i++) de[i] = POS;
+  if (D == 3)
+    for (int64_t i = 0; i < s->nfaces; i++) df[i] = POS;
+  for (int e = 0; e < ne; e++) {
+    if (dom[e] == IF) {
+      for (int i = 0; i <= D; i++) setb(nb_v, s->elv[(size_t)e * (D + 1) + i]);
+      for (int j = 0; j < nle; j++) setb(nb_e, s->el_edges[(size_t)e * nle + j]);
+      if (D == 3)
+        for (int j = 0; j < 4; j++) setb(nb_f, s->el_faces[(size_t)e * 4 + j]);
+      setb(nb_el, e);
+    } else if (dom[e] == NEG) {
+      for (int i = 0; i <= D; i++) dv[s->elv[(size_t)e * (D + 1) + i]] = NEG;
+      for (int j = 0; j < nle; j++) de[s->el_edges[(size_t)e * nle + j]] = NEG;
+      if (D == 3)
+        for (int j = 0; j < 4; j++) df[s->el_faces[(size_t)e * 4 + j]] = NEG;
+    }
+    dc[e] = cut_ratio[e] > 0.5 ? NEG : POS;
+  }
+  return 0;
+}
+
 int orc_facets_with_neighbor_types(const orc_space* s, const uint64_t* a, const uint64_t* b, int bnd_a,
                                    int bnd_b, int use_and, uint64_t* out) {
   const int64_t nf = s->nfacets;

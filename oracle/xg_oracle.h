@@ -69,6 +69,16 @@ int orc_space_facet_els(const orc_space*, int32_t* out /* nfacets*2 */);
  * bits[8][nwords] element bitsets per COMBINED_DOMAIN_TYPE (64 elements per word). */
 int orc_cutinfo(const orc_space*, const double* lset_vertex, uint8_t* dom, double* cut_ratio,
                 uint64_t* bits, int nthreads);
+/* BND elements: the boundary facets in facet order, vertices ascending (nbnd x D);
+ * returns nbnd.  Either output may be NULL. */
+int orc_boundary_elements(const orc_space*, int32_t* facets, int32_t* verts);
+/* CutInfo.Update for BND elements: dom, cut_ratio, bits[8][nwords] over the BND elements. */
+int orc_cutinfo_bnd(const orc_space*, const double* lset_vertex, uint8_t* dom, double* cut_ratio, uint64_t* bits);
+/* CutInfo.Update node part: cut-neighbouring node bitsets (vertices, edges, faces
+ * (3D), elements) and node domain types (vertices, edges, faces (3D), cells). */
+int orc_cutinfo_nodes(const orc_space*, const uint8_t* dom, const double* cut_ratio, uint64_t* nb_v,
+                      uint64_t* nb_e, uint64_t* nb_f, uint64_t* nb_el, uint8_t* dv, uint8_t* de, uint8_t* df,
+                      uint8_t* dc);
 int orc_facets_with_neighbor_types(const orc_space*, const uint64_t* a, const uint64_t* b,
                                    int bnd_a, int bnd_b, int use_and, uint64_t* out);
 double orc_integrate(const orc_space*, const double* lset_vertex, int dt, int order,
