@@ -201,17 +201,32 @@ def _lset_vec(levelset):
 # marking
 # ----------------------------------------------------------------------------
 class CutInfo:
-    """CutInformation (xfem/cutinfo.cpp): element domain types, cut ratios and
-    the combined-domain bitsets of a P1 level set."""
+    """CutInformation (xfem/cutinfo.cpp:61-284): element domain types, cut ratios
+    and the combined-domain bitsets of a P1 level set on the VOL and BND
+    elements (BND elements: the boundary facets in facet order), the
+    cut-neighbouring nodes and the domain type of every node."""
 
     def __init__(self, mesh, levelset=None, subdivlvl=0, time_order=-1, heapsize=None):
         self.mesh = mesh
         self.dm = device_mesh(mesh)
         ne = mesh.ne
         dev = _dev()
+        nb = np.zeros(1, dtype=np.int64)
+        _lib.call("xg_mesh_boundary", self.dm.h, nb.ctypes.data_as(ctypes.c_void_p), None)
+        self.nbnd = int(nb[0])
         self.dom = torch.zeros(ne, dtype=torch.uint8, device=dev)
         self.cut_ratio = torch.zeros(ne, dtype=torch.float64, device=dev)
         self.bits = torch.zeros((8, (ne + 63) // 64), dtype=torch.int64, device=dev)
+        self.dom_bnd = torch.zeros(max(self.nbnd, 1), dtype=torch.uint8, device=dev)
+        self.cut_ratio_bnd = torch.zeros(max(self.nbnd, 1), dtype=torch.float64, device=dev)
+        self.bits_bnd = torch.zeros((8, (self.nbnd + 63) // 64 or 1), dtype=torch.int64, device=dev)
+        dm = self.dm
+        w = lambda n: torch.zeros(max((n + 63) // 64, 1), dtype=torch.int64, device=dev)  # noqa: E731
+        self.cut_nb_nodes = {"vertex": w(dm.nv), "edge": w(dm.nedges), "face": w(dm.nfaces), "element": w(ne)}
+        self.dom_of_node = {"vertex": torch.zeros(dm.nv, dtype=torch.uint8, device=dev),
+                            "edge": torch.zeros(dm.nedges, dtype=torch.uint8, device=dev),
+                            "face": torch.zeros(max(dm.nfaces, 1), dtype=torch.uint8, device=dev),
+                            "cell": torch.zeros(ne, dtype=torch.uint8, device=dev)}
         self.levelset = None
         if levelset is not None:
             self.Update(levelset, subdivlvl, time_order)
@@ -223,16 +238,48 @@ class CutInfo:
         lv = _lset_vec(levelset)
         _lib.call("xg_cutinfo_update", self.dm.h, _vp(lv), _vp(self.dom), _vp(self.cut_ratio), _vp(self.bits),
                   _stream())
+        if self.nbnd:
+            _lib.call("xg_cutinfo_update_bnd", self.dm.h, _vp(lv), _vp(self.dom_bnd), _vp(self.cut_ratio_bnd),
+                      _vp(self.bits_bnd), _stream())
+        nb, dn = self.cut_nb_nodes, self.dom_of_node
+        three = self.mesh.dim == 3
+        _lib.call("xg_cutinfo_nodes", self.dm.h, _vp(self.dom), _vp(self.cut_ratio), _vp(nb["vertex"]),
+                  _vp(nb["edge"]), _vp(nb["face"]) if three else None, _vp(nb["element"]), _vp(dn["vertex"]),
+                  _vp(dn["edge"]), _vp(dn["face"]) if three else None, _vp(dn["cell"]), _stream())
 
-    def GetElementsOfType(self, domain_type, VorB=VOL):
-        if VorB != VOL:
-            raise NotImplementedError("boundary elements are not part of the GPU path")
-        cdt = {NEG: CDOM_NEG, POS: CDOM_POS, IF: CDOM_IF}.get(domain_type, domain_type) \
+    @staticmethod
+    def _cdt(domain_type):
+        return {NEG: CDOM_NEG, POS: CDOM_POS, IF: CDOM_IF}.get(domain_type, domain_type) \
             if isinstance(domain_type, int) and domain_type < 3 else domain_type
+
+    def GetElementsOfType(self, domain_type=IF, VorB=VOL):
+        cdt = self._cdt(domain_type)
+        if VorB == BND:
+            return BitArray(self.nbnd, self.bits_bnd[cdt].clone())
         return BitArray(self.mesh.ne, self.bits[cdt].clone())
 
     def GetCutRatios(self, VorB=VOL):
-        return self.cut_ratio
+        return self.cut_ratio_bnd[: self.nbnd] if VorB == BND else self.cut_ratio
+
+    def GetElementsWithThresholdContribution(self, domain_type=NEG, threshold=1.0, VorB=VOL):
+        if domain_type not in (NEG, POS):
+            raise ValueError("Unknown/Invalid type for dt: Only POS, NEG are implemented a.t.m.")
+        ratio = self.GetCutRatios(VorB)
+        n = self.nbnd if VorB == BND else self.mesh.ne
+        out = BitArray(n)
+        _lib.call("xg_elements_with_threshold", _vp(ratio), n, domain_type, float(threshold), _vp(out.words),
+                  _stream())
+        return out
+
+    def GetCutNeighboringNodes(self, node_type="vertex"):
+        """Nodes of cut elements (cut_neighboring_node of CutInformation)."""
+        n = {"vertex": self.dm.nv, "edge": self.dm.nedges, "face": self.dm.nfaces, "element": self.mesh.ne}[node_type]
+        return BitArray(n, self.cut_nb_nodes[node_type].clone())
+
+    def GetDomainOfNodes(self, node_type="vertex"):
+        """Domain type (NEG/POS) of every node (dom_of_node of CutInformation)."""
+        n = {"vertex": self.dm.nv, "edge": self.dm.nedges, "face": self.dm.nfaces, "cell": self.mesh.ne}[node_type]
+        return self.dom_of_node[node_type][:n]
 
     def Mesh(self):
         return self.mesh

@@ -100,6 +100,9 @@ def lib():
         L.orc_iso_integrate_mesh.restype = ctypes.c_double
         L.orc_iso_integrate_mesh.argtypes = [ctypes.c_int, ctypes.c_int, P, ctypes.c_int, P, P, ctypes.c_int,
                                              ctypes.c_int, ctypes.c_double, ctypes.c_int, P]
+        L.orc_boundary_elements.argtypes = [P, P, P]
+        L.orc_cutinfo_bnd.argtypes = [P, P, P, P, P]
+        L.orc_cutinfo_nodes.argtypes = [P, P, P, P, P, P, P, P, P, P, P]
         L.orc_pipeline.restype = ctypes.c_int64
         L.orc_pipeline.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         _lib = L
@@ -301,6 +304,40 @@ class Space:
         if r:
             raise RuntimeError("oracle cutinfo error %d" % r)
         return dom, ratio, bits
+
+    def boundary_elements(self):
+        n = lib().orc_boundary_elements(self.h, None, None)
+        D = self.mesh.dim
+        facets = np.zeros(n, dtype=np.int32)
+        verts = np.zeros((n, D), dtype=np.int32)
+        lib().orc_boundary_elements(self.h, _p(facets), _p(verts))
+        return facets, verts
+
+    def cutinfo_bnd(self, lset):
+        n = lib().orc_boundary_elements(self.h, None, None)
+        dom = np.zeros(n, dtype=np.uint8)
+        ratio = np.zeros(n)
+        bits = np.zeros((8, (n + 63) // 64), dtype=np.uint64)
+        l = np.ascontiguousarray(lset, dtype=np.float64)
+        r = lib().orc_cutinfo_bnd(self.h, _p(l), _p(dom), _p(ratio), _p(bits))
+        if r:
+            raise RuntimeError("oracle cutinfo_bnd error %d" % r)
+        return dom, ratio, bits
+
+    def cutinfo_nodes(self, dom, ratio):
+        info = np.zeros(5, dtype=np.int64)
+        lib().orc_space_info(self.h, _p(info))
+        nv, ne, D = self.mesh.nv, self.mesh.ne, self.mesh.dim
+        nedges, nfaces = int(info[1]), int(info[2])
+        w = lambda n: np.zeros((n + 63) // 64, dtype=np.uint64)  # noqa: E731
+        nb_v, nb_e, nb_f, nb_el = w(nv), w(nedges), w(max(nfaces, 1)), w(ne)
+        dv, de = np.zeros(nv, np.uint8), np.zeros(nedges, np.uint8)
+        df, dc = np.zeros(max(nfaces, 1), np.uint8), np.zeros(ne, np.uint8)
+        d8 = np.ascontiguousarray(dom, dtype=np.uint8)
+        rr = np.ascontiguousarray(ratio, dtype=np.float64)
+        lib().orc_cutinfo_nodes(self.h, _p(d8), _p(rr), _p(nb_v), _p(nb_e), _p(nb_f), _p(nb_el), _p(dv), _p(de),
+                                _p(df), _p(dc))
+        return (nb_v, nb_e, nb_f[: (nfaces + 63) // 64], nb_el), (dv, de, df[:nfaces], dc)
 
     def facets_with_neighbor_types(self, a, b, bnd_a=False, bnd_b=False, use_and=True):
         out = np.zeros((self.nfacets + 63) // 64, dtype=np.uint64)
