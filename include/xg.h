@@ -247,6 +247,31 @@ int xg_form_check(xg_form* form);
  * n = 0 switches it off.  The events are the caller's. */
 int xg_form_stage_events(xg_form* form, void* const* events, int n);
 
+/* ---- linear forms (xfem/symboliccutlfi.cpp) --------------------------------- */
+typedef enum {
+  XG_LTERM_SOURCE = 0,    /* coef * x^e0 y^e1 z^e2 * v                         */
+  XG_LTERM_SOURCE_GF = 1  /* coef * u_h * v, u_h = d_gf (dof vector, same space) */
+} xg_lterm_kind;
+/* One SymbolicCutLFI(cf * v * dCut(lset, domain, order, definedonelements)). */
+typedef struct {
+  int32_t kind;               /* xg_lterm_kind */
+  int32_t domain;             /* XG_NEG / XG_POS / XG_IF */
+  int32_t order;              /* -1: 2k (symboliccutlfi.cpp:93-94) */
+  int32_t e[3];               /* exponents of XG_LTERM_SOURCE */
+  double coef;
+  const double* d_gf;         /* XG_LTERM_SOURCE_GF */
+  const uint64_t* d_defined_on; /* element bits; NULL = all */
+} xg_lterm;
+typedef struct xg_lform xg_lform;
+/* At most 8 terms on a spatial H1 space. */
+int xg_lform_create(xg_space* space, const xg_lterm* terms, int32_t nterms, xg_lform** out);
+int xg_lform_destroy(xg_lform* lform);
+/* LinearForm::Assemble: element vectors (SymbolicCutLinearFormIntegrator::
+ * T_CalcElementVector, symboliccutlfi.cpp:57-180) summed per dof in ascending
+ * element order into d_out[ndof]; d_dom from xg_cutinfo_update for d_lset. */
+int xg_lform_assemble(xg_lform* lform, const double* d_lset, const uint8_t* d_dom, double* d_out, void* stream);
+int xg_lform_check(xg_lform* lform);
+
 /* ---- space-time (cutint/spacetimecutrule.cpp, spacetime/) ------------------------ */
 /* Space-time level sets are P1 in space and P_kt in time on the reference slab
  * tau in [0,1] (nodal Gauss-Lobatto time basis: kt=1 nodes {0,1}, kt=2 nodes

@@ -34,6 +34,7 @@ EXPORTS = [
     "xg_mlp_create", "xg_mlp_destroy", "xg_mlp_get_params", "xg_mlp_set_params", "xg_mlp_forward",
     "xg_mlp_loss_grad", "xg_mlp_adam_step", "xg_learned_moments_tet", "xg_learned_features",
     "xg_cutinfo_update_bnd", "xg_mesh_boundary", "xg_cutinfo_nodes", "xg_elements_with_threshold",
+    "xg_lform_create", "xg_lform_destroy", "xg_lform_assemble", "xg_lform_check",
 ]
 
 
@@ -53,6 +54,12 @@ class Term(ctypes.Structure):
         ("b", ctypes.c_double * 3),
         ("d_defined_on", ctypes.c_void_p),
     ]
+
+
+class LTerm(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("domain", ctypes.c_int32), ("order", ctypes.c_int32),
+                ("e", ctypes.c_int32 * 3), ("coef", ctypes.c_double), ("d_gf", ctypes.c_void_p),
+                ("d_defined_on", ctypes.c_void_p)]
 
 
 class StTerm(ctypes.Structure):
@@ -144,6 +151,10 @@ def load():
         "xg_mesh_boundary": (I, [P, P, P]),
         "xg_cutinfo_nodes": (I, [P, P, P, P, P, P, P, P, P, P, P, P]),
         "xg_elements_with_threshold": (I, [P, I64, I, D, P, P]),
+        "xg_lform_create": (I, [P, P, ctypes.c_int32, P]),
+        "xg_lform_destroy": (I, [P]),
+        "xg_lform_assemble": (I, [P, P, P, P, P]),
+        "xg_lform_check": (I, [P]),
         "xg_space_create_st": (I, [P, I, I, P]),
         "xg_space_info_st": (I, [P, P]),
         "xg_cutinfo_update_st": (I, [P, P, I, P, P, P, P]),

@@ -27,6 +27,7 @@ UNITS = [
     ("xg_st.cu", []),
     ("xg_iso.cu", ["-fmad=false"]),
     ("xg_learn.cu", []),
+    ("xg_lf.cu", []),
 ]
 
 

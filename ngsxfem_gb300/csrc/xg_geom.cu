@@ -14,6 +14,7 @@ static __constant__ RuleTable c_rules;
 
 int upload_rules_asm();  // xg_asm.cu
 int upload_rules_st();   // xg_st.cu
+int upload_rules_lf();   // xg_lf.cu
 
 int ensure_device_rules() {
   static std::mutex mu;
@@ -25,6 +26,7 @@ int ensure_device_rules() {
   XG_CUDA(cudaMemcpyToSymbol(c_rules, &host_rules(), sizeof(RuleTable)));
   int st = upload_rules_asm();
   if (!st) st = upload_rules_st();
+  if (!st) st = upload_rules_lf();
   if (st) return st;
   done.push_back(dev);
   return XG_OK;

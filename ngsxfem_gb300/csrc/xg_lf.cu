@@ -1,0 +1,247 @@
+// Linear forms on cut domains: SymbolicCutLinearFormIntegrator
+// (xfem/symboliccutlfi.cpp:57-180) and the vector assembly of
+// LinearForm::Assemble.
+//
+// Per element (thread per element, FP64): for every term whose domain the
+// element carries (uncut and matching: the element's own rule; cut: the
+// straight cut rule of the term's domain, interface weights with |F^-T n|),
+//   elvec_i += w_q |det F| g(x_q) phi_i(x_q),
+// g = coef * x^e0 y^e1 z^e2 or coef * u_h (u_h a function of the same space);
+// the default order is 2k (symboliccutlfi.cpp:93-94).  Then thread per dof:
+// the sum over the dof's (element, local) adjacency in ascending element
+// order -- a fixed order, no atomics.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "xg_basis.cuh"
+#include "xg_cut.cuh"
+#include "xg_internal.h"
+
+namespace xg {
+
+static __constant__ RuleTable c_rules;
+
+int upload_rules_lf() {
+  XG_CUDA(cudaMemcpyToSymbol(c_rules, &host_rules(), sizeof(RuleTable)));
+  return XG_OK;
+}
+
+constexpr int kMaxLTerms = 8;
+
+struct LfDesc {
+  int n;
+  xg_lterm t[kMaxLTerms];
+};
+
+namespace {
+
+__device__ __forceinline__ bool tbit64(const uint64_t* b, int64_t i) { return (b[i >> 6] >> (i & 63)) & 1ull; }
+
+__device__ __forceinline__ double ipow(double x, int e) {
+  double r = 1.0;
+  for (int k = 0; k < e; k++) r *= x;
+  return r;
+}
+
+template <int D, int K>
+__global__ void __launch_bounds__(128) k_lf_elvec(int ne, int nv, const int32_t* __restrict__ elv,
+                                                   const double* __restrict__ xyz, const double* __restrict__ lset,
+                                                   const uint8_t* __restrict__ dom,
+                                                   const int32_t* __restrict__ el_dofs, LfDesc d,
+                                                   double* __restrict__ elvec, int* err) {
+  constexpr int N = ndof_el(D, K);
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += gridDim.x * blockDim.x) {
+    double b[N];
+#pragma unroll
+    for (int i = 0; i < N; i++) b[i] = 0.0;
+    const int de = dom[e];
+    double xv[D + 1][3], l[D + 1];
+    int gv[4];
+#pragma unroll
+    for (int v = 0; v <= D; v++) {
+      const int vid = elv[(int64_t)v * ne + e];
+      gv[v] = vid;
+      l[v] = lset[vid];
+#pragma unroll
+      for (int c = 0; c < 3; c++) xv[v][c] = c < D ? xyz[(int64_t)c * nv + vid] : 0.0;
+    }
+    Geo<D> g;
+    make_geo<D>(xv, g);
+    const double meas = fabs(g.det);
+    int desc[N];
+#pragma unroll
+    for (int i = 0; i < N; i++) desc[i] = fn_desc<D, K>(i, gv);
+    for (int t = 0; t < d.n; t++) {
+      const xg_lterm& T = d.t[t];
+      if (T.d_defined_on && !tbit64(T.d_defined_on, e)) continue;
+      const int dt = T.domain;
+      const int p = clamp_order(T.order >= 0 ? T.order : 2 * K);
+      Sub subs[3];
+      int ns = 0;
+      bool whole = false;
+      if (de == XG_IF) {
+        ns = decompose<D>(l, dt, subs);
+        if (ns < 0) {
+          set_err(err, -ns);
+          continue;
+        }
+      } else if (de == dt) {
+        whole = true;
+        ns = 1;
+      } else {
+        continue;
+      }
+      const int sd = (dt == XG_IF) ? D - 1 : D;
+      const int off = c_rules.off[sd][p], cnt = c_rules.cnt[sd][p];
+      const double fac = dt == XG_IF ? if_factor<D>(g, l) : 1.0;
+      for (int s = 0; s < ns; s++) {
+        const double vol = whole ? 1.0 : simplex_volume(subs[s].p, sd + 1);
+        for (int q = 0; q < cnt; q++) {
+          double pt[3];
+          if (whole) {
+#pragma unroll
+            for (int k = 0; k < 3; k++) pt[k] = c_rules.x[off + q][k];
+          } else {
+            plain_point(subs[s], sd + 1, c_rules.x[off + q], pt);
+          }
+          double lam[D + 1], sl = 0.0;
+#pragma unroll
+          for (int k = 0; k < D; k++) {
+            lam[k] = pt[k];
+            sl += pt[k];
+          }
+          lam[D] = 1.0 - sl;
+          double phi[N];
+#pragma unroll
+          for (int i = 0; i < N; i++) phi[i] = eval_fn_value<D, double>(desc[i], lam);
+          double gval;
+          if (T.kind == XG_LTERM_SOURCE) {
+            double x[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+            for (int i = 0; i < D; i++) {
+              double sacc = g.x0[i];
+#pragma unroll
+              for (int k = 0; k < D; k++) sacc += g.F[i][k] * pt[k];
+              x[i] = sacc;
+            }
+            gval = T.coef * ipow(x[0], T.e[0]) * ipow(x[1], T.e[1]) * (D == 3 ? ipow(x[2], T.e[2]) : 1.0);
+          } else {
+            double u = 0.0;
+#pragma unroll
+            for (int j = 0; j < N; j++) u += T.d_gf[el_dofs[(int64_t)e * N + j]] * phi[j];
+            gval = T.coef * u;
+          }
+          const double w = c_rules.w[off + q] * vol * fac * meas * gval;
+#pragma unroll
+          for (int i = 0; i < N; i++) b[i] += w * phi[i];
+        }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+      if (!isfinite(b[i])) set_err(err, XG_ERR_NONFINITE);
+      elvec[(int64_t)e * N + i] = b[i];
+    }
+  }
+}
+
+__global__ void k_lf_gather(int64_t ndof, int nd, const int32_t* __restrict__ adj_ptr, const int32_t* __restrict__ adj,
+                            const double* __restrict__ elvec, double* __restrict__ out) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < ndof; r += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int a = adj_ptr[r]; a < adj_ptr[r + 1]; a++) {
+      const int v = adj[a];
+      s += elvec[(int64_t)(v >> 5) * nd + (v & 31)];
+    }
+    out[r] = s;
+  }
+}
+
+}  // namespace
+}  // namespace xg
+
+using namespace xg;
+
+struct xg_lform {
+  xg_space* space = nullptr;
+  LfDesc desc;
+  double* d_elvec = nullptr;
+  int* d_err = nullptr;
+};
+
+extern "C" {
+
+int xg_lform_create(xg_space* space, const xg_lterm* terms, int32_t n, xg_lform** out) {
+  if (!space || !out || n < 0 || n > kMaxLTerms || (n > 0 && !terms) || space->kt >= 1) {
+    set_last_error("xg_lform_create: spatial H1 space and at most 8 terms");
+    return XG_ERR_ARG;
+  }
+  for (int t = 0; t < n; t++) {
+    const xg_lterm& T = terms[t];
+    if ((T.kind != XG_LTERM_SOURCE && T.kind != XG_LTERM_SOURCE_GF) || T.domain < 0 || T.domain > 2 ||
+        T.order > kMaxOrder || (T.kind == XG_LTERM_SOURCE_GF && !T.d_gf) || T.e[0] < 0 || T.e[1] < 0 || T.e[2] < 0) {
+      set_last_error("xg_lform_create: invalid term");
+      return XG_ERR_ARG;
+    }
+  }
+  *out = nullptr;
+  auto* f = new xg_lform();
+  f->space = space;
+  std::memset(&f->desc, 0, sizeof(f->desc));
+  f->desc.n = n;
+  for (int t = 0; t < n; t++) f->desc.t[t] = terms[t];
+  cudaError_t e = cudaMalloc((void**)&f->d_elvec, sizeof(double) * (size_t)space->mesh->ne * space->nd);
+  if (!e) e = cudaMalloc((void**)&f->d_err, sizeof(int));
+  if (!e) e = cudaMemset(f->d_err, 0, sizeof(int));
+  if (e) {
+    cudaFree(f->d_elvec);
+    cudaFree(f->d_err);
+    delete f;
+    return cuda_fail(e, "xg_lform_create");
+  }
+  *out = f;
+  return XG_OK;
+}
+
+int xg_lform_destroy(xg_lform* f) {
+  if (!f) return XG_OK;
+  cudaFree(f->d_elvec);
+  cudaFree(f->d_err);
+  delete f;
+  return XG_OK;
+}
+
+int xg_lform_check(xg_lform* f) {
+  if (!f) return XG_ERR_ARG;
+  int h = 0;
+  XG_CUDA(cudaMemcpy(&h, f->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  XG_CUDA(cudaMemset(f->d_err, 0, sizeof(int)));
+  if (h) set_last_error(std::string("device error: ") + xg_status_string(h));
+  return h;
+}
+
+int xg_lform_assemble(xg_lform* f, const double* d_lset, const uint8_t* d_dom, double* d_out, void* stream) {
+  if (!f || !d_lset || !d_dom || !d_out) return XG_ERR_ARG;
+  xg_space* sp = f->space;
+  xg_mesh* m = sp->mesh;
+  cudaStream_t s = (cudaStream_t)stream;
+  const unsigned grid = (unsigned)std::max(1, std::min((m->ne + 127) / 128, 152 * 16));
+  const int D = m->dim, K = sp->order;
+#define XG_LF(DD, KK)                                                                                            \
+  k_lf_elvec<DD, KK><<<grid, 128, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, d_lset, d_dom, sp->d_el_dofs_aos, \
+                                          f->desc, f->d_elvec, f->d_err)
+  if (D == 2 && K == 1) XG_LF(2, 1);
+  else if (D == 2 && K == 2) XG_LF(2, 2);
+  else if (D == 2 && K == 3) XG_LF(2, 3);
+  else if (D == 3 && K == 1) XG_LF(3, 1);
+  else if (D == 3 && K == 2) XG_LF(3, 2);
+  else XG_LF(3, 3);
+#undef XG_LF
+  const unsigned g2 = (unsigned)std::max<int64_t>(1, std::min<int64_t>((sp->ndof + 255) / 256, 152 * 16));
+  k_lf_gather<<<g2, 256, 0, s>>>(sp->ndof, sp->nd, sp->d_dof_adj_ptr, sp->d_dof_adj, f->d_elvec, d_out);
+  XG_CUDA(cudaGetLastError());
+  return XG_OK;
+}
+
+}  // extern "C"

@@ -31,6 +31,7 @@ VOL, BND = "VOL", "BND"
 
 TERM_MASS, TERM_LAPLACE, TERM_NGRADU_V, TERM_U_NGRADV, TERM_CONV, TERM_GHOST_MASS = range(6)
 PREC_FP64, PREC_MIXED = 0, 1
+XG_LTERM_SOURCE, XG_LTERM_SOURCE_GF = 0, 1
 
 
 def _vp(t):
@@ -171,6 +172,16 @@ class GridFunction:
     def __init__(self, space):
         self.space = space
         self.vec = torch.zeros(space.ndof, dtype=torch.float64, device=_dev())
+
+    def _atom(self):
+        return _Expr([_Mono(scal=(("gf", self),))])
+
+    def __mul__(self, o):
+        if isinstance(o, (_Expr, int, float)):
+            return self._atom() * o
+        return NotImplemented
+
+    __rmul__ = __mul__
 
 
 def InterpolateToP1(f, gf, eps_perturbation=1e-14):
@@ -334,6 +345,10 @@ class _Expr:
             return x
         if isinstance(x, (int, float)):
             return _Expr([_Mono(c=float(x))])
+        if isinstance(x, GridFunction):
+            return x._atom()
+        if isinstance(x, _Monomial):
+            return _Expr([_Mono(scal=(("xyz", x.e),))])
         if isinstance(x, (tuple, list)):
             return _Expr([_Mono(vec=("b", tuple(float(v) for v in x)))])
         raise TypeError("unsupported coefficient %r" % (x,))
@@ -649,6 +664,100 @@ class BilinearForm:
             self._form = None
 
 
+class LinearForm:
+    """LinearForm over one H1 space: `f += coef * v * dCut(...)` with coef a
+    number, a monomial of x, y, z or a GridFunction of the same space;
+    `f.Assemble()` -> `f.vec` (device tensor, global dof numbering)
+    (xfem/symboliccutlfi.cpp:57-180)."""
+
+    def __init__(self, space, **kwargs):
+        self.space = space
+        self.integrals = []
+        self.vec = torch.zeros(space.ndof, dtype=torch.float64, device=_dev())
+        self._lf = None
+
+    def __iadd__(self, integral):
+        if isinstance(integral, _Integral):
+            self.integrals.append(integral)
+        elif isinstance(integral, _SumOfIntegrals):
+            self.integrals.extend(integral.items)
+        else:
+            raise TypeError("add integrand * dCut(...)")
+        self._lf = None
+        return self
+
+    def _terms(self):
+        out = []
+        for it in self.integrals:
+            m = it.measure
+            if m.kind != "cut":
+                raise NotImplementedError("linear forms: dCut integrals only")
+            for mono in it.expr.monos:
+                if mono.dots or mono.vec is not None or mono.hpow != 0:
+                    raise NotImplementedError("linear form integrands: coef * (monomial | GridFunction) * v")
+                atoms = list(mono.scal)
+                if ("v", False) not in atoms or any(a[0] == "u" for a in atoms):
+                    raise NotImplementedError("linear form integrands need the test function v once")
+                atoms.remove(("v", False))
+                kind, e, gf = XG_LTERM_SOURCE, (0, 0, 0), None
+                for a in atoms:
+                    if a[0] == "xyz" and kind == XG_LTERM_SOURCE and e == (0, 0, 0):
+                        e = a[1]
+                    elif a[0] == "gf" and gf is None and e == (0, 0, 0):
+                        kind, gf = XG_LTERM_SOURCE_GF, a[1]
+                        if gf.space.ndof != self.space.ndof or gf.space.order != self.space.order:
+                            raise ValueError("the coefficient GridFunction must live in the form's space")
+                    else:
+                        raise NotImplementedError("one monomial or one GridFunction factor per term")
+                out.append(dict(kind=kind, domain=m.domain_type, order=-1 if m.order is None else m.order, e=e,
+                                coef=mono.c, gf=gf, defined_on=m.definedonelements))
+        return out
+
+    def _levelset(self):
+        ls = [i.measure.levelset for i in self.integrals]
+        for l in ls[1:]:
+            if l is not ls[0]:
+                raise NotImplementedError("all dCut integrals of one linear form must share the level set")
+        return ls[0] if ls else None
+
+    def _build(self):
+        terms = self._terms()
+        arr = (_lib.LTerm * len(terms))()
+        self._keep = []
+        for k, t in enumerate(terms):
+            arr[k].kind, arr[k].domain, arr[k].order, arr[k].coef = t["kind"], t["domain"], t["order"], t["coef"]
+            for j in range(3):
+                arr[k].e[j] = t["e"][j]
+            arr[k].d_gf = t["gf"].vec.data_ptr() if t["gf"] is not None else None
+            d = t["defined_on"]
+            if d is not None:
+                self._keep.append(d)
+            arr[k].d_defined_on = d.words.data_ptr() if d is not None else None
+            if t["gf"] is not None:
+                self._keep.append(t["gf"])
+        h = ctypes.c_void_p()
+        _lib.call("xg_lform_create", self.space.h, arr, len(terms), ctypes.byref(h))
+        self._lf = h
+
+    def Assemble(self, cutinfo=None):
+        if self._lf is None:
+            self._build()
+        lset = self._levelset()
+        if lset is None:
+            raise NotImplementedError("linear forms without dCut integrals are not part of the GPU path")
+        if cutinfo is None:
+            cutinfo = CutInfo(self.space.mesh, lset)
+        _lib.call("xg_lform_assemble", self._lf, _vp(_lset_vec(lset)), _vp(cutinfo.dom), _vp(self.vec), _stream())
+        torch.cuda.synchronize()
+        _lib.check(_lib.load().xg_lform_check(self._lf), "device (linear form)")
+        return self
+
+    def __del__(self):
+        if getattr(self, "_lf", None) and _lib._lib is not None:
+            _lib.load().xg_lform_destroy(self._lf)
+            self._lf = None
+
+
 # ----------------------------------------------------------------------------
 # Integrate
 # ----------------------------------------------------------------------------
@@ -661,7 +770,14 @@ class _Monomial:
             return _Monomial(tuple(a + b for a, b in zip(self.e, o.e)))
         if isinstance(o, _Measure):
             return ("integral", self, o)
+        if isinstance(o, (_Expr, int, float)):
+            return _Expr([_Mono(scal=(("xyz", self.e),))]) * o
         raise TypeError("monomial coefficient functions only")
+
+    def __rmul__(self, o):
+        if isinstance(o, (int, float)):
+            return _Expr([_Mono(c=float(o), scal=(("xyz", self.e),))])
+        return self.__mul__(o)
 
     def __pow__(self, p):
         return _Monomial(tuple(a * int(p) for a in self.e))

@@ -103,6 +103,7 @@ def lib():
         L.orc_boundary_elements.argtypes = [P, P, P]
         L.orc_cutinfo_bnd.argtypes = [P, P, P, P, P]
         L.orc_cutinfo_nodes.argtypes = [P, P, P, P, P, P, P, P, P, P, P]
+        L.orc_linear_form.argtypes = [P, P, P, ctypes.c_int, P]
         L.orc_pipeline.restype = ctypes.c_int64
         L.orc_pipeline.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         _lib = L
@@ -265,6 +266,11 @@ def moment_exponents():
     return [(a, b, t - a - b) for t in range(5) for a in range(t, -1, -1) for b in range(t - a, -1, -1)]
 
 
+class LTerm(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("domain", ctypes.c_int), ("order", ctypes.c_int), ("e", ctypes.c_int * 3),
+                ("coef", ctypes.c_double), ("gf", ctypes.c_void_p), ("defined_on", ctypes.c_void_p)]
+
+
 class Space:
     """H1 space of order k over a simplex mesh, with the oracle's topology."""
 
@@ -338,6 +344,35 @@ class Space:
         lib().orc_cutinfo_nodes(self.h, _p(d8), _p(rr), _p(nb_v), _p(nb_e), _p(nb_f), _p(nb_el), _p(dv), _p(de),
                                 _p(df), _p(dc))
         return (nb_v, nb_e, nb_f[: (nfaces + 63) // 64], nb_el), (dv, de, df[:nfaces], dc)
+
+    def linear_form(self, lset, terms):
+        """terms: dicts kind (0 monomial source, 1 same-space function), domain, coef,
+        e (exponents), gf (dof vector), order, defined_on (bits)."""
+        arr = (LTerm * len(terms))()
+        keep = []
+        for k, t in enumerate(terms):
+            arr[k].kind, arr[k].domain, arr[k].order = t["kind"], t.get("domain", 0), t.get("order", -1)
+            for j in range(3):
+                arr[k].e[j] = t.get("e", (0, 0, 0))[j]
+            arr[k].coef = t.get("coef", 1.0)
+            gf = t.get("gf")
+            if gf is not None:
+                gf = np.ascontiguousarray(gf, dtype=np.float64)
+                keep.append(gf)
+            arr[k].gf = gf.ctypes.data if gf is not None else None
+            d = t.get("defined_on")
+            if d is not None:
+                d = np.ascontiguousarray(d, dtype=np.uint64)
+                keep.append(d)
+            arr[k].defined_on = d.ctypes.data if d is not None else None
+        info = np.zeros(5, dtype=np.int64)
+        lib().orc_space_info(self.h, _p(info))
+        out = np.zeros(int(info[0]))
+        l = np.ascontiguousarray(lset, dtype=np.float64)
+        r = lib().orc_linear_form(self.h, _p(l), ctypes.cast(arr, ctypes.c_void_p), len(terms), _p(out))
+        if r:
+            raise RuntimeError("oracle linear form error %d" % r)
+        return out
 
     def facets_with_neighbor_types(self, a, b, bnd_a=False, bnd_b=False, use_and=True):
         out = np.zeros((self.nfacets + 63) // 64, dtype=np.uint64)

@@ -1629,6 +1629,57 @@ orc_csr* orc_assemble_st(const orc_space* s, const double* lset_st, int kt_l, in
 extern "C" {
 
 // Integrate(1 * dCut(lset_st, dt, order, time_order)) over the space-time slab
+// SymbolicCutLinearFormIntegrator::T_CalcElementVector (xfem/symboliccutlfi.cpp:57-180):
+// elvec_i = sum_q w_q |det F| g(x_q) phi_i(x_q) over the cut rule of the term's
+// domain (order 2k by default, :93-94), g = coef * x^e0 y^e1 z^e2 or coef * u_h
+// (u_h a function of the same space); then the vector assembly over the
+// elements in ascending order.
+int orc_linear_form(const orc_space* s, const double* lset_vertex, const orc_lterm* terms, int nterms, double* out) {
+  const int D = s->D, n = s->nd;
+  std::fill(out, out + s->ndof, 0.0);
+  std::vector<double> pts, wts;
+  for (int e = 0; e < s->ne; e++) {
+    Geo g;
+    double l[4];
+    element_geo(s, e, g, l, lset_vertex);
+    int gv[4];
+    for (int i = 0; i <= D; i++) gv[i] = s->elv[(size_t)e * (D + 1) + i];
+    const int32_t* dofs = &s->el_dofs[(size_t)e * n];
+    double b[20] = {0};
+    for (int t = 0; t < nterms; t++) {
+      const orc_lterm& T = terms[t];
+      if (T.defined_on && !test_bit(T.defined_on, e)) continue;
+      const int order = T.order >= 0 ? T.order : 2 * s->k;
+      const int np = straight_cut_rule(g, l, T.domain, order, pts, wts);
+      if (np < -1) return np;
+      if (np <= 0) continue;
+      const double meas = std::fabs(g.det);
+      for (int q = 0; q < np; q++) {
+        double phi[20], dphi[20][3];
+        basis(D, s->k, gv, &pts[3 * q], phi, dphi);
+        double gval;
+        if (T.kind == ORC_LTERM_SOURCE) {
+          double x[3] = {0, 0, 0};
+          for (int i = 0; i < D; i++) {
+            double sacc = g.x0[i];
+            for (int k = 0; k < D; k++) sacc += g.F[i][k] * pts[3 * q + k];
+            x[i] = sacc;
+          }
+          gval = T.coef * std::pow(x[0], T.e[0]) * std::pow(x[1], T.e[1]) * (D == 3 ? std::pow(x[2], T.e[2]) : 1.0);
+        } else {
+          double u = 0.0;
+          for (int j = 0; j < n; j++) u += T.gf[dofs[j]] * phi[j];
+          gval = T.coef * u;
+        }
+        const double w = wts[q] * meas * gval;
+        for (int i = 0; i < n; i++) b[i] += w * phi[i];
+      }
+    }
+    for (int i = 0; i < n; i++) out[dofs[i]] += b[i];
+  }
+  return 0;
+}
+
 double orc_integrate_st(const orc_space* s, const double* lset_st, int kt, int dt, int order_space, int order_time) {
   double sum = 0;
   std::vector<double> pts, wts;

@@ -150,6 +150,18 @@ int orc_iso_moments_tet(int64_t n, const double* vals10, int order, int deform, 
  * red refinements with the straight cut rule of the P1 interpolant on each leaf. */
 int orc_subdiv_moments_tet(const double* vals10, int levels, double* out35);
 
+/* --- linear forms ---------------------------------------------------------- */
+enum { ORC_LTERM_SOURCE = 0, /* coef * x^e0 y^e1 z^e2 * v */
+       ORC_LTERM_SOURCE_GF = 1 /* coef * u_h * v, u_h = gf (dof vector of the same space) */ };
+typedef struct {
+  int kind, domain, order;  /* order -1: 2k */
+  int e[3];
+  double coef;
+  const double* gf;
+  const uint64_t* defined_on;
+} orc_lterm;
+int orc_linear_form(const orc_space*, const double* lset_vertex, const orc_lterm* terms, int nterms, double* out);
+
 /* Whole CPU pipeline (CutInfo + facet marking + assembly) for timing: returns nnz. */
 int64_t orc_pipeline(const orc_space*, const double* lset_vertex, const orc_term* terms, int nterms,
                      int ghost_facets, int nthreads);
