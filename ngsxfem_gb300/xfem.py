@@ -29,7 +29,7 @@ CDOM_NO, CDOM_NEG, CDOM_POS, CDOM_UNCUT, CDOM_IF, CDOM_HASNEG, CDOM_HASPOS, CDOM
 UNCUT, HASNEG, HASPOS, ANY = CDOM_UNCUT, CDOM_HASNEG, CDOM_HASPOS, CDOM_ANY
 VOL, BND = "VOL", "BND"
 
-TERM_MASS, TERM_LAPLACE, TERM_NGRADU_V, TERM_U_NGRADV, TERM_CONV, TERM_GHOST_MASS = range(6)
+TERM_MASS, TERM_LAPLACE, TERM_NGRADU_V, TERM_U_NGRADV, TERM_CONV, TERM_GHOST_MASS, TERM_DT_U_V = range(7)
 PREC_FP64, PREC_MIXED = 0, 1
 XG_LTERM_SOURCE, XG_LTERM_SOURCE_GF = 0, 1
 
@@ -168,6 +168,95 @@ class H1:
             self.h = None
 
 
+class ScalarTimeFE:
+    """Nodal time finite element on [0, 1] with Gauss-Lobatto nodes
+    (spacetime/python_spacetime.cpp:156, SpaceTimeFE.cpp:263-281): order 1
+    nodes {0, 1}, order 2 nodes {0, 1/2, 1}."""
+
+    def __init__(self, order=0, skip_first_nodes=False, only_first_nodes=False, **kwargs):
+        if skip_first_nodes or only_first_nodes or kwargs.get("skip_first_node") or kwargs.get("only_first_node"):
+            raise NotImplementedError("restricted time elements are not part of the GPU path")
+        self.order = int(order)
+
+    def __mul__(self, fes):
+        return SpaceTimeFESpace(fes, self)
+
+    __rmul__ = __mul__
+
+
+class SpaceTimeFESpace:
+    """Tensor product of an H1 space (order 1..2) and a ScalarTimeFE (order
+    1..2); dof (time dof i, space dof j) -> i * ndof_space + j."""
+
+    def __init__(self, spacefes, timefe, dirichlet=None, **kwargs):
+        self.base, self.tfe = spacefes, timefe
+        self.mesh = spacefes.mesh
+        self.order, self.order_time = spacefes.order, timefe.order
+        self.dm = device_mesh(self.mesh)
+        h = ctypes.c_void_p()
+        _lib.call("xg_space_create_st", self.dm.h, self.order, self.order_time, ctypes.byref(h))
+        self.h = h
+        info = np.zeros(6, dtype=np.int64)
+        _lib.call("xg_space_info_st", self.h, info.ctypes.data_as(ctypes.c_void_p))
+        self.ndof, self.ndof_el, _, _, self.ndof_space, self.ndof_el_space = (int(v) for v in info)
+
+    def TrialFunction(self):
+        return _Expr.atom(("u", False))
+
+    def TestFunction(self):
+        return _Expr.atom(("v", False))
+
+    def TnT(self):
+        return self.TrialFunction(), self.TestFunction()
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib._lib is not None:
+            _lib.load().xg_space_destroy(self.h)
+            self.h = None
+
+
+def _time_nodes(k):
+    return [0.0] if k == 0 else ([0.0, 1.0] if k == 1 else [0.0, 0.5, 1.0])
+
+
+def SpaceTimeInterpolateToP1(spacetime_cf, time=None, spacetime_gf=None, t0=0.0, dt=1.0, eps_perturbation=1e-14):
+    """Nodal in time, P1 in space (spacetime/python_spacetime.cpp:438): the
+    callable spacetime_cf(x, y[, z], t) at the vertices and the time nodes
+    t = t0 + dt * tau_i of the GridFunction's space-time P1 space, with
+    InterpolateToP1's |v| < eps -> eps perturbation on the device."""
+    gf = spacetime_gf
+    V = gf.space
+    if not isinstance(V, SpaceTimeFESpace) or V.order != 1:
+        raise TypeError("spacetime_gf must be a GridFunction of a P1 x P_k space-time space")
+    mesh = V.mesh
+    coords = [mesh.coords[:, k] for k in range(mesh.dim)]
+    vals = np.concatenate([np.asarray(spacetime_cf(*coords, t0 + dt * tau), dtype=np.float64)
+                           for tau in _time_nodes(V.order_time)])
+    gf.vec.copy_(torch.from_numpy(np.ascontiguousarray(vals)))
+    _lib.call("xg_interpolate_p1_perturb", _vp(gf.vec), gf.vec.numel(), eps_perturbation, _stream())
+    return gf
+
+
+def dtref(func):
+    """Time derivative on the reference time interval (python/__init__.py:129)."""
+    if isinstance(func, _Expr) and len(func.monos) == 1 and func.monos[0].scal == (("u", False),):
+        return _Expr([_Mono(c=func.monos[0].c, scal=(("dtu", False),))])
+    raise TypeError("dtref() of the space-time trial function only")
+
+
+class TimeVector:
+    """Convection field b(t) = b + bc cos(omega t) + bs sin(omega t) with
+    t = t0 + dt * tau on the slab (the time-dependent CoefficientFunction of
+    the space-time demo, reduced to what the GPU kernels evaluate)."""
+
+    def __init__(self, b=(0.0, 0.0, 0.0), bc=(0.0, 0.0, 0.0), bs=(0.0, 0.0, 0.0), omega=0.0, t0=0.0, dt=1.0):
+        pad = lambda v: tuple(float(a) for a in v) + (0.0,) * (3 - len(v))  # noqa: E731
+        self.key = (pad(b), pad(bc), pad(bs), float(omega), float(t0), float(dt))
+
+    def _expr(self):
+        return _Expr([_Mono(vec=("tb", self.key))])
+
+
 class GridFunction:
     def __init__(self, space):
         self.space = space
@@ -200,6 +289,10 @@ def InterpolateToP1(f, gf, eps_perturbation=1e-14):
 
 def _lset_vec(levelset):
     if isinstance(levelset, GridFunction):
+        if isinstance(levelset.space, SpaceTimeFESpace):
+            if levelset.space.order != 1:
+                raise ValueError("space-time level sets are P1 in space")
+            return levelset.vec
         if levelset.space.order != 1:
             raise ValueError("the straight-cut path needs a P1 level set (CF2GFForStraightCutRule)")
         return levelset.vec
@@ -247,6 +340,12 @@ class CutInfo:
             raise NotImplementedError("CutInfo on the GPU supports P1 level sets (subdivlvl=0, time_order<=0)")
         self.levelset = levelset
         lv = _lset_vec(levelset)
+        if isinstance(levelset, GridFunction) and isinstance(levelset.space, SpaceTimeFESpace):
+            # space-time prisms (time_order = 0): CutInformation::Update with the
+            # space-time cut rule of orders 0/0
+            _lib.call("xg_cutinfo_update_st", self.dm.h, _vp(lv), levelset.space.order_time, _vp(self.dom),
+                      _vp(self.cut_ratio), _vp(self.bits), _stream())
+            return
         _lib.call("xg_cutinfo_update", self.dm.h, _vp(lv), _vp(self.dom), _vp(self.cut_ratio), _vp(self.bits),
                   _stream())
         if self.nbnd:
@@ -347,6 +446,8 @@ class _Expr:
             return _Expr([_Mono(c=float(x))])
         if isinstance(x, GridFunction):
             return x._atom()
+        if isinstance(x, TimeVector):
+            return x._expr()
         if isinstance(x, _Monomial):
             return _Expr([_Mono(scal=(("xyz", x.e),))])
         if isinstance(x, (tuple, list)):
@@ -410,6 +511,10 @@ def grad(x):
     raise TypeError("grad() of a trial/test function or a P1 level set GridFunction only")
 
 
+def InnerProduct(a, b):
+    return _Expr.wrap(a) * _Expr.wrap(b)
+
+
 class _LsetGrad:
     def __init__(self, gf):
         self.gf = gf
@@ -438,13 +543,26 @@ class _Measure:
     def __init__(self, kind, levelset=None, domain_type=None, order=None, definedonelements=None, **kw):
         self.kind, self.levelset, self.domain_type, self.order = kind, levelset, domain_type, order
         self.definedonelements = definedonelements
+        self.scale = 1.0
         for k in ("deformation", "skeleton", "element_boundary", "element_vb", "definedon"):
             if kw.get(k) is not None and kw.get(k) is not False:
                 raise NotImplementedError("dCut/dFacetPatch option %r is not part of the GPU path" % k)
-        if kw.get("time_order", -1) not in (-1, None) or kw.get("subdivlvl") not in (None, 0):
-            raise NotImplementedError("space-time / subdivision rules are not part of dCut on the GPU path")
+        if kw.get("subdivlvl") not in (None, 0):
+            raise NotImplementedError("subdivision rules are not part of dCut on the GPU path")
+        t = kw.get("time_order", -1)
+        self.time_order = -1 if t is None else int(t)
+        self.tref = kw.get("tref")
         if kw.get("downscale", 1.0) != 1.0:
             raise NotImplementedError("downscale != 1 is not supported")
+
+    def __rmul__(self, c):
+        """delta_t * dCut(...): a measure scaled by a number."""
+        if not isinstance(c, (int, float)):
+            return NotImplemented
+        out = _Measure.__new__(_Measure)
+        out.__dict__.update(self.__dict__)
+        out.scale = self.scale * float(c)
+        return out
 
 
 def dCut(levelset, domain_type, order=None, subdivlvl=None, time_order=-1, levelset_domain=None, **kwargs):
@@ -487,17 +605,15 @@ class _Integral:
                     raise NotImplementedError("facet patch integrand outside the ghost-penalty form")
                 acc.setdefault((key, mono.hpow), 0.0)
                 acc[(key, mono.hpow)] += mono.c
-            hps = {k[1] for k in acc}
-            if len(hps) != 1:
-                raise NotImplementedError("mixed mesh-size powers in a facet patch integrand")
-            hp = hps.pop()
-            vals = {k[0]: v for k, v in acc.items()}
-            c_uv = vals.get((("u", False), ("v", False)), 0.0)
-            for key, sgn in sign.items():
-                if abs(vals.get(key, 0.0) - sgn * c_uv) > 1e-14 * max(1.0, abs(c_uv)):
-                    raise NotImplementedError("facet patch integrand is not c*(u-u.Other())*(v-v.Other())")
-            out.append(dict(kind=TERM_GHOST_MASS, domain=NEG, order=-1 if m.order is None else m.order, hpow=hp,
-                            coef=c_uv, b=(0.0, 0.0, 0.0), defined_on=m.definedonelements))
+            # one ghost-penalty term per power of the mesh size
+            for hp in sorted({k[1] for k in acc}):
+                vals = {k[0]: v for k, v in acc.items() if k[1] == hp}
+                c_uv = vals.get((("u", False), ("v", False)), 0.0)
+                for key, sgn in sign.items():
+                    if abs(vals.get(key, 0.0) - sgn * c_uv) > 1e-14 * max(1.0, abs(c_uv)):
+                        raise NotImplementedError("facet patch integrand is not c*(u-u.Other())*(v-v.Other())")
+                out.append(dict(kind=TERM_GHOST_MASS, domain=NEG, order=-1 if m.order is None else m.order,
+                                hpow=hp, coef=c_uv * m.scale, b=(0.0, 0.0, 0.0), defined_on=m.definedonelements))
             return out
         dom = m.domain_type
         for mono in self.expr.monos:
@@ -513,8 +629,14 @@ class _Integral:
                 for v in d:
                     if v[0] == "n" and nrm_gf is not None and v[1] != id(nrm_gf):
                         raise NotImplementedError("the normal must be Normalize(grad(levelset)) of the cut's level set")
+            tb = None
             if names == ["u", "v"] and not dots:
                 kind = TERM_MASS
+            elif names == ["dtu", "v"] and not dots:
+                kind = TERM_DT_U_V
+            elif names == ["v"] and len(dots) == 1 and set(dots[0]) == {"gu", "tb"}:
+                kind = TERM_CONV
+                tb = [x for x in mono.dots[0] if x[0] == "tb"][0][1]
             elif not names and dots == [("gu", "gv")]:
                 kind = TERM_LAPLACE
             elif names == ["v"] and dots == [("gu", "n")]:
@@ -528,7 +650,8 @@ class _Integral:
             else:
                 raise NotImplementedError("integrand term outside the supported menu: %s" % (names + dots,))
             out.append(dict(kind=kind, domain=dom, order=-1 if m.order is None else m.order, hpow=mono.hpow,
-                            coef=mono.c, b=b, defined_on=m.definedonelements))
+                            coef=mono.c * m.scale, b=b, defined_on=m.definedonelements, tb=tb,
+                            tref=m.tref, time_order=m.time_order))
         return out
 
 
@@ -602,7 +725,48 @@ class BilinearForm:
                 raise NotImplementedError("all dCut integrals of one form must share the level set")
         return ls[0]
 
+    def _build_st(self):
+        """Space-time form (xg_st_form_create): slab terms (time_order of the
+        measure) and fixed-time terms (tref), ghost-penalty patch terms."""
+        lset = self._levelset()
+        terms = []
+        for it in self.integrals:
+            terms += it.terms(lset)
+        orders = {t["time_order"] for t in terms if t.get("tref") is None and t["kind"] != TERM_GHOST_MASS}
+        orders |= {it.measure.time_order for it in self.integrals if it.measure.kind == "patch"}
+        orders.discard(-1)
+        if len(orders) > 1:
+            raise NotImplementedError("one time rule order per space-time form")
+        order_time = orders.pop() if orders else 2 * self.space.order_time
+        arr = (_lib.StTerm * len(terms))()
+        for k, t in enumerate(terms):
+            B = arr[k].base
+            B.kind, B.domain, B.order, B.hpow, B.coef = t["kind"], t["domain"], t["order"], t["hpow"], t["coef"]
+            for j in range(3):
+                B.b[j] = t["b"][j]
+            B.d_defined_on = None  # the space-time step marks HASNEG / IF / HASPOS and the ghost facets itself
+            tb = t.get("tb")
+            if tb is not None:
+                for j in range(3):
+                    B.b[j] = tb[0][j]
+                    arr[k].bc[j] = tb[1][j]
+                    arr[k].bs[j] = tb[2][j]
+                arr[k].omega, arr[k].t0, arr[k].dt = tb[3], tb[4], tb[5]
+            else:
+                arr[k].omega, arr[k].t0, arr[k].dt = 0.0, 0.0, 1.0
+            arr[k].tref = -1.0 if t.get("tref") is None else float(t["tref"])
+        h = ctypes.c_void_p()
+        kt_l = lset.space.order_time if isinstance(lset.space, SpaceTimeFESpace) else 0
+        _lib.call("xg_st_form_create", self.space.h, kt_l, order_time, arr, len(terms), self.precision, ctypes.byref(h))
+        self._form = h
+        self._terms = terms
+        cap = np.zeros(2, dtype=np.int64)
+        _lib.call("xg_form_capacity", h, cap.ctypes.data_as(ctypes.c_void_p))
+        self._alloc(int(cap[0]), int(cap[1]))
+
     def _build(self):
+        if isinstance(self.space, SpaceTimeFESpace):
+            return self._build_st()
         lset = self._levelset()
         terms = []
         for it in self.integrals:
@@ -641,10 +805,18 @@ class BilinearForm:
         c.cap_rows, c.cap_nnz = cap_rows, cap_nnz
         self._csr = c
 
-    def Assemble(self, cutinfo=None):
+    def Assemble(self, cutinfo=None, reallocate=False):
         if self._form is None:
             self._build()
         lset = self._levelset()
+        if isinstance(self.space, SpaceTimeFESpace):
+            # the space-time CutFEM step: marking, ghost facets and assembly in one call
+            _lib.call("xg_st_cutfem_step", self._form, _vp(_lset_vec(lset)), ctypes.byref(self._csr), _stream())
+            torch.cuda.synchronize()
+            _lib.check(_lib.load().xg_form_check(self._form), "device (space-time form)")
+            nrows, nnz = (int(x) for x in self._counts.cpu().tolist())
+            self.mat = SparseMatrix(self.space.ndof, self._row_dof, self._rowptr, self._cols, self._vals, nrows, nnz)
+            return self
         if cutinfo is None:
             if lset is None:
                 # no cut integrals: every element counts as NEG for domain-free terms
