@@ -1319,27 +1319,50 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_row_mark(ScatterArgs A, int6
     const int a0 = A.adj_ptr[r], a1 = A.adj_ptr[r + 1];
     for (int c0 = a0; c0 < a1; c0 += kEnt) {
       const int na = min(kEnt, a1 - c0);
-      load_entries(A, S, c0, na);
-      // own element columns of entries with an active element or an active facet
-      LaneIdx L;
-      L.init(lane, nd);
-      for (int t = lane; t < na * nd; t += 32, L.next()) {
-        const int a = L.g, j = L.j;
-        const int ee = S.ent_e[a];
-        bool any = ee >= 0;
-        for (int lf = 0; lf < A.nfl; lf++) any |= S.ent_nb[a * 4 + lf] >= 0;
-        if (any) {
+      const int nc = load_entries(A, S, c0, na);
+      // S.celem lists, in entry order, each contributing entry's element then
+      // the neighbours across its active facets; the active facets themselves
+      // are listed in S.grp as (entry << 2) | local facet
+      int nfa = 0;
+      {
+        int cnt = 0;
+        if (lane < na)
+          for (int lf = 0; lf < A.nfl; lf++) cnt += S.ent_nb[lane * 4 + lf] >= 0;
+        int x = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(0xffffffffu, x, o);
+          if (lane >= o) x += y;
+        }
+        nfa = __shfl_sync(0xffffffffu, x, 31);
+        if (lane < na) {
+          int k = x - cnt;
+          for (int lf = 0; lf < A.nfl; lf++)
+            if (S.ent_nb[lane * 4 + lf] >= 0) S.grp[k++] = (lane << 2) | lf;
+        }
+        // the entries whose own element contributes columns (active element or facet)
+        const bool any = lane < na && (S.ent_e[lane] >= 0 || cnt > 0);
+        const unsigned am = __ballot_sync(0xffffffffu, any);
+        if (any) S.celem[__popc(am & ((1u << lane) - 1))] = lane;
+        __syncwarp();
+        const int nown = __popc(am);
+        // own element columns from the static positions
+        LaneIdx L;
+        L.init(lane, nd);
+        for (int t = lane; t < nown * nd; t += 32, L.next()) {
+          const int a = S.celem[L.g];
+          const int ee = S.ent_e[a];
           const int e = ee >= 0 ? ee : ~ee;
-          sflags[A.fpos_el[((int64_t)e * nd + S.ent_i[a]) * nd + j]] = 1;
+          sflags[A.fpos_el[((int64_t)e * nd + S.ent_i[a]) * nd + L.j]] = 1;
         }
       }
+      (void)nc;
       // neighbour columns of the active facets
+      LaneIdx L;
       L.init(lane, nd);
-      for (int t = lane; t < na * 4 * nd; t += 32, L.next()) {
-        const int a = L.g >> 2, lf = L.g & 3, j = L.j;
-        if (lf >= A.nfl) continue;
+      for (int t = lane; t < nfa * nd; t += 32, L.next()) {
+        const int ga = S.grp[L.g], a = ga >> 2, lf = ga & 3, j = L.j;
         const int nb = S.ent_nb[a * 4 + lf];
-        if (nb < 0) continue;
         const int pos = lower_bound_sm(S.ucols, len, A.el_dofs[(int64_t)nb * nd + j]);
         sflags[min(pos, len - 1)] = 1;
         const int fs = S.ent_fs[a * 4 + lf];
