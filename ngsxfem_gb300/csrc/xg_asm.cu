@@ -1388,7 +1388,7 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_row_mark(ScatterArgs A, int6
 // (adjacency order; per entry its element row, then its active facets) over
 // the row's full-pattern positions, then written compressed to the active
 // columns in ascending order.
-template <typename T>
+template <typename T, bool SYM, bool ST>
 __global__ void __launch_bounds__(kRowWarps * 32) k_row_sum(ScatterArgs A, const T* __restrict__ elmat,
                                                              const T* __restrict__ famat,
                                                              const int64_t* __restrict__ rowptr,
@@ -1462,8 +1462,8 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_row_sum(ScatterArgs A, const
             double v;
             if (kind == 0) {
               const int64_t eo = (int64_t)S.ent_slot[a];
-              v = A.el_sym ? (double)elmat[eo * tri_size(nd) + (i <= j ? tri_index(i, j, nd) : tri_index(j, i, nd))]
-                           : (double)elmat[(eo * nd + i) * nd + j];
+              v = SYM ? (double)elmat[eo * tri_size(nd) + (i <= j ? tri_index(i, j, nd) : tri_index(j, i, nd))]
+                      : (double)elmat[(eo * nd + i) * nd + j];
               pos = A.fpos_el[own];
             } else {
               // patch matrices are spatial: local space-time index = time dof * nds + spatial dof
@@ -1471,7 +1471,7 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_row_sum(ScatterArgs A, const
               const int first = S.ent_first[a * 4 + lf], fs = S.ent_fs[a * 4 + lf];
               const int nds = A.nds, n2s = 2 * nds;
               int ir = 0, jr = i, ic = 0, jc = j;
-              if (A.kt1 > 1) {
+              if (ST) {
                 ir = i / nds;
                 jr = i - ir * nds;
                 ic = j / nds;
@@ -1480,9 +1480,10 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_row_sum(ScatterArgs A, const
               const int prow = first ? jr : nds + jr, pcol = h * nds + jc;
               const bool self = (h == 0) == (first != 0);
               if (fs < A.cap_fa) {
-                v = A.mt[ir * A.kt1 + ic] *
-                    (double)famat[(int64_t)fs * tri_size(n2s) +
-                                  (prow <= pcol ? tri_index(prow, pcol, n2s) : tri_index(pcol, prow, n2s))];
+                const double pv = (double)famat[(int64_t)fs * tri_size(n2s) +
+                                                (prow <= pcol ? tri_index(prow, pcol, n2s)
+                                                              : tri_index(pcol, prow, n2s))];
+                v = ST ? A.mt[ir * A.kt1 + ic] * pv : pv;
                 pos = self ? (int)A.fpos_el[own]
                            : (int)A.pbuf[(((int64_t)fs * 2 + (first ? 0 : 1)) * nd + i) * nd + j];
               } else {
@@ -1982,14 +1983,21 @@ int scatter_phase(xg_form* f, xg_csr* out, cudaStream_t s) {
   A.accn = f->sc_maxu;
   A.stage = f->sc_stage;
   A.wbytes = f->sm_wbytes;
-  if (f->precision == XG_PREC_FP64)
-    k_row_sum<double><<<f->grid_sm, kRowWarps * 32, f->sm_smem, s>>>(A, (const double*)f->d_elmat,
-                                                                   (const double*)f->d_famat, out->d_rowptr,
-                                                                   out->d_cols, out->d_vals, out->cap_nnz, f->d_err);
-  else
-    k_row_sum<float><<<f->grid_sm, kRowWarps * 32, f->sm_smem, s>>>(A, (const float*)f->d_elmat,
-                                                                  (const float*)f->d_famat, out->d_rowptr,
-                                                                  out->d_cols, out->d_vals, out->cap_nnz, f->d_err);
+  const bool st_form = A.kt1 > 1;
+#define XG_ROW_SUM(TT, SY, STF)                                                                               \
+  k_row_sum<TT, SY, STF><<<f->grid_sm, kRowWarps * 32, f->sm_smem, s>>>(A, (const TT*)f->d_elmat,           \
+                                                                        (const TT*)f->d_famat, out->d_rowptr, \
+                                                                        out->d_cols, out->d_vals, out->cap_nnz, f->d_err)
+  if (f->precision == XG_PREC_FP64) {
+    if (st_form) XG_ROW_SUM(double, false, true);
+    else if (A.el_sym) XG_ROW_SUM(double, true, false);
+    else XG_ROW_SUM(double, false, false);
+  } else {
+    if (st_form) XG_ROW_SUM(float, false, true);
+    else if (A.el_sym) XG_ROW_SUM(float, true, false);
+    else XG_ROW_SUM(float, false, false);
+  }
+#undef XG_ROW_SUM
   if (f->use_ev) cudaEventRecord(f->ev[7], s);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? XG_OK : cuda_fail(e, "xg_form_assemble");
@@ -2302,8 +2310,14 @@ int form_workspace(xg_form* f) {
       raised_mk = f->mk_smem;
     }
     if (f->sm_smem > raised_sm) {
-      bad |= cudaFuncSetAttribute(k_row_sum<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->sm_smem) != 0;
-      bad |= cudaFuncSetAttribute(k_row_sum<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->sm_smem) != 0;
+      const int sm = (int)f->sm_smem;
+      const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
+      bad |= cudaFuncSetAttribute(k_row_sum<double, false, false>, at, sm) != 0;
+      bad |= cudaFuncSetAttribute(k_row_sum<double, true, false>, at, sm) != 0;
+      bad |= cudaFuncSetAttribute(k_row_sum<double, false, true>, at, sm) != 0;
+      bad |= cudaFuncSetAttribute(k_row_sum<float, false, false>, at, sm) != 0;
+      bad |= cudaFuncSetAttribute(k_row_sum<float, true, false>, at, sm) != 0;
+      bad |= cudaFuncSetAttribute(k_row_sum<float, false, true>, at, sm) != 0;
       raised_sm = f->sm_smem;
     }
     if (bad) {
@@ -2312,7 +2326,7 @@ int form_workspace(xg_form* f) {
     }
   }
   f->grid_mk = grid_for(k_row_mark, kRowWarps * 32, f->mk_smem);
-  f->grid_sm = grid_for(k_row_sum<double>, kRowWarps * 32, f->sm_smem);
+  f->grid_sm = grid_for(k_row_sum<double, false, false>, kRowWarps * 32, f->sm_smem);
   return full_pattern_build(f);
 }
 
