@@ -20,9 +20,23 @@
 namespace xg {
 
 static __constant__ RuleTable c_rules;
+// FP32 copy of the rule points and weights: the mixed kernels place their
+// quadrature points in FP32 (the FP64 pipe of GB300 is narrow)
+struct RuleTableF {
+  float x[kRuleCap][3];
+  float w[kRuleCap];
+};
+static __constant__ RuleTableF c_rules_f;
 
 int upload_rules_asm() {
   XG_CUDA(cudaMemcpyToSymbol(c_rules, &host_rules(), sizeof(RuleTable)));
+  static RuleTableF rf;
+  const RuleTable& R = host_rules();
+  for (int q = 0; q < kRuleCap; q++) {
+    for (int k = 0; k < 3; k++) rf.x[q][k] = (float)R.x[q][k];
+    rf.w[q] = (float)R.w[q];
+  }
+  XG_CUDA(cudaMemcpyToSymbol(c_rules_f, &rf, sizeof(RuleTableF)));
   return XG_OK;
 }
 
@@ -641,7 +655,42 @@ __global__ void __launch_bounds__(CutCfg<D, K, SYM, T>::NT) k_elmat_cut(
       const T cM = (T)G.coef[q][0], cL = (T)G.coef[q][1], cN1 = (T)G.coef[q][2], cN2 = (T)G.coef[q][3],
               cC = (T)G.coef[q][4];
       const int used = Gq.used;
+      T nrmT[3], bT[3];
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        nrmT[k] = (T)G.nrm[k];
+        bT[k] = (T)Gq.b[k];
+      }
       for (int q0 = 0; q0 < maxpts; q0 += CH) {
+        if constexpr (sizeof(T) == 4) {
+          for (int qq = i; qq < CH; qq += N) {
+            const int qi = q0 + qq;
+            float w = 0.f, pt[3] = {0.25f, 0.25f, 0.25f};
+            if (qi < np) {
+              const CutSubS& SS = subs[le];
+              const int sidx = qi / nqb, b = qi % nqb;
+              const Sub& sub = SS.sub[dt][sidx];
+              const float* ip = c_rules_f.x[offb + b];
+              float ow = 1.f;
+              for (int m = 0; m < sd; ++m) ow -= ip[m];
+#pragma unroll
+              for (int k = 0; k < 3; k++) pt[k] = ow * (float)sub.p[0].c[k];
+              for (int m = 0; m < sd; ++m)
+#pragma unroll
+                for (int k = 0; k < 3; k++) pt[k] += ip[m] * (float)sub.p[m + 1].c[k];
+              w = c_rules_f.w[offb + b] * (float)SS.vol[dt][sidx];
+              if (dt == XG_IF) w *= (float)G.iffac;
+            }
+            float s3 = 0.f;
+#pragma unroll
+            for (int a = 0; a < D; a++) {
+              pts[le][qq][a] = pt[a];
+              s3 += pt[a];
+            }
+            pts[le][qq][D] = 1.f - s3;
+            pts[le][qq][D + 1] = w * (float)G.meas;
+          }
+        } else
         for (int qq = i; qq < CH; qq += N) {
           const int qi = q0 + qq;
           double w = 0.0, pt[3] = {0.25, 0.25, 0.25};
@@ -674,11 +723,11 @@ __global__ void __launch_bounds__(CutCfg<D, K, SYM, T>::NT) k_elmat_cut(
           T dn = 0, db = 0;
           if (need_dn) {
 #pragma unroll
-            for (int k = 0; k < D; k++) dn += (T)G.nrm[k] * grad[k];
+            for (int k = 0; k < D; k++) dn += nrmT[k] * grad[k];
           }
           if (need_db) {
 #pragma unroll
-            for (int k = 0; k < D; k++) db += (T)Gq.b[k] * grad[k];
+            for (int k = 0; k < D; k++) db += bT[k] * grad[k];
           }
           const T w = pts[le][qq][D + 1];
           tr[le][qq][i][0] = phi;
@@ -767,6 +816,8 @@ struct PaGeoS {
   int gv1[4], gv2[4];
   int facet;
   double coef[kMaxPatch];
+  float A12f[D][D], c12f[D], A21f[D][D], c21f[D];  // FP32 copies for the mixed kernel
+  float det1f, det2f, coeff[kMaxPatch];
 };
 
 // Reference-coordinate map between the two elements of a patch.  For affine
@@ -837,6 +888,19 @@ __global__ void k_patch_geo(int ne, int nv, const int32_t* __restrict__ elv, con
       if (P.hpow != 0 && h < 0) h = pow(G.det1, 1.0 / D);
       G.coef[pp] = !on ? 0.0 : (P.hpow == 0 ? P.c : P.c * pow(h, (double)P.hpow));
     }
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+      G.c12f[i] = (float)G.c12[i];
+      G.c21f[i] = (float)G.c21[i];
+#pragma unroll
+      for (int k = 0; k < D; k++) {
+        G.A12f[i][k] = (float)G.A12[i][k];
+        G.A21f[i][k] = (float)G.A21[i][k];
+      }
+    }
+    G.det1f = (float)G.det1;
+    G.det2f = (float)G.det2;
+    for (int pp = 0; pp < kMaxPatch; pp++) G.coeff[pp] = (float)G.coef[pp];
     pgeo[idx] = G;
   }
 }
@@ -876,6 +940,39 @@ __global__ void __launch_bounds__(PaCfg<D, K>::NT) k_patch(
       const int p = clamp_order(P.order);
       const int nq = c_rules.cnt[D][p], off = c_rules.off[D][p];
       for (int q0 = 0; q0 < 2 * nq; q0 += CH) {
+        if constexpr (sizeof(T) == 4) {
+          for (int qq = a; qq < CH; qq += N2) {
+            const int qi = q0 + qq;
+            float x1[3] = {0.25f, 0.25f, 0.25f}, x2[3] = {0.25f, 0.25f, 0.25f}, W = 0.f;
+            if (qi < 2 * nq && G.facet >= 0) {
+              const bool one = qi < nq;
+              const int r = off + (one ? qi : qi - nq);
+              float* xa = one ? x1 : x2;
+              float* xb = one ? x2 : x1;
+#pragma unroll
+              for (int k = 0; k < D; k++) xa[k] = c_rules_f.x[r][k];
+#pragma unroll
+              for (int i2 = 0; i2 < D; i2++) {
+                float sacc = one ? G.c12f[i2] : G.c21f[i2];
+#pragma unroll
+                for (int k = 0; k < D; k++) sacc += (one ? G.A12f[i2][k] : G.A21f[i2][k]) * xa[k];
+                xb[i2] = sacc;
+              }
+              W = c_rules_f.w[r] * (one ? G.det1f : G.det2f);
+            }
+            float s1 = 0.f, s2 = 0.f;
+#pragma unroll
+            for (int k = 0; k < D; k++) {
+              pts[lf][qq][k] = x1[k];
+              pts[lf][qq][D + 1 + k] = x2[k];
+              s1 += x1[k];
+              s2 += x2[k];
+            }
+            pts[lf][qq][D] = 1.f - s1;
+            pts[lf][qq][2 * D + 1] = 1.f - s2;
+            pts[lf][qq][2 * D + 2] = W * G.coeff[pp];
+          }
+        } else
         for (int qq = a; qq < CH; qq += N2) {
           const int qi = q0 + qq;
           double x1[3] = {0.25, 0.25, 0.25}, x2[3] = {0.25, 0.25, 0.25}, W = 0.0;
