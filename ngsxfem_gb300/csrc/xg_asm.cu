@@ -808,17 +808,37 @@ struct PaCfg {
   static constexpr int NACC = (FPB * E + NT - 1) / NT;
 };
 
-template <int D>
+// per-facet patch geometry in the kernel's precision (computed in FP64)
+template <int D, typename T>
 struct PaGeoS {
-  double A12[D][D], c12[D];  // xi_2 = A12 xi_1 + c12 (element 1 -> element 2 reference coordinates)
-  double A21[D][D], c21[D];
-  double det1, det2;
+  T A12[D][D], c12[D];  // xi_2 = A12 xi_1 + c12 (element 1 -> element 2 reference coordinates)
+  T A21[D][D], c21[D];
+  T det1, det2;
   int gv1[4], gv2[4];
   int facet;
-  double coef[kMaxPatch];
-  float A12f[D][D], c12f[D], A21f[D][D], c21f[D];  // FP32 copies for the mixed kernel
-  float det1f, det2f, coeff[kMaxPatch];
+  T coef[kMaxPatch];
 };
+
+template <typename T>
+__device__ __forceinline__ T rule_x(int r, int k);
+template <>
+__device__ __forceinline__ double rule_x<double>(int r, int k) {
+  return c_rules.x[r][k];
+}
+template <>
+__device__ __forceinline__ float rule_x<float>(int r, int k) {
+  return c_rules_f.x[r][k];
+}
+template <typename T>
+__device__ __forceinline__ T rule_w(int r);
+template <>
+__device__ __forceinline__ double rule_w<double>(int r) {
+  return c_rules.w[r];
+}
+template <>
+__device__ __forceinline__ float rule_w<float>(int r) {
+  return c_rules_f.w[r];
+}
 
 // Reference-coordinate map between the two elements of a patch.  For affine
 // elements the low-order guess of MapPatchIntegrationPoint
@@ -844,18 +864,18 @@ __device__ __forceinline__ void patch_map(const Geo<D>& from, const Geo<D>& to, 
 
 // Per active facet (thread per facet): the two element maps, the measures and
 // the patch coefficients, read by k_patch.
-template <int D>
+template <int D, typename T>
 __global__ void k_patch_geo(int ne, int nv, const int32_t* __restrict__ elv, const double* __restrict__ xyz,
                             int64_t nf, const int32_t* __restrict__ fel, FormDesc form,
                             const int32_t* __restrict__ list, const int* __restrict__ counts,
-                            PaGeoS<D>* __restrict__ pgeo, int64_t cap_fa, int* err) {
+                            PaGeoS<D, T>* __restrict__ pgeo, int64_t cap_fa, int* err) {
   const int count = counts[2];
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < count; idx += gridDim.x * blockDim.x) {
     if (idx >= cap_fa) {
       set_err(err, XG_ERR_CAPACITY);
       continue;
     }
-    PaGeoS<D> G;
+    PaGeoS<D, double> G;
     G.facet = list[idx];
     const int e1 = fel[G.facet], e2 = fel[nf + G.facet];
     double xv[D + 1][3];
@@ -888,30 +908,36 @@ __global__ void k_patch_geo(int ne, int nv, const int32_t* __restrict__ elv, con
       if (P.hpow != 0 && h < 0) h = pow(G.det1, 1.0 / D);
       G.coef[pp] = !on ? 0.0 : (P.hpow == 0 ? P.c : P.c * pow(h, (double)P.hpow));
     }
+    PaGeoS<D, T> O;
 #pragma unroll
     for (int i = 0; i < D; i++) {
-      G.c12f[i] = (float)G.c12[i];
-      G.c21f[i] = (float)G.c21[i];
+      O.c12[i] = (T)G.c12[i];
+      O.c21[i] = (T)G.c21[i];
 #pragma unroll
       for (int k = 0; k < D; k++) {
-        G.A12f[i][k] = (float)G.A12[i][k];
-        G.A21f[i][k] = (float)G.A21[i][k];
+        O.A12[i][k] = (T)G.A12[i][k];
+        O.A21[i][k] = (T)G.A21[i][k];
       }
     }
-    G.det1f = (float)G.det1;
-    G.det2f = (float)G.det2;
-    for (int pp = 0; pp < kMaxPatch; pp++) G.coeff[pp] = (float)G.coef[pp];
-    pgeo[idx] = G;
+    O.det1 = (T)G.det1;
+    O.det2 = (T)G.det2;
+    for (int pp = 0; pp < kMaxPatch; pp++) O.coef[pp] = (T)G.coef[pp];
+    for (int v = 0; v < 4; v++) {
+      O.gv1[v] = G.gv1[v];
+      O.gv2[v] = G.gv2[v];
+    }
+    O.facet = G.facet;
+    pgeo[idx] = O;
   }
 }
 
 template <int D, int K, typename T>
 __global__ void __launch_bounds__(PaCfg<D, K>::NT) k_patch(
-    FormDesc form, const PaGeoS<D>* __restrict__ pgeo, const int* __restrict__ counts,
+    FormDesc form, const PaGeoS<D, T>* __restrict__ pgeo, const int* __restrict__ counts,
     T* __restrict__ famat, int64_t cap_fa, int* err) {
   using C = PaCfg<D, K>;
   constexpr int N = C::N, N2 = C::N2, E = C::E, FPB = C::FPB, CH = C::CH, NT = C::NT, NACC = C::NACC;
-  __shared__ PaGeoS<D> geo[FPB];
+  __shared__ PaGeoS<D, T> geo[FPB];
   __shared__ T pts[FPB][CH][2 * D + 3];  // barycentrics in element 1 and 2, weight
   __shared__ T S[FPB][CH][N2];   // s_a = phi1_a / -phi2_(a-N)
   __shared__ T SW[FPB][CH][N2];  // weighted
@@ -928,7 +954,7 @@ __global__ void __launch_bounds__(PaCfg<D, K>::NT) k_patch(
       else geo[threadIdx.x].facet = -1;
     }
     __syncthreads();
-    const PaGeoS<D>& G = geo[lf];
+    const PaGeoS<D, T>& G = geo[lf];
     const bool mine1 = a < N;
     const int desc = G.facet >= 0 ? fn_desc<D, K>(mine1 ? a : a - N, mine1 ? G.gv1 : G.gv2) : 0;
     Acc<T> acc[NACC];
@@ -940,79 +966,36 @@ __global__ void __launch_bounds__(PaCfg<D, K>::NT) k_patch(
       const int p = clamp_order(P.order);
       const int nq = c_rules.cnt[D][p], off = c_rules.off[D][p];
       for (int q0 = 0; q0 < 2 * nq; q0 += CH) {
-        if constexpr (sizeof(T) == 4) {
-          for (int qq = a; qq < CH; qq += N2) {
-            const int qi = q0 + qq;
-            float x1[3] = {0.25f, 0.25f, 0.25f}, x2[3] = {0.25f, 0.25f, 0.25f}, W = 0.f;
-            if (qi < 2 * nq && G.facet >= 0) {
-              const bool one = qi < nq;
-              const int r = off + (one ? qi : qi - nq);
-              float* xa = one ? x1 : x2;
-              float* xb = one ? x2 : x1;
-#pragma unroll
-              for (int k = 0; k < D; k++) xa[k] = c_rules_f.x[r][k];
-#pragma unroll
-              for (int i2 = 0; i2 < D; i2++) {
-                float sacc = one ? G.c12f[i2] : G.c21f[i2];
-#pragma unroll
-                for (int k = 0; k < D; k++) sacc += (one ? G.A12f[i2][k] : G.A21f[i2][k]) * xa[k];
-                xb[i2] = sacc;
-              }
-              W = c_rules_f.w[r] * (one ? G.det1f : G.det2f);
-            }
-            float s1 = 0.f, s2 = 0.f;
-#pragma unroll
-            for (int k = 0; k < D; k++) {
-              pts[lf][qq][k] = x1[k];
-              pts[lf][qq][D + 1 + k] = x2[k];
-              s1 += x1[k];
-              s2 += x2[k];
-            }
-            pts[lf][qq][D] = 1.f - s1;
-            pts[lf][qq][2 * D + 1] = 1.f - s2;
-            pts[lf][qq][2 * D + 2] = W * G.coeff[pp];
-          }
-        } else
         for (int qq = a; qq < CH; qq += N2) {
           const int qi = q0 + qq;
-          double x1[3] = {0.25, 0.25, 0.25}, x2[3] = {0.25, 0.25, 0.25}, W = 0.0;
+          T x1[3] = {(T)0.25, (T)0.25, (T)0.25}, x2[3] = {(T)0.25, (T)0.25, (T)0.25}, W = 0;
           if (qi < 2 * nq && G.facet >= 0) {
-            if (qi < nq) {
+            const bool one = qi < nq;
+            const int r = off + (one ? qi : qi - nq);
+            T* xa = one ? x1 : x2;
+            T* xb = one ? x2 : x1;
 #pragma unroll
-              for (int k = 0; k < D; k++) x1[k] = c_rules.x[off + qi][k];
+            for (int k = 0; k < D; k++) xa[k] = rule_x<T>(r, k);
 #pragma unroll
-              for (int i2 = 0; i2 < D; i2++) {
-                double sacc = G.c12[i2];
+            for (int i2 = 0; i2 < D; i2++) {
+              T sacc = one ? G.c12[i2] : G.c21[i2];
 #pragma unroll
-                for (int k = 0; k < D; k++) sacc += G.A12[i2][k] * x1[k];
-                x2[i2] = sacc;
-              }
-              W = c_rules.w[off + qi] * G.det1;
-            } else {
-              const int m = qi - nq;
-#pragma unroll
-              for (int k = 0; k < D; k++) x2[k] = c_rules.x[off + m][k];
-#pragma unroll
-              for (int i1 = 0; i1 < D; i1++) {
-                double sacc = G.c21[i1];
-#pragma unroll
-                for (int k = 0; k < D; k++) sacc += G.A21[i1][k] * x2[k];
-                x1[i1] = sacc;
-              }
-              W = c_rules.w[off + m] * G.det2;
+              for (int k = 0; k < D; k++) sacc += (one ? G.A12[i2][k] : G.A21[i2][k]) * xa[k];
+              xb[i2] = sacc;
             }
+            W = rule_w<T>(r) * (one ? G.det1 : G.det2);
           }
-          double s1 = 0, s2 = 0;
+          T s1 = 0, s2 = 0;
 #pragma unroll
           for (int k = 0; k < D; k++) {
-            pts[lf][qq][k] = (T)x1[k];
-            pts[lf][qq][D + 1 + k] = (T)x2[k];
+            pts[lf][qq][k] = x1[k];
+            pts[lf][qq][D + 1 + k] = x2[k];
             s1 += x1[k];
             s2 += x2[k];
           }
-          pts[lf][qq][D] = (T)(1.0 - s1);
-          pts[lf][qq][2 * D + 1] = (T)(1.0 - s2);
-          pts[lf][qq][2 * D + 2] = (T)(W * G.coef[pp]);
+          pts[lf][qq][D] = (T)1 - s1;
+          pts[lf][qq][2 * D + 1] = (T)1 - s2;
+          pts[lf][qq][2 * D + 2] = W * G.coef[pp];
         }
         __syncthreads();
 #pragma unroll
@@ -1977,8 +1960,8 @@ int launch_patch(xg_form* f, cudaStream_t s) {
   xg_mesh* m = f->mesh;
   auto kp = k_patch<D, K, T>;
   if (!f->grid_fa) f->grid_fa = grid_for(kp, C::NT, 0);
-  PaGeoS<D>* pg = (PaGeoS<D>*)f->d_pgeo;
-  k_patch_geo<D><<<152 * 8, 128, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, m->nfacets, m->d_facet_els, f->desc,
+  PaGeoS<D, T>* pg = (PaGeoS<D, T>*)f->d_pgeo;
+  k_patch_geo<D, T><<<152 * 8, 128, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, m->nfacets, m->d_facet_els, f->desc,
                                          f->d_l_fa, f->d_counts, pg, f->cap_fa, f->d_err);
   kp<<<f->grid_fa, C::NT, 0, s>>>(f->desc, pg, f->d_counts, (T*)f->d_famat, f->cap_fa, f->d_err);
   cudaError_t e = cudaGetLastError();
@@ -2342,7 +2325,7 @@ int form_workspace(xg_form* f) {
   e = e ? e : A((void**)&f->d_bsum64, (size_t)f->nbsum64 * 8);
   e = e ? e : A(&f->d_elmat, (size_t)f->cap_el * nd * nd * esz);
   e = e ? e : A(&f->d_famat, f->has_patch ? (size_t)f->cap_fa * tri_size(2 * nds) * esz : 16);
-  e = e ? e : A(&f->d_pgeo, f->has_patch ? (size_t)f->cap_fa * sizeof(PaGeoS<3>) : 16);
+  e = e ? e : A(&f->d_pgeo, f->has_patch ? (size_t)f->cap_fa * sizeof(PaGeoS<3, double>) : 16);
   // cut elements beyond this capacity set themselves up inside the element kernel
   f->cap_cgeo = std::min<int64_t>(m->ne, std::max<int64_t>(65536, m->ne / 8));
   e = e ? e : A(&f->d_cgeo, (size_t)f->cap_cgeo * sizeof(CutGeoS));
