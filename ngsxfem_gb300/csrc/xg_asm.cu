@@ -8,10 +8,13 @@
 //   MapPatchIntegrationPoint                                   xfem/symboliccutbfi.cpp:1747-1846
 //   RestrictedBilinearForm graph / Restrict()                  utils/restrictedblf.cpp:7-168
 #include <algorithm>
+#include <array>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <thread>
+#include <vector>
 
 #include "xg_basis.cuh"
 #include "xg_cut.cuh"
@@ -28,6 +31,8 @@ struct RuleTableF {
 };
 static __constant__ RuleTableF c_rules_f;
 
+int upload_mono();
+
 int upload_rules_asm() {
   XG_CUDA(cudaMemcpyToSymbol(c_rules, &host_rules(), sizeof(RuleTable)));
   static RuleTableF rf;
@@ -37,7 +42,7 @@ int upload_rules_asm() {
     rf.w[q] = (float)R.w[q];
   }
   XG_CUDA(cudaMemcpyToSymbol(c_rules_f, &rf, sizeof(RuleTableF)));
-  return XG_OK;
+  return upload_mono();
 }
 
 __device__ __forceinline__ bool tbit(const uint64_t* b, int64_t i) { return (b[i >> 6] >> (i & 63)) & 1ull; }
@@ -582,11 +587,13 @@ __global__ void k_cut_geo(int ne, int nv, const int32_t* __restrict__ elv, const
   }
 }
 
+// Quadrature-point form of the cut element matrices, for the cut elements
+// from `first` on (those beyond the moment workspace; normally none).
 template <int D, int K, bool SYM, typename T>
 __global__ void __launch_bounds__(CutCfg<D, K, SYM, T>::NT) k_elmat_cut(
     int ne, int nv, const int32_t* __restrict__ elv, const double* __restrict__ xyz, const double* __restrict__ lset,
     FormDesc form, const int32_t* __restrict__ list, const int* __restrict__ counts, T* __restrict__ elmat, int* err,
-    int needs_mask, const CutGeoS* __restrict__ cg, const CutSubS* __restrict__ cs, int64_t cap) {
+    int needs_mask, const CutGeoS* __restrict__ cg, const CutSubS* __restrict__ cs, int64_t cap, int first) {
   using C = CutCfg<D, K, SYM, T>;
   constexpr int N = C::N, E = C::E, EPB = C::EPB, CH = C::CH, NT = C::NT, NACC = C::NACC, NF = C::NF;
   __shared__ CutGeoS geo[EPB];
@@ -599,16 +606,17 @@ __global__ void __launch_bounds__(CutCfg<D, K, SYM, T>::NT) k_elmat_cut(
   __shared__ int maxpts_s;
   static_assert(sizeof(geo) + sizeof(subs) + sizeof(pts) + sizeof(tr) + sizeof(te) < 48 * 1024,
                 "k_elmat_cut shared memory");
-  entry_tables(N, SYM, ep, eq);
   const int count = counts[1];
+  if (first >= count) return;
+  entry_tables(N, SYM, ep, eq);
   const int slot_base = counts[0];
   const int le = threadIdx.x / N, i = threadIdx.x % N;
 
-  for (int batch = blockIdx.x; batch * EPB < count; batch += gridDim.x) {
+  for (int batch = blockIdx.x; first + batch * EPB < count; batch += gridDim.x) {
     __syncthreads();
     if (threadIdx.x < EPB) {
       CutGeoS& G = geo[threadIdx.x];
-      const int idx = batch * EPB + threadIdx.x;
+      const int idx = first + batch * EPB + threadIdx.x;
       if (idx < count && idx < cap) {
         G = cg[idx];
         subs[threadIdx.x] = cs[idx];
@@ -788,6 +796,463 @@ __global__ void __launch_bounds__(CutCfg<D, K, SYM, T>::NT) k_elmat_cut(
           elmat[(int64_t)geo[el].slot * E + k] = v;
         }
       }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Cut elements by barycentric moments.  Every basis function is a polynomial
+// in the barycentric coordinates lambda, and so is every integrand of the term
+// menu, with element constants in front:
+//   mass        phi_p phi_q
+//   laplace     grad phi_p . grad phi_q = sum_ab G_ab d_a phi_p d_b phi_q,
+//               G_ab = grad lambda_a . grad lambda_b
+//   n.grad u v  sum_b nu_b phi_p d_b phi_q,     nu_b = n . grad lambda_b
+//   b.grad u v  sum_b beta_b phi_p d_b phi_q,   beta_b = b . grad lambda_b
+// (d_a = derivative by lambda_a).  The quadrature sum of the cut rule is
+// therefore a fixed integer combination of the rule's moments
+//   mu_gamma = sum_x w_x |det F| lambda(x)^gamma
+// -- the same sums, reassociated.  k_cut_moments computes the moments of every
+// (domain, rule) set of the form; k_cut_entries combines them with integer
+// tables built on the host.  Per cut P2 tet this takes about a seventh of the
+// FP64 operations of evaluating the functions at every point.
+// ---------------------------------------------------------------------------
+constexpr int kMaxMomDeg = 6;   // 2K for K <= 3
+constexpr int kMomEPB = 16, kMomCHP = 8, kMomPts = kMomEPB * kMomCHP, kMomNT = 256;
+constexpr int kEntEPB = 32, kEntNT = 256;
+
+__host__ __device__ constexpr int pair_count(int d) { return (d + 1) * (d + 2) / 2; }
+__host__ __device__ constexpr int mono_count(int nvar, int d) {
+  // number of monomials of degree <= d in nvar variables: binom(d + nvar, nvar)
+  return nvar == 3 ? (d + 1) * (d + 2) * (d + 3) / 6 : (d + 1) * (d + 2) * (d + 3) * (d + 4) / 24;
+}
+
+// moment index m -> (index of (e0, e1) in the pair table A, index of (e2, e3)
+// (3D) or e2 (2D) in the table B), graded order; [0] 2D (84 used), [1] 3D (210)
+static __constant__ uint16_t c_mono[2][210];
+
+struct MomDesc {
+  int nsets;
+  int dt[kMaxGroups], order[kMaxGroups], deg[kMaxGroups], M[kMaxGroups], off[kMaxGroups];
+  int set_of[kMaxGroups];  // moment set of every group
+  int MT;                  // moments per element over all sets
+  int NA, NB;              // widest power-pair tables
+};
+
+struct EntTabs {
+  const int32_t* ptr[4];  // [E+1] term offsets per entry: MASS, LAP, PD, DP
+  const int32_t* idx[4];  // monomial | aux << 16 (aux: packed (a <= b) for LAP, b for PD/DP)
+  const void* coef[4];    // integer coefficients in the kernel's precision
+};
+
+// A[pair(e0, e1)] = p0[e0] p1[e1] for e0 + e1 <= DD (pair(e0, e1) = s(s+1)/2 + e1, s = e0 + e1)
+template <int DD, typename T>
+__device__ __forceinline__ void fill_pairs(const T* p0, const T* p1, T* out) {
+#pragma unroll
+  for (int s = 0; s <= DD; s++)
+#pragma unroll
+    for (int e1 = 0; e1 <= s; e1++) out[s * (s + 1) / 2 + e1] = p0[s - e1] * p1[e1];
+}
+
+template <int DD, int D, typename T>
+__device__ __forceinline__ void point_tables(const T* lam, T w, T* a, T* b) {
+  T p0[DD + 1], p1[DD + 1], p2[DD + 1];
+  p0[0] = w;
+  p1[0] = (T)1;
+  p2[0] = (T)1;
+#pragma unroll
+  for (int e = 1; e <= DD; e++) {
+    p0[e] = p0[e - 1] * lam[0];
+    p1[e] = p1[e - 1] * lam[1];
+    p2[e] = p2[e - 1] * lam[2];
+  }
+  fill_pairs<DD, T>(p0, p1, a);
+  if constexpr (D == 3) {
+    T p3[DD + 1];
+    p3[0] = (T)1;
+#pragma unroll
+    for (int e = 1; e <= DD; e++) p3[e] = p3[e - 1] * lam[3];
+    fill_pairs<DD, T>(p2, p3, b);
+  } else {
+#pragma unroll
+    for (int e = 0; e <= DD; e++) b[e] = p2[e];
+  }
+}
+
+template <int D, typename T>
+__global__ void __launch_bounds__(kMomNT) k_cut_moments(MomDesc md, const CutGeoS* __restrict__ cg,
+                                                         const CutSubS* __restrict__ cs,
+                                                         const int* __restrict__ counts, int64_t cap,
+                                                         T* __restrict__ mu) {
+  extern __shared__ __align__(16) unsigned char mo_smem[];
+  T* A = (T*)mo_smem;                // [kMomPts][NA]: w lambda0^e0 lambda1^e1
+  T* B = A + kMomPts * md.NA;        // [kMomPts][NB]: lambda2^e2 lambda3^e3 (3D), lambda2^e2 (2D)
+  __shared__ int np_s[kMomEPB];
+  constexpr int NSLOT = (kMomEPB * mono_count(D + 1, kMaxMomDeg) + kMomNT - 1) / kMomNT;
+  const int count = (int)min((int64_t)counts[1], cap);
+  const int NA = md.NA, NB = md.NB;
+  for (int batch = blockIdx.x; batch * kMomEPB < count; batch += gridDim.x) {
+    const int base = batch * kMomEPB;
+    for (int s = 0; s < md.nsets; s++) {
+      const int dt = md.dt[s], d = md.deg[s], M = md.M[s];
+      const int sd = dt == XG_IF ? D - 1 : D;
+      const int nq = c_rules.cnt[sd][md.order[s]], offq = c_rules.off[sd][md.order[s]];
+      __syncthreads();
+      if (threadIdx.x < kMomEPB) {
+        const int idx = base + threadIdx.x;
+        np_s[threadIdx.x] = idx < count ? cg[idx].ns[dt] * nq : 0;
+      }
+      __syncthreads();
+      int maxnp = 0;
+#pragma unroll
+      for (int k = 0; k < kMomEPB; k++) maxnp = max(maxnp, np_s[k]);
+      Acc<T> acc[NSLOT];
+#pragma unroll
+      for (int r = 0; r < NSLOT; r++) acc[r].init();
+      for (int c0 = 0; c0 < maxnp; c0 += kMomCHP) {
+        if (threadIdx.x < kMomPts) {
+          const int el = threadIdx.x / kMomCHP, qi = c0 + threadIdx.x % kMomCHP;
+          if (qi < np_s[el]) {
+            const int idx = base + el;
+            const int sidx = qi / nq, bq = qi - sidx * nq;
+            const Sub& sub = cs[idx].sub[dt][sidx];
+            T lam[4], w;
+            if constexpr (sizeof(T) == 4) {
+              const float* ip = c_rules_f.x[offq + bq];
+              float ow = 1.f, pt[3];
+              for (int m = 0; m < sd; ++m) ow -= ip[m];
+#pragma unroll
+              for (int k = 0; k < 3; k++) pt[k] = ow * (float)sub.p[0].c[k];
+              for (int m = 0; m < sd; ++m)
+#pragma unroll
+                for (int k = 0; k < 3; k++) pt[k] += ip[m] * (float)sub.p[m + 1].c[k];
+              w = c_rules_f.w[offq + bq] * (float)cs[idx].vol[dt][sidx];
+              if (dt == XG_IF) w *= (float)cg[idx].iffac;
+              w *= (float)cg[idx].meas;
+              float s3 = 0.f;
+#pragma unroll
+              for (int k = 0; k < D; k++) {
+                lam[k] = pt[k];
+                s3 += pt[k];
+              }
+              lam[D] = 1.f - s3;
+            } else {
+              double pt[3];
+              plain_point(sub, sd + 1, c_rules.x[offq + bq], pt);
+              w = c_rules.w[offq + bq] * cs[idx].vol[dt][sidx];
+              if (dt == XG_IF) w *= cg[idx].iffac;
+              w *= cg[idx].meas;
+              double s3 = 0.0;
+#pragma unroll
+              for (int k = 0; k < D; k++) {
+                lam[k] = pt[k];
+                s3 += pt[k];
+              }
+              lam[D] = 1.0 - s3;
+            }
+            T* a = A + threadIdx.x * NA;
+            T* b = B + threadIdx.x * NB;
+            switch (d) {
+              case 0: point_tables<0, D, T>(lam, w, a, b); break;
+              case 1: point_tables<1, D, T>(lam, w, a, b); break;
+              case 2: point_tables<2, D, T>(lam, w, a, b); break;
+              case 3: point_tables<3, D, T>(lam, w, a, b); break;
+              case 4: point_tables<4, D, T>(lam, w, a, b); break;
+              case 5: point_tables<5, D, T>(lam, w, a, b); break;
+              default: point_tables<6, D, T>(lam, w, a, b); break;
+            }
+          }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < NSLOT; r++) {
+          const int t = threadIdx.x + r * kMomNT;
+          if (t < kMomEPB * M) {
+            const int el = t / M, m = t - el * M;
+            const int n = min(kMomCHP, np_s[el] - c0);
+            const int ab = c_mono[D - 2][m];
+            const T* a = A + el * kMomCHP * NA + (ab & 255);
+            const T* b = B + el * kMomCHP * NB + (ab >> 8);
+            for (int j = 0; j < n; j++) acc[r].add(a[j * NA] * b[j * NB]);
+          }
+        }
+        __syncthreads();
+      }
+#pragma unroll
+      for (int r = 0; r < NSLOT; r++) {
+        const int t = threadIdx.x + r * kMomNT;
+        if (t < kMomEPB * M) {
+          const int el = t / M, m = t - el * M;
+          if (base + el < count) mu[(int64_t)(base + el) * md.MT + md.off[s] + m] = acc[r].get();
+        }
+      }
+    }
+  }
+}
+
+// per cut element: Gram matrix of the barycentric gradients, the weights of
+// the first-derivative tables and the group coefficients
+template <int D, typename T>
+struct EntGeoS {
+  T G[(D + 1) * (D + 2) / 2];
+  T wpd[kMaxGroups][D + 1];  // phi_p d_b phi_q: cN1 nu_b + cC beta_b
+  T wdp[kMaxGroups][D + 1];  // d_b phi_p phi_q: cN2 nu_b
+  T cM[kMaxGroups], cL[kMaxGroups];
+  int act;  // groups whose defined_on holds the element
+  int idx, slot;
+  int gv[D + 1];
+};
+
+template <typename T>
+__device__ __forceinline__ T tab_sum(const int32_t* __restrict__ ptr, const int32_t* __restrict__ ix,
+                                     const T* __restrict__ cf, int k, const T* __restrict__ m) {
+  T s = 0;
+  const int t1 = __ldg(&ptr[k + 1]);
+  for (int t = __ldg(&ptr[k]); t < t1; t++) s += __ldg(&cf[t]) * m[__ldg(&ix[t]) & 0xffff];
+  return s;
+}
+template <typename T>
+__device__ __forceinline__ T tab_sum_w(const int32_t* __restrict__ ptr, const int32_t* __restrict__ ix,
+                                       const T* __restrict__ cf, int k, const T* __restrict__ m, const T* w) {
+  T s = 0;
+  const int t1 = __ldg(&ptr[k + 1]);
+  for (int t = __ldg(&ptr[k]); t < t1; t++) {
+    const int x = __ldg(&ix[t]);
+    s += (__ldg(&cf[t]) * w[x >> 16]) * m[x & 0xffff];
+  }
+  return s;
+}
+
+template <int D, int K, bool SYM, typename T>
+__global__ void __launch_bounds__(kEntNT) k_cut_entries(FormDesc form, MomDesc md, EntTabs tabs,
+                                                         const CutGeoS* __restrict__ cg,
+                                                         const int* __restrict__ counts, int64_t cap,
+                                                         const T* __restrict__ mu, T* __restrict__ elmat, int* err) {
+  constexpr int N = ndof_el(D, K), E = SYM ? tri_size(N) : N * N;
+  __shared__ EntGeoS<D, T> eg[kEntEPB];
+  __shared__ unsigned char ep[E], eq[E];
+  entry_tables(N, SYM, ep, eq);
+  const int count = (int)min((int64_t)counts[1], cap);
+  const T* cf[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) cf[k] = (const T*)tabs.coef[k];
+  for (int batch = blockIdx.x; batch * kEntEPB < count; batch += gridDim.x) {
+    __syncthreads();
+    if (threadIdx.x < kEntEPB) {
+      EntGeoS<D, T>& S = eg[threadIdx.x];
+      const int idx = batch * kEntEPB + threadIdx.x;
+      S.idx = idx < count ? idx : -1;
+      if (idx < count) {
+        const CutGeoS& C = cg[idx];
+        double g[D + 1][D], nu[D + 1];
+#pragma unroll
+        for (int a = 0; a <= D; a++) {
+          double s = 0.0;
+#pragma unroll
+          for (int k = 0; k < D; k++) {
+            g[a][k] = C.g[a][k];
+            s += C.nrm[k] * g[a][k];
+          }
+          nu[a] = s;
+        }
+#pragma unroll
+        for (int a = 0; a <= D; a++)
+#pragma unroll
+          for (int b = a; b <= D; b++) {
+            double s = 0.0;
+#pragma unroll
+            for (int k = 0; k < D; k++) s += g[a][k] * g[b][k];
+            S.G[tri_index(a, b, D + 1)] = (T)s;
+          }
+        int act = 0;
+        for (int q = 0; q < form.ngroups; q++) {
+          const GroupDesc& Gq = form.g[q];
+          if (!Gq.defined_on || tbit(Gq.defined_on, C.elem)) act |= 1 << q;
+          const int used = Gq.used;
+          S.cM[q] = (T)C.coef[q][0];
+          S.cL[q] = (T)C.coef[q][1];
+#pragma unroll
+          for (int b = 0; b <= D; b++) {
+            double pd = 0.0, dp = 0.0;
+            if (used & (1 << XG_TERM_NGRADU_V)) pd = C.coef[q][2] * nu[b];
+            if (used & (1 << XG_TERM_CONV)) {
+              double s = 0.0;
+#pragma unroll
+              for (int k = 0; k < D; k++) s += Gq.b[k] * g[b][k];
+              pd += C.coef[q][4] * s;
+            }
+            if (used & (1 << XG_TERM_U_NGRADV)) dp = C.coef[q][3] * nu[b];
+            S.wpd[q][b] = (T)pd;
+            S.wdp[q][b] = (T)dp;
+          }
+        }
+        S.act = act;
+        S.slot = C.slot;
+#pragma unroll
+        for (int v = 0; v <= D; v++) S.gv[v] = C.gv[v];
+      }
+    }
+    __syncthreads();
+    // element fastest: the lanes of a warp share the entry and its term lists
+    for (int t = threadIdx.x; t < kEntEPB * E; t += kEntNT) {
+      const int k = t / kEntEPB, el = t - k * kEntEPB;
+      const EntGeoS<D, T>& S = eg[el];
+      if (S.idx < 0) continue;
+      const T* mue = mu + (int64_t)S.idx * md.MT;
+      Acc<T> v;
+      v.init();
+      for (int q = 0; q < form.ngroups; q++) {
+        if (!((S.act >> q) & 1)) continue;
+        const int used = form.g[q].used;
+        const T* m = mue + md.off[md.set_of[q]];
+        if (used & (1 << XG_TERM_MASS)) v.add(S.cM[q] * tab_sum<T>(tabs.ptr[0], tabs.idx[0], cf[0], k, m));
+        if (used & (1 << XG_TERM_LAPLACE))
+          v.add(S.cL[q] * tab_sum_w<T>(tabs.ptr[1], tabs.idx[1], cf[1], k, m, S.G));
+        if (used & ((1 << XG_TERM_NGRADU_V) | (1 << XG_TERM_CONV)))
+          v.add(tab_sum_w<T>(tabs.ptr[2], tabs.idx[2], cf[2], k, m, S.wpd[q]));
+        if (used & (1 << XG_TERM_U_NGRADV)) v.add(tab_sum_w<T>(tabs.ptr[3], tabs.idx[3], cf[3], k, m, S.wdp[q]));
+      }
+      T r = v.get();
+      if (K == 3 && fn_sign<D, K>(ep[k], S.gv) * fn_sign<D, K>(eq[k], S.gv) < 0) r = -r;
+      if (!isfinite(r)) set_err(err, XG_ERR_NONFINITE);
+      elmat[(int64_t)S.slot * E + k] = r;
+    }
+  }
+}
+
+// ---- host side of the moment kernels ---------------------------------------
+using Expo = std::array<int, 4>;
+using Poly = std::map<Expo, long long>;
+
+// graded enumeration of the monomials of nvar barycentric variables up to kMaxMomDeg
+static std::vector<Expo> monomials(int nvar) {
+  std::vector<Expo> out;
+  for (int d = 0; d <= kMaxMomDeg; d++)
+    for (int e0 = d; e0 >= 0; e0--)
+      for (int e1 = d - e0; e1 >= 0; e1--) {
+        if (nvar == 3) {
+          out.push_back({e0, e1, d - e0 - e1, 0});
+        } else {
+          for (int e2 = d - e0 - e1; e2 >= 0; e2--) out.push_back({e0, e1, e2, d - e0 - e1 - e2});
+        }
+      }
+  return out;
+}
+
+static int pair_index(int a, int b) { return (a + b) * (a + b + 1) / 2 + b; }
+
+int upload_mono() {
+  uint16_t h[2][210] = {};
+  for (int D = 2; D <= 3; D++) {
+    const std::vector<Expo> ms = monomials(D + 1);
+    for (size_t m = 0; m < ms.size(); m++) {
+      const Expo& e = ms[m];
+      const int ia = pair_index(e[0], e[1]), ib = D == 3 ? pair_index(e[2], e[3]) : e[2];
+      h[D - 2][m] = (uint16_t)(ia | ib << 8);
+    }
+  }
+  XG_CUDA(cudaMemcpyToSymbol(c_mono, h, sizeof(h)));
+  return XG_OK;
+}
+
+static Poly basis_poly(int desc) {
+  const int type = desc & 15, a = (desc >> 4) & 15, b = (desc >> 8) & 15, c = (desc >> 12) & 15;
+  auto mono = [](std::initializer_list<int> vars) {
+    Expo e = {0, 0, 0, 0};
+    for (int v : vars) e[v]++;
+    return e;
+  };
+  Poly P;
+  if (type == 0) {
+    P[mono({a})] = 1;
+  } else if (type == 1) {
+    P[mono({a, b})] = 1;
+  } else if (type == 2) {
+    P[mono({a, a, b})] += 1;
+    P[mono({a, b, b})] -= 1;
+  } else {
+    P[mono({a, b, c})] = 1;
+  }
+  return P;
+}
+
+static Poly poly_mul(const Poly& x, const Poly& y) {
+  Poly r;
+  for (const auto& [ex, cx] : x)
+    for (const auto& [ey, cy] : y) {
+      Expo e;
+      for (int k = 0; k < 4; k++) e[k] = ex[k] + ey[k];
+      r[e] += cx * cy;
+    }
+  return r;
+}
+
+static Poly poly_diff(const Poly& x, int v) {
+  Poly r;
+  for (const auto& [e, c] : x)
+    if (e[v] > 0) {
+      Expo f = e;
+      f[v]--;
+      r[f] += c * e[v];
+    }
+  return r;
+}
+
+// Integer term tables for the canonical orientation (local vertex numbers as
+// global numbers; cubic edge functions flip with fn_sign): per entry (p, q)
+// and kind, the terms (aux, monomial, coefficient) of
+//   MASS phi_p phi_q, LAP sum_ab d_a phi_p d_b phi_q, PD phi_p d_b phi_q, DP d_b phi_p phi_q.
+template <int D, int K>
+void moment_tables(bool sym, std::vector<int32_t> (&ptr)[4], std::vector<int32_t> (&ix)[4],
+                   std::vector<double> (&cf)[4]) {
+  constexpr int N = ndof_el(D, K);
+  const int E = sym ? tri_size(N) : N * N;
+  const std::vector<Expo> ms = monomials(D + 1);
+  std::map<Expo, int> mindex;
+  for (size_t m = 0; m < ms.size(); m++) mindex[ms[m]] = (int)m;
+  int gv[4] = {0, 1, 2, 3};
+  std::vector<Poly> phi(N);
+  std::vector<std::array<Poly, 4>> dphi(N);
+  for (int i = 0; i < N; i++) {
+    phi[i] = basis_poly(fn_desc<D, K>(i, gv));
+    for (int a = 0; a <= D; a++) dphi[i][a] = poly_diff(phi[i], a);
+  }
+  for (int k = 0; k < 4; k++) {
+    ptr[k].assign(1, 0);
+    ix[k].clear();
+    cf[k].clear();
+  }
+  for (int k = 0; k < E; k++) {
+    int p, q;
+    if (sym) {
+      p = 0;
+      int rem = k;
+      while (rem >= N - p) {
+        rem -= N - p;
+        p++;
+      }
+      q = p + rem;
+    } else {
+      p = k / N;
+      q = k % N;
+    }
+    std::map<std::pair<int, int>, long long> t[4];
+    for (const auto& [e, c] : poly_mul(phi[p], phi[q])) t[0][{0, mindex.at(e)}] += c;
+    for (int a = 0; a <= D; a++)
+      for (int b = 0; b <= D; b++)
+        for (const auto& [e, c] : poly_mul(dphi[p][a], dphi[q][b]))
+          t[1][{tri_index(std::min(a, b), std::max(a, b), D + 1), mindex.at(e)}] += c;
+    for (int b = 0; b <= D; b++) {
+      for (const auto& [e, c] : poly_mul(phi[p], dphi[q][b])) t[2][{b, mindex.at(e)}] += c;
+      for (const auto& [e, c] : poly_mul(dphi[p][b], phi[q])) t[3][{b, mindex.at(e)}] += c;
+    }
+    for (int kind = 0; kind < 4; kind++) {
+      for (const auto& [key, c] : t[kind])
+        if (c != 0) {
+          ix[kind].push_back(key.second | key.first << 16);
+          cf[kind].push_back((double)c);
+        }
+      ptr[kind].push_back((int32_t)ix[kind].size());
     }
   }
 }
@@ -1632,6 +2097,14 @@ struct xg_form {
   int el_sym = 0;      // every volume group symmetric: packed element matrices
   double* d_tabs = nullptr;  // reference tables of the uncut kernel
   UncutTabs tabs = {};
+  MomDesc md = {};              // moment sets of the cut element kernels
+  EntTabs ent = {};             // their integer term tables
+  int32_t* d_mtab_i = nullptr;  // term offsets and indices
+  void* d_mtab_c = nullptr;     // term coefficients (kernel precision)
+  void* d_mu = nullptr;         // [cap_cgeo][mu_MT] moments of the cut elements (per step)
+  int64_t mu_MT = 0;
+  size_t mo_smem = 0;
+  int grid_mo = 0, grid_en = 0;
   int64_t nw32_el = 0, nw32_fa = 0, nw32_dof = 0;
   int64_t cap_el = 0, cap_fa = 0;
   // workspace
@@ -1693,7 +2166,8 @@ int form_free(xg_form* f) {
   void* ptrs[] = {f->d_full_ptr, f->d_tmp_cols, f->d_fpos_el, f->d_pbuf, f->d_flags, f->d_pgeo, f->d_cgeo, f->d_csub,
                   f->d_tabs, f->d_act_un, f->d_act_cut, f->d_act_fa, f->d_dof_bits, f->d_l_un, f->d_l_cut, f->d_l_fa,
                   f->d_el_slot, f->d_fa_slot, f->d_dof_row, f->d_rowcnt, f->d_counts, f->d_bsum, f->d_bsum64,
-                  f->d_elmat, f->d_famat, f->d_err, f->d_dom, f->d_ratio, f->d_bits, f->d_fbits};
+                  f->d_elmat, f->d_famat, f->d_err, f->d_dom, f->d_ratio, f->d_bits, f->d_fbits,
+                  f->d_mtab_i, f->d_mtab_c, f->d_mu};
   for (void* p : ptrs) cudaFree(p);
   delete f;
   return XG_OK;
@@ -1875,6 +2349,124 @@ std::vector<double> uncut_tables(const FormDesc& d, bool sym, size_t offs[][3]) 
   return buf;
 }
 
+// Moment sets of the cut element kernels: groups of one domain whose rule is
+// exact for their integrand (order >= degree) share one set, computed with the
+// rule of the set's degree; a group whose rule is below its integrand degree
+// keeps its own rule, so its moments reproduce that rule's sums.
+void build_moment_desc(xg_form* f) {
+  const int D = f->mesh->dim, K = f->space->order;
+  MomDesc& md = f->md;
+  std::memset(&md, 0, sizeof(md));
+  bool exact[kMaxGroups] = {};
+  for (int q = 0; q < f->desc.ngroups; q++) {
+    const GroupDesc& G = f->desc.g[q];
+    int deg = 0;
+    if (G.used & (1 << XG_TERM_MASS)) deg = std::max(deg, 2 * K);
+    if (G.used & (1 << XG_TERM_LAPLACE)) deg = std::max(deg, 2 * K - 2);
+    if (G.used & ((1 << XG_TERM_NGRADU_V) | (1 << XG_TERM_U_NGRADV) | (1 << XG_TERM_CONV)))
+      deg = std::max(deg, 2 * K - 1);
+    const int p = clamp_order(G.order);
+    const bool ex = p >= deg;
+    int s = -1;
+    for (int t = 0; t < md.nsets; t++)
+      if (md.dt[t] == G.domain && exact[t] == ex && (ex || md.order[t] == p)) s = t;
+    if (s < 0) {
+      s = md.nsets++;
+      md.dt[s] = G.domain;
+      md.order[s] = p;
+      exact[s] = ex;
+    }
+    md.deg[s] = std::max(md.deg[s], deg);
+    md.set_of[q] = s;
+  }
+  md.NA = md.NB = 1;
+  for (int s = 0; s < md.nsets; s++) {
+    if (exact[s]) md.order[s] = md.deg[s];
+    md.M[s] = mono_count(D + 1, md.deg[s]);
+    md.off[s] = md.MT;
+    md.MT += md.M[s];
+    md.NA = std::max(md.NA, pair_count(md.deg[s]));
+    md.NB = std::max(md.NB, D == 3 ? pair_count(md.deg[s]) : md.deg[s] + 1);
+  }
+  f->mo_smem = (size_t)kMomPts * (md.NA + md.NB) * (f->precision == XG_PREC_FP64 ? 8 : 4);
+}
+
+int upload_moment_tables(xg_form* f) {
+  build_moment_desc(f);
+  const int D = f->mesh->dim, K = f->space->order;
+  const bool sym = f->el_sym;
+  std::vector<int32_t> ptr[4], ix[4];
+  std::vector<double> cf[4];
+  if (D == 2) {
+    if (K == 1) moment_tables<2, 1>(sym, ptr, ix, cf);
+    else if (K == 2) moment_tables<2, 2>(sym, ptr, ix, cf);
+    else moment_tables<2, 3>(sym, ptr, ix, cf);
+  } else {
+    if (K == 1) moment_tables<3, 1>(sym, ptr, ix, cf);
+    else if (K == 2) moment_tables<3, 2>(sym, ptr, ix, cf);
+    else moment_tables<3, 3>(sym, ptr, ix, cf);
+  }
+  std::vector<int32_t> ibuf;
+  size_t ioff[4][2], coff[4], nc = 0;
+  for (int k = 0; k < 4; k++) {
+    ioff[k][0] = ibuf.size();
+    ibuf.insert(ibuf.end(), ptr[k].begin(), ptr[k].end());
+    ioff[k][1] = ibuf.size();
+    ibuf.insert(ibuf.end(), ix[k].begin(), ix[k].end());
+    coff[k] = nc;
+    nc += cf[k].size();
+  }
+  const bool fp64 = f->precision == XG_PREC_FP64;
+  std::vector<double> c64;
+  std::vector<float> c32;
+  for (int k = 0; k < 4; k++)
+    for (double c : cf[k]) {
+      c64.push_back(c);
+      c32.push_back((float)c);
+    }
+  cudaFree(f->d_mtab_i);
+  cudaFree(f->d_mtab_c);
+  f->d_mtab_i = nullptr;
+  f->d_mtab_c = nullptr;
+  const size_t csz = fp64 ? 8 : 4;
+  XG_CUDA(cudaMalloc((void**)&f->d_mtab_i, std::max<size_t>(ibuf.size(), 1) * 4));
+  XG_CUDA(cudaMalloc(&f->d_mtab_c, std::max<size_t>(nc, 1) * csz));
+  XG_CUDA(cudaMemcpy(f->d_mtab_i, ibuf.data(), ibuf.size() * 4, cudaMemcpyHostToDevice));
+  if (nc)
+    XG_CUDA(cudaMemcpy(f->d_mtab_c, fp64 ? (const void*)c64.data() : (const void*)c32.data(), nc * csz,
+                       cudaMemcpyHostToDevice));
+  for (int k = 0; k < 4; k++) {
+    f->ent.ptr[k] = f->d_mtab_i + ioff[k][0];
+    f->ent.idx[k] = f->d_mtab_i + ioff[k][1];
+    f->ent.coef[k] = (const char*)f->d_mtab_c + coff[k] * csz;
+  }
+  if (f->mo_smem > 48 * 1024) {
+    // the attribute is an upper bound shared by all forms: only ever raise it
+    static std::mutex mu;
+    static size_t raised[2][2] = {{48 * 1024, 48 * 1024}, {48 * 1024, 48 * 1024}};
+    std::lock_guard<std::mutex> lock(mu);
+    size_t& r = raised[D - 2][fp64 ? 0 : 1];
+    if (f->mo_smem > r) {
+      const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
+      cudaError_t e;
+      if (D == 2) e = fp64 ? cudaFuncSetAttribute(k_cut_moments<2, double>, at, (int)f->mo_smem)
+                           : cudaFuncSetAttribute(k_cut_moments<2, float>, at, (int)f->mo_smem);
+      else e = fp64 ? cudaFuncSetAttribute(k_cut_moments<3, double>, at, (int)f->mo_smem)
+                    : cudaFuncSetAttribute(k_cut_moments<3, float>, at, (int)f->mo_smem);
+      if (e) return cuda_fail(e, "xg_form: moment kernel shared memory");
+      r = f->mo_smem;
+    }
+  }
+  // the moment workspace grows if a rebuild needs more moments per element
+  if (f->d_mu && f->md.MT > f->mu_MT) {
+    cudaFree(f->d_mu);
+    f->d_mu = nullptr;
+    XG_CUDA(cudaMalloc(&f->d_mu, (size_t)f->cap_cgeo * f->md.MT * csz));
+    f->mu_MT = f->md.MT;
+  }
+  return XG_OK;
+}
+
 int upload_tables(xg_form* f) {
   size_t offs[kMaxGroups][3];
   std::vector<double> buf;
@@ -1892,15 +2484,16 @@ int upload_tables(xg_form* f) {
   cudaFree(f->d_tabs);
   f->d_tabs = nullptr;
   std::memset(&f->tabs, 0, sizeof(f->tabs));
-  if (buf.empty()) return XG_OK;
-  XG_CUDA(cudaMalloc((void**)&f->d_tabs, buf.size() * sizeof(double)));
-  XG_CUDA(cudaMemcpy(f->d_tabs, buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice));
-  for (int q = 0; q < f->desc.ngroups; q++) {
-    f->tabs.m[q] = offs[q][0] == (size_t)-1 ? nullptr : f->d_tabs + offs[q][0];
-    f->tabs.t[q] = offs[q][1] == (size_t)-1 ? nullptr : f->d_tabs + offs[q][1];
-    f->tabs.c[q] = offs[q][2] == (size_t)-1 ? nullptr : f->d_tabs + offs[q][2];
+  if (!buf.empty()) {
+    XG_CUDA(cudaMalloc((void**)&f->d_tabs, buf.size() * sizeof(double)));
+    XG_CUDA(cudaMemcpy(f->d_tabs, buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice));
+    for (int q = 0; q < f->desc.ngroups; q++) {
+      f->tabs.m[q] = offs[q][0] == (size_t)-1 ? nullptr : f->d_tabs + offs[q][0];
+      f->tabs.t[q] = offs[q][1] == (size_t)-1 ? nullptr : f->d_tabs + offs[q][1];
+      f->tabs.c[q] = offs[q][2] == (size_t)-1 ? nullptr : f->d_tabs + offs[q][2];
+    }
   }
-  return XG_OK;
+  return upload_moment_tables(f);
 }
 
 template <class K>
@@ -1930,9 +2523,13 @@ int launch_volume_sym(xg_form* f, const double* d_lset, const uint8_t* d_dom, cu
   xg_mesh* m = f->mesh;
   auto ku = k_elmat_uncut<D, K, SYM, T>;
   auto kc = k_elmat_cut<D, K, SYM, T>;
+  auto km = k_cut_moments<D, T>;
+  auto kn = k_cut_entries<D, K, SYM, T>;
   if (!f->grid_el_un) {
     f->grid_el_un = grid_for(ku, 256, 0);
     f->grid_el_cut = grid_for(kc, CC::NT, 0);
+    f->grid_mo = grid_for(km, kMomNT, f->mo_smem);
+    f->grid_en = grid_for(kn, kEntNT, 0);
   }
   ku<<<f->grid_el_un, 256, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, d_dom, f->desc, f->tabs, f->d_l_un, f->d_counts,
                                    (T*)f->d_elmat, f->d_err);
@@ -1940,9 +2537,14 @@ int launch_volume_sym(xg_form* f, const double* d_lset, const uint8_t* d_dom, cu
   k_cut_geo<D><<<152 * 4, 128, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, d_lset, f->desc, f->d_l_cut, f->d_counts,
                                        (CutGeoS*)f->d_cgeo, (CutSubS*)f->d_csub, f->cap_cgeo, f->d_err,
                                        f->needs_mask);
+  km<<<f->grid_mo, kMomNT, f->mo_smem, s>>>(f->md, (const CutGeoS*)f->d_cgeo, (const CutSubS*)f->d_csub,
+                                            f->d_counts, f->cap_cgeo, (T*)f->d_mu);
+  kn<<<f->grid_en, kEntNT, 0, s>>>(f->desc, f->md, f->ent, (const CutGeoS*)f->d_cgeo, f->d_counts, f->cap_cgeo,
+                                   (const T*)f->d_mu, (T*)f->d_elmat, f->d_err);
+  // cut elements beyond the workspace (none unless more than cap_cgeo are cut)
   kc<<<f->grid_el_cut, CC::NT, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, d_lset, f->desc, f->d_l_cut, f->d_counts,
                                       (T*)f->d_elmat, f->d_err, f->needs_mask, (const CutGeoS*)f->d_cgeo,
-                                      (const CutSubS*)f->d_csub, f->cap_cgeo);
+                                      (const CutSubS*)f->d_csub, f->cap_cgeo, (int)f->cap_cgeo);
   if (f->use_ev) cudaEventRecord(f->ev[4], s);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? XG_OK : cuda_fail(e, "k_elmat");
@@ -2328,8 +2930,16 @@ int form_workspace(xg_form* f) {
   e = e ? e : A(&f->d_pgeo, f->has_patch ? (size_t)f->cap_fa * sizeof(PaGeoS<3, double>) : 16);
   // cut elements beyond this capacity set themselves up inside the element kernel
   f->cap_cgeo = std::min<int64_t>(m->ne, std::max<int64_t>(65536, m->ne / 8));
+  // test hook: a smaller cut workspace sends the remaining cut elements through
+  // the quadrature-point kernel
+  if (const char* cap_env = std::getenv("XG_CUT_WORKSPACE")) {
+    const long long v = std::atoll(cap_env);
+    if (v > 0) f->cap_cgeo = std::min<int64_t>(f->cap_cgeo, v);
+  }
   e = e ? e : A(&f->d_cgeo, (size_t)f->cap_cgeo * sizeof(CutGeoS));
   e = e ? e : A(&f->d_csub, (size_t)f->cap_cgeo * sizeof(CutSubS));
+  f->mu_MT = std::max(f->md.MT, 1);
+  e = e ? e : A(&f->d_mu, (size_t)f->cap_cgeo * f->mu_MT * esz);
   e = e ? e : A((void**)&f->d_err, sizeof(int));
   e = e ? e : A((void**)&f->d_dom, (size_t)m->ne);
   e = e ? e : A((void**)&f->d_ratio, (size_t)m->ne * 8);
