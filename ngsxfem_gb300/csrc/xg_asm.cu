@@ -19,6 +19,7 @@
 #include "xg_basis.cuh"
 #include "xg_cut.cuh"
 #include "xg_internal.h"
+#include "xg_patch.cuh"
 
 namespace xg {
 
@@ -1278,6 +1279,8 @@ template <int D, typename T>
 struct PaGeoS {
   T A12[D][D], c12[D];  // xi_2 = A12 xi_1 + c12 (element 1 -> element 2 reference coordinates)
   T A21[D][D], c21[D];
+  T L21[D + 1][D + 1];  // lambda_2 = L21 lambda_1 (barycentric coordinates)
+  T L12[D + 1][D + 1];  // lambda_1 = L12 lambda_2
   T det1, det2;
   int gv1[4], gv2[4];
   int facet;
@@ -1383,6 +1386,23 @@ __global__ void k_patch_geo(int ne, int nv, const int32_t* __restrict__ elv, con
         O.A12[i][k] = (T)G.A12[i][k];
         O.A21[i][k] = (T)G.A21[i][k];
       }
+    }
+    // barycentric form of the maps: lambda_to[i] = sum_b L[i][b] lambda_from[b]
+    // (xi_to = A xi_from + c with 1 = sum_b lambda_from[b])
+#pragma unroll
+    for (int b = 0; b <= D; b++) {
+      double s12 = 0.0, s21 = 0.0;
+#pragma unroll
+      for (int i = 0; i < D; i++) {
+        const double l21 = (b < D ? G.A12[i][b] : 0.0) + G.c12[i];
+        const double l12 = (b < D ? G.A21[i][b] : 0.0) + G.c21[i];
+        O.L21[i][b] = (T)l21;
+        O.L12[i][b] = (T)l12;
+        s12 += l21;
+        s21 += l12;
+      }
+      O.L21[D][b] = (T)(1.0 - s12);
+      O.L12[D][b] = (T)(1.0 - s21);
     }
     O.det1 = (T)G.det1;
     O.det2 = (T)G.det2;
@@ -1501,6 +1521,197 @@ __global__ void __launch_bounds__(PaCfg<D, K>::NT) k_patch(
           }
         }
       }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Facet patches by basis change (every patch term of order >= 2K).  The
+// integrand (u1 - u2)(v1 - v2) has degree 2K on each element and the order-2K
+// rule integrates it exactly, so with x = [x1; x2] the coefficients of both
+// elements' functions:
+//   on T1:  (S1 x1 - C21 x2)^T  |det F1| Mh  (S1 x1 - C21 x2)
+//   on T2:  (C12 x1 - S2 x2)^T  |det F2| Mh  (C12 x1 - S2 x2)
+// Mh = reference mass matrix of the canonical basis, S = the elements' edge
+// orientation signs, C21 = the functions of T2 in the canonical basis of T1
+// (exact, from their values at T1's nodes) and C12 likewise.  With
+// W = Mh C the blocks of the patch matrix are
+//   (1,1)  det1 S1 Mh S1 + det2 C12^T W12
+//   (1,2)  -det1 S1 W21 - det2 (S2 W12)^T
+//   (2,2)  det1 C21^T W21 + det2 S2 Mh S2
+// the same integrals as the quadrature of k_patch, reassociated.
+// ---------------------------------------------------------------------------
+template <int D, int K>
+struct PxCfg {
+  static constexpr int N = ndof_el(D, K);
+  static constexpr int E = tri_size(2 * N);
+  static constexpr int FPB = N <= 10 ? 32 : 8;  // facets per block: the lanes of one unit of work
+  static constexpr int NT = 256;
+  static constexpr int NU = NT / FPB;           // units per pass of the block
+};
+
+// shared memory of k_patch_exact, facet index fastest (lanes = facets, so a
+// warp runs one unit of work -- a node, a column, an entry -- for FPB facets
+// without divergence: partially active warps would idle FP64 lanes)
+template <int D, int K, typename T>
+struct PxSmem {
+  static constexpr int N = PxCfg<D, K>::N, E = PxCfg<D, K>::E, F = PxCfg<D, K>::FPB;
+  T Ct[2][N][N][F];  // [0]: C21 (T2's functions in T1's canonical basis), [1]: C12
+  T Wt[2][N][N][F];  // Mh C
+  T nodes[2][N][D + 1][F];
+  T L[2][D + 1][D + 1][F];  // [0]: L21, [1]: L12
+  T det1[F], det2[F], c[F];
+  int gv1[D + 1][F], gv2[D + 1][F];
+  int idx[F];
+  T Mh[N][N];
+  int cnt[4];
+  unsigned char perm[N];
+  unsigned char ep[E], eq[E];
+};
+
+template <int D, int K, typename T>
+__global__ void __launch_bounds__(256) k_patch_exact(FormDesc form, const PaGeoS<D, T>* __restrict__ pgeo,
+                                                      const int* __restrict__ counts, const T* __restrict__ mhat,
+                                                      T* __restrict__ famat, int64_t cap_fa, int* err) {
+  using C = PxCfg<D, K>;
+  using S = PxSmem<D, K, T>;
+  constexpr int N = C::N, E = C::E, F = C::FPB, NT = C::NT, NU = C::NU;
+  extern __shared__ __align__(16) unsigned char px_raw[];
+  S& sm = *reinterpret_cast<S*>(px_raw);
+  entry_tables(2 * N, true, sm.ep, sm.eq);
+  for (int t = threadIdx.x; t < N * N; t += NT) sm.Mh[t / N][t % N] = mhat[t];
+  if (threadIdx.x == 0) {
+    int n = 0;
+    sm.cnt[0] = 0;
+    for (int d = 1; d <= 3; d++) {
+      for (int k = 0; k < N; k++)
+        if (canon_degree<D, K>(k) == d) sm.perm[n++] = (unsigned char)k;
+      sm.cnt[d] = n;
+    }
+  }
+  const int f = threadIdx.x % F, u0 = threadIdx.x / F;
+  const int count = counts[2];
+  for (int batch = blockIdx.x; batch * F < count; batch += gridDim.x) {
+    __syncthreads();
+    if (threadIdx.x < F) {
+      const int idx = batch * F + threadIdx.x;
+      const bool ok = idx < count && idx < cap_fa;
+      sm.idx[threadIdx.x] = ok ? idx : -1;
+      if (ok) {
+        const PaGeoS<D, T>& G = pgeo[idx];
+#pragma unroll
+        for (int i = 0; i <= D; i++)
+#pragma unroll
+          for (int b = 0; b <= D; b++) {
+            sm.L[0][i][b][threadIdx.x] = G.L21[i][b];
+            sm.L[1][i][b][threadIdx.x] = G.L12[i][b];
+          }
+        sm.det1[threadIdx.x] = G.det1;
+        sm.det2[threadIdx.x] = G.det2;
+        T c = 0;
+        for (int pp = 0; pp < form.npatch; pp++) c += G.coef[pp];
+        sm.c[threadIdx.x] = c;
+#pragma unroll
+        for (int v = 0; v <= D; v++) {
+          sm.gv1[v][threadIdx.x] = G.gv1[v];
+          sm.gv2[v][threadIdx.x] = G.gv2[v];
+        }
+      }
+    }
+    __syncthreads();
+    const bool live = sm.idx[f] >= 0;
+    // images of the canonical nodes under the barycentric maps
+    for (int u = u0; u < 2 * N; u += NU) {
+      const int sd = u / N, n = u % N;
+      if (!live) continue;
+      T out[D + 1];
+      node_image<D, K, T>(n, &sm.L[sd][0][0][f], (D + 1) * F, F, out);
+#pragma unroll
+      for (int i = 0; i <= D; i++) sm.nodes[sd][n][i][f] = out[i];
+    }
+    __syncthreads();
+    // column j of C: function j of the other element in this element's canonical basis
+    for (int u = u0; u < 2 * N; u += NU) {
+      const int sd = u / N, j = u % N;
+      if (!live) continue;
+      int gv[4] = {0, 0, 0, 0};
+#pragma unroll
+      for (int v = 0; v <= D; v++) gv[v] = sd == 0 ? sm.gv2[v][f] : sm.gv1[v][f];
+      const int desc = fn_desc<D, K>(j, gv);
+      T p[N];
+#pragma unroll
+      for (int n = 0; n < N; n++) {
+        T lam[D + 1];
+#pragma unroll
+        for (int i = 0; i <= D; i++) lam[i] = sm.nodes[sd][n][i][f];
+        p[n] = eval_fn_value<D, T>(desc, lam);
+      }
+      nodal_to_hier<D, K, T>(p, fn_degree(desc), &sm.Ct[sd][0][j][f], N * F);
+    }
+    __syncthreads();
+    // W = Mh C over the rows of degree <= the column's degree (the others are 0)
+    for (int u = u0; u < 2 * N * N; u += NU) {
+      const int r = u % N, j = (u / N) % N, sd = u / (N * N);
+      if (!live) continue;
+      const int nk = sm.cnt[canon_degree<D, K>(j)];
+      T s = 0;
+      for (int i = 0; i < nk; i++) {
+        const int k = sm.perm[i];
+        s += sm.Mh[r][k] * sm.Ct[sd][k][j][f];
+      }
+      sm.Wt[sd][r][j][f] = s;
+    }
+    __syncthreads();
+    if (!live) continue;
+    const int idx = sm.idx[f];
+    const T det1 = sm.det1[f], det2 = sm.det2[f], c = sm.c[f];
+    for (int k = u0; k < E; k += NU) {
+      const int a = sm.ep[k], b = sm.eq[k];
+      Acc<T> v;
+      v.init();
+      if (b < N) {  // (1,1)
+        int g1[4] = {0, 0, 0, 0};
+#pragma unroll
+        for (int q = 0; q <= D; q++) g1[q] = sm.gv1[q][f];
+        const bool flip = K == 3 && fn_sign<D, K>(a, g1) != fn_sign<D, K>(b, g1);
+        v.add(det1 * neg_if(sm.Mh[a][b], flip));
+        const int nk = sm.cnt[canon_degree<D, K>(a)];
+        T s = 0;
+        for (int i = 0; i < nk; i++) {
+          const int kk = sm.perm[i];
+          s += sm.Ct[1][kk][a][f] * sm.Wt[1][kk][b][f];
+        }
+        v.add(det2 * s);
+      } else if (a < N) {  // (1,2)
+        const int bb = b - N;
+        int g1[4] = {0, 0, 0, 0}, g2[4] = {0, 0, 0, 0};
+#pragma unroll
+        for (int q = 0; q <= D; q++) {
+          g1[q] = sm.gv1[q][f];
+          g2[q] = sm.gv2[q][f];
+        }
+        const T w1 = neg_if(sm.Wt[0][a][bb][f], K == 3 && fn_sign<D, K>(a, g1) < 0);
+        const T w2 = neg_if(sm.Wt[1][bb][a][f], K == 3 && fn_sign<D, K>(bb, g2) < 0);
+        v.add(neg_if(det1 * w1, true));
+        v.add(neg_if(det2 * w2, true));
+      } else {  // (2,2)
+        const int aa = a - N, bb = b - N;
+        const int nk = sm.cnt[canon_degree<D, K>(aa)];
+        T s = 0;
+        for (int i = 0; i < nk; i++) {
+          const int kk = sm.perm[i];
+          s += sm.Ct[0][kk][aa][f] * sm.Wt[0][kk][bb][f];
+        }
+        v.add(det1 * s);
+        int g2[4] = {0, 0, 0, 0};
+#pragma unroll
+        for (int q = 0; q <= D; q++) g2[q] = sm.gv2[q][f];
+        const bool flip = K == 3 && fn_sign<D, K>(aa, g2) != fn_sign<D, K>(bb, g2);
+        v.add(det2 * neg_if(sm.Mh[aa][bb], flip));
+      }
+      const T r = c * v.get();
+      if (!finite_bits(r)) set_err(err, XG_ERR_NONFINITE);
+      famat[(int64_t)idx * E + k] = r;
     }
   }
 }
@@ -2105,6 +2316,9 @@ struct xg_form {
   int64_t mu_MT = 0;
   size_t mo_smem = 0;
   int grid_mo = 0, grid_en = 0;
+  bool patch_exact = false;     // every patch term integrates exactly: basis-change patch kernel
+  void* d_mhat = nullptr;       // reference mass matrix of the canonical basis (kernel precision)
+  int grid_px = 0;
   int64_t nw32_el = 0, nw32_fa = 0, nw32_dof = 0;
   int64_t cap_el = 0, cap_fa = 0;
   // workspace
@@ -2167,7 +2381,7 @@ int form_free(xg_form* f) {
                   f->d_tabs, f->d_act_un, f->d_act_cut, f->d_act_fa, f->d_dof_bits, f->d_l_un, f->d_l_cut, f->d_l_fa,
                   f->d_el_slot, f->d_fa_slot, f->d_dof_row, f->d_rowcnt, f->d_counts, f->d_bsum, f->d_bsum64,
                   f->d_elmat, f->d_famat, f->d_err, f->d_dom, f->d_ratio, f->d_bits, f->d_fbits,
-                  f->d_mtab_i, f->d_mtab_c, f->d_mu};
+                  f->d_mtab_i, f->d_mtab_c, f->d_mu, f->d_mhat};
   for (void* p : ptrs) cudaFree(p);
   delete f;
   return XG_OK;
@@ -2391,7 +2605,70 @@ void build_moment_desc(xg_form* f) {
   f->mo_smem = (size_t)kMomPts * (md.NA + md.NB) * (f->precision == XG_PREC_FP64 ? 8 : 4);
 }
 
+// Reference mass matrix of the canonical basis (unit |det F|) for the
+// basis-change patch kernel, when every patch term's rule is exact (order >= 2K).
+template <int D, int K>
+std::vector<double> reference_mass() {
+  constexpr int N = ndof_el(D, K);
+  const RuleTable& R = host_rules();
+  const int p = clamp_order(2 * K), off = R.off[D][p], cnt = R.cnt[D][p];
+  int gv[4] = {0, 1, 2, 3};
+  std::vector<double> M((size_t)N * N, 0.0);
+  for (int x = 0; x < cnt; x++) {
+    double lam[D + 1], s = 0;
+    for (int a = 0; a < D; a++) {
+      lam[a] = R.x[off + x][a];
+      s += lam[a];
+    }
+    lam[D] = 1.0 - s;
+    double phi[N];
+    for (int i = 0; i < N; i++) phi[i] = eval_fn_value<D, double>(fn_desc<D, K>(i, gv), lam);
+    for (int i = 0; i < N; i++)
+      for (int j = 0; j < N; j++) M[(size_t)i * N + j] += R.w[off + x] * phi[i] * phi[j];
+  }
+  return M;
+}
+
+template <class K>
+int grid_for(K kernel, int threads, size_t smem);
+
+template <int D, int K, typename T>
+int patch_exact_setup(xg_form* f) {
+  auto kx = k_patch_exact<D, K, T>;
+  const size_t smem = sizeof(PxSmem<D, K, T>);
+  XG_CUDA(cudaFuncSetAttribute(kx, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  f->grid_px = grid_for(kx, PxCfg<D, K>::NT, smem);
+  return XG_OK;
+}
+
+template <typename T>
+int patch_exact_setup_t(xg_form* f) {
+  const int D = f->mesh->dim, K = f->space->order;
+  if (D == 2) return K == 1 ? patch_exact_setup<2, 1, T>(f) : (K == 2 ? patch_exact_setup<2, 2, T>(f) : patch_exact_setup<2, 3, T>(f));
+  return K == 1 ? patch_exact_setup<3, 1, T>(f) : (K == 2 ? patch_exact_setup<3, 2, T>(f) : patch_exact_setup<3, 3, T>(f));
+}
+
+int upload_patch_tables(xg_form* f) {
+  const int D = f->mesh->dim, K = f->space->order;
+  f->patch_exact = f->has_patch;
+  for (int pp = 0; pp < f->desc.npatch; pp++)
+    if (clamp_order(f->desc.p[pp].order) < 2 * K) f->patch_exact = false;
+  cudaFree(f->d_mhat);
+  f->d_mhat = nullptr;
+  if (!f->patch_exact) return XG_OK;
+  std::vector<double> M;
+  if (D == 2) M = K == 1 ? reference_mass<2, 1>() : (K == 2 ? reference_mass<2, 2>() : reference_mass<2, 3>());
+  else M = K == 1 ? reference_mass<3, 1>() : (K == 2 ? reference_mass<3, 2>() : reference_mass<3, 3>());
+  const bool fp64 = f->precision == XG_PREC_FP64;
+  std::vector<float> M32(M.begin(), M.end());
+  XG_CUDA(cudaMalloc(&f->d_mhat, M.size() * (fp64 ? 8 : 4)));
+  XG_CUDA(cudaMemcpy(f->d_mhat, fp64 ? (const void*)M.data() : (const void*)M32.data(), M.size() * (fp64 ? 8 : 4),
+                     cudaMemcpyHostToDevice));
+  return fp64 ? patch_exact_setup_t<double>(f) : patch_exact_setup_t<float>(f);
+}
+
 int upload_moment_tables(xg_form* f) {
+  if (int st = upload_patch_tables(f)) return st;
   build_moment_desc(f);
   const int D = f->mesh->dim, K = f->space->order;
   const bool sym = f->el_sym;
@@ -2565,7 +2842,14 @@ int launch_patch(xg_form* f, cudaStream_t s) {
   PaGeoS<D, T>* pg = (PaGeoS<D, T>*)f->d_pgeo;
   k_patch_geo<D, T><<<152 * 8, 128, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, m->nfacets, m->d_facet_els, f->desc,
                                          f->d_l_fa, f->d_counts, pg, f->cap_fa, f->d_err);
-  kp<<<f->grid_fa, C::NT, 0, s>>>(f->desc, pg, f->d_counts, (T*)f->d_famat, f->cap_fa, f->d_err);
+  if (f->patch_exact) {
+    auto kx = k_patch_exact<D, K, T>;
+    const size_t smem = sizeof(PxSmem<D, K, T>);
+    kx<<<f->grid_px, PxCfg<D, K>::NT, smem, s>>>(f->desc, pg, f->d_counts, (const T*)f->d_mhat, (T*)f->d_famat,
+                                                 f->cap_fa, f->d_err);
+  } else {
+    kp<<<f->grid_fa, C::NT, 0, s>>>(f->desc, pg, f->d_counts, (T*)f->d_famat, f->cap_fa, f->d_err);
+  }
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? XG_OK : cuda_fail(e, "k_patch");
 }

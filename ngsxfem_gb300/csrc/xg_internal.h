@@ -41,6 +41,20 @@ inline int clamp_order(int p) { return p < 0 ? 0 : (p > kMaxOrder ? kMaxOrder : 
 __device__ __forceinline__ void set_err(int* err, int code) {
   if (err) atomicCAS(err, 0, code);
 }
+
+// finiteness and sign flips on the bit pattern (integer pipe; the FP64 pipe of
+// GB300 is narrow and also issues comparisons and negations)
+__device__ __forceinline__ bool finite_bits(double v) {
+  return ((__double_as_longlong(v) >> 52) & 0x7ff) != 0x7ff;
+}
+__device__ __forceinline__ bool finite_bits(float v) { return ((__float_as_int(v) >> 23) & 0xff) != 0xff; }
+__device__ __forceinline__ double neg_if(double v, bool c) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v) ^ ((unsigned long long)c << 63);
+  return __longlong_as_double((long long)b);
+}
+__device__ __forceinline__ float neg_if(float v, bool c) {
+  return __uint_as_float(__float_as_uint(v) ^ ((unsigned)c << 31));
+}
 #endif
 
 // ---- errors ----------------------------------------------------------------------

@@ -195,6 +195,9 @@ FORMS = {
                        dict(kind=orc.TERM_GHOST_MASS, coef=0.1, hpow=-2)],
     "conv_pos": lambda orc: [dict(kind=orc.TERM_CONV, domain=orc.POS, b=(1.0, -0.5, 0.25)),
                              dict(kind=orc.TERM_MASS, domain=orc.POS)],
+    # a ghost-penalty rule below the integrand degree: the quadrature patch kernel
+    "ghost_low": lambda orc: [dict(kind=orc.TERM_LAPLACE, domain=orc.NEG),
+                              dict(kind=orc.TERM_GHOST_MASS, coef=0.1, hpow=-2, order=1)],
 }
 
 
