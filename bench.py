@@ -525,8 +525,31 @@ class Clocks:
 # DRAM bytes (read + write) per launch of the dominant kernel from one ncu
 # capture of the same workload (profiles/cutfem_step_3d_poisson_64cube_p2_fp64.md,
 # profiles/st_elmat_spacetime_256sq_p1p1_fp64.md)
-TRAFFIC = {("c2", "patch"): 4.921344e6 + 43.072256e6, ("c2", "scatter"): 660.390144e6 + 103.535104e6,
-           ("c2", "elmat_cut"): 6.448640e6 + 0.466944e6}
+TRAFFIC = {("c2", "patch"): 34.761216e6 + 47.612416e6, ("c2", "scatter"): 839.305216e6 + 102.750464e6,
+           ("c2", "elmat_cut"): 28.007168e6 + 0.047104e6 + 33.647360e6 + 0.001024e6}
+
+
+def patch_exact_flops(dim, k):
+    """FP64 operations of one facet patch in the basis-change kernel as
+    executed: the node images (2 (D+1)^2 per node and side), the columns of
+    both basis changes (an evaluation of about 3 operations per function and
+    node, about 4 per coefficient of the hierarchical solve), W = Mh C over the
+    rows of degree <= the column's degree, and the entries (block sums over
+    the same rows, 4 more per diagonal-block entry, 4 per coupling entry)."""
+    n = (k + 1) * (k + 2) // 2 if dim == 2 else (k + 1) * (k + 2) * (k + 3) // 6
+    nedge = 3 if dim == 2 else 6
+    deg = [1] * (dim + 1)
+    if k == 2:
+        deg += [2] * nedge
+    elif k == 3:
+        deg += [2, 3] * nedge + [3] * (1 if dim == 2 else 4)
+    cnt = {d: sum(1 for x in deg if x <= d) for d in (1, 2, 3)}
+    nodes = 2 * n * 2 * (dim + 1) * (dim + 1) / (dim + 1)
+    cols = 2 * n * (3 * n + 4 * n)
+    w = 2 * n * sum(2 * cnt[deg[j]] for j in range(n))
+    blocks = 2 * sum((n - a) * (2 * cnt[deg[a]] + 4) for a in range(n))
+    cross = n * n * 4
+    return nodes + cols + w + blocks + cross
 
 
 def fp64_peak(torch):
@@ -895,25 +918,26 @@ def main():
     dname = names[dom_i]
     achieved = alg[dname] / (stage_ms[dom_i] * 1e-3) / 1e9
     step_bytes = sum(alg.values())
-    # the FP64 element kernels run on the FP64 pipe: FLOPs of the patch stage as
-    # executed (the packed upper triangle of the (2n)^2 patch matrix, one FMA =
-    # 2 FLOPs per entry and point, 2 x NQ(2k) points per facet: the order-2k
-    # rule on both elements); the full-matrix count sum_q 2 (2n)^2 is reported
-    # beside it
+    # the FP64 element kernels run on the FP64 pipe.  Patch stage of a spatial
+    # form: FLOPs of the basis-change kernel as executed (patch_exact_flops);
+    # space-time patches use the quadrature kernel: the packed upper triangle
+    # of the (2n)^2 patch matrix, one FMA = 2 FLOPs per entry and point,
+    # 2 x NQ(2k) points per facet
     fp64 = None
     if dname == "patch" and gpu.prec == 0:
         nq = {(2, 2): 3, (2, 4): 6, (2, 6): 16, (3, 2): 4, (3, 4): 14, (3, 6): 64}
-        flops, flops_full = 0.0, 0.0
+        flops = 0.0
         for e in E:
             k = e["order"]
-            nd = e["ndof_el"] if not e["st"] else e["ndof_el"] // 2  # patches are spatial (P1 x P1 in time)
-            pts = e["n_facets"] * 2 * nq[(e["dim"], 2 * k)]
-            flops += pts * 2 * (2 * nd) * (2 * nd + 1) / 2
-            flops_full += pts * 2 * (2 * nd) ** 2
+            if e["st"]:
+                nd = e["ndof_el"] // 2  # patches are spatial (P1 x P1 in time)
+                flops += e["n_facets"] * 2 * nq[(e["dim"], 2 * k)] * 2 * (2 * nd) * (2 * nd + 1) / 2
+            else:
+                flops += e["n_facets"] * patch_exact_flops(e["dim"], k)
         peak_fp64 = fp64_peak(torch)
         ach = flops / (stage_ms[dom_i] * 1e-3) / 1e12
         fp64 = {"bound": "fp64", "kernel": dname, "achieved": ach, "peak": peak_fp64, "unit": "TFLOP/s",
-                "frac": ach / peak_fp64, "flops_per_step": flops, "flops_full_matrix_per_step": flops_full,
+                "frac": ach / peak_fp64, "flops_per_step": flops,
                 "peak_source": "measured here: cuBLAS DGEMM 4096^3 (torch.matmul float64), best of 3"}
     cfg.update({
         "n_tets_or_tris": int(sum(e["ne"] for e in E)), "n_cut": n_cut, "n_neg_uncut": sum(e["n_neg"] for e in E),

@@ -432,7 +432,8 @@ __global__ void __launch_bounds__(256) k_elmat_uncut(int ne, int nv, const int32
           for (int kk = 0; kk < 5; kk++) {
             const int hp = form.g[q].hpow[kk];
             if (hp != 0 && h < 0) h = pow(G.meas, 1.0 / D);
-            G.coef[q][kk] = hp == 0 ? form.g[q].c[kk] : form.g[q].c[kk] * pow(h, (double)hp);
+            // |det F| folded into the coefficients
+            G.coef[q][kk] = (hp == 0 ? form.g[q].c[kk] : form.g[q].c[kk] * pow(h, (double)hp)) * G.meas;
           }
           if (form.g[q].used & (1 << XG_TERM_CONV))
 #pragma unroll
@@ -468,9 +469,8 @@ __global__ void __launch_bounds__(256) k_elmat_uncut(int ne, int nv, const int32
           v += G.coef[q][4] * s;
         }
       }
-      v *= G.meas;
-      if (K == 3) v *= (double)(fn_sign<D, K>(ep[k], G.gv) * fn_sign<D, K>(eq[k], G.gv));
-      if (!isfinite(v)) set_err(err, XG_ERR_NONFINITE);
+      if (K == 3) v = neg_if(v, fn_sign<D, K>(ep[k], G.gv) != fn_sign<D, K>(eq[k], G.gv));
+      if (!finite_bits(v)) set_err(err, XG_ERR_NONFINITE);
       elmat[(int64_t)G.slot * E + k] = (T)v;
     }
   }
@@ -1114,8 +1114,8 @@ __global__ void __launch_bounds__(kEntNT) k_cut_entries(FormDesc form, MomDesc m
         if (used & (1 << XG_TERM_U_NGRADV)) v.add(tab_sum_w<T>(tabs.ptr[3], tabs.idx[3], cf[3], k, m, S.wdp[q]));
       }
       T r = v.get();
-      if (K == 3 && fn_sign<D, K>(ep[k], S.gv) * fn_sign<D, K>(eq[k], S.gv) < 0) r = -r;
-      if (!isfinite(r)) set_err(err, XG_ERR_NONFINITE);
+      if (K == 3) r = neg_if(r, fn_sign<D, K>(ep[k], S.gv) != fn_sign<D, K>(eq[k], S.gv));
+      if (!finite_bits(r)) set_err(err, XG_ERR_NONFINITE);
       elmat[(int64_t)S.slot * E + k] = r;
     }
   }

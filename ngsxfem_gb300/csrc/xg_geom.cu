@@ -42,47 +42,79 @@ __global__ void k_perturb(double* v, int64_t n, double eps) {
 // One thread per element, 32 elements per warp; the warp's ballots are the
 // 32-bit words of the 8 combined-domain bitsets.
 template <int D>
-__global__ void k_cutinfo(int ne, const int32_t* __restrict__ elv, const double* __restrict__ lset,
-                          uint8_t* __restrict__ dom, double* __restrict__ ratio, uint32_t* __restrict__ bits,
-                          int64_t nw32, int* err) {
+__global__ void __launch_bounds__(256) k_cutinfo(int ne, const int32_t* __restrict__ elv,
+                                                 const double* __restrict__ lset, uint8_t* __restrict__ dom,
+                                                 double* __restrict__ ratio, uint32_t* __restrict__ bits, int64_t nw32,
+                                                 int* err) {
+  // Sign classes first (integer tests on the bit patterns); the elements whose
+  // signs differ are compacted per block and take the order-0 cut rules
+  // densely, so no warp runs the FP64 rule path with a few active lanes.
+  // Uncut elements get ratio 1 (NEG) or 0 (POS), the exact value of
+  // NEG / (NEG + POS) with one part empty.
+  __shared__ int cut_list[256];
+  __shared__ int ncut;
+  __shared__ uint8_t tsm[256];
   const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
   const bool valid = e < ne;
-  int t = XG_POS;
+  int cdom = XG_POS;
   if (valid) {
     double l[D + 1];
 #pragma unroll
     for (int i = 0; i <= D; i++) l[i] = __ldg(&lset[__ldg(&elv[(int64_t)i * ne + e])]);
-    const double w0 = c_rules.w[c_rules.off[D][0]];
-    double part_vol[2] = {0.0, 0.0};
-    int cdom = check_if_straight_cut(l, D + 1);
-    if (cdom == XG_IF) {
-      // order-0 cut rules for POS then NEG, weights summed in rule order
+    cdom = check_if_straight_cut(l, D + 1);
+  }
+  if (threadIdx.x == 0) ncut = 0;
+  tsm[threadIdx.x] = (uint8_t)XG_POS;
+  __syncthreads();
+  const bool is_cut = valid && cdom == XG_IF;
+  const unsigned mc = __ballot_sync(0xffffffffu, is_cut);
+  int base = 0;
+  if (lane == 0 && mc) base = atomicAdd(&ncut, __popc(mc));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (is_cut) cut_list[base + __popc(mc & ((1u << lane) - 1))] = threadIdx.x;
+  if (valid && !is_cut) {
+    dom[e] = (uint8_t)cdom;
+    ratio[e] = cdom == XG_NEG ? 1.0 : 0.0;
+    tsm[threadIdx.x] = (uint8_t)cdom;
+  }
+  __syncthreads();
+  const int nc = ncut;
+  for (int k = threadIdx.x; k < nc; k += blockDim.x) {
+    const int tl = cut_list[k];
+    const int64_t ec = blockIdx.x * (int64_t)blockDim.x + tl;
+    double l[D + 1];
 #pragma unroll
-      for (int pass = 0; pass < 2; pass++) {
-        const int np = pass == 0 ? XG_POS : XG_NEG;
-        Sub subs[3];
-        int ns = decompose<D>(l, np, subs);
-        if (ns < 0) {
-          set_err(err, -ns);
-          ns = 0;
-        }
-        const double wb = c_rules.w[c_rules.off[D][0]];
-        for (int s = 0; s < ns; s++) part_vol[np] += wb * simplex_volume(subs[s].p, D + 1);
+    for (int i = 0; i <= D; i++) l[i] = __ldg(&lset[__ldg(&elv[(int64_t)i * ne + ec])]);
+    // order-0 cut rules for POS then NEG, weights summed in rule order
+    double part_vol[2] = {0.0, 0.0};
+#pragma unroll
+    for (int pass = 0; pass < 2; pass++) {
+      const int np = pass == 0 ? XG_POS : XG_NEG;
+      Sub subs[3];
+      int ns = decompose<D>(l, np, subs);
+      if (ns < 0) {
+        set_err(err, -ns);
+        ns = 0;
       }
-    } else {
-      part_vol[cdom] += w0;
+      const double wb = c_rules.w[c_rules.off[D][0]];
+      for (int s = 0; s < ns; s++) part_vol[np] += wb * simplex_volume(subs[s].p, D + 1);
     }
-    ratio[e] = part_vol[XG_NEG] / (part_vol[XG_NEG] + part_vol[XG_POS]);
+    ratio[ec] = part_vol[XG_NEG] / (part_vol[XG_NEG] + part_vol[XG_POS]);
+    int t;
     if (part_vol[XG_NEG] > 0.0) t = (part_vol[XG_POS] > 0.0) ? XG_IF : XG_NEG;
     else t = XG_POS;
-    dom[e] = (uint8_t)t;
+    dom[ec] = (uint8_t)t;
+    tsm[tl] = (uint8_t)t;
   }
+  __syncthreads();
+  const int t = tsm[threadIdx.x];
   const unsigned mneg = __ballot_sync(0xffffffffu, valid && t == XG_NEG);
   const unsigned mpos = __ballot_sync(0xffffffffu, valid && t == XG_POS);
   const unsigned mif = __ballot_sync(0xffffffffu, valid && t == XG_IF);
   const unsigned many = __ballot_sync(0xffffffffu, valid);
   const int64_t w = e >> 5;
-  if ((threadIdx.x & 31) == 0 && w < nw32) {
+  if (lane == 0 && w < nw32) {
     bits[0 * nw32 + w] = 0u;
     bits[1 * nw32 + w] = mneg;
     bits[2 * nw32 + w] = mpos;
