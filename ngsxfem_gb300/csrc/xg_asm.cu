@@ -9,6 +9,7 @@
 //   RestrictedBilinearForm graph / Restrict()                  utils/restrictedblf.cpp:7-168
 #include <algorithm>
 #include <array>
+#include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <map>
@@ -261,15 +262,22 @@ __global__ void k_active_elements(int ne, const uint8_t* __restrict__ dom, FormD
   }
 }
 
-// space-time forms: an element is active if a volume group contains it
-__global__ void k_active_st(int ne, StFormDesc form, uint32_t* bits, int64_t nw32) {
+// space-time forms: an element is active if a volume group contains it; the
+// elements uncut in the slab (NEG or POS over the whole slab) and the cut ones
+// go to separate lists
+__global__ void k_active_st(int ne, const uint8_t* __restrict__ dom, StFormDesc form, uint32_t* uncut_bits,
+                            uint32_t* cut_bits, int64_t nw32) {
   const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   bool act = false;
   if (e < ne)
     for (int g = 0; g < form.ngroups; g++)
       if (!form.g[g].defined_on || tbit(form.g[g].defined_on, e)) act = true;
-  const unsigned m = __ballot_sync(0xffffffffu, act);
-  if ((threadIdx.x & 31) == 0 && (e >> 5) < nw32) bits[e >> 5] = m;
+  const bool cut = act && dom[e] == XG_IF;
+  const unsigned mu = __ballot_sync(0xffffffffu, act && !cut), mc = __ballot_sync(0xffffffffu, cut);
+  if ((threadIdx.x & 31) == 0 && (e >> 5) < nw32) {
+    uncut_bits[e >> 5] = mu;
+    cut_bits[e >> 5] = mc;
+  }
 }
 
 __global__ void k_active_facets(int64_t nf, const int32_t* __restrict__ fel, FormDesc form, uint32_t* bits,
@@ -470,6 +478,133 @@ __global__ void __launch_bounds__(256) k_elmat_uncut(int ne, int nv, const int32
         }
       }
       if (K == 3) v = neg_if(v, fn_sign<D, K>(ep[k], G.gv) != fn_sign<D, K>(eq[k], G.gv));
+      if (!finite_bits(v)) set_err(err, XG_ERR_NONFINITE);
+      elmat[(int64_t)G.slot * E + k] = (T)v;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Space-time elements uncut in the slab (NEG or POS at every time of the
+// slab): the space-time rule is the time rule times the spatial standard rule
+// (cutint/spacetimecutrule.cpp:106-244 with one time interval and a
+// sign-definite level set at every time point), so with Phi = psi_a(tau) phi_j
+//   mass     sum_t w psi_a psi_b      x  spatial mass table
+//   laplace  sum_t w psi_a psi_b      x  sum_ab G_ab x gradient-pair tables
+//   conv     sum_r beta_r x convection tables,  beta = F^-1 sum_t w psi_a psi_b b(t)
+//   dt       sum_t w psi_a psi_b'     x  spatial mass table
+// (fixed-time groups: the single time tref with weight 1) -- the same sums,
+// reassociated.  The time sums are built on the host with the form's time rule.
+// ---------------------------------------------------------------------------
+struct StTimeTabs {
+  double tm[kMaxGroups][9];     // sum_t w psi_a psi_b  (a test, b trial time index)
+  double td[kMaxGroups][9];     // sum_t w psi_a psi_b'
+  double tb[kMaxGroups][9][3];  // sum_t w psi_a psi_b b(t)
+};
+
+template <int D, int KT>
+struct StUnGeoS {
+  double G[D * (D + 1) / 2];
+  double beta[kMaxGroups][(KT + 1) * (KT + 1)][D];
+  double coef[kMaxGroups][7];
+  int elem, slot, dom;
+};
+
+template <int D, int K, int KT, typename T>
+__global__ void __launch_bounds__(256) k_st_elmat_uncut(int ne, int nv, const int32_t* __restrict__ elv,
+                                                         const double* __restrict__ xyz,
+                                                         const uint8_t* __restrict__ dom, StFormDesc form,
+                                                         UncutTabs tabs, StTimeTabs tt,
+                                                         const int32_t* __restrict__ list,
+                                                         const int* __restrict__ counts, T* __restrict__ elmat,
+                                                         int* err) {
+  constexpr int NS = ndof_el(D, K), N = NS * (KT + 1), E = N * N, ES = NS * NS, NTT = (KT + 1) * (KT + 1);
+  constexpr int NG = D * (D + 1) / 2, EPB = (D == 3 || KT == 2) ? 16 : 32;
+  __shared__ StUnGeoS<D, KT> geo[EPB];
+  const int count = counts[0];
+  for (int batch = blockIdx.x; batch * EPB < count; batch += gridDim.x) {
+    __syncthreads();
+    if (threadIdx.x < EPB) {
+      StUnGeoS<D, KT>& G = geo[threadIdx.x];
+      const int idx = batch * EPB + threadIdx.x;
+      G.elem = idx < count ? list[idx] : -1;
+      G.slot = idx;
+      if (G.elem >= 0) {
+        const int e = G.elem;
+        double xv[D + 1][3];
+#pragma unroll
+        for (int v = 0; v <= D; v++) {
+          const int vid = elv[(int64_t)v * ne + e];
+#pragma unroll
+          for (int c = 0; c < 3; c++) xv[v][c] = c < D ? xyz[(int64_t)c * nv + vid] : 0.0;
+        }
+        Geo<D> g;
+        make_geo<D>(xv, g);
+        const double meas = fabs(g.det);
+        int k = 0;
+#pragma unroll
+        for (int a = 0; a < D; a++)
+#pragma unroll
+          for (int b = a; b < D; b++) {
+            double s = 0;
+#pragma unroll
+            for (int c = 0; c < D; c++) s += g.Finv[a][c] * g.Finv[b][c];
+            G.G[k++] = s;
+          }
+        G.dom = dom[e];
+        double h = -1.0;
+        for (int q = 0; q < form.ngroups; q++) {
+          const StGroupDesc& Gq = form.g[q];
+          for (int kk = 0; kk < 7; kk++) {
+            const int hp = Gq.hpow[kk];
+            if (hp != 0 && h < 0) h = pow(meas, 1.0 / D);
+            // |det F| folded into the coefficients
+            G.coef[q][kk] = (hp == 0 ? Gq.c[kk] : Gq.c[kk] * pow(h, (double)hp)) * meas;
+          }
+          if (Gq.used & (1 << XG_TERM_CONV))
+            for (int ti = 0; ti < NTT; ti++)
+#pragma unroll
+              for (int a = 0; a < D; a++) {
+                double s = 0;
+#pragma unroll
+                for (int c = 0; c < D; c++) s += g.Finv[a][c] * tt.tb[q][ti][c];
+                G.beta[q][ti][a] = s;
+              }
+        }
+      }
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < EPB * E; t += blockDim.x) {
+      const int le = t / E, k = t - le * E;
+      const StUnGeoS<D, KT>& G = geo[le];
+      if (G.elem < 0) continue;
+      const int pp = k / N, qv = k - pp * N;
+      const int ta = pp / NS, sj = pp - ta * NS, tb = qv / NS, sk = qv - tb * NS;
+      const int ks = sj * NS + sk, ti = ta * (KT + 1) + tb;
+      double v = 0.0;
+      for (int q = 0; q < form.ngroups; q++) {
+        const StGroupDesc& Gq = form.g[q];
+        if (Gq.domain != G.dom || (Gq.defined_on && !tbit(Gq.defined_on, G.elem))) continue;
+        const int used = Gq.used;
+        if (used & ((1 << XG_TERM_MASS) | (1 << 6))) {
+          double c = 0.0;
+          if (used & (1 << XG_TERM_MASS)) c += G.coef[q][XG_TERM_MASS] * tt.tm[q][ti];
+          if (used & (1 << 6)) c += G.coef[q][6] * tt.td[q][ti];
+          v += c * __ldg(&tabs.m[q][ks]);
+        }
+        if (used & (1 << XG_TERM_LAPLACE)) {
+          double s = 0;
+#pragma unroll
+          for (int a = 0; a < NG; a++) s += G.G[a] * __ldg(&tabs.t[q][a * ES + ks]);
+          v += G.coef[q][XG_TERM_LAPLACE] * tt.tm[q][ti] * s;
+        }
+        if (used & (1 << XG_TERM_CONV)) {
+          double s = 0;
+#pragma unroll
+          for (int a = 0; a < D; a++) s += G.beta[q][ti][a] * __ldg(&tabs.c[q][a * ES + ks]);
+          v += G.coef[q][XG_TERM_CONV] * s;
+        }
+      }
       if (!finite_bits(v)) set_err(err, XG_ERR_NONFINITE);
       elmat[(int64_t)G.slot * E + k] = (T)v;
     }
@@ -2368,6 +2503,7 @@ struct xg_form {
   // space-time forms
   bool st = false;
   StFormDesc stdesc = {};
+  StTimeTabs st_tt = {};  // time sums of the uncut space-time kernel
   std::vector<xg_st_term> st_terms;
   double mt[9] = {1, 0, 0, 0, 0, 0, 0, 0, 0};  // time mass of the time rule (patch factor)
 };
@@ -2742,6 +2878,99 @@ int upload_moment_tables(xg_form* f) {
     f->mu_MT = f->md.MT;
   }
   return XG_OK;
+}
+
+// Tables of the uncut space-time kernel: the spatial reference tables of
+// every group (the mass table also serves the d/dtau term) and the time sums
+// of the form's time rule (or of the fixed time tref).
+int st_uncut_tables(xg_form* f) {
+  const StFormDesc& d = f->stdesc;
+  const int D = f->mesh->dim, K = f->space->order, kt = f->space->kt;
+  FormDesc tmp;
+  std::memset(&tmp, 0, sizeof(tmp));
+  tmp.ngroups = d.ngroups;
+  for (int q = 0; q < d.ngroups; q++) {
+    const int used = d.g[q].used;
+    tmp.g[q].domain = d.g[q].domain;
+    tmp.g[q].order = d.g[q].order;
+    int u = 0;
+    if (used & ((1 << XG_TERM_MASS) | (1 << XG_TERM_DT_U_V))) u |= 1 << XG_TERM_MASS;
+    if (used & (1 << XG_TERM_LAPLACE)) u |= 1 << XG_TERM_LAPLACE;
+    if (used & (1 << XG_TERM_CONV)) u |= 1 << XG_TERM_CONV;
+    tmp.g[q].used = u;
+  }
+  size_t offs[kMaxGroups][3];
+  std::vector<double> buf;
+  if (D == 2) buf = K == 1 ? uncut_tables<2, 1>(tmp, false, offs) : uncut_tables<2, 2>(tmp, false, offs);
+  else buf = K == 1 ? uncut_tables<3, 1>(tmp, false, offs) : uncut_tables<3, 2>(tmp, false, offs);
+  cudaFree(f->d_tabs);
+  f->d_tabs = nullptr;
+  std::memset(&f->tabs, 0, sizeof(f->tabs));
+  if (!buf.empty()) {
+    XG_CUDA(cudaMalloc((void**)&f->d_tabs, buf.size() * sizeof(double)));
+    XG_CUDA(cudaMemcpy(f->d_tabs, buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice));
+    for (int q = 0; q < d.ngroups; q++) {
+      f->tabs.m[q] = offs[q][0] == (size_t)-1 ? nullptr : f->d_tabs + offs[q][0];
+      f->tabs.t[q] = offs[q][1] == (size_t)-1 ? nullptr : f->d_tabs + offs[q][1];
+      f->tabs.c[q] = offs[q][2] == (size_t)-1 ? nullptr : f->d_tabs + offs[q][2];
+    }
+  }
+  StTimeTabs& T = f->st_tt;
+  std::memset(&T, 0, sizeof(T));
+  const RuleTable& R = host_rules();
+  const int pt = clamp_order(d.order_time), offt = R.off[1][pt], nqt = R.cnt[1][pt];
+  for (int q = 0; q < d.ngroups; q++) {
+    const StGroupDesc& G = d.g[q];
+    const bool fixed = G.tref >= 0.0;
+    const int np = fixed ? 1 : nqt;
+    for (int x = 0; x < np; x++) {
+      const double tau = fixed ? G.tref : R.x[offt + x][0], w = fixed ? 1.0 : R.w[offt + x];
+      double psi[3], dpsi[3];
+      time_basis<double>(kt, tau, psi, dpsi);
+      double bt[3] = {G.b[0], G.b[1], G.b[2]};
+      if ((G.used & (1 << XG_TERM_CONV)) && G.omega != 0.0) {
+        const double tp = G.t0 + G.dt * tau;
+        const double cs = std::cos(G.omega * tp), sn = std::sin(G.omega * tp);
+        for (int r = 0; r < 3; r++) bt[r] += G.bc[r] * cs + G.bs[r] * sn;
+      }
+      for (int a = 0; a <= kt; a++)
+        for (int b = 0; b <= kt; b++) {
+          const int ti = a * (kt + 1) + b;
+          T.tm[q][ti] += w * psi[a] * psi[b];
+          T.td[q][ti] += w * psi[a] * dpsi[b];
+          for (int r = 0; r < 3; r++) T.tb[q][ti][r] += w * psi[a] * psi[b] * bt[r];
+        }
+    }
+  }
+  return XG_OK;
+}
+
+template <int D, int K, int KT, typename T>
+int launch_st_uncut(xg_form* f, cudaStream_t s) {
+  auto kern = k_st_elmat_uncut<D, K, KT, T>;
+  if (!f->grid_el_un) f->grid_el_un = grid_for(kern, 256, 0);
+  xg_mesh* m = f->mesh;
+  StFormDesc d = f->stdesc;
+  const int64_t nw = f->nw32_el / 2;
+  for (int q = 0; q < d.ngroups; q++)
+    d.g[q].defined_on = f->d_bits + (d.g[q].domain == XG_NEG ? XG_CDOM_HASNEG
+                                                              : (d.g[q].domain == XG_IF ? XG_CDOM_IF : XG_CDOM_HASPOS)) *
+                                        nw;
+  kern<<<f->grid_el_un, 256, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, f->d_dom, d, f->tabs, f->st_tt, f->d_l_un,
+                                     f->d_counts, (T*)f->d_elmat, f->d_err);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? XG_OK : cuda_fail(e, "k_st_elmat_uncut");
+}
+
+template <typename T>
+int dispatch_st_uncut(xg_form* f, cudaStream_t s) {
+  const int D = f->mesh->dim, K = f->space->order, KT = f->space->kt;
+  if (D == 2) {
+    if (K == 1) return KT == 1 ? launch_st_uncut<2, 1, 1, T>(f, s) : launch_st_uncut<2, 1, 2, T>(f, s);
+    return KT == 1 ? launch_st_uncut<2, 2, 1, T>(f, s) : launch_st_uncut<2, 2, 2, T>(f, s);
+  }
+  if (K == 1) return KT == 1 ? launch_st_uncut<3, 1, 1, T>(f, s) : launch_st_uncut<3, 1, 2, T>(f, s);
+  return KT == 1 ? launch_st_uncut<3, 2, 1, T>(f, s) : launch_st_uncut<3, 2, 2, T>(f, s);
 }
 
 int upload_tables(xg_form* f) {
@@ -3512,7 +3741,8 @@ int xg_st_form_create(xg_space* space, int kt_lset, int order_time, const xg_st_
     }
   }
   f->el_sym = 0;
-  int st = form_workspace(f);
+  int st = st_uncut_tables(f);
+  if (!st) st = form_workspace(f);
   if (st) {
     form_free(f);
     return st;
@@ -3542,11 +3772,12 @@ int xg_st_cutfem_step(xg_form* f, const double* d_lset_st, xg_csr* out, void* st
   FormDesc pd = f->desc;
   for (int p = 0; p < pd.npatch; p++) pd.p[p].defined_on = f->d_fbits;
   if (f->use_ev) cudaEventRecord(f->ev[1], s);
-  // work lists
-  k_active_st<<<(unsigned)((f->nw32_el * 32 + 255) / 256), 256, 0, s>>>(m->ne, d, f->d_act_un, f->nw32_el);
-  XG_CUDA(cudaMemsetAsync(f->d_act_cut, 0, f->nw32_el * 4, s));
+  // work lists: elements uncut in the slab, then the cut ones (slots after the uncut ones)
+  k_active_st<<<(unsigned)((f->nw32_el * 32 + 255) / 256), 256, 0, s>>>(m->ne, f->d_dom, d, f->d_act_un,
+                                                                        f->d_act_cut, f->nw32_el);
   if ((st = compact(f, f->d_act_un, f->nw32_el, f->d_l_un, f->d_el_slot, f->d_counts + 0, s))) return st;
-  XG_CUDA(cudaMemsetAsync(f->d_counts + 1, 0, sizeof(int), s));
+  if ((st = compact(f, f->d_act_cut, f->nw32_el, f->d_l_cut, f->d_el_slot, f->d_counts + 1, s, f->d_counts + 0)))
+    return st;
   FormDesc saved = f->desc;
   f->desc = pd;
   if (f->has_patch) {
@@ -3570,16 +3801,16 @@ int xg_st_cutfem_step(xg_form* f, const double* d_lset_st, xg_csr* out, void* st
     L.xyz = m->d_xyz;
     L.lset_st = d_lset_st;
     L.desc = d;
-    L.list = f->d_l_un;
-    L.count = f->d_counts + 0;
+    L.list = f->d_l_cut;
+    L.count = f->d_counts + 1;
+    L.slot_base = f->d_counts + 0;
     L.elmat = f->d_elmat;
     L.err = f->d_err;
-    st = launch_st_elmat(L, s);
+    st = f->precision == XG_PREC_FP64 ? dispatch_st_uncut<double>(f, s) : dispatch_st_uncut<float>(f, s);
+    if (f->use_ev) cudaEventRecord(f->ev[3], s);
+    if (!st) st = launch_st_elmat(L, s);
   }
-  if (f->use_ev) {
-    cudaEventRecord(f->ev[3], s);
-    cudaEventRecord(f->ev[4], s);
-  }
+  if (f->use_ev) cudaEventRecord(f->ev[4], s);
   if (!st && f->has_patch)
     st = f->precision == XG_PREC_FP64 ? dispatch_patch<double>(f, s) : dispatch_patch<float>(f, s);
   f->desc = saved;

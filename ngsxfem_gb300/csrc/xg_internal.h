@@ -121,6 +121,7 @@ struct StLaunch {
   StFormDesc desc;
   const int32_t* list;
   const int* count;
+  const int* slot_base;  // element-matrix slot of list entry 0 (device), or null for 0
   void* elmat;
   int* err;
 };

@@ -79,6 +79,7 @@ __global__ void __launch_bounds__(StCfg<D, K, KT>::NT) k_st_elmat(int ne, int nv
                                                                    const double* __restrict__ lset_st, StFormDesc form,
                                                                    const int32_t* __restrict__ list,
                                                                    const int* __restrict__ count_ptr,
+                                                                   const int* __restrict__ slot_base,
                                                                    T* __restrict__ elmat, int* err) {
   using C = StCfg<D, K, KT>;
   constexpr int NS = C::NS, N = C::N, EPB = C::EPB, NT = C::NT, CH = C::CH, MAXC = C::MAXC, NACC = C::NACC;
@@ -92,6 +93,7 @@ __global__ void __launch_bounds__(StCfg<D, K, KT>::NT) k_st_elmat(int ne, int nv
   __shared__ T te[EPB][CH][N][4];        // w*cM*Phi, w*cL*grad(as factor), w*cC*Phi, w*cT*Phi
   __shared__ int maxpts_s;
   const int count = *count_ptr;
+  const int sbase = slot_base ? *slot_base : 0;
   const int le = threadIdx.x / N, a = threadIdx.x % N;
   const int kl = form.kt_l;
 
@@ -101,7 +103,7 @@ __global__ void __launch_bounds__(StCfg<D, K, KT>::NT) k_st_elmat(int ne, int nv
       StGeoS<D>& G = geo[threadIdx.x];
       const int idx = batch * EPB + threadIdx.x;
       G.elem = idx < count ? list[idx] : -1;
-      G.slot = idx;
+      G.slot = sbase + idx;
       if (G.elem >= 0) {
         const int e = G.elem;
         double xv[D + 1][3];
@@ -327,7 +329,8 @@ static int launch_one(const StLaunch& a, cudaStream_t s) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, C::NT, 0);
     g = nsm * (per < 1 ? 1 : per);
   }
-  kern<<<g, C::NT, 0, s>>>(a.ne, a.nv, a.elv, a.xyz, a.lset_st, a.desc, a.list, a.count, (T*)a.elmat, a.err);
+  kern<<<g, C::NT, 0, s>>>(a.ne, a.nv, a.elv, a.xyz, a.lset_st, a.desc, a.list, a.count, a.slot_base, (T*)a.elmat,
+                           a.err);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? XG_OK : cuda_fail(e, "k_st_elmat");
 }
