@@ -33,7 +33,8 @@ struct StCfg {
   static constexpr int NS = ndof_el(D, K);
   static constexpr int N = NS * (KT + 1);
   static constexpr int EPB = N <= 8 ? 8 : (N <= 20 ? 4 : 2);
-  static constexpr int NT = N * EPB;
+  static constexpr int NTF = N * EPB;              // threads of the per-function phases
+  static constexpr int NT = (NTF + 31) / 32 * 32;  // whole warps for the contraction
   static constexpr int CH = 4;
   static constexpr int MAXC = (2 * (D + 1) + 1) * 4;  // time intervals x time points
   static constexpr int NACC = (EPB * N * N + NT - 1) / NT;
@@ -94,7 +95,9 @@ __global__ void __launch_bounds__(StCfg<D, K, KT>::NT) k_st_elmat(int ne, int nv
   __shared__ int maxpts_s;
   const int count = *count_ptr;
   const int sbase = slot_base ? *slot_base : 0;
-  const int le = threadIdx.x / N, a = threadIdx.x % N;
+  // threads beyond N * EPB only join the contraction
+  const bool fth = threadIdx.x < C::NTF;
+  const int le = fth ? threadIdx.x / N : 0, a = fth ? threadIdx.x % N : N;
   const int kl = form.kt_l;
 
   for (int batch = blockIdx.x; batch * EPB < count; batch += gridDim.x) {
@@ -136,7 +139,7 @@ __global__ void __launch_bounds__(StCfg<D, K, KT>::NT) k_st_elmat(int ne, int nv
     }
     __syncthreads();
     const StGeoS<D>& G = geo[le];
-    const int sidx = a % NS, tidx = a / NS;
+    const int sidx = fth ? a % NS : 0, tidx = fth ? a / NS : 0;
     const int desc = G.elem >= 0 ? fn_desc<D, K>(sidx, G.gv) : 0;
     T gT[D + 1][D];
 #pragma unroll
@@ -159,7 +162,7 @@ __global__ void __launch_bounds__(StCfg<D, K, KT>::NT) k_st_elmat(int ne, int nv
       const bool on = G.elem >= 0 && (!Gq.defined_on || tbit64(Gq.defined_on, G.elem));
       const int nco = !on ? 0 : (fixed ? 1 : (G.ncut - 1) * nqt);
       // combos: (time interval, time point) -> level set, classification, #points
-      for (int c = a; c < nco; c += N) {
+      for (int c = a; fth && c < nco; c += N) {
         StCombo& Cb = combo[le][c];
         if (fixed) {
           Cb.t = Gq.tref;
@@ -197,7 +200,7 @@ __global__ void __launch_bounds__(StCfg<D, K, KT>::NT) k_st_elmat(int ne, int nv
       const T cC = (T)G.coef[q][XG_TERM_CONV], cT = (T)G.coef[q][6];
       const int used = Gq.used;
       for (int q0 = 0; q0 < maxpts; q0 += CH) {
-        for (int qq = a; qq < CH; qq += N) {
+        for (int qq = a; fth && qq < CH; qq += N) {
           const int qi = q0 + qq;
           double lam[4] = {0.25, 0.25, 0.25, 0.25}, w = 0.0, tau = 0.0;
           if (qi < npl) {
@@ -252,7 +255,7 @@ __global__ void __launch_bounds__(StCfg<D, K, KT>::NT) k_st_elmat(int ne, int nv
         }
         __syncthreads();
 #pragma unroll
-        for (int qq = 0; qq < CH; qq++) {
+        for (int qq = 0; qq < (fth ? CH : 0); qq++) {
           T lam[D + 1];
 #pragma unroll
           for (int r = 0; r <= D; r++) lam[r] = (T)pts[le][qq][r];
