@@ -439,9 +439,9 @@ __global__ void __launch_bounds__(256) k_elmat_uncut(int ne, int nv, const int32
         for (int q = 0; q < form.ngroups; q++) {
           for (int kk = 0; kk < 5; kk++) {
             const int hp = form.g[q].hpow[kk];
-            if (hp != 0 && h < 0) h = pow(G.meas, 1.0 / D);
+            if (hp != 0 && h < 0) h = mesh_h<D>(G.meas);
             // |det F| folded into the coefficients
-            G.coef[q][kk] = (hp == 0 ? form.g[q].c[kk] : form.g[q].c[kk] * pow(h, (double)hp)) * G.meas;
+            G.coef[q][kk] = (hp == 0 ? form.g[q].c[kk] : form.g[q].c[kk] * int_pow(h, hp)) * G.meas;
           }
           if (form.g[q].used & (1 << XG_TERM_CONV))
 #pragma unroll
@@ -557,9 +557,9 @@ __global__ void __launch_bounds__(256) k_st_elmat_uncut(int ne, int nv, const in
           const StGroupDesc& Gq = form.g[q];
           for (int kk = 0; kk < 7; kk++) {
             const int hp = Gq.hpow[kk];
-            if (hp != 0 && h < 0) h = pow(meas, 1.0 / D);
+            if (hp != 0 && h < 0) h = mesh_h<D>(meas);
             // |det F| folded into the coefficients
-            G.coef[q][kk] = (hp == 0 ? Gq.c[kk] : Gq.c[kk] * pow(h, (double)hp)) * meas;
+            G.coef[q][kk] = (hp == 0 ? Gq.c[kk] : Gq.c[kk] * int_pow(h, hp)) * meas;
           }
           if (Gq.used & (1 << XG_TERM_CONV))
             for (int ti = 0; ti < NTT; ti++)
@@ -688,8 +688,8 @@ __device__ void cut_setup(int e, int ne, int nv, const int32_t* __restrict__ elv
   for (int q = 0; q < form.ngroups; q++)
     for (int k = 0; k < 5; k++) {
       const int hp = form.g[q].hpow[k];
-      if (hp != 0 && h < 0) h = pow(G.meas, 1.0 / D);
-      G.coef[q][k] = hp == 0 ? form.g[q].c[k] : form.g[q].c[k] * pow(h, (double)hp);
+      if (hp != 0 && h < 0) h = mesh_h<D>(G.meas);
+      G.coef[q][k] = hp == 0 ? form.g[q].c[k] : form.g[q].c[k] * int_pow(h, hp);
     }
   for (int dt = 0; dt < 3; dt++) {
     if (!((needs_mask >> dt) & 1)) continue;
@@ -1508,8 +1508,8 @@ __global__ void k_patch_geo(int ne, int nv, const int32_t* __restrict__ elv, con
     for (int pp = 0; pp < form.npatch; pp++) {
       const PatchDesc& P = form.p[pp];
       const bool on = !P.defined_on || tbit(P.defined_on, G.facet);
-      if (P.hpow != 0 && h < 0) h = pow(G.det1, 1.0 / D);
-      G.coef[pp] = !on ? 0.0 : (P.hpow == 0 ? P.c : P.c * pow(h, (double)P.hpow));
+      if (P.hpow != 0 && h < 0) h = mesh_h<D>(G.det1);
+      G.coef[pp] = !on ? 0.0 : (P.hpow == 0 ? P.c : P.c * int_pow(h, P.hpow));
     }
     PaGeoS<D, T> O;
 #pragma unroll

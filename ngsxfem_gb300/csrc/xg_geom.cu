@@ -41,52 +41,70 @@ __global__ void k_perturb(double* v, int64_t n, double eps) {
 // ---- CutInformation::Update, element part (xfem/cutinfo.cpp:83-132) ------------------
 // One thread per element, 32 elements per warp; the warp's ballots are the
 // 32-bit words of the 8 combined-domain bitsets.
+// Pass 1 (thread per element): sign classes by integer tests on the bit
+// patterns; uncut elements get their domain, ratio 1 (NEG) or 0 (POS) -- the
+// exact value of NEG / (NEG + POS) with one part empty -- and their bits; the
+// elements whose signs differ are marked IF in the bitsets and appended to a
+// list (warp-aggregated, order irrelevant: every element's result depends on
+// its own values only).
 template <int D>
 __global__ void __launch_bounds__(256) k_cutinfo(int ne, const int32_t* __restrict__ elv,
                                                  const double* __restrict__ lset, uint8_t* __restrict__ dom,
                                                  double* __restrict__ ratio, uint32_t* __restrict__ bits, int64_t nw32,
-                                                 int* err) {
-  // Sign classes first (integer tests on the bit patterns); the elements whose
-  // signs differ are compacted per block and take the order-0 cut rules
-  // densely, so no warp runs the FP64 rule path with a few active lanes.
-  // Uncut elements get ratio 1 (NEG) or 0 (POS), the exact value of
-  // NEG / (NEG + POS) with one part empty.
-  __shared__ int cut_list[256];
-  __shared__ int ncut;
-  __shared__ uint8_t tsm[256];
+                                                 int32_t* __restrict__ cutlist) {
   const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   const bool valid = e < ne;
-  int cdom = XG_POS;
+  int t = XG_POS;
   if (valid) {
     double l[D + 1];
 #pragma unroll
     for (int i = 0; i <= D; i++) l[i] = __ldg(&lset[__ldg(&elv[(int64_t)i * ne + e])]);
-    cdom = check_if_straight_cut(l, D + 1);
+    t = check_if_straight_cut(l, D + 1);
+    if (t != XG_IF) {
+      dom[e] = (uint8_t)t;
+      ratio[e] = t == XG_NEG ? 1.0 : 0.0;
+    }
   }
-  if (threadIdx.x == 0) ncut = 0;
-  tsm[threadIdx.x] = (uint8_t)XG_POS;
-  __syncthreads();
-  const bool is_cut = valid && cdom == XG_IF;
+  const bool is_cut = valid && t == XG_IF;
   const unsigned mc = __ballot_sync(0xffffffffu, is_cut);
-  int base = 0;
-  if (lane == 0 && mc) base = atomicAdd(&ncut, __popc(mc));
-  base = __shfl_sync(0xffffffffu, base, 0);
-  if (is_cut) cut_list[base + __popc(mc & ((1u << lane) - 1))] = threadIdx.x;
-  if (valid && !is_cut) {
-    dom[e] = (uint8_t)cdom;
-    ratio[e] = cdom == XG_NEG ? 1.0 : 0.0;
-    tsm[threadIdx.x] = (uint8_t)cdom;
+  if (mc) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(&cutlist[0], __popc(mc));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (is_cut) cutlist[1 + base + __popc(mc & ((1u << lane) - 1))] = (int32_t)e;
   }
-  __syncthreads();
-  const int nc = ncut;
-  for (int k = threadIdx.x; k < nc; k += blockDim.x) {
-    const int tl = cut_list[k];
-    const int64_t ec = blockIdx.x * (int64_t)blockDim.x + tl;
+  const unsigned mneg = __ballot_sync(0xffffffffu, valid && t == XG_NEG);
+  const unsigned mpos = __ballot_sync(0xffffffffu, valid && t == XG_POS);
+  const unsigned many = __ballot_sync(0xffffffffu, valid);
+  const int64_t w = e >> 5;
+  if (lane == 0 && w < nw32) {
+    bits[0 * nw32 + w] = 0u;
+    bits[1 * nw32 + w] = mneg;
+    bits[2 * nw32 + w] = mpos;
+    bits[3 * nw32 + w] = mneg | mpos;
+    bits[4 * nw32 + w] = mc;
+    bits[5 * nw32 + w] = mneg | mc;
+    bits[6 * nw32 + w] = mpos | mc;
+    bits[7 * nw32 + w] = many;
+  }
+}
+
+// Pass 2 (thread per listed element, dense): order-0 cut rules for POS then
+// NEG, weights summed in rule order (cutinfo.cpp:92-104); an element whose
+// parts are not both non-empty (all level-set values zero) moves from IF to
+// its class in the bitsets.
+template <int D>
+__global__ void __launch_bounds__(128) k_cutinfo_cut(int ne, const int32_t* __restrict__ elv,
+                                                     const double* __restrict__ lset, uint8_t* __restrict__ dom,
+                                                     double* __restrict__ ratio, uint32_t* __restrict__ bits,
+                                                     int64_t nw32, const int32_t* __restrict__ cutlist, int* err) {
+  const int n = cutlist[0];
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int e = cutlist[1 + k];
     double l[D + 1];
 #pragma unroll
-    for (int i = 0; i <= D; i++) l[i] = __ldg(&lset[__ldg(&elv[(int64_t)i * ne + ec])]);
-    // order-0 cut rules for POS then NEG, weights summed in rule order
+    for (int i = 0; i <= D; i++) l[i] = __ldg(&lset[__ldg(&elv[(int64_t)i * ne + e])]);
     double part_vol[2] = {0.0, 0.0};
 #pragma unroll
     for (int pass = 0; pass < 2; pass++) {
@@ -100,30 +118,31 @@ __global__ void __launch_bounds__(256) k_cutinfo(int ne, const int32_t* __restri
       const double wb = c_rules.w[c_rules.off[D][0]];
       for (int s = 0; s < ns; s++) part_vol[np] += wb * simplex_volume(subs[s].p, D + 1);
     }
-    ratio[ec] = part_vol[XG_NEG] / (part_vol[XG_NEG] + part_vol[XG_POS]);
+    ratio[e] = part_vol[XG_NEG] / (part_vol[XG_NEG] + part_vol[XG_POS]);
     int t;
     if (part_vol[XG_NEG] > 0.0) t = (part_vol[XG_POS] > 0.0) ? XG_IF : XG_NEG;
     else t = XG_POS;
-    dom[ec] = (uint8_t)t;
-    tsm[tl] = (uint8_t)t;
+    dom[e] = (uint8_t)t;
+    if (t != XG_IF) {
+      const int64_t w = e >> 5;
+      const uint32_t bit = 1u << (e & 31);
+      atomicAnd(&bits[4 * nw32 + w], ~bit);
+      atomicAnd(&bits[(t == XG_NEG ? 6 : 5) * nw32 + w], ~bit);
+      atomicOr(&bits[(t == XG_NEG ? 1 : 2) * nw32 + w], bit);
+      atomicOr(&bits[3 * nw32 + w], bit);
+    }
   }
-  __syncthreads();
-  const int t = tsm[threadIdx.x];
-  const unsigned mneg = __ballot_sync(0xffffffffu, valid && t == XG_NEG);
-  const unsigned mpos = __ballot_sync(0xffffffffu, valid && t == XG_POS);
-  const unsigned mif = __ballot_sync(0xffffffffu, valid && t == XG_IF);
-  const unsigned many = __ballot_sync(0xffffffffu, valid);
-  const int64_t w = e >> 5;
-  if (lane == 0 && w < nw32) {
-    bits[0 * nw32 + w] = 0u;
-    bits[1 * nw32 + w] = mneg;
-    bits[2 * nw32 + w] = mpos;
-    bits[3 * nw32 + w] = mneg | mpos;
-    bits[4 * nw32 + w] = mif;
-    bits[5 * nw32 + w] = mneg | mif;
-    bits[6 * nw32 + w] = mpos | mif;
-    bits[7 * nw32 + w] = many;
-  }
+}
+
+template <int D>
+int cutinfo_launch(int n, const int32_t* elv, const double* d_lset, uint8_t* d_dom, double* d_ratio, uint64_t* d_bits,
+                   int64_t nw64, int32_t* cutlist, int* err, cudaStream_t s) {
+  XG_CUDA(cudaMemsetAsync(cutlist, 0, sizeof(int32_t), s));
+  k_cutinfo<D><<<(unsigned)((nw64 * 64 + 255) / 256), 256, 0, s>>>(n, elv, d_lset, d_dom, d_ratio,
+                                                                   (uint32_t*)d_bits, 2 * nw64, cutlist);
+  k_cutinfo_cut<D><<<152 * 4, 128, 0, s>>>(n, elv, d_lset, d_dom, d_ratio, (uint32_t*)d_bits, 2 * nw64, cutlist,
+                                           err);
+  return XG_OK;
 }
 
 // ---- CutInformation::Update, node part (xfem/cutinfo.cpp:134-224) ----------------------
@@ -544,17 +563,14 @@ int xg_interpolate_p1_perturb(double* d_vals, int64_t n, double eps, void* strea
 int xg_cutinfo_update(xg_mesh* m, const double* d_lset, uint8_t* d_dom, double* d_ratio, uint64_t* d_bits,
                       void* stream) {
   if (!m || !d_lset || !d_dom || !d_ratio || !d_bits) return XG_ERR_ARG;
+  // the grid covers whole 64-bit words so every 32-bit half is written
   const int64_t nw64 = (m->ne + 63) / 64;
-  // grid covers whole 64-bit words so every 32-bit half is written
-  const int64_t nthreads = nw64 * 64;
   cudaStream_t s = (cudaStream_t)stream;
-  if (m->dim == 2)
-    k_cutinfo<2><<<nblk(nthreads, 256), 256, 0, s>>>(m->ne, m->d_elv, d_lset, d_dom, d_ratio, (uint32_t*)d_bits,
-                                                     2 * nw64, m->d_err);
-  else
-    k_cutinfo<3><<<nblk(nthreads, 256), 256, 0, s>>>(m->ne, m->d_elv, d_lset, d_dom, d_ratio, (uint32_t*)d_bits,
-                                                     2 * nw64, m->d_err);
-  return launch_check("k_cutinfo");
+  int st = m->dim == 2 ? cutinfo_launch<2>(m->ne, m->d_elv, d_lset, d_dom, d_ratio, d_bits, nw64, m->d_cutlist,
+                                           m->d_err, s)
+                       : cutinfo_launch<3>(m->ne, m->d_elv, d_lset, d_dom, d_ratio, d_bits, nw64, m->d_cutlist,
+                                           m->d_err, s);
+  return st ? st : launch_check("k_cutinfo");
 }
 
 int xg_cutinfo_update_bnd(xg_mesh* m, const double* d_lset, uint8_t* d_dom, double* d_ratio, uint64_t* d_bits,
@@ -564,13 +580,11 @@ int xg_cutinfo_update_bnd(xg_mesh* m, const double* d_lset, uint8_t* d_dom, doub
   const int64_t nw64 = (m->nbnd + 63) / 64;
   cudaStream_t s = (cudaStream_t)stream;
   // the (D-1)-simplices of the boundary with their vertices in ascending order
-  if (m->dim == 2)
-    k_cutinfo<1><<<nblk(nw64 * 64, 256), 256, 0, s>>>((int)m->nbnd, m->d_bnd_v, d_lset, d_dom, d_ratio,
-                                                      (uint32_t*)d_bits, 2 * nw64, m->d_err);
-  else
-    k_cutinfo<2><<<nblk(nw64 * 64, 256), 256, 0, s>>>((int)m->nbnd, m->d_bnd_v, d_lset, d_dom, d_ratio,
-                                                      (uint32_t*)d_bits, 2 * nw64, m->d_err);
-  return launch_check("k_cutinfo (BND)");
+  int st = m->dim == 2 ? cutinfo_launch<1>((int)m->nbnd, m->d_bnd_v, d_lset, d_dom, d_ratio, d_bits, nw64,
+                                           m->d_cutlist, m->d_err, s)
+                       : cutinfo_launch<2>((int)m->nbnd, m->d_bnd_v, d_lset, d_dom, d_ratio, d_bits, nw64,
+                                           m->d_cutlist, m->d_err, s);
+  return st ? st : launch_check("k_cutinfo (BND)");
 }
 
 int xg_cutinfo_nodes(xg_mesh* m, const uint8_t* d_dom, const double* d_ratio, uint64_t* d_nb_v, uint64_t* d_nb_e,

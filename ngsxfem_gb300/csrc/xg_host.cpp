@@ -380,7 +380,9 @@ int xg_mesh_create(int dim, int32_t nv, const double* h_coords, int32_t ne, cons
     return st;
   }
   m->d_el_facets = dim == 2 ? m->d_el_edges : m->d_el_faces;
-  if (cudaMalloc((void**)&m->d_err, sizeof(int)) != cudaSuccess || cudaMemset(m->d_err, 0, sizeof(int)) != cudaSuccess) {
+  if (cudaMalloc((void**)&m->d_err, sizeof(int)) != cudaSuccess || cudaMemset(m->d_err, 0, sizeof(int)) != cudaSuccess ||
+      cudaMalloc((void**)&m->d_cutlist, sizeof(int32_t) * ((size_t)std::max<int64_t>(m->ne, m->nbnd) + 1)) !=
+          cudaSuccess) {
     xg_mesh_destroy(m);
     set_last_error("xg_mesh_create: cudaMalloc failed");
     return XG_ERR_CUDA;
@@ -404,6 +406,7 @@ int xg_mesh_destroy(xg_mesh* m) {
   cudaFree(m->d_el_facets_aos);
   cudaFree(m->d_facet_els_aos);
   cudaFree(m->d_err);
+  cudaFree(m->d_cutlist);
   cudaFree(m->d_scratch);
   delete m;
   return XG_OK;

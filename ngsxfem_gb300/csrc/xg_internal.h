@@ -42,6 +42,18 @@ __device__ __forceinline__ void set_err(int* err, int code) {
   if (err) atomicCAS(err, 0, code);
 }
 
+// mesh size h = |det F|^(1/D) and h^hp for the integer powers of the
+// coefficients (cbrt / sqrt and repeated products instead of two pow calls)
+template <int D>
+__device__ __forceinline__ double mesh_h(double meas) {
+  return D == 3 ? cbrt(meas) : (D == 2 ? sqrt(meas) : meas);
+}
+__device__ __forceinline__ double int_pow(double h, int hp) {
+  double r = 1.0;
+  for (int k = 0; k < (hp < 0 ? -hp : hp); k++) r *= h;
+  return hp < 0 ? 1.0 / r : r;
+}
+
 // finiteness and sign flips on the bit pattern (integer pipe; the FP64 pipe of
 // GB300 is narrow and also issues comparisons and negations)
 __device__ __forceinline__ bool finite_bits(double v) {
@@ -146,6 +158,7 @@ struct xg_mesh {
   int64_t nbnd = 0;                    // BND elements: the boundary facets in facet order
   int32_t* d_bnd_v = nullptr;          // [dim][nbnd] their vertices, ascending
   int* d_err = nullptr;
+  int32_t* d_cutlist = nullptr;  // [max(ne, nbnd) + 1]: count, then the cut elements of the last marking
   // host
   std::vector<int32_t> h_elv;       // ne*(dim+1)
   std::vector<int32_t> h_el_edges;  // ne*nel_edges

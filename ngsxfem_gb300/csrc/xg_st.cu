@@ -132,8 +132,8 @@ __global__ void __launch_bounds__(StCfg<D, K, KT>::NT) k_st_elmat(int ne, int nv
         for (int q = 0; q < form.ngroups; q++)
           for (int k = 0; k < 7; k++) {
             const int hp = form.g[q].hpow[k];
-            if (hp != 0 && h < 0) h = pow(G.meas, 1.0 / D);
-            G.coef[q][k] = hp == 0 ? form.g[q].c[k] : form.g[q].c[k] * pow(h, (double)hp);
+            if (hp != 0 && h < 0) h = mesh_h<D>(G.meas);
+            G.coef[q][k] = hp == 0 ? form.g[q].c[k] : form.g[q].c[k] * int_pow(h, hp);
           }
       }
     }
