@@ -329,6 +329,35 @@ __global__ void k_mark_dofs(int ne, int nd, const int32_t* __restrict__ el_dofs,
 __host__ __device__ constexpr int tri_size(int n) { return n * (n + 1) / 2; }
 __host__ __device__ inline int tri_index(int p, int q, int n) { return p * n - p * (p - 1) / 2 + (q - p); }
 
+// Storage of element and patch matrices.  FP64: full n x n rows (row p
+// contiguous), so the scatter reads each matrix row as one segment; kernels
+// of symmetric forms compute the upper triangle and store both halves.  FP32
+// (mixed): packed upper triangles of symmetric matrices (half the bytes, which
+// matters more there than the segment reads).
+template <typename T>
+__host__ __device__ constexpr bool full_rows() {
+  return sizeof(T) == 8;
+}
+template <typename T>
+__host__ __device__ inline int64_t mat_stride(int n, bool sym) {
+  return full_rows<T>() || !sym ? (int64_t)n * n : (int64_t)tri_size(n);
+}
+// entry (p, q) of a matrix of the layout, p <= q when sym
+template <typename T>
+__device__ __forceinline__ void store_entry(T* __restrict__ m, int n, int p, int q, T v, bool sym) {
+  if (full_rows<T>() || !sym) {
+    m[p * n + q] = v;
+    if (sym && p != q) m[q * n + p] = v;
+  } else {
+    m[tri_index(p, q, n)] = v;
+  }
+}
+template <typename T>
+__device__ __forceinline__ T load_entry(const T* __restrict__ m, int n, int p, int q, bool sym) {
+  if (full_rows<T>() || !sym) return m[p * n + q];
+  return m[p <= q ? tri_index(p, q, n) : tri_index(q, p, n)];
+}
+
 // entry k -> (p, q) tables in shared memory
 __device__ __forceinline__ void entry_tables(int n, bool sym, unsigned char* ep, unsigned char* eq) {
   const int E = sym ? tri_size(n) : n * n;
@@ -479,7 +508,7 @@ __global__ void __launch_bounds__(256) k_elmat_uncut(int ne, int nv, const int32
       }
       if (K == 3) v = neg_if(v, fn_sign<D, K>(ep[k], G.gv) != fn_sign<D, K>(eq[k], G.gv));
       if (!finite_bits(v)) set_err(err, XG_ERR_NONFINITE);
-      elmat[(int64_t)G.slot * E + k] = (T)v;
+      store_entry<T>(elmat + (int64_t)G.slot * mat_stride<T>(N, SYM), N, ep[k], eq[k], (T)v, SYM);
     }
   }
 }
@@ -929,7 +958,7 @@ __global__ void __launch_bounds__(CutCfg<D, K, SYM, T>::NT) k_elmat_cut(
         if (geo[el].elem >= 0) {
           const T v = acc[m].get();
           if (!isfinite(v)) set_err(err, XG_ERR_NONFINITE);
-          elmat[(int64_t)geo[el].slot * E + k] = v;
+          store_entry<T>(elmat + (int64_t)geo[el].slot * mat_stride<T>(N, SYM), N, ep[k], eq[k], v, SYM);
         }
       }
     }
@@ -1251,7 +1280,7 @@ __global__ void __launch_bounds__(kEntNT) k_cut_entries(FormDesc form, MomDesc m
       T r = v.get();
       if (K == 3) r = neg_if(r, fn_sign<D, K>(ep[k], S.gv) != fn_sign<D, K>(eq[k], S.gv));
       if (!finite_bits(r)) set_err(err, XG_ERR_NONFINITE);
-      elmat[(int64_t)S.slot * E + k] = r;
+      store_entry<T>(elmat + (int64_t)S.slot * mat_stride<T>(N, SYM), N, ep[k], eq[k], r, SYM);
     }
   }
 }
@@ -1652,7 +1681,7 @@ __global__ void __launch_bounds__(PaCfg<D, K>::NT) k_patch(
           } else {
             const T v = acc[m].get();
             if (!isfinite(v)) set_err(err, XG_ERR_NONFINITE);
-            famat[(int64_t)idx * E + k] = v;
+            store_entry<T>(famat + (int64_t)idx * mat_stride<T>(N2, true), N2, ep[k], eq[k], v, true);
           }
         }
       }
@@ -1846,7 +1875,7 @@ __global__ void __launch_bounds__(256) k_patch_exact(FormDesc form, const PaGeoS
       }
       const T r = c * v.get();
       if (!finite_bits(r)) set_err(err, XG_ERR_NONFINITE);
-      famat[(int64_t)idx * E + k] = r;
+      store_entry<T>(famat + (int64_t)idx * mat_stride<T>(2 * N, true), 2 * N, a, b, r, true);
     }
   }
 }
@@ -2353,8 +2382,7 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_row_sum(ScatterArgs A, const
             double v;
             if (kind == 0) {
               const int64_t eo = (int64_t)S.ent_slot[a];
-              v = SYM ? (double)elmat[eo * tri_size(nd) + (i <= j ? tri_index(i, j, nd) : tri_index(j, i, nd))]
-                      : (double)elmat[(eo * nd + i) * nd + j];
+              v = (double)load_entry<T>(elmat + eo * mat_stride<T>(nd, SYM), nd, i, j, SYM);
               pos = A.fpos_el[own];
             } else {
               // patch matrices are spatial: local space-time index = time dof * nds + spatial dof
@@ -2371,9 +2399,8 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_row_sum(ScatterArgs A, const
               const int prow = first ? jr : nds + jr, pcol = h * nds + jc;
               const bool self = (h == 0) == (first != 0);
               if (fs < A.cap_fa) {
-                const double pv = (double)famat[(int64_t)fs * tri_size(n2s) +
-                                                (prow <= pcol ? tri_index(prow, pcol, n2s)
-                                                              : tri_index(pcol, prow, n2s))];
+                const double pv = (double)load_entry<T>(famat + (int64_t)fs * mat_stride<T>(n2s, true), n2s, prow,
+                                                        pcol, true);
                 v = ST ? A.mt[ir * A.kt1 + ic] * pv : pv;
                 pos = self ? (int)A.fpos_el[own]
                            : (int)A.pbuf[(((int64_t)fs * 2 + (first ? 0 : 1)) * nd + i) * nd + j];
@@ -3414,7 +3441,8 @@ int form_workspace(xg_form* f) {
   f->cap_el = m->ne;
   // facet-patch workspace: all facets when small, else a quarter of them
   const int nds = space->nds;  // patch matrices are spatial (space-time forms apply the time factor in the scatter)
-  const size_t fa_bytes = (size_t)m->nfacets * tri_size(2 * nds) * esz;
+  const size_t fa_stride = precision == XG_PREC_FP64 ? (size_t)(2 * nds) * (2 * nds) : (size_t)tri_size(2 * nds);
+  const size_t fa_bytes = (size_t)m->nfacets * fa_stride * esz;
   f->cap_fa = fa_bytes <= ((size_t)4 << 30) ? m->nfacets : std::max<int64_t>(m->nfacets / 4, 1);
   int64_t maxw = std::max(f->nw32_el, std::max(f->nw32_fa, f->nw32_dof));
   f->nbsum = (int)((maxw + kCChunk - 1) / kCChunk) + 1;
@@ -3439,7 +3467,7 @@ int form_workspace(xg_form* f) {
   e = e ? e : A((void**)&f->d_bsum, (size_t)f->nbsum * 4);
   e = e ? e : A((void**)&f->d_bsum64, (size_t)f->nbsum64 * 8);
   e = e ? e : A(&f->d_elmat, (size_t)f->cap_el * nd * nd * esz);
-  e = e ? e : A(&f->d_famat, f->has_patch ? (size_t)f->cap_fa * tri_size(2 * nds) * esz : 16);
+  e = e ? e : A(&f->d_famat, f->has_patch ? (size_t)f->cap_fa * fa_stride * esz : 16);
   e = e ? e : A(&f->d_pgeo, f->has_patch ? (size_t)f->cap_fa * sizeof(PaGeoS<3, double>) : 16);
   // cut elements beyond this capacity set themselves up inside the element kernel
   f->cap_cgeo = std::min<int64_t>(m->ne, std::max<int64_t>(65536, m->ne / 8));
@@ -3577,7 +3605,6 @@ int xg_form_assemble(xg_form* f, const double* d_lset, const uint8_t* d_dom, xg_
   }
   cudaStream_t s = (cudaStream_t)stream;
   xg_mesh* m = f->mesh;
-  xg_space* sp = f->space;
   int st;
   // 1. active elements / facets and their lists
   k_active_elements<<<(unsigned)((f->nw32_el * 32 + 255) / 256), 256, 0, s>>>(m->ne, d_dom, f->desc, f->d_act_un,

@@ -85,7 +85,7 @@ __host__ __device__ __forceinline__ void nodal_to_hier(const T* p, int deg, T* c
   constexpr int NE = D == 2 ? 3 : 6;
 #pragma unroll
   for (int c = 0; c <= D; c++) col[c * stride] = p[c];
-  if (K == 1) return;
+  if constexpr (K == 1) return;
   T alpha[NE];
 #pragma unroll
   for (int j = 0; j < NE; j++) {
