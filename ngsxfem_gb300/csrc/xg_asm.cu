@@ -2491,6 +2491,7 @@ struct xg_form {
   int32_t* d_l_un = nullptr;
   int32_t* d_l_cut = nullptr;
   int32_t* d_l_fa = nullptr;
+  int32_t* d_cutlist = nullptr;  // [ne + 1] cut elements of the step's marking
   int32_t* d_el_slot = nullptr;
   int32_t* d_fa_slot = nullptr;
   int32_t* d_dof_row = nullptr;
@@ -2544,7 +2545,7 @@ int form_free(xg_form* f) {
                   f->d_tabs, f->d_act_un, f->d_act_cut, f->d_act_fa, f->d_dof_bits, f->d_l_un, f->d_l_cut, f->d_l_fa,
                   f->d_el_slot, f->d_fa_slot, f->d_dof_row, f->d_rowcnt, f->d_counts, f->d_bsum, f->d_bsum64,
                   f->d_elmat, f->d_famat, f->d_err, f->d_dom, f->d_ratio, f->d_bits, f->d_fbits,
-                  f->d_mtab_i, f->d_mtab_c, f->d_mu, f->d_mhat};
+                  f->d_mtab_i, f->d_mtab_c, f->d_mu, f->d_mhat, f->d_cutlist};
   for (void* p : ptrs) cudaFree(p);
   delete f;
   return XG_OK;
@@ -3459,6 +3460,7 @@ int form_workspace(xg_form* f) {
   e = e ? e : A((void**)&f->d_l_un, (size_t)m->ne * 4);
   e = e ? e : A((void**)&f->d_l_cut, (size_t)m->ne * 4);
   e = e ? e : A((void**)&f->d_l_fa, (size_t)m->nfacets * 4);
+  e = e ? e : A((void**)&f->d_cutlist, ((size_t)m->ne + 1) * 4);
   e = e ? e : A((void**)&f->d_el_slot, (size_t)m->ne * 4);
   e = e ? e : A((void**)&f->d_fa_slot, (size_t)m->nfacets * 4);
   e = e ? e : A((void**)&f->d_dof_row, (size_t)space->ndof * 4);
@@ -3637,7 +3639,7 @@ int xg_cutfem_step(xg_form* f, const double* d_lset, xg_csr* out, void* stream) 
   if (!f || !d_lset || !out) return XG_ERR_ARG;
   xg_mesh* m = f->mesh;
   if (f->use_ev) cudaEventRecord(f->ev[0], (cudaStream_t)stream);
-  int st = xg_cutinfo_update(m, d_lset, f->d_dom, f->d_ratio, f->d_bits, stream);
+  int st = cutinfo_update_ws(m, d_lset, f->d_dom, f->d_ratio, f->d_bits, f->d_cutlist, stream);
   if (st) return st;
   const int64_t nw = f->nw32_el / 2;
   const uint64_t* hasneg = f->d_bits + XG_CDOM_HASNEG * nw;
@@ -3786,7 +3788,7 @@ int xg_st_cutfem_step(xg_form* f, const double* d_lset_st, xg_csr* out, void* st
   cudaStream_t s = (cudaStream_t)stream;
   xg_mesh* m = f->mesh;
   if (f->use_ev) cudaEventRecord(f->ev[0], s);
-  int st = xg_cutinfo_update_st(m, d_lset_st, f->stdesc.kt_l, f->d_dom, f->d_ratio, f->d_bits, stream);
+  int st = cutinfo_update_st_ws(m, d_lset_st, f->stdesc.kt_l, f->d_dom, f->d_ratio, f->d_bits, f->d_cutlist, stream);
   if (st) return st;
   const int64_t nw = f->nw32_el / 2;
   const uint64_t* hasneg = f->d_bits + XG_CDOM_HASNEG * nw;

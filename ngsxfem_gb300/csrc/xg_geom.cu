@@ -405,14 +405,76 @@ static int noalloc_partials(double** out) {
 // ---- space-time CutInfo (xfem/cutinfo.cpp:83-132 with time_order = 0) ---------------
 // SpaceTimeCutIntegrationRule with space and time orders 0: per time interval
 // one time point, per (sub-)simplex one point.
+// Space-time CutInfo (cutinfo.cpp:61-132 with the space-time rule of
+// spacetimecutrule.cpp:106-244, order 0).  Pass 1 (thread per element): an
+// element whose space-time nodal values all have one strict sign and whose
+// level set is P0/P1 in time keeps that sign over the whole slab: its domain,
+// ratio (1 or 0, the exact NEG / (NEG + POS)) and bits are written here; the
+// other elements go to a list (warp-aggregated, order irrelevant) and are left
+// out of the class bitsets, which pass 2 completes.
 template <int D>
-__global__ void k_cutinfo_st(int ne, int nv, const int32_t* __restrict__ elv, const double* __restrict__ lset_st,
-                             int kt, uint8_t* __restrict__ dom, double* __restrict__ ratio, uint32_t* __restrict__ bits,
-                             int64_t nw32, int* err) {
+__global__ void __launch_bounds__(128) k_cutinfo_st(int ne, int nv, const int32_t* __restrict__ elv,
+                                                    const double* __restrict__ lset_st, int kt,
+                                                    uint8_t* __restrict__ dom, double* __restrict__ ratio,
+                                                    uint32_t* __restrict__ bits, int64_t nw32,
+                                                    int32_t* __restrict__ cutlist) {
   const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
   const bool valid = e < ne;
-  int t = XG_POS;
-  if (valid) {
+  int t = -1;
+  if (valid && kt <= 1) {
+    bool hp = false, hn = false, hz = false;
+    for (int v = 0; v <= D; v++) {
+      const int vid = elv[(int64_t)v * ne + e];
+      for (int i = 0; i <= kt; i++) {
+        const double x = lset_st[(int64_t)i * nv + vid];
+        const bool p = d_pos(x), n = d_neg(x);
+        hp |= p;
+        hn |= n;
+        hz |= !p && !n;
+      }
+    }
+    if (!hz && hp != hn) t = hn ? XG_NEG : XG_POS;
+  }
+  if (t >= 0) {
+    dom[e] = (uint8_t)t;
+    ratio[e] = t == XG_NEG ? 1.0 : 0.0;
+  }
+  const bool listed = valid && t < 0;
+  const unsigned ml = __ballot_sync(0xffffffffu, listed);
+  if (ml) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(&cutlist[0], __popc(ml));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (listed) cutlist[1 + base + __popc(ml & ((1u << lane) - 1))] = (int32_t)e;
+  }
+  const unsigned mneg = __ballot_sync(0xffffffffu, valid && t == XG_NEG);
+  const unsigned mpos = __ballot_sync(0xffffffffu, valid && t == XG_POS);
+  const unsigned many = __ballot_sync(0xffffffffu, valid);
+  const int64_t w = e >> 5;
+  if (lane == 0 && w < nw32) {
+    bits[0 * nw32 + w] = 0u;
+    bits[1 * nw32 + w] = mneg;
+    bits[2 * nw32 + w] = mpos;
+    bits[3 * nw32 + w] = mneg | mpos;
+    bits[4 * nw32 + w] = 0u;
+    bits[5 * nw32 + w] = mneg;
+    bits[6 * nw32 + w] = mpos;
+    bits[7 * nw32 + w] = many;
+  }
+}
+
+// Pass 2 (thread per listed element, dense): time cut points, order-0 space-time
+// rules for POS then NEG, ratio and domain; the class bits are added atomically.
+template <int D>
+__global__ void __launch_bounds__(128) k_cutinfo_st_cut(int ne, int nv, const int32_t* __restrict__ elv,
+                                                        const double* __restrict__ lset_st, int kt,
+                                                        uint8_t* __restrict__ dom, double* __restrict__ ratio,
+                                                        uint32_t* __restrict__ bits, int64_t nw32,
+                                                        const int32_t* __restrict__ cutlist, int* err) {
+  const int nlist = cutlist[0];
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nlist; k += gridDim.x * blockDim.x) {
+    const int e = cutlist[1 + k];
     double lst[3 * (D + 1)];
     for (int v = 0; v <= D; v++) {
       const int vid = elv[(int64_t)v * ne + e];
@@ -440,31 +502,32 @@ __global__ void k_cutinfo_st(int ne, int nv, const int32_t* __restrict__ elv, co
             set_err(err, -ns);
             ns = 0;
           }
-          for (int k = 0; k < ns; k++) part_vol[np] += w0 * simplex_volume(subs[k].p, D + 1) * wt * (t1 - t0);
+          for (int q = 0; q < ns; q++) part_vol[np] += w0 * simplex_volume(subs[q].p, D + 1) * wt * (t1 - t0);
         } else if (cls == np) {
           part_vol[np] += w0 * wt * (t1 - t0);
         }
       }
     }
     ratio[e] = part_vol[XG_NEG] / (part_vol[XG_NEG] + part_vol[XG_POS]);
+    int t;
     if (part_vol[XG_NEG] > 0.0) t = (part_vol[XG_POS] > 0.0) ? XG_IF : XG_NEG;
     else t = XG_POS;
     dom[e] = (uint8_t)t;
-  }
-  const unsigned mneg = __ballot_sync(0xffffffffu, valid && t == XG_NEG);
-  const unsigned mpos = __ballot_sync(0xffffffffu, valid && t == XG_POS);
-  const unsigned mif = __ballot_sync(0xffffffffu, valid && t == XG_IF);
-  const unsigned many = __ballot_sync(0xffffffffu, valid);
-  const int64_t w = e >> 5;
-  if ((threadIdx.x & 31) == 0 && w < nw32) {
-    bits[0 * nw32 + w] = 0u;
-    bits[1 * nw32 + w] = mneg;
-    bits[2 * nw32 + w] = mpos;
-    bits[3 * nw32 + w] = mneg | mpos;
-    bits[4 * nw32 + w] = mif;
-    bits[5 * nw32 + w] = mneg | mif;
-    bits[6 * nw32 + w] = mpos | mif;
-    bits[7 * nw32 + w] = many;
+    const int64_t w = e >> 5;
+    const uint32_t bit = 1u << (e & 31);
+    if (t == XG_NEG) {
+      atomicOr(&bits[1 * nw32 + w], bit);
+      atomicOr(&bits[3 * nw32 + w], bit);
+      atomicOr(&bits[5 * nw32 + w], bit);
+    } else if (t == XG_POS) {
+      atomicOr(&bits[2 * nw32 + w], bit);
+      atomicOr(&bits[3 * nw32 + w], bit);
+      atomicOr(&bits[6 * nw32 + w], bit);
+    } else {
+      atomicOr(&bits[4 * nw32 + w], bit);
+      atomicOr(&bits[5 * nw32 + w], bit);
+      atomicOr(&bits[6 * nw32 + w], bit);
+    }
   }
 }
 
@@ -562,16 +625,27 @@ int xg_interpolate_p1_perturb(double* d_vals, int64_t n, double eps, void* strea
 
 int xg_cutinfo_update(xg_mesh* m, const double* d_lset, uint8_t* d_dom, double* d_ratio, uint64_t* d_bits,
                       void* stream) {
-  if (!m || !d_lset || !d_dom || !d_ratio || !d_bits) return XG_ERR_ARG;
+  if (!m) return XG_ERR_ARG;
+  return xg::cutinfo_update_ws(m, d_lset, d_dom, d_ratio, d_bits, m->d_cutlist, stream);
+}
+}  // extern "C"
+
+namespace xg {
+int cutinfo_update_ws(xg_mesh* m, const double* d_lset, uint8_t* d_dom, double* d_ratio, uint64_t* d_bits,
+                      int32_t* cutlist, void* stream) {
+  if (!m || !d_lset || !d_dom || !d_ratio || !d_bits || !cutlist) return XG_ERR_ARG;
   // the grid covers whole 64-bit words so every 32-bit half is written
   const int64_t nw64 = (m->ne + 63) / 64;
   cudaStream_t s = (cudaStream_t)stream;
-  int st = m->dim == 2 ? cutinfo_launch<2>(m->ne, m->d_elv, d_lset, d_dom, d_ratio, d_bits, nw64, m->d_cutlist,
+  int st = m->dim == 2 ? cutinfo_launch<2>(m->ne, m->d_elv, d_lset, d_dom, d_ratio, d_bits, nw64, cutlist,
                                            m->d_err, s)
-                       : cutinfo_launch<3>(m->ne, m->d_elv, d_lset, d_dom, d_ratio, d_bits, nw64, m->d_cutlist,
+                       : cutinfo_launch<3>(m->ne, m->d_elv, d_lset, d_dom, d_ratio, d_bits, nw64, cutlist,
                                            m->d_err, s);
   return st ? st : launch_check("k_cutinfo");
 }
+}  // namespace xg
+
+extern "C" {
 
 int xg_cutinfo_update_bnd(xg_mesh* m, const double* d_lset, uint8_t* d_dom, double* d_ratio, uint64_t* d_bits,
                           void* stream) {
@@ -689,17 +763,35 @@ int xg_integrate(xg_mesh* m, const double* d_lset, int dt, int order, int ex, in
 
 int xg_cutinfo_update_st(xg_mesh* m, const double* d_lset_st, int kt_lset, uint8_t* d_dom, double* d_ratio,
                          uint64_t* d_bits, void* stream) {
-  if (!m || !d_lset_st || !d_dom || !d_ratio || !d_bits || kt_lset < 0 || kt_lset > 2) return XG_ERR_ARG;
+  if (!m) return XG_ERR_ARG;
+  return xg::cutinfo_update_st_ws(m, d_lset_st, kt_lset, d_dom, d_ratio, d_bits, m->d_cutlist, stream);
+}
+}  // extern "C"
+
+namespace xg {
+int cutinfo_update_st_ws(xg_mesh* m, const double* d_lset_st, int kt_lset, uint8_t* d_dom, double* d_ratio,
+                         uint64_t* d_bits, int32_t* cutlist, void* stream) {
+  if (!m || !d_lset_st || !d_dom || !d_ratio || !d_bits || !cutlist || kt_lset < 0 || kt_lset > 2)
+    return XG_ERR_ARG;
   const int64_t nw64 = (m->ne + 63) / 64;
   cudaStream_t s = (cudaStream_t)stream;
-  if (m->dim == 2)
+  XG_CUDA(cudaMemsetAsync(cutlist, 0, sizeof(int32_t), s));
+  if (m->dim == 2) {
     k_cutinfo_st<2><<<nblk(nw64 * 64, 128), 128, 0, s>>>(m->ne, m->nv, m->d_elv, d_lset_st, kt_lset, d_dom, d_ratio,
-                                                         (uint32_t*)d_bits, 2 * nw64, m->d_err);
-  else
+                                                         (uint32_t*)d_bits, 2 * nw64, cutlist);
+    k_cutinfo_st_cut<2><<<152 * 8, 128, 0, s>>>(m->ne, m->nv, m->d_elv, d_lset_st, kt_lset, d_dom, d_ratio,
+                                                 (uint32_t*)d_bits, 2 * nw64, cutlist, m->d_err);
+  } else {
     k_cutinfo_st<3><<<nblk(nw64 * 64, 128), 128, 0, s>>>(m->ne, m->nv, m->d_elv, d_lset_st, kt_lset, d_dom, d_ratio,
-                                                         (uint32_t*)d_bits, 2 * nw64, m->d_err);
+                                                         (uint32_t*)d_bits, 2 * nw64, cutlist);
+    k_cutinfo_st_cut<3><<<152 * 8, 128, 0, s>>>(m->ne, m->nv, m->d_elv, d_lset_st, kt_lset, d_dom, d_ratio,
+                                                 (uint32_t*)d_bits, 2 * nw64, cutlist, m->d_err);
+  }
   return launch_check("k_cutinfo_st");
 }
+}  // namespace xg
+
+extern "C" {
 
 int xg_st_cut_rules(xg_mesh* m, const double* d_lset_st, int kt_lset, const int32_t* d_elems, int32_t n, int dt,
                     int order_space, int order_time, int32_t max_pts, int32_t* d_counts, double* d_pts, double* d_wts,

@@ -8,6 +8,8 @@
 
 #include "../../include/xg.h"
 
+struct xg_mesh;
+
 namespace xg {
 
 // ---- quadrature rule family (host-built, device __constant__) ------------------
@@ -138,6 +140,13 @@ struct StLaunch {
   int* err;
 };
 int launch_st_elmat(const StLaunch& a, cudaStream_t s);
+
+// CutInfo updates with a caller-owned list of the cut elements ([ne + 1] ints;
+// forms pass their own so that forms of one mesh may run concurrently)
+int cutinfo_update_ws(xg_mesh* m, const double* d_lset, uint8_t* d_dom, double* d_ratio, uint64_t* d_bits,
+                      int32_t* cutlist, void* stream);
+int cutinfo_update_st_ws(xg_mesh* m, const double* d_lset_st, int kt_lset, uint8_t* d_dom, double* d_ratio,
+                         uint64_t* d_bits, int32_t* cutlist, void* stream);
 
 }  // namespace xg
 
