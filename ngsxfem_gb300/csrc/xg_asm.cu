@@ -1881,14 +1881,15 @@ __global__ void __launch_bounds__(256) k_patch_exact(FormDesc form, const PaGeoS
 }
 
 // ============================================================================
-// Scatter: one warp per active row (the row of dof r).  The row's columns are
-// the dofs of the active elements containing r and, for every active facet of
-// an element containing r, the dofs of both elements of that facet patch.
-// At form creation the full pattern (every element and interior facet active)
-// is built once: sorted columns of every dof row (hash + sort, k_row_count)
-// and the position of every element column in its rows' full rows
-// (k_fpos_el).  Per step, pass 1 (k_row_mark) flags the active columns of each
-// active row over its full-row positions and counts them; pass 2 (k_row_sum)
+// Scatter.  The columns of the row of dof r are the dofs of the active
+// elements containing r and, for every active facet of an element containing
+// r, the dofs of both elements of that facet patch.  At form creation the full
+// pattern (every element and interior facet active) is built once: sorted
+// columns of every dof row (hash + sort, k_row_count) and the position of
+// every element column in its rows' full rows (k_fpos_el).  Per step, pass 1
+// flags the active columns over the full-row positions, element- and
+// facet-centric (k_row_clear, k_flag_elements, k_flag_facets), and counts
+// them per row (k_row_flagcount); pass 2 (k_row_sum, one warp per active row)
 // stages (position, value) pairs and adds them in the fixed order (adjacent
 // elements ascending; per element its own matrix row, then its facets in local
 // order, first then second element's columns) -- the sum order never depends
@@ -2209,98 +2210,88 @@ __global__ void k_fpos_el(ScatterArgs A, uint16_t* __restrict__ fpos, int* err) 
   }
 }
 
-// Pass 1 (per step): per active row, the active columns as flags over the
-// row's full-pattern positions (element columns from the static positions,
-// neighbour columns of active facets by a search of the full row, recorded in
-// pbuf for pass 2), and the count.
-__global__ void __launch_bounds__(kRowWarps * 32) k_row_mark(ScatterArgs A, int64_t* rowcnt, int* err) {
-  extern __shared__ __align__(16) unsigned char sm_rows[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const RowSm S = row_sm(A, sm_rows + (size_t)warp * A.wbytes);
-  uint8_t* sflags = (uint8_t*)S.hash;  // hs * 4 >= maxu bytes
+// Pass 1 (per step), element- and facet-centric: the active columns of the
+// active rows as byte flags over the rows' full-pattern positions.  Flag
+// writes are idempotent (every writer stores 1), so no ordering is needed.
+// (a) the active rows' flags are cleared (rows of earlier steps may hold
+// flags); (b) every active element flags its columns in the rows of its dofs
+// (static positions); (c) every active facet flags, in the rows of each
+// element's dofs, the element's own columns and the other element's columns
+// (found by a binary search of the sorted full row; the positions are kept
+// for pass 2); (d) per row the flags are counted.
+__global__ void __launch_bounds__(256) k_row_clear(ScatterArgs A) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int nrows = A.counts[3];
-  const int nd = A.nd;
-  for (int row = blockIdx.x * kRowWarps + warp; row < nrows; row += gridDim.x * kRowWarps) {
+  for (int row = warp; row < nrows; row += nwarps) {
     const int r = A.rows[row];
     const int64_t fo = A.full_ptr[r];
     const int len = (int)(A.full_ptr[r + 1] - fo);
-    if (len > A.maxu) {
-      if (lane == 0) {
-        set_err(err, XG_ERR_CAPACITY);
-        rowcnt[row] = 0;
-      }
+    for (int k = lane; k < len; k += 32) A.flags[fo + k] = 0;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_flag_elements(ScatterArgs A, const int32_t* __restrict__ l_un,
+                                                       const int32_t* __restrict__ l_cut) {
+  const int nd = A.nd, nun = A.counts[0], ncut = A.counts[1];
+  const int64_t total = (int64_t)(nun + ncut) * nd * nd;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t item = t / (nd * nd);
+    const int ij = (int)(t - item * nd * nd), i = ij / nd;
+    const int e = item < nun ? l_un[item] : l_cut[item - nun];
+    const int r = A.el_dofs[(int64_t)e * nd + i];
+    A.flags[A.full_ptr[r] + A.fpos_el[(int64_t)e * nd * nd + ij]] = 1;
+  }
+}
+
+// thread per (active facet, side, local row i, local column j): binary search
+// of the other element's dof j in the sorted full row of dof i
+__global__ void __launch_bounds__(256) k_flag_facets(ScatterArgs A, const int32_t* __restrict__ l_fa, int* err) {
+  const int nd = A.nd, nfa = A.counts[2];
+  const int64_t total = (int64_t)nfa * 2 * nd * nd;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t fs = t / (2 * nd * nd);
+    const int rem = (int)(t - fs * 2 * nd * nd), side = rem / (nd * nd), ij = rem - side * nd * nd;
+    const int i = ij / nd, j = ij - i * nd;
+    if (fs >= A.cap_fa) continue;  // reported by the patch kernels
+    const int2 pr = A.fel[l_fa[fs]];
+    const int er = side == 0 ? pr.x : pr.y, ec = side == 0 ? pr.y : pr.x;
+    const int r = A.el_dofs[(int64_t)er * nd + i], c = A.el_dofs[(int64_t)ec * nd + j];
+    const int64_t fo = A.full_ptr[r];
+    const int len = (int)(A.full_ptr[r + 1] - fo);
+    int lo = 0, hi = len;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (A.tmp_cols[fo + mid] < c) lo = mid + 1;
+      else hi = mid;
+    }
+    if (lo >= len || A.tmp_cols[fo + lo] != c) {
+      set_err(err, XG_ERR_CAPACITY);
       continue;
     }
-    for (int k = lane; k < len; k += 32) {
-      S.ucols[k] = A.tmp_cols[fo + k];
-      sflags[k] = 0;
-    }
-    __syncwarp();
-    const int a0 = A.adj_ptr[r], a1 = A.adj_ptr[r + 1];
-    for (int c0 = a0; c0 < a1; c0 += kEnt) {
-      const int na = min(kEnt, a1 - c0);
-      const int nc = load_entries(A, S, c0, na);
-      // S.celem lists, in entry order, each contributing entry's element then
-      // the neighbours across its active facets; the active facets themselves
-      // are listed in S.grp as (entry << 2) | local facet
-      int nfa = 0;
-      {
-        int cnt = 0;
-        if (lane < na)
-          for (int lf = 0; lf < A.nfl; lf++) cnt += S.ent_nb[lane * 4 + lf] >= 0;
-        int x = cnt;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const int y = __shfl_up_sync(0xffffffffu, x, o);
-          if (lane >= o) x += y;
-        }
-        nfa = __shfl_sync(0xffffffffu, x, 31);
-        if (lane < na) {
-          int k = x - cnt;
-          for (int lf = 0; lf < A.nfl; lf++)
-            if (S.ent_nb[lane * 4 + lf] >= 0) S.grp[k++] = (lane << 2) | lf;
-        }
-        // the entries whose own element contributes columns (active element or facet)
-        const bool any = lane < na && (S.ent_e[lane] >= 0 || cnt > 0);
-        const unsigned am = __ballot_sync(0xffffffffu, any);
-        if (any) S.celem[__popc(am & ((1u << lane) - 1))] = lane;
-        __syncwarp();
-        const int nown = __popc(am);
-        // own element columns from the static positions
-        LaneIdx L;
-        L.init(lane, nd);
-        for (int t = lane; t < nown * nd; t += 32, L.next()) {
-          const int a = S.celem[L.g];
-          const int ee = S.ent_e[a];
-          const int e = ee >= 0 ? ee : ~ee;
-          sflags[A.fpos_el[((int64_t)e * nd + S.ent_i[a]) * nd + L.j]] = 1;
-        }
-      }
-      (void)nc;
-      // neighbour columns of the active facets
-      LaneIdx L;
-      L.init(lane, nd);
-      for (int t = lane; t < nfa * nd; t += 32, L.next()) {
-        const int ga = S.grp[L.g], a = ga >> 2, lf = ga & 3, j = L.j;
-        const int nb = S.ent_nb[a * 4 + lf];
-        const int pos = lower_bound_sm(S.ucols, len, A.el_dofs[(int64_t)nb * nd + j]);
-        sflags[min(pos, len - 1)] = 1;
-        const int fs = S.ent_fs[a * 4 + lf];
-        if (fs < A.cap_fa)
-          A.pbuf[(((int64_t)fs * 2 + (S.ent_first[a * 4 + lf] ? 0 : 1)) * nd + S.ent_i[a]) * nd + j] = (uint16_t)pos;
-      }
-      __syncwarp();
-    }
+    A.flags[fo + lo] = 1;
+    A.pbuf[((fs * 2 + side) * nd + i) * nd + j] = (uint16_t)lo;
+    // the row element's own columns, already flagged when it is active
+    if (!el_active(A, er)) A.flags[fo + A.fpos_el[(int64_t)er * nd * nd + ij]] = 1;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_row_flagcount(ScatterArgs A, int64_t* __restrict__ rowcnt, int* err) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int nrows = A.counts[3];
+  for (int row = warp; row < nrows; row += nwarps) {
+    const int r = A.rows[row];
+    const int64_t fo = A.full_ptr[r];
+    const int len = (int)(A.full_ptr[r + 1] - fo);
     int cnt = 0;
-    for (int k = lane; k < len; k += 32) {
-      const uint8_t fl = sflags[k];
-      A.flags[fo + k] = fl;
-      cnt += fl;
-    }
+    for (int k = lane; k < len; k += 32) cnt += A.flags[fo + k];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-    if (lane == 0) rowcnt[row] = cnt;
-    __syncwarp();
+    if (lane == 0) {
+      if (len > A.maxu) set_err(err, XG_ERR_CAPACITY);
+      rowcnt[row] = cnt;
+    }
   }
 }
 
@@ -2506,8 +2497,8 @@ struct xg_form {
   int* d_err = nullptr;
   int sc_hs = 0, sc_maxu = 0, sc_stage = 0, sc_wbytes = 0;
   size_t sc_smem = 0;
-  int mk_wbytes = 0, sm_wbytes = 0, grid_mk = 0, grid_sm = 0;  // per-step scatter kernels
-  size_t mk_smem = 0, sm_smem = 0;
+  int sm_wbytes = 0, grid_sm = 0;  // per-step summing pass
+  size_t sm_smem = 0;
   int64_t full_nnz = 0;
   int64_t* d_full_ptr = nullptr;
   int32_t* d_tmp_cols = nullptr;  // full-pattern columns of every dof row (sorted), built at creation
@@ -3189,12 +3180,10 @@ int scatter_phase(xg_form* f, xg_csr* out, cudaStream_t s) {
   // 4. pattern and values
   ScatterArgs A = scatter_args(f);
   A.rows = out->d_row_dof;
-  A.hs = std::max(32, f->sc_maxu / 4);
-  A.ucn = f->sc_maxu;
-  A.accn = 0;
-  A.stage = 0;
-  A.wbytes = f->mk_wbytes;
-  k_row_mark<<<f->grid_mk, kRowWarps * 32, f->mk_smem, s>>>(A, f->d_rowcnt, f->d_err);
+  k_row_clear<<<152 * 8, 256, 0, s>>>(A);
+  k_flag_elements<<<152 * 16, 256, 0, s>>>(A, f->d_l_un, f->d_l_cut);
+  if (f->has_patch) k_flag_facets<<<152 * 16, 256, 0, s>>>(A, f->d_l_fa, f->d_err);
+  k_row_flagcount<<<152 * 8, 256, 0, s>>>(A, f->d_rowcnt, f->d_err);
   const int nb64 = (int)((sp->ndof + kSChunk - 1) / kSChunk);
   k_sum64_blocks<<<nb64, kSThreads, 0, s>>>(f->d_rowcnt, f->d_counts + 3, f->d_bsum64);
   k_scan64_small<<<1, 1024, 0, s>>>(f->d_bsum64, nb64);
@@ -3529,19 +3518,13 @@ int form_workspace(xg_form* f) {
   // per-step scatter kernels, each with its own shared layout: the marking pass
   // holds the full row's columns and its flags (in the hash region, maxu
   // bytes), the summing pass the accumulators and the staged values
-  f->mk_wbytes = (row_smem_bytes(std::max(32, f->sc_maxu / 4), f->sc_maxu, 0, 0) + 15) & ~15;
-  f->mk_smem = (size_t)kRowWarps * f->mk_wbytes;
   f->sm_wbytes = (row_smem_bytes(0, 0, f->sc_maxu, f->sc_stage) + 15) & ~15;
   f->sm_smem = (size_t)kRowWarps * f->sm_wbytes;
   {
     static std::mutex mu;
-    static size_t raised_mk = 48 * 1024, raised_sm = 48 * 1024;
+    static size_t raised_sm = 48 * 1024;
     std::lock_guard<std::mutex> lock(mu);
     bool bad = false;
-    if (f->mk_smem > raised_mk) {
-      bad |= cudaFuncSetAttribute(k_row_mark, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->mk_smem) != 0;
-      raised_mk = f->mk_smem;
-    }
     if (f->sm_smem > raised_sm) {
       const int sm = (int)f->sm_smem;
       const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
@@ -3558,7 +3541,6 @@ int form_workspace(xg_form* f) {
       return XG_ERR_CAPACITY;
     }
   }
-  f->grid_mk = grid_for(k_row_mark, kRowWarps * 32, f->mk_smem);
   f->grid_sm = grid_for(k_row_sum<double, false, false>, kRowWarps * 32, f->sm_smem);
   return full_pattern_build(f);
 }
