@@ -55,8 +55,8 @@ __device__ __forceinline__ bool tbit32(const uint32_t* b, int64_t i) { return (b
 // block popcounts -> single-block scan -> per-block write.
 // ============================================================================
 constexpr int kCThreads = 256;
-constexpr int kCWordsPerThread = 8;
-constexpr int kCChunk = kCThreads * kCWordsPerThread;  // 32-bit words per block
+constexpr int kCWarpWords = 16;                            // words per warp
+constexpr int kCChunk = (kCThreads / 32) * kCWarpWords;     // 32-bit words per block
 
 __device__ __forceinline__ int block_excl_scan_int(int v, int* total, int* sm /* >= 32 */) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -86,11 +86,8 @@ __device__ __forceinline__ int block_excl_scan_int(int v, int* total, int* sm /*
 
 __global__ void k_popc_blocks(const uint32_t* __restrict__ bits, int64_t nwords, int* __restrict__ bsum) {
   __shared__ int sm[32];
-  int64_t w0 = (int64_t)blockIdx.x * kCChunk + (int64_t)threadIdx.x * kCWordsPerThread;
-  int c = 0;
-#pragma unroll
-  for (int k = 0; k < kCWordsPerThread; k++)
-    if (w0 + k < nwords) c += __popc(bits[w0 + k]);
+  const int64_t w = (int64_t)blockIdx.x * kCChunk + threadIdx.x;
+  const int c = (threadIdx.x < kCChunk && w < nwords) ? __popc(bits[w]) : 0;
   int total;
   block_excl_scan_int(c, &total, sm);
   if (threadIdx.x == 0) bsum[blockIdx.x] = total;
@@ -115,29 +112,39 @@ __global__ void k_scan_small(int* __restrict__ v, int n, int* __restrict__ total
   if (threadIdx.x == 0) *total_out = carry;
 }
 
+// Warp per kCWarpWords consecutive words: lane l of the warp writes bit l of
+// each word, at the word's offset plus the set bits below it (coalesced).
 __global__ void k_write_list(const uint32_t* __restrict__ bits, int64_t nwords, const int* __restrict__ boff,
                              int32_t* __restrict__ list, int32_t* __restrict__ slot, const int* __restrict__ slot_base) {
   __shared__ int sm[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int sb = slot_base ? *slot_base : 0;
-  int64_t w0 = (int64_t)blockIdx.x * kCChunk + (int64_t)threadIdx.x * kCWordsPerThread;
-  uint32_t w[kCWordsPerThread];
-  int c = 0;
+  const int64_t w0 = (int64_t)blockIdx.x * kCChunk + (int64_t)wid * kCWarpWords;
+  const uint32_t mine = (lane < kCWarpWords && w0 + lane < nwords) ? bits[w0 + lane] : 0u;
+  // exclusive prefix of the words' counts within the warp, then over the block's warps
+  const int cnt = __popc(mine);
+  int x = cnt;
 #pragma unroll
-  for (int k = 0; k < kCWordsPerThread; k++) {
-    w[k] = (w0 + k < nwords) ? bits[w0 + k] : 0u;
-    c += __popc(w[k]);
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
   }
-  int pos = boff[blockIdx.x] + block_excl_scan_int(c, nullptr, sm);
-#pragma unroll
-  for (int k = 0; k < kCWordsPerThread; k++) {
-    uint32_t x = w[k];
-    while (x) {
-      int b = __ffs(x) - 1;
-      x &= x - 1;
-      int idx = (int)((w0 + k) * 32 + b);
+  const int wtotal = __shfl_sync(0xffffffffu, x, 31);
+  const int wexcl = x - cnt;
+  if (lane == 0) sm[wid] = wtotal;
+  __syncthreads();
+  int base = boff[blockIdx.x];
+  for (int k = 0; k < wid; k++) base += sm[k];
+  const unsigned below = (1u << lane) - 1;
+#pragma unroll 4
+  for (int k = 0; k < kCWarpWords; k++) {
+    const uint32_t word = __shfl_sync(0xffffffffu, mine, k);
+    const int off = __shfl_sync(0xffffffffu, wexcl, k);
+    if ((word >> lane) & 1u) {
+      const int pos = base + off + __popc(word & below);
+      const int idx = (int)((w0 + k) * 32 + lane);
       list[pos] = idx;
       if (slot) slot[idx] = pos + sb;
-      pos++;
     }
   }
 }
