@@ -129,7 +129,10 @@ int xg_interpolate_p1_perturb(double* d_vals, int64_t n, double eps, void* strea
  * volume fractions of the order-0 cut rules give cut_ratio = NEG/(NEG+POS)
  * and the domain type; d_bits receives the 8 COMBINED_DOMAIN_TYPE bitsets
  * ([8][ceil(ne/64)] words, row c = XG_CDOM value c).
- * Replaces CutInformation::Update(cf, subdivlvl=0, time_order=-1, lh). */
+ * Replaces CutInformation::Update(cf, subdivlvl=0, time_order=-1, lh).
+ * The marking uses a list of cut elements owned by the mesh: calls of
+ * xg_cutinfo_update, xg_cutinfo_update_bnd and xg_cutinfo_update_st on one mesh
+ * must not overlap (the forms' steps use their own lists and may). */
 int xg_cutinfo_update(xg_mesh* mesh, const double* d_lset, uint8_t* d_dom, double* d_cut_ratio,
                       uint64_t* d_bits, void* stream);
 /* CutInformation::Update for the BND elements (xfem/cutinfo.cpp:83-131 with
