@@ -299,25 +299,35 @@ __global__ void k_active_facets(int64_t nf, const int32_t* __restrict__ fel, For
 }
 
 // dofs of active elements and of both elements of active facets
-__global__ void k_mark_dofs(int ne, int nd, const int32_t* __restrict__ el_dofs, const int32_t* __restrict__ l_un,
+// active dofs: a byte per dof set by every active element and both elements
+// of every active facet (idempotent plain stores), then packed into bits by
+// warp ballot; the packing pass clears the bytes for the next step
+__global__ void k_mark_dofs(int ne, int nd, const int32_t* __restrict__ el_dofs_aos, const int32_t* __restrict__ l_un,
                             const int32_t* __restrict__ l_cut, const int32_t* __restrict__ l_fa,
                             const int* __restrict__ counts, int64_t nf, const int32_t* __restrict__ fel,
-                            unsigned* dof_bits) {
+                            uint8_t* __restrict__ dof_flag) {
   const int nun = counts[0], ncut = counts[1], nfa = counts[2];
   const int64_t total = (int64_t)(nun + ncut + 2 * nfa) * nd;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-    int64_t item = t / nd;
-    int j = (int)(t % nd);
+    const int64_t item = t / nd;
+    const int j = (int)(t - item * nd);
     int e;
     if (item < nun) e = l_un[item];
     else if (item < nun + ncut) e = l_cut[item - nun];
     else {
-      int64_t q = item - nun - ncut;
+      const int64_t q = item - nun - ncut;
       e = fel[(q & 1) * nf + l_fa[q >> 1]];
     }
-    int dof = el_dofs[(int64_t)j * ne + e];
-    atomicOr(&dof_bits[dof >> 5], 1u << (dof & 31));
+    dof_flag[el_dofs_aos[(int64_t)e * nd + j]] = 1;
   }
+}
+
+__global__ void k_pack_dofs(uint8_t* __restrict__ dof_flag, int64_t ndof, uint32_t* __restrict__ bits, int64_t nw32) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool on = i < ndof && dof_flag[i];
+  if (on) dof_flag[i] = 0;
+  const unsigned m = __ballot_sync(0xffffffffu, on);
+  if ((threadIdx.x & 31) == 0 && (i >> 5) < nw32) bits[i >> 5] = m;
 }
 
 // ============================================================================
@@ -727,9 +737,11 @@ __device__ void cut_setup(int e, int ne, int nv, const int32_t* __restrict__ elv
       if (hp != 0 && h < 0) h = mesh_h<D>(G.meas);
       G.coef[q][k] = hp == 0 ? form.g[q].c[k] : form.g[q].c[k] * int_pow(h, hp);
     }
+  P3 cut[4];
+  const int nc = calc_if_points<D>(G.l, cut);  // shared by the domains
   for (int dt = 0; dt < 3; dt++) {
     if (!((needs_mask >> dt) & 1)) continue;
-    int ns = decompose<D>(G.l, dt, SS.sub[dt]);
+    int ns = nc < 0 ? nc : decompose_cuts<D>(G.l, dt, cut, nc, SS.sub[dt]);
     if (ns < 0) {
       set_err(err, -ns);
       ns = 0;
@@ -2490,6 +2502,7 @@ struct xg_form {
   int32_t* d_l_cut = nullptr;
   int32_t* d_l_fa = nullptr;
   int32_t* d_cutlist = nullptr;  // [ne + 1] cut elements of the step's marking
+  uint8_t* d_dof_flag = nullptr;  // [ndof] active-dof bytes (zero between steps)
   int32_t* d_el_slot = nullptr;
   int32_t* d_fa_slot = nullptr;
   int32_t* d_dof_row = nullptr;
@@ -2543,7 +2556,7 @@ int form_free(xg_form* f) {
                   f->d_tabs, f->d_act_un, f->d_act_cut, f->d_act_fa, f->d_dof_bits, f->d_l_un, f->d_l_cut, f->d_l_fa,
                   f->d_el_slot, f->d_fa_slot, f->d_dof_row, f->d_rowcnt, f->d_counts, f->d_bsum, f->d_bsum64,
                   f->d_elmat, f->d_famat, f->d_err, f->d_dom, f->d_ratio, f->d_bits, f->d_fbits,
-                  f->d_mtab_i, f->d_mtab_c, f->d_mu, f->d_mhat, f->d_cutlist};
+                  f->d_mtab_i, f->d_mtab_c, f->d_mu, f->d_mhat, f->d_cutlist, f->d_dof_flag};
   for (void* p : ptrs) cudaFree(p);
   delete f;
   return XG_OK;
@@ -3180,9 +3193,10 @@ int scatter_phase(xg_form* f, xg_csr* out, cudaStream_t s) {
   xg_space* sp = f->space;
   int st;
   // 3. active dofs -> rows
-  XG_CUDA(cudaMemsetAsync(f->d_dof_bits, 0, f->nw32_dof * 4, s));
-  k_mark_dofs<<<152 * 8, 256, 0, s>>>(m->ne, sp->nd, sp->d_el_dofs, f->d_l_un, f->d_l_cut, f->d_l_fa, f->d_counts,
-                                      m->nfacets, m->d_facet_els, f->d_dof_bits);
+  k_mark_dofs<<<152 * 8, 256, 0, s>>>(m->ne, sp->nd, sp->d_el_dofs_aos, f->d_l_un, f->d_l_cut, f->d_l_fa,
+                                      f->d_counts, m->nfacets, m->d_facet_els, f->d_dof_flag);
+  k_pack_dofs<<<(unsigned)((f->nw32_dof * 32 + 255) / 256), 256, 0, s>>>(f->d_dof_flag, sp->ndof, f->d_dof_bits,
+                                                                        f->nw32_dof);
   if ((st = compact(f, f->d_dof_bits, f->nw32_dof, out->d_row_dof, f->d_dof_row, f->d_counts + 3, s))) return st;
   // 4. pattern and values
   ScatterArgs A = scatter_args(f);
@@ -3457,6 +3471,7 @@ int form_workspace(xg_form* f) {
   e = e ? e : A((void**)&f->d_l_cut, (size_t)m->ne * 4);
   e = e ? e : A((void**)&f->d_l_fa, (size_t)m->nfacets * 4);
   e = e ? e : A((void**)&f->d_cutlist, ((size_t)m->ne + 1) * 4);
+  e = e ? e : A((void**)&f->d_dof_flag, (size_t)space->ndof);
   e = e ? e : A((void**)&f->d_el_slot, (size_t)m->ne * 4);
   e = e ? e : A((void**)&f->d_fa_slot, (size_t)m->nfacets * 4);
   e = e ? e : A((void**)&f->d_dof_row, (size_t)space->ndof * 4);
@@ -3485,6 +3500,7 @@ int form_workspace(xg_form* f) {
   e = e ? e : A((void**)&f->d_bits, (size_t)8 * (f->nw32_el / 2) * 8);
   e = e ? e : A((void**)&f->d_fbits, (size_t)(f->nw32_fa / 2) * 8);
   if (e == cudaSuccess) e = cudaMemset(f->d_err, 0, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(f->d_dof_flag, 0, (size_t)space->ndof);
   if (e == cudaSuccess) e = cudaMemset(f->d_counts, 0, 8 * sizeof(int));
   if (e != cudaSuccess) return cuda_fail(e, "xg_form_create");
   int pst = full_pattern_probe(f, full_ptr);

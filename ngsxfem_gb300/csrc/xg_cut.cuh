@@ -113,10 +113,7 @@ __device__ __forceinline__ double simplex_volume(const P3* p, int np) {
 // Writes up to 3 sub-simplices; sub-simplex dimension is D (NEG/POS) or D-1 (IF).
 // Returns #sub-simplices or a negative xg error.
 template <int D>
-__device__ __forceinline__ int decompose(const double* l, int dt, Sub* subs) {
-  P3 cut[4];
-  int nc = calc_if_points<D>(l, cut);
-  if (nc < 0) return nc;
+__device__ __forceinline__ int decompose_cuts(const double* l, int dt, const P3* cut, int nc, Sub* subs) {
   P3 s[D + 1];
 #pragma unroll
   for (int i = 0; i <= D; i++)
@@ -164,6 +161,15 @@ __device__ __forceinline__ int decompose(const double* l, int dt, Sub* subs) {
     return 3;
   }
   return -XG_ERR_BAD_DECOMP;
+}
+
+// Decompose with the cut points of the level set (calc_if_points).
+template <int D>
+__device__ __forceinline__ int decompose(const double* l, int dt, Sub* subs) {
+  P3 cut[4];
+  const int nc = calc_if_points<D>(l, cut);
+  if (nc < 0) return nc;
+  return decompose_cuts<D>(l, dt, cut, nc, subs);
 }
 
 // Affine element geometry: x(xi) = x_D + F xi with F(:,k) = x_k - x_D.

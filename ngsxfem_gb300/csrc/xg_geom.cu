@@ -106,11 +106,13 @@ __global__ void __launch_bounds__(128) k_cutinfo_cut(int ne, const int32_t* __re
 #pragma unroll
     for (int i = 0; i <= D; i++) l[i] = __ldg(&lset[__ldg(&elv[(int64_t)i * ne + e])]);
     double part_vol[2] = {0.0, 0.0};
+    P3 cut[4];
+    const int nc = calc_if_points<D>(l, cut);  // shared by both passes
 #pragma unroll
     for (int pass = 0; pass < 2; pass++) {
       const int np = pass == 0 ? XG_POS : XG_NEG;
       Sub subs[3];
-      int ns = decompose<D>(l, np, subs);
+      int ns = nc < 0 ? nc : decompose_cuts<D>(l, np, cut, nc, subs);
       if (ns < 0) {
         set_err(err, -ns);
         ns = 0;
