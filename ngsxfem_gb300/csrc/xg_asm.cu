@@ -2318,7 +2318,7 @@ __global__ void __launch_bounds__(256) k_row_flagcount(ScatterArgs A, int64_t* _
 // (adjacency order; per entry its element row, then its active facets) over
 // the row's full-pattern positions, then written compressed to the active
 // columns in ascending order.
-template <typename T, bool SYM, bool ST>
+template <typename T, bool SYM, bool ST, int QQ>
 __global__ void __launch_bounds__(kRowWarps * 32) k_row_sum(ScatterArgs A, const T* __restrict__ elmat,
                                                              const T* __restrict__ famat,
                                                              const int64_t* __restrict__ rowptr,
@@ -2375,11 +2375,13 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_row_sum(ScatterArgs A, const
         const int gb = min(gpb, ng - g0);
         LaneIdx L;
         L.init(lane, nd);
-        for (int t0 = lane; t0 < gb * nd; t0 += 128) {
-          double vq[4];
-          int pq[4];
+        // QQ (position, value) loads per lane in flight: 6 for rows of 10 or more
+        // dofs per element, 4 below (measured; 8 is slower, registers)
+        for (int t0 = lane; t0 < gb * nd; t0 += 32 * QQ) {
+          double vq[QQ];
+          int pq[QQ];
 #pragma unroll
-          for (int q = 0; q < 4; q++) {
+          for (int q = 0; q < QQ; q++) {
             const int t = t0 + 32 * q;
             const bool in = t < gb * nd;
             const int g = g0 + (in ? L.g : gb - 1), j = in ? L.j : nd - 1;
@@ -2423,7 +2425,7 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_row_sum(ScatterArgs A, const
             pq[q] = in ? pos : -1;
           }
 #pragma unroll
-          for (int q = 0; q < 4; q++) {
+          for (int q = 0; q < QQ; q++) {
             const int t = t0 + 32 * q;
             if (t < gb * nd) {
               S.spos[t] = pq[q];
@@ -3217,10 +3219,17 @@ int scatter_phase(xg_form* f, xg_csr* out, cudaStream_t s) {
   A.stage = f->sc_stage;
   A.wbytes = f->sm_wbytes;
   const bool st_form = A.kt1 > 1;
-#define XG_ROW_SUM(TT, SY, STF)                                                                               \
-  k_row_sum<TT, SY, STF><<<f->grid_sm, kRowWarps * 32, f->sm_smem, s>>>(A, (const TT*)f->d_elmat,           \
-                                                                        (const TT*)f->d_famat, out->d_rowptr, \
-                                                                        out->d_cols, out->d_vals, out->cap_nnz, f->d_err)
+#define XG_ROW_SUM(TT, SY, STF)                                                                                \
+  do {                                                                                                       \
+    if (sp->nd >= 10)                                                                                        \
+      k_row_sum<TT, SY, STF, 6><<<f->grid_sm, kRowWarps * 32, f->sm_smem, s>>>(                              \
+          A, (const TT*)f->d_elmat, (const TT*)f->d_famat, out->d_rowptr, out->d_cols, out->d_vals,          \
+          out->cap_nnz, f->d_err);                                                                           \
+    else                                                                                                     \
+      k_row_sum<TT, SY, STF, 4><<<f->grid_sm, kRowWarps * 32, f->sm_smem, s>>>(                              \
+          A, (const TT*)f->d_elmat, (const TT*)f->d_famat, out->d_rowptr, out->d_cols, out->d_vals,          \
+          out->cap_nnz, f->d_err);                                                                           \
+  } while (0)
   if (f->precision == XG_PREC_FP64) {
     if (st_form) XG_ROW_SUM(double, false, true);
     else if (A.el_sym) XG_ROW_SUM(double, true, false);
@@ -3551,12 +3560,18 @@ int form_workspace(xg_form* f) {
     if (f->sm_smem > raised_sm) {
       const int sm = (int)f->sm_smem;
       const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
-      bad |= cudaFuncSetAttribute(k_row_sum<double, false, false>, at, sm) != 0;
-      bad |= cudaFuncSetAttribute(k_row_sum<double, true, false>, at, sm) != 0;
-      bad |= cudaFuncSetAttribute(k_row_sum<double, false, true>, at, sm) != 0;
-      bad |= cudaFuncSetAttribute(k_row_sum<float, false, false>, at, sm) != 0;
-      bad |= cudaFuncSetAttribute(k_row_sum<float, true, false>, at, sm) != 0;
-      bad |= cudaFuncSetAttribute(k_row_sum<float, false, true>, at, sm) != 0;
+      bad |= cudaFuncSetAttribute(k_row_sum<double, false, false, 4>, at, sm) != 0;
+      bad |= cudaFuncSetAttribute(k_row_sum<double, true, false, 4>, at, sm) != 0;
+      bad |= cudaFuncSetAttribute(k_row_sum<double, false, true, 4>, at, sm) != 0;
+      bad |= cudaFuncSetAttribute(k_row_sum<float, false, false, 4>, at, sm) != 0;
+      bad |= cudaFuncSetAttribute(k_row_sum<float, true, false, 4>, at, sm) != 0;
+      bad |= cudaFuncSetAttribute(k_row_sum<float, false, true, 4>, at, sm) != 0;
+      bad |= cudaFuncSetAttribute(k_row_sum<double, false, false, 6>, at, sm) != 0;
+      bad |= cudaFuncSetAttribute(k_row_sum<double, true, false, 6>, at, sm) != 0;
+      bad |= cudaFuncSetAttribute(k_row_sum<double, false, true, 6>, at, sm) != 0;
+      bad |= cudaFuncSetAttribute(k_row_sum<float, false, false, 6>, at, sm) != 0;
+      bad |= cudaFuncSetAttribute(k_row_sum<float, true, false, 6>, at, sm) != 0;
+      bad |= cudaFuncSetAttribute(k_row_sum<float, false, true, 6>, at, sm) != 0;
       raised_sm = f->sm_smem;
     }
     if (bad) {
@@ -3564,7 +3579,7 @@ int form_workspace(xg_form* f) {
       return XG_ERR_CAPACITY;
     }
   }
-  f->grid_sm = grid_for(k_row_sum<double, false, false>, kRowWarps * 32, f->sm_smem);
+  f->grid_sm = grid_for(k_row_sum<double, false, false, 4>, kRowWarps * 32, f->sm_smem);
   return full_pattern_build(f);
 }
 
