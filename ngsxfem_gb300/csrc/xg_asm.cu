@@ -1002,7 +1002,13 @@ __global__ void __launch_bounds__(CutCfg<D, K, SYM, T>::NT) k_elmat_cut(
 // FP64 operations of evaluating the functions at every point.
 // ---------------------------------------------------------------------------
 constexpr int kMaxMomDeg = 6;   // 2K for K <= 3
-constexpr int kMomEPB = 16, kMomCHP = 8, kMomPts = kMomEPB * kMomCHP, kMomNT = 256;
+constexpr int kMomPts = 128, kMomNT = 256;  // points per chunk of a block, threads
+// elements per block of the moment kernel (x points per element = kMomPts):
+// 8 x 16 for tets, 16 x 8 for triangles (measured)
+template <int D>
+__host__ __device__ constexpr int mom_epb() {
+  return D == 3 ? 8 : 16;
+}
 constexpr int kEntEPB = 32, kEntNT = 256;
 
 __host__ __device__ constexpr int pair_count(int d) { return (d + 1) * (d + 2) / 2; }
@@ -1068,6 +1074,7 @@ __global__ void __launch_bounds__(kMomNT) k_cut_moments(MomDesc md, const CutGeo
                                                          const CutSubS* __restrict__ cs,
                                                          const int* __restrict__ counts, int64_t cap,
                                                          T* __restrict__ mu) {
+  constexpr int kMomEPB = mom_epb<D>(), kMomCHP = kMomPts / kMomEPB;
   extern __shared__ __align__(16) unsigned char mo_smem[];
   T* A = (T*)mo_smem;                // [kMomPts][NA]: w lambda0^e0 lambda1^e1
   T* B = A + kMomPts * md.NA;        // [kMomPts][NB]: lambda2^e2 lambda3^e3 (3D), lambda2^e2 (2D)
