@@ -525,8 +525,8 @@ class Clocks:
 # DRAM bytes (read + write) per launch of the dominant kernel from one ncu
 # capture of the same workload (profiles/cutfem_step_3d_poisson_64cube_p2_fp64.md,
 # profiles/st_elmat_spacetime_256sq_p1p1_fp64.md)
-TRAFFIC = {("c2", "patch"): 35.128576e6 + 153.694208e6, ("c2", "scatter"): 721.479168e6 + 100.113664e6,
-           ("c2", "elmat_cut"): 33.021440e6 + 23.297280e6 + 28.007680e6 + 0.011776e6 + 36.972032e6 + 3.339776e6}
+TRAFFIC = {("c2", "patch"): 34.675968e6 + 153.309696e6, ("c2", "scatter"): 707.318272e6 + 99.713536e6,
+           ("c2", "elmat_cut"): 13.181184e6 + 9.851904e6 + 28.001792e6 + 0.007424e6 + 35.953920e6 + 2.345728e6}
 
 
 def patch_exact_flops(dim, k):
