@@ -1619,9 +1619,15 @@ template <int D, int K, typename T>
 struct PxSmem {
   static constexpr int N = PxCfg<D, K>::N, E = PxCfg<D, K>::E, F = PxCfg<D, K>::FPB;
   T Ct[2][N][N][F];  // [0]: C21 (T2's functions in T1's canonical basis), [1]: C12
-  T Wt[2][N][N][F];  // Mh C
-  T nodes[2][N][D + 1][F];
-  T L[2][D + 1][D + 1][F];  // [0]: L21, [1]: L12
+  // W = Mh C, written once C is complete, shares its storage with the maps and
+  // node images, which are needed only to build C (two blocks fit an SM)
+  union {
+    T Wt[2][N][N][F];
+    struct {
+      T nodes[2][N][D + 1][F];
+      T L[2][D + 1][D + 1][F];  // [0]: L21, [1]: L12
+    } pre;
+  };
   T det1[F], det2[F], c[F];
   int gv1[D + 1][F], gv2[D + 1][F];
   int idx[F];
@@ -1665,8 +1671,8 @@ __global__ void __launch_bounds__(256) k_patch_exact(FormDesc form, const PaGeoS
         for (int i = 0; i <= D; i++)
 #pragma unroll
           for (int b = 0; b <= D; b++) {
-            sm.L[0][i][b][threadIdx.x] = G.L21[i][b];
-            sm.L[1][i][b][threadIdx.x] = G.L12[i][b];
+            sm.pre.L[0][i][b][threadIdx.x] = G.L21[i][b];
+            sm.pre.L[1][i][b][threadIdx.x] = G.L12[i][b];
           }
         sm.det1[threadIdx.x] = G.det1;
         sm.det2[threadIdx.x] = G.det2;
@@ -1687,9 +1693,9 @@ __global__ void __launch_bounds__(256) k_patch_exact(FormDesc form, const PaGeoS
       const int sd = u / N, n = u % N;
       if (!live) continue;
       T out[D + 1];
-      node_image<D, K, T>(n, &sm.L[sd][0][0][f], (D + 1) * F, F, out);
+      node_image<D, K, T>(n, &sm.pre.L[sd][0][0][f], (D + 1) * F, F, out);
 #pragma unroll
-      for (int i = 0; i <= D; i++) sm.nodes[sd][n][i][f] = out[i];
+      for (int i = 0; i <= D; i++) sm.pre.nodes[sd][n][i][f] = out[i];
     }
     __syncthreads();
     // column j of C: function j of the other element in this element's canonical basis
@@ -1705,7 +1711,7 @@ __global__ void __launch_bounds__(256) k_patch_exact(FormDesc form, const PaGeoS
       for (int n = 0; n < N; n++) {
         T lam[D + 1];
 #pragma unroll
-        for (int i = 0; i <= D; i++) lam[i] = sm.nodes[sd][n][i][f];
+        for (int i = 0; i <= D; i++) lam[i] = sm.pre.nodes[sd][n][i][f];
         p[n] = eval_fn_value<D, T>(desc, lam);
       }
       nodal_to_hier<D, K, T>(p, fn_degree(desc), &sm.Ct[sd][0][j][f], N * F);
