@@ -49,7 +49,9 @@ typedef enum {
   XG_ERR_BAD_DECOMP = 5,   /* unsupported cut topology: straightcutrule.cpp:148,193 */
   XG_ERR_UNSUPPORTED = 6,  /* element type / order / term not supported */
   XG_ERR_NONFINITE = 7,    /* a non-finite weight or matrix entry was produced */
-  XG_ERR_NO_DEVICE = 8     /* no CUDA device, or the library was not built for it */
+  XG_ERR_NO_DEVICE = 8,    /* no CUDA device, or the library was not built for it */
+  XG_ERR_IF_BOUND = 9      /* quad / hex interface scaling above 1/sqrt(1-0.999^2):
+                              straightcutrule.cpp:273-286 */
 } xg_status;
 
 enum { XG_NEG = 0, XG_POS = 1, XG_IF = 2 };
@@ -104,6 +106,14 @@ int xg_device_ok(int* ok);
  * h_coords: nv*dim (AoS), h_elv: ne*(dim+1).  dim 2 (trig) or 3 (tet). */
 int xg_mesh_create(int dim, int32_t nv, const double* h_coords, int32_t ne, const int32_t* h_elv,
                    xg_mesh** out);
+/* Quadrilateral (dim 2) or hexahedral (dim 3) mesh: h_elv ne*2^dim with the
+ * corner order (0,0),(1,0),(1,1),(0,1) [then the same at z = 1]
+ * (cutint/straightcutrule.hpp:76-90); the element map is the bilinear /
+ * trilinear interpolation of the corners.  Such a mesh serves xg_cut_rules(_ex)
+ * and xg_integrate(_ex); entry points that need facet topology or H1 spaces
+ * return XG_ERR_UNSUPPORTED for it. */
+int xg_mesh_create_tensor(int dim, int32_t nv, const double* h_coords, int32_t ne, const int32_t* h_elv,
+                          xg_mesh** out);
 int xg_mesh_destroy(xg_mesh* mesh);
 /* out: [dim, nv, ne, nedges, nfaces, nfacets] */
 int xg_mesh_info(const xg_mesh* mesh, int64_t* h_out6);
@@ -172,6 +182,19 @@ int xg_elements_with_neighbor_facets(xg_mesh* mesh, const uint64_t* d_facets, ui
  * |F^-T n_ref|, to be multiplied by |det F|). */
 int xg_cut_rules(xg_mesh* mesh, const double* d_lset, const int32_t* d_elems, int32_t n, int dt, int order,
                  int32_t max_pts, int32_t* d_counts, double* d_pts, double* d_wts, void* stream);
+/* Direction policy of the quadrilateral / hexahedral rules
+ * (SWAP_DIMENSIONS_POLICY, utils/ngsxstd.hpp:10; Python FIRST / OPTIMAL /
+ * FALLBACK).  xg_cut_rules and xg_integrate use FIND_OPTIMAL, the reference's
+ * default (cutint/lsetintdomain.hpp:21); simplex meshes ignore it. */
+enum { XG_QUAD_FIRST_ALLOWED = 0, XG_QUAD_FIND_OPTIMAL = 1, XG_QUAD_ALWAYS_NONE = 2 };
+/* xg_cut_rules with the direction policy: LevelsetCutQuadrilateral
+ * (cutint/straightcutrule.cpp:206-501) on quadrilateral / hexahedral meshes. */
+int xg_cut_rules_ex(xg_mesh* mesh, const double* d_lset, const int32_t* d_elems, int32_t n, int dt, int order,
+                    int quad_dir_policy, int32_t max_pts, int32_t* d_counts, double* d_pts, double* d_wts,
+                    void* stream);
+/* Most points a quadrilateral (dim 2) / hexahedral (dim 3) rule of (dt, order)
+ * can have (a sufficient max_pts), or -1 for bad arguments. */
+int xg_quad_rule_capacity(int dim, int dt, int order);
 /* Number of points of the rule family for (element dim d, order p). */
 int xg_base_rule_size(int d, int p);
 /* Host copy of that rule (NGSolve's SelectIntegrationRule(ET, p) stand-in):
@@ -197,6 +220,9 @@ int xg_integrate(xg_mesh* mesh, const double* d_lset, int dt, int order, int ex,
  * calls share the array: calls that overlap on the GPU (different streams,
  * concurrent graphs) race and must be serialised by the caller.  The result
  * equals xg_integrate's up to the summation order (a fixed order per mesh). */
+/* xg_integrate with the quadrilateral / hexahedral direction policy. */
+int xg_integrate_ex(xg_mesh* mesh, const double* d_lset, int dt, int order, int quad_dir_policy, int ex, int ey,
+                    int ez, const uint64_t* d_defined_on, double* d_result, void* stream);
 int xg_integrate_noalloc(xg_mesh* mesh, const double* d_lset, int dt, int order, int ex, int ey, int ez,
                          const uint64_t* d_defined_on, double* d_result, void* stream);
 

@@ -15,7 +15,7 @@ STATUS = {
     0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "capacity exceeded",
     4: "cut requested on an uncut (sub-)simplex", 5: "unsupported cut topology",
     6: "unsupported element, order or term", 7: "non-finite weight or matrix entry",
-    8: "no usable CUDA device",
+    8: "no usable CUDA device", 9: "quadrilateral interface scaling factor above its bound",
 }
 
 # every symbol include/xg.h declares, checked by the CPU test suite
@@ -26,6 +26,7 @@ EXPORTS = [
     "xg_interpolate_p1_perturb", "xg_cutinfo_update", "xg_mesh_check",
     "xg_facets_with_neighbor_types", "xg_elements_with_neighbor_facets",
     "xg_cut_rules", "xg_base_rule_size", "xg_base_rule", "xg_integrate", "xg_integrate_noalloc",
+    "xg_mesh_create_tensor", "xg_cut_rules_ex", "xg_quad_rule_capacity", "xg_integrate_ex",
     "xg_form_create", "xg_form_destroy", "xg_form_set_defined_on", "xg_form_capacity",
     "xg_form_assemble", "xg_form_check", "xg_form_stage_events", "xg_cutfem_step", "xg_cutfem_marking",
     "xg_space_create_st", "xg_space_info_st", "xg_cutinfo_update_st", "xg_st_cut_rules", "xg_st_form_create",
@@ -105,6 +106,7 @@ def load():
         "xg_last_error": (ctypes.c_char_p, []),
         "xg_device_ok": (I, [P]),
         "xg_mesh_create": (I, [I, ctypes.c_int32, P, ctypes.c_int32, P, P]),
+        "xg_mesh_create_tensor": (I, [I, ctypes.c_int32, P, ctypes.c_int32, P, P]),
         "xg_mesh_destroy": (I, [P]),
         "xg_mesh_info": (I, [P, P]),
         "xg_mesh_facet_elements": (I, [P, P]),
@@ -118,9 +120,12 @@ def load():
         "xg_facets_with_neighbor_types": (I, [P, P, P, I, I, I, P, P]),
         "xg_elements_with_neighbor_facets": (I, [P, P, P, P]),
         "xg_cut_rules": (I, [P, P, P, ctypes.c_int32, I, I, ctypes.c_int32, P, P, P, P]),
+        "xg_cut_rules_ex": (I, [P, P, P, ctypes.c_int32, I, I, I, ctypes.c_int32, P, P, P, P]),
+        "xg_quad_rule_capacity": (I, [I, I, I]),
         "xg_base_rule_size": (I, [I, I]),
         "xg_base_rule": (I, [I, I, P, P, I]),
         "xg_integrate": (I, [P, P, I, I, I, I, I, P, P, P]),
+        "xg_integrate_ex": (I, [P, P, I, I, I, I, I, I, P, P, P]),
         "xg_integrate_noalloc": (I, [P, P, I, I, I, I, I, P, P, P]),
         "xg_form_create": (I, [P, P, ctypes.c_int32, I, P]),
         "xg_form_destroy": (I, [P]),

@@ -27,6 +27,7 @@ int ensure_device_rules() {
   int st = upload_rules_asm();
   if (!st) st = upload_rules_st();
   if (!st) st = upload_rules_lf();
+  if (!st) st = upload_rules_quad();
   if (st) return st;
   done.push_back(dev);
   return XG_OK;
@@ -614,6 +615,13 @@ static int launch_check(const char* what) {
 
 static inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
+// entry points that need simplices (facet topology, the simplex cut kernels)
+static int need_simplices(const xg_mesh* m, const char* what) {
+  if (!m->tensor) return XG_OK;
+  set_last_error(std::string(what) + ": quadrilateral / hexahedral meshes support xg_cut_rules and xg_integrate only");
+  return XG_ERR_UNSUPPORTED;
+}
+
 extern "C" {
 
 int xg_interpolate_p1_perturb(double* d_vals, int64_t n, double eps, void* stream) {
@@ -628,6 +636,7 @@ int xg_interpolate_p1_perturb(double* d_vals, int64_t n, double eps, void* strea
 int xg_cutinfo_update(xg_mesh* m, const double* d_lset, uint8_t* d_dom, double* d_ratio, uint64_t* d_bits,
                       void* stream) {
   if (!m) return XG_ERR_ARG;
+  if (int st_t = need_simplices(m, "xg_cutinfo_update")) return st_t;
   return xg::cutinfo_update_ws(m, d_lset, d_dom, d_ratio, d_bits, m->d_cutlist, stream);
 }
 }  // extern "C"
@@ -652,6 +661,7 @@ extern "C" {
 int xg_cutinfo_update_bnd(xg_mesh* m, const double* d_lset, uint8_t* d_dom, double* d_ratio, uint64_t* d_bits,
                           void* stream) {
   if (!m || !d_lset || !d_dom || !d_ratio || !d_bits) return XG_ERR_ARG;
+  if (int st_t = need_simplices(m, "xg_cutinfo_update_bnd")) return st_t;
   if (m->nbnd == 0) return XG_OK;
   const int64_t nw64 = (m->nbnd + 63) / 64;
   cudaStream_t s = (cudaStream_t)stream;
@@ -669,6 +679,7 @@ int xg_cutinfo_nodes(xg_mesh* m, const uint8_t* d_dom, const double* d_ratio, ui
   if (!m || !d_dom || !d_ratio || !d_nb_v || !d_nb_e || !d_nb_el || !d_dom_v || !d_dom_e || !d_dom_cell ||
       (m->dim == 3 && (!d_nb_f || !d_dom_f)))
     return XG_ERR_ARG;
+  if (int st_t = need_simplices(m, "xg_cutinfo_nodes")) return st_t;
   cudaStream_t s = (cudaStream_t)stream;
   XG_CUDA(cudaMemsetAsync(d_nb_v, 0, sizeof(uint64_t) * ((m->nv + 63) / 64), s));
   XG_CUDA(cudaMemsetAsync(d_nb_e, 0, sizeof(uint64_t) * ((m->nedges + 63) / 64), s));
@@ -708,6 +719,7 @@ int xg_mesh_check(xg_mesh* m) {
 int xg_facets_with_neighbor_types(xg_mesh* m, const uint64_t* d_a, const uint64_t* d_b, int bnd_a, int bnd_b,
                                   int use_and, uint64_t* d_out, void* stream) {
   if (!m || !d_a || !d_b || !d_out) return XG_ERR_ARG;
+  if (int st_t = need_simplices(m, "xg_facets_with_neighbor_types")) return st_t;
   const int64_t nw64 = (m->nfacets + 63) / 64;
   k_facet_mark<<<nblk(nw64 * 64, 256), 256, 0, (cudaStream_t)stream>>>(m->nfacets, m->d_facet_els, d_a, d_b, bnd_a,
                                                                        bnd_b, use_and, (uint32_t*)d_out, 2 * nw64);
@@ -716,6 +728,7 @@ int xg_facets_with_neighbor_types(xg_mesh* m, const uint64_t* d_a, const uint64_
 
 int xg_elements_with_neighbor_facets(xg_mesh* m, const uint64_t* d_facets, uint64_t* d_out, void* stream) {
   if (!m || !d_facets || !d_out) return XG_ERR_ARG;
+  if (int st_t = need_simplices(m, "xg_elements_with_neighbor_facets")) return st_t;
   cudaStream_t s = (cudaStream_t)stream;
   XG_CUDA(cudaMemsetAsync(d_out, 0, sizeof(uint64_t) * ((m->ne + 63) / 64), s));
   k_el_nbr_facets<<<nblk(m->nfacets, 256), 256, 0, s>>>(m->nfacets, m->d_facet_els, d_facets,
@@ -723,12 +736,15 @@ int xg_elements_with_neighbor_facets(xg_mesh* m, const uint64_t* d_facets, uint6
   return launch_check("k_el_nbr_facets");
 }
 
-int xg_cut_rules(xg_mesh* m, const double* d_lset, const int32_t* d_elems, int32_t n, int dt, int order,
-                 int32_t max_pts, int32_t* d_counts, double* d_pts, double* d_wts, void* stream) {
+int xg_cut_rules_ex(xg_mesh* m, const double* d_lset, const int32_t* d_elems, int32_t n, int dt, int order,
+                    int quad_dir_policy, int32_t max_pts, int32_t* d_counts, double* d_pts, double* d_wts,
+                    void* stream) {
   if (!m || !d_lset || !d_elems || n < 0 || dt < 0 || dt > 2 || order < 0 || order > kMaxOrder || max_pts <= 0 ||
-      !d_counts || !d_pts || !d_wts)
+      !d_counts || !d_pts || !d_wts || quad_dir_policy < 0 || quad_dir_policy > 2)
     return XG_ERR_ARG;
   if (n == 0) return XG_OK;
+  if (m->tensor)
+    return quad_cut_rules(m, d_lset, d_elems, n, dt, order, quad_dir_policy, max_pts, d_counts, d_pts, d_wts, stream);
   cudaStream_t s = (cudaStream_t)stream;
   if (m->dim == 2)
     k_cut_rules<2><<<nblk(n, 128), 128, 0, s>>>(m->ne, m->d_elv, m->d_xyz, m->nv, d_lset, d_elems, n, dt, order,
@@ -739,10 +755,24 @@ int xg_cut_rules(xg_mesh* m, const double* d_lset, const int32_t* d_elems, int32
   return launch_check("k_cut_rules");
 }
 
-int xg_integrate(xg_mesh* m, const double* d_lset, int dt, int order, int ex, int ey, int ez,
-                 const uint64_t* d_defined_on, double* d_result, void* stream) {
-  if (!m || !d_lset || !d_result || dt < 0 || dt > 2 || order < 0 || order > kMaxOrder || ex < 0 || ey < 0 || ez < 0)
+int xg_cut_rules(xg_mesh* m, const double* d_lset, const int32_t* d_elems, int32_t n, int dt, int order,
+                 int32_t max_pts, int32_t* d_counts, double* d_pts, double* d_wts, void* stream) {
+  return xg_cut_rules_ex(m, d_lset, d_elems, n, dt, order, XG_QUAD_FIND_OPTIMAL, max_pts, d_counts, d_pts, d_wts,
+                         stream);
+}
+
+int xg_quad_rule_capacity(int dim, int dt, int order) {
+  if ((dim != 2 && dim != 3) || dt < 0 || dt > 2 || order < 0 || order > kMaxOrder) return -1;
+  return quad_rule_capacity(dim, dt, order);
+}
+
+int xg_integrate_ex(xg_mesh* m, const double* d_lset, int dt, int order, int quad_dir_policy, int ex, int ey, int ez,
+                    const uint64_t* d_defined_on, double* d_result, void* stream) {
+  if (!m || !d_lset || !d_result || dt < 0 || dt > 2 || order < 0 || order > kMaxOrder || ex < 0 || ey < 0 ||
+      ez < 0 || quad_dir_policy < 0 || quad_dir_policy > 2)
     return XG_ERR_ARG;
+  if (m->tensor)
+    return quad_integrate(m, d_lset, dt, order, quad_dir_policy, ex, ey, ez, d_defined_on, d_result, stream);
   cudaStream_t s = (cudaStream_t)stream;
   const int nb = 152 * 4;
   if (m->scratch_bytes < nb * sizeof(double)) {
@@ -763,9 +793,15 @@ int xg_integrate(xg_mesh* m, const double* d_lset, int dt, int order, int ex, in
   return launch_check("k_integrate");
 }
 
+int xg_integrate(xg_mesh* m, const double* d_lset, int dt, int order, int ex, int ey, int ez,
+                 const uint64_t* d_defined_on, double* d_result, void* stream) {
+  return xg_integrate_ex(m, d_lset, dt, order, XG_QUAD_FIND_OPTIMAL, ex, ey, ez, d_defined_on, d_result, stream);
+}
+
 int xg_cutinfo_update_st(xg_mesh* m, const double* d_lset_st, int kt_lset, uint8_t* d_dom, double* d_ratio,
                          uint64_t* d_bits, void* stream) {
   if (!m) return XG_ERR_ARG;
+  if (int st_t = need_simplices(m, "xg_cutinfo_update_st")) return st_t;
   return xg::cutinfo_update_st_ws(m, d_lset_st, kt_lset, d_dom, d_ratio, d_bits, m->d_cutlist, stream);
 }
 }  // extern "C"
@@ -802,6 +838,7 @@ int xg_st_cut_rules(xg_mesh* m, const double* d_lset_st, int kt_lset, const int3
       order_space > kMaxOrder || order_time < 0 || order_time > kMaxOrder || max_pts <= 0 || !d_counts || !d_pts ||
       !d_wts)
     return XG_ERR_ARG;
+  if (int st_t = need_simplices(m, "xg_st_cut_rules")) return st_t;
   if (n == 0) return XG_OK;
   cudaStream_t s = (cudaStream_t)stream;
   if (m->dim == 2)
@@ -817,6 +854,7 @@ int xg_integrate_noalloc(xg_mesh* m, const double* d_lset, int dt, int order, in
                          const uint64_t* d_defined_on, double* d_result, void* stream) {
   if (!m || !d_lset || !d_result || dt < 0 || dt > 2 || order < 0 || order > kMaxOrder || ex < 0 || ey < 0 || ez < 0)
     return XG_ERR_ARG;
+  if (int st_t = need_simplices(m, "xg_integrate_noalloc")) return st_t;
   const int64_t nb64 = (m->ne + kNoAllocElemsPerBlock - 1) / kNoAllocElemsPerBlock;
   if (nb64 > kNoAllocMaxBlocks) {
     set_last_error("xg_integrate_noalloc: the mesh has " + std::to_string(m->ne) + " elements; the static scratch of " +

@@ -210,6 +210,7 @@ const char* xg_status_string(int s) {
     case XG_ERR_UNSUPPORTED: return "unsupported element, order or term";
     case XG_ERR_NONFINITE: return "non-finite weight or matrix entry";
     case XG_ERR_NO_DEVICE: return "no usable CUDA device";
+    case XG_ERR_IF_BOUND: return "quadrilateral interface scaling factor above its bound";
   }
   return "unknown status";
 }
@@ -395,6 +396,44 @@ int xg_mesh_create(int dim, int32_t nv, const double* h_coords, int32_t ne, cons
   return XG_OK;
 }
 
+int xg_mesh_create_tensor(int dim, int32_t nv, const double* h_coords, int32_t ne, const int32_t* h_elv,
+                          xg_mesh** out) {
+  if (!out || (dim != 2 && dim != 3) || nv <= 0 || ne <= 0 || !h_coords || !h_elv) {
+    set_last_error("xg_mesh_create_tensor: bad arguments");
+    return XG_ERR_ARG;
+  }
+  *out = nullptr;
+  const int nvl = 1 << dim;
+  for (size_t i = 0; i < (size_t)ne * nvl; i++)
+    if (h_elv[i] < 0 || h_elv[i] >= nv) {
+      set_last_error("xg_mesh_create_tensor: vertex index out of range");
+      return XG_ERR_ARG;
+    }
+  auto* m = new xg_mesh();
+  m->dim = dim; m->nv = nv; m->ne = ne; m->tensor = 1;
+  cudaGetDevice(&m->device);
+  m->h_elv.assign(h_elv, h_elv + (size_t)ne * nvl);
+  std::vector<double> xyz((size_t)dim * nv);
+  for (int v = 0; v < nv; v++)
+    for (int c = 0; c < dim; c++) xyz[(size_t)c * nv + v] = h_coords[(size_t)v * dim + c];
+  int st = XG_OK;
+  if ((st = upload(&m->d_xyz, xyz)) || (st = upload(&m->d_elv, to_soa(m->h_elv, ne, nvl)))) {
+    xg_mesh_destroy(m);
+    return st;
+  }
+  if (cudaMalloc((void**)&m->d_err, sizeof(int)) != cudaSuccess || cudaMemset(m->d_err, 0, sizeof(int)) != cudaSuccess) {
+    xg_mesh_destroy(m);
+    set_last_error("xg_mesh_create_tensor: cudaMalloc failed");
+    return XG_ERR_CUDA;
+  }
+  if ((st = ensure_device_rules())) {
+    xg_mesh_destroy(m);
+    return st;
+  }
+  *out = m;
+  return XG_OK;
+}
+
 int xg_mesh_destroy(xg_mesh* m) {
   if (!m) return XG_OK;
   cudaFree(m->d_xyz);
@@ -435,6 +474,10 @@ int xg_space_create(xg_mesh* m, int order, xg_space** out) {
   if (!m || !out || order < 1 || order > 3) {
     set_last_error("xg_space_create: order must be 1..3");
     return XG_ERR_ARG;
+  }
+  if (m->tensor) {
+    set_last_error("xg_space_create: H1 spaces are built on simplex meshes only");
+    return XG_ERR_UNSUPPORTED;
   }
   *out = nullptr;
   auto* s = new xg_space();
@@ -494,6 +537,10 @@ int xg_space_create_st(xg_mesh* m, int order, int order_time, xg_space** out) {
   if (!m || !out || order < 1 || order > 3 || order_time < 0 || order_time > 2) {
     set_last_error("xg_space_create_st: space order 1..3, time order 0..2");
     return XG_ERR_ARG;
+  }
+  if (m->tensor) {
+    set_last_error("xg_space_create_st: space-time spaces are built on simplex meshes only");
+    return XG_ERR_UNSUPPORTED;
   }
   *out = nullptr;
   xg_space* sp = nullptr;

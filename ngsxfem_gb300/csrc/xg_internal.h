@@ -148,16 +148,25 @@ int cutinfo_update_ws(xg_mesh* m, const double* d_lset, uint8_t* d_dom, double* 
 int cutinfo_update_st_ws(xg_mesh* m, const double* d_lset_st, int kt_lset, uint8_t* d_dom, double* d_ratio,
                          uint64_t* d_bits, int32_t* cutlist, void* stream);
 
+// quadrilateral / hexahedral meshes (xg_quad.cu)
+int upload_rules_quad();
+int quad_rule_capacity(int dim, int dt, int order);
+int quad_cut_rules(xg_mesh* m, const double* d_lset, const int32_t* d_elems, int32_t n, int dt, int order, int pol,
+                   int32_t max_pts, int32_t* d_counts, double* d_pts, double* d_wts, void* stream);
+int quad_integrate(xg_mesh* m, const double* d_lset, int dt, int order, int pol, int ex, int ey, int ez,
+                   const uint64_t* d_defined_on, double* d_result, void* stream);
+
 }  // namespace xg
 
 // ---- objects behind the opaque handles ------------------------------------------
 struct xg_mesh {
   int dim = 0, nv = 0, ne = 0, device = 0;
+  int tensor = 0;  // 1: quadrilaterals / hexahedra (2^dim vertices, no facet topology)
   int64_t nedges = 0, nfaces = 0, nfacets = 0;
   int max_vertex_elems = 0;  // max elements sharing a vertex
   // device (SoA)
   double* d_xyz = nullptr;       // [dim][nv]
-  int32_t* d_elv = nullptr;      // [dim+1][ne]
+  int32_t* d_elv = nullptr;      // [dim+1][ne] ([2^dim][ne] for tensor meshes)
   int32_t* d_el_edges = nullptr; // [3|6][ne]
   int32_t* d_el_faces = nullptr; // [4][ne] (3D)
   int32_t* d_el_facets = nullptr;// [dim+1][ne] (alias of edges / faces)

@@ -10,8 +10,13 @@ own and is stated here:
   [v000, v000+e_a, v000+e_a+e_b, v111] for the 6 permutations (a, b, c) of the
   axes, which is conforming across cubes.
 
+With quads=True / hexes=True the cells are kept whole: a quadrilateral lists
+its vertices (p00, p10, p11, p01), a hexahedron the same square at z0, then
+at z1 (the corner order of cutint/straightcutrule.hpp:76-90).
+
 Vertices are numbered with x fastest.  Arrays are numpy: coords (nv, dim)
-float64, elements (ne, dim+1) int32.
+float64, elements (ne, dim+1) int32 for simplices, (ne, 2^dim) for
+quadrilaterals and hexahedra.
 """
 import itertools
 
@@ -19,14 +24,20 @@ import numpy as np
 
 
 class Mesh:
-    """A simplex mesh held on the host: vertex coordinates and element vertices."""
+    """A mesh held on the host: vertex coordinates and element vertices, either
+    simplices (trig / tet) or tensor cells (quad / hex)."""
 
     def __init__(self, coords, elements):
         self.coords = np.ascontiguousarray(coords, dtype=np.float64)
         self.elements = np.ascontiguousarray(elements, dtype=np.int32)
         self.dim = self.coords.shape[1]
-        if self.elements.shape[1] != self.dim + 1:
-            raise ValueError("only simplex meshes (trig / tet) are supported")
+        nve = self.elements.shape[1]
+        if nve == self.dim + 1:
+            self.tensor = False
+        elif nve == 2 ** self.dim and self.dim in (2, 3):
+            self.tensor = True
+        else:
+            raise ValueError("elements must be simplices (dim+1 vertices) or quads / hexes (2^dim vertices)")
         self._device = None
 
     @property
@@ -44,7 +55,7 @@ class Mesh:
         return self.nv
 
 
-def MakeStructured2DMesh(nx=10, ny=10, xmin=0.0, xmax=1.0, ymin=0.0, ymax=1.0):
+def MakeStructured2DMesh(nx=10, ny=10, xmin=0.0, xmax=1.0, ymin=0.0, ymax=1.0, quads=False):
     xs = np.linspace(xmin, xmax, nx + 1)
     ys = np.linspace(ymin, ymax, ny + 1)
     X, Y = np.meshgrid(xs, ys, indexing="xy")
@@ -56,13 +67,15 @@ def MakeStructured2DMesh(nx=10, ny=10, xmin=0.0, xmax=1.0, ymin=0.0, ymax=1.0):
     p10 = p00 + 1
     p01 = p00 + (nx + 1)
     p11 = p01 + 1
+    if quads:
+        return Mesh(coords, np.stack([p00, p10, p11, p01], axis=1))
     t1 = np.stack([p00, p10, p11], axis=1)
     t2 = np.stack([p00, p11, p01], axis=1)
     el = np.stack([t1, t2], axis=1).reshape(-1, 3)
     return Mesh(coords, el)
 
 
-def MakeStructured3DMesh(nx=4, ny=None, nz=None, box=((0.0, 1.0), (0.0, 1.0), (0.0, 1.0))):
+def MakeStructured3DMesh(nx=4, ny=None, nz=None, box=((0.0, 1.0), (0.0, 1.0), (0.0, 1.0)), hexes=False):
     ny = nx if ny is None else ny
     nz = nx if nz is None else nz
     xs = np.linspace(box[0][0], box[0][1], nx + 1)
@@ -74,6 +87,10 @@ def MakeStructured3DMesh(nx=4, ny=None, nz=None, box=((0.0, 1.0), (0.0, 1.0), (0
     base = (i + (nx + 1) * (j + (ny + 1) * k)).ravel()
     step = [1, nx + 1, (nx + 1) * (ny + 1)]
     v111 = base + sum(step)
+    if hexes:
+        sx, sy, sz = step
+        sq = [base, base + sx, base + sx + sy, base + sy]
+        return Mesh(coords, np.stack(sq + [v + sz for v in sq], axis=1))
     tets = []
     for perm in itertools.permutations(range(3)):
         a, b, _ = perm

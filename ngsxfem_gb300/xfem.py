@@ -25,6 +25,9 @@ from . import _lib
 from .meshes import Mesh, MakeStructured2DMesh, MakeStructured3DMesh  # noqa: F401
 
 NEG, POS, IF = 0, 1, 2
+# direction policy of the quadrilateral / hexahedral cut rules
+# (python/python_ngsxfem.cpp:35-37: FIRST_ALLOWED, FIND_OPTIMAL, ALWAYS_NONE)
+FIRST, OPTIMAL, FALLBACK = 0, 1, 2
 CDOM_NO, CDOM_NEG, CDOM_POS, CDOM_UNCUT, CDOM_IF, CDOM_HASNEG, CDOM_HASPOS, CDOM_ANY = range(8)
 UNCUT, HASNEG, HASPOS, ANY = CDOM_UNCUT, CDOM_HASNEG, CDOM_HASPOS, CDOM_ANY
 VOL, BND = "VOL", "BND"
@@ -58,7 +61,8 @@ class DeviceMesh:
         _dev()
         self.mesh = mesh
         h = ctypes.c_void_p()
-        _lib.call("xg_mesh_create", mesh.dim, mesh.nv, mesh.coords.ctypes.data_as(ctypes.c_void_p), mesh.ne,
+        create = "xg_mesh_create_tensor" if getattr(mesh, "tensor", False) else "xg_mesh_create"
+        _lib.call(create, mesh.dim, mesh.nv, mesh.coords.ctypes.data_as(ctypes.c_void_p), mesh.ne,
                   mesh.elements.ctypes.data_as(ctypes.c_void_p), ctypes.byref(h))
         self.h = h
         info = np.zeros(6, dtype=np.int64)
@@ -135,12 +139,20 @@ class BitArray:
 
 
 class H1:
-    """H1 space of order 1..3 on a simplex mesh (libxg dof numbering)."""
+    """H1 space of order 1..3 on a simplex mesh (libxg dof numbering); on a
+    quadrilateral / hexahedral mesh order 1 only (the vertex values of a
+    bilinear / trilinear level set), which the cut rules and Integrate use."""
 
     def __init__(self, mesh, order=1, dgjumps=False, **kwargs):
         self.mesh = mesh
         self.order = int(order)
         self.dm = device_mesh(mesh)
+        if getattr(mesh, "tensor", False):
+            if self.order != 1:
+                raise ValueError("H1 on quadrilateral / hexahedral meshes: order 1 only")
+            self.h = None
+            self.ndof, self.ndof_el = mesh.nv, mesh.elements.shape[1]
+            return
         h = ctypes.c_void_p()
         _lib.call("xg_space_create", self.dm.h, self.order, ctypes.byref(h))
         self.h = h
@@ -149,6 +161,8 @@ class H1:
         self.ndof, self.ndof_el = int(info[0]), int(info[1])
 
     def element_dofs(self):
+        if self.h is None:
+            return self.mesh.elements.copy()
         out = np.zeros((self.mesh.ne, self.ndof_el), dtype=np.int32)
         _lib.call("xg_space_element_dofs", self.h, out.ctypes.data_as(ctypes.c_void_p))
         return out
@@ -552,6 +566,7 @@ class _Measure:
         t = kw.get("time_order", -1)
         self.time_order = -1 if t is None else int(t)
         self.tref = kw.get("tref")
+        self.quad_dir_policy = int(kw.get("quad_dir_policy", OPTIMAL))
         if kw.get("downscale", 1.0) != 1.0:
             raise NotImplementedError("downscale != 1 is not supported")
 
@@ -571,6 +586,8 @@ def dCut(levelset, domain_type, order=None, subdivlvl=None, time_order=-1, level
         levelset = levelset_domain["levelset"]
         domain_type = levelset_domain["domain_type"]
         order = levelset_domain.get("order", order)
+        if "quad_dir_policy" in levelset_domain:
+            kwargs.setdefault("quad_dir_policy", levelset_domain["quad_dir_policy"])
     return _Measure("cut", levelset, domain_type, order, kwargs.pop("definedonelements", None),
                     subdivlvl=subdivlvl, time_order=time_order, **kwargs)
 
@@ -968,13 +985,16 @@ def Integrate(levelset_domain=None, cf=None, mesh=None, order=5, integrand=None)
     else:
         lset, dt = levelset_domain["levelset"], levelset_domain["domain_type"]
         order = levelset_domain.get("order", order)
+        policy = levelset_domain.get("quad_dir_policy", OPTIMAL)
         mono = cf if isinstance(cf, _Monomial) else _Monomial()
         defined = None
+    if integrand is not None:
+        policy = getattr(meas, "quad_dir_policy", OPTIMAL)
     mesh = mesh if mesh is not None else lset.space.mesh
     dm = device_mesh(mesh)
     res = torch.zeros(1, dtype=torch.float64, device=_dev())
-    _lib.call("xg_integrate", dm.h, _vp(_lset_vec(lset)), dt, order, mono.e[0], mono.e[1], mono.e[2],
-              _vp(defined.words) if defined is not None else None, _vp(res), _stream())
+    _lib.call("xg_integrate_ex", dm.h, _vp(_lset_vec(lset)), dt, order, int(policy), mono.e[0], mono.e[1],
+              mono.e[2], _vp(defined.words) if defined is not None else None, _vp(res), _stream())
     dm.check()
     return float(res.item())
 
@@ -982,12 +1002,17 @@ def Integrate(levelset_domain=None, cf=None, mesh=None, order=5, integrand=None)
 # ----------------------------------------------------------------------------
 # rule export
 # ----------------------------------------------------------------------------
-def CutIntegrationRules(mesh, levelset, elements, domain_type, order, max_pts=None):
+def CutIntegrationRules(mesh, levelset, elements, domain_type, order, max_pts=None, quad_dir_policy=None):
     """StraightCutIntegrationRule for a list of elements; returns (counts,
-    points (n, max_pts, 3), weights (n, max_pts)) as device tensors."""
+    points (n, max_pts, 3), weights (n, max_pts)) as device tensors.  On
+    quadrilateral / hexahedral meshes quad_dir_policy (FIRST, OPTIMAL,
+    FALLBACK; default OPTIMAL) selects the direction of the tensor rule."""
     dm = device_mesh(mesh)
     el = torch.as_tensor(np.asarray(elements, dtype=np.int32)).to(_dev())
     n = el.numel()
+    policy = OPTIMAL if quad_dir_policy is None else int(quad_dir_policy)
+    if max_pts is None and getattr(mesh, "tensor", False):
+        max_pts = _lib.load().xg_quad_rule_capacity(mesh.dim, domain_type, order)
     if max_pts is None:
         sd = mesh.dim - 1 if domain_type == IF else mesh.dim
         max_pts = max(3 * _lib.load().xg_base_rule_size(sd, order), _lib.load().xg_base_rule_size(mesh.dim, order))
@@ -995,7 +1020,7 @@ def CutIntegrationRules(mesh, levelset, elements, domain_type, order, max_pts=No
     counts = torch.zeros(n, dtype=torch.int32, device=dev)
     pts = torch.zeros((n, max_pts, 3), dtype=torch.float64, device=dev)
     wts = torch.zeros((n, max_pts), dtype=torch.float64, device=dev)
-    _lib.call("xg_cut_rules", dm.h, _vp(_lset_vec(levelset)), _vp(el), n, domain_type, order, max_pts, _vp(counts),
-              _vp(pts), _vp(wts), _stream())
+    _lib.call("xg_cut_rules_ex", dm.h, _vp(_lset_vec(levelset)), _vp(el), n, domain_type, order, policy, max_pts,
+              _vp(counts), _vp(pts), _vp(wts), _stream())
     dm.check()
     return counts, pts, wts

@@ -56,8 +56,7 @@ _lib = None
 def lib():
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB):
-            build()
+        build()  # make: a no-op when the library is current
         L = ctypes.CDLL(LIB)
         P = ctypes.c_void_p
         L.orc_check_if_straight_cut.argtypes = [P, ctypes.c_int, ctypes.c_double]
@@ -106,6 +105,11 @@ def lib():
         L.orc_linear_form.argtypes = [P, P, P, ctypes.c_int, P]
         L.orc_pipeline.restype = ctypes.c_int64
         L.orc_pipeline.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        I = ctypes.c_int
+        L.orc_quad_cut_rule.argtypes = [I, P, I, I, I, P, P, I]
+        L.orc_quad_straight_cut_rule.argtypes = [I, P, P, I, I, I, P, P, I]
+        L.orc_quad_integrate.restype = ctypes.c_double
+        L.orc_quad_integrate.argtypes = [I, I, P, I, P, P, I, I, I, I, I, I, P]
         _lib = L
     return _lib
 
@@ -145,6 +149,43 @@ def straight_cut_rule(elcoords, lset, dt, order):
     if n < -1:
         raise RuntimeError("oracle cut rule error %d" % n)
     return pts[:n].copy(), w[:n].copy()
+
+
+# ---- quadrilaterals and hexahedra (cutint/straightcutrule.cpp:206-501) --------------
+QUAD_FIRST, QUAD_OPTIMAL, QUAD_FALLBACK = 0, 1, 2
+
+
+def quad_cut_rule(lset_vals, dt, order, policy=QUAD_OPTIMAL, elcoords=None, maxpts=8192):
+    """Cut rule on the unit square / cube for the multilinear level set with
+    the given vertex values (vertex order (0,0),(1,0),(1,1),(0,1) [, z = 1]).
+    With elcoords (nv x 3) the interface weights include the element map.
+    Returns (points, weights), None for "no rule"; raises on an error."""
+    l = np.ascontiguousarray(lset_vals, dtype=np.float64)
+    D = 2 if len(l) == 4 else 3
+    pts = np.zeros((maxpts, 3))
+    w = np.zeros(maxpts)
+    if elcoords is None:
+        n = lib().orc_quad_cut_rule(D, _p(l), dt, order, policy, _p(pts), _p(w), maxpts)
+    else:
+        xv = np.zeros((len(l), 3))
+        xv[:, :D] = np.asarray(elcoords, dtype=np.float64)[:, :D]
+        n = lib().orc_quad_straight_cut_rule(D, _p(xv), _p(l), dt, order, policy, _p(pts), _p(w), maxpts)
+    if n == -1:
+        return None
+    if n < -1:
+        raise RuntimeError("oracle quad rule status %d" % (-n - 1))
+    return pts[:n].copy(), w[:n].copy()
+
+
+def quad_integrate(mesh, lset, dt, order, policy=QUAD_OPTIMAL, exps=(0, 0, 0)):
+    """Integrate(x^a y^b z^c * dCut) on a quad / hex mesh; returns (value, status)."""
+    c = np.ascontiguousarray(mesh.coords, dtype=np.float64)
+    el = np.ascontiguousarray(mesh.elements, dtype=np.int32)
+    l = np.ascontiguousarray(lset, dtype=np.float64)
+    st = np.zeros(1, dtype=np.int32)
+    v = lib().orc_quad_integrate(c.shape[1], c.shape[0], _p(c), el.shape[0], _p(el), _p(l), dt, order, policy,
+                                 exps[0], exps[1], exps[2], _p(st))
+    return v, int(st[0])
 
 
 def time_basis(kt, tau):

@@ -166,6 +166,23 @@ int orc_linear_form(const orc_space*, const double* lset_vertex, const orc_lterm
 int64_t orc_pipeline(const orc_space*, const double* lset_vertex, const orc_term* terms, int nterms,
                      int ghost_facets, int nthreads);
 
+/* --- quadrilaterals and hexahedra (xg_oracle_quad.cpp) ------------------------
+ * Vertex order of an element: (0,0),(1,0),(1,1),(0,1) [then the same at z = 1];
+ * policy: 0 FIRST_ALLOWED, 1 FIND_OPTIMAL, 2 ALWAYS_NONE (utils/ngsxstd.hpp:10).
+ * Returns the point count, -1 for "no rule", or -(status) - 1 on an error
+ * (status as xg_status: 3 capacity, 4 plain cut, 5 decomposition, 7 NaN bound,
+ * 9 interface scaling bound). */
+int orc_quad_cut_rule(int D, const double* lset_vals, int dt, int order, int policy, double* pts, double* wts,
+                      int maxpts);
+/* The same rule with the interface weights of the bilinear / trilinear element
+ * with vertices xv[nv][3] (StraightCutIntegrationRule; an empty cut rule is
+ * "no rule", -1). */
+int orc_quad_straight_cut_rule(int D, const double* xv, const double* lset_vals, int dt, int order, int policy,
+                               double* pts, double* wts, int maxpts);
+/* Integrate(x^ex y^ey z^ez * dCut) on a quad / hex mesh: coords[nv][D], elv[ne][2^D]. */
+double orc_quad_integrate(int D, int nv, const double* coords, int ne, const int32_t* elv, const double* lset,
+                          int dt, int order, int policy, int ex, int ey, int ez, int* status);
+
 #ifdef __cplusplus
 }
 #endif

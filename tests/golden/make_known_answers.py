@@ -1,6 +1,6 @@
 """Writes known_answers.json: the closed-form values ngsxfem's own tests assert
 for the straight-cut path (tests/pytests/test_straightcutrule.py,
-tests/pytests/test_spacetimecutrule.py).  The reference cannot run here (it
+tests/pytests/test_spacetimecutrule.py, tests/pytests/test_quadchallenges.py).  The reference cannot run here (it
 needs NGSolve), so these closed forms are the golden vectors the oracle is
 pinned against.  Run: python tests/golden/make_known_answers.py
 """
@@ -28,6 +28,28 @@ out = {
     "circle_eoc": {  # :33-68, sqrt(x^2+y^2)-0.6 on [0,1]^2, mean EOC > 1.75
         "r": 0.6, "NEG": math.pi * 0.36 / 4, "POS": 1 - math.pi * 0.36 / 4, "IF": 0.6 * math.pi / 2,
         "min_mean_eoc": 1.75},
+    # quadrilaterals / hexahedra (the same files, quad=True / hexes=True, and
+    # tests/pytests/test_quadchallenges.py)
+    "orth_axis2d": {  # test_straightcutrule.py:237-257, lset 1-3x (or 1-3y), N=1, order 2
+        "slope": 3.0, "NEG": 2 / 3, "POS": 1 / 3, "IF": 1.0},
+    "orth_axis3d": {  # :260-279, lset 1-2x (y, z), N=1, order 2
+        "slope": 2.0, "NEG": 0.5, "POS": 0.5, "IF": 1.0},
+    "sphere_eoc": {  # :70-104, sqrt(x^2+y^2+z^2)-r on [0,1]^3 hexes 2^i, i<6, orders 2,4
+        "r": 0.7234436998, "NEG": math.pi * 0.7234436998 ** 3 / 6, "POS": 1 - math.pi * 0.7234436998 ** 3 / 6,
+        "orders": [2, 4], "n_ref": 6, "min_mean_eoc": 1.75},
+    "quad3d_planar": {  # test_quadchallenges.py:8-28: planar3d on 2x2x2 hexes, orders 2,4,8
+        "N": 2, "orders": [2, 4, 8]},
+    "quad3d_mono": {  # test_quadchallenges.py:31-57: mono3d on 5x5x5 hexes, order 4, OPTIMAL
+        "N": 5, "order": 4},
+    "zero_val": {  # test_quadchallenges.py:59-79: 2x2x2 hexes, POS, x^2, order 4, OPTIMAL
+        "N": 2, "order": 4, "alpha": 2, "POS": 2 ** (-5) / (8 + 24 + 22 + 6)},
+    "tpmc_hex": {  # test_quadchallenges.py:81-103: one hex, vertex values by vertex number of a
+        # mesh numbered z fastest (vertex 4x+2y+z), orders 2,4,6
+        "vals": [-4, 4, -1, -1, 2, -3, 5, -1], "orders": [2, 4, 6],
+        "NEG": 0.5167820912197415, "POS": 0.4825797907263282, "tol": 0.75, "IF_below": 10.0},
+    "tpmc_10": {  # test_quadchallenges.py:105-141: phi = x((7y-13)z+6) + y(3-8z) + 8z - 4
+        # on 10x10x10 hexes (interpolated exactly), orders 2,4
+        "orders": [2, 4], "NEG": 0.51681, "POS": 0.48319, "IF": 1.82169, "tol_vol": 1e-3, "tol_if": 5e-3},
 }
 path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "known_answers.json")
 with open(path, "w") as f:
