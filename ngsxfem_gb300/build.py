@@ -29,6 +29,7 @@ UNITS = [
     ("xg_learn.cu", []),
     ("xg_lf.cu", []),
     ("xg_quad.cu", ["-fmad=false"]),
+    ("xg_quad_int.cu", []),
 ]
 
 

@@ -28,6 +28,7 @@ int ensure_device_rules() {
   if (!st) st = upload_rules_st();
   if (!st) st = upload_rules_lf();
   if (!st) st = upload_rules_quad();
+  if (!st) st = upload_rules_quad_int();
   if (st) return st;
   done.push_back(dev);
   return XG_OK;

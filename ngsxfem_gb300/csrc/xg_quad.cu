@@ -1,13 +1,13 @@
-// Cut rules and Integrate on quadrilateral and hexahedral meshes.
+// Cut rules on quadrilateral and hexahedral meshes (rule export; Integrate
+// is in xg_quad_int.cu).
 //
 // The rule on the reference box is LevelsetCutQuadrilateral
 // (cutint/straightcutrule.cpp:206-501, unrolled in xg_quadcut.cuh); the
 // element map is the bilinear (trilinear) interpolation of the vertices, so
 // |det J| and the interface factor |J^-T n_ref| vary over the element and are
 // evaluated per point (TransformQuadUntrafoToIRInterface,
-// straightcutrule.cpp:558-578).  One thread builds and consumes the rule of
-// one element: a point is consumed as it is produced (callback), nothing is
-// stored, and the kernels are bound by the FP64 pipe of the rule construction.
+// straightcutrule.cpp:558-578).  One thread builds the rule of one element;
+// a point is written as it is produced (callback).
 // Compiled with -fmad=false: points and weights follow the CPU statement
 // operation by operation.
 #include <cuda_runtime.h>
@@ -115,14 +115,6 @@ __device__ __forceinline__ void gather(int ne, const int32_t* __restrict__ elv, 
   }
 }
 
-__device__ __forceinline__ double ipow(double x, int e) {
-  double r = 1.0;
-  for (int i = 0; i < e; i++) r *= x;
-  return r;
-}
-
-__device__ __forceinline__ bool tbit(const uint64_t* b, int64_t i) { return (b[i >> 6] >> (i & 63)) & 1ull; }
-
 }  // namespace
 
 // StraightCutIntegrationRule for listed quadrilaterals / hexahedra: rule
@@ -177,55 +169,6 @@ __global__ void __launch_bounds__(128) k_quad_rules(int ne, const int32_t* __res
   counts[i] = (cut && k == 0) ? -1 : k;
 }
 
-// Integrate(x^ex y^ey z^ez * dCut) over the elements of a quadrilateral /
-// hexahedral mesh (cutint/cutintegral.cpp:126-212): per thread a fixed set of
-// elements, per block a fixed reduction tree (deterministic).
-constexpr int kQIntThreads = 128;
-
-template <int D>
-__global__ void __launch_bounds__(kQIntThreads) k_quad_integrate(int ne, const int32_t* __restrict__ elv,
-                                                                 const double* __restrict__ xyz, int nv,
-                                                                 const double* __restrict__ lset, int dt, int order,
-                                                                 int pol, int ex, int ey, int ez,
-                                                                 const uint64_t* __restrict__ defined_on,
-                                                                 double* block_sums, int* err) {
-  __shared__ double red[kQIntThreads];
-  constexpr int NV = 1 << D;
-  double acc = 0.0;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
-    if (defined_on && !tbit(defined_on, e)) continue;
-    double l[NV], xv[NV][3];
-    gather<D>(ne, elv, xyz, nv, lset, (int)e, l, xv);
-    const bool cut = qc::qcheck(l, NV, 0.0) == XG_IF;
-    const qc::QL L = D == 2 ? qc::ql_quad(l) : qc::ql_hex(l);
-    auto emit = [&](const double* p, double w) {
-      double x[3], J[3][3], Ji[3][3];
-      tp_map<D>(xv, p, x, J);
-      const double det = tp_det_inv<D>(J, Ji);
-      if (cut && dt == XG_IF) w = w * tp_if_factor<D>(L, p, Ji);
-      const double fv = ipow(x[0], ex) * ipow(x[1], ey) * (D == 3 ? ipow(x[2], ez) : 1.0);
-      acc += w * fabs(det) * fv;
-    };
-    const int st = qc::tp_cut_rule<D>(&g_qrules, l, dt, order, pol, emit);
-    if (st > 0) set_err(err, st);
-  }
-  red[threadIdx.x] = acc;
-  __syncthreads();
-  for (int s = kQIntThreads / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) block_sums[blockIdx.x] = red[0];
-}
-
-__global__ void k_quad_sum_fixed(const double* v, int n, double* out) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    double s = 0.0;
-    for (int i = 0; i < n; i++) s += v[i];
-    out[0] = s;
-  }
-}
-
 // most points a rule of (dim, dt, order) can have: up to 3 (2D) / 5 (3D)
 // slabs between the xi breakpoints, each a tensor product over the segment
 // rule, or the simplex fallback (2 triangles / 6 tetrahedra, up to 3
@@ -258,28 +201,6 @@ int quad_cut_rules(xg_mesh* m, const double* d_lset, const int32_t* d_elems, int
     k_quad_rules<3><<<nblk_q(n, 128), 128, 0, s>>>(m->ne, m->d_elv, m->d_xyz, m->nv, d_lset, d_elems, n, dt, order,
                                                    pol, max_pts, d_counts, d_pts, d_wts, m->d_err);
   return launch_check_q("k_quad_rules");
-}
-
-int quad_integrate(xg_mesh* m, const double* d_lset, int dt, int order, int pol, int ex, int ey, int ez,
-                   const uint64_t* d_defined_on, double* d_result, void* stream) {
-  cudaStream_t s = (cudaStream_t)stream;
-  const int nb = 152 * 8;
-  if (m->scratch_bytes < nb * sizeof(double)) {
-    cudaFree(m->d_scratch);
-    m->d_scratch = nullptr;
-    m->scratch_bytes = 0;
-    XG_CUDA(cudaMalloc(&m->d_scratch, nb * sizeof(double)));
-    m->scratch_bytes = nb * sizeof(double);
-  }
-  double* bs = (double*)m->d_scratch;
-  if (m->dim == 2)
-    k_quad_integrate<2><<<nb, kQIntThreads, 0, s>>>(m->ne, m->d_elv, m->d_xyz, m->nv, d_lset, dt, order, pol, ex, ey,
-                                                    ez, d_defined_on, bs, m->d_err);
-  else
-    k_quad_integrate<3><<<nb, kQIntThreads, 0, s>>>(m->ne, m->d_elv, m->d_xyz, m->nv, d_lset, dt, order, pol, ex, ey,
-                                                    ez, d_defined_on, bs, m->d_err);
-  k_quad_sum_fixed<<<1, 32, 0, s>>>(bs, nb, d_result);
-  return launch_check_q("k_quad_integrate");
 }
 
 }  // namespace xg
