@@ -220,6 +220,22 @@ int xg_integrate(xg_mesh* mesh, const double* d_lset, int dt, int order, int ex,
  * calls share the array: calls that overlap on the GPU (different streams,
  * concurrent graphs) race and must be serialised by the caller.  The result
  * equals xg_integrate's up to the summation order (a fixed order per mesh). */
+/* Several level sets on a simplex mesh (cutint/mlsetintegration.cpp:6-180,
+ * cutint/straightcutrule.cpp:679-812): d_lsets holds nlsets (1..8) P1 level
+ * sets, [nlsets][nv] vertex values; the domain is the union of ndomains
+ * (1..256) tuples h_domains[ndomains][nlsets] (host, XG_NEG / XG_POS / XG_IF;
+ * a tuple with k IF entries is a codimension-k set).  Integrate of
+ * x^ex y^ey z^ez over that domain, deterministic fixed-order sum. */
+int xg_integrate_mlset(xg_mesh* mesh, const double* d_lsets, int32_t nlsets, const int8_t* h_domains,
+                       int32_t ndomains, int order, int ex, int ey, int ez, const uint64_t* d_defined_on,
+                       double* d_result, void* stream);
+/* The per-element rules of such a domain for listed elements (the tuples'
+ * parts concatenated; counts -1 = no rule), as xg_cut_rules. */
+int xg_cut_rules_mlset(xg_mesh* mesh, const double* d_lsets, int32_t nlsets, const int8_t* h_domains,
+                       int32_t ndomains, const int32_t* d_elems, int32_t n, int order, int32_t max_pts,
+                       int32_t* d_counts, double* d_pts, double* d_wts, void* stream);
+/* A sufficient max_pts for xg_cut_rules_mlset, or -1 for bad arguments. */
+int xg_mlset_rule_capacity(int dim, int32_t nlsets, int32_t ndomains, int order);
 /* xg_integrate with the quadrilateral / hexahedral direction policy. */
 int xg_integrate_ex(xg_mesh* mesh, const double* d_lset, int dt, int order, int quad_dir_policy, int ex, int ey,
                     int ez, const uint64_t* d_defined_on, double* d_result, void* stream);

@@ -3,9 +3,9 @@
     python -m ngsxfem_gb300.build          # builds if sources changed
     python -m ngsxfem_gb300.build --force
 
-xg_geom.cu and xg_quad.cu are compiled with -fmad=false: they hold the marking
-and rule-export kernels whose cut points, volumes and weights follow the CPU
-statement operation by operation.
+xg_geom.cu, xg_quad.cu and xg_mlset.cu are compiled with -fmad=false: they hold
+the marking and rule-export kernels whose cut points, volumes and weights
+follow the CPU statement operation by operation.
 """
 import os
 import shutil
@@ -30,6 +30,7 @@ UNITS = [
     ("xg_lf.cu", []),
     ("xg_quad.cu", ["-fmad=false"]),
     ("xg_quad_int.cu", []),
+    ("xg_mlset.cu", ["-fmad=false"]),
 ]
 
 

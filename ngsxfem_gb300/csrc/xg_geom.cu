@@ -29,6 +29,7 @@ int ensure_device_rules() {
   if (!st) st = upload_rules_lf();
   if (!st) st = upload_rules_quad();
   if (!st) st = upload_rules_quad_int();
+  if (!st) st = upload_rules_mlset();
   if (st) return st;
   done.push_back(dev);
   return XG_OK;

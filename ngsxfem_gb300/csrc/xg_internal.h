@@ -151,6 +151,7 @@ int cutinfo_update_st_ws(xg_mesh* m, const double* d_lset_st, int kt_lset, uint8
 // quadrilateral / hexahedral meshes (xg_quad.cu)
 int upload_rules_quad();
 int upload_rules_quad_int();
+int upload_rules_mlset();
 int quad_rule_capacity(int dim, int dt, int order);
 int quad_cut_rules(xg_mesh* m, const double* d_lset, const int32_t* d_elems, int32_t n, int dt, int order, int pol,
                    int32_t max_pts, int32_t* d_counts, double* d_pts, double* d_wts, void* stream);

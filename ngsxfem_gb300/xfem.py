@@ -990,6 +990,8 @@ def Integrate(levelset_domain=None, cf=None, mesh=None, order=5, integrand=None)
         defined = None
     if integrand is not None:
         policy = getattr(meas, "quad_dir_policy", OPTIMAL)
+    if isinstance(lset, (tuple, list)):
+        return _integrate_mlset(lset, dt, order, mono, defined, mesh)
     mesh = mesh if mesh is not None else lset.space.mesh
     dm = device_mesh(mesh)
     res = torch.zeros(1, dtype=torch.float64, device=_dev())
@@ -997,6 +999,55 @@ def Integrate(levelset_domain=None, cf=None, mesh=None, order=5, integrand=None)
               mono.e[2], _vp(defined.words) if defined is not None else None, _vp(res), _stream())
     dm.check()
     return float(res.item())
+
+
+def _mlset_args(lsets, domain):
+    """(device [M][nv] level-set values, host int8 [ntup][M] domain tuples)."""
+    from .mlset import DomainTypeArray
+    if not isinstance(domain, DomainTypeArray):
+        domain = DomainTypeArray(list(domain) if isinstance(domain, list) else domain)
+    M = len(lsets)
+    if len(domain.as_list[0]) != M:
+        raise ValueError("domain tuples of length %d for %d level sets" % (len(domain.as_list[0]), M))
+    nv = lsets[0].space.mesh.nv
+    vals = torch.stack([_lset_vec(g)[:nv] for g in lsets]).contiguous()
+    tup = np.ascontiguousarray(np.array(domain.as_list, dtype=np.int8).reshape(-1, M))
+    return vals, tup
+
+
+def _integrate_mlset(lsets, domain, order, mono, defined, mesh):
+    """Integrate over a region of several level sets
+    (cutint/mlsetintegration.cpp:6-180): xg_integrate_mlset."""
+    mesh = mesh if mesh is not None else lsets[0].space.mesh
+    dm = device_mesh(mesh)
+    vals, tup = _mlset_args(lsets, domain)
+    res = torch.zeros(1, dtype=torch.float64, device=_dev())
+    _lib.call("xg_integrate_mlset", dm.h, _vp(vals), vals.shape[0], tup.ctypes.data_as(ctypes.c_void_p),
+              tup.shape[0], order, mono.e[0], mono.e[1], mono.e[2],
+              _vp(defined.words) if defined is not None else None, _vp(res), _stream())
+    dm.check()
+    return float(res.item())
+
+
+def MultiLevelsetCutIntegrationRules(mesh, levelsets, domain, elements, order, max_pts=None):
+    """The per-element rules of a region of several level sets
+    (CreateMultiLevelsetCutIntegrationRule for listed elements): (counts,
+    points (n, max_pts, 3), weights (n, max_pts)) as device tensors, counts
+    -1 where the element has no part of the region."""
+    dm = device_mesh(mesh)
+    vals, tup = _mlset_args(levelsets, domain)
+    el = torch.as_tensor(np.asarray(elements, dtype=np.int32)).to(_dev())
+    n = el.numel()
+    if max_pts is None:
+        max_pts = _lib.load().xg_mlset_rule_capacity(mesh.dim, vals.shape[0], tup.shape[0], order)
+    dev = _dev()
+    counts = torch.zeros(n, dtype=torch.int32, device=dev)
+    pts = torch.zeros((n, max_pts, 3), dtype=torch.float64, device=dev)
+    wts = torch.zeros((n, max_pts), dtype=torch.float64, device=dev)
+    _lib.call("xg_cut_rules_mlset", dm.h, _vp(vals), vals.shape[0], tup.ctypes.data_as(ctypes.c_void_p),
+              tup.shape[0], _vp(el), n, order, max_pts, _vp(counts), _vp(pts), _vp(wts), _stream())
+    dm.check()
+    return counts, pts, wts
 
 
 # ----------------------------------------------------------------------------

@@ -110,6 +110,9 @@ def lib():
         L.orc_quad_straight_cut_rule.argtypes = [I, P, P, I, I, I, P, P, I]
         L.orc_quad_integrate.restype = ctypes.c_double
         L.orc_quad_integrate.argtypes = [I, I, P, I, P, P, I, I, I, I, I, I, P]
+        L.orc_mlset_cut_rule.argtypes = [I, P, I, P, I, P, I, P, P, I]
+        L.orc_mlset_integrate.restype = ctypes.c_double
+        L.orc_mlset_integrate.argtypes = [I, I, P, I, P, I, P, I, P, I, I, I, I, P]
         _lib = L
     return _lib
 
@@ -185,6 +188,45 @@ def quad_integrate(mesh, lset, dt, order, policy=QUAD_OPTIMAL, exps=(0, 0, 0)):
     st = np.zeros(1, dtype=np.int32)
     v = lib().orc_quad_integrate(c.shape[1], c.shape[0], _p(c), el.shape[0], _p(el), _p(l), dt, order, policy,
                                  exps[0], exps[1], exps[2], _p(st))
+    return v, int(st[0])
+
+
+# ---- several level sets (cutint/straightcutrule.cpp:679-812, mlsetintegration.cpp) --
+def _tuples(dts, M):
+    t = np.ascontiguousarray(np.array(dts, dtype=np.int32).reshape(-1, M))
+    return t, t.shape[0]
+
+
+def mlset_cut_rule(elcoords, lsets, dts, order, maxpts=20000):
+    """Rule of one simplex for the domain tuples dts (list of M-tuples), the M
+    level sets given by their vertex values lsets (M x (D+1)).  Returns
+    (points, weights) in reference coordinates, None for no rule."""
+    elc = np.ascontiguousarray(elcoords, dtype=np.float64)
+    D = elc.shape[1]
+    l = np.ascontiguousarray(lsets, dtype=np.float64)
+    M = l.shape[0]
+    t, nt = _tuples(dts, M)
+    pts = np.zeros((maxpts, 3))
+    w = np.zeros(maxpts)
+    n = lib().orc_mlset_cut_rule(D, _p(elc), M, _p(l), nt, _p(t), order, _p(pts), _p(w), maxpts)
+    if n == -1:
+        return None
+    if n < -1:
+        raise RuntimeError("oracle mlset rule status %d" % (-n - 1))
+    return pts[:n].copy(), w[:n].copy()
+
+
+def mlset_integrate(mesh, lsets, dts, order, exps=(0, 0, 0)):
+    """Integrate(x^a y^b z^c) over the union of the domain tuples dts of the
+    level sets lsets (M x nv); returns (value, status)."""
+    c = np.ascontiguousarray(mesh.coords, dtype=np.float64)
+    el = np.ascontiguousarray(mesh.elements, dtype=np.int32)
+    l = np.ascontiguousarray(lsets, dtype=np.float64)
+    M = l.shape[0]
+    t, nt = _tuples(dts, M)
+    st = np.zeros(1, dtype=np.int32)
+    v = lib().orc_mlset_integrate(c.shape[1], c.shape[0], _p(c), el.shape[0], _p(el), M, _p(l), nt, _p(t), order,
+                                  exps[0], exps[1], exps[2], _p(st))
     return v, int(st[0])
 
 

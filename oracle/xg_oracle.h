@@ -183,6 +183,18 @@ int orc_quad_straight_cut_rule(int D, const double* xv, const double* lset_vals,
 double orc_quad_integrate(int D, int nv, const double* coords, int ne, const int32_t* elv, const double* lset,
                           int dt, int order, int policy, int ex, int ey, int ez, int* status);
 
+/* --- several level sets on simplices (xg_oracle_mlset.cpp) --------------------
+ * lsets: M level sets' values, [M][D+1] at the element's vertices (rule) or
+ * [M][nv] at the mesh vertices (Integrate); dts: ntup domain tuples of M
+ * entries (NEG / POS / IF), their rules concatenated
+ * (CreateMultiLevelsetCutIntegrationRule).  The rule returns the point count,
+ * -1 for no rule or -(status)-1. */
+int orc_mlset_cut_rule(int D, const double* elc, int M, const double* lsets, int ntup, const int* dts, int order,
+                       double* pts, double* wts, int maxpts);
+double orc_mlset_integrate(int D, int nv, const double* coords, int ne, const int32_t* elv, int M,
+                           const double* lsets, int ntup, const int* dts, int order, int ex, int ey, int ez,
+                           int* status);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,6 +1,7 @@
 """Writes known_answers.json: the closed-form values ngsxfem's own tests assert
 for the straight-cut path (tests/pytests/test_straightcutrule.py,
-tests/pytests/test_spacetimecutrule.py, tests/pytests/test_quadchallenges.py).  The reference cannot run here (it
+tests/pytests/test_spacetimecutrule.py, tests/pytests/test_quadchallenges.py,
+tests/pytests/test_mlset_integration.py).  The reference cannot run here (it
 needs NGSolve), so these closed forms are the golden vectors the oracle is
 pinned against.  Run: python tests/golden/make_known_answers.py
 """
@@ -50,6 +51,19 @@ out = {
     "tpmc_10": {  # test_quadchallenges.py:105-141: phi = x((7y-13)z+6) + y(3-8z) + 8z - 4
         # on 10x10x10 hexes (interpolated exactly), orders 2,4
         "orders": [2, 4], "NEG": 0.51681, "POS": 0.48319, "IF": 1.82169, "tol_vol": 1e-3, "tol_if": 5e-3},
+    # several level sets (tests/pytests/test_mlset_integration.py)
+    "mlset2d": {  # :38-128, level sets y-1, 2x-y, -2x-y on [-1,1]x[-0.5,1.5], order 0
+        "box": [[-1.0, 1.0], [-0.5, 1.5]],
+        "area_neg0": 3.0, "triangle": 0.5, "complement": 3.5,
+        "side_t": 1.0, "side_r": math.sqrt(5 / 4), "side_l": math.sqrt(5 / 4), "perimeter": 1 + math.sqrt(5),
+        "x_plus_y": {"tl": 1.5, "tr": 0.5, "b": 0.0, "corners": 2.0}, "tol": 1e-12},
+    "mlset2d_ho": {  # :131-153, -y, x-1, y-1, -x on [-0.2,1.2]^2, x(1-x)y(1-y), order 4
+        "box": [[-0.2, 1.2], [-0.2, 1.2]], "value": 1 / 36, "tol": 1e-12},
+    "mlset3d": {  # :289-395, x -+ 0.5, y -+ 0.5, z -+ 0.5 on [-0.8,0.8]^3, order 0
+        "box": [-0.8, 0.8], "cube": 1.0, "complement": 1.6 ** 3 - 1.0, "side": 1.0, "surface": 6.0,
+        "edge": 1.0, "edges": 12.0,
+        "corners_x_plus_y_plus_z": {"ppp": 1.5, "ppn": 0.5, "pnp": 0.5, "npp": 0.5, "pnn": -0.5, "npn": -0.5,
+                                    "nnp": -0.5, "nnn": -1.5}, "tol": 1e-12},
 }
 path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "known_answers.json")
 with open(path, "w") as f:
