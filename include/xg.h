@@ -234,6 +234,12 @@ int xg_integrate_mlset(xg_mesh* mesh, const double* d_lsets, int32_t nlsets, con
 int xg_cut_rules_mlset(xg_mesh* mesh, const double* d_lsets, int32_t nlsets, const int8_t* h_domains,
                        int32_t ndomains, const int32_t* d_elems, int32_t n, int order, int32_t max_pts,
                        int32_t* d_counts, double* d_pts, double* d_wts, void* stream);
+/* MultiLevelsetCutInfo element markers (xfem/cutinfo.cpp:306-419) into d_bits
+ * (ceil(ne/64) words): mode 0 = GetElementsOfType (the level sets' domain types
+ * on the element equal one of the tuples), 1 = GetElementsWithContribution
+ * (the region's order-0 rule on the element has a positive weight sum). */
+int xg_mlset_mark(xg_mesh* mesh, const double* d_lsets, int32_t nlsets, const int8_t* h_domains, int32_t ndomains,
+                  int mode, uint64_t* d_bits, void* stream);
 /* A sufficient max_pts for xg_cut_rules_mlset, or -1 for bad arguments. */
 int xg_mlset_rule_capacity(int dim, int32_t nlsets, int32_t ndomains, int order);
 /* xg_integrate with the quadrilateral / hexahedral direction policy. */

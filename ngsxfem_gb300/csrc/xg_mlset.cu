@@ -138,6 +138,43 @@ __global__ void __launch_bounds__(kMlThreads) k_mlset_rules(int ne, const int32_
   counts[i] = k == 0 ? -1 : k;
 }
 
+// MultiLevelsetCutInformation markers (xfem/cutinfo.cpp:306-419): mode 0
+// marks elements whose level-set domain types equal a tuple, mode 1 those
+// whose order-0 rule of the region has a positive weight sum.  bits cleared
+// by the caller; bits are set with atomic OR (the result does not depend on
+// the order).
+template <int D>
+__global__ void __launch_bounds__(kMlThreads) k_mlset_mark(int ne, const int32_t* __restrict__ elv,
+                                                           const double* __restrict__ xyz, int nv,
+                                                           const double* __restrict__ lsets,
+                                                           const __grid_constant__ ml::MlDesc md, int mode,
+                                                           unsigned long long* bits, int* err) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
+    double xv[D + 1][3], lv[ml::kMaxLsets][D + 1];
+    gather_ml<D>(ne, elv, xyz, nv, lsets, md.M, (int)e, xv, lv);
+    bool mark = false;
+    if (mode == 0) {
+      int ldt[ml::kMaxLsets];
+      for (int m = 0; m < md.M; m++) ldt[m] = qc::qcheck(lv[m], D + 1, 0.0);
+      for (int t = 0; t < md.ntup && !mark; t++) {
+        bool match = true;
+        for (int m = 0; m < md.M; m++) match &= md.dt[t * md.M + m] == ldt[m];
+        mark = match;
+      }
+    } else {
+      ml::AGeo g;
+      ml::make_ageo<D>(xv, g);
+      double part = 0.0;
+      auto emit = [&](const double*, double w) { part += w; };
+      int npts = 0;
+      const int st = ml::element_rule<D>(&g_mrules, g, md.M, md.ntup, md.dt, lv, 0, emit, &npts);
+      if (st) set_err(err, st);
+      mark = st == 0 && npts > 0 && part > 0;
+    }
+    if (mark) atomicOr(bits + (e >> 6), 1ull << (e & 63));
+  }
+}
+
 static int launch_check_ml(const char* what) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, what);
@@ -181,6 +218,18 @@ int mlset_integrate(xg_mesh* m, const double* d_lsets, const ml::MlDesc& md, int
                                                          ey, ez, d_defined_on, bs, m->d_err);
   k_mlset_final<<<1, 32, 0, s>>>(bs, kMlBlocks, d_result);
   return launch_check_ml("k_mlset_integrate");
+}
+
+int mlset_mark(xg_mesh* m, const double* d_lsets, const ml::MlDesc& md, int mode, uint64_t* d_bits, void* stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  XG_CUDA(cudaMemsetAsync(d_bits, 0, sizeof(uint64_t) * (((size_t)m->ne + 63) / 64), s));
+  if (m->dim == 2)
+    k_mlset_mark<2><<<kMlBlocks, kMlThreads, 0, s>>>(m->ne, m->d_elv, m->d_xyz, m->nv, d_lsets, md, mode,
+                                                     (unsigned long long*)d_bits, m->d_err);
+  else
+    k_mlset_mark<3><<<kMlBlocks, kMlThreads, 0, s>>>(m->ne, m->d_elv, m->d_xyz, m->nv, d_lsets, md, mode,
+                                                     (unsigned long long*)d_bits, m->d_err);
+  return launch_check_ml("k_mlset_mark");
 }
 
 int mlset_cut_rules(xg_mesh* m, const double* d_lsets, const ml::MlDesc& md, const int32_t* d_elems, int32_t n,
@@ -232,6 +281,15 @@ int xg_cut_rules_mlset(xg_mesh* m, const double* d_lsets, int32_t nlsets, const 
   if (int st = mlset_desc(nlsets, h_domains, ndomains, &md)) return st;
   if (n == 0) return XG_OK;
   return mlset_cut_rules(m, d_lsets, md, d_elems, n, order, max_pts, d_counts, d_pts, d_wts, stream);
+}
+
+int xg_mlset_mark(xg_mesh* m, const double* d_lsets, int32_t nlsets, const int8_t* h_domains, int32_t ndomains,
+                  int mode, uint64_t* d_bits, void* stream) {
+  if (int st = mlset_mesh_ok(m, "xg_mlset_mark")) return st;
+  if (!d_lsets || !d_bits || (mode != 0 && mode != 1)) return XG_ERR_ARG;
+  ml::MlDesc md;
+  if (int st = mlset_desc(nlsets, h_domains, ndomains, &md)) return st;
+  return mlset_mark(m, d_lsets, md, mode, d_bits, stream);
 }
 
 int xg_mlset_rule_capacity(int dim, int32_t nlsets, int32_t ndomains, int order) {

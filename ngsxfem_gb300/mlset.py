@@ -193,3 +193,78 @@ def TensorIntersection(*args):
         if not isinstance(dta, DomainTypeArray):
             raise TypeError("TensorIntersection only possible for DomainTypeArrays")
     return DomainTypeArray([sum(c, ()) for c in product(*[dta.as_list for dta in args])])
+
+
+class MultiLevelsetCutInfo:
+    """Element markers of regions of several level sets
+    (MultiLevelsetCutInformation, xfem/cutinfo.cpp:286-419): the level sets are
+    copied at construction and by Update(); every marker handed out is kept
+    and recomputed in place by Update()."""
+
+    def __init__(self, mesh, levelset):
+        from .xfem import device_mesh
+        self.mesh = mesh
+        lsets = self._check(levelset)
+        self.M = len(lsets)
+        self._dm = device_mesh(mesh)
+        self._vals = self._copy(lsets)
+        self._markers = []  # (mode, int8 tuples, BitArray)
+
+    @staticmethod
+    def _check(levelset):
+        from .xfem import GridFunction
+        if not isinstance(levelset, (tuple, list)) or not all(isinstance(g, GridFunction) for g in levelset):
+            raise TypeError("MultiLevelsetCutInfo needs a tuple of P1 GridFunctions")
+        return tuple(levelset)
+
+    def _copy(self, lsets):
+        import torch
+        from .xfem import _lset_vec
+        return torch.stack([_lset_vec(g)[: self.mesh.nv] for g in lsets]).clone().contiguous()
+
+    def Mesh(self):
+        return self.mesh
+
+    def _tuples(self, domain):
+        import numpy as np
+        if not isinstance(domain, DomainTypeArray):
+            domain = DomainTypeArray(list(domain) if isinstance(domain, list) else domain)
+        if len(domain.as_list[0]) != self.M:
+            raise ValueError("domain tuples of length %d for %d level sets" % (len(domain.as_list[0]), self.M))
+        return np.ascontiguousarray(np.array(domain.as_list, dtype=np.int8).reshape(-1, self.M))
+
+    def _mark(self, mode, tup, bits):
+        import ctypes
+        from . import _lib
+        from .xfem import _stream, _vp
+        _lib.call("xg_mlset_mark", self._dm.h, _vp(self._vals), self.M, tup.ctypes.data_as(ctypes.c_void_p),
+                  tup.shape[0], mode, _vp(bits.words), _stream())
+        self._dm.check()
+
+    def _get(self, mode, domain):
+        from .xfem import BitArray
+        tup = self._tuples(domain)
+        key = sorted(map(tuple, tup.tolist()))
+        for m, t, bits in self._markers:
+            if m == mode and sorted(map(tuple, t.tolist())) == key:
+                return bits
+        bits = BitArray(self.mesh.ne)
+        self._mark(mode, tup, bits)
+        self._markers.append((mode, tup, bits))
+        return bits
+
+    def GetElementsOfType(self, domain_type):
+        """Elements whose level-set domain types equal one of the tuples."""
+        return self._get(0, domain_type)
+
+    def GetElementsWithContribution(self, domain_type):
+        """Elements on which the region has a part of positive measure."""
+        return self._get(1, domain_type)
+
+    def Update(self, levelset):
+        lsets = self._check(levelset)
+        if len(lsets) != self.M:
+            raise ValueError("the new level sets must be as many as the original ones")
+        self._vals.copy_(self._copy(lsets))
+        for mode, tup, bits in self._markers:
+            self._mark(mode, tup, bits)

@@ -113,6 +113,7 @@ def lib():
         L.orc_mlset_cut_rule.argtypes = [I, P, I, P, I, P, I, P, P, I]
         L.orc_mlset_integrate.restype = ctypes.c_double
         L.orc_mlset_integrate.argtypes = [I, I, P, I, P, I, P, I, P, I, I, I, I, P]
+        L.orc_mlset_mark.argtypes = [I, I, P, I, P, I, P, I, P, I, P]
         _lib = L
     return _lib
 
@@ -228,6 +229,22 @@ def mlset_integrate(mesh, lsets, dts, order, exps=(0, 0, 0)):
     v = lib().orc_mlset_integrate(c.shape[1], c.shape[0], _p(c), el.shape[0], _p(el), M, _p(l), nt, _p(t), order,
                                   exps[0], exps[1], exps[2], _p(st))
     return v, int(st[0])
+
+
+def mlset_mark(mesh, lsets, dts, mode):
+    """MultiLevelsetCutInfo markers (mode 0: elements of the tuples' types,
+    1: elements with a contribution); returns a bool array over the elements."""
+    c = np.ascontiguousarray(mesh.coords, dtype=np.float64)
+    el = np.ascontiguousarray(mesh.elements, dtype=np.int32)
+    l = np.ascontiguousarray(lsets, dtype=np.float64)
+    M = l.shape[0]
+    t, nt = _tuples(dts, M)
+    bits = np.zeros((el.shape[0] + 63) // 64, dtype=np.uint64)
+    st = lib().orc_mlset_mark(c.shape[1], c.shape[0], _p(c), el.shape[0], _p(el), M, _p(l), nt, _p(t), mode,
+                              _p(bits))
+    if st:
+        raise RuntimeError("oracle mlset marking status %d" % st)
+    return np.unpackbits(bits.view(np.uint8), bitorder="little")[: el.shape[0]].astype(bool)
 
 
 def time_basis(kt, tau):

@@ -194,6 +194,11 @@ int orc_mlset_cut_rule(int D, const double* elc, int M, const double* lsets, int
 double orc_mlset_integrate(int D, int nv, const double* coords, int ne, const int32_t* elv, int M,
                            const double* lsets, int ntup, const int* dts, int order, int ex, int ey, int ez,
                            int* status);
+/* MultiLevelsetCutInfo element markers: mode 0 GetElementsOfType (exact level-set
+ * domain types), 1 GetElementsWithContribution (positive weight sum of the
+ * region's order-0 rule).  Returns 0 or the first error status. */
+int orc_mlset_mark(int D, int nv, const double* coords, int ne, const int32_t* elv, int M, const double* lsets,
+                   int ntup, const int* dts, int mode, uint64_t* bits);
 
 #ifdef __cplusplus
 }

@@ -390,6 +390,53 @@ int orc_mlset_cut_rule(int D, const double* elc, int M, const double* lsets, int
   return (int)w.size();
 }
 
+// MultiLevelsetCutInformation (xfem/cutinfo.cpp:306-419): mode 0
+// (GetElementsOfDomainType) marks the elements whose level-set domain types
+// equal one of the tuples; mode 1 (GetElementsWithContribution) those whose
+// rule of the region (order 0) has a positive weight sum.  bits: ceil(ne/64)
+// words.  Returns 0 or the first error status.
+int orc_mlset_mark(int D, int nv, const double* coords, int ne, const int32_t* elv, int M, const double* lsets,
+                   int ntup, const int* dts, int mode, uint64_t* bits) {
+  if (M < 1 || M > 8) return E_UNSUPPORTED;
+  int status = 0;
+  for (int w = 0; w < (ne + 63) / 64; w++) bits[w] = 0;
+  for (int e = 0; e < ne; e++) {
+    double elc[12], lvals[8 * 4];
+    for (int v = 0; v <= D; v++) {
+      const int id = elv[(size_t)e * (D + 1) + v];
+      for (int i = 0; i < D; i++) elc[v * D + i] = coords[(size_t)id * D + i];
+      for (int m = 0; m < M; m++) lvals[m * (D + 1) + v] = lsets[(size_t)m * nv + id];
+    }
+    bool mark = false;
+    if (mode == 0) {
+      int ldt[8];
+      for (int m = 0; m < M; m++) ldt[m] = check_cut(std::vector<double>(lvals + m * (D + 1), lvals + (m + 1) * (D + 1)));
+      for (int t = 0; t < ntup && !mark; t++) {
+        bool match = true;
+        for (int m = 0; m < M; m++) match &= dts[t * M + m] == ldt[m];
+        mark = match;
+      }
+    } else {
+      const Geo g = make_geo(D, elc);
+      std::vector<const double*> lv;
+      for (int m = 0; m < M; m++) lv.push_back(lvals + m * (D + 1));
+      std::vector<V3> p;
+      std::vector<double> w;
+      try {
+        if (mlset_element_rule(g, M, lv, ntup, dts, 0, p, w)) {
+          double part = 0;
+          for (double x : w) part += x;
+          mark = part > 0;
+        }
+      } catch (const MErr& err) {
+        if (!status) status = err.code;
+      }
+    }
+    if (mark) bits[e >> 6] |= 1ull << (e & 63);
+  }
+  return status;
+}
+
 double orc_mlset_integrate(int D, int nv, const double* coords, int ne, const int32_t* elv, int M,
                            const double* lsets, int ntup, const int* dts, int order, int ex, int ey, int ez,
                            int* status) {

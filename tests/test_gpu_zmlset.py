@@ -121,3 +121,38 @@ def test_rules_match_oracle(xg, orc, D, seed):
             assert counts[e] == n, (e, counts[e], n)
             assert np.max(np.abs(pts[e, :n] - r[0]), initial=0) <= 1e-14
             assert np.max(np.abs(wts[e, :n] - r[1]) / np.maximum(1e-300, np.abs(r[1])), initial=0) <= 1e-13
+
+
+def test_multilevelset_cutinfo(xg, orc):
+    """MultiLevelsetCutInfo markers against the oracle's, and the Update
+    semantics of test_mlset_integration.py::test_multilevelsetcutinfo."""
+    from ngsxfem_gb300.mlset import DomainTypeArray, MultiLevelsetCutInfo
+    ref = KA["mlset2d"]
+    b = ref["box"]
+    m = MakeStructured2DMesh(7, 7, b[0][0], b[0][1], b[1][0], b[1][1])
+    X, Y = m.coords[:, 0], m.coords[:, 1]
+    L = np.array([orc.interpolate_p1_perturb(f) for f in (Y - 1, 2 * X - Y, -2 * X - Y)])
+    G = gfs(xg, m, L)
+    mlci = MultiLevelsetCutInfo(m, G)
+    tri = DomainTypeArray((xg.NEG, xg.NEG, xg.NEG))
+    for region in (tri, ~tri, tri.Boundary(), tri.Boundary().Boundary()):
+        for mode, get in ((0, mlci.GetElementsOfType), (1, mlci.GetElementsWithContribution)):
+            assert (get(region).numpy() == orc.mlset_mark(m, L, region.as_list, mode)).all()
+    neg = mlci.GetElementsOfType(tri).numpy()
+    assert (mlci.GetElementsWithContribution(tri.Boundary()).numpy() ==
+            (mlci.GetElementsWithContribution(tri).numpy() & ~neg)).all()
+    # markers follow Update, not the level sets they were built from
+    m2 = MakeStructured2DMesh(10, 10, -1, 1, -1, 1)
+    X2, Y2 = m2.coords[:, 0], m2.coords[:, 1]
+    H = gfs(xg, m2, [X2 + 0.5, X2 - 0.5])
+    ci = MultiLevelsetCutInfo(m2, H)
+    a0 = ci.GetElementsOfType((xg.POS, xg.NEG)).numpy().copy()
+    for g, v in zip(H, (Y2 + 0.5, Y2 - 0.5)):
+        g.vec.copy_(torch.from_numpy(v))
+    assert (ci.GetElementsOfType((xg.POS, xg.NEG)).numpy() == a0).all()
+    ci.Update(H)
+    assert not (ci.GetElementsOfType((xg.POS, xg.NEG)).numpy() == a0).all()
+    with pytest.raises(ValueError):
+        ci.GetElementsOfType((xg.NEG, xg.NEG, xg.NEG))
+    with pytest.raises(TypeError):
+        MultiLevelsetCutInfo(m2, (1.0, 2.0))

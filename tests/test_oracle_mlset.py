@@ -167,3 +167,28 @@ def test_c_abi_rejects_bad_domains():
     assert L.xg_mlset_rule_capacity(2, 2, 1, 0) == 9
     assert L.xg_mlset_rule_capacity(2, 9, 1, 0) == -1
     assert L.xg_mlset_rule_capacity(4, 2, 1, 0) == -1
+
+
+def test_marker_relations(orc):
+    """MultiLevelsetCutInfo relations asserted by test_mlset_integration.py,
+    on the oracle's markers."""
+    m, L = lsets_2d(orc)
+    tri = DomainTypeArray((NEG, NEG, NEG))
+    neg = orc.mlset_mark(m, L, tri.as_list, 0)
+    hasneg = orc.mlset_mark(m, L, tri.as_list, 1)
+    not_neg = orc.mlset_mark(m, L, (~tri).as_list, 1)
+    if_ = orc.mlset_mark(m, L, tri.Boundary().as_list, 1)
+    assert neg.any() and if_.any()
+    assert (~neg == not_neg).all()
+    assert (if_ == (hasneg & ~neg)).all()
+    m3, L3 = lsets_3d(orc)
+    cube = DomainTypeArray((NEG, POS, NEG, POS, NEG, POS))
+    neg3 = orc.mlset_mark(m3, L3, cube.as_list, 0)
+    has3 = orc.mlset_mark(m3, L3, cube.as_list, 1)
+    if3 = orc.mlset_mark(m3, L3, cube.Boundary().as_list, 1)
+    assert (~neg3 == orc.mlset_mark(m3, L3, (~cube).as_list, 1)).all()
+    assert (if3 == (has3 & ~neg3)).all()
+    sides = np.zeros_like(if3)
+    for t in cube.Boundary().as_list:
+        sides |= orc.mlset_mark(m3, L3, [t], 1)
+    assert (sides == if3).all()
