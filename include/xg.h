@@ -242,6 +242,17 @@ int xg_mlset_mark(xg_mesh* mesh, const double* d_lsets, int32_t nlsets, const in
                   int mode, uint64_t* d_bits, void* stream);
 /* A sufficient max_pts for xg_cut_rules_mlset, or -1 for bad arguments. */
 int xg_mlset_rule_capacity(int dim, int32_t nlsets, int32_t ndomains, int order);
+/* Mesh-level isoparametric integration of a P2 level set (LevelSetMeshAdaptation
+ * + Integrate: python/lsetcurv.py:281-356, lsetcurving/projshift.cpp:58-197,
+ * shiftintegrators.cpp:38-122, calcpointshift.cpp:143-201) on a simplex mesh:
+ * d_p2vals [ne][(D+1)(D+2)/2] the level set's values at each element's
+ * vertices, then edge midpoints (edges (0,1),(0,2),(1,2) / (0,1),(0,2),(0,3),
+ * (1,2),(1,3),(2,3)).  deform = 0 integrates the straight cut of the P1
+ * interpolant.  threshold < 0: no clipping of the shifts.  d_result[0] =
+ * integral of x^ex y^ey z^ez over the domain dt of the deformed mesh;
+ * d_nonconv[0] = Newton searches that did not converge. */
+int xg_iso_integrate_mesh(xg_mesh* mesh, const double* d_p2vals, int dt, int order, double threshold, int deform,
+                          int ex, int ey, int ez, double* d_result, int32_t* d_nonconv, void* stream);
 /* xg_integrate with the quadrilateral / hexahedral direction policy. */
 int xg_integrate_ex(xg_mesh* mesh, const double* d_lset, int dt, int order, int quad_dir_policy, int ex, int ey,
                     int ez, const uint64_t* d_defined_on, double* d_result, void* stream);

@@ -31,6 +31,7 @@ UNITS = [
     ("xg_quad.cu", ["-fmad=false"]),
     ("xg_quad_int.cu", []),
     ("xg_mlset.cu", ["-fmad=false"]),
+    ("xg_isomesh.cu", ["-fmad=false"]),
 ]
 
 

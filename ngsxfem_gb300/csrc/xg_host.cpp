@@ -446,6 +446,9 @@ int xg_mesh_destroy(xg_mesh* m) {
   cudaFree(m->d_facet_els_aos);
   cudaFree(m->d_err);
   cudaFree(m->d_cutlist);
+  cudaFree(m->d_edge_ptr);
+  cudaFree(m->d_edge_inc);
+  cudaFree(m->d_iso);
   cudaFree(m->d_scratch);
   delete m;
   return XG_OK;

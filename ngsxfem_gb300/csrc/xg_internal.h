@@ -152,6 +152,7 @@ int cutinfo_update_st_ws(xg_mesh* m, const double* d_lset_st, int kt_lset, uint8
 int upload_rules_quad();
 int upload_rules_quad_int();
 int upload_rules_mlset();
+int upload_rules_isomesh();
 int quad_rule_capacity(int dim, int dt, int order);
 int quad_cut_rules(xg_mesh* m, const double* d_lset, const int32_t* d_elems, int32_t n, int dt, int order, int pol,
                    int32_t max_pts, int32_t* d_counts, double* d_pts, double* d_wts, void* stream);
@@ -179,6 +180,10 @@ struct xg_mesh {
   int32_t* d_bnd_v = nullptr;          // [dim][nbnd] their vertices, ascending
   int* d_err = nullptr;
   int32_t* d_cutlist = nullptr;  // [max(ne, nbnd) + 1]: count, then the cut elements of the last marking
+  int32_t* d_edge_ptr = nullptr; // [nedges + 1] edge -> incident elements (isoparametric averaging)
+  int32_t* d_edge_inc = nullptr; // element * 8 + local edge, elements ascending
+  void* d_iso = nullptr;         // isoparametric workspace
+  size_t iso_bytes = 0;
   // host
   std::vector<int32_t> h_elv;       // ne*(dim+1)
   std::vector<int32_t> h_el_edges;  // ne*nel_edges

@@ -1029,6 +1029,59 @@ def _integrate_mlset(lsets, domain, order, mono, defined, mesh):
     return float(res.item())
 
 
+_TRI_EDGES = ((0, 1), (0, 2), (1, 2))
+_TET_EDGES = ((0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3))
+
+
+def P2ElementValues(mesh, f):
+    """(ne, (D+1)(D+2)/2) values of f (a callable on coordinate arrays) at each
+    element's vertices, then edge midpoints: the P2 nodal values the
+    isoparametric mapping takes."""
+    X = mesh.coords[mesh.elements]  # ne x (D+1) x D
+    pts = [X[:, v] for v in range(mesh.dim + 1)]
+    pts += [0.5 * (X[:, a] + X[:, b]) for a, b in (_TRI_EDGES if mesh.dim == 2 else _TET_EDGES)]
+    return np.stack([np.asarray(f(*[p[:, k] for k in range(mesh.dim)]), dtype=np.float64) for p in pts], axis=1)
+
+
+class LevelSetMeshAdaptation:
+    """Isoparametric integration for a P2 level set (python/lsetcurv.py:281-356:
+    LevelSetMeshAdaptation + CalcDeformation + Integrate on the deformed mesh),
+    on the GPU (xg_iso_integrate_mesh): per band element the shift of the
+    order-4 rule points to the level set of the P2 function (Newton along the
+    element's own gradient, discontinuous_qn), its L2 projection onto P2 with
+    the vertex coefficients dropped, the edge coefficients averaged over the
+    band elements, and the straight cut rule of the P1 interpolant mapped by
+    the deformation.  order 2 only."""
+
+    def __init__(self, mesh, order=2, threshold=-1.0, discontinuous_qn=True, **kwargs):
+        if order != 2:
+            raise NotImplementedError("the isoparametric mapping is built for order 2")
+        if not discontinuous_qn:
+            raise NotImplementedError("the search direction is the element's own gradient (discontinuous_qn=True)")
+        self.mesh, self.threshold = mesh, float(threshold)
+        self.p2 = None
+        self.nonconverged = 0
+
+    def CalcDeformation(self, levelset):
+        """levelset: a callable on coordinate arrays, or (ne, nn) P2 element values."""
+        vals = P2ElementValues(self.mesh, levelset) if callable(levelset) else np.asarray(levelset, np.float64)
+        self.p2 = torch.from_numpy(np.ascontiguousarray(vals)).to(_dev())
+        return self
+
+    def Integrate(self, domain_type, cf=None, order=4, deform=True):
+        if self.p2 is None:
+            raise RuntimeError("CalcDeformation first")
+        mono = cf if isinstance(cf, _Monomial) else _Monomial()
+        dm = device_mesh(self.mesh)
+        res = torch.zeros(1, dtype=torch.float64, device=_dev())
+        nc = torch.zeros(1, dtype=torch.int32, device=_dev())
+        _lib.call("xg_iso_integrate_mesh", dm.h, _vp(self.p2), domain_type, order, ctypes.c_double(self.threshold),
+                  1 if deform else 0, mono.e[0], mono.e[1], mono.e[2], _vp(res), _vp(nc), _stream())
+        dm.check()
+        self.nonconverged = int(nc.item())
+        return float(res.item())
+
+
 def MultiLevelsetCutIntegrationRules(mesh, levelsets, domain, elements, order, max_pts=None):
     """The per-element rules of a region of several level sets
     (CreateMultiLevelsetCutIntegrationRule for listed elements): (counts,
