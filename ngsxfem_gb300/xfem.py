@@ -1010,6 +1010,8 @@ def _mlset_args(lsets, domain):
     if len(domain.as_list[0]) != M:
         raise ValueError("domain tuples of length %d for %d level sets" % (len(domain.as_list[0]), M))
     nv = lsets[0].space.mesh.nv
+    if any(g.space.mesh is not lsets[0].space.mesh or _lset_vec(g).numel() < nv for g in lsets):
+        raise ValueError("the level sets must be P1 GridFunctions on one mesh")
     vals = torch.stack([_lset_vec(g)[:nv] for g in lsets]).contiguous()
     tup = np.ascontiguousarray(np.array(domain.as_list, dtype=np.int8).reshape(-1, M))
     return vals, tup
@@ -1065,6 +1067,10 @@ class LevelSetMeshAdaptation:
     def CalcDeformation(self, levelset):
         """levelset: a callable on coordinate arrays, or (ne, nn) P2 element values."""
         vals = P2ElementValues(self.mesh, levelset) if callable(levelset) else np.asarray(levelset, np.float64)
+        D = self.mesh.dim
+        if getattr(self.mesh, "tensor", False) or vals.shape != (self.mesh.ne, (D + 1) * (D + 2) // 2):
+            raise ValueError("P2 element values of shape (ne, %d) on a simplex mesh expected"
+                             % ((D + 1) * (D + 2) // 2))
         self.p2 = torch.from_numpy(np.ascontiguousarray(vals)).to(_dev())
         return self
 
