@@ -110,6 +110,8 @@ def lib():
         L.orc_quad_straight_cut_rule.argtypes = [I, P, P, I, I, I, P, P, I]
         L.orc_quad_integrate.restype = ctypes.c_double
         L.orc_quad_integrate.argtypes = [I, I, P, I, P, P, I, I, I, I, I, I, P]
+        L.orc_quad_integrate_mt.restype = ctypes.c_double
+        L.orc_quad_integrate_mt.argtypes = [I, I, P, I, P, P, I, I, I, I, I, I, I, P]
         L.orc_mlset_cut_rule.argtypes = [I, P, I, P, I, P, I, P, P, I]
         L.orc_mlset_integrate.restype = ctypes.c_double
         L.orc_mlset_integrate.argtypes = [I, I, P, I, P, I, P, I, P, I, I, I, I, P]
@@ -181,14 +183,18 @@ def quad_cut_rule(lset_vals, dt, order, policy=QUAD_OPTIMAL, elcoords=None, maxp
     return pts[:n].copy(), w[:n].copy()
 
 
-def quad_integrate(mesh, lset, dt, order, policy=QUAD_OPTIMAL, exps=(0, 0, 0)):
+def quad_integrate(mesh, lset, dt, order, policy=QUAD_OPTIMAL, exps=(0, 0, 0), nthreads=1):
     """Integrate(x^a y^b z^c * dCut) on a quad / hex mesh; returns (value, status)."""
     c = np.ascontiguousarray(mesh.coords, dtype=np.float64)
     el = np.ascontiguousarray(mesh.elements, dtype=np.int32)
     l = np.ascontiguousarray(lset, dtype=np.float64)
     st = np.zeros(1, dtype=np.int32)
-    v = lib().orc_quad_integrate(c.shape[1], c.shape[0], _p(c), el.shape[0], _p(el), _p(l), dt, order, policy,
-                                 exps[0], exps[1], exps[2], _p(st))
+    if nthreads > 1:
+        v = lib().orc_quad_integrate_mt(c.shape[1], c.shape[0], _p(c), el.shape[0], _p(el), _p(l), dt, order,
+                                        policy, exps[0], exps[1], exps[2], nthreads, _p(st))
+    else:
+        v = lib().orc_quad_integrate(c.shape[1], c.shape[0], _p(c), el.shape[0], _p(el), _p(l), dt, order, policy,
+                                     exps[0], exps[1], exps[2], _p(st))
     return v, int(st[0])
 
 

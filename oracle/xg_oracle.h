@@ -182,6 +182,10 @@ int orc_quad_straight_cut_rule(int D, const double* xv, const double* lset_vals,
 /* Integrate(x^ex y^ey z^ez * dCut) on a quad / hex mesh: coords[nv][D], elv[ne][2^D]. */
 double orc_quad_integrate(int D, int nv, const double* coords, int ne, const int32_t* elv, const double* lset,
                           int dt, int order, int policy, int ex, int ey, int ez, int* status);
+/* The same on nthreads host threads (contiguous element ranges, partial sums
+ * added in range order). */
+double orc_quad_integrate_mt(int D, int nv, const double* coords, int ne, const int32_t* elv, const double* lset,
+                             int dt, int order, int policy, int ex, int ey, int ez, int nthreads, int* status);
 
 /* --- several level sets on simplices (xg_oracle_mlset.cpp) --------------------
  * lsets: M level sets' values, [M][D+1] at the element's vertices (rule) or

@@ -28,8 +28,10 @@
 // (trilinear) interpolation of the vertices in the order
 // (0,0),(1,0),(1,1),(0,1) [, the same at z = 1].
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <set>
+#include <thread>
 #include <vector>
 
 #include "xg_oracle.h"
@@ -672,17 +674,14 @@ int orc_quad_straight_cut_rule(int D, const double* xv, const double* lset_vals,
   return n;
 }
 
-// Integrate(x^ex y^ey z^ez * dCut(lset, dt, order, quad_dir_policy)) over a
-// quadrilateral / hexahedral mesh: coords [nv][D], elements [ne][2^D], lset at
-// the vertices.  *status = 0 or the first error code.
-double orc_quad_integrate(int D, int nv, const double* coords, int ne, const int32_t* elv, const double* lset,
-                          int dt, int order, int policy, int ex, int ey, int ez, int* status) {
-  (void)nv;
+// Integrate(x^ex y^ey z^ez * dCut(lset, dt, order, quad_dir_policy)) over the
+// elements [e0, e1) of a quadrilateral / hexahedral mesh: coords [nv][D],
+// elements [ne][2^D], lset at the vertices.  *status = first error code.
+static double quad_integrate_range(int D, const double* coords, const int32_t* elv, const double* lset, int dt,
+                                   int order, int policy, int ex, int ey, int ez, int e0, int e1, int* status) {
   const int nve = D == 2 ? 4 : 8;
   double sum = 0;
-  if (status) *status = 0;
-  std::vector<double> pts(3 * 4096), wts(4096);
-  for (int e = 0; e < ne; e++) {
+  for (int e = e0; e < e1; e++) {
     double xv[8 * 3] = {0}, lv[8];
     for (int v = 0; v < nve; v++) {
       const int id = elv[(size_t)e * nve + v];
@@ -692,7 +691,7 @@ double orc_quad_integrate(int D, int nv, const double* coords, int ne, const int
     IR ir;
     const int n = quad_rule_untrafo(D, lv, dt, order, policy, ir);
     if (n < -1) {
-      if (status && *status == 0) *status = -n - 1;
+      if (*status == 0) *status = -n - 1;
       continue;
     }
     if (n <= 0) continue;
@@ -708,6 +707,45 @@ double orc_quad_integrate(int D, int nv, const double* coords, int ne, const int
       sum += w * std::fabs(det) * fv;
     }
   }
+  return sum;
+}
+
+double orc_quad_integrate(int D, int nv, const double* coords, int ne, const int32_t* elv, const double* lset,
+                          int dt, int order, int policy, int ex, int ey, int ez, int* status) {
+  (void)nv;
+  int st = 0;
+  const double v = quad_integrate_range(D, coords, elv, lset, dt, order, policy, ex, ey, ez, 0, ne, &st);
+  if (status) *status = st;
+  return v;
+}
+
+// the same with nthreads host threads taking chunks of 256 elements; the
+// chunk sums are added in chunk order (the result does not depend on the
+// thread count)
+double orc_quad_integrate_mt(int D, int nv, const double* coords, int ne, const int32_t* elv, const double* lset,
+                             int dt, int order, int policy, int ex, int ey, int ez, int nthreads, int* status) {
+  (void)nv;
+  if (nthreads < 1) nthreads = 1;
+  const int chunk = 256, nch = (ne + chunk - 1) / chunk;
+  std::vector<double> part(nch, 0.0);
+  std::vector<int> st(nch, 0);
+  std::atomic<int> next(0);
+  std::vector<std::thread> th;
+  for (int t = 0; t < nthreads; t++)
+    th.emplace_back([&]() {
+      for (int c = next.fetch_add(1); c < nch; c = next.fetch_add(1)) {
+        const int e0 = c * chunk, e1 = e0 + chunk < ne ? e0 + chunk : ne;
+        part[c] = quad_integrate_range(D, coords, elv, lset, dt, order, policy, ex, ey, ez, e0, e1, &st[c]);
+      }
+    });
+  for (auto& t : th) t.join();
+  double sum = 0;
+  int first = 0;
+  for (int c = 0; c < nch; c++) {
+    sum += part[c];
+    if (!first) first = st[c];
+  }
+  if (status) *status = first;
   return sum;
 }
 
