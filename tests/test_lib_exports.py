@@ -82,3 +82,54 @@ def test_rule_family_matches_oracle(lib):
             assert n == len(rw)
             assert np.max(np.abs(pts[:n] - rp)) <= 4e-16, (d, p)
             assert np.max(np.abs(w[:n] - rw)) <= 4e-16, (d, p)
+
+
+def declared_arity():
+    """Number of parameters of every xg_* function the headers declare."""
+    out = {}
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if not h.endswith(".h"):
+            continue
+        src = open(os.path.join(ROOT, "include", h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"\b(?:int|const char\*)\s+(xg_\w+)\s*\(([^)]*)\)\s*;", src, flags=re.S):
+            params = m.group(2).strip()
+            out[m.group(1)] = 0 if params in ("", "void") else params.count(",") + 1
+    return out
+
+
+def test_ctypes_signatures_match_the_header():
+    """The ctypes argument lists in ngsxfem_gb300/_lib.py have the arity the
+    header declares (a mismatch would only show on a GPU)."""
+    from ngsxfem_gb300 import _lib
+    arity = declared_arity()
+    sigs = _lib.SIGNATURES if hasattr(_lib, "SIGNATURES") else None
+    if sigs is None:
+        L = _lib.load()
+        sigs = {n: (None, getattr(L, n).argtypes) for n in _lib.EXPORTS}
+    bad = [(n, len(a), arity[n]) for n, (_, a) in sigs.items() if a is not None and n in arity and len(a) != arity[n]]
+    assert not bad, bad
+
+
+def test_call_sites_pass_the_declared_number_of_arguments():
+    """Every _lib.call("xg_...", ...) in the package, bench.py and the smoke
+    check passes as many arguments as the entry point takes."""
+    import ast
+    arity = declared_arity()
+    files = [os.path.join(ROOT, "ngsxfem_gb300", f) for f in os.listdir(os.path.join(ROOT, "ngsxfem_gb300"))
+             if f.endswith(".py")] + [os.path.join(ROOT, "bench.py"), os.path.join(ROOT, "__graft_entry__.py")]
+    checked, bad = 0, []
+    for path in files:
+        for node in ast.walk(ast.parse(open(path).read())):
+            if not (isinstance(node, ast.Call) and isinstance(node.func, ast.Attribute) and node.func.attr == "call"):
+                continue
+            if not node.args or not isinstance(node.args[0], ast.Constant) or not isinstance(node.args[0].value, str):
+                continue
+            name = node.args[0].value
+            if name not in arity or any(isinstance(a, ast.Starred) for a in node.args):
+                continue
+            checked += 1
+            if len(node.args) - 1 != arity[name]:
+                bad.append((os.path.basename(path), node.lineno, name, len(node.args) - 1, arity[name]))
+    assert checked > 40
+    assert not bad, bad
