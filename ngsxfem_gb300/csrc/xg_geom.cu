@@ -237,6 +237,11 @@ __global__ void k_cut_rules(int ne, const int32_t* __restrict__ elv, const doubl
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int e = elems[i];
+  if (e < 0 || e >= ne) {  // an element number outside the mesh: no read of it
+    set_err(err, XG_ERR_ARG);
+    counts[i] = 0;
+    return;
+  }
   double l[D + 1];
   double xv[D + 1][3];
 #pragma unroll
@@ -546,6 +551,11 @@ __global__ void k_st_cut_rules(int ne, const int32_t* __restrict__ elv, const do
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int e = elems[i];
+  if (e < 0 || e >= ne) {  // an element number outside the mesh: no read of it
+    set_err(err, XG_ERR_ARG);
+    counts[i] = 0;
+    return;
+  }
   double lst[3 * (D + 1)];
   double xv[D + 1][3];
   for (int v = 0; v <= D; v++) {
