@@ -101,6 +101,9 @@ const char* xg_last_error(void);
 int xg_device_ok(int* ok);
 
 /* ---- mesh (ngcomp::MeshAccess stand-in) ---------------------------------- */
+/* (xg_cutinfo_update also accepts quadrilateral / hexahedral meshes,
+ * xg_mesh_create_tensor: element part only, from the order-0 cut rules of
+ * LevelsetCutQuadrilateral with the FIND_OPTIMAL policy.) */
 /* Builds edges, faces and the facet->element table on the host and uploads
  * coordinates (SoA) and topology to the current device.
  * h_coords: nv*dim (AoS), h_elv: ne*(dim+1).  dim 2 (trig) or 3 (tet). */

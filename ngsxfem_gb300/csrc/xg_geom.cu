@@ -631,7 +631,8 @@ static inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / 
 // entry points that need simplices (facet topology, the simplex cut kernels)
 static int need_simplices(const xg_mesh* m, const char* what) {
   if (!m->tensor) return XG_OK;
-  set_last_error(std::string(what) + ": quadrilateral / hexahedral meshes support xg_cut_rules and xg_integrate only");
+  set_last_error(std::string(what) +
+                 ": quadrilateral / hexahedral meshes support xg_cut_rules, xg_integrate and xg_cutinfo_update only");
   return XG_ERR_UNSUPPORTED;
 }
 
@@ -649,7 +650,10 @@ int xg_interpolate_p1_perturb(double* d_vals, int64_t n, double eps, void* strea
 int xg_cutinfo_update(xg_mesh* m, const double* d_lset, uint8_t* d_dom, double* d_ratio, uint64_t* d_bits,
                       void* stream) {
   if (!m) return XG_ERR_ARG;
-  if (int st_t = need_simplices(m, "xg_cutinfo_update")) return st_t;
+  if (m->tensor) {
+    if (!d_lset || !d_dom || !d_ratio || !d_bits) return XG_ERR_ARG;
+    return xg::quad_cutinfo(m, d_lset, d_dom, d_ratio, d_bits, stream);
+  }
   return xg::cutinfo_update_ws(m, d_lset, d_dom, d_ratio, d_bits, m->d_cutlist, stream);
 }
 }  // extern "C"

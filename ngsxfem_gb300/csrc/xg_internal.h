@@ -158,6 +158,7 @@ int quad_cut_rules(xg_mesh* m, const double* d_lset, const int32_t* d_elems, int
                    int32_t max_pts, int32_t* d_counts, double* d_pts, double* d_wts, void* stream);
 int quad_integrate(xg_mesh* m, const double* d_lset, int dt, int order, int pol, int ex, int ey, int ez,
                    const uint64_t* d_defined_on, double* d_result, void* stream);
+int quad_cutinfo(xg_mesh* m, const double* d_lset, uint8_t* d_dom, double* d_ratio, uint64_t* d_bits, void* stream);
 
 }  // namespace xg
 

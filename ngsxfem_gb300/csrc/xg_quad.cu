@@ -169,6 +169,58 @@ __global__ void __launch_bounds__(128) k_quad_rules(int ne, const int32_t* __res
   counts[i] = (cut && k == 0) ? -1 : k;
 }
 
+// CutInformation::Update (xfem/cutinfo.cpp:61-132) on quadrilaterals /
+// hexahedra: the weights of the order-0 NEG and POS rules give the part
+// volumes, ratio = NEG / (NEG + POS), the domain type and the combined-domain
+// bits (rows: CDOM values; bits set with atomic OR on cleared words).
+template <int D>
+__global__ void __launch_bounds__(128) k_quad_cutinfo(int ne, const int32_t* __restrict__ elv,
+                                                      const double* __restrict__ xyz, int nv,
+                                                      const double* __restrict__ lset, int pol, uint8_t* __restrict__ dom,
+                                                      double* __restrict__ ratio, unsigned long long* bits, int64_t nw,
+                                                      int* err) {
+  constexpr int NV = 1 << D;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
+    double l[NV], xv[NV][3];
+    gather<D>(ne, elv, xyz, nv, lset, (int)e, l, xv);
+    double part[2] = {0.0, 0.0};  // [NEG, POS]
+    for (int np : {XG_POS, XG_NEG}) {
+      auto emit = [&](const double*, double w) { part[np] += w; };
+      const int st = qc::tp_cut_rule<D>(&g_qrules, l, np, 0, pol, emit);
+      if (st > 0) set_err(err, st);
+    }
+    ratio[e] = part[XG_NEG] / (part[XG_NEG] + part[XG_POS]);
+    const int d = part[XG_NEG] > 0.0 ? (part[XG_POS] > 0.0 ? XG_IF : XG_NEG) : XG_POS;
+    dom[e] = (uint8_t)d;
+    const unsigned long long bit = 1ull << (e & 63);
+    const int64_t w = e >> 6;
+    // NEG: NEG, UNCUT, HASNEG, ANY; POS: POS, UNCUT, HASPOS, ANY; IF: IF, HASNEG, HASPOS, ANY
+    const int r0 = d == XG_NEG ? XG_CDOM_NEG : (d == XG_POS ? XG_CDOM_POS : XG_CDOM_IF);
+    const int r1 = d == XG_IF ? XG_CDOM_HASNEG : XG_CDOM_UNCUT;
+    const int r2 = d == XG_NEG ? XG_CDOM_HASNEG : XG_CDOM_HASPOS;
+    atomicOr(bits + r0 * nw + w, bit);
+    atomicOr(bits + r1 * nw + w, bit);
+    atomicOr(bits + r2 * nw + w, bit);
+    atomicOr(bits + XG_CDOM_ANY * nw + w, bit);
+  }
+}
+
+int quad_cutinfo(xg_mesh* m, const double* d_lset, uint8_t* d_dom, double* d_ratio, uint64_t* d_bits, void* stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  const int64_t nw = ((int64_t)m->ne + 63) / 64;
+  XG_CUDA(cudaMemsetAsync(d_bits, 0, sizeof(uint64_t) * 8 * nw, s));
+  const unsigned nb = 152 * 8;
+  if (m->dim == 2)
+    k_quad_cutinfo<2><<<nb, 128, 0, s>>>(m->ne, m->d_elv, m->d_xyz, m->nv, d_lset, qc::POL_FIND_OPTIMAL, d_dom, d_ratio,
+                                         (unsigned long long*)d_bits, nw, m->d_err);
+  else
+    k_quad_cutinfo<3><<<nb, 128, 0, s>>>(m->ne, m->d_elv, m->d_xyz, m->nv, d_lset, qc::POL_FIND_OPTIMAL, d_dom, d_ratio,
+                                         (unsigned long long*)d_bits, nw, m->d_err);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "k_quad_cutinfo");
+  return XG_OK;
+}
+
 // most points a rule of (dim, dt, order) can have: up to 3 (2D) / 5 (3D)
 // slabs between the xi breakpoints, each a tensor product over the segment
 // rule, or the simplex fallback (2 triangles / 6 tetrahedra, up to 3

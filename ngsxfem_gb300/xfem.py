@@ -362,6 +362,8 @@ class CutInfo:
             return
         _lib.call("xg_cutinfo_update", self.dm.h, _vp(lv), _vp(self.dom), _vp(self.cut_ratio), _vp(self.bits),
                   _stream())
+        if getattr(self.mesh, "tensor", False):
+            return  # quadrilaterals / hexahedra: the element part only
         if self.nbnd:
             _lib.call("xg_cutinfo_update_bnd", self.dm.h, _vp(lv), _vp(self.dom_bnd), _vp(self.cut_ratio_bnd),
                       _vp(self.bits_bnd), _stream())
@@ -397,11 +399,15 @@ class CutInfo:
 
     def GetCutNeighboringNodes(self, node_type="vertex"):
         """Nodes of cut elements (cut_neighboring_node of CutInformation)."""
+        if getattr(self.mesh, "tensor", False):
+            raise NotImplementedError("node markers are built for simplex meshes")
         n = {"vertex": self.dm.nv, "edge": self.dm.nedges, "face": self.dm.nfaces, "element": self.mesh.ne}[node_type]
         return BitArray(n, self.cut_nb_nodes[node_type].clone())
 
     def GetDomainOfNodes(self, node_type="vertex"):
         """Domain type (NEG/POS) of every node (dom_of_node of CutInformation)."""
+        if getattr(self.mesh, "tensor", False):
+            raise NotImplementedError("node markers are built for simplex meshes")
         n = {"vertex": self.dm.nv, "edge": self.dm.nedges, "face": self.dm.nfaces, "cell": self.mesh.ne}[node_type]
         return self.dom_of_node[node_type][:n]
 

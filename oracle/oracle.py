@@ -110,6 +110,7 @@ def lib():
         L.orc_quad_straight_cut_rule.argtypes = [I, P, P, I, I, I, P, P, I]
         L.orc_quad_integrate.restype = ctypes.c_double
         L.orc_quad_integrate.argtypes = [I, I, P, I, P, P, I, I, I, I, I, I, P]
+        L.orc_quad_cutinfo.argtypes = [I, I, P, I, P, P, I, P, P, P]
         L.orc_quad_integrate_mt.restype = ctypes.c_double
         L.orc_quad_integrate_mt.argtypes = [I, I, P, I, P, P, I, I, I, I, I, I, I, P]
         L.orc_mlset_cut_rule.argtypes = [I, P, I, P, I, P, I, P, P, I]
@@ -181,6 +182,22 @@ def quad_cut_rule(lset_vals, dt, order, policy=QUAD_OPTIMAL, elcoords=None, maxp
     if n < -1:
         raise RuntimeError("oracle quad rule status %d" % (-n - 1))
     return pts[:n].copy(), w[:n].copy()
+
+
+def quad_cutinfo(mesh, lset, policy=QUAD_OPTIMAL):
+    """CutInfo on a quad / hex mesh: (dom, ratio, bits[8][nwords] as uint64)."""
+    c = np.ascontiguousarray(mesh.coords, dtype=np.float64)
+    el = np.ascontiguousarray(mesh.elements, dtype=np.int32)
+    l = np.ascontiguousarray(lset, dtype=np.float64)
+    ne = el.shape[0]
+    dom = np.zeros(ne, dtype=np.uint8)
+    ratio = np.zeros(ne)
+    bits = np.zeros((8, (ne + 63) // 64), dtype=np.uint64)
+    st = lib().orc_quad_cutinfo(c.shape[1], c.shape[0], _p(c), ne, _p(el), _p(l), policy, _p(dom), _p(ratio),
+                                _p(bits))
+    if st:
+        raise RuntimeError("oracle quad cutinfo status %d" % st)
+    return dom, ratio, bits
 
 
 def quad_integrate(mesh, lset, dt, order, policy=QUAD_OPTIMAL, exps=(0, 0, 0), nthreads=1):

@@ -179,6 +179,9 @@ int orc_quad_cut_rule(int D, const double* lset_vals, int dt, int order, int pol
  * "no rule", -1). */
 int orc_quad_straight_cut_rule(int D, const double* xv, const double* lset_vals, int dt, int order, int policy,
                                double* pts, double* wts, int maxpts);
+/* CutInfo.Update on a quad / hex mesh: dom, ratio, bits[8][ceil(ne/64)] as orc_cutinfo. */
+int orc_quad_cutinfo(int D, int nv, const double* coords, int ne, const int32_t* elv, const double* lset, int policy,
+                     uint8_t* dom, double* ratio, uint64_t* bits);
 /* Integrate(x^ex y^ey z^ez * dCut) on a quad / hex mesh: coords[nv][D], elv[ne][2^D]. */
 double orc_quad_integrate(int D, int nv, const double* coords, int ne, const int32_t* elv, const double* lset,
                           int dt, int order, int policy, int ex, int ey, int ez, int* status);

@@ -657,6 +657,40 @@ int orc_quad_cut_rule(int D, const double* lset_vals, int dt, int order, int pol
   return n;
 }
 
+// CutInformation::Update (xfem/cutinfo.cpp:61-132) on a quadrilateral /
+// hexahedral mesh: per element the weights of the order-0 NEG and POS rules,
+// ratio = NEG / (NEG + POS), domain IF / NEG / POS, bits[8][ceil(ne/64)] per
+// combined domain type.  Returns 0 or the first error status.
+int orc_quad_cutinfo(int D, int nv, const double* coords, int ne, const int32_t* elv, const double* lset, int policy,
+                     uint8_t* dom, double* ratio, uint64_t* bits) {
+  (void)nv;
+  (void)coords;
+  const int nve = D == 2 ? 4 : 8;
+  const int64_t nw = (ne + 63) / 64;
+  for (int64_t i = 0; i < 8 * nw; i++) bits[i] = 0;
+  int status = 0;
+  for (int e = 0; e < ne; e++) {
+    double lv[8];
+    for (int v = 0; v < nve; v++) lv[v] = lset[elv[(size_t)e * nve + v]];
+    double part[2] = {0.0, 0.0};  // [NEG, POS]
+    for (int np : {POS, NEG}) {
+      IR ir;
+      const int n = quad_rule_untrafo(D, lv, np, 0, policy, ir);
+      if (n < -1) {
+        if (!status) status = -n - 1;
+        continue;
+      }
+      for (double w : ir.w) part[np] += w;
+    }
+    ratio[e] = part[NEG] / (part[NEG] + part[POS]);
+    const int d = part[NEG] > 0.0 ? (part[POS] > 0.0 ? IF : NEG) : POS;
+    dom[e] = (uint8_t)d;
+    const int rows[3][4] = {{1, 3, 5, 7}, {2, 3, 6, 7}, {4, 5, 6, 7}};  // NEG, POS, IF
+    for (int r : rows[d]) bits[r * nw + (e >> 6)] |= 1ull << (e & 63);
+  }
+  return status;
+}
+
 int orc_quad_straight_cut_rule(int D, const double* xv, const double* lset_vals, int dt, int order, int policy,
                                double* pts, double* wts, int maxpts) {
   const int n = orc_quad_cut_rule(D, lset_vals, dt, order, policy, pts, wts, maxpts);

@@ -164,9 +164,9 @@ def test_tensor_mesh_rejects_simplex_only_calls(xg, orc):
     m = MakeStructured2DMesh(quads=True, nx=3, ny=3)
     with pytest.raises(Exception):
         xg.H1(m, order=2)
-    gf = xg.GridFunction(xg.H1(m, order=1))
+    a = xg.BitArray(m.ne)
     with pytest.raises(Exception):
-        xg.CutInfo(m, gf)
+        xg.GetFacetsWithNeighborTypes(m, a, b=a)
 
 
 def test_rule_capacity_and_bad_element(xg, orc):

@@ -205,3 +205,26 @@ def test_device_rule_code_matches_oracle_bitwise(orc, tmp_path):
     r = subprocess.run([exe], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
     assert " 0 mismatches" in r.stdout
+
+
+def test_cutinfo_ratios_give_the_volumes(orc):
+    """CutInfo on quads / hexes: the order-0 part volumes reproduce the planar
+    cut's NEG measure (uniform elements: sum of ratio x element volume; exact
+    in 2D), the domain types follow the ratios, and the bit rows are
+    consistent."""
+    for m, coef, ref in ((MakeStructured2DMesh(quads=True, nx=10, ny=10), KA["planar2d"]["lset"],
+                          KA["planar2d"]["values"]["NEG"]),
+                         (MakeStructured3DMesh(6, hexes=True), KA["planar3d"]["lset"], KA["planar3d"]["values"]["NEG"])):
+        l = vertex_lset(orc, m, planar(coef))
+        dom, ratio, bits = orc.quad_cutinfo(m, l)
+        vol = 1.0 / m.ne
+        # order-0 rules: the cut length of a quad is linear in the tensor
+        # direction (exact), the cut area of a hex quadratic (not exact)
+        assert abs(ratio.sum() * vol - ref) < (1e-13 if m.dim == 2 else 1e-3)
+        # uncut elements have ratio 1 / 0 (a cut element with a sliver part may round to them too)
+        assert (ratio[dom == 0] == 1.0).all() and (ratio[dom == 1] == 0.0).all()
+        assert ((ratio > 0) & (ratio < 1) <= (dom == 2)).all()
+        b = np.unpackbits(bits.view(np.uint8), axis=1, bitorder="little")[:, : m.ne].astype(bool)
+        assert (b[1] == (dom == 0)).all() and (b[2] == (dom == 1)).all() and (b[4] == (dom == 2)).all()
+        assert (b[3] == (b[1] | b[2])).all() and (b[5] == (b[1] | b[4])).all() and (b[6] == (b[2] | b[4])).all()
+        assert b[7].all() and not b[0].any()
