@@ -175,6 +175,38 @@ __global__ void __launch_bounds__(kMlThreads) k_mlset_mark(int ne, const int32_t
   }
 }
 
+// Integrate(x^ex y^ey z^ez * dCut(lset, dt, vb=BND)) over the boundary
+// elements (the boundary facets, vertices ascending): thread per boundary
+// element, fixed-order block sums.
+template <int D>
+__global__ void __launch_bounds__(kMlThreads) k_integrate_bnd(int64_t nbnd, const int32_t* __restrict__ bnd_v,
+                                                              const double* __restrict__ xyz, int nv,
+                                                              const double* __restrict__ lset, int dt, int order,
+                                                              int ex, int ey, int ez, double* block_sums, int* err) {
+  __shared__ double red[kMlThreads];
+  double acc = 0.0;
+  for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < nbnd; b += (int64_t)gridDim.x * blockDim.x) {
+    double xv[D][3], l[D];
+    for (int v = 0; v < D; v++) {
+      const int vid = bnd_v[(int64_t)v * nbnd + b];
+      l[v] = lset[vid];
+      for (int c = 0; c < 3; c++) xv[v][c] = c < D ? xyz[(int64_t)c * nv + vid] : 0.0;
+    }
+    auto emit = [&](const double* x, double w, double meas) {
+      acc += w * meas * (ipow_ml(x[0], ex) * ipow_ml(x[1], ey) * (D == 3 ? ipow_ml(x[2], ez) : 1.0));
+    };
+    const int st = ml::bnd_rule<D>(&g_mrules, xv, l, dt, order, emit);
+    if (st) set_err(err, st);
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = kMlThreads / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) block_sums[blockIdx.x] = red[0];
+}
+
 static int launch_check_ml(const char* what) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, what);
@@ -290,6 +322,39 @@ int xg_mlset_mark(xg_mesh* m, const double* d_lsets, int32_t nlsets, const int8_
   ml::MlDesc md;
   if (int st = mlset_desc(nlsets, h_domains, ndomains, &md)) return st;
   return mlset_mark(m, d_lsets, md, mode, d_bits, stream);
+}
+
+int xg_integrate_bnd(xg_mesh* m, const double* d_lset, int dt, int order, int ex, int ey, int ez, double* d_result,
+                     void* stream) {
+  if (int st = mlset_mesh_ok(m, "xg_integrate_bnd")) return st;
+  if (!d_lset || !d_result || dt < 0 || dt > 2 || order < 0 || order > kMaxOrder || ex < 0 || ey < 0 || ez < 0)
+    return XG_ERR_ARG;
+  if (dt == XG_IF && m->dim == 3) {
+    set_last_error("xg_integrate_bnd: the interface on boundary triangles (codimension 2) is not supported");
+    return XG_ERR_UNSUPPORTED;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t need = sizeof(double) * kMlBlocks;
+  if (m->scratch_bytes < need) {
+    cudaFree(m->d_scratch);
+    m->d_scratch = nullptr;
+    m->scratch_bytes = 0;
+    XG_CUDA(cudaMalloc(&m->d_scratch, need));
+    m->scratch_bytes = need;
+  }
+  double* bs = (double*)m->d_scratch;
+  if (m->nbnd == 0) {
+    XG_CUDA(cudaMemsetAsync(d_result, 0, sizeof(double), s));
+    return XG_OK;
+  }
+  if (m->dim == 2)
+    k_integrate_bnd<2><<<kMlBlocks, kMlThreads, 0, s>>>(m->nbnd, m->d_bnd_v, m->d_xyz, m->nv, d_lset, dt, order, ex,
+                                                       ey, ez, bs, m->d_err);
+  else
+    k_integrate_bnd<3><<<kMlBlocks, kMlThreads, 0, s>>>(m->nbnd, m->d_bnd_v, m->d_xyz, m->nv, d_lset, dt, order, ex,
+                                                       ey, ez, bs, m->d_err);
+  k_mlset_final<<<1, 32, 0, s>>>(bs, kMlBlocks, d_result);
+  return launch_check_ml("k_integrate_bnd");
 }
 
 int xg_mlset_rule_capacity(int dim, int32_t nlsets, int32_t ndomains, int order) {

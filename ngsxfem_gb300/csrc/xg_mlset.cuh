@@ -323,3 +323,58 @@ XG_QNI int element_rule(const RuleTable* Rp, const AGeo& g, int M, int ntup, con
 
 }  // namespace ml
 }  // namespace xg
+
+namespace xg {
+namespace ml {
+
+// StraightCutIntegrationRule on a boundary element (a (D-1)-simplex in D
+// dimensions; cutint/straightcutrule.cpp:582-677, the point measure of
+// :641-651 for IF on 2D boundary segments): emit(physical point, weight,
+// measure) with weight * measure the point's share.  xv: the D vertices, l
+// their level-set values.  Returns 0 or an xg error (IF on 3D boundary
+// triangles is not supported).
+template <int D, class E>
+XG_QNI int bnd_rule(const RuleTable* Rp, const double (*xv)[3], const double* l, int dt, int order, E& emit) {
+  const RuleTable& R = *Rp;
+  constexpr int d = D - 1;
+  double F[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+  for (int k = 0; k < d; k++)
+    for (int r = 0; r < 3; r++) F[r][k] = xv[k][r] - xv[d][r];
+  double meas;
+  if (d == 1) {
+    meas = qc::qnorm3(F[0][0], F[1][0], F[2][0]);
+  } else {
+    meas = qc::qnorm3(F[1][0] * F[2][1] - F[2][0] * F[1][1], F[2][0] * F[0][1] - F[0][0] * F[2][1],
+                      F[0][0] * F[1][1] - F[1][0] * F[0][1]);
+  }
+  auto to_phys = [&](const double* xi, double w) {
+    double x[3];
+    for (int r = 0; r < 3; r++) {
+      double s = xv[d][r];
+      for (int k = 0; k < d; k++) s += F[r][k] * xi[k];
+      x[r] = s;
+    }
+    emit(x, w, meas);
+  };
+  const int dom = qc::qcheck(l, d + 1, 0.0);
+  if (dom != XG_IF) {
+    if (dom != dt) return 0;
+    const int o = clamp_order(order), off = R.off[d][o], cnt = R.cnt[d][o];
+    for (int q = 0; q < cnt; q++) to_phys(R.x[off + q], R.w[off + q]);
+    return 0;
+  }
+  if (dt == XG_IF && d != 1) return XG_ERR_UNSUPPORTED;
+  Simp root;
+  for (int i = 0; i <= d; i++)
+    for (int k = 0; k < 3; k++) root.p[i].x[k] = (i < d && k == i) ? 1.0 : 0.0;
+  root.np = d + 1;
+  Simp ch[3];
+  const int n = split(root, l, dt, ch);
+  if (n < 0) return -n;
+  auto on_point = [&](const double* xi, double w) { to_phys(xi, dt == XG_IF ? w / meas : w); };
+  for (int c = 0; c < n; c++) qc::qsimplex_plain(Rp, ch[c].p, ch[c].np, order, on_point);
+  return 0;
+}
+
+}  // namespace ml
+}  // namespace xg

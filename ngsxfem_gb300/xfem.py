@@ -573,6 +573,7 @@ class _Measure:
         self.time_order = -1 if t is None else int(t)
         self.tref = kw.get("tref")
         self.quad_dir_policy = int(kw.get("quad_dir_policy", OPTIMAL))
+        self.vb = kw.get("vb", VOL)
         if kw.get("downscale", 1.0) != 1.0:
             raise NotImplementedError("downscale != 1 is not supported")
 
@@ -983,7 +984,17 @@ x, y, z = _Monomial((1, 0, 0)), _Monomial((0, 1, 0)), _Monomial((0, 0, 1))
 
 def Integrate(levelset_domain=None, cf=None, mesh=None, order=5, integrand=None):
     """Integrate(x^a y^b z^c * dCut(lset, dt, order)) on the GPU
-    (cutint/cutintegral.cpp:126-212): a deterministic fixed-order sum."""
+    (cutint/cutintegral.cpp:126-212): a deterministic fixed-order sum.  Also
+    called as Integrate(x**2 * dCut(...), mesh) or Integrate(dCut(...), mesh)."""
+    if isinstance(levelset_domain, _Measure):
+        levelset_domain = ("integral", _Monomial(), levelset_domain)
+    if isinstance(levelset_domain, tuple) and len(levelset_domain) == 3 and levelset_domain[0] == "integral":
+        integrand, levelset_domain = levelset_domain, None
+        if isinstance(cf, Mesh):
+            mesh, cf = cf, None
+    scale = integrand[2].scale if integrand is not None else 1.0
+    if scale != 1.0:
+        return scale * Integrate(levelset_domain, cf, mesh, order, ("integral", integrand[1], _unscaled(integrand[2])))
     if integrand is not None:
         _, mono, meas = integrand
         lset, dt, order = meas.levelset, meas.domain_type, meas.order if meas.order is not None else order
@@ -994,8 +1005,16 @@ def Integrate(levelset_domain=None, cf=None, mesh=None, order=5, integrand=None)
         policy = levelset_domain.get("quad_dir_policy", OPTIMAL)
         mono = cf if isinstance(cf, _Monomial) else _Monomial()
         defined = None
+    vb = VOL
     if integrand is not None:
         policy = getattr(meas, "quad_dir_policy", OPTIMAL)
+        vb = getattr(meas, "vb", VOL)
+    else:
+        vb = levelset_domain.get("vb", VOL)
+    if vb == BND:
+        if defined is not None:
+            raise NotImplementedError("definedonelements on boundary cut integrals")
+        return _integrate_bnd(lset, dt, order, mono, mesh)
     if isinstance(lset, (tuple, list)):
         return _integrate_mlset(lset, dt, order, mono, defined, mesh)
     mesh = mesh if mesh is not None else lset.space.mesh
@@ -1003,6 +1022,24 @@ def Integrate(levelset_domain=None, cf=None, mesh=None, order=5, integrand=None)
     res = torch.zeros(1, dtype=torch.float64, device=_dev())
     _lib.call("xg_integrate_ex", dm.h, _vp(_lset_vec(lset)), dt, order, int(policy), mono.e[0], mono.e[1],
               mono.e[2], _vp(defined.words) if defined is not None else None, _vp(res), _stream())
+    dm.check()
+    return float(res.item())
+
+
+def _unscaled(meas):
+    out = _Measure.__new__(_Measure)
+    out.__dict__.update(meas.__dict__)
+    out.scale = 1.0
+    return out
+
+
+def _integrate_bnd(lset, dt, order, mono, mesh):
+    """Integrate(f * dCut(lset, dt, vb=BND)): xg_integrate_bnd."""
+    mesh = mesh if mesh is not None else lset.space.mesh
+    dm = device_mesh(mesh)
+    res = torch.zeros(1, dtype=torch.float64, device=_dev())
+    _lib.call("xg_integrate_bnd", dm.h, _vp(_lset_vec(lset)), dt, order, mono.e[0], mono.e[1], mono.e[2], _vp(res),
+              _stream())
     dm.check()
     return float(res.item())
 

@@ -117,6 +117,8 @@ def lib():
         L.orc_mlset_integrate.restype = ctypes.c_double
         L.orc_mlset_integrate.argtypes = [I, I, P, I, P, I, P, I, P, I, I, I, I, P]
         L.orc_mlset_mark.argtypes = [I, I, P, I, P, I, P, I, P, I, P]
+        L.orc_integrate_bnd.restype = ctypes.c_double
+        L.orc_integrate_bnd.argtypes = [I, I, P, I, P, P, I, I, I, I, I, P]
         _lib = L
     return _lib
 
@@ -268,6 +270,17 @@ def mlset_mark(mesh, lsets, dts, mode):
     if st:
         raise RuntimeError("oracle mlset marking status %d" % st)
     return np.unpackbits(bits.view(np.uint8), bitorder="little")[: el.shape[0]].astype(bool)
+
+
+def integrate_bnd(mesh, lset, dt, order, exps=(0, 0, 0)):
+    """Integrate(x^a y^b z^c * dCut(lset, dt, vb=BND)); returns (value, status)."""
+    c = np.ascontiguousarray(mesh.coords, dtype=np.float64)
+    el = np.ascontiguousarray(mesh.elements, dtype=np.int32)
+    l = np.ascontiguousarray(lset, dtype=np.float64)
+    st = np.zeros(1, dtype=np.int32)
+    v = lib().orc_integrate_bnd(c.shape[1], c.shape[0], _p(c), el.shape[0], _p(el), _p(l), dt, order, exps[0],
+                                exps[1], exps[2], _p(st))
+    return v, int(st[0])
 
 
 def time_basis(kt, tau):

@@ -206,6 +206,14 @@ double orc_mlset_integrate(int D, int nv, const double* coords, int ne, const in
  * region's order-0 rule).  Returns 0 or the first error status. */
 int orc_mlset_mark(int D, int nv, const double* coords, int ne, const int32_t* elv, int M, const double* lsets,
                    int ntup, const int* dts, int mode, uint64_t* bits);
+/* Integrate(x^ex y^ey z^ez * dCut(lset, dt, vb=BND)) over the boundary elements of
+ * a simplex mesh (elements' facets that belong to one element); IF on 2D
+ * boundary segments is the point measure (each intersection point counts 1). */
+double orc_integrate_bnd(int D, int nv, const double* coords, int ne, const int32_t* elv, const double* lset, int dt,
+                         int order, int ex, int ey, int ez, int* status);
+/* The share of one boundary element (vertices xv[D][3], values l[D]). */
+double orc_bnd_element_integral(int D, const double* xv, const double* l, int dt, int order, int ex, int ey, int ez,
+                                int* status);
 
 #ifdef __cplusplus
 }

@@ -15,6 +15,7 @@
 //                                         (compatibility, condensing, parts)
 //   cutint/cutintegral.cpp:126-212       Integrate
 // The element geometry is affine: x = x_D + F xi with F(:,k) = x_k - x_D.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -480,3 +481,117 @@ double orc_mlset_integrate(int D, int nv, const double* coords, int ne, const in
 }
 
 }  // extern "C"
+
+// ---- boundary cut integration (dCut(lset, dt, vb=BND)) -------------------------------
+// StraightCutIntegrationRule on a boundary element (cutint/straightcutrule.cpp:
+// 582-677 with the ET_SEGM-in-2D point measure of :641-651) and Integrate over
+// the boundary elements (cutint/cutintegral.cpp:126-212).  Boundary elements:
+// the element facets that belong to one element, vertices ascending; the
+// reference simplex of dimension D-1 maps by x = x_last + F xi.
+namespace {
+
+double bnd_element_integral(int D, const double (*xv)[3], const double* l, int dt, int order, int ex, int ey, int ez) {
+  const int d = D - 1;  // dimension of the boundary element
+  // F (3 x d): columns x_k - x_d; measure: length (d = 1) or |F1 x F2| (d = 2)
+  double F[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+  for (int k = 0; k < d; k++)
+    for (int r = 0; r < 3; r++) F[r][k] = xv[k][r] - xv[d][r];
+  double meas;
+  if (d == 1) {
+    const double a[3] = {F[0][0], F[1][0], F[2][0]};
+    meas = norm3(a);
+  } else {
+    const double cr[3] = {F[1][0] * F[2][1] - F[2][0] * F[1][1], F[2][0] * F[0][1] - F[0][0] * F[2][1],
+                          F[0][0] * F[1][1] - F[1][0] * F[0][1]};
+    meas = norm3(cr);
+  }
+  std::vector<double> lv(l, l + d + 1);
+  const int dom = check_cut(lv);
+  std::vector<V3> pts;
+  std::vector<double> wts;
+  if (dom != IF) {
+    if (dom != dt) return 0.0;
+    const Rule1 r = base(d, order);
+    for (size_t q = 0; q < r.w.size(); q++) {
+      pts.push_back(V3{{r.p[3 * q], r.p[3 * q + 1], r.p[3 * q + 2]}});
+      wts.push_back(r.w[q]);
+    }
+  } else {
+    if (dt == IF && d != 1) throw MErr{E_UNSUPPORTED};
+    Simplex ref;
+    for (int i = 0; i <= d; i++) {
+      V3 v = {{0, 0, 0}};
+      if (i < d) v.x[i] = 1.0;
+      ref.push_back(v);
+    }
+    for (const Simplex& s : decompose(ref, lv, dt)) plain_rule(s, order, pts, wts);
+    if (dt == IF)  // point measure: weight / measure, so that weight * measure = 1
+      for (double& w : wts) w = w / meas;
+  }
+  double sum = 0;
+  for (size_t q = 0; q < wts.size(); q++) {
+    double x[3];
+    for (int r = 0; r < 3; r++) {
+      double s = xv[d][r];
+      for (int k = 0; k < d; k++) s += F[r][k] * pts[q].x[k];
+      x[r] = s;
+    }
+    const double fv = std::pow(x[0], ex) * std::pow(x[1], ey) * (D == 3 ? std::pow(x[2], ez) : 1.0);
+    sum += wts[q] * meas * fv;
+  }
+  return sum;
+}
+
+}  // namespace
+
+// one boundary element (vertices xv[D][3], values l[D]); *status on an error
+extern "C" double orc_bnd_element_integral(int D, const double* xv, const double* l, int dt, int order, int ex, int ey,
+                                           int ez, int* status) {
+  double v[3][3];
+  for (int i = 0; i < D; i++)
+    for (int r = 0; r < 3; r++) v[i][r] = xv[3 * i + r];
+  *status = 0;
+  try {
+    return bnd_element_integral(D, v, l, dt, order, ex, ey, ez);
+  } catch (const MErr& err) {
+    *status = err.code;
+  }
+  return 0.0;
+}
+
+extern "C" double orc_integrate_bnd(int D, int nv, const double* coords, int ne, const int32_t* elv,
+                                    const double* lset, int dt, int order, int ex, int ey, int ez, int* status) {
+  (void)nv;
+  if (status) *status = 0;
+  // facets (sorted vertex triples / pairs) and their element counts
+  std::vector<std::vector<int>> facets;
+  for (int e = 0; e < ne; e++)
+    for (int skip = 0; skip <= D; skip++) {
+      std::vector<int> f;
+      for (int v = 0; v <= D; v++)
+        if (v != skip) f.push_back(elv[(size_t)e * (D + 1) + v]);
+      std::sort(f.begin(), f.end());
+      facets.push_back(f);
+    }
+  std::sort(facets.begin(), facets.end());
+  double sum = 0;
+  for (size_t i = 0; i < facets.size();) {
+    size_t j = i;
+    while (j < facets.size() && facets[j] == facets[i]) j++;
+    if (j - i == 1) {
+      double xv[3][3] = {}, l[3];
+      for (int v = 0; v < D; v++) {
+        const int id = facets[i][v];
+        l[v] = lset[id];
+        for (int r = 0; r < D; r++) xv[v][r] = coords[(size_t)id * D + r];
+      }
+      try {
+        sum += bnd_element_integral(D, xv, l, dt, order, ex, ey, ez);
+      } catch (const MErr& err) {
+        if (status && *status == 0) *status = err.code;
+      }
+    }
+    i = j;
+  }
+  return sum;
+}

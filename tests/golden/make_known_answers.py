@@ -1,7 +1,7 @@
 """Writes known_answers.json: the closed-form values ngsxfem's own tests assert
 for the straight-cut path (tests/pytests/test_straightcutrule.py,
 tests/pytests/test_spacetimecutrule.py, tests/pytests/test_quadchallenges.py,
-tests/pytests/test_mlset_integration.py).  The reference cannot run here (it
+tests/pytests/test_mlset_integration.py, tests/pytests/test_bndcut.py).  The reference cannot run here (it
 needs NGSolve), so these closed forms are the golden vectors the oracle is
 pinned against.  Run: python tests/golden/make_known_answers.py
 """
@@ -64,6 +64,10 @@ out = {
         "edge": 1.0, "edges": 12.0,
         "corners_x_plus_y_plus_z": {"ppp": 1.5, "ppn": 0.5, "pnp": 0.5, "npp": 0.5, "pnn": -0.5, "npn": -0.5,
                                     "nnp": -0.5, "nnn": -1.5}, "tol": 1e-12},
+    # boundary cut integrals (tests/pytests/test_bndcut.py), lset x - cut on the unit square / cube
+    "bnd2d": {"cuts": [0.3, 0.5, 0.7], "NEG": "2 cut + 1", "IF_points": 2.0,
+              "if_x_at_half": 1.0, "if_y_at_half": 1.0, "perimeter": 4.0, "tol": 1e-10},
+    "bnd3d": {"cut": 0.3, "NEG": 1.0 + 4.0 * 0.3, "tol": 1e-10},
 }
 path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "known_answers.json")
 with open(path, "w") as f:

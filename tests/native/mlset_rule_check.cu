@@ -6,6 +6,8 @@
 // triangles and tetrahedra, 1..5 random linear level sets, level sets through
 // element vertices, random unions of domain tuples with NEG / POS / IF
 // entries (codimension 0..3), orders 0..5.
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <random>
@@ -14,6 +16,8 @@
 #include "xg_mlset.cuh"
 
 extern "C" int orc_base_rule(int d, int p, double* pts, double* wts, int maxpts);
+extern "C" double orc_bnd_element_integral(int D, const double* xv, const double* l, int dt, int order, int ex,
+                                           int ey, int ez, int* status);
 extern "C" int orc_mlset_cut_rule(int D, const double* elc, int M, const double* lsets, int ntup, const int* dts,
                                   int order, double* pts, double* wts, int maxpts);
 
@@ -113,11 +117,48 @@ static void run(std::mt19937_64& rng, int ncase) {
   }
 }
 
+// boundary elements: the share of random segments in 2D and triangles in 3D
+template <int D>
+static void run_bnd(std::mt19937_64& rng, int ncase) {
+  std::normal_distribution<double> nd(0.0, 1.0);
+  std::uniform_int_distribution<int> udt(0, 2), uord(0, 5), uex(0, 2);
+  for (int t = 0; t < ncase; t++) {
+    double xv[3][3] = {}, l[3];
+    for (int v = 0; v < D; v++) {
+      for (int i = 0; i < D; i++) xv[v][i] = nd(rng);
+      l[v] = nd(rng);
+    }
+    const int dt = udt(rng), order = uord(rng), ex = uex(rng), ey = uex(rng), ez = uex(rng);
+    double got = 0.0;
+    auto emit = [&](const double* x, double w, double meas) {
+      double fv = 1.0;
+      for (int k = 0; k < ex; k++) fv *= x[0];
+      double fy = 1.0;
+      for (int k = 0; k < ey; k++) fy *= x[1];
+      double fz = 1.0;
+      if (D == 3)
+        for (int k = 0; k < ez; k++) fz *= x[2];
+      got += w * meas * (fv * fy * fz);
+    };
+    const int st = xg::ml::bnd_rule<D>(&xg::g_tab, xv, l, dt, order, emit);
+    int ost = 0;
+    const double ref = orc_bnd_element_integral(D, &xv[0][0], l, dt, order, ex, ey, ez, &ost);
+    g_cases++;
+    const bool ok = st == ost && (st || std::fabs(got - ref) <= 1e-13 * std::max(1.0, std::fabs(ref)));
+    if (!ok) {
+      if (g_fail < 10) std::printf("BND MISMATCH D=%d dt=%d order=%d: %g vs %g (status %d/%d)\n", D, dt, order, got, ref, st, ost);
+      g_fail++;
+    }
+  }
+}
+
 int main() {
   fill_table();
   std::mt19937_64 rng(20261204);
   run<2>(rng, 20000);
   run<3>(rng, 20000);
+  run_bnd<2>(rng, 5000);
+  run_bnd<3>(rng, 5000);
   std::printf("%d cases, %d points, %d no-rule, %d error statuses, %d mismatches\n", g_cases, g_points, g_norule,
               g_errors, g_fail);
   return g_fail ? 1 : 0;
