@@ -265,3 +265,17 @@ def test_spacetime_moving_circle(orc):
     h = 1 / 32
     assert abs(sp.integrate_st(lst, 2, orc.NEG, 2, 4) - math.pi * 0.0625) < 2 * h * h
     assert abs(sp.integrate_st(lst, 2, orc.IF, 2, 4) - 2 * math.pi * 0.25) < 2 * h * h
+
+
+def test_single_cut_triangle_all_orders(orc):
+    """tests/pytests/test_localgeom.py: the triangle (0,0),(1,0),(0,1) cut by
+    x + y - 1/4 has NEG measure 1/32 and POS measure 1/2 - 1/32 at every rule
+    order 0..15, within 5e-16 (p+1)^2."""
+    from ngsxfem_gb300.meshes import Mesh
+    m = Mesh(np.array([[0.0, 0.0], [1.0, 0.0], [0.0, 1.0]]), np.array([[0, 1, 2]]))
+    sp = orc.Space(m, 1)
+    l = orc.interpolate_p1_perturb(m.coords[:, 0] + m.coords[:, 1] - 0.25)
+    for order in range(16):
+        neg, pos = sp.integrate(l, orc.NEG, order), sp.integrate(l, orc.POS, order)
+        tol = 5e-16 * (order + 1) ** 2
+        assert abs(neg - 1 / 32) < tol and abs(pos - (0.5 - 1 / 32)) < tol and abs(neg + pos - 0.5) < tol
