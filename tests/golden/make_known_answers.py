@@ -64,6 +64,8 @@ out = {
         "edge": 1.0, "edges": 12.0,
         "corners_x_plus_y_plus_z": {"ppp": 1.5, "ppn": 0.5, "pnp": 0.5, "npp": 0.5, "pnn": -0.5, "npn": -0.5,
                                     "nnp": -0.5, "nnn": -1.5}, "tol": 1e-12},
+    "mlset3d_lines": {  # test_mlset_integration.py:398-470, lines (codimension 2) in [-0.8,0.8]^3
+        "line": math.sqrt(2), "cross": 2 * math.sqrt(3), "lines": 1.9 * math.sqrt(3), "tol": 1e-12},
     # boundary cut integrals (tests/pytests/test_bndcut.py), lset x - cut on the unit square / cube
     "bnd2d": {"cuts": [0.3, 0.5, 0.7], "NEG": "2 cut + 1", "IF_points": 2.0,
               "if_x_at_half": 1.0, "if_y_at_half": 1.0, "perimeter": 4.0, "tol": 1e-10},

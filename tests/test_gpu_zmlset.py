@@ -156,3 +156,15 @@ def test_multilevelset_cutinfo(xg, orc):
         ci.GetElementsOfType((xg.NEG, xg.NEG, xg.NEG))
     with pytest.raises(TypeError):
         MultiLevelsetCutInfo(m2, (1.0, 2.0))
+
+
+def test_3d_line_lengths(xg, orc):
+    """Lines (codimension 2) of test_mlset_integration.py::test_3d_codim2_cross."""
+    from ngsxfem_gb300.mlset import DomainTypeArray
+    ref = KA["mlset3d_lines"]
+    m = MakeStructured3DMesh(5, 6, 7, box=((-0.8, 0.8),) * 3)
+    N, P, I, A = xg.NEG, xg.POS, xg.IF, xg.ANY
+    X, Y, Z = m.coords.T
+    G = gfs(xg, m, [orc.interpolate_p1_perturb(f) for f in (X - .5, -X - .5, Z - Y, X - Z, X + Z)])
+    cross = DomainTypeArray([(N, N, I, I, A), (N, N, I, A, I)])
+    assert abs(integ(xg, m, G, cross) - ref["cross"]) < ref["tol"]

@@ -192,3 +192,25 @@ def test_marker_relations(orc):
     for t in cube.Boundary().as_list:
         sides |= orc.mlset_mark(m3, L3, [t], 1)
     assert (sides == if3).all()
+
+
+def lines_cases():
+    """The three line regions of test_mlset_integration.py::test_3d_codim2_cross
+    as (level-set functions, region tuples, key); on meshes with different x
+    and y grids (an equal grid puts mesh faces on the plane x = y)."""
+    return [
+        (lambda X, Y, Z: (X - .5, X + .5, X - Y, Z), [(NEG, POS, IF, IF)], "line"),
+        (lambda X, Y, Z: (X - .5, -X - .5, Z - Y, X - Z, X + Z), [(NEG, NEG, IF, IF, ANY), (NEG, NEG, IF, ANY, IF)],
+         "cross"),
+        (lambda X, Y, Z: (X - .5, -X - .5, -Z - .5, Z + Y, X + Y, Z + Y + .1),
+         [(NEG, NEG, NEG, IF, IF, ANY), (NEG, NEG, NEG, ANY, IF, IF)], "lines"),
+    ]
+
+
+def test_3d_line_lengths(orc):
+    ref = KA["mlset3d_lines"]
+    for dims in ((5, 6, 7), (7, 9, 11)):
+        m = MakeStructured3DMesh(*dims, box=((-0.8, 0.8),) * 3)
+        for fs, tuples, key in lines_cases():
+            L = np.array([orc.interpolate_p1_perturb(f) for f in fs(*m.coords.T)])
+            assert abs(integ(orc, m, L, DomainTypeArray(tuples)) - ref[key]) < ref["tol"], (dims, key)
