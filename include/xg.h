@@ -247,9 +247,11 @@ int xg_mlset_mark(xg_mesh* mesh, const double* d_lsets, int32_t nlsets, const in
  * elements of a simplex mesh (the boundary facets; cutint/straightcutrule.cpp:
  * 582-677): NEG / POS parts of the boundary, and for dt = XG_IF in 2D the
  * intersection points of the interface with the boundary, each counting 1
- * (the point measure of :641-651).  XG_IF in 3D: XG_ERR_UNSUPPORTED. */
+ * (the point measure of :641-651).  XG_IF in 3D: XG_ERR_UNSUPPORTED.
+ * d_defined_on (optional): bitset over the BND elements (xg_mesh_boundary
+ * order), the definedon / definedonelements restriction of dCut. */
 int xg_integrate_bnd(xg_mesh* mesh, const double* d_lset, int dt, int order, int ex, int ey, int ez,
-                     double* d_result, void* stream);
+                     const uint64_t* d_defined_on, double* d_result, void* stream);
 /* A sufficient max_pts for xg_cut_rules_mlset, or -1 for bad arguments. */
 int xg_mlset_rule_capacity(int dim, int32_t nlsets, int32_t ndomains, int order);
 /* Mesh-level isoparametric integration of a P2 level set (LevelSetMeshAdaptation

@@ -134,7 +134,7 @@ def load():
         "xg_mlset_rule_capacity": (I, [I, ctypes.c_int32, ctypes.c_int32, I]),
         "xg_mlset_mark": (I, [P, P, ctypes.c_int32, P, ctypes.c_int32, I, P, P]),
         "xg_iso_integrate_mesh": (I, [P, P, I, I, ctypes.c_double, I, I, I, I, P, P, P]),
-        "xg_integrate_bnd": (I, [P, P, I, I, I, I, I, P, P]),
+        "xg_integrate_bnd": (I, [P, P, I, I, I, I, I, P, P, P]),
         "xg_integrate_noalloc": (I, [P, P, I, I, I, I, I, P, P, P]),
         "xg_form_create": (I, [P, P, ctypes.c_int32, I, P]),
         "xg_form_destroy": (I, [P]),

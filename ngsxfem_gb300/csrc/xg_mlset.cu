@@ -182,10 +182,13 @@ template <int D>
 __global__ void __launch_bounds__(kMlThreads) k_integrate_bnd(int64_t nbnd, const int32_t* __restrict__ bnd_v,
                                                               const double* __restrict__ xyz, int nv,
                                                               const double* __restrict__ lset, int dt, int order,
-                                                              int ex, int ey, int ez, double* block_sums, int* err) {
+                                                              int ex, int ey, int ez,
+                                                              const uint64_t* __restrict__ defined_on,
+                                                              double* block_sums, int* err) {
   __shared__ double red[kMlThreads];
   double acc = 0.0;
   for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < nbnd; b += (int64_t)gridDim.x * blockDim.x) {
+    if (defined_on && !tbit_ml(defined_on, b)) continue;
     double xv[D][3], l[D];
     for (int v = 0; v < D; v++) {
       const int vid = bnd_v[(int64_t)v * nbnd + b];
@@ -324,8 +327,8 @@ int xg_mlset_mark(xg_mesh* m, const double* d_lsets, int32_t nlsets, const int8_
   return mlset_mark(m, d_lsets, md, mode, d_bits, stream);
 }
 
-int xg_integrate_bnd(xg_mesh* m, const double* d_lset, int dt, int order, int ex, int ey, int ez, double* d_result,
-                     void* stream) {
+int xg_integrate_bnd(xg_mesh* m, const double* d_lset, int dt, int order, int ex, int ey, int ez,
+                     const uint64_t* d_defined_on, double* d_result, void* stream) {
   if (int st = mlset_mesh_ok(m, "xg_integrate_bnd")) return st;
   if (!d_lset || !d_result || dt < 0 || dt > 2 || order < 0 || order > kMaxOrder || ex < 0 || ey < 0 || ez < 0)
     return XG_ERR_ARG;
@@ -349,10 +352,10 @@ int xg_integrate_bnd(xg_mesh* m, const double* d_lset, int dt, int order, int ex
   }
   if (m->dim == 2)
     k_integrate_bnd<2><<<kMlBlocks, kMlThreads, 0, s>>>(m->nbnd, m->d_bnd_v, m->d_xyz, m->nv, d_lset, dt, order, ex,
-                                                       ey, ez, bs, m->d_err);
+                                                       ey, ez, d_defined_on, bs, m->d_err);
   else
     k_integrate_bnd<3><<<kMlBlocks, kMlThreads, 0, s>>>(m->nbnd, m->d_bnd_v, m->d_xyz, m->nv, d_lset, dt, order, ex,
-                                                       ey, ez, bs, m->d_err);
+                                                       ey, ez, d_defined_on, bs, m->d_err);
   k_mlset_final<<<1, 32, 0, s>>>(bs, kMlBlocks, d_result);
   return launch_check_ml("k_integrate_bnd");
 }

@@ -54,6 +54,61 @@ class Mesh:
     def GetNV(self):
         return self.nv
 
+    def boundary_elements(self):
+        """The BND elements of a simplex mesh: the facets that belong to one
+        element, each with its vertices ascending, in lexicographic order of
+        those vertex tuples (the order libxg numbers its facets and BND
+        elements in).  int32 array (nbnd, dim)."""
+        if self.tensor:
+            raise NotImplementedError("boundary elements of quadrilateral / hexahedral meshes")
+        if getattr(self, "_bnd", None) is None:
+            d = self.dim
+            f = np.concatenate([np.delete(self.elements, s, axis=1) for s in range(d + 1)])
+            f = np.sort(f, axis=1)
+            u, cnt = np.unique(f, axis=0, return_counts=True)
+            self._bnd = np.ascontiguousarray(u[cnt == 1], dtype=np.int32)
+        return self._bnd
+
+    def Boundaries(self, pattern):
+        """Region of the BND elements on the named sides of the mesh's bounding
+        box (a regular expression over the names, as NGSolve's
+        mesh.Boundaries): in 2D bottom (y = ymin), right (x = xmax), top
+        (y = ymax), left (x = xmin); in 3D left / right (x), front / back (y),
+        bottom / top (z), the names of netgen's unit_square and unit_cube.  A
+        BND element is on a side if all its vertices are."""
+        import re
+        names = (("left", 0, 0), ("right", 0, 1), ("bottom", 1, 0), ("top", 1, 1)) if self.dim == 2 else (
+            ("left", 0, 0), ("right", 0, 1), ("front", 1, 0), ("back", 1, 1), ("bottom", 2, 0), ("top", 2, 1))
+        bnd = self.boundary_elements()
+        lo, hi = self.coords.min(axis=0), self.coords.max(axis=0)
+        rx = re.compile(pattern)
+        mask = np.zeros(len(bnd), dtype=bool)
+        for name, axis, side in names:
+            if rx.fullmatch(name):
+                val = hi[axis] if side else lo[axis]
+                mask |= np.all(self.coords[bnd, axis] == val, axis=1)
+        return Region(self, mask)
+
+
+class Region:
+    """A set of BND elements of a mesh (mesh.Boundaries(...)): a boolean mask in
+    the order of Mesh.boundary_elements."""
+
+    def __init__(self, mesh, mask):
+        self.mesh, self.mask = mesh, np.asarray(mask, dtype=bool)
+
+    def Mask(self):
+        return self.mask
+
+    def __or__(self, o):
+        return Region(self.mesh, self.mask | o.mask)
+
+    def __and__(self, o):
+        return Region(self.mesh, self.mask & o.mask)
+
+    def __invert__(self):
+        return Region(self.mesh, ~self.mask)
+
 
 def MakeStructured2DMesh(nx=10, ny=10, xmin=0.0, xmax=1.0, ymin=0.0, ymax=1.0, quads=False):
     xs = np.linspace(xmin, xmax, nx + 1)

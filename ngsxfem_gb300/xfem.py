@@ -564,9 +564,12 @@ class _Measure:
         self.kind, self.levelset, self.domain_type, self.order = kind, levelset, domain_type, order
         self.definedonelements = definedonelements
         self.scale = 1.0
-        for k in ("deformation", "skeleton", "element_boundary", "element_vb", "definedon"):
+        for k in ("deformation", "skeleton", "element_boundary", "element_vb"):
             if kw.get(k) is not None and kw.get(k) is not False:
                 raise NotImplementedError("dCut/dFacetPatch option %r is not part of the GPU path" % k)
+        self.definedon = kw.get("definedon")
+        if self.definedon is not None and (kind != "cut" or kw.get("vb", VOL) != BND):
+            raise NotImplementedError("definedon (a region of BND elements) applies to dCut(..., vb=BND)")
         if kw.get("subdivlvl") not in (None, 0):
             raise NotImplementedError("subdivision rules are not part of dCut on the GPU path")
         t = kw.get("time_order", -1)
@@ -1012,9 +1015,8 @@ def Integrate(levelset_domain=None, cf=None, mesh=None, order=5, integrand=None)
     else:
         vb = levelset_domain.get("vb", VOL)
     if vb == BND:
-        if defined is not None:
-            raise NotImplementedError("definedonelements on boundary cut integrals")
-        return _integrate_bnd(lset, dt, order, mono, mesh)
+        region = getattr(meas, "definedon", None) if integrand is not None else levelset_domain.get("definedon")
+        return _integrate_bnd(lset, dt, order, mono, mesh, defined, region)
     if isinstance(lset, (tuple, list)):
         return _integrate_mlset(lset, dt, order, mono, defined, mesh)
     mesh = mesh if mesh is not None else lset.space.mesh
@@ -1033,13 +1035,25 @@ def _unscaled(meas):
     return out
 
 
-def _integrate_bnd(lset, dt, order, mono, mesh):
-    """Integrate(f * dCut(lset, dt, vb=BND)): xg_integrate_bnd."""
+def _integrate_bnd(lset, dt, order, mono, mesh, defined=None, region=None):
+    """Integrate(f * dCut(lset, dt, vb=BND[, definedon=mesh.Boundaries(..)]
+    [, definedonelements=BND BitArray])): xg_integrate_bnd; the two
+    restrictions intersect."""
     mesh = mesh if mesh is not None else lset.space.mesh
     dm = device_mesh(mesh)
+    nb = np.zeros(1, dtype=np.int64)
+    _lib.call("xg_mesh_boundary", dm.h, nb.ctypes.data_as(ctypes.c_void_p), None)
+    nbnd = int(nb[0])
+    if region is not None:
+        if region.mesh is not mesh or len(region.mask) != nbnd:
+            raise ValueError("definedon: a region of this mesh's BND elements (mesh.Boundaries)")
+        r = BitArray.from_numpy(region.mask)
+        defined = r if defined is None else defined & r
+    if defined is not None and len(defined) != nbnd:
+        raise ValueError("definedonelements on vb=BND: a BitArray over the %d BND elements" % nbnd)
     res = torch.zeros(1, dtype=torch.float64, device=_dev())
-    _lib.call("xg_integrate_bnd", dm.h, _vp(_lset_vec(lset)), dt, order, mono.e[0], mono.e[1], mono.e[2], _vp(res),
-              _stream())
+    _lib.call("xg_integrate_bnd", dm.h, _vp(_lset_vec(lset)), dt, order, mono.e[0], mono.e[1], mono.e[2],
+              _vp(defined.words) if defined is not None else None, _vp(res), _stream())
     dm.check()
     return float(res.item())
 

@@ -118,7 +118,7 @@ def lib():
         L.orc_mlset_integrate.argtypes = [I, I, P, I, P, I, P, I, P, I, I, I, I, P]
         L.orc_mlset_mark.argtypes = [I, I, P, I, P, I, P, I, P, I, P]
         L.orc_integrate_bnd.restype = ctypes.c_double
-        L.orc_integrate_bnd.argtypes = [I, I, P, I, P, P, I, I, I, I, I, P]
+        L.orc_integrate_bnd.argtypes = [I, I, P, I, P, P, I, I, I, I, I, P, P]
         _lib = L
     return _lib
 
@@ -272,14 +272,17 @@ def mlset_mark(mesh, lsets, dts, mode):
     return np.unpackbits(bits.view(np.uint8), bitorder="little")[: el.shape[0]].astype(bool)
 
 
-def integrate_bnd(mesh, lset, dt, order, exps=(0, 0, 0)):
-    """Integrate(x^a y^b z^c * dCut(lset, dt, vb=BND)); returns (value, status)."""
+def integrate_bnd(mesh, lset, dt, order, exps=(0, 0, 0), defined_on=None):
+    """Integrate(x^a y^b z^c * dCut(lset, dt, vb=BND)); defined_on: optional
+    boolean mask over the BND elements (boundary facets in lexicographic order
+    of their sorted vertices).  Returns (value, status)."""
     c = np.ascontiguousarray(mesh.coords, dtype=np.float64)
     el = np.ascontiguousarray(mesh.elements, dtype=np.int32)
     l = np.ascontiguousarray(lset, dtype=np.float64)
     st = np.zeros(1, dtype=np.int32)
+    mask = None if defined_on is None else np.ascontiguousarray(defined_on, dtype=np.uint8)
     v = lib().orc_integrate_bnd(c.shape[1], c.shape[0], _p(c), el.shape[0], _p(el), _p(l), dt, order, exps[0],
-                                exps[1], exps[2], _p(st))
+                                exps[1], exps[2], None if mask is None else _p(mask), _p(st))
     return v, int(st[0])
 
 

@@ -210,7 +210,7 @@ int orc_mlset_mark(int D, int nv, const double* coords, int ne, const int32_t* e
  * a simplex mesh (elements' facets that belong to one element); IF on 2D
  * boundary segments is the point measure (each intersection point counts 1). */
 double orc_integrate_bnd(int D, int nv, const double* coords, int ne, const int32_t* elv, const double* lset, int dt,
-                         int order, int ex, int ey, int ez, int* status);
+                         int order, int ex, int ey, int ez, const uint8_t* defined_on, int* status);
 /* The share of one boundary element (vertices xv[D][3], values l[D]). */
 double orc_bnd_element_integral(int D, const double* xv, const double* l, int dt, int order, int ex, int ey, int ez,
                                 int* status);

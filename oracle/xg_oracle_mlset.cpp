@@ -560,7 +560,8 @@ extern "C" double orc_bnd_element_integral(int D, const double* xv, const double
 }
 
 extern "C" double orc_integrate_bnd(int D, int nv, const double* coords, int ne, const int32_t* elv,
-                                    const double* lset, int dt, int order, int ex, int ey, int ez, int* status) {
+                                    const double* lset, int dt, int order, int ex, int ey, int ez,
+                                    const uint8_t* defined_on, int* status) {
   (void)nv;
   if (status) *status = 0;
   // facets (sorted vertex triples / pairs) and their element counts
@@ -575,10 +576,11 @@ extern "C" double orc_integrate_bnd(int D, int nv, const double* coords, int ne,
     }
   std::sort(facets.begin(), facets.end());
   double sum = 0;
+  int64_t b = 0;  // BND element number: boundary facets in lexicographic order
   for (size_t i = 0; i < facets.size();) {
     size_t j = i;
     while (j < facets.size() && facets[j] == facets[i]) j++;
-    if (j - i == 1) {
+    if (j - i == 1 && (!defined_on || defined_on[b])) {
       double xv[3][3] = {}, l[3];
       for (int v = 0; v < D; v++) {
         const int id = facets[i][v];
@@ -591,6 +593,7 @@ extern "C" double orc_integrate_bnd(int D, int nv, const double* coords, int ne,
         if (status && *status == 0) *status = err.code;
       }
     }
+    if (j - i == 1) b++;
     i = j;
   }
   return sum;

@@ -70,6 +70,10 @@ out = {
     "bnd2d": {"cuts": [0.3, 0.5, 0.7], "NEG": "2 cut + 1", "IF_points": 2.0,
               "if_x_at_half": 1.0, "if_y_at_half": 1.0, "perimeter": 4.0, "tol": 1e-10},
     "bnd3d": {"cut": 0.3, "NEG": 1.0 + 4.0 * 0.3, "tol": 1e-10},
+    # definedon=mesh.Boundaries(side) (test_bndcut.py:51-59, 203-217): NEG on the bottom side = cut;
+    # interface points on the bottom side at cut 0.5: 1, on the left side: 0
+    "bnd2d_definedon": {"cuts": [0.3, 0.7], "bottom_NEG": "cut", "bottom_IF_at_half": 1.0,
+                        "left_IF_at_half": 0.0, "tol": 1e-10},
 }
 path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "known_answers.json")
 with open(path, "w") as f:

@@ -39,3 +39,39 @@ def test_boundary_measures_3d(orc):
     assert st == 0 and abs(neg - ref["NEG"]) < ref["tol"]
     # the interface on boundary triangles (codimension 2) is not supported
     assert orc.integrate_bnd(m, l, orc.IF, 2)[1] == 6
+
+
+def test_boundary_regions_2d(orc):
+    """definedon=mesh.Boundaries(side): the oracle restricted to the BND
+    elements of one side of the square (test_bndcut.py:51-59, 203-217)."""
+    ref = KA["bnd2d_definedon"]
+    m = MakeStructured2DMesh(9, 9)
+    bottom, left = m.Boundaries("bottom").Mask(), m.Boundaries("left").Mask()
+    assert bottom.sum() == 9 and left.sum() == 9 and m.Boundaries("bottom|top|left|right").Mask().all()
+    for cut in ref["cuts"]:
+        l = orc.interpolate_p1_perturb(m.coords[:, 0] - cut)
+        assert abs(orc.integrate_bnd(m, l, orc.NEG, 2, defined_on=bottom)[0] - cut) < ref["tol"]
+    l = orc.interpolate_p1_perturb(m.coords[:, 0] - 0.5)
+    assert abs(orc.integrate_bnd(m, l, orc.IF, 0, defined_on=bottom)[0] - ref["bottom_IF_at_half"]) < ref["tol"]
+    assert abs(orc.integrate_bnd(m, l, orc.IF, 0, defined_on=left)[0] - ref["left_IF_at_half"]) < ref["tol"]
+    # an all-true mask equals no restriction; the sides add up to the whole boundary
+    full = orc.integrate_bnd(m, l, orc.NEG, 2)[0]
+    assert orc.integrate_bnd(m, l, orc.NEG, 2, defined_on=np.ones(len(bottom), bool))[0] == full
+    sides = sum(orc.integrate_bnd(m, l, orc.NEG, 2, defined_on=m.Boundaries(s).Mask())[0]
+                for s in ("bottom", "right", "top", "left"))
+    assert abs(sides - full) < 1e-14
+
+
+def test_boundary_elements_order():
+    """Mesh.boundary_elements: the facets of one element, vertices ascending,
+    lexicographic (the BND element order of libxg and of the oracle)."""
+    m = MakeStructured3DMesh(3)
+    b = m.boundary_elements()
+    assert len(b) == 6 * 2 * 3 * 3 and (np.diff(b, axis=1) > 0).all()
+    keys = [tuple(r) for r in b]
+    assert keys == sorted(keys)
+    sides = ["left", "right", "front", "back", "bottom", "top"]
+    masks = np.array([m.Boundaries(s).Mask() for s in sides])
+    assert (masks.sum(axis=0) == 1).all() and (masks.sum(axis=1) == 18).all()
+    x = m.coords[b]
+    assert np.all(x[masks[2]][..., 1] == 0.0) and np.all(x[masks[5]][..., 2] == 1.0)
