@@ -323,8 +323,12 @@ int xg_form_stage_events(xg_form* form, void* const* events, int n);
 
 /* ---- linear forms (xfem/symboliccutlfi.cpp) --------------------------------- */
 typedef enum {
-  XG_LTERM_SOURCE = 0,    /* coef * x^e0 y^e1 z^e2 * v                         */
-  XG_LTERM_SOURCE_GF = 1  /* coef * u_h * v, u_h = d_gf (dof vector, same space) */
+  XG_LTERM_SOURCE = 0,     /* coef * x^e0 y^e1 z^e2 * v                         */
+  XG_LTERM_SOURCE_GF = 1,  /* coef * u_h * v, u_h = d_gf (dof vector, same space) */
+  XG_LTERM_SOURCE_BND = 2  /* coef * x^e0 y^e1 z^e2 * v * dCut(lset, domain, vb=BND): the
+                              domain part of the BND elements (xg_integrate_bnd's rule, the
+                              trace of the owning element's basis); d_defined_on: bits over
+                              the BND elements; XG_IF in 2D only */
 } xg_lterm_kind;
 /* One SymbolicCutLFI(cf * v * dCut(lset, domain, order, definedonelements)). */
 typedef struct {

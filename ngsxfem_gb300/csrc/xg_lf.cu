@@ -10,6 +10,12 @@
 // the default order is 2k (symboliccutlfi.cpp:93-94).  Then thread per dof:
 // the sum over the dof's (element, local) adjacency in ascending element
 // order -- a fixed order, no atomics.
+//
+// Boundary terms (dCut(lset, dt, vb=BND)): thread per BND element, the
+// boundary rule of xg_mlset.cuh, the owning element's basis at the rule's
+// physical points (reference coordinates by F^-1); then thread per dof, the
+// sum over its (BND element, local) adjacency in ascending order, added to
+// the volume part.
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -17,13 +23,16 @@
 #include "xg_basis.cuh"
 #include "xg_cut.cuh"
 #include "xg_internal.h"
+#include "xg_mlset.cuh"
 
 namespace xg {
 
 static __constant__ RuleTable c_rules;
+static __device__ RuleTable g_lfb_rules;  // the boundary rule code reads its table by pointer
 
 int upload_rules_lf() {
   XG_CUDA(cudaMemcpyToSymbol(c_rules, &host_rules(), sizeof(RuleTable)));
+  XG_CUDA(cudaMemcpyToSymbol(g_lfb_rules, &host_rules(), sizeof(RuleTable)));
   return XG_OK;
 }
 
@@ -74,6 +83,7 @@ __global__ void __launch_bounds__(128) k_lf_elvec(int ne, int nv, const int32_t*
     for (int i = 0; i < N; i++) desc[i] = fn_desc<D, K>(i, gv);
     for (int t = 0; t < d.n; t++) {
       const xg_lterm& T = d.t[t];
+      if (T.kind == XG_LTERM_SOURCE_BND) continue;
       if (T.d_defined_on && !tbit64(T.d_defined_on, e)) continue;
       const int dt = T.domain;
       const int p = clamp_order(T.order >= 0 ? T.order : 2 * K);
@@ -146,6 +156,86 @@ __global__ void __launch_bounds__(128) k_lf_elvec(int ne, int nv, const int32_t*
   }
 }
 
+// boundary terms: bvec[b][i] for BND element b (vertices bnd_v, owner bnd_el[b])
+template <int D, int K>
+__global__ void __launch_bounds__(128) k_lf_bnd(int64_t nbnd, const int32_t* __restrict__ bnd_v,
+                                                 const int32_t* __restrict__ bnd_el, int ne, int nv,
+                                                 const int32_t* __restrict__ elv, const double* __restrict__ xyz,
+                                                 const double* __restrict__ lset, LfDesc d,
+                                                 double* __restrict__ bvec, int* err) {
+  constexpr int N = ndof_el(D, K);
+  for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < nbnd; b += (int64_t)gridDim.x * blockDim.x) {
+    double acc[N];
+#pragma unroll
+    for (int i = 0; i < N; i++) acc[i] = 0.0;
+    const int e = bnd_el[b];
+    double xv[D + 1][3];
+    int gv[4];
+#pragma unroll
+    for (int v = 0; v <= D; v++) {
+      const int vid = elv[(int64_t)v * ne + e];
+      gv[v] = vid;
+#pragma unroll
+      for (int c = 0; c < 3; c++) xv[v][c] = c < D ? xyz[(int64_t)c * nv + vid] : 0.0;
+    }
+    Geo<D> g;
+    make_geo<D>(xv, g);
+    int desc[N];
+#pragma unroll
+    for (int i = 0; i < N; i++) desc[i] = fn_desc<D, K>(i, gv);
+    double xb[D][3], lb[D];
+#pragma unroll
+    for (int v = 0; v < D; v++) {
+      const int vid = bnd_v[(int64_t)v * nbnd + b];
+      lb[v] = lset[vid];
+#pragma unroll
+      for (int c = 0; c < 3; c++) xb[v][c] = c < D ? xyz[(int64_t)c * nv + vid] : 0.0;
+    }
+    for (int t = 0; t < d.n; t++) {
+      const xg_lterm& T = d.t[t];
+      if (T.kind != XG_LTERM_SOURCE_BND || (T.d_defined_on && !tbit64(T.d_defined_on, b))) continue;
+      const int p = clamp_order(T.order >= 0 ? T.order : 2 * K);
+      auto emit = [&](const double* x, double w, double meas) {
+        double lam[D + 1], sl = 0.0;
+#pragma unroll
+        for (int k = 0; k < D; k++) {
+          double s = 0.0;
+#pragma unroll
+          for (int c = 0; c < D; c++) s += g.Finv[k][c] * (x[c] - g.x0[c]);
+          lam[k] = s;
+          sl += s;
+        }
+        lam[D] = 1.0 - sl;
+        const double gv2 = T.coef * ipow(x[0], T.e[0]) * ipow(x[1], T.e[1]) * (D == 3 ? ipow(x[2], T.e[2]) : 1.0);
+        const double wq = w * meas * gv2;
+#pragma unroll
+        for (int i = 0; i < N; i++) acc[i] += wq * eval_fn_value<D, double>(desc[i], lam);
+      };
+      const int st = ml::bnd_rule<D>(&g_lfb_rules, xb, lb, T.domain, p, emit);
+      if (st) set_err(err, st);
+    }
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+      if (!isfinite(acc[i])) set_err(err, XG_ERR_NONFINITE);
+      bvec[b * N + i] = acc[i];
+    }
+  }
+}
+
+// out[r] += the boundary contributions of dof r, BND elements ascending
+__global__ void k_lf_gather_bnd(int64_t ndof, int nd, const int32_t* __restrict__ adj_ptr,
+                                const int32_t* __restrict__ adj, const double* __restrict__ bvec,
+                                double* __restrict__ out) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < ndof; r += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int a = adj_ptr[r]; a < adj_ptr[r + 1]; a++) {
+      const int v = adj[a];
+      s += bvec[(int64_t)(v >> 5) * nd + (v & 31)];
+    }
+    out[r] += s;
+  }
+}
+
 __global__ void k_lf_gather(int64_t ndof, int nd, const int32_t* __restrict__ adj_ptr, const int32_t* __restrict__ adj,
                             const double* __restrict__ elvec, double* __restrict__ out) {
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < ndof; r += (int64_t)gridDim.x * blockDim.x) {
@@ -168,7 +258,49 @@ struct xg_lform {
   LfDesc desc;
   double* d_elvec = nullptr;
   int* d_err = nullptr;
+  // boundary terms: owner element per BND element, their vectors, and the
+  // dof -> (BND element * 32 + local) adjacency, BND elements ascending
+  bool has_bnd = false;
+  int32_t* d_bnd_el = nullptr;
+  double* d_bvec = nullptr;
+  int32_t* d_badj_ptr = nullptr;
+  int32_t* d_badj = nullptr;
 };
+
+static void lform_free(xg_lform* f) {
+  cudaFree(f->d_elvec);
+  cudaFree(f->d_err);
+  cudaFree(f->d_bnd_el);
+  cudaFree(f->d_bvec);
+  cudaFree(f->d_badj_ptr);
+  cudaFree(f->d_badj);
+  delete f;
+}
+
+static int lform_bnd_setup(xg_lform* f) {
+  const xg_space* sp = f->space;
+  const xg_mesh* m = sp->mesh;
+  const int64_t nbnd = m->nbnd;
+  if (nbnd >= (1 << 26)) return XG_ERR_CAPACITY;
+  const int nd = sp->nd;
+  std::vector<int32_t> owner((size_t)std::max<int64_t>(nbnd, 1), 0), ptr((size_t)sp->ndof + 1, 0);
+  for (int64_t b = 0; b < nbnd; b++) {
+    owner[b] = m->h_facet_els[2 * (size_t)m->h_bnd_facets[b]];
+    for (int i = 0; i < nd; i++) ptr[(size_t)sp->h_el_dofs[(size_t)owner[b] * nd + i] + 1]++;
+  }
+  for (int64_t r = 0; r < sp->ndof; r++) ptr[r + 1] += ptr[r];
+  std::vector<int32_t> fill(ptr.begin(), ptr.end() - 1), adj((size_t)std::max<int32_t>(ptr.back(), 1), 0);
+  for (int64_t b = 0; b < nbnd; b++)
+    for (int i = 0; i < nd; i++) adj[fill[sp->h_el_dofs[(size_t)owner[b] * nd + i]]++] = (int32_t)(b * 32 + i);
+  XG_CUDA(cudaMalloc((void**)&f->d_bnd_el, sizeof(int32_t) * owner.size()));
+  XG_CUDA(cudaMalloc((void**)&f->d_bvec, sizeof(double) * (size_t)std::max<int64_t>(nbnd, 1) * nd));
+  XG_CUDA(cudaMalloc((void**)&f->d_badj_ptr, sizeof(int32_t) * ptr.size()));
+  XG_CUDA(cudaMalloc((void**)&f->d_badj, sizeof(int32_t) * adj.size()));
+  XG_CUDA(cudaMemcpy(f->d_bnd_el, owner.data(), sizeof(int32_t) * owner.size(), cudaMemcpyHostToDevice));
+  XG_CUDA(cudaMemcpy(f->d_badj_ptr, ptr.data(), sizeof(int32_t) * ptr.size(), cudaMemcpyHostToDevice));
+  XG_CUDA(cudaMemcpy(f->d_badj, adj.data(), sizeof(int32_t) * adj.size(), cudaMemcpyHostToDevice));
+  return XG_OK;
+}
 
 extern "C" {
 
@@ -179,7 +311,12 @@ int xg_lform_create(xg_space* space, const xg_lterm* terms, int32_t n, xg_lform*
   }
   for (int t = 0; t < n; t++) {
     const xg_lterm& T = terms[t];
-    if ((T.kind != XG_LTERM_SOURCE && T.kind != XG_LTERM_SOURCE_GF) || T.domain < 0 || T.domain > 2 ||
+    if (T.kind == XG_LTERM_SOURCE_BND && T.domain == XG_IF && space->mesh->dim == 3) {
+      set_last_error("xg_lform_create: the interface on boundary triangles (codimension 2) is not supported");
+      return XG_ERR_UNSUPPORTED;
+    }
+    if ((T.kind != XG_LTERM_SOURCE && T.kind != XG_LTERM_SOURCE_GF && T.kind != XG_LTERM_SOURCE_BND) ||
+        T.domain < 0 || T.domain > 2 ||
         T.order > kMaxOrder || (T.kind == XG_LTERM_SOURCE_GF && !T.d_gf) || T.e[0] < 0 || T.e[1] < 0 || T.e[2] < 0) {
       set_last_error("xg_lform_create: invalid term");
       return XG_ERR_ARG;
@@ -195,10 +332,15 @@ int xg_lform_create(xg_space* space, const xg_lterm* terms, int32_t n, xg_lform*
   if (!e) e = cudaMalloc((void**)&f->d_err, sizeof(int));
   if (!e) e = cudaMemset(f->d_err, 0, sizeof(int));
   if (e) {
-    cudaFree(f->d_elvec);
-    cudaFree(f->d_err);
-    delete f;
+    lform_free(f);
     return cuda_fail(e, "xg_lform_create");
+  }
+  for (int t = 0; t < n; t++) f->has_bnd |= terms[t].kind == XG_LTERM_SOURCE_BND;
+  if (f->has_bnd) {
+    if (int st = lform_bnd_setup(f)) {
+      lform_free(f);
+      return st;
+    }
   }
   *out = f;
   return XG_OK;
@@ -206,9 +348,7 @@ int xg_lform_create(xg_space* space, const xg_lterm* terms, int32_t n, xg_lform*
 
 int xg_lform_destroy(xg_lform* f) {
   if (!f) return XG_OK;
-  cudaFree(f->d_elvec);
-  cudaFree(f->d_err);
-  delete f;
+  lform_free(f);
   return XG_OK;
 }
 
@@ -240,6 +380,20 @@ int xg_lform_assemble(xg_lform* f, const double* d_lset, const uint8_t* d_dom, d
 #undef XG_LF
   const unsigned g2 = (unsigned)std::max<int64_t>(1, std::min<int64_t>((sp->ndof + 255) / 256, 152 * 16));
   k_lf_gather<<<g2, 256, 0, s>>>(sp->ndof, sp->nd, sp->d_dof_adj_ptr, sp->d_dof_adj, f->d_elvec, d_out);
+  if (f->has_bnd && m->nbnd > 0) {
+    const unsigned gb = (unsigned)std::max<int64_t>(1, std::min<int64_t>((m->nbnd + 127) / 128, 152 * 16));
+#define XG_LFB(DD, KK)                                                                                      \
+  k_lf_bnd<DD, KK><<<gb, 128, 0, s>>>(m->nbnd, m->d_bnd_v, f->d_bnd_el, m->ne, m->nv, m->d_elv, m->d_xyz, d_lset, \
+                                      f->desc, f->d_bvec, f->d_err)
+    if (D == 2 && K == 1) XG_LFB(2, 1);
+    else if (D == 2 && K == 2) XG_LFB(2, 2);
+    else if (D == 2 && K == 3) XG_LFB(2, 3);
+    else if (D == 3 && K == 1) XG_LFB(3, 1);
+    else if (D == 3 && K == 2) XG_LFB(3, 2);
+    else XG_LFB(3, 3);
+#undef XG_LFB
+    k_lf_gather_bnd<<<g2, 256, 0, s>>>(sp->ndof, sp->nd, f->d_badj_ptr, f->d_badj, f->d_bvec, d_out);
+  }
   XG_CUDA(cudaGetLastError());
   return XG_OK;
 }

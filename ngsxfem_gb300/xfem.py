@@ -34,7 +34,7 @@ VOL, BND = "VOL", "BND"
 
 TERM_MASS, TERM_LAPLACE, TERM_NGRADU_V, TERM_U_NGRADV, TERM_CONV, TERM_GHOST_MASS, TERM_DT_U_V = range(7)
 PREC_FP64, PREC_MIXED = 0, 1
-XG_LTERM_SOURCE, XG_LTERM_SOURCE_GF = 0, 1
+XG_LTERM_SOURCE, XG_LTERM_SOURCE_GF, XG_LTERM_SOURCE_BND = 0, 1, 2
 
 
 def _vp(t):
@@ -865,9 +865,11 @@ class BilinearForm:
 
 class LinearForm:
     """LinearForm over one H1 space: `f += coef * v * dCut(...)` with coef a
-    number, a monomial of x, y, z or a GridFunction of the same space;
-    `f.Assemble()` -> `f.vec` (device tensor, global dof numbering)
-    (xfem/symboliccutlfi.cpp:57-180)."""
+    number, a monomial of x, y, z or a GridFunction of the same space, and
+    boundary terms `f += coef * v * dCut(lset, dt, vb=BND[, definedon=
+    mesh.Boundaries(..)][, definedonelements=BND BitArray])` with coef a
+    number or a monomial; `f.Assemble()` -> `f.vec` (device tensor, global
+    dof numbering) (xfem/symboliccutlfi.cpp:57-180)."""
 
     def __init__(self, space, **kwargs):
         self.space = space
@@ -908,8 +910,13 @@ class LinearForm:
                             raise ValueError("the coefficient GridFunction must live in the form's space")
                     else:
                         raise NotImplementedError("one monomial or one GridFunction factor per term")
+                defined = m.definedonelements
+                if getattr(m, "vb", VOL) == BND:
+                    if kind != XG_LTERM_SOURCE:
+                        raise NotImplementedError("boundary linear form integrands: coef * monomial * v")
+                    kind, defined = XG_LTERM_SOURCE_BND, _bnd_restriction(self.space.mesh, defined, m.definedon)
                 out.append(dict(kind=kind, domain=m.domain_type, order=-1 if m.order is None else m.order, e=e,
-                                coef=mono.c, gf=gf, defined_on=m.definedonelements))
+                                coef=mono.c, gf=gf, defined_on=defined))
         return out
 
     def _levelset(self):
@@ -1035,11 +1042,9 @@ def _unscaled(meas):
     return out
 
 
-def _integrate_bnd(lset, dt, order, mono, mesh, defined=None, region=None):
-    """Integrate(f * dCut(lset, dt, vb=BND[, definedon=mesh.Boundaries(..)]
-    [, definedonelements=BND BitArray])): xg_integrate_bnd; the two
-    restrictions intersect."""
-    mesh = mesh if mesh is not None else lset.space.mesh
+def _bnd_restriction(mesh, defined, region):
+    """The bitset over the BND elements of definedonelements (a BitArray over
+    them) and definedon (mesh.Boundaries(...)), intersected; None for all."""
     dm = device_mesh(mesh)
     nb = np.zeros(1, dtype=np.int64)
     _lib.call("xg_mesh_boundary", dm.h, nb.ctypes.data_as(ctypes.c_void_p), None)
@@ -1051,6 +1056,16 @@ def _integrate_bnd(lset, dt, order, mono, mesh, defined=None, region=None):
         defined = r if defined is None else defined & r
     if defined is not None and len(defined) != nbnd:
         raise ValueError("definedonelements on vb=BND: a BitArray over the %d BND elements" % nbnd)
+    return defined
+
+
+def _integrate_bnd(lset, dt, order, mono, mesh, defined=None, region=None):
+    """Integrate(f * dCut(lset, dt, vb=BND[, definedon=mesh.Boundaries(..)]
+    [, definedonelements=BND BitArray])): xg_integrate_bnd; the two
+    restrictions intersect."""
+    mesh = mesh if mesh is not None else lset.space.mesh
+    dm = device_mesh(mesh)
+    defined = _bnd_restriction(mesh, defined, region)
     res = torch.zeros(1, dtype=torch.float64, device=_dev())
     _lib.call("xg_integrate_bnd", dm.h, _vp(_lset_vec(lset)), dt, order, mono.e[0], mono.e[1], mono.e[2],
               _vp(defined.words) if defined is not None else None, _vp(res), _stream())

@@ -1648,6 +1648,7 @@ int orc_linear_form(const orc_space* s, const double* lset_vertex, const orc_lte
     double b[20] = {0};
     for (int t = 0; t < nterms; t++) {
       const orc_lterm& T = terms[t];
+      if (T.kind == ORC_LTERM_SOURCE_BND) continue;
       if (T.defined_on && !test_bit(T.defined_on, e)) continue;
       const int order = T.order >= 0 ? T.order : 2 * s->k;
       const int np = straight_cut_rule(g, l, T.domain, order, pts, wts);
@@ -1676,6 +1677,69 @@ int orc_linear_form(const orc_space* s, const double* lset_vertex, const orc_lte
       }
     }
     for (int i = 0; i < n; i++) out[dofs[i]] += b[i];
+  }
+  bool bnd_terms = false;
+  for (int t = 0; t < nterms; t++) bnd_terms |= terms[t].kind == ORC_LTERM_SOURCE_BND;
+  if (!bnd_terms) return 0;
+  // boundary terms (dCut(lset, dt, vb=BND)): BND elements = the facets of one
+  // element, vertices ascending, in lexicographic order; the trace of the
+  // owning element's basis at the boundary rule's physical points
+  std::vector<std::pair<std::vector<int>, int>> facets;
+  for (int e = 0; e < s->ne; e++)
+    for (int skip = 0; skip <= D; skip++) {
+      std::vector<int> f;
+      for (int v = 0; v <= D; v++)
+        if (v != skip) f.push_back(s->elv[(size_t)e * (D + 1) + v]);
+      std::sort(f.begin(), f.end());
+      facets.push_back({f, e});
+    }
+  std::sort(facets.begin(), facets.end());
+  int64_t b = 0;
+  double xs[3 * 512], ws[512];
+  for (size_t i = 0; i < facets.size();) {
+    size_t j = i;
+    while (j < facets.size() && facets[j].first == facets[i].first) j++;
+    if (j - i == 1) {
+      const int e = facets[i].second;
+      Geo g;
+      double l[4];
+      element_geo(s, e, g, l, lset_vertex);
+      int gv[4];
+      for (int v = 0; v <= D; v++) gv[v] = s->elv[(size_t)e * (D + 1) + v];
+      double xb[9] = {0}, lb[3];
+      for (int v = 0; v < D; v++) {
+        const int id = facets[i].first[v];
+        lb[v] = lset_vertex[id];
+        for (int r = 0; r < D; r++) xb[3 * v + r] = s->coords[(size_t)id * D + r];
+      }
+      const int32_t* dofs = &s->el_dofs[(size_t)e * n];
+      double bv[20] = {0};
+      for (int t = 0; t < nterms; t++) {
+        const orc_lterm& T = terms[t];
+        if (T.kind != ORC_LTERM_SOURCE_BND || (T.defined_on && !test_bit(T.defined_on, b))) continue;
+        const int order = T.order >= 0 ? T.order : 2 * s->k;
+        const int np = orc_bnd_element_rule(D, xb, lb, T.domain, order, xs, ws, 512);
+        if (np < 0) return np == -1 ? ERR_CAPACITY : np;
+        for (int q = 0; q < np; q++) {
+          const double* x = &xs[3 * q];
+          double xi[3] = {0, 0, 0};
+          for (int k = 0; k < D; k++) {
+            double acc = 0.0;
+            for (int c = 0; c < D; c++) acc += g.Finv[k][c] * (x[c] - g.x0[c]);
+            xi[k] = acc;
+          }
+          double phi[20], dphi[20][3];
+          basis(D, s->k, gv, xi, phi, dphi);
+          const double gval =
+              T.coef * std::pow(x[0], T.e[0]) * std::pow(x[1], T.e[1]) * (D == 3 ? std::pow(x[2], T.e[2]) : 1.0);
+          const double w = ws[q] * gval;
+          for (int r = 0; r < n; r++) bv[r] += w * phi[r];
+        }
+      }
+      for (int r = 0; r < n; r++) out[dofs[r]] += bv[r];
+      b++;
+    }
+    i = j;
   }
   return 0;
 }

@@ -152,7 +152,9 @@ int orc_subdiv_moments_tet(const double* vals10, int levels, double* out35);
 
 /* --- linear forms ---------------------------------------------------------- */
 enum { ORC_LTERM_SOURCE = 0, /* coef * x^e0 y^e1 z^e2 * v */
-       ORC_LTERM_SOURCE_GF = 1 /* coef * u_h * v, u_h = gf (dof vector of the same space) */ };
+       ORC_LTERM_SOURCE_GF = 1, /* coef * u_h * v, u_h = gf (dof vector of the same space) */
+       ORC_LTERM_SOURCE_BND = 2 /* coef * x^e0 y^e1 z^e2 * v on the domain part of the BND elements (vb=BND);
+                                   defined_on: bits over the BND elements */ };
 typedef struct {
   int kind, domain, order;  /* order -1: 2k */
   int e[3];
@@ -211,6 +213,10 @@ int orc_mlset_mark(int D, int nv, const double* coords, int ne, const int32_t* e
  * boundary segments is the point measure (each intersection point counts 1). */
 double orc_integrate_bnd(int D, int nv, const double* coords, int ne, const int32_t* elv, const double* lset, int dt,
                          int order, int ex, int ey, int ez, const uint8_t* defined_on, int* status);
+/* The rule of one boundary element (xv[D][3], l[D]): physical points xs (3 per
+ * point), weights ws = w * measure; the number of points, -1 above cap, or
+ * -(error code). */
+int orc_bnd_element_rule(int D, const double* xv, const double* l, int dt, int order, double* xs, double* ws, int cap);
 /* The share of one boundary element (vertices xv[D][3], values l[D]). */
 double orc_bnd_element_integral(int D, const double* xv, const double* l, int dt, int order, int ex, int ey, int ez,
                                 int* status);

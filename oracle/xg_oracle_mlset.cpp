@@ -490,7 +490,12 @@ double orc_mlset_integrate(int D, int nv, const double* coords, int ne, const in
 // reference simplex of dimension D-1 maps by x = x_last + F xi.
 namespace {
 
-double bnd_element_integral(int D, const double (*xv)[3], const double* l, int dt, int order, int ex, int ey, int ez) {
+// the rule of one boundary element in physical points xs (3 per point) and
+// weights ws = w * measure
+void bnd_element_rule(int D, const double (*xv)[3], const double* l, int dt, int order, std::vector<double>& xs,
+                      std::vector<double>& ws) {
+  xs.clear();
+  ws.clear();
   const int d = D - 1;  // dimension of the boundary element
   // F (3 x d): columns x_k - x_d; measure: length (d = 1) or |F1 x F2| (d = 2)
   double F[3][2] = {{0, 0}, {0, 0}, {0, 0}};
@@ -510,7 +515,7 @@ double bnd_element_integral(int D, const double (*xv)[3], const double* l, int d
   std::vector<V3> pts;
   std::vector<double> wts;
   if (dom != IF) {
-    if (dom != dt) return 0.0;
+    if (dom != dt) return;
     const Rule1 r = base(d, order);
     for (size_t q = 0; q < r.w.size(); q++) {
       pts.push_back(V3{{r.p[3 * q], r.p[3 * q + 1], r.p[3 * q + 2]}});
@@ -528,21 +533,49 @@ double bnd_element_integral(int D, const double (*xv)[3], const double* l, int d
     if (dt == IF)  // point measure: weight / measure, so that weight * measure = 1
       for (double& w : wts) w = w / meas;
   }
-  double sum = 0;
   for (size_t q = 0; q < wts.size(); q++) {
-    double x[3];
     for (int r = 0; r < 3; r++) {
       double s = xv[d][r];
       for (int k = 0; k < d; k++) s += F[r][k] * pts[q].x[k];
-      x[r] = s;
+      xs.push_back(s);
     }
+    ws.push_back(wts[q] * meas);
+  }
+}
+
+double bnd_element_integral(int D, const double (*xv)[3], const double* l, int dt, int order, int ex, int ey, int ez) {
+  std::vector<double> xs, ws;
+  bnd_element_rule(D, xv, l, dt, order, xs, ws);
+  double sum = 0;
+  for (size_t q = 0; q < ws.size(); q++) {
+    const double* x = &xs[3 * q];
     const double fv = std::pow(x[0], ex) * std::pow(x[1], ey) * (D == 3 ? std::pow(x[2], ez) : 1.0);
-    sum += wts[q] * meas * fv;
+    sum += ws[q] * fv;
   }
   return sum;
 }
 
 }  // namespace
+
+// the rule of one boundary element: physical points (3 per point) and weights
+// w * measure; returns the number of points, -1 when more than cap, or
+// -(error code)
+extern "C" int orc_bnd_element_rule(int D, const double* xv, const double* l, int dt, int order, double* xs, double* ws,
+                                    int cap) {
+  double v[3][3];
+  for (int i = 0; i < D; i++)
+    for (int r = 0; r < 3; r++) v[i][r] = xv[3 * i + r];
+  std::vector<double> px, pw;
+  try {
+    bnd_element_rule(D, v, l, dt, order, px, pw);
+  } catch (const MErr& err) {
+    return -err.code;
+  }
+  if ((int)pw.size() > cap) return -1;
+  std::copy(px.begin(), px.end(), xs);
+  std::copy(pw.begin(), pw.end(), ws);
+  return (int)pw.size();
+}
 
 // one boundary element (vertices xv[D][3], values l[D]); *status on an error
 extern "C" double orc_bnd_element_integral(int D, const double* xv, const double* l, int dt, int order, int ex, int ey,

@@ -97,3 +97,51 @@ def test_boundary_regions(xg, orc):
         assert abs(got - ref[key]) < ref["tol"]
     with pytest.raises(ValueError):
         xg.Integrate(xg.dCut(g, xg.NEG, vb=xg.BND, definedonelements=xg.BitArray(m.ne)), m)
+
+
+def bnd_bits(mask):
+    b = np.packbits(np.asarray(mask, bool), bitorder="little")
+    return np.concatenate([b, np.zeros((-b.size) % 8, np.uint8)]).view(np.uint64)
+
+
+def test_boundary_linear_form(xg, orc):
+    """LinearForm with v * dCut(lset, dt, vb=BND[, definedon]) against the
+    oracle's vector (1e-12 relative to its largest entry) and the closed
+    forms of test_bndcut.py:123-165."""
+    m = MakeStructured2DMesh(9, 9)
+    l = orc.interpolate_p1_perturb(m.coords[:, 0] - 0.4)
+    g = gf_of(xg, m, l)
+    bottom = m.Boundaries("bottom")
+    for k in (1, 2, 3):
+        V = xg.H1(m, order=k)
+        v = V.TestFunction()
+        sp = orc.Space(m, k)
+        cases = [
+            (v * xg.dCut(g, xg.NEG, vb=xg.BND), [dict(kind=2, domain=orc.NEG)]),
+            (xg.x * v * xg.dCut(g, xg.POS, vb=xg.BND, definedon=bottom),
+             [dict(kind=2, domain=orc.POS, e=(1, 0, 0), defined_on=bnd_bits(bottom.Mask()))]),
+            (2.0 * xg.y * v * xg.dCut(g, xg.IF, vb=xg.BND, order=0),
+             [dict(kind=2, domain=orc.IF, order=0, e=(0, 1, 0), coef=2.0)]),
+            (v * xg.dCut(g, xg.NEG) + v * xg.dCut(g, xg.NEG, vb=xg.BND),
+             [dict(kind=0, domain=orc.NEG), dict(kind=2, domain=orc.NEG)]),
+        ]
+        for integral, terms in cases:
+            f = xg.LinearForm(V)
+            f += integral
+            f.Assemble()
+            got = f.vec.cpu().numpy()
+            ref = sp.linear_form(l, terms)
+            assert np.max(np.abs(got - ref)) <= 1e-12 * max(1.0, np.max(np.abs(ref))), (k, terms)
+        f = xg.LinearForm(V)
+        f += v * xg.dCut(g, xg.NEG, vb=xg.BND, definedon=bottom)
+        f.Assemble()
+        c1 = np.zeros(V.ndof)
+        c1[:m.nv] = 1.0
+        assert abs(f.vec.cpu().numpy() @ c1 - 0.4) < 1e-12
+    m3 = MakeStructured3DMesh(4)
+    g3 = gf_of(xg, m3, orc.interpolate_p1_perturb(m3.coords[:, 0] - 0.3))
+    V3 = xg.H1(m3, order=2)
+    f = xg.LinearForm(V3)
+    f += V3.TestFunction() * xg.dCut(g3, xg.IF, vb=xg.BND)
+    with pytest.raises(RuntimeError):
+        f.Assemble()

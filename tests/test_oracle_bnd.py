@@ -7,6 +7,7 @@ import json
 import os
 
 import numpy as np
+import pytest
 
 from ngsxfem_gb300.meshes import MakeStructured2DMesh, MakeStructured3DMesh
 
@@ -75,3 +76,44 @@ def test_boundary_elements_order():
     assert (masks.sum(axis=0) == 1).all() and (masks.sum(axis=1) == 18).all()
     x = m.coords[b]
     assert np.all(x[masks[2]][..., 1] == 0.0) and np.all(x[masks[5]][..., 2] == 1.0)
+
+
+def bnd_bits(mask):
+    """A boolean mask over the BND elements as the oracle's uint64 bit words."""
+    b = np.packbits(np.asarray(mask, bool), bitorder="little")
+    return np.concatenate([b, np.zeros((-b.size) % 8, np.uint8)]).view(np.uint64)
+
+
+def test_boundary_linear_form(orc):
+    """v * dCut(lset, dt, vb=BND) (the reference's boundary linear forms,
+    test_bndcut.py:123-165): with c1 / cx the coefficients of the functions
+    1 and x (vertex dofs 1 / x, the others 0), b.c1 is the measure of the
+    domain part of the boundary and b.cx the integral of x over it."""
+    m = MakeStructured2DMesh(9, 9)
+    l = orc.interpolate_p1_perturb(m.coords[:, 0] - 0.4)
+    bottom = bnd_bits(m.Boundaries("bottom").Mask())
+    for k in (1, 2, 3):
+        sp = orc.Space(m, k)
+        b = sp.linear_form(l, [dict(kind=2, domain=orc.NEG)])
+        c1, cx = np.zeros(len(b)), np.zeros(len(b))
+        c1[:m.nv], cx[:m.nv] = 1.0, m.coords[:, 0]
+        assert abs(b @ c1 - 1.8) < 1e-13 and abs(b @ cx - 0.16) < 1e-13
+        if k == 1:
+            assert abs(b.sum() - 1.8) < 1e-13  # partition of unity
+        bb = sp.linear_form(l, [dict(kind=2, domain=orc.NEG, defined_on=bottom)])
+        assert abs(bb @ c1 - 0.4) < 1e-13
+        bi = sp.linear_form(l, [dict(kind=2, domain=orc.IF, order=0, e=(0, 1, 0))])
+        assert abs(bi @ c1 - 1.0) < 1e-13  # y at the interface points (0.4, 0) and (0.4, 1)
+        # volume and boundary terms add
+        bv = sp.linear_form(l, [dict(kind=0, domain=orc.NEG)])
+        both = sp.linear_form(l, [dict(kind=0, domain=orc.NEG), dict(kind=2, domain=orc.NEG)])
+        assert np.allclose(both, bv + b, rtol=0, atol=1e-15)
+    m3 = MakeStructured3DMesh(4)
+    l3 = orc.interpolate_p1_perturb(m3.coords[:, 0] - 0.3)
+    sp = orc.Space(m3, 2)
+    b = sp.linear_form(l3, [dict(kind=2, domain=orc.NEG)])
+    c1 = np.zeros(len(b))
+    c1[:m3.nv] = 1.0
+    assert abs(b @ c1 - 2.2) < 1e-13
+    with pytest.raises(RuntimeError):
+        sp.linear_form(l3, [dict(kind=2, domain=orc.IF)])
