@@ -23,7 +23,7 @@
 #include "xg_basis.cuh"
 #include "xg_cut.cuh"
 #include "xg_internal.h"
-#include "xg_mlset.cuh"
+#include "xg_lfbnd.cuh"
 
 namespace xg {
 
@@ -166,8 +166,6 @@ __global__ void __launch_bounds__(128) k_lf_bnd(int64_t nbnd, const int32_t* __r
   constexpr int N = ndof_el(D, K);
   for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < nbnd; b += (int64_t)gridDim.x * blockDim.x) {
     double acc[N];
-#pragma unroll
-    for (int i = 0; i < N; i++) acc[i] = 0.0;
     const int e = bnd_el[b];
     double xv[D + 1][3];
     int gv[4];
@@ -178,11 +176,6 @@ __global__ void __launch_bounds__(128) k_lf_bnd(int64_t nbnd, const int32_t* __r
 #pragma unroll
       for (int c = 0; c < 3; c++) xv[v][c] = c < D ? xyz[(int64_t)c * nv + vid] : 0.0;
     }
-    Geo<D> g;
-    make_geo<D>(xv, g);
-    int desc[N];
-#pragma unroll
-    for (int i = 0; i < N; i++) desc[i] = fn_desc<D, K>(i, gv);
     double xb[D][3], lb[D];
 #pragma unroll
     for (int v = 0; v < D; v++) {
@@ -191,29 +184,8 @@ __global__ void __launch_bounds__(128) k_lf_bnd(int64_t nbnd, const int32_t* __r
 #pragma unroll
       for (int c = 0; c < 3; c++) xb[v][c] = c < D ? xyz[(int64_t)c * nv + vid] : 0.0;
     }
-    for (int t = 0; t < d.n; t++) {
-      const xg_lterm& T = d.t[t];
-      if (T.kind != XG_LTERM_SOURCE_BND || (T.d_defined_on && !tbit64(T.d_defined_on, b))) continue;
-      const int p = clamp_order(T.order >= 0 ? T.order : 2 * K);
-      auto emit = [&](const double* x, double w, double meas) {
-        double lam[D + 1], sl = 0.0;
-#pragma unroll
-        for (int k = 0; k < D; k++) {
-          double s = 0.0;
-#pragma unroll
-          for (int c = 0; c < D; c++) s += g.Finv[k][c] * (x[c] - g.x0[c]);
-          lam[k] = s;
-          sl += s;
-        }
-        lam[D] = 1.0 - sl;
-        const double gv2 = T.coef * ipow(x[0], T.e[0]) * ipow(x[1], T.e[1]) * (D == 3 ? ipow(x[2], T.e[2]) : 1.0);
-        const double wq = w * meas * gv2;
-#pragma unroll
-        for (int i = 0; i < N; i++) acc[i] += wq * eval_fn_value<D, double>(desc[i], lam);
-      };
-      const int st = ml::bnd_rule<D>(&g_lfb_rules, xb, lb, T.domain, p, emit);
-      if (st) set_err(err, st);
-    }
+    const int st = lfb::element_vector<D, K>(&g_lfb_rules, xv, gv, xb, lb, d.t, d.n, b, acc);
+    if (st) set_err(err, st);
 #pragma unroll
     for (int i = 0; i < N; i++) {
       if (!isfinite(acc[i])) set_err(err, XG_ERR_NONFINITE);

@@ -117,3 +117,88 @@ def test_boundary_linear_form(orc):
     assert abs(b @ c1 - 2.2) < 1e-13
     with pytest.raises(RuntimeError):
         sp.linear_form(l3, [dict(kind=2, domain=orc.IF)])
+
+
+def owners(m):
+    """The element each BND element (Mesh.boundary_elements order) belongs to."""
+    own = {}
+    d = m.dim
+    for e, el in enumerate(m.elements):
+        for s in range(d + 1):
+            own[tuple(sorted(np.delete(el, s)))] = e
+    return np.array([own[tuple(r)] for r in m.boundary_elements()], dtype=np.int64)
+
+
+def test_boundary_linear_form_device_code(orc, tmp_path):
+    """csrc/xg_lfbnd.cuh (the body of the GPU kernel k_lf_bnd) compiled as
+    host code (tests/native/lf_bnd_check.cu): its element vectors, gathered
+    with the oracle space's dofs, equal orc_linear_form within 1e-13."""
+    import ctypes
+    import shutil
+    import subprocess
+
+    from ngsxfem_gb300 import _lib
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not found")
+    root = os.path.dirname(HERE)
+    libdir = os.path.dirname(orc.LIB)
+    so = str(tmp_path / "liblfb.so")
+    subprocess.check_call([nvcc, "-x", "cu", "-std=c++17", "-O1", "-shared", "-Xcompiler", "-fPIC", "-Xcompiler",
+                           "-ffp-contract=off", "-diag-suppress", "20011,20014",
+                           "-I", os.path.join(root, "ngsxfem_gb300", "csrc"), "-I", os.path.join(root, "include"),
+                           os.path.join(HERE, "native", "lf_bnd_check.cu"), "-L", libdir, "-loracle",
+                           "-Xlinker", "-rpath", "-Xlinker", libdir, "-o", so])
+    L = ctypes.CDLL(so)
+    P = ctypes.c_void_p
+    L.lfb_element_vectors.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int64, P, P, P, P, P, ctypes.c_int, P]
+    p = lambda a: a.ctypes.data_as(P)  # noqa: E731
+    cases = [(MakeStructured2DMesh(9, 7), lambda c: c[:, 0] - 0.4 + 0.1 * c[:, 1], (1, 2, 3)),
+             (MakeStructured3DMesh(3), lambda c: c[:, 0] - 0.3 + 0.2 * c[:, 2], (1, 2, 3))]
+    worst = 0.0
+    for m, f, ks in cases:
+        D = m.dim
+        l = orc.interpolate_p1_perturb(f(m.coords))
+        bnd, own = m.boundary_elements(), owners(m)
+        nb = len(bnd)
+        xv = np.zeros((nb, D + 1, 3))
+        xv[..., :D] = m.coords[m.elements[own]]
+        gv = np.ascontiguousarray(m.elements[own], dtype=np.int32)
+        xb = np.zeros((nb, D, 3))
+        xb[..., :D] = m.coords[bnd]
+        lb = np.ascontiguousarray(l[bnd])
+        bottom = m.Boundaries("bottom").Mask()
+        term_sets = [[dict(kind=2, domain=orc.NEG)],
+                     [dict(kind=2, domain=orc.POS, e=(1, 0, 1), coef=-1.5, defined_on=bottom, order=3)],
+                     [dict(kind=2, domain=orc.NEG, e=(0, 2, 0)), dict(kind=2, domain=orc.POS, order=1)]]
+        if D == 2:
+            term_sets.append([dict(kind=2, domain=orc.IF, order=0, e=(0, 1, 0), coef=2.0)])
+        for k in ks:
+            sp = orc.Space(m, k)
+            dofs = sp.el_dofs()
+            for terms in term_sets:
+                arr = (_lib.LTerm * len(terms))()
+                keep = []
+                for i, t in enumerate(terms):
+                    arr[i].kind, arr[i].domain, arr[i].order = 2, t["domain"], t.get("order", -1)
+                    arr[i].coef = t.get("coef", 1.0)
+                    for j in range(3):
+                        arr[i].e[j] = t.get("e", (0, 0, 0))[j]
+                    if t.get("defined_on") is not None:
+                        bits = bnd_bits(t["defined_on"])
+                        keep.append(bits)
+                        arr[i].d_defined_on = bits.ctypes.data
+                n = dofs.shape[1]
+                vec = np.zeros((nb, n))
+                st = L.lfb_element_vectors(D, k, nb, p(xv), p(gv), p(xb), p(lb), ctypes.cast(arr, P), len(terms),
+                                           p(vec))
+                assert st == 0
+                got = np.zeros(sp.ndof)
+                np.add.at(got, dofs[own], vec)
+                oterms = [dict(t, kind=2, defined_on=None if t.get("defined_on") is None else
+                               bnd_bits(t["defined_on"])) for t in terms]
+                ref = sp.linear_form(l, oterms)
+                err = np.max(np.abs(got - ref)) / max(1.0, np.max(np.abs(ref)))
+                worst = max(worst, err)
+                assert err < 1e-13, (D, k, terms, err)
+    assert worst < 1e-13
