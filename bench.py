@@ -663,11 +663,22 @@ class Clocks:
                 "samples": len(sm)}
 
 
-# DRAM bytes (read + write) per launch of the dominant kernel from one ncu
-# capture of the same workload (profiles/cutfem_step_3d_poisson_64cube_p2_fp64.md,
-# profiles/st_elmat_spacetime_256sq_p1p1_fp64.md)
-TRAFFIC = {("c2", "patch"): 34.675968e6 + 153.309696e6, ("c2", "scatter"): 707.318272e6 + 99.713536e6,
-           ("c2", "elmat_cut"): 13.181184e6 + 9.851904e6 + 28.001792e6 + 0.007424e6 + 35.953920e6 + 2.345728e6}
+# DRAM bytes (read + write) per launch of a stage's dominant kernel, from one
+# ncu capture of the same workload (scaled from a smaller case where the
+# entry says so).  Each entry names the kernel and the first 16 hex digits of
+# the sha256 of the source file it was captured on; when that file has
+# changed since, the line reports traffic null instead of a stale figure.
+TRAFFIC = {}
+
+
+def traffic_for(workload, stage):
+    t = TRAFFIC.get((workload, stage))
+    if t is None:
+        return None
+    import hashlib
+    with open(os.path.join(ROOT, t["source"]), "rb") as f:
+        sha = hashlib.sha256(f.read()).hexdigest()[:16]
+    return t["bytes"] if sha == t["sha16"] else None
 
 
 def patch_exact_flops(dim, k):
@@ -862,6 +873,75 @@ class Gpu:
             self._lib.check(self._lib.load().xg_form_check(ctypes.c_void_p(f)), "bench form")
 
 
+def fetch_csr(gpu, e):
+    """The entry's output as (global rows, global cols, vals) numpy arrays,
+    row-major with ascending columns."""
+    o = e["out"]
+    n, z = (int(x) for x in o["counts"].cpu().tolist())
+    rd = o["row_dof"][:n].cpu().numpy()
+    rp = o["rowptr"][: n + 1].cpu().numpy()
+    c = o["cols"][:z].cpu().numpy()
+    v = o["vals"][:z].cpu().numpy()
+    return np.repeat(rd.astype(np.int64), np.diff(rp)), rd[c], v
+
+
+def oracle_csr(e, nth):
+    """The oracle's matrix of the entry's step (CutInfo -> element and facet
+    sets -> assembly) on all host threads."""
+    from oracle import oracle as orc
+    kind, m, vals, order, terms = e["host"]
+    if kind == "st":
+        lst = np.stack([orc.interpolate_p1_perturb(x) for x in vals])
+        sp = orc.Space(m, 1)
+        _, _, bits = sp.cutinfo_st(lst, len(vals) - 1, nthreads=nth)
+        fb = sp.facets_with_neighbor_types(bits[5], bits[4], True, True, True)
+        t2 = [dict(t, defined_on=fb if t["kind"] == orc.TERM_GHOST_MASS else bits[5]) for t in terms]
+        rp, cols, rv = sp.assemble_st(lst, len(vals) - 1, 1, 2, t2, nthreads=nth)
+    else:
+        l = orc.interpolate_p1_perturb(vals)
+        sp = orc.Space(m, order)
+        _, _, bits = sp.cutinfo(l, nthreads=nth)
+        fb = sp.facets_with_neighbor_types(bits[5], bits[4], True, True, True)
+        t2 = [dict(t, defined_on=fb if t["kind"] == orc.TERM_GHOST_MASS else
+                   {orc.NEG: bits[5], orc.IF: bits[4], orc.POS: bits[6]}[t["domain"]]) for t in terms]
+        rp, cols, rv = sp.assemble(l, t2, nthreads=nth)
+    return np.repeat(np.arange(len(rp) - 1, dtype=np.int64), np.diff(rp)), cols, rv
+
+
+def max_rel_err(got, ref):
+    """(same pattern, max |got - ref| / max |ref|) of two row-major CSRs."""
+    same = len(got[2]) == len(ref[2]) and np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1])
+    if not same:
+        return False, None
+    scale = float(np.max(np.abs(ref[2]))) if len(ref[2]) else 1.0
+    return True, float(np.max(np.abs(got[2] - ref[2]))) / max(scale, 1e-300) if len(ref[2]) else 0.0
+
+
+def time_graph(gpu, steps, warmup, flush, clk=None):
+    """Mean device time (ms) of `steps` graph replays, L2 flushed before each."""
+    torch = gpu.torch
+    stream = gpu.stream
+    for _ in range(warmup):
+        gpu.launch()
+    gpu.check_forms()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    torch.cuda.synchronize()
+    if clk is not None:
+        clk.__enter__()
+    for k in range(steps):
+        flush.fill_(float(k))  # L2 flush between timed steps (not timed)
+        starts[k].record(stream)
+        gpu.launch()
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    if clk is not None:
+        clk.__exit__(None, None, None)
+    gpu.check_forms()
+    return float(np.mean([a.elapsed_time(b) for a, b in zip(starts, ends)]))
+
+
+
 def setup(args, gpu):
     """Builds the workload's forms and steps on the device; returns the config."""
     xg = gpu.xg
@@ -889,7 +969,8 @@ def setup(args, gpu):
             mk["order"] = order
             if args.workload == "c1":
                 mk["n_facets"] = 0  # no patch terms
-            gpu.add(form, lset, False, mk)
+            e = gpu.add(form, lset, False, mk)
+            e["host"] = ("plain", m, vals, order, (terms_c2 if args.workload == "c3" else tf)(order))
         if args.workload == "c3":
             cfg["groups"] = {str(k): {"n_tets": int(m.ne)} for k, (m, _) in groups.items()}
     else:
@@ -903,12 +984,14 @@ def setup(args, gpu):
         # one form per slab: the convection field's time origin is a form
         # parameter (t0 of b(t)), so each slab's form differs in t0 only
         for s in range(C5_SLABS):
-            lset = gpu.lset(c5_slab_values(m, s, args.kt))
+            st_vals = c5_slab_values(m, s, args.kt)
+            lset = gpu.lset(st_vals)
             form = gpu.st_form(sh, args.kt, 2, terms_c5(s * C5_DT))
             mk = gpu.marking_st(dm, lset, args.kt)
             mk["ndof_el"] = int(info[1])
             mk["order"] = 1
-            gpu.add(form, lset, True, mk)
+            e = gpu.add(form, lset, True, mk)
+            e["host"] = ("st", m, st_vals, 1, terms_c5(s * C5_DT))
         gpu.st_space = sh
     return cfg
 
@@ -930,6 +1013,8 @@ def main():
     ap.add_argument("--meshes", type=int, default=512)
     ap.add_argument("--kt", type=int, default=1, choices=[1, 2])
     ap.add_argument("--cpu-baseline", type=int, default=1)
+    ap.add_argument("--check", type=int, default=1, help="error of the step against the oracle")
+    ap.add_argument("--mixed", type=int, default=1, help="also time the mixed form (fp64 runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.workload == "c4":
@@ -959,27 +1044,14 @@ def main():
 
     # ---------------- device-resident timing (graph replay) ----------------
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > L2 (129 MB)
-    for _ in range(args.warmup):
-        gpu.launch()
-    gpu.check_forms()
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     if ws > 1:
         torch.distributed.barrier()
-    torch.cuda.synchronize()
-    with Clocks(local) as clk:
-        for k in range(args.steps):
-            flush.fill_(float(k))  # L2 flush between timed steps (not timed)
-            starts[k].record(stream)
-            gpu.launch()
-            ends[k].record(stream)
-        torch.cuda.synchronize()
-    ms = float(np.mean([s.elapsed_time(e) for s, e in zip(starts, ends)]))
+    clk = Clocks(local)
+    ms = time_graph(gpu, args.steps, args.warmup, flush, clk)
     if ws > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
-    gpu.check_forms()
     value = ws * n_cut / (ms * 1e-3)
 
     # ---------------- stage breakdown (eager steps with stage events) ----------------
@@ -1033,6 +1105,46 @@ def main():
     e2e_s = float(np.mean(e2e_times))
     h2d = sum(e["lset"].numel() * 8 for e in E)
     d2h = sum(16 + e["nrows"] * 4 + (e["nrows"] + 1) * 8 + e["nnz"] * 12 for e in E)
+
+    # ---------------- the mixed arm on the same workload ----------------
+    fp64_out = [fetch_csr(gpu, e) for e in E] if rank == 0 else None
+    mixed = None
+    if args.precision == "fp64" and args.mixed:
+        a2 = argparse.Namespace(**vars(args))
+        a2.precision = "mixed"
+        gm = Gpu(a2)
+        setup(a2, gm)
+        gm.graph()
+        if ws > 1:
+            torch.distributed.barrier()
+        ms_m = time_graph(gm, args.steps, args.warmup, flush)
+        if ws > 1:
+            t = torch.tensor([ms_m], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms_m = float(t.item())
+        mixed = {"value": ws * n_cut / (ms_m * 1e-3), "unit": UNIT, "ms_per_step": ms_m, "speedup_vs_fp64": ms / ms_m,
+                 "dtype": "f32 contractions (compensated), f64 geometry and sums"}
+        if rank == 0:
+            res = [max_rel_err(fetch_csr(gm, e), ref) for e, ref in zip(gm.entries, fp64_out)]
+            mixed["same_pattern_as_fp64"] = all(r[0] for r in res)
+            mixed["max_rel_err_vs_fp64"] = max((r[1] for r in res if r[1] is not None), default=None)
+            mixed["err_definition"] = "max |A_mixed - A_fp64| / max |A_fp64| over all entries of the step's matrices"
+        for f in {e["form"].value for e in gm.entries}:
+            _lib.load().xg_form_destroy(ctypes.c_void_p(f))
+        _lib.load().xg_step_graph_destroy(gm.g)
+        del gm
+
+    # ---------------- error of this arm against the oracle ----------------
+    check = None
+    if rank == 0 and args.check:
+        nth = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        res = [max_rel_err(got, oracle_csr(e, nth)) for e, got in zip(E, fp64_out)]
+        check = {"same_pattern": all(r[0] for r in res),
+                 "max_rel_err": max((r[1] for r in res if r[1] is not None), default=None),
+                 "against": "oracle (C++ restatement of the reference path, FP64), whole workload",
+                 "definition": "max |A_gpu - A_oracle| / max |A_oracle| over all entries of each step's matrix",
+                 "host_s": time.perf_counter() - t0}
 
     # ---------------- roofline ----------------
     # algorithmic bytes per stage: vertex ids, coordinates + level set per vertex,
@@ -1098,7 +1210,7 @@ def main():
                 "ms_per_step": e2e_s * 1e3},
         "stages_ms": {n: float(v) for n, v in zip(names, stage_ms)},
         "roofline": {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": peak_bw, "unit": "GB/s",
-                     "frac": achieved / peak_bw, "traffic": TRAFFIC.get((args.workload, dname)) if
+                     "frac": achieved / peak_bw, "traffic": traffic_for(args.workload, dname) if
                      (args.workload, args.n, args.order) == ("c2", 64, 2) or args.workload != "c2" else None,
                      "peak_source": "measured" if pk else "fallback",
                      "whole_step": {"achieved": step_bytes / (ms * 1e-3) / 1e9,
@@ -1106,6 +1218,11 @@ def main():
         "clocks": clk.summary(),
         "gpu_launches": args.steps * gpu.kernels,
     }
+    if check is not None:
+        out["max_rel_err"] = check["max_rel_err"]
+        out["error_check"] = check
+    if mixed is not None:
+        out["mixed"] = mixed
     if fp64 is not None:  # the bound that binds for the dominant kernel
         fp64["traffic"] = out["roofline"]["traffic"]
         fp64["hbm"] = out["roofline"]

@@ -210,19 +210,6 @@ int xg_base_rule(int d, int p, double* h_pts, double* h_wts, int max_pts);
 int xg_integrate(xg_mesh* mesh, const double* d_lset, int dt, int order, int ex, int ey, int ez,
                  const uint64_t* d_defined_on, double* d_result, void* stream);
 
-/* Allocation-free variant of xg_integrate (no counterpart in the reference).
- * For callers that cannot allocate device memory when they integrate: code
- * running while a stream is captured into a CUDA graph, real-time loops that
- * forbid allocator calls, hosts whose device memory belongs to another
- * allocator.  It calls no cudaMalloc/cudaFree; its per-block partial sums live
- * in a static 128 KiB device array that every GPU loading the library keeps
- * until exit, which limits it to meshes of at most 16384*4096 = 67,108,864
- * elements (larger meshes get XG_ERR_CAPACITY and a message).  The first call
- * on a device looks up the array's device address (cudaGetSymbolAddress) with
- * that device current; make that first call before any stream capture.  All
- * calls share the array: calls that overlap on the GPU (different streams,
- * concurrent graphs) race and must be serialised by the caller.  The result
- * equals xg_integrate's up to the summation order (a fixed order per mesh). */
 /* Several level sets on a simplex mesh (cutint/mlsetintegration.cpp:6-180,
  * cutint/straightcutrule.cpp:679-812): d_lsets holds nlsets (1..8) P1 level
  * sets, [nlsets][nv] vertex values; the domain is the union of ndomains
@@ -268,6 +255,21 @@ int xg_iso_integrate_mesh(xg_mesh* mesh, const double* d_p2vals, int dt, int ord
 /* xg_integrate with the quadrilateral / hexahedral direction policy. */
 int xg_integrate_ex(xg_mesh* mesh, const double* d_lset, int dt, int order, int quad_dir_policy, int ex, int ey,
                     int ez, const uint64_t* d_defined_on, double* d_result, void* stream);
+/* Allocation-free variant of xg_integrate (no counterpart in the reference).
+ * For callers that cannot allocate device memory when they integrate:
+ * real-time loops that forbid allocator calls (a cudaMalloc can synchronise
+ * the device and take milliseconds), and host applications whose device
+ * memory belongs to their own allocator or budget.  Simplex meshes only
+ * (quadrilateral / hexahedral meshes get XG_ERR_UNSUPPORTED; xg_integrate
+ * takes them).  It calls no cudaMalloc/cudaFree; its per-block partial sums live
+ * in a static 128 KiB device array that every GPU loading the library keeps
+ * until exit, which limits it to meshes of at most 16384*4096 = 67,108,864
+ * elements (larger meshes get XG_ERR_CAPACITY and a message).  The first call
+ * on a device looks up the array's device address (cudaGetSymbolAddress) with
+ * that device current; make that first call before any stream capture.  All
+ * calls share the array: calls that overlap on the GPU (different streams,
+ * concurrent graphs) race and must be serialised by the caller.  The result
+ * equals xg_integrate's up to the summation order (a fixed order per mesh). */
 int xg_integrate_noalloc(xg_mesh* mesh, const double* d_lset, int dt, int order, int ex, int ey, int ez,
                          const uint64_t* d_defined_on, double* d_result, void* stream);
 

@@ -2,12 +2,14 @@
 // topology (the ngcomp::MeshAccess tables the reference reads) and H1 dof
 // tables.  None of this runs per assembly step.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
 
 #include "xg_internal.h"
+#include "xg_topology.h"
 
 namespace xg {
 
@@ -176,10 +178,6 @@ const RuleTable& host_rules() {
 using namespace xg;
 
 namespace {
-const int TRI_EDGES[3][2] = {{0, 1}, {0, 2}, {1, 2}};
-const int TET_EDGES[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
-const int TET_FACES[4][3] = {{0, 1, 2}, {0, 1, 3}, {0, 2, 3}, {1, 2, 3}};
-
 template <class T>
 int upload(T** d, const std::vector<T>& h) {
   if (h.empty()) { *d = nullptr; return XG_OK; }
@@ -276,42 +274,10 @@ int xg_mesh_create(int dim, int32_t nv, const double* h_coords, int32_t ne, cons
       set_last_error("xg_mesh_create: vertex index out of range");
       return XG_ERR_ARG;
     }
-  // edges: unique (min,max) vertex pairs, numbered in lexicographic order
+  // edges and faces numbered in lexicographic order of their vertex tuples
   const int nel = dim == 2 ? 3 : 6;
-  std::vector<uint64_t> keys((size_t)ne * nel);
-  for (int e = 0; e < ne; e++)
-    for (int j = 0; j < nel; j++) {
-      int a = h_elv[(size_t)e * nvl + (dim == 2 ? TRI_EDGES[j][0] : TET_EDGES[j][0])];
-      int b = h_elv[(size_t)e * nvl + (dim == 2 ? TRI_EDGES[j][1] : TET_EDGES[j][1])];
-      if (a > b) std::swap(a, b);
-      keys[(size_t)e * nel + j] = ((uint64_t)a << 32) | (uint32_t)b;
-    }
-  {
-    std::vector<uint64_t> u(keys);
-    std::sort(u.begin(), u.end());
-    u.erase(std::unique(u.begin(), u.end()), u.end());
-    m->nedges = (int64_t)u.size();
-    m->h_el_edges.resize(keys.size());
-    for (size_t i = 0; i < keys.size(); i++)
-      m->h_el_edges[i] = (int32_t)(std::lower_bound(u.begin(), u.end(), keys[i]) - u.begin());
-  }
-  if (dim == 3) {
-    std::vector<uint64_t> fk((size_t)ne * 4);
-    for (int e = 0; e < ne; e++)
-      for (int j = 0; j < 4; j++) {
-        int v[3];
-        for (int q = 0; q < 3; q++) v[q] = h_elv[(size_t)e * 4 + TET_FACES[j][q]];
-        std::sort(v, v + 3);
-        fk[(size_t)e * 4 + j] = ((uint64_t)v[0] << 42) | ((uint64_t)v[1] << 21) | (uint64_t)v[2];
-      }
-    std::vector<uint64_t> u(fk);
-    std::sort(u.begin(), u.end());
-    u.erase(std::unique(u.begin(), u.end()), u.end());
-    m->nfaces = (int64_t)u.size();
-    m->h_el_faces.resize(fk.size());
-    for (size_t i = 0; i < fk.size(); i++)
-      m->h_el_faces[i] = (int32_t)(std::lower_bound(u.begin(), u.end(), fk[i]) - u.begin());
-  }
+  m->nedges = number_edges(dim, ne, h_elv, m->h_el_edges);
+  if (dim == 3) m->nfaces = number_faces(ne, h_elv, m->h_el_faces);
   m->nfacets = dim == 2 ? m->nedges : m->nfaces;
   const std::vector<int32_t>& elf = dim == 2 ? m->h_el_edges : m->h_el_faces;
   const int nfl = dim + 1;

@@ -253,7 +253,11 @@ static int lform_bnd_setup(xg_lform* f) {
   const xg_space* sp = f->space;
   const xg_mesh* m = sp->mesh;
   const int64_t nbnd = m->nbnd;
-  if (nbnd >= (1 << 26)) return XG_ERR_CAPACITY;
+  if (nbnd >= (1 << 26)) {
+    set_last_error("xg_lform_create: " + std::to_string(nbnd) +
+                   " boundary elements; boundary terms take at most 2^26 - 1");
+    return XG_ERR_CAPACITY;
+  }
   const int nd = sp->nd;
   std::vector<int32_t> owner((size_t)std::max<int64_t>(nbnd, 1), 0), ptr((size_t)sp->ndof + 1, 0);
   for (int64_t b = 0; b < nbnd; b++) {

@@ -145,3 +145,36 @@ def test_boundary_linear_form(xg, orc):
     f += V3.TestFunction() * xg.dCut(g3, xg.IF, vb=xg.BND)
     with pytest.raises(RuntimeError):
         f.Assemble()
+
+
+@pytest.mark.gpu
+def test_boundary_linear_form_3d(xg, orc):
+    """Boundary terms on tetrahedral meshes: NEG and POS traces of P1-P3 test
+    functions on the boundary triangles (the owner's basis at the physical
+    points of the boundary rule), with and without definedon=bottom, against
+    the oracle's vector within 1e-12 of its largest entry."""
+    m = MakeStructured3DMesh(4)
+    c = m.coords
+    l = orc.interpolate_p1_perturb(c[:, 0] + 0.5 * c[:, 1] - 0.3 * c[:, 2] - 0.45)
+    g = gf_of(xg, m, l)
+    bottom = m.Boundaries("bottom")
+    for k in (1, 2, 3):
+        V = xg.H1(m, order=k)
+        v = V.TestFunction()
+        sp = orc.Space(m, k)
+        for dt in (xg.NEG, xg.POS):
+            cases = [
+                (v * xg.dCut(g, dt, vb=xg.BND), [dict(kind=2, domain=dt)]),
+                (xg.y * v * xg.dCut(g, dt, vb=xg.BND, definedon=bottom),
+                 [dict(kind=2, domain=dt, e=(0, 1, 0), defined_on=bnd_bits(bottom.Mask()))]),
+                (xg.z * v * xg.dCut(g, dt, vb=xg.BND),
+                 [dict(kind=2, domain=dt, e=(0, 0, 1))]),
+            ]
+            for integral, terms in cases:
+                f = xg.LinearForm(V)
+                f += integral
+                f.Assemble()
+                got = f.vec.cpu().numpy()
+                ref = sp.linear_form(l, terms)
+                assert np.max(np.abs(ref)) > 0
+                assert np.max(np.abs(got - ref)) <= 1e-12 * np.max(np.abs(ref)), (k, dt, terms)

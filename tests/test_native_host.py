@@ -36,3 +36,9 @@ def test_moment_tables_reproduce_the_integrands(tmp_path):
 
 def test_patch_basis_change_is_exact(tmp_path):
     _run(tmp_path, "patch_basis_check")
+
+
+def test_edge_and_face_numbering_beyond_2_21_vertices(tmp_path):
+    """xg_mesh_create numbers faces by full sorted vertex triples: vertex
+    numbers up to 2^24 keep every face distinct and the lexicographic order."""
+    _run(tmp_path, "topology_check")
