@@ -32,6 +32,7 @@ UNITS = [
     ("xg_quad_int.cu", []),
     ("xg_mlset.cu", ["-fmad=false"]),
     ("xg_isomesh.cu", ["-fmad=false"]),
+    ("xg_rows.cu", []),
 ]
 
 

@@ -20,6 +20,7 @@
 #include "xg_basis.cuh"
 #include "xg_cut.cuh"
 #include "xg_internal.h"
+#include "xg_rows.h"
 #include "xg_moments.cuh"
 #include "xg_patch.cuh"
 
@@ -306,7 +307,8 @@ __global__ void k_active_facets(int64_t nf, const int32_t* __restrict__ fel, For
 __global__ void k_mark_dofs(int ne, int nd, const int32_t* __restrict__ el_dofs_aos, const int32_t* __restrict__ l_un,
                             const int32_t* __restrict__ l_cut, const int32_t* __restrict__ l_fa,
                             const int* __restrict__ counts, int64_t nf, const int32_t* __restrict__ fel,
-                            uint8_t* __restrict__ dof_flag) {
+                            uint8_t* __restrict__ dof_flag, const int32_t* __restrict__ el_rowslot,
+                            uint8_t* __restrict__ act_slot) {
   const int nun = counts[0], ncut = counts[1], nfa = counts[2];
   const int64_t total = (int64_t)(nun + ncut + 2 * nfa) * nd;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
@@ -320,6 +322,8 @@ __global__ void k_mark_dofs(int ne, int nd, const int32_t* __restrict__ el_dofs_
       e = fel[(q & 1) * nf + l_fa[q >> 1]];
     }
     dof_flag[el_dofs_aos[(int64_t)e * nd + j]] = 1;
+    // spatial scatter: the active element's row slot (xg_rows.h)
+    if (act_slot && item < nun + ncut) act_slot[el_rowslot[(int64_t)e * nd + j]] = 1;
   }
 }
 
@@ -366,6 +370,26 @@ __device__ __forceinline__ void store_entry(T* __restrict__ m, int n, int p, int
     if (sym && p != q) m[q * n + p] = v;
   } else {
     m[tri_index(p, q, n)] = v;
+  }
+}
+// Output of the element and patch kernels.  Compact (rowslot == nullptr):
+// matrix `slot` at m + slot * mat_stride, or at m + slot * n * n with full
+// rows in both precisions (`full`: the patch matrices of spatial forms).  Rows
+// (element rows of spatial forms, xg_rows.h): row p of matrix `key` at
+// m + rowslot[key * n + p] * n, full rows in both precisions.
+template <typename T>
+__device__ __forceinline__ void store_out(T* __restrict__ m, const int32_t* __restrict__ rowslot, int64_t key,
+                                          int64_t slot, int n, int p, int q, T v, bool sym, bool full = false) {
+  if (rowslot) {
+    const int32_t* rs = rowslot + key * n;
+    m[(int64_t)__ldg(&rs[p]) * n + q] = v;
+    if (sym && p != q) m[(int64_t)__ldg(&rs[q]) * n + p] = v;
+  } else if (full) {  // compact, full rows in both precisions
+    T* b = m + slot * (int64_t)n * n;
+    b[p * n + q] = v;
+    if (sym && p != q) b[q * n + p] = v;
+  } else {
+    store_entry<T>(m + slot * mat_stride<T>(n, sym), n, p, q, v, sym);
   }
 }
 template <typename T>
@@ -442,7 +466,8 @@ __global__ void __launch_bounds__(256) k_elmat_uncut(int ne, int nv, const int32
                                                      const double* __restrict__ xyz,
                                                      const uint8_t* __restrict__ dom, FormDesc form, UncutTabs tabs,
                                                      const int32_t* __restrict__ list,
-                                                     const int* __restrict__ counts, T* __restrict__ elmat, int* err) {
+                                                     const int* __restrict__ counts, T* __restrict__ elmat, int* err,
+                                                     const int32_t* __restrict__ rowslot) {
   using C = UnCfg<D, K, SYM, T>;
   constexpr int N = C::N, E = C::E, EPB = C::EPB, NG = D * (D + 1) / 2;
   __shared__ UnGeoS<D> geo[EPB];
@@ -524,7 +549,7 @@ __global__ void __launch_bounds__(256) k_elmat_uncut(int ne, int nv, const int32
       }
       if (K == 3) v = neg_if(v, fn_sign<D, K>(ep[k], G.gv) != fn_sign<D, K>(eq[k], G.gv));
       if (!finite_bits(v)) set_err(err, XG_ERR_NONFINITE);
-      store_entry<T>(elmat + (int64_t)G.slot * mat_stride<T>(N, SYM), N, ep[k], eq[k], (T)v, SYM);
+      store_out<T>(elmat, rowslot, G.elem, G.slot, N, ep[k], eq[k], (T)v, SYM);
     }
   }
 }
@@ -776,7 +801,8 @@ template <int D, int K, bool SYM, typename T>
 __global__ void __launch_bounds__(CutCfg<D, K, SYM, T>::NT) k_elmat_cut(
     int ne, int nv, const int32_t* __restrict__ elv, const double* __restrict__ xyz, const double* __restrict__ lset,
     FormDesc form, const int32_t* __restrict__ list, const int* __restrict__ counts, T* __restrict__ elmat, int* err,
-    int needs_mask, const CutGeoS* __restrict__ cg, const CutSubS* __restrict__ cs, int64_t cap, int first) {
+    int needs_mask, const CutGeoS* __restrict__ cg, const CutSubS* __restrict__ cs, int64_t cap, int first,
+    const int32_t* __restrict__ rowslot) {
   using C = CutCfg<D, K, SYM, T>;
   constexpr int N = C::N, E = C::E, EPB = C::EPB, CH = C::CH, NT = C::NT, NACC = C::NACC, NF = C::NF;
   __shared__ CutGeoS geo[EPB];
@@ -976,7 +1002,7 @@ __global__ void __launch_bounds__(CutCfg<D, K, SYM, T>::NT) k_elmat_cut(
         if (geo[el].elem >= 0) {
           const T v = acc[m].get();
           if (!isfinite(v)) set_err(err, XG_ERR_NONFINITE);
-          store_entry<T>(elmat + (int64_t)geo[el].slot * mat_stride<T>(N, SYM), N, ep[k], eq[k], v, SYM);
+          store_out<T>(elmat, rowslot, geo[el].elem, geo[el].slot, N, ep[k], eq[k], v, SYM);
         }
       }
     }
@@ -1183,7 +1209,7 @@ struct EntGeoS {
   T wdp[kMaxGroups][D + 1];  // d_b phi_p phi_q: cN2 nu_b
   T cM[kMaxGroups], cL[kMaxGroups];
   int act;  // groups whose defined_on holds the element
-  int idx, slot;
+  int idx, slot, elem;
   int gv[D + 1];
 };
 
@@ -1211,7 +1237,8 @@ template <int D, int K, bool SYM, typename T>
 __global__ void __launch_bounds__(kEntNT) k_cut_entries(FormDesc form, MomDesc md, EntTabs tabs,
                                                          const CutGeoS* __restrict__ cg,
                                                          const int* __restrict__ counts, int64_t cap,
-                                                         const T* __restrict__ mu, T* __restrict__ elmat, int* err) {
+                                                         const T* __restrict__ mu, T* __restrict__ elmat, int* err,
+                                                         const int32_t* __restrict__ rowslot) {
   constexpr int N = ndof_el(D, K), E = SYM ? tri_size(N) : N * N;
   __shared__ EntGeoS<D, T> eg[kEntEPB];
   __shared__ unsigned char ep[E], eq[E];
@@ -1272,6 +1299,7 @@ __global__ void __launch_bounds__(kEntNT) k_cut_entries(FormDesc form, MomDesc m
         }
         S.act = act;
         S.slot = C.slot;
+        S.elem = C.elem;
 #pragma unroll
         for (int v = 0; v <= D; v++) S.gv[v] = C.gv[v];
       }
@@ -1299,7 +1327,7 @@ __global__ void __launch_bounds__(kEntNT) k_cut_entries(FormDesc form, MomDesc m
       T r = v.get();
       if (K == 3) r = neg_if(r, fn_sign<D, K>(ep[k], S.gv) != fn_sign<D, K>(eq[k], S.gv));
       if (!finite_bits(r)) set_err(err, XG_ERR_NONFINITE);
-      store_entry<T>(elmat + (int64_t)S.slot * mat_stride<T>(N, SYM), N, ep[k], eq[k], r, SYM);
+      store_out<T>(elmat, rowslot, S.elem, S.slot, N, ep[k], eq[k], r, SYM);
     }
   }
 }
@@ -1481,7 +1509,7 @@ __global__ void k_patch_geo(int ne, int nv, const int32_t* __restrict__ elv, con
 template <int D, int K, typename T>
 __global__ void __launch_bounds__(PaCfg<D, K>::NT) k_patch(
     FormDesc form, const PaGeoS<D, T>* __restrict__ pgeo, const int* __restrict__ counts,
-    T* __restrict__ famat, int64_t cap_fa, int* err) {
+    T* __restrict__ famat, int64_t cap_fa, int* err, int full_rows) {
   using C = PaCfg<D, K>;
   constexpr int N = C::N, N2 = C::N2, E = C::E, FPB = C::FPB, CH = C::CH, NT = C::NT, NACC = C::NACC;
   __shared__ PaGeoS<D, T> geo[FPB];
@@ -1579,7 +1607,7 @@ __global__ void __launch_bounds__(PaCfg<D, K>::NT) k_patch(
           } else {
             const T v = acc[m].get();
             if (!isfinite(v)) set_err(err, XG_ERR_NONFINITE);
-            store_entry<T>(famat + (int64_t)idx * mat_stride<T>(N2, true), N2, ep[k], eq[k], v, true);
+            store_out<T>(famat, nullptr, idx, idx, N2, ep[k], eq[k], v, true, full_rows != 0);
           }
         }
       }
@@ -1640,7 +1668,8 @@ struct PxSmem {
 template <int D, int K, typename T>
 __global__ void __launch_bounds__(256) k_patch_exact(FormDesc form, const PaGeoS<D, T>* __restrict__ pgeo,
                                                       const int* __restrict__ counts, const T* __restrict__ mhat,
-                                                      T* __restrict__ famat, int64_t cap_fa, int* err) {
+                                                      T* __restrict__ famat, int64_t cap_fa, int* err,
+                                                      int full_rows) {
   using C = PxCfg<D, K>;
   using S = PxSmem<D, K, T>;
   constexpr int N = C::N, E = C::E, F = C::FPB, NT = C::NT, NU = C::NU;
@@ -1779,7 +1808,7 @@ __global__ void __launch_bounds__(256) k_patch_exact(FormDesc form, const PaGeoS
       }
       const T r = c * v.get();
       if (!finite_bits(r)) set_err(err, XG_ERR_NONFINITE);
-      store_entry<T>(famat + (int64_t)idx * mat_stride<T>(2 * N, true), 2 * N, a, b, r, true);
+      store_out<T>(famat, nullptr, idx, idx, 2 * N, a, b, r, true, full_rows != 0);
     }
   }
 }
@@ -2432,6 +2461,19 @@ struct xg_form {
   StTimeTabs st_tt = {};  // time sums of the uncut space-time kernel
   std::vector<xg_st_term> st_terms;
   double mt[9] = {1, 0, 0, 0, 0, 0, 0, 0, 0};  // time mass of the time rule (patch factor)
+  // spatial forms: element rows in the row-major layout of xg_rows.h
+  bool rows = false;
+  int32_t* d_el_rowslot = nullptr;  // [ne][nd]
+  uint16_t* d_pos_rows = nullptr;   // [ne * nd][nd]
+  uint16_t* d_nbpos = nullptr;      // [ne * nd * nfl][nd]
+  int32_t* d_cand_fs = nullptr;     // [ne * nd * nfl]
+  uint8_t* d_act_slot = nullptr;    // [ne * nd]
+  int32_t* d_vcols = nullptr;       // [full_nnz]
+  double* d_vvals = nullptr;        // [full_nnz]
+  long long* d_bsum_rows = nullptr;
+  int nbsum_rows = 0;
+  int rows_W = 0, rows_copies = 1, rows_grid = 0;
+  size_t rows_smem = 0;
 };
 
 namespace {
@@ -2443,7 +2485,9 @@ int form_free(xg_form* f) {
                   f->d_tabs, f->d_act_un, f->d_act_cut, f->d_act_fa, f->d_dof_bits, f->d_l_un, f->d_l_cut, f->d_l_fa,
                   f->d_el_slot, f->d_fa_slot, f->d_dof_row, f->d_rowcnt, f->d_counts, f->d_bsum, f->d_bsum64,
                   f->d_elmat, f->d_famat, f->d_err, f->d_dom, f->d_ratio, f->d_bits, f->d_fbits,
-                  f->d_mtab_i, f->d_mtab_c, f->d_mu, f->d_mhat, f->d_cutlist, f->d_dof_flag};
+                  f->d_mtab_i, f->d_mtab_c, f->d_mu, f->d_mhat, f->d_cutlist, f->d_dof_flag,
+                  f->d_el_rowslot, f->d_pos_rows, f->d_nbpos, f->d_cand_fs, f->d_act_slot, f->d_vcols, f->d_vvals,
+                  f->d_bsum_rows};
   for (void* p : ptrs) cudaFree(p);
   delete f;
   return XG_OK;
@@ -2963,8 +3007,9 @@ int launch_volume_sym(xg_form* f, const double* d_lset, const uint8_t* d_dom, cu
     f->grid_mo = grid_for(km, kMomNT, f->mo_smem);
     f->grid_en = grid_for(kn, kEntNT, 0);
   }
+  const int32_t* ers = f->rows ? f->d_el_rowslot : nullptr;  // spatial forms: element rows by row slot
   ku<<<f->grid_el_un, 256, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, d_dom, f->desc, f->tabs, f->d_l_un, f->d_counts,
-                                   (T*)f->d_elmat, f->d_err);
+                                   (T*)f->d_elmat, f->d_err, ers);
   if (f->use_ev) cudaEventRecord(f->ev[3], s);
   k_cut_geo<D><<<152 * 4, 128, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, d_lset, f->desc, f->d_l_cut, f->d_counts,
                                        (CutGeoS*)f->d_cgeo, (CutSubS*)f->d_csub, f->cap_cgeo, f->d_err,
@@ -2972,11 +3017,11 @@ int launch_volume_sym(xg_form* f, const double* d_lset, const uint8_t* d_dom, cu
   km<<<f->grid_mo, kMomNT, f->mo_smem, s>>>(f->md, (const CutGeoS*)f->d_cgeo, (const CutSubS*)f->d_csub,
                                             f->d_counts, f->cap_cgeo, (T*)f->d_mu);
   kn<<<f->grid_en, kEntNT, 0, s>>>(f->desc, f->md, f->ent, (const CutGeoS*)f->d_cgeo, f->d_counts, f->cap_cgeo,
-                                   (const T*)f->d_mu, (T*)f->d_elmat, f->d_err);
+                                   (const T*)f->d_mu, (T*)f->d_elmat, f->d_err, ers);
   // cut elements beyond the workspace (none unless more than cap_cgeo are cut)
   kc<<<f->grid_el_cut, CC::NT, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, d_lset, f->desc, f->d_l_cut, f->d_counts,
                                       (T*)f->d_elmat, f->d_err, f->needs_mask, (const CutGeoS*)f->d_cgeo,
-                                      (const CutSubS*)f->d_csub, f->cap_cgeo, (int)f->cap_cgeo);
+                                      (const CutSubS*)f->d_csub, f->cap_cgeo, (int)f->cap_cgeo, ers);
   if (f->use_ev) cudaEventRecord(f->ev[4], s);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? XG_OK : cuda_fail(e, "k_elmat");
@@ -2995,15 +3040,16 @@ int launch_patch(xg_form* f, cudaStream_t s) {
   auto kp = k_patch<D, K, T>;
   if (!f->grid_fa) f->grid_fa = grid_for(kp, C::NT, 0);
   PaGeoS<D, T>* pg = (PaGeoS<D, T>*)f->d_pgeo;
+  const int frs = f->rows ? 1 : 0;  // spatial forms: full patch rows in both precisions
   k_patch_geo<D, T><<<152 * 8, 128, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, m->nfacets, m->d_facet_els, f->desc,
                                          f->d_l_fa, f->d_counts, pg, f->cap_fa, f->d_err);
   if (f->patch_exact) {
     auto kx = k_patch_exact<D, K, T>;
     const size_t smem = sizeof(PxSmem<D, K, T>);
     kx<<<f->grid_px, PxCfg<D, K>::NT, smem, s>>>(f->desc, pg, f->d_counts, (const T*)f->d_mhat, (T*)f->d_famat,
-                                                 f->cap_fa, f->d_err);
+                                                 f->cap_fa, f->d_err, frs);
   } else {
-    kp<<<f->grid_fa, C::NT, 0, s>>>(f->desc, pg, f->d_counts, (T*)f->d_famat, f->cap_fa, f->d_err);
+    kp<<<f->grid_fa, C::NT, 0, s>>>(f->desc, pg, f->d_counts, (T*)f->d_famat, f->cap_fa, f->d_err, frs);
   }
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? XG_OK : cuda_fail(e, "k_patch");
@@ -3074,17 +3120,61 @@ ScatterArgs scatter_args(xg_form* f) {
   return A;
 }
 
-// active dofs -> rows, then the two scatter passes
-int scatter_phase(xg_form* f, xg_csr* out, cudaStream_t s) {
+RowsArgs rows_args(xg_form* f, const int32_t* rows) {
+  RowsArgs R;
   xg_mesh* m = f->mesh;
+  xg_space* sp = f->space;
+  R.ne = m->ne;
+  R.nd = sp->nd;
+  R.nfl = m->dim + 1;
+  R.n2 = 2 * sp->nd;
+  R.W = f->rows_W;
+  R.copies = f->rows_copies;
+  R.el_dofs = sp->d_el_dofs_aos;
+  R.el_facets = m->d_el_facets_aos;
+  R.fel = m->d_facet_els_aos;
+  R.adj_ptr = sp->d_dof_adj_ptr;
+  R.adj = sp->d_dof_adj;
+  R.l_fa = f->d_l_fa;
+  R.rows = rows;
+  R.dof_row = f->d_dof_row;
+  R.counts = f->d_counts;
+  R.full_ptr = f->d_full_ptr;
+  R.tmp_cols = f->d_tmp_cols;
+  R.el_rowslot = f->d_el_rowslot;
+  R.pos_rows = f->d_pos_rows;
+  R.nbpos = f->has_patch ? f->d_nbpos : nullptr;
+  R.act_slot = f->d_act_slot;
+  R.cand_fs = f->has_patch ? f->d_cand_fs : nullptr;
+  R.vcols = f->d_vcols;
+  R.vvals = f->d_vvals;
+  R.rowcnt = f->d_rowcnt;
+  R.cap_fa = f->cap_fa;
+  R.bsum = f->d_bsum_rows;
+  R.nbsum = f->nbsum_rows;
+  R.err = f->d_err;
+  return R;
+}
+
+// active dofs -> rows (ascending) and dof -> row; spatial forms also mark the
+// row slots of the active elements
+int mark_rows(xg_form* f, xg_csr* out, cudaStream_t s) {
+  xg_mesh* m = f->mesh;
+  xg_space* sp = f->space;
+  k_mark_dofs<<<152 * 8, 256, 0, s>>>(m->ne, sp->nd, sp->d_el_dofs_aos, f->d_l_un, f->d_l_cut, f->d_l_fa,
+                                      f->d_counts, m->nfacets, m->d_facet_els, f->d_dof_flag, f->d_el_rowslot,
+                                      f->rows ? f->d_act_slot : nullptr);
+  k_pack_dofs<<<(unsigned)((f->nw32_dof * 32 + 255) / 256), 256, 0, s>>>(f->d_dof_flag, sp->ndof, f->d_dof_bits,
+                                                                        f->nw32_dof);
+  return compact(f, f->d_dof_bits, f->nw32_dof, out->d_row_dof, f->d_dof_row, f->d_counts + 3, s);
+}
+
+// active dofs -> rows, then the two scatter passes (space-time forms)
+int scatter_phase(xg_form* f, xg_csr* out, cudaStream_t s) {
   xg_space* sp = f->space;
   int st;
   // 3. active dofs -> rows
-  k_mark_dofs<<<152 * 8, 256, 0, s>>>(m->ne, sp->nd, sp->d_el_dofs_aos, f->d_l_un, f->d_l_cut, f->d_l_fa,
-                                      f->d_counts, m->nfacets, m->d_facet_els, f->d_dof_flag);
-  k_pack_dofs<<<(unsigned)((f->nw32_dof * 32 + 255) / 256), 256, 0, s>>>(f->d_dof_flag, sp->ndof, f->d_dof_bits,
-                                                                        f->nw32_dof);
-  if ((st = compact(f, f->d_dof_bits, f->nw32_dof, out->d_row_dof, f->d_dof_row, f->d_counts + 3, s))) return st;
+  if ((st = mark_rows(f, out, s))) return st;
   // 4. pattern and values
   ScatterArgs A = scatter_args(f);
   A.rows = out->d_row_dof;
@@ -3294,9 +3384,11 @@ int full_pattern_build(xg_form* f) {
   const int64_t ndof = sp->ndof;
   const int64_t nd = sp->nd;
   auto A_ = [&](void** p, size_t bytes) { return cudaMalloc(p, bytes ? bytes : 16); };
-  cudaError_t e = A_((void**)&f->d_fpos_el, (size_t)m->ne * nd * nd * 2);
-  if (!e) e = A_((void**)&f->d_pbuf, f->has_patch ? (size_t)f->cap_fa * 2 * nd * nd * 2 : 16);
-  if (!e) e = A_((void**)&f->d_flags, (size_t)f->full_nnz);
+  // the per-row scatter of space-time forms keeps element-column positions by
+  // element; the row layout of spatial forms by row slot (rows_static_build)
+  cudaError_t e = A_(f->rows ? (void**)&f->d_pos_rows : (void**)&f->d_fpos_el, (size_t)m->ne * nd * nd * 2);
+  if (!e && !f->rows) e = A_((void**)&f->d_pbuf, f->has_patch ? (size_t)f->cap_fa * 2 * nd * nd * 2 : 16);
+  if (!e && !f->rows) e = A_((void**)&f->d_flags, (size_t)f->full_nnz);
   int32_t* d_rows = nullptr;
   if (!e) e = A_((void**)&d_rows, sizeof(int32_t) * (size_t)std::max<int64_t>(ndof, 1));
   if (e) {
@@ -3316,8 +3408,16 @@ int full_pattern_build(xg_form* f) {
   ScatterArgs A = scatter_args(f);
   A.rows = d_rows;
   k_row_count<<<f->grid_sc, kRowWarps * 32, f->sc_smem>>>(A, f->d_rowcnt, f->d_err);
-  const int64_t nt = (int64_t)m->ne * nd * nd;
-  k_fpos_el<<<(unsigned)std::min<int64_t>((nt + 255) / 256, 152 * 64), 256>>>(A, f->d_fpos_el, f->d_err);
+  if (f->rows) {
+    const int rst = rows_static_build(rows_args(f, nullptr), f->has_patch, nullptr);
+    if (rst) {
+      cudaFree(d_rows);
+      return rst;
+    }
+  } else {
+    const int64_t nt = (int64_t)m->ne * nd * nd;
+    k_fpos_el<<<(unsigned)std::min<int64_t>((nt + 255) / 256, 152 * 64), 256>>>(A, f->d_fpos_el, f->d_err);
+  }
   e = cudaGetLastError();
   int herr = 0;
   if (!e) e = cudaMemcpy(&herr, f->d_err, sizeof(int), cudaMemcpyDeviceToHost);
@@ -3346,7 +3446,9 @@ int form_workspace(xg_form* f) {
   f->cap_el = m->ne;
   // facet-patch workspace: all facets when small, else a quarter of them
   const int nds = space->nds;  // patch matrices are spatial (space-time forms apply the time factor in the scatter)
-  const size_t fa_stride = precision == XG_PREC_FP64 ? (size_t)(2 * nds) * (2 * nds) : (size_t)tri_size(2 * nds);
+  f->rows = !f->st;
+  const size_t fa_stride = precision == XG_PREC_FP64 || f->rows ? (size_t)(2 * nds) * (2 * nds)
+                                                                 : (size_t)tri_size(2 * nds);
   const size_t fa_bytes = (size_t)m->nfacets * fa_stride * esz;
   f->cap_fa = fa_bytes <= ((size_t)4 << 30) ? m->nfacets : std::max<int64_t>(m->nfacets / 4, 1);
   int64_t maxw = std::max(f->nw32_el, std::max(f->nw32_fa, f->nw32_dof));
@@ -3465,6 +3567,28 @@ int form_workspace(xg_form* f) {
     }
   }
   f->grid_sm = grid_for(k_row_sum<double, false, false, 4>, kRowWarps * 32, f->sm_smem);
+  if (f->rows) {
+    const int64_t ndof = space->ndof, ncand = (int64_t)m->ne * nd * (m->dim + 1);
+    f->rows_W = (f->max_unique + 31) / 32;
+    f->rows_copies = std::min(4, std::max(1, 32 / nd));
+    f->nbsum_rows = (int)((ndof + 2047) / 2048) + 2;
+    e = A((void**)&f->d_el_rowslot, (size_t)m->ne * nd * 4);
+    e = e ? e : A((void**)&f->d_nbpos, f->has_patch ? (size_t)ncand * nd * 2 : 16);
+    e = e ? e : A((void**)&f->d_cand_fs, f->has_patch ? (size_t)ncand * 4 : 16);
+    e = e ? e : A((void**)&f->d_act_slot, (size_t)m->ne * nd);
+    e = e ? e : A((void**)&f->d_vcols, (size_t)f->full_nnz * 4);
+    e = e ? e : A((void**)&f->d_vvals, (size_t)f->full_nnz * 8);
+    e = e ? e : A((void**)&f->d_bsum_rows, (size_t)f->nbsum_rows * 8);
+    if (e == cudaSuccess) e = cudaMemset(f->d_act_slot, 0, (size_t)m->ne * nd);
+    if (e != cudaSuccess) return cuda_fail(e, "xg_form_create");
+    const RowsArgs R = rows_args(f, nullptr);
+    f->rows_smem = rows_accum_smem(R);
+    f->rows_grid = std::min(rows_accum_grid(R, true, f->rows_smem), rows_accum_grid(R, false, f->rows_smem));
+    if (!f->rows_grid) {
+      set_last_error("xg_form_create: row-pass shared memory too large for this mesh");
+      return XG_ERR_CAPACITY;
+    }
+  }
   return full_pattern_build(f);
 }
 
@@ -3528,6 +3652,22 @@ int xg_form_assemble(xg_form* f, const double* d_lset, const uint8_t* d_dom, xg_
     XG_CUDA(cudaMemsetAsync(f->d_counts + 2, 0, sizeof(int), s));
   }
   if (f->use_ev) cudaEventRecord(f->ev[2], s);
+  if (f->rows) {
+    // 2. element rows at their static slots, patch matrices by facet slot;
+    // 3. active rows; 4. fixed-order row sums and the compressed output
+    const bool fp64 = f->precision == XG_PREC_FP64;
+    if ((st = fp64 ? dispatch_volume<double>(f, d_lset, d_dom, s) : dispatch_volume<float>(f, d_lset, d_dom, s)))
+      return st;
+    if (f->has_patch && (st = fp64 ? dispatch_patch<double>(f, s) : dispatch_patch<float>(f, s))) return st;
+    if (f->use_ev) cudaEventRecord(f->ev[5], s);
+    if ((st = mark_rows(f, out, s))) return st;
+    if (f->use_ev) cudaEventRecord(f->ev[6], s);
+    st = rows_scatter(rows_args(f, out->d_row_dof), f->space->ndof, f->has_patch, fp64, f->d_elmat, f->d_famat,
+                      out->d_rowptr, out->d_counts, out->d_cols, out->d_vals, out->cap_nnz, f->rows_grid,
+                      f->rows_smem, s);
+    if (f->use_ev) cudaEventRecord(f->ev[7], s);
+    return st;
+  }
   // 2. element and patch matrices (the cut list's slots follow the uncut list's)
   if (f->precision == XG_PREC_FP64) {
     if ((st = dispatch_volume<double>(f, d_lset, d_dom, s))) return st;
