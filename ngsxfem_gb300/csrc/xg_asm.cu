@@ -425,6 +425,11 @@ struct UncutTabs {
   const double* m[kMaxGroups];  // [E]
   const double* t[kMaxGroups];  // [D(D+1)/2][E] gradient-pair tables, (a<=b) row-major
   const double* c[kMaxGroups];  // [D][E] convection tables (full storage only)
+  // FP32 copies for the mixed form's contractions (spatial forms)
+  const float* mf[kMaxGroups];
+  const float* tf[kMaxGroups];
+  const float* cf[kMaxGroups];
+  int ok_f;  // the FP32 copies exist
 };
 
 // physical-gradient Gram matrix of the barycentric coordinates, G = F^-1 F^-T (a<=b)
@@ -434,6 +439,10 @@ struct UnGeoS {
   double G[D * (D + 1) / 2];
   double beta[kMaxGroups][D];
   double coef[kMaxGroups][5];
+  // FP32 copies for the mixed form's contractions
+  float Gf[D * (D + 1) / 2];
+  float betaf[kMaxGroups][D];
+  float coeff[kMaxGroups][5];
   double meas;
   int gv[D + 1];
   int elem, slot, dom;
@@ -522,9 +531,53 @@ __global__ void __launch_bounds__(256) k_elmat_uncut(int ne, int nv, const int32
               G.beta[q][a] = s;
             }
         }
+        if (sizeof(T) == 4) {  // the mixed form contracts in FP32
+#pragma unroll
+          for (int a = 0; a < D * (D + 1) / 2; a++) G.Gf[a] = (float)G.G[a];
+          for (int q = 0; q < form.ngroups; q++) {
+#pragma unroll
+            for (int kk = 0; kk < 5; kk++) G.coeff[q][kk] = (float)G.coef[q][kk];
+            if (form.g[q].used & (1 << XG_TERM_CONV))
+#pragma unroll
+              for (int a = 0; a < D; a++) G.betaf[q][a] = (float)G.beta[q][a];
+          }
+        }
       }
     }
     __syncthreads();
+    if (sizeof(T) == 4 && tabs.ok_f) {
+      // mixed form: FP32 contractions of the FP32 tables, compensated sum over
+      // the groups' terms
+      for (int t = threadIdx.x; t < EPB * E; t += blockDim.x) {
+        const int le = t / E, k = t % E;
+        const UnGeoS<D>& G = geo[le];
+        if (G.elem < 0) continue;
+        Acc<float> v;
+        v.init();
+        for (int q = 0; q < form.ngroups; q++) {
+          const GroupDesc& Gq = form.g[q];
+          if (Gq.domain != G.dom || (Gq.defined_on && !tbit(Gq.defined_on, G.elem))) continue;
+          if (Gq.used & (1 << XG_TERM_MASS)) v.add(G.coeff[q][0] * __ldg(&tabs.mf[q][k]));
+          if (Gq.used & (1 << XG_TERM_LAPLACE)) {
+            float s = 0.f;
+#pragma unroll
+            for (int a = 0; a < NG; a++) s = fmaf(G.Gf[a], __ldg(&tabs.tf[q][a * E + k]), s);
+            v.add(G.coeff[q][1] * s);
+          }
+          if (Gq.used & (1 << XG_TERM_CONV)) {
+            float s = 0.f;
+#pragma unroll
+            for (int a = 0; a < D; a++) s = fmaf(G.betaf[q][a], __ldg(&tabs.cf[q][a * E + k]), s);
+            v.add(G.coeff[q][4] * s);
+          }
+        }
+        float r = v.get();
+        if (K == 3) r = neg_if(r, fn_sign<D, K>(ep[k], G.gv) != fn_sign<D, K>(eq[k], G.gv));
+        if (!isfinite(r)) set_err(err, XG_ERR_NONFINITE);
+        store_out<T>(elmat, rowslot, G.elem, G.slot, N, ep[k], eq[k], (T)r, SYM);
+      }
+      continue;
+    }
     for (int t = threadIdx.x; t < EPB * E; t += blockDim.x) {
       const int le = t / E, k = t % E;
       const UnGeoS<D>& G = geo[le];
@@ -2395,6 +2448,7 @@ struct xg_form {
   int needs_mask = 0;  // domains needing decompositions on cut elements
   int el_sym = 0;      // every volume group symmetric: packed element matrices
   double* d_tabs = nullptr;  // reference tables of the uncut kernel
+  float* d_tabs_f = nullptr;  // their FP32 copies (mixed form)
   UncutTabs tabs = {};
   MomDesc md = {};              // moment sets of the cut element kernels
   EntTabs ent = {};             // their integer term tables
@@ -2482,7 +2536,7 @@ int form_workspace(xg_form* f);
 
 int form_free(xg_form* f) {
   void* ptrs[] = {f->d_full_ptr, f->d_tmp_cols, f->d_fpos_el, f->d_pbuf, f->d_flags, f->d_pgeo, f->d_cgeo, f->d_csub,
-                  f->d_tabs, f->d_act_un, f->d_act_cut, f->d_act_fa, f->d_dof_bits, f->d_l_un, f->d_l_cut, f->d_l_fa,
+                  f->d_tabs, f->d_tabs_f, f->d_act_un, f->d_act_cut, f->d_act_fa, f->d_dof_bits, f->d_l_un, f->d_l_cut, f->d_l_fa,
                   f->d_el_slot, f->d_fa_slot, f->d_dof_row, f->d_rowcnt, f->d_counts, f->d_bsum, f->d_bsum64,
                   f->d_elmat, f->d_famat, f->d_err, f->d_dom, f->d_ratio, f->d_bits, f->d_fbits,
                   f->d_mtab_i, f->d_mtab_c, f->d_mu, f->d_mhat, f->d_cutlist, f->d_dof_flag,
@@ -2959,15 +3013,24 @@ int upload_tables(xg_form* f) {
   }
   cudaFree(f->d_tabs);
   f->d_tabs = nullptr;
+  cudaFree(f->d_tabs_f);
+  f->d_tabs_f = nullptr;
   std::memset(&f->tabs, 0, sizeof(f->tabs));
   if (!buf.empty()) {
     XG_CUDA(cudaMalloc((void**)&f->d_tabs, buf.size() * sizeof(double)));
     XG_CUDA(cudaMemcpy(f->d_tabs, buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice));
+    std::vector<float> buf_f(buf.begin(), buf.end());
+    XG_CUDA(cudaMalloc((void**)&f->d_tabs_f, buf_f.size() * sizeof(float)));
+    XG_CUDA(cudaMemcpy(f->d_tabs_f, buf_f.data(), buf_f.size() * sizeof(float), cudaMemcpyHostToDevice));
     for (int q = 0; q < f->desc.ngroups; q++) {
       f->tabs.m[q] = offs[q][0] == (size_t)-1 ? nullptr : f->d_tabs + offs[q][0];
       f->tabs.t[q] = offs[q][1] == (size_t)-1 ? nullptr : f->d_tabs + offs[q][1];
       f->tabs.c[q] = offs[q][2] == (size_t)-1 ? nullptr : f->d_tabs + offs[q][2];
+      f->tabs.mf[q] = offs[q][0] == (size_t)-1 ? nullptr : f->d_tabs_f + offs[q][0];
+      f->tabs.tf[q] = offs[q][1] == (size_t)-1 ? nullptr : f->d_tabs_f + offs[q][1];
+      f->tabs.cf[q] = offs[q][2] == (size_t)-1 ? nullptr : f->d_tabs_f + offs[q][2];
     }
+    f->tabs.ok_f = 1;
   }
   return upload_moment_tables(f);
 }

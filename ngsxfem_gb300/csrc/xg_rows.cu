@@ -14,7 +14,8 @@
 //                 copy; the copies are added in a fixed order); every added
 //                 position is flagged, and the flagged columns (global dof
 //                 numbers) and their sums are written compacted at the row's
-//                 full-pattern offset, and counted
+//                 full-pattern offset (the copies merged 32 positions per
+//                 warp instruction), and counted
 //   scan          row pointers of the output
 //   k_rows_copy   warp per active row: the compacted row into the output,
 //                 columns mapped to row numbers.
@@ -33,6 +34,20 @@ constexpr int kSPer = 8;
 constexpr int kSChunk = kSThreads * kSPer;
 constexpr int kQL = 4;          // warp instructions' loads in flight in the accumulation loops
 constexpr int kCandBatch = 128;  // patch-row candidates of a row loaded at once
+
+// FP32 -> FP64 on the integer pipe (GB300 issues the conversion instruction
+// on its narrow FP64 pipe, which the row sums already load).  Exact for
+// normal numbers, zeros, infinities and NaNs; FP32 subnormals (below 1.2e-38
+// in magnitude) become signed zeros.
+__device__ __forceinline__ double to_f64(double x) { return x; }
+__device__ __forceinline__ double to_f64(float x) {
+  const unsigned u = __float_as_uint(x), e = (u >> 23) & 0xffu, sign = u & 0x80000000u;
+  const unsigned m_hi = (u & 0x7fffffu) >> 3, m_lo = u << 29;
+  const unsigned ebits = e == 0xffu ? 0x7ff00000u : (e + 896u) << 20;
+  const unsigned hi = e == 0 ? sign : sign | ebits | m_hi;
+  const unsigned lo = e == 0 ? 0u : m_lo;
+  return __hiloint2double((int)hi, (int)lo);
+}
 
 // position of column c in the sorted full row at fo (length len), -1 if absent
 __device__ __forceinline__ int full_search(const int32_t* __restrict__ cols, int64_t fo, int len, int c) {
@@ -179,17 +194,18 @@ __global__ void __launch_bounds__(kRowsWarps * 32) k_rows_accum(RowsArgs A, cons
         if (on && k < nent) {
           const int64_t a = a0 + k, o = a * ND + jl;
           const bool act = A.act_slot[a] != 0;
-          v[q] = (double)elrows[o];
+          v[q] = to_f64(elrows[o]);
           const int pp = A.pos_rows[o];
           p[q] = act ? pp : -1;
         }
       }
 #pragma unroll
       for (int q = 0; q < kQL; q++)
-        if (p[q] >= 0 && p[q] < len) {
-          acc[cl * LEN + p[q]] += v[q];
-          fl[p[q]] = 1;
-        }
+        if (k0 + q * ce < nent)  // warp-uniform: waves past the row's entries issue no FP64 add
+          if (p[q] >= 0 && p[q] < len) {
+            acc[cl * LEN + p[q]] += v[q];
+            fl[p[q]] = 1;
+          }
     }
     __syncwarp();
     for (int k = lane; k < nent; k += 32) A.act_slot[a0 + k] = 0;  // cleared for the next step
@@ -232,52 +248,61 @@ __global__ void __launch_bounds__(kRowsWarps * 32) k_rows_accum(RowsArgs A, cons
             const int64_t cc = cb + clist[k];
             const int side = (prow % N2) >= ND;
             const int col0 = (h == 0) == (side == 0) ? 0 : ND;  // own half at side * ND
-            v[q] = (double)farows[(int64_t)prow * N2 + col0 + jl];
+            v[q] = to_f64(farows[(int64_t)prow * N2 + col0 + jl]);
             p[q] = h == 0 ? A.pos_rows[(cc / NFL) * ND + jl] : A.nbpos[cc * ND + jl];
           }
         }
 #pragma unroll
         for (int q = 0; q < kQL; q++)
-          if (p[q] >= 0 && p[q] < len) {
-            acc[cl * LEN + p[q]] += v[q];
-            fl[p[q]] = 1;
-          }
+          if (k0 + q * ce < nh)  // warp-uniform, as above
+            if (p[q] >= 0 && p[q] < len) {
+              acc[cl * LEN + p[q]] += v[q];
+              fl[p[q]] = 1;
+            }
       }
       __syncwarp();
     }
     __syncwarp();
-    // flagged columns in ascending order, compacted at the row's full offset
-    // (global dof numbers; k_rows_copy maps them to rows); the copies added
-    // in order and cleared, the flags cleared
-    int base = 0;
+    // flagged columns in ascending order (collected into a position list,
+    // 32 merged per warp instruction), compacted at the row's full offset as
+    // global dof numbers (k_rows_copy maps them to rows); the copies added in
+    // order and cleared, the flags cleared
+    int* plist = clist;  // [2 kCandBatch] (the candidate lists are free here)
+    constexpr int PL = 2 * kCandBatch;
+    int base = 0, nl = 0;
+    auto flush = [&]() {
+      __syncwarp();
+      for (int i = lane; i < nl; i += 32) {
+        const int k = plist[i];
+        const int col = A.tmp_cols[fo + k];
+        double s = acc[k];
+        acc[k] = 0.0;
+        for (int cc = 1; cc < C; cc++) {
+          s += acc[cc * LEN + k];
+          acc[cc * LEN + k] = 0.0;
+        }
+        A.vcols[fo + base + i] = col;
+        A.vvals[fo + base + i] = s;
+      }
+      base += nl;
+      nl = 0;
+      __syncwarp();
+    };
     for (int w0 = 0; w0 < nw; w0 += 4) {
-      bool set[4];
-      int col[4];
+      if (nl > PL - 128) flush();
 #pragma unroll
       for (int u = 0; u < 4; u++) {
         const int k = 32 * (w0 + u) + lane;
-        set[u] = w0 + u < nw && fl[k];
-        col[u] = set[u] ? A.tmp_cols[fo + k] : 0;
-      }
-#pragma unroll
-      for (int u = 0; u < 4; u++) {
-        const unsigned bits = __ballot_sync(0xffffffffu, set[u]);
-        if (set[u]) {
-          const int k = 32 * (w0 + u) + lane;
+        const bool set = w0 + u < nw && fl[k];
+        const unsigned bits = __ballot_sync(0xffffffffu, set);
+        if (set) {
+          plist[nl + __popc(bits & below)] = k;
           fl[k] = 0;
-          double s = acc[k];
-          acc[k] = 0.0;
-          for (int cc = 1; cc < C; cc++) {
-            s += acc[cc * LEN + k];
-            acc[cc * LEN + k] = 0.0;
-          }
-          const int64_t o = fo + base + __popc(bits & below);
-          A.vcols[o] = col[u];
-          A.vvals[o] = s;
         }
-        base += __popc(bits);
+        nl += __popc(bits);
       }
     }
+    flush();
     if (lane == 0) A.rowcnt[row] = base;
     __syncwarp();
     r = r_next;
