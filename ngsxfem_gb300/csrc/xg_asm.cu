@@ -3496,6 +3496,9 @@ int full_pattern_build(xg_form* f) {
   return XG_OK;
 }
 
+// largest compaction scratch of the row scatter (bytes); see xg_rows.h
+constexpr double kRowsScratchBytes = 8.0 * (1 << 30);
+
 // device workspace of a form, sized for the whole mesh
 int form_workspace(xg_form* f) {
   xg_space* space = f->space;
@@ -3639,8 +3642,15 @@ int form_workspace(xg_form* f) {
     e = e ? e : A((void**)&f->d_nbpos, f->has_patch ? (size_t)ncand * nd * 2 : 16);
     e = e ? e : A((void**)&f->d_cand_fs, f->has_patch ? (size_t)ncand * 4 : 16);
     e = e ? e : A((void**)&f->d_act_slot, (size_t)m->ne * nd);
-    e = e ? e : A((void**)&f->d_vcols, (size_t)f->full_nnz * 4);
-    e = e ? e : A((void**)&f->d_vvals, (size_t)f->full_nnz * 8);
+    // compaction scratch by full-pattern offset while it stays modest; larger
+    // forms count their rows first and sum straight into the output
+    double budget = kRowsScratchBytes;
+    // test hook: a smaller budget sends the form through the direct path
+    if (const char* sb = std::getenv("XG_ROWS_SCRATCH_BYTES")) budget = std::atof(sb);
+    if ((double)f->full_nnz * 12.0 <= budget) {
+      e = e ? e : A((void**)&f->d_vcols, (size_t)f->full_nnz * 4);
+      e = e ? e : A((void**)&f->d_vvals, (size_t)f->full_nnz * 8);
+    }
     e = e ? e : A((void**)&f->d_bsum_rows, (size_t)f->nbsum_rows * 8);
     if (e == cudaSuccess) e = cudaMemset(f->d_act_slot, 0, (size_t)m->ne * nd);
     if (e != cudaSuccess) return cuda_fail(e, "xg_form_create");

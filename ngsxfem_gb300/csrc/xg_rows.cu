@@ -19,8 +19,12 @@
 //   scan          row pointers of the output
 //   k_rows_copy   warp per active row: the compacted row into the output,
 //                 columns mapped to row numbers.
+// Forms whose full pattern is too large for the compaction scratch run
+// k_rows_count (the same flags, counted) and the scan first; k_rows_accum
+// then writes each row straight into the output.
 // No atomics touch values: the sums are formed in the same order on every run.
 #include <algorithm>
+#include <map>
 #include <mutex>
 
 #include "xg_internal.h"
@@ -145,9 +149,12 @@ __global__ void __launch_bounds__(256) k_fa_mark(RowsArgs A) {
 
 // ND dofs per element, NFL facets per element (compile time: the index
 // arithmetic of the inner loops divides by them)
-template <typename T, int ND, int NFL>
+template <typename T, int ND, int NFL, bool DIRECT>
 __global__ void __launch_bounds__(kRowsWarps * 32) k_rows_accum(RowsArgs A, const T* __restrict__ elrows,
-                                                                 const T* __restrict__ farows) {
+                                                                 const T* __restrict__ farows,
+                                                                 const int64_t* __restrict__ rowptr,
+                                                                 int32_t* __restrict__ cols, double* __restrict__ vals,
+                                                                 int64_t cap_nnz) {
   constexpr int N2 = 2 * ND;
   extern __shared__ __align__(16) unsigned char sm_acc[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -172,10 +179,13 @@ __global__ void __launch_bounds__(kRowsWarps * 32) k_rows_accum(RowsArgs A, cons
     const int len = (int)(A.full_ptr[r + 1] - fo), nw = (len + 31) >> 5;
     const int a0 = A.adj_ptr[r], a1 = A.adj_ptr[r + 1];
     const int r_next = row + stride < nrows ? A.rows[row + stride] : 0;  // next row's dof, in flight
-    if (nw > A.W) {
+    // DIRECT: the row's place in the output, from the counting pass and the scan
+    const int64_t rp = DIRECT ? rowptr[row] : 0;
+    const int64_t ucnt = DIRECT ? rowptr[row + 1] - rp : 0;
+    if (nw > A.W || (DIRECT && rp + ucnt > cap_nnz)) {
       if (lane == 0) {
         set_err(A.err, XG_ERR_CAPACITY);
-        A.rowcnt[row] = 0;
+        if (!DIRECT) A.rowcnt[row] = 0;
       }
       r = r_next;
       continue;
@@ -281,8 +291,15 @@ __global__ void __launch_bounds__(kRowsWarps * 32) k_rows_accum(RowsArgs A, cons
           s += acc[cc * LEN + k];
           acc[cc * LEN + k] = 0.0;
         }
-        A.vcols[fo + base + i] = col;
-        A.vvals[fo + base + i] = s;
+        if (DIRECT) {
+          if (base + i < ucnt) {
+            cols[rp + base + i] = A.dof_row[col];
+            vals[rp + base + i] = s;
+          }
+        } else {
+          A.vcols[fo + base + i] = col;
+          A.vvals[fo + base + i] = s;
+        }
       }
       base += nl;
       nl = 0;
@@ -303,9 +320,93 @@ __global__ void __launch_bounds__(kRowsWarps * 32) k_rows_accum(RowsArgs A, cons
       }
     }
     flush();
-    if (lane == 0) A.rowcnt[row] = base;
+    if (lane == 0) {
+      if (DIRECT) {
+        if (base != ucnt) set_err(A.err, XG_ERR_CAPACITY);
+      } else {
+        A.rowcnt[row] = base;
+      }
+    }
     __syncwarp();
     r = r_next;
+  }
+}
+
+// Counting pass of the direct path (forms whose full pattern is too large
+// for the compaction scratch): the same positions as k_rows_accum, flagged
+// per row and counted; nothing is cleared (the accumulation pass clears).
+template <int ND, int NFL>
+__global__ void __launch_bounds__(kRowsWarps * 32) k_rows_count(RowsArgs A) {
+  extern __shared__ __align__(16) unsigned char sm_cnt[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int LEN = A.W * 32;
+  int* clist = (int*)sm_cnt + (size_t)warp * (2 * kCandBatch + LEN / 4);
+  int* cpi = clist + kCandBatch;
+  unsigned char* fl = (unsigned char*)(cpi + kCandBatch);
+  for (int k = lane; k < LEN; k += 32) fl[k] = 0;
+  __syncwarp();
+  const int nrows = A.counts[3];
+  const unsigned below = (1u << lane) - 1;
+  for (int row = blockIdx.x * kRowsWarps + warp; row < nrows; row += gridDim.x * kRowsWarps) {
+    const int r = A.rows[row];
+    const int64_t fo = A.full_ptr[r];
+    const int len = (int)(A.full_ptr[r + 1] - fo), nw = (len + 31) >> 5;
+    const int a0 = A.adj_ptr[r], a1 = A.adj_ptr[r + 1];
+    if (nw > A.W) {
+      if (lane == 0) {
+        set_err(A.err, XG_ERR_CAPACITY);
+        A.rowcnt[row] = 0;
+      }
+      continue;
+    }
+    const int n = (a1 - a0) * ND;
+    for (int t = lane; t < n; t += 32) {
+      const int k = t / ND;
+      const int64_t a = a0 + k;
+      if (A.act_slot[a]) {
+        const int p = A.pos_rows[a * ND + (t - k * ND)];
+        if (p < len) fl[p] = 1;
+      }
+    }
+    const int64_t cb = (int64_t)a0 * NFL, cend = A.cand_fs ? (int64_t)a1 * NFL : cb;
+    for (int64_t c0 = cb; c0 < cend; c0 += kCandBatch) {
+      int pi[kCandBatch / 32];
+#pragma unroll
+      for (int u = 0; u < kCandBatch / 32; u++) {
+        const int64_t c = c0 + 32 * u + lane;
+        pi[u] = c < cend ? A.cand_fs[c] : -1;
+      }
+      int nact = 0;
+#pragma unroll
+      for (int u = 0; u < kCandBatch / 32; u++) {
+        const unsigned m = __ballot_sync(0xffffffffu, pi[u] >= 0);
+        if (pi[u] >= 0) {
+          const int k = nact + __popc(m & below);
+          clist[k] = (int)(c0 - cb) + 32 * u + lane;
+          cpi[k] = pi[u];
+        }
+        nact += __popc(m);
+      }
+      __syncwarp();
+      const int nt = nact * 2 * ND;
+      for (int t = lane; t < nt; t += 32) {
+        const int hk = t / ND, j = t - hk * ND, k = hk >> 1;
+        const int64_t cc = cb + clist[k];
+        const int p = (hk & 1) == 0 ? A.pos_rows[(cc / NFL) * ND + j] : A.nbpos[cc * ND + j];
+        if (p < len) fl[p] = 1;
+      }
+      __syncwarp();
+    }
+    __syncwarp();
+    int cnt = 0;
+    for (int w = 0; w < nw; w++) {
+      const int k = 32 * w + lane;
+      const bool set = fl[k] != 0;
+      if (set) fl[k] = 0;
+      cnt += __popc(__ballot_sync(0xffffffffu, set));
+    }
+    if (lane == 0) A.rowcnt[row] = cnt;
+    __syncwarp();
   }
 }
 
@@ -429,17 +530,34 @@ unsigned blocks_for(int64_t n, int64_t cap) {
   return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, cap));
 }
 
-// the accumulation kernel of the element type (dofs per element, facets per element)
-template <typename T>
+// the accumulation / counting kernels of the element type (dofs per element,
+// facets per element)
+template <typename T, bool DIRECT>
 const void* accum_kernel(int nd, int nfl) {
   if (nfl == 3) {
-    if (nd == 3) return (const void*)k_rows_accum<T, 3, 3>;
-    if (nd == 6) return (const void*)k_rows_accum<T, 6, 3>;
-    if (nd == 10) return (const void*)k_rows_accum<T, 10, 3>;
+    if (nd == 3) return (const void*)k_rows_accum<T, 3, 3, DIRECT>;
+    if (nd == 6) return (const void*)k_rows_accum<T, 6, 3, DIRECT>;
+    if (nd == 10) return (const void*)k_rows_accum<T, 10, 3, DIRECT>;
   } else if (nfl == 4) {
-    if (nd == 4) return (const void*)k_rows_accum<T, 4, 4>;
-    if (nd == 10) return (const void*)k_rows_accum<T, 10, 4>;
-    if (nd == 20) return (const void*)k_rows_accum<T, 20, 4>;
+    if (nd == 4) return (const void*)k_rows_accum<T, 4, 4, DIRECT>;
+    if (nd == 10) return (const void*)k_rows_accum<T, 10, 4, DIRECT>;
+    if (nd == 20) return (const void*)k_rows_accum<T, 20, 4, DIRECT>;
+  }
+  return nullptr;
+}
+const void* accum_kernel_of(bool fp64, bool direct, int nd, int nfl) {
+  if (fp64) return direct ? accum_kernel<double, true>(nd, nfl) : accum_kernel<double, false>(nd, nfl);
+  return direct ? accum_kernel<float, true>(nd, nfl) : accum_kernel<float, false>(nd, nfl);
+}
+const void* count_kernel(int nd, int nfl) {
+  if (nfl == 3) {
+    if (nd == 3) return (const void*)k_rows_count<3, 3>;
+    if (nd == 6) return (const void*)k_rows_count<6, 3>;
+    if (nd == 10) return (const void*)k_rows_count<10, 3>;
+  } else if (nfl == 4) {
+    if (nd == 4) return (const void*)k_rows_count<4, 4>;
+    if (nd == 10) return (const void*)k_rows_count<10, 4>;
+    if (nd == 20) return (const void*)k_rows_count<20, 4>;
   }
   return nullptr;
 }
@@ -466,19 +584,25 @@ size_t rows_accum_smem(const RowsArgs& A) {
 }
 
 int rows_accum_grid(const RowsArgs& A, bool fp64, size_t smem) {
-  const void* k = fp64 ? accum_kernel<double>(A.nd, A.nfl) : accum_kernel<float>(A.nd, A.nfl);
-  if (!k) return 0;
+  const bool direct = A.vcols == nullptr;
+  const void* k = accum_kernel_of(fp64, direct, A.nd, A.nfl);
+  const void* kc = count_kernel(A.nd, A.nfl);
+  if (!k || !kc) return 0;
   {
     // the attribute is an upper bound shared by all forms: only ever raise it
     static std::mutex mu;
-    static size_t raised[2] = {48 * 1024, 48 * 1024};
+    static std::map<const void*, size_t> raised;
     std::lock_guard<std::mutex> lock(mu);
-    if (smem > raised[fp64]) {
-      if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
-        cudaGetLastError();
-        return 0;
+    for (const void* kk : {k, kc}) {
+      size_t& cur = raised[kk];
+      if (cur == 0) cur = 48 * 1024;
+      if (smem > cur) {
+        if (cudaFuncSetAttribute(kk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+          cudaGetLastError();
+          return 0;
+        }
+        cur = smem;
       }
-      raised[fp64] = smem;
     }
   }
   return grid_of(k, kRowsWarps * 32, smem);
@@ -487,27 +611,39 @@ int rows_accum_grid(const RowsArgs& A, bool fp64, size_t smem) {
 int rows_scatter(const RowsArgs& A, int64_t ndof, bool has_patch, bool fp64, const void* elrows,
                  const void* farows, int64_t* out_rowptr, int64_t* out_counts, int32_t* cols, double* vals,
                  int64_t cap_nnz, int grid, size_t smem, cudaStream_t s) {
-  if (has_patch) k_fa_mark<<<152 * 8, 256, 0, s>>>(A);
-  {
-    const void* k = fp64 ? accum_kernel<double>(A.nd, A.nfl) : accum_kernel<float>(A.nd, A.nfl);
-    if (!k) {
-      set_last_error("rows_scatter: unsupported element type");
-      return XG_ERR_UNSUPPORTED;
-    }
-    RowsArgs a = A;
-    void* args[] = {&a, const_cast<void**>(&elrows), const_cast<void**>(&farows)};
-    cudaError_t e = cudaLaunchKernel(k, dim3(grid), dim3(kRowsWarps * 32), args, smem, s);
-    if (e != cudaSuccess) return cuda_fail(e, "k_rows_accum");
+  const bool direct = A.vcols == nullptr;  // no compaction scratch: count, scan, then sum into the output
+  const void* k = accum_kernel_of(fp64, direct, A.nd, A.nfl);
+  const void* kc = count_kernel(A.nd, A.nfl);
+  if (!k || !kc) {
+    set_last_error("rows_scatter: unsupported element type");
+    return XG_ERR_UNSUPPORTED;
   }
   const int nb = (int)std::max<int64_t>(1, (ndof + kSChunk - 1) / kSChunk);
   if (nb > A.nbsum) {
     set_last_error("rows_scatter: scan workspace too small");
     return XG_ERR_CAPACITY;
   }
+  if (has_patch) k_fa_mark<<<152 * 8, 256, 0, s>>>(A);
+  RowsArgs a = A;
+  if (direct) {
+    void* cargs[] = {&a};
+    cudaError_t e = cudaLaunchKernel(kc, dim3(grid), dim3(kRowsWarps * 32), cargs, smem, s);
+    if (e != cudaSuccess) return cuda_fail(e, "k_rows_count");
+  }
+  void* args[] = {&a, const_cast<void**>(&elrows), const_cast<void**>(&farows), &out_rowptr, &cols, &vals, &cap_nnz};
+  if (!direct) {
+    cudaError_t e = cudaLaunchKernel(k, dim3(grid), dim3(kRowsWarps * 32), args, smem, s);
+    if (e != cudaSuccess) return cuda_fail(e, "k_rows_accum");
+  }
   k_scan_blocks<<<nb, kSThreads, 0, s>>>(A.rowcnt, A.counts + 3, A.bsum);
   k_scan_top<<<1, 1024, 0, s>>>(A.bsum, nb);
   k_scan_apply<<<nb, kSThreads, 0, s>>>(A.rowcnt, A.counts + 3, A.bsum, out_rowptr, out_counts, cap_nnz, A.err);
-  k_rows_copy<<<152 * 16, 256, 0, s>>>(A, out_rowptr, cols, vals, cap_nnz);
+  if (direct) {
+    cudaError_t e = cudaLaunchKernel(k, dim3(grid), dim3(kRowsWarps * 32), args, smem, s);
+    if (e != cudaSuccess) return cuda_fail(e, "k_rows_accum");
+  } else {
+    k_rows_copy<<<152 * 16, 256, 0, s>>>(A, out_rowptr, cols, vals, cap_nnz);
+  }
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? XG_OK : cuda_fail(e, "rows_scatter");
 }

@@ -58,7 +58,9 @@ struct RowsArgs {
   int32_t* cand_fs;           // [ne * nd * nfl] patch row of a candidate this step, -1 otherwise
                               // (nullptr without patch terms)
   int32_t* vcols;             // [full_nnz] compacted columns (global dofs) of each active row at its full offset
-  double* vvals;              // [full_nnz] compacted values likewise
+  double* vvals;              // [full_nnz] compacted values likewise (both nullptr for forms whose full
+                              // pattern is too large: a counting pass and the scan come first and the
+                              // accumulation pass writes into the output)
   int64_t* rowcnt;            // [ndof] active columns per row
   int64_t cap_fa;
   long long* bsum;            // scan block sums
