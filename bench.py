@@ -851,6 +851,20 @@ class Gpu:
         return {"n_if": int((d == 2).sum()), "n_neg": int((d == 0).sum()), "n_facets": n_fa, "ne": dm.ne,
                 "dim": dm.dim}
 
+    def autotune(self):
+        """xg_form_autotune on every spatial entry (its own level set and
+        output); returns the per-process table."""
+        for e in self.entries:
+            if not e["st"]:
+                self._lib.call("xg_form_autotune", e["form"], ctypes.c_void_p(e["lset"].data_ptr()),
+                               ctypes.byref(e["out"]["csr"]), self.sp)
+        self.torch.cuda.synchronize()
+        L = self._lib.load()
+        need = L.xg_autotune_table(None, 0)
+        buf = ctypes.create_string_buffer(int(need))
+        L.xg_autotune_table(buf, need)
+        return json.loads(buf.value.decode() or "{}")
+
     # --- graph
     def graph(self):
         n = len(self.entries)
@@ -1015,6 +1029,7 @@ def main():
     ap.add_argument("--cpu-baseline", type=int, default=1)
     ap.add_argument("--check", type=int, default=1, help="error of the step against the oracle")
     ap.add_argument("--mixed", type=int, default=1, help="also time the mixed form (fp64 runs)")
+    ap.add_argument("--autotune", type=int, default=1, help="tune the launch choices before timing")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.workload == "c4":
@@ -1040,6 +1055,8 @@ def main():
     cfg = setup(args, gpu)
     E = gpu.entries
     n_cut = sum(e["n_if"] for e in E)
+    if args.autotune:
+        cfg["autotune"] = gpu.autotune()
     gpu.graph()
 
     # ---------------- device-resident timing (graph replay) ----------------
@@ -1123,6 +1140,8 @@ def main():
         a2.precision = "mixed"
         gm = Gpu(a2)
         setup(a2, gm)
+        if args.autotune:
+            gm.autotune()
         gm.graph()
         if ws > 1:
             torch.distributed.barrier()

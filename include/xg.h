@@ -463,12 +463,33 @@ int xg_learned_moments_tet(xg_mlp* mlp, const double* d_vals10, int64_t n, doubl
  * distinct forms must write distinct outputs.  Stage events are off inside the
  * graph.  Check each form with xg_form_check after a launch. */
 typedef struct xg_step_graph xg_step_graph;
+/* Spatial forms whose patch matrices come from the basis-change kernel (patch
+ * terms of order >= 2k), taking one step each in the graph, share one
+ * persistent launch for those matrices: work items (form, batch of facets)
+ * from a queue ordered by decreasing cost per item, taken by the blocks from
+ * an atomic counter (work stealing); the matrices are bit-identical to the
+ * per-form kernel's. */
 int xg_step_graph_create(xg_form* const* forms, const double* const* d_lsets, const xg_csr* outs, int32_t n,
                          xg_step_graph** out);
 int xg_step_graph_launch(xg_step_graph* graph, void* stream);
 /* Number of kernel nodes of the graph (the kernels one launch runs). */
 int xg_step_graph_kernel_count(const xg_step_graph* graph, int64_t* h_out);
 int xg_step_graph_destroy(xg_step_graph* graph);
+
+/* ---- autotuner --------------------------------------------------------------- */
+/* No counterpart in the reference.  Times, on this form and level set
+ * (d_lset, output out as for xg_cutfem_step; several steps run), the launch
+ * choices of the spatial step per (device, dimension, order, precision):
+ * elements per block of the uncut element kernel (16, 32), rows per block of
+ * the row passes (4, 8, 16 warps) and accumulator copies of the row sums (1..4,
+ * which fix their summation order: every choice is deterministic), blocks per
+ * SM of the basis-change patch kernel; keeps the fastest of each (median of
+ * three timed steps of its stage) in a per-process table that forms created
+ * later with the same key use.  Space-time forms: nothing to tune (XG_OK). */
+int xg_form_autotune(xg_form* form, const double* d_lset, xg_csr* out, void* stream);
+/* The table as JSON text into buf (cap bytes, NUL-terminated, truncated if
+ * short); returns the bytes the full text needs. */
+int64_t xg_autotune_table(char* buf, int64_t cap);
 
 #ifdef __cplusplus
 }

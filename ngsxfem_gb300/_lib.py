@@ -33,7 +33,7 @@ EXPORTS = [
     "xg_form_assemble", "xg_form_check", "xg_form_stage_events", "xg_cutfem_step", "xg_cutfem_marking",
     "xg_space_create_st", "xg_space_info_st", "xg_cutinfo_update_st", "xg_st_cut_rules", "xg_st_form_create",
     "xg_st_cutfem_step", "xg_step_graph_create", "xg_step_graph_launch", "xg_step_graph_destroy",
-    "xg_step_graph_kernel_count", "xg_iso_moments_tet", "xg_mlp_param_count", "xg_learned_points",
+    "xg_step_graph_kernel_count", "xg_form_autotune", "xg_autotune_table", "xg_iso_moments_tet", "xg_mlp_param_count", "xg_learned_points",
     "xg_mlp_create", "xg_mlp_destroy", "xg_mlp_get_params", "xg_mlp_set_params", "xg_mlp_forward",
     "xg_mlp_loss_grad", "xg_mlp_adam_step", "xg_learned_moments_tet", "xg_learned_features",
     "xg_cutinfo_update_bnd", "xg_mesh_boundary", "xg_cutinfo_nodes", "xg_elements_with_threshold",
@@ -149,6 +149,8 @@ def load():
         "xg_step_graph_launch": (I, [P, P]),
         "xg_step_graph_destroy": (I, [P]),
         "xg_step_graph_kernel_count": (I, [P, P]),
+        "xg_form_autotune": (I, [P, P, P, P]),
+        "xg_autotune_table": (I64, [P, I64]),
         "xg_iso_moments_tet": (I, [P, I64, I, I, P, P, P]),
         "xg_mlp_param_count": (I, [P]),
         "xg_learned_points": (I, [P]),

@@ -448,11 +448,12 @@ struct UnGeoS {
   int elem, slot, dom;
 };
 
-template <int D, int K, bool SYM, typename T>
+// EPB: elements per block (the autotuner's choice among kUncutEpb)
+template <int D, int K, bool SYM, typename T, int EPB_ = 32>
 struct UnCfg {
   static constexpr int N = ndof_el(D, K);
   static constexpr int E = SYM ? tri_size(N) : N * N;
-  static constexpr int EPB = 32;
+  static constexpr int EPB = EPB_;
   static constexpr int NT = 256;
 };
 
@@ -470,14 +471,14 @@ __device__ __forceinline__ int fn_sign(int i, const int* gv) {
   return gv[a] < gv[b] ? 1 : -1;
 }
 
-template <int D, int K, bool SYM, typename T>
+template <int D, int K, bool SYM, typename T, int EPB_>
 __global__ void __launch_bounds__(256) k_elmat_uncut(int ne, int nv, const int32_t* __restrict__ elv,
                                                      const double* __restrict__ xyz,
                                                      const uint8_t* __restrict__ dom, FormDesc form, UncutTabs tabs,
                                                      const int32_t* __restrict__ list,
                                                      const int* __restrict__ counts, T* __restrict__ elmat, int* err,
                                                      const int32_t* __restrict__ rowslot) {
-  using C = UnCfg<D, K, SYM, T>;
+  using C = UnCfg<D, K, SYM, T, EPB_>;
   constexpr int N = C::N, E = C::E, EPB = C::EPB, NG = D * (D + 1) / 2;
   __shared__ UnGeoS<D> geo[EPB];
   __shared__ unsigned char ep[E], eq[E];
@@ -1718,16 +1719,25 @@ struct PxSmem {
   unsigned char ep[E], eq[E];
 };
 
+// One form's share of the basis-change patch work.
+template <int D, typename T>
+struct PxJob {
+  const PaGeoS<D, T>* pgeo;
+  const int* counts;  // [2] active facets
+  const T* mhat;      // reference mass matrix of the element's order
+  T* famat;
+  int64_t cap_fa;
+  int* err;
+  int full_rows;
+  int npatch;
+  int K;
+};
+
+// per-block tables of the order: entry order, Mh, rows by canonical degree
 template <int D, int K, typename T>
-__global__ void __launch_bounds__(256) k_patch_exact(FormDesc form, const PaGeoS<D, T>* __restrict__ pgeo,
-                                                      const int* __restrict__ counts, const T* __restrict__ mhat,
-                                                      T* __restrict__ famat, int64_t cap_fa, int* err,
-                                                      int full_rows) {
+__device__ void px_init(PxSmem<D, K, T>& sm, const T* __restrict__ mhat) {
   using C = PxCfg<D, K>;
-  using S = PxSmem<D, K, T>;
-  constexpr int N = C::N, E = C::E, F = C::FPB, NT = C::NT, NU = C::NU;
-  extern __shared__ __align__(16) unsigned char px_raw[];
-  S& sm = *reinterpret_cast<S*>(px_raw);
+  constexpr int N = C::N, NT = C::NT;
   entry_tables(2 * N, true, sm.ep, sm.eq);
   for (int t = threadIdx.x; t < N * N; t += NT) sm.Mh[t / N][t % N] = mhat[t];
   if (threadIdx.x == 0) {
@@ -1739,130 +1749,209 @@ __global__ void __launch_bounds__(256) k_patch_exact(FormDesc form, const PaGeoS
       sm.cnt[d] = n;
     }
   }
+}
+
+// the patch matrices of F facets (batch `batch` of the job's active facets);
+// the block's tables must hold the job's order (px_init)
+template <int D, int K, typename T>
+__device__ void px_batch(const PxJob<D, T>& J, int batch, PxSmem<D, K, T>& sm) {
+  using C = PxCfg<D, K>;
+  constexpr int N = C::N, E = C::E, F = C::FPB, NU = C::NU;
   const int f = threadIdx.x % F, u0 = threadIdx.x / F;
-  const int count = counts[2];
-  for (int batch = blockIdx.x; batch * F < count; batch += gridDim.x) {
-    __syncthreads();
-    if (threadIdx.x < F) {
-      const int idx = batch * F + threadIdx.x;
-      const bool ok = idx < count && idx < cap_fa;
-      sm.idx[threadIdx.x] = ok ? idx : -1;
-      if (ok) {
-        const PaGeoS<D, T>& G = pgeo[idx];
+  const int count = J.counts[2];
+  const int64_t cap_fa = J.cap_fa;
+  const PaGeoS<D, T>* __restrict__ pgeo = J.pgeo;
+  __syncthreads();
+  if (threadIdx.x < F) {
+    const int idx = batch * F + threadIdx.x;
+    const bool ok = idx < count && idx < cap_fa;
+    sm.idx[threadIdx.x] = ok ? idx : -1;
+    if (ok) {
+      const PaGeoS<D, T>& G = pgeo[idx];
 #pragma unroll
-        for (int i = 0; i <= D; i++)
+      for (int i = 0; i <= D; i++)
 #pragma unroll
-          for (int b = 0; b <= D; b++) {
-            sm.pre.L[0][i][b][threadIdx.x] = G.L21[i][b];
-            sm.pre.L[1][i][b][threadIdx.x] = G.L12[i][b];
-          }
-        sm.det1[threadIdx.x] = G.det1;
-        sm.det2[threadIdx.x] = G.det2;
-        T c = 0;
-        for (int pp = 0; pp < form.npatch; pp++) c += G.coef[pp];
-        sm.c[threadIdx.x] = c;
-#pragma unroll
-        for (int v = 0; v <= D; v++) {
-          sm.gv1[v][threadIdx.x] = G.gv1[v];
-          sm.gv2[v][threadIdx.x] = G.gv2[v];
+        for (int b = 0; b <= D; b++) {
+          sm.pre.L[0][i][b][threadIdx.x] = G.L21[i][b];
+          sm.pre.L[1][i][b][threadIdx.x] = G.L12[i][b];
         }
+      sm.det1[threadIdx.x] = G.det1;
+      sm.det2[threadIdx.x] = G.det2;
+      T c = 0;
+      for (int pp = 0; pp < J.npatch; pp++) c += G.coef[pp];
+      sm.c[threadIdx.x] = c;
+#pragma unroll
+      for (int v = 0; v <= D; v++) {
+        sm.gv1[v][threadIdx.x] = G.gv1[v];
+        sm.gv2[v][threadIdx.x] = G.gv2[v];
       }
     }
-    __syncthreads();
-    const bool live = sm.idx[f] >= 0;
-    // images of the canonical nodes under the barycentric maps
-    for (int u = u0; u < 2 * N; u += NU) {
-      const int sd = u / N, n = u % N;
-      if (!live) continue;
-      T out[D + 1];
-      node_image<D, K, T>(n, &sm.pre.L[sd][0][0][f], (D + 1) * F, F, out);
+  }
+  __syncthreads();
+  const bool live = sm.idx[f] >= 0;
+  // images of the canonical nodes under the barycentric maps
+  for (int u = u0; u < 2 * N; u += NU) {
+    const int sd = u / N, n = u % N;
+    if (!live) continue;
+    T out[D + 1];
+    node_image<D, K, T>(n, &sm.pre.L[sd][0][0][f], (D + 1) * F, F, out);
 #pragma unroll
-      for (int i = 0; i <= D; i++) sm.pre.nodes[sd][n][i][f] = out[i];
+    for (int i = 0; i <= D; i++) sm.pre.nodes[sd][n][i][f] = out[i];
+  }
+  __syncthreads();
+  // column j of C: function j of the other element in this element's canonical basis
+  for (int u = u0; u < 2 * N; u += NU) {
+    const int sd = u / N, j = u % N;
+    if (!live) continue;
+    int gv[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int v = 0; v <= D; v++) gv[v] = sd == 0 ? sm.gv2[v][f] : sm.gv1[v][f];
+    const int desc = fn_desc<D, K>(j, gv);
+    T p[N];
+#pragma unroll
+    for (int n = 0; n < N; n++) {
+      T lam[D + 1];
+#pragma unroll
+      for (int i = 0; i <= D; i++) lam[i] = sm.pre.nodes[sd][n][i][f];
+      p[n] = eval_fn_value<D, T>(desc, lam);
     }
-    __syncthreads();
-    // column j of C: function j of the other element in this element's canonical basis
-    for (int u = u0; u < 2 * N; u += NU) {
-      const int sd = u / N, j = u % N;
-      if (!live) continue;
-      int gv[4] = {0, 0, 0, 0};
-#pragma unroll
-      for (int v = 0; v <= D; v++) gv[v] = sd == 0 ? sm.gv2[v][f] : sm.gv1[v][f];
-      const int desc = fn_desc<D, K>(j, gv);
-      T p[N];
-#pragma unroll
-      for (int n = 0; n < N; n++) {
-        T lam[D + 1];
-#pragma unroll
-        for (int i = 0; i <= D; i++) lam[i] = sm.pre.nodes[sd][n][i][f];
-        p[n] = eval_fn_value<D, T>(desc, lam);
-      }
-      nodal_to_hier<D, K, T>(p, fn_degree(desc), &sm.Ct[sd][0][j][f], N * F);
+    nodal_to_hier<D, K, T>(p, fn_degree(desc), &sm.Ct[sd][0][j][f], N * F);
+  }
+  __syncthreads();
+  // W = Mh C over the rows of degree <= the column's degree (the others are 0)
+  for (int u = u0; u < 2 * N * N; u += NU) {
+    const int r = u % N, j = (u / N) % N, sd = u / (N * N);
+    if (!live) continue;
+    const int nk = sm.cnt[canon_degree<D, K>(j)];
+    T s = 0;
+    for (int i = 0; i < nk; i++) {
+      const int k = sm.perm[i];
+      s += sm.Mh[r][k] * sm.Ct[sd][k][j][f];
     }
-    __syncthreads();
-    // W = Mh C over the rows of degree <= the column's degree (the others are 0)
-    for (int u = u0; u < 2 * N * N; u += NU) {
-      const int r = u % N, j = (u / N) % N, sd = u / (N * N);
-      if (!live) continue;
-      const int nk = sm.cnt[canon_degree<D, K>(j)];
+    sm.Wt[sd][r][j][f] = s;
+  }
+  __syncthreads();
+  if (!live) return;
+  const int idx = sm.idx[f];
+  const T det1 = sm.det1[f], det2 = sm.det2[f], c = sm.c[f];
+  for (int k = u0; k < E; k += NU) {
+    const int a = sm.ep[k], b = sm.eq[k];
+    Acc<T> v;
+    v.init();
+    if (b < N) {  // (1,1)
+      int g1[4] = {0, 0, 0, 0};
+#pragma unroll
+      for (int q = 0; q <= D; q++) g1[q] = sm.gv1[q][f];
+      const bool flip = K == 3 && fn_sign<D, K>(a, g1) != fn_sign<D, K>(b, g1);
+      v.add(det1 * neg_if(sm.Mh[a][b], flip));
+      const int nk = sm.cnt[canon_degree<D, K>(a)];
       T s = 0;
       for (int i = 0; i < nk; i++) {
-        const int k = sm.perm[i];
-        s += sm.Mh[r][k] * sm.Ct[sd][k][j][f];
+        const int kk = sm.perm[i];
+        s += sm.Ct[1][kk][a][f] * sm.Wt[1][kk][b][f];
       }
-      sm.Wt[sd][r][j][f] = s;
+      v.add(det2 * s);
+    } else if (a < N) {  // (1,2)
+      const int bb = b - N;
+      int g1[4] = {0, 0, 0, 0}, g2[4] = {0, 0, 0, 0};
+#pragma unroll
+      for (int q = 0; q <= D; q++) {
+        g1[q] = sm.gv1[q][f];
+        g2[q] = sm.gv2[q][f];
+      }
+      const T w1 = neg_if(sm.Wt[0][a][bb][f], K == 3 && fn_sign<D, K>(a, g1) < 0);
+      const T w2 = neg_if(sm.Wt[1][bb][a][f], K == 3 && fn_sign<D, K>(bb, g2) < 0);
+      v.add(neg_if(det1 * w1, true));
+      v.add(neg_if(det2 * w2, true));
+    } else {  // (2,2)
+      const int aa = a - N, bb = b - N;
+      const int nk = sm.cnt[canon_degree<D, K>(aa)];
+      T s = 0;
+      for (int i = 0; i < nk; i++) {
+        const int kk = sm.perm[i];
+        s += sm.Ct[0][kk][aa][f] * sm.Wt[0][kk][bb][f];
+      }
+      v.add(det1 * s);
+      int g2[4] = {0, 0, 0, 0};
+#pragma unroll
+      for (int q = 0; q <= D; q++) g2[q] = sm.gv2[q][f];
+      const bool flip = K == 3 && fn_sign<D, K>(aa, g2) != fn_sign<D, K>(bb, g2);
+      v.add(det2 * neg_if(sm.Mh[aa][bb], flip));
     }
+    const T r = c * v.get();
+    if (!finite_bits(r)) set_err(J.err, XG_ERR_NONFINITE);
+    store_out<T>(J.famat, nullptr, idx, idx, 2 * N, a, b, r, true, J.full_rows != 0);
+  }
+}
+
+template <int D, int K, typename T>
+__global__ void __launch_bounds__(256) k_patch_exact(PxJob<D, T> J) {
+  using S = PxSmem<D, K, T>;
+  extern __shared__ __align__(16) unsigned char px_raw[];
+  S& sm = *reinterpret_cast<S*>(px_raw);
+  px_init<D, K, T>(sm, J.mhat);
+  constexpr int F = PxCfg<D, K>::FPB;
+  for (int batch = blockIdx.x; batch * F < J.counts[2]; batch += gridDim.x) px_batch<D, K, T>(J, batch, sm);
+}
+
+// Several forms' patch matrices in one persistent launch (batched steps of
+// several forms): the work items are (form, batch of facets), enumerated in
+// the jobs' order -- the host sorts the jobs by decreasing cost per item, so
+// the queue is cost-sorted and the most expensive items start first -- and
+// every block takes its next item from a global counter (work stealing), so
+// blocks that drew cheap items take more of them.  Each item is the same
+// px_batch work as k_patch_exact: the results are bit-identical.
+constexpr int kMaxPxJobs = 16;
+template <int D, typename T>
+struct PxJobs {
+  PxJob<D, T> job[kMaxPxJobs];
+  int n;
+  int* queue;  // item counter, zero at launch
+};
+
+template <int D, typename T>
+__global__ void __launch_bounds__(256) k_patch_exact_multi(const __grid_constant__ PxJobs<D, T> Q) {
+  extern __shared__ __align__(16) unsigned char px_raw[];
+  __shared__ long long first[kMaxPxJobs + 1];
+  __shared__ int item_s;
+  if (threadIdx.x == 0) {
+    long long acc = 0;
+    for (int j = 0; j < Q.n; j++) {
+      first[j] = acc;
+      const int K = Q.job[j].K;
+      const int F = K == 1 ? PxCfg<D, 1>::FPB : (K == 2 ? PxCfg<D, 2>::FPB : PxCfg<D, 3>::FPB);
+      const long long cnt = min((long long)Q.job[j].counts[2], (long long)Q.job[j].cap_fa);
+      acc += (cnt + F - 1) / F;
+    }
+    first[Q.n] = acc;
+  }
+  __syncthreads();
+  const long long total = first[Q.n];
+  int cur = -1;
+  for (;;) {
     __syncthreads();
-    if (!live) continue;
-    const int idx = sm.idx[f];
-    const T det1 = sm.det1[f], det2 = sm.det2[f], c = sm.c[f];
-    for (int k = u0; k < E; k += NU) {
-      const int a = sm.ep[k], b = sm.eq[k];
-      Acc<T> v;
-      v.init();
-      if (b < N) {  // (1,1)
-        int g1[4] = {0, 0, 0, 0};
-#pragma unroll
-        for (int q = 0; q <= D; q++) g1[q] = sm.gv1[q][f];
-        const bool flip = K == 3 && fn_sign<D, K>(a, g1) != fn_sign<D, K>(b, g1);
-        v.add(det1 * neg_if(sm.Mh[a][b], flip));
-        const int nk = sm.cnt[canon_degree<D, K>(a)];
-        T s = 0;
-        for (int i = 0; i < nk; i++) {
-          const int kk = sm.perm[i];
-          s += sm.Ct[1][kk][a][f] * sm.Wt[1][kk][b][f];
-        }
-        v.add(det2 * s);
-      } else if (a < N) {  // (1,2)
-        const int bb = b - N;
-        int g1[4] = {0, 0, 0, 0}, g2[4] = {0, 0, 0, 0};
-#pragma unroll
-        for (int q = 0; q <= D; q++) {
-          g1[q] = sm.gv1[q][f];
-          g2[q] = sm.gv2[q][f];
-        }
-        const T w1 = neg_if(sm.Wt[0][a][bb][f], K == 3 && fn_sign<D, K>(a, g1) < 0);
-        const T w2 = neg_if(sm.Wt[1][bb][a][f], K == 3 && fn_sign<D, K>(bb, g2) < 0);
-        v.add(neg_if(det1 * w1, true));
-        v.add(neg_if(det2 * w2, true));
-      } else {  // (2,2)
-        const int aa = a - N, bb = b - N;
-        const int nk = sm.cnt[canon_degree<D, K>(aa)];
-        T s = 0;
-        for (int i = 0; i < nk; i++) {
-          const int kk = sm.perm[i];
-          s += sm.Ct[0][kk][aa][f] * sm.Wt[0][kk][bb][f];
-        }
-        v.add(det1 * s);
-        int g2[4] = {0, 0, 0, 0};
-#pragma unroll
-        for (int q = 0; q <= D; q++) g2[q] = sm.gv2[q][f];
-        const bool flip = K == 3 && fn_sign<D, K>(aa, g2) != fn_sign<D, K>(bb, g2);
-        v.add(det2 * neg_if(sm.Mh[aa][bb], flip));
-      }
-      const T r = c * v.get();
-      if (!finite_bits(r)) set_err(err, XG_ERR_NONFINITE);
-      store_out<T>(famat, nullptr, idx, idx, 2 * N, a, b, r, true, full_rows != 0);
+    if (threadIdx.x == 0) item_s = atomicAdd(Q.queue, 1);
+    __syncthreads();
+    const long long item = item_s;
+    if (item >= total) break;
+    int j = 0;
+    while (item >= first[j + 1]) j++;
+    const int batch = (int)(item - first[j]);
+    const PxJob<D, T>& J = Q.job[j];
+    if (J.K == 1) {
+      auto& sm = *reinterpret_cast<PxSmem<D, 1, T>*>(px_raw);
+      if (cur != j) px_init<D, 1, T>(sm, J.mhat);
+      px_batch<D, 1, T>(J, batch, sm);
+    } else if (J.K == 2) {
+      auto& sm = *reinterpret_cast<PxSmem<D, 2, T>*>(px_raw);
+      if (cur != j) px_init<D, 2, T>(sm, J.mhat);
+      px_batch<D, 2, T>(J, batch, sm);
+    } else {
+      auto& sm = *reinterpret_cast<PxSmem<D, 3, T>*>(px_raw);
+      if (cur != j) px_init<D, 3, T>(sm, J.mhat);
+      px_batch<D, 3, T>(J, batch, sm);
     }
+    cur = j;
   }
 }
 
@@ -2517,6 +2606,7 @@ struct xg_form {
   double mt[9] = {1, 0, 0, 0, 0, 0, 0, 0, 0};  // time mass of the time rule (patch factor)
   // spatial forms: element rows in the row-major layout of xg_rows.h
   bool rows = false;
+  bool defer_patch = false;  // batched graph: the basis-change patch kernel runs for several forms at once
   int32_t* d_el_rowslot = nullptr;  // [ne][nd]
   uint16_t* d_pos_rows = nullptr;   // [ne * nd][nd]
   uint16_t* d_nbpos = nullptr;      // [ne * nd * nfl][nd]
@@ -2526,13 +2616,19 @@ struct xg_form {
   double* d_vvals = nullptr;        // [full_nnz]
   long long* d_bsum_rows = nullptr;
   int nbsum_rows = 0;
-  int rows_W = 0, rows_copies = 1, rows_grid = 0;
+  int rows_W = 0, rows_copies = 1, rows_grid = 0, rows_warps = 8;
   size_t rows_smem = 0;
+  // launch configuration chosen by the autotuner (xg_form_autotune)
+  int tune_uncut_epb = 32;  // uncut elements per block: 16 or 32
+  int grid_el_un16 = 0;
+  int px_bps = 0;           // blocks per SM of the basis-change patch kernel (0: occupancy)
+  int px_occ = 1;           // its occupancy limit (blocks per SM)
 };
 
 namespace {
 
 int form_workspace(xg_form* f);
+int apply_cached_tune(xg_form* f);
 
 int form_free(xg_form* f) {
   void* ptrs[] = {f->d_full_ptr, f->d_tmp_cols, f->d_fpos_el, f->d_pbuf, f->d_flags, f->d_pgeo, f->d_cgeo, f->d_csub,
@@ -2798,6 +2894,7 @@ int patch_exact_setup(xg_form* f) {
   const size_t smem = sizeof(PxSmem<D, K, T>);
   XG_CUDA(cudaFuncSetAttribute(kx, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   f->grid_px = grid_for(kx, PxCfg<D, K>::NT, smem);
+  f->px_occ = std::max(1, f->grid_px / 152);
   return XG_OK;
 }
 
@@ -3060,19 +3157,25 @@ template <int D, int K, bool SYM, typename T>
 int launch_volume_sym(xg_form* f, const double* d_lset, const uint8_t* d_dom, cudaStream_t s) {
   using CC = CutCfg<D, K, SYM, T>;
   xg_mesh* m = f->mesh;
-  auto ku = k_elmat_uncut<D, K, SYM, T>;
+  auto ku = k_elmat_uncut<D, K, SYM, T, 32>;
+  auto ku16 = k_elmat_uncut<D, K, SYM, T, 16>;
   auto kc = k_elmat_cut<D, K, SYM, T>;
   auto km = k_cut_moments<D, T>;
   auto kn = k_cut_entries<D, K, SYM, T>;
   if (!f->grid_el_un) {
     f->grid_el_un = grid_for(ku, 256, 0);
+    f->grid_el_un16 = grid_for(ku16, 256, 0);
     f->grid_el_cut = grid_for(kc, CC::NT, 0);
     f->grid_mo = grid_for(km, kMomNT, f->mo_smem);
     f->grid_en = grid_for(kn, kEntNT, 0);
   }
   const int32_t* ers = f->rows ? f->d_el_rowslot : nullptr;  // spatial forms: element rows by row slot
-  ku<<<f->grid_el_un, 256, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, d_dom, f->desc, f->tabs, f->d_l_un, f->d_counts,
-                                   (T*)f->d_elmat, f->d_err, ers);
+  if (f->tune_uncut_epb == 16)
+    ku16<<<f->grid_el_un16, 256, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, d_dom, f->desc, f->tabs, f->d_l_un,
+                                         f->d_counts, (T*)f->d_elmat, f->d_err, ers);
+  else
+    ku<<<f->grid_el_un, 256, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, d_dom, f->desc, f->tabs, f->d_l_un,
+                                     f->d_counts, (T*)f->d_elmat, f->d_err, ers);
   if (f->use_ev) cudaEventRecord(f->ev[3], s);
   k_cut_geo<D><<<152 * 4, 128, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, d_lset, f->desc, f->d_l_cut, f->d_counts,
                                        (CutGeoS*)f->d_cgeo, (CutSubS*)f->d_csub, f->cap_cgeo, f->d_err,
@@ -3096,6 +3199,21 @@ int launch_volume(xg_form* f, const double* d_lset, const uint8_t* d_dom, cudaSt
                    : launch_volume_sym<D, K, false, T>(f, d_lset, d_dom, s);
 }
 
+template <int D, typename T>
+PxJob<D, T> px_job(xg_form* f) {
+  PxJob<D, T> J;
+  J.pgeo = (const PaGeoS<D, T>*)f->d_pgeo;
+  J.counts = f->d_counts;
+  J.mhat = (const T*)f->d_mhat;
+  J.famat = (T*)f->d_famat;
+  J.cap_fa = f->cap_fa;
+  J.err = f->d_err;
+  J.full_rows = f->rows ? 1 : 0;  // spatial forms: full patch rows in both precisions
+  J.npatch = f->desc.npatch;
+  J.K = f->space->order;
+  return J;
+}
+
 template <int D, int K, typename T>
 int launch_patch(xg_form* f, cudaStream_t s) {
   using C = PaCfg<D, K>;
@@ -3107,10 +3225,13 @@ int launch_patch(xg_form* f, cudaStream_t s) {
   k_patch_geo<D, T><<<152 * 8, 128, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, m->nfacets, m->d_facet_els, f->desc,
                                          f->d_l_fa, f->d_counts, pg, f->cap_fa, f->d_err);
   if (f->patch_exact) {
-    auto kx = k_patch_exact<D, K, T>;
-    const size_t smem = sizeof(PxSmem<D, K, T>);
-    kx<<<f->grid_px, PxCfg<D, K>::NT, smem, s>>>(f->desc, pg, f->d_counts, (const T*)f->d_mhat, (T*)f->d_famat,
-                                                 f->cap_fa, f->d_err, frs);
+    // batched steps of several forms run this part in one persistent launch
+    // for all of them (k_patch_exact_multi)
+    if (!f->defer_patch) {
+      auto kx = k_patch_exact<D, K, T>;
+      const size_t smem = sizeof(PxSmem<D, K, T>);
+      kx<<<f->grid_px, PxCfg<D, K>::NT, smem, s>>>(px_job<D, T>(f));
+    }
   } else {
     kp<<<f->grid_fa, C::NT, 0, s>>>(f->desc, pg, f->d_counts, (T*)f->d_famat, f->cap_fa, f->d_err, frs);
   }
@@ -3193,6 +3314,7 @@ RowsArgs rows_args(xg_form* f, const int32_t* rows) {
   R.n2 = 2 * sp->nd;
   R.W = f->rows_W;
   R.copies = f->rows_copies;
+  R.warps = f->rows_warps;
   R.el_dofs = sp->d_el_dofs_aos;
   R.el_facets = m->d_el_facets_aos;
   R.fel = m->d_facet_els_aos;
@@ -3367,6 +3489,7 @@ int xg_form_create(xg_space* space, const xg_term* terms, int32_t nterms, int pr
   int st = build_desc(f);
   if (!st) st = upload_tables(f);
   if (!st) st = form_workspace(f);
+  if (!st) st = apply_cached_tune(f);
   if (st) {
     form_free(f);
     return st;
@@ -3699,7 +3822,56 @@ int xg_form_check(xg_form* f) {
   return h;
 }
 
+}  // extern "C"
+
+namespace {
+int rows_front(xg_form* f, const double* d_lset, const uint8_t* d_dom, cudaStream_t s);
+int rows_back(xg_form* f, xg_csr* out, cudaStream_t s);
+int assemble_front(xg_form* f, const double* d_lset, const uint8_t* d_dom, xg_csr* out, void* stream);
+}  // namespace
+
+extern "C" {
+
 int xg_form_assemble(xg_form* f, const double* d_lset, const uint8_t* d_dom, xg_csr* out, void* stream) {
+  if (!out || !out->d_row_dof || !out->d_rowptr || !out->d_cols || !out->d_vals || !out->d_counts) return XG_ERR_ARG;
+  int st = assemble_front(f, d_lset, d_dom, out, stream);
+  if (st) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  return f->rows ? rows_back(f, out, s) : scatter_phase(f, out, s);
+}
+
+}  // extern "C"
+
+namespace {
+
+// the element and patch kernels of one step (spatial forms: the element rows
+// at their static slots and the patch matrices by facet slot; the patch
+// matrices are left out when the form's patches run in a batched launch)
+int rows_front(xg_form* f, const double* d_lset, const uint8_t* d_dom, cudaStream_t s) {
+  const bool fp64 = f->precision == XG_PREC_FP64;
+  int st;
+  if ((st = fp64 ? dispatch_volume<double>(f, d_lset, d_dom, s) : dispatch_volume<float>(f, d_lset, d_dom, s)))
+    return st;
+  if (f->has_patch && (st = fp64 ? dispatch_patch<double>(f, s) : dispatch_patch<float>(f, s))) return st;
+  if (f->use_ev) cudaEventRecord(f->ev[5], s);
+  return XG_OK;
+}
+
+// active rows, then the fixed-order row sums and the compressed output
+int rows_back(xg_form* f, xg_csr* out, cudaStream_t s) {
+  int st;
+  if ((st = mark_rows(f, out, s))) return st;
+  if (f->use_ev) cudaEventRecord(f->ev[6], s);
+  st = rows_scatter(rows_args(f, out->d_row_dof), f->space->ndof, f->has_patch, f->precision == XG_PREC_FP64,
+                    f->d_elmat, f->d_famat, out->d_rowptr, out->d_counts, out->d_cols, out->d_vals, out->cap_nnz,
+                    f->rows_grid, f->rows_smem, s);
+  if (f->use_ev) cudaEventRecord(f->ev[7], s);
+  return st;
+}
+
+// checks, active sets and lists, and (spatial forms) the element and patch
+// kernels; space-time-shaped forms also their element and patch matrices
+int assemble_front(xg_form* f, const double* d_lset, const uint8_t* d_dom, xg_csr* out, void* stream) {
   if (!f || !d_lset || !d_dom || !out || !out->d_row_dof || !out->d_rowptr || !out->d_cols || !out->d_vals ||
       !out->d_counts)
     return XG_ERR_ARG;
@@ -3725,22 +3897,7 @@ int xg_form_assemble(xg_form* f, const double* d_lset, const uint8_t* d_dom, xg_
     XG_CUDA(cudaMemsetAsync(f->d_counts + 2, 0, sizeof(int), s));
   }
   if (f->use_ev) cudaEventRecord(f->ev[2], s);
-  if (f->rows) {
-    // 2. element rows at their static slots, patch matrices by facet slot;
-    // 3. active rows; 4. fixed-order row sums and the compressed output
-    const bool fp64 = f->precision == XG_PREC_FP64;
-    if ((st = fp64 ? dispatch_volume<double>(f, d_lset, d_dom, s) : dispatch_volume<float>(f, d_lset, d_dom, s)))
-      return st;
-    if (f->has_patch && (st = fp64 ? dispatch_patch<double>(f, s) : dispatch_patch<float>(f, s))) return st;
-    if (f->use_ev) cudaEventRecord(f->ev[5], s);
-    if ((st = mark_rows(f, out, s))) return st;
-    if (f->use_ev) cudaEventRecord(f->ev[6], s);
-    st = rows_scatter(rows_args(f, out->d_row_dof), f->space->ndof, f->has_patch, fp64, f->d_elmat, f->d_famat,
-                      out->d_rowptr, out->d_counts, out->d_cols, out->d_vals, out->cap_nnz, f->rows_grid,
-                      f->rows_smem, s);
-    if (f->use_ev) cudaEventRecord(f->ev[7], s);
-    return st;
-  }
+  if (f->rows) return rows_front(f, d_lset, d_dom, s);
   // 2. element and patch matrices (the cut list's slots follow the uncut list's)
   if (f->precision == XG_PREC_FP64) {
     if ((st = dispatch_volume<double>(f, d_lset, d_dom, s))) return st;
@@ -3750,10 +3907,19 @@ int xg_form_assemble(xg_form* f, const double* d_lset, const uint8_t* d_dom, xg_
     if (f->has_patch && (st = dispatch_patch<float>(f, s))) return st;
   }
   if (f->use_ev) cudaEventRecord(f->ev[5], s);
-  return scatter_phase(f, out, s);
+  return XG_OK;
 }
 
-int xg_cutfem_step(xg_form* f, const double* d_lset, xg_csr* out, void* stream) {
+}  // namespace
+
+extern "C" {
+
+}  // extern "C"
+
+namespace {
+// marking, the form's effective element / facet sets, and the front of the
+// assembly (up to the element and patch kernels)
+int cutfem_front(xg_form* f, const double* d_lset, xg_csr* out, void* stream) {
   if (!f || !d_lset || !out) return XG_ERR_ARG;
   xg_mesh* m = f->mesh;
   if (f->use_ev) cudaEventRecord(f->ev[0], (cudaStream_t)stream);
@@ -3775,9 +3941,21 @@ int xg_cutfem_step(xg_form* f, const double* d_lset, xg_csr* out, void* stream) 
   }
   for (int p = 0; p < f->desc.npatch; p++) f->desc.p[p].defined_on = f->d_fbits;
   if (f->use_ev) cudaEventRecord(f->ev[1], (cudaStream_t)stream);
-  st = xg_form_assemble(f, d_lset, f->d_dom, out, stream);
+  st = assemble_front(f, d_lset, f->d_dom, out, stream);
   f->desc = saved;
   return st;
+}
+
+}  // namespace
+
+extern "C" {
+
+int xg_cutfem_step(xg_form* f, const double* d_lset, xg_csr* out, void* stream) {
+  if (!f || !d_lset || !out) return XG_ERR_ARG;
+  int st = cutfem_front(f, d_lset, out, stream);
+  if (st) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  return f->rows ? rows_back(f, out, s) : scatter_phase(f, out, s);
 }
 
 int xg_form_stage_events(xg_form* f, void* const* events, int n) {
@@ -3978,11 +4156,277 @@ int xg_cutfem_marking(xg_form* f, const uint8_t** d_dom, const double** d_ratio,
 
 }  // extern "C"
 
+// ============================================================================
+// Autotuner.  Per (device, dimension, order, precision) it times, on the
+// caller's form and level set, the launch choices that do not change any
+// result bit: elements per block of the uncut element kernel (16 or 32),
+// blocks per SM of the basis-change patch kernel (1 .. its occupancy) and
+// rows per block (4, 8, 16 warps) of the row passes; and the row sums'
+// accumulator copies (1 .. min(4, 32 / dofs per element)), which fix the
+// summation order of the row sums (every configuration is deterministic; the
+// chosen one is used for every later step and form of that key).  Each
+// choice is the fastest median of three steps of its own stage (CUDA events
+// on the launching stream), searched one knob at a time; the table is cached
+// per process and applied to forms created afterwards.
+// ============================================================================
+namespace {
+
+struct TuneRec {
+  int uncut_epb = 32, rows_warps = 8, rows_copies = 1, px_bps = 0;
+  float ms_uncut = 0, ms_rows = 0, ms_patch = 0;
+};
+std::mutex g_tune_mu;
+std::map<std::string, TuneRec> g_tune;
+
+std::string tune_key(const xg_form* f) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  return std::to_string(dev) + "/d" + std::to_string(f->mesh->dim) + "/k" + std::to_string(f->space->order) + "/" +
+         (f->precision == XG_PREC_FP64 ? "fp64" : "mixed");
+}
+
+int apply_tune(xg_form* f, const TuneRec& t) {
+  f->tune_uncut_epb = t.uncut_epb;
+  f->rows_warps = t.rows_warps;
+  f->rows_copies = t.rows_copies;
+  const RowsArgs R = rows_args(f, nullptr);
+  const size_t smem = rows_accum_smem(R);
+  const int grid = rows_accum_grid(R, f->precision == XG_PREC_FP64, smem);
+  if (!grid) return XG_ERR_CAPACITY;
+  f->rows_smem = smem;
+  f->rows_grid = grid;
+  if (t.px_bps > 0) f->grid_px = 152 * std::min(t.px_bps, f->px_occ);
+  f->px_bps = t.px_bps;
+  return XG_OK;
+}
+
+int apply_cached_tune(xg_form* f) {
+  if (f->st || !f->rows) return XG_OK;
+  TuneRec t;
+  bool found = false;
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    auto it = g_tune.find(tune_key(f));
+    if (it != g_tune.end()) {
+      t = it->second;
+      found = true;
+    }
+  }
+  return found ? apply_tune(f, t) : XG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int xg_form_autotune(xg_form* f, const double* d_lset, xg_csr* out, void* stream) {
+  if (!f || !d_lset || !out) return XG_ERR_ARG;
+  if (f->st || !f->rows) return XG_OK;  // space-time forms keep their fixed launches
+  const std::string key = tune_key(f);
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) return apply_tune(f, it->second);
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaEvent_t ev[8];
+  for (int i = 0; i < 8; i++)
+    if (cudaEventCreate(&ev[i]) != cudaSuccess) {
+      for (int k = 0; k < i; k++) cudaEventDestroy(ev[k]);
+      return cuda_fail(cudaGetLastError(), "xg_form_autotune");
+    }
+  const bool use_ev = f->use_ev;
+  cudaEvent_t saved_ev[8];
+  for (int i = 0; i < 8; i++) {
+    saved_ev[i] = f->ev[i];
+    f->ev[i] = ev[i];
+  }
+  f->use_ev = true;
+  int st = XG_OK;
+  // median time (ms) of stage a -> b over three steps
+  auto stage = [&](int a, int b) -> float {
+    float t[3];
+    for (int r = 0; r < 3 && !st; r++) {
+      if ((st = xg_cutfem_step(f, d_lset, out, stream))) break;
+      if (cudaStreamSynchronize(s) != cudaSuccess) {
+        st = cuda_fail(cudaGetLastError(), "xg_form_autotune");
+        break;
+      }
+      if ((st = xg_form_check(f))) break;
+      cudaEventElapsedTime(&t[r], ev[a], ev[b]);
+    }
+    if (st) return 1e30f;
+    std::sort(t, t + 3);
+    return t[1];
+  };
+  TuneRec best;
+  best.rows_copies = f->rows_copies;
+  best.rows_warps = f->rows_warps;
+  if ((st = apply_tune(f, best)) == XG_OK) stage(0, 7);  // warm-up
+  // uncut elements per block
+  if (!st) {
+    float bt = 1e30f;
+    for (int epb : {32, 16}) {
+      TuneRec t = best;
+      t.uncut_epb = epb;
+      if ((st = apply_tune(f, t))) break;
+      const float ms = stage(2, 3);
+      if (ms < bt) {
+        bt = ms;
+        best.uncut_epb = epb;
+        best.ms_uncut = ms;
+      }
+    }
+  }
+  // row passes: rows per block, accumulator copies
+  if (!st) {
+    float bt = 1e30f;
+    const int cmax = std::min(4, std::max(1, 32 / f->space->nd));
+    for (int w : {4, 8, 16})
+      for (int c = 1; c <= cmax && !st; c++) {
+        TuneRec t = best;
+        t.rows_warps = w;
+        t.rows_copies = c;
+        if (apply_tune(f, t)) continue;  // shared memory too large for this choice
+        const float ms = stage(6, 7);
+        if (ms < bt) {
+          bt = ms;
+          best.rows_warps = w;
+          best.rows_copies = c;
+          best.ms_rows = ms;
+        }
+      }
+  }
+  // basis-change patch kernel: blocks per SM
+  if (!st && f->has_patch && f->patch_exact) {
+    float bt = 1e30f;
+    for (int b = 1; b <= f->px_occ && !st; b++) {
+      TuneRec t = best;
+      t.px_bps = b;
+      if ((st = apply_tune(f, t))) break;
+      const float ms = stage(4, 5);
+      if (ms < bt) {
+        bt = ms;
+        best.px_bps = b;
+        best.ms_patch = ms;
+      }
+    }
+  }
+  for (int i = 0; i < 8; i++) {
+    f->ev[i] = saved_ev[i];
+    cudaEventDestroy(ev[i]);
+  }
+  f->use_ev = use_ev;
+  if (st) return st;
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tune[key] = best;
+  }
+  return apply_tune(f, best);
+}
+
+int64_t xg_autotune_table(char* buf, int64_t cap) {
+  std::string j = "{";
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    bool first = true;
+    for (const auto& kv : g_tune) {
+      const TuneRec& t = kv.second;
+      char line[512];
+      std::snprintf(line, sizeof(line),
+                    "%s\"%s\": {\"uncut_elements_per_block\": %d, \"row_pass_rows_per_block\": %d, "
+                    "\"row_pass_accumulator_copies\": %d, \"patch_blocks_per_sm\": %d, \"ms_uncut\": %.4f, "
+                    "\"ms_rows\": %.4f, \"ms_patch\": %.4f}",
+                    first ? "" : ", ", kv.first.c_str(), t.uncut_epb, t.rows_warps, t.rows_copies, t.px_bps,
+                    t.ms_uncut, t.ms_rows, t.ms_patch);
+      j += line;
+      first = false;
+    }
+  }
+  j += "}";
+  if (buf && cap > 0) {
+    const int64_t n = std::min<int64_t>(cap - 1, (int64_t)j.size());
+    std::memcpy(buf, j.data(), (size_t)n);
+    buf[n] = 0;
+  }
+  return (int64_t)j.size() + 1;
+}
+
+}  // extern "C"
+
 struct xg_step_graph {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   int64_t kernels = 0;
+  int* d_queue = nullptr;  // work counters of the batched patch launches
 };
+
+namespace {
+
+// work per item of the basis-change patch kernel (relative): facets per item
+// x patch entries x the basis size of the contractions
+int64_t px_item_cost(int D, int K) {
+  const int N = D == 2 ? (K + 1) * (K + 2) / 2 : (K + 1) * (K + 2) * (K + 3) / 6;
+  const int F = N <= 10 ? 32 : 8;
+  return (int64_t)F * (2 * N) * (2 * N) * N;
+}
+
+// The basis-change patch matrices of several forms (same dimension and
+// precision, spatial, kernels deferred by their steps) in one persistent
+// launch per kMaxPxJobs forms: jobs ordered by decreasing cost per item.
+template <int D, typename T>
+int launch_patch_multi_t(std::vector<xg_form*> fs, int* d_queue, cudaStream_t s) {
+  std::stable_sort(fs.begin(), fs.end(), [](xg_form* a, xg_form* b) {
+    return px_item_cost(D, a->space->order) > px_item_cost(D, b->space->order);
+  });
+  const void* kern = (const void*)k_patch_exact_multi<D, T>;
+  const size_t smem = std::max(sizeof(PxSmem<D, 1, T>), std::max(sizeof(PxSmem<D, 2, T>), sizeof(PxSmem<D, 3, T>)));
+  {
+    static std::mutex mu;
+    static bool raised = false;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!raised) {
+      XG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      raised = true;
+    }
+  }
+  static int grid = 0;
+  if (!grid) grid = grid_for(k_patch_exact_multi<D, T>, 256, smem);
+  for (size_t c0 = 0; c0 < fs.size(); c0 += kMaxPxJobs) {
+    PxJobs<D, T> Q;
+    std::memset(&Q, 0, sizeof(Q));
+    Q.n = (int)std::min<size_t>(kMaxPxJobs, fs.size() - c0);
+    Q.queue = d_queue + c0 / kMaxPxJobs;
+    for (int j = 0; j < Q.n; j++) Q.job[j] = px_job<D, T>(fs[c0 + j]);
+    XG_CUDA(cudaMemsetAsync(Q.queue, 0, sizeof(int), s));
+    void* args[] = {&Q};
+    XG_CUDA(cudaLaunchKernel(kern, dim3(grid), dim3(256), args, smem, s));
+  }
+  return XG_OK;
+}
+
+// groups the forms by (dimension, precision); d_queue holds one counter per
+// kMaxPxJobs forms of each group (at most forms.size() in all)
+int launch_patch_multi(const std::vector<xg_form*>& forms, int* d_queue, cudaStream_t s) {
+  int used = 0;
+  for (int D = 2; D <= 3; D++)
+    for (int fp = 0; fp < 2; fp++) {
+      std::vector<xg_form*> g;
+      for (xg_form* f : forms)
+        if (f->mesh->dim == D && (f->precision == XG_PREC_FP64) == (fp == 1)) g.push_back(f);
+      if (g.empty()) continue;
+      int st;
+      if (D == 2) st = fp ? launch_patch_multi_t<2, double>(g, d_queue + used, s)
+                          : launch_patch_multi_t<2, float>(g, d_queue + used, s);
+      else st = fp ? launch_patch_multi_t<3, double>(g, d_queue + used, s)
+                   : launch_patch_multi_t<3, float>(g, d_queue + used, s);
+      if (st) return st;
+      used += (int)((g.size() + kMaxPxJobs - 1) / kMaxPxJobs);
+    }
+  return XG_OK;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -3990,6 +4434,7 @@ int xg_step_graph_destroy(xg_step_graph* g) {
   if (!g) return XG_OK;
   if (g->exec) cudaGraphExecDestroy(g->exec);
   if (g->graph) cudaGraphDestroy(g->graph);
+  cudaFree(g->d_queue);
   delete g;
   return XG_OK;
 }
@@ -4016,40 +4461,82 @@ int xg_step_graph_create(xg_form* const* forms, const double* const* d_lsets, co
             return XG_ERR_ARG;
           }
   const int nb = (int)distinct.size();
+  // Forms whose patch matrices come from the basis-change kernel share one
+  // persistent, work-stealing launch (k_patch_exact_multi) when each form
+  // takes one step in the graph: every branch runs its step up to the patch
+  // geometry, the batched launch waits for all of them, and every branch's
+  // row sums wait for it.
+  std::vector<xg_form*> multi;
+  if (nb == n)
+    for (xg_form* f : distinct)
+      if (f->rows && f->has_patch && f->patch_exact) multi.push_back(f);
+  if (multi.size() < 2) multi.clear();
+  int* d_queue = nullptr;
+  if (!multi.empty()) XG_CUDA(cudaMalloc((void**)&d_queue, multi.size() * sizeof(int)));
   std::vector<cudaStream_t> streams(nb, nullptr);
-  std::vector<cudaEvent_t> done(nb, nullptr);
-  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> done(nb, nullptr), front(nb, nullptr);
+  cudaEvent_t fork = nullptr, batched = nullptr;
   std::vector<xg_csr> o(outs, outs + n);
   std::vector<bool> use_ev(nb);
   auto release = [&]() {
     for (int b = 0; b < nb; b++) {
       if (streams[b]) cudaStreamDestroy(streams[b]);
       if (done[b]) cudaEventDestroy(done[b]);
+      if (front[b]) cudaEventDestroy(front[b]);
       distinct[b]->use_ev = use_ev[b];
+      distinct[b]->defer_patch = false;
     }
     if (fork) cudaEventDestroy(fork);
+    if (batched) cudaEventDestroy(batched);
   };
   cudaError_t e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&batched, cudaEventDisableTiming);
   for (int b = 0; b < nb && e == cudaSuccess; b++) {
     use_ev[b] = distinct[b]->use_ev;
     distinct[b]->use_ev = false;
     e = cudaStreamCreateWithFlags(&streams[b], cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&done[b], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&front[b], cudaEventDisableTiming);
   }
   if (e != cudaSuccess) {
     release();
+    cudaFree(d_queue);
     return cuda_fail(e, "xg_step_graph_create");
   }
+  for (xg_form* f : multi) f->defer_patch = true;
   // capture on branch 0's stream; the others fork from it and join back
   cudaStream_t s0 = streams[0];
   e = cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) e = cudaEventRecord(fork, s0);
   for (int b = 1; b < nb && e == cudaSuccess; b++) e = cudaStreamWaitEvent(streams[b], fork, 0);
   int st = XG_OK;
-  for (int i = 0; i < n && e == cudaSuccess && !st; i++) {
-    xg_form* f = forms[i];
-    void* s = (void*)streams[branch[i]];
-    st = f->st ? xg_st_cutfem_step(f, d_lsets[i], &o[i], s) : xg_cutfem_step(f, d_lsets[i], &o[i], s);
+  if (multi.empty()) {
+    for (int i = 0; i < n && e == cudaSuccess && !st; i++) {
+      xg_form* f = forms[i];
+      void* s = (void*)streams[branch[i]];
+      st = f->st ? xg_st_cutfem_step(f, d_lsets[i], &o[i], s) : xg_cutfem_step(f, d_lsets[i], &o[i], s);
+    }
+  } else {
+    // fronts on their branches (entries are distinct forms: entry i is branch i)
+    for (int i = 0; i < n && e == cudaSuccess && !st; i++) {
+      xg_form* f = forms[i];
+      void* s = (void*)streams[branch[i]];
+      if (f->st) st = xg_st_cutfem_step(f, d_lsets[i], &o[i], s);
+      else if (f->rows) st = cutfem_front(f, d_lsets[i], &o[i], s);
+      else st = xg_cutfem_step(f, d_lsets[i], &o[i], s);
+    }
+    for (int b = 1; b < nb && e == cudaSuccess; b++) {
+      e = cudaEventRecord(front[b], streams[b]);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(s0, front[b], 0);
+    }
+    if (e == cudaSuccess && !st) st = launch_patch_multi(multi, d_queue, s0);
+    if (e == cudaSuccess && !st) e = cudaEventRecord(batched, s0);
+    for (int b = 1; b < nb && e == cudaSuccess; b++) e = cudaStreamWaitEvent(streams[b], batched, 0);
+    // the row sums of the spatial forms
+    for (int i = 0; i < n && e == cudaSuccess && !st; i++) {
+      xg_form* f = forms[i];
+      if (f->rows && !f->st) st = rows_back(f, &o[i], streams[branch[i]]);
+    }
   }
   for (int b = 1; b < nb && e == cudaSuccess; b++) {
     e = cudaEventRecord(done[b], streams[b]);
@@ -4060,6 +4547,7 @@ int xg_step_graph_create(xg_form* const* forms, const double* const* d_lsets, co
   if (e == cudaSuccess) e = e2;
   auto* g = new xg_step_graph();
   g->graph = graph;
+  g->d_queue = d_queue;
   if (e == cudaSuccess && !st) e = cudaGraphInstantiate(&g->exec, graph, 0);
   if (e == cudaSuccess && !st) {
     size_t nn = 0;

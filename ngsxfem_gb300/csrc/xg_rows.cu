@@ -150,7 +150,7 @@ __global__ void __launch_bounds__(256) k_fa_mark(RowsArgs A) {
 // ND dofs per element, NFL facets per element (compile time: the index
 // arithmetic of the inner loops divides by them)
 template <typename T, int ND, int NFL, bool DIRECT>
-__global__ void __launch_bounds__(kRowsWarps * 32) k_rows_accum(RowsArgs A, const T* __restrict__ elrows,
+__global__ void __launch_bounds__(kRowsMaxWarps * 32) k_rows_accum(RowsArgs A, const T* __restrict__ elrows,
                                                                  const T* __restrict__ farows,
                                                                  const int64_t* __restrict__ rowptr,
                                                                  int32_t* __restrict__ cols, double* __restrict__ vals,
@@ -160,7 +160,7 @@ __global__ void __launch_bounds__(kRowsWarps * 32) k_rows_accum(RowsArgs A, cons
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int LEN = A.W * 32, C = A.copies;
   double* acc = (double*)sm_acc + (size_t)warp * C * LEN;
-  int* clist = (int*)((double*)sm_acc + (size_t)kRowsWarps * C * LEN) + (size_t)warp * (2 * kCandBatch + LEN / 4);
+  int* clist = (int*)((double*)sm_acc + (size_t)A.warps * C * LEN) + (size_t)warp * (2 * kCandBatch + LEN / 4);
   int* cpi = clist + kCandBatch;                            // [kCandBatch] patch rows of the batch's candidates
   unsigned char* fl = (unsigned char*)(cpi + kCandBatch);  // [LEN] touched positions of the row
   for (int k = lane; k < C * LEN; k += 32) acc[k] = 0.0;
@@ -171,8 +171,8 @@ __global__ void __launch_bounds__(kRowsWarps * 32) k_rows_accum(RowsArgs A, cons
   const int cl = lane / ND, jl = lane - cl * ND;
   const bool on = cl < ce;
   const unsigned below = (1u << lane) - 1;
-  const int stride = gridDim.x * kRowsWarps;
-  int row = blockIdx.x * kRowsWarps + warp;
+  const int stride = gridDim.x * A.warps;
+  int row = blockIdx.x * A.warps + warp;
   int r = row < nrows ? A.rows[row] : 0;
   for (; row < nrows; row += stride) {
     const int64_t fo = A.full_ptr[r];
@@ -336,7 +336,7 @@ __global__ void __launch_bounds__(kRowsWarps * 32) k_rows_accum(RowsArgs A, cons
 // for the compaction scratch): the same positions as k_rows_accum, flagged
 // per row and counted; nothing is cleared (the accumulation pass clears).
 template <int ND, int NFL>
-__global__ void __launch_bounds__(kRowsWarps * 32) k_rows_count(RowsArgs A) {
+__global__ void __launch_bounds__(kRowsMaxWarps * 32) k_rows_count(RowsArgs A) {
   extern __shared__ __align__(16) unsigned char sm_cnt[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int LEN = A.W * 32;
@@ -347,7 +347,7 @@ __global__ void __launch_bounds__(kRowsWarps * 32) k_rows_count(RowsArgs A) {
   __syncwarp();
   const int nrows = A.counts[3];
   const unsigned below = (1u << lane) - 1;
-  for (int row = blockIdx.x * kRowsWarps + warp; row < nrows; row += gridDim.x * kRowsWarps) {
+  for (int row = blockIdx.x * A.warps + warp; row < nrows; row += gridDim.x * A.warps) {
     const int r = A.rows[row];
     const int64_t fo = A.full_ptr[r];
     const int len = (int)(A.full_ptr[r + 1] - fo), nw = (len + 31) >> 5;
@@ -579,7 +579,7 @@ int rows_static_build(const RowsArgs& A, bool has_patch, cudaStream_t s) {
 }
 
 size_t rows_accum_smem(const RowsArgs& A) {
-  return (size_t)kRowsWarps *
+  return (size_t)A.warps *
          ((size_t)A.copies * A.W * 32 * sizeof(double) + (2 * kCandBatch + A.W * 8) * sizeof(int));
 }
 
@@ -605,7 +605,7 @@ int rows_accum_grid(const RowsArgs& A, bool fp64, size_t smem) {
       }
     }
   }
-  return grid_of(k, kRowsWarps * 32, smem);
+  return grid_of(k, A.warps * 32, smem);
 }
 
 int rows_scatter(const RowsArgs& A, int64_t ndof, bool has_patch, bool fp64, const void* elrows,
@@ -627,19 +627,19 @@ int rows_scatter(const RowsArgs& A, int64_t ndof, bool has_patch, bool fp64, con
   RowsArgs a = A;
   if (direct) {
     void* cargs[] = {&a};
-    cudaError_t e = cudaLaunchKernel(kc, dim3(grid), dim3(kRowsWarps * 32), cargs, smem, s);
+    cudaError_t e = cudaLaunchKernel(kc, dim3(grid), dim3(A.warps * 32), cargs, smem, s);
     if (e != cudaSuccess) return cuda_fail(e, "k_rows_count");
   }
   void* args[] = {&a, const_cast<void**>(&elrows), const_cast<void**>(&farows), &out_rowptr, &cols, &vals, &cap_nnz};
   if (!direct) {
-    cudaError_t e = cudaLaunchKernel(k, dim3(grid), dim3(kRowsWarps * 32), args, smem, s);
+    cudaError_t e = cudaLaunchKernel(k, dim3(grid), dim3(A.warps * 32), args, smem, s);
     if (e != cudaSuccess) return cuda_fail(e, "k_rows_accum");
   }
   k_scan_blocks<<<nb, kSThreads, 0, s>>>(A.rowcnt, A.counts + 3, A.bsum);
   k_scan_top<<<1, 1024, 0, s>>>(A.bsum, nb);
   k_scan_apply<<<nb, kSThreads, 0, s>>>(A.rowcnt, A.counts + 3, A.bsum, out_rowptr, out_counts, cap_nnz, A.err);
   if (direct) {
-    cudaError_t e = cudaLaunchKernel(k, dim3(grid), dim3(kRowsWarps * 32), args, smem, s);
+    cudaError_t e = cudaLaunchKernel(k, dim3(grid), dim3(A.warps * 32), args, smem, s);
     if (e != cudaSuccess) return cuda_fail(e, "k_rows_accum");
   } else {
     k_rows_copy<<<152 * 16, 256, 0, s>>>(A, out_rowptr, cols, vals, cap_nnz);

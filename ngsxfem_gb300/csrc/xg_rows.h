@@ -37,7 +37,8 @@ namespace xg {
 struct RowsArgs {
   int ne, nd, nfl, n2;        // elements, dofs per element, facets per element, 2 nd
   int W;                      // 32-bit words of a row (full rows up to 32 W columns)
-  int copies;                 // accumulator copies per warp in the accumulation pass
+  int copies;                 // accumulator copies per warp in the accumulation pass (1..4)
+  int warps;                  // warps (rows in flight) per block of the row passes (<= kRowsMaxWarps)
   const int32_t* el_dofs;     // [ne][nd]
   const int32_t* el_facets;   // [ne][nfl]
   const int2* fel;            // [nf] first / second element of a facet (-1: boundary)
@@ -80,10 +81,10 @@ int rows_scatter(const RowsArgs& A, int64_t ndof, bool has_patch, bool fp64, con
                  const void* farows, int64_t* out_rowptr, int64_t* out_counts, int32_t* cols, double* vals,
                  int64_t cap_nnz, int grid, size_t smem, cudaStream_t s);
 // Shared bytes per block of the accumulation pass and its grid (blocks of
-// kRowsWarps warps); 0 from rows_accum_grid if the element type is not
+// A.warps warps); 0 from rows_accum_grid if the element type is not
 // supported or the shared memory is too large.
 size_t rows_accum_smem(const RowsArgs& A);
 int rows_accum_grid(const RowsArgs& A, bool fp64, size_t smem);
-constexpr int kRowsWarps = 8;
+constexpr int kRowsMaxWarps = 16;
 
 }  // namespace xg

@@ -257,3 +257,81 @@ def test_spacetime_slabs_one_graph(xg, orc):
     for f in forms:
         xg._lib.load().xg_form_destroy(f)
     xg._lib.load().xg_space_destroy(sh)
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_batched_patch_launch_matches_eager(xg, orc, prec):
+    """Distinct forms with basis-change patches (orders 1-3, 2D and 3D) share
+    one persistent work-stealing patch launch per dimension in the graph: the
+    graph's matrices equal the eager per-form steps bit for bit."""
+    groups = batch_groups(7, 5e3, seed=9)
+    m2 = MakeStructured2DMesh(14, 11, -1, 1, -1, 1)
+    cases = [(m, vals, k) for k, (m, vals) in groups.items()]
+    cases.append((m2, np.sqrt((m2.coords ** 2).sum(1)) - 0.55, 3))
+    cases.append((m2, np.sqrt((m2.coords ** 2).sum(1)) - 0.45, 2))
+    forms, lsets, spaces = [], [], []
+    for m, vals, k in cases:
+        gf = xg.GridFunction(xg.H1(m, 1))
+        xg.InterpolateToP1(vals, gf)
+        V = xg.H1(m, order=k)
+        spaces.append(V)
+        lsets.append(gf.vec)
+        forms.append(plain_form(xg, V, C2_TERMS(orc, k), prec))
+    eager = []
+    for f, l, V in zip(forms, lsets, spaces):
+        b = output(xg, f, V.ndof)
+        xg._lib.call("xg_cutfem_step", f, xg._vp(l), ctypes.byref(b._csr), xg._stream())
+        torch.cuda.synchronize()
+        xg._lib.check(xg._lib.load().xg_form_check(f), "eager")
+        eager.append(coo(xg, b, V.ndof))
+    outs = [output(xg, f, V.ndof) for f, V in zip(forms, spaces)]
+    g = graph(xg, forms, lsets, outs)
+    for _ in range(2):
+        xg._lib.call("xg_step_graph_launch", g, xg._stream())
+        torch.cuda.synchronize()
+        for f in forms:
+            xg._lib.check(xg._lib.load().xg_form_check(f), "graph")
+        for b, V, ref in zip(outs, spaces, eager):
+            got = coo(xg, b, V.ndof)
+            assert all(np.array_equal(x, y) for x, y in zip(got, ref))
+    xg._lib.call("xg_step_graph_destroy", g)
+    for f in forms:
+        xg._lib.load().xg_form_destroy(f)
+
+
+def test_autotune_keeps_parity_and_determinism(xg, orc):
+    """The autotuner times launch choices on the form and keeps the fastest;
+    the tuned step still matches the oracle within 1e-12, repeats bit for bit,
+    and the table names every tuned key."""
+    import json
+    m = MakeStructured3DMesh(9)
+    c = m.coords - 0.5
+    vals = np.sqrt((c ** 2).sum(1)) - 0.31
+    gf = xg.GridFunction(xg.H1(m, 1))
+    xg.InterpolateToP1(vals, gf)
+    for k in (1, 2):
+        V = xg.H1(m, order=k)
+        f = plain_form(xg, V, C2_TERMS(orc, k), 0)
+        b = output(xg, f, V.ndof)
+        xg._lib.call("xg_form_autotune", f, xg._vp(gf.vec), ctypes.byref(b._csr), xg._stream())
+        res = []
+        for _ in range(2):
+            xg._lib.call("xg_cutfem_step", f, xg._vp(gf.vec), ctypes.byref(b._csr), xg._stream())
+            torch.cuda.synchronize()
+            xg._lib.check(xg._lib.load().xg_form_check(f), "tuned")
+            res.append(coo(xg, b, V.ndof))
+        assert all(np.array_equal(x, y) for x, y in zip(res[0], res[1]))
+        sp, rr, rc, rv = oracle_csr(orc, m, gf.vec.cpu().numpy(), k, C2_TERMS(orc, k))
+        r, cc, v = canon(*res[0])
+        rr, rc, rv = canon(rr, rc, rv)
+        assert np.array_equal(r, rr) and np.array_equal(cc, rc)
+        assert np.max(np.abs(v - rv)) / np.max(np.abs(rv)) < 1e-12
+        xg._lib.load().xg_form_destroy(f)
+    need = xg._lib.load().xg_autotune_table(None, 0)
+    buf = ctypes.create_string_buffer(int(need))
+    xg._lib.load().xg_autotune_table(buf, need)
+    table = json.loads(buf.value.decode())
+    assert any(key.endswith("/d3/k1/fp64") for key in table) and any(key.endswith("/d3/k2/fp64") for key in table)
+    for rec in table.values():
+        assert rec["row_pass_rows_per_block"] in (4, 8, 16) and 1 <= rec["row_pass_accumulator_copies"] <= 4
+        assert rec["uncut_elements_per_block"] in (16, 32)

@@ -15,7 +15,7 @@ def declared():
         if h.endswith(".h"):
             src = open(os.path.join(ROOT, "include", h)).read()
             src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-            names += re.findall(r"\b(?:int|const char\*)\s+(xg_\w+)\s*\(", src)
+            names += re.findall(r"\b(?:int|int64_t|const char\*)\s+(xg_\w+)\s*\(", src)
     return sorted(set(names))
 
 
