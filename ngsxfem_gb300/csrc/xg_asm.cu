@@ -4243,10 +4243,11 @@ int xg_form_autotune(xg_form* f, const double* d_lset, xg_csr* out, void* stream
   }
   f->use_ev = true;
   int st = XG_OK;
-  // median time (ms) of stage a -> b over three steps
+  // median time (ms) of stage a -> b over kReps steps
+  constexpr int kReps = 5;
   auto stage = [&](int a, int b) -> float {
-    float t[3];
-    for (int r = 0; r < 3 && !st; r++) {
+    float t[kReps];
+    for (int r = 0; r < kReps && !st; r++) {
       if ((st = xg_cutfem_step(f, d_lset, out, stream))) break;
       if (cudaStreamSynchronize(s) != cudaSuccess) {
         st = cuda_fail(cudaGetLastError(), "xg_form_autotune");
@@ -4256,9 +4257,12 @@ int xg_form_autotune(xg_form* f, const double* d_lset, xg_csr* out, void* stream
       cudaEventElapsedTime(&t[r], ev[a], ev[b]);
     }
     if (st) return 1e30f;
-    std::sort(t, t + 3);
-    return t[1];
+    std::sort(t, t + kReps);
+    return t[kReps / 2];
   };
+  // a choice replaces the incumbent only when it is faster by more than 3 %
+  // (the medians of different choices differ by noise of about that size)
+  constexpr float kGain = 0.97f;
   TuneRec best;
   best.rows_copies = f->rows_copies;
   best.rows_warps = f->rows_warps;
@@ -4271,7 +4275,7 @@ int xg_form_autotune(xg_form* f, const double* d_lset, xg_csr* out, void* stream
       t.uncut_epb = epb;
       if ((st = apply_tune(f, t))) break;
       const float ms = stage(2, 3);
-      if (ms < bt) {
+      if (ms < kGain * bt) {
         bt = ms;
         best.uncut_epb = epb;
         best.ms_uncut = ms;
@@ -4282,30 +4286,39 @@ int xg_form_autotune(xg_form* f, const double* d_lset, xg_csr* out, void* stream
   if (!st) {
     float bt = 1e30f;
     const int cmax = std::min(4, std::max(1, 32 / f->space->nd));
+    // the incumbent (the form's default) first
+    std::vector<std::pair<int, int>> cand = {{best.rows_warps, best.rows_copies}};
     for (int w : {4, 8, 16})
-      for (int c = 1; c <= cmax && !st; c++) {
+      for (int c = 1; c <= cmax; c++)
+        if (w != best.rows_warps || c != best.rows_copies) cand.push_back({w, c});
+    for (const auto& wc : cand) {
+      if (st) break;
+      {
+        const int w = wc.first, c = wc.second;
         TuneRec t = best;
         t.rows_warps = w;
         t.rows_copies = c;
         if (apply_tune(f, t)) continue;  // shared memory too large for this choice
         const float ms = stage(6, 7);
-        if (ms < bt) {
+        if (ms < kGain * bt) {
           bt = ms;
           best.rows_warps = w;
           best.rows_copies = c;
           best.ms_rows = ms;
         }
       }
+    }
   }
   // basis-change patch kernel: blocks per SM
   if (!st && f->has_patch && f->patch_exact) {
     float bt = 1e30f;
-    for (int b = 1; b <= f->px_occ && !st; b++) {
+    // the incumbent (occupancy) first, then fewer blocks per SM
+    for (int b = f->px_occ; b >= 1 && !st; b--) {
       TuneRec t = best;
       t.px_bps = b;
       if ((st = apply_tune(f, t))) break;
       const float ms = stage(4, 5);
-      if (ms < bt) {
+      if (ms < kGain * bt) {
         bt = ms;
         best.px_bps = b;
         best.ms_patch = ms;
