@@ -481,7 +481,7 @@ int xg_step_graph_destroy(xg_step_graph* graph);
  * (d_lset, output out as for xg_cutfem_step; several steps run), the launch
  * choices of the spatial step per (device, dimension, order, precision):
  * elements per block of the uncut element kernel (16, 32), rows per block of
- * the row passes (4, 8, 16 warps) and accumulator copies of the row sums (1..4,
+ * the row passes (4 or 8 warps) and accumulator copies of the row sums (1..4,
  * which fix their summation order: every choice is deterministic), blocks per
  * SM of the basis-change patch kernel; keeps the fastest of each (median of
  * three timed steps of its stage) in a per-process table that forms created

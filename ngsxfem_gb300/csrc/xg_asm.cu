@@ -4161,7 +4161,7 @@ int xg_cutfem_marking(xg_form* f, const uint8_t** d_dom, const double** d_ratio,
 // caller's form and level set, the launch choices that do not change any
 // result bit: elements per block of the uncut element kernel (16 or 32),
 // blocks per SM of the basis-change patch kernel (1 .. its occupancy) and
-// rows per block (4, 8, 16 warps) of the row passes; and the row sums'
+// rows per block (4 or 8 warps) of the row passes; and the row sums'
 // accumulator copies (1 .. min(4, 32 / dofs per element)), which fix the
 // summation order of the row sums (every configuration is deterministic; the
 // chosen one is used for every later step and form of that key).  Each
@@ -4288,7 +4288,7 @@ int xg_form_autotune(xg_form* f, const double* d_lset, xg_csr* out, void* stream
     const int cmax = std::min(4, std::max(1, 32 / f->space->nd));
     // the incumbent (the form's default) first
     std::vector<std::pair<int, int>> cand = {{best.rows_warps, best.rows_copies}};
-    for (int w : {4, 8, 16})
+    for (int w : {4, 8})
       for (int c = 1; c <= cmax; c++)
         if (w != best.rows_warps || c != best.rows_copies) cand.push_back({w, c});
     for (const auto& wc : cand) {

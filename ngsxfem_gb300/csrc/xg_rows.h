@@ -85,6 +85,6 @@ int rows_scatter(const RowsArgs& A, int64_t ndof, bool has_patch, bool fp64, con
 // supported or the shared memory is too large.
 size_t rows_accum_smem(const RowsArgs& A);
 int rows_accum_grid(const RowsArgs& A, bool fp64, size_t smem);
-constexpr int kRowsMaxWarps = 16;
+constexpr int kRowsMaxWarps = 8;
 
 }  // namespace xg

@@ -333,5 +333,5 @@ def test_autotune_keeps_parity_and_determinism(xg, orc):
     table = json.loads(buf.value.decode())
     assert any(key.endswith("/d3/k1/fp64") for key in table) and any(key.endswith("/d3/k2/fp64") for key in table)
     for rec in table.values():
-        assert rec["row_pass_rows_per_block"] in (4, 8, 16) and 1 <= rec["row_pass_accumulator_copies"] <= 4
+        assert rec["row_pass_rows_per_block"] in (4, 8) and 1 <= rec["row_pass_accumulator_copies"] <= 4
         assert rec["uncut_elements_per_block"] in (16, 32)
