@@ -50,8 +50,9 @@ typedef enum {
   XG_ERR_UNSUPPORTED = 6,  /* element type / order / term not supported */
   XG_ERR_NONFINITE = 7,    /* a non-finite weight or matrix entry was produced */
   XG_ERR_NO_DEVICE = 8,    /* no CUDA device, or the library was not built for it */
-  XG_ERR_IF_BOUND = 9      /* quad / hex interface scaling above 1/sqrt(1-0.999^2):
+  XG_ERR_IF_BOUND = 9,     /* quad / hex interface scaling above 1/sqrt(1-0.999^2):
                               straightcutrule.cpp:273-286 */
+  XG_ERR_TIMEOUT = 10      /* a bounded device-side wait gave up (the kernel stopped its work) */
 } xg_status;
 
 enum { XG_NEG = 0, XG_POS = 1, XG_IF = 2 };
@@ -431,6 +432,13 @@ int xg_mlp_get_params(const xg_mlp* mlp, float* d_out, void* stream);
 int xg_mlp_set_params(xg_mlp* mlp, const float* d_in, void* stream);
 /* y[B][24] = MLP(x[B][10]) (x from xg_learned_features); B <= 4,194,240 */
 int xg_mlp_forward(xg_mlp* mlp, const float* d_x, int64_t B, float* d_y, void* stream);
+/* The same forward pass on the sm_103a tensor cores (tcgen05.mma, BF16
+ * operands including the activations, FP32 accumulation in tensor memory),
+ * the three layers fused per tile of 128 rows; xg_learned_moments_tet uses it.
+ * Its device status (XG_ERR_TIMEOUT if a bounded wait gave up) is read and
+ * cleared by xg_mlp_check. */
+int xg_mlp_forward_tc(xg_mlp* mlp, const float* d_x, int64_t B, float* d_y, void* stream);
+int xg_mlp_check(xg_mlp* mlp);
 /* mean over the batch of sum_a ((U y / 256 - t)_a / s)^2, V = U R the thin QR of
  * V[a][i] = p_i^a (weights at the points: R^-1 y); t[B][35]
  * the moment defects, s[B] the scales; gradient into d_grad (flat, like the

@@ -34,7 +34,7 @@ EXPORTS = [
     "xg_space_create_st", "xg_space_info_st", "xg_cutinfo_update_st", "xg_st_cut_rules", "xg_st_form_create",
     "xg_st_cutfem_step", "xg_step_graph_create", "xg_step_graph_launch", "xg_step_graph_destroy",
     "xg_step_graph_kernel_count", "xg_form_autotune", "xg_autotune_table", "xg_iso_moments_tet", "xg_mlp_param_count", "xg_learned_points",
-    "xg_mlp_create", "xg_mlp_destroy", "xg_mlp_get_params", "xg_mlp_set_params", "xg_mlp_forward",
+    "xg_mlp_create", "xg_mlp_destroy", "xg_mlp_get_params", "xg_mlp_set_params", "xg_mlp_forward", "xg_mlp_forward_tc", "xg_mlp_check",
     "xg_mlp_loss_grad", "xg_mlp_adam_step", "xg_learned_moments_tet", "xg_learned_features",
     "xg_cutinfo_update_bnd", "xg_mesh_boundary", "xg_cutinfo_nodes", "xg_elements_with_threshold",
     "xg_lform_create", "xg_lform_destroy", "xg_lform_assemble", "xg_lform_check",
@@ -159,6 +159,8 @@ def load():
         "xg_mlp_get_params": (I, [P, P, P]),
         "xg_mlp_set_params": (I, [P, P, P]),
         "xg_mlp_forward": (I, [P, P, I64, P, P]),
+        "xg_mlp_forward_tc": (I, [P, P, I64, P, P]),
+        "xg_mlp_check": (I, [P]),
         "xg_mlp_loss_grad": (I, [P, P, P, P, I64, P, P, P]),
         "xg_mlp_adam_step": (I, [P, P, ctypes.c_float, I64, P]),
         "xg_learned_moments_tet": (I, [P, P, I64, D, P, P, P]),

@@ -33,6 +33,7 @@ UNITS = [
     ("xg_mlset.cu", ["-fmad=false"]),
     ("xg_isomesh.cu", ["-fmad=false"]),
     ("xg_rows.cu", []),
+    ("xg_mlp_tc.cu", []),
 ]
 
 

@@ -209,6 +209,7 @@ const char* xg_status_string(int s) {
     case XG_ERR_NONFINITE: return "non-finite weight or matrix entry";
     case XG_ERR_NO_DEVICE: return "no usable CUDA device";
     case XG_ERR_IF_BOUND: return "quadrilateral interface scaling factor above its bound";
+    case XG_ERR_TIMEOUT: return "a bounded device wait timed out";
   }
   return "unknown status";
 }

@@ -33,6 +33,12 @@ namespace xg {
 
 int tet_moments_launch(const double* d_vals, int64_t n, int order, int deform, double* d_out, int32_t* d_nonconv,
                        cudaStream_t s, const int32_t* d_list, const int32_t* d_count);  // xg_iso.cu
+// tensor-core inference (xg_mlp_tc.cu)
+extern const int kTcPackedBytes;
+int mlp_tc_pack(const float* d_params, int64_t off_w1, int64_t off_w2, int64_t off_w3, void* d_packed,
+                cudaStream_t s);
+int mlp_tc_forward(const float* d_x, int64_t B, const void* d_packed, const float* d_b1, const float* d_b2,
+                   const float* d_b3, float* d_y, int* d_err, cudaStream_t s);
 
 namespace {
 
@@ -331,6 +337,8 @@ struct xg_mlp {
   float *dh1 = nullptr, *dh2 = nullptr, *li = nullptr, *part = nullptr;
   int32_t* list = nullptr;  // fallback elements
   int32_t* count = nullptr;
+  void* tcw = nullptr;  // BF16 weight images of the tensor-core inference kernel
+  int* err = nullptr;   // device status of the tensor-core kernel
 };
 
 namespace {
@@ -488,6 +496,9 @@ int xg_mlp_create(uint64_t seed, xg_mlp** out) {
   fill(kOffW3, kHid, kOut, 0.1f);
   cudaError_t e = cudaMalloc((void**)&m->p, kNumParams * 4);
   if (!e) e = cudaMalloc((void**)&m->pb, kNumParams * 2);
+  if (!e) e = cudaMalloc(&m->tcw, kTcPackedBytes);
+  if (!e) e = cudaMalloc((void**)&m->err, sizeof(int));
+  if (!e) e = cudaMemset(m->err, 0, sizeof(int));
   if (!e) e = cudaMalloc((void**)&m->m, kNumParams * 4);
   if (!e) e = cudaMalloc((void**)&m->v, kNumParams * 4);
   if (!e) e = cudaMalloc((void**)&m->g, kNumParams * 4);
@@ -497,6 +508,8 @@ int xg_mlp_create(uint64_t seed, xg_mlp** out) {
   if (e) {
     cudaFree(m->p);
     cudaFree(m->pb);
+    cudaFree(m->tcw);
+    cudaFree(m->err);
     cudaFree(m->m);
     cudaFree(m->v);
     cudaFree(m->g);
@@ -504,6 +517,10 @@ int xg_mlp_create(uint64_t seed, xg_mlp** out) {
     return cuda_fail(e, "xg_mlp_create");
   }
   k_to_bf16<<<grid1(kNumParams), 256>>>(m->p, m->pb, kNumParams);
+  if ((st = mlp_tc_pack(m->p, kOffW1, kOffW2, kOffW3, m->tcw, nullptr))) {
+    xg_mlp_destroy(m);
+    return st;
+  }
   *out = m;
   return XG_OK;
 }
@@ -513,6 +530,8 @@ int xg_mlp_destroy(xg_mlp* m) {
   mlp_free_ws(m);
   cudaFree(m->p);
   cudaFree(m->pb);
+  cudaFree(m->tcw);
+  cudaFree(m->err);
   cudaFree(m->m);
   cudaFree(m->v);
   cudaFree(m->g);
@@ -532,7 +551,7 @@ int xg_mlp_set_params(xg_mlp* m, const float* d_in, void* stream) {
   XG_CUDA(cudaMemcpyAsync(m->p, d_in, kNumParams * 4, cudaMemcpyDeviceToDevice, s));
   k_to_bf16<<<grid1(kNumParams), 256, 0, s>>>(m->p, m->pb, kNumParams);
   XG_CUDA(cudaGetLastError());
-  return XG_OK;
+  return mlp_tc_pack(m->p, kOffW1, kOffW2, kOffW3, m->tcw, s);
 }
 
 int xg_mlp_forward(xg_mlp* m, const float* d_x, int64_t B, float* d_y, void* stream) {
@@ -571,7 +590,22 @@ int xg_mlp_adam_step(xg_mlp* m, const float* d_grad, float lr, int64_t t, void* 
                                            c1, c2);
   k_to_bf16<<<grid1(kNumParams), 256, 0, s>>>(m->p, m->pb, kNumParams);
   XG_CUDA(cudaGetLastError());
-  return XG_OK;
+  return mlp_tc_pack(m->p, kOffW1, kOffW2, kOffW3, m->tcw, s);
+}
+
+int xg_mlp_forward_tc(xg_mlp* m, const float* d_x, int64_t B, float* d_y, void* stream) {
+  if (!m || !d_x || !d_y || B < 0) return XG_ERR_ARG;
+  return mlp_tc_forward(d_x, B, m->tcw, m->p + kOffB1, m->p + kOffB2, m->p + kOffB3, d_y, m->err,
+                        (cudaStream_t)stream);
+}
+
+int xg_mlp_check(xg_mlp* m) {
+  if (!m) return XG_ERR_ARG;
+  int h = 0;
+  XG_CUDA(cudaMemcpy(&h, m->err, sizeof(int), cudaMemcpyDeviceToHost));
+  XG_CUDA(cudaMemset(m->err, 0, sizeof(int)));
+  if (h) set_last_error(std::string("device error: ") + xg_status_string(h));
+  return h;
 }
 
 int xg_learned_features(const double* d_vals10, int64_t n, float* d_x, void* stream) {
@@ -592,7 +626,9 @@ int xg_learned_moments_tet(xg_mlp* m, const double* d_vals10, int64_t n, double 
   // straight cut part (exact for degree <= 4 on the P1 sub-tetrahedra: order 4)
   if ((st = tet_moments_launch(d_vals10, n, 4, 0, d_out35, nullptr, s, nullptr, nullptr))) return st;
   k_features<<<grid1(n), 256, 0, s>>>(d_vals10, n, m->x);
-  if ((st = forward(m, n, s))) return st;
+  // the network on the tensor cores (all three layers per 128-row tile)
+  if ((st = mlp_tc_forward(m->x, n, m->tcw, m->p + kOffB1, m->p + kOffB2, m->p + kOffB3, m->y, m->err, s)))
+    return st;
   k_add_correction<<<grid1(n), 256, 0, s>>>(m->y, d_vals10, n, d_out35);
   if (kappa_max >= 0.0) {
     // plain (isoparametric, order 8) rule on the elements the network does not take

@@ -96,6 +96,17 @@ def forward(params, x):
     return y, (x, z1, h1, z2, h2)
 
 
+def forward_bf16_activations(params, x):
+    """The network as the tensor-core inference kernel runs it: the input
+    features and both hidden activations also rounded to BF16 before each
+    product (FP32 biases, exact products, FP64 sums here)."""
+    p = unpack(params)
+    x = bf16(np.asarray(x, dtype=np.float32))
+    h1 = bf16(silu(x @ bf16(p["W1"]) + p["b1"]).astype(np.float32))
+    h2 = bf16(silu(h1 @ bf16(p["W2"]) + p["b2"]).astype(np.float32))
+    return h2 @ bf16(p["W3"]) + p["b3"]
+
+
 def loss_grad(params, x, t, s):
     """(loss, flat gradient) of the batch objective."""
     p = unpack(params)

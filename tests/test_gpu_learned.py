@@ -92,6 +92,36 @@ def test_network_forward_and_gradient_vs_oracle(xg, B):
     xg._lib.call("xg_mlp_destroy", mlp)
 
 
+@pytest.mark.parametrize("B", [1, 127, 128, 129, 40000])
+def test_tensor_core_forward_vs_oracle(xg, B):
+    """The fused tcgen05 inference kernel (BF16 operands and activations, FP32
+    accumulation in tensor memory) against the numpy statement with the same
+    BF16 roundings: within 2e-3 of the output scale (a few BF16 ulps of the
+    activations that round differently after FP32 vs FP64 sums), and within
+    3e-2 of the FP32-activation forward."""
+    mlp = ctypes.c_void_p()
+    xg._lib.call("xg_mlp_create", 99, ctypes.byref(mlp))
+    p = params_of(xg, mlp)
+    rng = np.random.default_rng(B + 5)
+    x = rng.uniform(-1, 1, (B, 10)).astype(np.float32)
+    d_x = dev(x, torch.float32)
+    y_tc = torch.full((B, 24), float("nan"), dtype=torch.float32, device="cuda")
+    y_ref32 = torch.zeros((B, 24), dtype=torch.float32, device="cuda")
+    for _ in range(2):  # two calls in a row: the persistent kernel leaves nothing behind
+        xg._lib.call("xg_mlp_forward_tc", mlp, xg._vp(d_x), B, xg._vp(y_tc), xg._stream())
+        torch.cuda.synchronize()
+        xg._lib.check(xg._lib.load().xg_mlp_check(mlp), "tensor-core forward")
+    xg._lib.call("xg_mlp_forward", mlp, xg._vp(d_x), B, xg._vp(y_ref32), xg._stream())
+    torch.cuda.synchronize()
+    got = y_tc.cpu().numpy()
+    assert np.all(np.isfinite(got))
+    ref = L.forward_bf16_activations(p.cpu().numpy().astype(np.float64), x)
+    scale = max(1.0, np.abs(ref).max())
+    assert np.max(np.abs(got - ref)) <= 2e-3 * scale, np.max(np.abs(got - ref)) / scale
+    assert np.max(np.abs(got - y_ref32.cpu().numpy())) <= 3e-2 * scale
+    xg._lib.call("xg_mlp_destroy", mlp)
+
+
 def test_features_match_oracle(xg):
     v = L.spec_values(500, np.random.default_rng(2))
     x = torch.zeros((500, 10), dtype=torch.float32, device="cuda")
