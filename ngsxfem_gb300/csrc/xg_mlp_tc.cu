@@ -122,8 +122,8 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t phase) {
   return false;
 }
 
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
-  uint32_t r[32];
+// 32 consecutive accumulator columns of this thread's row into r (no wait)
+__device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, uint32_t* r) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
       "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n"
@@ -132,26 +132,37 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
         "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
         "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
       : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+  uint32_t r[32];
+  tmem_ld32_nowait(taddr, r);
+  tmem_wait_ld();
 #pragma unroll
   for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
-__device__ __forceinline__ float silu_tc(float z) { return z / (1.f + __expf(-z)); }
+// SiLU with the fast reciprocal division (the result is rounded to BF16)
+__device__ __forceinline__ float silu_tc(float z) { return __fdividef(z, 1.f + __expf(-z)); }
 
-// 32 accumulator columns of one row -> bias, SiLU, BF16 -> the activation tile
+// 64 accumulator columns of one row (two loads, one wait) -> bias, SiLU,
+// BF16 -> the activation tile
 __device__ __forceinline__ void epilogue_hidden(uint32_t taddr, const float* bias, int c0, int row,
                                                 unsigned char* H) {
-  float v[32];
-  tmem_ld32(taddr, v);
+  uint32_t r[64];
+  tmem_ld32_nowait(taddr, r);
+  tmem_ld32_nowait(taddr + 32u, r + 32);
+  tmem_wait_ld();
 #pragma unroll
-  for (int g = 0; g < 4; g++) {
+  for (int g = 0; g < 8; g++) {
     uint32_t w[4];
 #pragma unroll
     for (int q = 0; q < 4; q++) {
       const int c = g * 8 + 2 * q;
-      const __nv_bfloat162 h =
-          __floats2bfloat162_rn(silu_tc(v[c] + bias[c0 + c]), silu_tc(v[c + 1] + bias[c0 + c + 1]));
+      const __nv_bfloat162 h = __floats2bfloat162_rn(silu_tc(__uint_as_float(r[c]) + bias[c0 + c]),
+                                                     silu_tc(__uint_as_float(r[c + 1]) + bias[c0 + c + 1]));
       w[q] = *reinterpret_cast<const uint32_t*>(&h);
     }
     *reinterpret_cast<uint4*>(H + tc_off(row, c0 + g * 8, kTcHid)) = make_uint4(w[0], w[1], w[2], w[3]);
@@ -236,8 +247,8 @@ __global__ void __launch_bounds__(256, 1) k_mlp_tc(const float* __restrict__ x, 
     __syncthreads();  // every thread sees the same abort flag
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (abort_s) break;
-    for (int cc = 0; cc < 4; cc++) {
-      const int c0 = half * 128 + cc * 32;
+    for (int cc = 0; cc < 2; cc++) {
+      const int c0 = half * 128 + cc * 64;
       epilogue_hidden(tm + lane_base + (uint32_t)c0, s_b1, c0, row_l, H);
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -255,8 +266,8 @@ __global__ void __launch_bounds__(256, 1) k_mlp_tc(const float* __restrict__ x, 
     __syncthreads();  // every thread sees the same abort flag
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (abort_s) break;
-    for (int cc = 0; cc < 4; cc++) {
-      const int c0 = half * 128 + cc * 32;
+    for (int cc = 0; cc < 2; cc++) {
+      const int c0 = half * 128 + cc * 64;
       epilogue_hidden(tm + lane_base + (uint32_t)c0, s_b2, c0, row_l, H);
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
