@@ -82,6 +82,23 @@ def terms_c2(order):
     ]
 
 
+def terms_dg(order):
+    """demos/fictdom_dg.py:120-135 (unfitted DG Poisson on an L2 space):
+    stiffness on NEG, Nitsche on IF, the symmetric interior-penalty skeleton
+    on the facets between HASNEG elements (cut to NEG), ghost penalty."""
+    lam = 10.0 * order * order
+    return [
+        dict(kind=1, domain=0, coef=1.0, hpow=0),       # grad u . grad v on NEG
+        dict(kind=2, domain=2, coef=-1.0, hpow=0),      # -(n.grad u) v on IF
+        dict(kind=3, domain=2, coef=-1.0, hpow=0),      # -(n.grad v) u on IF
+        dict(kind=0, domain=2, coef=lam, hpow=-1),      # lambda/h u v on IF
+        dict(kind=7, domain=0, coef=lam, hpow=-1),      # lambda/h [u][v] on the NEG part of the facets
+        dict(kind=8, domain=0, coef=-0.5, hpow=0),      # -{grad u . n_F}[v]
+        dict(kind=9, domain=0, coef=-0.5, hpow=0),      # -[u]{grad v . n_F}
+        dict(kind=5, domain=0, coef=0.1, hpow=-2),      # 0.1/h^2 (u-u')(v-v') on ghost facets
+    ]
+
+
 def terms_c1():
     return [
         dict(kind=0, domain=0, coef=1.0, hpow=0),       # u v on NEG (order 2)
@@ -145,6 +162,10 @@ def c5_slab_values(m, slab, kt_l):
 
 
 def workload_config(args):
+    if args.workload == "dg":
+        return {"workload": "3D unfitted DG Poisson (fictdom_dg form), %d^3x6 Kuhn tets, L2 P%d: NEG stiffness + "
+                            "Nitsche IF + interior-penalty / flux skeleton on the NEG part of the (HASNEG, HASNEG) "
+                            "facets + ghost penalty 0.1/h^2" % (args.n, args.order)}
     if args.workload == "c2":
         return {"workload": "3D CutFEM Poisson, %d^3x6 Kuhn tets, P%d, NEG stiffness + Nitsche IF + ghost "
                             "penalty 0.1/h^2" % (args.n, args.order)}
@@ -175,9 +196,10 @@ def cpu_prepare(args, sample):
             jobs.append(("st", sp, lst, terms_c5(s * C5_DT)))
         desc = "all %d slabs" % C5_SLABS if len(slabs) == C5_SLABS else "slabs %s of %d" % (slabs, C5_SLABS)
         return jobs, desc
-    if args.workload == "c2":
+    if args.workload in ("c2", "dg"):
         m, vals = c2_mesh(args.n)
-        groups = [(m, vals, args.order, terms_c2(args.order), True)]
+        tf = terms_dg if args.workload == "dg" else terms_c2
+        groups = [(m, vals, args.order, tf(args.order), True)]
         desc = "full workload"
     elif args.workload == "c1":
         copies = args.copies if not sample else min(args.copies, 64)
@@ -190,7 +212,8 @@ def cpu_prepare(args, sample):
         desc = "full workload" if count == args.meshes else "the first %d of the %d meshes" % (count, args.meshes)
     jobs = []
     for m, vals, order, terms, ghost in groups:
-        jobs.append(("plain", orc.Space(m, order), orc.interpolate_p1_perturb(vals), terms, ghost))
+        sp = orc.Space(m, order, l2=args.workload == "dg")
+        jobs.append(("plain", sp, orc.interpolate_p1_perturb(vals), terms, ghost))
     return jobs, desc
 
 
@@ -849,7 +872,9 @@ class Gpu:
         self.entries.append(e)
         return e
 
-    def marking_plain(self, dm, lset):
+    def marking_plain(self, dm, lset, skeleton=False):
+        """Counts of the step's sets; with skeleton=True the facet count is that
+        of the ghost facets joined with the (HASNEG, HASNEG) skeleton facets."""
         torch, xg = self.torch, self.xg
         ne, nf = dm.ne, dm.nfacets
         dom = torch.zeros(ne, dtype=torch.uint8, device="cuda")
@@ -859,6 +884,11 @@ class Gpu:
         self._lib.call("xg_cutinfo_update", dm.h, xg._vp(lset), xg._vp(dom), xg._vp(ratio), xg._vp(bits), self.sp)
         self._lib.call("xg_facets_with_neighbor_types", dm.h, xg._vp(bits[5]), xg._vp(bits[4]), 1, 1, 1, xg._vp(fb),
                        self.sp)
+        if skeleton:
+            fs = torch.zeros_like(fb)
+            self._lib.call("xg_facets_with_neighbor_types", dm.h, xg._vp(bits[5]), xg._vp(bits[5]), 1, 1, 1,
+                           xg._vp(fs), self.sp)
+            fb = fb | fs
         dm.check()
         return self._counts(dom, fb, nf, dm)
 
@@ -945,11 +975,15 @@ def oracle_csr(e, nth):
         rp, cols, rv = sp.assemble_st(lst, len(vals) - 1, 1, 2, t2, nthreads=nth)
     else:
         l = orc.interpolate_p1_perturb(vals)
-        sp = orc.Space(m, order)
+        sp = orc.Space(m, order, l2=e.get("l2", False))
         _, _, bits = sp.cutinfo(l, nthreads=nth)
         fb = sp.facets_with_neighbor_types(bits[5], bits[4], True, True, True)
+        # skeleton terms: NEG on (HASNEG, HASNEG) facets, POS on (HASPOS, HASPOS), whole facets on the ghost facets
+        fsk = {orc.NEG: sp.facets_with_neighbor_types(bits[5], bits[5], True, True, True),
+               orc.POS: sp.facets_with_neighbor_types(bits[6], bits[6], True, True, True), orc.WHOLE: fb}
         t2 = [dict(t, defined_on=fb if t["kind"] == orc.TERM_GHOST_MASS else
-                   {orc.NEG: bits[5], orc.IF: bits[4], orc.POS: bits[6]}[t["domain"]]) for t in terms]
+                   (fsk[t["domain"]] if t["kind"] >= orc.TERM_SKEL_JUMP else
+                    {orc.NEG: bits[5], orc.IF: bits[4], orc.POS: bits[6]}[t["domain"]])) for t in terms]
         rp, cols, rv = sp.assemble(l, t2, nthreads=nth)
     return np.repeat(np.arange(len(rp) - 1, dtype=np.int64), np.diff(rp)), cols, rv
 
@@ -992,11 +1026,11 @@ def setup(args, gpu):
     """Builds the workload's forms and steps on the device; returns the config."""
     xg = gpu.xg
     cfg = workload_config(args)
-    if args.workload in ("c2", "c1", "c3"):
-        if args.workload == "c2":
+    if args.workload in ("c2", "c1", "c3", "dg"):
+        if args.workload in ("c2", "dg"):
             m, vals = c2_mesh(args.n)
             groups = {args.order: (m, vals)}
-            tf = terms_c2
+            tf = terms_dg if args.workload == "dg" else terms_c2
         elif args.workload == "c1":
             m, vals = c1_mesh(args.copies)
             groups = {1: (m, vals)}
@@ -1006,17 +1040,18 @@ def setup(args, gpu):
             groups = c3_groups(args.meshes)
             cfg["host_mesh_gen_s"] = time.perf_counter() - t0
         for order, (m, vals) in groups.items():
-            V = xg.H1(m, order=order)
+            V = xg.L2(m, order=order) if args.workload == "dg" else xg.H1(m, order=order)
             lset = gpu.lset(vals)
             form = gpu.form(V.h, (terms_c2 if args.workload == "c3" else tf)(order))
             gpu.keep += [V, m]
-            mk = gpu.marking_plain(V.dm, lset)
+            mk = gpu.marking_plain(V.dm, lset, skeleton=args.workload == "dg")
             mk["ndof_el"] = V.ndof_el
             mk["order"] = order
             if args.workload == "c1":
                 mk["n_facets"] = 0  # no patch terms
             e = gpu.add(form, lset, False, mk)
             e["host"] = ("plain", m, vals, order, (terms_c2 if args.workload == "c3" else tf)(order))
+            e["l2"] = args.workload == "dg"
         if args.workload == "c3":
             cfg["groups"] = {str(k): {"n_tets": int(m.ne)} for k, (m, _) in groups.items()}
     else:
@@ -1049,7 +1084,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="xg", choices=["xg", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c3", "c4", "c5", "hex"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c3", "c4", "c5", "hex", "dg"])
     ap.add_argument("--train", type=int, default=2000000)
     ap.add_argument("--epochs", type=int, default=8)
     ap.add_argument("--kappa", type=float, default=0.05)
@@ -1239,7 +1274,7 @@ def main():
     # of the (2n)^2 patch matrix, one FMA = 2 FLOPs per entry and point,
     # 2 x NQ(2k) points per facet
     fp64 = None
-    if dname == "patch" and gpu.prec == 0:
+    if dname == "patch" and gpu.prec == 0 and args.workload != "dg":
         nq = {(2, 2): 3, (2, 4): 6, (2, 6): 16, (3, 2): 4, (3, 4): 14, (3, 6): 64}
         flops = 0.0
         for e in E:
@@ -1260,8 +1295,11 @@ def main():
         "nnz": sum(e["nnz"] for e in E), "precision": args.precision, "steps_per_graph": len(E),
         "l2": "flushed between timed steps (512 MB write)", "parallelism": "replicas only",
         "timing": "CUDA graph replay of the whole step, CUDA events on the launching stream"})
-    if args.workload == "c2":
+    if args.workload in ("c2", "dg"):
         cfg["order"] = args.order
+    if args.workload == "dg":
+        cfg["facets_note"] = "n_ghost_facets counts the ghost facets joined with the (HASNEG, HASNEG) skeleton facets"
+        cfg["space"] = "L2 (element-local dofs)"
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,

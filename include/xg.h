@@ -55,7 +55,7 @@ typedef enum {
   XG_ERR_TIMEOUT = 10      /* a bounded device-side wait gave up (the kernel stopped its work) */
 } xg_status;
 
-enum { XG_NEG = 0, XG_POS = 1, XG_IF = 2 };
+enum { XG_NEG = 0, XG_POS = 1, XG_IF = 2, XG_WHOLE = 3 /* skeleton terms: the whole facet */ };
 enum {
   XG_CDOM_NO = 0, XG_CDOM_NEG = 1, XG_CDOM_POS = 2, XG_CDOM_UNCUT = 3,
   XG_CDOM_IF = 4, XG_CDOM_HASNEG = 5, XG_CDOM_HASPOS = 6, XG_CDOM_ANY = 7
@@ -73,7 +73,23 @@ typedef enum {
   XG_TERM_U_NGRADV = 3,   /* c * u * (n . grad v)           */
   XG_TERM_CONV = 4,       /* c * (b . grad u) * v           */
   XG_TERM_GHOST_MASS = 5, /* c * (u - u') * (v - v') on a facet patch (dFacetPatch) */
-  XG_TERM_DT_U_V = 6      /* space-time: c * v * d/dtau u (dtref), space-time forms only */
+  XG_TERM_DT_U_V = 6,     /* space-time: c * v * d/dtau u (dtref), space-time forms only */
+  /* Skeleton terms on interior facets F (SymbolicCutFacetBilinearFormIntegrator,
+   * symboliccutbfi.cpp:886-1572, for domain XG_NEG / XG_POS: F cut to the
+   * domain by the P1 level set; SymbolicFacetBilinearFormIntegrator2,
+   * :1574-1735, for XG_WHOLE: all of F).  u / v live on the facet's first
+   * element, u' / v' on the second, n_F is the unit normal of F out of the
+   * first element; d_defined_on holds facet bits.  Integrated exactly with the
+   * reference's facet rule order 2 * order of the space (the term's order is
+   * not used).  XG_IF (codim-2 skeleton rules) is not supported. */
+  XG_TERM_SKEL_JUMP = 7,   /* c * (u - u') * (v - v')                                   */
+  XG_TERM_SKEL_FLUX = 8,   /* c * ((grad u + grad u') . n_F) * (v - v')                 */
+  XG_TERM_SKEL_FLUX_T = 9, /* c * (u - u') * ((grad v + grad v') . n_F)                 */
+  XG_TERM_SKEL_DN1 = 10,   /* c * [d_n u][d_n v], [d^k_n w] = d^k_nF w - d^k_nF w'; the
+                              reference's dn(w, k) - (-1)^k dn(w.Other(), k)
+                              (DiffOpDuDnk, ghostpenalty.cpp:221-365, python_xfem.cpp:1068) */
+  XG_TERM_SKEL_DN2 = 11,   /* c * [d^2_n u][d^2_n v] */
+  XG_TERM_SKEL_DN3 = 12    /* c * [d^3_n u][d^3_n v] */
 } xg_term_kind;
 
 typedef enum { XG_PREC_FP64 = 0, XG_PREC_MIXED = 1 } xg_precision;
@@ -128,6 +144,10 @@ int xg_mesh_facet_elements(const xg_mesh* mesh, int32_t* h_out);
 /* Dof numbering: vertices, then (order-1) dofs per edge (edges sorted by
  * vertex pair), then for order 3 one bubble per face (3D) / cell (2D). */
 int xg_space_create(xg_mesh* mesh, int order, xg_space** out);
+/* Discontinuous space (L2(mesh, order, dgjumps=True) of the reference's
+ * discontinuous-Galerkin forms): the element basis of xg_space_create with
+ * element-local dofs, dof(e, i) = e * ndof_per_element + i. */
+int xg_space_create_l2(xg_mesh* mesh, int order, xg_space** out);
 int xg_space_destroy(xg_space* space);
 /* out: [ndof, ndof_per_element, order] */
 int xg_space_info(const xg_space* space, int64_t* h_out3);
@@ -275,10 +295,15 @@ int xg_integrate_noalloc(xg_mesh* mesh, const double* d_lset, int dt, int order,
                          const uint64_t* d_defined_on, double* d_result, void* stream);
 
 /* ---- bilinear forms ---------------------------------------------------------- */
-/* A form is a list of integrators over one H1 space (trial = test space).
- * Volume terms run on their element sets with the cut rule of their domain;
- * patch terms run on their facet sets.  Creation uploads the term table and
- * sizes the workspace for the whole mesh (no allocation during assembly). */
+/* A form is a list of integrators over one space (H1 or L2; trial = test
+ * space).  Volume terms run on their element sets with the cut rule of their
+ * domain; patch and skeleton terms run on their facet sets (the facet's
+ * matrix is the sum of both kinds).  Creation uploads the term table and
+ * sizes the workspace for the whole mesh (no allocation during assembly).
+ * In xg_cutfem_step the skeleton terms run on the facets between two HASNEG
+ * (XG_NEG) or two HASPOS (XG_POS) elements and on the ghost facets
+ * (XG_WHOLE), as in demos/fictdom_dg.py.  Space-time forms take no skeleton
+ * terms. */
 int xg_form_create(xg_space* space, const xg_term* terms, int32_t nterms, int precision, xg_form** out);
 int xg_form_destroy(xg_form* form);
 /* Replace the element/facet set of term t (device bitset, NULL = all). */

@@ -22,7 +22,7 @@ STATUS = {
 EXPORTS = [
     "xg_status_string", "xg_last_error", "xg_device_ok",
     "xg_mesh_create", "xg_mesh_destroy", "xg_mesh_info", "xg_mesh_facet_elements",
-    "xg_space_create", "xg_space_destroy", "xg_space_info", "xg_space_element_dofs",
+    "xg_space_create", "xg_space_create_l2", "xg_space_destroy", "xg_space_info", "xg_space_element_dofs",
     "xg_interpolate_p1_perturb", "xg_cutinfo_update", "xg_mesh_check",
     "xg_facets_with_neighbor_types", "xg_elements_with_neighbor_facets",
     "xg_cut_rules", "xg_base_rule_size", "xg_base_rule", "xg_integrate", "xg_integrate_noalloc",
@@ -113,6 +113,7 @@ def load():
         "xg_mesh_info": (I, [P, P]),
         "xg_mesh_facet_elements": (I, [P, P]),
         "xg_space_create": (I, [P, I, P]),
+        "xg_space_create_l2": (I, [P, I, P]),
         "xg_space_destroy": (I, [P]),
         "xg_space_info": (I, [P, P]),
         "xg_space_element_dofs": (I, [P, P]),

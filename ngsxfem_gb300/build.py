@@ -34,6 +34,7 @@ UNITS = [
     ("xg_isomesh.cu", ["-fmad=false"]),
     ("xg_rows.cu", []),
     ("xg_mlp_tc.cu", []),
+    ("xg_skel.cu", []),
 ]
 
 

@@ -293,9 +293,12 @@ __global__ void k_active_facets(int64_t nf, const int32_t* __restrict__ fel, For
                                 int64_t nw32) {
   const int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   bool act = false;
-  if (f < nf && fel[nf + f] >= 0)
+  if (f < nf && fel[nf + f] >= 0) {
     for (int p = 0; p < form.npatch; p++)
       if (!form.p[p].defined_on || tbit(form.p[p].defined_on, f)) act = true;
+    for (int p = 0; p < form.nskel; p++)
+      if (!form.s[p].defined_on || tbit(form.s[p].defined_on, f)) act = true;
+  }
   unsigned m = __ballot_sync(0xffffffffu, act);
   if ((threadIdx.x & 31) == 0 && (f >> 5) < nw32) bits[f >> 5] = m;
 }
@@ -2595,6 +2598,7 @@ struct xg_form {
   double* d_ratio = nullptr;
   uint64_t* d_bits = nullptr;
   uint64_t* d_fbits = nullptr;
+  uint64_t* d_fbits_sk = nullptr;  // [2][facet words]: skeleton facets of the CutFEM step (NEG, POS)
   bool has_patch = false;
   cudaEvent_t ev[8] = {};
   bool use_ev = false;
@@ -2634,7 +2638,7 @@ int form_free(xg_form* f) {
   void* ptrs[] = {f->d_full_ptr, f->d_tmp_cols, f->d_fpos_el, f->d_pbuf, f->d_flags, f->d_pgeo, f->d_cgeo, f->d_csub,
                   f->d_tabs, f->d_tabs_f, f->d_act_un, f->d_act_cut, f->d_act_fa, f->d_dof_bits, f->d_l_un, f->d_l_cut, f->d_l_fa,
                   f->d_el_slot, f->d_fa_slot, f->d_dof_row, f->d_rowcnt, f->d_counts, f->d_bsum, f->d_bsum64,
-                  f->d_elmat, f->d_famat, f->d_err, f->d_dom, f->d_ratio, f->d_bits, f->d_fbits,
+                  f->d_elmat, f->d_famat, f->d_err, f->d_dom, f->d_ratio, f->d_bits, f->d_fbits, f->d_fbits_sk,
                   f->d_mtab_i, f->d_mtab_c, f->d_mu, f->d_mhat, f->d_cutlist, f->d_dof_flag,
                   f->d_el_rowslot, f->d_pos_rows, f->d_nbpos, f->d_cand_fs, f->d_act_slot, f->d_vcols, f->d_vvals,
                   f->d_bsum_rows};
@@ -2677,6 +2681,36 @@ int build_desc(xg_form* f) {
       P.c = T.coef;
       P.hpow = T.hpow;
       f->term_slot[t] = d.npatch++;
+      f->has_patch = true;
+      continue;
+    }
+    if (T.kind >= XG_TERM_SKEL_JUMP && T.kind <= XG_TERM_SKEL_DN3) {
+      // skeleton terms: grouped by (region, facet set), one facet rule per group
+      const int kk = T.kind - XG_TERM_SKEL_JUMP;
+      if (T.domain != XG_NEG && T.domain != XG_POS && T.domain != XG_WHOLE) {
+        set_last_error("xg_form: skeleton terms run on XG_NEG, XG_POS or XG_WHOLE (codim-2 rules are not built)");
+        return XG_ERR_UNSUPPORTED;
+      }
+      if (kk >= 3 && kk - 2 > f->space->order) {
+        set_last_error("xg_form: normal-derivative order above the order of the space");
+        return XG_ERR_ARG;
+      }
+      int g = -1;
+      for (int q = 0; q < d.nskel; q++)
+        if (d.s[q].region == T.domain && d.s[q].defined_on == T.d_defined_on && !((d.s[q].used >> kk) & 1)) g = q;
+      if (g < 0) {
+        if (d.nskel >= kMaxSkel) {
+          set_last_error("xg_form: too many skeleton term groups");
+          return XG_ERR_UNSUPPORTED;
+        }
+        g = d.nskel++;
+        d.s[g].region = T.domain;
+        d.s[g].defined_on = T.d_defined_on;
+      }
+      d.s[g].c[kk] = T.coef;
+      d.s[g].hpow[kk] = T.hpow;
+      d.s[g].used |= 1 << kk;
+      f->term_slot[t] = g;
       f->has_patch = true;
       continue;
     }
@@ -2907,7 +2941,7 @@ int patch_exact_setup_t(xg_form* f) {
 
 int upload_patch_tables(xg_form* f) {
   const int D = f->mesh->dim, K = f->space->order;
-  f->patch_exact = f->has_patch;
+  f->patch_exact = f->has_patch && f->desc.npatch > 0;
   for (int pp = 0; pp < f->desc.npatch; pp++)
     if (clamp_order(f->desc.p[pp].order) < 2 * K) f->patch_exact = false;
   cudaFree(f->d_mhat);
@@ -3639,7 +3673,10 @@ int form_workspace(xg_form* f) {
   const size_t fa_stride = precision == XG_PREC_FP64 || f->rows ? (size_t)(2 * nds) * (2 * nds)
                                                                  : (size_t)tri_size(2 * nds);
   const size_t fa_bytes = (size_t)m->nfacets * fa_stride * esz;
-  f->cap_fa = fa_bytes <= ((size_t)4 << 30) ? m->nfacets : std::max<int64_t>(m->nfacets / 4, 1);
+  // forms with skeleton terms (discontinuous-Galerkin skeletons touch most
+  // facets) keep a slot for every facet up to 48 GiB
+  const size_t fa_budget = f->desc.nskel > 0 ? ((size_t)48 << 30) : ((size_t)4 << 30);
+  f->cap_fa = fa_bytes <= fa_budget ? m->nfacets : std::max<int64_t>(m->nfacets / 4, 1);
   int64_t maxw = std::max(f->nw32_el, std::max(f->nw32_fa, f->nw32_dof));
   f->nbsum = (int)((maxw + kCChunk - 1) / kCChunk) + 1;
   f->nbsum64 = (int)((space->ndof + kSChunk - 1) / kSChunk) + 1;
@@ -3684,6 +3721,8 @@ int form_workspace(xg_form* f) {
   e = e ? e : A((void**)&f->d_ratio, (size_t)m->ne * 8);
   e = e ? e : A((void**)&f->d_bits, (size_t)8 * (f->nw32_el / 2) * 8);
   e = e ? e : A((void**)&f->d_fbits, (size_t)(f->nw32_fa / 2) * 8);
+  // CutFEM step: the skeleton facet sets (HASNEG | HASNEG, HASPOS | HASPOS)
+  e = e ? e : A((void**)&f->d_fbits_sk, f->desc.nskel ? (size_t)2 * (f->nw32_fa / 2) * 8 : 16);
   if (e == cudaSuccess) e = cudaMemset(f->d_err, 0, sizeof(int));
   if (e == cudaSuccess) e = cudaMemset(f->d_dof_flag, 0, (size_t)space->ndof);
   if (e == cudaSuccess) e = cudaMemset(f->d_counts, 0, 8 * sizeof(int));
@@ -3844,6 +3883,30 @@ int xg_form_assemble(xg_form* f, const double* d_lset, const uint8_t* d_dom, xg_
 
 namespace {
 
+// skeleton terms of the active facets, after the facet-patch terms (which
+// write the facet matrices; without them this kernel writes)
+int launch_skel(xg_form* f, const double* d_lset, cudaStream_t s) {
+  xg_mesh* m = f->mesh;
+  SkelLaunch A;
+  A.dim = m->dim;
+  A.order = f->space->order;
+  A.ne = m->ne;
+  A.nv = m->nv;
+  A.elv = m->d_elv;
+  A.xyz = m->d_xyz;
+  A.nf = m->nfacets;
+  A.fel = m->d_facet_els;
+  A.lset = d_lset;
+  A.l_fa = f->d_l_fa;
+  A.counts = f->d_counts;
+  A.famat = f->d_famat;
+  A.cap_fa = f->cap_fa;
+  A.accumulate = f->desc.npatch > 0 ? 1 : 0;
+  A.fp64 = f->precision == XG_PREC_FP64 ? 1 : 0;
+  A.err = f->d_err;
+  return skel_launch(A, f->desc, s);
+}
+
 // the element and patch kernels of one step (spatial forms: the element rows
 // at their static slots and the patch matrices by facet slot; the patch
 // matrices are left out when the form's patches run in a batched launch)
@@ -3852,7 +3915,9 @@ int rows_front(xg_form* f, const double* d_lset, const uint8_t* d_dom, cudaStrea
   int st;
   if ((st = fp64 ? dispatch_volume<double>(f, d_lset, d_dom, s) : dispatch_volume<float>(f, d_lset, d_dom, s)))
     return st;
-  if (f->has_patch && (st = fp64 ? dispatch_patch<double>(f, s) : dispatch_patch<float>(f, s))) return st;
+  if (f->has_patch && f->desc.npatch > 0 && (st = fp64 ? dispatch_patch<double>(f, s) : dispatch_patch<float>(f, s)))
+    return st;
+  if (f->desc.nskel > 0 && (st = launch_skel(f, d_lset, s))) return st;
   if (f->use_ev) cudaEventRecord(f->ev[5], s);
   return XG_OK;
 }
@@ -3933,6 +3998,15 @@ int cutfem_front(xg_form* f, const double* d_lset, xg_csr* out, void* stream) {
     st = xg_facets_with_neighbor_types(m, hasneg, ifb, 1, 1, 1, f->d_fbits, stream);
     if (st) return st;
   }
+  uint64_t* fb_neg = f->d_fbits_sk;
+  uint64_t* fb_pos = f->d_fbits_sk + f->nw32_fa / 2;
+  bool sk_neg = false, sk_pos = false;
+  for (int q = 0; q < f->desc.nskel; q++) {
+    sk_neg |= f->desc.s[q].region == XG_NEG;
+    sk_pos |= f->desc.s[q].region == XG_POS;
+  }
+  if (sk_neg && (st = xg_facets_with_neighbor_types(m, hasneg, hasneg, 1, 1, 1, fb_neg, stream))) return st;
+  if (sk_pos && (st = xg_facets_with_neighbor_types(m, haspos, haspos, 1, 1, 1, fb_pos, stream))) return st;
   // effective element / facet sets of the CutFEM form
   FormDesc saved = f->desc;
   for (int q = 0; q < f->desc.ngroups; q++) {
@@ -3940,6 +4014,12 @@ int cutfem_front(xg_form* f, const double* d_lset, xg_csr* out, void* stream) {
     G.defined_on = G.domain == XG_NEG ? hasneg : (G.domain == XG_IF ? ifb : haspos);
   }
   for (int p = 0; p < f->desc.npatch; p++) f->desc.p[p].defined_on = f->d_fbits;
+  // skeleton terms (demos/fictdom_dg.py:100-135): facets inside the domain's
+  // elements, whole-facet terms on the ghost facets
+  for (int q = 0; q < f->desc.nskel; q++) {
+    SkelDesc& S = f->desc.s[q];
+    S.defined_on = S.region == XG_NEG ? fb_neg : (S.region == XG_POS ? fb_pos : f->d_fbits);
+  }
   if (f->use_ev) cudaEventRecord(f->ev[1], (cudaStream_t)stream);
   st = assemble_front(f, d_lset, f->d_dom, out, stream);
   f->desc = saved;
@@ -4482,7 +4562,7 @@ int xg_step_graph_create(xg_form* const* forms, const double* const* d_lsets, co
   std::vector<xg_form*> multi;
   if (nb == n)
     for (xg_form* f : distinct)
-      if (f->rows && f->has_patch && f->patch_exact) multi.push_back(f);
+      if (f->rows && f->has_patch && f->patch_exact && f->desc.npatch > 0 && f->desc.nskel == 0) multi.push_back(f);
   if (multi.size() < 2) multi.clear();
   int* d_queue = nullptr;
   if (!multi.empty()) XG_CUDA(cudaMalloc((void**)&d_queue, multi.size() * sizeof(int)));

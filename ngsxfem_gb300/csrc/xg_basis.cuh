@@ -94,6 +94,45 @@ __host__ __device__ __forceinline__ T eval_fn_value(int desc, const T* lam) {
   return lam[a] * lam[b] * lam[c];
 }
 
+// Derivatives of order 0..J along a fixed direction of function `desc`, with
+// del[i] the derivative of lambda_i along it: every function is a product of
+// at most three affine factors (the cubic edge function lambda_a lambda_b
+// (lambda_a - lambda_b)), so along x + t n it is a cubic in t whose j-th
+// coefficient times j! is the j-th derivative.  out[j], j = 0..J.
+template <int J, typename T>
+__host__ __device__ __forceinline__ void eval_fn_dir(int desc, const T* lam, const T* del, T* out) {
+  const int type = desc & 15, a = (desc >> 4) & 15, b = (desc >> 8) & 15, c = (desc >> 12) & 15;
+  T v[3], d[3];
+  int m;
+  v[0] = lam[a];
+  d[0] = del[a];
+  if (type == 0) {
+    m = 1;
+  } else {
+    v[1] = lam[b];
+    d[1] = del[b];
+    m = type == 1 ? 2 : 3;
+    if (type == 2) {
+      v[2] = lam[a] - lam[b];
+      d[2] = del[a] - del[b];
+    } else if (type == 3) {
+      v[2] = lam[c];
+      d[2] = del[c];
+    }
+  }
+  T p0 = 1, p1 = 0, p2 = 0, p3 = 0;  // coefficients of t^0..t^3
+  for (int i = 0; i < m; i++) {
+    p3 = p3 * v[i] + p2 * d[i];
+    p2 = p2 * v[i] + p1 * d[i];
+    p1 = p1 * v[i] + p0 * d[i];
+    p0 = p0 * v[i];
+  }
+  out[0] = p0;
+  if (J >= 1) out[1] = p1;
+  if (J >= 2) out[2] = (T)2 * p2;
+  if (J >= 3) out[3] = (T)6 * p3;
+}
+
 // FP64 accumulation for the plain path; FP32 with Kahan compensation per
 // entry for the mixed path.
 template <typename T>

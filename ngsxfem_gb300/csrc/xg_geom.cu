@@ -31,6 +31,7 @@ int ensure_device_rules() {
   if (!st) st = upload_rules_quad_int();
   if (!st) st = upload_rules_mlset();
   if (!st) st = upload_rules_isomesh();
+  if (!st) st = upload_rules_skel();
   if (st) return st;
   done.push_back(dev);
   return XG_OK;

@@ -503,6 +503,48 @@ int xg_space_create(xg_mesh* m, int order, xg_space** out) {
   return XG_OK;
 }
 
+int xg_space_create_l2(xg_mesh* m, int order, xg_space** out) {
+  if (!m || !out || order < 1 || order > 3) {
+    set_last_error("xg_space_create_l2: order must be 1..3");
+    return XG_ERR_ARG;
+  }
+  if (m->tensor) {
+    set_last_error("xg_space_create_l2: L2 spaces are built on simplex meshes only");
+    return XG_ERR_UNSUPPORTED;
+  }
+  *out = nullptr;
+  auto* s = new xg_space();
+  const int D = m->dim, ne = m->ne;
+  s->mesh = m;
+  s->order = order;
+  s->nd = D == 2 ? (order + 1) * (order + 2) / 2 : (order + 1) * (order + 2) * (order + 3) / 6;
+  s->nds = s->nd;
+  const int nd = s->nd;
+  s->ndof = (int64_t)ne * nd;
+  s->ndof_s = s->ndof;
+  if (s->ndof >= ((int64_t)1 << 31)) {
+    delete s;
+    set_last_error("xg_space_create_l2: more than 2^31 dofs");
+    return XG_ERR_CAPACITY;
+  }
+  s->h_el_dofs.resize((size_t)s->ndof);
+  std::vector<int32_t> ptr(s->ndof + 1), adj((size_t)s->ndof);
+  for (int64_t i = 0; i < s->ndof; i++) {
+    s->h_el_dofs[i] = (int32_t)i;
+    ptr[i + 1] = (int32_t)(i + 1);
+    adj[i] = (int32_t)((i / nd) * 32 + i % nd);
+  }
+  s->max_adj = 1;
+  int st;
+  if ((st = upload(&s->d_el_dofs, to_soa(s->h_el_dofs, ne, nd))) || (st = upload(&s->d_el_dofs_aos, s->h_el_dofs)) ||
+      (st = upload(&s->d_dof_adj_ptr, ptr)) || (st = upload(&s->d_dof_adj, adj))) {
+    xg_space_destroy(s);
+    return st;
+  }
+  *out = s;
+  return XG_OK;
+}
+
 int xg_space_create_st(xg_mesh* m, int order, int order_time, xg_space** out) {
   if (!m || !out || order < 1 || order > 3 || order_time < 0 || order_time > 2) {
     set_last_error("xg_space_create_st: space order 1..3, time order 0..2");

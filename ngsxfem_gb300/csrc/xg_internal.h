@@ -100,11 +100,24 @@ struct PatchDesc {
   double c;
   int hpow;
 };
+// skeleton terms (XG_TERM_SKEL_*) with equal (region, defined_on) share one
+// facet rule; c / hpow per kind, index kind - XG_TERM_SKEL_JUMP
+constexpr int kMaxSkel = 4;
+constexpr int kSkelKinds = 6;
+struct SkelDesc {
+  int region;                  // XG_NEG / XG_POS: the facet cut to the domain; XG_WHOLE: all of it
+  const uint64_t* defined_on;  // facet bits, NULL = every interior facet
+  int used;                    // bit (kind - XG_TERM_SKEL_JUMP)
+  double c[kSkelKinds];
+  int hpow[kSkelKinds];
+};
 struct FormDesc {
   int ngroups;
   GroupDesc g[kMaxGroups];
   int npatch;
   PatchDesc p[kMaxPatch];
+  int nskel;
+  SkelDesc s[kMaxSkel];
 };
 
 // space-time volume terms with equal (domain, order, defined_on, tref,
@@ -153,6 +166,28 @@ int upload_rules_quad();
 int upload_rules_quad_int();
 int upload_rules_mlset();
 int upload_rules_isomesh();
+int upload_rules_skel();  // xg_skel.cu
+
+// skeleton terms of a form (xg_skel.cu): the facet matrices of the active
+// facet list, written into (accumulate = 0) or added to (1) famat, full rows
+// of 2 nd per facet slot
+struct SkelLaunch {
+  int dim, order;
+  int ne, nv;
+  const int32_t* elv;   // [D+1][ne]
+  const double* xyz;    // [3][nv]
+  int64_t nf;
+  const int32_t* fel;   // [2][nf]
+  const double* lset;   // P1 vertex values
+  const int32_t* l_fa;  // active facets
+  const int* counts;    // [2]: number of active facets
+  void* famat;
+  int64_t cap_fa;
+  int accumulate;
+  int fp64;
+  int* err;
+};
+int skel_launch(const SkelLaunch& a, const FormDesc& form, cudaStream_t s);
 int quad_rule_capacity(int dim, int dt, int order);
 int quad_cut_rules(xg_mesh* m, const double* d_lset, const int32_t* d_elems, int32_t n, int dt, int order, int pol,
                    int32_t max_pts, int32_t* d_counts, double* d_pts, double* d_wts, void* stream);

@@ -14,7 +14,9 @@ script written like demos/fictdom.py:95-133 keeps its structure:
 Every operation runs on the GPU through libxg (include/xg.h); device memory is
 held in torch tensors.  Integrands are parsed into the term menu of the C ABI
 (mass, Laplace, Nitsche normal-derivative terms, convection, ghost-penalty
-patch mass); anything outside the menu raises.
+patch mass, and on interior facets the jump / average skeleton terms and
+normal-derivative jumps of discontinuous-Galerkin forms, demos/fictdom_dg.py);
+anything outside the menu raises.
 """
 import ctypes
 
@@ -25,6 +27,7 @@ from . import _lib
 from .meshes import Mesh, MakeStructured2DMesh, MakeStructured3DMesh  # noqa: F401
 
 NEG, POS, IF = 0, 1, 2
+WHOLE = 3  # skeleton terms over the whole facet (dx(skeleton=True))
 # direction policy of the quadrilateral / hexahedral cut rules
 # (python/python_ngsxfem.cpp:35-37: FIRST_ALLOWED, FIND_OPTIMAL, ALWAYS_NONE)
 FIRST, OPTIMAL, FALLBACK = 0, 1, 2
@@ -33,6 +36,7 @@ UNCUT, HASNEG, HASPOS, ANY = CDOM_UNCUT, CDOM_HASNEG, CDOM_HASPOS, CDOM_ANY
 VOL, BND = "VOL", "BND"
 
 TERM_MASS, TERM_LAPLACE, TERM_NGRADU_V, TERM_U_NGRADV, TERM_CONV, TERM_GHOST_MASS, TERM_DT_U_V = range(7)
+TERM_SKEL_JUMP, TERM_SKEL_FLUX, TERM_SKEL_FLUX_T, TERM_SKEL_DN1, TERM_SKEL_DN2, TERM_SKEL_DN3 = range(7, 13)
 PREC_FP64, PREC_MIXED = 0, 1
 XG_LTERM_SOURCE, XG_LTERM_SOURCE_GF, XG_LTERM_SOURCE_BND = 0, 1, 2
 
@@ -180,6 +184,25 @@ class H1:
         if getattr(self, "h", None) and _lib._lib is not None:
             _lib.load().xg_space_destroy(self.h)
             self.h = None
+
+
+class L2(H1):
+    """Discontinuous space L2(mesh, order, dgjumps=True) of order 1..3 on a
+    simplex mesh: the H1 element basis with element-local dofs,
+    dof(e, i) = e * ndof_per_element + i (xg_space_create_l2)."""
+
+    def __init__(self, mesh, order=1, dgjumps=True, **kwargs):
+        self.mesh = mesh
+        self.order = int(order)
+        self.dm = device_mesh(mesh)
+        if getattr(mesh, "tensor", False):
+            raise NotImplementedError("L2 spaces are built on simplex meshes")
+        h = ctypes.c_void_p()
+        _lib.call("xg_space_create_l2", self.dm.h, self.order, ctypes.byref(h))
+        self.h = h
+        info = np.zeros(3, dtype=np.int64)
+        _lib.call("xg_space_info", self.h, info.ctypes.data_as(ctypes.c_void_p))
+        self.ndof, self.ndof_el = int(info[0]), int(info[1])
 
 
 class ScalarTimeFE:
@@ -518,8 +541,11 @@ class _Expr:
     def Other(self):
         out = []
         for m in self.monos:
-            scal = tuple((a[0], True) if a[0] in ("u", "v") else a for a in m.scal)
-            out.append(_Mono(m.c, m.hpow, scal, m.dots, m.vec))
+            scal = tuple(((a[0], True) + tuple(a[2:])) if a[0] in ("u", "v", "dnu", "dnv") else a for a in m.scal)
+            vec = m.vec
+            if vec is not None and vec[0] in ("gu", "gv"):
+                vec = (vec[0], True)
+            out.append(_Mono(m.c, m.hpow, scal, m.dots, vec))
         return _Expr(out)
 
 
@@ -533,6 +559,22 @@ def grad(x):
 
 def InnerProduct(a, b):
     return _Expr.wrap(a) * _Expr.wrap(b)
+
+
+def dn(proxy, order, comp=-1, hdiv=False):
+    """k-th derivative of a trial / test function along the outward unit normal
+    of the facet's element it lives on (python_xfem.cpp:1068-1150, DiffOpDuDnk):
+    for u.Other() that is the second element's normal, so the jump across a
+    facet is dn(u, k) - (-1)^k dn(u.Other(), k).  Skeleton integrals only."""
+    if comp != -1 or hdiv:
+        raise NotImplementedError("dn of scalar H1 / L2 functions only")
+    if not (isinstance(proxy, _Expr) and len(proxy.monos) == 1 and len(proxy.monos[0].scal) == 1
+            and proxy.monos[0].scal[0][0] in ("u", "v") and proxy.monos[0].c == 1.0):
+        raise TypeError("dn() of a trial or test function (or its .Other())")
+    name, other = proxy.monos[0].scal[0][:2]
+    if not 1 <= int(order) <= 3:
+        raise NotImplementedError("dn of order 1..3")
+    return _Expr([_Mono(scal=(("dn" + name, other, int(order)),))])
 
 
 class _LsetGrad:
@@ -551,6 +593,11 @@ class _SpecialCF:
     def mesh_size(self):
         return _Expr([_Mono(hpow=1)])
 
+    def normal(self, dim=None):
+        """Unit normal of a facet, out of the facet's first element (skeleton
+        integrals)."""
+        return _Expr([_Mono(vec=("nF", None))])
+
 
 specialcf = _SpecialCF()
 
@@ -564,7 +611,12 @@ class _Measure:
         self.kind, self.levelset, self.domain_type, self.order = kind, levelset, domain_type, order
         self.definedonelements = definedonelements
         self.scale = 1.0
-        for k in ("deformation", "skeleton", "element_boundary", "element_vb"):
+        self.skeleton = bool(kw.get("skeleton", False))
+        if self.skeleton and kind not in ("cut", "skel"):
+            raise NotImplementedError("skeleton=True applies to dCut and dx")
+        if self.skeleton and kind == "cut" and domain_type not in (NEG, POS):
+            raise NotImplementedError("dCut(..., skeleton=True) on NEG or POS (codim-2 skeleton rules are not built)")
+        for k in ("deformation", "element_boundary", "element_vb"):
             if kw.get(k) is not None and kw.get(k) is not False:
                 raise NotImplementedError("dCut/dFacetPatch option %r is not part of the GPU path" % k)
         self.definedon = kw.get("definedon")
@@ -600,6 +652,16 @@ def dCut(levelset, domain_type, order=None, subdivlvl=None, time_order=-1, level
             kwargs.setdefault("quad_dir_policy", levelset_domain["quad_dir_policy"])
     return _Measure("cut", levelset, domain_type, order, kwargs.pop("definedonelements", None),
                     subdivlvl=subdivlvl, time_order=time_order, **kwargs)
+
+
+def dx(skeleton=False, definedonelements=None, **kwargs):
+    """Whole-facet skeleton integrals (SymbolicFacetBilinearFormIntegrator2,
+    symboliccutbfi.cpp:1574-1735), e.g. the derivative-jump ghost penalty
+    dn-jumps * dx(skeleton=True, definedonelements=ghost_facets).  Volume
+    integrals without a level set are not part of the GPU path."""
+    if not skeleton:
+        raise NotImplementedError("dx without skeleton=True: use dCut for element integrals")
+    return _Measure("skel", None, WHOLE, kwargs.pop("order", None), definedonelements, skeleton=True, **kwargs)
 
 
 def dFacetPatch(**kwargs):
@@ -642,6 +704,8 @@ class _Integral:
                 out.append(dict(kind=TERM_GHOST_MASS, domain=NEG, order=-1 if m.order is None else m.order,
                                 hpow=hp, coef=c_uv * m.scale, b=(0.0, 0.0, 0.0), defined_on=m.definedonelements))
             return out
+        if m.skeleton:
+            return self._skeleton_terms()
         dom = m.domain_type
         for mono in self.expr.monos:
             if mono.vec is not None:
@@ -679,6 +743,70 @@ class _Integral:
             out.append(dict(kind=kind, domain=dom, order=-1 if m.order is None else m.order, hpow=mono.hpow,
                             coef=mono.c * m.scale, b=b, defined_on=m.definedonelements, tb=tb,
                             tref=m.tref, time_order=m.time_order))
+        return out
+
+
+    def _skeleton_terms(self):
+        """Skeleton integrand -> XG_TERM_SKEL_* terms.  Every monomial is
+        c * h^p * (trial factor) * (test factor), a factor being the value or
+        the j-th derivative along n_F of the function on the facet's first
+        (side 0) or second (side 1, .Other()) element; dn(w.Other(), k) is
+        turned to n_F with (-1)^k.  The coefficients of each (trial kind, test
+        kind) block must form one menu term: [u][v] (value, value), the
+        flux {grad u . n_F}[v] (first derivative, value), its transpose, or
+        [d^k u][d^k v] (k, k)."""
+        m = self.measure
+        blocks = {}
+        for mono in self.expr.monos:
+            if mono.vec is not None:
+                raise TypeError("integrand is a vector, not a scalar")
+            fac = {}
+            c = mono.c
+            for a in mono.scal:
+                if a[0] in ("u", "v"):
+                    fac.setdefault(a[0], []).append((0, 1 if a[1] else 0))
+                elif a[0] in ("dnu", "dnv"):
+                    k = a[2]
+                    if a[1] and k % 2 == 1:
+                        c = -c  # the second element's outward normal is -n_F
+                    fac.setdefault(a[0][2], []).append((k, 1 if a[1] else 0))
+                else:
+                    raise NotImplementedError("skeleton integrands: trial / test values and normal derivatives")
+            for d in mono.dots:
+                names = [x[0] for x in d]
+                if "nF" not in names:
+                    raise NotImplementedError("skeleton integrands: gradients only as grad(.) * specialcf.normal")
+                g = d[1] if d[0][0] == "nF" else d[0]
+                if g[0] not in ("gu", "gv"):
+                    raise NotImplementedError("skeleton integrands: gradients only as grad(.) * specialcf.normal")
+                fac.setdefault(g[0][1], []).append((1, 1 if g[1] else 0))
+            if len(fac.get("u", [])) != 1 or len(fac.get("v", [])) != 1:
+                raise NotImplementedError("skeleton integrands need one trial and one test factor per product")
+            (ku, su), (kv, sv) = fac["u"][0], fac["v"][0]
+            key = (mono.hpow, ku, kv)
+            blocks.setdefault(key, np.zeros((2, 2)))
+            blocks[key][su, sv] += c
+        jump = np.array([[1.0, -1.0], [-1.0, 1.0]])
+        mean_jump = np.array([[1.0, -1.0], [1.0, -1.0]])  # [su][sv]: trial mean, test jump
+        out = []
+        for (hp, ku, kv), B in sorted(blocks.items()):
+            if ku == kv == 0:
+                kind, P = TERM_SKEL_JUMP, jump
+            elif ku == 1 and kv == 0:
+                kind, P = TERM_SKEL_FLUX, mean_jump
+            elif ku == 0 and kv == 1:
+                kind, P = TERM_SKEL_FLUX_T, mean_jump.T
+            elif ku == kv and ku >= 1:
+                kind, P = TERM_SKEL_DN1 + ku - 1, jump
+            else:
+                raise NotImplementedError("skeleton integrand block (%d, %d) is outside the menu" % (ku, kv))
+            cc = B[0, 0] / P[0, 0]
+            if np.abs(B - cc * P).max() > 1e-14 * max(1.0, abs(cc)):
+                raise NotImplementedError("skeleton integrand is not a jump / average product: %s" % B.tolist())
+            if cc == 0.0:
+                continue
+            out.append(dict(kind=kind, domain=m.domain_type, order=-1, hpow=hp, coef=cc * m.scale, b=(0.0, 0.0, 0.0),
+                            defined_on=m.definedonelements, tb=None, tref=None, time_order=-1))
         return out
 
 

@@ -12,8 +12,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liboracle.so")
 
-NEG, POS, IF = 0, 1, 2
+NEG, POS, IF, WHOLE = 0, 1, 2, 3
 TERM_MASS, TERM_LAPLACE, TERM_NGRADU_V, TERM_U_NGRADV, TERM_CONV, TERM_GHOST_MASS, TERM_DT_U_V = range(7)
+TERM_SKEL_JUMP, TERM_SKEL_FLUX, TERM_SKEL_FLUX_T, TERM_SKEL_DN1, TERM_SKEL_DN2, TERM_SKEL_DN3 = range(7, 13)
 
 
 class Term(ctypes.Structure):
@@ -65,6 +66,12 @@ def lib():
         L.orc_straight_cut_rule.argtypes = [ctypes.c_int, P, P, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int]
         L.orc_space_create.restype = P
         L.orc_space_create.argtypes = [ctypes.c_int, ctypes.c_int, P, ctypes.c_int, P, ctypes.c_int]
+        L.orc_space_create_l2.restype = P
+        L.orc_space_create_l2.argtypes = [ctypes.c_int, ctypes.c_int, P, ctypes.c_int, P, ctypes.c_int]
+        L.orc_facet_matrix.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P]
+        L.orc_fd_stencil.argtypes = [ctypes.c_int, ctypes.c_int, P, P]
+        L.orc_assemble_ex.restype = P
+        L.orc_assemble_ex.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.orc_space_destroy.argtypes = [P]
         L.orc_space_info.argtypes = [P, P]
         L.orc_space_el_dofs.argtypes = [P, P]
@@ -410,13 +417,24 @@ class LTerm(ctypes.Structure):
                 ("coef", ctypes.c_double), ("gf", ctypes.c_void_p), ("defined_on", ctypes.c_void_p)]
 
 
-class Space:
-    """H1 space of order k over a simplex mesh, with the oracle's topology."""
+def fd_stencil(k, acc=4):
+    """Central finite-difference stencil of DiffOpDuDnk (offsets -w..w) and its
+    step factor (times the element size)."""
+    c = np.zeros(16)
+    eps = np.zeros(1)
+    w = lib().orc_fd_stencil(k, acc, _p(c), _p(eps))
+    return c[: 2 * w + 1].copy(), float(eps[0])
 
-    def __init__(self, mesh, order):
+
+class Space:
+    """H1 space of order k over a simplex mesh, with the oracle's topology
+    (l2=True: the discontinuous space, element-local dofs)."""
+
+    def __init__(self, mesh, order, l2=False):
         self.mesh = mesh
         self.order = order
-        self.h = lib().orc_space_create(mesh.dim, mesh.nv, _p(mesh.coords), mesh.ne, _p(mesh.elements), order)
+        create = lib().orc_space_create_l2 if l2 else lib().orc_space_create
+        self.h = create(mesh.dim, mesh.nv, _p(mesh.coords), mesh.ne, _p(mesh.elements), order)
         if not self.h:
             raise ValueError("bad space")
         info = np.zeros(5, dtype=np.int64)
@@ -566,11 +584,24 @@ class Space:
             raise RuntimeError("oracle patch matrix error %d" % r)
         return out
 
-    def assemble(self, lset, terms, nthreads=1):
+    def facet_matrix(self, lset, terms, f, dn_fd=False):
+        """Patch and skeleton terms of facet f ((2n)^2, row = test)."""
+        arr, keep = self._terms(terms)
+        n = 2 * self.ndof_el
+        out = np.zeros((n, n))
+        l = None if lset is None else np.ascontiguousarray(lset, dtype=np.float64)
+        r = lib().orc_facet_matrix(self.h, _p(l), ctypes.cast(arr, ctypes.c_void_p), len(terms), f, int(dn_fd),
+                                   _p(out))
+        if r:
+            raise RuntimeError("oracle facet matrix error %d" % r)
+        return out
+
+    def assemble(self, lset, terms, nthreads=1, dn_fd=False):
         """Returns scipy-free CSR triple (rowptr int64, cols int32, vals float64) over all dofs."""
         arr, keep = self._terms(terms)
         l = np.ascontiguousarray(lset, dtype=np.float64)
-        c = lib().orc_assemble(self.h, _p(l), ctypes.cast(arr, ctypes.c_void_p), len(terms), nthreads)
+        c = lib().orc_assemble_ex(self.h, _p(l), ctypes.cast(arr, ctypes.c_void_p), len(terms), nthreads,
+                                  int(dn_fd))
         if not c:
             raise RuntimeError("oracle assembly error")
         nnz = lib().orc_csr_nnz(c)

@@ -702,6 +702,24 @@ orc_space* orc_space_create(int D, int nv, const double* coords, int ne, const i
 
 void orc_space_destroy(orc_space* s) { delete s; }
 
+// L2(mesh, order, dgjumps=True) stand-in: the H1 element basis with
+// element-local dofs (the reference's L2 uses NGSolve's own discontinuous
+// basis; any basis of P_k per element spans the same space).
+orc_space* orc_space_create_l2(int D, int nv, const double* coords, int ne, const int32_t* elv, int order) {
+  orc_space* s = orc_space_create(D, nv, coords, ne, elv, order);
+  if (!s) return nullptr;
+  s->ndof = (int64_t)ne * s->nd;
+  for (int e = 0; e < ne; e++)
+    for (int i = 0; i < s->nd; i++) s->el_dofs[(size_t)e * s->nd + i] = (int32_t)((int64_t)e * s->nd + i);
+  s->dof_adj_ptr.assign(s->ndof + 1, 0);
+  s->dof_adj.resize(s->el_dofs.size());
+  for (int64_t i = 0; i < s->ndof; i++) {
+    s->dof_adj_ptr[i + 1] = i + 1;
+    s->dof_adj[i] = (int32_t)((i / s->nd) * 32 + i % s->nd);
+  }
+  return s;
+}
+
 int orc_space_info(const orc_space* s, int64_t* out) {
   out[0] = s->ndof; out[1] = s->nedges; out[2] = s->nfaces; out[3] = s->nfacets; out[4] = s->nd;
   return 0;
@@ -780,7 +798,7 @@ int element_matrix(const orc_space* s, const double* lset_vertex, const orc_term
   }
   for (int t = 0; t < nterms; t++) {
     const orc_term& T = terms[t];
-    if (T.kind == ORC_TERM_GHOST_MASS) continue;
+    if (T.kind == ORC_TERM_GHOST_MASS || T.kind >= ORC_TERM_SKEL_JUMP) continue;
     if (T.defined_on && !test_bit(T.defined_on, e)) continue;
     int order = T.order >= 0 ? T.order : default_order(T.kind, s->k);
     int np = straight_cut_rule(g, l, T.domain, order, pts, wts);
@@ -909,6 +927,290 @@ int patch_matrix(const orc_space* s, const orc_term* terms, int nterms, int f, d
     }
   }
   return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Skeleton terms on interior facets.
+//
+// SymbolicCutFacetBilinearFormIntegrator::T_CalcFacetMatrix
+// (symboliccutbfi.cpp:886-1572): the facet's level-set values (the P1 vertex
+// values) give StraightCutIntegrationRuleUntransformed on the facet simplex
+// with order 2 * maxorder (:947-1042); the rule is mapped into both elements
+// (Facet2ElementTrafo, :1044-1048) and weighted by the facet measure of the
+// first element's mapped point (:1126-1130, codim 1).  The uncut facet
+// integrator SymbolicFacetBilinearFormIntegrator2 (:1574-1735) is the same on
+// the plain facet rule.  Test and trial functions of the first element fill
+// rows / columns [0, n), those of the second (.Other()) [n, 2n) (:1098-1109).
+// The integrands are the menu ORC_TERM_SKEL_*; dn(w, k) of the reference
+// (python_xfem.cpp:1068-1150, DiffOpDuDnk) differentiates along the normal of
+// the element w lives on, so with n_F = the first element's outward normal
+// the jump [d^k_n w] = d^k_nF w - d^k_nF w' is dn(w, k) - (-1)^k dn(w.Other(), k).
+// ---------------------------------------------------------------------------
+
+// CentralFDStencils (ghostpenalty.cpp:8-140): the central stencil of width
+// w = acc/2 + floor(k - 1/2)/2 with sum_l c_l (l - w)^m / m! = delta_{m,k}
+// (m = 0 .. 2w), by Gaussian elimination with partial pivoting; GetOptimalEps
+// = ((2w + 1) eps_mach)^(1 / (acc + k)).
+int fd_stencil(int k, int acc, double* c, double* eps) {
+  const int w = (acc + 1) / 2 + (int)(k - 0.5) / 2, n = 2 * w + 1;
+  std::vector<double> A((size_t)n * (n + 1));
+  double inv_fact = 1.0;
+  for (int m = 0; m < n; m++) {
+    if (m > 0) inv_fact /= m;
+    for (int l = 0; l < n; l++) A[(size_t)m * (n + 1) + l] = std::pow((double)(l - w), m) * inv_fact;
+    A[(size_t)m * (n + 1) + n] = m == k ? 1.0 : 0.0;
+  }
+  for (int col = 0; col < n; col++) {
+    int piv = col;
+    for (int r = col + 1; r < n; r++)
+      if (std::fabs(A[(size_t)r * (n + 1) + col]) > std::fabs(A[(size_t)piv * (n + 1) + col])) piv = r;
+    if (piv != col)
+      for (int q = 0; q <= n; q++) std::swap(A[(size_t)col * (n + 1) + q], A[(size_t)piv * (n + 1) + q]);
+    for (int r = 0; r < n; r++) {
+      if (r == col) continue;
+      const double fct = A[(size_t)r * (n + 1) + col] / A[(size_t)col * (n + 1) + col];
+      for (int q = col; q <= n; q++) A[(size_t)r * (n + 1) + q] -= fct * A[(size_t)col * (n + 1) + q];
+    }
+  }
+  for (int l = 0; l < n; l++) c[l] = A[(size_t)l * (n + 1) + n] / A[(size_t)l * (n + 1) + l];
+  *eps = std::pow((2 * w + 1) * 2.220446049250313e-16, 1.0 / (acc + k));
+  return w;
+}
+
+// barycentric coordinates of the physical point x in element g
+void phys_to_lam(const Geo& g, const double* x, double* lam) {
+  const int D = g.D;
+  double s = 0;
+  for (int i = 0; i < D; i++) {
+    double v = 0;
+    for (int k = 0; k < D; k++) v += g.Finv[i][k] * (x[k] - g.x0[k]);
+    lam[i] = v;
+    s += v;
+  }
+  lam[D] = 1.0 - s;
+}
+
+// d lambda_i / d n (physical direction n) for all D + 1 barycentrics
+void lam_dir(const Geo& g, const double* n, double* del) {
+  const int D = g.D;
+  double s = 0;
+  for (int i = 0; i < D; i++) {
+    double v = 0;
+    for (int k = 0; k < D; k++) v += g.Finv[i][k] * n[k];
+    del[i] = v;
+    s += v;
+  }
+  del[D] = -s;
+}
+
+// j-th derivative along t of prod_m lambda_f[m](x + t n) at t = 0: j! times the
+// coefficient of t^j in prod_m (lam_f[m] + t del_f[m])
+double prod_dir(const int* f, int nf, const double* lam, const double* del, int j) {
+  if (j > nf) return 0.0;
+  double poly[4] = {1.0, 0.0, 0.0, 0.0};
+  for (int m = 0; m < nf; m++) {
+    for (int p = m + 1; p >= 1; p--) poly[p] = poly[p] * lam[f[m]] + poly[p - 1] * del[f[m]];
+    poly[0] *= lam[f[m]];
+  }
+  double fact = 1.0;
+  for (int i = 2; i <= j; i++) fact *= i;
+  return fact * poly[j];
+}
+
+// j-th derivative along n of every basis function (the products of basis())
+void basis_dir(int D, int k, const int* gv, const double* lam, const double* del, int j, double* out) {
+  int n = 0;
+  for (int i = 0; i <= D; i++) {
+    const int f[1] = {i};
+    out[n++] = prod_dir(f, 1, lam, del, j);
+  }
+  if (k >= 2) {
+    const int ne = D == 2 ? 3 : 6;
+    for (int e = 0; e < ne; e++) {
+      const int a = D == 2 ? TRI_EDGES[e][0] : TET_EDGES[e][0];
+      const int b = D == 2 ? TRI_EDGES[e][1] : TET_EDGES[e][1];
+      const int si = gv[a] < gv[b] ? a : b, ei = gv[a] < gv[b] ? b : a;
+      const int q[2] = {si, ei};
+      out[n++] = prod_dir(q, 2, lam, del, j);
+      if (k >= 3) {
+        const int c1[3] = {si, si, ei}, c2[3] = {si, ei, ei};
+        out[n++] = prod_dir(c1, 3, lam, del, j) - prod_dir(c2, 3, lam, del, j);
+      }
+    }
+  }
+  if (k >= 3) {
+    const int nf = D == 2 ? 1 : 4;
+    for (int f = 0; f < nf; f++) {
+      const int t[3] = {D == 2 ? 0 : TET_FACES[f][0], D == 2 ? 1 : TET_FACES[f][1], D == 2 ? 2 : TET_FACES[f][2]};
+      out[n++] = prod_dir(t, 3, lam, del, j);
+    }
+  }
+}
+
+// DiffOpDuDnk<D, k>::GenerateMatrix, version 2 (ghostpenalty.cpp:268-340) on an
+// affine element: the basis values at x + (i - w) eps n, eps = h * GetOptimalEps,
+// h = |det F|^(1/D) (the reference takes sqrt / cbrt of the signed determinant),
+// combined with the stencil and scaled by eps^-k.  The back-mapping of the
+// shifted points is exact for affine elements (its Newton loop stops at once).
+void basis_dn_fd(const Geo& g, int k_fe, const int* gv, const double* x, const double* nside, int k, double* out) {
+  const int D = g.D, n = ndof_el(D, k_fe);
+  double c[16], epsf;
+  const int w = fd_stencil(k, 4, c, &epsf);
+  const double h = std::pow(std::fabs(g.det), 1.0 / D);
+  const double eps = h * epsf;
+  std::fill(out, out + n, 0.0);
+  double phi[20], dphi[20][3];
+  for (int i = 0; i <= 2 * w; i++) {
+    double xi[3] = {0, 0, 0}, lam[4];
+    for (int d = 0; d < D; d++) xi[d] = x[d] + (i - w) * eps * nside[d];
+    phys_to_lam(g, xi, lam);
+    basis(D, k_fe, gv, lam, phi, dphi);
+    for (int a = 0; a < n; a++) out[a] += c[i] * phi[a];
+  }
+  const double fac = std::pow(1.0 / eps, k);
+  for (int a = 0; a < n; a++) out[a] *= fac;
+}
+
+// the facet rule in the facet's reference coordinates: the plain rule of the
+// (D-1)-simplex (ORC_WHOLE) or its straight-cut rule for the domain
+int facet_rule(int d, const double* lf, int region, int order, std::vector<double>& pts, std::vector<double>& wts) {
+  if (region == ORC_WHOLE) {
+    const Rule& r = get_rule(d, order);
+    pts = r.p;
+    wts = r.w;
+    return r.size();
+  }
+  Geo gd;
+  gd.D = d;
+  return straight_cut_rule(gd, lf, region, order, pts, wts);
+}
+
+bool is_skel(int kind) { return kind >= ORC_TERM_SKEL_JUMP && kind <= ORC_TERM_SKEL_DN3; }
+
+// skeleton terms of facet f added to elmat ((2n)^2, row = test)
+int skel_add(const orc_space* s, const double* lset_vertex, const orc_term* terms, int nterms, int f, int dn_fd,
+             double* elmat) {
+  const int D = s->D, n = s->nd, n2 = 2 * n, d = D - 1;
+  const int e1 = s->facet_els[2 * f], e2 = s->facet_els[2 * f + 1];
+  if (e1 < 0 || e2 < 0) return -5;
+  Geo g1, g2;
+  element_geo(s, e1, g1, nullptr, nullptr);
+  element_geo(s, e2, g2, nullptr, nullptr);
+  const int* gv1 = &s->elv[(size_t)e1 * (D + 1)];
+  const int* gv2 = &s->elv[(size_t)e2 * (D + 1)];
+  // the facet: e1's vertices except the one e2 does not have (e1's local order)
+  int opp1 = -1, fv[3], nfv = 0;
+  for (int i = 0; i <= D; i++) {
+    bool shared = false;
+    for (int j = 0; j <= D; j++) shared |= gv1[i] == gv2[j];
+    if (!shared) opp1 = i;
+    else if (nfv < D) fv[nfv++] = gv1[i];
+  }
+  if (opp1 < 0 || nfv != D) return -5;
+  double X[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, lf[3];
+  for (int i = 0; i < D; i++) {
+    for (int c = 0; c < D; c++) X[i][c] = s->coords[(size_t)fv[i] * D + c];
+    lf[i] = lset_vertex ? lset_vertex[fv[i]] : 0.0;
+  }
+  double meas;
+  if (d == 1) {
+    const double v[3] = {X[0][0] - X[1][0], X[0][1] - X[1][1], 0.0};
+    meas = l2norm3(v);
+  } else {
+    double a[3], b[3];
+    for (int c = 0; c < 3; c++) { a[c] = X[0][c] - X[2][c]; b[c] = X[1][c] - X[2][c]; }
+    const double cr[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+    meas = l2norm3(cr);
+  }
+  // outward normal of e1: -grad lambda_opp1 / |grad lambda_opp1|
+  double nF[3] = {0, 0, 0};
+  {
+    double gl[3] = {0, 0, 0};
+    for (int c = 0; c < D; c++) {
+      double v = 0;
+      if (opp1 < D) v = g1.Finv[opp1][c];
+      else for (int i = 0; i < D; i++) v -= g1.Finv[i][c];
+      gl[c] = v;
+    }
+    const double nn = l2norm3(gl);
+    for (int c = 0; c < 3; c++) nF[c] = -gl[c] / nn;
+  }
+  const double mnF[3] = {-nF[0], -nF[1], -nF[2]};
+  double del1[4], del2[4];
+  lam_dir(g1, nF, del1);
+  lam_dir(g2, nF, del2);
+  const double h1 = std::pow(std::fabs(g1.det), 1.0 / D);
+  std::vector<double> pts, wts;
+  std::vector<double> P((size_t)4 * n2);  // P[j][a]: d^j_nF of function a (a < n: e1, else e2)
+  for (int t = 0; t < nterms; t++) {
+    const orc_term& T = terms[t];
+    if (!is_skel(T.kind)) continue;
+    if (T.defined_on && !test_bit(T.defined_on, f)) continue;
+    if (T.domain == ORC_IF) return -6;  // codim-2 skeleton rules are not part of the menu
+    const int np = facet_rule(d, lf, T.domain, 2 * s->k, pts, wts);
+    if (np < -1) return np;
+    if (np <= 0) continue;
+    double c = T.coef;
+    if (T.hpow != 0) c *= std::pow(h1, (double)T.hpow);
+    const int kd = T.kind >= ORC_TERM_SKEL_DN1 ? T.kind - ORC_TERM_SKEL_DN1 + 1 : 0;
+    for (int q = 0; q < np; q++) {
+      const double* xi = &pts[3 * q];
+      double x[3] = {0, 0, 0}, rest = 1.0;
+      for (int m = 0; m < d; m++) rest -= xi[m];
+      for (int c2 = 0; c2 < D; c2++) {
+        double v = rest * X[d][c2];
+        for (int m = 0; m < d; m++) v += xi[m] * X[m][c2];
+        x[c2] = v;
+      }
+      double lam1[4], lam2[4];
+      phys_to_lam(g1, x, lam1);
+      phys_to_lam(g2, x, lam2);
+      for (int j = 0; j <= 1; j++) {
+        basis_dir(D, s->k, gv1, lam1, del1, j, &P[(size_t)j * n2]);
+        basis_dir(D, s->k, gv2, lam2, del2, j, &P[(size_t)j * n2 + n]);
+      }
+      if (kd > 0) {
+        double* Pk = &P[(size_t)2 * n2];
+        if (!dn_fd) {
+          basis_dir(D, s->k, gv1, lam1, del1, kd, Pk);
+          basis_dir(D, s->k, gv2, lam2, del2, kd, Pk + n);
+        } else {
+          // dn(w, k) of each side along its own outward normal, turned to n_F
+          basis_dn_fd(g1, s->k, gv1, x, nF, kd, Pk);
+          basis_dn_fd(g2, s->k, gv2, x, mnF, kd, Pk + n);
+          if (kd & 1)
+            for (int a = 0; a < n; a++) Pk[n + a] = -Pk[n + a];
+        }
+      }
+      const double W = wts[q] * meas * c;
+      const double* P0 = &P[0];
+      const double* P1 = &P[(size_t)n2];
+      const double* Pk = &P[(size_t)2 * n2];
+      for (int a = 0; a < n2; a++) {  // test
+        const double sa = a < n ? 1.0 : -1.0;
+        for (int b = 0; b < n2; b++) {  // trial
+          const double sb = b < n ? 1.0 : -1.0;
+          double v;
+          switch (T.kind) {
+            case ORC_TERM_SKEL_JUMP: v = sa * P0[a] * sb * P0[b]; break;
+            case ORC_TERM_SKEL_FLUX: v = P1[b] * sa * P0[a]; break;
+            case ORC_TERM_SKEL_FLUX_T: v = sb * P0[b] * P1[a]; break;
+            default: v = sa * Pk[a] * sb * Pk[b]; break;
+          }
+          elmat[a * n2 + b] += W * v;
+        }
+      }
+    }
+  }
+  return 0;
+}
+
+// patch terms, then skeleton terms, of facet f
+int facet_matrix(const orc_space* s, const double* lset_vertex, const orc_term* terms, int nterms, int f, int dn_fd,
+                 double* elmat) {
+  const int r = patch_matrix(s, terms, nterms, f, elmat);
+  if (r) return r;
+  return skel_add(s, lset_vertex, terms, nterms, f, dn_fd, elmat);
 }
 
 }  // namespace
@@ -1164,19 +1466,33 @@ int orc_patch_matrix(const orc_space* s, const orc_term* terms, int nterms, int 
   return patch_matrix(s, terms, nterms, f, elmat);
 }
 
+int orc_facet_matrix(const orc_space* s, const double* lset_vertex, const orc_term* terms, int nterms, int f,
+                     int dn_fd, double* elmat) {
+  return facet_matrix(s, lset_vertex, terms, nterms, f, dn_fd, elmat);
+}
+
+int orc_fd_stencil(int k, int acc, double* c, double* eps) { return fd_stencil(k, acc, c, eps); }
+
 orc_csr* orc_assemble(const orc_space* s, const double* lset_vertex, const orc_term* terms, int nterms,
                       int nthreads) {
+  return orc_assemble_ex(s, lset_vertex, terms, nterms, nthreads, 0);
+}
+
+orc_csr* orc_assemble_ex(const orc_space* s, const double* lset_vertex, const orc_term* terms, int nterms,
+                         int nthreads, int dn_fd) {
   const int ne = s->ne, n = s->nd, n2 = 2 * n;
   const int64_t nf = s->nfacets;
-  // active elements: in the definedon set of some volume term
+  // active elements: in the definedon set of some volume term; active facets:
+  // interior facets in the definedon set of some patch or skeleton term
+  auto facet_term = [](int kind) { return kind == ORC_TERM_GHOST_MASS || kind >= ORC_TERM_SKEL_JUMP; };
   std::vector<int32_t> el_slot(ne, -1), fa_slot(nf, -1);
   bool any_vol = false, any_patch = false;
-  for (int t = 0; t < nterms; t++) (terms[t].kind == ORC_TERM_GHOST_MASS ? any_patch : any_vol) = true;
+  for (int t = 0; t < nterms; t++) (facet_term(terms[t].kind) ? any_patch : any_vol) = true;
   int nact = 0;
   for (int e = 0; e < ne && any_vol; e++) {
     bool act = false;
     for (int t = 0; t < nterms; t++)
-      if (terms[t].kind != ORC_TERM_GHOST_MASS && (!terms[t].defined_on || test_bit(terms[t].defined_on, e))) act = true;
+      if (!facet_term(terms[t].kind) && (!terms[t].defined_on || test_bit(terms[t].defined_on, e))) act = true;
     if (act) el_slot[e] = nact++;
   }
   int nfa = 0;
@@ -1184,7 +1500,7 @@ orc_csr* orc_assemble(const orc_space* s, const double* lset_vertex, const orc_t
     if (s->facet_els[2 * f + 1] < 0) continue;
     bool act = false;
     for (int t = 0; t < nterms; t++)
-      if (terms[t].kind == ORC_TERM_GHOST_MASS && (!terms[t].defined_on || test_bit(terms[t].defined_on, f))) act = true;
+      if (facet_term(terms[t].kind) && (!terms[t].defined_on || test_bit(terms[t].defined_on, f))) act = true;
     if (act) fa_slot[f] = nfa++;
   }
   std::vector<int32_t> el_list(nact), fa_list(nfa);
@@ -1200,7 +1516,7 @@ orc_csr* orc_assemble(const orc_space* s, const double* lset_vertex, const orc_t
   });
   parallel_for(nfa, nthreads, [&](int64_t b, int64_t en) {
     for (int64_t i = b; i < en; i++) {
-      int r = patch_matrix(s, terms, nterms, fa_list[i], &fam[(size_t)i * n2 * n2]);
+      int r = facet_matrix(s, lset_vertex, terms, nterms, fa_list[i], dn_fd, &fam[(size_t)i * n2 * n2]);
       if (r) err = r;
     }
   });
@@ -1220,7 +1536,9 @@ void orc_csr_destroy(orc_csr* c) { delete c; }
 // CutFEM pipeline as in demos/fictdom.py:95-133: CutInfo -> HASNEG / IF element
 // sets -> ghost facets (HASNEG, IF) -> assembly.  Volume terms on NEG get the
 // HASNEG set, IF terms the IF set, POS terms the HASPOS set; patch terms get the
-// ghost facets.
+// ghost facets.  Skeleton terms (demos/fictdom_dg.py:100-135): on NEG the
+// facets between two HASNEG elements, on POS between two HASPOS elements, on
+// whole facets the ghost facets.
 int64_t orc_pipeline(const orc_space* s, const double* lset_vertex, const orc_term* terms, int nterms,
                      int ghost_facets, int nthreads) {
   const int ne = s->ne;
@@ -1233,9 +1551,14 @@ int64_t orc_pipeline(const orc_space* s, const double* lset_vertex, const orc_te
   const uint64_t* ifb = &bits[4 * nw];
   const uint64_t* haspos = &bits[6 * nw];
   if (ghost_facets) orc_facets_with_neighbor_types(s, hasneg, ifb, 1, 1, 1, fb.data());
+  std::vector<uint64_t> fneg(nfw), fpos(nfw);
+  orc_facets_with_neighbor_types(s, hasneg, hasneg, 1, 1, 1, fneg.data());
+  orc_facets_with_neighbor_types(s, haspos, haspos, 1, 1, 1, fpos.data());
   std::vector<orc_term> t2(terms, terms + nterms);
   for (auto& t : t2) {
     if (t.kind == ORC_TERM_GHOST_MASS) t.defined_on = fb.data();
+    else if (t.kind >= ORC_TERM_SKEL_JUMP)
+      t.defined_on = t.domain == ORC_NEG ? fneg.data() : (t.domain == ORC_POS ? fpos.data() : fb.data());
     else t.defined_on = t.domain == ORC_NEG ? hasneg : (t.domain == ORC_IF ? ifb : haspos);
   }
   orc_csr* c = orc_assemble(s, lset_vertex, t2.data(), nterms, nthreads);

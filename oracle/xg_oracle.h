@@ -21,8 +21,9 @@
 extern "C" {
 #endif
 
-/* Domain types, same values as ngsxfem utils/ngsxstd.hpp:16-35. */
-enum { ORC_NEG = 0, ORC_POS = 1, ORC_IF = 2 };
+/* Domain types, same values as ngsxfem utils/ngsxstd.hpp:16-35.  ORC_WHOLE
+ * (skeleton terms only): the whole facet, no level-set restriction. */
+enum { ORC_NEG = 0, ORC_POS = 1, ORC_IF = 2, ORC_WHOLE = 3 };
 
 /* Term kinds; identical numbering to the product's XG_TERM_*. */
 enum {
@@ -32,7 +33,16 @@ enum {
   ORC_TERM_U_NGRADV = 3,   /* c * u * (n . grad v)               */
   ORC_TERM_CONV = 4,       /* c * (b . grad u) * v               */
   ORC_TERM_GHOST_MASS = 5, /* c * (u - u.Other()) * (v - v.Other()) on a facet patch */
-  ORC_TERM_DT_U_V = 6      /* space-time: c * v * d/dtau u (dtref) */
+  ORC_TERM_DT_U_V = 6,     /* space-time: c * v * d/dtau u (dtref) */
+  /* skeleton terms on interior facets F (u / v: element 1 of the facet, u' / v':
+   * element 2, n_F: unit normal of F pointing out of element 1), over F in the
+   * domain (ORC_NEG / ORC_POS: the cut facet) or the whole facet (ORC_WHOLE) */
+  ORC_TERM_SKEL_JUMP = 7,    /* c * (u - u') * (v - v')                               */
+  ORC_TERM_SKEL_FLUX = 8,    /* c * ((grad u + grad u') . n_F) * (v - v')             */
+  ORC_TERM_SKEL_FLUX_T = 9,  /* c * (u - u') * ((grad v + grad v') . n_F)             */
+  ORC_TERM_SKEL_DN1 = 10,    /* c * [d_n u] [d_n v], [d^k_n w] = d^k_n w - d^k_n w'  */
+  ORC_TERM_SKEL_DN2 = 11,    /* c * [d^2_n u] [d^2_n v]                              */
+  ORC_TERM_SKEL_DN3 = 12     /* c * [d^3_n u] [d^3_n v]                              */
 };
 
 typedef struct {
@@ -89,12 +99,28 @@ int orc_element_matrix(const orc_space*, const double* lset_vertex, const orc_te
                        int e, double* elmat);
 /* Facet-patch matrix of patch terms on facet f: (2n)^2, dofs [el1, el2]. */
 int orc_patch_matrix(const orc_space*, const orc_term* terms, int nterms, int f, double* elmat);
+/* Facet matrix of facet f: its patch terms plus its skeleton terms (row = test,
+ * col = trial, dofs [el1, el2]).  dn_fd = 0: exact normal derivatives; 1: the
+ * reference's central finite differences of DiffOpDuDnk (ghostpenalty.cpp:
+ * 221-365, version 2, accuracy 4) for the ORC_TERM_SKEL_DN* terms. */
+int orc_facet_matrix(const orc_space*, const double* lset_vertex, const orc_term* terms, int nterms, int f,
+                     int dn_fd, double* elmat);
+/* Central finite-difference stencil of DiffOpDuDnk for the k-th derivative at
+ * accuracy acc: c[0 .. 2w] on the offsets -w .. w (returns w) and the step
+ * factor of GetOptimalEps (times the element size h). */
+int orc_fd_stencil(int k, int acc, double* c, double* eps);
+/* Discontinuous (L2) space of order k: the same element basis with element-
+ * local dofs, dof(e, i) = e * ndof_el + i. */
+orc_space* orc_space_create_l2(int D, int nv, const double* coords, int ne, const int32_t* elv, int order);
 
 typedef struct orc_csr orc_csr;
 /* Full assembly: volume terms over their elements, patch terms over their facets,
  * summed into a CSR over all dofs (rows of untouched dofs are empty). */
 orc_csr* orc_assemble(const orc_space*, const double* lset_vertex, const orc_term* terms, int nterms,
                       int nthreads);
+/* orc_assemble with the normal-derivative mode of orc_facet_matrix. */
+orc_csr* orc_assemble_ex(const orc_space*, const double* lset_vertex, const orc_term* terms, int nterms,
+                         int nthreads, int dn_fd);
 int64_t orc_csr_nnz(const orc_csr*);
 void orc_csr_get(const orc_csr*, int64_t* rowptr, int32_t* cols, double* vals);
 void orc_csr_destroy(orc_csr*);
