@@ -279,8 +279,13 @@ def c4_train_values(n, seed):
 
 def run_c4(args):
     ws, rank = dist_env()
+    sub = args.plain == "subdiv"
+    L = args.subdivlvl
+    plain_name = ("subdivision rule, level %d (the reference's CutIntegrationRule for a P2 level set, "
+                  "cutint/xintegration.cpp:1626-1754)" % L) if sub else \
+        "isoparametric rule (LevelSetMeshAdaptation + straight cut, order 8)"
     cfg = {"workload": "learned cut quadrature, P2 torus (R=0.3, r=0.1) on 48^3x6 Kuhn tets; MLP 10-256-256-24 "
-                       "trained on %d P2 value sets" % args.train}
+                       "trained on %d P2 value sets; plain = %s" % (args.train, plain_name)}
     m, vals = c4_eval_values()
     n = len(vals)
     cfg.update({"n_tets": int(m.ne), "n_cut": n})
@@ -289,12 +294,17 @@ def run_c4(args):
             return
         from oracle import oracle as orc
         nth = os.cpu_count() or 1
+        def rule():
+            if sub:
+                orc.subdiv_moments_p2(vals, L, nth)
+            else:
+                orc.iso_moments_tet(vals, 8, True, nth)
         for _ in range(args.warmup):
-            orc.iso_moments_tet(vals, 8, True, nth)
+            rule()
         times = []
         for _ in range(args.steps):
             t0 = time.perf_counter()
-            orc.iso_moments_tet(vals, 8, True, nth)
+            rule()
             times.append(time.perf_counter() - t0)
         t = float(np.mean(times))
         print(json.dumps({
@@ -302,7 +312,7 @@ def run_c4(args):
             "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
             "cpu_baseline": {"value": n / t, "unit": UNIT, "cores": nth, "kind": "port",
-                             "sample": "all cut elements per step: per-element isoparametric rule (oracle)"},
+                             "sample": "all cut elements per step: per-element %s (oracle)" % plain_name},
             "e2e": {"value": n / t, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
         return
     import torch
@@ -319,12 +329,22 @@ def run_c4(args):
         _lib.call("xg_iso_moments_tet", vp(d_v), d_v.shape[0], order, deform, vp(out), None, sp)
         return out
 
+    sd_err = torch.zeros(1, dtype=torch.int32, device="cuda")
+
+    def subdiv_moments(d_v, level, out=None):
+        out = out if out is not None else torch.zeros((d_v.shape[0], 35), dtype=torch.float64, device="cuda")
+        _lib.call("xg_subdiv_moments_tet", vp(d_v), d_v.shape[0], level, vp(out), vp(sd_err), sp)
+        return out
+
     # ---- training set and its targets (GPU isoparametric rule) ----
     t0 = time.perf_counter()
     v_tr = torch.from_numpy(c4_train_values(args.train, SEED)).cuda()
-    iso_tr = moments(v_tr, 8, 1)
     nc_tr = torch.zeros(args.train, dtype=torch.int32, device="cuda")
-    _lib.call("xg_iso_moments_tet", vp(v_tr), args.train, 8, 1, vp(iso_tr), vp(nc_tr), sp)
+    if sub:
+        iso_tr = subdiv_moments(v_tr, L)
+    else:
+        iso_tr = moments(v_tr, 8, 1)
+        _lib.call("xg_iso_moments_tet", vp(v_tr), args.train, 8, 1, vp(iso_tr), vp(nc_tr), sp)
     p1_tr = moments(v_tr, 4, 0)
     t_tr = (iso_tr - p1_tr).float()
     # samples the network is not meant to take (the fallback's): defects above
@@ -395,12 +415,16 @@ def run_c4(args):
     out_p1 = torch.zeros_like(out_plain)
 
     def plain():
-        moments(d_v, 8, 1, out_plain)
+        if sub:
+            subdiv_moments(d_v, L, out_plain)
+        else:
+            moments(d_v, 8, 1, out_plain)
 
     nfb = torch.zeros(1, dtype=torch.int32, device="cuda")
 
     def learned(kappa=args.kappa):
-        _lib.call("xg_learned_moments_tet", mlp, vp(d_v), n, ctypes.c_double(kappa), vp(out_learn), vp(nfb), sp)
+        _lib.call("xg_learned_moments_tet_ex", mlp, vp(d_v), n, ctypes.c_double(kappa), L if sub else -1,
+                  vp(out_learn), vp(nfb), sp)
 
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
@@ -435,6 +459,15 @@ def run_c4(args):
                 "frac_le_1e-3": float((e <= 1e-3).mean())}
     errs = {"definition": "max over the 35 moments of |m - m_plain| / (measure of the element)",
             "learned_vs_plain": stats(e_learn), "straight_cut_vs_plain": stats(e_p1)}
+    if sub:
+        # the isoparametric rule and the finer subdivision against the plain rule
+        out_iso = moments(d_v, 8, 1)
+        out_fine = subdiv_moments(d_v, L + 1)
+        torch.cuda.synchronize()
+        errs["isoparametric_vs_plain"] = stats(np.abs(out_iso.cpu().numpy() - ref).max(1) * 6)
+        errs["subdivision_level_%d_vs_plain" % (L + 1)] = stats(np.abs(out_fine.cpu().numpy() - ref).max(1) * 6)
+        assert int(sd_err.item()) == 0, "subdivision rule error %d" % int(sd_err.item())
+        del out_iso, out_fine
     sweep = {}
     for kap in (0.0, 0.01, 0.02, 0.05, -1.0):
         learned(kap)
@@ -466,7 +499,7 @@ def run_c4(args):
                 "plain_ms": ms_plain, "learned_ms": ms_learn, "learned_speedup_vs_plain": ms_plain / ms_learn,
                 "kappa_max": args.kappa, "fallback_frac": n_fallback / n, "train_kept": n_tr,
                 "errors": errs, "l2": "flushed between timed steps (512 MB write)",
-                "plain": "GPU per-element isoparametric rule (FP64), the reference's P2 workflow"})
+                "plain": "GPU " + plain_name + " (FP64), also the fallback and the judge of the error"})
     out = {
         "metric": METRIC, "value": n / (ms_learn * 1e-3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_learn, "higher_is_better": True, "scaling": "weak",
@@ -487,12 +520,17 @@ def run_c4(args):
     if args.cpu_baseline:
         from oracle import oracle as orc
         nth = os.cpu_count() or 1
-        orc.iso_moments_tet(vals, 8, True, nth)
+        def rule():
+            if sub:
+                orc.subdiv_moments_p2(vals, L, nth)
+            else:
+                orc.iso_moments_tet(vals, 8, True, nth)
+        rule()
         t0 = time.perf_counter()
-        orc.iso_moments_tet(vals, 8, True, nth)
+        rule()
         tc = time.perf_counter() - t0
         out["cpu_baseline"] = {"value": n / tc, "unit": UNIT, "cores": nth, "kind": "port",
-                               "sample": "all cut elements: per-element isoparametric rule (oracle), 1 timed pass"}
+                               "sample": "all cut elements: per-element %s (oracle), 1 timed pass" % plain_name}
     _lib.call("xg_mlp_destroy", mlp)
     print(json.dumps(out))
 
@@ -1088,6 +1126,9 @@ def main():
     ap.add_argument("--train", type=int, default=2000000)
     ap.add_argument("--epochs", type=int, default=8)
     ap.add_argument("--kappa", type=float, default=0.05)
+    ap.add_argument("--plain", default="subdiv", choices=["subdiv", "iso"],
+                    help="c4: the plain rule (targets, fallback, judge): subdivision or isoparametric")
+    ap.add_argument("--subdivlvl", type=int, default=3, help="c4: level of the subdivision rule")
     ap.add_argument("--n", type=int, default=64)
     ap.add_argument("--order", type=int, default=2)
     ap.add_argument("--copies", type=int, default=512)

@@ -294,6 +294,24 @@ int xg_integrate_ex(xg_mesh* mesh, const double* d_lset, int dt, int order, int 
 int xg_integrate_noalloc(xg_mesh* mesh, const double* d_lset, int dt, int order, int ex, int ey, int ez,
                          const uint64_t* d_defined_on, double* d_result, void* stream);
 
+/* Integrate(x^ex y^ey z^ez * dCut(lset_h, dt, order, subdivlvl)) for a level
+ * set of order 1..3 given by its coefficients d_lset_coefs in the H1 space
+ * `space` (the reference's CutIntegrationRule for level sets that are not P1,
+ * cutint/xintegration.cpp:102-116, 1626-1754): each element's simplex is
+ * checked on a lattice of spacing 2^-subdivlvl, cut simplices are refined by
+ * the reference's children down to level 0, and cut level-0 simplices get
+ * the straight cut of their vertex values.  subdivlvl 0..6. */
+int xg_integrate_subdiv(xg_space* space, const double* d_lset_coefs, int dt, int order, int subdivlvl, int ex,
+                        int ey, int ez, const uint64_t* d_defined_on, double* d_result, void* stream);
+/* The same rule on n reference tetrahedra with a P2 level set given by its
+ * values at the vertices (1,0,0),(0,1,0),(0,0,1),(0,0,0) and the midpoints
+ * of the edges (0,1),(0,2),(0,3),(1,2),(1,3),(2,3) (d_vals10: n x 10): the 35
+ * NEG moments x^a y^b z^c, a + b + c <= 4 (by degree, then a, then b
+ * descending) per element, order-4 rules (d_out35: n x 35).  Rule errors go
+ * to d_err (may be NULL). */
+int xg_subdiv_moments_tet(const double* d_vals10, int64_t n, int subdivlvl, double* d_out35, int* d_err,
+                          void* stream);
+
 /* ---- bilinear forms ---------------------------------------------------------- */
 /* A form is a list of integrators over one space (H1 or L2; trial = test
  * space).  Volume terms run on their element sets with the cut rule of their
@@ -483,6 +501,14 @@ int xg_learned_features(const double* d_vals10, int64_t n, float* d_x10, void* s
  * (order 8) instead; their number goes to d_nfallback (optional). */
 int xg_learned_moments_tet(xg_mlp* mlp, const double* d_vals10, int64_t n, double kappa_max, double* d_out35,
                            int32_t* d_nfallback, void* stream);
+/* xg_learned_moments_tet with the plain rule chosen: plain_subdivlvl < 0 the
+ * isoparametric rule (as above); 0..6 the subdivision rule of that level
+ * (xg_subdiv_moments_tet), the reference's own rule for a P2 level set
+ * without mesh deformation (cutint/xintegration.cpp:1626-1754), which then
+ * serves as the fallback.  Rule errors go to the network's status word
+ * (xg_mlp_check). */
+int xg_learned_moments_tet_ex(xg_mlp* mlp, const double* d_vals10, int64_t n, double kappa_max, int plain_subdivlvl,
+                              double* d_out35, int32_t* d_nfallback, void* stream);
 
 /* ---- batched steps in one CUDA graph --------------------------------------- */
 /* No counterpart in the reference, which assembles one form per

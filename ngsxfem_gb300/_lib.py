@@ -25,7 +25,7 @@ EXPORTS = [
     "xg_space_create", "xg_space_create_l2", "xg_space_destroy", "xg_space_info", "xg_space_element_dofs",
     "xg_interpolate_p1_perturb", "xg_cutinfo_update", "xg_mesh_check",
     "xg_facets_with_neighbor_types", "xg_elements_with_neighbor_facets",
-    "xg_cut_rules", "xg_base_rule_size", "xg_base_rule", "xg_integrate", "xg_integrate_noalloc",
+    "xg_cut_rules", "xg_base_rule_size", "xg_base_rule", "xg_integrate", "xg_integrate_noalloc", "xg_integrate_subdiv", "xg_subdiv_moments_tet",
     "xg_mesh_create_tensor", "xg_cut_rules_ex", "xg_quad_rule_capacity", "xg_integrate_ex",
     "xg_integrate_mlset", "xg_cut_rules_mlset", "xg_mlset_rule_capacity", "xg_mlset_mark",
     "xg_iso_integrate_mesh", "xg_integrate_bnd",
@@ -35,7 +35,7 @@ EXPORTS = [
     "xg_st_cutfem_step", "xg_step_graph_create", "xg_step_graph_launch", "xg_step_graph_destroy",
     "xg_step_graph_kernel_count", "xg_form_autotune", "xg_autotune_table", "xg_iso_moments_tet", "xg_mlp_param_count", "xg_learned_points",
     "xg_mlp_create", "xg_mlp_destroy", "xg_mlp_get_params", "xg_mlp_set_params", "xg_mlp_forward", "xg_mlp_forward_tc", "xg_mlp_check",
-    "xg_mlp_loss_grad", "xg_mlp_adam_step", "xg_learned_moments_tet", "xg_learned_features",
+    "xg_mlp_loss_grad", "xg_mlp_adam_step", "xg_learned_moments_tet", "xg_learned_moments_tet_ex", "xg_learned_features",
     "xg_cutinfo_update_bnd", "xg_mesh_boundary", "xg_cutinfo_nodes", "xg_elements_with_threshold",
     "xg_lform_create", "xg_lform_destroy", "xg_lform_assemble", "xg_lform_check",
 ]
@@ -137,6 +137,8 @@ def load():
         "xg_iso_integrate_mesh": (I, [P, P, I, I, ctypes.c_double, I, I, I, I, P, P, P]),
         "xg_integrate_bnd": (I, [P, P, I, I, I, I, I, P, P, P]),
         "xg_integrate_noalloc": (I, [P, P, I, I, I, I, I, P, P, P]),
+        "xg_integrate_subdiv": (I, [P, P, I, I, I, I, I, I, P, P, P]),
+        "xg_subdiv_moments_tet": (I, [P, ctypes.c_int64, I, P, P, P]),
         "xg_form_create": (I, [P, P, ctypes.c_int32, I, P]),
         "xg_form_destroy": (I, [P]),
         "xg_form_set_defined_on": (I, [P, ctypes.c_int32, P]),
@@ -165,6 +167,7 @@ def load():
         "xg_mlp_loss_grad": (I, [P, P, P, P, I64, P, P, P]),
         "xg_mlp_adam_step": (I, [P, P, ctypes.c_float, I64, P]),
         "xg_learned_moments_tet": (I, [P, P, I64, D, P, P, P]),
+        "xg_learned_moments_tet_ex": (I, [P, P, I64, D, I, P, P, P]),
         "xg_learned_features": (I, [P, I64, P, P]),
         "xg_cutinfo_update_bnd": (I, [P, P, P, P, P, P]),
         "xg_mesh_boundary": (I, [P, P, P]),

@@ -35,6 +35,7 @@ UNITS = [
     ("xg_rows.cu", []),
     ("xg_mlp_tc.cu", []),
     ("xg_skel.cu", []),
+    ("xg_subdiv.cu", []),
 ]
 
 

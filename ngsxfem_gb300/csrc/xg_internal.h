@@ -167,6 +167,12 @@ int upload_rules_quad_int();
 int upload_rules_mlset();
 int upload_rules_isomesh();
 int upload_rules_skel();  // xg_skel.cu
+int upload_rules_subdiv();  // xg_subdiv.cu
+// per-element NEG moments of P2 level sets on the reference tetrahedron by
+// the subdivision rule (xg_subdiv.cu); with d_list, only the d_count listed
+// elements
+int subdiv_moments_launch(const double* d_vals10, int64_t n, int levels, double* d_out35, const int32_t* d_list,
+                          const int32_t* d_count, int* d_err, cudaStream_t s);
 
 // skeleton terms of a form (xg_skel.cu): the facet matrices of the active
 // facet list, written into (accumulate = 0) or added to (1) famat, full rows

@@ -618,7 +618,12 @@ int xg_learned_features(const double* d_vals10, int64_t n, float* d_x, void* str
 
 int xg_learned_moments_tet(xg_mlp* m, const double* d_vals10, int64_t n, double kappa_max, double* d_out35,
                            int32_t* d_nfallback, void* stream) {
-  if (!m || !d_vals10 || !d_out35 || n < 0 || n > kMaxRows) return XG_ERR_ARG;
+  return xg_learned_moments_tet_ex(m, d_vals10, n, kappa_max, -1, d_out35, d_nfallback, stream);
+}
+
+int xg_learned_moments_tet_ex(xg_mlp* m, const double* d_vals10, int64_t n, double kappa_max, int plain_subdivlvl,
+                              double* d_out35, int32_t* d_nfallback, void* stream) {
+  if (!m || !d_vals10 || !d_out35 || n < 0 || n > kMaxRows || plain_subdivlvl > 6) return XG_ERR_ARG;
   if (n == 0) return XG_OK;
   cudaStream_t s = (cudaStream_t)stream;
   int st = mlp_reserve(m, n);
@@ -634,7 +639,14 @@ int xg_learned_moments_tet(xg_mlp* m, const double* d_vals10, int64_t n, double 
     // plain (isoparametric, order 8) rule on the elements the network does not take
     XG_CUDA(cudaMemsetAsync(m->count, 0, sizeof(int32_t), s));
     k_fallback_list<<<grid1(n), 256, 0, s>>>(m->x, d_vals10, n, kappa_max, m->list, m->count);
-    if ((st = tet_moments_launch(d_vals10, n, 8, 1, d_out35, nullptr, s, m->list, m->count))) return st;
+    if (plain_subdivlvl >= 0) {
+      // the plain rule is the subdivision rule of that level
+      if ((st = ensure_device_rules())) return st;
+      if ((st = subdiv_moments_launch(d_vals10, n, plain_subdivlvl, d_out35, m->list, m->count, m->err, s)))
+        return st;
+    } else if ((st = tet_moments_launch(d_vals10, n, 8, 1, d_out35, nullptr, s, m->list, m->count))) {
+      return st;
+    }
     if (d_nfallback) XG_CUDA(cudaMemcpyAsync(d_nfallback, m->count, sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
   } else if (d_nfallback) {
     XG_CUDA(cudaMemsetAsync(d_nfallback, 0, sizeof(int32_t), s));

@@ -299,6 +299,50 @@ class GridFunction:
         self.space = space
         self.vec = torch.zeros(space.ndof, dtype=torch.float64, device=_dev())
 
+    def Set(self, f):
+        """Interpolation of f(x, y[, z]) (vectorised over numpy arrays) into the
+        H1 / L2 space of order 1..3: the function's values at the canonical
+        nodes of every element (vertices; edge midpoints for order 2; edge
+        points at 1/3, 2/3 and face centroids for order 3) give the
+        hierarchical coefficients (the relations of csrc/xg_patch.cuh
+        nodal_to_hier), with the cubic edge functions oriented by global vertex
+        numbers.  Exact for polynomials of the space's degree."""
+        V = self.space
+        mesh, k = V.mesh, V.order
+        if isinstance(V, SpaceTimeFESpace) or getattr(mesh, "tensor", False):
+            raise NotImplementedError("Set on simplex H1 / L2 spaces")
+        D = mesh.dim
+        X = mesh.coords[mesh.elements]                      # ne x (D+1) x D
+        ev = lambda P: np.asarray(f(*[P[..., c] for c in range(D)]), dtype=np.float64)  # noqa: E731
+        cols = [ev(X[:, i]) for i in range(D + 1)]
+        edges = [(0, 1), (0, 2), (1, 2)] if D == 2 else [(0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3)]
+        alpha = {}
+        if k >= 2:
+            gv = mesh.elements
+            for j, (a, b) in enumerate(edges):
+                pa, pb = cols[a], cols[b]
+                if k == 2:
+                    al = 4 * ev(0.5 * (X[:, a] + X[:, b])) - 2 * (pa + pb)
+                    cols.append(al)
+                else:
+                    q1 = ev(X[:, a] / 3 + 2 * X[:, b] / 3) - (pa + 2 * pb) / 3
+                    q2 = ev(2 * X[:, a] / 3 + X[:, b] / 3) - (2 * pa + pb) / 3
+                    al = 2.25 * (q1 + q2)
+                    sign = np.where(gv[:, a] < gv[:, b], 1.0, -1.0)
+                    cols += [al, 6.75 * (q2 - q1) * sign]
+                alpha[(a, b)] = al
+        if k == 3:
+            faces = [(0, 1, 2)] if D == 2 else [(0, 1, 2), (0, 1, 3), (0, 2, 3), (1, 2, 3)]
+            for a, b, c in faces:
+                cen = ev((X[:, a] + X[:, b] + X[:, c]) / 3)
+                e = alpha[(a, b)] + alpha[(a, c)] + alpha[(b, c)]
+                cols.append(27 * (cen - (cols[a] + cols[b] + cols[c]) / 3 - e / 9))
+        loc = np.stack(cols, 1)
+        out = np.zeros(V.ndof)
+        out[V.element_dofs()] = loc
+        self.vec.copy_(torch.from_numpy(out))
+        return self
+
     def _atom(self):
         return _Expr([_Mono(scal=(("gf", self),))])
 
@@ -622,8 +666,7 @@ class _Measure:
         self.definedon = kw.get("definedon")
         if self.definedon is not None and (kind != "cut" or kw.get("vb", VOL) != BND):
             raise NotImplementedError("definedon (a region of BND elements) applies to dCut(..., vb=BND)")
-        if kw.get("subdivlvl") not in (None, 0):
-            raise NotImplementedError("subdivision rules are not part of dCut on the GPU path")
+        self.subdivlvl = int(kw.get("subdivlvl") or 0)
         t = kw.get("time_order", -1)
         self.time_order = -1 if t is None else int(t)
         self.tref = kw.get("tref")
@@ -679,6 +722,9 @@ class _Integral:
     def terms(self, nrm_gf):
         """Maps the integrand onto the C ABI term menu (list of dicts)."""
         m = self.measure
+        if getattr(m, "subdivlvl", 0):
+            raise NotImplementedError("bilinear forms on subdivision rules (subdivlvl > 0) are not built; "
+                                      "Integrate takes them")
         out = []
         if m.kind == "patch":
             # expect c * (u - u')(v - v') = c*(uv - u'v - uv' + u'v')
@@ -1154,6 +1200,15 @@ def Integrate(levelset_domain=None, cf=None, mesh=None, order=5, integrand=None)
         return _integrate_bnd(lset, dt, order, mono, mesh, defined, region)
     if isinstance(lset, (tuple, list)):
         return _integrate_mlset(lset, dt, order, mono, defined, mesh)
+    subdivlvl = getattr(meas, "subdivlvl", 0) if integrand is not None else levelset_domain.get("subdivlvl", 0)
+    if isinstance(lset, GridFunction) and not isinstance(lset.space, SpaceTimeFESpace) and lset.space.order > 1:
+        # a level set that is not P1: the subdivision rule (the reference's
+        # CutIntegrationRule path, cutint/xintegration.cpp:102-116)
+        res = torch.zeros(1, dtype=torch.float64, device=_dev())
+        _lib.call("xg_integrate_subdiv", lset.space.h, _vp(lset.vec), dt, order, int(subdivlvl or 0), mono.e[0],
+                  mono.e[1], mono.e[2], _vp(defined.words) if defined is not None else None, _vp(res), _stream())
+        device_mesh(lset.space.mesh).check()
+        return float(res.item())
     mesh = mesh if mesh is not None else lset.space.mesh
     dm = device_mesh(mesh)
     res = torch.zeros(1, dtype=torch.float64, device=_dev())

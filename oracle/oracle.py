@@ -72,6 +72,12 @@ def lib():
         L.orc_fd_stencil.argtypes = [ctypes.c_int, ctypes.c_int, P, P]
         L.orc_assemble_ex.restype = P
         L.orc_assemble_ex.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.orc_subdiv_rule.argtypes = [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P,
+                                      ctypes.c_int]
+        L.orc_integrate_subdiv.restype = ctypes.c_double
+        L.orc_integrate_subdiv.argtypes = [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_int, P, P]
+        L.orc_subdiv_moments_p2.argtypes = [ctypes.c_int64, P, ctypes.c_int, P, ctypes.c_int]
         L.orc_space_destroy.argtypes = [P]
         L.orc_space_info.argtypes = [P, P]
         L.orc_space_el_dofs.argtypes = [P, P]
@@ -417,6 +423,17 @@ class LTerm(ctypes.Structure):
                 ("coef", ctypes.c_double), ("gf", ctypes.c_void_p), ("defined_on", ctypes.c_void_p)]
 
 
+def subdiv_moments_p2(vals10, levels, nthreads=1):
+    """NEG moments of P2 level sets on the reference tetrahedron by the
+    subdivision rule (n x 10 values -> n x 35)."""
+    v = np.ascontiguousarray(vals10, dtype=np.float64)
+    out = np.zeros((v.shape[0], 35))
+    r = lib().orc_subdiv_moments_p2(v.shape[0], _p(v), levels, _p(out), nthreads)
+    if r:
+        raise RuntimeError("oracle subdivision rule error %d" % r)
+    return out
+
+
 def fd_stencil(k, acc=4):
     """Central finite-difference stencil of DiffOpDuDnk (offsets -w..w) and its
     step factor (times the element size)."""
@@ -583,6 +600,26 @@ class Space:
         if r:
             raise RuntimeError("oracle patch matrix error %d" % r)
         return out
+
+    def subdiv_rule(self, lset_coefs, e, dt, order, subdivlvl, maxpts=200000):
+        """Subdivision rule of element e (physical points, physical weights) for
+        the level set given by its coefficients in this space."""
+        c = np.ascontiguousarray(lset_coefs, dtype=np.float64)
+        pts = np.zeros((maxpts, 3))
+        wts = np.zeros(maxpts)
+        n = lib().orc_subdiv_rule(self.h, _p(c), e, dt, order, subdivlvl, _p(pts), _p(wts), maxpts)
+        if n < 0:
+            raise RuntimeError("oracle subdivision rule error %d" % n)
+        return pts[:n].copy(), wts[:n].copy()
+
+    def integrate_subdiv(self, lset_coefs, dt, order, subdivlvl, ex=0, ey=0, ez=0, defined_on=None):
+        c = np.ascontiguousarray(lset_coefs, dtype=np.float64)
+        d = None if defined_on is None else np.ascontiguousarray(defined_on, dtype=np.uint64)
+        st = ctypes.c_int(0)
+        v = lib().orc_integrate_subdiv(self.h, _p(c), dt, order, subdivlvl, ex, ey, ez, _p(d), ctypes.byref(st))
+        if st.value:
+            raise RuntimeError("oracle subdivision rule error %d" % st.value)
+        return v
 
     def facet_matrix(self, lset, terms, f, dn_fd=False):
         """Patch and skeleton terms of facet f ((2n)^2, row = test)."""

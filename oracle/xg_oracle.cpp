@@ -1457,6 +1457,280 @@ double orc_integrate(const orc_space* s, const double* lset_vertex, int dt, int 
   return sum;
 }
 
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Subdivision cut rules for a higher-order level set (subdivlvl): the
+// reference's CutIntegrationRule (cutint/xintegration.cpp:1626-1754) with
+// NumericalIntegrationStrategy<ET_TRIG / ET_TET, ET_POINT>::MakeQuadRule
+// (:757-1063).  A simplex (reference coordinates) at refinement level L is
+// checked on the lattice of its points with spacing 1/2^L (CheckIfCut,
+// :620-751; CutIntegrationRule sets no distance threshold, so the check is
+// the sign of the level set at every lattice point, >= 0 counting as
+// positive).  An uncut simplex gets the plain rule of its domain; a cut one
+// is refined into the reference's children (:820-914) down to level 0,
+// where the vertex signs decide (Simplex::CheckIfCut, xdecompose.hpp:34-80:
+// a side whose share of sum |l| is below 1e-14 does not count) and a cut
+// simplex gets the straight-cut rule of its vertex values (CutSimplex::MakeQuad,
+// :1084-1550: the region and interface of the linear interpolant).  Every
+// rule is built on the physical image of its simplex, so points are physical
+// and weights are physical measures; integrals of polynomials equal the
+// reference's up to rounding.
+// ---------------------------------------------------------------------------
+namespace {
+
+// children of the red refinement, as barycentric weights on the parent's
+// vertices (xintegration.cpp:826-833, 896-906) and vertex lists (:836-841, 898-906)
+const double SUB_TRI_BARY[6][3] = {{0, 0, 1}, {.5, 0, .5}, {1, 0, 0}, {0, .5, .5}, {.5, .5, 0}, {0, 1, 0}};
+const int SUB_TRI_KIDS[4][3] = {{0, 1, 3}, {1, 2, 4}, {1, 3, 4}, {3, 4, 5}};
+const double SUB_TET_BARY[10][4] = {{0, 0, 0, 1}, {.5, 0, 0, .5}, {1, 0, 0, 0}, {0, .5, 0, .5}, {.5, .5, 0, 0},
+                                    {0, 1, 0, 0}, {0, 0, .5, .5}, {.5, 0, .5, 0}, {0, .5, .5, 0}, {0, 0, 1, 0}};
+const int SUB_TET_KIDS[8][4] = {{1, 2, 4, 7}, {3, 4, 5, 8}, {6, 7, 8, 9}, {3, 4, 8, 6},
+                                {3, 4, 1, 6}, {0, 1, 3, 6}, {8, 6, 1, 7}, {8, 4, 1, 7}};
+
+struct Subdiv {
+  int D, k;
+  const int* gv;        // the element's vertex ids (orientation of the basis)
+  const double* coef;   // the level set's element coefficients (H1 basis of order k)
+  Geo g;                // the element map
+  int dt, order;
+  std::vector<double> P, W;  // physical points (3 per point) and weights
+  int err = 0;
+};
+
+double subdiv_lset(const Subdiv& S, const double* xi) {
+  double phi[20], dphi[20][3];
+  basis(S.D, S.k, S.gv, xi, phi, dphi);
+  double v = 0.0;
+  const int n = ndof_el(S.D, S.k);
+  for (int i = 0; i < n; i++) v += S.coef[i] * phi[i];
+  return v;
+}
+
+// NumericalIntegrationStrategy::CheckIfCut without a distance threshold
+int subdiv_lattice(const Subdiv& S, const double (*v)[3], int L) {
+  const int D = S.D, np = 1 << L;
+  const double dx = 1.0 / np;
+  bool pos = false, neg = false;
+  int I[3] = {0, 0, 0};
+  for (;;) {
+    double xi[3] = {0, 0, 0};
+    for (int d = 0; d < D; d++) xi[d] = v[0][d];
+    for (int j = 0; j < D; j++)
+      for (int d = 0; d < D; d++) xi[d] += I[j] * dx * (v[j + 1][d] - v[0][d]);
+    if (subdiv_lset(S, xi) >= 0.0) pos = true;
+    else neg = true;
+    if (pos && neg) return IF;
+    // next lattice index (I[0] fastest, sum <= np)
+    I[0]++;
+    int c = 0;
+    while (c < D) {
+      int sum = 0;
+      for (int i = 0; i < D; i++) sum += I[i];
+      if (sum <= np) break;
+      if (c == D - 1) return pos ? POS : NEG;
+      I[c] = 0;
+      I[c + 1]++;
+      c++;
+    }
+  }
+}
+
+// Simplex::CheckIfCut on the vertex values
+int subdiv_vertex_domain(const double* l, int n) {
+  bool pos = false, neg = false;
+  double sp = 0.0, sn = 0.0;
+  for (int i = 0; i < n; i++) {
+    if (l[i] >= 0.0) {
+      sp += l[i];
+      pos = true;
+    } else {
+      sn -= l[i];
+      neg = true;
+    }
+  }
+  const double s = sp + sn;
+  if (sp / s < 1e-14) pos = false;
+  if (sn / s < 1e-14) neg = false;
+  if (pos && neg) return IF;
+  return pos ? POS : (neg ? NEG : POS);
+}
+
+// a rule on the physical image of the reference-coordinate simplex v: the
+// plain rule (cut = false) or the straight cut of the vertex values l
+void subdiv_fill(Subdiv& S, const double (*v)[3], const double* l, bool cut) {
+  const int D = S.D;
+  double elc[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int i = 0; i <= D; i++)
+    for (int r = 0; r < D; r++) {
+      double x = S.g.x0[r];
+      for (int c = 0; c < D; c++) x += S.g.F[r][c] * v[i][c];
+      elc[i * D + r] = x;
+    }
+  Geo gs;
+  make_geo(D, elc, gs);
+  std::vector<double> p, w;
+  int n;
+  if (cut) {
+    // a vertex value of exactly 0 counts as positive (CutSimplex::MakeQuad,
+    // :1140-1180: such a vertex is cut against its negative neighbours at the
+    // vertex itself): the smallest positive normal double does the same
+    double lc[4];
+    for (int i = 0; i <= D; i++) lc[i] = l[i] == 0.0 ? 2.2250738585072014e-308 : l[i];
+    n = straight_cut_rule(gs, lc, S.dt, S.order, p, w);
+    if (n < -1) {
+      S.err = n;
+      return;
+    }
+  } else {
+    // FillSimplexWithRule (:218-264): point = (1 - sum ip) X0 + sum ip_m X_{m+1},
+    // weight = w |det(X1 - X0, ...)|
+    Sub sub;
+    sub.np = D + 1;
+    for (int i = 0; i <= D; i++)
+      for (int r = 0; r < 3; r++) sub.p[i].c[r] = r < D ? elc[i * D + r] : 0.0;
+    plain_rule(sub, S.order, p, w);
+    for (size_t q = 0; q < w.size(); q++) {
+      S.P.insert(S.P.end(), &p[3 * q], &p[3 * q] + 3);
+      S.W.push_back(w[q]);
+    }
+    return;
+  }
+  const double meas = std::fabs(gs.det);
+  for (int q = 0; q < n; q++) {
+    double x[3] = {0, 0, 0};
+    for (int r = 0; r < D; r++) {
+      double s = gs.x0[r];
+      for (int c = 0; c < D; c++) s += gs.F[r][c] * p[3 * q + c];
+      x[r] = s;
+    }
+    S.P.insert(S.P.end(), x, x + 3);
+    S.W.push_back(w[q] * meas);
+  }
+}
+
+// NumericalIntegrationStrategy::MakeQuadRule on the simplex v at level L
+void subdiv_quad(Subdiv& S, const double (*v)[3], int L) {
+  const int D = S.D;
+  const int dself = subdiv_lattice(S, v, L);
+  if (dself != IF) {
+    if (dself == S.dt) subdiv_fill(S, v, nullptr, false);
+    return;
+  }
+  if (L > 0) {
+    const int nk = D == 2 ? 4 : 8;
+    for (int c = 0; c < nk; c++) {
+      double w[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+      for (int j = 0; j <= D; j++)
+        for (int d = 0; d <= D; d++) {
+          const double b = D == 2 ? SUB_TRI_BARY[SUB_TRI_KIDS[c][j]][d] : SUB_TET_BARY[SUB_TET_KIDS[c][j]][d];
+          for (int r = 0; r < D; r++) w[j][r] += b * v[d][r];
+        }
+      subdiv_quad(S, w, L - 1);
+    }
+    return;
+  }
+  double l[4];
+  for (int i = 0; i <= D; i++) l[i] = subdiv_lset(S, v[i]);
+  const int dv = subdiv_vertex_domain(l, D + 1);
+  if (dv == IF) subdiv_fill(S, v, l, true);
+  else if (dv == S.dt) subdiv_fill(S, v, nullptr, false);
+}
+
+// the rule of element e for the level set coefficients of the space s (order k)
+int subdiv_rule(const orc_space* s, const double* lset_coefs, int e, int dt, int order, int subdivlvl, Subdiv& S) {
+  const int D = s->D;
+  S.D = D;
+  S.k = s->k;
+  S.gv = &s->elv[(size_t)e * (D + 1)];
+  double c[20];
+  for (int i = 0; i < s->nd; i++) c[i] = lset_coefs[s->el_dofs[(size_t)e * s->nd + i]];
+  S.coef = c;
+  element_geo(s, e, S.g, nullptr, nullptr);
+  S.dt = dt;
+  S.order = order;
+  S.P.clear();
+  S.W.clear();
+  S.err = 0;
+  double v[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};  // reference vertices (1,0,0),(0,1,0),(0,0,1),(0,0,0)
+  for (int i = 0; i < D; i++) v[i][i] = 1.0;
+  subdiv_quad(S, v, subdivlvl);
+  S.coef = nullptr;
+  return S.err;
+}
+
+}  // namespace
+
+extern "C" {
+
+double orc_integrate_subdiv(const orc_space* s, const double* lset_coefs, int dt, int order, int subdivlvl, int ex,
+                            int ey, int ez, const uint64_t* defined_on, int* status) {
+  const int D = s->D;
+  double sum = 0.0;
+  Subdiv S;
+  if (status) *status = 0;
+  for (int e = 0; e < s->ne; e++) {
+    if (defined_on && !test_bit(defined_on, e)) continue;
+    const int st = subdiv_rule(s, lset_coefs, e, dt, order, subdivlvl, S);
+    if (st && status) *status = st;
+    for (size_t q = 0; q < S.W.size(); q++) {
+      const double* x = &S.P[3 * q];
+      const double fv = std::pow(x[0], ex) * std::pow(x[1], ey) * (D == 3 ? std::pow(x[2], ez) : 1.0);
+      sum += S.W[q] * fv;
+    }
+  }
+  return sum;
+}
+
+int orc_subdiv_rule(const orc_space* s, const double* lset_coefs, int e, int dt, int order, int subdivlvl,
+                    double* pts, double* wts, int maxpts) {
+  Subdiv S;
+  const int st = subdiv_rule(s, lset_coefs, e, dt, order, subdivlvl, S);
+  if (st) return st;
+  const int n = (int)S.W.size();
+  if (n > maxpts) return ERR_CAPACITY;
+  std::memcpy(pts, S.P.data(), sizeof(double) * 3 * n);
+  std::memcpy(wts, S.W.data(), sizeof(double) * n);
+  return n;
+}
+
+// NEG moments (x^a y^b z^c, a + b + c <= 4; by degree, then a, then b
+// descending) of P2 level sets on the reference tetrahedron, given by their
+// values at the vertices and edge midpoints (edges (0,1),(0,2),(0,3),(1,2),
+// (1,3),(2,3)), by the subdivision rule of the given level, order 4
+int orc_subdiv_moments_p2(int64_t n, const double* vals10, int levels, double* out35, int nthreads) {
+  const double ref[12] = {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0};
+  const int32_t elv[4] = {0, 1, 2, 3};
+  orc_space* s = orc_space_create(3, 4, ref, 1, elv, 2);
+  std::atomic<int> err(0);
+  parallel_for(n, nthreads, [&](int64_t b, int64_t en) {
+    Subdiv S;
+    std::vector<double> c(s->ndof);
+    for (int64_t e = b; e < en; e++) {
+      const double* p = vals10 + e * 10;
+      for (int i = 0; i < 4; i++) c[s->el_dofs[i]] = p[i];
+      for (int j = 0; j < 6; j++)
+        c[s->el_dofs[4 + j]] = 4.0 * p[4 + j] - 2.0 * (p[TET_EDGES[j][0]] + p[TET_EDGES[j][1]]);
+      const int st = subdiv_rule(s, c.data(), 0, NEG, 4, levels, S);
+      if (st) err = st;
+      double* m = out35 + e * 35;
+      for (int k = 0; k < 35; k++) m[k] = 0.0;
+      for (size_t q = 0; q < S.W.size(); q++) {
+        const double x = S.P[3 * q], y = S.P[3 * q + 1], z = S.P[3 * q + 2];
+        const double px[5] = {1, x, x * x, x * x * x, x * x * x * x};
+        const double py[5] = {1, y, y * y, y * y * y, y * y * y * y};
+        const double pz[5] = {1, z, z * z, z * z * z, z * z * z * z};
+        int k = 0;
+        for (int t = 0; t <= 4; t++)
+          for (int a = t; a >= 0; a--)
+            for (int bb = t - a; bb >= 0; bb--) m[k++] += S.W[q] * px[a] * py[bb] * pz[t - a - bb];
+      }
+    }
+  });
+  orc_space_destroy(s);
+  return err.load();
+}
+
 int orc_element_matrix(const orc_space* s, const double* lset_vertex, const orc_term* terms, int nterms, int e,
                        double* elmat) {
   return element_matrix(s, lset_vertex, terms, nterms, e, elmat);

@@ -109,6 +109,21 @@ int orc_facet_matrix(const orc_space*, const double* lset_vertex, const orc_term
  * accuracy acc: c[0 .. 2w] on the offsets -w .. w (returns w) and the step
  * factor of GetOptimalEps (times the element size h). */
 int orc_fd_stencil(int k, int acc, double* c, double* eps);
+/* Subdivision cut rules of a higher-order level set (the reference's
+ * CutIntegrationRule with subdivlvl, cutint/xintegration.cpp:1626-1754 and
+ * NumericalIntegrationStrategy::MakeQuadRule): lset_coefs are the level set's
+ * coefficients in the space s (H1 of order 1..3).  orc_subdiv_rule returns the
+ * number of points of element e (physical points, 3 per point, and physical
+ * weights) or an error; orc_integrate_subdiv integrates x^ex y^ey z^ez over
+ * the domain (status: the first rule error, 0 if none). */
+int orc_subdiv_rule(const orc_space* s, const double* lset_coefs, int e, int dt, int order, int subdivlvl,
+                    double* pts, double* wts, int maxpts);
+double orc_integrate_subdiv(const orc_space* s, const double* lset_coefs, int dt, int order, int subdivlvl, int ex,
+                            int ey, int ez, const uint64_t* defined_on, int* status);
+/* NEG moments (35, monomials of degree <= 4) of n P2 level sets on the
+ * reference tetrahedron (values at the vertices and edge midpoints) by the
+ * subdivision rule of the given level. */
+int orc_subdiv_moments_p2(int64_t n, const double* vals10, int levels, double* out35, int nthreads);
 /* Discontinuous (L2) space of order k: the same element basis with element-
  * local dofs, dof(e, i) = e * ndof_el + i. */
 orc_space* orc_space_create_l2(int D, int nv, const double* coords, int ne, const int32_t* elv, int order);

@@ -161,6 +161,35 @@ def test_fallback_takes_the_plain_rule(xg):
     xg._lib.call("xg_mlp_destroy", mlp)
 
 
+def test_fallback_takes_the_subdivision_rule(xg, orc):
+    """With the subdivision rule as the plain rule (plain_subdivlvl = 2) and
+    kappa_max = 0 every element in the band takes that rule: the result
+    equals xg_subdiv_moments_tet bit for bit, and the oracle's rule within
+    1e-13."""
+    v = L.resolved_values(2000, np.random.default_rng(19))
+    d_v = dev(v)
+    mlp = ctypes.c_void_p()
+    xg._lib.call("xg_mlp_create", 3, ctypes.byref(mlp))
+    out = torch.zeros((len(v), 35), dtype=torch.float64, device="cuda")
+    nf = torch.zeros(1, dtype=torch.int32, device="cuda")
+    xg._lib.call("xg_learned_moments_tet_ex", mlp, xg._vp(d_v), len(v), ctypes.c_double(0.0), 2, xg._vp(out),
+                 xg._vp(nf), xg._stream())
+    ref = torch.zeros_like(out)
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    xg._lib.call("xg_subdiv_moments_tet", xg._vp(d_v), len(v), 2, xg._vp(ref), xg._vp(err), xg._stream())
+    torch.cuda.synchronize()
+    xg._lib.check(xg._lib.load().xg_mlp_check(mlp), "learned")
+    assert int(err.item()) == 0
+    p1 = v[:, :4]
+    band = (np.where(np.abs(p1) < 1e-14, 1e-14, p1).min(1) < 0) & (np.where(np.abs(p1) < 1e-14, 1e-14, p1).max(1) > 0)
+    assert int(nf.item()) == band.sum()
+    got = out.cpu().numpy()
+    assert np.array_equal(got[band], ref.cpu().numpy()[band])
+    orc_m = orc.subdiv_moments_p2(v, 2, 8)
+    assert np.abs(got[band] - orc_m[band]).max() < 1e-13
+    xg._lib.call("xg_mlp_destroy", mlp)
+
+
 def test_training_gains_over_the_method_without_it(xg):
     """A short GPU training run on mildly curved elements (targets: the
     isoparametric moments; training samples whose defect exceeds 5 % of the

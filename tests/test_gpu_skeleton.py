@@ -156,3 +156,69 @@ def test_python_dg_script(xg, orc):
              dict(kind=orc.TERM_GHOST_MASS, coef=0.1, hpow=-2, defined_on=gpb),
              dict(kind=orc.TERM_SKEL_DN2, domain=orc.WHOLE, coef=0.01, hpow=3, defined_on=gpb)]
     compare(sp, sp.assemble(l, terms), a.mat, 1e-12)
+
+
+def quadratic_coefs(mesh, el_dofs, ndof, order, p):
+    """Coefficients of a quadratic polynomial in the element basis: vertex
+    values, 4 p(mid) - 2 (p_a + p_b) on the quadratic edge functions, 0 on the
+    cubic edge and face functions."""
+    D = mesh.dim
+    edges = [(0, 1), (0, 2), (1, 2)] if D == 2 else [(0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3)]
+    out = np.zeros(ndof)
+    for e in range(mesh.ne):
+        X = mesh.coords[mesh.elements[e]]
+        loc = [p(X[i]) for i in range(D + 1)]
+        if order >= 2:
+            for a_, b_ in edges:
+                loc.append(4 * p(0.5 * (X[a_] + X[b_])) - 2 * (p(X[a_]) + p(X[b_])))
+                if order == 3:
+                    loc.append(0.0)
+        loc += [0.0] * (el_dofs.shape[1] - len(loc))
+        out[el_dofs[e]] = loc
+    return out
+
+
+@pytest.mark.parametrize("dim,order", [(2, 2), (2, 3), (3, 2)])
+def test_unfitted_dg_solve_reproduces_quadratic(xg, dim, order):
+    """Unfitted symmetric interior-penalty DG (the fictdom_dg form) on L2 P2 /
+    P3 with the planar boundary x = c: u = x^2 - c^2 solves -laplace u = -2
+    with u = 0 on the cut and homogeneous Neumann data on the box sides.  The
+    method is consistent and u lies in the space, so the solution of the
+    assembled system is u itself."""
+    import scipy.sparse as sps
+    import scipy.sparse.linalg as spla
+    from ngsxfem_gb300.meshes import MakeStructured2DMesh, MakeStructured3DMesh
+    c = 0.537
+    m = MakeStructured2DMesh(8, 7) if dim == 2 else MakeStructured3DMesh(4)
+    V1 = xg.H1(m, order=1)
+    gf = xg.GridFunction(V1)
+    xg.InterpolateToP1(m.coords[:, 0] - c, gf)
+    ci = xg.CutInfo(m, gf)
+    hasneg, hasif = ci.GetElementsOfType(xg.HASNEG), ci.GetElementsOfType(xg.IF)
+    ba_gp = xg.GetFacetsWithNeighborTypes(m, a=hasneg, b=hasif)
+    ba_fd = xg.GetFacetsWithNeighborTypes(m, a=hasneg, b=hasneg)
+    V = xg.L2(m, order=order, dgjumps=True)
+    u, v = V.TnT()
+    h = xg.specialcf.mesh_size
+    nh = xg.Normalize(xg.grad(gf))
+    nF = xg.specialcf.normal(dim)
+    lam = 20.0 * order ** 2
+    flux_u = -0.5 * (xg.grad(u) + xg.grad(u.Other())) * nF
+    flux_v = -0.5 * (xg.grad(v) + xg.grad(v.Other())) * nF
+    jump_u, jump_v = u - u.Other(), v - v.Other()
+    a = xg.BilinearForm(V)
+    a += xg.grad(u) * xg.grad(v) * xg.dCut(gf, xg.NEG, definedonelements=hasneg)
+    a += (lam / h * jump_u * jump_v + flux_u * jump_v + flux_v * jump_u) * \
+        xg.dCut(gf, xg.NEG, skeleton=True, definedonelements=ba_fd)
+    a += (-xg.grad(u) * nh * v - xg.grad(v) * nh * u + lam / h * u * v) * xg.dCut(gf, xg.IF, definedonelements=hasif)
+    a += 0.1 / h ** 2 * (u - u.Other()) * (v - v.Other()) * xg.dFacetPatch(definedonelements=ba_gp)
+    a.Assemble(ci)
+    f = xg.LinearForm(V)
+    f += -2.0 * v * xg.dCut(gf, xg.NEG, definedonelements=hasneg)
+    f.Assemble(ci)
+    A = a.mat.to_scipy().tocsr()
+    act = a.mat.row_dof[: a.mat.nrows].cpu().numpy()
+    Aa = A[act][:, act]
+    x = spla.spsolve(sps.csc_matrix(Aa), f.vec.cpu().numpy()[act])
+    ue = quadratic_coefs(m, V.element_dofs(), V.ndof, order, lambda X: X[0] ** 2 - c * c)[act]
+    assert np.abs(x - ue).max() < 1e-9 * max(1.0, np.abs(ue).max()), np.abs(x - ue).max()
