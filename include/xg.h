@@ -367,6 +367,33 @@ int xg_form_check(xg_form* form);
  * n = 0 switches it off.  The events are the caller's. */
 int xg_form_stage_events(xg_form* form, void* const* events, int n);
 
+/* ---- bilinear forms on regions of several level sets ------------------- */
+/* SymbolicCutBFI with a multi-level-set LevelsetIntegrationDomain
+ * (symboliccutbfi.cpp:76-486 on the rules of cutint/mlsetintegration.cpp:
+ * 6-180, e.g. tests/pytests/test_mlset_poisson.py): a region term integrates
+ * its kind over the union of ntup domain tuples of the M level sets (entries
+ * XG_NEG / XG_POS / XG_IF, the codimension given by the IF entries); the
+ * normal of XG_TERM_NGRADU_V / _U_NGRADV is grad(l)/|grad(l)| of the P1
+ * level set normal_lset (an outer normal pointing into POS; a sign goes into
+ * coef). */
+typedef struct {
+  int32_t kind;             /* XG_TERM_MASS .. XG_TERM_CONV */
+  int32_t order;            /* -1: the default of the kind */
+  int32_t hpow;
+  int32_t normal_lset;
+  double coef;
+  double b[3];              /* XG_TERM_CONV */
+  int32_t ntup;             /* 1..256 */
+  const int8_t* h_tuples;   /* host [ntup][M] */
+  const uint64_t* d_defined_on; /* element bits, NULL = all */
+} xg_mlterm;
+/* patch_terms: XG_TERM_GHOST_MASS terms with their facet sets (d_defined_on). */
+int xg_mlset_form_create(xg_space* space, int32_t M, const xg_mlterm* terms, int32_t nterms,
+                         const xg_term* patch_terms, int32_t npatch, int precision, xg_form** out);
+/* d_lsets: [M][nv] P1 vertex values.  The active elements are the union of
+ * the region terms' element sets; the CSR as xg_form_assemble's. */
+int xg_mlset_form_assemble(xg_form* form, const double* d_lsets, xg_csr* out, void* stream);
+
 /* ---- linear forms (xfem/symboliccutlfi.cpp) --------------------------------- */
 typedef enum {
   XG_LTERM_SOURCE = 0,     /* coef * x^e0 y^e1 z^e2 * v                         */

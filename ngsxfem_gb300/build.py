@@ -36,6 +36,7 @@ UNITS = [
     ("xg_mlp_tc.cu", []),
     ("xg_skel.cu", []),
     ("xg_subdiv.cu", []),
+    ("xg_mlform.cu", []),
 ]
 
 

@@ -2534,6 +2534,12 @@ struct xg_form {
   xg_space* space = nullptr;
   xg_mesh* mesh = nullptr;
   int precision = XG_PREC_FP64;
+  // terms on regions of several level sets (xg_mlset_form_create)
+  bool ml = false;
+  int ml_M = 0;
+  std::vector<MlTermDev> ml_terms;
+  MlTermDev* d_ml_terms = nullptr;
+  int8_t* d_ml_tuples = nullptr;
   std::vector<xg_term> terms;
   std::vector<int> term_slot;  // group index (volume) or patch index
   FormDesc desc;
@@ -2641,7 +2647,7 @@ int form_free(xg_form* f) {
                   f->d_elmat, f->d_famat, f->d_err, f->d_dom, f->d_ratio, f->d_bits, f->d_fbits, f->d_fbits_sk,
                   f->d_mtab_i, f->d_mtab_c, f->d_mu, f->d_mhat, f->d_cutlist, f->d_dof_flag,
                   f->d_el_rowslot, f->d_pos_rows, f->d_nbpos, f->d_cand_fs, f->d_act_slot, f->d_vcols, f->d_vvals,
-                  f->d_bsum_rows};
+                  f->d_bsum_rows, f->d_ml_terms, f->d_ml_tuples};
   for (void* p : ptrs) cudaFree(p);
   delete f;
   return XG_OK;
@@ -3873,6 +3879,10 @@ extern "C" {
 
 int xg_form_assemble(xg_form* f, const double* d_lset, const uint8_t* d_dom, xg_csr* out, void* stream) {
   if (!out || !out->d_row_dof || !out->d_rowptr || !out->d_cols || !out->d_vals || !out->d_counts) return XG_ERR_ARG;
+  if (f && f->ml) {
+    set_last_error("xg_form_assemble: forms on several level sets take xg_mlset_form_assemble");
+    return XG_ERR_ARG;
+  }
   int st = assemble_front(f, d_lset, d_dom, out, stream);
   if (st) return st;
   cudaStream_t s = (cudaStream_t)stream;
@@ -4032,6 +4042,10 @@ extern "C" {
 
 int xg_cutfem_step(xg_form* f, const double* d_lset, xg_csr* out, void* stream) {
   if (!f || !d_lset || !out) return XG_ERR_ARG;
+  if (f->ml) {
+    set_last_error("xg_cutfem_step: forms on several level sets take xg_mlset_form_assemble");
+    return XG_ERR_ARG;
+  }
   int st = cutfem_front(f, d_lset, out, stream);
   if (st) return st;
   cudaStream_t s = (cudaStream_t)stream;
@@ -4673,6 +4687,161 @@ int xg_step_graph_launch(xg_step_graph* g, void* stream) {
   if (!g || !g->exec) return XG_ERR_ARG;
   XG_CUDA(cudaGraphLaunch(g->exec, (cudaStream_t)stream));
   return XG_OK;
+}
+
+}  // extern "C"
+
+// ============================================================================
+// Bilinear forms on regions of several level sets (xg_mlset_form_*): the
+// element matrices of the region terms by their multi-level-set rules
+// (csrc/xg_mlform.cu), the facet-patch terms and the row scatter of the
+// spatial forms.
+// ============================================================================
+namespace {
+
+// active elements: in the element set of some region term (all without one)
+__global__ void k_ml_active(int ne, const MlTermDev* __restrict__ terms, int nterms, uint32_t* bits, int64_t nw32) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  bool act = false;
+  if (e < ne)
+    for (int t = 0; t < nterms; t++)
+      if (!terms[t].defined_on || tbit(terms[t].defined_on, e)) act = true;
+  const unsigned m = __ballot_sync(0xffffffffu, act);
+  if ((threadIdx.x & 31) == 0 && (e >> 5) < nw32) bits[e >> 5] = m;
+}
+
+}  // namespace
+
+extern "C" {
+
+int xg_mlset_form_create(xg_space* space, int32_t M, const xg_mlterm* terms, int32_t nterms,
+                         const xg_term* patch_terms, int32_t npatch, int precision, xg_form** out) {
+  if (!space || !out || M < 1 || M > 8 || nterms < 1 || !terms || npatch < 0 || (npatch > 0 && !patch_terms) ||
+      (precision != XG_PREC_FP64 && precision != XG_PREC_MIXED)) {
+    set_last_error("xg_mlset_form_create: bad arguments (1 <= M <= 8, at least one region term)");
+    return XG_ERR_ARG;
+  }
+  if (space->kt >= 0 || space->mesh->tensor) {
+    set_last_error("xg_mlset_form_create: spatial spaces on simplex meshes");
+    return XG_ERR_UNSUPPORTED;
+  }
+  for (int t = 0; t < npatch; t++)
+    if (patch_terms[t].kind != XG_TERM_GHOST_MASS) {
+      set_last_error("xg_mlset_form_create: the patch terms are XG_TERM_GHOST_MASS");
+      return XG_ERR_ARG;
+    }
+  std::vector<MlTermDev> mt(nterms);
+  std::vector<int8_t> tup;
+  for (int t = 0; t < nterms; t++) {
+    const xg_mlterm& T = terms[t];
+    if (T.kind < XG_TERM_MASS || T.kind > XG_TERM_CONV || T.ntup < 1 || T.ntup > 256 || !T.h_tuples ||
+        T.normal_lset < 0 || T.normal_lset >= M) {
+      set_last_error("xg_mlset_form_create: bad region term (kind MASS..CONV, 1..256 tuples, normal level set)");
+      return XG_ERR_ARG;
+    }
+    const int order = T.order >= 0 ? T.order : default_order(T.kind, space->order);
+    if (order > kMaxOrder) {
+      set_last_error("xg_mlset_form_create: integration order above 8");
+      return XG_ERR_UNSUPPORTED;
+    }
+    MlTermDev& D = mt[t];
+    D.kind = T.kind;
+    D.order = order;
+    D.hpow = T.hpow;
+    D.normal_lset = T.normal_lset;
+    D.ntup = T.ntup;
+    D.tup_off = (int)tup.size();
+    D.coef = T.coef;
+    for (int k = 0; k < 3; k++) D.b[k] = T.b[k];
+    D.defined_on = T.d_defined_on;
+    for (int k = 0; k < T.ntup * M; k++) {
+      const int8_t v = T.h_tuples[k];
+      if (v != XG_NEG && v != XG_POS && v != XG_IF) {
+        set_last_error("xg_mlset_form_create: domain tuples hold XG_NEG / XG_POS / XG_IF");
+        return XG_ERR_ARG;
+      }
+      tup.push_back(v);
+    }
+  }
+  int st = ensure_device_rules();
+  if (st) return st;
+  *out = nullptr;
+  auto* f = new xg_form();
+  f->space = space;
+  f->mesh = space->mesh;
+  f->precision = precision;
+  f->terms.assign(patch_terms, patch_terms + npatch);
+  f->ml = true;
+  f->ml_M = M;
+  f->ml_terms = mt;
+  st = build_desc(f);
+  if (!st) st = upload_tables(f);
+  if (!st) st = form_workspace(f);
+  if (!st) st = apply_cached_tune(f);
+  if (!st) {
+    cudaError_t e = cudaMalloc((void**)&f->d_ml_terms, mt.size() * sizeof(MlTermDev));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&f->d_ml_tuples, tup.size());
+    if (e == cudaSuccess)
+      e = cudaMemcpy(f->d_ml_terms, mt.data(), mt.size() * sizeof(MlTermDev), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(f->d_ml_tuples, tup.data(), tup.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) st = cuda_fail(e, "xg_mlset_form_create");
+  }
+  if (st) {
+    form_free(f);
+    return st;
+  }
+  *out = f;
+  return XG_OK;
+}
+
+int xg_mlset_form_assemble(xg_form* f, const double* d_lsets, xg_csr* out, void* stream) {
+  if (!f || !f->ml || !d_lsets || !out || !out->d_row_dof || !out->d_rowptr || !out->d_cols || !out->d_vals ||
+      !out->d_counts)
+    return XG_ERR_ARG;
+  if (out->cap_rows < f->space->ndof) {
+    set_last_error("xg_mlset_form_assemble: cap_rows below ndof");
+    return XG_ERR_CAPACITY;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  xg_mesh* m = f->mesh;
+  int st;
+  // active elements (all in the second list) and facets
+  XG_CUDA(cudaMemsetAsync(f->d_act_un, 0, f->nw32_el * 4, s));
+  k_ml_active<<<(unsigned)((f->nw32_el * 32 + 255) / 256), 256, 0, s>>>(m->ne, f->d_ml_terms, (int)f->ml_terms.size(),
+                                                                        f->d_act_cut, f->nw32_el);
+  if ((st = compact(f, f->d_act_un, f->nw32_el, f->d_l_un, f->d_el_slot, f->d_counts + 0, s))) return st;
+  if ((st = compact(f, f->d_act_cut, f->nw32_el, f->d_l_cut, f->d_el_slot, f->d_counts + 1, s, f->d_counts + 0)))
+    return st;
+  if (f->has_patch) {
+    k_active_facets<<<(unsigned)((f->nw32_fa * 32 + 255) / 256), 256, 0, s>>>(m->nfacets, m->d_facet_els, f->desc,
+                                                                              f->d_act_fa, f->nw32_fa);
+    if ((st = compact(f, f->d_act_fa, f->nw32_fa, f->d_l_fa, f->d_fa_slot, f->d_counts + 2, s))) return st;
+  } else {
+    XG_CUDA(cudaMemsetAsync(f->d_act_fa, 0, f->nw32_fa * 4, s));
+    XG_CUDA(cudaMemsetAsync(f->d_counts + 2, 0, sizeof(int), s));
+  }
+  MlFormLaunch L;
+  L.dim = m->dim;
+  L.order = f->space->order;
+  L.M = f->ml_M;
+  L.ne = m->ne;
+  L.nv = m->nv;
+  L.elv = m->d_elv;
+  L.xyz = m->d_xyz;
+  L.lsets = d_lsets;
+  L.terms = f->d_ml_terms;
+  L.nterms = (int)f->ml_terms.size();
+  L.tuples = f->d_ml_tuples;
+  L.list = f->d_l_cut;
+  L.counts = f->d_counts;
+  L.rowslot = f->d_el_rowslot;
+  L.elmat = f->d_elmat;
+  L.fp64 = f->precision == XG_PREC_FP64 ? 1 : 0;
+  L.err = f->d_err;
+  if ((st = mlform_launch(L, s))) return st;
+  const bool fp64 = f->precision == XG_PREC_FP64;
+  if (f->has_patch && (st = fp64 ? dispatch_patch<double>(f, s) : dispatch_patch<float>(f, s))) return st;
+  return rows_back(f, out, s);
 }
 
 }  // extern "C"

@@ -168,6 +168,35 @@ int upload_rules_mlset();
 int upload_rules_isomesh();
 int upload_rules_skel();  // xg_skel.cu
 int upload_rules_subdiv();  // xg_subdiv.cu
+int upload_rules_mlform();  // xg_mlform.cu
+
+// a bilinear-form term on a region of several level sets (device copy)
+struct MlTermDev {
+  int kind, order, hpow, normal_lset;
+  int ntup, tup_off;           // the region: ntup tuples of M entries at tuples + tup_off
+  double coef;
+  double b[3];
+  const uint64_t* defined_on;  // element bits, NULL = all
+};
+// the element matrices of such terms for the listed elements (xg_mlform.cu),
+// written at the elements' row slots
+struct MlFormLaunch {
+  int dim, order, M;
+  int ne, nv;
+  const int32_t* elv;
+  const double* xyz;
+  const double* lsets;         // [M][nv]
+  const MlTermDev* terms;
+  int nterms;
+  const int8_t* tuples;
+  const int32_t* list;         // active elements
+  const int* counts;           // [1]: their number
+  const int32_t* rowslot;
+  void* elmat;
+  int fp64;
+  int* err;
+};
+int mlform_launch(const MlFormLaunch& launch, cudaStream_t s);
 // per-element NEG moments of P2 level sets on the reference tetrahedron by
 // the subdivision rule (xg_subdiv.cu); with d_list, only the d_count listed
 // elements

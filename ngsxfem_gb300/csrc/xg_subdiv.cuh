@@ -54,6 +54,43 @@ XG_QHD double lset_at(const Elem<D, K>& el, const double* xi) {
   return v;
 }
 
+// lattice point of index I (spacing 1/2^L) of simplex v
+template <int D>
+XG_QHD void lattice_point(const double (*v)[3], const int* I, double dx, double* xi) {
+  for (int d = 0; d < 3; d++) xi[d] = d < D ? v[0][d] : 0.0;
+  for (int j = 0; j < D; j++)
+    for (int d = 0; d < D; d++) xi[d] += I[j] * dx * (v[j + 1][d] - v[0][d]);
+}
+
+#ifdef __CUDACC__
+// CheckIfCut with the lattice points split over the lanes of a warp (every
+// lane of the warp calls it with the same simplex; the answer is the same)
+template <int D, int K>
+__device__ __forceinline__ int lattice_domain_warp(const Elem<D, K>& el, const double (*v)[3], int L) {
+  const int np = 1 << L, lane = threadIdx.x & 31;
+  const double dx = 1.0 / np;
+  // lattice points: I with I_0 + .. + I_{D-1} <= np, enumerated by a flat index
+  const int side = np + 1, total = D == 2 ? side * side : side * side * side;
+  bool pos = false, neg = false;
+  for (int t0 = 0; t0 < total; t0 += 32) {
+    const int t = t0 + lane;
+    if (t < total) {
+      int I[3] = {t % side, (t / side) % side, D == 3 ? t / (side * side) : 0};
+      if (I[0] + I[1] + I[2] <= np) {
+        double xi[3];
+        lattice_point<D>(v, I, dx, xi);
+        if (lset_at(el, xi) >= 0.0) pos = true;
+        else neg = true;
+      }
+    }
+    pos = __any_sync(0xffffffffu, pos);
+    neg = __any_sync(0xffffffffu, neg);
+    if (pos && neg) return XG_IF;
+  }
+  return pos ? XG_POS : XG_NEG;
+}
+#endif
+
 // CheckIfCut on the lattice of simplex v (reference coordinates) at level L
 template <int D, int K>
 XG_QHD int lattice_domain(const Elem<D, K>& el, const double (*v)[3], int L) {
@@ -145,8 +182,10 @@ XG_QNI int fill(const RuleTable* Rp, const Elem<D, K>& el, const double (*v)[3],
 }
 
 // the rule of one element: emit(physical point, physical weight) per point;
-// returns 0 or the first xg error of a cut
-template <int D, int K, class E>
+// returns 0 or the first xg error of a cut.  WARP: every lane of a warp runs
+// it for the same element (the lattice checks split over the lanes, every
+// lane sees every point)
+template <int D, int K, class E, bool WARP = false>
 XG_QNI int element_rule(const RuleTable* Rp, const Elem<D, K>& el, int dt, int order, int levels, E& emit) {
   struct Frame {
     double v[4][3];
@@ -162,7 +201,11 @@ XG_QNI int element_rule(const RuleTable* Rp, const Elem<D, K>& el, int dt, int o
   while (sp > 0) {
     Frame& f = st[sp - 1];
     if (f.next < 0) {
+#ifdef __CUDA_ARCH__
+      const int dself = WARP ? lattice_domain_warp(el, f.v, f.L) : lattice_domain(el, f.v, f.L);
+#else
       const int dself = lattice_domain(el, f.v, f.L);
+#endif
       if (dself != XG_IF || f.L == 0) {
         if (dself != XG_IF) {
           if (dself == dt) fill(Rp, el, f.v, (const double*)nullptr, dt, order, emit);

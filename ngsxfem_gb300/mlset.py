@@ -165,6 +165,28 @@ class DomainTypeArray:
         return DomainTypeArray(out)
 
 
+def _outer_normals(self, lsets):
+    """For each piece of self.Boundary() the outward unit normal
+    (python/mlset.py GetOuterNormals): Normalize(grad(l_i)) of the level set
+    whose entry is IF on the piece, negated where the region is POS in it."""
+    from .xfem import Normalize, grad
+    if self.codim > 0:
+        raise NotImplementedError("GetOuterNormals is available for codim = 0")
+    out = {}
+    bnd = self.Boundary()
+    for dtt in self.as_list:
+        for i, dt in enumerate(dtt):
+            piece = dtt[:i] + (IF,) + dtt[i + 1:]
+            if piece not in bnd:
+                continue
+            n = Normalize(grad(lsets[i]))
+            out[piece] = -1.0 * n if dt == POS else n
+    return out
+
+
+DomainTypeArray.GetOuterNormals = _outer_normals
+
+
 def TensorUnion(*args):
     """Union of regions of disjoint sets of level sets (the other level sets'
     entries ANY): the tuples grow to the total number of level sets."""

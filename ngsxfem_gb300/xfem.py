@@ -762,9 +762,17 @@ class _Integral:
             names = sorted(a[0] for a in scal)
             dots = [tuple(sorted((d[0][0], d[1][0]))) for d in mono.dots]
             kind, b = None, (0.0, 0.0, 0.0)
+            nrm_index = 0
             for d in mono.dots:
                 for v in d:
-                    if v[0] == "n" and nrm_gf is not None and v[1] != id(nrm_gf):
+                    if v[0] != "n" or nrm_gf is None:
+                        continue
+                    if isinstance(nrm_gf, (tuple, list)):
+                        ids = [id(g) for g in nrm_gf]
+                        if v[1] not in ids:
+                            raise NotImplementedError("the normal must be Normalize(grad(l)) of one of the level sets")
+                        nrm_index = ids.index(v[1])
+                    elif v[1] != id(nrm_gf):
                         raise NotImplementedError("the normal must be Normalize(grad(levelset)) of the cut's level set")
             tb = None
             if names == ["u", "v"] and not dots:
@@ -788,7 +796,7 @@ class _Integral:
                 raise NotImplementedError("integrand term outside the supported menu: %s" % (names + dots,))
             out.append(dict(kind=kind, domain=dom, order=-1 if m.order is None else m.order, hpow=mono.hpow,
                             coef=mono.c * m.scale, b=b, defined_on=m.definedonelements, tb=tb,
-                            tref=m.tref, time_order=m.time_order))
+                            tref=m.tref, time_order=m.time_order, normal_lset=nrm_index))
         return out
 
 
@@ -922,9 +930,67 @@ class BilinearForm:
         if not ls:
             return None
         for l in ls[1:]:
-            if l is not ls[0]:
-                raise NotImplementedError("all dCut integrals of one form must share the level set")
+            same = (l is ls[0]) or (isinstance(l, (tuple, list)) and isinstance(ls[0], (tuple, list)) and
+                                    len(l) == len(ls[0]) and all(a is b for a, b in zip(l, ls[0])))
+            if not same:
+                raise NotImplementedError("all dCut integrals of one form must share the level set(s)")
         return ls[0]
+
+    def _build_ml(self, lsets):
+        """Form on regions of several level sets (xg_mlset_form_create): the
+        region terms of the dCut integrals (domain types: a tuple, a list of
+        tuples or a DomainTypeArray), the normals Normalize(grad(l_i)) of the
+        level sets, ghost-penalty patch terms."""
+        from .mlset import DomainTypeArray
+        M = len(lsets)
+        region, patch = [], []
+        for it in self.integrals:
+            if it.measure.kind == "patch":
+                patch += it.terms(None)
+                continue
+            if it.measure.kind != "cut" or getattr(it.measure, "skeleton", False):
+                raise NotImplementedError("forms on several level sets take dCut region terms and dFacetPatch")
+            dom = it.measure.domain_type
+            if not isinstance(dom, DomainTypeArray):
+                dom = DomainTypeArray(list(dom) if isinstance(dom, list) else dom)
+            tup = np.ascontiguousarray(np.array(dom.as_list, dtype=np.int8).reshape(-1, M))
+            for t in it.terms(lsets):
+                if t["kind"] not in (TERM_MASS, TERM_LAPLACE, TERM_NGRADU_V, TERM_U_NGRADV, TERM_CONV) or \
+                        t.get("tb") is not None:
+                    raise NotImplementedError("region terms: mass, Laplace, Nitsche normal terms, convection")
+                t["tuples"] = tup
+                region.append(t)
+        arr = (_lib.MlTerm * len(region))()
+        self._keep = []
+        for k, t in enumerate(region):
+            arr[k].kind, arr[k].order, arr[k].hpow = t["kind"], t["order"], t["hpow"]
+            arr[k].normal_lset, arr[k].coef = t["normal_lset"], t["coef"]
+            for j in range(3):
+                arr[k].b[j] = t["b"][j]
+            arr[k].ntup = t["tuples"].shape[0]
+            arr[k].h_tuples = t["tuples"].ctypes.data
+            self._keep.append(t["tuples"])
+            d = t["defined_on"]
+            if d is not None:
+                self._keep.append(d)
+            arr[k].d_defined_on = d.words.data_ptr() if d is not None else None
+        parr = (_lib.Term * max(len(patch), 1))()
+        for k, t in enumerate(patch):
+            parr[k].kind, parr[k].domain, parr[k].order, parr[k].hpow = t["kind"], 0, t["order"], t["hpow"]
+            parr[k].coef = t["coef"]
+            d = t["defined_on"]
+            if d is not None:
+                self._keep.append(d)
+            parr[k].d_defined_on = d.words.data_ptr() if d is not None else None
+        h = ctypes.c_void_p()
+        _lib.call("xg_mlset_form_create", self.space.h, M, arr, len(region), parr, len(patch), self.precision,
+                  ctypes.byref(h))
+        self._form = h
+        self._terms = region + patch
+        self._ml = True
+        cap = np.zeros(2, dtype=np.int64)
+        _lib.call("xg_form_capacity", h, cap.ctypes.data_as(ctypes.c_void_p))
+        self._alloc(int(cap[0]), int(cap[1]))
 
     def _build_st(self):
         """Space-time form (xg_st_form_create): slab terms (time_order of the
@@ -969,6 +1035,8 @@ class BilinearForm:
         if isinstance(self.space, SpaceTimeFESpace):
             return self._build_st()
         lset = self._levelset()
+        if isinstance(lset, (tuple, list)):
+            return self._build_ml(lset)
         terms = []
         for it in self.integrals:
             terms += it.terms(lset)
@@ -1010,6 +1078,15 @@ class BilinearForm:
         if self._form is None:
             self._build()
         lset = self._levelset()
+        if isinstance(lset, (tuple, list)):
+            nv = lset[0].space.mesh.nv
+            vals = torch.stack([_lset_vec(g)[:nv] for g in lset]).contiguous()
+            _lib.call("xg_mlset_form_assemble", self._form, _vp(vals), ctypes.byref(self._csr), _stream())
+            torch.cuda.synchronize()
+            _lib.check(_lib.load().xg_form_check(self._form), "device (form on several level sets)")
+            nrows, nnz = (int(x) for x in self._counts.cpu().tolist())
+            self.mat = SparseMatrix(self.space.ndof, self._row_dof, self._rowptr, self._cols, self._vals, nrows, nnz)
+            return self
         if isinstance(self.space, SpaceTimeFESpace):
             # the space-time CutFEM step: marking, ghost facets and assembly in one call
             _lib.call("xg_st_cutfem_step", self._form, _vp(_lset_vec(lset)), ctypes.byref(self._csr), _stream())

@@ -29,6 +29,20 @@ class Term(ctypes.Structure):
     ]
 
 
+class MlTerm(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int),
+        ("order", ctypes.c_int),
+        ("hpow", ctypes.c_int),
+        ("normal_lset", ctypes.c_int),
+        ("coef", ctypes.c_double),
+        ("b", ctypes.c_double * 3),
+        ("ntup", ctypes.c_int),
+        ("dts", ctypes.c_void_p),
+        ("defined_on", ctypes.c_void_p),
+    ]
+
+
 class StTerm(ctypes.Structure):
     _fields_ = [
         ("kind", ctypes.c_int),
@@ -78,6 +92,8 @@ def lib():
         L.orc_integrate_subdiv.argtypes = [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                            ctypes.c_int, P, P]
         L.orc_subdiv_moments_p2.argtypes = [ctypes.c_int64, P, ctypes.c_int, P, ctypes.c_int]
+        L.orc_mlset_assemble.restype = P
+        L.orc_mlset_assemble.argtypes = [P, ctypes.c_int, P, P, ctypes.c_int, P, ctypes.c_int, ctypes.c_int]
         L.orc_space_destroy.argtypes = [P]
         L.orc_space_info.argtypes = [P, P]
         L.orc_space_el_dofs.argtypes = [P, P]
@@ -620,6 +636,41 @@ class Space:
         if st.value:
             raise RuntimeError("oracle subdivision rule error %d" % st.value)
         return v
+
+    def mlset_assemble(self, lsets, terms, patch_terms=(), nthreads=1):
+        """Terms on regions of several level sets (lsets: M x nv vertex values;
+        terms: dicts kind, tuples (ntup x M), coef, hpow, order, normal_lset, b,
+        defined_on) and patch terms; CSR triple over all dofs."""
+        L = np.ascontiguousarray(lsets, dtype=np.float64)
+        M = L.shape[0]
+        arr = (MlTerm * len(terms))()
+        keep = []
+        for i, t in enumerate(terms):
+            arr[i].kind, arr[i].order = t["kind"], t.get("order", -1)
+            arr[i].hpow, arr[i].normal_lset = t.get("hpow", 0), t.get("normal_lset", 0)
+            arr[i].coef = t.get("coef", 1.0)
+            for k in range(3):
+                arr[i].b[k] = t.get("b", (0.0, 0.0, 0.0))[k]
+            tup = np.ascontiguousarray(np.array(t["tuples"], dtype=np.int32).reshape(-1, M))
+            keep.append(tup)
+            arr[i].ntup, arr[i].dts = tup.shape[0], tup.ctypes.data
+            d = t.get("defined_on")
+            if d is not None:
+                d = np.ascontiguousarray(d, dtype=np.uint64)
+                keep.append(d)
+            arr[i].defined_on = d.ctypes.data if d is not None else None
+        parr, pkeep = self._terms(list(patch_terms))
+        c = lib().orc_mlset_assemble(self.h, M, _p(L), ctypes.cast(arr, ctypes.c_void_p), len(terms),
+                                     ctypes.cast(parr, ctypes.c_void_p), len(patch_terms), nthreads)
+        if not c:
+            raise RuntimeError("oracle mlset assembly error")
+        nnz = lib().orc_csr_nnz(c)
+        rowptr = np.zeros(self.ndof + 1, dtype=np.int64)
+        cols = np.zeros(nnz, dtype=np.int32)
+        vals = np.zeros(nnz)
+        lib().orc_csr_get(c, _p(rowptr), _p(cols), _p(vals))
+        lib().orc_csr_destroy(c)
+        return rowptr, cols, vals
 
     def facet_matrix(self, lset, terms, f, dn_fd=False):
         """Patch and skeleton terms of facet f ((2n)^2, row = test)."""

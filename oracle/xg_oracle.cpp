@@ -1752,6 +1752,103 @@ orc_csr* orc_assemble(const orc_space* s, const double* lset_vertex, const orc_t
   return orc_assemble_ex(s, lset_vertex, terms, nterms, nthreads, 0);
 }
 
+// Bilinear forms on regions of several level sets: SymbolicCutBFI with a
+// multi-level-set LevelsetIntegrationDomain (symboliccutbfi.cpp:76-486 with
+// CreateMultiLevelsetCutIntegrationRule, cutint/mlsetintegration.cpp:6-180):
+// per active element and term the rule of the term's region
+// (orc_mlset_cut_rule) and the term's integrand at its points; the patch
+// terms as in orc_assemble; summed into a CSR over all dofs.
+orc_csr* orc_mlset_assemble(const orc_space* s, int M, const double* lsets, const orc_mlterm* terms, int nterms,
+                            const orc_term* patch_terms, int npatch, int nthreads) {
+  const int ne = s->ne, n = s->nd, n2 = 2 * n, D = s->D;
+  const int64_t nf = s->nfacets, nv = s->nv;
+  std::vector<int32_t> el_slot(ne, -1), fa_slot(nf, -1);
+  int nact = 0;
+  for (int e = 0; e < ne; e++) {
+    bool act = false;
+    for (int t = 0; t < nterms; t++)
+      if (!terms[t].defined_on || test_bit(terms[t].defined_on, e)) act = true;
+    if (act) el_slot[e] = nact++;
+  }
+  int nfa = 0;
+  for (int64_t f = 0; f < nf && npatch > 0; f++) {
+    if (s->facet_els[2 * f + 1] < 0) continue;
+    bool act = false;
+    for (int t = 0; t < npatch; t++)
+      if (!patch_terms[t].defined_on || test_bit(patch_terms[t].defined_on, f)) act = true;
+    if (act) fa_slot[f] = nfa++;
+  }
+  std::vector<int32_t> el_list(nact), fa_list(nfa);
+  for (int e = 0; e < ne; e++) if (el_slot[e] >= 0) el_list[el_slot[e]] = e;
+  for (int64_t f = 0; f < nf; f++) if (fa_slot[f] >= 0) fa_list[fa_slot[f]] = (int32_t)f;
+  std::vector<double> elm((size_t)nact * n * n, 0.0), fam((size_t)nfa * n2 * n2);
+  std::atomic<int> err(0);
+  parallel_for(nact, nthreads, [&](int64_t b, int64_t en) {
+    std::vector<double> pts(3 * 20000), wts(20000);
+    double elc[12], lv[8 * 4], phi[20], dphi[20][3], gp[20][3];
+    for (int64_t i = b; i < en; i++) {
+      const int e = el_list[i];
+      Geo g;
+      element_geo(s, e, g, nullptr, nullptr);
+      for (int v = 0; v <= D; v++) {
+        const int vid = s->elv[(size_t)e * (D + 1) + v];
+        for (int c = 0; c < D; c++) elc[v * D + c] = s->coords[(size_t)vid * D + c];
+        for (int m = 0; m < M; m++) lv[m * (D + 1) + v] = lsets[(size_t)m * nv + vid];
+      }
+      const int* gv = &s->elv[(size_t)e * (D + 1)];
+      const double meas = std::fabs(g.det);
+      double* A = &elm[(size_t)i * n * n];
+      for (int t = 0; t < nterms; t++) {
+        const orc_mlterm& T = terms[t];
+        if (T.defined_on && !test_bit(T.defined_on, e)) continue;
+        const int order = T.order >= 0 ? T.order : default_order(T.kind, s->k);
+        const int np = orc_mlset_cut_rule(D, elc, M, lv, T.ntup, T.dts, order, pts.data(), wts.data(), 20000);
+        if (np < -1) { err = np; continue; }
+        if (np <= 0) continue;
+        double c = T.coef;
+        if (T.hpow != 0) c *= std::pow(meas, (double)T.hpow / D);
+        // unit normal of the P1 level set T.normal_lset
+        double nrm[3] = {0, 0, 0};
+        if (T.kind == ORC_TERM_NGRADU_V || T.kind == ORC_TERM_U_NGRADV) {
+          double gr[3] = {0, 0, 0}, gl[3];
+          const double* l = &lv[T.normal_lset * (D + 1)];
+          for (int k = 0; k < D; k++) gr[k] = l[k] - l[D];
+          phys_grad(g, gr, gl);
+          const double nn = l2norm3(gl);
+          for (int k = 0; k < 3; k++) nrm[k] = gl[k] / nn;
+        }
+        for (int q = 0; q < np; q++) {
+          basis(D, s->k, gv, &pts[3 * q], phi, dphi);
+          for (int a = 0; a < n; a++) phys_grad(g, dphi[a], gp[a]);
+          const double W = wts[q] * meas * c;
+          for (int a = 0; a < n; a++)      // test
+            for (int bb = 0; bb < n; bb++) {  // trial
+              double v;
+              switch (T.kind) {
+                case ORC_TERM_MASS: v = phi[a] * phi[bb]; break;
+                case ORC_TERM_LAPLACE: v = gp[a][0] * gp[bb][0] + gp[a][1] * gp[bb][1] + gp[a][2] * gp[bb][2]; break;
+                case ORC_TERM_NGRADU_V: v = (nrm[0] * gp[bb][0] + nrm[1] * gp[bb][1] + nrm[2] * gp[bb][2]) * phi[a]; break;
+                case ORC_TERM_U_NGRADV: v = phi[bb] * (nrm[0] * gp[a][0] + nrm[1] * gp[a][1] + nrm[2] * gp[a][2]); break;
+                case ORC_TERM_CONV: v = (T.b[0] * gp[bb][0] + T.b[1] * gp[bb][1] + T.b[2] * gp[bb][2]) * phi[a]; break;
+                default: v = 0.0;
+              }
+              A[a * n + bb] += W * v;
+            }
+        }
+      }
+    }
+  });
+  parallel_for(nfa, nthreads, [&](int64_t b, int64_t en) {
+    for (int64_t i = b; i < en; i++) {
+      const int r = patch_matrix(s, patch_terms, npatch, fa_list[i], &fam[(size_t)i * n2 * n2]);
+      if (r) err = r;
+    }
+  });
+  if (err.load()) return nullptr;
+  return gather_csr(s->ndof, n, s->el_dofs, s->dof_adj_ptr, s->dof_adj, s->D + 1, s->el_facets, s->facet_els,
+                    el_slot, elm, fa_slot, fam, nthreads);
+}
+
 orc_csr* orc_assemble_ex(const orc_space* s, const double* lset_vertex, const orc_term* terms, int nterms,
                          int nthreads, int dn_fd) {
   const int ne = s->ne, n = s->nd, n2 = 2 * n;

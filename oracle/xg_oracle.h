@@ -133,6 +133,22 @@ typedef struct orc_csr orc_csr;
  * summed into a CSR over all dofs (rows of untouched dofs are empty). */
 orc_csr* orc_assemble(const orc_space*, const double* lset_vertex, const orc_term* terms, int nterms,
                       int nthreads);
+/* A term on a region of several level sets: the integrand of kind (MASS,
+ * LAPLACE, NGRADU_V, U_NGRADV, CONV) over the union of ntup domain tuples
+ * dts [ntup][M]; the normal of NGRADU_V / U_NGRADV is grad(l)/|grad(l)| of the
+ * P1 level set normal_lset. */
+typedef struct {
+  int kind, order, hpow, normal_lset;
+  double coef;
+  double b[3];
+  int ntup;
+  const int* dts;
+  const uint64_t* defined_on; /* element bits; NULL = all */
+} orc_mlterm;
+/* Assembly of terms on regions of M level sets (lsets [M][nv], vertex values)
+ * plus facet-patch terms (GHOST_MASS with their facet sets). */
+orc_csr* orc_mlset_assemble(const orc_space* s, int M, const double* lsets, const orc_mlterm* terms, int nterms,
+                            const orc_term* patch_terms, int npatch, int nthreads);
 /* orc_assemble with the normal-derivative mode of orc_facet_matrix. */
 orc_csr* orc_assemble_ex(const orc_space*, const double* lset_vertex, const orc_term* terms, int nterms,
                          int nthreads, int dn_fd);

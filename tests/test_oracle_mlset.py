@@ -214,3 +214,37 @@ def test_3d_line_lengths(orc):
         for fs, tuples, key in lines_cases():
             L = np.array([orc.interpolate_p1_perturb(f) for f in fs(*m.coords.T)])
             assert abs(integ(orc, m, L, DomainTypeArray(tuples)) - ref[key]) < ref["tol"], (dims, key)
+
+
+@pytest.mark.parametrize("k", [1, 2, 3])
+def test_mlset_forms_known_answers(orc, k):
+    """orc_mlset_assemble on the unit square as the region of four lines:
+    1^T M 1 = 1 (area), the boundary pieces' mass sums to the perimeter 4,
+    the stiffness matrix annihilates constants and x^T K x = |region|."""
+    m = MakeStructured2DMesh(7, 7, -0.2, 1.2, -0.2, 1.2)
+    X, Y = m.coords.T
+    L = np.stack([orc.interpolate_p1_perturb(v) for v in (-Y, X - 1, Y - 1, -X)])
+    sp = orc.Space(m, k)
+    NEG, IF = orc.NEG, orc.IF
+    sq = [(NEG,) * 4]
+    bnd = [(IF, NEG, NEG, NEG), (NEG, IF, NEG, NEG), (NEG, NEG, IF, NEG), (NEG, NEG, NEG, IF)]
+    one = np.zeros(sp.ndof)
+    xs = np.zeros(sp.ndof)
+    el = sp.el_dofs()
+    for e in range(m.ne):
+        one[el[e][:3]] = 1.0
+        xs[el[e][:3]] = m.coords[m.elements[e], 0]
+
+    def dense(csr):
+        rp, cols, vals = csr
+        A = np.zeros((sp.ndof, sp.ndof))
+        for r in range(sp.ndof):
+            A[r, cols[rp[r]:rp[r + 1]]] += vals[rp[r]:rp[r + 1]]
+        return A
+    Mm = dense(sp.mlset_assemble(L, [dict(kind=orc.TERM_MASS, tuples=sq)]))
+    assert abs(one @ Mm @ one - 1.0) < 1e-13
+    Mb = dense(sp.mlset_assemble(L, [dict(kind=orc.TERM_MASS, tuples=bnd)]))
+    assert abs(one @ Mb @ one - 4.0) < 1e-13
+    K = dense(sp.mlset_assemble(L, [dict(kind=orc.TERM_LAPLACE, tuples=sq)]))
+    assert np.abs(K @ one).max() < 1e-12
+    assert abs(xs @ K @ xs - 1.0) < 1e-13
