@@ -327,6 +327,27 @@ int xg_form_destroy(xg_form* form);
 /* Replace the element/facet set of term t (device bitset, NULL = all). */
 int xg_form_set_defined_on(xg_form* form, int32_t t, const uint64_t* d_defined_on);
 
+/* Boundary terms (dCut(lset, dt, vb=BND) in a BilinearForm): c * h^hpow * u * v
+ * over the domain part (XG_NEG / XG_POS; XG_IF in 2D: the cut points) of the
+ * BND elements in d_defined_on (bits over the BND elements, which are the
+ * boundary facets in facet order; NULL = all), with the straight cut of the
+ * P1 level set on the boundary facet and h of the owning element.  The
+ * reference's SymbolicCutBFI on boundary elements
+ * (xfem/symboliccutbfi.cpp:76-486 with vb == BND, the rule of
+ * cutint/straightcutrule.cpp:582-677).  Every owner of a BND element in a
+ * term's set joins the active elements; its matrix is the sum of its volume
+ * and boundary terms.  Spatial forms on simplex meshes; order -1 = 2k. */
+typedef struct {
+  int32_t kind;   /* XG_TERM_MASS */
+  int32_t domain; /* XG_NEG, XG_POS, XG_IF (2D) */
+  int32_t order;
+  int32_t hpow;
+  double coef;
+  const uint64_t* d_defined_on;
+} xg_bterm;
+/* Replace the form's boundary terms (at most 8; nterms 0 removes them). */
+int xg_form_set_bnd_terms(xg_form* form, const xg_bterm* terms, int32_t nterms);
+
 /* Output matrix in compressed-row form over the form's active dofs (the dofs
  * of elements and facet patches that carry a term, numbered ascending as
  * ngcomp::CompressedFESpace / Restrict() does):

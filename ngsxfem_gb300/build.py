@@ -37,6 +37,7 @@ UNITS = [
     ("xg_skel.cu", []),
     ("xg_subdiv.cu", []),
     ("xg_mlform.cu", []),
+    ("xg_bform.cu", []),
 ]
 
 

@@ -2542,6 +2542,10 @@ struct xg_form {
   int8_t* d_ml_tuples = nullptr;
   std::vector<xg_term> terms;
   std::vector<int> term_slot;  // group index (volume) or patch index
+  // boundary terms (xg_form_set_bnd_terms) and the elements owning BND elements
+  BndDesc bnd = {};
+  int n_own = 0;
+  int32_t* d_own = nullptr;  // [n_own] owners, [n_own + 1] pointers, [nbnd] BND elements
   FormDesc desc;
   int needs_mask = 0;  // domains needing decompositions on cut elements
   int el_sym = 0;      // every volume group symmetric: packed element matrices
@@ -2647,7 +2651,7 @@ int form_free(xg_form* f) {
                   f->d_elmat, f->d_famat, f->d_err, f->d_dom, f->d_ratio, f->d_bits, f->d_fbits, f->d_fbits_sk,
                   f->d_mtab_i, f->d_mtab_c, f->d_mu, f->d_mhat, f->d_cutlist, f->d_dof_flag,
                   f->d_el_rowslot, f->d_pos_rows, f->d_nbpos, f->d_cand_fs, f->d_act_slot, f->d_vcols, f->d_vvals,
-                  f->d_bsum_rows, f->d_ml_terms, f->d_ml_tuples};
+                  f->d_bsum_rows, f->d_ml_terms, f->d_ml_tuples, f->d_own};
   for (void* p : ptrs) cudaFree(p);
   delete f;
   return XG_OK;
@@ -3849,6 +3853,64 @@ int xg_form_set_defined_on(xg_form* f, int32_t t, const uint64_t* d_defined_on) 
   return st ? st : upload_tables(f);
 }
 
+int xg_form_set_bnd_terms(xg_form* f, const xg_bterm* terms, int32_t nterms) {
+  if (!f || nterms < 0 || (nterms > 0 && !terms)) return XG_ERR_ARG;
+  if (nterms > kMaxBnd) {
+    set_last_error("xg_form_set_bnd_terms: at most 8 boundary terms");
+    return XG_ERR_CAPACITY;
+  }
+  xg_mesh* m = f->mesh;
+  if (nterms > 0 && (!f->rows || f->ml || m->tensor)) {
+    set_last_error("xg_form_set_bnd_terms: boundary terms need a spatial form on a simplex mesh");
+    return XG_ERR_UNSUPPORTED;
+  }
+  BndDesc d = {};
+  for (int t = 0; t < nterms; t++) {
+    const xg_bterm& T = terms[t];
+    if (T.kind != XG_TERM_MASS || (T.domain != XG_NEG && T.domain != XG_POS && T.domain != XG_IF) ||
+        T.order > kMaxOrder) {
+      set_last_error("xg_form_set_bnd_terms: mass terms on NEG, POS or IF of order <= 8");
+      return XG_ERR_ARG;
+    }
+    if (T.domain == XG_IF && m->dim == 3) {
+      set_last_error("xg_form_set_bnd_terms: IF on boundary triangles (3D) is not supported");
+      return XG_ERR_UNSUPPORTED;
+    }
+    BndTermDev& B = d.t[d.n++];
+    B.domain = T.domain;
+    B.order = T.order >= 0 ? T.order : 2 * f->space->order;
+    B.hpow = T.hpow;
+    B.coef = T.coef;
+    B.defined_on = T.d_defined_on;
+  }
+  if (nterms > 0 && !f->d_own && m->nbnd > 0) {
+    // owners ascending, their BND elements ascending (the boundary facets in
+    // facet order; the owner is the facet's first element)
+    const int64_t nb = m->nbnd;
+    std::vector<int32_t> cnt(m->ne, 0);
+    for (int64_t b = 0; b < nb; b++) cnt[m->h_facet_els[2 * (int64_t)m->h_bnd_facets[b]]]++;
+    std::vector<int32_t> own, ptr(1, 0), pos(m->ne, -1);
+    for (int e = 0; e < m->ne; e++)
+      if (cnt[e]) {
+        pos[e] = ptr.back();
+        own.push_back(e);
+        ptr.push_back(ptr.back() + cnt[e]);
+      }
+    std::vector<int32_t> lst(nb);
+    for (int64_t b = 0; b < nb; b++) lst[pos[m->h_facet_els[2 * (int64_t)m->h_bnd_facets[b]]]++] = (int32_t)b;
+    const int no = (int)own.size();
+    std::vector<int32_t> h(own);
+    h.insert(h.end(), ptr.begin(), ptr.end());
+    h.insert(h.end(), lst.begin(), lst.end());
+    XG_CUDA(cudaSetDevice(m->device));
+    XG_CUDA(cudaMalloc((void**)&f->d_own, h.size() * sizeof(int32_t)));
+    XG_CUDA(cudaMemcpy(f->d_own, h.data(), h.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    f->n_own = no;
+  }
+  f->bnd = d;
+  return XG_OK;
+}
+
 int xg_form_capacity(const xg_form* f, int64_t* o) {
   if (!f || !o) return XG_ERR_ARG;
   // the largest pattern any level set can produce on this mesh (every element
@@ -3917,6 +3979,33 @@ int launch_skel(xg_form* f, const double* d_lset, cudaStream_t s) {
   return skel_launch(A, f->desc, s);
 }
 
+// boundary terms: the owners of BND elements and their element rows
+BndFormLaunch bnd_args(xg_form* f, const double* d_lset) {
+  xg_mesh* m = f->mesh;
+  BndFormLaunch L;
+  L.dim = m->dim;
+  L.order = f->space->order;
+  L.ne = m->ne;
+  L.nv = m->nv;
+  L.elv = m->d_elv;
+  L.xyz = m->d_xyz;
+  L.lset = d_lset;
+  L.nbnd = m->nbnd;
+  L.bnd_v = m->d_bnd_v;
+  L.n_own = f->n_own;
+  L.own_el = f->d_own;
+  L.own_ptr = f->d_own + f->n_own;
+  L.own_bnd = f->d_own + 2 * f->n_own + 1;
+  L.d = f->bnd;
+  L.act_un = f->d_act_un;
+  L.act_cut = f->d_act_cut;
+  L.rowslot = f->d_el_rowslot;
+  L.elmat = f->d_elmat;
+  L.fp64 = f->precision == XG_PREC_FP64 ? 1 : 0;
+  L.err = f->d_err;
+  return L;
+}
+
 // the element and patch kernels of one step (spatial forms: the element rows
 // at their static slots and the patch matrices by facet slot; the patch
 // matrices are left out when the form's patches run in a batched launch)
@@ -3925,6 +4014,7 @@ int rows_front(xg_form* f, const double* d_lset, const uint8_t* d_dom, cudaStrea
   int st;
   if ((st = fp64 ? dispatch_volume<double>(f, d_lset, d_dom, s) : dispatch_volume<float>(f, d_lset, d_dom, s)))
     return st;
+  if (f->bnd.n > 0 && (st = bnd_elmat_launch(bnd_args(f, d_lset), s))) return st;
   if (f->has_patch && f->desc.npatch > 0 && (st = fp64 ? dispatch_patch<double>(f, s) : dispatch_patch<float>(f, s)))
     return st;
   if (f->desc.nskel > 0 && (st = launch_skel(f, d_lset, s))) return st;
@@ -3960,6 +4050,7 @@ int assemble_front(xg_form* f, const double* d_lset, const uint8_t* d_dom, xg_cs
   // 1. active elements / facets and their lists
   k_active_elements<<<(unsigned)((f->nw32_el * 32 + 255) / 256), 256, 0, s>>>(m->ne, d_dom, f->desc, f->d_act_un,
                                                                               f->d_act_cut, f->nw32_el);
+  if (f->bnd.n > 0 && (st = bnd_active_launch(bnd_args(f, d_lset), s))) return st;
   if ((st = compact(f, f->d_act_un, f->nw32_el, f->d_l_un, f->d_el_slot, f->d_counts + 0, s))) return st;
   if ((st = compact(f, f->d_act_cut, f->nw32_el, f->d_l_cut, f->d_el_slot, f->d_counts + 1, s, f->d_counts + 0)))
     return st;

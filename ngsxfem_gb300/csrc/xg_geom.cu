@@ -34,6 +34,7 @@ int ensure_device_rules() {
   if (!st) st = upload_rules_skel();
   if (!st) st = upload_rules_subdiv();
   if (!st) st = upload_rules_mlform();
+  if (!st) st = upload_rules_bform();
   if (st) return st;
   done.push_back(dev);
   return XG_OK;

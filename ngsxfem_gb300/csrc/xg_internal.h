@@ -223,6 +223,41 @@ struct SkelLaunch {
   int* err;
 };
 int skel_launch(const SkelLaunch& a, const FormDesc& form, cudaStream_t s);
+
+// boundary terms of bilinear forms (xg_form_set_bnd_terms; xg_bform.cu)
+constexpr int kMaxBnd = 8;
+struct BndTermDev {
+  int domain, order, hpow;
+  double coef;
+  const uint64_t* defined_on;  // BND element bits; NULL = all
+};
+struct BndDesc {
+  int n;
+  BndTermDev t[kMaxBnd];
+};
+struct BndFormLaunch {
+  int dim, order;
+  int ne, nv;
+  const int32_t* elv;    // [D+1][ne]
+  const double* xyz;     // [D][nv]
+  const double* lset;    // P1 vertex values
+  int64_t nbnd;
+  const int32_t* bnd_v;  // [D][nbnd]
+  int n_own;             // elements owning a BND element, ascending
+  const int32_t* own_el;
+  const int32_t* own_ptr;  // [n_own + 1]
+  const int32_t* own_bnd;  // their BND elements, ascending per owner
+  BndDesc d;
+  uint32_t* act_un;
+  const uint32_t* act_cut;
+  const int32_t* rowslot;  // [ne][nd] element row slots
+  void* elmat;
+  int fp64;
+  int* err;
+};
+int bnd_active_launch(const BndFormLaunch& a, cudaStream_t s);
+int bnd_elmat_launch(const BndFormLaunch& a, cudaStream_t s);
+int upload_rules_bform();
 int quad_rule_capacity(int dim, int dt, int order);
 int quad_cut_rules(xg_mesh* m, const double* d_lset, const int32_t* d_elems, int32_t n, int dt, int order, int pol,
                    int32_t max_pts, int32_t* d_counts, double* d_pts, double* d_wts, void* stream);

@@ -8,10 +8,9 @@
 //                           <= 4 in reference coordinates) of a P2 level set
 //                           given by its values at the vertices and edge
 //                           midpoints of the reference tetrahedron
-// One warp per element: every lane walks the element's refinement tree with
-// the lattice checks split over the lanes, and the lanes share out the rule
-// points (Integrate) or the moments; the sums run in a fixed order (lanes,
-// warps of a block, blocks), so repeated calls give the same bits.
+// One thread per element walks the element's refinement tree; the integral
+// is summed per thread, per block in a fixed tree and over the blocks in
+// order, so repeated calls give the same bits.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -41,24 +40,18 @@ __device__ __forceinline__ double sd_ipow(double x, int e) {
   return r;
 }
 
-// one warp per element: every lane walks the element's refinement tree (the
-// lattice checks split over the lanes) and sees every rule point; lane l sums
-// the points q with q mod 32 = l, the lanes' sums meet in a fixed shuffle tree
 template <int D, int K>
-__global__ void __launch_bounds__(kSdThreads) k_subdiv_integrate(int ne, int nv, const int32_t* __restrict__ elv,
-                                                                  const double* __restrict__ xyz,
-                                                                  const int32_t* __restrict__ el_dofs,
-                                                                  const double* __restrict__ coefs, int dt, int order,
-                                                                  int levels, int ex, int ey, int ez,
-                                                                  const uint64_t* __restrict__ defined_on,
-                                                                  double* __restrict__ block_sums, int* err) {
-  __shared__ double red[kSdThreads / 32];
+__global__ void __launch_bounds__(kSdThreads, 3) k_subdiv_integrate(int ne, int nv, const int32_t* __restrict__ elv,
+                                                                     const double* __restrict__ xyz,
+                                                                     const int32_t* __restrict__ el_dofs,
+                                                                     const double* __restrict__ coefs, int dt,
+                                                                     int order, int levels, int ex, int ey, int ez,
+                                                                     const uint64_t* __restrict__ defined_on,
+                                                                     double* __restrict__ block_sums, int* err) {
+  __shared__ double red[kSdThreads];
   constexpr int N = ndof_el(D, K);
-  const int lane = threadIdx.x & 31;
-  const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   double acc = 0.0;
-  for (int64_t e = warp0; e < ne; e += nwarps) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
     if (defined_on && !sd_bit(defined_on, e)) continue;
     sd::Elem<D, K> el;
     int gv[4] = {0, 0, 0, 0};
@@ -75,22 +68,19 @@ __global__ void __launch_bounds__(kSdThreads) k_subdiv_integrate(int ne, int nv,
       el.coef[i] = coefs[el_dofs[(int64_t)i * ne + e]];
       el.desc[i] = fn_desc<D, K>(i, gv);
     }
-    int q = 0;
     auto emit = [&](const double* x, double w) {
-      if ((q & 31) == lane) acc += w * sd_ipow(x[0], ex) * sd_ipow(x[1], ey) * (D == 3 ? sd_ipow(x[2], ez) : 1.0);
-      q++;
+      acc += w * sd_ipow(x[0], ex) * sd_ipow(x[1], ey) * (D == 3 ? sd_ipow(x[2], ez) : 1.0);
     };
-    const int st = sd::element_rule<D, K, decltype(emit), true>(&g_sd_rules, el, dt, order, levels, emit);
-    if (st && lane == 0) set_err(err, st);
+    const int st = sd::element_rule<D, K>(&g_sd_rules, el, dt, order, levels, emit);
+    if (st) set_err(err, st);
   }
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-  if (lane == 0) red[threadIdx.x >> 5] = acc;
+  red[threadIdx.x] = acc;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int w = 0; w < kSdThreads / 32; w++) s += red[w];
-    block_sums[blockIdx.x] = s;
+  for (int s = kSdThreads / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
   }
+  if (threadIdx.x == 0) block_sums[blockIdx.x] = red[0];
 }
 
 __global__ void k_sd_sum(const double* v, int n, double* out) {
@@ -102,45 +92,21 @@ __global__ void k_sd_sum(const double* v, int n, double* out) {
 }
 
 // the 35 NEG moments x^a y^b z^c (a + b + c <= 4, by degree, then a, then b
-// descending) of each reference tetrahedron, one warp per element: every lane
-// walks the element's
-// refinement tree (the lattice checks split over the lanes) and sees every
-// rule point; lane l accumulates moments l and l + 32, so no lane holds more
-// than two sums and the result needs no reduction across lanes
-__global__ void __launch_bounds__(kSdThreads) k_subdiv_moments_warp(int64_t n, const double* __restrict__ vals10,
-                                                                     int levels, double* __restrict__ out35,
-                                                                     const int32_t* __restrict__ list,
-                                                                     const int32_t* __restrict__ count, int* err) {
+// descending) of each reference tetrahedron, thread per element (a warp per
+// element, with the lattice checks split over its lanes and every lane
+// walking the tree, measured about half as fast: the tree walk and the rule
+// points, not the checks, are the work)
+__global__ void __launch_bounds__(kSdThreads, 3) k_subdiv_moments(int64_t n, const double* __restrict__ vals10,
+                                                                  int levels, double* __restrict__ out35,
+                                                                  const int32_t* __restrict__ list,
+                                                                  const int32_t* __restrict__ count, int* err) {
   const int E[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
-  const int lane = threadIdx.x & 31;
-  // exponents of moments lane and lane + 32 (by degree, then a, then b descending)
-  int ea[2] = {0, 0}, eb[2] = {0, 0}, ec[2] = {0, 0};
-  {
-    int k = 0;
-    for (int t = 0; t <= 4; t++)
-      for (int a = t; a >= 0; a--)
-        for (int b = t - a; b >= 0; b--) {
-          if (k == lane) {
-            ea[0] = a;
-            eb[0] = b;
-            ec[0] = t - a - b;
-          }
-          if (k == lane + 32) {
-            ea[1] = a;
-            eb[1] = b;
-            ec[1] = t - a - b;
-          }
-          k++;
-        }
-  }
-  const bool two = lane + 32 < 35;
   const int64_t items = list ? (int64_t)*count : n;
-  const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t it = warp0; it < items; it += nwarps) {
+  for (int64_t it = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; it < items;
+       it += (int64_t)gridDim.x * blockDim.x) {
     const int64_t e = list ? (int64_t)list[it] : it;
     if (e < 0 || e >= n) {
-      if (lane == 0) set_err(err, XG_ERR_ARG);
+      set_err(err, XG_ERR_ARG);
       continue;
     }
     sd::Elem<3, 2> el;
@@ -150,18 +116,24 @@ __global__ void __launch_bounds__(kSdThreads) k_subdiv_moments_warp(int64_t n, c
       for (int c = 0; c < 3; c++) el.F[r][c] = r == c ? 1.0 : 0.0;
     }
     const double* p = vals10 + e * 10;
+    // P2 nodal values -> the H1 coefficients: vertex values, 4 p(mid) - 2 (p_a + p_b)
     for (int i = 0; i < 4; i++) el.coef[i] = p[i];
     for (int j = 0; j < 6; j++) el.coef[4 + j] = 4.0 * p[4 + j] - 2.0 * (p[E[j][0]] + p[E[j][1]]);
     for (int i = 0; i < 10; i++) el.desc[i] = fn_desc<3, 2>(i, gv);
-    double m0 = 0.0, m1 = 0.0;
+    double m[35];
+    for (int k = 0; k < 35; k++) m[k] = 0.0;
     auto emit = [&](const double* x, double w) {
-      m0 += w * sd_ipow(x[0], ea[0]) * sd_ipow(x[1], eb[0]) * sd_ipow(x[2], ec[0]);
-      m1 += w * sd_ipow(x[0], ea[1]) * sd_ipow(x[1], eb[1]) * sd_ipow(x[2], ec[1]);
+      const double px[5] = {1, x[0], x[0] * x[0], x[0] * x[0] * x[0], x[0] * x[0] * x[0] * x[0]};
+      const double py[5] = {1, x[1], x[1] * x[1], x[1] * x[1] * x[1], x[1] * x[1] * x[1] * x[1]};
+      const double pz[5] = {1, x[2], x[2] * x[2], x[2] * x[2] * x[2], x[2] * x[2] * x[2] * x[2]};
+      int k = 0;
+      for (int t = 0; t <= 4; t++)
+        for (int a = t; a >= 0; a--)
+          for (int b = t - a; b >= 0; b--) m[k++] += w * px[a] * py[b] * pz[t - a - b];
     };
-    const int st = sd::element_rule<3, 2, decltype(emit), true>(&g_sd_rules, el, XG_NEG, 4, levels, emit);
-    if (st && lane == 0) set_err(err, st);
-    out35[e * 35 + lane] = m0;
-    if (two) out35[e * 35 + lane + 32] = m1;
+    const int st = sd::element_rule<3, 2>(&g_sd_rules, el, XG_NEG, 4, levels, emit);
+    if (st) set_err(err, st);
+    for (int k = 0; k < 35; k++) out35[e * 35 + k] = m[k];
   }
 }
 
@@ -177,10 +149,9 @@ void launch_int(xg_space* sp, const double* coefs, int dt, int order, int levels
 
 int subdiv_moments_launch(const double* d_vals10, int64_t n, int levels, double* d_out35, const int32_t* d_list,
                           const int32_t* d_count, int* d_err, cudaStream_t s) {
-  // one warp per element
-  const int64_t blocks = (n * 32 + kSdThreads - 1) / kSdThreads;
-  k_subdiv_moments_warp<<<(unsigned)(blocks < kSdBlocks * 4 ? (blocks > 0 ? blocks : 1) : kSdBlocks * 4), kSdThreads,
-                          0, s>>>(n, d_vals10, levels, d_out35, d_list, d_count, d_err);
+  const int64_t blocks = (n + kSdThreads - 1) / kSdThreads;
+  k_subdiv_moments<<<(unsigned)(blocks < kSdBlocks ? (blocks > 0 ? blocks : 1) : kSdBlocks), kSdThreads, 0, s>>>(
+      n, d_vals10, levels, d_out35, d_list, d_count, d_err);
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? XG_OK : cuda_fail(e, "k_subdiv_moments_tet");
 }

@@ -1037,10 +1037,13 @@ class BilinearForm:
         lset = self._levelset()
         if isinstance(lset, (tuple, list)):
             return self._build_ml(lset)
-        terms = []
+        terms, bterms = [], []
         for it in self.integrals:
-            terms += it.terms(lset)
-        arr = (_lib.Term * len(terms))()
+            if it.measure.kind == "cut" and getattr(it.measure, "vb", VOL) == BND:
+                bterms += self._bnd_terms(it, lset)
+            else:
+                terms += it.terms(lset)
+        arr = (_lib.Term * max(len(terms), 1))()
         self._keep = []
         for k, t in enumerate(terms):
             arr[k].kind, arr[k].domain, arr[k].order, arr[k].hpow = t["kind"], t["domain"], t["order"], t["hpow"]
@@ -1057,9 +1060,39 @@ class BilinearForm:
         _lib.call("xg_form_create", self.space.h, arr, len(terms), self.precision, ctypes.byref(h))
         self._form = h
         self._terms = terms
+        if bterms:
+            barr = (_lib.BTerm * len(bterms))()
+            for k, t in enumerate(bterms):
+                barr[k].kind, barr[k].domain, barr[k].order, barr[k].hpow = t["kind"], t["domain"], t["order"], t["hpow"]
+                barr[k].coef = t["coef"]
+                d = t["defined_on"]
+                if d is not None:
+                    self._keep.append(d)
+                barr[k].d_defined_on = d.words.data_ptr() if d is not None else None
+            _lib.call("xg_form_set_bnd_terms", h, barr, len(bterms))
+            self._bterms = bterms
         cap = np.zeros(2, dtype=np.int64)
         _lib.call("xg_form_capacity", h, cap.ctypes.data_as(ctypes.c_void_p))
         self._alloc(int(cap[0]), int(cap[1]))
+
+    def _bnd_terms(self, it, lset):
+        """Boundary terms c * u * v * dCut(lset, dt, vb=BND[, definedon=
+        mesh.Boundaries(..)][, definedonelements=BND BitArray]) (the
+        reference's SymbolicCutBFI on boundary elements): mass terms only, the
+        two restrictions intersected."""
+        m = it.measure
+        if getattr(m, "subdivlvl", 0):
+            raise NotImplementedError("boundary terms take the straight cut of a P1 level set")
+        mesh = self.space.mesh
+        defined = _bnd_restriction(mesh, m.definedonelements, getattr(m, "definedon", None))
+        out = []
+        for mono in it.expr.monos:
+            if mono.vec is not None or mono.dots or sorted(a[0] for a in mono.scal) != ["u", "v"] or \
+                    any(a[1] for a in mono.scal):
+                raise NotImplementedError("boundary terms of bilinear forms: c * u * v (times powers of h)")
+            out.append(dict(kind=TERM_MASS, domain=m.domain_type, order=-1 if m.order is None else m.order,
+                            hpow=mono.hpow, coef=mono.c * m.scale, defined_on=defined))
+        return out
 
     def _alloc(self, cap_rows, cap_nnz):
         dev = _dev()

@@ -29,6 +29,17 @@ class Term(ctypes.Structure):
     ]
 
 
+class BTerm(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int),
+        ("domain", ctypes.c_int),
+        ("order", ctypes.c_int),
+        ("hpow", ctypes.c_int),
+        ("coef", ctypes.c_double),
+        ("defined_on", ctypes.c_void_p),
+    ]
+
+
 class MlTerm(ctypes.Structure):
     _fields_ = [
         ("kind", ctypes.c_int),
@@ -92,6 +103,8 @@ def lib():
         L.orc_integrate_subdiv.argtypes = [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                            ctypes.c_int, P, P]
         L.orc_subdiv_moments_p2.argtypes = [ctypes.c_int64, P, ctypes.c_int, P, ctypes.c_int]
+        L.orc_assemble_bnd.restype = P
+        L.orc_assemble_bnd.argtypes = [P, P, P, ctypes.c_int, P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.orc_mlset_assemble.restype = P
         L.orc_mlset_assemble.argtypes = [P, ctypes.c_int, P, P, ctypes.c_int, P, ctypes.c_int, ctypes.c_int]
         L.orc_space_destroy.argtypes = [P]
@@ -684,12 +697,26 @@ class Space:
             raise RuntimeError("oracle facet matrix error %d" % r)
         return out
 
-    def assemble(self, lset, terms, nthreads=1, dn_fd=False):
-        """Returns scipy-free CSR triple (rowptr int64, cols int32, vals float64) over all dofs."""
+    def assemble(self, lset, terms, nthreads=1, dn_fd=False, bterms=()):
+        """Returns scipy-free CSR triple (rowptr int64, cols int32, vals float64) over all dofs.
+        bterms: boundary terms (dicts: domain, coef, order, hpow, defined_on
+        over the BND elements), mass terms of orc_assemble_bnd."""
         arr, keep = self._terms(terms)
         l = np.ascontiguousarray(lset, dtype=np.float64)
-        c = lib().orc_assemble_ex(self.h, _p(l), ctypes.cast(arr, ctypes.c_void_p), len(terms), nthreads,
-                                  int(dn_fd))
+        barr = (BTerm * max(len(bterms), 1))()
+        for i, t in enumerate(bterms):
+            barr[i].kind = TERM_MASS
+            barr[i].domain = t["domain"]
+            barr[i].order = t.get("order", -1)
+            barr[i].hpow = t.get("hpow", 0)
+            barr[i].coef = t.get("coef", 1.0)
+            d = t.get("defined_on")
+            if d is not None:
+                d = np.ascontiguousarray(d, dtype=np.uint64)
+                keep.append(d)
+            barr[i].defined_on = d.ctypes.data if d is not None else None
+        c = lib().orc_assemble_bnd(self.h, _p(l), ctypes.cast(arr, ctypes.c_void_p), len(terms),
+                                   ctypes.cast(barr, ctypes.c_void_p), len(bterms), nthreads, int(dn_fd))
         if not c:
             raise RuntimeError("oracle assembly error")
         nnz = lib().orc_csr_nnz(c)

@@ -1749,7 +1749,7 @@ int orc_fd_stencil(int k, int acc, double* c, double* eps) { return fd_stencil(k
 
 orc_csr* orc_assemble(const orc_space* s, const double* lset_vertex, const orc_term* terms, int nterms,
                       int nthreads) {
-  return orc_assemble_ex(s, lset_vertex, terms, nterms, nthreads, 0);
+  return orc_assemble_bnd(s, lset_vertex, terms, nterms, nullptr, 0, nthreads, 0);
 }
 
 // Bilinear forms on regions of several level sets: SymbolicCutBFI with a
@@ -1851,6 +1851,17 @@ orc_csr* orc_mlset_assemble(const orc_space* s, int M, const double* lsets, cons
 
 orc_csr* orc_assemble_ex(const orc_space* s, const double* lset_vertex, const orc_term* terms, int nterms,
                          int nthreads, int dn_fd) {
+  return orc_assemble_bnd(s, lset_vertex, terms, nterms, nullptr, 0, nthreads, dn_fd);
+}
+
+// orc_assemble with boundary terms: SymbolicCutBFI with vb == BND
+// (symboliccutbfi.cpp:76-486 on a boundary element, the rule of
+// straightcutrule.cpp:582-677 on the boundary facet): per BND element (the
+// boundary facets in facet order) in a term's set, the term's integrand with
+// the owning element's basis at the boundary rule's physical points, added
+// to the owner's element matrix; the owners join the active elements.
+orc_csr* orc_assemble_bnd(const orc_space* s, const double* lset_vertex, const orc_term* terms, int nterms,
+                          const orc_bterm* bterms, int nbterms, int nthreads, int dn_fd) {
   const int ne = s->ne, n = s->nd, n2 = 2 * n;
   const int64_t nf = s->nfacets;
   // active elements: in the definedon set of some volume term; active facets:
@@ -1859,10 +1870,23 @@ orc_csr* orc_assemble_ex(const orc_space* s, const double* lset_vertex, const or
   std::vector<int32_t> el_slot(ne, -1), fa_slot(nf, -1);
   bool any_vol = false, any_patch = false;
   for (int t = 0; t < nterms; t++) (facet_term(terms[t].kind) ? any_patch : any_vol) = true;
+  // BND elements (boundary facets in facet order) and their owners
+  std::vector<int32_t> bfac, bown;
+  std::vector<uint8_t> bnd_act(ne, 0);
+  if (nbterms > 0) {
+    for (int64_t f = 0; f < nf; f++)
+      if (s->facet_els[2 * f + 1] < 0) {
+        const int b = (int)bfac.size();
+        bfac.push_back((int32_t)f);
+        bown.push_back(s->facet_els[2 * f]);
+        for (int t = 0; t < nbterms; t++)
+          if (!bterms[t].defined_on || test_bit(bterms[t].defined_on, b)) bnd_act[s->facet_els[2 * f]] = 1;
+      }
+  }
   int nact = 0;
-  for (int e = 0; e < ne && any_vol; e++) {
-    bool act = false;
-    for (int t = 0; t < nterms; t++)
+  for (int e = 0; e < ne; e++) {
+    bool act = bnd_act[e] != 0;
+    for (int t = 0; t < nterms && any_vol; t++)
       if (!facet_term(terms[t].kind) && (!terms[t].defined_on || test_bit(terms[t].defined_on, e))) act = true;
     if (act) el_slot[e] = nact++;
   }
@@ -1885,6 +1909,50 @@ orc_csr* orc_assemble_ex(const orc_space* s, const double* lset_vertex, const or
       if (r) err = r;
     }
   });
+  // boundary terms, BND elements ascending
+  for (size_t bi = 0; bi < bfac.size(); bi++) {
+    const int e = bown[bi], f = bfac[bi], D = s->D;
+    double* A = &elm[(size_t)el_slot[e] * n * n];
+    Geo g;
+    element_geo(s, e, g, nullptr, nullptr);
+    const int* gv = &s->elv[(size_t)e * (D + 1)];
+    int lf = 0;
+    while (s->el_facets[(size_t)e * (D + 1) + lf] != f) lf++;
+    int v[3];
+    for (int q = 0; q < D; q++) v[q] = gv[D == 2 ? TRI_EDGES[lf][q] : TET_FACES[lf][q]];
+    std::sort(v, v + D);
+    double xb[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, lb[3];
+    for (int q = 0; q < D; q++) {
+      lb[q] = lset_vertex[v[q]];
+      for (int r = 0; r < D; r++) xb[3 * q + r] = s->coords[(size_t)v[q] * D + r];
+    }
+    double xs[3 * 512], ws[512], phi[20], dphi[20][3];
+    for (int t = 0; t < nbterms; t++) {
+      const orc_bterm& T = bterms[t];
+      if (T.defined_on && !test_bit(T.defined_on, (int64_t)bi)) continue;
+      const int order = T.order >= 0 ? T.order : 2 * s->k;
+      const int np = orc_bnd_element_rule(D, xb, lb, T.domain, order, xs, ws, 512);
+      if (np < 0) {
+        err = np == -1 ? ERR_CAPACITY : np;
+        continue;
+      }
+      double c = T.coef;
+      if (T.hpow != 0) c *= std::pow(std::pow(std::fabs(g.det), 1.0 / D), (double)T.hpow);
+      for (int q = 0; q < np; q++) {
+        const double* x = &xs[3 * q];
+        double xi[3] = {0, 0, 0};
+        for (int k = 0; k < D; k++) {
+          double acc = 0.0;
+          for (int cc = 0; cc < D; cc++) acc += g.Finv[k][cc] * (x[cc] - g.x0[cc]);
+          xi[k] = acc;
+        }
+        basis(D, s->k, gv, xi, phi, dphi);
+        const double w = ws[q] * c;
+        for (int a = 0; a < n; a++)
+          for (int bb = 0; bb < n; bb++) A[a * n + bb] += w * phi[a] * phi[bb];
+      }
+    }
+  }
   parallel_for(nfa, nthreads, [&](int64_t b, int64_t en) {
     for (int64_t i = b; i < en; i++) {
       int r = facet_matrix(s, lset_vertex, terms, nterms, fa_list[i], dn_fd, &fam[(size_t)i * n2 * n2]);

@@ -149,6 +149,17 @@ typedef struct {
  * plus facet-patch terms (GHOST_MASS with their facet sets). */
 orc_csr* orc_mlset_assemble(const orc_space* s, int M, const double* lsets, const orc_mlterm* terms, int nterms,
                             const orc_term* patch_terms, int npatch, int nthreads);
+/* A boundary term (dCut(lset, domain, vb=BND)): c * u * v over the domain
+ * part of the BND elements (the boundary facets in facet order) in its set. */
+typedef struct {
+  int kind;        /* ORC_TERM_MASS */
+  int domain;      /* ORC_NEG / ORC_POS */
+  int order, hpow; /* h of the owning element */
+  double coef;
+  const uint64_t* defined_on; /* BND element bits; NULL = all */
+} orc_bterm;
+orc_csr* orc_assemble_bnd(const orc_space* s, const double* lset_vertex, const orc_term* terms, int nterms,
+                          const orc_bterm* bterms, int nbterms, int nthreads, int dn_fd);
 /* orc_assemble with the normal-derivative mode of orc_facet_matrix. */
 orc_csr* orc_assemble_ex(const orc_space*, const double* lset_vertex, const orc_term* terms, int nterms,
                          int nthreads, int dn_fd);

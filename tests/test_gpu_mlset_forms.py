@@ -39,6 +39,9 @@ def setup(xg, D, n):
     hasneg = mlci.GetElementsWithContribution(region)
     els_if = hasneg & ~mlci.GetElementsOfType(region)
     facets_gp = xg.GetFacetsWithNeighborTypes(m, a=hasneg, b=els_if, use_and=True)
+    # the elements with a contribution to each boundary piece (els_if_singe of
+    # test_mlset_poisson.py)
+    region.els_bnd = {piece: mlci.GetElementsWithContribution(piece) for piece in region.Boundary()}
     return m, lsets, region, hasneg, facets_gp
 
 
@@ -51,7 +54,8 @@ def poisson_form(xg, V, lsets, region, hasneg, facets_gp, k, mass=False):
         return a
     a += xg.grad(u) * xg.grad(v) * xg.dCut(lsets, region, definedonelements=hasneg)
     for piece, n in region.GetOuterNormals(lsets).items():
-        a += (-xg.grad(u) * n * v - xg.grad(v) * n * u + (10.0 * k * k / h) * u * v) * xg.dCut(lsets, piece)
+        a += (-xg.grad(u) * n * v - xg.grad(v) * n * u + (10.0 * k * k / h) * u * v) * \
+            xg.dCut(lsets, piece, definedonelements=region.els_bnd[piece])
     a += 0.1 / h ** 2 * (u - u.Other()) * (v - v.Other()) * xg.dFacetPatch(definedonelements=facets_gp)
     return a
 
@@ -63,9 +67,10 @@ def oracle_terms(orc, region, lsets, hasneg, k):
     for piece, n in region.GetOuterNormals(lsets).items():
         i = piece.index(orc.IF)
         sign = n.monos[0].c
-        terms += [dict(kind=orc.TERM_NGRADU_V, tuples=[piece], coef=-sign, normal_lset=i),
-                  dict(kind=orc.TERM_U_NGRADV, tuples=[piece], coef=-sign, normal_lset=i),
-                  dict(kind=orc.TERM_MASS, tuples=[piece], coef=10.0 * k * k, hpow=-1)]
+        bits = region.els_bnd[piece].words.cpu().numpy()
+        terms += [dict(kind=orc.TERM_NGRADU_V, tuples=[piece], coef=-sign, normal_lset=i, defined_on=bits),
+                  dict(kind=orc.TERM_U_NGRADV, tuples=[piece], coef=-sign, normal_lset=i, defined_on=bits),
+                  dict(kind=orc.TERM_MASS, tuples=[piece], coef=10.0 * k * k, hpow=-1, defined_on=bits)]
     assert all(len(t["tuples"][0]) == M for t in terms)
     return terms
 
