@@ -110,11 +110,12 @@ def test_mlset_poisson_converges(xg, k):
     """tests/pytests/test_mlset_poisson.py's problem: -laplace u = f on the unit
     square given by four level sets, u = 16 x (1-x) y (1-y) (zero on the
     boundary, imposed by Nitsche).  Load vector M f_h (the region's mass matrix
-    times the interpolant), error |u_h - I u|_M in the region's mass norm: it
-    decreases at order >= k + 1 - 1/4."""
+    times the interpolant), error |u_h - I u|_M in the region's mass norm on
+    four meshes: as in the reference's convergence study, the first rate is
+    left out and the mean of the others is >= k + 1 - 1/4."""
     import scipy.sparse.linalg as spla
     errs = []
-    for n in (6, 12, 24):
+    for n in (6, 12, 24, 48):
         m, lsets, region, hasneg, facets_gp = setup(xg, 2, n)
         V = xg.H1(m, order=k)
         a = poisson_form(xg, V, lsets, region, hasneg, facets_gp, k)
@@ -131,5 +132,5 @@ def test_mlset_poisson_converges(xg, k):
         e = np.zeros(V.ndof)
         e[act] = x - uex.vec.cpu().numpy()[act]
         errs.append(np.sqrt(e @ (Mm @ e)))
-    rates = [np.log2(errs[i] / errs[i + 1]) for i in range(2)]
-    assert min(rates) > k + 1 - 0.25, (errs, rates)
+    rates = [np.log2(errs[i] / errs[i + 1]) for i in range(3)]
+    assert np.mean(rates[1:]) > k + 1 - 0.25, (errs, rates)
