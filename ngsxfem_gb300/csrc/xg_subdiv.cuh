@@ -17,11 +17,11 @@
 //                           (CutSimplex::MakeQuad); a vertex value of 0 is
 //                           positive and is cut against its negative
 //                           neighbours at the vertex
-// The reference refines breadth by recursion; here one thread walks the same
-// tree depth first with an explicit stack (children in order) and hands every
-// rule point to a callback, on the physical image of each simplex, so points
-// are physical and weights are physical measures (NEG / POS volumes, IF
-// surface measure).
+// The reference refines breadth by recursion; here a thread walks the same
+// tree (or one subtree of it) depth first with an explicit stack (children in
+// order) and hands every rule point to a callback, on the physical image of
+// each simplex, so points are physical and weights are physical measures
+// (NEG / POS volumes, IF surface measure).
 #pragma once
 #include "xg_basis.cuh"
 #include "xg_quadcut.cuh"
@@ -62,35 +62,6 @@ XG_QHD void lattice_point(const double (*v)[3], const int* I, double dx, double*
     for (int d = 0; d < D; d++) xi[d] += I[j] * dx * (v[j + 1][d] - v[0][d]);
 }
 
-#ifdef __CUDACC__
-// CheckIfCut with the lattice points split over the lanes of a warp (every
-// lane of the warp calls it with the same simplex; the answer is the same)
-template <int D, int K>
-__device__ __forceinline__ int lattice_domain_warp(const Elem<D, K>& el, const double (*v)[3], int L) {
-  const int np = 1 << L, lane = threadIdx.x & 31;
-  const double dx = 1.0 / np;
-  // lattice points: I with I_0 + .. + I_{D-1} <= np, enumerated by a flat index
-  const int side = np + 1, total = D == 2 ? side * side : side * side * side;
-  bool pos = false, neg = false;
-  for (int t0 = 0; t0 < total; t0 += 32) {
-    const int t = t0 + lane;
-    if (t < total) {
-      int I[3] = {t % side, (t / side) % side, D == 3 ? t / (side * side) : 0};
-      if (I[0] + I[1] + I[2] <= np) {
-        double xi[3];
-        lattice_point<D>(v, I, dx, xi);
-        if (lset_at(el, xi) >= 0.0) pos = true;
-        else neg = true;
-      }
-    }
-    pos = __any_sync(0xffffffffu, pos);
-    neg = __any_sync(0xffffffffu, neg);
-    if (pos && neg) return XG_IF;
-  }
-  return pos ? XG_POS : XG_NEG;
-}
-#endif
-
 // CheckIfCut on the lattice of simplex v (reference coordinates) at level L
 template <int D, int K>
 XG_QHD int lattice_domain(const Elem<D, K>& el, const double (*v)[3], int L) {
@@ -99,10 +70,8 @@ XG_QHD int lattice_domain(const Elem<D, K>& el, const double (*v)[3], int L) {
   bool pos = false, neg = false;
   int I[3] = {0, 0, 0};
   for (;;) {
-    double xi[3] = {0.0, 0.0, 0.0};
-    for (int d = 0; d < D; d++) xi[d] = v[0][d];
-    for (int j = 0; j < D; j++)
-      for (int d = 0; d < D; d++) xi[d] += I[j] * dx * (v[j + 1][d] - v[0][d]);
+    double xi[3];
+    lattice_point<D>(v, I, dx, xi);
     if (lset_at(el, xi) >= 0.0) pos = true;
     else neg = true;
     if (pos && neg) return XG_IF;
@@ -181,12 +150,12 @@ XG_QNI int fill(const RuleTable* Rp, const Elem<D, K>& el, const double (*v)[3],
   return qc::qcut_simplex<D>(Rp, s, lc, dt, order, emit);
 }
 
-// the rule of one element: emit(physical point, physical weight) per point;
-// returns 0 or the first xg error of a cut.  WARP: every lane of a warp runs
-// it for the same element (the lattice checks split over the lanes, every
-// lane sees every point)
-template <int D, int K, class E, bool WARP = false>
-XG_QNI int element_rule(const RuleTable* Rp, const Elem<D, K>& el, int dt, int order, int levels, E& emit) {
+// the rule of the sub-simplex v (reference coordinates) of an element at
+// refinement level L: emit(physical point, physical weight) per point;
+// returns 0 or the first xg error of a cut
+template <int D, int K, class E>
+XG_QNI int node_rule(const RuleTable* Rp, const Elem<D, K>& el, const double (*v)[3], int L, int dt, int order,
+                     E& emit) {
   struct Frame {
     double v[4][3];
     int L, next;
@@ -194,18 +163,14 @@ XG_QNI int element_rule(const RuleTable* Rp, const Elem<D, K>& el, int dt, int o
   Frame st[kMaxLevels + 1];
   int sp = 1;
   for (int i = 0; i < 4; i++)
-    for (int r = 0; r < 3; r++) st[0].v[i][r] = (i < D && r == i) ? 1.0 : 0.0;  // (1,0,0),(0,1,0),(0,0,1),(0,0,0)
-  st[0].L = levels;
+    for (int r = 0; r < 3; r++) st[0].v[i][r] = v[i][r];
+  st[0].L = L;
   st[0].next = -1;
   int status = 0;
   while (sp > 0) {
     Frame& f = st[sp - 1];
     if (f.next < 0) {
-#ifdef __CUDA_ARCH__
-      const int dself = WARP ? lattice_domain_warp(el, f.v, f.L) : lattice_domain(el, f.v, f.L);
-#else
       const int dself = lattice_domain(el, f.v, f.L);
-#endif
       if (dself != XG_IF || f.L == 0) {
         if (dself != XG_IF) {
           if (dself == dt) fill(Rp, el, f.v, (const double*)nullptr, dt, order, emit);
@@ -237,6 +202,20 @@ XG_QNI int element_rule(const RuleTable* Rp, const Elem<D, K>& el, int dt, int o
     sp++;
   }
   return status;
+}
+
+// the reference simplex (1,0,0),(0,1,0),(0,0,1),(0,0,0) (first D+1 rows)
+XG_QHD void ref_simplex(int D, double (*v)[3]) {
+  for (int i = 0; i < 4; i++)
+    for (int r = 0; r < 3; r++) v[i][r] = (i < D && r == i) ? 1.0 : 0.0;
+}
+
+// the rule of one element (the whole refinement tree from level `levels`)
+template <int D, int K, class E>
+XG_QNI int element_rule(const RuleTable* Rp, const Elem<D, K>& el, int dt, int order, int levels, E& emit) {
+  double v[4][3];
+  ref_simplex(D, v);
+  return node_rule(Rp, el, v, levels, dt, order, emit);
 }
 
 }  // namespace sd
