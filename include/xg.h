@@ -348,6 +348,33 @@ typedef struct {
 /* Replace the form's boundary terms (at most 8; nterms 0 removes them). */
 int xg_form_set_bnd_terms(xg_form* form, const xg_bterm* terms, int32_t nterms);
 
+/* Volume terms with a coefficient field (`gf * u * v * dCut(...)`,
+ * `gf * grad(u) * grad(v) * dCut(...)`, x^e factors): the integrand of kind
+ * XG_TERM_MASS, _LAPLACE, _NGRADU_V, _U_NGRADV or _CONV times
+ * c * h^hpow * x^e0 y^e1 z^e2 * gf(x), evaluated at the points of the
+ * domain's cut rule (the reference evaluates any CoefficientFunction at the
+ * rule's points, xfem/symboliccutbfi.cpp:168-194; default order: the
+ * kind's, trial + test order minus the derivatives, :107-111).  gf is a
+ * GridFunction of an H1 space of order 1..3 on the form's mesh (gf_space,
+ * d_gf its coefficients) or absent (gf_space NULL).  The elements of the
+ * term's set whose domain type is the term's domain or IF join the active
+ * elements; their matrices are the sums of all their terms.  Spatial forms on
+ * simplex meshes. */
+typedef struct {
+  int32_t kind;
+  int32_t domain; /* XG_NEG, XG_POS, XG_IF */
+  int32_t order;  /* -1: the kind's default */
+  int32_t hpow;
+  double coef;
+  double b[3];    /* convection vector (XG_TERM_CONV) */
+  int32_t e[3];   /* exponents of the monomial factor */
+  const xg_space* gf_space;
+  const double* d_gf;
+  const uint64_t* d_defined_on;
+} xg_cterm;
+/* Replace the form's coefficient terms (at most 8; nterms 0 removes them). */
+int xg_form_set_coef_terms(xg_form* form, const xg_cterm* terms, int32_t nterms);
+
 /* Output matrix in compressed-row form over the form's active dofs (the dofs
  * of elements and facet patches that carry a term, numbered ascending as
  * ngcomp::CompressedFESpace / Restrict() does):

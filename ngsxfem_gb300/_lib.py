@@ -29,7 +29,7 @@ EXPORTS = [
     "xg_mesh_create_tensor", "xg_cut_rules_ex", "xg_quad_rule_capacity", "xg_integrate_ex",
     "xg_integrate_mlset", "xg_cut_rules_mlset", "xg_mlset_rule_capacity", "xg_mlset_mark",
     "xg_iso_integrate_mesh", "xg_integrate_bnd",
-    "xg_mlset_form_create", "xg_mlset_form_assemble", "xg_form_create", "xg_form_destroy", "xg_form_set_defined_on", "xg_form_set_bnd_terms", "xg_form_capacity",
+    "xg_mlset_form_create", "xg_mlset_form_assemble", "xg_form_create", "xg_form_destroy", "xg_form_set_defined_on", "xg_form_set_bnd_terms", "xg_form_set_coef_terms", "xg_form_capacity",
     "xg_form_assemble", "xg_form_check", "xg_form_stage_events", "xg_cutfem_step", "xg_cutfem_marking",
     "xg_space_create_st", "xg_space_info_st", "xg_cutinfo_update_st", "xg_st_cut_rules", "xg_st_form_create",
     "xg_st_cutfem_step", "xg_step_graph_create", "xg_step_graph_launch", "xg_step_graph_destroy",
@@ -86,6 +86,21 @@ class BTerm(ctypes.Structure):
         ("order", ctypes.c_int32),
         ("hpow", ctypes.c_int32),
         ("coef", ctypes.c_double),
+        ("d_defined_on", ctypes.c_void_p),
+    ]
+
+
+class CTerm(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int32),
+        ("domain", ctypes.c_int32),
+        ("order", ctypes.c_int32),
+        ("hpow", ctypes.c_int32),
+        ("coef", ctypes.c_double),
+        ("b", ctypes.c_double * 3),
+        ("e", ctypes.c_int32 * 3),
+        ("gf_space", ctypes.c_void_p),
+        ("d_gf", ctypes.c_void_p),
         ("d_defined_on", ctypes.c_void_p),
     ]
 
@@ -170,6 +185,7 @@ def load():
         "xg_form_destroy": (I, [P]),
         "xg_form_set_defined_on": (I, [P, ctypes.c_int32, P]),
         "xg_form_set_bnd_terms": (I, [P, P, ctypes.c_int32]),
+        "xg_form_set_coef_terms": (I, [P, P, ctypes.c_int32]),
         "xg_form_capacity": (I, [P, P]),
         "xg_form_assemble": (I, [P, P, P, P, P]),
         "xg_form_check": (I, [P]),

@@ -38,6 +38,7 @@ UNITS = [
     ("xg_subdiv.cu", []),
     ("xg_mlform.cu", []),
     ("xg_bform.cu", []),
+    ("xg_cform.cu", []),
 ]
 
 

@@ -2546,6 +2546,8 @@ struct xg_form {
   BndDesc bnd = {};
   int n_own = 0;
   int32_t* d_own = nullptr;  // [n_own] owners, [n_own + 1] pointers, [nbnd] BND elements
+  // volume terms with a coefficient field (xg_form_set_coef_terms)
+  CoefDesc cdesc = {};
   FormDesc desc;
   int needs_mask = 0;  // domains needing decompositions on cut elements
   int el_sym = 0;      // every volume group symmetric: packed element matrices
@@ -3911,6 +3913,54 @@ int xg_form_set_bnd_terms(xg_form* f, const xg_bterm* terms, int32_t nterms) {
   return XG_OK;
 }
 
+int xg_form_set_coef_terms(xg_form* f, const xg_cterm* terms, int32_t nterms) {
+  if (!f || nterms < 0 || (nterms > 0 && !terms)) return XG_ERR_ARG;
+  if (nterms > kMaxCoef) {
+    set_last_error("xg_form_set_coef_terms: at most 8 coefficient terms");
+    return XG_ERR_CAPACITY;
+  }
+  xg_mesh* m = f->mesh;
+  if (nterms > 0 && (!f->rows || f->ml || m->tensor)) {
+    set_last_error("xg_form_set_coef_terms: coefficient terms need a spatial form on a simplex mesh");
+    return XG_ERR_UNSUPPORTED;
+  }
+  CoefDesc d = {};
+  for (int t = 0; t < nterms; t++) {
+    const xg_cterm& T = terms[t];
+    const bool kind_ok = T.kind == XG_TERM_MASS || T.kind == XG_TERM_LAPLACE || T.kind == XG_TERM_NGRADU_V ||
+                         T.kind == XG_TERM_U_NGRADV || T.kind == XG_TERM_CONV;
+    if (!kind_ok || (T.domain != XG_NEG && T.domain != XG_POS && T.domain != XG_IF) || T.order > kMaxOrder ||
+        T.e[0] < 0 || T.e[1] < 0 || T.e[2] < 0) {
+      set_last_error("xg_form_set_coef_terms: kinds MASS, LAPLACE, NGRADU_V, U_NGRADV, CONV on NEG, POS or IF, "
+                     "order <= 8, exponents >= 0");
+      return XG_ERR_ARG;
+    }
+    const xg_space* g = T.gf_space;
+    if (g && (!T.d_gf || g->mesh != m || g->kt >= 0 || g->ndof != g->ndof_s || g->order < 1 || g->order > 3 ||
+              g->nd != ndof_el(m->dim, g->order))) {
+      set_last_error("xg_form_set_coef_terms: the coefficient is a GridFunction of an H1 space of order 1..3 "
+                     "on the form's mesh");
+      return XG_ERR_ARG;
+    }
+    CoefTermDev& C = d.t[d.n++];
+    C.kind = T.kind;
+    C.domain = T.domain;
+    C.order = T.order >= 0 ? T.order : default_order(T.kind, f->space->order);
+    C.hpow = T.hpow;
+    C.coef = T.coef;
+    for (int k = 0; k < 3; k++) {
+      C.b[k] = T.b[k];
+      C.e[k] = T.e[k];
+    }
+    C.gf_order = g ? g->order : 0;
+    C.gf_dofs = g ? g->d_el_dofs : nullptr;
+    C.gf = g ? T.d_gf : nullptr;
+    C.defined_on = T.d_defined_on;
+  }
+  f->cdesc = d;
+  return XG_OK;
+}
+
 int xg_form_capacity(const xg_form* f, int64_t* o) {
   if (!f || !o) return XG_ERR_ARG;
   // the largest pattern any level set can produce on this mesh (every element
@@ -4006,6 +4056,32 @@ BndFormLaunch bnd_args(xg_form* f, const double* d_lset) {
   return L;
 }
 
+// coefficient terms: their active elements and their element rows
+CoefFormLaunch coef_args(xg_form* f, const double* d_lset, const uint8_t* d_dom) {
+  xg_mesh* m = f->mesh;
+  CoefFormLaunch L;
+  L.dim = m->dim;
+  L.order = f->space->order;
+  L.ne = m->ne;
+  L.nv = m->nv;
+  L.elv = m->d_elv;
+  L.xyz = m->d_xyz;
+  L.lset = d_lset;
+  L.dom = d_dom;
+  L.d = f->cdesc;
+  L.act_un = f->d_act_un;
+  L.act_cut = f->d_act_cut;
+  L.nw32 = f->nw32_el;
+  L.l_un = f->d_l_un;
+  L.l_cut = f->d_l_cut;
+  L.counts = f->d_counts;
+  L.rowslot = f->d_el_rowslot;
+  L.elmat = f->d_elmat;
+  L.fp64 = f->precision == XG_PREC_FP64 ? 1 : 0;
+  L.err = f->d_err;
+  return L;
+}
+
 // the element and patch kernels of one step (spatial forms: the element rows
 // at their static slots and the patch matrices by facet slot; the patch
 // matrices are left out when the form's patches run in a batched launch)
@@ -4015,6 +4091,7 @@ int rows_front(xg_form* f, const double* d_lset, const uint8_t* d_dom, cudaStrea
   if ((st = fp64 ? dispatch_volume<double>(f, d_lset, d_dom, s) : dispatch_volume<float>(f, d_lset, d_dom, s)))
     return st;
   if (f->bnd.n > 0 && (st = bnd_elmat_launch(bnd_args(f, d_lset), s))) return st;
+  if (f->cdesc.n > 0 && (st = coef_elmat_launch(coef_args(f, d_lset, d_dom), s))) return st;
   if (f->has_patch && f->desc.npatch > 0 && (st = fp64 ? dispatch_patch<double>(f, s) : dispatch_patch<float>(f, s)))
     return st;
   if (f->desc.nskel > 0 && (st = launch_skel(f, d_lset, s))) return st;
@@ -4051,6 +4128,7 @@ int assemble_front(xg_form* f, const double* d_lset, const uint8_t* d_dom, xg_cs
   k_active_elements<<<(unsigned)((f->nw32_el * 32 + 255) / 256), 256, 0, s>>>(m->ne, d_dom, f->desc, f->d_act_un,
                                                                               f->d_act_cut, f->nw32_el);
   if (f->bnd.n > 0 && (st = bnd_active_launch(bnd_args(f, d_lset), s))) return st;
+  if (f->cdesc.n > 0 && (st = coef_active_launch(coef_args(f, d_lset, d_dom), s))) return st;
   if ((st = compact(f, f->d_act_un, f->nw32_el, f->d_l_un, f->d_el_slot, f->d_counts + 0, s))) return st;
   if ((st = compact(f, f->d_act_cut, f->nw32_el, f->d_l_cut, f->d_el_slot, f->d_counts + 1, s, f->d_counts + 0)))
     return st;

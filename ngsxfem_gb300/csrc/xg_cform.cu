@@ -1,0 +1,237 @@
+// Volume terms of bilinear forms with a coefficient field: the integrand of a
+// menu kind (mass, Laplace, the Nitsche normal terms, convection) times
+// c h^p x^e gf(x), gf a GridFunction of an H1 space on the form's mesh.  The
+// reference evaluates its CoefficientFunction at the points of the cut rule
+// and contracts (xfem/symboliccutbfi.cpp:76-313, the evaluation at
+// :168-194); the rule is StraightCutIntegrationRule
+// (cutint/straightcutrule.cpp:582-677: the standard rule on uncut elements of
+// the term's domain, the sub-simplices of Decompose on cut ones, the
+// interface factor for IF), with the rule code of xg_cut.cuh.  Thread per
+// active element, FP64 sums added to the element's rows after the volume
+// kernels wrote them (one thread owns an element's rows: no atomics, a fixed
+// order).
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "xg_basis.cuh"
+#include "xg_cut.cuh"
+#include "xg_internal.h"
+
+namespace xg {
+
+static __device__ RuleTable g_cf_rules;
+
+int upload_rules_cform() {
+  XG_CUDA(cudaMemcpyToSymbol(g_cf_rules, &host_rules(), sizeof(RuleTable)));
+  return XG_OK;
+}
+
+namespace {
+
+__device__ __forceinline__ bool cf_bit64(const uint64_t* b, int64_t i) { return (b[i >> 6] >> (i & 63)) & 1ull; }
+__device__ __forceinline__ bool cf_bit32(const uint32_t* b, int64_t i) { return (b[i >> 5] >> (i & 31)) & 1u; }
+
+__device__ __forceinline__ double cf_ipow(double x, int e) {
+  double r = 1.0;
+  for (int k = 0; k < e; k++) r *= x;
+  return r;
+}
+
+// does term T contribute on element e of domain type dom
+__device__ __forceinline__ bool term_on(const CoefTermDev& T, int64_t e, int dom) {
+  if (T.defined_on && !cf_bit64(T.defined_on, e)) return false;
+  return dom == XG_IF || dom == T.domain;
+}
+
+// descriptor of local function i of an H1 element of runtime order k
+template <int D>
+__device__ __forceinline__ int desc_rt(int k, int i, const int* gv) {
+  return k == 1 ? fn_desc<D, 1>(i, gv) : (k == 2 ? fn_desc<D, 2>(i, gv) : fn_desc<D, 3>(i, gv));
+}
+
+// elements with a coefficient term join the active elements (in the uncut
+// list unless they are listed as cut already); a warp owns one bit word
+__global__ void k_coef_active(int ne, const uint8_t* __restrict__ dom, CoefDesc d, uint32_t* __restrict__ act_un,
+                              const uint32_t* __restrict__ act_cut, int64_t nw32) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  bool add = false;
+  if (e < ne && !cf_bit32(act_cut, e)) {
+    const int de = dom[e];
+    for (int t = 0; t < d.n && !add; t++) add = term_on(d.t[t], e, de);
+  }
+  const unsigned m = __ballot_sync(0xffffffffu, add);
+  if ((threadIdx.x & 31) == 0 && m && (e >> 5) < nw32) act_un[e >> 5] |= m;
+}
+
+template <int D, int K, typename T>
+__global__ void __launch_bounds__(128) k_coef_elmat(CoefFormLaunch L) {
+  constexpr int N = ndof_el(D, K);
+  const int n_un = L.counts[0], n = n_un + L.counts[1];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int e = i < n_un ? L.l_un[i] : L.l_cut[i - n_un];
+    double xv[4][3], l[4];
+    int gv[4] = {0, 0, 0, 0};
+    for (int v = 0; v <= D; v++) {
+      gv[v] = L.elv[(int64_t)v * L.ne + e];
+      l[v] = L.lset[gv[v]];
+      for (int c = 0; c < 3; c++) xv[v][c] = c < D ? L.xyz[(int64_t)c * L.nv + gv[v]] : 0.0;
+    }
+    const int cdom = check_if_straight_cut(l, D + 1);
+    bool any = false;
+    for (int t = 0; t < L.d.n; t++) any |= term_on(L.d.t[t], e, cdom);
+    if (!any) continue;
+    Geo<D> g;
+    make_geo<D>(xv, g);
+    const double meas = fabs(g.det), h = mesh_h<D>(meas);
+    // physical gradients of the barycentrics, the level set's unit normal
+    double gl[D + 1][D], nrm[D];
+    double nn = 0.0;
+    for (int k = 0; k < D; k++) {
+      double s = 0.0, sl = 0.0;
+      for (int a = 0; a < D; a++) {
+        gl[a][k] = g.Finv[a][k];
+        s += g.Finv[a][k];
+        sl += g.Finv[a][k] * (l[a] - l[D]);
+      }
+      gl[D][k] = -s;
+      nrm[k] = sl;
+      nn += sl * sl;
+    }
+    {
+      const double inv = 1.0 / sqrt(nn);
+      for (int k = 0; k < D; k++) nrm[k] *= inv;
+    }
+    int desc[N];
+    for (int a = 0; a < N; a++) desc[a] = fn_desc<D, K>(a, gv);
+    double A[N * N];
+    for (int k = 0; k < N * N; k++) A[k] = 0.0;
+    for (int t = 0; t < L.d.n; t++) {
+      const CoefTermDev& Tm = L.d.t[t];
+      if (!term_on(Tm, e, cdom)) continue;
+      const double c = Tm.hpow == 0 ? Tm.coef : Tm.coef * int_pow(h, Tm.hpow);
+      // the coefficient field on this element
+      const int kg = Tm.gf_order, ng = kg > 0 ? ndof_el(D, kg) : 0;
+      double cg[20];
+      int dg[20];
+      for (int a = 0; a < ng; a++) {
+        cg[a] = Tm.gf[Tm.gf_dofs[(int64_t)a * L.ne + e]];
+        dg[a] = desc_rt<D>(kg, a, gv);
+      }
+      auto point = [&](const double* xi, double w) {
+        double lam[D + 1], sl = 0.0;
+        for (int k = 0; k < D; k++) {
+          lam[k] = xi[k];
+          sl += xi[k];
+        }
+        lam[D] = 1.0 - sl;
+        double f = 1.0;
+        if (ng > 0) {
+          f = 0.0;
+          for (int a = 0; a < ng; a++) f += cg[a] * eval_fn_value<D, double>(dg[a], lam);
+        }
+        if (Tm.e[0] | Tm.e[1] | Tm.e[2]) {
+          double x[3] = {0.0, 0.0, 0.0};
+          for (int r = 0; r < D; r++) {
+            double s = g.x0[r];
+            for (int k = 0; k < D; k++) s += g.F[r][k] * xi[k];
+            x[r] = s;
+          }
+          f *= cf_ipow(x[0], Tm.e[0]) * cf_ipow(x[1], Tm.e[1]) * (D == 3 ? cf_ipow(x[2], Tm.e[2]) : 1.0);
+        }
+        double phi[N], gr[N][D], dn[N];
+        for (int a = 0; a < N; a++) {
+          eval_fn<D, double>(desc[a], lam, gl, phi[a], gr[a]);
+          double s = 0.0;
+          for (int k = 0; k < D; k++) s += (Tm.kind == XG_TERM_CONV ? Tm.b[k] : nrm[k]) * gr[a][k];
+          dn[a] = s;
+        }
+        const double W = w * meas * c * f;
+        for (int a = 0; a < N; a++)      // test
+          for (int b = 0; b < N; b++) {  // trial
+            double v;
+            switch (Tm.kind) {
+              case XG_TERM_MASS: v = phi[a] * phi[b]; break;
+              case XG_TERM_LAPLACE: {
+                v = 0.0;
+                for (int k = 0; k < D; k++) v += gr[a][k] * gr[b][k];
+                break;
+              }
+              case XG_TERM_U_NGRADV: v = phi[b] * dn[a]; break;
+              default: v = dn[b] * phi[a]; break;  // XG_TERM_NGRADU_V, XG_TERM_CONV
+            }
+            A[a * N + b] += W * v;
+          }
+      };
+      const int p = clamp_order(Tm.order);
+      if (cdom != XG_IF) {
+        const int off = g_cf_rules.off[D][p], cnt = g_cf_rules.cnt[D][p];
+        for (int q = 0; q < cnt; q++) point(g_cf_rules.x[off + q], g_cf_rules.w[off + q]);
+        continue;
+      }
+      Sub subs[3];
+      const int ns = decompose<D>(l, Tm.domain, subs);
+      if (ns < 0) {
+        set_err(L.err, -ns);
+        continue;
+      }
+      const int sd = Tm.domain == XG_IF ? D - 1 : D;
+      const int off = g_cf_rules.off[sd][p], cnt = g_cf_rules.cnt[sd][p];
+      const double fac = Tm.domain == XG_IF ? if_factor<D>(g, l) : 1.0;
+      for (int s = 0; s < ns; s++) {
+        const double trafofac = simplex_volume(subs[s].p, sd + 1);
+        for (int q = 0; q < cnt; q++) {
+          double pt[3];
+          plain_point(subs[s], sd + 1, g_cf_rules.x[off + q], pt);
+          double w = g_cf_rules.w[off + q] * trafofac;
+          if (Tm.domain == XG_IF) w = w * fac;
+          point(pt, w);
+        }
+      }
+    }
+    for (int a = 0; a < N; a++) {
+      T* row = (T*)L.elmat + (int64_t)L.rowslot[(int64_t)e * N + a] * N;
+      for (int b = 0; b < N; b++) {
+        const double v = (double)row[b] + A[a * N + b];
+        if (!finite_bits(v)) set_err(L.err, XG_ERR_NONFINITE);
+        row[b] = (T)v;
+      }
+    }
+  }
+}
+
+template <int D, int K, typename T>
+int launch_t(const CoefFormLaunch& L, cudaStream_t s) {
+  k_coef_elmat<D, K, T><<<152 * 8, 128, 0, s>>>(L);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? XG_OK : cuda_fail(e, "k_coef_elmat");
+}
+
+template <typename T>
+int launch_k(const CoefFormLaunch& L, cudaStream_t s) {
+  if (L.dim == 2) {
+    if (L.order == 1) return launch_t<2, 1, T>(L, s);
+    if (L.order == 2) return launch_t<2, 2, T>(L, s);
+    return launch_t<2, 3, T>(L, s);
+  }
+  if (L.order == 1) return launch_t<3, 1, T>(L, s);
+  if (L.order == 2) return launch_t<3, 2, T>(L, s);
+  return launch_t<3, 3, T>(L, s);
+}
+
+}  // namespace
+
+int coef_active_launch(const CoefFormLaunch& L, cudaStream_t s) {
+  if (L.d.n <= 0 || L.ne <= 0) return XG_OK;
+  k_coef_active<<<(unsigned)((L.nw32 * 32 + 255) / 256), 256, 0, s>>>(L.ne, L.dom, L.d, L.act_un, L.act_cut, L.nw32);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? XG_OK : cuda_fail(e, "k_coef_active");
+}
+
+int coef_elmat_launch(const CoefFormLaunch& L, cudaStream_t s) {
+  if (L.d.n <= 0) return XG_OK;
+  if (L.dim < 2 || L.dim > 3 || L.order < 1 || L.order > 3) return XG_ERR_UNSUPPORTED;
+  return L.fp64 ? launch_k<double>(L, s) : launch_k<float>(L, s);
+}
+
+}  // namespace xg

@@ -35,6 +35,7 @@ int ensure_device_rules() {
   if (!st) st = upload_rules_subdiv();
   if (!st) st = upload_rules_mlform();
   if (!st) st = upload_rules_bform();
+  if (!st) st = upload_rules_cform();
   if (st) return st;
   done.push_back(dev);
   return XG_OK;

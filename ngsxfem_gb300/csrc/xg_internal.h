@@ -255,6 +255,43 @@ struct BndFormLaunch {
   int fp64;
   int* err;
 };
+// volume terms with a coefficient field (xg_form_set_coef_terms; xg_cform.cu)
+constexpr int kMaxCoef = 8;
+struct CoefTermDev {
+  int kind, domain, order, hpow;
+  double coef, b[3];
+  int e[3];
+  int gf_order;            // 0: no coefficient field
+  const int32_t* gf_dofs;  // [nd_gf][ne] element dofs of its space
+  const double* gf;        // its coefficients
+  const uint64_t* defined_on;
+};
+struct CoefDesc {
+  int n;
+  CoefTermDev t[kMaxCoef];
+};
+struct CoefFormLaunch {
+  int dim, order;
+  int ne, nv;
+  const int32_t* elv;
+  const double* xyz;
+  const double* lset;      // P1 vertex values
+  const uint8_t* dom;      // element domain types
+  CoefDesc d;
+  uint32_t* act_un;
+  const uint32_t* act_cut;
+  int64_t nw32;
+  const int32_t* l_un;     // active elements: uncut list, then cut list
+  const int32_t* l_cut;
+  const int* counts;
+  const int32_t* rowslot;
+  void* elmat;
+  int fp64;
+  int* err;
+};
+int coef_active_launch(const CoefFormLaunch& a, cudaStream_t s);
+int coef_elmat_launch(const CoefFormLaunch& a, cudaStream_t s);
+int upload_rules_cform();
 int bnd_active_launch(const BndFormLaunch& a, cudaStream_t s);
 int bnd_elmat_launch(const BndFormLaunch& a, cudaStream_t s);
 int upload_rules_bform();

@@ -757,6 +757,15 @@ class _Integral:
             if mono.vec is not None:
                 raise TypeError("integrand is a vector, not a scalar")
             scal = [a for a in mono.scal]
+            # coefficient factors: one GridFunction, monomials of x, y, z
+            gfs = [a[1] for a in scal if a[0] == "gf"]
+            ex = [0, 0, 0]
+            for a in scal:
+                if a[0] == "xyz":
+                    ex = [p + q for p, q in zip(ex, a[1])]
+            scal = [a for a in scal if a[0] not in ("gf", "xyz")]
+            if len(gfs) > 1:
+                raise NotImplementedError("one GridFunction factor per integrand term")
             if any(a[1] for a in scal if a[0] in ("u", "v")):
                 raise NotImplementedError(".Other() is only meaningful on facet patches")
             names = sorted(a[0] for a in scal)
@@ -796,7 +805,8 @@ class _Integral:
                 raise NotImplementedError("integrand term outside the supported menu: %s" % (names + dots,))
             out.append(dict(kind=kind, domain=dom, order=-1 if m.order is None else m.order, hpow=mono.hpow,
                             coef=mono.c * m.scale, b=b, defined_on=m.definedonelements, tb=tb,
-                            tref=m.tref, time_order=m.time_order, normal_lset=nrm_index))
+                            tref=m.tref, time_order=m.time_order, normal_lset=nrm_index,
+                            gf=gfs[0] if gfs else None, e=tuple(ex)))
         return out
 
 
@@ -956,7 +966,7 @@ class BilinearForm:
             tup = np.ascontiguousarray(np.array(dom.as_list, dtype=np.int8).reshape(-1, M))
             for t in it.terms(lsets):
                 if t["kind"] not in (TERM_MASS, TERM_LAPLACE, TERM_NGRADU_V, TERM_U_NGRADV, TERM_CONV) or \
-                        t.get("tb") is not None:
+                        t.get("tb") is not None or t.get("gf") is not None or any(t.get("e", (0, 0, 0))):
                     raise NotImplementedError("region terms: mass, Laplace, Nitsche normal terms, convection")
                 t["tuples"] = tup
                 region.append(t)
@@ -999,6 +1009,8 @@ class BilinearForm:
         terms = []
         for it in self.integrals:
             terms += it.terms(lset)
+        if any(t.get("gf") is not None or any(t.get("e", (0, 0, 0))) for t in terms):
+            raise NotImplementedError("space-time forms take constant coefficients")
         orders = {t["time_order"] for t in terms if t.get("tref") is None and t["kind"] != TERM_GHOST_MASS}
         orders |= {it.measure.time_order for it in self.integrals if it.measure.kind == "patch"}
         orders.discard(-1)
@@ -1037,12 +1049,13 @@ class BilinearForm:
         lset = self._levelset()
         if isinstance(lset, (tuple, list)):
             return self._build_ml(lset)
-        terms, bterms = [], []
+        terms, bterms, cterms = [], [], []
         for it in self.integrals:
             if it.measure.kind == "cut" and getattr(it.measure, "vb", VOL) == BND:
                 bterms += self._bnd_terms(it, lset)
-            else:
-                terms += it.terms(lset)
+                continue
+            for t in it.terms(lset):
+                (cterms if t.get("gf") is not None or any(t.get("e", (0, 0, 0))) else terms).append(t)
         arr = (_lib.Term * max(len(terms), 1))()
         self._keep = []
         for k, t in enumerate(terms):
@@ -1071,6 +1084,29 @@ class BilinearForm:
                 barr[k].d_defined_on = d.words.data_ptr() if d is not None else None
             _lib.call("xg_form_set_bnd_terms", h, barr, len(bterms))
             self._bterms = bterms
+        if cterms:
+            carr = (_lib.CTerm * len(cterms))()
+            for k, t in enumerate(cterms):
+                if t["kind"] not in (TERM_MASS, TERM_LAPLACE, TERM_NGRADU_V, TERM_U_NGRADV, TERM_CONV) or \
+                        t.get("tb") is not None:
+                    raise NotImplementedError("coefficient fields multiply mass, Laplace, Nitsche and convection terms")
+                carr[k].kind, carr[k].domain, carr[k].order, carr[k].hpow = t["kind"], t["domain"], t["order"], t["hpow"]
+                carr[k].coef = t["coef"]
+                for j in range(3):
+                    carr[k].b[j] = t["b"][j]
+                    carr[k].e[j] = t["e"][j]
+                g = t["gf"]
+                if g is not None:
+                    if not isinstance(g.space, H1) or g.space.mesh is not self.space.mesh:
+                        raise ValueError("the coefficient GridFunction must live in an H1 space of the form's mesh")
+                    self._keep.append(g)
+                    carr[k].gf_space, carr[k].d_gf = g.space.h, g.vec.data_ptr()
+                d = t["defined_on"]
+                if d is not None:
+                    self._keep.append(d)
+                carr[k].d_defined_on = d.words.data_ptr() if d is not None else None
+            _lib.call("xg_form_set_coef_terms", h, carr, len(cterms))
+            self._cterms = cterms
         cap = np.zeros(2, dtype=np.int64)
         _lib.call("xg_form_capacity", h, cap.ctypes.data_as(ctypes.c_void_p))
         self._alloc(int(cap[0]), int(cap[1]))

@@ -40,6 +40,21 @@ class BTerm(ctypes.Structure):
     ]
 
 
+class CTerm(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int),
+        ("domain", ctypes.c_int),
+        ("order", ctypes.c_int),
+        ("hpow", ctypes.c_int),
+        ("coef", ctypes.c_double),
+        ("b", ctypes.c_double * 3),
+        ("e", ctypes.c_int * 3),
+        ("gf_order", ctypes.c_int),
+        ("gf_el", ctypes.c_void_p),
+        ("defined_on", ctypes.c_void_p),
+    ]
+
+
 class MlTerm(ctypes.Structure):
     _fields_ = [
         ("kind", ctypes.c_int),
@@ -103,6 +118,9 @@ def lib():
         L.orc_integrate_subdiv.argtypes = [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                            ctypes.c_int, P, P]
         L.orc_subdiv_moments_p2.argtypes = [ctypes.c_int64, P, ctypes.c_int, P, ctypes.c_int]
+        L.orc_assemble_full.restype = P
+        L.orc_assemble_full.argtypes = [P, P, P, ctypes.c_int, P, ctypes.c_int, P, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_int]
         L.orc_assemble_bnd.restype = P
         L.orc_assemble_bnd.argtypes = [P, P, P, ctypes.c_int, P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.orc_mlset_assemble.restype = P
@@ -697,10 +715,12 @@ class Space:
             raise RuntimeError("oracle facet matrix error %d" % r)
         return out
 
-    def assemble(self, lset, terms, nthreads=1, dn_fd=False, bterms=()):
+    def assemble(self, lset, terms, nthreads=1, dn_fd=False, bterms=(), cterms=()):
         """Returns scipy-free CSR triple (rowptr int64, cols int32, vals float64) over all dofs.
         bterms: boundary terms (dicts: domain, coef, order, hpow, defined_on
-        over the BND elements), mass terms of orc_assemble_bnd."""
+        over the BND elements), mass terms of orc_assemble_bnd.  cterms:
+        volume terms with a coefficient field (dicts: kind, domain, coef,
+        order, hpow, b, e, gf_order, gf_el [ne][nd_gf], defined_on)."""
         arr, keep = self._terms(terms)
         l = np.ascontiguousarray(lset, dtype=np.float64)
         barr = (BTerm * max(len(bterms), 1))()
@@ -715,8 +735,30 @@ class Space:
                 d = np.ascontiguousarray(d, dtype=np.uint64)
                 keep.append(d)
             barr[i].defined_on = d.ctypes.data if d is not None else None
-        c = lib().orc_assemble_bnd(self.h, _p(l), ctypes.cast(arr, ctypes.c_void_p), len(terms),
-                                   ctypes.cast(barr, ctypes.c_void_p), len(bterms), nthreads, int(dn_fd))
+        carr = (CTerm * max(len(cterms), 1))()
+        for i, t in enumerate(cterms):
+            carr[i].kind = t["kind"]
+            carr[i].domain = t.get("domain", NEG)
+            carr[i].order = t.get("order", -1)
+            carr[i].hpow = t.get("hpow", 0)
+            carr[i].coef = t.get("coef", 1.0)
+            for k in range(3):
+                carr[i].b[k] = t.get("b", (0.0, 0.0, 0.0))[k]
+                carr[i].e[k] = t.get("e", (0, 0, 0))[k]
+            g = t.get("gf_el")
+            if g is not None:
+                g = np.ascontiguousarray(g, dtype=np.float64)
+                keep.append(g)
+                carr[i].gf_order = t["gf_order"]
+            carr[i].gf_el = g.ctypes.data if g is not None else None
+            d = t.get("defined_on")
+            if d is not None:
+                d = np.ascontiguousarray(d, dtype=np.uint64)
+                keep.append(d)
+            carr[i].defined_on = d.ctypes.data if d is not None else None
+        c = lib().orc_assemble_full(self.h, _p(l), ctypes.cast(arr, ctypes.c_void_p), len(terms),
+                                    ctypes.cast(barr, ctypes.c_void_p), len(bterms),
+                                    ctypes.cast(carr, ctypes.c_void_p), len(cterms), nthreads, int(dn_fd))
         if not c:
             raise RuntimeError("oracle assembly error")
         nnz = lib().orc_csr_nnz(c)

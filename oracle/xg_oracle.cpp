@@ -828,6 +828,77 @@ int element_matrix(const orc_space* s, const double* lset_vertex, const orc_term
   return 0;
 }
 
+// Coefficient terms: T_CalcElementMatrixAdd with the CoefficientFunction
+// evaluated at the rule's points (symboliccutbfi.cpp:168-194), here a field
+// given by its element coefficients times a monomial of x; added to elmat.
+int element_matrix_coef(const orc_space* s, const double* lset_vertex, const orc_cterm* terms, int nterms, int e,
+                        double* elmat) {
+  const int D = s->D, n = s->nd;
+  Geo g;
+  double l[4];
+  element_geo(s, e, g, l, lset_vertex);
+  const int* gv = &s->elv[(size_t)e * (D + 1)];
+  std::vector<double> pts, wts;
+  double phi[20], dphi[20][3], gphys[20][3], phig[20], dphig[20][3];
+  double gl[3] = {0, 0, 0}, nrm[3];
+  {
+    double gr[3] = {0, 0, 0};
+    for (int k = 0; k < D; k++) gr[k] = l[k] - l[D];
+    phys_grad(g, gr, gl);
+    double nn = l2norm3(gl);
+    for (int c = 0; c < 3; c++) nrm[c] = gl[c] / nn;
+  }
+  for (int t = 0; t < nterms; t++) {
+    const orc_cterm& T = terms[t];
+    if (T.defined_on && !test_bit(T.defined_on, e)) continue;
+    const int order = T.order >= 0 ? T.order : default_order(T.kind, s->k);
+    const int np = straight_cut_rule(g, l, T.domain, order, pts, wts);
+    if (np < -1) return np;
+    if (np <= 0) continue;
+    double c = T.coef;
+    if (T.hpow != 0) c *= std::pow(std::pow(std::fabs(g.det), 1.0 / D), (double)T.hpow);
+    const double meas = std::fabs(g.det);
+    const int ng = T.gf_order > 0 ? (D == 2 ? (T.gf_order + 1) * (T.gf_order + 2) / 2
+                                            : (T.gf_order + 1) * (T.gf_order + 2) * (T.gf_order + 3) / 6)
+                                  : 0;
+    for (int q = 0; q < np; q++) {
+      const double* xi = &pts[3 * q];
+      basis(D, s->k, gv, xi, phi, dphi);
+      for (int i = 0; i < n; i++) phys_grad(g, dphi[i], gphys[i]);
+      double f = 1.0;
+      if (ng > 0) {
+        basis(D, T.gf_order, gv, xi, phig, dphig);
+        f = 0.0;
+        for (int i = 0; i < ng; i++) f += T.gf_el[(size_t)e * ng + i] * phig[i];
+      }
+      if (T.e[0] || T.e[1] || T.e[2]) {
+        double x[3] = {0, 0, 0};
+        for (int r = 0; r < D; r++) {
+          double acc = g.x0[r];
+          for (int k = 0; k < D; k++) acc += g.F[r][k] * xi[k];
+          x[r] = acc;
+        }
+        for (int r = 0; r < 3; r++)
+          for (int p = 0; p < T.e[r]; p++) f *= x[r];
+      }
+      const double w = wts[q] * meas * c * f;
+      const double* bb = T.kind == ORC_TERM_CONV ? T.b : nrm;
+      for (int i = 0; i < n; i++)      // test
+        for (int j = 0; j < n; j++) {  // trial
+          double v;
+          switch (T.kind) {
+            case ORC_TERM_MASS: v = phi[i] * phi[j]; break;
+            case ORC_TERM_LAPLACE: v = gphys[i][0] * gphys[j][0] + gphys[i][1] * gphys[j][1] + gphys[i][2] * gphys[j][2]; break;
+            case ORC_TERM_U_NGRADV: v = phi[j] * (bb[0] * gphys[i][0] + bb[1] * gphys[i][1] + bb[2] * gphys[i][2]); break;
+            default: v = (bb[0] * gphys[j][0] + bb[1] * gphys[j][1] + bb[2] * gphys[j][2]) * phi[i]; break;
+          }
+          elmat[i * n + j] += w * v;
+        }
+    }
+  }
+  return 0;
+}
+
 // MapPatchIntegrationPoint (symboliccutbfi.cpp:1747-1846) for affine elements.
 void map_patch_point(const Geo& from, const Geo& to, const double* xi_from, double w_from, double* xi_to,
                      double* w_to) {
@@ -1862,6 +1933,14 @@ orc_csr* orc_assemble_ex(const orc_space* s, const double* lset_vertex, const or
 // to the owner's element matrix; the owners join the active elements.
 orc_csr* orc_assemble_bnd(const orc_space* s, const double* lset_vertex, const orc_term* terms, int nterms,
                           const orc_bterm* bterms, int nbterms, int nthreads, int dn_fd) {
+  return orc_assemble_full(s, lset_vertex, terms, nterms, bterms, nbterms, nullptr, 0, nthreads, dn_fd);
+}
+
+// ... and volume terms with a coefficient field (element_matrix_coef), whose
+// element sets join the active elements
+orc_csr* orc_assemble_full(const orc_space* s, const double* lset_vertex, const orc_term* terms, int nterms,
+                           const orc_bterm* bterms, int nbterms, const orc_cterm* cterms, int ncterms, int nthreads,
+                           int dn_fd) {
   const int ne = s->ne, n = s->nd, n2 = 2 * n;
   const int64_t nf = s->nfacets;
   // active elements: in the definedon set of some volume term; active facets:
@@ -1888,6 +1967,8 @@ orc_csr* orc_assemble_bnd(const orc_space* s, const double* lset_vertex, const o
     bool act = bnd_act[e] != 0;
     for (int t = 0; t < nterms && any_vol; t++)
       if (!facet_term(terms[t].kind) && (!terms[t].defined_on || test_bit(terms[t].defined_on, e))) act = true;
+    for (int t = 0; t < ncterms; t++)
+      if (!cterms[t].defined_on || test_bit(cterms[t].defined_on, e)) act = true;
     if (act) el_slot[e] = nact++;
   }
   int nfa = 0;
@@ -1906,6 +1987,8 @@ orc_csr* orc_assemble_bnd(const orc_space* s, const double* lset_vertex, const o
   parallel_for(nact, nthreads, [&](int64_t b, int64_t en) {
     for (int64_t i = b; i < en; i++) {
       int r = element_matrix(s, lset_vertex, terms, nterms, el_list[i], &elm[(size_t)i * n * n]);
+      if (!r && ncterms > 0)
+        r = element_matrix_coef(s, lset_vertex, cterms, ncterms, el_list[i], &elm[(size_t)i * n * n]);
       if (r) err = r;
     }
   });

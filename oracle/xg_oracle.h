@@ -160,6 +160,22 @@ typedef struct {
 } orc_bterm;
 orc_csr* orc_assemble_bnd(const orc_space* s, const double* lset_vertex, const orc_term* terms, int nterms,
                           const orc_bterm* bterms, int nbterms, int nthreads, int dn_fd);
+/* A volume term with a coefficient field: the integrand of kind (MASS,
+ * LAPLACE, NGRADU_V, U_NGRADV, CONV) times c h^hpow x^e gf(x), evaluated at
+ * the points of the straight cut rule; gf given per element in the
+ * element's basis order ([ne][ndof_el(D, gf_order)]), gf_order 0 = none. */
+typedef struct {
+  int kind, domain, order, hpow;
+  double coef;
+  double b[3];
+  int e[3];
+  int gf_order;
+  const double* gf_el;
+  const uint64_t* defined_on;
+} orc_cterm;
+orc_csr* orc_assemble_full(const orc_space* s, const double* lset_vertex, const orc_term* terms, int nterms,
+                           const orc_bterm* bterms, int nbterms, const orc_cterm* cterms, int ncterms, int nthreads,
+                           int dn_fd);
 /* orc_assemble with the normal-derivative mode of orc_facet_matrix. */
 orc_csr* orc_assemble_ex(const orc_space*, const double* lset_vertex, const orc_term* terms, int nterms,
                          int nthreads, int dn_fd);
