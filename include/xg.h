@@ -271,6 +271,12 @@ int xg_mlset_rule_capacity(int dim, int32_t nlsets, int32_t ndomains, int order)
  * interpolant.  threshold < 0: no clipping of the shifts.  d_result[0] =
  * integral of x^ex y^ey z^ez over the domain dt of the deformed mesh;
  * d_nonconv[0] = Newton searches that did not converge. */
+/* The deformation of xg_iso_integrate_mesh alone: d_gdef[edge][3] (edges in
+ * the mesh's edge numbering) = the physical edge coefficients J theta of the
+ * P2 shift, averaged over the band elements sharing the edge; 0 off the
+ * band.  For bilinear forms on the deformed mesh (xg_cterm.d_deform). */
+int xg_iso_deformation(xg_mesh* mesh, const double* d_p2vals, double threshold, double* d_gdef, int32_t* d_nonconv,
+                       void* stream);
 int xg_iso_integrate_mesh(xg_mesh* mesh, const double* d_p2vals, int dt, int order, double threshold, int deform,
                           int ex, int ey, int ez, double* d_result, int32_t* d_nonconv, void* stream);
 /* xg_integrate with the quadrilateral / hexahedral direction policy. */
@@ -371,6 +377,13 @@ typedef struct {
   const xg_space* gf_space;
   const double* d_gf;
   const uint64_t* d_defined_on;
+  /* the mesh deformation (xg_iso_deformation: [nedges][3] physical edge
+   * coefficients of the P2 shift) or NULL: with it the term is integrated on
+   * the deformed mesh (dCut(..., deformation=...)): the straight cut rule of
+   * the P1 level set on the reference element mapped by xhat + Theta(xhat),
+   * weights times |det(J A)| (IF: times |(J A)^-T n_ref|), gradients by
+   * (J A)^-T, h = |det(J A)|^(1/D) at the point, x the deformed point. */
+  const double* d_deform;
 } xg_cterm;
 /* Replace the form's coefficient terms (at most 8; nterms 0 removes them). */
 int xg_form_set_coef_terms(xg_form* form, const xg_cterm* terms, int32_t nterms);

@@ -28,7 +28,7 @@ EXPORTS = [
     "xg_cut_rules", "xg_base_rule_size", "xg_base_rule", "xg_integrate", "xg_integrate_noalloc", "xg_integrate_subdiv", "xg_subdiv_moments_tet",
     "xg_mesh_create_tensor", "xg_cut_rules_ex", "xg_quad_rule_capacity", "xg_integrate_ex",
     "xg_integrate_mlset", "xg_cut_rules_mlset", "xg_mlset_rule_capacity", "xg_mlset_mark",
-    "xg_iso_integrate_mesh", "xg_integrate_bnd",
+    "xg_iso_integrate_mesh", "xg_iso_deformation", "xg_integrate_bnd",
     "xg_mlset_form_create", "xg_mlset_form_assemble", "xg_form_create", "xg_form_destroy", "xg_form_set_defined_on", "xg_form_set_bnd_terms", "xg_form_set_coef_terms", "xg_form_capacity",
     "xg_form_assemble", "xg_form_check", "xg_form_stage_events", "xg_cutfem_step", "xg_cutfem_marking",
     "xg_space_create_st", "xg_space_info_st", "xg_cutinfo_update_st", "xg_st_cut_rules", "xg_st_form_create",
@@ -102,6 +102,7 @@ class CTerm(ctypes.Structure):
         ("gf_space", ctypes.c_void_p),
         ("d_gf", ctypes.c_void_p),
         ("d_defined_on", ctypes.c_void_p),
+        ("d_deform", ctypes.c_void_p),
     ]
 
 
@@ -175,6 +176,7 @@ def load():
         "xg_mlset_rule_capacity": (I, [I, ctypes.c_int32, ctypes.c_int32, I]),
         "xg_mlset_mark": (I, [P, P, ctypes.c_int32, P, ctypes.c_int32, I, P, P]),
         "xg_iso_integrate_mesh": (I, [P, P, I, I, ctypes.c_double, I, I, I, I, P, P, P]),
+        "xg_iso_deformation": (I, [P, P, ctypes.c_double, P, P, P]),
         "xg_integrate_bnd": (I, [P, P, I, I, I, I, I, P, P, P]),
         "xg_integrate_noalloc": (I, [P, P, I, I, I, I, I, P, P, P]),
         "xg_integrate_subdiv": (I, [P, P, I, I, I, I, I, I, P, P, P]),

@@ -3956,6 +3956,7 @@ int xg_form_set_coef_terms(xg_form* f, const xg_cterm* terms, int32_t nterms) {
     C.gf_dofs = g ? g->d_el_dofs : nullptr;
     C.gf = g ? T.d_gf : nullptr;
     C.defined_on = T.d_defined_on;
+    C.gdef = T.d_deform;
   }
   f->cdesc = d;
   return XG_OK;
@@ -4066,6 +4067,7 @@ CoefFormLaunch coef_args(xg_form* f, const double* d_lset, const uint8_t* d_dom)
   L.nv = m->nv;
   L.elv = m->d_elv;
   L.xyz = m->d_xyz;
+  L.el_edges = m->d_el_edges;
   L.lset = d_lset;
   L.dom = d_dom;
   L.d = f->cdesc;

@@ -17,6 +17,7 @@
 #include "xg_basis.cuh"
 #include "xg_cut.cuh"
 #include "xg_internal.h"
+#include "xg_isomesh.cuh"
 
 namespace xg {
 
@@ -118,7 +119,26 @@ __global__ void __launch_bounds__(128) k_coef_elmat(CoefFormLaunch L) {
         cg[a] = Tm.gf[Tm.gf_dofs[(int64_t)a * L.ne + e]];
         dg[a] = desc_rt<D>(kg, a, gv);
       }
-      auto point = [&](const double* xi, double w) {
+      // the deformation in the reference frame: theta_j = J^-1 gdef(edge j)
+      const bool deformed = Tm.gdef != nullptr;
+      double theta[6][3];
+      if (deformed) {
+        constexpr int NE = D == 2 ? 3 : 6;
+        for (int j = 0; j < NE; j++) {
+          const int ed = L.el_edges[(int64_t)j * L.ne + e];
+          for (int r = 0; r < 3; r++) {
+            double sr = 0.0;
+            if (r < D)
+              for (int k = 0; k < D; k++) sr += g.Finv[r][k] * Tm.gdef[(int64_t)ed * 3 + k];
+            theta[j][r] = sr;
+          }
+        }
+      }
+      // the integrand at reference point xi with weight W (physical measure
+      // included), physical barycentric gradients gp, unit normal np,
+      // physical point xp and the coefficient cp
+      auto point = [&](const double* xi, double W, const double (*gp)[D], const double* np, const double* xp,
+                       double cp) {
         double lam[D + 1], sl = 0.0;
         for (int k = 0; k < D; k++) {
           lam[k] = xi[k];
@@ -130,23 +150,16 @@ __global__ void __launch_bounds__(128) k_coef_elmat(CoefFormLaunch L) {
           f = 0.0;
           for (int a = 0; a < ng; a++) f += cg[a] * eval_fn_value<D, double>(dg[a], lam);
         }
-        if (Tm.e[0] | Tm.e[1] | Tm.e[2]) {
-          double x[3] = {0.0, 0.0, 0.0};
-          for (int r = 0; r < D; r++) {
-            double s = g.x0[r];
-            for (int k = 0; k < D; k++) s += g.F[r][k] * xi[k];
-            x[r] = s;
-          }
-          f *= cf_ipow(x[0], Tm.e[0]) * cf_ipow(x[1], Tm.e[1]) * (D == 3 ? cf_ipow(x[2], Tm.e[2]) : 1.0);
-        }
+        if (Tm.e[0] | Tm.e[1] | Tm.e[2])
+          f *= cf_ipow(xp[0], Tm.e[0]) * cf_ipow(xp[1], Tm.e[1]) * (D == 3 ? cf_ipow(xp[2], Tm.e[2]) : 1.0);
         double phi[N], gr[N][D], dn[N];
         for (int a = 0; a < N; a++) {
-          eval_fn<D, double>(desc[a], lam, gl, phi[a], gr[a]);
-          double s = 0.0;
-          for (int k = 0; k < D; k++) s += (Tm.kind == XG_TERM_CONV ? Tm.b[k] : nrm[k]) * gr[a][k];
-          dn[a] = s;
+          eval_fn<D, double>(desc[a], lam, gp, phi[a], gr[a]);
+          double sd = 0.0;
+          for (int k = 0; k < D; k++) sd += (Tm.kind == XG_TERM_CONV ? Tm.b[k] : np[k]) * gr[a][k];
+          dn[a] = sd;
         }
-        const double W = w * meas * c * f;
+        const double Wt = W * cp * f;
         for (int a = 0; a < N; a++)      // test
           for (int b = 0; b < N; b++) {  // trial
             double v;
@@ -160,13 +173,71 @@ __global__ void __launch_bounds__(128) k_coef_elmat(CoefFormLaunch L) {
               case XG_TERM_U_NGRADV: v = phi[b] * dn[a]; break;
               default: v = dn[b] * phi[a]; break;  // XG_TERM_NGRADU_V, XG_TERM_CONV
             }
-            A[a * N + b] += W * v;
+            A[a * N + b] += Wt * v;
           }
+      };
+      const double ifac = Tm.domain == XG_IF && cdom == XG_IF && !deformed ? if_factor<D>(g, l) : 1.0;
+      // rule point xi of the reference element with reference weight wr
+      auto ref_point = [&](const double* xi, double wr) {
+        if (!deformed) {
+          double xp[3] = {0.0, 0.0, 0.0};
+          for (int r = 0; r < D; r++) {
+            double sr = g.x0[r];
+            for (int k = 0; k < D; k++) sr += g.F[r][k] * xi[k];
+            xp[r] = sr;
+          }
+          point(xi, wr * meas * ifac, gl, nrm, xp, c);
+          return;
+        }
+        double y[3], Am[3][3], F[3][3], Fi[3][3], detF;
+        iso::deform_at<D>(theta, xi, y, Am);
+        for (int r = 0; r < 3; r++)
+          for (int k = 0; k < 3; k++) {
+            double sr = 0.0;
+            for (int q = 0; q < 3; q++) sr += (r < D && q < D ? g.F[r][q] : (r == q ? 1.0 : 0.0)) * Am[q][k];
+            F[r][k] = sr;
+          }
+        if (!iso::invert<D>(F, Fi, &detF)) {
+          set_err(L.err, XG_ERR_NONFINITE);
+          return;
+        }
+        const double adet = fabs(detF);
+        // physical gradients: Fi^T times the reference gradients
+        double gp[D + 1][D], np[D];
+        double nn2 = 0.0;
+        for (int k = 0; k < D; k++) {
+          double sa = 0.0, sn = 0.0;
+          for (int a = 0; a < D; a++) {
+            gp[a][k] = Fi[a][k];
+            sa += Fi[a][k];
+            sn += Fi[a][k] * (l[a] - l[D]);
+          }
+          gp[D][k] = -sa;
+          np[k] = sn;
+          nn2 += sn * sn;
+        }
+        const double inv = 1.0 / sqrt(nn2);
+        for (int k = 0; k < D; k++) np[k] *= inv;
+        double w = wr * adet;
+        if (Tm.domain == XG_IF) {
+          // |F^-T n_ref|, n_ref the unit reference gradient of the level set
+          double gr2 = 0.0;
+          for (int k = 0; k < D; k++) gr2 += (l[k] - l[D]) * (l[k] - l[D]);
+          w *= sqrt(nn2 / gr2);
+        }
+        double xp[3] = {0.0, 0.0, 0.0};
+        for (int r = 0; r < D; r++) {
+          double sr = g.x0[r];
+          for (int k = 0; k < D; k++) sr += g.F[r][k] * y[k];
+          xp[r] = sr;
+        }
+        const double cp = Tm.hpow == 0 ? Tm.coef : Tm.coef * int_pow(mesh_h<D>(adet), Tm.hpow);
+        point(xi, w, gp, np, xp, cp);
       };
       const int p = clamp_order(Tm.order);
       if (cdom != XG_IF) {
         const int off = g_cf_rules.off[D][p], cnt = g_cf_rules.cnt[D][p];
-        for (int q = 0; q < cnt; q++) point(g_cf_rules.x[off + q], g_cf_rules.w[off + q]);
+        for (int q = 0; q < cnt; q++) ref_point(g_cf_rules.x[off + q], g_cf_rules.w[off + q]);
         continue;
       }
       Sub subs[3];
@@ -177,15 +248,12 @@ __global__ void __launch_bounds__(128) k_coef_elmat(CoefFormLaunch L) {
       }
       const int sd = Tm.domain == XG_IF ? D - 1 : D;
       const int off = g_cf_rules.off[sd][p], cnt = g_cf_rules.cnt[sd][p];
-      const double fac = Tm.domain == XG_IF ? if_factor<D>(g, l) : 1.0;
       for (int s = 0; s < ns; s++) {
         const double trafofac = simplex_volume(subs[s].p, sd + 1);
         for (int q = 0; q < cnt; q++) {
           double pt[3];
           plain_point(subs[s], sd + 1, g_cf_rules.x[off + q], pt);
-          double w = g_cf_rules.w[off + q] * trafofac;
-          if (Tm.domain == XG_IF) w = w * fac;
-          point(pt, w);
+          ref_point(pt, g_cf_rules.w[off + q] * trafofac);
         }
       }
     }

@@ -265,6 +265,7 @@ struct CoefTermDev {
   const int32_t* gf_dofs;  // [nd_gf][ne] element dofs of its space
   const double* gf;        // its coefficients
   const uint64_t* defined_on;
+  const double* gdef;      // mesh deformation [nedges][3] (physical edge coefficients) or NULL
 };
 struct CoefDesc {
   int n;
@@ -275,6 +276,7 @@ struct CoefFormLaunch {
   int ne, nv;
   const int32_t* elv;
   const double* xyz;
+  const int32_t* el_edges; // [nedges per element][ne]
   const double* lset;      // P1 vertex values
   const uint8_t* dom;      // element domain types
   CoefDesc d;

@@ -160,6 +160,42 @@ static int iso_incidence(xg_mesh* m) {
   return XG_OK;
 }
 
+// the mesh-level deformation alone: d_gdef[edge][3] = the averaged physical
+// edge coefficients J theta of the band elements (0 elsewhere)
+extern "C" int xg_iso_deformation(xg_mesh* m, const double* d_p2vals, double threshold, double* d_gdef,
+                                  int32_t* d_nonconv, void* stream) {
+  if (!m || !d_p2vals || !d_gdef || !d_nonconv) return XG_ERR_ARG;
+  if (m->tensor) {
+    set_last_error("xg_iso_deformation: simplex meshes only");
+    return XG_ERR_UNSUPPORTED;
+  }
+  if (m->ne >= (1 << 28)) return XG_ERR_CAPACITY;
+  if (int st = iso_incidence(m)) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int nel = m->dim == 2 ? 3 : 6;
+  const size_t n_contrib = (size_t)m->ne * nel * 3;
+  const size_t need = sizeof(double) * n_contrib + (size_t)m->ne;
+  if (m->iso_bytes < need) {
+    cudaFree(m->d_iso);
+    m->d_iso = nullptr;
+    m->iso_bytes = 0;
+    XG_CUDA(cudaMalloc(&m->d_iso, need));
+    m->iso_bytes = need;
+  }
+  double* contrib = (double*)m->d_iso;
+  uint8_t* band = (uint8_t*)(contrib + n_contrib);
+  XG_CUDA(cudaMemsetAsync(d_nonconv, 0, sizeof(int32_t), s));
+  if (m->dim == 2)
+    k_iso_contrib<2><<<kIsoBlocks, kIsoThreads, 0, s>>>(m->ne, m->d_elv, m->d_xyz, m->nv, d_p2vals, threshold, contrib,
+                                                        band, d_nonconv, m->d_err);
+  else
+    k_iso_contrib<3><<<kIsoBlocks, kIsoThreads, 0, s>>>(m->ne, m->d_elv, m->d_xyz, m->nv, d_p2vals, threshold, contrib,
+                                                        band, d_nonconv, m->d_err);
+  k_iso_average<<<kIsoBlocks, kIsoThreads, 0, s>>>(m->nedges, nel, m->d_edge_ptr, m->d_edge_inc, contrib, band,
+                                                   d_gdef);
+  return iso_check("k_iso_deformation");
+}
+
 extern "C" int xg_iso_integrate_mesh(xg_mesh* m, const double* d_p2vals, int dt, int order, double threshold,
                                      int deform, int ex, int ey, int ez, double* d_result, int32_t* d_nonconv,
                                      void* stream) {

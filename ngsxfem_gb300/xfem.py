@@ -660,9 +660,14 @@ class _Measure:
             raise NotImplementedError("skeleton=True applies to dCut and dx")
         if self.skeleton and kind == "cut" and domain_type not in (NEG, POS):
             raise NotImplementedError("dCut(..., skeleton=True) on NEG or POS (codim-2 skeleton rules are not built)")
-        for k in ("deformation", "element_boundary", "element_vb"):
+        for k in ("element_boundary", "element_vb"):
             if kw.get(k) is not None and kw.get(k) is not False:
                 raise NotImplementedError("dCut/dFacetPatch option %r is not part of the GPU path" % k)
+        self.deformation = kw.get("deformation")
+        if self.deformation is not None:
+            if kind != "cut" or not isinstance(self.deformation, LevelSetMeshAdaptation):
+                raise NotImplementedError("deformation: dCut(..., deformation=LevelSetMeshAdaptation(..)"
+                                          ".CalcDeformation(..)) only (patch terms on the deformed mesh are not built)")
         self.definedon = kw.get("definedon")
         if self.definedon is not None and (kind != "cut" or kw.get("vb", VOL) != BND):
             raise NotImplementedError("definedon (a region of BND elements) applies to dCut(..., vb=BND)")
@@ -1054,8 +1059,11 @@ class BilinearForm:
             if it.measure.kind == "cut" and getattr(it.measure, "vb", VOL) == BND:
                 bterms += self._bnd_terms(it, lset)
                 continue
+            deform = getattr(it.measure, "deformation", None)
             for t in it.terms(lset):
-                (cterms if t.get("gf") is not None or any(t.get("e", (0, 0, 0))) else terms).append(t)
+                t["deform"] = deform
+                generic = t.get("gf") is not None or any(t.get("e", (0, 0, 0))) or deform is not None
+                (cterms if generic else terms).append(t)
         arr = (_lib.Term * max(len(terms), 1))()
         self._keep = []
         for k, t in enumerate(terms):
@@ -1105,6 +1113,10 @@ class BilinearForm:
                 if d is not None:
                     self._keep.append(d)
                 carr[k].d_defined_on = d.words.data_ptr() if d is not None else None
+                if t.get("deform") is not None:
+                    gd = t["deform"]._edge_deformation()
+                    self._keep.append(gd)
+                    carr[k].d_deform = gd.data_ptr()
             _lib.call("xg_form_set_coef_terms", h, carr, len(cterms))
             self._cterms = cterms
         cap = np.zeros(2, dtype=np.int64)
@@ -1473,7 +1485,42 @@ class LevelSetMeshAdaptation:
             raise ValueError("P2 element values of shape (ne, %d) on a simplex mesh expected"
                              % ((D + 1) * (D + 2) // 2))
         self.p2 = torch.from_numpy(np.ascontiguousarray(vals)).to(_dev())
+        self._gdef = None
         return self
+
+    def _edge_deformation(self):
+        """[nedges][3] physical edge coefficients of the deformation
+        (xg_iso_deformation), computed once per CalcDeformation."""
+        if self.p2 is None:
+            raise RuntimeError("CalcDeformation first")
+        if getattr(self, "_gdef", None) is None:
+            dm = device_mesh(self.mesh)
+            info = np.zeros(8, dtype=np.int64)
+            _lib.call("xg_mesh_info", dm.h, info.ctypes.data_as(ctypes.c_void_p))
+            gd = torch.zeros((int(info[3]), 3), dtype=torch.float64, device=_dev())
+            nc = torch.zeros(1, dtype=torch.int32, device=_dev())
+            _lib.call("xg_iso_deformation", dm.h, _vp(self.p2), ctypes.c_double(self.threshold), _vp(gd), _vp(nc),
+                      _stream())
+            dm.check()
+            self.nonconverged = int(nc.item())
+            self._gdef = gd
+        return self._gdef
+
+    @property
+    def lset_p1(self):
+        """The P1 level set of the deformed-mesh forms: the P2 level set's
+        vertex values with the |v| < 1e-14 -> 1e-14 perturbation."""
+        if self.p2 is None:
+            raise RuntimeError("CalcDeformation first")
+        D = self.mesh.dim
+        vals = np.zeros(self.mesh.nv)
+        p2 = self.p2.cpu().numpy()
+        for i in range(D + 1):
+            vals[self.mesh.elements[:, i]] = p2[:, i]
+        vals = np.where(np.abs(vals) < 1e-14, 1e-14, vals)
+        g = GridFunction(H1(self.mesh, order=1))
+        g.vec.copy_(torch.from_numpy(vals))
+        return g
 
     def Integrate(self, domain_type, cf=None, order=4, deform=True):
         if self.p2 is None:

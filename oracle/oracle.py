@@ -52,6 +52,7 @@ class CTerm(ctypes.Structure):
         ("gf_order", ctypes.c_int),
         ("gf_el", ctypes.c_void_p),
         ("defined_on", ctypes.c_void_p),
+        ("theta_el", ctypes.c_void_p),
     ]
 
 
@@ -159,6 +160,7 @@ def lib():
         L.orc_iso_integrate_mesh.restype = ctypes.c_double
         L.orc_iso_integrate_mesh.argtypes = [ctypes.c_int, ctypes.c_int, P, ctypes.c_int, P, P, ctypes.c_int,
                                              ctypes.c_int, ctypes.c_double, ctypes.c_int, P]
+        L.orc_iso_theta_mesh.argtypes = [ctypes.c_int, ctypes.c_int, P, ctypes.c_int, P, P, ctypes.c_double, P, P]
         L.orc_boundary_elements.argtypes = [P, P, P]
         L.orc_cutinfo_bnd.argtypes = [P, P, P, P, P]
         L.orc_cutinfo_nodes.argtypes = [P, P, P, P, P, P, P, P, P, P, P]
@@ -432,6 +434,19 @@ def iso_integrate_mesh(mesh, p2vals, dt, order, threshold=-1.0, deform=True):
     r = lib().orc_iso_integrate_mesh(mesh.dim, mesh.nv, _p(mesh.coords), mesh.ne, _p(mesh.elements), _p(v), dt, order,
                                      threshold, int(deform), ctypes.byref(nc))
     return r, nc.value
+
+
+def iso_theta_mesh(mesh, p2vals, threshold=-1.0):
+    """The mesh-level deformation per element: (ne, 6, 3) edge coefficients in
+    each element's reference frame, and the count of non-converged searches."""
+    v = np.ascontiguousarray(p2vals, dtype=np.float64)
+    out = np.zeros((mesh.ne, 6, 3))
+    nc = ctypes.c_int(0)
+    r = lib().orc_iso_theta_mesh(mesh.dim, mesh.nv, _p(mesh.coords), mesh.ne, _p(mesh.elements), _p(v), threshold,
+                                 _p(out), ctypes.byref(nc))
+    if r:
+        raise RuntimeError("oracle deformation error %d" % r)
+    return out, nc.value
 
 
 def p2_nodal_values(mesh, f):
@@ -756,6 +771,11 @@ class Space:
                 d = np.ascontiguousarray(d, dtype=np.uint64)
                 keep.append(d)
             carr[i].defined_on = d.ctypes.data if d is not None else None
+            th = t.get("theta_el")
+            if th is not None:
+                th = np.ascontiguousarray(th, dtype=np.float64)
+                keep.append(th)
+            carr[i].theta_el = th.ctypes.data if th is not None else None
         c = lib().orc_assemble_full(self.h, _p(l), ctypes.cast(arr, ctypes.c_void_p), len(terms),
                                     ctypes.cast(barr, ctypes.c_void_p), len(bterms),
                                     ctypes.cast(carr, ctypes.c_void_p), len(cterms), nthreads, int(dn_fd))

@@ -852,7 +852,15 @@ int element_matrix_coef(const orc_space* s, const double* lset_vertex, const orc
     const orc_cterm& T = terms[t];
     if (T.defined_on && !test_bit(T.defined_on, e)) continue;
     const int order = T.order >= 0 ? T.order : default_order(T.kind, s->k);
-    const int np = straight_cut_rule(g, l, T.domain, order, pts, wts);
+    // on the deformed mesh: the rule of the reference element (its weights
+    // in reference measure), mapped point by point
+    const double* th = T.theta_el ? T.theta_el + (size_t)e * 18 : nullptr;
+    Geo gref;
+    if (th) {
+      const double ref2[6] = {1, 0, 0, 1, 0, 0}, ref3[12] = {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0};
+      make_geo(D, D == 2 ? ref2 : ref3, gref);
+    }
+    const int np = straight_cut_rule(th ? gref : g, l, T.domain, order, pts, wts);
     if (np < -1) return np;
     if (np <= 0) continue;
     double c = T.coef;
@@ -864,25 +872,77 @@ int element_matrix_coef(const orc_space* s, const double* lset_vertex, const orc
     for (int q = 0; q < np; q++) {
       const double* xi = &pts[3 * q];
       basis(D, s->k, gv, xi, phi, dphi);
-      for (int i = 0; i < n; i++) phys_grad(g, dphi[i], gphys[i]);
+      double wq = wts[q] * meas, cq = c, xq[3] = {0, 0, 0};
+      const double* bnq = nrm;
+      double nq[3] = {0, 0, 0};
+      if (!th) {
+        for (int i = 0; i < n; i++) phys_grad(g, dphi[i], gphys[i]);
+        for (int r = 0; r < D; r++) {
+          double acc = g.x0[r];
+          for (int k = 0; k < D; k++) acc += g.F[r][k] * xi[k];
+          xq[r] = acc;
+        }
+      } else {
+        // y = xi + Theta(xi), A = I + grad Theta (edge shapes lambda_a lambda_b), F = J A
+        double lam[4], sl = 0.0;
+        for (int k = 0; k < D; k++) {
+          lam[k] = xi[k];
+          sl += xi[k];
+        }
+        lam[D] = 1.0 - sl;
+        double y[3] = {xi[0], xi[1], D == 3 ? xi[2] : 0.0}, Am[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+        const int E2[3][2] = {{0, 1}, {0, 2}, {1, 2}}, E3[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+        for (int j = 0; j < (D == 2 ? 3 : 6); j++) {
+          const int a = D == 2 ? E2[j][0] : E3[j][0], b = D == 2 ? E2[j][1] : E3[j][1];
+          const double ph = lam[a] * lam[b];
+          double dph[3];
+          for (int k = 0; k < D; k++) {
+            const double da = a < D ? (a == k ? 1.0 : 0.0) : -1.0, db = b < D ? (b == k ? 1.0 : 0.0) : -1.0;
+            dph[k] = da * lam[b] + lam[a] * db;
+          }
+          for (int r = 0; r < D; r++) {
+            y[r] += th[j * 3 + r] * ph;
+            for (int k = 0; k < D; k++) Am[r][k] += th[j * 3 + r] * dph[k];
+          }
+        }
+        double elc[12];
+        Geo gd;  // the point's Jacobian F = J A as an element map (for its inverse and determinant)
+        {
+          double F[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+          for (int r = 0; r < D; r++)
+            for (int k = 0; k < D; k++)
+              for (int q2 = 0; q2 < D; q2++) F[r][k] += g.F[r][q2] * Am[q2][k];
+          for (int v = 0; v <= D; v++)
+            for (int r = 0; r < D; r++) elc[v * D + r] = v < D ? F[r][v] : 0.0;
+          make_geo(D, elc, gd);
+        }
+        for (int i = 0; i < n; i++) phys_grad(gd, dphi[i], gphys[i]);
+        double gr[3] = {0, 0, 0}, gp[3];
+        for (int k = 0; k < D; k++) gr[k] = l[k] - l[D];
+        phys_grad(gd, gr, gp);
+        const double gpn = l2norm3(gp), grn = l2norm3(gr);
+        for (int r = 0; r < 3; r++) nq[r] = gp[r] / gpn;
+        bnq = nq;
+        wq = wts[q] * std::fabs(gd.det);
+        if (T.domain == ORC_IF) wq *= gpn / grn;
+        if (T.hpow != 0) cq = T.coef * std::pow(std::pow(std::fabs(gd.det), 1.0 / D), (double)T.hpow);
+        for (int r = 0; r < D; r++) {
+          double acc = g.x0[r];
+          for (int k = 0; k < D; k++) acc += g.F[r][k] * y[k];
+          xq[r] = acc;
+        }
+      }
       double f = 1.0;
       if (ng > 0) {
         basis(D, T.gf_order, gv, xi, phig, dphig);
         f = 0.0;
         for (int i = 0; i < ng; i++) f += T.gf_el[(size_t)e * ng + i] * phig[i];
       }
-      if (T.e[0] || T.e[1] || T.e[2]) {
-        double x[3] = {0, 0, 0};
-        for (int r = 0; r < D; r++) {
-          double acc = g.x0[r];
-          for (int k = 0; k < D; k++) acc += g.F[r][k] * xi[k];
-          x[r] = acc;
-        }
+      if (T.e[0] || T.e[1] || T.e[2])
         for (int r = 0; r < 3; r++)
-          for (int p = 0; p < T.e[r]; p++) f *= x[r];
-      }
-      const double w = wts[q] * meas * c * f;
-      const double* bb = T.kind == ORC_TERM_CONV ? T.b : nrm;
+          for (int p = 0; p < T.e[r]; p++) f *= xq[r];
+      const double w = wq * cq * f;
+      const double* bb = T.kind == ORC_TERM_CONV ? T.b : bnq;
       for (int i = 0; i < n; i++)      // test
         for (int j = 0; j < n; j++) {  // trial
           double v;

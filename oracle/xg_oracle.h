@@ -172,6 +172,7 @@ typedef struct {
   int gf_order;
   const double* gf_el;
   const uint64_t* defined_on;
+  const double* theta_el; /* [ne][6][3] deformation (orc_iso_theta_mesh) or NULL: the term on the deformed mesh */
 } orc_cterm;
 orc_csr* orc_assemble_full(const orc_space* s, const double* lset_vertex, const orc_term* terms, int nterms,
                            const orc_bterm* bterms, int nbterms, const orc_cterm* cterms, int ncterms, int nthreads,
@@ -224,6 +225,11 @@ int orc_iso_cut_rule(int D, const double* elc, const double* p2vals, int dt, int
  * deformed), as Integrate(levelset_domain, cf=1, order) after
  * mesh.SetDeformation(CalcDeformation(lset_ho)).  p2vals: ne x nnodes per
  * element (element-local node order above). */
+/* The mesh-level deformation of orc_iso_integrate_mesh per element: theta_out
+ * [ne][6][3] = the averaged edge coefficients in each element's reference
+ * frame (edges (0,1),(0,2),(1,2) / the six tet edges, unused rows 0). */
+int orc_iso_theta_mesh(int D, int nv, const double* coords, int ne, const int32_t* elv, const double* p2vals,
+                       double threshold, double* theta_out, int* nonconv);
 double orc_iso_integrate_mesh(int D, int nv, const double* coords, int ne, const int32_t* elv, const double* p2vals,
                               int dt, int order, double threshold, int deform, int* nonconv);
 /* NEG-part moments (35, degree <= 4, graded order) of the reference tet for n

@@ -478,6 +478,64 @@ int orc_iso_moments_tet(int64_t n, const double* vals10, int order, int deform, 
   return 0;
 }
 
+int orc_iso_theta_mesh(int D, int nv, const double* coords, int ne, const int32_t* elv, const double* p2vals,
+                       double threshold, double* theta_out, int* nonconv) {
+  // the averaging of orc_iso_integrate_mesh, each element's edge
+  // coefficients returned in its reference frame
+  (void)nv;
+  const int nn = (D + 1) * (D + 2) / 2, nle = nedges(D);
+  const int (*E)[2] = edges(D);
+  std::vector<uint64_t> keys((size_t)ne * nle);
+  for (int e = 0; e < ne; e++)
+    for (int j = 0; j < nle; j++) {
+      uint64_t a = (uint32_t)elv[e * (D + 1) + E[j][0]], b = (uint32_t)elv[e * (D + 1) + E[j][1]];
+      if (a > b) std::swap(a, b);
+      keys[(size_t)e * nle + j] = (a << 32) | b;
+    }
+  std::vector<uint64_t> uk(keys);
+  std::sort(uk.begin(), uk.end());
+  uk.erase(std::unique(uk.begin(), uk.end()), uk.end());
+  std::vector<int32_t> eid(keys.size());
+  for (size_t i = 0; i < keys.size(); i++) eid[i] = (int32_t)(std::lower_bound(uk.begin(), uk.end(), keys[i]) - uk.begin());
+  std::vector<double> gdef(uk.size() * 3, 0.0), fac(uk.size(), 0.0);
+  std::vector<Affine> aff(ne);
+  int nc = 0;
+  for (int e = 0; e < ne; e++) {
+    double elc[12];
+    for (int i = 0; i <= D; i++)
+      for (int r = 0; r < D; r++) elc[i * D + r] = coords[(size_t)elv[e * (D + 1) + i] * D + r];
+    if (!make_affine(D, elc, aff[e])) return -2;
+    double p1[4];
+    perturbed_p1(D, p2vals + (size_t)e * nn, p1);
+    double theta[6][3];
+    if (!deformation(D, aff[e], p2vals + (size_t)e * nn, p1, threshold, theta, &nc)) continue;
+    for (int j = 0; j < nle; j++) {
+      const int g = eid[(size_t)e * nle + j];
+      for (int r = 0; r < D; r++) {
+        double acc = 0.0;
+        for (int c = 0; c < D; c++) acc += aff[e].J[r][c] * theta[j][c];
+        gdef[(size_t)g * 3 + r] += acc;
+      }
+      fac[g] += 1.0;
+    }
+  }
+  for (size_t g = 0; g < uk.size(); g++)
+    if (fac[g] > 0)
+      for (int r = 0; r < 3; r++) gdef[g * 3 + r] /= fac[g];
+  for (int e = 0; e < ne; e++)
+    for (int j = 0; j < 6; j++)
+      for (int r = 0; r < 3; r++) {
+        double acc = 0.0;
+        if (j < nle && r < D) {
+          const int g = eid[(size_t)e * nle + j];
+          for (int c = 0; c < D; c++) acc += aff[e].Ji[r][c] * gdef[(size_t)g * 3 + c];
+        }
+        theta_out[((size_t)e * 6 + j) * 3 + r] = acc;
+      }
+  if (nonconv) *nonconv = nc;
+  return 0;
+}
+
 double orc_iso_integrate_mesh(int D, int nv, const double* coords, int ne, const int32_t* elv, const double* p2vals,
                               int dt, int order, double threshold, int deform, int* nonconv) {
   // ProjectShift over the band elements (projshift.cpp:58-135): element
