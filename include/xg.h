@@ -408,6 +408,25 @@ typedef struct {
   int64_t cap_nnz;
 } xg_csr;
 
+/* Bilinear forms of the Q1 space (dofs = the mesh's vertices) on a
+ * quadrilateral / hexahedral mesh (xg_mesh_create_tensor): SymbolicCutBFI on
+ * ET_QUAD / ET_HEX (xfem/symboliccutbfi.cpp:76-486) with the quad branch of
+ * StraightCutIntegrationRule (cutint/straightcutrule.cpp:206-501, 582-677;
+ * policy: XG_QUAD_FIRST_ALLOWED / _FIND_OPTIMAL / _ALWAYS_NONE).  Terms (xg_term):
+ * MASS, LAPLACE, NGRADU_V / U_NGRADV (normal: the unit gradient of the
+ * multilinear level set at the point), CONV, on NEG / POS / IF; order -1 = 2
+ * (trial + test order); h = |det J|^(1/D) at the point.  An element is active
+ * for a term if it is in the term's set and its domain type is the term's
+ * domain or IF.  Output as xg_form_assemble (xg_csr over the active vertices,
+ * ascending), values summed in a fixed order.  Device errors go to the mesh's
+ * error word (xg_mesh_check). */
+typedef struct xg_quad_form xg_quad_form;
+int xg_quad_form_create(xg_mesh* mesh, const xg_term* terms, int32_t nterms, int policy, xg_quad_form** out);
+int xg_quad_form_destroy(xg_quad_form* form);
+/* out: [rows, nnz] sufficient for every level set (all elements active). */
+int xg_quad_form_capacity(const xg_quad_form* form, int64_t* out2);
+int xg_quad_form_assemble(xg_quad_form* form, const double* d_lset, xg_csr* out, void* stream);
+
 /* out: [cap_rows, cap_nnz] sufficient for any level set on this mesh. */
 int xg_form_capacity(const xg_form* form, int64_t* h_out2);
 

@@ -39,6 +39,7 @@ UNITS = [
     ("xg_mlform.cu", []),
     ("xg_bform.cu", []),
     ("xg_cform.cu", []),
+    ("xg_qform.cu", []),
 ]
 
 

@@ -36,6 +36,7 @@ int ensure_device_rules() {
   if (!st) st = upload_rules_mlform();
   if (!st) st = upload_rules_bform();
   if (!st) st = upload_rules_cform();
+  if (!st) st = upload_rules_qform();
   if (st) return st;
   done.push_back(dev);
   return XG_OK;

@@ -294,6 +294,7 @@ struct CoefFormLaunch {
 int coef_active_launch(const CoefFormLaunch& a, cudaStream_t s);
 int coef_elmat_launch(const CoefFormLaunch& a, cudaStream_t s);
 int upload_rules_cform();
+int upload_rules_qform();  // xg_qform.cu
 int bnd_active_launch(const BndFormLaunch& a, cudaStream_t s);
 int bnd_elmat_launch(const BndFormLaunch& a, cudaStream_t s);
 int upload_rules_bform();

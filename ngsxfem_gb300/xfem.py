@@ -1048,9 +1048,49 @@ class BilinearForm:
         _lib.call("xg_form_capacity", h, cap.ctypes.data_as(ctypes.c_void_p))
         self._alloc(int(cap[0]), int(cap[1]))
 
+    def _build_quad(self, lset):
+        """Q1 form on a quadrilateral / hexahedral mesh (xg_quad_form_create):
+        volume terms of the menu, no facet or boundary terms."""
+        terms = []
+        for it in self.integrals:
+            m = it.measure
+            if m.kind != "cut" or getattr(m, "vb", VOL) == BND or m.skeleton or \
+                    getattr(m, "deformation", None) is not None:
+                raise NotImplementedError("forms on quadrilateral / hexahedral meshes take dCut volume terms")
+            for t in it.terms(lset):
+                if t["kind"] not in (TERM_MASS, TERM_LAPLACE, TERM_NGRADU_V, TERM_U_NGRADV, TERM_CONV) or \
+                        t.get("tb") is not None or t.get("gf") is not None or any(t.get("e", (0, 0, 0))):
+                    raise NotImplementedError("quad / hex forms: mass, Laplace, Nitsche and convection terms")
+                terms.append(t)
+        pols = {it.measure.quad_dir_policy for it in self.integrals}
+        if len(pols) > 1:
+            raise NotImplementedError("one quad_dir_policy per form")
+        arr = (_lib.Term * max(len(terms), 1))()
+        self._keep = []
+        for k, t in enumerate(terms):
+            arr[k].kind, arr[k].domain, arr[k].order, arr[k].hpow = t["kind"], t["domain"], t["order"], t["hpow"]
+            arr[k].coef = t["coef"]
+            for j in range(3):
+                arr[k].b[j] = t["b"][j]
+            d = t["defined_on"]
+            if d is not None:
+                self._keep.append(d)
+            arr[k].d_defined_on = d.words.data_ptr() if d is not None else None
+        h = ctypes.c_void_p()
+        _lib.call("xg_quad_form_create", device_mesh(self.space.mesh).h, arr, len(terms), pols.pop(),
+                  ctypes.byref(h))
+        self._form = h
+        self._quad = True
+        self._terms = terms
+        cap = np.zeros(2, dtype=np.int64)
+        _lib.call("xg_quad_form_capacity", h, cap.ctypes.data_as(ctypes.c_void_p))
+        self._alloc(int(cap[0]), int(cap[1]))
+
     def _build(self):
         if isinstance(self.space, SpaceTimeFESpace):
             return self._build_st()
+        if getattr(self.space.mesh, "tensor", False):
+            return self._build_quad(self._levelset())
         lset = self._levelset()
         if isinstance(lset, (tuple, list)):
             return self._build_ml(lset)
@@ -1159,6 +1199,14 @@ class BilinearForm:
         if self._form is None:
             self._build()
         lset = self._levelset()
+        if getattr(self, "_quad", False):
+            dm = device_mesh(self.space.mesh)
+            _lib.call("xg_quad_form_assemble", self._form, _vp(_lset_vec(lset)), ctypes.byref(self._csr), _stream())
+            torch.cuda.synchronize()
+            dm.check()
+            nrows, nnz = (int(x) for x in self._counts.cpu().tolist())
+            self.mat = SparseMatrix(self.space.ndof, self._row_dof, self._rowptr, self._cols, self._vals, nrows, nnz)
+            return self
         if isinstance(lset, (tuple, list)):
             nv = lset[0].space.mesh.nv
             vals = torch.stack([_lset_vec(g)[:nv] for g in lset]).contiguous()
@@ -1191,7 +1239,10 @@ class BilinearForm:
 
     def __del__(self):
         if getattr(self, "_form", None) and _lib._lib is not None:
-            _lib.load().xg_form_destroy(self._form)
+            if getattr(self, "_quad", False):
+                _lib.load().xg_quad_form_destroy(self._form)
+            else:
+                _lib.load().xg_form_destroy(self._form)
             self._form = None
 
 

@@ -160,6 +160,9 @@ def lib():
         L.orc_iso_integrate_mesh.restype = ctypes.c_double
         L.orc_iso_integrate_mesh.argtypes = [ctypes.c_int, ctypes.c_int, P, ctypes.c_int, P, P, ctypes.c_int,
                                              ctypes.c_int, ctypes.c_double, ctypes.c_int, P]
+        L.orc_quad_assemble.restype = P
+        L.orc_quad_assemble.argtypes = [ctypes.c_int, ctypes.c_int, P, ctypes.c_int, P, P, P, ctypes.c_int,
+                                        ctypes.c_int, ctypes.c_int, P]
         L.orc_iso_theta_mesh.argtypes = [ctypes.c_int, ctypes.c_int, P, ctypes.c_int, P, P, ctypes.c_double, P, P]
         L.orc_boundary_elements.argtypes = [P, P, P]
         L.orc_cutinfo_bnd.argtypes = [P, P, P, P, P]
@@ -434,6 +437,23 @@ def iso_integrate_mesh(mesh, p2vals, dt, order, threshold=-1.0, deform=True):
     r = lib().orc_iso_integrate_mesh(mesh.dim, mesh.nv, _p(mesh.coords), mesh.ne, _p(mesh.elements), _p(v), dt, order,
                                      threshold, int(deform), ctypes.byref(nc))
     return r, nc.value
+
+
+def quad_assemble(mesh, lset, terms, policy=1, nthreads=1):
+    """Bilinear form of the Q1 space on a quad / hex mesh (orc_quad_assemble):
+    CSR triple over the mesh's vertices and the first rule error (0: none)."""
+    arr, keep = Space._terms(terms)
+    l = np.ascontiguousarray(lset, dtype=np.float64)
+    st = ctypes.c_int(0)
+    c = lib().orc_quad_assemble(mesh.dim, mesh.nv, _p(mesh.coords), mesh.ne, _p(mesh.elements), _p(l),
+                                ctypes.cast(arr, ctypes.c_void_p), len(terms), policy, nthreads, ctypes.byref(st))
+    nnz = lib().orc_csr_nnz(c)
+    rowptr = np.zeros(mesh.nv + 1, dtype=np.int64)
+    cols = np.zeros(nnz, dtype=np.int32)
+    vals = np.zeros(nnz)
+    lib().orc_csr_get(c, _p(rowptr), _p(cols), _p(vals))
+    lib().orc_csr_destroy(c)
+    return (rowptr, cols, vals), st.value
 
 
 def iso_theta_mesh(mesh, p2vals, threshold=-1.0):

@@ -1878,6 +1878,24 @@ int orc_facet_matrix(const orc_space* s, const double* lset_vertex, const orc_te
 
 int orc_fd_stencil(int k, int acc, double* c, double* eps) { return fd_stencil(k, acc, c, eps); }
 
+// CSR over ndof dofs from element matrices alone (no facets): el_dofs
+// [ne][n], el_slot[e] the element's matrix in elm or -1; per dof its
+// elements ascending (the gather of gather_csr).
+orc_csr* orc_csr_from_elements(int64_t ndof, int n, int ne, const int32_t* el_dofs, const int32_t* el_slot,
+                               const double* elm, int64_t nslots, int nthreads) {
+  std::vector<int32_t> dofs(el_dofs, el_dofs + (size_t)ne * n), slot(el_slot, el_slot + ne);
+  std::vector<int64_t> ptr(ndof + 1, 0);
+  for (int32_t d : dofs) ptr[d + 1]++;
+  for (int64_t r = 0; r < ndof; r++) ptr[r + 1] += ptr[r];
+  std::vector<int32_t> adj(dofs.size());
+  std::vector<int64_t> fill(ptr.begin(), ptr.end() - 1);
+  for (int e = 0; e < ne; e++)
+    for (int i = 0; i < n; i++) adj[fill[dofs[(size_t)e * n + i]]++] = e * 32 + i;
+  std::vector<double> m(elm, elm + (size_t)nslots * n * n), none;
+  std::vector<int32_t> nof;
+  return gather_csr(ndof, n, dofs, ptr, adj, 0, nof, nof, slot, m, nof, none, nthreads);
+}
+
 orc_csr* orc_assemble(const orc_space* s, const double* lset_vertex, const orc_term* terms, int nterms,
                       int nthreads) {
   return orc_assemble_bnd(s, lset_vertex, terms, nterms, nullptr, 0, nthreads, 0);

@@ -274,6 +274,20 @@ int orc_quad_straight_cut_rule(int D, const double* xv, const double* lset_vals,
 /* CutInfo.Update on a quad / hex mesh: dom, ratio, bits[8][ceil(ne/64)] as orc_cutinfo. */
 int orc_quad_cutinfo(int D, int nv, const double* coords, int ne, const int32_t* elv, const double* lset, int policy,
                      uint8_t* dom, double* ratio, uint64_t* bits);
+/* Bilinear form on a quad / hex mesh with the Q1 space (dofs = vertices):
+ * SymbolicCutBFI on ET_QUAD / ET_HEX (xfem/symboliccutbfi.cpp:76-486), the
+ * rule of StraightCutIntegrationRule for quads (straightcutrule.cpp:582-677),
+ * terms of kind MASS, LAPLACE, NGRADU_V, U_NGRADV (normal: the pointwise
+ * unit gradient of the multilinear level set), CONV; default order 2 (trial +
+ * test order, no derivative reduction on quads); h = |det J|^(1/D) at the
+ * point.  An element is active for a term if it is in the term's set and its
+ * domain type is the term's domain or IF.  CSR over all nv dofs. */
+orc_csr* orc_quad_assemble(int D, int nv, const double* coords, int ne, const int32_t* elv, const double* lset,
+                           const orc_term* terms, int nterms, int policy, int nthreads, int* status);
+/* CSR from element matrices alone (el_slot[e] < 0: inactive), per dof its
+ * elements ascending. */
+orc_csr* orc_csr_from_elements(int64_t ndof, int n, int ne, const int32_t* el_dofs, const int32_t* el_slot,
+                               const double* elm, int64_t nslots, int nthreads);
 /* Integrate(x^ex y^ey z^ez * dCut) on a quad / hex mesh: coords[nv][D], elv[ne][2^D]. */
 double orc_quad_integrate(int D, int nv, const double* coords, int ne, const int32_t* elv, const double* lset,
                           int dt, int order, int policy, int ex, int ey, int ez, int* status);

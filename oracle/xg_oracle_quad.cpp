@@ -744,6 +744,98 @@ static double quad_integrate_range(int D, const double* coords, const int32_t* e
   return sum;
 }
 
+orc_csr* orc_quad_assemble(int D, int nv, const double* coords, int ne, const int32_t* elv, const double* lset,
+                           const orc_term* terms, int nterms, int policy, int nthreads, int* status) {
+  const int nve = D == 2 ? 4 : 8;
+  static const int cx[8] = {0, 1, 1, 0, 0, 1, 1, 0}, cy[8] = {0, 0, 1, 1, 0, 0, 1, 1}, cz[8] = {0, 0, 0, 0, 1, 1, 1, 1};
+  std::vector<int32_t> slot(ne, -1);
+  std::vector<double> elm;
+  int st = 0, nact = 0;
+  for (int e = 0; e < ne; e++) {
+    double xv[8 * 3] = {0}, lv[8];
+    for (int v = 0; v < nve; v++) {
+      const int id = elv[(size_t)e * nve + v];
+      lv[v] = lset[id];
+      for (int i = 0; i < D; i++) xv[3 * v + i] = coords[(size_t)id * D + i];
+    }
+    const std::vector<double> lvec(lv, lv + nve);
+    const int dom = check_cut(lvec);
+    auto on = [&](const orc_term& T) {
+      if (T.defined_on && !((T.defined_on[e >> 6] >> (e & 63)) & 1u)) return false;
+      return dom == IF || dom == T.domain;
+    };
+    bool any = false;
+    for (int t = 0; t < nterms; t++) any |= on(terms[t]);
+    if (!any) continue;
+    slot[e] = nact++;
+    elm.resize((size_t)nact * nve * nve, 0.0);
+    double* A = &elm[(size_t)slot[e] * nve * nve];
+    Lset l(lvec, nve);
+    for (int t = 0; t < nterms; t++) {
+      const orc_term& T = terms[t];
+      if (!on(T)) continue;
+      IR ir;
+      const int n = quad_rule_untrafo(D, lv, T.domain, T.order >= 0 ? T.order : 2, policy, ir);
+      if (n < -1) {
+        if (!st) st = -n - 1;
+        continue;
+      }
+      for (int q = 0; q < n; q++) {
+        double x[3], J[3][3], Ji[3][3];
+        tp_map(D, xv, ir.p[q], x, J);
+        const double det = det_inv(D, J, Ji), adet = std::fabs(det);
+        double w = ir.w[q] * adet;
+        if (dom == IF && T.domain == IF) w *= if_weight_factor(D, l, ir.p[q], Ji);
+        double c = T.coef;
+        if (T.hpow != 0) c *= std::pow(std::pow(adet, 1.0 / D), (double)T.hpow);
+        // Q1 shapes and physical gradients (grad_x = J^-T grad_xi)
+        double N[8], G[8][3];
+        const double* p = ir.p[q].x;
+        for (int v = 0; v < nve; v++) {
+          const double fx = cx[v] ? p[0] : 1 - p[0], gx = cx[v] ? 1.0 : -1.0;
+          const double fy = cy[v] ? p[1] : 1 - p[1], gy = cy[v] ? 1.0 : -1.0;
+          const double fz = D == 3 ? (cz[v] ? p[2] : 1 - p[2]) : 1.0, gz = cz[v] ? 1.0 : -1.0;
+          N[v] = fx * fy * fz;
+          const double dN[3] = {gx * fy * fz, fx * gy * fz, fx * fy * gz};
+          for (int k = 0; k < 3; k++) {
+            double acc = 0.0;
+            if (k < D)
+              for (int j = 0; j < D; j++) acc += Ji[j][k] * dN[j];
+            G[v][k] = acc;
+          }
+        }
+        double nrm[3] = {0, 0, 0};
+        if (T.kind == ORC_TERM_NGRADU_V || T.kind == ORC_TERM_U_NGRADV) {
+          const V3 g = l.grad(ir.p[q]);
+          double nn = 0.0;
+          for (int k = 0; k < D; k++) {
+            double acc = 0.0;
+            for (int j = 0; j < D; j++) acc += Ji[j][k] * g.x[j];
+            nrm[k] = acc;
+            nn += acc * acc;
+          }
+          nn = std::sqrt(nn);
+          for (int k = 0; k < D; k++) nrm[k] /= nn;
+        }
+        const double* bb = T.kind == ORC_TERM_CONV ? T.b : nrm;
+        for (int a = 0; a < nve; a++)      // test
+          for (int b = 0; b < nve; b++) {  // trial
+            double v;
+            switch (T.kind) {
+              case ORC_TERM_MASS: v = N[a] * N[b]; break;
+              case ORC_TERM_LAPLACE: v = G[a][0] * G[b][0] + G[a][1] * G[b][1] + G[a][2] * G[b][2]; break;
+              case ORC_TERM_U_NGRADV: v = N[b] * (bb[0] * G[a][0] + bb[1] * G[a][1] + bb[2] * G[a][2]); break;
+              default: v = (bb[0] * G[b][0] + bb[1] * G[b][1] + bb[2] * G[b][2]) * N[a]; break;
+            }
+            A[a * nve + b] += w * c * v;
+          }
+      }
+    }
+  }
+  if (status) *status = st;
+  return orc_csr_from_elements(nv, nve, ne, elv, slot.data(), elm.data(), nact, nthreads);
+}
+
 double orc_quad_integrate(int D, int nv, const double* coords, int ne, const int32_t* elv, const double* lset,
                           int dt, int order, int policy, int ex, int ey, int ez, int* status) {
   (void)nv;
