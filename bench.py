@@ -981,6 +981,17 @@ class Gpu:
     def launch(self):
         self._lib.call("xg_step_graph_launch", self.g, self.sp)
 
+    def graph_on(self, key):
+        """A second graph of the same steps writing the outputs e[key]
+        (double-buffered end-to-end runs); the steps' level sets are shared."""
+        n = len(self.entries)
+        forms = (ctypes.c_void_p * n)(*[e["form"].value for e in self.entries])
+        lsets = (ctypes.c_void_p * n)(*[e["lset"].data_ptr() for e in self.entries])
+        outs = (self._lib.Csr * n)(*[e[key]["csr"] for e in self.entries])
+        g = ctypes.c_void_p()
+        self._lib.call("xg_step_graph_create", forms, lsets, outs, n, ctypes.byref(g))
+        return g
+
     def check_forms(self):
         self.torch.cuda.synchronize()
         for f in {e["form"].value for e in self.entries}:
@@ -1227,9 +1238,73 @@ def main():
         if k >= 2:
             e2e_times.append(time.perf_counter() - t0)
     gpu.check_forms()
-    e2e_s = float(np.mean(e2e_times))
+    e2e_serial_s = float(np.mean(e2e_times))
     h2d = sum(e["lset"].numel() * 8 for e in E)
     d2h = sum(16 + e["nrows"] * 4 + (e["nrows"] + 1) * 8 + e["nnz"] * 12 for e in E)
+
+    # pipelined: two output sets and two graphs; the read-back of step k runs
+    # on a copy stream while step k + 1 computes into the other set (every
+    # step still copies its level set in and its whole matrix out)
+    e2e_pipe_s = None
+    try:
+        for e in E:
+            e["out2"] = gpu.out(int(e["out"]["csr"].cap_rows), int(e["out"]["csr"].cap_nnz))
+            e["h_out2"] = {k: torch.empty_like(v).pin_memory() for k, v in e["h_out"].items()}
+        g2 = gpu.graph_on("out2")
+    except (RuntimeError, torch.cuda.OutOfMemoryError):
+        g2 = None
+    if g2 is not None:
+        cs = torch.cuda.Stream()
+        done = [torch.cuda.Event(), torch.cuda.Event()]
+        freed = [torch.cuda.Event(), torch.cuda.Event()]
+        for ev in freed:
+            ev.record(stream)
+        keys = (("out", "h_out"), ("out2", "h_out2"))
+
+        def issue_copy(k):
+            """Host waits for step k's counts, then queues its read-back on the
+            copy stream after the step's graph."""
+            b = k % 2
+            done[b].synchronize()
+            with torch.cuda.stream(cs):
+                cs.wait_event(done[b])
+                for e in E:
+                    o, h = e[keys[b][0]], e[keys[b][1]]
+                    r, z = int(h["counts"][0]), int(h["counts"][1])
+                    h["row_dof"][:r].copy_(o["row_dof"][:r], non_blocking=True)
+                    h["rowptr"][: r + 1].copy_(o["rowptr"][: r + 1], non_blocking=True)
+                    h["cols"][:z].copy_(o["cols"][:z], non_blocking=True)
+                    h["vals"][:z].copy_(o["vals"][:z], non_blocking=True)
+                freed[b].record(cs)
+
+        nsteps, warm = args.steps, 2
+        for k in range(nsteps + warm):
+            if k == warm:
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+            b = k % 2
+            stream.wait_event(freed[b])  # the read-back of step k - 2 left this output set
+            for e in E:
+                e["lset"].copy_(e["h_lset"], non_blocking=True)
+            _lib.call("xg_step_graph_launch", gpu.g if b == 0 else g2, gpu.sp)
+            for e in E:
+                e[keys[b][1]]["counts"].copy_(e[keys[b][0]]["counts"], non_blocking=True)
+            done[b].record(stream)
+            if k > 0:
+                issue_copy(k - 1)
+        issue_copy(nsteps + warm - 1)
+        torch.cuda.synchronize()
+        e2e_pipe_s = (time.perf_counter() - t0) / nsteps
+        gpu.check_forms()
+        # the last step's copy equals the serial read-back's size
+        for e in E:
+            b = (nsteps + warm - 1) % 2
+            assert int(e[keys[b][1]]["counts"][1]) == e["nnz"]
+        _lib.load().xg_step_graph_destroy(g2)
+        for e in E:
+            e.pop("out2", None)
+            e.pop("h_out2", None)
+    e2e_s = e2e_pipe_s if e2e_pipe_s is not None else e2e_serial_s
 
     # ---------------- the mixed arm on the same workload ----------------
     fp64_out = [fetch_csr(gpu, e) for e in E] if rank == 0 else None
@@ -1346,7 +1421,11 @@ def main():
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if gpu.prec == 0 else "f32+f64", "data": "synthetic", "config": cfg,
         "e2e": {"value": ws * n_cut / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "ms_per_step": e2e_s * 1e3},
+                "ms_per_step": e2e_s * 1e3,
+                "mode": "pipelined: two output sets, the read-back of step k on a copy stream overlaps step k + 1"
+                if e2e_pipe_s is not None else "serial",
+                "serial": {"value": ws * n_cut / e2e_serial_s, "ms_per_step": e2e_serial_s * 1e3,
+                           "mode": "copy in, step, counts, copy out, synchronise; one step at a time"}},
         "stages_ms": {n: float(v) for n, v in zip(names, stage_ms)},
         "roofline": {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": peak_bw, "unit": "GB/s",
                      "frac": achieved / peak_bw, "traffic": traffic_for(args.workload, dname) if
