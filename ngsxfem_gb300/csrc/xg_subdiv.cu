@@ -8,16 +8,20 @@
 //                           <= 4 in reference coordinates) of a P2 level set
 //                           given by its values at the vertices and edge
 //                           midpoints of the reference tetrahedron
-// A group of NC^2 threads (NC = 8 children in 3D, 4 in 2D) runs one element:
-// the lattice checks of the root and of its children are split over the
-// group's threads (sign flags in shared memory), then every thread walks the
-// subtree of one grandchild (or the thread of a first-level leaf fills it), so
-// a cut element's tree is spread over 64 threads instead of walked by one.
-// Per-thread sums are reduced in a fixed tree, per block and over the blocks
-// in order, so repeated calls give the same bits.
+// Integrate: a group of NC^2 threads (NC = 8 children in 3D, 4 in 2D) runs
+// one element: the lattice checks of the root and of its children are split
+// over the group's threads (sign flags in shared memory), then every thread
+// walks the subtree of one grandchild (or the thread of a first-level leaf
+// fills it); per-thread sums are reduced in a fixed tree, per block and over
+// the blocks in order.  Moments: the trees of all elements level by level
+// (one thread per node and level, then one thread per leaf), so the warps of
+// each kernel run the same kind of work; the leaves' moments are summed per
+// element in a fixed order.  Repeated calls give the same bits.
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <utility>
+#include <vector>
 
 #include "xg_internal.h"
 #include "xg_subdiv.cuh"
@@ -177,71 +181,6 @@ __global__ void k_sd_sum(const double* v, int n, double* out) {
   }
 }
 
-// the 35 NEG moments x^a y^b z^c (a + b + c <= 4, by degree, then a, then b
-// descending) of each reference tetrahedron, 64 threads per element (the
-// group's sums reduced by warp shuffles, then the two warps in order)
-__global__ void __launch_bounds__(kSdThreads) k_subdiv_moments(int64_t n, const double* __restrict__ vals10,
-                                                               int levels, double* __restrict__ out35,
-                                                               const int32_t* __restrict__ list,
-                                                               const int32_t* __restrict__ count, int* err) {
-  constexpr int TPE = Grp<3>::TPE, EPB = Grp<3>::EPB, WPE = TPE / 32;
-  __shared__ int flags[EPB][Grp<3>::NC + 1];
-  __shared__ double red[EPB * WPE][35];
-  const int E[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
-  const int le = threadIdx.x / TPE, t = threadIdx.x % TPE, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int64_t items = list ? (int64_t)*count : n;
-  for (int64_t base = (int64_t)blockIdx.x * EPB; base < items; base += (int64_t)gridDim.x * EPB) {
-    const int64_t it = base + le;
-    int64_t e = -1;
-    if (it < items) {
-      e = list ? (int64_t)list[it] : it;
-      if (e < 0 || e >= n) {
-        if (t == 0) set_err(err, XG_ERR_ARG);
-        e = -1;
-      }
-    }
-    const bool live = e >= 0;
-    sd::Elem<3, 2> el;
-    if (live) {
-      const int gv[4] = {0, 1, 2, 3};
-      for (int r = 0; r < 3; r++) {
-        el.x0[r] = 0.0;
-        for (int c = 0; c < 3; c++) el.F[r][c] = r == c ? 1.0 : 0.0;
-      }
-      const double* p = vals10 + e * 10;
-      // P2 nodal values -> the H1 coefficients: vertex values, 4 p(mid) - 2 (p_a + p_b)
-      for (int i = 0; i < 4; i++) el.coef[i] = p[i];
-      for (int j = 0; j < 6; j++) el.coef[4 + j] = 4.0 * p[4 + j] - 2.0 * (p[E[j][0]] + p[E[j][1]]);
-      for (int i = 0; i < 10; i++) el.desc[i] = fn_desc<3, 2>(i, gv);
-    }
-    double m[35];
-    for (int k = 0; k < 35; k++) m[k] = 0.0;
-    auto emit = [&](const double* x, double wq) {
-      const double px[5] = {1, x[0], x[0] * x[0], x[0] * x[0] * x[0], x[0] * x[0] * x[0] * x[0]};
-      const double py[5] = {1, x[1], x[1] * x[1], x[1] * x[1] * x[1], x[1] * x[1] * x[1] * x[1]};
-      const double pz[5] = {1, x[2], x[2] * x[2], x[2] * x[2] * x[2], x[2] * x[2] * x[2] * x[2]};
-      int k = 0;
-      for (int tt = 0; tt <= 4; tt++)
-        for (int a = tt; a >= 0; a--)
-          for (int b = tt - a; b >= 0; b--) m[k++] += wq * px[a] * py[b] * pz[tt - a - b];
-    };
-    const int st = group_rule<3, 2>(&g_sd_rules, el, live, XG_NEG, 4, levels, t, flags[le], emit);
-    if (st) set_err(err, st);
-    for (int k = 0; k < 35; k++) {
-      double v = m[k];
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      if (lane == 0) red[w][k] = v;
-    }
-    __syncthreads();
-    if (live && t < 35) {
-      double v = red[le * WPE][t];
-      for (int q = 1; q < WPE; q++) v += red[le * WPE + q][t];
-      out35[e * 35 + t] = v;
-    }
-    __syncthreads();
-  }
-}
-
 template <int D, int K>
 void launch_int(xg_space* sp, const double* coefs, int dt, int order, int levels, int ex, int ey, int ez,
                 const uint64_t* defined_on, double* bs, cudaStream_t s) {
@@ -250,15 +189,364 @@ void launch_int(xg_space* sp, const double* coefs, int dt, int order, int levels
                                                            dt, order, levels, ex, ey, ez, defined_on, bs, m->d_err);
 }
 
+// ---- breadth-first moments ---------------------------------------------------------
+// The tree of every element level by level: a node is (item, path) with the
+// path's 3-bit digits the child indices from the root, so a thread rebuilds
+// its simplex with the same child() arithmetic as the depth-first walk.
+// Per level one thread per node classifies it (the checks of sd::node_rule:
+// expand, plain leaf, cut leaf or nothing), scans give the children's and
+// leaves' positions in node order, and the leaves are filled densely (one
+// thread per leaf: the warps of a fill kernel run the same rule), then each
+// element's moments are summed over its leaves, level by level, in order.
+
+enum { SD_NONE = 0, SD_EXPAND = 1, SD_PLAIN = 2, SD_CUT = 3 };
+
+struct SdNode {
+  int32_t item;
+  uint32_t path;
+};
+
+__device__ __forceinline__ void sd_elem(const double* __restrict__ vals10, int64_t e, sd::Elem<3, 2>& el) {
+  const int E[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+  const int gv[4] = {0, 1, 2, 3};
+  for (int r = 0; r < 3; r++) {
+    el.x0[r] = 0.0;
+    for (int c = 0; c < 3; c++) el.F[r][c] = r == c ? 1.0 : 0.0;
+  }
+  const double* p = vals10 + e * 10;
+  for (int i = 0; i < 4; i++) el.coef[i] = p[i];
+  for (int j = 0; j < 6; j++) el.coef[4 + j] = 4.0 * p[4 + j] - 2.0 * (p[E[j][0]] + p[E[j][1]]);
+  for (int i = 0; i < 10; i++) el.desc[i] = fn_desc<3, 2>(i, gv);
+}
+
+__device__ __forceinline__ void sd_simplex(uint32_t path, int depth, double (*v)[3]) {
+  sd::ref_simplex(3, v);
+  for (int d = 0; d < depth; d++) {
+    double w[4][3];
+    sd::child<3>(v, (int)((path >> (3 * d)) & 7u), w);
+    for (int i = 0; i < 4; i++)
+      for (int r = 0; r < 3; r++) v[i][r] = w[i][r];
+  }
+}
+
+// the element of item i (a list entry or the item itself)
+__device__ __forceinline__ int64_t sd_item_elem(const int32_t* list, int64_t base, int32_t item) {
+  return list ? (int64_t)list[base + item] : base + item;
+}
+
+__global__ void __launch_bounds__(128) k_sd_classify(const SdNode* __restrict__ nodes, int64_t nn,
+                                                     const double* __restrict__ vals10, const int32_t* __restrict__ list,
+                                                     int64_t base, int depth, int lev, uint8_t* __restrict__ cls,
+                                                     int32_t* __restrict__ cnt3) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nn; i += (int64_t)gridDim.x * blockDim.x) {
+    const SdNode nd = nodes[i];
+    sd::Elem<3, 2> el;
+    sd_elem(vals10, sd_item_elem(list, base, nd.item), el);
+    double v[4][3];
+    sd_simplex(nd.path, depth, v);
+    const int dself = sd::lattice_domain(el, v, lev);
+    int c;
+    if (dself != XG_IF) {
+      c = dself == XG_NEG ? SD_PLAIN : SD_NONE;
+    } else if (lev == 0) {
+      double l[4];
+      for (int k = 0; k < 4; k++) l[k] = sd::lset_at(el, v[k]);
+      const int dv = sd::vertex_domain(l, 4);
+      c = dv == XG_IF ? SD_CUT : (dv == XG_NEG ? SD_PLAIN : SD_NONE);
+    } else {
+      c = SD_EXPAND;
+    }
+    cls[i] = (uint8_t)c;
+    cnt3[i] = c == SD_EXPAND ? 8 : 0;
+    cnt3[nn + i] = c == SD_PLAIN ? 1 : 0;
+    cnt3[2 * nn + i] = c == SD_CUT ? 1 : 0;
+  }
+}
+
+// exclusive scan of int32 counts (per-block scans, one block over the block
+// sums, offsets added); totals to tot
+constexpr int kSdScan = 1024;
+__global__ void __launch_bounds__(kSdScan) k_sd_scan_local(const int32_t* __restrict__ in, int64_t n,
+                                                           int32_t* __restrict__ out, int32_t* __restrict__ bsum) {
+  __shared__ int32_t sh[kSdScan];
+  const int64_t i = blockIdx.x * (int64_t)kSdScan + threadIdx.x;
+  const int32_t x = i < n ? in[i] : 0;
+  sh[threadIdx.x] = x;
+  __syncthreads();
+  for (int o = 1; o < kSdScan; o <<= 1) {
+    const int32_t y = threadIdx.x >= o ? sh[threadIdx.x - o] : 0;
+    __syncthreads();
+    sh[threadIdx.x] += y;
+    __syncthreads();
+  }
+  if (i < n) out[i] = sh[threadIdx.x] - x;
+  if (threadIdx.x == kSdScan - 1) bsum[blockIdx.x] = sh[threadIdx.x];
+}
+__global__ void k_sd_scan_top(int32_t* bsum, int nb, int32_t* tot) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    int32_t acc = 0;
+    for (int b = 0; b < nb; b++) {
+      const int32_t x = bsum[b];
+      bsum[b] = acc;
+      acc += x;
+    }
+    *tot = acc;
+  }
+}
+__global__ void k_sd_scan_add(int32_t* out, int64_t n, const int32_t* bsum) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] += bsum[i / kSdScan];
+}
+
+__global__ void __launch_bounds__(128) k_sd_emit(const SdNode* __restrict__ nodes, int64_t nn,
+                                                 const uint8_t* __restrict__ cls, const int32_t* __restrict__ pos3,
+                                                 int depth, SdNode* __restrict__ next, SdNode* __restrict__ plain,
+                                                 SdNode* __restrict__ cut, int32_t* __restrict__ plain_depth) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nn; i += (int64_t)gridDim.x * blockDim.x) {
+    const SdNode nd = nodes[i];
+    const int c = cls[i];
+    if (c == SD_EXPAND) {
+      const int64_t o = pos3[i];
+      for (int k = 0; k < 8; k++) next[o + k] = SdNode{nd.item, nd.path | ((uint32_t)k << (3 * depth))};
+    } else if (c == SD_PLAIN) {
+      plain[pos3[nn + i]] = nd;
+      plain_depth[pos3[nn + i]] = depth;
+    } else if (c == SD_CUT) {
+      cut[pos3[2 * nn + i]] = nd;
+    }
+  }
+}
+
+__device__ __forceinline__ void sd_moments_point(const double* x, double w, double* m) {
+  const double px[5] = {1, x[0], x[0] * x[0], x[0] * x[0] * x[0], x[0] * x[0] * x[0] * x[0]};
+  const double py[5] = {1, x[1], x[1] * x[1], x[1] * x[1] * x[1], x[1] * x[1] * x[1] * x[1]};
+  const double pz[5] = {1, x[2], x[2] * x[2], x[2] * x[2] * x[2], x[2] * x[2] * x[2] * x[2]};
+  int k = 0;
+  for (int t = 0; t <= 4; t++)
+    for (int a = t; a >= 0; a--)
+      for (int b = t - a; b >= 0; b--) m[k++] += w * px[a] * py[b] * pz[t - a - b];
+}
+
+// one thread per leaf: its 35 moments (plain rule, or the straight cut of the
+// vertex values on a level-0 simplex)
+__global__ void __launch_bounds__(128) k_sd_fill(const SdNode* __restrict__ leaves, const int32_t* __restrict__ depths,
+                                                 int64_t nl, int cut_depth, const double* __restrict__ vals10,
+                                                 const int32_t* __restrict__ list, int64_t base,
+                                                 double* __restrict__ mom, int* err) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nl; i += (int64_t)gridDim.x * blockDim.x) {
+    const SdNode nd = leaves[i];
+    sd::Elem<3, 2> el;
+    sd_elem(vals10, sd_item_elem(list, base, nd.item), el);
+    double v[4][3];
+    sd_simplex(nd.path, depths ? depths[i] : cut_depth, v);
+    double m[35];
+    for (int k = 0; k < 35; k++) m[k] = 0.0;
+    auto emit = [&](const double* x, double w) { sd_moments_point(x, w, m); };
+    if (depths) {
+      sd::fill(&g_sd_rules, el, v, (const double*)nullptr, XG_NEG, 4, emit);
+    } else {
+      double l[4];
+      for (int k = 0; k < 4; k++) l[k] = sd::lset_at(el, v[k]);
+      const int st = sd::fill(&g_sd_rules, el, v, l, XG_NEG, 4, emit);
+      if (st) set_err(err, st);
+    }
+    for (int k = 0; k < 35; k++) mom[i * 35 + k] = m[k];
+  }
+}
+
+// per (item, moment): the sums over the item's leaves, plain leaves level by
+// level, then the cut leaves, each range in order (leaves sorted by item
+// within a level)
+struct SdSegs {
+  int n;
+  int64_t off[sd::kMaxLevels + 2];
+};
+__device__ __forceinline__ int64_t sd_lower(const SdNode* a, int64_t lo, int64_t hi, int32_t item) {
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (a[mid].item < item) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+__global__ void __launch_bounds__(128) k_sd_reduce(int64_t items, const SdNode* __restrict__ plain,
+                                                   const double* __restrict__ mp, SdSegs ps,
+                                                   const SdNode* __restrict__ cut, const double* __restrict__ mc,
+                                                   int64_t ncut, const int32_t* __restrict__ list, int64_t base,
+                                                   double* __restrict__ out35) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < items * 35;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t it = (int32_t)(t / 35);
+    const int k = (int)(t % 35);
+    double acc = 0.0;
+    for (int s2 = 0; s2 < ps.n; s2++) {
+      const int64_t lo = sd_lower(plain, ps.off[s2], ps.off[s2 + 1], it);
+      const int64_t hi = sd_lower(plain, lo, ps.off[s2 + 1], it + 1);
+      for (int64_t j = lo; j < hi; j++) acc += mp[j * 35 + k];
+    }
+    const int64_t lo = sd_lower(cut, 0, ncut, it), hi = sd_lower(cut, lo, ncut, it + 1);
+    for (int64_t j = lo; j < hi; j++) acc += mc[j * 35 + k];
+    out35[sd_item_elem(list, base, it) * 35 + k] = acc;
+  }
+}
+
+int sd_scan(const int32_t* in, int64_t n, int32_t* out, int32_t* bsum, int32_t* tot, cudaStream_t s) {
+  const int nb = (int)((n + kSdScan - 1) / kSdScan);
+  k_sd_scan_local<<<nb, kSdScan, 0, s>>>(in, n, out, bsum);
+  k_sd_scan_top<<<1, 32, 0, s>>>(bsum, nb, tot);
+  k_sd_scan_add<<<nb, kSdScan, 0, s>>>(out, n, bsum);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? XG_OK : cuda_fail(e, "k_sd_scan");
+}
+
+unsigned sd_grid(int64_t n) {
+  const int64_t b = (n + 127) / 128;
+  return (unsigned)(b < 152 * 64 ? (b > 0 ? b : 1) : 152 * 64);
+}
+
+// device scratch of one call, stream-ordered (released when the call's work is done)
+struct SdBuf {
+  void* p = nullptr;
+  cudaStream_t s = nullptr;
+  SdBuf() = default;
+  SdBuf(const SdBuf&) = delete;
+  SdBuf& operator=(const SdBuf&) = delete;
+  SdBuf(SdBuf&& o) noexcept : p(o.p), s(o.s) { o.p = nullptr; }
+  SdBuf& operator=(SdBuf&& o) noexcept {
+    if (this != &o) {
+      release();
+      p = o.p;
+      s = o.s;
+      o.p = nullptr;
+    }
+    return *this;
+  }
+  int get(size_t bytes, cudaStream_t st) {
+    release();
+    s = st;
+    const cudaError_t e = cudaMallocAsync(&p, bytes ? bytes : 8, st);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return cuda_fail(e, "cudaMallocAsync");
+    }
+    return XG_OK;
+  }
+  void release() {
+    if (p) cudaFreeAsync(p, s);
+    p = nullptr;
+  }
+  ~SdBuf() { release(); }
+};
+
+// the moments of items [base, base + items) of the list (or of the elements)
+int sd_bfs_chunk(const double* d_vals10, const int32_t* d_list, int64_t base, int64_t items, int levels,
+                 double* d_out35, int* d_err, cudaStream_t s) {
+  // roots
+  SdBuf b_cur;
+  if (int st = b_cur.get(sizeof(SdNode) * items, s)) return st;
+  {
+    std::vector<SdNode> h(items);
+    for (int64_t i = 0; i < items; i++) h[i] = SdNode{(int32_t)i, 0u};
+    XG_CUDA(cudaMemcpyAsync(b_cur.p, h.data(), sizeof(SdNode) * items, cudaMemcpyHostToDevice, s));
+    XG_CUDA(cudaStreamSynchronize(s));  // h leaves scope
+  }
+  std::vector<SdBuf> plain_b, pdepth_b, cutb;
+  std::vector<int64_t> nplain;
+  int64_t ncut = 0;
+  SdBuf cut_final;
+  SdNode* cur = (SdNode*)b_cur.p;
+  SdBuf next_b;
+  int64_t nn = items;
+  SdBuf cur_owner;
+  for (int depth = 0; depth <= levels && nn > 0; depth++) {
+    const int lev = levels - depth;
+    SdBuf w;
+    const int nb = (int)((3 * nn + kSdScan - 1) / kSdScan);
+    if (int st = w.get(nn + 8 * 6 * nn + 4 * (size_t)nb + 64, s)) return st;
+    uint8_t* cls = (uint8_t*)w.p;
+    int32_t* cnt3 = (int32_t*)(((uintptr_t)w.p + nn + 15) & ~(uintptr_t)15);
+    int32_t* pos3 = cnt3 + 3 * nn;
+    int32_t* tots = pos3 + 3 * nn;
+    int32_t* bsum = tots + 4;
+    k_sd_classify<<<sd_grid(nn), 128, 0, s>>>(cur, nn, d_vals10, d_list, base, depth, lev, cls, cnt3);
+    for (int q = 0; q < 3; q++)
+      if (int st = sd_scan(cnt3 + q * nn, nn, pos3 + q * nn, bsum, tots + q, s)) return st;
+    int32_t h_t[3];
+    XG_CUDA(cudaMemcpyAsync(h_t, tots, sizeof(h_t), cudaMemcpyDeviceToHost, s));
+    XG_CUDA(cudaStreamSynchronize(s));
+    SdBuf nb_next, nb_plain, nb_pd, nb_cut;
+    if (int st = nb_next.get(sizeof(SdNode) * (size_t)h_t[0], s)) return st;
+    if (int st = nb_plain.get(sizeof(SdNode) * (size_t)h_t[1], s)) return st;
+    if (int st = nb_pd.get(sizeof(int32_t) * (size_t)h_t[1], s)) return st;
+    if (int st = nb_cut.get(sizeof(SdNode) * (size_t)h_t[2], s)) return st;
+    k_sd_emit<<<sd_grid(nn), 128, 0, s>>>(cur, nn, cls, pos3, depth, (SdNode*)nb_next.p, (SdNode*)nb_plain.p,
+                                          (SdNode*)nb_cut.p, (int32_t*)nb_pd.p);
+    XG_CUDA(cudaGetLastError());
+    nplain.push_back(h_t[1]);
+    plain_b.push_back(std::move(nb_plain));
+    pdepth_b.push_back(std::move(nb_pd));
+    if (h_t[2] > 0) {
+      ncut = h_t[2];  // cut leaves appear only at level 0 (the last depth)
+      cut_final = std::move(nb_cut);
+    }
+    cur_owner = std::move(next_b);
+    next_b = std::move(nb_next);
+    cur = (SdNode*)next_b.p;
+    nn = h_t[0];
+  }
+  // plain leaves of all levels in one array (level-major), cut leaves
+  int64_t np = 0;
+  for (int64_t x : nplain) np += x;
+  SdBuf allp, alld, mp, mc;
+  if (int st = allp.get(sizeof(SdNode) * np, s)) return st;
+  if (int st = alld.get(sizeof(int32_t) * np, s)) return st;
+  if (int st = mp.get(sizeof(double) * 35 * np, s)) return st;
+  if (int st = mc.get(sizeof(double) * 35 * ncut, s)) return st;
+  SdSegs segs = {};
+  segs.n = (int)nplain.size();
+  int64_t o = 0;
+  for (size_t q = 0; q < nplain.size(); q++) {
+    segs.off[q] = o;
+    if (nplain[q]) {
+      XG_CUDA(cudaMemcpyAsync((SdNode*)allp.p + o, plain_b[q].p, sizeof(SdNode) * nplain[q], cudaMemcpyDeviceToDevice, s));
+      XG_CUDA(cudaMemcpyAsync((int32_t*)alld.p + o, pdepth_b[q].p, sizeof(int32_t) * nplain[q],
+                              cudaMemcpyDeviceToDevice, s));
+    }
+    o += nplain[q];
+  }
+  segs.off[nplain.size()] = o;
+  if (np > 0)
+    k_sd_fill<<<sd_grid(np), 128, 0, s>>>((const SdNode*)allp.p, (const int32_t*)alld.p, np, 0, d_vals10, d_list, base,
+                                          (double*)mp.p, d_err);
+  if (ncut > 0)
+    k_sd_fill<<<sd_grid(ncut), 128, 0, s>>>((const SdNode*)cut_final.p, nullptr, ncut, levels, d_vals10, d_list, base,
+                                            (double*)mc.p, d_err);
+  k_sd_reduce<<<sd_grid(items * 35), 128, 0, s>>>(items, (const SdNode*)allp.p, (const double*)mp.p, segs,
+                                                  (const SdNode*)cut_final.p, (const double*)mc.p, ncut, d_list, base,
+                                                  d_out35);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? XG_OK : cuda_fail(e, "k_sd_bfs");
+}
+
 }  // namespace
 
 int subdiv_moments_launch(const double* d_vals10, int64_t n, int levels, double* d_out35, const int32_t* d_list,
                           const int32_t* d_count, int* d_err, cudaStream_t s) {
-  const int64_t blocks = (n + Grp<3>::EPB - 1) / Grp<3>::EPB;
-  k_subdiv_moments<<<(unsigned)(blocks < kSdBlocks * 4 ? (blocks > 0 ? blocks : 1) : kSdBlocks * 4), kSdThreads, 0, s>>>(
-      n, d_vals10, levels, d_out35, d_list, d_count, d_err);
-  const cudaError_t e = cudaGetLastError();
-  return e == cudaSuccess ? XG_OK : cuda_fail(e, "k_subdiv_moments_tet");
+  int64_t items = n;
+  if (d_list) {
+    int32_t c = 0;
+    XG_CUDA(cudaMemcpyAsync(&c, d_count, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    XG_CUDA(cudaStreamSynchronize(s));
+    items = c < 0 ? 0 : (c > n ? n : c);
+  }
+  // chunks of items keep the leaf arrays bounded (about 130 leaves per cut
+  // element at level 3, 35 moments each)
+  const int64_t chunk = (int64_t)1 << 15;
+  for (int64_t b = 0; b < items; b += chunk) {
+    const int64_t m = items - b < chunk ? items - b : chunk;
+    if (int st = sd_bfs_chunk(d_vals10, d_list, b, m, levels, d_out35, d_err, s)) return st;
+  }
+  return XG_OK;
 }
 
 }  // namespace xg
