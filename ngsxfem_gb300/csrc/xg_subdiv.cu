@@ -242,15 +242,16 @@ __global__ void __launch_bounds__(128) k_sd_classify(const SdNode* __restrict__ 
     const SdNode nd = nodes[i];
     sd::Elem<3, 2> el;
     sd_elem(vals10, sd_item_elem(list, base, nd.item), el);
-    double v[4][3];
+    double v[4][3], q[10];
     sd_simplex(nd.path, depth, v);
-    const int dself = sd::lattice_domain(el, v, lev);
+    sd_quadratic(el, q);
+    const int dself = sd_qlattice(q, v, lev);
     int c;
     if (dself != XG_IF) {
       c = dself == XG_NEG ? SD_PLAIN : SD_NONE;
     } else if (lev == 0) {
       double l[4];
-      for (int k = 0; k < 4; k++) l[k] = sd::lset_at(el, v[k]);
+      for (int k = 0; k < 4; k++) l[k] = sd_qval(q, v[k]);
       const int dv = sd::vertex_domain(l, 4);
       c = dv == XG_IF ? SD_CUT : (dv == XG_NEG ? SD_PLAIN : SD_NONE);
     } else {
@@ -282,16 +283,27 @@ __global__ void __launch_bounds__(kSdScan) k_sd_scan_local(const int32_t* __rest
   if (i < n) out[i] = sh[threadIdx.x] - x;
   if (threadIdx.x == kSdScan - 1) bsum[blockIdx.x] = sh[threadIdx.x];
 }
-__global__ void k_sd_scan_top(int32_t* bsum, int nb, int32_t* tot) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    int32_t acc = 0;
-    for (int b = 0; b < nb; b++) {
-      const int32_t x = bsum[b];
-      bsum[b] = acc;
-      acc += x;
+// one block: exclusive scan of the block sums, 1024 at a time with a carry
+__global__ void __launch_bounds__(kSdScan) k_sd_scan_top(int32_t* bsum, int nb, int32_t* tot) {
+  __shared__ int32_t sh[kSdScan];
+  int32_t carry = 0;
+  for (int b0 = 0; b0 < nb; b0 += kSdScan) {
+    const int i = b0 + threadIdx.x;
+    const int32_t x = i < nb ? bsum[i] : 0;
+    sh[threadIdx.x] = x;
+    __syncthreads();
+    for (int o = 1; o < kSdScan; o <<= 1) {
+      const int32_t y = threadIdx.x >= o ? sh[threadIdx.x - o] : 0;
+      __syncthreads();
+      sh[threadIdx.x] += y;
+      __syncthreads();
     }
-    *tot = acc;
+    if (i < nb) bsum[i] = carry + sh[threadIdx.x] - x;
+    const int32_t blk = sh[kSdScan - 1];
+    __syncthreads();
+    carry += blk;
   }
+  if (threadIdx.x == 0) *tot = carry;
 }
 __global__ void k_sd_scan_add(int32_t* out, int64_t n, const int32_t* bsum) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -317,14 +329,77 @@ __global__ void __launch_bounds__(128) k_sd_emit(const SdNode* __restrict__ node
   }
 }
 
+// m[k] += w x^a y^b z^c in the moments' order, with the products w x^a y^b
+// formed once per (a, b)
 __device__ __forceinline__ void sd_moments_point(const double* x, double w, double* m) {
-  const double px[5] = {1, x[0], x[0] * x[0], x[0] * x[0] * x[0], x[0] * x[0] * x[0] * x[0]};
-  const double py[5] = {1, x[1], x[1] * x[1], x[1] * x[1] * x[1], x[1] * x[1] * x[1] * x[1]};
-  const double pz[5] = {1, x[2], x[2] * x[2], x[2] * x[2] * x[2], x[2] * x[2] * x[2] * x[2]};
+  double wx[5], py[5], pz[5];
+  wx[0] = w;
+  py[0] = 1.0;
+  pz[0] = 1.0;
+#pragma unroll
+  for (int i = 1; i < 5; i++) {
+    wx[i] = wx[i - 1] * x[0];
+    py[i] = py[i - 1] * x[1];
+    pz[i] = pz[i - 1] * x[2];
+  }
   int k = 0;
+#pragma unroll
   for (int t = 0; t <= 4; t++)
-    for (int a = t; a >= 0; a--)
-      for (int b = t - a; b >= 0; b--) m[k++] += w * px[a] * py[b] * pz[t - a - b];
+#pragma unroll
+    for (int a = t; a >= 0; a--) {
+      const double wxy0 = wx[a];
+#pragma unroll
+      for (int b = t - a; b >= 0; b--) m[k++] += (wxy0 * py[b]) * pz[t - a - b];
+    }
+}
+
+// the P2 level set of an element as a quadratic in x, y, z: q[0] + q[1] x +
+// q[2] y + q[3] z + q[4] x^2 + q[5] y^2 + q[6] z^2 + q[7] xy + q[8] xz + q[9] yz
+// (lambda_i = x_i for i < 3, lambda_3 = 1 - x - y - z; vertex functions
+// lambda_i, edge functions lambda_a lambda_b)
+__device__ __forceinline__ void sd_quadratic(const sd::Elem<3, 2>& el, double* q) {
+  const double L[4][4] = {{0, 1, 0, 0}, {0, 0, 1, 0}, {0, 0, 0, 1}, {1, -1, -1, -1}};  // const, x, y, z
+  const int E[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+  for (int k = 0; k < 10; k++) q[k] = 0.0;
+  for (int v = 0; v < 4; v++)
+    for (int k = 0; k < 4; k++) q[k] += el.coef[v] * L[v][k];
+  for (int j = 0; j < 6; j++) {
+    const double* A = L[E[j][0]];
+    const double* B = L[E[j][1]];
+    const double c = el.coef[4 + j];
+    q[0] += c * A[0] * B[0];
+    q[1] += c * (A[0] * B[1] + A[1] * B[0]);
+    q[2] += c * (A[0] * B[2] + A[2] * B[0]);
+    q[3] += c * (A[0] * B[3] + A[3] * B[0]);
+    q[4] += c * A[1] * B[1];
+    q[5] += c * A[2] * B[2];
+    q[6] += c * A[3] * B[3];
+    q[7] += c * (A[1] * B[2] + A[2] * B[1]);
+    q[8] += c * (A[1] * B[3] + A[3] * B[1]);
+    q[9] += c * (A[2] * B[3] + A[3] * B[2]);
+  }
+}
+__device__ __forceinline__ double sd_qval(const double* q, const double* x) {
+  return q[0] + x[0] * (q[1] + q[4] * x[0] + q[7] * x[1] + q[8] * x[2]) + x[1] * (q[2] + q[5] * x[1] + q[9] * x[2]) +
+         x[2] * (q[3] + q[6] * x[2]);
+}
+// CheckIfCut on the lattice of simplex v at level L (sd::lattice_domain with
+// the quadratic form)
+__device__ __forceinline__ int sd_qlattice(const double* q, const double (*v)[3], int L) {
+  const int np = 1 << L;
+  const double dx = 1.0 / np;
+  bool pos = false, neg = false;
+  for (int i2 = 0; i2 <= np; i2++)
+    for (int i1 = 0; i1 + i2 <= np; i1++)
+      for (int i0 = 0; i0 + i1 + i2 <= np; i0++) {
+        const int I[3] = {i0, i1, i2};
+        double xi[3];
+        sd::lattice_point<3>(v, I, dx, xi);
+        if (sd_qval(q, xi) >= 0.0) pos = true;
+        else neg = true;
+        if (pos && neg) return XG_IF;
+      }
+  return pos ? XG_POS : XG_NEG;
 }
 
 // one thread per leaf: its 35 moments (plain rule, or the straight cut of the
@@ -345,8 +420,9 @@ __global__ void __launch_bounds__(128) k_sd_fill(const SdNode* __restrict__ leav
     if (depths) {
       sd::fill(&g_sd_rules, el, v, (const double*)nullptr, XG_NEG, 4, emit);
     } else {
-      double l[4];
-      for (int k = 0; k < 4; k++) l[k] = sd::lset_at(el, v[k]);
+      double l[4], q[10];
+      sd_quadratic(el, q);
+      for (int k = 0; k < 4; k++) l[k] = sd_qval(q, v[k]);
       const int st = sd::fill(&g_sd_rules, el, v, l, XG_NEG, 4, emit);
       if (st) set_err(err, st);
     }
@@ -393,7 +469,7 @@ __global__ void __launch_bounds__(128) k_sd_reduce(int64_t items, const SdNode* 
 int sd_scan(const int32_t* in, int64_t n, int32_t* out, int32_t* bsum, int32_t* tot, cudaStream_t s) {
   const int nb = (int)((n + kSdScan - 1) / kSdScan);
   k_sd_scan_local<<<nb, kSdScan, 0, s>>>(in, n, out, bsum);
-  k_sd_scan_top<<<1, 32, 0, s>>>(bsum, nb, tot);
+  k_sd_scan_top<<<1, kSdScan, 0, s>>>(bsum, nb, tot);
   k_sd_scan_add<<<nb, kSdScan, 0, s>>>(out, n, bsum);
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? XG_OK : cuda_fail(e, "k_sd_scan");
