@@ -234,6 +234,79 @@ __device__ __forceinline__ int64_t sd_item_elem(const int32_t* list, int64_t bas
   return list ? (int64_t)list[base + item] : base + item;
 }
 
+// m[k] += w x^a y^b z^c in the moments' order, with the products w x^a y^b
+// formed once per (a, b)
+__device__ __forceinline__ void sd_moments_point(const double* x, double w, double* m) {
+  double wx[5], py[5], pz[5];
+  wx[0] = w;
+  py[0] = 1.0;
+  pz[0] = 1.0;
+#pragma unroll
+  for (int i = 1; i < 5; i++) {
+    wx[i] = wx[i - 1] * x[0];
+    py[i] = py[i - 1] * x[1];
+    pz[i] = pz[i - 1] * x[2];
+  }
+  int k = 0;
+#pragma unroll
+  for (int t = 0; t <= 4; t++)
+#pragma unroll
+    for (int a = t; a >= 0; a--) {
+      const double wxy0 = wx[a];
+#pragma unroll
+      for (int b = t - a; b >= 0; b--) m[k++] += (wxy0 * py[b]) * pz[t - a - b];
+    }
+}
+
+// the P2 level set of an element as a quadratic in x, y, z: q[0] + q[1] x +
+// q[2] y + q[3] z + q[4] x^2 + q[5] y^2 + q[6] z^2 + q[7] xy + q[8] xz + q[9] yz
+// (lambda_i = x_i for i < 3, lambda_3 = 1 - x - y - z; vertex functions
+// lambda_i, edge functions lambda_a lambda_b)
+__device__ __forceinline__ void sd_quadratic(const sd::Elem<3, 2>& el, double* q) {
+  const double L[4][4] = {{0, 1, 0, 0}, {0, 0, 1, 0}, {0, 0, 0, 1}, {1, -1, -1, -1}};  // const, x, y, z
+  const int E[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+  for (int k = 0; k < 10; k++) q[k] = 0.0;
+  for (int v = 0; v < 4; v++)
+    for (int k = 0; k < 4; k++) q[k] += el.coef[v] * L[v][k];
+  for (int j = 0; j < 6; j++) {
+    const double* A = L[E[j][0]];
+    const double* B = L[E[j][1]];
+    const double c = el.coef[4 + j];
+    q[0] += c * A[0] * B[0];
+    q[1] += c * (A[0] * B[1] + A[1] * B[0]);
+    q[2] += c * (A[0] * B[2] + A[2] * B[0]);
+    q[3] += c * (A[0] * B[3] + A[3] * B[0]);
+    q[4] += c * A[1] * B[1];
+    q[5] += c * A[2] * B[2];
+    q[6] += c * A[3] * B[3];
+    q[7] += c * (A[1] * B[2] + A[2] * B[1]);
+    q[8] += c * (A[1] * B[3] + A[3] * B[1]);
+    q[9] += c * (A[2] * B[3] + A[3] * B[2]);
+  }
+}
+__device__ __forceinline__ double sd_qval(const double* q, const double* x) {
+  return q[0] + x[0] * (q[1] + q[4] * x[0] + q[7] * x[1] + q[8] * x[2]) + x[1] * (q[2] + q[5] * x[1] + q[9] * x[2]) +
+         x[2] * (q[3] + q[6] * x[2]);
+}
+// CheckIfCut on the lattice of simplex v at level L (sd::lattice_domain with
+// the quadratic form)
+__device__ __forceinline__ int sd_qlattice(const double* q, const double (*v)[3], int L) {
+  const int np = 1 << L;
+  const double dx = 1.0 / np;
+  bool pos = false, neg = false;
+  for (int i2 = 0; i2 <= np; i2++)
+    for (int i1 = 0; i1 + i2 <= np; i1++)
+      for (int i0 = 0; i0 + i1 + i2 <= np; i0++) {
+        const int I[3] = {i0, i1, i2};
+        double xi[3];
+        sd::lattice_point<3>(v, I, dx, xi);
+        if (sd_qval(q, xi) >= 0.0) pos = true;
+        else neg = true;
+        if (pos && neg) return XG_IF;
+      }
+  return pos ? XG_POS : XG_NEG;
+}
+
 __global__ void __launch_bounds__(128) k_sd_classify(const SdNode* __restrict__ nodes, int64_t nn,
                                                      const double* __restrict__ vals10, const int32_t* __restrict__ list,
                                                      int64_t base, int depth, int lev, uint8_t* __restrict__ cls,
@@ -327,79 +400,6 @@ __global__ void __launch_bounds__(128) k_sd_emit(const SdNode* __restrict__ node
       cut[pos3[2 * nn + i]] = nd;
     }
   }
-}
-
-// m[k] += w x^a y^b z^c in the moments' order, with the products w x^a y^b
-// formed once per (a, b)
-__device__ __forceinline__ void sd_moments_point(const double* x, double w, double* m) {
-  double wx[5], py[5], pz[5];
-  wx[0] = w;
-  py[0] = 1.0;
-  pz[0] = 1.0;
-#pragma unroll
-  for (int i = 1; i < 5; i++) {
-    wx[i] = wx[i - 1] * x[0];
-    py[i] = py[i - 1] * x[1];
-    pz[i] = pz[i - 1] * x[2];
-  }
-  int k = 0;
-#pragma unroll
-  for (int t = 0; t <= 4; t++)
-#pragma unroll
-    for (int a = t; a >= 0; a--) {
-      const double wxy0 = wx[a];
-#pragma unroll
-      for (int b = t - a; b >= 0; b--) m[k++] += (wxy0 * py[b]) * pz[t - a - b];
-    }
-}
-
-// the P2 level set of an element as a quadratic in x, y, z: q[0] + q[1] x +
-// q[2] y + q[3] z + q[4] x^2 + q[5] y^2 + q[6] z^2 + q[7] xy + q[8] xz + q[9] yz
-// (lambda_i = x_i for i < 3, lambda_3 = 1 - x - y - z; vertex functions
-// lambda_i, edge functions lambda_a lambda_b)
-__device__ __forceinline__ void sd_quadratic(const sd::Elem<3, 2>& el, double* q) {
-  const double L[4][4] = {{0, 1, 0, 0}, {0, 0, 1, 0}, {0, 0, 0, 1}, {1, -1, -1, -1}};  // const, x, y, z
-  const int E[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
-  for (int k = 0; k < 10; k++) q[k] = 0.0;
-  for (int v = 0; v < 4; v++)
-    for (int k = 0; k < 4; k++) q[k] += el.coef[v] * L[v][k];
-  for (int j = 0; j < 6; j++) {
-    const double* A = L[E[j][0]];
-    const double* B = L[E[j][1]];
-    const double c = el.coef[4 + j];
-    q[0] += c * A[0] * B[0];
-    q[1] += c * (A[0] * B[1] + A[1] * B[0]);
-    q[2] += c * (A[0] * B[2] + A[2] * B[0]);
-    q[3] += c * (A[0] * B[3] + A[3] * B[0]);
-    q[4] += c * A[1] * B[1];
-    q[5] += c * A[2] * B[2];
-    q[6] += c * A[3] * B[3];
-    q[7] += c * (A[1] * B[2] + A[2] * B[1]);
-    q[8] += c * (A[1] * B[3] + A[3] * B[1]);
-    q[9] += c * (A[2] * B[3] + A[3] * B[2]);
-  }
-}
-__device__ __forceinline__ double sd_qval(const double* q, const double* x) {
-  return q[0] + x[0] * (q[1] + q[4] * x[0] + q[7] * x[1] + q[8] * x[2]) + x[1] * (q[2] + q[5] * x[1] + q[9] * x[2]) +
-         x[2] * (q[3] + q[6] * x[2]);
-}
-// CheckIfCut on the lattice of simplex v at level L (sd::lattice_domain with
-// the quadratic form)
-__device__ __forceinline__ int sd_qlattice(const double* q, const double (*v)[3], int L) {
-  const int np = 1 << L;
-  const double dx = 1.0 / np;
-  bool pos = false, neg = false;
-  for (int i2 = 0; i2 <= np; i2++)
-    for (int i1 = 0; i1 + i2 <= np; i1++)
-      for (int i0 = 0; i0 + i1 + i2 <= np; i0++) {
-        const int I[3] = {i0, i1, i2};
-        double xi[3];
-        sd::lattice_point<3>(v, I, dx, xi);
-        if (sd_qval(q, xi) >= 0.0) pos = true;
-        else neg = true;
-        if (pos && neg) return XG_IF;
-      }
-  return pos ? XG_POS : XG_NEG;
 }
 
 // one thread per leaf: its 35 moments (plain rule, or the straight cut of the
