@@ -387,6 +387,14 @@ typedef struct {
 } xg_cterm;
 /* Replace the form's coefficient terms (at most 8; nterms 0 removes them). */
 int xg_form_set_coef_terms(xg_form* form, const xg_cterm* terms, int32_t nterms);
+/* The form's facet-patch terms on the deformed mesh (dFacetPatch(...,
+ * deformation=...); d_gdef from xg_iso_deformation, NULL = undeformed):
+ * SymbolicFacetPatchBFI::T_CalcFacetMatrix with MapPatchIntegrationPoint on
+ * the deformed maps (xfem/symboliccutbfi.cpp:1747-1846, 1982-2377): each
+ * element's rule of the term's order, every point sent into the other
+ * element by the vertex-based guess and Newton steps with the deformed
+ * Jacobian, weights |det (J A)| of the point's own element. */
+int xg_form_set_deformation(xg_form* form, const double* d_gdef);
 
 /* Output matrix in compressed-row form over the form's active dofs (the dofs
  * of elements and facet patches that carry a term, numbered ascending as

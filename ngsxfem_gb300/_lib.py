@@ -29,7 +29,7 @@ EXPORTS = [
     "xg_mesh_create_tensor", "xg_cut_rules_ex", "xg_quad_rule_capacity", "xg_integrate_ex",
     "xg_integrate_mlset", "xg_cut_rules_mlset", "xg_mlset_rule_capacity", "xg_mlset_mark",
     "xg_iso_integrate_mesh", "xg_iso_deformation", "xg_integrate_bnd",
-    "xg_mlset_form_create", "xg_mlset_form_assemble", "xg_form_create", "xg_form_destroy", "xg_form_set_defined_on", "xg_form_set_bnd_terms", "xg_form_set_coef_terms", "xg_form_capacity",
+    "xg_mlset_form_create", "xg_mlset_form_assemble", "xg_form_create", "xg_form_destroy", "xg_form_set_defined_on", "xg_form_set_bnd_terms", "xg_form_set_coef_terms", "xg_form_set_deformation", "xg_form_capacity",
     "xg_quad_form_create", "xg_quad_form_destroy", "xg_quad_form_capacity", "xg_quad_form_assemble",
     "xg_form_assemble", "xg_form_check", "xg_form_stage_events", "xg_cutfem_step", "xg_cutfem_marking",
     "xg_space_create_st", "xg_space_info_st", "xg_cutinfo_update_st", "xg_st_cut_rules", "xg_st_form_create",
@@ -189,6 +189,7 @@ def load():
         "xg_form_set_defined_on": (I, [P, ctypes.c_int32, P]),
         "xg_form_set_bnd_terms": (I, [P, P, ctypes.c_int32]),
         "xg_form_set_coef_terms": (I, [P, P, ctypes.c_int32]),
+        "xg_form_set_deformation": (I, [P, P]),
         "xg_quad_form_create": (I, [P, P, ctypes.c_int32, I, P]),
         "xg_quad_form_destroy": (I, [P]),
         "xg_quad_form_capacity": (I, [P, P]),

@@ -2548,6 +2548,7 @@ struct xg_form {
   int32_t* d_own = nullptr;  // [n_own] owners, [n_own + 1] pointers, [nbnd] BND elements
   // volume terms with a coefficient field (xg_form_set_coef_terms)
   CoefDesc cdesc = {};
+  const double* d_patch_deform = nullptr;  // xg_form_set_deformation: patch terms on the deformed mesh
   FormDesc desc;
   int needs_mask = 0;  // domains needing decompositions on cut elements
   int el_sym = 0;      // every volume group symmetric: packed element matrices
@@ -3962,6 +3963,16 @@ int xg_form_set_coef_terms(xg_form* f, const xg_cterm* terms, int32_t nterms) {
   return XG_OK;
 }
 
+int xg_form_set_deformation(xg_form* f, const double* d_gdef) {
+  if (!f) return XG_ERR_ARG;
+  if (d_gdef && (!f->rows || f->ml || f->mesh->tensor)) {
+    set_last_error("xg_form_set_deformation: spatial forms on simplex meshes");
+    return XG_ERR_UNSUPPORTED;
+  }
+  f->d_patch_deform = d_gdef;
+  return XG_OK;
+}
+
 int xg_form_capacity(const xg_form* f, int64_t* o) {
   if (!f || !o) return XG_ERR_ARG;
   // the largest pattern any level set can produce on this mesh (every element
@@ -4094,8 +4105,33 @@ int rows_front(xg_form* f, const double* d_lset, const uint8_t* d_dom, cudaStrea
     return st;
   if (f->bnd.n > 0 && (st = bnd_elmat_launch(bnd_args(f, d_lset), s))) return st;
   if (f->cdesc.n > 0 && (st = coef_elmat_launch(coef_args(f, d_lset, d_dom), s))) return st;
-  if (f->has_patch && f->desc.npatch > 0 && (st = fp64 ? dispatch_patch<double>(f, s) : dispatch_patch<float>(f, s)))
-    return st;
+  if (f->has_patch && f->desc.npatch > 0) {
+    if (f->d_patch_deform) {
+      xg_mesh* m = f->mesh;
+      PatchDefLaunch P;
+      P.dim = m->dim;
+      P.order = f->space->order;
+      P.ne = m->ne;
+      P.nv = m->nv;
+      P.elv = m->d_elv;
+      P.xyz = m->d_xyz;
+      P.el_edges = m->d_el_edges;
+      P.gdef = f->d_patch_deform;
+      P.nf = m->nfacets;
+      P.fel = m->d_facet_els;
+      P.l_fa = f->d_l_fa;
+      P.counts = f->d_counts;
+      P.npatch = f->desc.npatch;
+      for (int q = 0; q < kMaxPatch; q++) P.p[q] = f->desc.p[q];
+      P.famat = f->d_famat;
+      P.cap_fa = f->cap_fa;
+      P.fp64 = fp64 ? 1 : 0;
+      P.err = f->d_err;
+      if ((st = patch_def_launch(P, s))) return st;
+    } else if ((st = fp64 ? dispatch_patch<double>(f, s) : dispatch_patch<float>(f, s))) {
+      return st;
+    }
+  }
   if (f->desc.nskel > 0 && (st = launch_skel(f, d_lset, s))) return st;
   if (f->use_ev) cudaEventRecord(f->ev[5], s);
   return XG_OK;
@@ -4747,7 +4783,8 @@ int xg_step_graph_create(xg_form* const* forms, const double* const* d_lsets, co
   std::vector<xg_form*> multi;
   if (nb == n)
     for (xg_form* f : distinct)
-      if (f->rows && f->has_patch && f->patch_exact && f->desc.npatch > 0 && f->desc.nskel == 0) multi.push_back(f);
+      if (f->rows && f->has_patch && f->patch_exact && f->desc.npatch > 0 && f->desc.nskel == 0 && !f->d_patch_deform)
+        multi.push_back(f);
   if (multi.size() < 2) multi.clear();
   int* d_queue = nullptr;
   if (!multi.empty()) XG_CUDA(cudaMalloc((void**)&d_queue, multi.size() * sizeof(int)));

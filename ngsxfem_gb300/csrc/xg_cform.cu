@@ -287,7 +287,176 @@ int launch_k(const CoefFormLaunch& L, cudaStream_t s) {
   return launch_t<3, 3, T>(L, s);
 }
 
+// MapPatchIntegrationPoint (symboliccutbfi.cpp:1747-1846) on the deformed
+// maps: the point xi_from of element `from` sent into element `to` (low-order
+// guess from the vertex positions, which the deformation keeps, then Newton
+// with the deformed Jacobian, at most 15 steps to 1e-12 sqrt(det)); returns
+// |det (J A)| of `from` at the point
+template <int D>
+__device__ double map_patch_def(const Geo<D>& gf, const double (*thf)[3], const Geo<D>& gt, const double (*tht)[3],
+                                const double* xi_from, double* xi_to) {
+  double y[3], Am[3][3], F[3][3], Fi[3][3], vec[3] = {0.0, 0.0, 0.0}, det_from;
+  iso::deform_at<D>(thf, xi_from, y, Am);
+  for (int r = 0; r < 3; r++)
+    for (int k = 0; k < 3; k++) {
+      double sr = 0.0;
+      if (r < D && k < D)
+        for (int q = 0; q < D; q++) sr += gf.F[r][q] * Am[q][k];
+      F[r][k] = r < D && k < D ? sr : (r == k ? 1.0 : 0.0);
+    }
+  for (int r = 0; r < D; r++) {
+    double sr = gf.x0[r];
+    for (int k = 0; k < D; k++) sr += gf.F[r][k] * y[k];
+    vec[r] = sr;
+  }
+  iso::invert<D>(F, Fi, &det_from);
+  const double h = sqrt(det_from);  // NaN for a negative determinant: one step, as in the affine statement
+  double x00[3] = {0.0, 0.0, 0.0};
+  for (int i = 0; i < D; i++) {
+    double sr = 0.0;
+    for (int k = 0; k < D; k++) sr += gt.Finv[i][k] * (vec[k] - gt.x0[k]);
+    x00[i] = sr;
+  }
+  double x0[3] = {x00[0], x00[1], x00[2]};
+  int its = 0;
+  double diffn = 0.0;
+  while (its == 0 || (diffn > 1e-12 * h && its < 15)) {
+    double yt[3], At[3][3], Ft[3][3], Fti[3][3], dt;
+    iso::deform_at<D>(tht, x0, yt, At);
+    double diff[3] = {0.0, 0.0, 0.0};
+    for (int r = 0; r < D; r++) {
+      double sr = gt.x0[r];
+      for (int k = 0; k < D; k++) sr += gt.F[r][k] * yt[k];
+      diff[r] = vec[r] - sr;
+    }
+    for (int r = 0; r < 3; r++)
+      for (int k = 0; k < 3; k++) {
+        double sr = 0.0;
+        if (r < D && k < D)
+          for (int q = 0; q < D; q++) sr += gt.F[r][q] * At[q][k];
+        Ft[r][k] = r < D && k < D ? sr : (r == k ? 1.0 : 0.0);
+      }
+    iso::invert<D>(Ft, Fti, &dt);
+    diffn = 0.0;
+    for (int i = 0; i < D; i++) diffn += diff[i] * diff[i];
+    diffn = sqrt(diffn);
+    for (int i = 0; i < D; i++) {
+      double sr = 0.0;
+      for (int k = 0; k < D; k++) sr += Fti[i][k] * diff[k];
+      x0[i] += sr;
+    }
+    its++;
+  }
+  double dist = 0.0;
+  for (int i = 0; i < D; i++) dist += (x0[i] - x00[i]) * (x0[i] - x00[i]);
+  dist = sqrt(dist);
+  const bool fail = its >= 15 || diffn > 1e-12 * h || dist > 10.0;
+  for (int i = 0; i < 3; i++) xi_to[i] = fail ? x00[i] : x0[i];
+  return fabs(det_from);
+}
+
+// facet-patch terms on the deformed mesh, thread per active facet: both
+// elements' rules of the term's order, every point mapped into the other
+// element, c (u1 - u2)(v1 - v2) with the point's physical weight, written as
+// the facet slot's full rows (in place of the affine patch kernels)
+template <int D, int K, typename T>
+__global__ void __launch_bounds__(64) k_patch_def(PatchDefLaunch L) {
+  constexpr int N = ndof_el(D, K), N2 = 2 * N, NE = D == 2 ? 3 : 6;
+  const int count = L.counts[2];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count && i < L.cap_fa; i += gridDim.x * blockDim.x) {
+    const int f = L.l_fa[i];
+    const int e[2] = {L.fel[f], L.fel[L.nf + f]};
+    Geo<D> g[2];
+    int gv[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
+    double th[2][6][3];
+    for (int sd = 0; sd < 2; sd++) {
+      double xv[4][3];
+      for (int v = 0; v <= D; v++) {
+        gv[sd][v] = L.elv[(int64_t)v * L.ne + e[sd]];
+        for (int c = 0; c < 3; c++) xv[v][c] = c < D ? L.xyz[(int64_t)c * L.nv + gv[sd][v]] : 0.0;
+      }
+      make_geo<D>(xv, g[sd]);
+      for (int j = 0; j < 6; j++)
+        for (int r = 0; r < 3; r++) {
+          double sr = 0.0;
+          if (j < NE && r < D) {
+            const int ed = L.el_edges[(int64_t)j * L.ne + e[sd]];
+            for (int k = 0; k < D; k++) sr += g[sd].Finv[r][k] * L.gdef[(int64_t)ed * 3 + k];
+          }
+          th[sd][j][r] = sr;
+        }
+    }
+    int desc[2][N];
+    for (int a = 0; a < N; a++) {
+      desc[0][a] = fn_desc<D, K>(a, gv[0]);
+      desc[1][a] = fn_desc<D, K>(a, gv[1]);
+    }
+    double A[N2 * N2];
+    for (int k = 0; k < N2 * N2; k++) A[k] = 0.0;
+    const double h1 = mesh_h<D>(fabs(g[0].det));
+    for (int pp = 0; pp < L.npatch; pp++) {
+      const PatchDesc& P = L.p[pp];
+      if (P.defined_on && !cf_bit64(P.defined_on, f)) continue;
+      const double c = P.hpow == 0 ? P.c : P.c * int_pow(h1, P.hpow);
+      const int o = clamp_order(P.order), off = g_cf_rules.off[D][o], cnt = g_cf_rules.cnt[D][o];
+      for (int l = 0; l < 2 * cnt; l++) {
+        const int sd = l < cnt ? 0 : 1, q = l < cnt ? l : l - cnt;
+        const double* xi = g_cf_rules.x[off + q];
+        double xo[3];
+        const double W = g_cf_rules.w[off + q] * c * map_patch_def<D>(g[sd], th[sd], g[1 - sd], th[1 - sd], xi, xo);
+        const double* x1 = sd == 0 ? xi : xo;
+        const double* x2 = sd == 0 ? xo : xi;
+        double lam1[D + 1], lam2[D + 1], s1 = 0.0, s2 = 0.0;
+        for (int k = 0; k < D; k++) {
+          lam1[k] = x1[k];
+          lam2[k] = x2[k];
+          s1 += x1[k];
+          s2 += x2[k];
+        }
+        lam1[D] = 1.0 - s1;
+        lam2[D] = 1.0 - s2;
+        double sh[N2];
+        for (int a = 0; a < N; a++) {
+          sh[a] = eval_fn_value<D, double>(desc[0][a], lam1);
+          sh[N + a] = -eval_fn_value<D, double>(desc[1][a], lam2);
+        }
+        for (int a = 0; a < N2; a++)
+          for (int b = 0; b < N2; b++) A[a * N2 + b] += W * sh[a] * sh[b];
+      }
+    }
+    T* out = (T*)L.famat + (int64_t)i * N2 * N2;
+    for (int k = 0; k < N2 * N2; k++) {
+      if (!finite_bits(A[k])) set_err(L.err, XG_ERR_NONFINITE);
+      out[k] = (T)A[k];
+    }
+  }
+}
+
+template <int D, int K, typename T>
+int launch_pd(const PatchDefLaunch& L, cudaStream_t s) {
+  k_patch_def<D, K, T><<<152 * 8, 64, 0, s>>>(L);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? XG_OK : cuda_fail(e, "k_patch_def");
+}
+
+template <typename T>
+int launch_pdk(const PatchDefLaunch& L, cudaStream_t s) {
+  if (L.dim == 2) {
+    if (L.order == 1) return launch_pd<2, 1, T>(L, s);
+    if (L.order == 2) return launch_pd<2, 2, T>(L, s);
+    return launch_pd<2, 3, T>(L, s);
+  }
+  if (L.order == 1) return launch_pd<3, 1, T>(L, s);
+  if (L.order == 2) return launch_pd<3, 2, T>(L, s);
+  return launch_pd<3, 3, T>(L, s);
+}
+
 }  // namespace
+
+int patch_def_launch(const PatchDefLaunch& L, cudaStream_t s) {
+  if (L.dim < 2 || L.dim > 3 || L.order < 1 || L.order > 3) return XG_ERR_UNSUPPORTED;
+  return L.fp64 ? launch_pdk<double>(L, s) : launch_pdk<float>(L, s);
+}
 
 int coef_active_launch(const CoefFormLaunch& L, cudaStream_t s) {
   if (L.d.n <= 0 || L.ne <= 0) return XG_OK;

@@ -291,6 +291,26 @@ struct CoefFormLaunch {
   int fp64;
   int* err;
 };
+// facet-patch terms on the deformed mesh (xg_form_set_deformation; xg_cform.cu)
+struct PatchDefLaunch {
+  int dim, order;
+  int ne, nv;
+  const int32_t* elv;
+  const double* xyz;
+  const int32_t* el_edges;
+  const double* gdef;      // [nedges][3]
+  int64_t nf;
+  const int32_t* fel;      // [2][nf]
+  const int32_t* l_fa;     // active facets
+  const int* counts;       // [2]: their number
+  int npatch;
+  PatchDesc p[kMaxPatch];
+  void* famat;             // [slot][2n][2n] full rows
+  int64_t cap_fa;
+  int fp64;
+  int* err;
+};
+int patch_def_launch(const PatchDefLaunch& a, cudaStream_t s);
 int coef_active_launch(const CoefFormLaunch& a, cudaStream_t s);
 int coef_elmat_launch(const CoefFormLaunch& a, cudaStream_t s);
 int upload_rules_cform();

@@ -665,9 +665,9 @@ class _Measure:
                 raise NotImplementedError("dCut/dFacetPatch option %r is not part of the GPU path" % k)
         self.deformation = kw.get("deformation")
         if self.deformation is not None:
-            if kind != "cut" or not isinstance(self.deformation, LevelSetMeshAdaptation):
-                raise NotImplementedError("deformation: dCut(..., deformation=LevelSetMeshAdaptation(..)"
-                                          ".CalcDeformation(..)) only (patch terms on the deformed mesh are not built)")
+            if kind not in ("cut", "patch") or not isinstance(self.deformation, LevelSetMeshAdaptation):
+                raise NotImplementedError("deformation: dCut / dFacetPatch(..., deformation="
+                                          "LevelSetMeshAdaptation(..).CalcDeformation(..))")
         self.definedon = kw.get("definedon")
         if self.definedon is not None and (kind != "cut" or kw.get("vb", VOL) != BND):
             raise NotImplementedError("definedon (a region of BND elements) applies to dCut(..., vb=BND)")
@@ -1121,6 +1121,15 @@ class BilinearForm:
         _lib.call("xg_form_create", self.space.h, arr, len(terms), self.precision, ctypes.byref(h))
         self._form = h
         self._terms = terms
+        pdef = {id(it.measure.deformation): it.measure.deformation for it in self.integrals
+                if it.measure.kind == "patch"}
+        if len(pdef) > 1:
+            raise NotImplementedError("the facet-patch terms of one form share one deformation (or none)")
+        pd = next(iter(pdef.values())) if pdef else None
+        if pd is not None:
+            gd = pd._edge_deformation()
+            self._keep.append(gd)
+            _lib.call("xg_form_set_deformation", h, gd.data_ptr())
         if bterms:
             barr = (_lib.BTerm * len(bterms))()
             for k, t in enumerate(bterms):

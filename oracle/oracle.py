@@ -120,7 +120,7 @@ def lib():
                                            ctypes.c_int, P, P]
         L.orc_subdiv_moments_p2.argtypes = [ctypes.c_int64, P, ctypes.c_int, P, ctypes.c_int]
         L.orc_assemble_full.restype = P
-        L.orc_assemble_full.argtypes = [P, P, P, ctypes.c_int, P, ctypes.c_int, P, ctypes.c_int, ctypes.c_int,
+        L.orc_assemble_full.argtypes = [P, P, P, ctypes.c_int, P, ctypes.c_int, P, ctypes.c_int, P, ctypes.c_int,
                                         ctypes.c_int]
         L.orc_assemble_bnd.restype = P
         L.orc_assemble_bnd.argtypes = [P, P, P, ctypes.c_int, P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
@@ -750,7 +750,7 @@ class Space:
             raise RuntimeError("oracle facet matrix error %d" % r)
         return out
 
-    def assemble(self, lset, terms, nthreads=1, dn_fd=False, bterms=(), cterms=()):
+    def assemble(self, lset, terms, nthreads=1, dn_fd=False, bterms=(), cterms=(), theta_patch=None):
         """Returns scipy-free CSR triple (rowptr int64, cols int32, vals float64) over all dofs.
         bterms: boundary terms (dicts: domain, coef, order, hpow, defined_on
         over the BND elements), mass terms of orc_assemble_bnd.  cterms:
@@ -796,9 +796,10 @@ class Space:
                 th = np.ascontiguousarray(th, dtype=np.float64)
                 keep.append(th)
             carr[i].theta_el = th.ctypes.data if th is not None else None
+        tp = None if theta_patch is None else np.ascontiguousarray(theta_patch, dtype=np.float64)
         c = lib().orc_assemble_full(self.h, _p(l), ctypes.cast(arr, ctypes.c_void_p), len(terms),
                                     ctypes.cast(barr, ctypes.c_void_p), len(bterms),
-                                    ctypes.cast(carr, ctypes.c_void_p), len(cterms), nthreads, int(dn_fd))
+                                    ctypes.cast(carr, ctypes.c_void_p), len(cterms), _p(tp), nthreads, int(dn_fd))
         if not c:
             raise RuntimeError("oracle assembly error")
         nnz = lib().orc_csr_nnz(c)

@@ -1337,9 +1337,152 @@ int skel_add(const orc_space* s, const double* lset_vertex, const orc_term* term
 }
 
 // patch terms, then skeleton terms, of facet f
+// The deformed element map x(xi) = x0 + F (xi + Theta(xi)) (edge shapes
+// lambda_a lambda_b, th[6][3] in the reference frame) and its Jacobian F A.
+void deformed_map(const Geo& g, const double* th, const double* xi, double* x, double (*FA)[3]) {
+  const int D = g.D;
+  double lam[4], sl = 0.0;
+  for (int k = 0; k < D; k++) {
+    lam[k] = xi[k];
+    sl += xi[k];
+  }
+  lam[D] = 1.0 - sl;
+  double y[3] = {xi[0], xi[1], D == 3 ? xi[2] : 0.0}, Am[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  const int E2[3][2] = {{0, 1}, {0, 2}, {1, 2}}, E3[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+  for (int j = 0; j < (D == 2 ? 3 : 6); j++) {
+    const int a = D == 2 ? E2[j][0] : E3[j][0], b = D == 2 ? E2[j][1] : E3[j][1];
+    const double ph = lam[a] * lam[b];
+    for (int k = 0; k < D; k++) {
+      const double da = a < D ? (a == k ? 1.0 : 0.0) : -1.0, db = b < D ? (b == k ? 1.0 : 0.0) : -1.0;
+      const double dph = da * lam[b] + lam[a] * db;
+      for (int r = 0; r < D; r++) Am[r][k] += th[j * 3 + r] * dph;
+    }
+    for (int r = 0; r < D; r++) y[r] += th[j * 3 + r] * ph;
+  }
+  for (int r = 0; r < 3; r++) {
+    x[r] = 0.0;
+    for (int k = 0; k < 3; k++) FA[r][k] = 0.0;
+  }
+  for (int r = 0; r < D; r++) {
+    double acc = g.x0[r];
+    for (int k = 0; k < D; k++) acc += g.F[r][k] * y[k];
+    x[r] = acc;
+    for (int k = 0; k < D; k++)
+      for (int q = 0; q < D; q++) FA[r][k] += g.F[r][q] * Am[q][k];
+  }
+}
+
+// the D x D matrix as a Geo (for its inverse and determinant)
+Geo as_geo(int D, const double (*M)[3]) {
+  double elc[12];
+  for (int v = 0; v <= D; v++)
+    for (int r = 0; r < D; r++) elc[v * D + r] = v < D ? M[r][v] : 0.0;
+  Geo g;
+  make_geo(D, elc, g);
+  return g;
+}
+
+// MapPatchIntegrationPoint (symboliccutbfi.cpp:1747-1846) with the deformed
+// maps: the point of `from` at xi_from sent into `to`; the low-order guess
+// uses the vertex positions (which the deformation leaves in place), the
+// Newton steps the deformed Jacobian at the current point.  Returns
+// |det| of `from` at the point (the physical weight factor).
+double map_patch_point_def(const Geo& from, const double* thf, const Geo& to, const double* tht, const double* xi_from,
+                           double* xi_to) {
+  const int D = from.D;
+  double vec[3], FA[3][3];
+  deformed_map(from, thf, xi_from, vec, FA);
+  const double det_from = as_geo(D, FA).det;
+  const double h = std::sqrt(det_from);  // NaN for a negative determinant, as in the affine statement
+  double x00[3] = {0, 0, 0}, f[3];
+  for (int i = 0; i < D; i++) f[i] = vec[i] - to.x0[i];
+  for (int i = 0; i < D; i++) {
+    double sacc = 0;
+    for (int k = 0; k < D; k++) sacc += to.Finv[i][k] * f[k];
+    x00[i] = sacc;
+  }
+  double x0[3] = {x00[0], x00[1], x00[2]};
+  const double eps = 1e-12;
+  const int maxit = 15;
+  int its = 0;
+  double diffn = 0;
+  while (its == 0 || (diffn > eps * h && its < maxit)) {
+    double xt[3], Ft[3][3];
+    deformed_map(to, tht, x0, xt, Ft);
+    const Geo gt = as_geo(D, Ft);
+    double diff[3] = {0, 0, 0};
+    for (int i = 0; i < D; i++) diff[i] = vec[i] - xt[i];
+    diffn = 0;
+    for (int i = 0; i < D; i++) diffn += diff[i] * diff[i];
+    diffn = std::sqrt(diffn);
+    for (int i = 0; i < D; i++) {
+      double sacc = 0;
+      for (int k = 0; k < D; k++) sacc += gt.Finv[i][k] * diff[k];
+      x0[i] += sacc;
+    }
+    its++;
+  }
+  double dist = 0;
+  for (int i = 0; i < D; i++) dist += (x0[i] - x00[i]) * (x0[i] - x00[i]);
+  dist = std::sqrt(dist);
+  const bool fail = its >= maxit || diffn > eps * h || dist > 10.0;
+  for (int i = 0; i < 3; i++) xi_to[i] = fail ? x00[i] : x0[i];
+  return std::fabs(det_from);
+}
+
+// the patch terms of facet f on the deformed mesh (theta [ne][6][3]): both
+// elements' order-2k rules, each point mapped into the other element, weight
+// w |det (J A)| of its own element, coefficient with the first element's h
+int patch_matrix_def(const orc_space* s, const orc_term* terms, int nterms, int f, const double* theta,
+                     double* elmat) {
+  const int D = s->D, n = s->nd, n2 = 2 * n;
+  std::fill(elmat, elmat + n2 * n2, 0.0);
+  int e1 = s->facet_els[2 * f], e2 = s->facet_els[2 * f + 1];
+  if (e1 < 0 || e2 < 0) return -5;
+  Geo g1, g2;
+  element_geo(s, e1, g1, nullptr, nullptr);
+  element_geo(s, e2, g2, nullptr, nullptr);
+  const double* th1 = theta + (size_t)e1 * 18;
+  const double* th2 = theta + (size_t)e2 * 18;
+  const int* gv1 = &s->elv[(size_t)e1 * (D + 1)];
+  const int* gv2 = &s->elv[(size_t)e2 * (D + 1)];
+  for (int t = 0; t < nterms; t++) {
+    const orc_term& T = terms[t];
+    if (T.kind != ORC_TERM_GHOST_MASS) continue;
+    if (T.defined_on && !test_bit(T.defined_on, f)) continue;
+    const int order = T.order >= 0 ? T.order : 2 * s->k;
+    const Rule& r = get_rule(D, order);
+    const int nq = r.size();
+    const double c = hcoef(T, g1);
+    double phi1[20], phi2[20], dphi[20][3], sh[40];
+    for (int l = 0; l < 2 * nq; l++) {
+      const int m = l < nq ? l : l - nq;
+      double xi[3] = {r.p[3 * m], r.p[3 * m + 1], r.p[3 * m + 2]}, xo[3];
+      double W;
+      if (l < nq) {
+        W = r.w[m] * map_patch_point_def(g1, th1, g2, th2, xi, xo);
+        basis(D, s->k, gv1, xi, phi1, dphi);
+        basis(D, s->k, gv2, xo, phi2, dphi);
+      } else {
+        W = r.w[m] * map_patch_point_def(g2, th2, g1, th1, xi, xo);
+        basis(D, s->k, gv1, xo, phi1, dphi);
+        basis(D, s->k, gv2, xi, phi2, dphi);
+      }
+      for (int i = 0; i < n; i++) {
+        sh[i] = phi1[i];
+        sh[n + i] = -phi2[i];
+      }
+      W *= c;
+      for (int i = 0; i < n2; i++)
+        for (int j = 0; j < n2; j++) elmat[i * n2 + j] += W * sh[i] * sh[j];
+    }
+  }
+  return 0;
+}
+
 int facet_matrix(const orc_space* s, const double* lset_vertex, const orc_term* terms, int nterms, int f, int dn_fd,
-                 double* elmat) {
-  const int r = patch_matrix(s, terms, nterms, f, elmat);
+                 double* elmat, const double* theta = nullptr) {
+  const int r = theta ? patch_matrix_def(s, terms, nterms, f, theta, elmat) : patch_matrix(s, terms, nterms, f, elmat);
   if (r) return r;
   return skel_add(s, lset_vertex, terms, nterms, f, dn_fd, elmat);
 }
@@ -2011,14 +2154,14 @@ orc_csr* orc_assemble_ex(const orc_space* s, const double* lset_vertex, const or
 // to the owner's element matrix; the owners join the active elements.
 orc_csr* orc_assemble_bnd(const orc_space* s, const double* lset_vertex, const orc_term* terms, int nterms,
                           const orc_bterm* bterms, int nbterms, int nthreads, int dn_fd) {
-  return orc_assemble_full(s, lset_vertex, terms, nterms, bterms, nbterms, nullptr, 0, nthreads, dn_fd);
+  return orc_assemble_full(s, lset_vertex, terms, nterms, bterms, nbterms, nullptr, 0, nullptr, nthreads, dn_fd);
 }
 
 // ... and volume terms with a coefficient field (element_matrix_coef), whose
 // element sets join the active elements
 orc_csr* orc_assemble_full(const orc_space* s, const double* lset_vertex, const orc_term* terms, int nterms,
-                           const orc_bterm* bterms, int nbterms, const orc_cterm* cterms, int ncterms, int nthreads,
-                           int dn_fd) {
+                           const orc_bterm* bterms, int nbterms, const orc_cterm* cterms, int ncterms,
+                           const double* theta_patch, int nthreads, int dn_fd) {
   const int ne = s->ne, n = s->nd, n2 = 2 * n;
   const int64_t nf = s->nfacets;
   // active elements: in the definedon set of some volume term; active facets:
@@ -2116,7 +2259,7 @@ orc_csr* orc_assemble_full(const orc_space* s, const double* lset_vertex, const 
   }
   parallel_for(nfa, nthreads, [&](int64_t b, int64_t en) {
     for (int64_t i = b; i < en; i++) {
-      int r = facet_matrix(s, lset_vertex, terms, nterms, fa_list[i], dn_fd, &fam[(size_t)i * n2 * n2]);
+      int r = facet_matrix(s, lset_vertex, terms, nterms, fa_list[i], dn_fd, &fam[(size_t)i * n2 * n2], theta_patch);
       if (r) err = r;
     }
   });

@@ -174,9 +174,12 @@ typedef struct {
   const uint64_t* defined_on;
   const double* theta_el; /* [ne][6][3] deformation (orc_iso_theta_mesh) or NULL: the term on the deformed mesh */
 } orc_cterm;
+/* theta_patch: the mesh deformation per element ([ne][6][3], orc_iso_theta_mesh)
+ * for the facet-patch terms (MapPatchIntegrationPoint on the deformed maps),
+ * or NULL. */
 orc_csr* orc_assemble_full(const orc_space* s, const double* lset_vertex, const orc_term* terms, int nterms,
-                           const orc_bterm* bterms, int nbterms, const orc_cterm* cterms, int ncterms, int nthreads,
-                           int dn_fd);
+                           const orc_bterm* bterms, int nbterms, const orc_cterm* cterms, int ncterms,
+                           const double* theta_patch, int nthreads, int dn_fd);
 /* orc_assemble with the normal-derivative mode of orc_facet_matrix. */
 orc_csr* orc_assemble_ex(const orc_space*, const double* lset_vertex, const orc_term* terms, int nterms,
                          int nthreads, int dn_fd);

@@ -32,8 +32,11 @@ def words(b):
     return b.words.cpu().numpy()
 
 
-@pytest.mark.parametrize("D,k,N", [(2, 1, 8), (2, 2, 8), (3, 1, 4), (3, 2, 4)])
-def test_deformed_nitsche_form_parity(xg, orc, D, k, N):
+@pytest.mark.parametrize("D,k,N,dpatch", [(2, 1, 8, False), (2, 2, 8, True), (3, 1, 4, True), (3, 2, 4, False),
+                                          (2, 3, 6, True)])
+def test_deformed_nitsche_form_parity(xg, orc, D, k, N, dpatch):
+    """The form of demos/fictdom.py on the deformed mesh (the ghost penalty
+    deformed too when dpatch)."""
     if D == 2:
         m = MakeStructured2DMesh(N, N, -1, 1, -1, 1)
         phi = lambda x, y: np.sqrt(x * x + y * y) - 0.5  # noqa: E731
@@ -60,13 +63,15 @@ def test_deformed_nitsche_form_parity(xg, orc, D, k, N):
                               dict(kind=orc.TERM_NGRADU_V, domain=orc.IF, coef=-1.0, defined_on=words(ifb), **dn),
                               dict(kind=orc.TERM_U_NGRADV, domain=orc.IF, coef=-1.0, defined_on=words(ifb), **dn),
                               dict(kind=orc.TERM_MASS, domain=orc.IF, coef=10.0 * k * k, hpow=-1,
-                                   defined_on=words(ifb), **dn)])
+                                   defined_on=words(ifb), **dn)],
+                      theta_patch=theta if dpatch else None)
     for prec, tol in ((xg.PREC_FP64, 1e-10), (xg.PREC_MIXED, 1e-5)):
         a = xg.BilinearForm(V, precision=prec)
         a += xg.grad(u) * xg.grad(v) * xg.dCut(lsetp1, xg.NEG, definedonelements=hasneg, deformation=deformation)
         a += (-xg.grad(u) * n * v - xg.grad(v) * n * u + (10.0 * k * k / h) * u * v) * \
             xg.dCut(lsetp1, xg.IF, definedonelements=ifb, deformation=deformation)
-        a += 0.1 / h ** 2 * (u - u.Other()) * (v - v.Other()) * xg.dFacetPatch(definedonelements=gp)
+        a += 0.1 / h ** 2 * (u - u.Other()) * (v - v.Other()) * \
+            xg.dFacetPatch(definedonelements=gp, deformation=deformation if dpatch else None)
         a.Assemble()
         compare(sp, ref, a.mat, tol)
 

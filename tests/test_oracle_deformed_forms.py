@@ -65,3 +65,23 @@ def test_zero_deformation_gives_the_plain_terms(k):
         A = dense(sp, sp.assemble(l, [], cterms=[t]))
         B = dense(sp, sp.assemble(l, [], cterms=[dict(t, theta_el=zero)]))
         assert np.abs(A - B).max() < 1e-13 * np.abs(A).max(), kind
+
+
+@pytest.mark.parametrize("k", [1, 2])
+def test_deformed_patch(k):
+    """dFacetPatch(deformation=...): MapPatchIntegrationPoint on the deformed
+    maps.  A zero deformation gives the affine patch matrices; the deformed
+    matrices are symmetric, annihilate the constants (u = 1 on both
+    elements) and differ from the affine ones."""
+    m, p2, l, theta, sp, one = circle(8, k)
+    dom, _, bits = sp.cutinfo(l)
+    fb = sp.facets_with_neighbor_types(bits[5], bits[4], True, True, True)
+    gp = [dict(kind=orc.TERM_GHOST_MASS, coef=0.1, hpow=-2, defined_on=fb)]
+    A0 = dense(sp, sp.assemble(l, gp))
+    Az = dense(sp, sp.assemble(l, gp, theta_patch=np.zeros_like(theta)))
+    Ad = dense(sp, sp.assemble(l, gp, theta_patch=theta))
+    scale = np.abs(A0).max()
+    assert np.abs(Az - A0).max() < 1e-13 * scale
+    assert np.abs(Ad - Ad.T).max() < 1e-14 * scale
+    assert np.abs(Ad @ one).max() < 1e-12 * scale
+    assert np.abs(Ad - A0).max() > 1e-6 * scale
