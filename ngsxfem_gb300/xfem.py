@@ -1099,7 +1099,9 @@ class BilinearForm:
             if it.measure.kind == "cut" and getattr(it.measure, "vb", VOL) == BND:
                 bterms += self._bnd_terms(it, lset)
                 continue
-            deform = getattr(it.measure, "deformation", None)
+            # volume terms on the deformed mesh go to the coefficient kernel;
+            # deformed patch terms stay patch terms (xg_form_set_deformation)
+            deform = getattr(it.measure, "deformation", None) if it.measure.kind == "cut" else None
             for t in it.terms(lset):
                 t["deform"] = deform
                 generic = t.get("gf") is not None or any(t.get("e", (0, 0, 0))) or deform is not None
