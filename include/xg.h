@@ -314,7 +314,10 @@ int xg_integrate_subdiv(xg_space* space, const double* d_lset_coefs, int dt, int
  * of the edges (0,1),(0,2),(0,3),(1,2),(1,3),(2,3) (d_vals10: n x 10): the 35
  * NEG moments x^a y^b z^c, a + b + c <= 4 (by degree, then a, then b
  * descending) per element, order-4 rules (d_out35: n x 35).  Rule errors go
- * to d_err (may be NULL). */
+ * to d_err (may be NULL).  The trees are built level by level with
+ * stream-ordered scratch (cudaMallocAsync): the call synchronises the stream
+ * once per tree level to size the next level's lists, so it cannot be
+ * captured into a CUDA graph. */
 int xg_subdiv_moments_tet(const double* d_vals10, int64_t n, int subdivlvl, double* d_out35, int* d_err,
                           void* stream);
 
@@ -620,8 +623,9 @@ int xg_learned_moments_tet(xg_mlp* mlp, const double* d_vals10, int64_t n, doubl
  * isoparametric rule (as above); 0..6 the subdivision rule of that level
  * (xg_subdiv_moments_tet), the reference's own rule for a P2 level set
  * without mesh deformation (cutint/xintegration.cpp:1626-1754), which then
- * serves as the fallback.  Rule errors go to the network's status word
- * (xg_mlp_check). */
+ * serves as the fallback (the stream is synchronised as for
+ * xg_subdiv_moments_tet, once more to read the fallback count).  Rule errors
+ * go to the network's status word (xg_mlp_check). */
 int xg_learned_moments_tet_ex(xg_mlp* mlp, const double* d_vals10, int64_t n, double kappa_max, int plain_subdivlvl,
                               double* d_out35, int32_t* d_nfallback, void* stream);
 
