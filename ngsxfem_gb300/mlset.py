@@ -10,10 +10,11 @@ intersection (tuples of different codimension combine into the common
 boundary: entries that differ between NEG / POS and IF become IF), the
 complement among the tuples of the same codimension, Boundary() (an entry is
 replaced by IF unless both of its volume neighbours belong to the region) and
-Compress (tuples of zero measure for given level sets are dropped).  The
-CoefficientFunction helpers (Indicator, IndicatorSmoothed, GetOuterNormals)
-have no counterpart here.  The tuples are kept sorted, so the integration
-order is fixed.
+Compress (tuples of zero measure for given level sets are dropped), and
+GetOuterNormals (the unit normals of the boundary pieces, for the Nitsche
+terms of a BilinearForm).  The CoefficientFunction helpers Indicator and
+IndicatorSmoothed have no counterpart here.  The tuples are kept sorted, so
+the integration order is fixed.
 """
 from itertools import product
 
