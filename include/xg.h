@@ -507,6 +507,10 @@ typedef struct {
 typedef struct xg_lform xg_lform;
 /* At most 8 terms on a spatial H1 space. */
 int xg_lform_create(xg_space* space, const xg_lterm* terms, int32_t nterms, xg_lform** out);
+/* The form's volume terms on the deformed mesh (d_gdef from xg_iso_deformation,
+ * NULL = undeformed): the straight cut rule mapped by xhat + Theta(xhat),
+ * weights |det (J A)| (IF: times |(J A)^-T n_ref|), x the deformed point. */
+int xg_lform_set_deformation(xg_lform* form, const double* d_gdef);
 int xg_lform_destroy(xg_lform* lform);
 /* LinearForm::Assemble: element vectors (SymbolicCutLinearFormIntegrator::
  * T_CalcElementVector, symboliccutlfi.cpp:57-180) summed per dof in ascending

@@ -38,7 +38,7 @@ EXPORTS = [
     "xg_mlp_create", "xg_mlp_destroy", "xg_mlp_get_params", "xg_mlp_set_params", "xg_mlp_forward", "xg_mlp_forward_tc", "xg_mlp_check",
     "xg_mlp_loss_grad", "xg_mlp_adam_step", "xg_learned_moments_tet", "xg_learned_moments_tet_ex", "xg_learned_features",
     "xg_cutinfo_update_bnd", "xg_mesh_boundary", "xg_cutinfo_nodes", "xg_elements_with_threshold",
-    "xg_lform_create", "xg_lform_destroy", "xg_lform_assemble", "xg_lform_check",
+    "xg_lform_create", "xg_lform_set_deformation", "xg_lform_destroy", "xg_lform_assemble", "xg_lform_check",
 ]
 
 
@@ -226,6 +226,7 @@ def load():
         "xg_cutinfo_nodes": (I, [P, P, P, P, P, P, P, P, P, P, P, P]),
         "xg_elements_with_threshold": (I, [P, I64, I, D, P, P]),
         "xg_lform_create": (I, [P, P, ctypes.c_int32, P]),
+        "xg_lform_set_deformation": (I, [P, P]),
         "xg_lform_destroy": (I, [P]),
         "xg_lform_assemble": (I, [P, P, P, P, P]),
         "xg_lform_check": (I, [P]),

@@ -23,6 +23,7 @@
 #include "xg_basis.cuh"
 #include "xg_cut.cuh"
 #include "xg_internal.h"
+#include "xg_isomesh.cuh"
 #include "xg_lfbnd.cuh"
 
 namespace xg {
@@ -41,6 +42,8 @@ constexpr int kMaxLTerms = 8;
 struct LfDesc {
   int n;
   xg_lterm t[kMaxLTerms];
+  const double* gdef;        // mesh deformation [nedges][3] of the volume terms, or NULL
+  const int32_t* el_edges;   // [nedges per element][ne]
 };
 
 namespace {
@@ -81,6 +84,20 @@ __global__ void __launch_bounds__(128) k_lf_elvec(int ne, int nv, const int32_t*
     int desc[N];
 #pragma unroll
     for (int i = 0; i < N; i++) desc[i] = fn_desc<D, K>(i, gv);
+    // the deformed mesh: theta_j = J^-1 gdef(edge j), the reference frame
+    double theta[6][3];
+    if (d.gdef) {
+      constexpr int NE = D == 2 ? 3 : 6;
+      for (int j = 0; j < 6; j++)
+        for (int r = 0; r < 3; r++) {
+          double sr = 0.0;
+          if (j < NE && r < D) {
+            const int ed = d.el_edges[(int64_t)j * ne + e];
+            for (int k = 0; k < D; k++) sr += g.Finv[r][k] * d.gdef[(int64_t)ed * 3 + k];
+          }
+          theta[j][r] = sr;
+        }
+    }
     for (int t = 0; t < d.n; t++) {
       const xg_lterm& T = d.t[t];
       if (T.kind == XG_LTERM_SOURCE_BND) continue;
@@ -126,13 +143,42 @@ __global__ void __launch_bounds__(128) k_lf_elvec(int ne, int nv, const int32_t*
 #pragma unroll
           for (int i = 0; i < N; i++) phi[i] = eval_fn_value<D, double>(desc[i], lam);
           double gval;
+          // on the deformed mesh: the point y = pt + Theta(pt), the weight
+          // |det (J A)| (IF: times |(J A)^-T n_ref|) instead of |det J| fac
+          double y[3] = {pt[0], pt[1], pt[2]}, wdef = meas * fac;
+          if (d.gdef) {
+            double Am[3][3], F[3][3], Fi[3][3], detF;
+            iso::deform_at<D>(theta, pt, y, Am);
+            for (int r = 0; r < 3; r++)
+              for (int k = 0; k < 3; k++) {
+                double sr = 0.0;
+                if (r < D && k < D)
+                  for (int q2 = 0; q2 < D; q2++) sr += g.F[r][q2] * Am[q2][k];
+                F[r][k] = r < D && k < D ? sr : (r == k ? 1.0 : 0.0);
+              }
+            if (!iso::invert<D>(F, Fi, &detF)) {
+              set_err(err, XG_ERR_NONFINITE);
+              continue;
+            }
+            wdef = fabs(detF);
+            if (dt == XG_IF) {
+              double nn = 0.0, gn = 0.0;
+              for (int k = 0; k < D; k++) {
+                double sr = 0.0;
+                for (int j = 0; j < D; j++) sr += Fi[j][k] * (l[j] - l[D]);
+                nn += sr * sr;
+                gn += (l[k] - l[D]) * (l[k] - l[D]);
+              }
+              wdef *= sqrt(nn / gn);
+            }
+          }
           if (T.kind == XG_LTERM_SOURCE) {
             double x[3] = {0.0, 0.0, 0.0};
 #pragma unroll
             for (int i = 0; i < D; i++) {
               double sacc = g.x0[i];
 #pragma unroll
-              for (int k = 0; k < D; k++) sacc += g.F[i][k] * pt[k];
+              for (int k = 0; k < D; k++) sacc += g.F[i][k] * y[k];
               x[i] = sacc;
             }
             gval = T.coef * ipow(x[0], T.e[0]) * ipow(x[1], T.e[1]) * (D == 3 ? ipow(x[2], T.e[2]) : 1.0);
@@ -142,7 +188,7 @@ __global__ void __launch_bounds__(128) k_lf_elvec(int ne, int nv, const int32_t*
             for (int j = 0; j < N; j++) u += T.d_gf[el_dofs[(int64_t)e * N + j]] * phi[j];
             gval = T.coef * u;
           }
-          const double w = c_rules.w[off + q] * vol * fac * meas * gval;
+          const double w = c_rules.w[off + q] * vol * wdef * gval;
 #pragma unroll
           for (int i = 0; i < N; i++) b[i] += w * phi[i];
         }
@@ -335,6 +381,13 @@ int xg_lform_check(xg_lform* f) {
   XG_CUDA(cudaMemset(f->d_err, 0, sizeof(int)));
   if (h) set_last_error(std::string("device error: ") + xg_status_string(h));
   return h;
+}
+
+int xg_lform_set_deformation(xg_lform* f, const double* d_gdef) {
+  if (!f) return XG_ERR_ARG;
+  f->desc.gdef = d_gdef;
+  f->desc.el_edges = f->space->mesh->d_el_edges;
+  return XG_OK;
 }
 
 int xg_lform_assemble(xg_lform* f, const double* d_lset, const uint8_t* d_dom, double* d_out, void* stream) {

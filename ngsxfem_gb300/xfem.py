@@ -1322,6 +1322,11 @@ class LinearForm:
 
     def _build(self):
         terms = self._terms()
+        defs = {id(it.measure.deformation): it.measure.deformation for it in self.integrals
+                if getattr(it.measure, "vb", VOL) != BND}
+        if len(defs) > 1:
+            raise NotImplementedError("the volume terms of one linear form share one deformation (or none)")
+        self._deform = next(iter(defs.values())) if defs else None
         arr = (_lib.LTerm * len(terms))()
         self._keep = []
         for k, t in enumerate(terms):
@@ -1338,6 +1343,10 @@ class LinearForm:
         h = ctypes.c_void_p()
         _lib.call("xg_lform_create", self.space.h, arr, len(terms), ctypes.byref(h))
         self._lf = h
+        if self._deform is not None:
+            gd = self._deform._edge_deformation()
+            self._keep.append(gd)
+            _lib.call("xg_lform_set_deformation", h, gd.data_ptr())
 
     def Assemble(self, cutinfo=None):
         if self._lf is None:
@@ -1415,6 +1424,15 @@ def Integrate(levelset_domain=None, cf=None, mesh=None, order=5, integrand=None)
         vb = getattr(meas, "vb", VOL)
     else:
         vb = levelset_domain.get("vb", VOL)
+    deform = getattr(meas, "deformation", None) if integrand is not None else levelset_domain.get("deformation")
+    if deform is not None:
+        # Integrate on the deformed mesh: the adaptation's own mapped rule, for
+        # its P1 level set (lset_p1) on all elements
+        if vb == BND or defined is not None or isinstance(lset, (tuple, list)):
+            raise NotImplementedError("Integrate with a deformation: VOL, one level set, no definedonelements")
+        if not torch.equal(_lset_vec(lset)[: deform.mesh.nv], _lset_vec(deform.lset_p1)[: deform.mesh.nv]):
+            raise ValueError("Integrate with a deformation takes the adaptation's lset_p1 as the level set")
+        return deform.Integrate(dt, mono, order=order)
     if vb == BND:
         region = getattr(meas, "definedon", None) if integrand is not None else levelset_domain.get("definedon")
         return _integrate_bnd(lset, dt, order, mono, mesh, defined, region)

@@ -94,3 +94,44 @@ def test_deformed_mass_converges_to_the_area(xg):
         errs.append(abs(one @ (a.mat.to_scipy() @ one) - 0.25 * math.pi))
     eoc = [math.log2(p / q) for p, q in zip(errs[:-1], errs[1:])]
     assert errs[-1] < 1e-5 and min(eoc) > 2.75, (errs, eoc)
+
+
+@pytest.mark.parametrize("k", [1, 2])
+def test_deformed_linear_form(xg, orc, k):
+    """LinearForm on the deformed mesh (the right-hand side of
+    demos/fictdom.py with `deformation=`): f = x y on NEG and 2 on IF.  With
+    the vertex functions summing to 1, b = M_f 1 for the oracle's deformed
+    mass matrices with the same coefficients."""
+    m = MakeStructured2DMesh(8, 8, -1, 1, -1, 1)
+    phi = lambda x, y: np.sqrt(x * x + y * y) - 0.5  # noqa: E731
+    adap = xg.LevelSetMeshAdaptation(m, order=2, threshold=0.2)
+    deformation = adap.CalcDeformation(phi)
+    lsetp1 = adap.lset_p1
+    V = xg.H1(m, order=k)
+    v = V.TestFunction()
+    f = xg.LinearForm(V)
+    f += xg.x * xg.y * v * xg.dCut(lsetp1, xg.NEG, deformation=deformation)
+    f += 2.0 * v * xg.dCut(lsetp1, xg.IF, deformation=deformation)
+    f.Assemble()
+    got = f.vec.cpu().numpy()
+    theta, _ = orc.iso_theta_mesh(m, xg.P2ElementValues(m, phi), threshold=0.2)
+    sp = orc.Space(m, k)
+    rp, cols, vals = sp.assemble(lsetp1.vec.cpu().numpy(), [], cterms=[
+        dict(kind=orc.TERM_MASS, domain=orc.NEG, e=(1, 1, 0), theta_el=theta),
+        dict(kind=orc.TERM_MASS, domain=orc.IF, coef=2.0, theta_el=theta)])
+    A = np.zeros((sp.ndof, sp.ndof))
+    np.add.at(A, (np.repeat(np.arange(sp.ndof), np.diff(rp)), cols), vals)
+    one = np.zeros(sp.ndof)
+    one[: m.nv] = 1.0
+    ref = A @ one
+    assert np.abs(got - ref).max() < 1e-10 * np.abs(ref).max()
+
+
+def test_integrate_with_deformation(xg):
+    m = MakeStructured2DMesh(16, 16, -1, 1, -1, 1)
+    adap = xg.LevelSetMeshAdaptation(m, order=2, threshold=0.2)
+    deformation = adap.CalcDeformation(lambda x, y: np.sqrt(x * x + y * y) - 0.5)
+    lsetp1 = adap.lset_p1
+    a = xg.Integrate(xg.dCut(lsetp1, xg.NEG, order=2, deformation=deformation), m)
+    assert a == adap.Integrate(xg.NEG, order=2)
+    assert abs(a - 0.25 * math.pi) < 1e-4
