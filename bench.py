@@ -511,11 +511,17 @@ def run_c4(args):
                      "achieved": mlp_fwd["tensor_core_tflops"], "peak": peak_tc, "unit": "TFLOP/s",
                      "frac": mlp_fwd["tensor_core_tflops"] / peak_tc, "traffic": None,
                      "peak_source": "measured bf16" if pk else "fallback",
-                     "learned_path_whole": {"achieved": ach, "frac": ach / peak_tc}},
+                     "learned_path_whole": {"achieved": ach, "frac": ach / peak_tc},
+                     "dominant_stage": "the fallback's subdivision rule (k_sd_fill, FP64-bound: 88 % of the FP64 "
+                                       "pipe with full warps in the ncu capture of the same kernels)"
+                     if sub else "the fallback's isoparametric rule (k_tet_moments, FP64)"},
         "mlp_forward": mlp_fwd,
         "clocks": clk.summary(),
-        # moments, features, the fused network, correction, fallback (memset, list, moments)
-        "gpu_launches": args.steps * (4 + (3 if args.kappa >= 0 else 0)),
+        # moments, features, the fused network, correction; the fallback: memset and list, then
+        # (subdivision) per tree level classify + three scans of three kernels + emit, the plain and
+        # cut leaf fills and the per-element sums (one chunk of at most 32,768 elements), or
+        # (isoparametric) one kernel
+        "gpu_launches": args.steps * (4 + ((2 + ((L + 1) * 11 + 3 if sub else 1)) if args.kappa >= 0 else 0)),
     }
     if args.cpu_baseline:
         from oracle import oracle as orc
