@@ -2549,6 +2549,8 @@ struct xg_form {
   // volume terms with a coefficient field (xg_form_set_coef_terms)
   CoefDesc cdesc = {};
   const double* d_patch_deform = nullptr;  // xg_form_set_deformation: patch terms on the deformed mesh
+  cudaStream_t side = nullptr;             // the facet kernels' stream (forked from and joined into the step's)
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   FormDesc desc;
   int needs_mask = 0;  // domains needing decompositions on cut elements
   int el_sym = 0;      // every volume group symmetric: packed element matrices
@@ -2656,6 +2658,9 @@ int form_free(xg_form* f) {
                   f->d_el_rowslot, f->d_pos_rows, f->d_nbpos, f->d_cand_fs, f->d_act_slot, f->d_vcols, f->d_vvals,
                   f->d_bsum_rows, f->d_ml_terms, f->d_ml_tuples, f->d_own};
   for (void* p : ptrs) cudaFree(p);
+  if (f->side) cudaStreamDestroy(f->side);
+  if (f->ev_fork) cudaEventDestroy(f->ev_fork);
+  if (f->ev_join) cudaEventDestroy(f->ev_join);
   delete f;
   return XG_OK;
 }
@@ -3995,6 +4000,7 @@ int xg_form_check(xg_form* f) {
 
 namespace {
 int rows_front(xg_form* f, const double* d_lset, const uint8_t* d_dom, cudaStream_t s);
+int rows_front_facets(xg_form* f, const double* d_lset, cudaStream_t s);
 int rows_back(xg_form* f, xg_csr* out, cudaStream_t s);
 int assemble_front(xg_form* f, const double* d_lset, const uint8_t* d_dom, xg_csr* out, void* stream);
 }  // namespace
@@ -4101,10 +4107,42 @@ CoefFormLaunch coef_args(xg_form* f, const double* d_lset, const uint8_t* d_dom)
 int rows_front(xg_form* f, const double* d_lset, const uint8_t* d_dom, cudaStream_t s) {
   const bool fp64 = f->precision == XG_PREC_FP64;
   int st;
+  // the facet kernels (patch, skeleton) write the facet matrices, the element
+  // kernels the element rows: without stage events they run on a second
+  // stream of the form, forked from and joined back into s (in a captured
+  // step they become concurrent branches of the graph)
+  const bool fork = !f->use_ev && f->has_patch && (f->desc.npatch > 0 || f->desc.nskel > 0);
+  cudaStream_t sf = s;
+  if (fork) {
+    if (!f->side) {
+      XG_CUDA(cudaStreamCreateWithFlags(&f->side, cudaStreamNonBlocking));
+      XG_CUDA(cudaEventCreateWithFlags(&f->ev_fork, cudaEventDisableTiming));
+      XG_CUDA(cudaEventCreateWithFlags(&f->ev_join, cudaEventDisableTiming));
+    }
+    XG_CUDA(cudaEventRecord(f->ev_fork, s));
+    XG_CUDA(cudaStreamWaitEvent(f->side, f->ev_fork, 0));
+    sf = f->side;
+    if ((st = rows_front_facets(f, d_lset, sf))) return st;
+  }
   if ((st = fp64 ? dispatch_volume<double>(f, d_lset, d_dom, s) : dispatch_volume<float>(f, d_lset, d_dom, s)))
     return st;
   if (f->bnd.n > 0 && (st = bnd_elmat_launch(bnd_args(f, d_lset), s))) return st;
   if (f->cdesc.n > 0 && (st = coef_elmat_launch(coef_args(f, d_lset, d_dom), s))) return st;
+  if (fork) {
+    XG_CUDA(cudaEventRecord(f->ev_join, sf));
+    XG_CUDA(cudaStreamWaitEvent(s, f->ev_join, 0));
+  } else if ((st = rows_front_facets(f, d_lset, s))) {
+    return st;
+  }
+  if (f->use_ev) cudaEventRecord(f->ev[5], s);
+  return XG_OK;
+}
+
+// the facet kernels of one step: the patch matrices (affine: the basis-change
+// or quadrature kernels; deformed: k_patch_def), then the skeleton terms
+int rows_front_facets(xg_form* f, const double* d_lset, cudaStream_t s) {
+  const bool fp64 = f->precision == XG_PREC_FP64;
+  int st;
   if (f->has_patch && f->desc.npatch > 0) {
     if (f->d_patch_deform) {
       xg_mesh* m = f->mesh;
@@ -4133,7 +4171,6 @@ int rows_front(xg_form* f, const double* d_lset, const uint8_t* d_dom, cudaStrea
     }
   }
   if (f->desc.nskel > 0 && (st = launch_skel(f, d_lset, s))) return st;
-  if (f->use_ev) cudaEventRecord(f->ev[5], s);
   return XG_OK;
 }
 
