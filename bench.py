@@ -767,7 +767,13 @@ class Clocks:
 # entry says so).  Each entry names the kernel and the first 16 hex digits of
 # the sha256 of the source file it was captured on; when that file has
 # changed since, the line reports traffic null instead of a stale figure.
-TRAFFIC = {}
+# DRAM bytes (read + write) per launch of a stage's dominant kernel from one
+# ncu capture (dram__bytes_read.sum + dram__bytes_write.sum, one pass, on the
+# full-size workload), valid while the kernel's source file is unchanged
+TRAFFIC = {
+    ("c2", "patch"): {"bytes": 74788096 + 197305600, "source": "ngsxfem_gb300/csrc/xg_asm.cu",
+                      "sha16": "6196d8fa9c33b089"},
+}
 
 
 def traffic_for(workload, stage):
