@@ -319,8 +319,175 @@ __global__ void __launch_bounds__(StCfg<D, K, KT>::NT) k_st_elmat(int ne, int nv
   }
 }
 
+// P1 in space: the moment form.  With the spatial functions the barycentrics
+// lambda_j, every term's spatial integral at a time point is a combination
+// of the measure mu, the first moments mu_j = int lambda_j and the second
+// moments mu_jk = int lambda_j lambda_k of the part at that time point:
+//   mass       c psi_i psi_i' mu_jj'
+//   Laplace    c psi_i psi_i' mu (grad lambda_j . grad lambda_j')
+//   convection c psi_i psi_i' mu_j (b(t) . grad lambda_j')
+//   d/dtau     c psi_i dpsi_i' mu_jj'
+// (test (i, j), trial (i', j')).  One thread per prism: the time cuts, per
+// (time interval, time point) the level set, the part's rule points (the
+// straight cut of Decompose or the standard rule, as the quadrature-point
+// kernel above) summed into the moments, then the entries; FP64 throughout.
+template <int D, int KT, typename T>
+__global__ void __launch_bounds__(128) k_st_elmat_p1(int ne, int nv, const int32_t* __restrict__ elv,
+                                                     const double* __restrict__ xyz,
+                                                     const double* __restrict__ lset_st, StFormDesc form,
+                                                     const int32_t* __restrict__ list,
+                                                     const int* __restrict__ count_ptr,
+                                                     const int* __restrict__ slot_base, T* __restrict__ elmat,
+                                                     int* err) {
+  constexpr int NS = D + 1, NTB = KT + 1, N = NS * NTB, NM = NS * (NS + 1) / 2;
+  const int count = *count_ptr;
+  const int sbase = slot_base ? *slot_base : 0;
+  const int kl = form.kt_l;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < count; idx += gridDim.x * blockDim.x) {
+    const int e = list[idx];
+    double xv[D + 1][3], lst[3 * 4];
+    for (int v = 0; v <= D; v++) {
+      const int vid = elv[(int64_t)v * ne + e];
+      for (int i = 0; i <= kl; i++) lst[i * (D + 1) + v] = lset_st[(int64_t)i * nv + vid];
+      for (int c = 0; c < 3; c++) xv[v][c] = c < D ? xyz[(int64_t)c * nv + vid] : 0.0;
+    }
+    Geo<D> g;
+    make_geo<D>(xv, g);
+    const double meas = fabs(g.det);
+    double gl[D + 1][D];  // physical gradients of the barycentrics
+    for (int k = 0; k < D; k++) {
+      double sg = 0.0;
+      for (int a = 0; a < D; a++) {
+        gl[a][k] = g.Finv[a][k];
+        sg += g.Finv[a][k];
+      }
+      gl[D][k] = -sg;
+    }
+    double cut[2 * 4 + 2];
+    const int ncut = time_cuts<D>(kl, lst, cut);
+    double A[N * N];
+    for (int k = 0; k < N * N; k++) A[k] = 0.0;
+    double h = -1.0;
+    for (int q = 0; q < form.ngroups; q++) {
+      const StGroupDesc& Gq = form.g[q];
+      if (Gq.defined_on && !tbit64(Gq.defined_on, e)) continue;
+      double cf[7];
+      for (int k = 0; k < 7; k++) {
+        const int hp = Gq.hpow[k];
+        if (hp != 0 && h < 0) h = mesh_h<D>(meas);
+        cf[k] = hp == 0 ? Gq.c[k] : Gq.c[k] * int_pow(h, hp);
+      }
+      const bool uM = (Gq.used >> XG_TERM_MASS) & 1, uL = (Gq.used >> XG_TERM_LAPLACE) & 1;
+      const bool uC = (Gq.used >> XG_TERM_CONV) & 1, uT = (Gq.used >> 6) & 1;
+      const int ps = clamp_order(Gq.order), dt = Gq.domain;
+      const int sd = dt == XG_IF ? D - 1 : D;
+      const int nqc = c_rules.cnt[sd][ps], offc = c_rules.off[sd][ps];
+      const int nqs = c_rules.cnt[D][ps], offs = c_rules.off[D][ps];
+      const int pt = clamp_order(form.order_time);
+      const int nqt = c_rules.cnt[1][pt], offt = c_rules.off[1][pt];
+      const bool fixed = Gq.tref >= 0.0;
+      const int nco = fixed ? 1 : (ncut - 1) * nqt;
+      for (int c = 0; c < nco; c++) {
+        double t, wt, l[4];
+        if (fixed) {
+          t = Gq.tref;
+          wt = 1.0;
+          lset_trace<D>(kl, lst, Gq.tref, l);
+        } else {
+          const int iv = c / nqt, iq = c % nqt;
+          const double t0 = cut[iv], t1 = cut[iv + 1];
+          t = t0 + c_rules.x[offt + iq][0] * (t1 - t0);
+          wt = c_rules.w[offt + iq] * (t1 - t0);
+          lset_at<D>(kl, lst, t, l);
+        }
+        const int cls = check_if_straight_cut(l, D + 1);
+        if (cls != XG_IF && cls != dt) continue;
+        // the part's moments at this time point (reference measure)
+        double mu = 0.0, m1[NS], m2[NM];
+        for (int j = 0; j < NS; j++) m1[j] = 0.0;
+        for (int j = 0; j < NM; j++) m2[j] = 0.0;
+        auto point = [&](const double* xi, double w) {
+          double lam[NS], sl = 0.0;
+          for (int r = 0; r < D; r++) {
+            lam[r] = xi[r];
+            sl += xi[r];
+          }
+          lam[D] = 1.0 - sl;
+          mu += w;
+          int k = 0;
+          for (int j = 0; j < NS; j++) {
+            const double wl = w * lam[j];
+            m1[j] += wl;
+            for (int jj = j; jj < NS; jj++) m2[k++] += wl * lam[jj];
+          }
+        };
+        if (cls == XG_IF) {
+          Sub subs[3];
+          const int ns = decompose<D>(l, dt, subs);
+          if (ns < 0) {
+            set_err(err, -ns);
+            continue;
+          }
+          const double fac = dt == XG_IF ? if_factor<D>(g, l) : 1.0;
+          for (int s2 = 0; s2 < ns; s2++) {
+            const double vol = simplex_volume(subs[s2].p, sd + 1) * fac;
+            for (int b = 0; b < nqc; b++) {
+              double xi[3];
+              plain_point(subs[s2], sd + 1, c_rules.x[offc + b], xi);
+              point(xi, c_rules.w[offc + b] * vol);
+            }
+          }
+        } else {
+          for (int b = 0; b < nqs; b++) point(c_rules.x[offs + b], c_rules.w[offs + b]);
+        }
+        // time basis at t, the convection field b(t)
+        double psi[3], dpsi[3];
+        time_basis<double>(KT, t, psi, dpsi);
+        double bt[3] = {Gq.b[0], Gq.b[1], Gq.b[2]};
+        if (uC && Gq.omega != 0.0) {
+          const double tp = Gq.t0 + Gq.dt * t;
+          const double cs = cos(Gq.omega * tp), sn = sin(Gq.omega * tp);
+          for (int r = 0; r < 3; r++) bt[r] += Gq.bc[r] * cs + Gq.bs[r] * sn;
+        }
+        double bg[NS];  // b(t) . grad lambda_j
+        for (int j = 0; j < NS; j++) {
+          double sb = 0.0;
+          for (int k = 0; k < D; k++) sb += bt[k] * gl[j][k];
+          bg[j] = sb;
+        }
+        const double W = wt * meas;
+        for (int j = 0; j < NS; j++)
+          for (int jj = 0; jj < NS; jj++) {
+            const int lo = j < jj ? j : jj, hi = j < jj ? jj : j;
+            const double mjj = m2[lo * NS - lo * (lo - 1) / 2 + (hi - lo)];
+            double G = 0.0;
+            for (int k = 0; k < D; k++) G += gl[j][k] * gl[jj][k];
+            const double sM = (uM ? cf[XG_TERM_MASS] * mjj : 0.0) + (uL ? cf[XG_TERM_LAPLACE] * mu * G : 0.0) +
+                              (uC ? cf[XG_TERM_CONV] * m1[j] * bg[jj] : 0.0);
+            const double sT = uT ? cf[6] * mjj : 0.0;
+            for (int i = 0; i < NTB; i++)
+              for (int ii = 0; ii < NTB; ii++)
+                A[(i * NS + j) * N + ii * NS + jj] += W * (psi[i] * psi[ii] * sM + psi[i] * dpsi[ii] * sT);
+          }
+      }
+    }
+    T* out = elmat + (int64_t)(sbase + idx) * N * N;
+    for (int k = 0; k < N * N; k++) {
+      if (!finite_bits(A[k])) set_err(err, XG_ERR_NONFINITE);
+      out[k] = (T)A[k];
+    }
+  }
+}
+
 template <int D, int K, int KT, typename T>
 static int launch_one(const StLaunch& a, cudaStream_t s) {
+  if (K == 1) {
+    const int grid = 152 * 16;
+    k_st_elmat_p1<D, KT, T><<<grid, 128, 0, s>>>(a.ne, a.nv, a.elv, a.xyz, a.lset_st, a.desc, a.list, a.count,
+                                                 a.slot_base, (T*)a.elmat, a.err);
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? XG_OK : cuda_fail(e, "k_st_elmat_p1");
+  }
   using C = StCfg<D, K, KT>;
   auto kern = k_st_elmat<D, K, KT, T>;
   static int grid[2] = {0, 0};
