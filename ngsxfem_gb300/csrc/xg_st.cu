@@ -365,6 +365,16 @@ __global__ void __launch_bounds__(128) k_st_elmat_p1(int ne, int nv, const int32
     }
     double cut[2 * 4 + 2];
     const int ncut = time_cuts<D>(kl, lst, cut);
+    double GG[NM];  // grad lambda_j . grad lambda_k, j <= k
+    {
+      int k2 = 0;
+      for (int j = 0; j < NS; j++)
+        for (int jj = j; jj < NS; jj++) {
+          double sg = 0.0;
+          for (int k = 0; k < D; k++) sg += gl[j][k] * gl[jj][k];
+          GG[k2++] = sg;
+        }
+    }
     double A[N * N];
     for (int k = 0; k < N * N; k++) A[k] = 0.0;
     double h = -1.0;
@@ -456,18 +466,24 @@ __global__ void __launch_bounds__(128) k_st_elmat_p1(int ne, int nv, const int32
           bg[j] = sb;
         }
         const double W = wt * meas;
+        // the time factors W psi_i psi_i' and W psi_i dpsi_i'
+        double PP[NTB][NTB], PD[NTB][NTB];
+        for (int i = 0; i < NTB; i++)
+          for (int ii = 0; ii < NTB; ii++) {
+            PP[i][ii] = W * psi[i] * psi[ii];
+            PD[i][ii] = W * psi[i] * dpsi[ii];
+          }
+        const double cM = uM ? cf[XG_TERM_MASS] : 0.0, cL = uL ? cf[XG_TERM_LAPLACE] * mu : 0.0;
+        const double cC = uC ? cf[XG_TERM_CONV] : 0.0, cT = uT ? cf[6] : 0.0;
         for (int j = 0; j < NS; j++)
           for (int jj = 0; jj < NS; jj++) {
             const int lo = j < jj ? j : jj, hi = j < jj ? jj : j;
-            const double mjj = m2[lo * NS - lo * (lo - 1) / 2 + (hi - lo)];
-            double G = 0.0;
-            for (int k = 0; k < D; k++) G += gl[j][k] * gl[jj][k];
-            const double sM = (uM ? cf[XG_TERM_MASS] * mjj : 0.0) + (uL ? cf[XG_TERM_LAPLACE] * mu * G : 0.0) +
-                              (uC ? cf[XG_TERM_CONV] * m1[j] * bg[jj] : 0.0);
-            const double sT = uT ? cf[6] * mjj : 0.0;
+            const int kk = lo * NS - lo * (lo - 1) / 2 + (hi - lo);
+            const double sM = cM * m2[kk] + cL * GG[kk] + cC * m1[j] * bg[jj];
+            const double sT = cT * m2[kk];
             for (int i = 0; i < NTB; i++)
               for (int ii = 0; ii < NTB; ii++)
-                A[(i * NS + j) * N + ii * NS + jj] += W * (psi[i] * psi[ii] * sM + psi[i] * dpsi[ii] * sT);
+                A[(i * NS + j) * N + ii * NS + jj] += PP[i][ii] * sM + PD[i][ii] * sT;
           }
       }
     }
