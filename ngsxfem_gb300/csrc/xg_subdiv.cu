@@ -8,15 +8,12 @@
 //                           <= 4 in reference coordinates) of a P2 level set
 //                           given by its values at the vertices and edge
 //                           midpoints of the reference tetrahedron
-// Integrate: a group of NC^2 threads (NC = 8 children in 3D, 4 in 2D) runs
-// one element: the lattice checks of the root and of its children are split
-// over the group's threads (sign flags in shared memory), then every thread
-// walks the subtree of one grandchild (or the thread of a first-level leaf
-// fills it); per-thread sums are reduced in a fixed tree, per block and over
-// the blocks in order.  Moments: the trees of all elements level by level
-// (one thread per node and level, then one thread per leaf), so the warps of
-// each kernel run the same kind of work; the leaves' moments are summed per
-// element in a fixed order.  Repeated calls give the same bits.
+// Both build the trees of all elements level by level (one thread per node
+// and level, then one thread per leaf), so the warps of each kernel run the
+// same kind of work; the leaves' values (the integral, or the moments per
+// element) are summed in a fixed order, so repeated calls give the same
+// bits.  A thread walking one element's tree depth first (sd::element_rule,
+// the host check's path) ran its FP64 instructions 5.5 of 32 lanes full.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -48,145 +45,12 @@ __device__ __forceinline__ double sd_ipow(double x, int e) {
   return r;
 }
 
-template <int D>
-struct Grp {
-  static constexpr int NC = D == 3 ? 8 : 4;  // children of a simplex
-  static constexpr int TPE = NC * NC;        // threads per element
-  static constexpr int EPB = kSdThreads / TPE;
-};
-
-// sign flags (bit 0: a lattice point >= 0, bit 1: one < 0) of the lattice of
-// simplex v at level L, the share of thread t of nt
-template <int D, int K>
-__device__ int lattice_flags(const sd::Elem<D, K>& el, const double (*v)[3], int L, int t, int nt) {
-  const int np = 1 << L, side = np + 1, total = D == 2 ? side * side : side * side * side;
-  const double dx = 1.0 / np;
-  int f = 0;
-  for (int q = t; q < total && f != 3; q += nt) {
-    int I[3] = {q % side, (q / side) % side, D == 3 ? q / (side * side) : 0};
-    if (I[0] + I[1] + I[2] > np) continue;
-    double xi[3];
-    sd::lattice_point<D>(v, I, dx, xi);
-    f |= sd::lset_at(el, xi) >= 0.0 ? 1 : 2;
-  }
-  return f;
-}
-
-// thread t of an element's group: its share of the element's rule.  flags:
-// the element's NC + 1 shared words; every thread of the block calls this
-// (the block synchronises four times), those without an element pass live = false.
-// The tree is the serial one of sd::element_rule: the root checked at level
-// L, its children (if it is cut and L >= 1) at L - 1, each cut child's
-// children walked by sd::node_rule from level L - 2.
-template <int D, int K, class E>
-__device__ int group_rule(const RuleTable* Rp, const sd::Elem<D, K>& el, bool live, int dt, int order, int L, int t,
-                          int* flags, E& emit) {
-  constexpr int NC = Grp<D>::NC, TPE = Grp<D>::TPE;
-  const int S = L < 2 ? L : 2;  // tree levels split over the group
-  double root[4][3];
-  sd::ref_simplex(D, root);
-  __syncthreads();  // the group's flags of the previous element are read
-  if (t <= NC) flags[t] = 0;
-  __syncthreads();
-  if (live && S >= 1) {
-    const int f = lattice_flags(el, root, L, t, TPE);
-    if (f) atomicOr(&flags[0], f);
-  }
-  __syncthreads();
-  const bool root_cut = flags[0] == 3;
-  if (live && S >= 2 && root_cut) {
-    double cv[4][3];
-    sd::child<D>(root, t / NC, cv);
-    const int f = lattice_flags(el, cv, L - 1, t % NC, NC);
-    if (f) atomicOr(&flags[1 + t / NC], f);
-  }
-  __syncthreads();
-  if (!live) return 0;
-  if (S == 0) return t == 0 ? sd::node_rule(Rp, el, root, L, dt, order, emit) : 0;
-  if (!root_cut) {
-    // an uncut root (flags 1: POS, 2: NEG) is filled as a whole
-    if (t == 0 && (flags[0] == 1 ? XG_POS : XG_NEG) == dt) sd::fill(Rp, el, root, (const double*)nullptr, dt, order, emit);
-    return 0;
-  }
-  double cv[4][3];
-  if (S == 1) {
-    if (t >= NC) return 0;
-    sd::child<D>(root, t, cv);
-    return sd::node_rule(Rp, el, cv, L - 1, dt, order, emit);
-  }
-  const int c1 = t / NC, c2 = t % NC, fc = flags[1 + c1];
-  sd::child<D>(root, c1, cv);
-  if (fc != 3) {
-    if (c2 == 0 && (fc == 1 ? XG_POS : XG_NEG) == dt) sd::fill(Rp, el, cv, (const double*)nullptr, dt, order, emit);
-    return 0;
-  }
-  double gv[4][3];
-  sd::child<D>(cv, c2, gv);
-  return sd::node_rule(Rp, el, gv, L - 2, dt, order, emit);
-}
-
-template <int D, int K>
-__global__ void __launch_bounds__(kSdThreads) k_subdiv_integrate(int ne, int nv, const int32_t* __restrict__ elv,
-                                                                  const double* __restrict__ xyz,
-                                                                  const int32_t* __restrict__ el_dofs,
-                                                                  const double* __restrict__ coefs, int dt, int order,
-                                                                  int levels, int ex, int ey, int ez,
-                                                                  const uint64_t* __restrict__ defined_on,
-                                                                  double* __restrict__ block_sums, int* err) {
-  constexpr int N = ndof_el(D, K), TPE = Grp<D>::TPE, EPB = Grp<D>::EPB;
-  __shared__ double red[kSdThreads];
-  __shared__ int flags[EPB][Grp<D>::NC + 1];
-  const int le = threadIdx.x / TPE, t = threadIdx.x % TPE;
-  double acc = 0.0;
-  for (int64_t base = (int64_t)blockIdx.x * EPB; base < ne; base += (int64_t)gridDim.x * EPB) {
-    const int64_t e = base + le;
-    bool live = e < ne && (!defined_on || sd_bit(defined_on, e));
-    sd::Elem<D, K> el;
-    if (live) {
-      int gv[4] = {0, 0, 0, 0};
-      double xv[4][3];
-      for (int v = 0; v <= D; v++) {
-        gv[v] = elv[(int64_t)v * ne + e];
-        for (int c = 0; c < 3; c++) xv[v][c] = c < D ? xyz[(int64_t)c * nv + gv[v]] : 0.0;
-      }
-      for (int r = 0; r < 3; r++) {
-        el.x0[r] = xv[D][r];
-        for (int c = 0; c < 3; c++) el.F[r][c] = c < D ? xv[c][r] - xv[D][r] : 0.0;
-      }
-      for (int i = 0; i < N; i++) {
-        el.coef[i] = coefs[el_dofs[(int64_t)i * ne + e]];
-        el.desc[i] = fn_desc<D, K>(i, gv);
-      }
-    }
-    auto emit = [&](const double* x, double w) {
-      acc += w * sd_ipow(x[0], ex) * sd_ipow(x[1], ey) * (D == 3 ? sd_ipow(x[2], ez) : 1.0);
-    };
-    const int st = group_rule<D, K>(&g_sd_rules, el, live, dt, order, levels, t, flags[le], emit);
-    if (st) set_err(err, st);
-  }
-  red[threadIdx.x] = acc;
-  __syncthreads();
-  for (int s = kSdThreads / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) block_sums[blockIdx.x] = red[0];
-}
-
 __global__ void k_sd_sum(const double* v, int n, double* out) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
     double s = 0.0;
     for (int i = 0; i < n; i++) s += v[i];
     out[0] = s;
   }
-}
-
-template <int D, int K>
-void launch_int(xg_space* sp, const double* coefs, int dt, int order, int levels, int ex, int ey, int ez,
-                const uint64_t* defined_on, double* bs, cudaStream_t s) {
-  xg_mesh* m = sp->mesh;
-  k_subdiv_integrate<D, K><<<kSdBlocks, kSdThreads, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, sp->d_el_dofs, coefs,
-                                                           dt, order, levels, ex, ey, ez, defined_on, bs, m->d_err);
 }
 
 // ---- breadth-first moments ---------------------------------------------------------
@@ -385,14 +249,15 @@ __global__ void k_sd_scan_add(int32_t* out, int64_t n, const int32_t* bsum) {
 
 __global__ void __launch_bounds__(128) k_sd_emit(const SdNode* __restrict__ nodes, int64_t nn,
                                                  const uint8_t* __restrict__ cls, const int32_t* __restrict__ pos3,
-                                                 int depth, SdNode* __restrict__ next, SdNode* __restrict__ plain,
-                                                 SdNode* __restrict__ cut, int32_t* __restrict__ plain_depth) {
+                                                 int depth, int nch, SdNode* __restrict__ next,
+                                                 SdNode* __restrict__ plain, SdNode* __restrict__ cut,
+                                                 int32_t* __restrict__ plain_depth) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nn; i += (int64_t)gridDim.x * blockDim.x) {
     const SdNode nd = nodes[i];
     const int c = cls[i];
     if (c == SD_EXPAND) {
       const int64_t o = pos3[i];
-      for (int k = 0; k < 8; k++) next[o + k] = SdNode{nd.item, nd.path | ((uint32_t)k << (3 * depth))};
+      for (int k = 0; k < nch; k++) next[o + k] = SdNode{nd.item, nd.path | ((uint32_t)k << (3 * depth))};
     } else if (c == SD_PLAIN) {
       plain[pos3[nn + i]] = nd;
       plain_depth[pos3[nn + i]] = depth;
@@ -555,7 +420,7 @@ int sd_bfs_chunk(const double* d_vals10, const int32_t* d_list, int64_t base, in
     if (int st = nb_plain.get(sizeof(SdNode) * (size_t)h_t[1], s)) return st;
     if (int st = nb_pd.get(sizeof(int32_t) * (size_t)h_t[1], s)) return st;
     if (int st = nb_cut.get(sizeof(SdNode) * (size_t)h_t[2], s)) return st;
-    k_sd_emit<<<sd_grid(nn), 128, 0, s>>>(cur, nn, cls, pos3, depth, (SdNode*)nb_next.p, (SdNode*)nb_plain.p,
+    k_sd_emit<<<sd_grid(nn), 128, 0, s>>>(cur, nn, cls, pos3, depth, 8, (SdNode*)nb_next.p, (SdNode*)nb_plain.p,
                                           (SdNode*)nb_cut.p, (int32_t*)nb_pd.p);
     XG_CUDA(cudaGetLastError());
     nplain.push_back(h_t[1]);
@@ -604,6 +469,230 @@ int sd_bfs_chunk(const double* d_vals10, const int32_t* d_list, int64_t base, in
   return e == cudaSuccess ? XG_OK : cuda_fail(e, "k_sd_bfs");
 }
 
+// ---- breadth-first Integrate --------------------------------------------------------
+// The same level-by-level tree for the elements of a mesh and a level set of
+// order K given by its H1 coefficients: nodes (element, path), per level a
+// classification (the roots outside the element set drop out), the leaves
+// filled one thread each with the integrand x^e, and the leaf values summed
+// in a fixed order (block ranges, then the blocks, then the chunks).
+
+struct SdMesh {
+  int ne, nv;
+  const int32_t* elv;
+  const double* xyz;
+  const int32_t* el_dofs;  // [nd][ne]
+  const double* coefs;
+  const uint64_t* defined_on;
+};
+
+template <int D, int K>
+__device__ __forceinline__ void sdi_elem(const SdMesh& M, int64_t e, sd::Elem<D, K>& el) {
+  int gv[4] = {0, 0, 0, 0};
+  double xv[4][3];
+  for (int v = 0; v <= D; v++) {
+    gv[v] = M.elv[(int64_t)v * M.ne + e];
+    for (int c = 0; c < 3; c++) xv[v][c] = c < D ? M.xyz[(int64_t)c * M.nv + gv[v]] : 0.0;
+  }
+  for (int r = 0; r < 3; r++) {
+    el.x0[r] = xv[D][r];
+    for (int c = 0; c < 3; c++) el.F[r][c] = c < D ? xv[c][r] - xv[D][r] : 0.0;
+  }
+  for (int i = 0; i < sd::Elem<D, K>::N; i++) {
+    el.coef[i] = M.coefs[M.el_dofs[(int64_t)i * M.ne + e]];
+    el.desc[i] = fn_desc<D, K>(i, gv);
+  }
+}
+
+template <int D>
+__device__ __forceinline__ void sdi_simplex(uint32_t path, int depth, double (*v)[3]) {
+  sd::ref_simplex(D, v);
+  for (int d = 0; d < depth; d++) {
+    double w[4][3];
+    sd::child<D>(v, (int)((path >> (3 * d)) & 7u), w);
+    for (int i = 0; i < 4; i++)
+      for (int r = 0; r < 3; r++) v[i][r] = w[i][r];
+  }
+}
+
+template <int D, int K>
+__global__ void __launch_bounds__(128) k_sdi_classify(const SdNode* __restrict__ nodes, int64_t nn, SdMesh M,
+                                                      int64_t base, int depth, int lev, int dt,
+                                                      uint8_t* __restrict__ cls, int32_t* __restrict__ cnt3) {
+  constexpr int NC = D == 2 ? 4 : 8;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nn; i += (int64_t)gridDim.x * blockDim.x) {
+    const SdNode nd = nodes[i];
+    const int64_t e = base + nd.item;
+    int c = SD_NONE;
+    if (depth > 0 || !M.defined_on || sd_bit(M.defined_on, e)) {
+      sd::Elem<D, K> el;
+      sdi_elem<D, K>(M, e, el);
+      double v[4][3];
+      sdi_simplex<D>(nd.path, depth, v);
+      const int dself = sd::lattice_domain(el, v, lev);
+      if (dself != XG_IF) {
+        c = dself == dt ? SD_PLAIN : SD_NONE;
+      } else if (lev == 0) {
+        double l[4];
+        for (int k = 0; k <= D; k++) l[k] = sd::lset_at(el, v[k]);
+        const int dv = sd::vertex_domain(l, D + 1);
+        c = dv == XG_IF ? SD_CUT : (dv == dt ? SD_PLAIN : SD_NONE);
+      } else {
+        c = SD_EXPAND;
+      }
+    }
+    cls[i] = (uint8_t)c;
+    cnt3[i] = c == SD_EXPAND ? NC : 0;
+    cnt3[nn + i] = c == SD_PLAIN ? 1 : 0;
+    cnt3[2 * nn + i] = c == SD_CUT ? 1 : 0;
+  }
+}
+
+// one thread per leaf: the integral of x^e over its part
+template <int D, int K>
+__global__ void __launch_bounds__(128) k_sdi_fill(const SdNode* __restrict__ leaves,
+                                                  const int32_t* __restrict__ depths, int64_t nl, int cut_depth,
+                                                  SdMesh M, int64_t base, int dt, int order, int ex, int ey, int ez,
+                                                  double* __restrict__ val, int* err) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nl; i += (int64_t)gridDim.x * blockDim.x) {
+    const SdNode nd = leaves[i];
+    sd::Elem<D, K> el;
+    sdi_elem<D, K>(M, base + nd.item, el);
+    double v[4][3];
+    sdi_simplex<D>(nd.path, depths ? depths[i] : cut_depth, v);
+    double acc = 0.0;
+    auto emit = [&](const double* x, double w) {
+      acc += w * sd_ipow(x[0], ex) * sd_ipow(x[1], ey) * (D == 3 ? sd_ipow(x[2], ez) : 1.0);
+    };
+    if (depths) {
+      sd::fill(&g_sd_rules, el, v, (const double*)nullptr, dt, order, emit);
+    } else {
+      double l[4];
+      for (int k = 0; k <= D; k++) l[k] = sd::lset_at(el, v[k]);
+      const int st = sd::fill(&g_sd_rules, el, v, l, dt, order, emit);
+      if (st) set_err(err, st);
+    }
+    val[i] = acc;
+  }
+}
+
+// fixed-order sum of n values: block b sums its range [b * per, (b + 1) * per)
+// in a tree, then one thread adds the blocks' sums in order into out
+__global__ void __launch_bounds__(kSdThreads) k_sdi_blocks(const double* __restrict__ v, int64_t n,
+                                                          double* __restrict__ bs) {
+  __shared__ double red[kSdThreads];
+  const int64_t per = (n + gridDim.x - 1) / gridDim.x;
+  const int64_t b0 = blockIdx.x * per, b1 = b0 + per < n ? b0 + per : n;
+  double acc = 0.0;
+  for (int64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) acc += v[i];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int st = kSdThreads / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st) red[threadIdx.x] += red[threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) bs[blockIdx.x] = red[0];
+}
+
+template <int D, int K>
+int sdi_chunk(const SdMesh& M, int64_t base, int64_t items, int levels, int dt, int order, int ex, int ey, int ez,
+              double* d_partial, int* d_err, cudaStream_t s) {
+  constexpr int NC = D == 2 ? 4 : 8;
+  SdBuf b_cur;
+  if (int st = b_cur.get(sizeof(SdNode) * items, s)) return st;
+  {
+    std::vector<SdNode> h(items);
+    for (int64_t i = 0; i < items; i++) h[i] = SdNode{(int32_t)i, 0u};
+    XG_CUDA(cudaMemcpyAsync(b_cur.p, h.data(), sizeof(SdNode) * items, cudaMemcpyHostToDevice, s));
+    XG_CUDA(cudaStreamSynchronize(s));
+  }
+  std::vector<SdBuf> plain_b, pdepth_b;
+  std::vector<int64_t> nplain;
+  int64_t ncut = 0;
+  SdBuf cut_final, next_b, cur_owner;
+  SdNode* cur = (SdNode*)b_cur.p;
+  int64_t nn = items;
+  for (int depth = 0; depth <= levels && nn > 0; depth++) {
+    const int lev = levels - depth;
+    SdBuf w;
+    const int nb = (int)((3 * nn + kSdScan - 1) / kSdScan);
+    if (int st = w.get(nn + 8 * 6 * nn + 4 * (size_t)nb + 64, s)) return st;
+    uint8_t* cls = (uint8_t*)w.p;
+    int32_t* cnt3 = (int32_t*)(((uintptr_t)w.p + nn + 15) & ~(uintptr_t)15);
+    int32_t* pos3 = cnt3 + 3 * nn;
+    int32_t* tots = pos3 + 3 * nn;
+    int32_t* bsum = tots + 4;
+    k_sdi_classify<D, K><<<sd_grid(nn), 128, 0, s>>>(cur, nn, M, base, depth, lev, dt, cls, cnt3);
+    for (int q = 0; q < 3; q++)
+      if (int st = sd_scan(cnt3 + q * nn, nn, pos3 + q * nn, bsum, tots + q, s)) return st;
+    int32_t h_t[3];
+    XG_CUDA(cudaMemcpyAsync(h_t, tots, sizeof(h_t), cudaMemcpyDeviceToHost, s));
+    XG_CUDA(cudaStreamSynchronize(s));
+    SdBuf nb_next, nb_plain, nb_pd, nb_cut;
+    if (int st = nb_next.get(sizeof(SdNode) * (size_t)h_t[0], s)) return st;
+    if (int st = nb_plain.get(sizeof(SdNode) * (size_t)h_t[1], s)) return st;
+    if (int st = nb_pd.get(sizeof(int32_t) * (size_t)h_t[1], s)) return st;
+    if (int st = nb_cut.get(sizeof(SdNode) * (size_t)h_t[2], s)) return st;
+    k_sd_emit<<<sd_grid(nn), 128, 0, s>>>(cur, nn, cls, pos3, depth, NC, (SdNode*)nb_next.p, (SdNode*)nb_plain.p,
+                                          (SdNode*)nb_cut.p, (int32_t*)nb_pd.p);
+    XG_CUDA(cudaGetLastError());
+    nplain.push_back(h_t[1]);
+    plain_b.push_back(std::move(nb_plain));
+    pdepth_b.push_back(std::move(nb_pd));
+    if (h_t[2] > 0) {
+      ncut = h_t[2];  // cut leaves appear only at level 0 (the last depth)
+      cut_final = std::move(nb_cut);
+    }
+    cur_owner = std::move(next_b);
+    next_b = std::move(nb_next);
+    cur = (SdNode*)next_b.p;
+    nn = h_t[0];
+  }
+  // values of the plain leaves (level-major) and the cut leaves, then their sum
+  int64_t np = 0;
+  for (int64_t x : nplain) np += x;
+  SdBuf vals, bs;
+  if (int st = vals.get(sizeof(double) * (np + ncut), s)) return st;
+  if (int st = bs.get(sizeof(double) * kSdBlocks, s)) return st;
+  double* val = (double*)vals.p;
+  int64_t o = 0;
+  for (size_t q = 0; q < nplain.size(); q++) {
+    if (nplain[q])
+      k_sdi_fill<D, K><<<sd_grid(nplain[q]), 128, 0, s>>>((const SdNode*)plain_b[q].p, (const int32_t*)pdepth_b[q].p,
+                                                          nplain[q], 0, M, base, dt, order, ex, ey, ez, val + o, d_err);
+    o += nplain[q];
+  }
+  if (ncut > 0)
+    k_sdi_fill<D, K><<<sd_grid(ncut), 128, 0, s>>>((const SdNode*)cut_final.p, nullptr, ncut, levels, M, base, dt,
+                                                    order, ex, ey, ez, val + o, d_err);
+  const int64_t nv = np + ncut;
+  const int nbk = (int)(nv < kSdBlocks * (int64_t)kSdThreads ? (nv + kSdThreads - 1) / kSdThreads : kSdBlocks);
+  if (nv > 0) {
+    k_sdi_blocks<<<nbk, kSdThreads, 0, s>>>(val, nv, (double*)bs.p);
+    k_sd_sum<<<1, 32, 0, s>>>((const double*)bs.p, nbk, d_partial);
+  } else {
+    XG_CUDA(cudaMemsetAsync(d_partial, 0, sizeof(double), s));
+  }
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? XG_OK : cuda_fail(e, "k_sdi");
+}
+
+template <int D, int K>
+int sdi_run(const SdMesh& M, int levels, int dt, int order, int ex, int ey, int ez, double* d_result, int* d_err,
+            cudaStream_t s) {
+  const int64_t chunk = (int64_t)1 << 15, ne = M.ne;
+  const int64_t nch = (ne + chunk - 1) / chunk;
+  SdBuf parts;
+  if (int st = parts.get(sizeof(double) * (nch > 0 ? nch : 1), s)) return st;
+  for (int64_t c = 0; c < nch; c++) {
+    const int64_t b = c * chunk, m = ne - b < chunk ? ne - b : chunk;
+    if (int st = sdi_chunk<D, K>(M, b, m, levels, dt, order, ex, ey, ez, (double*)parts.p + c, d_err, s)) return st;
+  }
+  if (nch > 0) k_sd_sum<<<1, 32, 0, s>>>((const double*)parts.p, (int)nch, d_result);
+  else XG_CUDA(cudaMemsetAsync(d_result, 0, sizeof(double), s));
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? XG_OK : cuda_fail(e, "k_sd_sum");
+}
+
 }  // namespace
 
 int subdiv_moments_launch(const double* d_vals10, int64_t n, int levels, double* d_out35, const int32_t* d_list,
@@ -646,28 +735,23 @@ int xg_integrate_subdiv(xg_space* sp, const double* d_lset_coefs, int dt, int or
   if (st) return st;
   xg_mesh* m = sp->mesh;
   cudaStream_t s = (cudaStream_t)stream;
-  const size_t need = kSdBlocks * sizeof(double);
-  if (m->scratch_bytes < need) {
-    cudaFree(m->d_scratch);
-    m->d_scratch = nullptr;
-    m->scratch_bytes = 0;
-    XG_CUDA(cudaMalloc(&m->d_scratch, need));
-    m->scratch_bytes = need;
-  }
-  double* bs = (double*)m->d_scratch;
+  SdMesh M;
+  M.ne = m->ne;
+  M.nv = m->nv;
+  M.elv = m->d_elv;
+  M.xyz = m->d_xyz;
+  M.el_dofs = sp->d_el_dofs;
+  M.coefs = d_lset_coefs;
+  M.defined_on = d_defined_on;
   const int D = m->dim, K = sp->order;
   if (D == 2) {
-    if (K == 1) launch_int<2, 1>(sp, d_lset_coefs, dt, order, subdivlvl, ex, ey, ez, d_defined_on, bs, s);
-    else if (K == 2) launch_int<2, 2>(sp, d_lset_coefs, dt, order, subdivlvl, ex, ey, ez, d_defined_on, bs, s);
-    else launch_int<2, 3>(sp, d_lset_coefs, dt, order, subdivlvl, ex, ey, ez, d_defined_on, bs, s);
-  } else {
-    if (K == 1) launch_int<3, 1>(sp, d_lset_coefs, dt, order, subdivlvl, ex, ey, ez, d_defined_on, bs, s);
-    else if (K == 2) launch_int<3, 2>(sp, d_lset_coefs, dt, order, subdivlvl, ex, ey, ez, d_defined_on, bs, s);
-    else launch_int<3, 3>(sp, d_lset_coefs, dt, order, subdivlvl, ex, ey, ez, d_defined_on, bs, s);
+    if (K == 1) return sdi_run<2, 1>(M, subdivlvl, dt, order, ex, ey, ez, d_result, m->d_err, s);
+    if (K == 2) return sdi_run<2, 2>(M, subdivlvl, dt, order, ex, ey, ez, d_result, m->d_err, s);
+    return sdi_run<2, 3>(M, subdivlvl, dt, order, ex, ey, ez, d_result, m->d_err, s);
   }
-  k_sd_sum<<<1, 32, 0, s>>>(bs, kSdBlocks, d_result);
-  const cudaError_t e = cudaGetLastError();
-  return e == cudaSuccess ? XG_OK : cuda_fail(e, "k_subdiv_integrate");
+  if (K == 1) return sdi_run<3, 1>(M, subdivlvl, dt, order, ex, ey, ez, d_result, m->d_err, s);
+  if (K == 2) return sdi_run<3, 2>(M, subdivlvl, dt, order, ex, ey, ez, d_result, m->d_err, s);
+  return sdi_run<3, 3>(M, subdivlvl, dt, order, ex, ey, ez, d_result, m->d_err, s);
 }
 
 int xg_subdiv_moments_tet(const double* d_vals10, int64_t n, int subdivlvl, double* d_out35, int* d_err,
