@@ -274,7 +274,9 @@ int xg_mlset_rule_capacity(int dim, int32_t nlsets, int32_t ndomains, int order)
 /* The deformation of xg_iso_integrate_mesh alone: d_gdef[edge][3] (edges in
  * the mesh's edge numbering) = the physical edge coefficients J theta of the
  * P2 shift, averaged over the band elements sharing the edge; 0 off the
- * band.  For bilinear forms on the deformed mesh (xg_cterm.d_deform). */
+ * band.  For bilinear forms on the deformed mesh (xg_cterm.d_deform).  It
+ * uses the mesh's isoparametric workspace, as xg_iso_integrate_mesh does:
+ * those calls on one mesh must not overlap on the GPU. */
 int xg_iso_deformation(xg_mesh* mesh, const double* d_p2vals, double threshold, double* d_gdef, int32_t* d_nonconv,
                        void* stream);
 int xg_iso_integrate_mesh(xg_mesh* mesh, const double* d_p2vals, int dt, int order, double threshold, int deform,
