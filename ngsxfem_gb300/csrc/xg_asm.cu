@@ -2551,6 +2551,7 @@ struct xg_form {
   const double* d_patch_deform = nullptr;  // xg_form_set_deformation: patch terms on the deformed mesh
   cudaStream_t side = nullptr;             // the facet kernels' stream (forked from and joined into the step's)
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  bool rows_marked = false;  // the step's active rows were marked in rows_front
   FormDesc desc;
   int needs_mask = 0;  // domains needing decompositions on cut elements
   int el_sym = 0;      // every volume group symmetric: packed element matrices
@@ -3999,7 +4000,7 @@ int xg_form_check(xg_form* f) {
 }  // extern "C"
 
 namespace {
-int rows_front(xg_form* f, const double* d_lset, const uint8_t* d_dom, cudaStream_t s);
+int rows_front(xg_form* f, const double* d_lset, const uint8_t* d_dom, xg_csr* out, cudaStream_t s);
 int rows_front_facets(xg_form* f, const double* d_lset, cudaStream_t s);
 int rows_back(xg_form* f, xg_csr* out, cudaStream_t s);
 int assemble_front(xg_form* f, const double* d_lset, const uint8_t* d_dom, xg_csr* out, void* stream);
@@ -4104,7 +4105,7 @@ CoefFormLaunch coef_args(xg_form* f, const double* d_lset, const uint8_t* d_dom)
 // the element and patch kernels of one step (spatial forms: the element rows
 // at their static slots and the patch matrices by facet slot; the patch
 // matrices are left out when the form's patches run in a batched launch)
-int rows_front(xg_form* f, const double* d_lset, const uint8_t* d_dom, cudaStream_t s) {
+int rows_front(xg_form* f, const double* d_lset, const uint8_t* d_dom, xg_csr* out, cudaStream_t s) {
   const bool fp64 = f->precision == XG_PREC_FP64;
   int st;
   // the facet kernels (patch, skeleton) write the facet matrices, the element
@@ -4112,6 +4113,7 @@ int rows_front(xg_form* f, const double* d_lset, const uint8_t* d_dom, cudaStrea
   // stream of the form, forked from and joined back into s (in a captured
   // step they become concurrent branches of the graph)
   const bool fork = !f->use_ev && f->has_patch && (f->desc.npatch > 0 || f->desc.nskel > 0);
+  f->rows_marked = false;
   cudaStream_t sf = s;
   if (fork) {
     if (!f->side) {
@@ -4129,6 +4131,10 @@ int rows_front(xg_form* f, const double* d_lset, const uint8_t* d_dom, cudaStrea
   if (f->bnd.n > 0 && (st = bnd_elmat_launch(bnd_args(f, d_lset), s))) return st;
   if (f->cdesc.n > 0 && (st = coef_elmat_launch(coef_args(f, d_lset, d_dom), s))) return st;
   if (fork) {
+    // the active rows need only the lists: they are marked while the facet
+    // kernels run (rows_back then skips this pass)
+    if ((st = mark_rows(f, out, s))) return st;
+    f->rows_marked = true;
     XG_CUDA(cudaEventRecord(f->ev_join, sf));
     XG_CUDA(cudaStreamWaitEvent(s, f->ev_join, 0));
   } else if ((st = rows_front_facets(f, d_lset, s))) {
@@ -4177,7 +4183,8 @@ int rows_front_facets(xg_form* f, const double* d_lset, cudaStream_t s) {
 // active rows, then the fixed-order row sums and the compressed output
 int rows_back(xg_form* f, xg_csr* out, cudaStream_t s) {
   int st;
-  if ((st = mark_rows(f, out, s))) return st;
+  if (!f->rows_marked && (st = mark_rows(f, out, s))) return st;
+  f->rows_marked = false;
   if (f->use_ev) cudaEventRecord(f->ev[6], s);
   st = rows_scatter(rows_args(f, out->d_row_dof), f->space->ndof, f->has_patch, f->precision == XG_PREC_FP64,
                     f->d_elmat, f->d_famat, out->d_rowptr, out->d_counts, out->d_cols, out->d_vals, out->cap_nnz,
@@ -4216,7 +4223,7 @@ int assemble_front(xg_form* f, const double* d_lset, const uint8_t* d_dom, xg_cs
     XG_CUDA(cudaMemsetAsync(f->d_counts + 2, 0, sizeof(int), s));
   }
   if (f->use_ev) cudaEventRecord(f->ev[2], s);
-  if (f->rows) return rows_front(f, d_lset, d_dom, s);
+  if (f->rows) return rows_front(f, d_lset, d_dom, out, s);
   // 2. element and patch matrices (the cut list's slots follow the uncut list's)
   if (f->precision == XG_PREC_FP64) {
     if ((st = dispatch_volume<double>(f, d_lset, d_dom, s))) return st;
