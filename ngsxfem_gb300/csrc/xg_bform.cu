@@ -6,7 +6,8 @@
 // owner's basis at the rule's physical points (the relations of
 // xg_lfbnd.cuh), summed in FP64 and added to the owner's element rows (which
 // the volume kernels wrote first); one thread owns an element's rows, so the
-// sums need no atomics and are formed in the same order on every run.
+// sums need no atomics and are formed in the same order on every run.  An
+// owner is active when one of its BND elements has a part in a term's domain.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -29,19 +30,25 @@ namespace {
 __device__ __forceinline__ bool bf_bit64(const uint64_t* b, int64_t i) { return (b[i >> 6] >> (i & 63)) & 1ull; }
 __device__ __forceinline__ bool bf_bit32(const uint32_t* b, int64_t i) { return (b[i >> 5] >> (i & 31)) & 1u; }
 
-// owners with a boundary term on one of their BND elements join the active
-// elements (as uncut-list elements when they are not active already)
-__global__ void k_bnd_active(int n_own, const int32_t* __restrict__ own_el, const int32_t* __restrict__ own_ptr,
-                             const int32_t* __restrict__ own_bnd, BndDesc d, uint32_t* __restrict__ act_un,
-                             const uint32_t* __restrict__ act_cut) {
+// owners of a BND element that has a part in a boundary term's domain (its
+// straight-cut domain type, CheckIfStraightCut of its vertex values, is the
+// term's domain or IF) join the active elements (as uncut-list elements
+// when they are not active already)
+__global__ void k_bnd_active(BndFormLaunch L) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n_own) return;
-  const int e = own_el[i];
+  if (i >= L.n_own) return;
+  const int e = L.own_el[i];
   bool on = false;
-  for (int j = own_ptr[i]; j < own_ptr[i + 1] && !on; j++)
-    for (int t = 0; t < d.n; t++)
-      if (!d.t[t].defined_on || bf_bit64(d.t[t].defined_on, own_bnd[j])) on = true;
-  if (on && !bf_bit32(act_cut, e)) atomicOr(&act_un[e >> 5], 1u << (e & 31));
+  for (int j = L.own_ptr[i]; j < L.own_ptr[i + 1] && !on; j++) {
+    const int b = L.own_bnd[j];
+    double l[3];
+    for (int v = 0; v < L.dim; v++) l[v] = L.lset[L.bnd_v[(int64_t)v * L.nbnd + b]];
+    const int dom = qc::qcheck(l, L.dim, 0.0);
+    for (int t = 0; t < L.d.n; t++)
+      if ((!L.d.t[t].defined_on || bf_bit64(L.d.t[t].defined_on, b)) && (dom == XG_IF || dom == L.d.t[t].domain))
+        on = true;
+  }
+  if (on && !bf_bit32(L.act_cut, e)) atomicOr(&L.act_un[e >> 5], 1u << (e & 31));
 }
 
 template <int D, int K, typename T>
@@ -137,8 +144,7 @@ int launch_k(const BndFormLaunch& L, cudaStream_t s) {
 
 int bnd_active_launch(const BndFormLaunch& L, cudaStream_t s) {
   if (L.n_own <= 0) return XG_OK;
-  k_bnd_active<<<(L.n_own + 127) / 128, 128, 0, s>>>(L.n_own, L.own_el, L.own_ptr, L.own_bnd, L.d, L.act_un,
-                                                     L.act_cut);
+  k_bnd_active<<<(L.n_own + 127) / 128, 128, 0, s>>>(L);
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? XG_OK : cuda_fail(e, "k_bnd_active");
 }

@@ -2179,8 +2179,21 @@ orc_csr* orc_assemble_full(const orc_space* s, const double* lset_vertex, const 
         const int b = (int)bfac.size();
         bfac.push_back((int32_t)f);
         bown.push_back(s->facet_els[2 * f]);
+        // the BND element's domain type (CheckIfStraightCut of its vertex values)
+        const int e0 = s->facet_els[2 * f], D = s->D;
+        int lf = 0;
+        while (s->el_facets[(size_t)e0 * (D + 1) + lf] != f) lf++;
+        bool hp = false, hn = false;
+        for (int q = 0; q < D; q++) {
+          const int vq = s->elv[(size_t)e0 * (D + 1) + (D == 2 ? TRI_EDGES[lf][q] : TET_FACES[lf][q])];
+          hp |= lset_vertex[vq] > 0.0;
+          hn |= lset_vertex[vq] < 0.0;
+        }
+        const int dom = (hp && hn) || (!hp && !hn) ? ORC_IF : (hn ? ORC_NEG : ORC_POS);
         for (int t = 0; t < nbterms; t++)
-          if (!bterms[t].defined_on || test_bit(bterms[t].defined_on, b)) bnd_act[s->facet_els[2 * f]] = 1;
+          if ((!bterms[t].defined_on || test_bit(bterms[t].defined_on, b)) &&
+              (dom == ORC_IF || dom == bterms[t].domain))
+            bnd_act[e0] = 1;
       }
   }
   int nact = 0;
