@@ -345,9 +345,11 @@ int xg_form_set_defined_on(xg_form* form, int32_t t, const uint64_t* d_defined_o
  * P1 level set on the boundary facet and h of the owning element.  The
  * reference's SymbolicCutBFI on boundary elements
  * (xfem/symboliccutbfi.cpp:76-486 with vb == BND, the rule of
- * cutint/straightcutrule.cpp:582-677).  Every owner of a BND element in a
- * term's set joins the active elements; its matrix is the sum of its volume
- * and boundary terms.  Spatial forms on simplex meshes; order -1 = 2k. */
+ * cutint/straightcutrule.cpp:582-677).  The owner of a BND element in a
+ * term's set whose domain type (CheckIfStraightCut of its vertex values) is
+ * the term's domain or IF joins the active elements; its matrix is the sum
+ * of its volume and boundary terms.  Spatial forms on simplex meshes; order
+ * -1 = 2k. */
 typedef struct {
   int32_t kind;   /* XG_TERM_MASS */
   int32_t domain; /* XG_NEG, XG_POS, XG_IF (2D) */
