@@ -2196,13 +2196,22 @@ orc_csr* orc_assemble_full(const orc_space* s, const double* lset_vertex, const 
             bnd_act[e0] = 1;
       }
   }
+  // an element is active for a volume term in whose set it lies if its
+  // domain type (CheckIfStraightCut of its vertex values) is the term's
+  // domain or IF: elements without a part in the term's domain add nothing
   int nact = 0;
   for (int e = 0; e < ne; e++) {
     bool act = bnd_act[e] != 0;
+    double le[4];
+    for (int i = 0; i <= s->D; i++) le[i] = lset_vertex[s->elv[(size_t)e * (s->D + 1) + i]];
+    const int dom = check_if_straight_cut(le, s->D + 1);
     for (int t = 0; t < nterms && any_vol; t++)
-      if (!facet_term(terms[t].kind) && (!terms[t].defined_on || test_bit(terms[t].defined_on, e))) act = true;
+      if (!facet_term(terms[t].kind) && (!terms[t].defined_on || test_bit(terms[t].defined_on, e)) &&
+          (dom == ORC_IF || dom == terms[t].domain))
+        act = true;
     for (int t = 0; t < ncterms; t++)
-      if (!cterms[t].defined_on || test_bit(cterms[t].defined_on, e)) act = true;
+      if ((!cterms[t].defined_on || test_bit(cterms[t].defined_on, e)) && (dom == ORC_IF || dom == cterms[t].domain))
+        act = true;
     if (act) el_slot[e] = nact++;
   }
   int nfa = 0;
