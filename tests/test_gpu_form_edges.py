@@ -91,3 +91,27 @@ def test_vertex_zeros_and_determinism(xg, orc):
     one = np.ones(mq.nv)
     Q = q.mat.to_scipy()
     assert abs(one @ (Q @ one) - 1.0) < 1e-12  # the interface x = 0.5 has length 1
+
+
+@pytest.mark.parametrize("D,k", [(2, 2), (3, 1)])
+def test_terms_without_element_sets(xg, orc, D, k):
+    """Terms without definedonelements: the elements with a part in the
+    term's domain are active (the same set on the GPU and in the oracle)."""
+    m = MakeStructured2DMesh(9, 9) if D == 2 else MakeStructured3DMesh(4)
+    c = m.coords
+    l = orc.interpolate_p1_perturb(((c - 0.3) ** 2).sum(axis=1) - 0.36)
+    g = gf_of(xg, m, l)
+    V = xg.H1(m, order=k)
+    u, v = V.TnT()
+    a = xg.BilinearForm(V)
+    a += xg.grad(u) * xg.grad(v) * xg.dCut(g, xg.NEG) + 3.0 * u * v * xg.dCut(g, xg.IF)
+    a.Assemble()
+    sp = orc.Space(m, k)
+    rp, cols, vals = sp.assemble(l, [dict(kind=orc.TERM_LAPLACE, domain=orc.NEG),
+                                     dict(kind=orc.TERM_MASS, domain=orc.IF, coef=3.0)])
+    r, cc, vv = a.mat.global_coo()
+    ref = {(int(p), int(q)): float(x) for p, q, x in zip(np.repeat(np.arange(sp.ndof), np.diff(rp)), cols, vals)}
+    got = {(int(p), int(q)): float(x) for p, q, x in zip(r, cc, vv)}
+    assert set(ref) == set(got)
+    scale = max(abs(x) for x in ref.values())
+    assert max(abs(got[q] - ref[q]) for q in ref) < 1e-12 * scale
