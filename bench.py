@@ -762,14 +762,11 @@ class Clocks:
                 "samples": len(sm)}
 
 
-# DRAM bytes (read + write) per launch of a stage's dominant kernel, from one
-# ncu capture of the same workload (scaled from a smaller case where the
-# entry says so).  Each entry names the kernel and the first 16 hex digits of
-# the sha256 of the source file it was captured on; when that file has
-# changed since, the line reports traffic null instead of a stale figure.
 # DRAM bytes (read + write) per launch of a stage's dominant kernel from one
 # ncu capture (dram__bytes_read.sum + dram__bytes_write.sum, one pass, on the
-# full-size workload), valid while the kernel's source file is unchanged
+# full-size workload).  Each entry names the first 16 hex digits of the
+# sha256 of the source file it was captured on; when that file has changed
+# since, the line reports traffic null instead of a stale figure.
 TRAFFIC = {
     ("c2", "patch"): {"bytes": 72624896 + 195189504, "source": "ngsxfem_gb300/csrc/xg_asm.cu",
                       "sha16": "a290a28fa15eec8a"},

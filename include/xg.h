@@ -231,6 +231,26 @@ int xg_base_rule(int d, int p, double* h_pts, double* h_wts, int max_pts);
 int xg_integrate(xg_mesh* mesh, const double* d_lset, int dt, int order, int ex, int ey, int ez,
                  const uint64_t* d_defined_on, double* d_result, void* stream);
 
+/* One product of an xg_integrate_fields integrand:
+ * coef * x^e[0] y^e[1] z^e[2] * field[f0] * field[f1] (f0, f1 = -1: no factor). */
+typedef struct {
+  double coef;
+  int32_t e[3];
+  int32_t f0, f1;
+} xg_fmono;
+/* Integrate(cf * dCut(lset, dt, order)) with cf a sum of nmonos (<= 16)
+ * xg_fmono products over nfields (<= 4) GridFunctions: spaces[i] (host array)
+ * a spatial H1 or L2 space of order 1..3 on `mesh`, d_fields[i] (host array
+ * of device pointers) its coefficient vector.  The reference's Integrate with
+ * a CoefficientFunction of GridFunctions evaluated at the points of the
+ * straight cut rule (cutint/cutintegral.cpp:126-212), e.g. the L2 error
+ * (gfu - gfex)^2 of its demos.  Simplex meshes.  Deterministic fixed-order
+ * sum into d_result[0]; shares the mesh's scratch with xg_integrate (calls on
+ * one mesh are serialised on one stream). */
+int xg_integrate_fields(xg_mesh* mesh, const double* d_lset, int dt, int order, int32_t nfields,
+                        xg_space* const* spaces, const double* const* d_fields, int32_t nmonos,
+                        const xg_fmono* monos, const uint64_t* d_defined_on, double* d_result, void* stream);
+
 /* Several level sets on a simplex mesh (cutint/mlsetintegration.cpp:6-180,
  * cutint/straightcutrule.cpp:679-812): d_lsets holds nlsets (1..8) P1 level
  * sets, [nlsets][nv] vertex values; the domain is the union of ndomains

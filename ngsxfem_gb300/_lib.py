@@ -26,7 +26,7 @@ EXPORTS = [
     "xg_interpolate_p1_perturb", "xg_cutinfo_update", "xg_mesh_check",
     "xg_facets_with_neighbor_types", "xg_elements_with_neighbor_facets",
     "xg_cut_rules", "xg_base_rule_size", "xg_base_rule", "xg_integrate", "xg_integrate_noalloc", "xg_integrate_subdiv", "xg_subdiv_moments_tet",
-    "xg_mesh_create_tensor", "xg_cut_rules_ex", "xg_quad_rule_capacity", "xg_integrate_ex",
+    "xg_mesh_create_tensor", "xg_cut_rules_ex", "xg_quad_rule_capacity", "xg_integrate_ex", "xg_integrate_fields",
     "xg_integrate_mlset", "xg_cut_rules_mlset", "xg_mlset_rule_capacity", "xg_mlset_mark",
     "xg_iso_integrate_mesh", "xg_iso_deformation", "xg_integrate_bnd",
     "xg_mlset_form_create", "xg_mlset_form_assemble", "xg_form_create", "xg_form_destroy", "xg_form_set_defined_on", "xg_form_set_bnd_terms", "xg_form_set_coef_terms", "xg_form_set_deformation", "xg_form_capacity",
@@ -107,6 +107,15 @@ class CTerm(ctypes.Structure):
     ]
 
 
+class FMono(ctypes.Structure):
+    _fields_ = [
+        ("coef", ctypes.c_double),
+        ("e", ctypes.c_int32 * 3),
+        ("f0", ctypes.c_int32),
+        ("f1", ctypes.c_int32),
+    ]
+
+
 class StTerm(ctypes.Structure):
     _fields_ = [
         ("base", Term),
@@ -171,6 +180,7 @@ def load():
         "xg_base_rule": (I, [I, I, P, P, I]),
         "xg_integrate": (I, [P, P, I, I, I, I, I, P, P, P]),
         "xg_integrate_ex": (I, [P, P, I, I, I, I, I, I, P, P, P]),
+        "xg_integrate_fields": (I, [P, P, I, I, I, P, P, I, P, P, P, P]),
         "xg_integrate_mlset": (I, [P, P, ctypes.c_int32, P, ctypes.c_int32, I, I, I, I, P, P, P]),
         "xg_cut_rules_mlset": (I, [P, P, ctypes.c_int32, P, ctypes.c_int32, P, ctypes.c_int32, I, ctypes.c_int32,
                                    P, P, P, P]),

@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <string>
 
 #include "xg_basis.cuh"
 #include "xg_cut.cuh"
@@ -472,3 +473,183 @@ int coef_elmat_launch(const CoefFormLaunch& L, cudaStream_t s) {
 }
 
 }  // namespace xg
+
+// ---- Integrate of polynomials in GridFunctions --------------------------------------
+// The reference's Integrate with a CoefficientFunction of GridFunctions
+// (cutint/cutintegral.cpp:126-212; the CoefficientFunction evaluated at the
+// points of StraightCutIntegrationRule, cutint/straightcutrule.cpp:582-677),
+// for sums of products c x^e f_a f_b.  Thread per element (grid-stride, a
+// fixed assignment), the block sums by a fixed tree and the blocks summed in
+// order: deterministic.
+namespace xg {
+namespace {
+
+constexpr int kMaxFields = 4, kMaxFMonos = 16, kFiThreads = 256, kFiBlocks = 152 * 4;
+
+struct FieldsDesc {
+  int nf, nm;
+  int order[kMaxFields];
+  const int32_t* dofs[kMaxFields];  // [nd_i][ne]
+  const double* v[kMaxFields];
+  double c[kMaxFMonos];
+  int e[kMaxFMonos][3];
+  int f0[kMaxFMonos], f1[kMaxFMonos];
+};
+
+template <int D>
+__global__ void __launch_bounds__(kFiThreads)
+    k_integrate_fields(int ne, int nv, const int32_t* __restrict__ elv, const double* __restrict__ xyz,
+                       const double* __restrict__ lset, int dt, int order, FieldsDesc F,
+                       const uint64_t* __restrict__ defined_on, double* __restrict__ block_sums, int* err) {
+  __shared__ double red[kFiThreads];
+  double acc = 0.0;
+  const int p = clamp_order(order);
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
+    if (defined_on && !cf_bit64(defined_on, e)) continue;
+    double l[4], xv[4][3];
+    int gv[4] = {0, 0, 0, 0};
+    for (int v = 0; v <= D; v++) {
+      gv[v] = elv[(int64_t)v * ne + e];
+      l[v] = lset[gv[v]];
+      for (int c = 0; c < 3; c++) xv[v][c] = c < D ? xyz[(int64_t)c * nv + gv[v]] : 0.0;
+    }
+    const int cdom = check_if_straight_cut(l, D + 1);
+    if (cdom != XG_IF && cdom != dt) continue;
+    Geo<D> g;
+    make_geo<D>(xv, g);
+    const double meas = fabs(g.det);
+    auto point = [&](const double* xi, double w) {
+      double lam[D + 1], sl = 0.0, xp[3] = {0.0, 0.0, 0.0};
+      for (int k = 0; k < D; k++) {
+        lam[k] = xi[k];
+        sl += xi[k];
+      }
+      lam[D] = 1.0 - sl;
+      for (int r = 0; r < D; r++) {
+        double sr = g.x0[r];
+        for (int k = 0; k < D; k++) sr += g.F[r][k] * xi[k];
+        xp[r] = sr;
+      }
+      double fv[kMaxFields];
+      for (int i = 0; i < F.nf; i++) {
+        const int k = F.order[i], nd = ndof_el(D, k);
+        double s = 0.0;
+        for (int a = 0; a < nd; a++)
+          s += F.v[i][F.dofs[i][(int64_t)a * ne + e]] * eval_fn_value<D, double>(desc_rt<D>(k, a, gv), lam);
+        fv[i] = s;
+      }
+      double val = 0.0;
+      for (int m = 0; m < F.nm; m++) {
+        double t = F.c[m] * cf_ipow(xp[0], F.e[m][0]) * cf_ipow(xp[1], F.e[m][1]) *
+                   (D == 3 ? cf_ipow(xp[2], F.e[m][2]) : 1.0);
+        if (F.f0[m] >= 0) t *= fv[F.f0[m]];
+        if (F.f1[m] >= 0) t *= fv[F.f1[m]];
+        val += t;
+      }
+      acc += w * meas * val;
+    };
+    if (cdom != XG_IF) {
+      const int off = g_cf_rules.off[D][p], cnt = g_cf_rules.cnt[D][p];
+      for (int q = 0; q < cnt; q++) point(g_cf_rules.x[off + q], g_cf_rules.w[off + q]);
+      continue;
+    }
+    Sub subs[3];
+    const int ns = decompose<D>(l, dt, subs);
+    if (ns < 0) {
+      set_err(err, -ns);
+      continue;
+    }
+    const int sd = dt == XG_IF ? D - 1 : D;
+    const int off = g_cf_rules.off[sd][p], cnt = g_cf_rules.cnt[sd][p];
+    const double fac = dt == XG_IF ? if_factor<D>(g, l) : 1.0;
+    for (int s = 0; s < ns; s++) {
+      const double trafofac = simplex_volume(subs[s].p, sd + 1);
+      for (int q = 0; q < cnt; q++) {
+        double pt[3];
+        plain_point(subs[s], sd + 1, g_cf_rules.x[off + q], pt);
+        point(pt, g_cf_rules.w[off + q] * trafofac * fac);
+      }
+    }
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = kFiThreads / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) block_sums[blockIdx.x] = red[0];
+}
+
+__global__ void k_fi_sum(const double* __restrict__ v, int n, double* __restrict__ out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < n; i++) s += v[i];
+    out[0] = s;
+  }
+}
+
+}  // namespace
+}  // namespace xg
+
+using namespace xg;
+
+extern "C" int xg_integrate_fields(xg_mesh* m, const double* d_lset, int dt, int order, int32_t nfields,
+                                   xg_space* const* spaces, const double* const* d_fields, int32_t nmonos,
+                                   const xg_fmono* monos, const uint64_t* d_defined_on, double* d_result,
+                                   void* stream) {
+  if (!m || !d_lset || !d_result || dt < 0 || dt > 2 || order < 0 || order > kMaxOrder || nfields < 0 ||
+      nmonos < 0 || (nfields > 0 && (!spaces || !d_fields)) || (nmonos > 0 && !monos))
+    return XG_ERR_ARG;
+  if (nfields > kMaxFields || nmonos > kMaxFMonos) {
+    set_last_error("xg_integrate_fields: at most " + std::to_string(kMaxFields) + " fields and " +
+                   std::to_string(kMaxFMonos) + " products");
+    return XG_ERR_UNSUPPORTED;
+  }
+  if (m->tensor) {
+    set_last_error("xg_integrate_fields: simplex meshes only");
+    return XG_ERR_UNSUPPORTED;
+  }
+  FieldsDesc F{};
+  F.nf = nfields;
+  F.nm = nmonos;
+  for (int i = 0; i < nfields; i++) {
+    const xg_space* sp = spaces[i];
+    if (!sp || !d_fields[i] || sp->mesh != m || sp->kt >= 0 || sp->order < 1 || sp->order > 3) {
+      set_last_error("xg_integrate_fields: field " + std::to_string(i) +
+                     " needs a spatial space of order 1..3 on the mesh and its coefficient vector");
+      return XG_ERR_ARG;
+    }
+    F.order[i] = sp->order;
+    F.dofs[i] = sp->d_el_dofs;
+    F.v[i] = d_fields[i];
+  }
+  for (int k = 0; k < nmonos; k++) {
+    const xg_fmono& q = monos[k];
+    if (q.e[0] < 0 || q.e[1] < 0 || q.e[2] < 0 || q.f0 < -1 || q.f0 >= nfields || q.f1 < -1 || q.f1 >= nfields)
+      return XG_ERR_ARG;
+    F.c[k] = q.coef;
+    for (int r = 0; r < 3; r++) F.e[k][r] = q.e[r];
+    F.f0[k] = q.f0;
+    F.f1[k] = q.f1;
+  }
+  if (int st = ensure_device_rules()) return st;
+  const size_t need = kFiBlocks * sizeof(double);
+  if (m->scratch_bytes < need) {
+    cudaFree(m->d_scratch);
+    m->d_scratch = nullptr;
+    m->scratch_bytes = 0;
+    XG_CUDA(cudaMalloc(&m->d_scratch, need));
+    m->scratch_bytes = need;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  double* bs = (double*)m->d_scratch;
+  if (m->dim == 2)
+    k_integrate_fields<2><<<kFiBlocks, kFiThreads, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, d_lset, dt, order, F,
+                                                           d_defined_on, bs, m->d_err);
+  else
+    k_integrate_fields<3><<<kFiBlocks, kFiThreads, 0, s>>>(m->ne, m->nv, m->d_elv, m->d_xyz, d_lset, dt, order, F,
+                                                           d_defined_on, bs, m->d_err);
+  k_fi_sum<<<1, 32, 0, s>>>(bs, kFiBlocks, d_result);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? XG_OK : cuda_fail(e, "k_integrate_fields");
+}

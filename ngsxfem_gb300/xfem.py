@@ -347,11 +347,32 @@ class GridFunction:
         return _Expr([_Mono(scal=(("gf", self),))])
 
     def __mul__(self, o):
-        if isinstance(o, (_Expr, int, float)):
+        if isinstance(o, (_Expr, int, float, _Measure, GridFunction, _Monomial)):
             return self._atom() * o
         return NotImplemented
 
-    __rmul__ = __mul__
+    def __rmul__(self, o):
+        if isinstance(o, (_Expr, int, float, GridFunction, _Monomial)):
+            return _Expr.wrap(o) * self._atom()
+        return NotImplemented
+
+    # coefficient-function arithmetic (integrands of Integrate and forms)
+    def __add__(self, o):
+        return self._atom() + o
+
+    __radd__ = __add__
+
+    def __sub__(self, o):
+        return self._atom() - o
+
+    def __rsub__(self, o):
+        return _Expr.wrap(o) - self._atom()
+
+    def __neg__(self):
+        return -self._atom()
+
+    def __pow__(self, p):
+        return self._atom() ** p
 
 
 def InterpolateToP1(f, gf, eps_perturbation=1e-14):
@@ -538,7 +559,22 @@ class _Expr:
         if isinstance(x, _Monomial):
             return _Expr([_Mono(scal=(("xyz", x.e),))])
         if isinstance(x, (tuple, list)):
-            return _Expr([_Mono(vec=("b", tuple(float(v) for v in x)))])
+            if all(isinstance(v, (int, float)) for v in x):
+                return _Expr([_Mono(vec=("b", tuple(float(v) for v in x)))])
+            # a vector with coefficient-field components, e.g.
+            # CoefficientFunction((gf_x, gf_y)): the sum of its components
+            # times the unit vectors (the constant components as one vector)
+            const = [float(v) if isinstance(v, (int, float)) else 0.0 for v in x]
+            monos = [_Mono(vec=("b", tuple(const)))] if any(const) else []
+            for i, v in enumerate(x):
+                if isinstance(v, (int, float)):
+                    continue
+                unit = tuple(1.0 if j == i else 0.0 for j in range(len(x)))
+                for m in _Expr.wrap(v).monos:
+                    if m.vec is not None or m.dots or any(a[0] not in ("gf", "xyz") for a in m.scal):
+                        raise TypeError("vector components: numbers, GridFunctions, x, y, z and their products")
+                    monos.append(_Mono(m.c, m.hpow, m.scal, (), ("b", unit)))
+            return _Expr(monos)
         raise TypeError("unsupported coefficient %r" % (x,))
 
     def __add__(self, o):
@@ -577,10 +613,17 @@ class _Expr:
         return _Expr.wrap(o) * _Expr([_Mono(1.0 / m.c, -m.hpow)])
 
     def __pow__(self, p):
-        if len(self.monos) != 1 or self.monos[0].scal or self.monos[0].vec is not None or int(p) != p:
-            raise TypeError("only powers of the mesh size / constants are supported")
-        m = self.monos[0]
-        return _Expr([_Mono(m.c ** p, m.hpow * int(p))])
+        if int(p) != p:
+            raise TypeError("integer powers only")
+        if len(self.monos) == 1 and not self.monos[0].scal and self.monos[0].vec is None and not self.monos[0].dots:
+            m = self.monos[0]
+            return _Expr([_Mono(m.c ** p, m.hpow * int(p))])
+        if p < 1:
+            raise TypeError("powers >= 1 of expressions with coefficient fields")
+        out = self
+        for _ in range(int(p) - 1):
+            out = out * self
+        return out
 
     def Other(self):
         out = []
@@ -1379,7 +1422,7 @@ class _Monomial:
             return _Monomial(tuple(a + b for a, b in zip(self.e, o.e)))
         if isinstance(o, _Measure):
             return ("integral", self, o)
-        if isinstance(o, (_Expr, int, float)):
+        if isinstance(o, (_Expr, int, float, GridFunction)):
             return _Expr([_Mono(scal=(("xyz", self.e),))]) * o
         raise TypeError("monomial coefficient functions only")
 
@@ -1395,10 +1438,76 @@ class _Monomial:
 x, y, z = _Monomial((1, 0, 0)), _Monomial((0, 1, 0)), _Monomial((0, 0, 1))
 
 
+def _integrate_fields(expr, meas, order):
+    """Integrate(cf * dCut(lset, dt)) for cf a polynomial in GridFunctions
+    (at most two factors per product, at most four fields) and x, y, z:
+    xg_integrate_fields (the reference's Integrate with a CoefficientFunction
+    of GridFunctions, cutint/cutintegral.cpp:126-212), e.g. the L2 error
+    Integrate((gfu - gfex) ** 2 * dCut(lsetp1, NEG), mesh)."""
+    if meas.kind != "cut" or meas.skeleton or meas.vb != VOL or meas.deformation is not None or meas.subdivlvl:
+        raise NotImplementedError("Integrate of GridFunction integrands: dCut(P1 level set, dt[, order, "
+                                  "definedonelements]) on volume elements")
+    lset = meas.levelset
+    if not isinstance(lset, GridFunction) or isinstance(lset.space, SpaceTimeFESpace):
+        raise NotImplementedError("Integrate of GridFunction integrands takes one spatial P1 level set")
+    lv = _lset_vec(lset)
+    mesh = lset.space.mesh
+    fields, monos = [], {}
+    for m in expr.monos:
+        if m.vec is not None or m.dots or m.hpow:
+            raise NotImplementedError("Integrate integrands: products of GridFunctions and x, y, z")
+        gfs, ex = [], [0, 0, 0]
+        for a in m.scal:
+            if a[0] == "gf":
+                gfs.append(a[1])
+            elif a[0] == "xyz":
+                ex = [p + q for p, q in zip(ex, a[1])]
+            else:
+                raise NotImplementedError("Integrate integrands: products of GridFunctions and x, y, z")
+        if len(gfs) > 2:
+            raise NotImplementedError("Integrate integrands: at most two GridFunction factors per product")
+        idx = []
+        for g in gfs:
+            if isinstance(g.space, SpaceTimeFESpace) or g.space.mesh is not mesh:
+                raise ValueError("the GridFunctions must live in spatial spaces of the level set's mesh")
+            k = next((i for i, f in enumerate(fields) if f is g), None)
+            if k is None:
+                fields.append(g)
+                k = len(fields) - 1
+            idx.append(k)
+        key = (tuple(ex), tuple(sorted(idx)))
+        monos[key] = monos.get(key, 0.0) + m.c
+    if len(fields) > 4 or len(monos) > 16:
+        raise NotImplementedError("Integrate integrands: at most 4 GridFunctions and 16 distinct products")
+    arr = (_lib.FMono * max(len(monos), 1))()
+    for i, ((ex, idx), c) in enumerate(monos.items()):
+        arr[i].coef = c
+        for r in range(3):
+            arr[i].e[r] = ex[r]
+        arr[i].f0 = idx[0] if len(idx) > 0 else -1
+        arr[i].f1 = idx[1] if len(idx) > 1 else -1
+    sp = (ctypes.c_void_p * max(len(fields), 1))(*[f.space.h.value for f in fields])
+    dv = (ctypes.c_void_p * max(len(fields), 1))(*[f.vec.data_ptr() for f in fields])
+    dm = device_mesh(mesh)
+    res = torch.zeros(1, dtype=torch.float64, device=_dev())
+    defined = meas.definedonelements
+    q = meas.order if meas.order is not None else order
+    _lib.call("xg_integrate_fields", dm.h, _vp(lv), meas.domain_type, int(q), len(fields), sp, dv, len(monos), arr,
+              _vp(defined.words) if defined is not None else None, _vp(res), _stream())
+    dm.check()
+    return meas.scale * float(res.item())
+
+
 def Integrate(levelset_domain=None, cf=None, mesh=None, order=5, integrand=None):
     """Integrate(x^a y^b z^c * dCut(lset, dt, order)) on the GPU
     (cutint/cutintegral.cpp:126-212): a deterministic fixed-order sum.  Also
     called as Integrate(x**2 * dCut(...), mesh) or Integrate(dCut(...), mesh)."""
+    if isinstance(levelset_domain, _Integral):
+        return _integrate_fields(levelset_domain.expr, levelset_domain.measure, order)
+    if isinstance(levelset_domain, dict) and isinstance(cf, (_Expr, GridFunction)):
+        meas = dCut(levelset_domain["levelset"], levelset_domain["domain_type"], levelset_domain.get("order", order),
+                    **{k: v for k, v in levelset_domain.items() if k not in ("levelset", "domain_type", "order")})
+        return _integrate_fields(_Expr.wrap(cf), meas, order)
     if isinstance(levelset_domain, _Measure):
         levelset_domain = ("integral", _Monomial(), levelset_domain)
     if isinstance(levelset_domain, tuple) and len(levelset_domain) == 3 and levelset_domain[0] == "integral":

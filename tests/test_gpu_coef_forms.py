@@ -104,3 +104,36 @@ def test_planar_field_integrals(xg):
     b.Assemble()
     B = b.mat.to_scipy()
     assert abs(xv @ (B @ xv) - (0.35 + mx)) < 1e-13
+
+
+@pytest.mark.parametrize("D,k", [(2, 2), (3, 1), (3, 2)])
+def test_vector_field_convection_parity(xg, orc, D, k):
+    """CoefficientFunction((b_x, b_y[, b_z])) * grad(u) * v with GridFunction
+    components (and a constant one in 3D): one convection term per component,
+    with the unit vector and the component's field, the constant components as
+    one plain convection term."""
+    m = MakeStructured2DMesh(8, 8) if D == 2 else MakeStructured3DMesh(4)
+    c = m.coords
+    l = orc.interpolate_p1_perturb(((c - 0.3) ** 2).sum(axis=1) - 0.36)
+    g = gf_of(xg, m, l)
+    hasneg = xg.CutInfo(m, g).GetElementsOfType(xg.HASNEG)
+    Vg = xg.H1(m, order=1)
+    bx = xg.GridFunction(Vg).Set(lambda *p: 1.0 + p[1])
+    by = xg.GridFunction(Vg).Set(lambda *p: -0.5 * p[0])
+    comps = (bx, by) if D == 2 else (bx, by, 0.25)
+    V = xg.H1(m, order=k)
+    u, v = V.TnT()
+    sp, spg = orc.Space(m, k), orc.Space(m, 1)
+    w = words(hasneg)
+    cterms = [dict(kind=orc.TERM_CONV, domain=orc.NEG, b=tuple(1.0 if j == i else 0.0 for j in range(3)),
+                   gf_order=1, gf_el=f.vec.cpu().numpy()[spg.el_dofs()], defined_on=w)
+              for i, f in enumerate((bx, by))]
+    terms = [dict(kind=orc.TERM_LAPLACE, domain=orc.NEG, defined_on=w)]
+    if D == 3:
+        terms.append(dict(kind=orc.TERM_CONV, domain=orc.NEG, b=(0.0, 0.0, 0.25), defined_on=w))
+    ref = sp.assemble(l, terms, cterms=cterms)
+    a = xg.BilinearForm(V)
+    a += xg.grad(u) * xg.grad(v) * xg.dCut(g, xg.NEG, definedonelements=hasneg)
+    a += xg.CoefficientFunction(comps) * xg.grad(u) * v * xg.dCut(g, xg.NEG, definedonelements=hasneg)
+    a.Assemble()
+    compare(sp, ref, a.mat, 1e-12)

@@ -47,6 +47,8 @@ def test_planar_coefficient_integrals(orc, k):
     one[: m.nv] = 1.0
     x = np.zeros(sp.ndof)
     x[: m.nv] = X
+    y = np.zeros(sp.ndof)
+    y[: m.nv] = Y
     gx = field(orc, m, 1, lambda p: p[:, 0])
     gxx = field(orc, m, 2, lambda p: p[:, 0] ** 2)
     g1x = field(orc, m, 1, lambda p: 1.0 + p[:, 0])
@@ -60,6 +62,10 @@ def test_planar_coefficient_integrals(orc, k):
         (dict(kind=orc.TERM_LAPLACE, gf_order=1, gf_el=g1x, order=2), x, x, AREA + MX),
         (dict(kind=M, domain=orc.IF, gf_order=1, gf_el=gx, order=2), one, one, LEN * 0.35),
         (dict(kind=M, domain=orc.POS, gf_order=1, gf_el=gx), one, one, 0.5 - MX),
+        # a component of a vector field: (gx e_0) . grad(x) = x, (gx e_1) . grad(y) = x
+        (dict(kind=orc.TERM_CONV, b=(1.0, 0.0, 0.0), gf_order=1, gf_el=gx, order=2), x, one, MX),
+        (dict(kind=orc.TERM_CONV, b=(0.0, 1.0, 0.0), gf_order=1, gf_el=gx, order=2), y, one, MX),
+        (dict(kind=orc.TERM_CONV, b=(0.0, 1.0, 0.0), gf_order=1, gf_el=gx, order=2), x, one, 0.0),
     ]
     for ct, u, v, val in cases:
         ct = dict(dict(domain=orc.NEG), **ct)
