@@ -232,19 +232,21 @@ int xg_integrate(xg_mesh* mesh, const double* d_lset, int dt, int order, int ex,
                  const uint64_t* d_defined_on, double* d_result, void* stream);
 
 /* One product of an xg_integrate_fields integrand:
- * coef * x^e[0] y^e[1] z^e[2] * field[f0] * field[f1] (f0, f1 = -1: no factor). */
+ * coef * x^e[0] y^e[1] z^e[2] * F0 * F1 with F0 = field[f0] (d0 = -1) or its
+ * derivative along x_d0 (d0 = 0..dim-1), F1 likewise (f0, f1 = -1: no factor). */
 typedef struct {
   double coef;
   int32_t e[3];
   int32_t f0, f1;
+  int32_t d0, d1;
 } xg_fmono;
 /* Integrate(cf * dCut(lset, dt, order)) with cf a sum of nmonos (<= 16)
  * xg_fmono products over nfields (<= 4) GridFunctions: spaces[i] (host array)
  * a spatial H1 or L2 space of order 1..3 on `mesh`, d_fields[i] (host array
  * of device pointers) its coefficient vector.  The reference's Integrate with
  * a CoefficientFunction of GridFunctions evaluated at the points of the
- * straight cut rule (cutint/cutintegral.cpp:126-212), e.g. the L2 error
- * (gfu - gfex)^2 of its demos.  Simplex meshes.  Deterministic fixed-order
+ * straight cut rule (cutint/cutintegral.cpp:126-212), e.g. the L2 and H1
+ * errors (gfu - gfex)^2, (grad gfu - grad gfex)^2 of its demos.  Simplex meshes.  Deterministic fixed-order
  * sum into d_result[0]; shares the mesh's scratch with xg_integrate (calls on
  * one mesh are serialised on one stream). */
 int xg_integrate_fields(xg_mesh* mesh, const double* d_lset, int dt, int order, int32_t nfields,

@@ -113,6 +113,8 @@ class FMono(ctypes.Structure):
         ("e", ctypes.c_int32 * 3),
         ("f0", ctypes.c_int32),
         ("f1", ctypes.c_int32),
+        ("d0", ctypes.c_int32),
+        ("d1", ctypes.c_int32),
     ]
 
 

@@ -478,7 +478,8 @@ int coef_elmat_launch(const CoefFormLaunch& L, cudaStream_t s) {
 // The reference's Integrate with a CoefficientFunction of GridFunctions
 // (cutint/cutintegral.cpp:126-212; the CoefficientFunction evaluated at the
 // points of StraightCutIntegrationRule, cutint/straightcutrule.cpp:582-677),
-// for sums of products c x^e f_a f_b.  Thread per element (grid-stride, a
+// for sums of products c x^e f_a f_b, each factor a field's value or one of
+// its partial derivatives (the H1 error (grad gfu - grad gfex)^2).  Thread per element (grid-stride, a
 // fixed assignment), the block sums by a fixed tree and the blocks summed in
 // order: deterministic.
 namespace xg {
@@ -489,11 +490,13 @@ constexpr int kMaxFields = 4, kMaxFMonos = 16, kFiThreads = 256, kFiBlocks = 152
 struct FieldsDesc {
   int nf, nm;
   int order[kMaxFields];
+  int grad[kMaxFields];             // some product takes a derivative of the field
   const int32_t* dofs[kMaxFields];  // [nd_i][ne]
   const double* v[kMaxFields];
   double c[kMaxFMonos];
   int e[kMaxFMonos][3];
   int f0[kMaxFMonos], f1[kMaxFMonos];
+  int d0[kMaxFMonos], d1[kMaxFMonos];  // -1: the value, else the derivative along x_d
 };
 
 template <int D>
@@ -518,6 +521,15 @@ __global__ void __launch_bounds__(kFiThreads)
     Geo<D> g;
     make_geo<D>(xv, g);
     const double meas = fabs(g.det);
+    double gl[D + 1][D];  // physical gradients of the barycentrics
+    for (int k = 0; k < D; k++) {
+      double sg = 0.0;
+      for (int a = 0; a < D; a++) {
+        gl[a][k] = g.Finv[a][k];
+        sg += g.Finv[a][k];
+      }
+      gl[D][k] = -sg;
+    }
     auto point = [&](const double* xi, double w) {
       double lam[D + 1], sl = 0.0, xp[3] = {0.0, 0.0, 0.0};
       for (int k = 0; k < D; k++) {
@@ -530,20 +542,33 @@ __global__ void __launch_bounds__(kFiThreads)
         for (int k = 0; k < D; k++) sr += g.F[r][k] * xi[k];
         xp[r] = sr;
       }
-      double fv[kMaxFields];
+      // factor table: [field][0] the value, [field][1 + d] the derivative along x_d
+      double fv[kMaxFields][4];
       for (int i = 0; i < F.nf; i++) {
         const int k = F.order[i], nd = ndof_el(D, k);
-        double s = 0.0;
-        for (int a = 0; a < nd; a++)
-          s += F.v[i][F.dofs[i][(int64_t)a * ne + e]] * eval_fn_value<D, double>(desc_rt<D>(k, a, gv), lam);
-        fv[i] = s;
+        double s = 0.0, sg[D];
+        for (int d = 0; d < D; d++) sg[d] = 0.0;
+        for (int a = 0; a < nd; a++) {
+          const double ca = F.v[i][F.dofs[i][(int64_t)a * ne + e]];
+          if (F.grad[i]) {
+            double ph, gr[D];
+            eval_fn<D, double>(desc_rt<D>(k, a, gv), lam, gl, ph, gr);
+            s += ca * ph;
+            for (int d = 0; d < D; d++) sg[d] += ca * gr[d];
+          } else {
+            s += ca * eval_fn_value<D, double>(desc_rt<D>(k, a, gv), lam);
+          }
+        }
+        fv[i][0] = s;
+        fv[i][1] = fv[i][2] = fv[i][3] = 0.0;
+        for (int d = 0; d < D; d++) fv[i][1 + d] = sg[d];
       }
       double val = 0.0;
       for (int m = 0; m < F.nm; m++) {
         double t = F.c[m] * cf_ipow(xp[0], F.e[m][0]) * cf_ipow(xp[1], F.e[m][1]) *
                    (D == 3 ? cf_ipow(xp[2], F.e[m][2]) : 1.0);
-        if (F.f0[m] >= 0) t *= fv[F.f0[m]];
-        if (F.f1[m] >= 0) t *= fv[F.f1[m]];
+        if (F.f0[m] >= 0) t *= fv[F.f0[m]][1 + F.d0[m]];
+        if (F.f1[m] >= 0) t *= fv[F.f1[m]][1 + F.d1[m]];
         val += t;
       }
       acc += w * meas * val;
@@ -625,12 +650,18 @@ extern "C" int xg_integrate_fields(xg_mesh* m, const double* d_lset, int dt, int
   }
   for (int k = 0; k < nmonos; k++) {
     const xg_fmono& q = monos[k];
-    if (q.e[0] < 0 || q.e[1] < 0 || q.e[2] < 0 || q.f0 < -1 || q.f0 >= nfields || q.f1 < -1 || q.f1 >= nfields)
+    if (q.e[0] < 0 || q.e[1] < 0 || q.e[2] < 0 || q.f0 < -1 || q.f0 >= nfields || q.f1 < -1 || q.f1 >= nfields ||
+        q.d0 < -1 || q.d0 >= m->dim || q.d1 < -1 || q.d1 >= m->dim || (q.f0 < 0 && q.d0 >= 0) ||
+        (q.f1 < 0 && q.d1 >= 0))
       return XG_ERR_ARG;
     F.c[k] = q.coef;
     for (int r = 0; r < 3; r++) F.e[k][r] = q.e[r];
     F.f0[k] = q.f0;
     F.f1[k] = q.f1;
+    F.d0[k] = q.d0;
+    F.d1[k] = q.d1;
+    if (q.d0 >= 0) F.grad[q.f0] = 1;
+    if (q.d1 >= 0) F.grad[q.f1] = 1;
   }
   if (int st = ensure_device_rules()) return st;
   const size_t need = kFiBlocks * sizeof(double);

@@ -664,8 +664,13 @@ def dn(proxy, order, comp=-1, hdiv=False):
     return _Expr([_Mono(scal=(("dn" + name, other, int(order)),))])
 
 
-class _LsetGrad:
+class _LsetGrad(_Expr):
+    """grad(gf) of a GridFunction: a vector expression (Integrate's H1 errors,
+    (grad(gfu) - grad(gfex)) ** 2); Normalize(grad(lset)) is the level set's
+    unit normal."""
+
     def __init__(self, gf):
+        super().__init__([_Mono(vec=("ggf", gf))])
         self.gf = gf
 
 
@@ -1452,40 +1457,61 @@ def _integrate_fields(expr, meas, order):
         raise NotImplementedError("Integrate of GridFunction integrands takes one spatial P1 level set")
     lv = _lset_vec(lset)
     mesh = lset.space.mesh
+    D = mesh.dim
     fields, monos = [], {}
+
+    def field_index(g):
+        if isinstance(g.space, SpaceTimeFESpace) or g.space.mesh is not mesh:
+            raise ValueError("the GridFunctions must live in spatial spaces of the level set's mesh")
+        k = next((i for i, f in enumerate(fields) if f is g), None)
+        if k is None:
+            fields.append(g)
+            k = len(fields) - 1
+        return k
+
+    bad = "Integrate integrands: products of GridFunctions, their gradients and x, y, z"
     for m in expr.monos:
-        if m.vec is not None or m.dots or m.hpow:
-            raise NotImplementedError("Integrate integrands: products of GridFunctions and x, y, z")
-        gfs, ex = [], [0, 0, 0]
+        if m.vec is not None or m.hpow:
+            raise NotImplementedError(bad)
+        # a product of sums: every dot product of two vectors is a sum over
+        # the directions (factors (field, -1) = value, (field, d) = d/dx_d)
+        branches = [(m.c, [])]
+        ex = [0, 0, 0]
         for a in m.scal:
             if a[0] == "gf":
-                gfs.append(a[1])
+                branches = [(c, f + [(field_index(a[1]), -1)]) for c, f in branches]
             elif a[0] == "xyz":
                 ex = [p + q for p, q in zip(ex, a[1])]
             else:
-                raise NotImplementedError("Integrate integrands: products of GridFunctions and x, y, z")
-        if len(gfs) > 2:
-            raise NotImplementedError("Integrate integrands: at most two GridFunction factors per product")
-        idx = []
-        for g in gfs:
-            if isinstance(g.space, SpaceTimeFESpace) or g.space.mesh is not mesh:
-                raise ValueError("the GridFunctions must live in spatial spaces of the level set's mesh")
-            k = next((i for i, f in enumerate(fields) if f is g), None)
-            if k is None:
-                fields.append(g)
-                k = len(fields) - 1
-            idx.append(k)
-        key = (tuple(ex), tuple(sorted(idx)))
-        monos[key] = monos.get(key, 0.0) + m.c
+                raise NotImplementedError(bad)
+        for d in m.dots:
+            comps = []
+            for v in d:
+                if v[0] == "ggf":
+                    k = field_index(v[1])
+                    comps.append([(1.0, [(k, r)]) for r in range(D)])
+                elif v[0] == "b":
+                    b = list(v[1]) + [0.0] * (3 - len(v[1]))
+                    comps.append([(b[r], []) for r in range(D)])
+                else:
+                    raise NotImplementedError(bad)
+            branches = [(c * ca * cb, f + fa + fb) for c, f in branches
+                        for (ca, fa), (cb, fb) in zip(comps[0], comps[1]) if ca * cb != 0.0]
+        for c, f in branches:
+            if len(f) > 2:
+                raise NotImplementedError("Integrate integrands: at most two GridFunction factors per product")
+            key = (tuple(ex), tuple(sorted(f)))
+            monos[key] = monos.get(key, 0.0) + c
+    monos = {k: c for k, c in monos.items() if c != 0.0}
     if len(fields) > 4 or len(monos) > 16:
         raise NotImplementedError("Integrate integrands: at most 4 GridFunctions and 16 distinct products")
     arr = (_lib.FMono * max(len(monos), 1))()
-    for i, ((ex, idx), c) in enumerate(monos.items()):
+    for i, ((ex, f), c) in enumerate(monos.items()):
         arr[i].coef = c
         for r in range(3):
             arr[i].e[r] = ex[r]
-        arr[i].f0 = idx[0] if len(idx) > 0 else -1
-        arr[i].f1 = idx[1] if len(idx) > 1 else -1
+        arr[i].f0, arr[i].d0 = f[0] if len(f) > 0 else (-1, -1)
+        arr[i].f1, arr[i].d1 = f[1] if len(f) > 1 else (-1, -1)
     sp = (ctypes.c_void_p * max(len(fields), 1))(*[f.space.h.value for f in fields])
     dv = (ctypes.c_void_p * max(len(fields), 1))(*[f.vec.data_ptr() for f in fields])
     dm = device_mesh(mesh)

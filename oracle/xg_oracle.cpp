@@ -1734,17 +1734,20 @@ double orc_integrate(const orc_space* s, const double* lset_vertex, int dt, int 
 // Integrate of a polynomial in coefficient fields and x, y, z over the
 // straight cut rule: cutint/cutintegral.cpp:126-212 with a CoefficientFunction
 // made of GridFunctions, evaluated at the rule's points (the error norms of
-// the reference's demos, e.g. (gfu - gfex)^2).  Field i has order f_order[i]
-// and element coefficients f_el[i] [ne][nd_i] in this oracle's basis;
-// product m is coef[m] x^e3[3m] y^e3[3m+1] z^e3[3m+2] f[f0[m]] f[f1[m]]
-// (-1: no factor).
+// the reference's demos, e.g. (gfu - gfex)^2, (grad gfu - grad gfex)^2).
+// Field i has order f_order[i] and element coefficients f_el[i] [ne][nd_i]
+// in this oracle's basis; product m is coef[m] x^e3[3m] y^e3[3m+1]
+// z^e3[3m+2] F0 F1, F0 the value of field f0[m] (d0[m] = -1) or its
+// derivative along x_d0[m], F1 likewise (f = -1: no factor; d0 / d1 NULL:
+// values only).
 double orc_integrate_fields(const orc_space* s, const double* lset_vertex, int dt, int order, int nf,
                             const int* f_order, const double* const* f_el, int nm, const double* coef,
-                            const int* e3, const int* f0, const int* f1, const uint64_t* defined_on) {
+                            const int* e3, const int* f0, const int* f1, const int* d0, const int* d1,
+                            const uint64_t* defined_on) {
   const int D = s->D;
   double sum = 0;
   std::vector<double> pts, wts;
-  double phi[20], dphi[20][3], fv[8];
+  double phi[20], dphi[20][3], fv[8][4];
   for (int e = 0; e < s->ne; e++) {
     if (defined_on && !test_bit(defined_on, e)) continue;
     Geo g;
@@ -1765,16 +1768,22 @@ double orc_integrate_fields(const orc_space* s, const double* lset_vertex, int d
       for (int i = 0; i < nf && i < 8; i++) {
         const int k = f_order[i], nd = D == 2 ? (k + 1) * (k + 2) / 2 : (k + 1) * (k + 2) * (k + 3) / 6;
         basis(D, k, gv, xi, phi, dphi);
-        double v = 0.0;
-        for (int a = 0; a < nd; a++) v += f_el[i][(size_t)e * nd + a] * phi[a];
-        fv[i] = v;
+        double v = 0.0, dr[3] = {0, 0, 0}, dp[3];
+        for (int a = 0; a < nd; a++) {
+          const double c = f_el[i][(size_t)e * nd + a];
+          v += c * phi[a];
+          for (int r = 0; r < 3; r++) dr[r] += c * dphi[a][r];
+        }
+        phys_grad(g, dr, dp);
+        fv[i][0] = v;
+        for (int r = 0; r < 3; r++) fv[i][1 + r] = dp[r];
       }
       double val = 0.0;
       for (int m = 0; m < nm; m++) {
         double t = coef[m] * std::pow(x[0], e3[3 * m]) * std::pow(x[1], e3[3 * m + 1]) *
                    (D == 3 ? std::pow(x[2], e3[3 * m + 2]) : 1.0);
-        if (f0[m] >= 0) t *= fv[f0[m]];
-        if (f1[m] >= 0) t *= fv[f1[m]];
+        if (f0[m] >= 0) t *= fv[f0[m]][d0 ? 1 + d0[m] : 0];
+        if (f1[m] >= 0) t *= fv[f1[m]][d1 ? 1 + d1[m] : 0];
         val += t;
       }
       sum += wts[q] * meas * val;

@@ -93,12 +93,15 @@ int orc_facets_with_neighbor_types(const orc_space*, const uint64_t* a, const ui
                                    int bnd_a, int bnd_b, int use_and, uint64_t* out);
 double orc_integrate(const orc_space*, const double* lset_vertex, int dt, int order,
                      int ex, int ey, int ez, const uint64_t* defined_on);
-/* Integrate of sum_m coef[m] x^e3[3m] y^e3[3m+1] z^e3[3m+2] f[f0[m]] f[f1[m]]
- * over the straight cut rule; field i: order f_order[i], element
- * coefficients f_el[i] [ne][nd_i] (at most 8 fields; -1: no factor). */
+/* Integrate of sum_m coef[m] x^e3[3m] y^e3[3m+1] z^e3[3m+2] F0 F1 over the
+ * straight cut rule, F0 = f[f0[m]] (d0[m] = -1) or its derivative along
+ * x_d0[m], F1 likewise; field i: order f_order[i], element coefficients
+ * f_el[i] [ne][nd_i] (at most 8 fields; f = -1: no factor; d0 / d1 NULL:
+ * values only). */
 double orc_integrate_fields(const orc_space*, const double* lset_vertex, int dt, int order, int nf,
                             const int* f_order, const double* const* f_el, int nm, const double* coef,
-                            const int* e3, const int* f0, const int* f1, const uint64_t* defined_on);
+                            const int* e3, const int* f0, const int* f1, const int* d0, const int* d1,
+                            const uint64_t* defined_on);
 
 /* Element matrix of the sum of volume terms on element e (row = test, col = trial). */
 int orc_element_matrix(const orc_space*, const double* lset_vertex, const orc_term* terms, int nterms,

@@ -1,8 +1,9 @@
-"""Integrate of polynomials in GridFunctions on the GPU (xg_integrate_fields,
-csrc/xg_cform.cu; `Integrate((gfu - gfex) ** 2 * dCut(lset, NEG), mesh)`, the
-error norm of the reference's demos, cutint/cutintegral.cpp:126-212) against
-the oracle (orc_integrate_fields).  Bar: within 1e-12 of the integral of the
-absolute integrand's scale; repeated calls bit-identical."""
+"""Integrate of polynomials in GridFunctions and their gradients on the GPU
+(xg_integrate_fields, csrc/xg_cform.cu; `Integrate((gfu - gfex) ** 2 *
+dCut(lset, NEG), mesh)` and `(grad(gfu) - grad(gfex)) ** 2`, the L2 and H1
+errors of the reference's demos, cutint/cutintegral.cpp:126-212) against the
+oracle (orc_integrate_fields).  Bar: within 1e-12 of the integral of the
+integrand's squared parts; repeated calls bit-identical."""
 import numpy as np
 import pytest
 import torch
@@ -82,3 +83,36 @@ def test_interpolated_polynomials_are_exact(xg, orc, D):
             got = xg.Integrate(gf * xg.dCut(g, dt, order=4), m)
             ref = xg.Integrate(xg.x ** 2 * xg.dCut(g, dt, order=4), m) + 2 * xg.Integrate(xg.y * xg.dCut(g, dt, order=4), m)
             assert abs(got - ref) < 1e-13 * max(1.0, abs(ref)), (space, dt, got, ref)
+
+
+@pytest.mark.parametrize("D,k,n", [(2, 2, 9), (2, 3, 6), (3, 1, 4), (3, 2, 3)])
+def test_h1_error_parity(xg, orc, D, k, n):
+    """The H1 error (grad(gfu) - grad(gfex)) ** 2 and grad(gfu) . (f_x, f_y[, f_z])
+    against the oracle's derivative products."""
+    m, l, g = case(xg, orc, D, n)
+    V, V2 = xg.H1(m, order=k), xg.H1(m, order=2)
+    rng = np.random.default_rng(3 + k)
+    gfu = xg.GridFunction(V)
+    gfu.vec.copy_(torch.from_numpy(rng.standard_normal(V.ndof)))
+    gfex = xg.GridFunction(V2)
+    gfex.vec.copy_(torch.from_numpy(rng.standard_normal(V2.ndof)))
+    comps = [xg.GridFunction(xg.H1(m, order=1)) for _ in range(D)]
+    for cmp in comps:
+        cmp.vec.copy_(torch.from_numpy(rng.standard_normal(m.nv)))
+    sp, sp2, sp1 = orc.Space(m, k), orc.Space(m, 2), orc.Space(m, 1)
+    fu = (k, gfu.vec.cpu().numpy()[sp.el_dofs()])
+    fe = (2, gfex.vec.cpu().numpy()[sp2.el_dofs()])
+    fc = [(1, cmp.vec.cpu().numpy()[sp1.el_dofs()]) for cmp in comps]
+    z = (0, 0, 0)
+    for dt in (xg.NEG, xg.POS, xg.IF):
+        q = 2 * k + 2
+        err = xg.Integrate((xg.grad(gfu) - xg.grad(gfex)) ** 2 * xg.dCut(g, dt, order=q), m)
+        prods = [(c, z, a, b, d, d) for d in range(D) for c, a, b in ((1.0, 0, 0), (-2.0, 0, 1), (1.0, 1, 1))]
+        ref = sp.integrate_fields(l, dt, q, [fu, fe], prods)
+        scale = sp.integrate_fields(l, dt, q, [fu, fe], [(1.0, z, a, a, d, d) for d in range(D) for a in (0, 1)])
+        assert abs(err - ref) < 1e-12 * scale, (dt, err, ref)
+        dot = xg.Integrate(xg.grad(gfu) * xg.CoefficientFunction(tuple(comps)) * xg.dCut(g, dt, order=q), m)
+        ref2 = sp.integrate_fields(l, dt, q, [fu] + fc, [(1.0, z, 0, 1 + d, d, -1) for d in range(D)])
+        scale2 = sp.integrate_fields(l, dt, q, [fu] + fc, [(1.0, z, 0, 0, d, d) for d in range(D)] +
+                                     [(1.0, z, 1 + d, 1 + d) for d in range(D)])
+        assert abs(dot - ref2) < 1e-12 * scale2, (dt, dot, ref2)

@@ -61,7 +61,7 @@ def test_integrate_of_fields_builds_the_products(monkeypatch):
         def __init__(self, mesh, order):
             self.mesh, self.order, self.h = mesh, order, ctypes.c_void_p(1)
 
-    mesh = object()
+    mesh = types.SimpleNamespace(dim=2)
 
     def gf(order):
         g = object.__new__(X.GridFunction)
@@ -77,14 +77,24 @@ def test_integrate_of_fields_builds_the_products(monkeypatch):
 
     def products():
         a = seen["a"]
-        return a[2], a[3], a[4], [(a[8][i].coef, tuple(a[8][i].e), a[8][i].f0, a[8][i].f1) for i in range(a[7])]
+        return a[2], a[3], a[4], [(a[8][i].coef, tuple(a[8][i].e), a[8][i].f0, a[8][i].f1, a[8][i].d0, a[8][i].d1)
+                                  for i in range(a[7])]
 
     lset, gu, ge = gf(1), gf(2), gf(2)
     X.Integrate((gu - ge) ** 2 * X.dCut(lset, X.NEG, order=4), mesh)
     assert seen["name"] == "xg_integrate_fields"
     z = (0, 0, 0)
-    assert products() == (X.NEG, 4, 2, [(1.0, z, 0, 0), (-2.0, z, 0, 1), (1.0, z, 1, 1)])
+    assert products() == (X.NEG, 4, 2, [(1.0, z, 0, 0, -1, -1), (-2.0, z, 0, 1, -1, -1), (1.0, z, 1, 1, -1, -1)])
     X.Integrate(levelset_domain={"levelset": lset, "domain_type": X.IF}, cf=X.x * gu + 3, mesh=mesh, order=3)
-    assert products() == (X.IF, 3, 1, [(1.0, (1, 0, 0), 0, -1), (3.0, z, -1, -1)])
+    assert products() == (X.IF, 3, 1, [(1.0, (1, 0, 0), 0, -1, -1, -1), (3.0, z, -1, -1, -1, -1)])
     with pytest.raises(NotImplementedError):
         X.Integrate(gu * gu * ge * X.dCut(lset, X.NEG), mesh)
+    # the H1 error: (grad gu - grad ge)^2 = sum_d (d_d gu)^2 - 2 d_d gu d_d ge + (d_d ge)^2
+    X.Integrate((X.grad(gu) - X.grad(ge)) ** 2 * X.dCut(lset, X.NEG), mesh)
+    want = [(c, z, a, b, d, d) for d in (0, 1) for c, a, b in ((1.0, 0, 0), (-2.0, 0, 1), (1.0, 1, 1))]
+    assert sorted(products()[3]) == sorted(want)
+    # against a vector of fields: grad(gu) . (gx, gy) = gx d_0 gu + gy d_1 gu
+    # (fields numbered as they appear: gx 0, gu 1, gy 2)
+    gx, gy = gf(1), gf(1)
+    X.Integrate(X.grad(gu) * X.CoefficientFunction((gx, gy)) * X.dCut(lset, X.NEG), mesh)
+    assert sorted(products()[3]) == sorted([(1.0, z, 0, 1, -1, 0), (1.0, z, 1, 2, 1, -1)])

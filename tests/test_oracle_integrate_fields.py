@@ -72,3 +72,43 @@ def test_products_are_the_mass_matrix(D, k):
         sq = sp.integrate_fields(l, dt, 2 * k, [(k, a[ed]), (k, b[ed])],
                                  [(1.0, (0, 0, 0), 0, 0), (-2.0, (0, 0, 0), 0, 1), (1.0, (0, 0, 0), 1, 1)])
         assert abs(sq - (a - b) @ M @ (a - b)) < 1e-12 * np.abs(M).sum()
+
+
+def test_planar_derivative_integrals():
+    """d/dx of the field x is 1: int_NEG |grad x|^2 = int_NEG d_x x = the area,
+    int_NEG d_y x = 0, int_NEG x d_x(x^2) = 2 int x^2."""
+    m = MakeStructured2DMesh(9, 9)
+    X, Y = m.coords.T
+    sp = orc.Space(m, 1)
+    l = X + 0.5 * Y - 0.6
+    gx = (1, field(m, 1, lambda p: p[:, 0]))
+    gxx = (2, field(m, 2, lambda p: p[:, 0] ** 2))
+    z = (0, 0, 0)
+    cases = [
+        ([gx], [(1.0, z, 0, 0, 0, 0), (1.0, z, 0, 0, 1, 1)], 0.35),
+        ([gx], [(1.0, z, 0, -1, 0, -1)], 0.35),
+        ([gx], [(1.0, z, 0, -1, 1, -1)], 0.0),
+        ([gx, gxx], [(1.0, z, 0, 1, -1, 0)], 2 * MXX),
+    ]
+    for fields, monos, val in cases:
+        got = sp.integrate_fields(l, orc.NEG, 4, fields, monos)
+        assert abs(got - val) < 1e-13, (monos, got, val)
+
+
+@pytest.mark.parametrize("D,k", [(2, 2), (3, 1), (3, 3)])
+def test_gradient_products_are_the_stiffness_matrix(D, k):
+    """int_dt grad f_a . grad f_b = a^T K_dt b with K the Laplace matrix on dt."""
+    m = MakeStructured2DMesh(7, 7) if D == 2 else MakeStructured3DMesh(3)
+    c = m.coords
+    l = orc.interpolate_p1_perturb(((c - 0.3) ** 2).sum(axis=1) - 0.36)
+    sp = orc.Space(m, k)
+    rng = np.random.default_rng(7)
+    a, b = rng.standard_normal(sp.ndof), rng.standard_normal(sp.ndof)
+    ed = sp.el_dofs()
+    for dt in (orc.NEG, orc.POS, orc.IF):
+        rp, cols, vals = sp.assemble(l, [dict(kind=orc.TERM_LAPLACE, domain=dt, order=2 * k)])
+        K = np.zeros((sp.ndof, sp.ndof))
+        np.add.at(K, (np.repeat(np.arange(sp.ndof), np.diff(rp)), cols), vals)
+        got = sp.integrate_fields(l, dt, 2 * k, [(k, a[ed]), (k, b[ed])],
+                                  [(1.0, (0, 0, 0), 0, 1, d, d) for d in range(D)])
+        assert abs(got - a @ K @ b) < 1e-12 * np.abs(K).sum(), (dt, got, a @ K @ b)
