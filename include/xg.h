@@ -89,7 +89,9 @@ typedef enum {
                               reference's dn(w, k) - (-1)^k dn(w.Other(), k)
                               (DiffOpDuDnk, ghostpenalty.cpp:221-365, python_xfem.cpp:1068) */
   XG_TERM_SKEL_DN2 = 11,   /* c * [d^2_n u][d^2_n v] */
-  XG_TERM_SKEL_DN3 = 12    /* c * [d^3_n u][d^3_n v] */
+  XG_TERM_SKEL_DN3 = 12,   /* c * [d^3_n u][d^3_n v] */
+  XG_TERM_NGRADU_NGRADV = 13 /* c * (n . grad u) * (n . grad v): the normal-diffusion term of
+                                TraceFEM; coefficient terms (xg_cterm) only */
 } xg_term_kind;
 
 typedef enum { XG_PREC_FP64 = 0, XG_PREC_MIXED = 1 } xg_precision;
@@ -385,7 +387,7 @@ int xg_form_set_bnd_terms(xg_form* form, const xg_bterm* terms, int32_t nterms);
 
 /* Volume terms with a coefficient field (`gf * u * v * dCut(...)`,
  * `gf * grad(u) * grad(v) * dCut(...)`, x^e factors): the integrand of kind
- * XG_TERM_MASS, _LAPLACE, _NGRADU_V, _U_NGRADV or _CONV times
+ * XG_TERM_MASS, _LAPLACE, _NGRADU_V, _U_NGRADV, _CONV or _NGRADU_NGRADV times
  * c * h^hpow * x^e0 y^e1 z^e2 * gf(x), evaluated at the points of the
  * domain's cut rule (the reference evaluates any CoefficientFunction at the
  * rule's points, xfem/symboliccutbfi.cpp:168-194; default order: the
@@ -393,11 +395,13 @@ int xg_form_set_bnd_terms(xg_form* form, const xg_bterm* terms, int32_t nterms);
  * GridFunction of an H1 space of order 1..3 on the form's mesh (gf_space,
  * d_gf its coefficients) or absent (gf_space NULL).  The elements of the
  * term's set whose domain type is the term's domain or IF join the active
- * elements; their matrices are the sums of all their terms.  Spatial forms on
- * simplex meshes. */
+ * elements; their matrices are the sums of all their terms.  Domain XG_WHOLE
+ * (`dx(definedonelements=...)`, e.g. TraceFEM's normal diffusion): the
+ * element's own rule on every element of the set, cut or not.  Spatial forms
+ * on simplex meshes. */
 typedef struct {
   int32_t kind;
-  int32_t domain; /* XG_NEG, XG_POS, XG_IF */
+  int32_t domain; /* XG_NEG, XG_POS, XG_IF, XG_WHOLE */
   int32_t order;  /* -1: the kind's default */
   int32_t hpow;
   double coef;

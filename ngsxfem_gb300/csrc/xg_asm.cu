@@ -2674,6 +2674,7 @@ int default_order(int kind, int k) {
     case XG_TERM_U_NGRADV:
     case XG_TERM_CONV: return 2 * k - 1;
     case XG_TERM_GHOST_MASS: return 2 * k;
+    case XG_TERM_NGRADU_NGRADV: return 2 * k - 2;
   }
   return 2 * k;
 }
@@ -3935,11 +3936,11 @@ int xg_form_set_coef_terms(xg_form* f, const xg_cterm* terms, int32_t nterms) {
   for (int t = 0; t < nterms; t++) {
     const xg_cterm& T = terms[t];
     const bool kind_ok = T.kind == XG_TERM_MASS || T.kind == XG_TERM_LAPLACE || T.kind == XG_TERM_NGRADU_V ||
-                         T.kind == XG_TERM_U_NGRADV || T.kind == XG_TERM_CONV;
-    if (!kind_ok || (T.domain != XG_NEG && T.domain != XG_POS && T.domain != XG_IF) || T.order > kMaxOrder ||
-        T.e[0] < 0 || T.e[1] < 0 || T.e[2] < 0) {
-      set_last_error("xg_form_set_coef_terms: kinds MASS, LAPLACE, NGRADU_V, U_NGRADV, CONV on NEG, POS or IF, "
-                     "order <= 8, exponents >= 0");
+                         T.kind == XG_TERM_U_NGRADV || T.kind == XG_TERM_CONV || T.kind == XG_TERM_NGRADU_NGRADV;
+    if (!kind_ok || (T.domain != XG_NEG && T.domain != XG_POS && T.domain != XG_IF && T.domain != XG_WHOLE) ||
+        T.order > kMaxOrder || T.e[0] < 0 || T.e[1] < 0 || T.e[2] < 0) {
+      set_last_error("xg_form_set_coef_terms: kinds MASS, LAPLACE, NGRADU_V, U_NGRADV, CONV, NGRADU_NGRADV on NEG, "
+                     "POS, IF or WHOLE, order <= 8, exponents >= 0");
       return XG_ERR_ARG;
     }
     const xg_space* g = T.gf_space;

@@ -1,12 +1,14 @@
 // Volume terms of bilinear forms with a coefficient field: the integrand of a
-// menu kind (mass, Laplace, the Nitsche normal terms, convection) times
+// menu kind (mass, Laplace, the Nitsche normal terms, convection, the
+// normal-normal stiffness (n . grad u)(n . grad v) of TraceFEM) times
 // c h^p x^e gf(x), gf a GridFunction of an H1 space on the form's mesh.  The
 // reference evaluates its CoefficientFunction at the points of the cut rule
 // and contracts (xfem/symboliccutbfi.cpp:76-313, the evaluation at
 // :168-194); the rule is StraightCutIntegrationRule
 // (cutint/straightcutrule.cpp:582-677: the standard rule on uncut elements of
 // the term's domain, the sub-simplices of Decompose on cut ones, the
-// interface factor for IF), with the rule code of xg_cut.cuh.  Thread per
+// interface factor for IF; domain XG_WHOLE, dx(definedonelements=...): the
+// element's own rule), with the rule code of xg_cut.cuh.  Thread per
 // active element, FP64 sums added to the element's rows after the volume
 // kernels wrote them (one thread owns an element's rows: no atomics, a fixed
 // order).
@@ -40,10 +42,11 @@ __device__ __forceinline__ double cf_ipow(double x, int e) {
   return r;
 }
 
-// does term T contribute on element e of domain type dom
+// does term T contribute on element e of domain type dom (XG_WHOLE: the
+// whole element, cut or not)
 __device__ __forceinline__ bool term_on(const CoefTermDev& T, int64_t e, int dom) {
   if (T.defined_on && !cf_bit64(T.defined_on, e)) return false;
-  return dom == XG_IF || dom == T.domain;
+  return dom == XG_IF || dom == T.domain || T.domain == XG_WHOLE;
 }
 
 // descriptor of local function i of an H1 element of runtime order k
@@ -172,6 +175,7 @@ __global__ void __launch_bounds__(128) k_coef_elmat(CoefFormLaunch L) {
                 break;
               }
               case XG_TERM_U_NGRADV: v = phi[b] * dn[a]; break;
+              case XG_TERM_NGRADU_NGRADV: v = dn[b] * dn[a]; break;
               default: v = dn[b] * phi[a]; break;  // XG_TERM_NGRADU_V, XG_TERM_CONV
             }
             A[a * N + b] += Wt * v;
@@ -236,7 +240,7 @@ __global__ void __launch_bounds__(128) k_coef_elmat(CoefFormLaunch L) {
         point(xi, w, gp, np, xp, cp);
       };
       const int p = clamp_order(Tm.order);
-      if (cdom != XG_IF) {
+      if (cdom != XG_IF || Tm.domain == XG_WHOLE) {
         const int off = g_cf_rules.off[D][p], cnt = g_cf_rules.cnt[D][p];
         for (int q = 0; q < cnt; q++) ref_point(g_cf_rules.x[off + q], g_cf_rules.w[off + q]);
         continue;

@@ -37,6 +37,7 @@ VOL, BND = "VOL", "BND"
 
 TERM_MASS, TERM_LAPLACE, TERM_NGRADU_V, TERM_U_NGRADV, TERM_CONV, TERM_GHOST_MASS, TERM_DT_U_V = range(7)
 TERM_SKEL_JUMP, TERM_SKEL_FLUX, TERM_SKEL_FLUX_T, TERM_SKEL_DN1, TERM_SKEL_DN2, TERM_SKEL_DN3 = range(7, 13)
+TERM_NGRADU_NGRADV = 13
 PREC_FP64, PREC_MIXED = 0, 1
 XG_LTERM_SOURCE, XG_LTERM_SOURCE_GF, XG_LTERM_SOURCE_BND = 0, 1, 2
 
@@ -713,8 +714,8 @@ class _Measure:
                 raise NotImplementedError("dCut/dFacetPatch option %r is not part of the GPU path" % k)
         self.deformation = kw.get("deformation")
         if self.deformation is not None:
-            if kind not in ("cut", "patch") or not isinstance(self.deformation, LevelSetMeshAdaptation):
-                raise NotImplementedError("deformation: dCut / dFacetPatch(..., deformation="
+            if kind not in ("cut", "patch", "vol") or not isinstance(self.deformation, LevelSetMeshAdaptation):
+                raise NotImplementedError("deformation: dCut / dFacetPatch / dx(..., deformation="
                                           "LevelSetMeshAdaptation(..).CalcDeformation(..))")
         self.definedon = kw.get("definedon")
         if self.definedon is not None and (kind != "cut" or kw.get("vb", VOL) != BND):
@@ -751,12 +752,16 @@ def dCut(levelset, domain_type, order=None, subdivlvl=None, time_order=-1, level
 
 
 def dx(skeleton=False, definedonelements=None, **kwargs):
-    """Whole-facet skeleton integrals (SymbolicFacetBilinearFormIntegrator2,
-    symboliccutbfi.cpp:1574-1735), e.g. the derivative-jump ghost penalty
-    dn-jumps * dx(skeleton=True, definedonelements=ghost_facets).  Volume
-    integrals without a level set are not part of the GPU path."""
+    """Whole-element integrals (the element's own rule, cut or not) on the
+    elements of definedonelements (all without it), e.g. TraceFEM's normal
+    diffusion (grad(u) * n) * (grad(v) * n) * dx(definedonelements=ba_IF,
+    deformation=...) in a BilinearForm with dCut terms of the same level set;
+    with skeleton=True whole-facet skeleton integrals
+    (SymbolicFacetBilinearFormIntegrator2, symboliccutbfi.cpp:1574-1735), e.g.
+    the derivative-jump ghost penalty dn-jumps * dx(skeleton=True,
+    definedonelements=ghost_facets)."""
     if not skeleton:
-        raise NotImplementedError("dx without skeleton=True: use dCut for element integrals")
+        return _Measure("vol", None, WHOLE, kwargs.pop("order", None), definedonelements, **kwargs)
     return _Measure("skel", None, WHOLE, kwargs.pop("order", None), definedonelements, skeleton=True, **kwargs)
 
 
@@ -822,10 +827,12 @@ class _Integral:
             if any(a[1] for a in scal if a[0] in ("u", "v")):
                 raise NotImplementedError(".Other() is only meaningful on facet patches")
             names = sorted(a[0] for a in scal)
-            dots = [tuple(sorted((d[0][0], d[1][0]))) for d in mono.dots]
             kind, b = None, (0.0, 0.0, 0.0)
             nrm_index = 0
-            for d in mono.dots:
+            # n . n = 1 for the unit normal of one level set
+            mono_dots = [d for d in mono.dots if not (d[0][0] == "n" and d[1][0] == "n" and d[0][1] == d[1][1])]
+            dots = [tuple(sorted((d[0][0], d[1][0]))) for d in mono_dots]
+            for d in mono_dots:
                 for v in d:
                     if v[0] != "n" or nrm_gf is None:
                         continue
@@ -843,16 +850,18 @@ class _Integral:
                 kind = TERM_DT_U_V
             elif names == ["v"] and len(dots) == 1 and set(dots[0]) == {"gu", "tb"}:
                 kind = TERM_CONV
-                tb = [x for x in mono.dots[0] if x[0] == "tb"][0][1]
+                tb = [x for x in mono_dots[0] if x[0] == "tb"][0][1]
             elif not names and dots == [("gu", "gv")]:
                 kind = TERM_LAPLACE
+            elif not names and sorted(dots) == [("gu", "n"), ("gv", "n")]:
+                kind = TERM_NGRADU_NGRADV
             elif names == ["v"] and dots == [("gu", "n")]:
                 kind = TERM_NGRADU_V
             elif names == ["u"] and dots == [("gv", "n")]:
                 kind = TERM_U_NGRADV
             elif names == ["v"] and len(dots) == 1 and set(dots[0]) == {"gu", "b"}:
                 kind = TERM_CONV
-                bv = [x for x in mono.dots[0] if x[0] == "b"][0][1]
+                bv = [x for x in mono_dots[0] if x[0] == "b"][0][1]
                 b = tuple(list(bv) + [0.0] * (3 - len(bv)))
             else:
                 raise NotImplementedError("integrand term outside the supported menu: %s" % (names + dots,))
@@ -1149,10 +1158,11 @@ class BilinearForm:
                 continue
             # volume terms on the deformed mesh go to the coefficient kernel;
             # deformed patch terms stay patch terms (xg_form_set_deformation)
-            deform = getattr(it.measure, "deformation", None) if it.measure.kind == "cut" else None
+            deform = getattr(it.measure, "deformation", None) if it.measure.kind in ("cut", "vol") else None
             for t in it.terms(lset):
                 t["deform"] = deform
-                generic = t.get("gf") is not None or any(t.get("e", (0, 0, 0))) or deform is not None
+                generic = t.get("gf") is not None or any(t.get("e", (0, 0, 0))) or deform is not None or \
+                    t["kind"] == TERM_NGRADU_NGRADV or it.measure.kind == "vol"
                 (cterms if generic else terms).append(t)
         arr = (_lib.Term * max(len(terms), 1))()
         self._keep = []
@@ -1194,9 +1204,10 @@ class BilinearForm:
         if cterms:
             carr = (_lib.CTerm * len(cterms))()
             for k, t in enumerate(cterms):
-                if t["kind"] not in (TERM_MASS, TERM_LAPLACE, TERM_NGRADU_V, TERM_U_NGRADV, TERM_CONV) or \
-                        t.get("tb") is not None:
-                    raise NotImplementedError("coefficient fields multiply mass, Laplace, Nitsche and convection terms")
+                if t["kind"] not in (TERM_MASS, TERM_LAPLACE, TERM_NGRADU_V, TERM_U_NGRADV, TERM_CONV,
+                                     TERM_NGRADU_NGRADV) or t.get("tb") is not None:
+                    raise NotImplementedError("coefficient fields and dx terms: mass, Laplace, Nitsche, convection "
+                                              "and normal-normal terms")
                 carr[k].kind, carr[k].domain, carr[k].order, carr[k].hpow = t["kind"], t["domain"], t["order"], t["hpow"]
                 carr[k].coef = t["coef"]
                 for j in range(3):

@@ -15,6 +15,7 @@ LIB = os.path.join(HERE, "_build", "liboracle.so")
 NEG, POS, IF, WHOLE = 0, 1, 2, 3
 TERM_MASS, TERM_LAPLACE, TERM_NGRADU_V, TERM_U_NGRADV, TERM_CONV, TERM_GHOST_MASS, TERM_DT_U_V = range(7)
 TERM_SKEL_JUMP, TERM_SKEL_FLUX, TERM_SKEL_FLUX_T, TERM_SKEL_DN1, TERM_SKEL_DN2, TERM_SKEL_DN3 = range(7, 13)
+TERM_NGRADU_NGRADV = 13
 
 
 class Term(ctypes.Structure):

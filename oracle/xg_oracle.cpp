@@ -763,6 +763,7 @@ int default_order(int kind, int k) {
     case ORC_TERM_LAPLACE: return 2 * k - 2;
     case ORC_TERM_NGRADU_V: case ORC_TERM_U_NGRADV: case ORC_TERM_CONV: return 2 * k - 1;
     case ORC_TERM_GHOST_MASS: return 2 * k;
+    case ORC_TERM_NGRADU_NGRADV: return 2 * k - 2;
   }
   return 2 * k;
 }
@@ -860,7 +861,16 @@ int element_matrix_coef(const orc_space* s, const double* lset_vertex, const orc
       const double ref2[6] = {1, 0, 0, 1, 0, 0}, ref3[12] = {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0};
       make_geo(D, D == 2 ? ref2 : ref3, gref);
     }
-    const int np = straight_cut_rule(th ? gref : g, l, T.domain, order, pts, wts);
+    // the whole element (dx): the element's own rule, whatever the cut
+    int np;
+    if (T.domain == ORC_WHOLE) {
+      const Rule& r = get_rule(D, order);
+      pts = r.p;
+      wts = r.w;
+      np = r.size();
+    } else {
+      np = straight_cut_rule(th ? gref : g, l, T.domain, order, pts, wts);
+    }
     if (np < -1) return np;
     if (np <= 0) continue;
     double c = T.coef;
@@ -950,6 +960,10 @@ int element_matrix_coef(const orc_space* s, const double* lset_vertex, const orc
             case ORC_TERM_MASS: v = phi[i] * phi[j]; break;
             case ORC_TERM_LAPLACE: v = gphys[i][0] * gphys[j][0] + gphys[i][1] * gphys[j][1] + gphys[i][2] * gphys[j][2]; break;
             case ORC_TERM_U_NGRADV: v = phi[j] * (bb[0] * gphys[i][0] + bb[1] * gphys[i][1] + bb[2] * gphys[i][2]); break;
+            case ORC_TERM_NGRADU_NGRADV:
+              v = (bb[0] * gphys[j][0] + bb[1] * gphys[j][1] + bb[2] * gphys[j][2]) *
+                  (bb[0] * gphys[i][0] + bb[1] * gphys[i][1] + bb[2] * gphys[i][2]);
+              break;
             default: v = (bb[0] * gphys[j][0] + bb[1] * gphys[j][1] + bb[2] * gphys[j][2]) * phi[i]; break;
           }
           elmat[i * n + j] += w * v;
@@ -2271,7 +2285,8 @@ orc_csr* orc_assemble_full(const orc_space* s, const double* lset_vertex, const 
           (dom == ORC_IF || dom == terms[t].domain))
         act = true;
     for (int t = 0; t < ncterms; t++)
-      if ((!cterms[t].defined_on || test_bit(cterms[t].defined_on, e)) && (dom == ORC_IF || dom == cterms[t].domain))
+      if ((!cterms[t].defined_on || test_bit(cterms[t].defined_on, e)) &&
+          (dom == ORC_IF || dom == cterms[t].domain || cterms[t].domain == ORC_WHOLE))
         act = true;
     if (act) el_slot[e] = nact++;
   }

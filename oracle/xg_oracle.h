@@ -42,7 +42,8 @@ enum {
   ORC_TERM_SKEL_FLUX_T = 9,  /* c * (u - u') * ((grad v + grad v') . n_F)             */
   ORC_TERM_SKEL_DN1 = 10,    /* c * [d_n u] [d_n v], [d^k_n w] = d^k_n w - d^k_n w'  */
   ORC_TERM_SKEL_DN2 = 11,    /* c * [d^2_n u] [d^2_n v]                              */
-  ORC_TERM_SKEL_DN3 = 12     /* c * [d^3_n u] [d^3_n v]                              */
+  ORC_TERM_SKEL_DN3 = 12,    /* c * [d^3_n u] [d^3_n v]                              */
+  ORC_TERM_NGRADU_NGRADV = 13 /* c * (n . grad u) (n . grad v); coefficient terms (orc_cterm) */
 };
 
 typedef struct {
@@ -170,9 +171,11 @@ typedef struct {
 orc_csr* orc_assemble_bnd(const orc_space* s, const double* lset_vertex, const orc_term* terms, int nterms,
                           const orc_bterm* bterms, int nbterms, int nthreads, int dn_fd);
 /* A volume term with a coefficient field: the integrand of kind (MASS,
- * LAPLACE, NGRADU_V, U_NGRADV, CONV) times c h^hpow x^e gf(x), evaluated at
- * the points of the straight cut rule; gf given per element in the
- * element's basis order ([ne][ndof_el(D, gf_order)]), gf_order 0 = none. */
+ * LAPLACE, NGRADU_V, U_NGRADV, CONV, NGRADU_NGRADV) times c h^hpow x^e gf(x),
+ * evaluated at the points of the straight cut rule (domain ORC_WHOLE: the
+ * element's own rule, cut or not, as dx(definedonelements=...)); gf given
+ * per element in the element's basis order ([ne][ndof_el(D, gf_order)]),
+ * gf_order 0 = none. */
 typedef struct {
   int kind, domain, order, hpow;
   double coef;

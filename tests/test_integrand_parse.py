@@ -98,3 +98,24 @@ def test_integrate_of_fields_builds_the_products(monkeypatch):
     gx, gy = gf(1), gf(1)
     X.Integrate(X.grad(gu) * X.CoefficientFunction((gx, gy)) * X.dCut(lset, X.NEG), mesh)
     assert sorted(products()[3]) == sorted([(1.0, z, 0, 1, -1, 0), (1.0, z, 1, 2, 1, -1)])
+
+
+def test_tracefem_integrands():
+    """P(grad u) . P(grad v) with P(w) = w - (w . n) n on the interface: the
+    Laplacian, two normal-normal terms with -1 and one with +1 (n . n = 1);
+    (grad u . n)(grad v . n) * dx(definedonelements=...) is a whole-element
+    normal-normal term."""
+    lset = object.__new__(X.GridFunction)
+    n = X.Normalize(X.grad(lset))
+    u, v = X._Expr.atom(("u", False)), X._Expr.atom(("v", False))
+
+    def P(w):
+        return w - (w * n) * n
+
+    t = (P(X.grad(u)) * P(X.grad(v)) * X._Measure("cut", lset, X.IF)).terms(lset)
+    got = sorted((x["kind"], x["coef"]) for x in t)
+    assert got == sorted([(X.TERM_LAPLACE, 1.0), (X.TERM_NGRADU_NGRADV, -1.0), (X.TERM_NGRADU_NGRADV, -1.0),
+                          (X.TERM_NGRADU_NGRADV, 1.0)])
+    h = X.specialcf.mesh_size
+    t = ((1.0 / h) * (X.grad(u) * n) * (X.grad(v) * n) * X.dx(definedonelements=None)).terms(lset)
+    assert [(x["kind"], x["domain"], x["hpow"]) for x in t] == [(X.TERM_NGRADU_NGRADV, X.WHOLE, -1)]

@@ -91,3 +91,35 @@ def test_unit_field_gives_the_plain_terms(orc, D, k):
         A = dense(sp, sp.assemble(l, [t]))
         B = dense(sp, sp.assemble(l, [], cterms=[dict(t, gf_order=1, gf_el=g1)]))
         assert np.abs(A - B).max() < 1e-13 * np.abs(A).max(), kind
+
+
+@pytest.mark.parametrize("k", [1, 2])
+def test_planar_normal_and_whole_element_terms(orc, k):
+    """The TraceFEM terms on the planar cut (n = (1, 1/2) / sqrt(1.25)):
+    (n . grad x)^2 over NEG = 0.35 * 0.8, n_x n_y over the interface =
+    0.4 * |IF|, the tangential Laplacian (Laplace - normal-normal) of x over
+    the interface = (1 - 0.8) |IF|; whole elements (dx): the mass of the
+    interface elements is their area, without a set the square's."""
+    m = MakeStructured2DMesh(9, 9)
+    X, Y = m.coords.T
+    sp = orc.Space(m, k)
+    l = X + 0.5 * Y - 0.6
+    one, x, y = np.zeros(sp.ndof), np.zeros(sp.ndof), np.zeros(sp.ndof)
+    one[: m.nv], x[: m.nv], y[: m.nv] = 1.0, X, Y
+    NN = orc.TERM_NGRADU_NGRADV
+    A = dense(sp, sp.assemble(l, [], cterms=[dict(kind=NN, domain=orc.NEG)]))
+    assert abs(x @ A @ x - 0.35 * 0.8) < 1e-13
+    B = dense(sp, sp.assemble(l, [], cterms=[dict(kind=NN, domain=orc.IF)]))
+    assert abs(x @ B @ y - 0.4 * LEN) < 1e-13
+    T = dense(sp, sp.assemble(l, [], cterms=[dict(kind=orc.TERM_LAPLACE, domain=orc.IF),
+                                             dict(kind=NN, domain=orc.IF, coef=-1.0)]))
+    assert abs(x @ T @ x - 0.2 * LEN) < 1e-13
+    dom, _, bits = sp.cutinfo(l)
+    n_if = int(np.sum(np.asarray(dom) == orc.IF))
+    W = dense(sp, sp.assemble(l, [], cterms=[dict(kind=orc.TERM_MASS, domain=orc.WHOLE, defined_on=bits[4])]))
+    assert abs(one @ W @ one - n_if / 162.0) < 1e-13
+    W1 = dense(sp, sp.assemble(l, [], cterms=[dict(kind=orc.TERM_MASS, domain=orc.WHOLE)]))
+    assert abs(one @ W1 @ one - 1.0) < 1e-13
+    # the normal-normal term on whole elements: (n . grad x)^2 = 0.8 over them
+    Wn = dense(sp, sp.assemble(l, [], cterms=[dict(kind=NN, domain=orc.WHOLE, defined_on=bits[4])]))
+    assert abs(x @ Wn @ x - 0.8 * n_if / 162.0) < 1e-13
