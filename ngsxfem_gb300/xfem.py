@@ -134,6 +134,21 @@ class BitArray:
         return BitArray(self.n, (~self.words) & self._mask())
 
     @staticmethod
+    def from_bool(mask):
+        """Packs a device bool tensor into a BitArray on the same device."""
+        n = int(mask.numel())
+        pad = (-n) % 64
+        m = torch.cat([mask.reshape(-1).to(torch.int64), torch.zeros(pad, dtype=torch.int64, device=mask.device)])
+        weights = torch.ones(64, dtype=torch.int64, device=mask.device) << torch.arange(64, device=mask.device)
+        # distinct bits: the sum is the OR (bit 63 wraps to the sign bit)
+        return BitArray(n, (m.reshape(-1, 64) * weights).sum(dim=1))
+
+    def bool_tensor(self):
+        """The bits as a device bool tensor of length n."""
+        i = torch.arange(self.n, device=self.words.device)
+        return ((self.words[i >> 6] >> (i & 63)) & 1).bool()
+
+    @staticmethod
     def from_numpy(bits):
         bits = np.asarray(bits, dtype=bool)
         n = bits.size
@@ -181,8 +196,22 @@ class H1:
     def TnT(self):
         return self.TrialFunction(), self.TestFunction()
 
+    def FreeDofs(self, coupling=False):
+        """All dofs, or those of the active elements of a Restrict(...) view
+        (no Dirichlet dofs: boundary conditions are imposed weakly)."""
+        active = getattr(self, "_active_elements", None)
+        if active is None:
+            return BitArray.from_bool(torch.ones(self.ndof, dtype=torch.bool, device=_dev()))
+        return GetDofsOfElements(self, active)
+
+    def _element_dofs_device(self):
+        if getattr(self, "_el_dofs_dev", None) is None:
+            self._el_dofs_dev = torch.from_numpy(self.element_dofs().astype(np.int64)).to(_dev())
+        return self._el_dofs_dev
+
     def __del__(self):
-        if getattr(self, "h", None) and _lib._lib is not None:
+        # a Restrict(...) view shares the handle of the space it was made from
+        if getattr(self, "h", None) and getattr(self, "_owner", True) and _lib._lib is not None:
             _lib.load().xg_space_destroy(self.h)
             self.h = None
 
@@ -374,6 +403,37 @@ class GridFunction:
 
     def __pow__(self, p):
         return self._atom() ** p
+
+
+def GetDofsOfElements(space, a, heapsize=None):
+    """The dofs of the elements in the BitArray a (the reference's
+    GetDofsOfElements), marked on the device from the space's element-dof
+    table."""
+    el = space._element_dofs_device()
+    if a.n != el.shape[0]:
+        raise ValueError("the BitArray must have one bit per element of the space's mesh")
+    mask = torch.zeros(space.ndof, dtype=torch.bool, device=_dev())
+    mask[el[a.bool_tensor()].reshape(-1)] = True
+    return BitArray.from_bool(mask)
+
+
+def Restrict(space, active_elements):
+    """A view of the space whose FreeDofs() are the dofs of the active
+    elements (the reference's Restrict(fes, ba)).  The dof numbering stays
+    the space's: the assembled matrix holds the rows of the active elements
+    only, and FreeDofs() selects them for a solver."""
+    view = object.__new__(type(space))
+    view.__dict__.update(space.__dict__)
+    view._base, view._owner, view._active_elements = space, False, active_elements
+    return view
+
+
+def Compress(space, active_dofs):
+    """Compress(fes, GetDofsOfElements(fes, ba)): the space with FreeDofs() =
+    active_dofs (numbering kept, as Restrict)."""
+    view = Restrict(space, None)
+    view.FreeDofs = lambda coupling=False: active_dofs
+    return view
 
 
 def InterpolateToP1(f, gf, eps_perturbation=1e-14):
@@ -972,6 +1032,19 @@ class SparseMatrix:
         import scipy.sparse as sp
         r, c, v = self.global_coo()
         return sp.csr_matrix((v, (r, c)), shape=(self.ndof, self.ndof))
+
+
+def RestrictedBilinearForm(space, name="a", element_restriction=None, facet_restriction=None, check_unused=True,
+                           **kwargs):
+    """The reference's RestrictedBilinearForm (utils/restrictedblf.cpp:7-168):
+    a BilinearForm whose sparsity graph holds only the couplings of the
+    restricted elements and facets.  Here every form's pattern is that of its
+    active elements and facets already (the integrators' definedonelements
+    decide them), so this is a BilinearForm; the restrictions are kept as
+    attributes."""
+    a = BilinearForm(space, **kwargs)
+    a.element_restriction, a.facet_restriction = element_restriction, facet_restriction
+    return a
 
 
 class BilinearForm:
