@@ -518,7 +518,7 @@ int xg_mlset_form_assemble(xg_form* form, const double* d_lsets, xg_csr* out, vo
 /* ---- linear forms (xfem/symboliccutlfi.cpp) --------------------------------- */
 typedef enum {
   XG_LTERM_SOURCE = 0,     /* coef * x^e0 y^e1 z^e2 * v                         */
-  XG_LTERM_SOURCE_GF = 1,  /* coef * u_h * v, u_h = d_gf (dof vector, same space) */
+  XG_LTERM_SOURCE_GF = 1,  /* coef * u_h * v, u_h = d_gf (dof vector of gf_space, NULL: the form's space) */
   XG_LTERM_SOURCE_BND = 2  /* coef * x^e0 y^e1 z^e2 * v * dCut(lset, domain, vb=BND): the
                               domain part of the BND elements (xg_integrate_bnd's rule, the
                               trace of the owning element's basis); d_defined_on: bits over
@@ -533,6 +533,8 @@ typedef struct {
   double coef;
   const double* d_gf;         /* XG_LTERM_SOURCE_GF */
   const uint64_t* d_defined_on; /* element bits; NULL = all */
+  const xg_space* gf_space;   /* XG_LTERM_SOURCE_GF: u_h's space (spatial H1 / L2 of order 1..3 on the
+                                 form's mesh); NULL: the form's space */
 } xg_lterm;
 typedef struct xg_lform xg_lform;
 /* At most 8 terms on a spatial H1 space. */

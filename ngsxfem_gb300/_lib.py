@@ -63,7 +63,7 @@ class Term(ctypes.Structure):
 class LTerm(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int32), ("domain", ctypes.c_int32), ("order", ctypes.c_int32),
                 ("e", ctypes.c_int32 * 3), ("coef", ctypes.c_double), ("d_gf", ctypes.c_void_p),
-                ("d_defined_on", ctypes.c_void_p)]
+                ("d_defined_on", ctypes.c_void_p), ("gf_space", ctypes.c_void_p)]
 
 
 class MlTerm(ctypes.Structure):

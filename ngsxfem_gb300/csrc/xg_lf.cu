@@ -6,7 +6,8 @@
 // element carries (uncut and matching: the element's own rule; cut: the
 // straight cut rule of the term's domain, interface weights with |F^-T n|),
 //   elvec_i += w_q |det F| g(x_q) phi_i(x_q),
-// g = coef * x^e0 y^e1 z^e2 or coef * u_h (u_h a function of the same space);
+// g = coef * x^e0 y^e1 z^e2 or coef * u_h (u_h a function of the form's space
+// or of another H1 / L2 space of the mesh, by its own basis);
 // the default order is 2k (symboliccutlfi.cpp:93-94).  Then thread per dof:
 // the sum over the dof's (element, local) adjacency in ascending element
 // order -- a fixed order, no atomics.
@@ -42,6 +43,8 @@ constexpr int kMaxLTerms = 8;
 struct LfDesc {
   int n;
   xg_lterm t[kMaxLTerms];
+  int gf_order[kMaxLTerms];           // XG_LTERM_SOURCE_GF in another space: its order (0: the form's space)
+  const int32_t* gf_dofs[kMaxLTerms]; // and its element dofs [nd][ne]
   const double* gdef;        // mesh deformation [nedges][3] of the volume terms, or NULL
   const int32_t* el_edges;   // [nedges per element][ne]
 };
@@ -49,6 +52,12 @@ struct LfDesc {
 namespace {
 
 __device__ __forceinline__ bool tbit64(const uint64_t* b, int64_t i) { return (b[i >> 6] >> (i & 63)) & 1ull; }
+
+// descriptor of local function i of an H1 element of runtime order k
+template <int D>
+__device__ __forceinline__ int lf_desc_rt(int k, int i, const int* gv) {
+  return k == 1 ? fn_desc<D, 1>(i, gv) : (k == 2 ? fn_desc<D, 2>(i, gv) : fn_desc<D, 3>(i, gv));
+}
 
 __device__ __forceinline__ double ipow(double x, int e) {
   double r = 1.0;
@@ -182,10 +191,17 @@ __global__ void __launch_bounds__(128) k_lf_elvec(int ne, int nv, const int32_t*
               x[i] = sacc;
             }
             gval = T.coef * ipow(x[0], T.e[0]) * ipow(x[1], T.e[1]) * (D == 3 ? ipow(x[2], T.e[2]) : 1.0);
-          } else {
+          } else if (d.gf_order[t] == 0) {
             double u = 0.0;
 #pragma unroll
             for (int j = 0; j < N; j++) u += T.d_gf[el_dofs[(int64_t)e * N + j]] * phi[j];
+            gval = T.coef * u;
+          } else {
+            // u_h of another space: its own basis at the point
+            const int kg = d.gf_order[t], ng = ndof_el(D, kg);
+            double u = 0.0;
+            for (int j = 0; j < ng; j++)
+              u += T.d_gf[d.gf_dofs[t][(int64_t)j * ne + e]] * eval_fn_value<D, double>(lf_desc_rt<D>(kg, j, gv), lam);
             gval = T.coef * u;
           }
           const double w = c_rules.w[off + q] * vol * wdef * gval;
@@ -337,6 +353,14 @@ int xg_lform_create(xg_space* space, const xg_lterm* terms, int32_t n, xg_lform*
       set_last_error("xg_lform_create: the interface on boundary triangles (codimension 2) is not supported");
       return XG_ERR_UNSUPPORTED;
     }
+    const xg_space* gs = T.kind == XG_LTERM_SOURCE_GF ? T.gf_space : nullptr;
+    if (gs && gs != space &&
+        (gs->mesh != space->mesh || gs->kt >= 0 || gs->order < 1 || gs->order > 3 ||
+         gs->nd != ndof_el(space->mesh->dim, gs->order))) {
+      set_last_error("xg_lform_create: the source GridFunction needs a spatial H1 / L2 space of order 1..3 on "
+                     "the form's mesh");
+      return XG_ERR_ARG;
+    }
     if ((T.kind != XG_LTERM_SOURCE && T.kind != XG_LTERM_SOURCE_GF && T.kind != XG_LTERM_SOURCE_BND) ||
         T.domain < 0 || T.domain > 2 ||
         T.order > kMaxOrder || (T.kind == XG_LTERM_SOURCE_GF && !T.d_gf) || T.e[0] < 0 || T.e[1] < 0 || T.e[2] < 0) {
@@ -349,7 +373,14 @@ int xg_lform_create(xg_space* space, const xg_lterm* terms, int32_t n, xg_lform*
   f->space = space;
   std::memset(&f->desc, 0, sizeof(f->desc));
   f->desc.n = n;
-  for (int t = 0; t < n; t++) f->desc.t[t] = terms[t];
+  for (int t = 0; t < n; t++) {
+    f->desc.t[t] = terms[t];
+    const xg_space* gs = terms[t].kind == XG_LTERM_SOURCE_GF ? terms[t].gf_space : nullptr;
+    if (gs && gs != space) {
+      f->desc.gf_order[t] = gs->order;
+      f->desc.gf_dofs[t] = gs->d_el_dofs;
+    }
+  }
   cudaError_t e = cudaMalloc((void**)&f->d_elvec, sizeof(double) * (size_t)space->mesh->ne * space->nd);
   if (!e) e = cudaMalloc((void**)&f->d_err, sizeof(int));
   if (!e) e = cudaMemset(f->d_err, 0, sizeof(int));

@@ -1432,8 +1432,11 @@ class LinearForm:
                         e = a[1]
                     elif a[0] == "gf" and gf is None and e == (0, 0, 0):
                         kind, gf = XG_LTERM_SOURCE_GF, a[1]
-                        if gf.space.ndof != self.space.ndof or gf.space.order != self.space.order:
-                            raise ValueError("the coefficient GridFunction must live in the form's space")
+                        gs = gf.space
+                        if isinstance(gs, SpaceTimeFESpace) or gs.mesh is not self.space.mesh or \
+                                getattr(gs, "h", None) is None:
+                            raise ValueError("the coefficient GridFunction must live in a spatial H1 / L2 space "
+                                             "of the form's mesh")
                     else:
                         raise NotImplementedError("one monomial or one GridFunction factor per term")
                 defined = m.definedonelements
@@ -1466,6 +1469,7 @@ class LinearForm:
             for j in range(3):
                 arr[k].e[j] = t["e"][j]
             arr[k].d_gf = t["gf"].vec.data_ptr() if t["gf"] is not None else None
+            arr[k].gf_space = t["gf"].space.h.value if t["gf"] is not None else None
             d = t["defined_on"]
             if d is not None:
                 self._keep.append(d)

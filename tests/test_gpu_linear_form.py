@@ -103,3 +103,29 @@ def test_linear_form_python_api(xg, orc, case):
     f2.Assemble()
     mx = xg.Integrate(levelset_domain={"levelset": gf, "domain_type": xg.NEG, "order": 3}, mesh=m, cf=xg.x)
     assert abs(float(f2.vec.sum().item()) - 2 * mx) <= 1e-12 * max(1.0, abs(mx))
+
+
+@pytest.mark.parametrize("D,k", [(2, 1), (2, 2), (3, 2)])
+def test_source_from_another_space(xg, D, k):
+    """A GridFunction source of another space (H1 of order 3, L2 of order 2)
+    holding the same polynomial as the form's space gives the same vector
+    (its own basis evaluated at the rule's points)."""
+    m = MakeStructured2DMesh(9, 9) if D == 2 else MakeStructured3DMesh(4)
+    g = xg.GridFunction(xg.H1(m, order=1))
+    xg.InterpolateToP1(((m.coords - 0.4) ** 2).sum(axis=1) - 0.3 ** 2, g)
+    poly = (lambda *p: 1.0 + p[0] - 0.5 * p[1]) if k == 1 else (lambda *p: 1.0 + p[0] * p[1] - p[D - 1] ** 2)
+    V = xg.H1(m, order=k)
+    u, v = V.TnT()
+    sources = [xg.GridFunction(V).Set(poly), xg.GridFunction(xg.H1(m, order=3)).Set(poly),
+               xg.GridFunction(xg.L2(m, order=2)).Set(poly)]
+    for dt in (xg.NEG, xg.IF):
+        vecs = []
+        for s in sources:
+            f = xg.LinearForm(V)
+            f += 1.5 * s * v * xg.dCut(g, dt)
+            f.Assemble()
+            vecs.append(f.vec.cpu().numpy().copy())
+        scale = np.abs(vecs[0]).max()
+        assert scale > 0
+        for w in vecs[1:]:
+            assert np.abs(w - vecs[0]).max() < 1e-13 * scale, dt
