@@ -250,10 +250,13 @@ typedef struct {
  * straight cut rule (cutint/cutintegral.cpp:126-212), e.g. the L2 and H1
  * errors (gfu - gfex)^2, (grad gfu - grad gfex)^2 of its demos.  Simplex meshes.  Deterministic fixed-order
  * sum into d_result[0]; shares the mesh's scratch with xg_integrate (calls on
- * one mesh are serialised on one stream). */
+ * one mesh are serialised on one stream).  d_deform (xg_iso_deformation's
+ * [nedges][3], or NULL): on the deformed mesh, the straight cut rule of the P1
+ * level set mapped by xhat + Theta(xhat) as in xg_cterm.d_deform. */
 int xg_integrate_fields(xg_mesh* mesh, const double* d_lset, int dt, int order, int32_t nfields,
                         xg_space* const* spaces, const double* const* d_fields, int32_t nmonos,
-                        const xg_fmono* monos, const uint64_t* d_defined_on, double* d_result, void* stream);
+                        const xg_fmono* monos, const uint64_t* d_defined_on, const double* d_deform,
+                        double* d_result, void* stream);
 
 /* Several level sets on a simplex mesh (cutint/mlsetintegration.cpp:6-180,
  * cutint/straightcutrule.cpp:679-812): d_lsets holds nlsets (1..8) P1 level

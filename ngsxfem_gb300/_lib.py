@@ -182,7 +182,7 @@ def load():
         "xg_base_rule": (I, [I, I, P, P, I]),
         "xg_integrate": (I, [P, P, I, I, I, I, I, P, P, P]),
         "xg_integrate_ex": (I, [P, P, I, I, I, I, I, I, P, P, P]),
-        "xg_integrate_fields": (I, [P, P, I, I, I, P, P, I, P, P, P, P]),
+        "xg_integrate_fields": (I, [P, P, I, I, I, P, P, I, P, P, P, P, P]),
         "xg_integrate_mlset": (I, [P, P, ctypes.c_int32, P, ctypes.c_int32, I, I, I, I, P, P, P]),
         "xg_cut_rules_mlset": (I, [P, P, ctypes.c_int32, P, ctypes.c_int32, P, ctypes.c_int32, I, ctypes.c_int32,
                                    P, P, P, P]),

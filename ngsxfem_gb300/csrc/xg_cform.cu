@@ -501,6 +501,8 @@ struct FieldsDesc {
   int e[kMaxFMonos][3];
   int f0[kMaxFMonos], f1[kMaxFMonos];
   int d0[kMaxFMonos], d1[kMaxFMonos];  // -1: the value, else the derivative along x_d
+  const double* gdef;                  // mesh deformation [nedges][3] or NULL
+  const int32_t* el_edges;             // [nedges per element][ne]
 };
 
 template <int D>
@@ -534,16 +536,65 @@ __global__ void __launch_bounds__(kFiThreads)
       }
       gl[D][k] = -sg;
     }
-    auto point = [&](const double* xi, double w) {
-      double lam[D + 1], sl = 0.0, xp[3] = {0.0, 0.0, 0.0};
+    const double ifac = dt == XG_IF && cdom == XG_IF && !F.gdef ? if_factor<D>(g, l) : 1.0;
+    // the deformation in the reference frame: theta_j = J^-1 gdef(edge j)
+    double theta[6][3];
+    if (F.gdef) {
+      constexpr int NE = D == 2 ? 3 : 6;
+      for (int j = 0; j < 6; j++)
+        for (int r = 0; r < 3; r++) {
+          double sr = 0.0;
+          if (j < NE && r < D) {
+            const int ed = F.el_edges[(int64_t)j * ne + e];
+            for (int k = 0; k < D; k++) sr += g.Finv[r][k] * F.gdef[(int64_t)ed * 3 + k];
+          }
+          theta[j][r] = sr;
+        }
+    }
+    // the rule point xi of the reference element with reference weight wr
+    auto point = [&](const double* xi, double wr) {
+      double lam[D + 1], sl = 0.0, xp[3] = {0.0, 0.0, 0.0}, y[3] = {xi[0], xi[1], D == 3 ? xi[2] : 0.0};
       for (int k = 0; k < D; k++) {
         lam[k] = xi[k];
         sl += xi[k];
       }
       lam[D] = 1.0 - sl;
+      double w = wr * meas * ifac, gd[D + 1][D];
+      const double(*gp)[D] = gl;
+      if (F.gdef) {
+        // x = x0 + J (xi + Theta(xi)), F = J (I + grad Theta): weight |det F|
+        // (IF: times |F^-T n_ref|), gradients through F^-T
+        double Am[3][3], Fm[3][3], Fi[3][3], detF;
+        iso::deform_at<D>(theta, xi, y, Am);
+        for (int r = 0; r < 3; r++)
+          for (int k = 0; k < 3; k++) {
+            double sr = 0.0;
+            for (int q = 0; q < 3; q++) sr += (r < D && q < D ? g.F[r][q] : (r == q ? 1.0 : 0.0)) * Am[q][k];
+            Fm[r][k] = sr;
+          }
+        if (!iso::invert<D>(Fm, Fi, &detF)) {
+          set_err(err, XG_ERR_NONFINITE);
+          return;
+        }
+        double nn2 = 0.0, gr2 = 0.0;
+        for (int k = 0; k < D; k++) {
+          double sa = 0.0, sn = 0.0;
+          for (int a = 0; a < D; a++) {
+            gd[a][k] = Fi[a][k];
+            sa += Fi[a][k];
+            sn += Fi[a][k] * (l[a] - l[D]);
+          }
+          gd[D][k] = -sa;
+          nn2 += sn * sn;
+          gr2 += (l[k] - l[D]) * (l[k] - l[D]);
+        }
+        w = wr * fabs(detF);
+        if (dt == XG_IF) w *= sqrt(nn2 / gr2);
+        gp = gd;
+      }
       for (int r = 0; r < D; r++) {
         double sr = g.x0[r];
-        for (int k = 0; k < D; k++) sr += g.F[r][k] * xi[k];
+        for (int k = 0; k < D; k++) sr += g.F[r][k] * y[k];
         xp[r] = sr;
       }
       // factor table: [field][0] the value, [field][1 + d] the derivative along x_d
@@ -556,7 +607,7 @@ __global__ void __launch_bounds__(kFiThreads)
           const double ca = F.v[i][F.dofs[i][(int64_t)a * ne + e]];
           if (F.grad[i]) {
             double ph, gr[D];
-            eval_fn<D, double>(desc_rt<D>(k, a, gv), lam, gl, ph, gr);
+            eval_fn<D, double>(desc_rt<D>(k, a, gv), lam, gp, ph, gr);
             s += ca * ph;
             for (int d = 0; d < D; d++) sg[d] += ca * gr[d];
           } else {
@@ -575,7 +626,7 @@ __global__ void __launch_bounds__(kFiThreads)
         if (F.f1[m] >= 0) t *= fv[F.f1[m]][1 + F.d1[m]];
         val += t;
       }
-      acc += w * meas * val;
+      acc += w * val;
     };
     if (cdom != XG_IF) {
       const int off = g_cf_rules.off[D][p], cnt = g_cf_rules.cnt[D][p];
@@ -590,13 +641,12 @@ __global__ void __launch_bounds__(kFiThreads)
     }
     const int sd = dt == XG_IF ? D - 1 : D;
     const int off = g_cf_rules.off[sd][p], cnt = g_cf_rules.cnt[sd][p];
-    const double fac = dt == XG_IF ? if_factor<D>(g, l) : 1.0;
     for (int s = 0; s < ns; s++) {
       const double trafofac = simplex_volume(subs[s].p, sd + 1);
       for (int q = 0; q < cnt; q++) {
         double pt[3];
         plain_point(subs[s], sd + 1, g_cf_rules.x[off + q], pt);
-        point(pt, g_cf_rules.w[off + q] * trafofac * fac);
+        point(pt, g_cf_rules.w[off + q] * trafofac);
       }
     }
   }
@@ -624,8 +674,8 @@ using namespace xg;
 
 extern "C" int xg_integrate_fields(xg_mesh* m, const double* d_lset, int dt, int order, int32_t nfields,
                                    xg_space* const* spaces, const double* const* d_fields, int32_t nmonos,
-                                   const xg_fmono* monos, const uint64_t* d_defined_on, double* d_result,
-                                   void* stream) {
+                                   const xg_fmono* monos, const uint64_t* d_defined_on, const double* d_deform,
+                                   double* d_result, void* stream) {
   if (!m || !d_lset || !d_result || dt < 0 || dt > 2 || order < 0 || order > kMaxOrder || nfields < 0 ||
       nmonos < 0 || (nfields > 0 && (!spaces || !d_fields)) || (nmonos > 0 && !monos))
     return XG_ERR_ARG;
@@ -667,6 +717,8 @@ extern "C" int xg_integrate_fields(xg_mesh* m, const double* d_lset, int dt, int
     if (q.d0 >= 0) F.grad[q.f0] = 1;
     if (q.d1 >= 0) F.grad[q.f1] = 1;
   }
+  F.gdef = d_deform;
+  F.el_edges = m->d_el_edges;
   if (int st = ensure_device_rules()) return st;
   const size_t need = kFiBlocks * sizeof(double);
   if (m->scratch_bytes < need) {

@@ -1537,9 +1537,9 @@ def _integrate_fields(expr, meas, order):
     xg_integrate_fields (the reference's Integrate with a CoefficientFunction
     of GridFunctions, cutint/cutintegral.cpp:126-212), e.g. the L2 error
     Integrate((gfu - gfex) ** 2 * dCut(lsetp1, NEG), mesh)."""
-    if meas.kind != "cut" or meas.skeleton or meas.vb != VOL or meas.deformation is not None or meas.subdivlvl:
+    if meas.kind != "cut" or meas.skeleton or meas.vb != VOL or meas.subdivlvl:
         raise NotImplementedError("Integrate of GridFunction integrands: dCut(P1 level set, dt[, order, "
-                                  "definedonelements]) on volume elements")
+                                  "definedonelements, deformation]) on volume elements")
     lset = meas.levelset
     if not isinstance(lset, GridFunction) or isinstance(lset.space, SpaceTimeFESpace):
         raise NotImplementedError("Integrate of GridFunction integrands takes one spatial P1 level set")
@@ -1606,8 +1606,9 @@ def _integrate_fields(expr, meas, order):
     res = torch.zeros(1, dtype=torch.float64, device=_dev())
     defined = meas.definedonelements
     q = meas.order if meas.order is not None else order
+    gdef = meas.deformation._edge_deformation() if meas.deformation is not None else None
     _lib.call("xg_integrate_fields", dm.h, _vp(lv), meas.domain_type, int(q), len(fields), sp, dv, len(monos), arr,
-              _vp(defined.words) if defined is not None else None, _vp(res), _stream())
+              _vp(defined.words) if defined is not None else None, _vp(gdef), _vp(res), _stream())
     dm.check()
     return meas.scale * float(res.item())
 

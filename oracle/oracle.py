@@ -137,7 +137,7 @@ def lib():
         L.orc_integrate.argtypes = [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, P]
         L.orc_integrate_fields.restype = ctypes.c_double
         L.orc_integrate_fields.argtypes = [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int, P, P,
-                                           P, P, P, P, P]
+                                           P, P, P, P, P, P]
         L.orc_element_matrix.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int, P]
         L.orc_patch_matrix.argtypes = [P, P, ctypes.c_int, ctypes.c_int, P]
         L.orc_assemble.restype = P
@@ -646,7 +646,7 @@ class Space:
         d = None if defined_on is None else np.ascontiguousarray(defined_on, dtype=np.uint64)
         return lib().orc_integrate(self.h, _p(l), dt, order, ex, ey, ez, _p(d))
 
-    def integrate_fields(self, lset, dt, order, fields, monos, defined_on=None):
+    def integrate_fields(self, lset, dt, order, fields, monos, defined_on=None, theta=None):
         """Integrate of sum_m c_m x^e_m F_a F_b over the straight cut rule.
         fields: list of (order, element coefficients [ne][nd]); monos: list of
         (c, (ex, ey, ez), a, b[, da, db]), a / b field indices or -1, da / db
@@ -664,8 +664,9 @@ class Space:
         f1 = np.array([m[3] for m in monos], dtype=np.int32)
         d0 = np.array([m[4] if len(m) > 4 else -1 for m in monos], dtype=np.int32)
         d1 = np.array([m[5] if len(m) > 5 else -1 for m in monos], dtype=np.int32)
+        th = None if theta is None else np.ascontiguousarray(theta, dtype=np.float64)
         return lib().orc_integrate_fields(self.h, _p(l), dt, order, len(fe), _p(fo), ctypes.cast(fp, ctypes.c_void_p),
-                                          len(monos), _p(c), _p(e3), _p(f0), _p(f1), _p(d0), _p(d1), _p(d))
+                                          len(monos), _p(c), _p(e3), _p(f0), _p(f1), _p(d0), _p(d1), _p(d), _p(th))
 
     @staticmethod
     def _terms(terms):

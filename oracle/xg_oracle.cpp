@@ -1757,26 +1757,72 @@ double orc_integrate(const orc_space* s, const double* lset_vertex, int dt, int 
 double orc_integrate_fields(const orc_space* s, const double* lset_vertex, int dt, int order, int nf,
                             const int* f_order, const double* const* f_el, int nm, const double* coef,
                             const int* e3, const int* f0, const int* f1, const int* d0, const int* d1,
-                            const uint64_t* defined_on) {
+                            const uint64_t* defined_on, const double* theta_mesh) {
   const int D = s->D;
   double sum = 0;
   std::vector<double> pts, wts;
   double phi[20], dphi[20][3], fv[8][4];
+  Geo gref;
+  {
+    const double ref2[6] = {1, 0, 0, 1, 0, 0}, ref3[12] = {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0};
+    make_geo(D, D == 2 ? ref2 : ref3, gref);
+  }
   for (int e = 0; e < s->ne; e++) {
     if (defined_on && !test_bit(defined_on, e)) continue;
     Geo g;
     double l[4];
     element_geo(s, e, g, l, lset_vertex);
-    const int n = straight_cut_rule(g, l, dt, order, pts, wts);
+    // on the deformed mesh: the rule of the reference element, mapped point by point
+    const double* th = theta_mesh ? theta_mesh + (size_t)e * 18 : nullptr;
+    const int n = straight_cut_rule(th ? gref : g, l, dt, order, pts, wts);
     if (n <= 0) continue;
     const int* gv = &s->elv[(size_t)e * (D + 1)];
     const double meas = std::fabs(g.det);
     for (int q = 0; q < n; q++) {
       const double* xi = &pts[3 * q];
+      double y[3] = {xi[0], xi[1], D == 3 ? xi[2] : 0.0}, wq = wts[q] * meas;
+      Geo gd = g;  // the map whose inverse takes the gradients (the point's Jacobian when deformed)
+      if (th) {
+        // y = xi + Theta(xi), A = I + grad Theta (edge shapes lambda_a lambda_b), F = J A
+        double lam[4], sl = 0.0, Am[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+        for (int k = 0; k < D; k++) {
+          lam[k] = xi[k];
+          sl += xi[k];
+        }
+        lam[D] = 1.0 - sl;
+        const int E2[3][2] = {{0, 1}, {0, 2}, {1, 2}}, E3[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+        for (int j = 0; j < (D == 2 ? 3 : 6); j++) {
+          const int a = D == 2 ? E2[j][0] : E3[j][0], b = D == 2 ? E2[j][1] : E3[j][1];
+          const double ph = lam[a] * lam[b];
+          double dph[3];
+          for (int k = 0; k < D; k++) {
+            const double da = a < D ? (a == k ? 1.0 : 0.0) : -1.0, db = b < D ? (b == k ? 1.0 : 0.0) : -1.0;
+            dph[k] = da * lam[b] + lam[a] * db;
+          }
+          for (int r = 0; r < D; r++) {
+            y[r] += th[j * 3 + r] * ph;
+            for (int k = 0; k < D; k++) Am[r][k] += th[j * 3 + r] * dph[k];
+          }
+        }
+        double elc[12], F[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        for (int r = 0; r < D; r++)
+          for (int k = 0; k < D; k++)
+            for (int q2 = 0; q2 < D; q2++) F[r][k] += g.F[r][q2] * Am[q2][k];
+        for (int v = 0; v <= D; v++)
+          for (int r = 0; r < D; r++) elc[v * D + r] = v < D ? F[r][v] : 0.0;
+        make_geo(D, elc, gd);
+        wq = wts[q] * std::fabs(gd.det);
+        if (dt == ORC_IF) {
+          double gr[3] = {0, 0, 0}, gp[3];
+          for (int k = 0; k < D; k++) gr[k] = l[k] - l[D];
+          phys_grad(gd, gr, gp);
+          wq *= l2norm3(gp) / l2norm3(gr);
+        }
+      }
       double x[3] = {0, 0, 0};
       for (int i = 0; i < D; i++) {
         double sacc = g.x0[i];
-        for (int k = 0; k < D; k++) sacc += g.F[i][k] * xi[k];
+        for (int k = 0; k < D; k++) sacc += g.F[i][k] * y[k];
         x[i] = sacc;
       }
       for (int i = 0; i < nf && i < 8; i++) {
@@ -1788,7 +1834,7 @@ double orc_integrate_fields(const orc_space* s, const double* lset_vertex, int d
           v += c * phi[a];
           for (int r = 0; r < 3; r++) dr[r] += c * dphi[a][r];
         }
-        phys_grad(g, dr, dp);
+        phys_grad(gd, dr, dp);
         fv[i][0] = v;
         for (int r = 0; r < 3; r++) fv[i][1 + r] = dp[r];
       }
@@ -1800,7 +1846,7 @@ double orc_integrate_fields(const orc_space* s, const double* lset_vertex, int d
         if (f1[m] >= 0) t *= fv[f1[m]][d1 ? 1 + d1[m] : 0];
         val += t;
       }
-      sum += wts[q] * meas * val;
+      sum += wq * val;
     }
   }
   return sum;

@@ -102,7 +102,7 @@ double orc_integrate(const orc_space*, const double* lset_vertex, int dt, int or
 double orc_integrate_fields(const orc_space*, const double* lset_vertex, int dt, int order, int nf,
                             const int* f_order, const double* const* f_el, int nm, const double* coef,
                             const int* e3, const int* f0, const int* f1, const int* d0, const int* d1,
-                            const uint64_t* defined_on);
+                            const uint64_t* defined_on, const double* theta_mesh /* [ne][6][3] or NULL */);
 
 /* Element matrix of the sum of volume terms on element e (row = test, col = trial). */
 int orc_element_matrix(const orc_space*, const double* lset_vertex, const orc_term* terms, int nterms,

@@ -116,3 +116,36 @@ def test_h1_error_parity(xg, orc, D, k, n):
         scale2 = sp.integrate_fields(l, dt, q, [fu] + fc, [(1.0, z, 0, 0, d, d) for d in range(D)] +
                                      [(1.0, z, 1 + d, 1 + d) for d in range(D)])
         assert abs(dot - ref2) < 1e-12 * scale2, (dt, dot, ref2)
+
+
+@pytest.mark.parametrize("dt_name", ["NEG", "IF"])
+def test_deformed_field_integrals(xg, orc, dt_name):
+    """Integrate((gfu) ** 2 * dCut(lsetp1, dt, deformation=...)) and its H1
+    part against the oracle on its own deformation (separate Newton
+    searches: 1e-10), and the constant field against the monomial Integrate
+    on the same deformation (1e-12)."""
+    dt = getattr(xg, dt_name)
+    m = MakeStructured2DMesh(8, 8, -1, 1, -1, 1)
+    phi = lambda x, y: np.sqrt(x * x + y * y) - 0.5  # noqa: E731
+    adap = xg.LevelSetMeshAdaptation(m, order=2, threshold=0.2)
+    deformation = adap.CalcDeformation(phi)
+    lsetp1 = adap.lset_p1
+    V = xg.H1(m, order=2)
+    rng = np.random.default_rng(4)
+    gfu = xg.GridFunction(V)
+    gfu.vec.copy_(torch.from_numpy(rng.standard_normal(V.ndof)))
+    one = xg.GridFunction(xg.H1(m, order=1)).Set(lambda x, y: np.ones_like(x))
+    theta, _ = orc.iso_theta_mesh(m, xg.P2ElementValues(m, phi), threshold=0.2)
+    sp = orc.Space(m, 2)
+    fa = (2, gfu.vec.cpu().numpy()[sp.el_dofs()])
+    l = lsetp1.vec.cpu().numpy()
+    z = (0, 0, 0)
+    ds = xg.dCut(lsetp1, dt, deformation=deformation, order=4)
+    got = xg.Integrate(gfu * gfu * ds, m)
+    ref = sp.integrate_fields(l, dt, 4, [fa], [(1.0, z, 0, 0)], theta=theta)
+    assert abs(got - ref) < 1e-10 * abs(ref), (got, ref)
+    got_h1 = xg.Integrate(xg.grad(gfu) ** 2 * ds, m)
+    ref_h1 = sp.integrate_fields(l, dt, 4, [fa], [(1.0, z, 0, 0, d, d) for d in range(2)], theta=theta)
+    assert abs(got_h1 - ref_h1) < 1e-10 * abs(ref_h1), (got_h1, ref_h1)
+    meas = xg.Integrate(one * ds, m)
+    assert abs(meas - xg.Integrate(ds, m)) < 1e-12 * abs(meas)

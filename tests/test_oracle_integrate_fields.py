@@ -112,3 +112,30 @@ def test_gradient_products_are_the_stiffness_matrix(D, k):
         got = sp.integrate_fields(l, dt, 2 * k, [(k, a[ed]), (k, b[ed])],
                                   [(1.0, (0, 0, 0), 0, 1, d, d) for d in range(D)])
         assert abs(got - a @ K @ b) < 1e-12 * np.abs(K).sum(), (dt, got, a @ K @ b)
+
+
+def test_deformed_field_integrals():
+    """On the deformed mesh (orc_iso_theta_mesh): a zero deformation gives the
+    plain integrals, and the constant field 1 gives the deformed measure of
+    orc_iso_integrate_mesh (NEG and IF)."""
+    m = MakeStructured2DMesh(8, 8, -1, 1, -1, 1)
+    p2 = orc.p2_nodal_values(m, lambda p: np.sqrt(p[..., 0] ** 2 + p[..., 1] ** 2) - 0.5)
+    l = np.zeros(m.nv)
+    for i in range(3):
+        l[m.elements[:, i]] = p2[:, i]
+    l = np.where(np.abs(l) < 1e-14, 1e-14, l)
+    theta, _ = orc.iso_theta_mesh(m, p2, threshold=0.2)
+    sp = orc.Space(m, 2)
+    rng = np.random.default_rng(2)
+    a = rng.standard_normal(sp.ndof)
+    fa = (2, a[sp.el_dofs()])
+    one = (1, np.ones((m.ne, 3)))
+    z = (0, 0, 0)
+    prods = [(1.0, z, 0, 0), (1.0, z, 0, 0, 0, 0), (0.5, (1, 0, 0), 0, -1, 1, -1)]
+    for dt in (orc.NEG, orc.IF):
+        plain = sp.integrate_fields(l, dt, 4, [fa], prods)
+        zero = sp.integrate_fields(l, dt, 4, [fa], prods, theta=np.zeros_like(theta))
+        assert abs(plain - zero) < 1e-13 * max(1.0, abs(plain))
+        meas, _ = orc.iso_integrate_mesh(m, p2, dt, 4, threshold=0.2)
+        got = sp.integrate_fields(l, dt, 4, [one], [(1.0, z, 0, -1)], theta=theta)
+        assert abs(got - meas) < 1e-13, (dt, got, meas)
