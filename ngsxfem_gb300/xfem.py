@@ -422,6 +422,8 @@ def Restrict(space, active_elements):
     elements (the reference's Restrict(fes, ba)).  The dof numbering stays
     the space's: the assembled matrix holds the rows of the active elements
     only, and FreeDofs() selects them for a solver."""
+    if not isinstance(space, H1) or getattr(space, "h", None) is None:
+        raise NotImplementedError("Restrict / Compress of spatial H1 / L2 spaces on simplex meshes")
     view = object.__new__(type(space))
     view.__dict__.update(space.__dict__)
     view._base, view._owner, view._active_elements = space, False, active_elements

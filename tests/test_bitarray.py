@@ -20,3 +20,17 @@ def test_pack_unpack_round_trip(monkeypatch):
         assert torch.equal(a.words.cpu(), b.words.cpu())
         assert np.array_equal(a.bool_tensor().cpu().numpy(), bits)
         assert np.array_equal(a.numpy(), bits)
+
+
+def test_restrict_takes_spatial_spaces_only():
+    """Restrict / Compress views share the space's handle; space-time spaces
+    (their own lifetime) and tensor-mesh H1 (no handle) are refused."""
+    import pytest
+
+    st = object.__new__(X.SpaceTimeFESpace)
+    with pytest.raises(NotImplementedError):
+        X.Restrict(st, None)
+    quad = object.__new__(X.H1)
+    quad.h = None
+    with pytest.raises(NotImplementedError):
+        X.Compress(quad, None)
